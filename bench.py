@@ -1,0 +1,295 @@
+"""Benchmark of the AStrO hot path on one GB300 (config: 64x32x32 brick8 heterogeneous block).
+
+Metric: element matrices per second (the element-evaluation + global-assembly pass), plus the
+static solve to 1e-10 FP64 relative residual reported in the "solve" object.
+  value   FP32 element kernels (sparse-B, orthotropic C) assembled into the device block-CSR
+          matrix, inputs resident in HBM; one step = one pass over all 65,536 elements
+          (8 colour launches).  L2 is flushed between timed steps.
+  e2e     getElasticSolnLoad(buildMat=1) through the C ABI (astro_el_soln_load) with host
+          buffers: state/load upload, FP64 element kernels, assembly, and the export of the
+          reference CSR matrix (values + columns) and the residual load to host memory.
+  solve   mixed-precision Jacobi-FGMRES(50) (FP32 inner, FP64 residual refinement) to 1e-10 and
+          the plain FP64 Jacobi-GMRES(50) comparator, seconds each (CUDA events).
+`--impl reference` times the CPU restatement of the reference (the oracle) on a bounded sample of
+the same workload with all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "element mats/s (64x32x32 brick8 block: element eval + assembly); s to 1e-10 FP64 rel resid"
+UNIT = "elements/s"
+
+
+def _parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--nx", type=int, default=64)
+    p.add_argument("--ny", type=int, default=32)
+    p.add_argument("--nz", type=int, default=32)
+    p.add_argument("--no-solve", action="store_true")
+    p.add_argument("--solve-max-iters", type=int, default=60000)
+    return p.parse_args()
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return rank, ws
+
+
+def _config(a):
+    return {"workload": f"cfg2 heterogeneous block {a.nx}x{a.ny}x{a.nz} brick8 (seed 0)",
+            "elements": a.nx * a.ny * a.nz, "dof": 3 * (a.nx + 1) * (a.ny + 1) * (a.nz + 1),
+            "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas only"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def _oracle_rate(model, nel, threads):
+    """Oracle (CPU restatement) element matrices per second on elements 1..nel, split over threads."""
+    from oracle import Oracle
+    o = Oracle(model)
+    chunks = np.array_split(np.arange(1, nel + 1), threads)
+
+    def work(c):
+        if len(c):
+            o.element_matrices(int(c[0]), int(c[-1]))
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=work, args=(c,)) for c in chunks]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    dt = time.perf_counter() - t0
+    return nel / dt, dt
+
+
+def run_reference(a):
+    rank, ws = _dist()
+    if rank != 0:
+        return 0
+    from misc_gb300 import model as M
+    m = M.config2(nx=a.nx, ny=a.ny, nz=a.nz)
+    cores = os.cpu_count() or 1
+    sample = min(m.num_els, 512 * cores)
+    for _ in range(max(a.warmup, 0)):
+        _oracle_rate(m, min(sample, 64 * cores), cores)
+    times = []
+    for _ in range(a.steps):
+        r, dt = _oracle_rate(m, sample, cores)
+        times.append(dt)
+    tot = sum(times)
+    val = a.steps * sample / tot
+    line = {"metric": METRIC, "value": val, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": _config(a), "impl": "reference",
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"brick8 element matrices of elements 1..{sample} per step (oracle restatement "
+                                       f"of r_getElRuk, FP64), split over {cores} host threads"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(a):
+    rank, ws = _dist()
+    import ctypes as C
+
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from misc_gb300 import model as M
+    from misc_gb300.astro import SOLVER_FGMRES_MIXED, SOLVER_GMRES_JACOBI_FP64, AstroGPU, load_library
+    m = M.config2(nx=a.nx, ny=a.ny, nz=a.nz)
+    g = AstroGPU(m)
+    L = load_library()
+    E = m.num_els
+    # device-resident FP32 path
+    g.assemble_fp32()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    stream = C.c_void_p()
+    # the library launches on its own stream: time with CUDA events recorded on that stream via
+    # the runtime API (torch events would only see torch's stream)
+    cudart = C.CDLL("libcudart.so")
+    cudart.cudaEventCreate.argtypes = [C.POINTER(C.c_void_p)]
+    cudart.cudaEventRecord.argtypes = [C.c_void_p, C.c_void_p]
+    cudart.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
+    cudart.cudaEventSynchronize.argtypes = [C.c_void_p]
+    cudart.cudaDeviceSynchronize.argtypes = []
+    s = L.astro_ctx_stream(g.h)
+    ev = [C.c_void_p() for _ in range(2 * a.steps)]
+    for e in ev:
+        cudart.cudaEventCreate(C.byref(e))
+    for _ in range(a.warmup):
+        L.astro_assemble_fp32_async(g.h)
+        flush.fill_(1)
+    torch.cuda.synchronize()
+    cudart.cudaDeviceSynchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = Clocks()
+    clk.start()
+    t0 = time.perf_counter()
+    for k in range(a.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        cudart.cudaEventRecord(ev[2 * k], s)
+        rc = L.astro_assemble_fp32_async(g.h)
+        assert rc == 0
+        cudart.cudaEventRecord(ev[2 * k + 1], s)
+    cudart.cudaDeviceSynchronize()
+    wall = time.perf_counter() - t0
+    ms = []
+    for k in range(a.steps):
+        f = C.c_float()
+        cudart.cudaEventElapsedTime(C.byref(f), ev[2 * k], ev[2 * k + 1])
+        ms.append(f.value)
+    clocks = clk.stop()
+    tot_ms = sum(ms)
+    if ws > 1:
+        t = torch.tensor([tot_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    value = ws * E * a.steps / (tot_ms * 1e-3)
+    ms_step = tot_ms / a.steps
+    # e2e: FP64 drop-in call with host buffers
+    n = g.n
+    load = np.zeros(n)
+    mat = np.zeros(g.el_mat_size)
+    cols = np.zeros(g.el_mat_size, np.int32)
+    disp = np.zeros(n)
+    st = M.make_state(n, disp=disp)
+    from misc_gb300.astro import _d, _i
+    for _ in range(max(1, a.warmup // 2)):
+        load[:] = 0
+        L.astro_el_soln_load(g.h, 1, C.byref(st), _d(load), None, _d(mat), _i(cols), None)
+    e2e_steps = max(3, min(a.steps, 10))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        load[:] = 0
+        rc = L.astro_el_soln_load(g.h, 1, C.byref(st), _d(load), None, _d(mat), _i(cols), None)
+        assert rc == 0
+    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    # FP64 device-resident (kernel only) for reference
+    g.getElasticSolnLoad(1, export=False)
+    # roofline of the assembly pass
+    peaks = _peaks()
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    nnz = g.dims.num_blocks * 9
+    alg_bytes = nnz * 4 + m.num_nodes * 24 + E * (8 * 4 + 9 * 8)
+    achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "config": _config(a),
+            "e2e": {"value": E / e2e_dt, "unit": UNIT, "path": "astro_el_soln_load FP64 with host buffers",
+                    "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8 + g.el_mat_size * 12},
+            "gpu_launches": a.steps * g.dims.num_colors,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": None, "kernel": "hex8_kernel<float> (8 colour launches = 1 assembly pass)",
+                         "algorithmic_bytes": alg_bytes, "peak_source": "measured" if peaks else "fallback"},
+            "clocks": clocks, "wall_s": wall}
+    if not a.no_solve and rank == 0:
+        g.scaleElasticMPC()
+        b = g.static_rhs()
+        res = {}
+        for name, meth in (("fgmres_mixed", SOLVER_FGMRES_MIXED), ("gmres_fp64", SOLVER_GMRES_JACOBI_FP64)):
+            u, stt = g.solve_static(b, method=meth, rtol=1e-10, restart=50, max_iters=a.solve_max_iters,
+                                    allow_maxit=True)
+            res[name] = {"seconds": stt.seconds, "iterations": stt.iterations, "restarts": stt.restarts,
+                         "refinements": stt.refinements, "rel_residual": stt.rel_residual, "status": stt.status}
+        res["metric"] = "s to 1e-10 FP64 rel resid (Jacobi, restart 50)"
+        line["solve"] = res
+    # CPU baseline: oracle, 1 core, bounded sample
+    if rank == 0:
+        rate, dt = _oracle_rate(m, 1024, 1)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": "brick8 element matrices of elements 1..1024 (oracle restatement, FP64, "
+                                          "single thread)"}
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    a = _parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,254 @@
+/*
+ * astro_gpu.h -- C ABI of the GB300 (sm_103a) implementation of AStrO's structural hot path:
+ * element stiffness/residual evaluation (brick8 solids, shell4 shells, real and complex-step),
+ * global assembly, and the linear solve (row-skyline LDL^T factor/solve, restarted GMRES).
+ *
+ * The entry points mirror the Fortran subroutines that AStrO_runJob drives, so a thin
+ * iso_c_binding shim can route those subroutines here.  Conventions follow the reference:
+ *   - node, element, section, material and DOF numbers are 1-based, as in the Fortran;
+ *   - "range" arrays are prefix sums with lower bound 0 (Fortran ARange(0:n)), passed as a
+ *     pointer to element 0;
+ *   - 2-D arrays are column-major (nodeList(3,N) is x1,y1,z1,x2,...);
+ *   - a CSR column index of 0 marks an unused slot and is skipped;
+ *   - the global DOF numbering is the reference's component-major nDofIndex.
+ * Every function returns ASTRO_OK (0) or a positive ASTRO_ERR_* code; astro_last_error() gives
+ * the message.  One host thread per context; calls are synchronous at return.
+ */
+#ifndef ASTRO_GPU_H
+#define ASTRO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ASTRO_OK 0
+#define ASTRO_ERR_ARG 1          /* bad argument or size */
+#define ASTRO_ERR_CUDA 2         /* CUDA runtime error (message has the CUDA error string) */
+#define ASTRO_ERR_UNSUPPORTED 3  /* element type / mesh mix not handled by this library */
+#define ASTRO_ERR_PIVOT 4        /* zero or non-finite pivot in an LDL^T or LU factorisation */
+#define ASTRO_ERR_NAN 5          /* non-finite value in a vector or residual */
+#define ASTRO_ERR_BREAKDOWN 6    /* Krylov breakdown (zero Arnoldi vector norm) */
+#define ASTRO_ERR_MAXIT 7        /* iteration limit reached before the tolerance */
+#define ASTRO_ERR_STATE 8        /* call out of order (e.g. solve before factorisation) */
+#define ASTRO_ERR_NOMEM 9        /* device allocation failed */
+
+/* Design-variable categories supported by the complex-step path (reference dCategory/dSubCat). */
+#define ASTRO_DCAT_LAYUP_THICKNESS 1   /* 'layup' / 'thickness' of layer d_layer */
+#define ASTRO_DCAT_ELASTIC_MODULUS 2   /* 'elastic' / 'modulus' component d_component (1..3) */
+
+/* Model arrays: the reference's module globals (Working/AStrO_globalData.f90) as flat arrays.
+ * Element types: 8 = brick8 (2x2x2 Gauss), 41 = shell4 (4 Gauss points, 8 condensed
+ * incompatible-mode DOF).  Constraints are given as expanded equations: equation k has terms
+ * mpc_range[k-1]..mpc_range[k]-1 (0-based term index), each term (node, dof, coef). */
+typedef struct astro_model {
+    int32_t num_nodes;
+    int32_t num_els;
+    const double *node_list;        /* nodeList(3,num_nodes) */
+    const int32_t *element_list;    /* elementList(8,num_els), 0 = unused slot */
+    const int32_t *element_type;    /* elementType(num_els) */
+    const int32_t *element_section; /* elementSection(num_els) */
+    int32_t num_sections;
+    const int32_t *section_mat_id;  /* sectionMatId(num_sections): solid sections */
+    const double *section_orient;   /* sectionOrient(3,3*num_sections): rows are local axes */
+    const int32_t *sec_layup_range; /* secLayupRange(0:num_sections) */
+    const int32_t *layup_mat_id;    /* layupMatId(num_layers) */
+    const double *layup_thickness;  /* layupThickness(num_layers) */
+    const double *layup_angle;      /* layupAngle(num_layers), radians */
+    const double *section_z_offset; /* sectionZOffset(num_sections) */
+    int32_t num_materials;
+    const double *material_elastic; /* materialElastic(9,num_materials): E1 E2 E3 nu12 nu13 nu23 G12 G13 G23 */
+    const double *material_density; /* materialDensity(num_materials) */
+    int32_t num_mpc;                /* number of constraint equations (elMPCDim) */
+    const int32_t *mpc_range;       /* (0:num_mpc) prefix sums over terms */
+    const int32_t *mpc_node;        /* node per term */
+    const int32_t *mpc_dof;         /* DOF component 1..6 per term */
+    const double *mpc_coef;         /* coefficient per term */
+    const double *mpc_rhs;          /* right-hand side per equation */
+    int32_t num_dvars;              /* design variables (0 if none) */
+    const int32_t *el_to_d_range;   /* elToDRange(0:num_els) */
+    const int32_t *el_to_d;         /* elToD: design variable per entry */
+    const double *el_to_coef;       /* elToCoef */
+    const int32_t *d_category;      /* ASTRO_DCAT_* per design variable */
+    const int32_t *d_component;     /* dComponent */
+    const int32_t *d_layer;         /* dLayer */
+    const double *d_value;          /* r_dVec */
+} astro_model;
+
+/* Sizes produced by analysis preparation (reference analysisPrep, Working/AStrO_bookKeeping.f90:794). */
+typedef struct astro_dims {
+    int32_t el_mat_dim;      /* elMatDim: number of global DOF */
+    int32_t el_mat_size;     /* elMatSize: CSR slots of the stiffness matrix */
+    int32_t el_mat_lt_size;  /* elMatLTSize: row-skyline size */
+    int32_t el_mpc_dim;      /* constraint equations */
+    int32_t el_mpc_size;     /* constraint terms */
+    int32_t int_vec_size;    /* intVecSize: condensed internal DOF */
+    int32_t int_mat_size;    /* intMatSize */
+    int32_t solver_max_bw;   /* solverMaxBW (node-rank bandwidth cap of the skyline profile) */
+    int32_t dof_per_node;    /* 3 (solid mesh) or 6 (shell mesh) */
+    int32_t num_blocks;      /* node-block nonzeros of the internal block-CSR matrix */
+    int32_t num_colors;      /* element colours (launches per assembly pass) */
+} astro_dims;
+
+/* Nodal state in global DOF numbering (length el_mat_dim) and internal-DOF state (int_vec_size).
+ * Any pointer may be NULL (= zeros). */
+typedef struct astro_state {
+    const double *node_disp, *node_vel, *node_acc;
+    const double *prev_disp, *prev_vel, *prev_acc;
+    const double *internal_disp, *prev_int_disp;
+    int32_t dynamic;         /* 1: add Newmark inertia (r_getElRu dynamic branch) */
+    double nm_beta, nm_gamma, del_t;
+} astro_state;
+
+/* Options and statistics of the spec solvers (astro_solve_static). */
+#define ASTRO_SOLVER_GMRES_JACOBI_FP64 0   /* plain FP64 Jacobi-GMRES(m): the comparator */
+#define ASTRO_SOLVER_FGMRES_MIXED 1        /* FP32 inner Jacobi-GMRES, FP64 refinement */
+#define ASTRO_SOLVER_FGMRES_LEARNED 2      /* FP32 inner FGMRES with the learned preconditioner */
+typedef struct astro_solve_opts {
+    int32_t method;          /* ASTRO_SOLVER_* */
+    int32_t restart;         /* Krylov basis size m (50) */
+    int32_t max_iters;       /* total inner iterations cap */
+    double rtol;             /* target ||b - A x||_2 / ||b||_2 in FP64 with A = K + C^T C */
+    double inner_rtol;       /* inner relative tolerance for the refinement methods */
+} astro_solve_opts;
+
+typedef struct astro_solve_stats {
+    int32_t iterations;      /* total inner (Arnoldi) iterations */
+    int32_t restarts;        /* restart cycles */
+    int32_t refinements;     /* FP64 refinement steps */
+    int32_t status;          /* ASTRO_OK or error code */
+    double rel_residual;     /* final FP64 true relative residual */
+    double seconds;          /* device time of the solve, CUDA events */
+} astro_solve_stats;
+
+typedef struct astro_ctx astro_ctx;
+
+/* ---- context ------------------------------------------------------------------------------ */
+
+/* Builds the context: uploads the model, runs analysis preparation (node reordering, DOF map,
+ * CSR/skyline structure, constraint matrix, element colouring and scatter maps) and keeps all
+ * device mirrors until astro_ctx_destroy.  Replaces analysisPrep
+ * (Working/AStrO_bookKeeping.f90:794-1039) together with the model upload. */
+int astro_ctx_create(const astro_model *model, astro_ctx **out);
+int astro_ctx_destroy(astro_ctx *ctx);
+/* Copies the last error message of ctx (or of the last failed astro_ctx_create when ctx is
+ * NULL) into buf (NUL-terminated, at most len bytes). */
+int astro_last_error(const astro_ctx *ctx, char *buf, int32_t len);
+
+/* Host-only variant of the analysis preparation (no GPU needed), for inspection and tests:
+ * fills dims and, when non-NULL, currentRank(num_nodes), nDofIndex(6,num_nodes),
+ * elMatRange(0:n), elMatLTRange(0:n), the exported CSR column numbers el_mat_cols[el_mat_size]
+ * (the order astro_el_soln_load produces) and the number of element colours.  No counterpart in
+ * the reference beyond analysisPrep itself (Working/AStrO_bookKeeping.f90:794-1039). */
+int astro_prep_host(const astro_model *model, astro_dims *dims, int32_t *current_rank,
+                    int32_t *n_dof_index, int32_t *el_mat_range, int32_t *el_mat_lt_range,
+                    int32_t *el_mat_cols, int32_t *num_colors);
+
+int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
+/* The CUDA stream (cudaStream_t) the context launches on, for callers that order their own work
+ * or record timing events around the library's kernels. */
+void *astro_ctx_stream(const astro_ctx *ctx);
+/* Reference analysisPrep outputs: currentRank(num_nodes), nDofIndex(6,num_nodes),
+ * elMatRange(0:n), elMatLTRange(0:n), and the unscaled constraint matrix
+ * elMPCMatRange(0:m), elMPCMatCols, elMPCMat, elMPCRHS.  NULL pointers are skipped. */
+int astro_get_prep(const astro_ctx *ctx, int32_t *current_rank, int32_t *n_dof_index,
+                   int32_t *el_mat_range, int32_t *el_mat_lt_range,
+                   int32_t *mpc_range, int32_t *mpc_cols, double *mpc_mat, double *mpc_rhs);
+
+/* ---- element evaluation and assembly ------------------------------------------------------ */
+
+/* getElasticSolnLoad(buildMat) (Working/AStrO_commandFunctions.f90:260-351).
+ * Evaluates every element at `state` on the GPU in FP64.  elastic_load[n] and
+ * int_elastic_load[int_vec_size] are accumulated in place: load(dof) -= Ru (as the reference).
+ * If build_mat == 1 the stiffness is assembled on the device (kept for the solvers) and, when
+ * the pointers are non-NULL, exported in the reference CSR layout: elastic_mat[el_mat_size],
+ * el_mat_cols[el_mat_size] (same column order as the reference's find-or-insert), and the
+ * condensed internal rows int_elastic_mat[int_mat_size]. */
+int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro_state *state,
+                       double *elastic_load, double *int_elastic_load,
+                       double *elastic_mat, int32_t *el_mat_cols, double *int_elastic_mat);
+
+/* Mixed-precision assembly used by the refinement solvers: element matrices evaluated in FP32
+ * (isotropic/orthotropic sparse-B formulation) and assembled at zero state into the device
+ * block-CSR matrix in both FP32 and FP64 storage.  The FP64 copy is the system matrix A. */
+int astro_assemble_fp32(astro_ctx *ctx);
+/* Same as astro_assemble_fp32 without the final stream synchronisation (for timing loops);
+ * requires a prior astro_assemble_fp32 on the context. */
+int astro_assemble_fp32_async(astro_ctx *ctx);
+
+/* Per-element matrices, for parity tests.  precision 64 or 32.  ke_out holds num_els blocks of
+ * nd x nd column-major doubles (nd = 24 for brick8/shell4 after condensation), ru_out num_els
+ * blocks of nd (may be NULL).  Evaluated at `state` (NULL = zero state). */
+int astro_element_matrices(astro_ctx *ctx, int32_t precision, const astro_state *state,
+                           double *ke_out, double *ru_out);
+
+/* Complex-step residual sensitivity dRu/dd for design variable dvar (1-based), at the nodal
+ * state `state` (getdRelasticdD, Working/AStrO_commandFunctions.f90:1172-1375, element part):
+ * the elements that depend on dvar are re-evaluated in complex FP64 with d_value[dvar] + i*h,
+ * and drudd[n] = Im(Ru)/h is scattered in global DOF numbering (accumulated, not zeroed). */
+int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const astro_state *state,
+                       double *drudd, double *int_drudd);
+
+/* ---- constraints and loads ---------------------------------------------------------------- */
+
+/* scaleElasticMPC (Working/AStrO_commandFunctions.f90:537-566): rows of C normalised to unit
+ * 2-norm, then scaled by 100*max|K| of the last assembled stiffness.  Device copy updated;
+ * scaled values exported when the pointers are non-NULL. */
+int astro_scale_mpc(astro_ctx *ctx, double *mpc_mat, double *mpc_rhs);
+/* getElasticConstraintLoad (:506-535): elastic_load += C^T (rhs - C u). */
+int astro_constraint_load(astro_ctx *ctx, const double *node_disp, double *elastic_load);
+/* Consistent surface load (intended semantics of getElasticAppliedLoad surface branch,
+ * :353-504 / r_getElSurfaceTraction, Working/AStrO_r_elementEqns.f90:1923-2018):
+ * for each (element, face) pair, elastic_load += integral of N^T t dA over the true face area,
+ * with t = traction[3] + (-pressure) * outward face normal. */
+int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el,
+                       const int32_t *face_num, const double *traction, double pressure,
+                       double *elastic_load);
+
+/* ---- linear solve ------------------------------------------------------------------------- */
+
+/* convertToLTri (Working/AStrO_bookKeeping.f90:754-792): row-skyline lTri = (K inside the
+ * profile) + C^T C inside the profile, from the device-resident K and scaled C.  Exported to
+ * l_tri[el_mat_lt_size] when non-NULL; the device copy stays for astro_ldl_fact_resident. */
+int astro_convert_to_ltri(astro_ctx *ctx, double *l_tri);
+
+/* getSparseLDLFact (Working/AStrO_solvers.f90:10-78), same arguments: LDL^T of the row-skyline
+ * matrix ALTri (ASize values, row ranges ARange(0:n)) overwritten in place, on the GPU. */
+int astro_ldl_fact(astro_ctx *ctx, double *a_l_tri, int32_t a_size, const int32_t *a_range,
+                   int32_t n);
+/* Factorises the device-resident skyline built by astro_convert_to_ltri, in place. */
+int astro_ldl_fact_resident(astro_ctx *ctx);
+
+/* solveSparseLDLFact (Working/AStrO_solvers.f90:83-126), same arguments: solves
+ * L D L^T soln = rhs with a factor from getSparseLDLFact.  z_vec (Ldim) is scratch. */
+int astro_ldl_solve(astro_ctx *ctx, double *soln, const double *rhs, const double *l_mat,
+                    int32_t l_size, const int32_t *l_range, int32_t l_dim, double *z_vec);
+
+/* gMRes (Working/AStrO_solvers.f90:128-297), same arguments: restarted, left-preconditioned
+ * GMRES(numVecs) on A = Amat + Cmat^T Cmat with the skyline LDL^T factor Pmat as
+ * preconditioner, convergence when the preconditioned residual norm is <= 1e-12 (single
+ * precision literal, as the reference) or after maxIt/numVecs+1 restarts.  x_vec is the
+ * initial guess on entry and the solution on exit. */
+int astro_gmres(astro_ctx *ctx, double *x_vec, const double *a_mat, const int32_t *a_cols,
+                const int32_t *a_range, int32_t a_size, int32_t a_dim, const double *c_mat,
+                const int32_t *c_cols, const int32_t *c_range, int32_t c_size, int32_t c_dim,
+                const double *p_mat, const int32_t *p_range, int32_t p_size,
+                const double *b_vec, int32_t num_vecs, int32_t max_it);
+
+/* North-star static solve of (K + C^T C) u = f with device-resident K (from astro_el_soln_load
+ * or astro_assemble_fp32) and scaled C.  f and u are host arrays in global DOF numbering;
+ * u is the initial guess on entry.  Convergence is judged by the FP64 true relative residual. */
+int astro_solve_static(astro_ctx *ctx, const double *f, double *u, const astro_solve_opts *opts,
+                       astro_solve_stats *stats);
+
+/* y = (K + C^T C) x for host vectors in global DOF numbering, with the device-resident K
+ * (kind 64: FP64 values from astro_el_soln_load, 32: FP32 values from astro_assemble_fp32) and
+ * the scaled constraints; the operator of the gMRes matvec (Working/AStrO_solvers.f90:143-169). */
+int astro_apply_operator(astro_ctx *ctx, int32_t kind, const double *x, double *y);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ASTRO_GPU_H */

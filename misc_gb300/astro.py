@@ -1,0 +1,294 @@
+"""Host-side mirror of AStrO's hot-path subroutines over the GB300 C ABI (include/astro_gpu.h).
+
+Method names follow the Fortran subroutines they replace (Working/AStrO_commandFunctions.f90,
+Working/AStrO_solvers.f90, Working/AStrO_bookKeeping.f90); arrays use the reference's numbering
+(1-based DOF numbers, range arrays with lower bound 0, CSR column 0 = empty slot).  Everything
+runs in libastro_gpu.so on the GPU; there is no CPU fallback: a missing library or device raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .model import AstroStateC, Model, make_state
+
+I32P = C.POINTER(C.c_int32)
+F64P = C.POINTER(C.c_double)
+
+ASTRO_OK = 0
+ERRORS = {1: "ASTRO_ERR_ARG", 2: "ASTRO_ERR_CUDA", 3: "ASTRO_ERR_UNSUPPORTED", 4: "ASTRO_ERR_PIVOT",
+          5: "ASTRO_ERR_NAN", 6: "ASTRO_ERR_BREAKDOWN", 7: "ASTRO_ERR_MAXIT", 8: "ASTRO_ERR_STATE",
+          9: "ASTRO_ERR_NOMEM"}
+SOLVER_GMRES_JACOBI_FP64 = 0
+SOLVER_FGMRES_MIXED = 1
+SOLVER_FGMRES_LEARNED = 2
+
+_LIB = None
+
+
+class AstroError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class DimsC(C.Structure):
+    _fields_ = [(k, C.c_int32) for k in ("el_mat_dim", "el_mat_size", "el_mat_lt_size", "el_mpc_dim", "el_mpc_size",
+                                         "int_vec_size", "int_mat_size", "solver_max_bw", "dof_per_node",
+                                         "num_blocks", "num_colors")]
+
+
+class SolveOptsC(C.Structure):
+    _fields_ = [("method", C.c_int32), ("restart", C.c_int32), ("max_iters", C.c_int32), ("rtol", C.c_double),
+                ("inner_rtol", C.c_double)]
+
+
+class SolveStatsC(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("restarts", C.c_int32), ("refinements", C.c_int32),
+                ("status", C.c_int32), ("rel_residual", C.c_double), ("seconds", C.c_double)]
+
+
+def lib_path():
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libastro_gpu.so")
+
+
+def load_library():
+    """Loads the in-tree libastro_gpu.so (built by misc_gb300/build.py or __graft_entry__.build())."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    p = lib_path()
+    if not os.path.exists(p):
+        raise RuntimeError(f"libastro_gpu.so not built ({p}); run __graft_entry__.build()")
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    sig = {
+        "astro_ctx_create": ([vp, C.POINTER(vp)], C.c_int),
+        "astro_ctx_destroy": ([vp], C.c_int),
+        "astro_last_error": ([vp, C.c_char_p, C.c_int32], C.c_int),
+        "astro_get_dims": ([vp, C.POINTER(DimsC)], C.c_int),
+        "astro_get_prep": ([vp, I32P, I32P, I32P, I32P, I32P, I32P, F64P, F64P], C.c_int),
+        "astro_el_soln_load": ([vp, C.c_int32, vp, F64P, F64P, F64P, I32P, F64P], C.c_int),
+        "astro_assemble_fp32": ([vp], C.c_int),
+        "astro_assemble_fp32_async": ([vp], C.c_int),
+        "astro_element_matrices": ([vp, C.c_int32, vp, F64P, F64P], C.c_int),
+        "astro_drdd_complex": ([vp, C.c_int32, C.c_double, vp, F64P, F64P], C.c_int),
+        "astro_scale_mpc": ([vp, F64P, F64P], C.c_int),
+        "astro_constraint_load": ([vp, F64P, F64P], C.c_int),
+        "astro_surface_load": ([vp, C.c_int32, I32P, I32P, F64P, C.c_double, F64P], C.c_int),
+        "astro_convert_to_ltri": ([vp, F64P], C.c_int),
+        "astro_ldl_fact": ([vp, F64P, C.c_int32, I32P, C.c_int32], C.c_int),
+        "astro_ldl_fact_resident": ([vp], C.c_int),
+        "astro_ldl_solve": ([vp, F64P, F64P, F64P, C.c_int32, I32P, C.c_int32, F64P], C.c_int),
+        "astro_gmres": ([vp, F64P, F64P, I32P, I32P, C.c_int32, C.c_int32, F64P, I32P, I32P, C.c_int32, C.c_int32,
+                         F64P, I32P, C.c_int32, F64P, C.c_int32, C.c_int32], C.c_int),
+        "astro_solve_static": ([vp, F64P, F64P, C.POINTER(SolveOptsC), C.POINTER(SolveStatsC)], C.c_int),
+        "astro_apply_operator": ([vp, C.c_int32, F64P, F64P], C.c_int),
+        "astro_ctx_stream": ([vp], C.c_void_p),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _LIB = L
+    return L
+
+
+def _p(a, t):
+    return C.cast(None, t) if a is None else a.ctypes.data_as(t)
+
+
+def _d(a):
+    return _p(a, F64P)
+
+
+def _i(a):
+    return _p(a, I32P)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class AstroGPU:
+    """One model resident on the GPU (astro_ctx).  Construction runs analysisPrep."""
+
+    def __init__(self, model: Model):
+        self.L = load_library()
+        self.model = model
+        self._mc = model.as_c()
+        h = C.c_void_p()
+        rc = self.L.astro_ctx_create(C.byref(self._mc), C.byref(h))
+        if rc != ASTRO_OK:
+            raise AstroError(rc, self._err(None))
+        self.h = h
+        d = DimsC()
+        self._check(self.L.astro_get_dims(self.h, C.byref(d)))
+        self.dims = d
+        self.n = d.el_mat_dim
+        self.el_mat_size = d.el_mat_size
+        self.lt_size = d.el_mat_lt_size
+        self.mpc_dim = d.el_mpc_dim
+        self.mpc_size = d.el_mpc_size
+        self.int_vec_size = d.int_vec_size
+        self.int_mat_size = d.int_mat_size
+        self.solver_max_bw = d.solver_max_bw
+        N = model.num_nodes
+        self.current_rank = np.zeros(N, np.int32)
+        self.n_dof_index = np.zeros((N, 6), np.int32)
+        self.el_mat_range = np.zeros(self.n + 1, np.int32)
+        self.lt_range = np.zeros(self.n + 1, np.int32)
+        self.mpc_range = np.zeros(self.mpc_dim + 1, np.int32)
+        self.mpc_cols = np.zeros(max(self.mpc_size, 1), np.int32)
+        self.mpc_mat = np.zeros(max(self.mpc_size, 1))
+        self.mpc_rhs = np.zeros(max(self.mpc_dim, 1))
+        self._check(self.L.astro_get_prep(self.h, _i(self.current_rank), _i(self.n_dof_index), _i(self.el_mat_range),
+                                          _i(self.lt_range), _i(self.mpc_range), _i(self.mpc_cols),
+                                          _d(self.mpc_mat), _d(self.mpc_rhs)))
+
+    # -- plumbing -------------------------------------------------------------------------------
+    def _err(self, h):
+        buf = C.create_string_buffer(512)
+        self.L.astro_last_error(h, buf, 512)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc, allow=()):
+        if rc != ASTRO_OK and rc not in allow:
+            raise AstroError(rc, self._err(self.h))
+        return rc
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.astro_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- getElasticSolnLoad -----------------------------------------------------------------------
+    def getElasticSolnLoad(self, buildMat=1, state=None, elastic_load=None, int_elastic_load=None, export=True):
+        """Working/AStrO_commandFunctions.f90:260.  Returns (elasticLoad, intElasticLoad, elasticMat,
+        elMatCols, intElasticMat); loads are accumulated (-= Ru) into the given arrays."""
+        load = np.zeros(self.n) if elastic_load is None else elastic_load
+        iload = np.zeros(max(self.int_vec_size, 1)) if int_elastic_load is None else int_elastic_load
+        mat = cols = imat = None
+        if buildMat == 1 and export:
+            mat = np.zeros(self.el_mat_size)
+            cols = np.zeros(self.el_mat_size, np.int32)
+            imat = np.zeros(max(self.int_mat_size, 1))
+        self._check(self.L.astro_el_soln_load(self.h, buildMat, C.byref(state) if state is not None else None,
+                                              _d(load), _d(iload), _d(mat), _i(cols), _d(imat)))
+        return load, iload, mat, cols, imat
+
+    def assemble_fp32(self):
+        self._check(self.L.astro_assemble_fp32(self.h))
+
+    def element_matrices(self, precision=64, state=None, with_residual=False):
+        E = self.model.num_els
+        ke = np.zeros((E, 24, 24))
+        ru = np.zeros((E, 24)) if with_residual else None
+        self._check(self.L.astro_element_matrices(self.h, precision, C.byref(state) if state is not None else None,
+                                                  _d(ke), _d(ru)))
+        ke = np.transpose(ke, (0, 2, 1)).copy()  # column-major per element
+        return (ke, ru) if with_residual else ke
+
+    # -- constraints and loads ------------------------------------------------------------------
+    def scaleElasticMPC(self):
+        mm = np.zeros(max(self.mpc_size, 1))
+        mr = np.zeros(max(self.mpc_dim, 1))
+        self._check(self.L.astro_scale_mpc(self.h, _d(mm), _d(mr)))
+        return mm[:self.mpc_size], mr[:self.mpc_dim]
+
+    def getElasticConstraintLoad(self, node_disp, elastic_load):
+        self._check(self.L.astro_constraint_load(self.h, _d(_f64(node_disp)) if node_disp is not None else None,
+                                                 _d(elastic_load)))
+        return elastic_load
+
+    def surface_load(self, face_el, face_num, traction=(0.0, 0.0, 0.0), pressure=0.0, elastic_load=None):
+        load = np.zeros(self.n) if elastic_load is None else elastic_load
+        fe, fn = _i32(face_el), _i32(face_num)
+        tr = _f64(traction)
+        self._check(self.L.astro_surface_load(self.h, len(fe), _i(fe), _i(fn), _d(tr), float(pressure), _d(load)))
+        return load
+
+    def applied_load(self, load=None):
+        """Consistent surface load of the model's faces plus its point loads (getElasticAppliedLoad)."""
+        m = self.model
+        load = np.zeros(self.n) if load is None else load
+        if len(m.face_el):
+            self.surface_load(m.face_el, m.face_num, m.traction, m.pressure, load)
+        for nd, dof, v in m.point_loads:
+            load[self.n_dof_index[nd - 1, dof - 1] - 1] += v
+        return load
+
+    # -- solves ---------------------------------------------------------------------------------
+    def solve_static(self, f, u0=None, method=SOLVER_GMRES_JACOBI_FP64, restart=50, rtol=1e-10, max_iters=200000,
+                     inner_rtol=1e-4, allow_maxit=False):
+        u = np.zeros(self.n) if u0 is None else _f64(u0).copy()
+        o = SolveOptsC(method, restart, max_iters, rtol, inner_rtol)
+        st = SolveStatsC()
+        rc = self.L.astro_solve_static(self.h, _d(_f64(f)), _d(u), C.byref(o), C.byref(st))
+        self._check(rc, allow=(7,) if allow_maxit else ())
+        return u, st
+
+    def apply_operator(self, x, kind=64):
+        y = np.zeros(self.n)
+        self._check(self.L.astro_apply_operator(self.h, kind, _d(_f64(x)), _d(y)))
+        return y
+
+    def convertToLTri(self):
+        lt = np.zeros(self.lt_size)
+        self._check(self.L.astro_convert_to_ltri(self.h, _d(lt)))
+        return lt
+
+    def getSparseLDLFact(self, a_l_tri, a_range):
+        a = _f64(a_l_tri).copy()
+        r = _i32(a_range)
+        self._check(self.L.astro_ldl_fact(self.h, _d(a), len(a), _i(r), len(r) - 1))
+        return a
+
+    def solveSparseLDLFact(self, rhs, l_mat, l_range):
+        n = len(l_range) - 1
+        x = np.zeros(n)
+        z = np.zeros(n)
+        lm = _f64(l_mat)
+        self._check(self.L.astro_ldl_solve(self.h, _d(x), _d(_f64(rhs)), _d(lm), len(lm), _i(_i32(l_range)), n, _d(z)))
+        return x
+
+    def gMRes(self, x_vec, a_mat, a_cols, a_range, c_mat, c_cols, c_range, p_mat, p_range, b_vec, num_vecs, max_it):
+        x = _f64(x_vec).copy()
+        am, ac, ar = _f64(a_mat), _i32(a_cols), _i32(a_range)
+        cm, cc, cr = _f64(c_mat), _i32(c_cols), _i32(c_range)
+        pm, pr = _f64(p_mat), _i32(p_range)
+        self._check(self.L.astro_gmres(self.h, _d(x), _d(am), _i(ac), _i(ar), len(am), len(ar) - 1, _d(cm), _i(cc),
+                                       _i(cr), len(cm), len(cr) - 1, _d(pm), _i(pr), len(pm), _d(_f64(b_vec)),
+                                       num_vecs, max_it))
+        return x
+
+    def getdRelasticdD(self, dvar, h=1e-30, state=None):
+        out = np.zeros(self.n)
+        iout = np.zeros(max(self.int_vec_size, 1))
+        self._check(self.L.astro_drdd_complex(self.h, dvar, h, C.byref(state) if state is not None else None,
+                                              _d(out), _d(iout)))
+        return out, iout
+
+    # -- convenience ----------------------------------------------------------------------------
+    def static_rhs(self, mpc_rhs_scaled=True):
+        """b = constraint load (zero displacement) + applied load, after scaleElasticMPC."""
+        b = np.zeros(self.n)
+        self.getElasticConstraintLoad(np.zeros(self.n), b)
+        self.applied_load(b)
+        return b
+
+
+__all__ = ["AstroGPU", "AstroError", "load_library", "make_state", "AstroStateC", "SOLVER_GMRES_JACOBI_FP64",
+           "SOLVER_FGMRES_MIXED", "SOLVER_FGMRES_LEARNED"]

@@ -1,0 +1,130 @@
+// Internal state of the GB300 library behind include/astro_gpu.h.
+//
+// Data layout in HBM (one context = one model on one GPU):
+//   * nodes are renumbered by the reference's breadth-first ordering (currentRank); all device
+//     vectors are node-major by rank: x[(rank-1)*dpn + c], dpn = DOF per node (3 solid, 6 shell);
+//   * the stiffness lives as a block-CSR (BSR) matrix over node ranks with dpn x dpn row-major
+//     blocks, block columns sorted by rank; FP64 values (faithful path) and/or FP32 values
+//     (mixed-precision path);
+//   * elements are stored in colour-major order: elements of one colour share no node, so a
+//     colour's element matrices are added into the BSR without atomics (deterministic);
+//   * the reference's scalar CSR (component-major DOF numbering, find-or-insert column order) is
+//     produced only on export through a per-block position table.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/astro_gpu.h"
+
+#define ASTRO_MAX_COLORS 64
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+template <class T> static inline T *dptr(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
+
+struct AstroPrep {
+    // reference analysisPrep outputs (1-based values, as the Fortran)
+    int N = 0, E = 0, dpn = 0, n = 0;
+    int solverMaxBW = 0;
+    std::vector<int> currentRank, originalRank, nDofIndex;  // nDofIndex(6,N)
+    std::vector<int> elMatRange, elMatLTRange;
+    int elMatSize = 0, ltSize = 0;
+    std::vector<int> intVecRange, intMatRange;
+    int intVecSize = 0, intMatSize = 0;
+    // node adjacency in the reference's first-seen order (nodalConn without empty slots)
+    std::vector<int> adjPtr, adj;  // 1-based node ids
+    // block CSR over ranks (0-based)
+    std::vector<int> bRowPtr, bCol;
+    int nb = 0;
+    // per element: block index of local node pair (a,b), npe x npe
+    int npe = 0;
+    std::vector<int> elBlk;
+    // colouring
+    int ncolors = 0;
+    std::vector<int> colorPtr, colorEls;  // colorEls: 0-based element ids grouped by colour
+    // reference CSR position of each (block, column component): elMatRange(dof-1) excluded, i.e.
+    // position within the row, 0-based; size nb*dpn
+    std::vector<int> csrPosInRow;
+    // constraints (reference DOF numbering, 1-based columns, 0 = empty slot)
+    int mpcDim = 0, mpcSize = 0;
+    std::vector<int> mpcRange, mpcCols;
+    std::vector<double> mpcMat, mpcRhs;
+};
+
+struct astro_ctx {
+    std::string err;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    AstroPrep P;
+    // host model copy
+    std::vector<double> nodes;  // (N,3)
+    std::vector<int> elist;     // (E,8)
+    std::vector<int> etype, esec;
+    std::vector<double> elMat;  // per element materialElastic(9) (solids)
+    std::vector<double> secABD, secMass;  // per section ABD(9,9), sMass(6,6) (shells)
+    std::vector<double> secOrient;        // per section 3x3 column-major
+    std::vector<double> elThickness;      // per element total shell thickness (complex step / loads)
+    int hasShell = 0, hasSolid = 0;
+    int orientIdentity = 1;
+    // device model
+    DevBuf d_nodes, d_elist, d_elMat, d_esec, d_secABD, d_secOrient, d_colorEls, d_elBlk;
+    DevBuf d_rank;          // currentRank (N) 1-based
+    DevBuf d_bRowPtr, d_bCol, d_bRow, d_etype;
+    DevBuf d_K64, d_K32;    // BSR values
+    int haveK64 = 0, haveK32 = 0;
+    DevBuf d_csrPos, d_elMatRangeRank;  // export tables
+    DevBuf d_intMat;        // condensed internal rows (shell), E*256 doubles
+    // constraints on device (internal DOF numbering)
+    DevBuf d_mpcRange, d_mpcCol, d_mpcVal, d_mpcRhs;
+    int mpcScaled = 0;
+    // penalty C^T C as CSR over internal rows (host-built after scaling)
+    DevBuf d_penRow, d_penPtr, d_penCol, d_penVal;
+    int penRows = 0;
+    std::vector<double> mpcScaledHost, mpcRhsScaledHost;
+    // skyline (reference DOF numbering) on device
+    DevBuf d_ltRange, d_lt;
+    int haveLT = 0, ltFactored = 0;
+    // scratch
+    DevBuf d_scratch;
+    DevBuf d_status;  // int status words written by kernels
+    int quirkShellMeanRot = 0;
+};
+
+// error helpers
+int set_err(astro_ctx *c, int code, const std::string &msg);
+int cuda_check(astro_ctx *c, cudaError_t e, const char *what);
+#define CK(call)                                                  \
+    do {                                                          \
+        cudaError_t e__ = (call);                                 \
+        if (e__ != cudaSuccess) return cuda_check(ctx, e__, #call); \
+    } while (0)
+
+int dev_alloc(astro_ctx *c, DevBuf &b, size_t bytes);
+void dev_free(DevBuf &b);
+int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes);
+
+// host analysis preparation (prep.cpp)
+int astro_prep_build(astro_ctx *c, const astro_model *m);
+
+// kernels' host entry points
+int launch_hex8_assemble(astro_ctx *ctx, int precision, int store);           // elem_hex8.cu
+int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *ke_host); // elem_hex8.cu
+int launch_shell4_assemble(astro_ctx *ctx, const astro_state *s, double *d_loadInt, double *d_intLoad,
+                           int buildMat, double *ke_host, double *ru_host);  // elem_shell4.cu
+int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // elem_shell4.cu
+int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu
+int export_csr(astro_ctx *ctx, double *elastic_mat, int32_t *el_mat_cols);  // assemble.cu
+double bsr_absmax(astro_ctx *ctx, int *status);                             // assemble.cu
+int ref_to_int_vec(astro_ctx *ctx, const double *d_ref, double *d_int, int n); // assemble.cu
+int int_to_ref_vec(astro_ctx *ctx, const double *d_int, double *d_ref, int n); // assemble.cu
+int surface_load_dev(astro_ctx *ctx, int nf, const int *d_faceEl, const int *d_faceNum, const double *tr,
+                     double pressure, double *d_loadInt);                   // assemble.cu
+int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt);       // elem_hex8.cu
+int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru);   // elem_hex8.cu

@@ -1,0 +1,583 @@
+// C-ABI entry points (include/astro_gpu.h): context life cycle, model upload, and the
+// reference-facing calls (getElasticSolnLoad, scaleElasticMPC, getElasticConstraintLoad, the
+// surface load, the static solve).  Host arrays use the reference's numbering; device arrays
+// use the rank-major layout described in astro_internal.h.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+
+#include "astro_internal.h"
+
+static std::mutex g_err_mu;
+static std::string g_create_err;
+
+int set_err(astro_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    else {
+        std::lock_guard<std::mutex> g(g_err_mu);
+        g_create_err = msg;
+    }
+    return code;
+}
+
+int cuda_check(astro_ctx *c, cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return ASTRO_OK;
+    return set_err(c, e == cudaErrorMemoryAllocation ? ASTRO_ERR_NOMEM : ASTRO_ERR_CUDA,
+                   std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int dev_alloc(astro_ctx *c, DevBuf &b, size_t bytes) {
+    dev_free(b);
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        return cuda_check(c, e, "cudaMalloc");
+    }
+    b.bytes = bytes;
+    return ASTRO_OK;
+}
+
+void dev_free(DevBuf &b) {
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+}
+
+int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
+    int rc = dev_alloc(c, b, bytes);
+    if (rc) return rc;
+    if (bytes) {
+        cudaError_t e = cudaMemcpy(b.p, h, bytes, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_check(c, e, "upload");
+    }
+    return ASTRO_OK;
+}
+
+static void free_all(astro_ctx *c) {
+    DevBuf *bufs[] = {&c->d_nodes,  &c->d_elist,   &c->d_elMat,   &c->d_esec,    &c->d_secABD,   &c->d_secOrient,
+                      &c->d_colorEls, &c->d_elBlk, &c->d_rank,    &c->d_bRowPtr, &c->d_bCol,     &c->d_bRow,
+                      &c->d_etype,  &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
+                      &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
+                      &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
+                      &c->d_status};
+    for (DevBuf *b : bufs) dev_free(*b);
+}
+
+// internal (rank-major) index of reference DOF d (1-based)
+static inline int ref2int(const AstroPrep &P, int d) {
+    const int c = (d - 1) / P.N, r = (d - 1) % P.N;
+    return r * P.dpn + c;
+}
+
+extern "C" int astro_last_error(const astro_ctx *ctx, char *buf, int32_t len) {
+    if (!buf || len <= 0) return ASTRO_ERR_ARG;
+    std::string s;
+    if (ctx) s = ctx->err;
+    else {
+        std::lock_guard<std::mutex> g(g_err_mu);
+        s = g_create_err;
+    }
+    std::strncpy(buf, s.c_str(), (size_t)len - 1);
+    buf[len - 1] = 0;
+    return ASTRO_OK;
+}
+
+extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
+    if (!m || !out) return set_err(nullptr, ASTRO_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (m->num_nodes <= 0 || m->num_els <= 0 || !m->node_list || !m->element_list || !m->element_type ||
+        !m->element_section)
+        return set_err(nullptr, ASTRO_ERR_ARG, "model has no nodes/elements");
+    int ndev = 0;
+    cudaError_t ce = cudaGetDeviceCount(&ndev);
+    if (ce != cudaSuccess || ndev == 0)
+        return set_err(nullptr, ASTRO_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(ce));
+    astro_ctx *ctx = new astro_ctx();
+    int rc = astro_prep_build(ctx, m);
+    if (rc) {
+        set_err(nullptr, rc, ctx->err);
+        delete ctx;
+        return rc;
+    }
+    AstroPrep &P = ctx->P;
+    cudaGetDevice(&ctx->device);
+    if ((ce = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        set_err(nullptr, ASTRO_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(ce));
+        delete ctx;
+        return ASTRO_ERR_CUDA;
+    }
+    // host model copies
+    ctx->nodes.assign(m->node_list, m->node_list + 3 * (size_t)P.N);
+    ctx->elist.assign(m->element_list, m->element_list + 8 * (size_t)P.E);
+    ctx->etype.assign(m->element_type, m->element_type + P.E);
+    ctx->esec.assign(m->element_section, m->element_section + P.E);
+    const int S = m->num_sections;
+    ctx->secOrient.assign(9 * (size_t)std::max(S, 1), 0.0);
+    for (int s = 0; s < S; ++s)
+        for (int k = 0; k < 9; ++k) ctx->secOrient[9 * s + k] = m->section_orient[9 * s + k];
+    auto fail = [&](int code, const std::string &msg) {
+        set_err(nullptr, code, msg);
+        free_all(ctx);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        delete ctx;
+        return code;
+    };
+    for (int e = 0; e < P.E; ++e) {
+        int s = ctx->esec[e];
+        if (s < 1 || s > S) return fail(ASTRO_ERR_ARG, "element_section out of range");
+    }
+    if (ctx->hasSolid) {
+        ctx->elMat.resize(9 * (size_t)P.E);
+        std::vector<double> orientEl(9 * (size_t)P.E);
+        for (int e = 0; e < P.E; ++e) {
+            int s = ctx->esec[e];
+            int mat = m->section_mat_id[s - 1];
+            if (mat < 1 || mat > m->num_materials) return fail(ASTRO_ERR_ARG, "section material out of range");
+            for (int k = 0; k < 9; ++k) ctx->elMat[9 * (size_t)e + k] = m->material_elastic[9 * (size_t)(mat - 1) + k];
+            for (int k = 0; k < 9; ++k) {
+                double v = ctx->secOrient[9 * (s - 1) + k];
+                orientEl[9 * (size_t)e + k] = v;
+                if (v != ((k % 4 == 0) ? 1.0 : 0.0)) ctx->orientIdentity = 0;
+            }
+        }
+        if ((rc = upload(ctx, ctx->d_elMat, ctx->elMat.data(), sizeof(double) * ctx->elMat.size())))
+            return fail(rc, ctx->err);
+        if ((rc = upload(ctx, ctx->d_secOrient, orientEl.data(), sizeof(double) * orientEl.size())))
+            return fail(rc, ctx->err);
+    }
+    if (m->num_dvars > 0) {
+        for (int d = 0; d < m->num_dvars; ++d) {
+            int cat = m->d_category[d];
+            if (cat != ASTRO_DCAT_LAYUP_THICKNESS && cat != ASTRO_DCAT_ELASTIC_MODULUS)
+                return fail(ASTRO_ERR_UNSUPPORTED, "design-variable category not supported");
+        }
+    }
+    // device structures
+    std::vector<int> rank1(P.N), bRow(P.nb), colorEls(P.colorEls);
+    for (int a = 1; a <= P.N; ++a) rank1[a - 1] = P.currentRank[a];
+    for (int r = 0; r < P.N; ++r)
+        for (int k = P.bRowPtr[r]; k < P.bRowPtr[r + 1]; ++k) bRow[k] = r;
+#define UP(buf, vec)                                                                          \
+    if ((rc = upload(ctx, ctx->buf, (vec).data(), sizeof((vec)[0]) * (vec).size()))) return fail(rc, ctx->err);
+    UP(d_nodes, ctx->nodes);
+    UP(d_elist, ctx->elist);
+    UP(d_etype, ctx->etype);
+    UP(d_esec, ctx->esec);
+    UP(d_rank, rank1);
+    UP(d_bRowPtr, P.bRowPtr);
+    UP(d_bCol, P.bCol);
+    UP(d_bRow, bRow);
+    UP(d_colorEls, colorEls);
+    UP(d_elBlk, P.elBlk);
+    UP(d_csrPos, P.csrPosInRow);
+    UP(d_elMatRangeRank, P.elMatRange);
+#undef UP
+    if ((rc = dev_alloc(ctx, ctx->d_status, 256))) return fail(rc, ctx->err);
+    cudaMemset(ctx->d_status.p, 0, 256);
+    if (ctx->hasShell && (rc = shell_sections_prepare(ctx, m))) return fail(rc, ctx->err);
+    // unscaled constraints in internal numbering
+    ctx->mpcScaledHost = P.mpcMat;
+    ctx->mpcRhsScaledHost = P.mpcRhs;
+    *out = ctx;
+    return ASTRO_OK;
+}
+
+extern "C" int astro_ctx_destroy(astro_ctx *ctx) {
+    if (!ctx) return ASTRO_OK;
+    cudaStreamSynchronize(ctx->stream);
+    free_all(ctx);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return ASTRO_OK;
+}
+
+extern "C" int astro_get_dims(const astro_ctx *ctx, astro_dims *o) {
+    if (!ctx || !o) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    o->el_mat_dim = P.n;
+    o->el_mat_size = P.elMatSize;
+    o->el_mat_lt_size = P.ltSize;
+    o->el_mpc_dim = P.mpcDim;
+    o->el_mpc_size = P.mpcSize;
+    o->int_vec_size = P.intVecSize;
+    o->int_mat_size = P.intMatSize;
+    o->solver_max_bw = P.solverMaxBW;
+    o->dof_per_node = P.dpn;
+    o->num_blocks = P.nb;
+    o->num_colors = P.ncolors;
+    return ASTRO_OK;
+}
+
+extern "C" void *astro_ctx_stream(const astro_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+extern "C" int astro_get_prep(const astro_ctx *ctx, int32_t *current_rank, int32_t *n_dof_index, int32_t *el_mat_range,
+                              int32_t *el_mat_lt_range, int32_t *mpc_range, int32_t *mpc_cols, double *mpc_mat,
+                              double *mpc_rhs) {
+    if (!ctx) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    if (current_rank) std::copy(P.currentRank.begin() + 1, P.currentRank.end(), current_rank);
+    if (n_dof_index) std::copy(P.nDofIndex.begin(), P.nDofIndex.end(), n_dof_index);
+    if (el_mat_range) std::copy(P.elMatRange.begin(), P.elMatRange.end(), el_mat_range);
+    if (el_mat_lt_range) std::copy(P.elMatLTRange.begin(), P.elMatLTRange.end(), el_mat_lt_range);
+    if (mpc_range) std::copy(P.mpcRange.begin(), P.mpcRange.end(), mpc_range);
+    if (mpc_cols) std::copy(P.mpcCols.begin(), P.mpcCols.end(), mpc_cols);
+    if (mpc_mat) std::copy(P.mpcMat.begin(), P.mpcMat.end(), mpc_mat);
+    if (mpc_rhs) std::copy(P.mpcRhs.begin(), P.mpcRhs.end(), mpc_rhs);
+    return ASTRO_OK;
+}
+
+static int ensure_K(astro_ctx *ctx, int which) {
+    const size_t nv = (size_t)ctx->P.nb * ctx->P.dpn * ctx->P.dpn;
+    int rc;
+    if ((which & 2) && !ctx->d_K64.p && (rc = dev_alloc(ctx, ctx->d_K64, nv * sizeof(double)))) return rc;
+    if ((which & 1) && !ctx->d_K32.p && (rc = dev_alloc(ctx, ctx->d_K32, nv * sizeof(float)))) return rc;
+    return ASTRO_OK;
+}
+
+// state vectors (reference numbering, host) -> internal layout on the device
+struct DevState {
+    DevBuf disp, vel, acc, pdisp, pvel, pacc, idisp, pidisp;
+    ~DevState() {
+        DevBuf *b[] = {&disp, &vel, &acc, &pdisp, &pvel, &pacc, &idisp, &pidisp};
+        for (auto *x : b) dev_free(*x);
+    }
+};
+
+static int state_vec_up(astro_ctx *ctx, const double *h, DevBuf &dst) {
+    if (!h) return ASTRO_OK;
+    const int n = ctx->P.n;
+    DevBuf tmp;
+    int rc = upload(ctx, tmp, h, sizeof(double) * n);
+    if (!rc) rc = dev_alloc(ctx, dst, sizeof(double) * n);
+    if (!rc) rc = ref_to_int_vec(ctx, dptr<double>(tmp), dptr<double>(dst), n);
+    if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "state upload");
+    dev_free(tmp);
+    return rc;
+}
+
+extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro_state *state, double *elastic_load,
+                                  double *int_elastic_load, double *elastic_mat, int32_t *el_mat_cols,
+                                  double *int_elastic_mat) {
+    if (!ctx || !elastic_load) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    const int n = P.n;
+    int rc;
+    DevState S;
+    if (state) {
+        if ((rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
+        if (ctx->hasShell) {
+            if ((rc = state_vec_up(ctx, state->prev_disp, S.pdisp))) return rc;
+            if ((rc = state_vec_up(ctx, state->prev_vel, S.pvel))) return rc;
+            if ((rc = state_vec_up(ctx, state->prev_acc, S.pacc))) return rc;
+        }
+    }
+    DevBuf dl;
+    if ((rc = state_vec_up(ctx, elastic_load, dl))) return rc;
+    if (build_mat == 1) {
+        if ((rc = ensure_K(ctx, 2))) return rc;
+        if ((rc = bsr_zero(ctx, 2))) return rc;
+    }
+    if (ctx->hasSolid) {
+        rc = hex8_soln_load(ctx, build_mat == 1, S.disp.p ? dptr<double>(S.disp) : nullptr, dptr<double>(dl));
+    } else {
+        DevBuf il;
+        if (int_elastic_load && P.intVecSize) {
+            if ((rc = upload(ctx, il, int_elastic_load, sizeof(double) * P.intVecSize))) return rc;
+        }
+        rc = launch_shell4_assemble(ctx, state, dptr<double>(dl), il.p ? dptr<double>(il) : nullptr, build_mat == 1,
+                                    nullptr, nullptr);
+        if (!rc && il.p)
+            rc = cuda_check(ctx, cudaMemcpy(int_elastic_load, il.p, sizeof(double) * P.intVecSize, cudaMemcpyDeviceToHost),
+                            "int load download");
+        dev_free(il);
+    }
+    if (rc) {
+        dev_free(dl);
+        return rc;
+    }
+    if (build_mat == 1) ctx->haveK64 = 1;
+    // load back to reference numbering
+    DevBuf dref;
+    if ((rc = dev_alloc(ctx, dref, sizeof(double) * n))) return rc;
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(dl), dptr<double>(dref), n))) return rc;
+    CK(cudaMemcpyAsync(elastic_load, dref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    dev_free(dref);
+    dev_free(dl);
+    if (build_mat == 1 && elastic_mat) {
+        if ((rc = export_csr(ctx, elastic_mat, el_mat_cols))) return rc;
+    }
+    if (build_mat == 1 && int_elastic_mat && P.intMatSize && ctx->d_intMat.p) {
+        CK(cudaMemcpy(int_elastic_mat, ctx->d_intMat.p, sizeof(double) * P.intMatSize, cudaMemcpyDeviceToHost));
+    }
+    ctx->mpcScaled = 0;
+    ctx->haveLT = 0;
+    ctx->ltFactored = 0;
+    return ASTRO_OK;
+}
+
+extern "C" int astro_assemble_fp32(astro_ctx *ctx) {
+    if (!ctx) return ASTRO_ERR_ARG;
+    if (!ctx->hasSolid) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 assembly is implemented for brick8 meshes");
+    int rc;
+    if ((rc = ensure_K(ctx, 1))) return rc;
+    if ((rc = bsr_zero(ctx, 1))) return rc;
+    if ((rc = launch_hex8_assemble(ctx, 32, 1))) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->haveK32 = 1;
+    return ASTRO_OK;
+}
+
+// Timed-path variant used by the benchmark: assembly only, no synchronisation.
+extern "C" int astro_assemble_fp32_async(astro_ctx *ctx) {
+    if (!ctx || !ctx->d_K32.p) return ASTRO_ERR_STATE;
+    int rc = bsr_zero(ctx, 1);
+    if (!rc) rc = launch_hex8_assemble(ctx, 32, 1);
+    return rc;
+}
+
+extern "C" int astro_element_matrices(astro_ctx *ctx, int32_t precision, const astro_state *state, double *ke_out,
+                                      double *ru_out) {
+    if (!ctx || !ke_out || (precision != 64 && precision != 32)) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    DevBuf dk, dr;
+    int rc;
+    if ((rc = dev_alloc(ctx, dk, sizeof(double) * 576 * (size_t)P.E))) return rc;
+    if (ru_out && (rc = dev_alloc(ctx, dr, sizeof(double) * 24 * (size_t)P.E))) return rc;
+    DevState S;
+    if (state && state->node_disp && (rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
+    if (ctx->hasSolid) {
+        if (precision == 32) {
+            if (S.disp.p) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 element kernel evaluates the zero state only");
+            rc = launch_hex8_element_mats(ctx, 32, dptr<double>(dk));
+        } else {
+            rc = hex8_element_mats_state(ctx, S.disp.p ? dptr<double>(S.disp) : nullptr, dptr<double>(dk),
+                                         dr.p ? dptr<double>(dr) : nullptr);
+        }
+    } else {
+        if (precision == 32) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 shell kernel not provided");
+        rc = launch_shell4_assemble(ctx, state, nullptr, nullptr, 1, dptr<double>(dk), dr.p ? dptr<double>(dr) : nullptr);
+    }
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ke_out, dk.p, sizeof(double) * 576 * (size_t)P.E, cudaMemcpyDeviceToHost, ctx->stream));
+    if (ru_out) CK(cudaMemcpyAsync(ru_out, dr.p, sizeof(double) * 24 * (size_t)P.E, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    dev_free(dk);
+    dev_free(dr);
+    return ASTRO_OK;
+}
+
+// Penalty matrix C^T C in internal numbering, grouped by block row.
+static int build_penalty(astro_ctx *ctx) {
+    const AstroPrep &P = ctx->P;
+    std::map<std::pair<int, int>, double> pen;
+    for (int r = 0; r < P.mpcDim; ++r)
+        for (int a = P.mpcRange[r]; a < P.mpcRange[r + 1]; ++a) {
+            if (!P.mpcCols[a]) continue;
+            const int ia = ref2int(P, P.mpcCols[a]);
+            for (int b = P.mpcRange[r]; b < P.mpcRange[r + 1]; ++b) {
+                if (!P.mpcCols[b]) continue;
+                const int ib = ref2int(P, P.mpcCols[b]);
+                pen[{ia, ib}] += ctx->mpcScaledHost[a] * ctx->mpcScaledHost[b];
+            }
+        }
+    std::vector<int> ptr(P.N + 1, 0), prow, pcol;
+    std::vector<double> pval;
+    for (auto &kv : pen) ptr[kv.first.first / P.dpn + 1]++;
+    for (int r = 0; r < P.N; ++r) ptr[r + 1] += ptr[r];
+    prow.resize(pen.size());
+    pcol.resize(pen.size());
+    pval.resize(pen.size());
+    std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    for (auto &kv : pen) {
+        int br = kv.first.first / P.dpn;
+        int t = fill[br]++;
+        prow[t] = kv.first.first % P.dpn;
+        pcol[t] = kv.first.second;
+        pval[t] = kv.second;
+    }
+    int rc;
+    ctx->penRows = (int)pen.size();
+    if ((rc = upload(ctx, ctx->d_penPtr, ptr.data(), sizeof(int) * ptr.size()))) return rc;
+    if ((rc = upload(ctx, ctx->d_penRow, prow.data(), sizeof(int) * prow.size()))) return rc;
+    if ((rc = upload(ctx, ctx->d_penCol, pcol.data(), sizeof(int) * pcol.size()))) return rc;
+    if ((rc = upload(ctx, ctx->d_penVal, pval.data(), sizeof(double) * pval.size()))) return rc;
+    return ASTRO_OK;
+}
+
+extern "C" int astro_scale_mpc(astro_ctx *ctx, double *mpc_mat, double *mpc_rhs) {
+    if (!ctx) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    double maxMat = 0.0;
+    int st = ASTRO_OK;
+    if (ctx->haveK64) {
+        maxMat = bsr_absmax(ctx, &st);
+    } else if (ctx->haveK32) {
+        // max |K| of the FP32 matrix, through an FP64 staging copy
+        const size_t nv = (size_t)P.nb * P.dpn * P.dpn;
+        std::vector<float> h(nv);
+        CK(cudaMemcpy(h.data(), ctx->d_K32.p, nv * sizeof(float), cudaMemcpyDeviceToHost));
+        for (float v : h) maxMat = std::max(maxMat, (double)std::fabs(v));
+    } else {
+        return set_err(ctx, ASTRO_ERR_STATE, "scale_mpc called before the stiffness was assembled");
+    }
+    if (st) return st;
+    ctx->mpcScaledHost = P.mpcMat;
+    ctx->mpcRhsScaledHost = P.mpcRhs;
+    for (int r = 0; r < P.mpcDim; ++r) {
+        double mag = 0.0;
+        for (int k = P.mpcRange[r]; k < P.mpcRange[r + 1]; ++k) mag += ctx->mpcScaledHost[k] * ctx->mpcScaledHost[k];
+        mag = std::sqrt(mag);
+        for (int k = P.mpcRange[r]; k < P.mpcRange[r + 1]; ++k) ctx->mpcScaledHost[k] = (1.0 / mag) * ctx->mpcScaledHost[k];
+        ctx->mpcRhsScaledHost[r] = (1.0 / mag) * ctx->mpcRhsScaledHost[r];
+    }
+    for (auto &v : ctx->mpcScaledHost) v = 100.0 * maxMat * v;
+    for (auto &v : ctx->mpcRhsScaledHost) v = 100.0 * maxMat * v;
+    int rc = build_penalty(ctx);
+    if (rc) return rc;
+    ctx->mpcScaled = 1;
+    if (mpc_mat) std::copy(ctx->mpcScaledHost.begin(), ctx->mpcScaledHost.end(), mpc_mat);
+    if (mpc_rhs) std::copy(ctx->mpcRhsScaledHost.begin(), ctx->mpcRhsScaledHost.end(), mpc_rhs);
+    return ASTRO_OK;
+}
+
+extern "C" int astro_constraint_load(astro_ctx *ctx, const double *node_disp, double *elastic_load) {
+    if (!ctx || !elastic_load) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    // tiny (one entry per constrained DOF): C^T (rhs - C u) on the host, in the reference's order
+    std::vector<double> t(ctx->mpcRhsScaledHost);
+    for (int r = 0; r < P.mpcDim; ++r)
+        for (int k = P.mpcRange[r]; k < P.mpcRange[r + 1]; ++k)
+            if (P.mpcCols[k] && node_disp) t[r] -= ctx->mpcScaledHost[k] * node_disp[P.mpcCols[k] - 1];
+    for (int r = 0; r < P.mpcDim; ++r)
+        for (int k = P.mpcRange[r]; k < P.mpcRange[r + 1]; ++k)
+            if (P.mpcCols[k]) elastic_load[P.mpcCols[k] - 1] += ctx->mpcScaledHost[k] * t[r];
+    return ASTRO_OK;
+}
+
+extern "C" int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el, const int32_t *face_num,
+                                  const double *traction, double pressure, double *elastic_load) {
+    if (!ctx || !elastic_load || nfaces < 0 || (nfaces && (!face_el || !face_num))) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    for (int f = 0; f < nfaces; ++f) {
+        int e = face_el[f], fn = face_num[f];
+        if (e < 1 || e > P.E) return set_err(ctx, ASTRO_ERR_ARG, "face element out of range");
+        int nfmax = ctx->etype[e - 1] == 8 ? 6 : 2;
+        if (fn < 1 || fn > nfmax) return set_err(ctx, ASTRO_ERR_ARG, "face number out of range");
+    }
+    double tr[3] = {0, 0, 0};
+    if (traction) std::copy(traction, traction + 3, tr);
+    DevBuf dfe, dfn, dl, dref;
+    int rc;
+    if ((rc = upload(ctx, dfe, face_el, sizeof(int) * nfaces))) return rc;
+    if ((rc = upload(ctx, dfn, face_num, sizeof(int) * nfaces))) return rc;
+    if ((rc = state_vec_up(ctx, elastic_load, dl))) return rc;
+    if ((rc = surface_load_dev(ctx, nfaces, dptr<int>(dfe), dptr<int>(dfn), tr, pressure, dptr<double>(dl)))) return rc;
+    if ((rc = dev_alloc(ctx, dref, sizeof(double) * P.n))) return rc;
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(dl), dptr<double>(dref), P.n))) return rc;
+    CK(cudaMemcpyAsync(elastic_load, dref.p, sizeof(double) * P.n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    dev_free(dfe);
+    dev_free(dfn);
+    dev_free(dl);
+    dev_free(dref);
+    return ASTRO_OK;
+}
+
+int krylov_solve_static(astro_ctx *ctx, const double *d_b, double *d_x, const astro_solve_opts *o, astro_solve_stats *st);
+int krylov_apply(astro_ctx *ctx, int kind, const double *d_x, double *d_y);
+
+extern "C" int astro_solve_static(astro_ctx *ctx, const double *f, double *u, const astro_solve_opts *opts,
+                                  astro_solve_stats *stats) {
+    if (!ctx || !f || !u || !opts) return ASTRO_ERR_ARG;
+    if (opts->rtol <= 0) return set_err(ctx, ASTRO_ERR_ARG, "rtol must be positive");
+    if (!ctx->mpcScaled && ctx->P.mpcDim > 0)
+        return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run before the solve");
+    if (opts->method == ASTRO_SOLVER_FGMRES_LEARNED)
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "learned preconditioner not available in this build");
+    const int n = ctx->P.n;
+    DevBuf db, dx;
+    int rc;
+    if ((rc = state_vec_up(ctx, f, db))) return rc;
+    if ((rc = state_vec_up(ctx, u, dx))) return rc;
+    rc = krylov_solve_static(ctx, dptr<double>(db), dptr<double>(dx), opts, stats);
+    if (rc && rc != ASTRO_ERR_MAXIT) {
+        dev_free(db);
+        dev_free(dx);
+        return rc;
+    }
+    DevBuf dref;
+    int rc2;
+    if ((rc2 = dev_alloc(ctx, dref, sizeof(double) * n))) return rc2;
+    if ((rc2 = int_to_ref_vec(ctx, dptr<double>(dx), dptr<double>(dref), n))) return rc2;
+    CK(cudaMemcpyAsync(u, dref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    dev_free(dref);
+    dev_free(db);
+    dev_free(dx);
+    return rc;
+}
+
+// y = (K + C^T C) x for host vectors in reference numbering (kind 64: FP64 K, 32: FP32 K).
+extern "C" int astro_apply_operator(astro_ctx *ctx, int32_t kind, const double *x, double *y) {
+    if (!ctx || !x || !y) return ASTRO_ERR_ARG;
+    if ((kind == 64 && !ctx->haveK64) || (kind == 32 && !ctx->haveK32)) return set_err(ctx, ASTRO_ERR_STATE, "no matrix");
+    const int n = ctx->P.n;
+    DevBuf dx, dy, dref;
+    int rc;
+    if ((rc = state_vec_up(ctx, x, dx))) return rc;
+    if ((rc = dev_alloc(ctx, dy, sizeof(double) * n))) return rc;
+    if ((rc = krylov_apply(ctx, kind, dptr<double>(dx), dptr<double>(dy)))) return rc;
+    if ((rc = dev_alloc(ctx, dref, sizeof(double) * n))) return rc;
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(dy), dptr<double>(dref), n))) return rc;
+    CK(cudaMemcpyAsync(y, dref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int i = 0; i < n; ++i) y[i] = -y[i];  // the residual kernel returned 0 - A x
+    dev_free(dx);
+    dev_free(dy);
+    dev_free(dref);
+    return ASTRO_OK;
+}
+
+// Host-only analysis preparation, callable without a GPU: the integer set-up of
+// astro_ctx_create.  Pass NULL arrays to obtain only the sizes.  el_mat_cols receives the
+// column numbers that astro_el_soln_load exports (the reference's find-or-insert order).
+extern "C" int astro_prep_host(const astro_model *m, astro_dims *dims, int32_t *current_rank, int32_t *n_dof_index,
+                               int32_t *el_mat_range, int32_t *el_mat_lt_range, int32_t *el_mat_cols,
+                               int32_t *num_colors) {
+    if (!m || !dims) return set_err(nullptr, ASTRO_ERR_ARG, "null argument");
+    astro_ctx tmp;
+    int rc = astro_prep_build(&tmp, m);
+    if (rc) return set_err(nullptr, rc, tmp.err);
+    const AstroPrep &P = tmp.P;
+    dims->el_mat_dim = P.n;
+    dims->el_mat_size = P.elMatSize;
+    dims->el_mat_lt_size = P.ltSize;
+    dims->el_mpc_dim = P.mpcDim;
+    dims->el_mpc_size = P.mpcSize;
+    dims->int_vec_size = P.intVecSize;
+    dims->int_mat_size = P.intMatSize;
+    dims->solver_max_bw = P.solverMaxBW;
+    dims->dof_per_node = P.dpn;
+    dims->num_blocks = P.nb;
+    dims->num_colors = P.ncolors;
+    if (num_colors) *num_colors = P.ncolors;
+    if (current_rank) std::copy(P.currentRank.begin() + 1, P.currentRank.end(), current_rank);
+    if (n_dof_index) std::copy(P.nDofIndex.begin(), P.nDofIndex.end(), n_dof_index);
+    if (el_mat_range) std::copy(P.elMatRange.begin(), P.elMatRange.end(), el_mat_range);
+    if (el_mat_lt_range) std::copy(P.elMatLTRange.begin(), P.elMatLTRange.end(), el_mat_lt_range);
+    if (el_mat_cols) {
+        for (int r = 0; r < P.N; ++r)
+            for (int k = P.bRowPtr[r]; k < P.bRowPtr[r + 1]; ++k)
+                for (int i = 0; i < P.dpn; ++i)
+                    for (int j = 0; j < P.dpn; ++j) {
+                        const int dofRow = r + 1 + i * P.N;
+                        const long long idx = (long long)P.elMatRange[dofRow - 1] + P.csrPosInRow[(size_t)k * P.dpn + j];
+                        el_mat_cols[idx] = P.bCol[k] + 1 + j * P.N;
+                    }
+    }
+    return ASTRO_OK;
+}

@@ -1,0 +1,365 @@
+// brick8 element stiffness/residual and colour-ordered assembly into the block-CSR matrix.
+//
+// Formulation (same quantities as r_getElRuk's solid branch, Working/AStrO_r_elementEqns.f90:
+// 2424-2530, written in block form): at each of the 2x2x2 Gauss points (+-1/sqrt(3), unit
+// weights, :363-376) with shape derivatives Nx taken in the local frame (locNds = orient *
+// globNds, :471-478; Jacobian inverse by cofactors, :212-238),
+//   ux      = sum_a disp(:,a) Nx(a,:)            (displacement gradient)
+//   strain  = Green-Lagrange strain of r_getNLStrain (:634-648), stress = C strain
+//   G       = orient + ux^T                        (the first strain derivative is Bloc(Nx_a) G)
+//   K_ab   += w detJ [ G^T Bloc(Nx_a)^T C Bloc(Nx_b) G + (Nx_a^T S Nx_b) I3 ]
+//   Ru_a   += w detJ G^T Bloc(Nx_a)^T stress
+// with S the stress tensor (second strain derivative, :663-676).  C = S^-1 of the engineering
+// constants (r_getMaterialStiffness, Working/AStrO_r_designPropertyFunctions.f90:8-80) is formed
+// per element by an unpivoted LU exactly as the reference.
+//
+// Mapping: one warp per element; lane l owns the node-pair blocks (a,b) = (l/8, l%8) and
+// (l/8+4, l%8), i.e. 18 accumulators; lanes 0..7 evaluate node a's shape data and reduce the
+// Jacobian and displacement gradient by shuffles.  Elements are processed colour by colour so a
+// colour's blocks land in disjoint block rows: plain read-add-write, no atomics, bit-reproducible.
+#include "astro_internal.h"
+
+namespace {
+
+constexpr int kWarpsPerBlock = 4;
+
+template <class T> struct Hex8Args {
+    const double *nodes;     // (N,3) by node id
+    const int *elist;        // (E,8)
+    const int *rank;         // currentRank (N) 1-based, indexed by node id - 1
+    const int *colorEls;     // element ids of this colour
+    int count;               // elements in this colour
+    const int *elBlk;        // (E,64)
+    const double *elMat;     // (E,9) engineering constants
+    const double *orient;    // (E,9) column-major orientation, or nullptr for identity
+    const double *disp;      // internal-layout displacement (rank-major, 3 per node) or nullptr
+    T *Kbsr;                 // BSR values (nb*9) or nullptr
+    double *Kbsr64;          // FP64 BSR to add into as well (FP32 kernel writing both) or nullptr
+    double *loadInt;         // internal-layout load, -= Ru (or nullptr)
+    double *keOut;           // element matrices (E, 24,24) column-major, element DOF order, or nullptr
+    double *ruOut;           // (E,24) or nullptr
+};
+
+// C = S^-1 by the reference's unpivoted LU (r_GetInvLU / r_LUFactor / r_SolveLUxb).
+template <class T> __device__ void material_c(const double *ep, T C[6][6]) {
+    T S[6][6];
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) S[i][j] = T(0);
+    T E1 = T(ep[0]), E2 = T(ep[1]), E3 = T(ep[2]);
+    S[0][0] = T(1) / E1;
+    S[0][1] = -T(ep[3]) / E1;
+    S[0][2] = -T(ep[4]) / E1;
+    S[1][1] = T(1) / E2;
+    S[1][2] = -T(ep[5]) / E2;
+    S[2][2] = T(1) / E3;
+    S[3][3] = T(1) / T(ep[6]);
+    S[4][4] = T(1) / T(ep[7]);
+    S[5][5] = T(1) / T(ep[8]);
+    for (int i = 1; i < 6; ++i)
+        for (int j = 0; j < i; ++j) S[i][j] = S[j][i];
+    // LU in place (Doolittle, no pivoting), row i1 then column i1
+    for (int i1 = 0; i1 < 6; ++i1) {
+        for (int i2 = i1; i2 < 6; ++i2)
+            for (int i3 = 0; i3 < i1; ++i3) S[i1][i2] -= S[i1][i3] * S[i3][i2];
+        T f = T(1) / S[i1][i1];
+        for (int i2 = i1 + 1; i2 < 6; ++i2) {
+            for (int i3 = 0; i3 < i1; ++i3) S[i2][i1] -= S[i2][i3] * S[i3][i1];
+            S[i2][i1] = f * S[i2][i1];
+        }
+    }
+    for (int col = 0; col < 6; ++col) {
+        T z[6], x[6];
+        for (int i = 0; i < 6; ++i) {
+            z[i] = (i == col) ? T(1) : T(0);
+            for (int k = 0; k < i; ++k) z[i] -= S[i][k] * z[k];
+        }
+        x[5] = z[5] / S[5][5];
+        for (int i = 4; i >= 0; --i) {
+            T f = T(1) / S[i][i], dp = T(0);
+            for (int k = i + 1; k < 6; ++k) dp += S[i][k] * x[k];
+            x[i] = f * (z[i] - dp);
+        }
+        for (int i = 0; i < 6; ++i) C[i][col] = x[i];
+    }
+}
+
+// M = Bloc(g)^T C Bloc(h), Bloc the 6x3 small-strain operator in Voigt order
+// [e11, e22, e33, g12, g13, g23].
+template <class T> __device__ __forceinline__ void btcb(const T C[6][6], const T g[3], const T h[3], T M[3][3]) {
+    T CB[6][3];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        CB[i][0] = C[i][0] * h[0] + C[i][3] * h[1] + C[i][4] * h[2];
+        CB[i][1] = C[i][1] * h[1] + C[i][3] * h[0] + C[i][5] * h[2];
+        CB[i][2] = C[i][2] * h[2] + C[i][4] * h[0] + C[i][5] * h[1];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        M[0][k] = g[0] * CB[0][k] + g[1] * CB[3][k] + g[2] * CB[4][k];
+        M[1][k] = g[1] * CB[1][k] + g[0] * CB[3][k] + g[2] * CB[5][k];
+        M[2][k] = g[2] * CB[2][k] + g[0] * CB[4][k] + g[1] * CB[5][k];
+    }
+}
+
+template <class T> __device__ __forceinline__ T wsum8(T v) {
+    // sum over lanes 0..7 (the other lanes hold zeros) delivered to all lanes
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+template <class T, bool GENERAL>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A) {
+    __shared__ T sNx[kWarpsPerBlock][8][3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int item = blockIdx.x * kWarpsPerBlock + w;
+    if (item >= A.count) return;
+    const int e = A.colorEls[item];
+    const int a = lane & 7;   // node handled in the per-node phase (lanes 0..7 meaningful)
+    const int bA0 = lane >> 3, bA1 = (lane >> 3) + 4, bB = lane & 7;
+    // material
+    T C[6][6];
+    material_c<T>(A.elMat + 9 * (size_t)e, C);
+    T Or[3][3];
+    if (GENERAL && A.orient) {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) Or[i][j] = T(A.orient[9 * (size_t)e + 3 * j + i]);
+    } else {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) Or[i][j] = (i == j) ? T(1) : T(0);
+    }
+    // node data (lanes 0..7)
+    const int nd = A.elist[8 * (size_t)e + a];
+    T X[3], U[3] = {T(0), T(0), T(0)};
+    {
+        T g0 = T(A.nodes[3 * (size_t)(nd - 1)]), g1 = T(A.nodes[3 * (size_t)(nd - 1) + 1]),
+          g2 = T(A.nodes[3 * (size_t)(nd - 1) + 2]);
+        for (int i = 0; i < 3; ++i) X[i] = Or[i][0] * g0 + Or[i][1] * g1 + Or[i][2] * g2;
+        if (GENERAL && A.disp) {
+            const int r = A.rank[nd - 1] - 1;
+            for (int i = 0; i < 3; ++i) U[i] = T(A.disp[3 * (size_t)r + i]);
+        }
+    }
+    const T sa = (a == 1 || a == 2 || a == 5 || a == 6) ? T(1) : T(-1);
+    const T ta = (a == 2 || a == 3 || a == 6 || a == 7) ? T(1) : T(-1);
+    const T ua = (a >= 4) ? T(1) : T(-1);
+    const T g = T(0.57735026918962576451);  // 1/sqrt(3) (r_1rt3)
+    T acc0[3][3], acc1[3][3], ru[3] = {T(0), T(0), T(0)};
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) acc0[i][j] = acc1[i][j] = T(0);
+    for (int gp = 0; gp < 8; ++gp) {
+        const T s1 = (gp & 1) ? g : -g, s2 = (gp & 2) ? g : -g, s3 = (gp & 4) ? g : -g;
+        // shape derivatives of node a (r_EvalNs brick8 branch)
+        T Ns[3];
+        Ns[0] = T(0.125) * sa * (T(1) + ta * s2) * (T(1) + ua * s3);
+        Ns[1] = T(0.125) * ta * (T(1) + sa * s1) * (T(1) + ua * s3);
+        Ns[2] = T(0.125) * ua * (T(1) + sa * s1) * (T(1) + ta * s2);
+        const bool act = lane < 8;
+        T J[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) J[i][j] = wsum8<T>(act ? X[i] * Ns[j] : T(0));
+        // cofactor inverse (r_getDetInv)
+        T a11 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        T a12 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        T a13 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        T det = J[0][0] * a11 + J[0][1] * a12 + J[0][2] * a13;
+        T di = T(1) / det;
+        T I[3][3];
+        I[0][0] = di * a11;
+        I[1][0] = di * a12;
+        I[2][0] = di * a13;
+        I[0][1] = di * (J[0][2] * J[2][1] - J[0][1] * J[2][2]);
+        I[1][1] = di * (J[0][0] * J[2][2] - J[0][2] * J[2][0]);
+        I[2][1] = di * (J[0][1] * J[2][0] - J[0][0] * J[2][1]);
+        I[0][2] = di * (J[0][1] * J[1][2] - J[0][2] * J[1][1]);
+        I[1][2] = di * (J[0][2] * J[1][0] - J[0][0] * J[1][2]);
+        I[2][2] = di * (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
+        T nx[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) nx[j] = Ns[0] * I[0][j] + Ns[1] * I[1][j] + Ns[2] * I[2][j];
+        if (act) {
+            sNx[w][a][0] = nx[0];
+            sNx[w][a][1] = nx[1];
+            sNx[w][a][2] = nx[2];
+        }
+        __syncwarp();
+        const T wdet = det;  // unit Gauss weights
+        T Gm[3][3], S3[3][3], stress[6];
+        bool nonlin = false;
+        if (GENERAL) {
+            T ux[3][3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) ux[i][j] = wsum8<T>(act ? U[i] * nx[j] : T(0));
+            // Green-Lagrange strain (r_getNLStrain dv = dv2 = 0)
+            T uxL[3][3];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) uxL[i][j] = Or[i][0] * ux[0][j] + Or[i][1] * ux[1][j] + Or[i][2] * ux[2][j];
+            T st[6];
+            st[0] = uxL[0][0] + T(0.5) * (ux[0][0] * ux[0][0] + ux[1][0] * ux[1][0] + ux[2][0] * ux[2][0]);
+            st[1] = uxL[1][1] + T(0.5) * (ux[0][1] * ux[0][1] + ux[1][1] * ux[1][1] + ux[2][1] * ux[2][1]);
+            st[2] = uxL[2][2] + T(0.5) * (ux[0][2] * ux[0][2] + ux[1][2] * ux[1][2] + ux[2][2] * ux[2][2]);
+            st[3] = uxL[0][1] + uxL[1][0] + ux[0][0] * ux[0][1] + ux[1][0] * ux[1][1] + ux[2][0] * ux[2][1];
+            st[4] = uxL[0][2] + uxL[2][0] + ux[0][0] * ux[0][2] + ux[1][0] * ux[1][2] + ux[2][0] * ux[2][2];
+            st[5] = uxL[1][2] + uxL[2][1] + ux[0][2] * ux[0][1] + ux[1][2] * ux[1][1] + ux[2][2] * ux[2][1];
+            for (int i = 0; i < 6; ++i) {
+                stress[i] = T(0);
+                for (int k = 0; k < 6; ++k) stress[i] += C[i][k] * st[k];
+            }
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    Gm[i][j] = Or[i][j] + ux[j][i];
+                    if (Gm[i][j] != ((i == j) ? T(1) : T(0))) nonlin = true;
+                }
+            S3[0][0] = stress[0];
+            S3[1][1] = stress[1];
+            S3[2][2] = stress[2];
+            S3[0][1] = S3[1][0] = stress[3];
+            S3[0][2] = S3[2][0] = stress[4];
+            S3[1][2] = S3[2][1] = stress[5];
+            // residual of node a (lanes 0..7)
+            if (act) {
+                T bs[3];  // Bloc(nx)^T stress
+                bs[0] = nx[0] * stress[0] + nx[1] * stress[3] + nx[2] * stress[4];
+                bs[1] = nx[1] * stress[1] + nx[0] * stress[3] + nx[2] * stress[5];
+                bs[2] = nx[2] * stress[2] + nx[0] * stress[4] + nx[1] * stress[5];
+                for (int v = 0; v < 3; ++v) ru[v] += wdet * (Gm[0][v] * bs[0] + Gm[1][v] * bs[1] + Gm[2][v] * bs[2]);
+            }
+        }
+        // blocks (bA0,bB) and (bA1,bB)
+        T h[3] = {sNx[w][bB][0], sNx[w][bB][1], sNx[w][bB][2]};
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int ia = half ? bA1 : bA0;
+            T gg[3] = {sNx[w][ia][0], sNx[w][ia][1], sNx[w][ia][2]};
+            T M[3][3];
+            btcb<T>(C, gg, h, M);
+            T (&acc)[3][3] = half ? acc1 : acc0;
+            if (GENERAL && nonlin) {
+                T MG[3][3];
+                for (int i = 0; i < 3; ++i)
+                    for (int k = 0; k < 3; ++k) MG[i][k] = M[i][0] * Gm[0][k] + M[i][1] * Gm[1][k] + M[i][2] * Gm[2][k];
+                T geo = T(0);
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) geo += gg[i] * S3[i][j] * h[j];
+                for (int i = 0; i < 3; ++i)
+                    for (int k = 0; k < 3; ++k)
+                        acc[i][k] += wdet * (Gm[0][i] * MG[0][k] + Gm[1][i] * MG[1][k] + Gm[2][i] * MG[2][k] +
+                                             ((i == k) ? geo : T(0)));
+            } else {
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) acc[i][k] += wdet * M[i][k];
+            }
+        }
+        __syncwarp();
+    }
+    // outputs
+    const int *blk = A.elBlk + 64 * (size_t)e;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const int ia = half ? bA1 : bA0;
+        T (&acc)[3][3] = half ? acc1 : acc0;
+        const int k = blk[ia * 8 + bB];
+        if (A.Kbsr) {
+            T *dst = A.Kbsr + 9 * (size_t)k;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) dst[3 * i + j] += acc[i][j];
+        }
+        if (A.Kbsr64) {
+            double *dst = A.Kbsr64 + 9 * (size_t)k;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) dst[3 * i + j] += (double)acc[i][j];
+        }
+        if (A.keOut) {
+            double *ke = A.keOut + 576 * (size_t)e;
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) ke[(size_t)(8 * j + bB) * 24 + (8 * i + ia)] = (double)acc[i][j];
+        }
+    }
+    if (GENERAL && lane < 8) {
+        if (A.loadInt) {
+            const int r = A.rank[nd - 1] - 1;
+            for (int v = 0; v < 3; ++v) A.loadInt[3 * (size_t)r + v] -= (double)ru[v];
+        }
+        if (A.ruOut)
+            for (int v = 0; v < 3; ++v) A.ruOut[24 * (size_t)e + 8 * v + a] = (double)ru[v];
+    }
+}
+
+}  // namespace
+
+// precision 64: general FP64 kernel (state, orientation); 32: FP32 kernel at zero state.
+// store bit 1: FP32 BSR, bit 2: FP64 BSR (the FP32 kernel adds its values into both when asked).
+static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_disp, double *d_loadInt, double *d_ke,
+                    double *d_ru) {
+    const AstroPrep &P = ctx->P;
+    for (int col = 0; col < P.ncolors; ++col) {
+        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+        if (!cnt) continue;
+        dim3 grid((cnt + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
+        if (precision == 64) {
+            Hex8Args<double> A;
+            A.nodes = dptr<double>(ctx->d_nodes);
+            A.elist = dptr<int>(ctx->d_elist);
+            A.rank = dptr<int>(ctx->d_rank);
+            A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+            A.count = cnt;
+            A.elBlk = dptr<int>(ctx->d_elBlk);
+            A.elMat = dptr<double>(ctx->d_elMat);
+            A.orient = ctx->orientIdentity ? nullptr : dptr<double>(ctx->d_secOrient);
+            A.disp = d_disp;
+            A.Kbsr = (store & 2) ? dptr<double>(ctx->d_K64) : nullptr;
+            A.Kbsr64 = nullptr;
+            A.loadInt = d_loadInt;
+            A.keOut = d_ke;
+            A.ruOut = d_ru;
+            hex8_kernel<double, true><<<grid, block, 0, ctx->stream>>>(A);
+        } else {
+            Hex8Args<float> A;
+            A.nodes = dptr<double>(ctx->d_nodes);
+            A.elist = dptr<int>(ctx->d_elist);
+            A.rank = dptr<int>(ctx->d_rank);
+            A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+            A.count = cnt;
+            A.elBlk = dptr<int>(ctx->d_elBlk);
+            A.elMat = dptr<double>(ctx->d_elMat);
+            A.orient = nullptr;
+            A.disp = nullptr;
+            A.Kbsr = (store & 1) ? dptr<float>(ctx->d_K32) : nullptr;
+            A.Kbsr64 = (store & 2) ? dptr<double>(ctx->d_K64) : nullptr;
+            A.loadInt = nullptr;
+            A.keOut = d_ke;
+            A.ruOut = nullptr;
+            hex8_kernel<float, false><<<grid, block, 0, ctx->stream>>>(A);
+        }
+    }
+    return cuda_check(ctx, cudaGetLastError(), "hex8 kernel launch");
+}
+
+int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
+    if (precision == 32 && !ctx->orientIdentity)
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 brick8 kernel needs identity section orientation");
+    return hex8_run(ctx, precision, store, nullptr, nullptr, nullptr, nullptr);
+}
+
+int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt) {
+    return hex8_run(ctx, 64, buildMat ? 2 : 0, d_disp, d_loadInt, nullptr, nullptr);
+}
+
+int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
+    return hex8_run(ctx, precision, 0, nullptr, nullptr, d_ke, nullptr);
+}
+
+int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru) {
+    return hex8_run(ctx, 64, 0, d_disp, nullptr, d_ke, d_ru);
+}

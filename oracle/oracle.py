@@ -1,0 +1,232 @@
+"""ctypes wrapper of the oracle library (test infrastructure only)."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+I32P = C.POINTER(C.c_int32)
+F64P = C.POINTER(C.c_double)
+
+
+def lib_path():
+    return os.path.join(_HERE, "_build", "liborc.so")
+
+
+def build(force=False):
+    """Compiles the oracle with its Makefile (a few seconds)."""
+    srcs = ["oracle_api.cpp", "oracle_elements.hpp", "oracle_element_driver.hpp"]
+    out = lib_path()
+    if not force and os.path.exists(out):
+        t = os.path.getmtime(out)
+        if all(os.path.getmtime(os.path.join(_HERE, s)) <= t for s in srcs):
+            return out
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return out
+
+
+def _lib():
+    global _LIB
+    if _LIB is None:
+        build()
+        L = C.CDLL(lib_path())
+        L.orc_create.restype = C.c_void_p
+        L.orc_create.argtypes = [C.c_void_p]
+        L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_dims.argtypes = [C.c_void_p, I32P]
+        L.orc_get_prep.argtypes = [C.c_void_p, I32P, I32P, I32P, I32P, I32P, I32P, F64P, F64P]
+        L.orc_element.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, F64P, F64P]
+        L.orc_element_c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_double,
+                                    F64P, F64P, F64P, F64P]
+        L.orc_element_matrices.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, F64P]
+        L.orc_el_soln_load.argtypes = [C.c_void_p, C.c_int, C.c_void_p, F64P, F64P, F64P, I32P, F64P]
+        L.orc_scale_mpc.argtypes = [F64P, C.c_int, F64P, F64P, I32P, C.c_int]
+        L.orc_constraint_load.argtypes = [F64P, I32P, I32P, F64P, C.c_int, F64P, F64P]
+        L.orc_convert_to_ltri.argtypes = [F64P, I32P, C.c_int, F64P, I32P, I32P, C.c_int, C.c_int,
+                                          F64P, I32P, I32P, C.c_int, C.c_int]
+        L.orc_ldl_fact.argtypes = [F64P, C.c_int, I32P, C.c_int]
+        L.orc_ldl_solve.argtypes = [F64P, F64P, F64P, C.c_int, I32P, C.c_int, F64P]
+        L.orc_gmres.restype = C.c_int
+        L.orc_gmres.argtypes = [F64P, F64P, I32P, I32P, C.c_int, C.c_int, F64P, I32P, I32P, C.c_int, C.c_int,
+                                F64P, I32P, C.c_int, F64P, C.c_int, C.c_int]
+        L.orc_update_external_rhs.argtypes = [C.c_void_p, F64P, F64P, F64P]
+        L.orc_update_internal_soln.argtypes = [C.c_void_p, F64P, F64P, F64P, F64P]
+        L.orc_surface_load.argtypes = [C.c_void_p, C.c_int, I32P, I32P, F64P, C.c_double, F64P]
+        _LIB = L
+    return _LIB
+
+
+def _p(a, t):
+    return C.cast(None, t) if a is None else a.ctypes.data_as(t)
+
+
+def _i(a):
+    return _p(a, I32P)
+
+
+def _d(a):
+    return _p(a, F64P)
+
+
+class Oracle:
+    """Analysis-prepared model on the CPU (reference analysisPrep) plus the hot-path routines."""
+
+    def __init__(self, model):
+        self.model = model
+        self.mc = model.as_c()
+        self.L = _lib()
+        self.h = self.L.orc_create(C.byref(self.mc))
+        if not self.h:
+            raise ValueError("oracle: unsupported model")
+        d = np.zeros(8, np.int32)
+        self.L.orc_dims(self.h, _i(d))
+        (self.n, self.el_mat_size, self.lt_size, self.mpc_dim, self.mpc_size, self.int_vec_size,
+         self.int_mat_size, self.solver_max_bw) = [int(x) for x in d]
+        N = model.num_nodes
+        self.current_rank = np.zeros(N, np.int32)
+        self.n_dof_index = np.zeros((N, 6), np.int32)
+        self.el_mat_range = np.zeros(self.n + 1, np.int32)
+        self.lt_range = np.zeros(self.n + 1, np.int32)
+        self.mpc_range = np.zeros(self.mpc_dim + 1, np.int32)
+        self.mpc_cols = np.zeros(self.mpc_size, np.int32)
+        self.mpc_mat = np.zeros(self.mpc_size)
+        self.mpc_rhs = np.zeros(self.mpc_dim)
+        self.L.orc_get_prep(self.h, _i(self.current_rank), _i(self.n_dof_index), _i(self.el_mat_range),
+                            _i(self.lt_range), _i(self.mpc_range), _i(self.mpc_cols), _d(self.mpc_mat),
+                            _d(self.mpc_rhs))
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.L.orc_destroy(self.h)
+        except Exception:
+            pass
+
+    # -- elements -------------------------------------------------------------------------------
+    def element(self, el, build_mat=1, state=None):
+        ru = np.zeros(33)
+        k = np.zeros((33, 33), order="F")
+        rc = self.L.orc_element(self.h, el, build_mat, C.byref(state) if state is not None else None, _d(ru),
+                                k.ctypes.data_as(F64P))
+        assert rc == 0
+        return ru, k
+
+    def element_c(self, el, dvar, h, build_mat=0, state=None):
+        rr, ri = np.zeros(33), np.zeros(33)
+        kr, ki = np.zeros((33, 33), order="F"), np.zeros((33, 33), order="F")
+        rc = self.L.orc_element_c(self.h, el, build_mat, C.byref(state) if state is not None else None, dvar, h,
+                                  _d(rr), _d(ri), kr.ctypes.data_as(F64P), ki.ctypes.data_as(F64P))
+        assert rc == 0
+        return rr + 1j * ri, kr + 1j * ki
+
+    def element_matrices(self, el0=1, el1=None, state=None):
+        """Condensed nodal element matrices (24x24) of elements el0..el1 (1-based, inclusive)."""
+        if el1 is None:
+            el1 = self.model.num_els
+        out = np.zeros((el1 - el0 + 1, 24, 24))
+        rc = self.L.orc_element_matrices(self.h, el0, el1, C.byref(state) if state is not None else None,
+                                         _d(out))
+        assert rc == 0
+        return np.transpose(out, (0, 2, 1)).copy()   # stored column-major per element
+
+    def el_soln_load(self, build_mat=1, state=None, elastic_load=None, int_elastic_load=None):
+        n = self.n
+        load = np.zeros(n) if elastic_load is None else elastic_load
+        iload = np.zeros(max(self.int_vec_size, 1)) if int_elastic_load is None else int_elastic_load
+        mat = np.zeros(self.el_mat_size)
+        cols = np.zeros(self.el_mat_size, np.int32)
+        imat = np.zeros(max(self.int_mat_size, 1))
+        rc = self.L.orc_el_soln_load(self.h, build_mat, C.byref(state) if state is not None else None, _d(load),
+                                     _d(iload), _d(mat), _i(cols), _d(imat))
+        assert rc == 0
+        return load, iload, mat, cols, imat
+
+    # -- constraints, loads ---------------------------------------------------------------------
+    def scale_mpc(self, elastic_mat):
+        mm = self.mpc_mat.copy()
+        mr = self.mpc_rhs.copy()
+        self.L.orc_scale_mpc(_d(elastic_mat), len(elastic_mat), _d(mm), _d(mr), _i(self.mpc_range), self.mpc_dim)
+        return mm, mr
+
+    def constraint_load(self, mpc_mat, mpc_rhs, node_disp, elastic_load):
+        self.L.orc_constraint_load(_d(mpc_mat), _i(self.mpc_cols), _i(self.mpc_range), _d(mpc_rhs), self.mpc_dim,
+                                   _d(node_disp), _d(elastic_load))
+
+    def applied_load(self, load=None):
+        """Consistent surface load of the model's faces plus its point loads."""
+        m = self.model
+        load = np.zeros(self.n) if load is None else load
+        if len(m.face_el):
+            fe = np.ascontiguousarray(m.face_el, np.int32)
+            fn = np.ascontiguousarray(m.face_num, np.int32)
+            tr = np.ascontiguousarray(m.traction, np.float64)
+            self.L.orc_surface_load(self.h, len(fe), _i(fe), _i(fn), _d(tr), float(m.pressure), _d(load))
+        for nd, dof, v in m.point_loads:
+            load[self.n_dof_index[nd - 1, dof - 1] - 1] += v
+        return load
+
+    def convert_to_ltri(self, mat, cols, mpc_mat):
+        lt = np.zeros(self.lt_size)
+        self.L.orc_convert_to_ltri(_d(lt), _i(self.lt_range), self.lt_size, _d(mat), _i(cols),
+                                   _i(self.el_mat_range), len(mat), self.n, _d(mpc_mat), _i(self.mpc_cols),
+                                   _i(self.mpc_range), self.mpc_size, self.mpc_dim)
+        return lt
+
+    # -- solvers (pure functions of their arguments) ----------------------------------------------
+    @staticmethod
+    def ldl_fact(lt, lt_range):
+        a = lt.copy()
+        _lib().orc_ldl_fact(_d(a), len(a), _i(lt_range), len(lt_range) - 1)
+        return a
+
+    @staticmethod
+    def ldl_solve(fac, lt_range, rhs):
+        n = len(lt_range) - 1
+        x = np.zeros(n)
+        z = np.zeros(n)
+        _lib().orc_ldl_solve(_d(x), _d(np.ascontiguousarray(rhs, np.float64)), _d(fac), len(fac), _i(lt_range), n,
+                             _d(z))
+        return x
+
+    def gmres(self, mat, cols, mpc_mat, fac, b, x0=None, num_vecs=None, max_it=None):
+        n = self.n
+        x = np.zeros(n) if x0 is None else x0.copy()
+        if num_vecs is None:
+            num_vecs = n // 2 if n < 200 else 100
+        if max_it is None:
+            max_it = n
+        cyc = self.L.orc_gmres(_d(x), _d(mat), _i(cols), _i(self.el_mat_range), len(mat), n, _d(mpc_mat),
+                               _i(self.mpc_cols), _i(self.mpc_range), self.mpc_size, self.mpc_dim, _d(fac),
+                               _i(self.lt_range), len(fac), _d(np.ascontiguousarray(b, np.float64)), num_vecs,
+                               max_it)
+        return x, cyc
+
+    # -- helpers for tests ----------------------------------------------------------------------
+    def csr_scipy(self, mat, cols):
+        import scipy.sparse as sp
+        n = self.n
+        rows = np.repeat(np.arange(n), np.diff(self.el_mat_range))
+        keep = cols > 0
+        return sp.csr_matrix((mat[keep], (rows[keep], cols[keep] - 1)), shape=(n, n))
+
+    def mpc_scipy(self, mpc_mat):
+        import scipy.sparse as sp
+        rows = np.repeat(np.arange(self.mpc_dim), np.diff(self.mpc_range))
+        keep = self.mpc_cols > 0
+        return sp.csr_matrix((mpc_mat[keep], (rows[keep], self.mpc_cols[keep] - 1)), shape=(self.mpc_dim, self.n))
+
+    def static_system(self):
+        """(A = K + C^T C, b) of the linear static step from zero state with the scaled constraints."""
+        load, iload, mat, cols, imat = self.el_soln_load(1)
+        mm, mr = self.scale_mpc(mat)
+        b = np.zeros(self.n)
+        self.constraint_load(mm, mr, np.zeros(self.n), b)
+        self.applied_load(b)
+        K = self.csr_scipy(mat, cols)
+        Cm = self.mpc_scipy(mm)
+        return (K + (Cm.T @ Cm)).tocsr(), b, mat, cols, mm, mr

@@ -1,0 +1,870 @@
+// ORACLE (test infrastructure only): model-level restatement of AStrO's hot path -- analysis
+// preparation (node reordering, DOF map, CSR/skyline structure, constraints), getElasticSolnLoad
+// assembly, constraint scaling/loads, convertToLTri, the skyline LDL^T factor/solve and the
+// reference GMRES -- exported as plain C functions for ctypes.  Only tests/, smoke() and the
+// CPU-baseline leg of bench.py load this library.  See oracle_elements.hpp for the parity status.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <vector>
+
+#include "oracle_element_driver.hpp"
+
+using namespace orc;
+
+int orc::g_quirk_mean_rot_derivative = 0;
+
+struct OracleCtx {
+    const astro_model *m;
+    int numNodes, numEls;
+    int solverMaxBW;
+    std::vector<int> currentRank, originalRank, nDofIndex;  // nDofIndex(6,N)
+    std::vector<int> nCRange, nodalConn;
+    int elMatDim, elMatSize, elMatLTSize;
+    std::vector<int> elMatRange, elMatLTRange;
+    std::vector<int> intVecRange, intMatRange;
+    int intVecSize, intMatSize;
+    int mpcDim, mpcSize;
+    std::vector<int> mpcRange, mpcCols;
+    std::vector<double> mpcMat, mpcRhs;
+};
+
+// solverMaxBW as set by the *solve command (Working/AStrO_runJob.f90:106-114): smallest b with
+// b^3 >= 27*numNodes^2, evaluated in default (32-bit, wrapping) integers as the reference does.
+static int solver_max_bw(int numNodes) {
+    int32_t nnd2 = (int32_t)((uint32_t)27u * (uint32_t)numNodes * (uint32_t)numNodes);
+    int32_t b = 1, bw3 = 1;
+    while (bw3 < nnd2) {
+        b = b + 1;
+        bw3 = (int32_t)((uint32_t)b * (uint32_t)b * (uint32_t)b);
+    }
+    return b;
+}
+
+// levelSortNodes, Working/AStrO_bookKeeping.f90:233-331 (breadth-first reordering from the node
+// of fewest element-node incidences; nearest-node restart when a component is exhausted).
+static void levelSortNodes(OracleCtx &c, int &nextAvail, int stopLength, int ndof, std::vector<int> &ndInserted,
+                           std::vector<int> &ndBlockNum, int &currentBlock, int solverBlockDim) {
+    const astro_model *m = c.m;
+    const int numNodes = c.numNodes;
+    auto nRange = [&](int i) { return c.nCRange[i]; };
+    auto ndofOf = [&](int nd) { return c.nDofIndex[6 * (nd - 1)]; };
+    auto nearest = [&](int from) {
+        double minDist = 1e100;
+        int stNd = 0;
+        for (int i4 = 1; i4 <= numNodes; ++i4) {
+            if (ndInserted[i4 - 1] == 0 && ndofOf(i4) == ndof) {
+                double v0 = m->node_list[3 * (i4 - 1)] - m->node_list[3 * (from - 1)];
+                double v1 = m->node_list[3 * (i4 - 1) + 1] - m->node_list[3 * (from - 1) + 1];
+                double v2 = m->node_list[3 * (i4 - 1) + 2] - m->node_list[3 * (from - 1) + 2];
+                double dist = std::sqrt(v0 * v0 + v1 * v1 + v2 * v2);
+                if (dist < minDist) {
+                    minDist = dist;
+                    stNd = i4;
+                }
+            }
+        }
+        return stNd;
+    };
+    int minCon = 1000, stNd = 0;
+    for (int i1 = 1; i1 <= numNodes; ++i1) {
+        if (ndofOf(i1) == ndof) {
+            int i2 = nRange(i1) - nRange(i1 - 1);
+            if (i2 < minCon) {
+                stNd = i1;
+                minCon = i2;
+            }
+        }
+    }
+    c.originalRank[nextAvail - 1] = stNd;
+    int currentNd = stNd, currentInd = nextAvail, blockSt = nextAvail;
+    currentBlock++;
+    ndBlockNum[stNd - 1] = currentBlock;
+    nextAvail++;
+    ndInserted[stNd - 1] = 1;
+    while (nextAvail <= stopLength) {
+        int i1 = nRange(currentNd - 1) + 1;
+        while (i1 <= nRange(currentNd)) {
+            int i2 = c.nodalConn[i1 - 1];
+            if (i2 != 0 && ndInserted[i2 - 1] == 0) {
+                c.originalRank[nextAvail - 1] = i2;
+                nextAvail++;
+                ndInserted[i2 - 1] = 1;
+                ndBlockNum[i2 - 1] = currentBlock;
+                int i3 = nextAvail - blockSt;
+                if (i3 == solverBlockDim && nextAvail <= numNodes) {
+                    stNd = nearest(i2);
+                    c.originalRank[nextAvail - 1] = stNd;
+                    currentNd = stNd;
+                    currentInd = nextAvail;
+                    ndInserted[stNd - 1] = 1;
+                    blockSt = nextAvail;
+                    currentBlock++;
+                    ndBlockNum[stNd - 1] = currentBlock;
+                    nextAvail++;
+                    i1 = nRange(currentNd - 1);
+                }
+            }
+            i1++;
+        }
+        currentInd++;
+        if (currentInd == nextAvail && nextAvail <= stopLength) {
+            int from = c.originalRank[nextAvail - 2];
+            stNd = nearest(from);
+            c.originalRank[nextAvail - 1] = stNd;
+            currentInd = nextAvail;
+            ndInserted[stNd - 1] = 1;
+            ndBlockNum[stNd - 1] = currentBlock;
+            nextAvail++;
+        }
+        if (currentInd <= numNodes) currentNd = c.originalRank[currentInd - 1];
+    }
+}
+
+static GState to_gstate(const astro_state *s) {
+    GState g;
+    if (!s) return g;
+    g.disp = s->node_disp;
+    g.vel = s->node_vel;
+    g.acc = s->node_acc;
+    g.pdisp = s->prev_disp;
+    g.pvel = s->prev_vel;
+    g.pacc = s->prev_acc;
+    g.intDisp = s->internal_disp;
+    g.pIntDisp = s->prev_int_disp;
+    g.dynamic = s->dynamic;
+    g.beta = s->nm_beta;
+    g.gamma = s->nm_gamma;
+    g.delT = s->del_t;
+    return g;
+}
+
+extern "C" {
+
+// analysisPrep, Working/AStrO_bookKeeping.f90:794-1039, with allocateElasticMat (:333-411) and
+// buildElasticMPC (:474-612) for pre-expanded equations.  Returns NULL on unsupported input.
+OracleCtx *orc_create(const astro_model *m) {
+    OracleCtx *c = new OracleCtx();
+    c->m = m;
+    const int N = m->num_nodes, E = m->num_els;
+    c->numNodes = N;
+    c->numEls = E;
+    c->solverMaxBW = solver_max_bw(N);
+    c->currentRank.assign(N, 0);
+    c->originalRank.assign(N, 0);
+    c->nDofIndex.assign(6 * N, 0);
+    c->nCRange.assign(N + 1, 0);
+    for (int i1 = 1; i1 <= E; ++i1) {
+        int eT = m->element_type[i1 - 1];
+        int ndof = (eT == 41 || eT == 3 || eT == 2) ? 6 : 3;
+        for (int i2 = 1; i2 <= 8; ++i2) {
+            int i3 = m->element_list[8 * (i1 - 1) + i2 - 1];
+            if (i3 != 0) {
+                for (int i4 = 1; i4 <= 8; ++i4) {
+                    int i5 = m->element_list[8 * (i1 - 1) + i4 - 1];
+                    if (i5 != 0 && i5 != i3) c->nCRange[i3]++;
+                }
+                c->nDofIndex[6 * (i3 - 1)] = ndof;
+            }
+        }
+    }
+    int numSolidNds = 0;
+    for (int i1 = 1; i1 <= N; ++i1)
+        if (c->nDofIndex[6 * (i1 - 1)] == 3) numSolidNds++;
+    int numSectionNds = N - numSolidNds;
+    for (int i1 = 2; i1 <= N; ++i1) c->nCRange[i1] += c->nCRange[i1 - 1];
+    int nCSize = c->nCRange[N];
+    c->nodalConn.assign(nCSize, 0);
+    for (int i1 = 1; i1 <= E; ++i1)
+        for (int i2 = 1; i2 <= 8; ++i2) {
+            int i3 = m->element_list[8 * (i1 - 1) + i2 - 1];
+            if (i3 == 0) continue;
+            for (int i4 = 1; i4 <= 8; ++i4) {
+                int i5 = m->element_list[8 * (i1 - 1) + i4 - 1];
+                if (i5 == 0 || i5 == i3) continue;
+                int i6 = c->nCRange[i3 - 1] + 1;
+                int inserted = 0;
+                while (i6 <= c->nCRange[i3] && inserted == 0) {
+                    if (c->nodalConn[i6 - 1] == 0) {
+                        c->nodalConn[i6 - 1] = i5;
+                        inserted = 1;
+                    } else if (c->nodalConn[i6 - 1] == i5) {
+                        inserted = 1;
+                    }
+                    i6++;
+                }
+            }
+        }
+    std::vector<int> ndInserted(N, 0), ndBlockNum(N, 0);
+    int nextAvail = 1, currentBlock = 0;
+    if (numSolidNds > 0) levelSortNodes(*c, nextAvail, numSolidNds, 3, ndInserted, ndBlockNum, currentBlock, N);
+    if (nextAvail <= N) levelSortNodes(*c, nextAvail, N, 6, ndInserted, ndBlockNum, currentBlock, N);
+    for (int i1 = 1; i1 <= N; ++i1) c->currentRank[c->originalRank[i1 - 1] - 1] = i1;
+    for (int i1 = 1; i1 <= N; ++i1) {
+        int t = c->nDofIndex[6 * (i1 - 1)];
+        if (t == 3) {
+            for (int i2 = 1; i2 <= 3; ++i2) c->nDofIndex[6 * (i1 - 1) + i2 - 1] = c->currentRank[i1 - 1] + (i2 - 1) * numSolidNds;
+        } else if (t == 6) {
+            for (int i2 = 1; i2 <= 6; ++i2)
+                c->nDofIndex[6 * (i1 - 1) + i2 - 1] = c->currentRank[i1 - 1] + (i2 - 1) * numSectionNds + 2 * numSolidNds;
+        }
+    }
+    const int n = 3 * numSolidNds + 6 * numSectionNds;
+    c->elMatDim = n;
+    c->intVecRange.assign(E + 1, 0);
+    c->intMatRange.assign(E + 1, 0);
+    for (int i1 = 1; i1 <= E; ++i1) {
+        int t = m->element_type[i1 - 1];
+        if (t == 41) {
+            c->intVecRange[i1] = 8;
+            c->intMatRange[i1] = 256;
+        } else if (t != 8) {
+            delete c;
+            return nullptr;
+        }
+    }
+    for (int i1 = 2; i1 <= E; ++i1) {
+        c->intVecRange[i1] += c->intVecRange[i1 - 1];
+        c->intMatRange[i1] += c->intMatRange[i1 - 1];
+    }
+    c->intVecSize = c->intVecRange[E];
+    c->intMatSize = c->intMatRange[E];
+    // allocateElasticMat
+    auto ndi = [&](int comp, int nd) { return c->nDofIndex[6 * (nd - 1) + comp - 1]; };
+    c->elMatRange.assign(n + 1, 0);
+    c->elMatLTRange.assign(n + 1, 0);
+    for (int i1 = 1; i1 <= N; ++i1)
+        for (int i2 = 1; i2 <= 6; ++i2) {
+            int i3 = ndi(i2, i1);
+            if (i3 == 0) continue;
+            for (int i4 = 1; i4 <= 6; ++i4)
+                if (ndi(i4, i1) != 0) c->elMatRange[i3]++;
+            for (int i4 = c->nCRange[i1 - 1] + 1; i4 <= c->nCRange[i1]; ++i4) {
+                int i5 = c->nodalConn[i4 - 1];
+                if (i5 == 0) continue;
+                for (int i6 = 1; i6 <= 6; ++i6)
+                    if (ndi(i6, i5) != 0) c->elMatRange[i3]++;
+            }
+        }
+    for (int i1 = 2; i1 <= n; ++i1) c->elMatRange[i1] += c->elMatRange[i1 - 1];
+    c->elMatSize = c->elMatRange[n];
+    for (int i1 = 1; i1 <= N; ++i1)
+        for (int i2 = 1; i2 <= 6; ++i2) {
+            int i3 = ndi(i2, i1);
+            if (i3 == 0) continue;
+            c->elMatLTRange[i3] = 1;
+            for (int i4 = c->nCRange[i1 - 1] + 1; i4 <= c->nCRange[i1]; ++i4) {
+                int i5 = c->nodalConn[i4 - 1];
+                if (i5 == 0) continue;
+                int i6 = c->currentRank[i1 - 1] - c->currentRank[i5 - 1];
+                if (i6 >= 0 && i6 <= c->solverMaxBW) {
+                    int i7 = ndi(i2, i5);
+                    if (i7 != 0 && i7 <= i3) {
+                        int i8 = i3 - i7 + 1;
+                        if (i8 > c->elMatLTRange[i3]) c->elMatLTRange[i3] = i8;
+                    }
+                }
+            }
+        }
+    for (int i1 = 2; i1 <= n; ++i1) c->elMatLTRange[i1] += c->elMatLTRange[i1 - 1];
+    c->elMatLTSize = c->elMatLTRange[n];
+    // buildElasticMPC for expanded equations: duplicate columns in a row are skipped (slot stays 0)
+    c->mpcDim = m->num_mpc;
+    c->mpcRange.assign(c->mpcDim + 1, 0);
+    for (int k = 0; k <= c->mpcDim; ++k) c->mpcRange[k] = m->num_mpc ? m->mpc_range[k] : 0;
+    c->mpcSize = c->mpcRange[c->mpcDim];
+    c->mpcCols.assign(c->mpcSize, 0);
+    c->mpcMat.assign(c->mpcSize, 0.0);
+    c->mpcRhs.assign(c->mpcDim, 0.0);
+    for (int r = 1; r <= c->mpcDim; ++r) {
+        for (int t = c->mpcRange[r - 1]; t < c->mpcRange[r]; ++t) {
+            int col = ndi(m->mpc_dof[t], m->mpc_node[t]);
+            for (int s = c->mpcRange[r - 1]; s < c->mpcRange[r]; ++s) {
+                if (c->mpcCols[s] == 0) {
+                    c->mpcMat[s] = m->mpc_coef[t];
+                    c->mpcCols[s] = col;
+                    break;
+                } else if (c->mpcCols[s] == col) {
+                    break;
+                }
+            }
+        }
+        c->mpcRhs[r - 1] = m->mpc_rhs[r - 1];
+    }
+    return c;
+}
+
+void orc_destroy(OracleCtx *c) { delete c; }
+
+// Debug probe: shell deformation vectors def(9) at the Gauss points of element el at `s`.
+int orc_debug_shell_def(const OracleCtx *c, int el, const astro_state *s, double *out) {
+    ElemData<double> e;
+    DPert<double> p;
+    GState g = to_gstate(s);
+    if (t_getElementData(e, c->m, c->nDofIndex.data(), c->intVecRange.data(), el, g, p) != 0) return 1;
+    A1<double, 3> elRot;
+    elRot.fill(0.0);
+    for (int i1 = 1; i1 <= e.numNds; ++i1)
+        for (int k = 1; k <= 3; ++k) elRot(k) += e.disp(3 + k, i1) / e.numNds;
+    A2<double, 3, 48> instOri;
+    A2<double, 3, 16> drIdrG;
+    t_getInstOrient(instOri, drIdrG, e.orient, elRot);
+    for (int gp = 1; gp <= e.numIntPts; ++gp) {
+        A1<double, 11> Nvec;
+        A2<double, 11, 3> Nx;
+        double detJ;
+        t_getIntPtData(Nvec, Nx, detJ, e.locNds, e.intPts[gp - 1], 41, 4);
+        A2<double, 6, 11> U;
+        t_getInstDof(U, e.disp, e.globNds, instOri, e.orient, elRot, drIdrG, 4, e.dofTable, 0, 0);
+        A1<double, 3> ptRot;
+        ptRot.fill(0.0);
+        for (int i2 = 1; i2 <= 4; ++i2)
+            for (int k = 1; k <= 3; ++k) ptRot(k) += U(3 + k, i2) * Nvec(i2);
+        A2<double, 3, 3> ux, rx;
+        ux.fill(0.0);
+        rx.fill(0.0);
+        for (int i2 = 1; i2 <= 3; ++i2)
+            for (int i3 = 1; i3 <= 3; ++i3)
+                for (int i4 = 1; i4 <= 10; ++i4) {
+                    ux(i2, i3) += U(i2, i4) * Nx(i4, i3);
+                    rx(i2, i3) += U(i2 + 3, i4) * Nx(i4, i3);
+                }
+        A1<double, 9> d;
+        t_getShellDef(d, ux, ptRot, rx);
+        for (int k = 0; k < 9; ++k) out[(gp - 1) * 9 + k] = d.a[k];
+    }
+    return 0;
+}
+
+void orc_set_quirk(int which, int value) {
+    if (which == 1) g_quirk_mean_rot_derivative = value;
+}
+
+void orc_dims(const OracleCtx *c, int32_t *out) {
+    out[0] = c->elMatDim;
+    out[1] = c->elMatSize;
+    out[2] = c->elMatLTSize;
+    out[3] = c->mpcDim;
+    out[4] = c->mpcSize;
+    out[5] = c->intVecSize;
+    out[6] = c->intMatSize;
+    out[7] = c->solverMaxBW;
+}
+
+void orc_get_prep(const OracleCtx *c, int32_t *currentRank, int32_t *nDofIndex, int32_t *elMatRange,
+                  int32_t *elMatLTRange, int32_t *mpcRange, int32_t *mpcCols, double *mpcMat, double *mpcRhs) {
+    if (currentRank) std::copy(c->currentRank.begin(), c->currentRank.end(), currentRank);
+    if (nDofIndex) std::copy(c->nDofIndex.begin(), c->nDofIndex.end(), nDofIndex);
+    if (elMatRange) std::copy(c->elMatRange.begin(), c->elMatRange.end(), elMatRange);
+    if (elMatLTRange) std::copy(c->elMatLTRange.begin(), c->elMatLTRange.end(), elMatLTRange);
+    if (mpcRange) std::copy(c->mpcRange.begin(), c->mpcRange.end(), mpcRange);
+    if (mpcCols) std::copy(c->mpcCols.begin(), c->mpcCols.end(), mpcCols);
+    if (mpcMat) std::copy(c->mpcMat.begin(), c->mpcMat.end(), mpcMat);
+    if (mpcRhs) std::copy(c->mpcRhs.begin(), c->mpcRhs.end(), mpcRhs);
+}
+
+
+// One element (1-based) in FP64: Ru(33) and dRdU(33,33) column-major, before condensation.
+int orc_element(const OracleCtx *c, int el, int buildMat, const astro_state *s, double *Ru, double *dRdU) {
+    A1<double, 33> R;
+    A2<double, 33, 33> K;
+    DPert<double> p;
+    if (t_element(R, K, c->m, c->nDofIndex.data(), c->intVecRange.data(), el, buildMat, to_gstate(s), p) != 0)
+        return 1;
+    for (int k = 0; k < 33; ++k) Ru[k] = R.a[k];
+    if (dRdU) std::memcpy(dRdU, &K(1, 1), sizeof(double) * 33 * 33);
+    return 0;
+}
+
+// One element in complex FP64 with design variable dvar perturbed by i*h: real and imaginary
+// parts of Ru(33) and dRdU(33,33).
+int orc_element_c(const OracleCtx *c, int el, int buildMat, const astro_state *s, int dvar, double h, double *RuRe,
+                  double *RuIm, double *KRe, double *KIm) {
+    A1<cd, 33> R;
+    A2<cd, 33, 33> K;
+    DPert<cd> p;
+    p.dvar = dvar;
+    p.h = h;
+    if (t_element(R, K, c->m, c->nDofIndex.data(), c->intVecRange.data(), el, buildMat, to_gstate(s), p) != 0)
+        return 1;
+    for (int k = 0; k < 33; ++k) {
+        RuRe[k] = R.a[k].real();
+        RuIm[k] = R.a[k].imag();
+    }
+    if (KRe)
+        for (int j = 1; j <= 33; ++j)
+            for (int i = 1; i <= 33; ++i) {
+                KRe[(j - 1) * 33 + i - 1] = K(i, j).real();
+                KIm[(j - 1) * 33 + i - 1] = K(i, j).imag();
+            }
+    return 0;
+}
+
+// Element matrices of elements el0..el1 (1-based, inclusive) in FP64 after static condensation,
+// nodal part only (nd x nd per element, column-major, nd = numNds*dofPerNd = 24).  Used by the
+// CPU baseline timing and the per-element parity tests.
+int orc_element_matrices(const OracleCtx *c, int el0, int el1, const astro_state *s, double *ke_out) {
+    GState g = to_gstate(s);
+    DPert<double> p;
+    for (int el = el0; el <= el1; ++el) {
+        A1<double, 33> R;
+        A2<double, 33, 33> K;
+        if (t_element(R, K, c->m, c->nDofIndex.data(), c->intVecRange.data(), el, 1, g, p) != 0) return 1;
+        int t = c->m->element_type[el - 1];
+        if (t == 41) t_condenseMat(K, 25, 32);
+        double *o = ke_out + (size_t)(el - el0) * 576;
+        for (int j = 1; j <= 24; ++j)
+            for (int i = 1; i <= 24; ++i) o[(j - 1) * 24 + i - 1] = K(i, j);
+    }
+    return 0;
+}
+
+// getElasticSolnLoad, Working/AStrO_commandFunctions.f90:260-351 (Q7 resolved: CSR columns start
+// zeroed by this call).  elasticLoad(n) and intElasticLoad are accumulated (-= Ru).
+int orc_el_soln_load(const OracleCtx *c, int buildMat, const astro_state *s, double *elasticLoad,
+                     double *intElasticLoad, double *elasticMat, int32_t *elMatCols, double *intElasticMat) {
+    const astro_model *m = c->m;
+    GState g = to_gstate(s);
+    DPert<double> p;
+    if (buildMat == 1) {
+        std::fill(elasticMat, elasticMat + c->elMatSize, 0.0);
+        std::fill(elMatCols, elMatCols + c->elMatSize, 0);
+    }
+    for (int i1 = 1; i1 <= c->numEls; ++i1) {
+        A1<double, 33> Ru;
+        A2<double, 33, 33> dRdU;
+        ElemData<double> e;
+        if (t_element(Ru, dRdU, m, c->nDofIndex.data(), c->intVecRange.data(), i1, buildMat, g, p, &e) != 0) return 1;
+        int i3 = e.numNds * e.dofPerNd;
+        for (int i2 = 1; i2 <= i3; ++i2) {
+            int i4 = e.dofTable[i2 - 1][0];
+            int i5 = m->element_list[8 * (i1 - 1) + e.dofTable[i2 - 1][1] - 1];
+            int i6 = c->nDofIndex[6 * (i5 - 1) + i4 - 1];
+            elasticLoad[i6 - 1] -= Ru(i2);
+        }
+        if (e.numIntDof != 0 && intElasticLoad) {
+            int i4 = c->intVecRange[i1 - 1] + 1, i5 = c->intVecRange[i1];
+            for (int k = i4; k <= i5; ++k) intElasticLoad[k - 1] -= Ru(i3 + k - i4 + 1);
+        }
+        if (buildMat == 1) {
+            if (e.numIntDof > 0) {
+                int i2 = e.numNds * e.dofPerNd + 1, i3b = e.numNds * e.dofPerNd + e.numIntDof;
+                t_condenseMat(dRdU, i2, i3b);
+                int i4 = c->intMatRange[i1 - 1] + 1;
+                if (intElasticMat)
+                    for (int i5 = 1; i5 <= i3b; ++i5)
+                        for (int i6 = i2; i6 <= i3b; ++i6) intElasticMat[(i4++) - 1] = dRdU(i6, i5);
+            }
+            int i2 = e.numNds * e.dofPerNd;
+            for (int i3c = 1; i3c <= i2; ++i3c) {
+                int i5 = e.dofTable[i3c - 1][0];
+                int i6 = m->element_list[8 * (i1 - 1) + e.dofTable[i3c - 1][1] - 1];
+                int kGi = c->nDofIndex[6 * (i6 - 1) + i5 - 1];
+                for (int i4 = 1; i4 <= i2; ++i4) {
+                    int v = e.dofTable[i4 - 1][0];
+                    int nd = m->element_list[8 * (i1 - 1) + e.dofTable[i4 - 1][1] - 1];
+                    int kGj = c->nDofIndex[6 * (nd - 1) + v - 1];
+                    int k = c->elMatRange[kGi - 1] + 1;
+                    int inserted = 0;
+                    while (inserted == 0 && k <= c->elMatRange[kGi]) {
+                        int col = elMatCols[k - 1];
+                        if (col == 0) {
+                            elasticMat[k - 1] = dRdU(i3c, i4);
+                            elMatCols[k - 1] = kGj;
+                            inserted = 1;
+                        } else if (col == kGj) {
+                            elasticMat[k - 1] += dRdU(i3c, i4);
+                            inserted = 1;
+                        }
+                        k++;
+                    }
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+// scaleElasticMPC, Working/AStrO_commandFunctions.f90:537-566 (in place on the given arrays)
+void orc_scale_mpc(const double *elasticMat, int elMatSize, double *mpcMat, double *mpcRhs, const int32_t *mpcRange,
+                   int mpcDim) {
+    double maxMat = 0.0;
+    for (int i1 = 0; i1 < elMatSize; ++i1) {
+        double r = std::fabs(elasticMat[i1]);
+        if (r > maxMat) maxMat = r;
+    }
+    for (int i1 = 1; i1 <= mpcDim; ++i1) {
+        int i3 = mpcRange[i1 - 1] + 1, i4 = mpcRange[i1];
+        double rowMag = 0.0;
+        for (int i2 = i3; i2 <= i4; ++i2) rowMag += mpcMat[i2 - 1] * mpcMat[i2 - 1];
+        rowMag = std::sqrt(rowMag);
+        for (int i2 = i3; i2 <= i4; ++i2) mpcMat[i2 - 1] = (1.0 / rowMag) * mpcMat[i2 - 1];
+        mpcRhs[i1 - 1] = (1.0 / rowMag) * mpcRhs[i1 - 1];
+    }
+    int mpcSize = mpcRange[mpcDim];
+    for (int k = 0; k < mpcSize; ++k) mpcMat[k] = 100.0 * maxMat * mpcMat[k];
+    for (int k = 0; k < mpcDim; ++k) mpcRhs[k] = 100.0 * maxMat * mpcRhs[k];
+}
+
+// getElasticConstraintLoad, :506-535
+void orc_constraint_load(const double *mpcMat, const int32_t *mpcCols, const int32_t *mpcRange, const double *mpcRhs,
+                         int mpcDim, const double *nodeDisp, double *elasticLoad) {
+    std::vector<double> t(mpcRhs, mpcRhs + mpcDim);
+    for (int i1 = 1; i1 <= mpcDim; ++i1)
+        for (int i2 = mpcRange[i1 - 1] + 1; i2 <= mpcRange[i1]; ++i2) {
+            int i3 = mpcCols[i2 - 1];
+            if (i3 != 0 && nodeDisp) t[i1 - 1] -= mpcMat[i2 - 1] * nodeDisp[i3 - 1];
+        }
+    for (int i1 = 1; i1 <= mpcDim; ++i1)
+        for (int i2 = mpcRange[i1 - 1] + 1; i2 <= mpcRange[i1]; ++i2) {
+            int i3 = mpcCols[i2 - 1];
+            if (i3 != 0) elasticLoad[i3 - 1] += mpcMat[i2 - 1] * t[i1 - 1];
+        }
+}
+
+// convertToLTri, Working/AStrO_bookKeeping.f90:754-792
+void orc_convert_to_ltri(double *lTri, const int32_t *lTRange, int lTSize, const double *mainMat, const int32_t *mainCols,
+                         const int32_t *mainRange, int mainSize, int mainDim, const double *cMat, const int32_t *cCols,
+                         const int32_t *cRange, int cSize, int cDim) {
+    (void)mainSize;
+    (void)cSize;
+    std::fill(lTri, lTri + lTSize, 0.0);
+    for (int i1 = 1; i1 <= mainDim; ++i1) {
+        int minCol = i1 - lTRange[i1] + lTRange[i1 - 1] + 1;
+        for (int i2 = mainRange[i1 - 1] + 1; i2 <= mainRange[i1]; ++i2) {
+            int i3 = mainCols[i2 - 1];
+            if (i3 >= minCol && i3 <= i1) {
+                int i4 = lTRange[i1] - i1 + i3;
+                lTri[i4 - 1] += mainMat[i2 - 1];
+            }
+        }
+    }
+    for (int i1 = 1; i1 <= cDim; ++i1)
+        for (int i2 = cRange[i1 - 1] + 1; i2 <= cRange[i1]; ++i2) {
+            int i4 = cCols[i2 - 1];
+            if (i4 == 0) continue;
+            int minCol = i4 - lTRange[i4] + lTRange[i4 - 1] + 1;
+            for (int i3 = cRange[i1 - 1] + 1; i3 <= cRange[i1]; ++i3) {
+                int i5 = cCols[i3 - 1];
+                if (i5 >= minCol && i5 <= i4) {
+                    int i6 = lTRange[i4] - i4 + i5;
+                    lTri[i6 - 1] += cMat[i2 - 1] * cMat[i3 - 1];
+                }
+            }
+        }
+}
+
+// getSparseLDLFact, Working/AStrO_solvers.f90:10-78
+void orc_ldl_fact(double *ALTri, int ASize, const int32_t *ARange, int n) {
+    (void)ASize;
+    std::vector<int> rowStCol(n + 1);
+    std::vector<double> diagvec(n + 1);
+    int maxBW = 0;
+    for (int i1 = 1; i1 <= n; ++i1) {
+        int rowLen = ARange[i1] - ARange[i1 - 1];
+        rowStCol[i1] = i1 - rowLen + 1;
+        if (rowLen > maxBW) maxBW = rowLen;
+    }
+    std::vector<double> dLprod(maxBW + 1);
+    for (int i1 = 1; i1 <= n; ++i1) {
+        int i3 = ARange[i1];
+        int i2 = ARange[i1 - 1] + 1;
+        int i5 = maxBW, i6 = i1 - 1;
+        for (int i4 = i3 - 1; i4 >= i2; --i4) {
+            dLprod[i5] = diagvec[i6] * ALTri[i4 - 1];
+            i5--;
+            i6--;
+        }
+        i5 = i1 - i3 + i2;
+        double diag = ALTri[i3 - 1];
+        for (int i4 = i2; i4 <= i3 - 1; ++i4) {
+            diag -= diagvec[i5] * ALTri[i4 - 1] * ALTri[i4 - 1];
+            i5++;
+        }
+        diagvec[i1] = diag;
+        ALTri[i3 - 1] = diag;
+        double fact = 1.0 / diag;
+        int imax = std::min(n, i1 + maxBW);
+        for (int j = i1 + 1; j <= imax; ++j) {
+            int stCol = std::max(rowStCol[i1], rowStCol[j]);
+            int rowLen = i1 - stCol;
+            if (rowLen >= 0) {
+                int a = maxBW - rowLen + 1;
+                int b = ARange[j] - (j - stCol);
+                int t = b + rowLen;
+                double d = ALTri[t - 1];
+                for (int k = 0; k <= rowLen - 1; ++k) d -= dLprod[a + k] * ALTri[b + k - 1];
+                ALTri[t - 1] = d * fact;
+            }
+        }
+    }
+}
+
+// solveSparseLDLFact, Working/AStrO_solvers.f90:83-126
+void orc_ldl_solve(double *soln, const double *rhs, const double *Lmat, int LSize, const int32_t *LRange, int Ldim,
+                   double *zVec) {
+    (void)LSize;
+    int maxBW = 0;
+    for (int i1 = 1; i1 <= Ldim; ++i1) {
+        int i2 = LRange[i1 - 1] + 1;
+        int rowLen = LRange[i1] - i2;
+        if (rowLen > maxBW) maxBW = rowLen;
+        int stCol = i1 - rowLen;
+        zVec[i1 - 1] = rhs[i1 - 1];
+        for (int i3 = 0; i3 <= rowLen - 1; ++i3) zVec[i1 - 1] -= Lmat[i2 + i3 - 1] * zVec[stCol + i3 - 1];
+    }
+    for (int i1 = Ldim; i1 >= 1; --i1) {
+        double dtProd = 0.0;
+        double diag = Lmat[LRange[i1] - 1];
+        int imax = std::min(Ldim, i1 + maxBW);
+        for (int i2 = i1 + 1; i2 <= imax; ++i2) {
+            int rowLen = LRange[i2] - LRange[i2 - 1];
+            int stCol = i2 - rowLen + 1;
+            if (stCol <= i1) {
+                int i3 = LRange[i2] + i1 - i2;
+                dtProd += Lmat[i3 - 1] * soln[i2 - 1];
+            }
+        }
+        dtProd = dtProd * diag;
+        soln[i1 - 1] = (zVec[i1 - 1] - dtProd) / diag;
+    }
+}
+
+// rFactorMat (triDiag = 2 branch used by gMRes), Working/AStrO_solvers.f90:299-353
+static void rFactorMat(std::vector<double> &A, int rowDim, int colDim) {
+    auto a = [&](int i, int j) -> double & { return A[(size_t)(j - 1) * rowDim + i - 1]; };
+    for (int i1 = 1; i1 <= colDim; ++i1) {
+        int maxRow = std::min(i1 + 1, rowDim), maxCol = colDim;
+        for (int i2 = i1 + 1; i2 <= maxRow; ++i2) {
+            if (std::fabs(a(i2, i1)) > F(1e-10)) {
+                double theta;
+                if (a(i1, i1) == 0.0)
+                    theta = F(1.570796326794897);
+                else
+                    theta = std::atan(a(i2, i1) / a(i1, i1));
+                double st = std::sin(theta), ct = std::cos(theta);
+                for (int i3 = i1; i3 <= maxCol; ++i3) {
+                    double a1 = ct * a(i1, i3) + st * a(i2, i3);
+                    double a2 = -st * a(i1, i3) + ct * a(i2, i3);
+                    a(i1, i3) = a1;
+                    a(i2, i3) = a2;
+                }
+                a(i2, i1) = theta;
+            }
+        }
+    }
+}
+
+// solveRFactor (triDiag = 2), :355-404
+static void solveRFactor(double *soln, const std::vector<double> &A, double *bVec, int rowDim, int colDim) {
+    auto a = [&](int i, int j) { return A[(size_t)(j - 1) * rowDim + i - 1]; };
+    for (int i1 = 1; i1 <= colDim; ++i1) {
+        int maxRow = std::min(i1 + 1, rowDim);
+        for (int i2 = i1 + 1; i2 <= maxRow; ++i2) {
+            if (std::fabs(a(i2, i1)) > F(1e-10)) {
+                double st = std::sin(a(i2, i1)), ct = std::cos(a(i2, i1));
+                double r1 = ct * bVec[i1 - 1] + st * bVec[i2 - 1];
+                double r2 = -st * bVec[i1 - 1] + ct * bVec[i2 - 1];
+                bVec[i1 - 1] = r1;
+                bVec[i2 - 1] = r2;
+            }
+        }
+    }
+    for (int i1 = colDim; i1 >= 1; --i1) {
+        soln[i1 - 1] = bVec[i1 - 1];
+        for (int i2 = i1 + 1; i2 <= colDim; ++i2) soln[i1 - 1] -= a(i1, i2) * soln[i2 - 1];
+        soln[i1 - 1] = soln[i1 - 1] / a(i1, i1);
+    }
+}
+
+// (A + C^T C) x with the reference's loop order: C x, C^T(.), then A x added.
+static void ref_matvec(std::vector<double> &out, const double *x, const double *Amat, const int32_t *Acols,
+                       const int32_t *ARange, int ADim, const double *Cmat, const int32_t *Ccols, const int32_t *CRange,
+                       int CDim, std::vector<double> &t1) {
+    std::fill(t1.begin(), t1.end(), 0.0);
+    for (int i1 = 1; i1 <= CDim; ++i1)
+        for (int i2 = CRange[i1 - 1] + 1; i2 <= CRange[i1]; ++i2) {
+            int i3 = Ccols[i2 - 1];
+            if (i3 != 0) t1[i1 - 1] += Cmat[i2 - 1] * x[i3 - 1];
+        }
+    std::fill(out.begin(), out.end(), 0.0);
+    for (int i1 = 1; i1 <= CDim; ++i1)
+        for (int i2 = CRange[i1 - 1] + 1; i2 <= CRange[i1]; ++i2) {
+            int i3 = Ccols[i2 - 1];
+            if (i3 != 0) out[i3 - 1] += Cmat[i2 - 1] * t1[i1 - 1];
+        }
+    for (int i1 = 1; i1 <= ADim; ++i1)
+        for (int i2 = ARange[i1 - 1] + 1; i2 <= ARange[i1]; ++i2) {
+            int i3 = Acols[i2 - 1];
+            if (i3 != 0) out[i1 - 1] += Amat[i2 - 1] * x[i3 - 1];
+        }
+}
+
+// gMRes, Working/AStrO_solvers.f90:128-297.  Returns the number of restart cycles run.
+int orc_gmres(double *xVec, const double *Amat, const int32_t *Acols, const int32_t *ARange, int ASize, int ADim,
+              const double *Cmat, const int32_t *Ccols, const int32_t *CRange, int CSize, int CDim, const double *Pmat,
+              const int32_t *PRange, int PSize, const double *bVec, int numVecs, int maxIt) {
+    (void)ASize;
+    (void)CSize;
+    const int n = ADim;
+    std::vector<double> zVec(n), rVec(n), tempV1(std::max(n, numVecs + 1)), tempV2(std::max(n, numVecs + 1));
+    std::vector<double> hMat((size_t)n * (numVecs + 1)), h2Ah((size_t)(numVecs + 1) * numVecs);
+    std::vector<double> cbuf(std::max(CDim, 1)), mv(n), rhs(n);
+    auto H = [&](int i, int j) -> double & { return hMat[(size_t)(j - 1) * n + i - 1]; };
+    auto G = [&](int i, int j) -> double & { return h2Ah[(size_t)(j - 1) * (numVecs + 1) + i - 1]; };
+    ref_matvec(mv, xVec, Amat, Acols, ARange, ADim, Cmat, Ccols, CRange, CDim, cbuf);
+    for (int i = 0; i < n; ++i) rhs[i] = bVec[i] - mv[i];
+    orc_ldl_solve(rVec.data(), rhs.data(), Pmat, PSize, PRange, n, zVec.data());
+    double resMag = 0.0;
+    for (int i = 0; i < n; ++i) resMag += rVec[i] * rVec[i];
+    resMag = std::sqrt(resMag);
+    int maxOutIt = maxIt / numVecs + 1;
+    int i4 = 0;
+    std::vector<double> col(n);
+    while (resMag > F(1e-12) && i4 < maxOutIt) {
+        for (int i = 1; i <= n; ++i) H(i, 1) = (1.0 / resMag) * rVec[i - 1];
+        std::fill(h2Ah.begin(), h2Ah.end(), 0.0);
+        for (int i5 = 2; i5 <= numVecs + 1; ++i5) {
+            ref_matvec(mv, &H(1, i5 - 1), Amat, Acols, ARange, ADim, Cmat, Ccols, CRange, CDim, cbuf);
+            orc_ldl_solve(&H(1, i5), mv.data(), Pmat, PSize, PRange, n, zVec.data());
+            for (int i1 = 1; i1 <= i5 - 1; ++i1) {
+                double dp = 0.0;
+                for (int i2 = 1; i2 <= n; ++i2) dp += H(i2, i1) * H(i2, i5);
+                for (int i2 = 1; i2 <= n; ++i2) H(i2, i5) = H(i2, i5) - dp * H(i2, i1);
+                G(i1, i5 - 1) = dp;
+            }
+            double dp = 0.0;
+            for (int i2 = 1; i2 <= n; ++i2) dp += H(i2, i5) * H(i2, i5);
+            dp = std::sqrt(dp);
+            for (int i2 = 1; i2 <= n; ++i2) H(i2, i5) = (1.0 / dp) * H(i2, i5);
+            G(i5, i5 - 1) = dp;
+        }
+        rFactorMat(h2Ah, numVecs + 1, numVecs);
+        std::fill(tempV1.begin(), tempV1.end(), 0.0);
+        for (int i1 = 1; i1 <= n; ++i1)
+            for (int i2 = 1; i2 <= numVecs + 1; ++i2) tempV1[i2 - 1] += H(i1, i2) * rVec[i1 - 1];
+        std::fill(tempV2.begin(), tempV2.begin() + numVecs, 0.0);
+        solveRFactor(tempV2.data(), h2Ah, tempV1.data(), numVecs + 1, numVecs);
+        for (int i1 = 1; i1 <= n; ++i1)
+            for (int i2 = 1; i2 <= numVecs; ++i2) xVec[i1 - 1] += H(i1, i2) * tempV2[i2 - 1];
+        ref_matvec(mv, xVec, Amat, Acols, ARange, ADim, Cmat, Ccols, CRange, CDim, cbuf);
+        for (int i = 0; i < n; ++i) rhs[i] = bVec[i] - mv[i];
+        orc_ldl_solve(rVec.data(), rhs.data(), Pmat, PSize, PRange, n, zVec.data());
+        resMag = 0.0;
+        for (int i = 0; i < n; ++i) resMag += rVec[i] * rVec[i];
+        resMag = std::sqrt(resMag);
+        i4++;
+    }
+    return i4;
+}
+
+// updateExternalRHS (Working/AStrO_commandFunctions.f90:568-607) with the Q9 loop bound resolved
+// to the internal rows nodalDof+1..totalDof.
+void orc_update_external_rhs(const OracleCtx *c, double *extVec, const double *intVec, const double *intElasticMat) {
+    const astro_model *m = c->m;
+    for (int i1 = 1; i1 <= c->numEls; ++i1) {
+        if (m->element_type[i1 - 1] != 41) continue;
+        const int nodalDof = 24, totalDof = 32;
+        A2<double, 33, 33> K;
+        K.fill(0.0);
+        int i4 = c->intMatRange[i1 - 1] + 1;
+        for (int i2 = 1; i2 <= totalDof; ++i2)
+            for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) K(i3, i2) = intElasticMat[(i4++) - 1];
+        double t1[33] = {0}, t2[33] = {0}, z[33] = {0};
+        int v0 = c->intVecRange[i1 - 1];
+        for (int k = 1; k <= 8; ++k) t2[nodalDof + k - 1] = intVec[v0 + k - 1];
+        t_SolveLUxb(t1, &K(1, 1), t2, z, 33, nodalDof + 1, totalDof);
+        for (int i2 = 1; i2 <= nodalDof; ++i2) {
+            int comp = (i2 - 1) / 4 + 1, lnd = (i2 - 1) % 4 + 1;
+            int nd = m->element_list[8 * (i1 - 1) + lnd - 1];
+            int i6 = c->nDofIndex[6 * (nd - 1) + comp - 1];
+            for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) extVec[i6 - 1] -= K(i3, i2) * t1[i3 - 1];
+        }
+    }
+}
+
+// updateInternalSoln (:609-651), Q9 resolved likewise.
+void orc_update_internal_soln(const OracleCtx *c, const double *extSoln, double *intSoln, const double *intRHS,
+                              const double *intElasticMat) {
+    const astro_model *m = c->m;
+    for (int i1 = 1; i1 <= c->numEls; ++i1) {
+        if (m->element_type[i1 - 1] != 41) continue;
+        const int nodalDof = 24, totalDof = 32;
+        A2<double, 33, 33> K;
+        K.fill(0.0);
+        int i4 = c->intMatRange[i1 - 1] + 1;
+        for (int i2 = 1; i2 <= totalDof; ++i2)
+            for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) K(i3, i2) = intElasticMat[(i4++) - 1];
+        double t1[33] = {0}, t2[33] = {0}, z[33] = {0};
+        int v0 = c->intVecRange[i1 - 1];
+        for (int k = 1; k <= 8; ++k) t2[nodalDof + k - 1] = intRHS ? intRHS[v0 + k - 1] : 0.0;
+        for (int i2 = 1; i2 <= nodalDof; ++i2) {
+            int comp = (i2 - 1) / 4 + 1, lnd = (i2 - 1) % 4 + 1;
+            int nd = m->element_list[8 * (i1 - 1) + lnd - 1];
+            int i6 = c->nDofIndex[6 * (nd - 1) + comp - 1];
+            for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) t2[i3 - 1] -= K(i3, i2) * extSoln[i6 - 1];
+        }
+        t_SolveLUxb(t1, &K(1, 1), t2, z, 33, nodalDof + 1, totalDof);
+        for (int k = 1; k <= 8; ++k) intSoln[v0 + k - 1] += t1[nodalDof + k - 1];
+    }
+}
+
+// Consistent surface load with the intended semantics of the reference's surface branch
+// (getElasticAppliedLoad :441-500, r_getElSurfaceTraction Working/AStrO_r_elementEqns.f90:1923-2018,
+// faces from r_getElementFaces :288-332): Q8 resolved -- true face area (|dx/ds x dx/dt|), face
+// shape function k applied to the face's k-th element node, contributions accumulated over faces.
+// t = traction - pressure * n, with n the face normal of r_getElSurfaceNormal.
+void orc_surface_load(const OracleCtx *c, int nfaces, const int32_t *faceEl, const int32_t *faceNum,
+                      const double *traction, double pressure, double *elasticLoad) {
+    const astro_model *m = c->m;
+    static const int hexF[6][4] = {{4, 3, 2, 1}, {5, 6, 7, 8}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {4, 1, 5, 8}};
+    static const int shF[2][4] = {{1, 2, 3, 4}, {1, 4, 3, 2}};
+    const double rt3 = 1.0 / std::sqrt(3.0);
+    for (int f = 0; f < nfaces; ++f) {
+        int el = faceEl[f], fn = faceNum[f];
+        int t = m->element_type[el - 1];
+        const int *fl = (t == 8) ? hexF[fn - 1] : shF[fn - 1];
+        double X[4][3];
+        int nodes[4];
+        for (int k = 0; k < 4; ++k) {
+            nodes[k] = m->element_list[8 * (el - 1) + fl[k] - 1];
+            for (int d = 0; d < 3; ++d) X[k][d] = m->node_list[3 * (nodes[k] - 1) + d];
+        }
+        double v1[3], v2[3], nv[3];
+        for (int d = 0; d < 3; ++d) {
+            v1[d] = X[2][d] - X[0][d];
+            v2[d] = X[3][d] - X[1][d];
+        }
+        nv[0] = v1[1] * v2[2] - v1[2] * v2[1];
+        nv[1] = v1[2] * v2[0] - v1[0] * v2[2];
+        nv[2] = v1[0] * v2[1] - v1[1] * v2[0];
+        double mag = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+        for (int d = 0; d < 3; ++d) nv[d] /= mag;
+        double tr[3];
+        for (int d = 0; d < 3; ++d) tr[d] = traction[d] - pressure * nv[d];
+        const double gp[4][2] = {{-rt3, -rt3}, {rt3, -rt3}, {-rt3, rt3}, {rt3, rt3}};
+        for (int g = 0; g < 4; ++g) {
+            double s = gp[g][0], r = gp[g][1];
+            double N[4] = {0.25 * (1 - s) * (1 - r), 0.25 * (1 + s) * (1 - r), 0.25 * (1 + s) * (1 + r),
+                           0.25 * (1 - s) * (1 + r)};
+            double Ns[4] = {-0.25 * (1 - r), 0.25 * (1 - r), 0.25 * (1 + r), -0.25 * (1 + r)};
+            double Nr[4] = {-0.25 * (1 - s), -0.25 * (1 + s), 0.25 * (1 + s), 0.25 * (1 - s)};
+            double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
+            for (int k = 0; k < 4; ++k)
+                for (int d = 0; d < 3; ++d) {
+                    a[d] += Ns[k] * X[k][d];
+                    b[d] += Nr[k] * X[k][d];
+                }
+            double cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
+            double dA = std::sqrt(cx * cx + cy * cy + cz * cz);
+            for (int k = 0; k < 4; ++k)
+                for (int d = 0; d < 3; ++d) {
+                    int dof = c->nDofIndex[6 * (nodes[k] - 1) + d];
+                    elasticLoad[dof - 1] += tr[d] * N[k] * dA;
+                }
+        }
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,813 @@
+// ORACLE (test infrastructure only): CPU restatement of AStrO's element path, used by tests/,
+// __graft_entry__.smoke() and bench.py's cpu_baseline leg as the checker.  Never linked into
+// or called by the GPU product path.
+//
+// Parity status: the reference (Fortran 90) cannot be compiled here (no Fortran compiler) and
+// ships no tests or golden outputs, so this restatement is pinned by mechanics known-answer
+// tests (rigid-body modes, patch test, symmetric PSD stiffness, plate/beam tip deflection) and
+// by complex-step vs finite-difference checks -- "parity unpinned" against the reference binary.
+//
+// One template over T in {double, std::complex<double>} restates both twins
+// Working/AStrO_r_*.f90 and Working/AStrO_c_*.f90 (textually identical after renaming).
+// Fortran default-real (float32) literals are reproduced exactly as (double)(float)x.
+// Undefined behaviour in the reference is resolved to its evident intent:
+//   Q1 r_sin mapTheta1 uninitialised for 0<=theta<=2pi  -> mapTheta1 = theta
+//   Q3 stale i3 in ptRot of the shell derivative loops -> i3 = 0
+//   Q5 local node index / vel-acc swap in the state gather -> global node, no swap
+// Arrays use 1-based (row, col) accessors over column-major storage to follow the source.
+#pragma once
+#include <cmath>
+#include <complex>
+#include <cstring>
+
+namespace orc {
+
+typedef std::complex<double> cd;
+
+// Test-only switch (default 0 = the reference's derivative): adds the mean-rotation term that
+// r_getInstDof's rotation derivative omits.  Used only to quantify that omission in tests.
+extern int g_quirk_mean_rot_derivative;
+
+static inline double F(double x) { return (double)(float)x; }  // Fortran default-real literal
+static inline double absT(double x) { return std::fabs(x); }
+static inline double absT(const cd &x) { return std::abs(x); }
+static inline double realT(double x) { return x; }
+static inline double realT(const cd &x) { return x.real(); }
+template <class T> T pert_imag(double h);
+template <> inline double pert_imag<double>(double) { return 0.0; }
+template <> inline cd pert_imag<cd>(double h) { return cd(0.0, h); }
+
+// Constants, Working/AStrO_constantVals.f90:6-38.
+template <class T> struct KC;
+template <> struct KC<double> {
+    static double o6() { return 1.0 / 6.0; }
+    static double o3() { return 1.0 / 3.0; }
+    static double rt3() { return 1.0 / std::sqrt(3.0); }
+    static double pi() { return F(3.141592653589793); }
+    static double pi180() { return F(0.01745329251994); }
+};
+template <> struct KC<cd> {
+    static double o6() { return 0.166666666666666; }
+    static double o3() { return 0.333333333333333; }
+    static double rt3() { return F(0.577350269189626); }
+    static double pi() { return F(3.14159265358979323846); }
+    static double pi180() { return F(0.01745329251994); }
+};
+
+template <class T, int R, int C> struct A2 {
+    T a[C][R];
+    T &operator()(int i, int j) { return a[j - 1][i - 1]; }
+    const T &operator()(int i, int j) const { return a[j - 1][i - 1]; }
+    void fill(T v) { for (int j = 0; j < C; ++j) for (int i = 0; i < R; ++i) a[j][i] = v; }
+    T *col(int j) { return a[j - 1]; }
+};
+template <class T, int N> struct A1 {
+    T a[N];
+    T &operator()(int i) { return a[i - 1]; }
+    const T &operator()(int i) const { return a[i - 1]; }
+    void fill(T v) { for (int i = 0; i < N; ++i) a[i] = v; }
+};
+
+// ---- Working/AStrO_r_overloadFunctions.f90 -------------------------------------------------
+
+// r_greater, :6-22
+template <class T> int t_greater(const T &inp1, const T &inp2) {
+    T i2shft = inp2 + T(F(1e-1) * absT(inp1 - inp2)) * T(1.0);
+    return (absT(inp1 - i2shft) < absT(inp1 - inp2)) ? 1 : 0;
+}
+
+// r_sqrt, :24-44 (Newton from 1, |del| <= 1e-13 (float literal) or 50 iterations)
+template <class T> T t_sqrt(const T &inpt) {
+    T sqt = T(1.0), del = T(1.0);
+    int ct = 0;
+    while (absT(del) > F(1e-13) && ct < 50) {
+        T fVal = sqt * sqt - inpt;
+        T dF = T(2.0) * sqt;
+        del = -fVal / dF;
+        sqt = sqt + del;
+        ct++;
+    }
+    return sqt;
+}
+
+// r_sin0_90, :46-85 (7-term Taylor series with float32 coefficients)
+template <class T> T t_sin0_90(const T &theta) {
+    T c[7], sT, thetSq;
+    if (absT(theta) < F(0.7853981633974483)) {
+        thetSq = theta * theta;
+        c[0] = T(1.0);
+        c[1] = -T(1.0) * F(1.666666666666666e-1);
+        c[2] = T(1.0) * F(8.333333333333333e-3);
+        c[3] = -T(1.0) * F(1.984126984126984e-4);
+        c[4] = T(1.0) * F(2.755731922398589e-6);
+        c[5] = -T(1.0) * F(2.505210838544171e-8);
+        c[6] = T(1.0) * F(1.6059043836821614e-10);
+        sT = c[6];
+        for (int i1 = 5; i1 >= 0; --i1) sT = sT * thetSq + c[i1];
+        sT = sT * theta;
+    } else {
+        T d = theta - 0.5 * KC<T>::pi();
+        thetSq = d * d;
+        c[0] = T(1.0);
+        c[1] = -T(0.5);
+        c[2] = T(1.0) * F(4.1666666666666666e-2);
+        c[3] = -T(1.0) * F(1.388888888888889e-3);
+        c[4] = T(1.0) * F(2.4801587301587301e-5);
+        c[5] = -T(1.0) * F(2.755731922398589e-7);
+        c[6] = T(1.0) * F(2.0876756987868098e-9);
+        sT = c[6];
+        for (int i1 = 5; i1 >= 0; --i1) sT = sT * thetSq + c[i1];
+    }
+    return sT;
+}
+
+// r_sin, :87-136 (Q1 resolved: mapTheta1 = theta when no wrap applies)
+template <class T> T t_sin(const T &theta) {
+    const double pi = KC<T>::pi();
+    T mapTheta1 = theta;
+    if (t_greater(theta, T(2.0 * pi))) {
+        int i1 = (int)absT(0.5 * theta / pi);
+        mapTheta1 = theta - (double)i1 * 2.0 * pi;
+    }
+    if (t_greater(T(0.0), theta)) {
+        int i1 = (int)absT(0.5 * theta / pi);
+        mapTheta1 = theta + (double)(i1 + 1) * 2.0 * pi;
+    }
+    if (t_greater(mapTheta1, T(1.5 * pi))) return -t_sin0_90(T(2.0 * pi) - mapTheta1);
+    if (t_greater(mapTheta1, T(pi))) return -t_sin0_90(mapTheta1 - pi);
+    if (t_greater(mapTheta1, T(0.5 * pi))) return t_sin0_90(T(pi) - mapTheta1);
+    return t_sin0_90(mapTheta1);
+}
+
+// r_cos, :138-148
+template <class T> T t_cos(const T &theta) { return t_sin(theta + 0.5 * KC<T>::pi()); }
+
+// r_asin, :150-171
+template <class T> T t_asin(const T &sn) {
+    T aS = T(0.0), dt = T(1.0);
+    int i1 = 0;
+    while (absT(dt) > F(1e-13) && i1 < 20) {
+        T fVal = t_sin(aS) - sn;
+        T dF = t_cos(aS);
+        dt = -fVal / dF;
+        aS = aS + dt;
+        i1++;
+    }
+    return aS;
+}
+
+// ---- Working/AStrO_r_designPropertyFunctions.f90 -------------------------------------------
+
+// r_LUFactor, :1015-1041 (no pivoting; rows/cols stRow..endRow of an n x n column-major array)
+template <class T> void t_LUFactor(T *A, int n, int st, int en) {
+    auto a = [&](int i, int j) -> T & { return A[(j - 1) * n + (i - 1)]; };
+    for (int i1 = st; i1 <= en; ++i1) {
+        for (int i2 = i1; i2 <= en; ++i2)
+            for (int i3 = st; i3 <= i1 - 1; ++i3) a(i1, i2) = a(i1, i2) - a(i1, i3) * a(i3, i2);
+        T fact = T(1.0) / a(i1, i1);
+        for (int i2 = i1 + 1; i2 <= en; ++i2) {
+            for (int i3 = st; i3 <= i1 - 1; ++i3) a(i2, i1) = a(i2, i1) - a(i2, i3) * a(i3, i1);
+            a(i2, i1) = fact * a(i2, i1);
+        }
+    }
+}
+
+// r_SolveLUxb, :1043-1073
+template <class T> void t_SolveLUxb(T *x, const T *LU, const T *b, T *z, int n, int st, int en) {
+    auto lu = [&](int i, int j) -> const T & { return LU[(j - 1) * n + (i - 1)]; };
+    z[st - 1] = b[st - 1];
+    for (int i1 = st + 1; i1 <= en; ++i1) {
+        z[i1 - 1] = b[i1 - 1];
+        for (int i2 = st; i2 <= i1 - 1; ++i2) z[i1 - 1] = z[i1 - 1] - lu(i1, i2) * z[i2 - 1];
+    }
+    x[en - 1] = z[en - 1] / lu(en, en);
+    for (int i1 = en - 1; i1 >= st; --i1) {
+        T fact = T(1.0) / lu(i1, i1);
+        T dp = T(0.0);
+        for (int i2 = i1 + 1; i2 <= en; ++i2) dp = dp + lu(i1, i2) * x[i2 - 1];
+        x[i1 - 1] = fact * (z[i1 - 1] - dp);
+    }
+}
+
+// r_GetInvLU, :996-1013
+template <class T> void t_GetInvLU(T *Ainv, T *A, int n, int st, int en) {
+    T f[33], z[33];
+    t_LUFactor(A, n, st, en);
+    for (int i1 = st; i1 <= en; ++i1) {
+        for (int k = 0; k < n; ++k) f[k] = T(0.0);
+        f[i1 - 1] = T(1.0);
+        t_SolveLUxb(Ainv + (i1 - 1) * n, A, f, z, n, st, en);
+    }
+}
+
+// r_rotateAlpha, :1075-1463.  aGI = aGL rotated by the rotation vector rot, or its first (dv1)
+// or second (dv1,dv2) derivative with respect to the components of rot.
+template <class T>
+void t_rotateAlpha(A2<T, 3, 3> &aGI, const A2<T, 3, 3> &aGL, const A1<T, 3> &rot, int dv1, int dv2) {
+    const double o6 = KC<T>::o6(), o3 = KC<T>::o3();
+    aGI.fill(T(0.0));
+    A1<T, 3> rLoc, drLoc1, drLoc2, nRot, dnRot1, dnRot2, d2nRot, drot1, drot2;
+    A2<T, 3, 3> a1, a2, aTemp, da11, da21, da12, da22, d2a1, d2a2, daTemp1, d2aTemp;
+    T Rmag, tVal, sR, cR;
+    if (dv1 + dv2 == 0) {
+        tVal = rot(1) * rot(1) + rot(2) * rot(2) + rot(3) * rot(3);
+        Rmag = t_sqrt(tVal);
+        if (absT(Rmag) < F(1e-5)) {
+            rLoc.fill(T(0.0));
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 1; i2 <= 3; ++i2) rLoc(i1) = rLoc(i1) + aGL(i1, i2) * rot(i2);
+            tVal = o6 * (rLoc(3) * rLoc(3) + rLoc(1) * rLoc(1) + rLoc(2) * rLoc(2));
+            aTemp(1, 1) = T(1.0) - 0.5 * (rLoc(2) * rLoc(2) + rLoc(3) * rLoc(3));
+            aTemp(2, 1) = 0.5 * rLoc(1) * rLoc(2) - rLoc(3) + tVal * rLoc(3);
+            aTemp(3, 1) = 0.5 * rLoc(1) * rLoc(3) + rLoc(2) - tVal * rLoc(2);
+            aTemp(1, 2) = 0.5 * rLoc(1) * rLoc(2) + rLoc(3) - tVal * rLoc(3);
+            aTemp(2, 2) = T(1.0) - 0.5 * (rLoc(1) * rLoc(1) + rLoc(3) * rLoc(3));
+            aTemp(3, 2) = 0.5 * rLoc(2) * rLoc(3) - rLoc(1) + tVal * rLoc(1);
+            aTemp(1, 3) = 0.5 * rLoc(1) * rLoc(3) - rLoc(2) + tVal * rLoc(2);
+            aTemp(2, 3) = 0.5 * rLoc(2) * rLoc(3) + rLoc(1) - tVal * rLoc(1);
+            aTemp(3, 3) = T(1.0) - 0.5 * (rLoc(1) * rLoc(1) + rLoc(2) * rLoc(2));
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) aGI(i1, i2) = aGI(i1, i2) + aTemp(i1, i3) * aGL(i3, i2);
+        } else {
+            sR = t_sin(Rmag);
+            cR = t_cos(Rmag);
+            for (int k = 1; k <= 3; ++k) nRot(k) = (T(1.0) / Rmag) * rot(k);
+            for (int k = 1; k <= 3; ++k) a1(1, k) = nRot(k);
+            int i1 = 1;
+            if (absT(nRot(2)) < absT(nRot(1))) i1 = 2;
+            if (absT(nRot(3)) < absT(nRot(i1))) i1 = 3;
+            a1(3, i1) = T(0.0);
+            tVal = T(1.0) - nRot(i1) * nRot(i1);
+            a1(2, i1) = t_sqrt(tVal);
+            for (int i2 = 1; i2 <= 3; ++i2)
+                if (i2 != i1) a1(2, i2) = -a1(1, i1) * a1(1, i2) / a1(2, i1);
+            a1(3, 1) = a1(1, 2) * a1(2, 3) - a1(1, 3) * a1(2, 2);
+            a1(3, 2) = a1(1, 3) * a1(2, 1) - a1(1, 1) * a1(2, 3);
+            a1(3, 3) = a1(1, 1) * a1(2, 2) - a1(1, 2) * a1(2, 1);
+            for (int k = 1; k <= 3; ++k) a2(1, k) = a1(1, k);
+            for (int k = 1; k <= 3; ++k) {
+                a2(2, k) = cR * a1(2, k) - sR * a1(3, k);
+                a2(3, k) = sR * a1(2, k) + cR * a1(3, k);
+            }
+            aTemp.fill(T(0.0));
+            for (int i1b = 1; i1b <= 3; ++i1b)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) aTemp(i1b, i2) = aTemp(i1b, i2) + a2(i3, i1b) * a1(i3, i2);
+            aGI.fill(T(0.0));
+            for (int i1b = 1; i1b <= 3; ++i1b)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) aGI(i1b, i2) = aGI(i1b, i2) + aGL(i1b, i3) * aTemp(i3, i2);
+        }
+    } else if (dv1 * dv2 == 0) {
+        drot1.fill(T(0.0));
+        drot1(dv1) = T(1.0);
+        tVal = rot(1) * rot(1) + rot(2) * rot(2) + rot(3) * rot(3);
+        Rmag = t_sqrt(tVal);
+        if (absT(Rmag) < F(1e-5)) {
+            rLoc.fill(T(0.0));
+            drLoc1.fill(T(0.0));
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 1; i2 <= 3; ++i2) {
+                    rLoc(i1) = rLoc(i1) + aGL(i1, i2) * rot(i2);
+                    drLoc1(i1) = drLoc1(i1) + aGL(i1, i2) * drot1(i2);
+                }
+            tVal = o6 * (rLoc(3) * rLoc(3) + rLoc(1) * rLoc(1) + rLoc(2) * rLoc(2));
+            T dtVal1 = o3 * (drLoc1(3) * rLoc(3) + drLoc1(1) * rLoc(1) + drLoc1(2) * rLoc(2));
+            daTemp1(1, 1) = -(rLoc(2) * drLoc1(2) + rLoc(3) * drLoc1(3));
+            daTemp1(2, 1) = 0.5 * (drLoc1(1) * rLoc(2) + rLoc(1) * drLoc1(2)) - drLoc1(3) + dtVal1 * rLoc(3) + tVal * drLoc1(3);
+            daTemp1(3, 1) = 0.5 * (drLoc1(1) * rLoc(3) + rLoc(1) * drLoc1(3)) + drLoc1(2) - dtVal1 * rLoc(2) - tVal * drLoc1(2);
+            daTemp1(1, 2) = 0.5 * (drLoc1(1) * rLoc(2) + rLoc(1) * drLoc1(2)) + drLoc1(3) - dtVal1 * rLoc(3) - tVal * drLoc1(3);
+            daTemp1(2, 2) = -(rLoc(1) * drLoc1(1) + rLoc(3) * drLoc1(3));
+            daTemp1(3, 2) = 0.5 * (drLoc1(2) * rLoc(3) + rLoc(2) * drLoc1(3)) - drLoc1(1) + dtVal1 * rLoc(1) + tVal * drLoc1(1);
+            daTemp1(1, 3) = 0.5 * (drLoc1(1) * rLoc(3) + rLoc(1) * drLoc1(3)) - drLoc1(2) + dtVal1 * rLoc(2) + tVal * drLoc1(2);
+            daTemp1(2, 3) = 0.5 * (drLoc1(2) * rLoc(3) + rLoc(2) * drLoc1(3)) + drLoc1(1) - dtVal1 * rLoc(1) - tVal * drLoc1(1);
+            daTemp1(3, 3) = -(drLoc1(1) * rLoc(1) + drLoc1(2) * rLoc(2));
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) aGI(i1, i2) = aGI(i1, i2) + daTemp1(i1, i3) * aGL(i3, i2);
+        } else {
+            tVal = rot(1) * rot(1) + rot(2) * rot(2) + rot(3) * rot(3);
+            T dRmag1 = t_sqrt(tVal);
+            dRmag1 = (T(1.0) / dRmag1) * (rot(dv1) * drot1(dv1));
+            sR = t_sin(Rmag);
+            cR = t_cos(Rmag);
+            T dsR1 = cR * dRmag1;
+            T dcR1 = -sR * dRmag1;
+            for (int k = 1; k <= 3; ++k) {
+                nRot(k) = (T(1.0) / Rmag) * rot(k);
+                dnRot1(k) = (T(-1.0) / (Rmag * Rmag)) * dRmag1 * rot(k) + (T(1.0) / Rmag) * drot1(k);
+                a1(1, k) = nRot(k);
+                da11(1, k) = dnRot1(k);
+            }
+            int i1 = 1;
+            if (absT(nRot(2)) < absT(nRot(1))) i1 = 2;
+            if (absT(nRot(3)) < absT(nRot(i1))) i1 = 3;
+            a1(3, i1) = T(0.0);
+            da11(3, i1) = T(0.0);
+            tVal = T(1.0) - nRot(i1) * nRot(i1);
+            a1(2, i1) = t_sqrt(tVal);
+            da11(2, i1) = -nRot(i1) * dnRot1(i1) / a1(2, i1);
+            for (int i2 = 1; i2 <= 3; ++i2) {
+                if (i2 != i1) {
+                    a1(2, i2) = -a1(1, i1) * a1(1, i2) / a1(2, i1);
+                    da11(2, i2) = -da11(1, i1) * a1(1, i2) / a1(2, i1) - a1(1, i1) * da11(1, i2) / a1(2, i1);
+                    da11(2, i2) = da11(2, i2) + a1(1, i1) * a1(1, i2) * da11(2, i1) / (a1(2, i1) * a1(2, i1));
+                }
+            }
+            a1(3, 1) = a1(1, 2) * a1(2, 3) - a1(1, 3) * a1(2, 2);
+            da11(3, 1) = da11(1, 2) * a1(2, 3) + a1(1, 2) * da11(2, 3) - da11(1, 3) * a1(2, 2) - a1(1, 3) * da11(2, 2);
+            a1(3, 2) = a1(1, 3) * a1(2, 1) - a1(1, 1) * a1(2, 3);
+            da11(3, 2) = da11(1, 3) * a1(2, 1) + a1(1, 3) * da11(2, 1) - da11(1, 1) * a1(2, 3) - a1(1, 1) * da11(2, 3);
+            a1(3, 3) = a1(1, 1) * a1(2, 2) - a1(1, 2) * a1(2, 1);
+            da11(3, 3) = da11(1, 1) * a1(2, 2) + a1(1, 1) * da11(2, 2) - da11(1, 2) * a1(2, 1) - a1(1, 2) * da11(2, 1);
+            for (int k = 1; k <= 3; ++k) {
+                a2(1, k) = a1(1, k);
+                da21(1, k) = da11(1, k);
+            }
+            for (int k = 1; k <= 3; ++k) {
+                a2(2, k) = cR * a1(2, k) - sR * a1(3, k);
+                da21(2, k) = dcR1 * a1(2, k) + cR * da11(2, k) - dsR1 * a1(3, k) - sR * da11(3, k);
+            }
+            for (int k = 1; k <= 3; ++k) {
+                a2(3, k) = sR * a1(2, k) + cR * a1(3, k);
+                da21(3, k) = dsR1 * a1(2, k) + sR * da11(2, k) + dcR1 * a1(3, k) + cR * da11(3, k);
+            }
+            daTemp1.fill(T(0.0));
+            for (int i1b = 1; i1b <= 3; ++i1b)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3)
+                        daTemp1(i1b, i2) = daTemp1(i1b, i2) + da21(i3, i1b) * a1(i3, i2) + a2(i3, i1b) * da11(i3, i2);
+            aGI.fill(T(0.0));
+            for (int i1b = 1; i1b <= 3; ++i1b)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) aGI(i1b, i2) = aGI(i1b, i2) + aGL(i1b, i3) * daTemp1(i3, i2);
+        }
+    } else {
+        drot1.fill(T(0.0));
+        drot2.fill(T(0.0));
+        drot1(dv1) = T(1.0);
+        drot2(dv2) = T(1.0);
+        tVal = rot(1) * rot(1) + rot(2) * rot(2) + rot(3) * rot(3);
+        Rmag = t_sqrt(tVal);
+        if (absT(Rmag) < F(1e-5)) {
+            rLoc.fill(T(0.0));
+            drLoc1.fill(T(0.0));
+            drLoc2.fill(T(0.0));
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 1; i2 <= 3; ++i2) {
+                    rLoc(i1) = rLoc(i1) + aGL(i1, i2) * rot(i2);
+                    drLoc1(i1) = drLoc1(i1) + aGL(i1, i2) * drot1(i2);
+                    drLoc2(i1) = drLoc2(i1) + aGL(i1, i2) * drot2(i2);
+                }
+            tVal = o6 * (rLoc(3) * rLoc(3) + rLoc(1) * rLoc(1) + rLoc(2) * rLoc(2));
+            T dtVal1 = o3 * (drLoc1(3) * rLoc(3) + drLoc1(1) * rLoc(1) + drLoc1(2) * rLoc(2));
+            T dtVal2 = o3 * (drLoc2(3) * rLoc(3) + drLoc2(1) * rLoc(1) + drLoc2(2) * rLoc(2));
+            T d2tVal = o3 * (drLoc1(3) * drLoc2(3) + drLoc1(1) * drLoc2(1) + drLoc1(2) * drLoc2(2));
+            d2aTemp(1, 1) = -(drLoc2(2) * drLoc1(2) + drLoc2(3) * drLoc1(3));
+            d2aTemp(2, 1) = 0.5 * (drLoc1(1) * drLoc2(2) + drLoc2(1) * drLoc1(2)) + d2tVal * rLoc(3) + dtVal1 * drLoc2(3) + dtVal2 * drLoc1(3);
+            d2aTemp(3, 1) = 0.5 * (drLoc1(1) * drLoc2(3) + drLoc2(1) * drLoc1(3)) - d2tVal * rLoc(2) - dtVal1 * drLoc2(2) - dtVal2 * drLoc1(2);
+            d2aTemp(1, 2) = 0.5 * (drLoc1(1) * drLoc2(2) + drLoc2(1) * drLoc1(2)) - d2tVal * rLoc(3) - dtVal1 * drLoc2(3) - dtVal2 * drLoc1(3);
+            d2aTemp(2, 2) = -(drLoc2(1) * drLoc1(1) + drLoc2(3) * drLoc1(3));
+            d2aTemp(3, 2) = 0.5 * (drLoc1(2) * drLoc2(3) + drLoc2(2) * drLoc1(3)) + d2tVal * rLoc(1) + dtVal1 * drLoc2(1) + dtVal2 * drLoc1(1);
+            d2aTemp(1, 3) = 0.5 * (drLoc1(1) * drLoc2(3) + drLoc2(1) * drLoc1(3)) + d2tVal * rLoc(2) + dtVal1 * drLoc2(2) + dtVal2 * drLoc1(2);
+            d2aTemp(2, 3) = 0.5 * (drLoc1(2) * drLoc2(3) + drLoc2(2) * drLoc1(3)) - d2tVal * rLoc(1) + dtVal1 * drLoc2(1) + dtVal2 * drLoc1(1);
+            d2aTemp(3, 3) = -(drLoc1(1) * drLoc2(1) + drLoc1(2) * drLoc2(2));
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) aGI(i1, i2) = aGI(i1, i2) + d2aTemp(i1, i3) * aGL(i3, i2);
+        } else {
+            T dRmag1 = T(1.0) / Rmag;
+            T dRmag2 = dRmag1;
+            T d2Rmag = (dv1 == dv2) ? dRmag1 * drot1(dv1) * drot2(dv1) : T(0.0);
+            d2Rmag = d2Rmag - (dRmag1 * dRmag1 * dRmag1) * rot(dv1) * drot1(dv1) * rot(dv2) * drot2(dv2);
+            dRmag1 = dRmag1 * (rot(dv1) * drot1(dv1));
+            dRmag2 = dRmag2 * (rot(dv2) * drot2(dv2));
+            sR = t_sin(Rmag);
+            cR = t_cos(Rmag);
+            T dsR1 = cR * dRmag1, dsR2 = cR * dRmag2;
+            T d2sR = -sR * dRmag2 * dRmag1 + cR * d2Rmag;
+            T dcR1 = -sR * dRmag1, dcR2 = -sR * dRmag2;
+            T d2cR = -cR * dRmag2 * dRmag1 - sR * d2Rmag;
+            for (int k = 1; k <= 3; ++k) {
+                nRot(k) = (T(1.0) / Rmag) * rot(k);
+                dnRot1(k) = (T(-1.0) / (Rmag * Rmag)) * dRmag1 * rot(k) + (T(1.0) / Rmag) * drot1(k);
+                dnRot2(k) = (T(-1.0) / (Rmag * Rmag)) * dRmag2 * rot(k) + (T(1.0) / Rmag) * drot2(k);
+                d2nRot(k) = (2.0 * dRmag1 * dRmag2 / Rmag) * rot(k) - d2Rmag * rot(k) - dRmag1 * drot2(k) - dRmag2 * drot1(k);
+                d2nRot(k) = (T(1.0) / (Rmag * Rmag)) * d2nRot(k);
+                a1(1, k) = nRot(k);
+                da11(1, k) = dnRot1(k);
+                da12(1, k) = dnRot2(k);
+                d2a1(1, k) = d2nRot(k);
+            }
+            int i1 = 1;
+            if (absT(nRot(2)) < absT(nRot(1))) i1 = 2;
+            if (absT(nRot(3)) < absT(nRot(i1))) i1 = 3;
+            a1(3, i1) = T(0.0);
+            da11(3, i1) = T(0.0);
+            da12(3, i1) = T(0.0);
+            d2a1(3, i1) = T(0.0);
+            tVal = T(1.0) - nRot(i1) * nRot(i1);
+            a1(2, i1) = t_sqrt(tVal);
+            da11(2, i1) = -nRot(i1) * dnRot1(i1) * (T(1.0) / a1(2, i1));
+            da12(2, i1) = -nRot(i1) * dnRot2(i1) * (T(1.0) / a1(2, i1));
+            d2a1(2, i1) = -(dnRot2(i1) * dnRot1(i1) + nRot(i1) * d2nRot(i1)) * (T(1.0) / a1(2, i1));
+            tVal = (T(1.0) / (a1(2, i1) * a1(2, i1) * a1(2, i1)));
+            d2a1(2, i1) = d2a1(2, i1) - nRot(i1) * dnRot1(i1) * nRot(i1) * dnRot2(i1) * tVal;
+            for (int i2 = 1; i2 <= 3; ++i2) {
+                if (i2 == i1) continue;
+                const T q = a1(2, i1);
+                a1(2, i2) = -a1(1, i1) * a1(1, i2) / q;
+                da11(2, i2) = -da11(1, i1) * a1(1, i2) / q - a1(1, i1) * da11(1, i2) / q;
+                da11(2, i2) = da11(2, i2) + a1(1, i1) * a1(1, i2) * da11(2, i1) / (q * q);
+                da12(2, i2) = -da12(1, i1) * a1(1, i2) / q - a1(1, i1) * da12(1, i2) / q;
+                da12(2, i2) = da12(2, i2) + a1(1, i1) * a1(1, i2) * da12(2, i1) / (q * q);
+                d2a1(2, i2) = -(d2a1(1, i1) * a1(1, i2) + da11(1, i1) * da12(1, i2)) / q;
+                d2a1(2, i2) = d2a1(2, i2) - (da12(1, i1) * da11(1, i2) + a1(1, i1) * d2a1(1, i2)) / q;
+                d2a1(2, i2) = d2a1(2, i2) + da11(1, i1) * a1(1, i2) * da12(2, i1) / (q * q);
+                d2a1(2, i2) = d2a1(2, i2) + a1(1, i1) * da11(1, i2) * da12(2, i1) / (q * q);
+                d2a1(2, i2) = d2a1(2, i2) + da12(1, i1) * a1(1, i2) * da11(2, i1) / (q * q);
+                d2a1(2, i2) = d2a1(2, i2) + a1(1, i1) * da12(1, i2) * da11(2, i1) / (q * q);
+                d2a1(2, i2) = d2a1(2, i2) + a1(1, i1) * a1(1, i2) * d2a1(2, i1) / (q * q);
+                d2a1(2, i2) = d2a1(2, i2) - 2.0 * a1(1, i1) * a1(1, i2) * da11(2, i1) * da12(2, i1) / (q * q * q);
+            }
+            // third rows: cross products of rows 1 and 2, with product-rule derivatives
+            const int cp[3][2] = {{2, 3}, {3, 1}, {1, 2}};
+            for (int k = 1; k <= 3; ++k) {
+                int p = cp[k - 1][0], q = cp[k - 1][1];
+                a1(3, k) = a1(1, p) * a1(2, q) - a1(1, q) * a1(2, p);
+                da11(3, k) = da11(1, p) * a1(2, q) + a1(1, p) * da11(2, q) - da11(1, q) * a1(2, p) - a1(1, q) * da11(2, p);
+                da12(3, k) = da12(1, p) * a1(2, q) + a1(1, p) * da12(2, q) - da12(1, q) * a1(2, p) - a1(1, q) * da12(2, p);
+                d2a1(3, k) = d2a1(1, p) * a1(2, q) + da11(1, p) * da12(2, q) + da12(1, p) * da11(2, q) + a1(1, p) * d2a1(2, q);
+                d2a1(3, k) = d2a1(3, k) - d2a1(1, q) * a1(2, p) - da11(1, q) * da12(2, p) - da12(1, q) * da11(2, p) - a1(1, q) * d2a1(2, p);
+            }
+            for (int k = 1; k <= 3; ++k) {
+                a2(1, k) = a1(1, k);
+                da21(1, k) = da11(1, k);
+                da22(1, k) = da12(1, k);
+                d2a2(1, k) = d2a1(1, k);
+            }
+            for (int k = 1; k <= 3; ++k) {
+                a2(2, k) = cR * a1(2, k) - sR * a1(3, k);
+                da21(2, k) = dcR1 * a1(2, k) + cR * da11(2, k) - dsR1 * a1(3, k) - sR * da11(3, k);
+                da22(2, k) = dcR2 * a1(2, k) + cR * da12(2, k) - dsR2 * a1(3, k) - sR * da12(3, k);
+                d2a2(2, k) = d2cR * a1(2, k) + dcR1 * da12(2, k) + dcR2 * da11(2, k) + cR * d2a1(2, k);
+                d2a2(2, k) = d2a2(2, k) - d2sR * a1(3, k) - dsR1 * da12(3, k) - dsR2 * da11(3, k) - sR * d2a1(3, k);
+            }
+            for (int k = 1; k <= 3; ++k) {
+                a2(3, k) = sR * a1(2, k) + cR * a1(3, k);
+                da21(3, k) = dsR1 * a1(2, k) + sR * da11(2, k) + dcR1 * a1(3, k) + cR * da11(3, k);
+                da22(3, k) = dsR2 * a1(2, k) + sR * da12(2, k) + dcR2 * a1(3, k) + cR * da12(3, k);
+                d2a2(3, k) = d2sR * a1(2, k) + dsR1 * da12(2, k) + dsR2 * da11(2, k) + sR * d2a1(2, k);
+                d2a2(3, k) = d2a2(3, k) + d2cR * a1(3, k) + dcR1 * da12(3, k) + dcR2 * da11(3, k) + cR * d2a1(3, k);
+            }
+            d2aTemp.fill(T(0.0));
+            for (int i1b = 1; i1b <= 3; ++i1b)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) {
+                        d2aTemp(i1b, i2) = d2aTemp(i1b, i2) + d2a2(i3, i1b) * a1(i3, i2) + da21(i3, i1b) * da12(i3, i2);
+                        d2aTemp(i1b, i2) = d2aTemp(i1b, i2) + da22(i3, i1b) * da11(i3, i2) + a2(i3, i1b) * d2a1(i3, i2);
+                    }
+            aGI.fill(T(0.0));
+            for (int i1b = 1; i1b <= 3; ++i1b)
+                for (int i2 = 1; i2 <= 3; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3) aGI(i1b, i2) = aGI(i1b, i2) + aGL(i1b, i3) * d2aTemp(i3, i2);
+        }
+    }
+}
+
+// ---- Working/AStrO_r_elementEqns.f90 -------------------------------------------------------
+
+// r_EvalN, :11-89 (types 8 and 41)
+template <class T> void t_EvalN(A1<T, 11> &n, const T *s, int eType) {
+    const T s1 = s[0], s2 = s[1], s3 = s[2];
+    const T one(1.0);
+    n.fill(T(0.0));
+    if (eType == 8) {
+        n(1) = 0.125 * (one - s1) * (one - s2) * (one - s3);
+        n(2) = 0.125 * (one + s1) * (one - s2) * (one - s3);
+        n(3) = 0.125 * (one + s1) * (one + s2) * (one - s3);
+        n(4) = 0.125 * (one - s1) * (one + s2) * (one - s3);
+        n(5) = 0.125 * (one - s1) * (one - s2) * (one + s3);
+        n(6) = 0.125 * (one + s1) * (one - s2) * (one + s3);
+        n(7) = 0.125 * (one + s1) * (one + s2) * (one + s3);
+        n(8) = 0.125 * (one - s1) * (one + s2) * (one + s3);
+    }
+    if (eType == 41) {
+        n(1) = 0.25 * (one - s1) * (one - s2);
+        n(2) = 0.25 * (one + s1) * (one - s2);
+        n(3) = 0.25 * (one + s1) * (one + s2);
+        n(4) = 0.25 * (one - s1) * (one + s2);
+        n(5) = one - s1 * s1;
+        n(6) = one - s2 * s2;
+        n(7) = (one - s1 * s1) * (one - s2);
+        n(8) = (one - s2 * s2) * (one + s1);
+        n(9) = (one - s1 * s1) * (one + s2);
+        n(10) = (one - s2 * s2) * (one - s1);
+    }
+}
+
+// r_EvalNs, :94-210
+template <class T> void t_EvalNs(A2<T, 11, 3> &Ns, const T *s, int eType) {
+    const T s1 = s[0], s2 = s[1], s3 = s[2];
+    const T one(1.0);
+    Ns.fill(T(0.0));
+    if (eType == 8) {
+        Ns(1, 1) = -0.125 * (one - s2) * (one - s3);
+        Ns(2, 1) = 0.125 * (one - s2) * (one - s3);
+        Ns(3, 1) = 0.125 * (one + s2) * (one - s3);
+        Ns(4, 1) = -0.125 * (one + s2) * (one - s3);
+        Ns(5, 1) = -0.125 * (one - s2) * (one + s3);
+        Ns(6, 1) = 0.125 * (one - s2) * (one + s3);
+        Ns(7, 1) = 0.125 * (one + s2) * (one + s3);
+        Ns(8, 1) = -0.125 * (one + s2) * (one + s3);
+        Ns(1, 2) = -0.125 * (one - s1) * (one - s3);
+        Ns(2, 2) = -0.125 * (one + s1) * (one - s3);
+        Ns(3, 2) = 0.125 * (one + s1) * (one - s3);
+        Ns(4, 2) = 0.125 * (one - s1) * (one - s3);
+        Ns(5, 2) = -0.125 * (one - s1) * (one + s3);
+        Ns(6, 2) = -0.125 * (one + s1) * (one + s3);
+        Ns(7, 2) = 0.125 * (one + s1) * (one + s3);
+        Ns(8, 2) = 0.125 * (one - s1) * (one + s3);
+        Ns(1, 3) = -0.125 * (one - s1) * (one - s2);
+        Ns(2, 3) = -0.125 * (one + s1) * (one - s2);
+        Ns(3, 3) = -0.125 * (one + s1) * (one + s2);
+        Ns(4, 3) = -0.125 * (one - s1) * (one + s2);
+        Ns(5, 3) = 0.125 * (one - s1) * (one - s2);
+        Ns(6, 3) = 0.125 * (one + s1) * (one - s2);
+        Ns(7, 3) = 0.125 * (one + s1) * (one + s2);
+        Ns(8, 3) = 0.125 * (one - s1) * (one + s2);
+    }
+    if (eType == 41) {
+        Ns(1, 1) = -0.25 * (one - s2);
+        Ns(1, 2) = -0.25 * (one - s1);
+        Ns(2, 1) = 0.25 * (one - s2);
+        Ns(2, 2) = -0.25 * (one + s1);
+        Ns(3, 1) = 0.25 * (one + s2);
+        Ns(3, 2) = 0.25 * (one + s1);
+        Ns(4, 1) = -0.25 * (one + s2);
+        Ns(4, 2) = 0.25 * (one - s1);
+        Ns(5, 1) = -s1 - s1;
+        Ns(6, 2) = -s2 - s2;
+        Ns(7, 1) = (-s1 - s1) * (one - s2);
+        Ns(7, 2) = -(one - s1 * s1);
+        Ns(8, 1) = (one - s2 * s2);
+        Ns(8, 2) = (-s2 - s2) * (one + s1);
+        Ns(9, 1) = (-s1 - s1) * (one + s2);
+        Ns(9, 2) = (one - s1 * s1);
+        Ns(10, 1) = -(one - s2 * s2);
+        Ns(10, 2) = (-s2 - s2) * (one - s1);
+    }
+}
+
+// r_getDetInv, :212-238
+template <class T> T t_getDetInv(A2<T, 3, 3> &I, const A2<T, 3, 3> &A) {
+    T Adj11 = A(2, 2) * A(3, 3) - A(2, 3) * A(3, 2);
+    T Adj12 = A(2, 3) * A(3, 1) - A(2, 1) * A(3, 3);
+    T Adj13 = A(2, 1) * A(3, 2) - A(2, 2) * A(3, 1);
+    T D = A(1, 1) * Adj11 + A(1, 2) * Adj12 + A(1, 3) * Adj13;
+    T Dinv = T(1.0) / D;
+    I(1, 1) = Dinv * Adj11;
+    I(2, 1) = Dinv * Adj12;
+    I(3, 1) = Dinv * Adj13;
+    I(1, 2) = Dinv * (A(1, 3) * A(3, 2) - A(1, 2) * A(3, 3));
+    I(2, 2) = Dinv * (A(1, 1) * A(3, 3) - A(1, 3) * A(3, 1));
+    I(3, 2) = Dinv * (A(1, 2) * A(3, 1) - A(1, 1) * A(3, 2));
+    I(1, 3) = Dinv * (A(1, 2) * A(2, 3) - A(1, 3) * A(2, 2));
+    I(2, 3) = Dinv * (A(1, 3) * A(2, 1) - A(1, 1) * A(2, 3));
+    I(3, 3) = Dinv * (A(1, 1) * A(2, 2) - A(1, 2) * A(2, 1));
+    return D;
+}
+
+// r_getIntPtData, :580-620
+template <class T>
+void t_getIntPtData(A1<T, 11> &Nvec, A2<T, 11, 3> &Nx, T &detJ, const A2<T, 3, 10> &locNds, const T *sPt,
+                    int eType, int numNds) {
+    A2<T, 11, 3> Ns;
+    A2<T, 3, 3> dxds, dsdx;
+    t_EvalN(Nvec, sPt, eType);
+    t_EvalNs(Ns, sPt, eType);
+    dxds.fill(T(0.0));
+    for (int i1 = 1; i1 <= 3; ++i1)
+        for (int i2 = 1; i2 <= 3; ++i2)
+            for (int i3 = 1; i3 <= numNds; ++i3) dxds(i1, i2) = dxds(i1, i2) + locNds(i1, i3) * Ns(i3, i2);
+    if (eType == 41) dxds(3, 3) = T(1.0);
+    detJ = t_getDetInv(dsdx, dxds);
+    Nx.fill(T(0.0));
+    for (int i1 = 1; i1 <= 11; ++i1)
+        for (int i2 = 1; i2 <= 3; ++i2)
+            for (int i3 = 1; i3 <= 3; ++i3) Nx(i1, i2) = Nx(i1, i2) + Ns(i1, i3) * dsdx(i3, i2);
+}
+
+// r_getNLStrain, :622-679
+template <class T>
+void t_getNLStrain(A1<T, 6> &strain, const A2<T, 3, 3> &ux, const A2<T, 11, 3> &Nx, const A2<T, 3, 3> &orient,
+                   int dv, int dv2, const int dofTable[33][2]) {
+    strain.fill(T(0.0));
+    if (dv + dv2 == 0) {
+        A2<T, 3, 3> uxL;
+        uxL.fill(T(0.0));
+        for (int i1 = 1; i1 <= 3; ++i1)
+            for (int i2 = 1; i2 <= 3; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3) uxL(i1, i2) = uxL(i1, i2) + orient(i1, i3) * ux(i3, i2);
+        strain(1) = uxL(1, 1) + 0.5 * (ux(1, 1) * ux(1, 1) + ux(2, 1) * ux(2, 1) + ux(3, 1) * ux(3, 1));
+        strain(2) = uxL(2, 2) + 0.5 * (ux(1, 2) * ux(1, 2) + ux(2, 2) * ux(2, 2) + ux(3, 2) * ux(3, 2));
+        strain(3) = uxL(3, 3) + 0.5 * (ux(1, 3) * ux(1, 3) + ux(2, 3) * ux(2, 3) + ux(3, 3) * ux(3, 3));
+        strain(4) = uxL(1, 2) + uxL(2, 1) + ux(1, 1) * ux(1, 2) + ux(2, 1) * ux(2, 2) + ux(3, 1) * ux(3, 2);
+        strain(5) = uxL(1, 3) + uxL(3, 1) + ux(1, 1) * ux(1, 3) + ux(2, 1) * ux(2, 3) + ux(3, 1) * ux(3, 3);
+        strain(6) = uxL(2, 3) + uxL(3, 2) + ux(1, 3) * ux(1, 2) + ux(2, 3) * ux(2, 2) + ux(3, 3) * ux(3, 2);
+    } else if (dv * dv2 == 0) {
+        int var, nd;
+        if (dv != 0) {
+            var = dofTable[dv - 1][0];
+            nd = dofTable[dv - 1][1];
+        } else {
+            var = dofTable[dv2 - 1][0];
+            nd = dofTable[dv2 - 1][1];
+        }
+        strain(1) = orient(1, var) * Nx(nd, 1) + Nx(nd, 1) * ux(var, 1);
+        strain(2) = orient(2, var) * Nx(nd, 2) + Nx(nd, 2) * ux(var, 2);
+        strain(3) = orient(3, var) * Nx(nd, 3) + Nx(nd, 3) * ux(var, 3);
+        strain(4) = orient(1, var) * Nx(nd, 2) + orient(2, var) * Nx(nd, 1) + Nx(nd, 1) * ux(var, 2) + Nx(nd, 2) * ux(var, 1);
+        strain(5) = orient(1, var) * Nx(nd, 3) + orient(3, var) * Nx(nd, 1) + Nx(nd, 1) * ux(var, 3) + Nx(nd, 3) * ux(var, 1);
+        strain(6) = orient(2, var) * Nx(nd, 3) + orient(3, var) * Nx(nd, 2) + Nx(nd, 2) * ux(var, 3) + Nx(nd, 3) * ux(var, 2);
+    } else {
+        int var = dofTable[dv - 1][0], nd = dofTable[dv - 1][1];
+        int var2 = dofTable[dv2 - 1][0], nd2 = dofTable[dv2 - 1][1];
+        if (var == var2) {
+            strain(1) = Nx(nd, 1) * Nx(nd2, 1);
+            strain(2) = Nx(nd, 2) * Nx(nd2, 2);
+            strain(3) = Nx(nd, 3) * Nx(nd2, 3);
+            strain(4) = Nx(nd, 1) * Nx(nd2, 2) + Nx(nd2, 1) * Nx(nd, 2);
+            strain(5) = Nx(nd, 1) * Nx(nd2, 3) + Nx(nd2, 1) * Nx(nd, 3);
+            strain(6) = Nx(nd, 2) * Nx(nd2, 3) + Nx(nd2, 2) * Nx(nd, 3);
+        }
+    }
+}
+
+// r_getShellDef, :681-697
+template <class T>
+void t_getShellDef(A1<T, 9> &def, const A2<T, 3, 3> &ux, const A1<T, 3> &rot, const A2<T, 3, 3> &rx) {
+    def(1) = ux(1, 1);
+    def(2) = ux(2, 2);
+    def(3) = ux(1, 2) + ux(2, 1);
+    def(4) = rx(2, 1);
+    def(5) = -rx(1, 2);
+    def(6) = rx(2, 2) - rx(1, 1);
+    def(7) = ux(3, 1) + rot(2);
+    def(8) = ux(3, 2) - rot(1);
+    def(9) = 2.0 * rot(3) - ux(2, 1) + ux(1, 2);
+}
+
+// r_getInstOrient, :714-772.  instOri(3,48): column block (a,b) at 12a+3b holds the derivative of
+// the instantaneous frame with respect to rotation components a,b (0 = none); drIdrG(3,16) the
+// corresponding axial vectors.
+template <class T>
+void t_getInstOrient(A2<T, 3, 48> &instOri, A2<T, 3, 16> &drIdrG, const A2<T, 3, 3> &locOri, const A1<T, 3> &rot) {
+    A2<T, 3, 3> tempAl, prod, base;
+    instOri.fill(T(0.0));
+    drIdrG.fill(T(0.0));
+    t_rotateAlpha(base, locOri, rot, 0, 0);
+    for (int j = 1; j <= 3; ++j)
+        for (int i = 1; i <= 3; ++i) instOri(i, j) = base(i, j);
+    auto put = [&](int c0, const A2<T, 3, 3> &m) {
+        for (int j = 1; j <= 3; ++j)
+            for (int i = 1; i <= 3; ++i) instOri(i, c0 + j) = m(i, j);
+    };
+    auto axial = [&](int col) {
+        prod.fill(T(0.0));
+        for (int a = 1; a <= 3; ++a)
+            for (int b = 1; b <= 3; ++b)
+                for (int c = 1; c <= 3; ++c) prod(a, b) = prod(a, b) + tempAl(a, c) * instOri(b, c);
+        drIdrG(1, col) = prod(2, 3);
+        drIdrG(2, col) = prod(3, 1);
+        drIdrG(3, col) = prod(1, 2);
+    };
+    for (int i1 = 1; i1 <= 3; ++i1) {
+        t_rotateAlpha(tempAl, locOri, rot, i1, 0);
+        put(12 * i1, tempAl);
+        put(3 * i1, tempAl);
+        axial(4 * i1);
+        axial(i1);
+        for (int i2 = i1; i2 <= 3; ++i2) {
+            t_rotateAlpha(tempAl, locOri, rot, i1, i2);
+            put(12 * i1 + 3 * i2, tempAl);
+            put(12 * i2 + 3 * i1, tempAl);
+            axial(4 * i1 + i2);
+            axial(4 * i2 + i1);
+        }
+    }
+}
+
+// r_getInstDof, :774-891
+template <class T>
+void t_getInstDof(A2<T, 6, 11> &instU, const A2<T, 6, 11> &globU, const A2<T, 3, 10> &globNds,
+                  const A2<T, 3, 48> &instOri, const A2<T, 3, 3> &locOri, const A1<T, 3> &rot,
+                  const A2<T, 3, 16> &drIdrG, int numNds, const int dofTable[33][2], int dv, int dv2) {
+    if (dv + dv2 == 0) {
+        instU.fill(T(0.0));
+        for (int i1 = 1; i1 <= 3; ++i1)
+            for (int i2 = 1; i2 <= numNds; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3)
+                    instU(i1, i2) = instU(i1, i2) + instOri(i1, i3) * (globU(i3, i2) + globNds(i3, i2)) -
+                                    locOri(i1, i3) * globNds(i3, i2);
+        for (int i1 = 1; i1 <= 33; ++i1) {
+            if (dofTable[i1 - 1][1] > numNds) {
+                int i2 = dofTable[i1 - 1][0], i3 = dofTable[i1 - 1][1];
+                instU(i2, i3) = globU(i2, i3);
+            }
+        }
+        A1<T, 3> delRot;
+        for (int i1 = 1; i1 <= numNds; ++i1) {
+            for (int k = 4; k <= 6; ++k) instU(k, i1) = T(0.0);
+            for (int k = 1; k <= 3; ++k) delRot(k) = globU(3 + k, i1) - rot(k);
+            for (int i2 = 1; i2 <= 3; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3) {
+                    instU(i2 + 3, i1) = instU(i2 + 3, i1) + drIdrG(i2, i3) * delRot(i3);
+                    for (int i4 = 1; i4 <= 3; ++i4) {
+                        int i5 = 4 * i3 + i4;
+                        instU(i2 + 3, i1) = instU(i2 + 3, i1) + 0.5 * drIdrG(i2, i5) * delRot(i3) * delRot(i4);
+                    }
+                }
+        }
+    } else if (dv * dv2 == 0) {
+        int nd, var;
+        if (dv != 0) {
+            nd = dofTable[dv - 1][1];
+            var = dofTable[dv - 1][0];
+        } else {
+            nd = dofTable[dv2 - 1][1];
+            var = dofTable[dv2 - 1][0];
+        }
+        instU.fill(T(0.0));
+        if (var > 0 && var < 4) {
+            if (nd <= numNds) {
+                for (int k = 1; k <= 3; ++k) instU(k, nd) = instOri(k, var);
+            } else {
+                instU(var, nd) = T(1.0);
+            }
+        } else {
+            int i5 = 3 * (var - 3);
+            double nnInv = 1.0 / (double)numNds;
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 1; i2 <= numNds; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3)
+                        instU(i1, i2) = instU(i1, i2) + nnInv * instOri(i1, i5 + i3) * (globU(i3, i2) + globNds(i3, i2));
+            A1<T, 3> delRot, ddelRot;
+            for (int k = 1; k <= 3; ++k) {
+                delRot(k) = globU(3 + k, nd) - rot(k);
+                ddelRot(k) = T(0.0);
+            }
+            ddelRot(var - 3) = T(1.0);
+            if (g_quirk_mean_rot_derivative) {
+                // consistent derivative (not the reference): every node's relative rotation
+                // also depends on the element mean rotation through -1/numNds
+                for (int j = 1; j <= numNds; ++j)
+                    for (int i2 = 1; i2 <= 3; ++i2) instU(i2 + 3, j) = instU(i2 + 3, j) - nnInv * drIdrG(i2, var - 3);
+            }
+            for (int i2 = 1; i2 <= 3; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3) {
+                    instU(i2 + 3, nd) = instU(i2 + 3, nd) + drIdrG(i2, i3) * ddelRot(i3);
+                    for (int i4 = 1; i4 <= 3; ++i4) {
+                        int ii = 4 * i3 + i4;
+                        instU(i2 + 3, nd) = instU(i2 + 3, nd) +
+                                            0.5 * drIdrG(i2, ii) * (ddelRot(i3) * delRot(i4) + delRot(i3) * ddelRot(i4));
+                    }
+                }
+        }
+    } else {
+        int nd, var, nd2, var2;
+        if (dofTable[dv - 1][0] < dofTable[dv2 - 1][0]) {
+            nd = dofTable[dv - 1][1];
+            var = dofTable[dv - 1][0];
+            nd2 = dofTable[dv2 - 1][1];
+            var2 = dofTable[dv2 - 1][0];
+        } else {
+            nd = dofTable[dv2 - 1][1];
+            var = dofTable[dv2 - 1][0];
+            nd2 = dofTable[dv - 1][1];
+            var2 = dofTable[dv - 1][0];
+        }
+        double nnInv = 1.0 / (double)numNds;
+        instU.fill(T(0.0));
+        if (var < 4 && var2 >= 4) {
+            int i1 = 3 * (var2 - 3);
+            for (int k = 1; k <= 3; ++k) instU(k, nd) = nnInv * instOri(k, i1 + var);
+        } else if (var >= 4 && var2 >= 4) {
+            nnInv = nnInv * nnInv;
+            int i1 = 12 * (var - 3) + 3 * (var2 - 3);
+            for (int i2 = 1; i2 <= 3; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3)
+                    for (int i4 = 1; i4 <= numNds; ++i4)
+                        instU(i2, i4) = instU(i2, i4) + instOri(i2, i1 + i3) * (globU(i3, i4) + globNds(i3, i4));
+            for (int i4 = 1; i4 <= numNds; ++i4)
+                for (int k = 1; k <= 6; ++k) instU(k, i4) = nnInv * instU(k, i4);
+            if (nd == nd2) {
+                int ii = 4 * (var - 3) + (var2 - 3);
+                for (int k = 1; k <= 3; ++k) instU(3 + k, nd) = drIdrG(k, ii);
+            }
+        }
+    }
+}
+
+}  // namespace orc

@@ -1,0 +1,133 @@
+"""Known-answer tests of the CPU oracle (mechanics, not reference outputs: the reference ships
+none).  They pin the restatement: rigid-body modes, symmetry, patch test, beam theory, the
+skyline LDL^T and the reference GMRES."""
+import ctypes
+
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from misc_gb300 import model as M
+from oracle import Oracle
+from oracle.oracle import _lib
+
+
+def _rigid_modes_hex(X):
+    modes = []
+    for c in range(3):
+        u = np.zeros((3, 8)); u[c, :] = 1; modes.append(u.ravel())
+    for a, b in [(0, 1), (1, 2), (0, 2)]:
+        u = np.zeros((3, 8)); u[a, :] = -X[:, b]; u[b, :] = X[:, a]; modes.append(u.ravel())
+    return modes
+
+
+def test_hex8_rigid_symmetric_psd():
+    m = M.hex_block(3, 2, 2, lx=1.0, ly=0.7, lz=0.6, seed=3)
+    o = Oracle(m)
+    for el in (1, 5, 12):
+        _, k = o.element(el)
+        K = k[:24, :24]
+        s = np.abs(K).max()
+        assert np.abs(K - K.T).max() <= 1e-14 * s
+        X = m.node_list[m.element_list[el - 1] - 1]
+        for u in _rigid_modes_hex(X):
+            assert np.abs(K @ u).max() <= 1e-12 * s
+        ev = np.linalg.eigvalsh(K)
+        assert ev[6] > 1e-6 * ev[-1] and ev[0] > -1e-12 * ev[-1]
+
+
+def test_hex8_patch_test_linear_field():
+    """A linear displacement field produces no internal force at interior nodes."""
+    m = M.hex_block(3, 3, 3, lx=1.0, ly=1.0, lz=1.0, seed=5, jitter=0.2, sigma=0.0)
+    o = Oracle(m)
+    load, _, mat, cols, _ = o.el_soln_load(1)
+    K = o.csr_scipy(mat, cols)
+    G = np.array([[1e-3, 2e-4, -3e-4], [5e-4, -1e-3, 1e-4], [2e-4, 3e-4, 7e-4]])
+    X = m.node_list
+    U = X @ G.T
+    u = np.zeros(o.n)
+    for a in range(m.num_nodes):
+        for c in range(3):
+            u[o.n_dof_index[a, c] - 1] = U[a, c]
+    f = K @ u
+    interior = [a for a in range(m.num_nodes) if np.all((X[a] > 1e-9) & (X[a] < 1 - 1e-9))]
+    assert interior
+    fi = np.array([f[o.n_dof_index[a, c] - 1] for a in interior for c in range(3)])
+    assert np.abs(fi).max() <= 1e-9 * np.abs(f).max()
+
+
+def test_shell_reference_tangent_omits_mean_rotation_term():
+    """The reference's shell tangent (r_getInstDof rotation derivative) omits the dependence of
+    the element mean rotation on each nodal rotation; rigid rotations then load the element.
+    The oracle keeps that behaviour by default; the diagnostic switch restores invariance."""
+    L = _lib()
+    L.orc_set_quirk.argtypes = [ctypes.c_int, ctypes.c_int]
+    m = M.plate_shell(nx=1, ny=1, lx=1.0, ly=1.0, t=0.1, E=1e6, nu=0.0, clamp=None, y0=0.0)
+    X = m.node_list[m.element_list[0, :4] - 1]
+    u = np.zeros((6, 4)); u[2] = X[:, 1]; u[3] = 1.0   # rigid rotation about x
+    v = np.zeros(33); v[:24] = u.ravel()
+    try:
+        for q, expect_zero in ((0, False), (1, True)):
+            L.orc_set_quirk(1, q)
+            _, k = Oracle(m).element(1)
+            r = np.abs(k @ v).max() / np.abs(k).max()
+            assert (r < 1e-12) == expect_zero
+    finally:
+        L.orc_set_quirk(1, 0)
+
+
+def test_shell_cantilever_beam_theory_with_consistent_tangent():
+    """shellBeam fixture (Working/shellBeamModelInput.yaml): tip load 2, L = 10, t = 0.1, E = 1e6.
+    With the consistent tangent the tip deflection lies between the plate-strip (7.28) and
+    Euler-Bernoulli (8.0) values; the reference's own tangent gives about 31.6."""
+    L = _lib()
+    L.orc_set_quirk.argtypes = [ctypes.c_int, ctypes.c_int]
+    m = M.shell_beam()
+    try:
+        L.orc_set_quirk(1, 1)
+        o = Oracle(m)
+        A, b, *_ = o.static_system()
+        x = spla.spsolve(A.tocsc(), b)
+        w = x[o.n_dof_index[10, 2] - 1]
+        assert 7.2 < w < 8.05
+    finally:
+        L.orc_set_quirk(1, 0)
+    o = Oracle(m)
+    A, b, *_ = o.static_system()
+    w_ref = spla.spsolve(A.tocsc(), b)[o.n_dof_index[10, 2] - 1]
+    assert 30.0 < w_ref < 33.0
+
+
+def test_skyline_ldl_and_reference_gmres():
+    m = M.hex_block(4, 2, 2, lx=1.0, ly=0.5, lz=0.5, seed=1)
+    o = Oracle(m)
+    A, b, mat, cols, mm, mr = o.static_system()
+    lt = o.convert_to_ltri(mat, cols, mm)
+    fac = o.ldl_fact(lt, o.lt_range)
+    # the factor solves the skyline matrix itself exactly
+    n = o.n
+    S = np.zeros((n, n))
+    for i in range(n):
+        r0, r1 = o.lt_range[i], o.lt_range[i + 1]
+        S[i, i - (r1 - r0) + 1:i + 1] = lt[r0:r1]
+    S = np.tril(S) + np.tril(S, -1).T
+    y = np.random.default_rng(0).standard_normal(n)
+    x = o.ldl_solve(fac, o.lt_range, S @ y)
+    assert np.linalg.norm(x - y) <= 1e-8 * np.linalg.norm(y)
+    xd = spla.spsolve(A.tocsc(), b)
+    xg, cyc = o.gmres(mat, cols, mm, fac, b)
+    assert np.linalg.norm(xg - xd) <= 1e-6 * np.linalg.norm(xd)
+
+
+def test_solver_max_bw_wraps_like_fortran_integers():
+    """solverMaxBW = min b with b^3 >= 27*numNodes^2 in 32-bit wrapping integers
+    (Working/AStrO_runJob.f90:106-114): 155 for 369 nodes, 1289 for 70,785 nodes (wrapped)."""
+    m = M.config1()
+    assert Oracle(m).solver_max_bw == 155
+    nn = 70785
+    t = np.int64(27) * nn * nn
+    t32 = np.int64(((t + 2**31) % 2**32) - 2**31)
+    b = 1
+    while b**3 < t32:
+        b += 1
+    assert b == 1289
