@@ -146,6 +146,13 @@ int astro_prep_host(const astro_model *model, astro_dims *dims, int32_t *current
                     int32_t *el_mat_cols, int32_t *num_colors);
 
 int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
+/* Behaviour switches.  ASTRO_OPT_SHELL_MEAN_ROT_TERM (default 0 = the reference): when 1, the
+ * shell4 rotation derivative also carries the dependence of the element mean rotation on each
+ * nodal rotation, which r_getInstDof (Working/AStrO_r_elementEqns.f90:835-858) omits; with it the
+ * tangent is invariant under rigid rotations.  No counterpart in the reference. */
+#define ASTRO_OPT_SHELL_MEAN_ROT_TERM 1
+int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value);
+
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that order their own work
  * or record timing events around the library's kernels. */
 void *astro_ctx_stream(const astro_ctx *ctx);

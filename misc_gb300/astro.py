@@ -292,3 +292,13 @@ class AstroGPU:
 
 __all__ = ["AstroGPU", "AstroError", "load_library", "make_state", "AstroStateC", "SOLVER_GMRES_JACOBI_FP64",
            "SOLVER_FGMRES_MIXED", "SOLVER_FGMRES_LEARNED"]
+
+
+def _set_option(self, option, value):
+    self.L.astro_set_option.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    self.L.astro_set_option.restype = C.c_int
+    self._check(self.L.astro_set_option(self.h, option, value))
+
+
+AstroGPU.set_option = _set_option
+OPT_SHELL_MEAN_ROT_TERM = 1

@@ -20,6 +20,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
          "--expt-relaxed-constexpr"]
+if os.environ.get("ASTRO_BOUNDS_CHECK"):
+    FLAGS += ["-DASTRO_BOUNDS_CHECK"]
+    BUILD = BUILD + "_checked"
 
 
 def lib_path():

@@ -49,6 +49,8 @@ struct AstroPrep {
     // colouring
     int ncolors = 0;
     std::vector<int> colorPtr, colorEls;  // colorEls: 0-based element ids grouped by colour
+    // bit (a*npe+b) of elFirst[e]: element e is the first (in colour order) to touch block (a,b)
+    std::vector<unsigned long long> elFirst;
     // reference CSR position of each (block, column component): elMatRange(dof-1) excluded, i.e.
     // position within the row, 0-based; size nb*dpn
     std::vector<int> csrPosInRow;
@@ -76,7 +78,7 @@ struct astro_ctx {
     // device model
     DevBuf d_nodes, d_elist, d_elMat, d_esec, d_secABD, d_secOrient, d_colorEls, d_elBlk;
     DevBuf d_rank;          // currentRank (N) 1-based
-    DevBuf d_bRowPtr, d_bCol, d_bRow, d_etype;
+    DevBuf d_bRowPtr, d_bCol, d_bRow, d_etype, d_elFirst;
     DevBuf d_K64, d_K32;    // BSR values
     int haveK64 = 0, haveK32 = 0;
     DevBuf d_csrPos, d_elMatRangeRank;  // export tables
@@ -116,8 +118,15 @@ int astro_prep_build(astro_ctx *c, const astro_model *m);
 // kernels' host entry points
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store);           // elem_hex8.cu
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *ke_host); // elem_hex8.cu
-int launch_shell4_assemble(astro_ctx *ctx, const astro_state *s, double *d_loadInt, double *d_intLoad,
-                           int buildMat, double *ke_host, double *ru_host);  // elem_shell4.cu
+// device state of a shell evaluation (internal layout; any pointer may be null = zeros)
+struct ShellDevState {
+    const double *disp = nullptr, *pdisp = nullptr, *pvel = nullptr, *pacc = nullptr;
+    const double *idisp = nullptr, *pidisp = nullptr;
+    int dynamic = 0;
+    double beta = 0.25, gamma = 0.5, delT = 0.0;
+};
+int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &s, double *d_loadInt, double *d_intLoad,
+                           int buildMat, double *d_ke, double *d_ru);  // elem_shell4.cu
 int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // elem_shell4.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu
 int export_csr(astro_ctx *ctx, double *elastic_mat, int32_t *el_mat_cols);  // assemble.cu

@@ -59,7 +59,7 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 static void free_all(astro_ctx *c) {
     DevBuf *bufs[] = {&c->d_nodes,  &c->d_elist,   &c->d_elMat,   &c->d_esec,    &c->d_secABD,   &c->d_secOrient,
                       &c->d_colorEls, &c->d_elBlk, &c->d_rank,    &c->d_bRowPtr, &c->d_bCol,     &c->d_bRow,
-                      &c->d_etype,  &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
+                      &c->d_etype,  &c->d_elFirst, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
                       &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status};
@@ -172,6 +172,7 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
     UP(d_bRow, bRow);
     UP(d_colorEls, colorEls);
     UP(d_elBlk, P.elBlk);
+    UP(d_elFirst, P.elFirst);
     UP(d_csrPos, P.csrPosInRow);
     UP(d_elMatRangeRank, P.elMatRange);
 #undef UP
@@ -258,6 +259,29 @@ static int state_vec_up(astro_ctx *ctx, const double *h, DevBuf &dst) {
     return rc;
 }
 
+// Shell evaluation state on the device: nodal vectors converted to the internal layout (in S),
+// internal-DOF vectors uploaded as they are (all elements are shell4, 8 internal DOF each).
+static int shell_state(astro_ctx *ctx, const astro_state *state, DevState &S, ShellDevState &ds) {
+    int rc;
+    if (!state) return ASTRO_OK;
+    const size_t ni = (size_t)ctx->P.intVecSize;
+    if (state->internal_disp && (rc = upload(ctx, S.idisp, state->internal_disp, sizeof(double) * ni))) return rc;
+    if (state->prev_int_disp && (rc = upload(ctx, S.pidisp, state->prev_int_disp, sizeof(double) * ni))) return rc;
+    ds.disp = S.disp.p ? dptr<double>(S.disp) : nullptr;
+    ds.pdisp = S.pdisp.p ? dptr<double>(S.pdisp) : nullptr;
+    ds.pvel = S.pvel.p ? dptr<double>(S.pvel) : nullptr;
+    ds.pacc = S.pacc.p ? dptr<double>(S.pacc) : nullptr;
+    ds.idisp = S.idisp.p ? dptr<double>(S.idisp) : nullptr;
+    ds.pidisp = S.pidisp.p ? dptr<double>(S.pidisp) : nullptr;
+    ds.dynamic = state->dynamic;
+    ds.beta = state->nm_beta;
+    ds.gamma = state->nm_gamma;
+    ds.delT = state->del_t;
+    if (ds.dynamic && !(ds.delT > 0.0 && ds.beta > 0.0))
+        return set_err(ctx, ASTRO_ERR_ARG, "dynamic evaluation needs del_t > 0 and nm_beta > 0");
+    return ASTRO_OK;
+}
+
 extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro_state *state, double *elastic_load,
                                   double *int_elastic_load, double *elastic_mat, int32_t *el_mat_cols,
                                   double *int_elastic_mat) {
@@ -280,6 +304,8 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
         if ((rc = ensure_K(ctx, 2))) return rc;
         if ((rc = bsr_zero(ctx, 2))) return rc;
     }
+    if (state && state->dynamic && ctx->hasSolid)
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
     if (ctx->hasSolid) {
         rc = hex8_soln_load(ctx, build_mat == 1, S.disp.p ? dptr<double>(S.disp) : nullptr, dptr<double>(dl));
     } else {
@@ -287,7 +313,9 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
         if (int_elastic_load && P.intVecSize) {
             if ((rc = upload(ctx, il, int_elastic_load, sizeof(double) * P.intVecSize))) return rc;
         }
-        rc = launch_shell4_assemble(ctx, state, dptr<double>(dl), il.p ? dptr<double>(il) : nullptr, build_mat == 1,
+        ShellDevState ds;
+        if ((rc = shell_state(ctx, state, S, ds))) return rc;
+        rc = launch_shell4_assemble(ctx, ds, dptr<double>(dl), il.p ? dptr<double>(il) : nullptr, build_mat == 1,
                                     nullptr, nullptr);
         if (!rc && il.p)
             rc = cuda_check(ctx, cudaMemcpy(int_elastic_load, il.p, sizeof(double) * P.intVecSize, cudaMemcpyDeviceToHost),
@@ -324,7 +352,7 @@ extern "C" int astro_assemble_fp32(astro_ctx *ctx) {
     if (!ctx->hasSolid) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 assembly is implemented for brick8 meshes");
     int rc;
     if ((rc = ensure_K(ctx, 1))) return rc;
-    if ((rc = bsr_zero(ctx, 1))) return rc;
+    // every block is written first by its first-touching element: no zeroing pass
     if ((rc = launch_hex8_assemble(ctx, 32, 1))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->haveK32 = 1;
@@ -334,9 +362,7 @@ extern "C" int astro_assemble_fp32(astro_ctx *ctx) {
 // Timed-path variant used by the benchmark: assembly only, no synchronisation.
 extern "C" int astro_assemble_fp32_async(astro_ctx *ctx) {
     if (!ctx || !ctx->d_K32.p) return ASTRO_ERR_STATE;
-    int rc = bsr_zero(ctx, 1);
-    if (!rc) rc = launch_hex8_assemble(ctx, 32, 1);
-    return rc;
+    return launch_hex8_assemble(ctx, 32, 1);
 }
 
 extern "C" int astro_element_matrices(astro_ctx *ctx, int32_t precision, const astro_state *state, double *ke_out,
@@ -359,7 +385,9 @@ extern "C" int astro_element_matrices(astro_ctx *ctx, int32_t precision, const a
         }
     } else {
         if (precision == 32) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 shell kernel not provided");
-        rc = launch_shell4_assemble(ctx, state, nullptr, nullptr, 1, dptr<double>(dk), dr.p ? dptr<double>(dr) : nullptr);
+        ShellDevState ds;
+        if ((rc = shell_state(ctx, state, S, ds))) return rc;
+        rc = launch_shell4_assemble(ctx, ds, nullptr, nullptr, 1, dptr<double>(dk), dr.p ? dptr<double>(dr) : nullptr);
     }
     if (rc) return rc;
     CK(cudaMemcpyAsync(ke_out, dk.p, sizeof(double) * 576 * (size_t)P.E, cudaMemcpyDeviceToHost, ctx->stream));
@@ -580,4 +608,28 @@ extern "C" int astro_prep_host(const astro_model *m, astro_dims *dims, int32_t *
                     }
     }
     return ASTRO_OK;
+}
+
+int shell_kernel_attrs(char *buf, int len);
+// Kernel resource attributes and runtime limits (diagnostics; launches nothing).
+extern "C" int astro_debug_info(char *buf, int32_t len) {
+    if (!buf || len <= 0) return ASTRO_ERR_ARG;
+    return shell_kernel_attrs(buf, len);
+}
+
+// Status word written by bounds-checked builds (0 = no violation, else the site number).
+extern "C" int astro_debug_status(astro_ctx *ctx, int32_t *status) {
+    if (!ctx || !status) return ASTRO_ERR_ARG;
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(status, ctx->d_status.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    return ASTRO_OK;
+}
+
+extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
+    if (!ctx) return ASTRO_ERR_ARG;
+    if (option == ASTRO_OPT_SHELL_MEAN_ROT_TERM) {
+        ctx->quirkShellMeanRot = value ? 1 : 0;
+        return ASTRO_OK;
+    }
+    return set_err(ctx, ASTRO_ERR_ARG, "unknown option");
 }

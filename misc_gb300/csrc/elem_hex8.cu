@@ -296,7 +296,157 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// FP32 assembly kernel for the zero state with identity section orientation (the small-strain
+// stiffness of the brick8 element, the mixed-precision solver's matrix).  Per element (one warp):
+//   * C from the orthotropic engineering constants in closed form (3x3 normal block inverse,
+//     shear moduli on the diagonal), the same matrix r_getMaterialStiffness forms by LU;
+//   * the eight Gauss-point Jacobians in two rounds: lane (g, a) with g = lane/8 (+4), a = lane%8
+//     forms node a's contribution to J at point g and the eight lanes of a point reduce it with
+//     three xor-shuffles, then invert it and write Nx(a) to shared memory;
+//   * lane l accumulates the node-pair blocks (l/8, l%8) and (l/8+4, l%8) over the points with
+//     the sparse orthotropic B^T C B (about 27 FMA per block per point);
+//   * the 3x3 blocks are added into the block-CSR matrix; the first element (in colour order) to
+//     touch a block writes it, so an assembly pass needs no zeroing, and the old values of the
+//     other blocks are fetched before the arithmetic so their latency overlaps it.
+constexpr int kFW = 8;  // warps per CTA
+
+struct Hex8FastArgs {
+    const double *nodes;
+    const int *elist;
+    const int *colorEls;
+    int count;
+    const int *elBlk;
+    const unsigned long long *elFirst;
+    const double *elMat;
+    float *K;          // BSR FP32 or null
+    double *keOut;     // element matrices (E,24,24) column-major, element DOF order, or null
+};
+
+__global__ void __launch_bounds__(32 * kFW) hex8_fast_kernel(Hex8FastArgs A) {
+    __shared__ float sNx[kFW][8][8][3];
+    __shared__ float sDet[kFW][8];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int item = blockIdx.x * kFW + w;
+    if (item >= A.count) return;
+    const int e = A.colorEls[item];
+    const int a0 = lane >> 3, a1 = a0 + 4, b = lane & 7;
+    // block targets and old values (prefetched)
+    const int k0 = A.elBlk[64 * (size_t)e + a0 * 8 + b], k1 = A.elBlk[64 * (size_t)e + a1 * 8 + b];
+    const unsigned long long first = A.elFirst[e];
+    const bool f0 = (first >> (a0 * 8 + b)) & 1ull, f1 = (first >> (a1 * 8 + b)) & 1ull;
+    float o0[9], o1[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        o0[q] = (A.K && !f0) ? A.K[9 * (size_t)k0 + q] : 0.f;
+        o1[q] = (A.K && !f1) ? A.K[9 * (size_t)k1 + q] : 0.f;
+    }
+    // material: closed-form orthotropic C
+    const double *ep = A.elMat + 9 * (size_t)e;
+    const float E1 = (float)ep[0], E2 = (float)ep[1], E3 = (float)ep[2];
+    const float s11 = 1.f / E1, s22 = 1.f / E2, s33 = 1.f / E3;
+    const float s12 = -(float)ep[3] / E1, s13 = -(float)ep[4] / E1, s23 = -(float)ep[5] / E2;
+    const float c11c = s22 * s33 - s23 * s23, c12c = s13 * s23 - s12 * s33, c13c = s12 * s23 - s13 * s22;
+    const float det = s11 * c11c + s12 * c12c + s13 * c13c, id = 1.f / det;
+    const float C11 = c11c * id, C12 = c12c * id, C13 = c13c * id;
+    const float C22 = (s11 * s33 - s13 * s13) * id, C23 = (s13 * s12 - s11 * s23) * id;
+    const float C33 = (s11 * s22 - s12 * s12) * id;
+    const float C44 = (float)ep[6], C55 = (float)ep[7], C66 = (float)ep[8];
+    // node a = lane & 7 coordinates
+    const int na = A.elist[8 * (size_t)e + b];
+    const float X0 = (float)A.nodes[3 * (size_t)(na - 1)], X1 = (float)A.nodes[3 * (size_t)(na - 1) + 1],
+                X2 = (float)A.nodes[3 * (size_t)(na - 1) + 2];
+    const float sa = (b == 1 || b == 2 || b == 5 || b == 6) ? 1.f : -1.f;
+    const float ta = (b == 2 || b == 3 || b == 6 || b == 7) ? 1.f : -1.f;
+    const float ua = (b >= 4) ? 1.f : -1.f;
+    const float g = 0.57735026918962576451f;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const int gp = a0 + 4 * half;  // Gauss point of this 8-lane group
+        const float s1 = (gp & 1) ? g : -g, s2 = (gp & 2) ? g : -g, s3 = (gp & 4) ? g : -g;
+        const float n0 = 0.125f * sa * (1.f + ta * s2) * (1.f + ua * s3);
+        const float n1 = 0.125f * ta * (1.f + sa * s1) * (1.f + ua * s3);
+        const float n2 = 0.125f * ua * (1.f + sa * s1) * (1.f + ta * s2);
+        float J[9] = {X0 * n0, X0 * n1, X0 * n2, X1 * n0, X1 * n1, X1 * n2, X2 * n0, X2 * n1, X2 * n2};
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            J[q] += __shfl_xor_sync(0xffffffffu, J[q], 1);
+            J[q] += __shfl_xor_sync(0xffffffffu, J[q], 2);
+            J[q] += __shfl_xor_sync(0xffffffffu, J[q], 4);
+        }
+        const float a11 = J[4] * J[8] - J[5] * J[7], a12 = J[5] * J[6] - J[3] * J[8], a13 = J[3] * J[7] - J[4] * J[6];
+        const float dt = J[0] * a11 + J[1] * a12 + J[2] * a13, di = 1.f / dt;
+        const float I00 = di * a11, I10 = di * a12, I20 = di * a13;
+        const float I01 = di * (J[2] * J[7] - J[1] * J[8]), I11 = di * (J[0] * J[8] - J[2] * J[6]),
+                    I21 = di * (J[1] * J[6] - J[0] * J[7]);
+        const float I02 = di * (J[1] * J[5] - J[2] * J[4]), I12 = di * (J[2] * J[3] - J[0] * J[5]),
+                    I22 = di * (J[0] * J[4] - J[1] * J[3]);
+        sNx[w][gp][b][0] = n0 * I00 + n1 * I10 + n2 * I20;
+        sNx[w][gp][b][1] = n0 * I01 + n1 * I11 + n2 * I21;
+        sNx[w][gp][b][2] = n0 * I02 + n1 * I12 + n2 * I22;
+        if (b == 0) sDet[w][gp] = dt;
+    }
+    __syncwarp();
+    float K0[9] = {}, K1[9] = {};
+#pragma unroll
+    for (int gp = 0; gp < 8; ++gp) {
+        const float wd = sDet[w][gp];
+        const float h0 = sNx[w][gp][b][0] * wd, h1 = sNx[w][gp][b][1] * wd, h2 = sNx[w][gp][b][2] * wd;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int a = half ? a1 : a0;
+            const float g0 = sNx[w][gp][a][0], g1 = sNx[w][gp][a][1], g2 = sNx[w][gp][a][2];
+            float *Kb = half ? K1 : K0;
+            Kb[0] += g0 * C11 * h0 + g1 * C44 * h1 + g2 * C55 * h2;
+            Kb[1] += g0 * C12 * h1 + g1 * C44 * h0;
+            Kb[2] += g0 * C13 * h2 + g2 * C55 * h0;
+            Kb[3] += g1 * C12 * h0 + g0 * C44 * h1;
+            Kb[4] += g1 * C22 * h1 + g0 * C44 * h0 + g2 * C66 * h2;
+            Kb[5] += g1 * C23 * h2 + g2 * C66 * h1;
+            Kb[6] += g2 * C13 * h0 + g0 * C55 * h2;
+            Kb[7] += g2 * C23 * h1 + g1 * C66 * h2;
+            Kb[8] += g2 * C33 * h2 + g0 * C55 * h0 + g1 * C66 * h1;
+        }
+    }
+    if (A.K) {
+        float *d0 = A.K + 9 * (size_t)k0, *d1 = A.K + 9 * (size_t)k1;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            d0[q] = o0[q] + K0[q];
+            d1[q] = o1[q] + K1[q];
+        }
+    }
+    if (A.keOut) {
+        double *ke = A.keOut + 576 * (size_t)e;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                ke[(size_t)(8 * j + b) * 24 + (8 * i + a0)] = (double)K0[3 * i + j];
+                ke[(size_t)(8 * j + b) * 24 + (8 * i + a1)] = (double)K1[3 * i + j];
+            }
+    }
+}
+
 }  // namespace
+
+static int hex8_fast_run(astro_ctx *ctx, float *K, double *d_ke) {
+    const AstroPrep &P = ctx->P;
+    Hex8FastArgs A;
+    A.nodes = dptr<double>(ctx->d_nodes);
+    A.elist = dptr<int>(ctx->d_elist);
+    A.elBlk = dptr<int>(ctx->d_elBlk);
+    A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
+    A.elMat = dptr<double>(ctx->d_elMat);
+    A.K = K;
+    A.keOut = d_ke;
+    for (int col = 0; col < P.ncolors; ++col) {
+        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+        if (!cnt) continue;
+        A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+        A.count = cnt;
+        hex8_fast_kernel<<<(cnt + kFW - 1) / kFW, 32 * kFW, 0, ctx->stream>>>(A);
+    }
+    return cuda_check(ctx, cudaGetLastError(), "hex8 fast kernel launch");
+}
 
 // precision 64: general FP64 kernel (state, orientation); 32: FP32 kernel at zero state.
 // store bit 1: FP32 BSR, bit 2: FP64 BSR (the FP32 kernel adds its values into both when asked).
@@ -347,8 +497,11 @@ static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_di
 }
 
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
-    if (precision == 32 && !ctx->orientIdentity)
-        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 brick8 kernel needs identity section orientation");
+    if (precision == 32) {
+        if (!ctx->orientIdentity)
+            return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 brick8 kernel needs identity section orientation");
+        return hex8_fast_run(ctx, (store & 1) ? dptr<float>(ctx->d_K32) : nullptr, nullptr);
+    }
     return hex8_run(ctx, precision, store, nullptr, nullptr, nullptr, nullptr);
 }
 
@@ -357,6 +510,11 @@ int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d
 }
 
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
+    if (precision == 32) {
+        if (!ctx->orientIdentity)
+            return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 brick8 kernel needs identity section orientation");
+        return hex8_fast_run(ctx, nullptr, d_ke);
+    }
     return hex8_run(ctx, precision, 0, nullptr, nullptr, d_ke, nullptr);
 }
 

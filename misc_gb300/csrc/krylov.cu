@@ -2,56 +2,56 @@
 //
 //   * K is the device block-CSR matrix (dpn x dpn blocks, FP64 or FP32 values); C^T C (the
 //     scaled penalty of scaleElasticMPC) is kept in FP64 as a per-block-row list and fused into
-//     the SpMV;
-//   * preconditioner: Jacobi, applied on the right (A D^-1 y = b, x = D^-1 y), so the Arnoldi
-//     residual estimate is the residual of the unpreconditioned system;
+//     the SpMV, which runs one warp per block row (coalesced block values, gathered x);
+//   * preconditioner: Jacobi on the right (A D^-1 y = b, x = D^-1 y), so the Arnoldi residual
+//     estimate is the residual of the unpreconditioned system;
 //   * orthogonalisation: classical Gram-Schmidt with one re-orthogonalisation (CGS2).  The Krylov
-//     basis is stored row-interleaved, V[i*ldv + k], so the per-row work of every pass (SpMV
-//     output dotted with all basis vectors, basis update, norm) reads contiguous rows: one warp
-//     per block row, lanes over basis vectors.  Dot products are reduced deterministically
-//     (per-CTA partials, then one reduction CTA).  Givens rotations and the convergence test run
-//     on the device; one Arnoldi step is 6 launches and a restart cycle is captured once as a
-//     CUDA graph and replayed, the host reading one status word per cycle;
-//   * precision: the plain solver runs everything in FP64 (the comparator).  The mixed solver
-//     runs the Krylov cycles in FP32 (FP32 matrix and basis, FP64 dot accumulation) inside an
-//     FP64 iterative refinement whose residual b - A x is formed in FP64.
-// The reference's own gMRes (Working/AStrO_solvers.f90:128-297) is restated separately in
-// refgmres.cu; this file implements the spec comparator and its mixed-precision variant.
+//     basis is stored vector-major (V[k*ld + i]); every pass is bandwidth-shaped: the dot
+//     products stage a chunk of w in shared memory and let each warp stream whole basis vectors
+//     over that chunk (one warp reduction per vector), the updates run one thread per row.
+//     Dot products are reduced deterministically (per-CTA partials, then one reduction CTA).
+//     Givens rotations and the stopping test run on the device; one Arnoldi step is 7 launches
+//     and a restart cycle is captured once as a CUDA graph and replayed, the host reading one
+//     status word per cycle;
+//   * precision: the plain solver runs in FP64 throughout (the comparator).  The mixed solver
+//     runs the Krylov cycles in FP32 (FP32 matrix and basis; dot products accumulated in FP64)
+//     inside an FP64 iterative refinement whose residual b - A x is formed in FP64.
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "astro_internal.h"
 
 namespace {
 
 constexpr int kMaxM = 64;
-constexpr int kCtas = 608;  // 4 x 152 SMs
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+constexpr int kChunk = 256;   // rows per CTA in the dot-product passes (one row per thread)
 
 struct GmresCtl {
     double H[(kMaxM + 1) * kMaxM];  // column-major (m+1) x m, Givens-rotated in place
     double cs[kMaxM], sn[kMaxM], g[kMaxM + 1];
     double h1[kMaxM + 1];
     double y[kMaxM];
-    double inv;      // 1 / ||w|| of the last step
+    double inv;      // 1 / ||w|| of the last step (scales w into the next basis vector)
     double target;   // absolute residual target
     double resest;   // |g[j]| after the last step
-    int j;           // number of completed Arnoldi steps in this cycle
-    int done;        // 1 = converged or broke down: later steps are no-ops
+    int j;           // completed Arnoldi steps in this cycle
+    int done;        // converged / broke down / cycle full: later steps are no-ops
     int breakdown;
     int nonfinite;
 };
 
 template <class TM> struct Op {
-    const int *rowPtr;  // block rows (N+1)
-    const int *col;     // block columns
-    const TM *K;        // values
-    const int *penPtr;  // (N+1) penalty entries per block row
-    const int *penRow;  // component within the block row
-    const int *penCol;  // internal column index
+    const int *rowPtr;
+    const int *col;
+    const TM *K;
+    const int *penPtr;  // (N+1) penalty entries per block row, or null
+    const int *penRow;
+    const int *penCol;
     const double *penVal;
-    const double *dinv; // Jacobi (n)
+    const double *dinv;  // Jacobi inverse diagonal (n) or null
     int N, dpn;
 };
 
@@ -60,32 +60,48 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// y_r = sum over the block row of K x (x optionally scaled by dinv and by a scalar), plus the
-// penalty rows.  Computed by one warp, result in all lanes (dpn values).
+// y_r = (A (s * dinv .* x))_r for block row r, one warp; result in all lanes.
 template <class TM, class TX, int DPN>
-__device__ __forceinline__ void row_apply(const Op<TM> &op, int r, const TX *x, double xs, bool scale, double out[DPN]) {
+__device__ __forceinline__ void row_apply(const Op<TM> &op, int r, const TX *__restrict__ x, double xs, double out[DPN]) {
     const int b0 = op.rowPtr[r], b1 = op.rowPtr[r + 1];
     const int lane = threadIdx.x & 31;
     double acc[DPN];
 #pragma unroll
     for (int i = 0; i < DPN; ++i) acc[i] = 0.0;
     const int nval = (b1 - b0) * DPN * DPN;
-    const TM *Kr = op.K + (size_t)b0 * DPN * DPN;
-    for (int t = lane; t < nval; t += 32) {
-        const int blk = t / (DPN * DPN), rem = t - blk * (DPN * DPN);
-        const int i = rem / DPN, j = rem - i * DPN;
-        const int c = op.col[b0 + blk] * DPN + j;
-        double xv = (double)x[c] * xs;
-        if (scale) xv *= op.dinv[c];
-        const double p = (double)Kr[t] * xv;
+    const TM *__restrict__ Kr = op.K + (size_t)b0 * DPN * DPN;
+    // four values per lane in flight: index loads, then gathers, then products
+    for (int t0 = lane; t0 < nval; t0 += 128) {
+        int cc[4], ii[4];
+        double kv[4];
 #pragma unroll
-        for (int q = 0; q < DPN; ++q) acc[q] += (q == i) ? p : 0.0;
+        for (int u = 0; u < 4; ++u) {
+            const int t = t0 + 32 * u;
+            const bool ok = t < nval;
+            const int tt = ok ? t : 0;
+            const int blk = tt / (DPN * DPN), rem = tt - blk * (DPN * DPN);
+            ii[u] = ok ? rem / DPN : -1;
+            cc[u] = __ldg(op.col + b0 + blk) * DPN + (rem - (rem / DPN) * DPN);
+            kv[u] = ok ? (double)Kr[tt] : 0.0;
+        }
+        double xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            xv[u] = (double)x[cc[u]] * xs;
+            if (op.dinv) xv[u] *= op.dinv[cc[u]];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const double p = kv[u] * xv[u];
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) acc[q] += (q == ii[u]) ? p : 0.0;
+        }
     }
     if (op.penPtr) {
         for (int t = op.penPtr[r] + lane; t < op.penPtr[r + 1]; t += 32) {
             const int c = op.penCol[t];
             double xv = (double)x[c] * xs;
-            if (scale) xv *= op.dinv[c];
+            if (op.dinv) xv *= op.dinv[c];
             const double p = op.penVal[t] * xv;
             const int i = op.penRow[t];
 #pragma unroll
@@ -96,124 +112,143 @@ __device__ __forceinline__ void row_apply(const Op<TM> &op, int r, const TX *x, 
     for (int q = 0; q < DPN; ++q) out[q] = warp_sum(acc[q]);
 }
 
-// Step kernel 1: v_j = w_prev * inv (stored into V column j, rows of this warp), then
-// w = A D^-1 v_j, partial dots p[k] = sum_i V[i][k] w[i] for k <= j.
+// v_j = wprev * inv (rows of this warp written to V[j]); w = A D^-1 v_j.  One warp per block row.
 template <class TM, class TV, int DPN>
-__global__ void __launch_bounds__(kThreads) k_arnoldi_spmv(Op<TM> op, TV *V, int ldv, TV *w, const TV *wprev,
-                                                           GmresCtl *ctl, double *part) {
+__global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restrict__ V, size_t ld, const TV *__restrict__ wprev,
+                                                        TV *__restrict__ w, const GmresCtl *__restrict__ ctl) {
     if (ctl->done) return;
+    const int r = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    if (r >= op.N) return;
+    const int lane = threadIdx.x & 31;
     const int j = ctl->j;
     const double inv = ctl->inv;
-    __shared__ double sp[kWarps][kMaxM + 1];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    double p0 = 0.0, p1 = 0.0;  // partial dots for k = lane and k = lane + 32
-    for (int r = blockIdx.x * kWarps + wid; r < op.N; r += gridDim.x * kWarps) {
-        // the SpMV input is v_j = wprev * inv (column j of V is written by the warps owning those rows)
-        double y[DPN];
-        row_apply<TM, TV, DPN>(op, r, wprev, inv, true, y);
+    double y[DPN];
+    row_apply<TM, TV, DPN>(op, r, wprev, inv, y);
+    if (lane < DPN) {
+        const size_t i = (size_t)r * DPN + lane;
+        double yv = 0.0;
 #pragma unroll
-        for (int q = 0; q < DPN; ++q) {
-            const size_t i = (size_t)r * DPN + q;
-            if (lane == 0) {
-                V[i * ldv + j] = (TV)((double)wprev[i] * inv);
-                w[i] = (TV)y[q];
-            }
-        }
-        __syncwarp();
-#pragma unroll
-        for (int q = 0; q < DPN; ++q) {
-            const size_t i = (size_t)r * DPN + q;
-            const double wv = (double)(TV)y[q];
-            if (lane <= j) {
-                const double vk = (lane == j) ? (double)(TV)((double)wprev[i] * inv) : (double)V[i * ldv + lane];
-                p0 += vk * wv;
-            }
-            if (lane + 32 <= j) {
-                const int k = lane + 32;
-                const double vk = (k == j) ? (double)(TV)((double)wprev[i] * inv) : (double)V[i * ldv + k];
-                p1 += vk * wv;
-            }
-        }
-    }
-    sp[wid][lane] = p0;
-    if (lane + 32 <= kMaxM) sp[wid][lane + 32] = p1;
-    __syncthreads();
-    for (int k = threadIdx.x; k <= j; k += blockDim.x) {
-        double s = 0.0;
-        for (int q = 0; q < kWarps; ++q) s += sp[q][k];
-        part[(size_t)blockIdx.x * (kMaxM + 1) + k] = s;
+        for (int q = 0; q < DPN; ++q) yv = (q == lane) ? y[q] : yv;
+        V[(size_t)j * ld + i] = (TV)((double)wprev[i] * inv);
+        w[i] = (TV)yv;
     }
 }
 
-// Reduction of the per-CTA partials into ctl->h1 (pass 1) or added into the Hessenberg column
-// (pass 2).  mode 0: h1 = sum; mode 1: h1 = sum and H[:,j] = h1_prev + sum (keeps h1 = pass-2
-// coefficients for the update).
+// partial dot products of w with V[0..j] over a chunk of rows: part[cta][k]
+template <class TV>
+__device__ __forceinline__ void chunk_dots(int n, const TV *__restrict__ V, size_t ld, const double *sw, int row0, int cnt,
+                                           int j, double *part) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    // kChunk = 256 rows: eight values per lane per basis vector, loaded together
+    for (int k = wid; k <= j; k += kWarps) {
+        const TV *__restrict__ vk = V + (size_t)k * ld + row0;
+        double v[kChunk / 32];
+#pragma unroll
+        for (int u = 0; u < kChunk / 32; ++u) {
+            const int t = lane + 32 * u;
+            v[u] = (t < cnt) ? (double)vk[t] : 0.0;
+        }
+        double s = 0.0;
+#pragma unroll
+        for (int u = 0; u < kChunk / 32; ++u) {
+            const int t = lane + 32 * u;
+            s += (t < cnt) ? v[u] * sw[t] : 0.0;
+        }
+        s = warp_sum(s);
+        if (lane == 0) part[(size_t)blockIdx.x * (kMaxM + 1) + k] = s;
+    }
+}
+
+template <class TV>
+__global__ void __launch_bounds__(kThreads) k_dots(int n, const TV *__restrict__ V, size_t ld, const TV *__restrict__ w,
+                                                   const GmresCtl *__restrict__ ctl, double *part) {
+    if (ctl->done) return;
+    __shared__ double sw[kChunk];
+    const int row0 = blockIdx.x * kChunk;
+    const int cnt = min(kChunk, n - row0);
+    for (int t = threadIdx.x; t < cnt; t += kThreads) sw[t] = (double)w[row0 + t];
+    __syncthreads();
+    chunk_dots<TV>(n, V, ld, sw, row0, cnt, ctl->j, part);
+}
+
+// w -= V[0..j] h1; then either the partial dots with V (mode 0) or the partial ||w||^2 (mode 1)
+template <class TV>
+__global__ void __launch_bounds__(kThreads) k_update(int n, const TV *__restrict__ V, size_t ld, TV *__restrict__ w,
+                                                     const GmresCtl *__restrict__ ctl, double *part, int mode) {
+    if (ctl->done) return;
+    __shared__ double sw[kChunk];
+    __shared__ double sh[kMaxM + 1];
+    __shared__ double sred[kWarps];
+    const int j = ctl->j;
+    for (int k = threadIdx.x; k <= j; k += kThreads) sh[k] = ctl->h1[k];
+    __syncthreads();
+    const int row0 = blockIdx.x * kChunk;
+    const int cnt = min(kChunk, n - row0);
+    double nrm = 0.0;
+    const int t = threadIdx.x;  // kChunk == kThreads: one row per thread
+    if (t < cnt) {
+        const int i = row0 + t;
+        double s = (double)w[i];
+        int k = 0;
+        // eight basis values in flight per thread
+        for (; k + 8 <= j + 1; k += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = (double)V[(size_t)(k + u) * ld + i];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s -= sh[k + u] * v[u];
+        }
+        for (; k <= j; ++k) s -= sh[k] * (double)V[(size_t)k * ld + i];
+        const TV wv = (TV)s;
+        w[i] = wv;
+        sw[t] = (double)wv;
+        nrm = (double)wv * (double)wv;
+    }
+    __syncthreads();
+    if (mode == 0) {
+        chunk_dots<TV>(n, V, ld, sw, row0, cnt, j, part);
+    } else {
+        nrm = warp_sum(nrm);
+        if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = nrm;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int q = 0; q < kWarps; ++q) s += sred[q];
+            part[(size_t)blockIdx.x * (kMaxM + 1)] = s;
+        }
+    }
+}
+
+// sum of part[q*stride + off] over q = lane, lane+32, ... < nparts, eight loads in flight
+__device__ __forceinline__ double lane_sum(const double *part, int nparts, size_t stride, int off, int lane) {
+    double s = 0.0;
+    for (int q0 = lane; q0 < nparts; q0 += 256) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int q = q0 + 32 * u;
+            v[u] = (q < nparts) ? part[(size_t)q * stride + off] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    return s;
+}
+
+// Reduction of the per-CTA dot partials: mode 0 sets h1 and H[:,j], mode 1 sets h1 and adds it
+// to H[:,j].
 __global__ void k_reduce_dots(GmresCtl *ctl, const double *part, int nparts, int mode) {
     if (ctl->done) return;
     const int j = ctl->j;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int k = wid; k <= j; k += blockDim.x >> 5) {
         double s = 0.0;
-        for (int q = lane; q < nparts; q += 32) s += part[(size_t)q * (kMaxM + 1) + k];
+        s = lane_sum(part, nparts, kMaxM + 1, k, lane);
         s = warp_sum(s);
         if (lane == 0) {
-            if (mode == 0) {
-                ctl->h1[k] = s;
-                ctl->H[(size_t)j * (kMaxM + 1) + k] = s;
-            } else {
-                ctl->h1[k] = s;
-                ctl->H[(size_t)j * (kMaxM + 1) + k] += s;
-            }
-        }
-    }
-}
-
-// w' = w - sum_k h1[k] V[i][k]; then either partial dots of w' with V (pass 1 -> 2) or the
-// partial squared norm (final pass).
-template <class TV, int DPN>
-__global__ void __launch_bounds__(kThreads) k_update(int N, TV *V, int ldv, TV *w, GmresCtl *ctl, double *part,
-                                                     int lastPass) {
-    if (ctl->done) return;
-    const int j = ctl->j;
-    __shared__ double sp[kWarps][kMaxM + 1];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const double h0 = (lane <= j) ? ctl->h1[lane] : 0.0;
-    const double h1 = (lane + 32 <= j) ? ctl->h1[lane + 32] : 0.0;
-    double p0 = 0.0, p1 = 0.0, nrm = 0.0;
-    for (int r = blockIdx.x * kWarps + wid; r < N; r += gridDim.x * kWarps) {
-#pragma unroll
-        for (int q = 0; q < DPN; ++q) {
-            const size_t i = (size_t)r * DPN + q;
-            const double v0 = (lane <= j) ? (double)V[i * ldv + lane] : 0.0;
-            const double v1 = (lane + 32 <= j) ? (double)V[i * ldv + lane + 32] : 0.0;
-            double s = warp_sum(h0 * v0 + h1 * v1);
-            const double wn = (double)(TV)((double)w[i] - s);
-            if (lane == 0) w[i] = (TV)wn;
-            if (lastPass) {
-                nrm += (lane == 0) ? wn * wn : 0.0;
-            } else {
-                p0 += v0 * wn;
-                p1 += v1 * wn;
-            }
-        }
-    }
-    if (lastPass) {
-        nrm = warp_sum(nrm);
-        if (lane == 0) sp[wid][0] = nrm;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0.0;
-            for (int q = 0; q < kWarps; ++q) s += sp[q][0];
-            part[(size_t)blockIdx.x * (kMaxM + 1)] = s;
-        }
-    } else {
-        sp[wid][lane] = p0;
-        if (lane + 32 <= kMaxM) sp[wid][lane + 32] = p1;
-        __syncthreads();
-        for (int k = threadIdx.x; k <= j; k += blockDim.x) {
-            double s = 0.0;
-            for (int q = 0; q < kWarps; ++q) s += sp[q][k];
-            part[(size_t)blockIdx.x * (kMaxM + 1) + k] = s;
+            ctl->h1[k] = s;
+            if (mode == 0) ctl->H[(size_t)j * (kMaxM + 1) + k] = s;
+            else ctl->H[(size_t)j * (kMaxM + 1) + k] += s;
         }
     }
 }
@@ -224,7 +259,7 @@ __global__ void k_control(GmresCtl *ctl, const double *part, int nparts, int m) 
     const int j = ctl->j;
     const int lane = threadIdx.x;
     double s = 0.0;
-    for (int q = lane; q < nparts; q += 32) s += part[(size_t)q * (kMaxM + 1)];
+    s = lane_sum(part, nparts, kMaxM + 1, 0, lane);
     s = warp_sum(s);
     if (lane != 0) return;
     const double nrm = sqrt(s);
@@ -256,7 +291,7 @@ __global__ void k_control(GmresCtl *ctl, const double *part, int nparts, int m) 
         ctl->done = 1;
         return;
     }
-    if (nrm == 0.0 || nrm <= 1e-300) {
+    if (!(nrm > 1e-300)) {
         ctl->breakdown = 1;
         ctl->done = 1;
         ctl->inv = 0.0;
@@ -266,7 +301,7 @@ __global__ void k_control(GmresCtl *ctl, const double *part, int nparts, int m) 
     if (ctl->resest <= ctl->target || ctl->j >= m) ctl->done = 1;
 }
 
-// Least squares solve H y = g (upper triangular j x j), one thread.
+// Least squares H y = g (upper triangular j x j), one thread.
 __global__ void k_lsq(GmresCtl *ctl) {
     const int j = ctl->j;
     for (int i = j - 1; i >= 0; --i) {
@@ -276,45 +311,54 @@ __global__ void k_lsq(GmresCtl *ctl) {
     }
 }
 
-// x += D^-1 V y (columns 0..j-1).  x in FP64 or TV.
-template <class TV, class TXo>
-__global__ void __launch_bounds__(kThreads) k_xupdate(int n, const TV *V, int ldv, const double *dinv, GmresCtl *ctl,
-                                                      TXo *x) {
+// x += D^-1 V[0..j-1] y
+template <class TV, class TX>
+__global__ void __launch_bounds__(kThreads) k_xupdate(int n, const TV *__restrict__ V, size_t ld, const double *__restrict__ dinv,
+                                                      const GmresCtl *__restrict__ ctl, TX *__restrict__ x) {
+    __shared__ double sy[kMaxM];
     const int j = ctl->j;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const double y0 = (lane < j) ? ctl->y[lane] : 0.0;
-    const double y1 = (lane + 32 < j) ? ctl->y[lane + 32] : 0.0;
-    for (int i = blockIdx.x * kWarps + wid; i < n; i += gridDim.x * kWarps) {
-        const double v0 = (lane < j) ? (double)V[(size_t)i * ldv + lane] : 0.0;
-        const double v1 = (lane + 32 < j) ? (double)V[(size_t)i * ldv + lane + 32] : 0.0;
-        const double s = warp_sum(y0 * v0 + y1 * v1);
-        if (lane == 0) x[i] = (TXo)((double)x[i] + dinv[i] * s);
+    for (int k = threadIdx.x; k < j; k += kThreads) sy[k] = ctl->y[k];
+    __syncthreads();
+    for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+        double s = 0.0;
+        int k = 0;
+        for (; k + 8 <= j; k += 8) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = (double)V[(size_t)(k + u) * ld + i];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += sy[k + u] * v[u];
+        }
+        for (; k < j; ++k) s += sy[k] * (double)V[(size_t)k * ld + i];
+        x[i] = (TX)((double)x[i] + dinv[i] * s);
     }
 }
 
-// r = b - A x (FP64 arithmetic; K values TM; x in TX), partial ||r||^2 and ||b||^2.
+// r = b - A x (FP64 arithmetic), partial ||r||^2 and ||b||^2 per CTA.  One warp per block row.
 template <class TM, class TX, class TR, int DPN>
-__global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *x, const double *b, TR *r, double *part) {
+__global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *__restrict__ x, const double *__restrict__ b,
+                                                       TR *__restrict__ r, double *part) {
     __shared__ double sp[kWarps][2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int row = blockIdx.x * kWarps + wid;
     double rr = 0.0, bb = 0.0;
-    for (int row = blockIdx.x * kWarps + wid; row < op.N; row += gridDim.x * kWarps) {
+    if (row < op.N) {
         double y[DPN];
         if (x) {
-            row_apply<TM, TX, DPN>(op, row, x, 1.0, false, y);
+            row_apply<TM, TX, DPN>(op, row, x, 1.0, y);
         } else {
 #pragma unroll
             for (int q = 0; q < DPN; ++q) y[q] = 0.0;
         }
-        if (lane == 0) {
+        if (lane < DPN) {
+            const size_t i = (size_t)row * DPN + lane;
+            double yv = 0.0;
 #pragma unroll
-            for (int q = 0; q < DPN; ++q) {
-                const size_t i = (size_t)row * DPN + q;
-                const double v = b[i] - y[q];
-                r[i] = (TR)v;
-                rr += v * v;
-                bb += b[i] * b[i];
-            }
+            for (int q = 0; q < DPN; ++q) yv = (q == lane) ? y[q] : yv;
+            const double v = b[i] - yv;
+            r[i] = (TR)v;
+            rr = v * v;
+            bb = b[i] * b[i];
         }
     }
     rr = warp_sum(rr);
@@ -335,16 +379,12 @@ __global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *x, c
     }
 }
 
-// Start of a cycle: beta = ||r||, inv = 1/beta, g = [beta, 0...], j = 0, done = (beta <= target).
-__global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, double targetAbs, int useTarget) {
+// Start of a cycle: beta = ||r||, inv = 1/beta, g = [beta, 0...], j = 0.
+__global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, double targetAbs) {
     const int lane = threadIdx.x;
-    double a = 0.0, c = 0.0;
-    for (int q = lane; q < nparts; q += 32) {
-        a += part[2 * q];
-        c += part[2 * q + 1];
-    }
+    double a = 0.0;
+    a = lane_sum(part, nparts, 2, 0, lane);
     a = warp_sum(a);
-    c = warp_sum(c);
     if (lane != 0) return;
     const double beta = sqrt(a);
     ctl->j = 0;
@@ -354,15 +394,10 @@ __global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, dou
     for (int k = 1; k <= kMaxM; ++k) ctl->g[k] = 0.0;
     ctl->resest = beta;
     ctl->inv = beta > 0.0 ? 1.0 / beta : 0.0;
-    ctl->target = useTarget ? targetAbs : ctl->target;
-    ctl->done = (beta <= ctl->target || beta == 0.0 || ctl->nonfinite) ? 1 : 0;
-    ctl->h1[kMaxM] = c;  // ||b||^2 of the residual call, for the host
+    ctl->target = targetAbs;
+    ctl->done = (beta <= targetAbs || beta == 0.0 || ctl->nonfinite) ? 1 : 0;
 }
 
-__global__ void k_cast_d2f(const double *a, float *b, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
-}
 __global__ void k_zero_f(float *a, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = 0.f;
@@ -373,8 +408,7 @@ __global__ void k_axpy_f2d(double *x, const float *d, int n) {
 }
 
 // Jacobi inverse diagonal: 1 / (K_ii + (C^T C)_ii)
-template <class TM>
-__global__ void k_dinv(Op<TM> op, double *dinv) {
+template <class TM> __global__ void k_dinv(Op<TM> op, double *dinv) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= op.N) return;
     const int dpn = op.dpn;
@@ -395,9 +429,11 @@ __global__ void k_dinv(Op<TM> op, double *dinv) {
 // ---------------------------------------------------------------------------------------------
 
 struct GmresWork {
-    DevBuf V, w0, w1, part, ctl, dinv, rres, xs, bf;
-    int n = 0, m = 0, ldv = 0;
-    int tv = 0;  // sizeof TV
+    DevBuf V, w0, w1, part, ctl, dinv, rres, xs;
+    int n = 0, m = 0;
+    size_t ld = 0;
+    int nChunks = 0, nRowCtas = 0;
+    std::vector<double> hp;
 };
 
 template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *K, const double *dinv) {
@@ -415,51 +451,65 @@ template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *K, const dou
     return op;
 }
 
-// One restart cycle of m Arnoldi steps (recorded into a graph by the caller).
 template <class TM, class TV, int DPN>
 static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m) {
     cudaStream_t s = ctx->stream;
     TV *V = dptr<TV>(W.V), *wa = dptr<TV>(W.w0), *wb = dptr<TV>(W.w1);
     GmresCtl *ctl = dptr<GmresCtl>(W.ctl);
     double *part = dptr<double>(W.part);
+    const int n = W.n;
     for (int step = 0; step < m; ++step) {
-        TV *wprev = (step % 2 == 0) ? wa : wb;  // holds the unnormalised previous vector
+        TV *wprev = (step % 2 == 0) ? wa : wb;
         TV *wnew = (step % 2 == 0) ? wb : wa;
-        k_arnoldi_spmv<TM, TV, DPN><<<kCtas, kThreads, 0, s>>>(op, V, W.ldv, wnew, wprev, ctl, part);
-        k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, kCtas, 0);
-        k_update<TV, DPN><<<kCtas, kThreads, 0, s>>>(op.N, V, W.ldv, wnew, ctl, part, 0);
-        k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, kCtas, 1);
-        k_update<TV, DPN><<<kCtas, kThreads, 0, s>>>(op.N, V, W.ldv, wnew, ctl, part, 1);
-        k_control<<<1, 32, 0, s>>>(ctl, part, kCtas, m);
+        k_spmv_step<TM, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, V, W.ld, wprev, wnew, ctl);
+        k_dots<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part);
+        k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, W.nChunks, 0);
+        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 0);
+        k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, W.nChunks, 1);
+        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 1);
+        k_control<<<1, 32, 0, s>>>(ctl, part, W.nChunks, m);
     }
 }
 
-// Solve A x = b with restarted Jacobi-GMRES(m) in precision TV on matrix values TM.
-// x (TV) in/out on device, b (double) on device.  Returns status; *iters, *cycles accumulate.
+static double sum_parts(astro_ctx *ctx, GmresWork &W, int which, int *rc) {
+    const int np = W.nRowCtas;
+    W.hp.resize(2 * (size_t)np);
+    cudaError_t e = cudaMemcpyAsync(W.hp.data(), W.part.p, sizeof(double) * 2 * np, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    *rc = cuda_check(ctx, e, "residual partials");
+    double s = 0.0;
+    for (int q = 0; q < np; ++q) s += W.hp[2 * q + which];
+    return s;
+}
+
+// Restarted Jacobi-GMRES(m) on A x = b in precision TV with matrix values TM.  x (TV) in/out
+// on the device, b (double) on the device.
 template <class TM, class TV, int DPN>
-static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const double *b, double rtolAbs,
-                       int maxCycles, int m, int *iters, int *cycles, double *finalRes, int checkTrue) {
+static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const double *b, double tgtAbs, int maxCycles,
+                       int m, int *iters, int *cycles, double *finalRes) {
     cudaStream_t s = ctx->stream;
-    const int n = ctx->P.n;
     Op<TM> op = make_op<TM>(ctx, K, dptr<double>(W.dinv));
+    Op<TM> opNo = make_op<TM>(ctx, K, nullptr);
     GmresCtl *ctl = dptr<GmresCtl>(W.ctl);
     double *part = dptr<double>(W.part);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    // residual r = b - A x into w0 (TV), starting the cycle
-    k_residual<TM, TV, TV, DPN><<<kCtas, kThreads, 0, s>>>(op, x, b, dptr<TV>(W.w0), part);
-    k_cycle_start<<<1, 32, 0, s>>>(ctl, part, kCtas, rtolAbs, 1);
+    k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(opNo, x, b, dptr<TV>(W.w0), part);
+    k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, tgtAbs);
     enqueue_cycle<TM, TV, DPN>(ctx, W, op, m);
     k_lsq<<<1, 1, 0, s>>>(ctl);
-    k_xupdate<TV, TV><<<kCtas, kThreads, 0, s>>>(n, dptr<TV>(W.V), W.ldv, dptr<double>(W.dinv), ctl, x);
+    k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<double>(W.dinv), ctl, x);
     CK(cudaStreamEndCapture(s, &graph));
     CK(cudaGraphInstantiate(&exec, graph, 0));
     int status = ASTRO_OK;
-    GmresCtl hc;
+    struct {
+        double resest;
+        int j, done, breakdown, nonfinite;
+    } hc;
     for (int cyc = 0; cyc < maxCycles; ++cyc) {
         CK(cudaGraphLaunch(exec, s));
-        CK(cudaMemcpyAsync(&hc.resest, &ctl->resest, sizeof(double) + sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&hc, &ctl->resest, sizeof(hc), cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         *iters += hc.j;
         *cycles += 1;
@@ -468,11 +518,9 @@ static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const d
             status = ASTRO_ERR_NAN;
             break;
         }
-        if (hc.resest <= rtolAbs) break;
-        if (hc.breakdown) break;  // exact solution in the Krylov space (lucky breakdown)
+        if (hc.resest <= tgtAbs || hc.breakdown) break;
         if (cyc == maxCycles - 1) status = ASTRO_ERR_MAXIT;
     }
-    (void)checkTrue;
     cudaGraphExecDestroy(exec);
     cudaGraphDestroy(graph);
     return status;
@@ -482,13 +530,15 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
     const int n = ctx->P.n;
     W.n = n;
     W.m = m;
-    W.ldv = ((m + 1 + 3) / 4) * 4;
-    W.tv = tv;
+    W.ld = ((size_t)n + 31) / 32 * 32;
+    W.nChunks = (n + kChunk - 1) / kChunk;
+    W.nRowCtas = (ctx->P.N + kWarps - 1) / kWarps;
+    const size_t nparts = std::max((size_t)W.nChunks * (kMaxM + 1), (size_t)2 * W.nRowCtas);
     int rc;
-    if ((rc = dev_alloc(ctx, W.V, (size_t)n * W.ldv * tv))) return rc;
+    if ((rc = dev_alloc(ctx, W.V, W.ld * (m + 1) * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.w0, (size_t)n * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.w1, (size_t)n * tv))) return rc;
-    if ((rc = dev_alloc(ctx, W.part, sizeof(double) * (size_t)kCtas * (kMaxM + 1)))) return rc;
+    if ((rc = dev_alloc(ctx, W.part, sizeof(double) * nparts))) return rc;
     if ((rc = dev_alloc(ctx, W.ctl, sizeof(GmresCtl)))) return rc;
     if ((rc = dev_alloc(ctx, W.dinv, sizeof(double) * (size_t)n))) return rc;
     if ((rc = dev_alloc(ctx, W.rres, sizeof(double) * (size_t)n))) return rc;
@@ -498,39 +548,31 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
 }
 
 static void work_free(GmresWork &W) {
-    dev_free(W.V);
-    dev_free(W.w0);
-    dev_free(W.w1);
-    dev_free(W.part);
-    dev_free(W.ctl);
-    dev_free(W.dinv);
-    dev_free(W.rres);
-    dev_free(W.xs);
-    dev_free(W.bf);
+    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.part, &W.ctl, &W.dinv, &W.rres, &W.xs};
+    for (auto *x : b) dev_free(*x);
 }
 
-// True FP64 residual ||b - A x|| / ||b|| with A from K64 (kind 64) or K32 (kind 32).
+// r = b - A x with A from K64 (kind 64) or K32 (kind 32); returns ||r||/||b|| (||r|| if b = 0).
 template <int DPN>
 static int true_residual(astro_ctx *ctx, GmresWork &W, int kind, const double *x, const double *b, double *rel,
-                         double *r_out) {
+                         double *r_out, double *rnorm = nullptr, double *bnorm = nullptr) {
     cudaStream_t s = ctx->stream;
     double *part = dptr<double>(W.part);
     if (kind == 64) {
         Op<double> op = make_op<double>(ctx, dptr<double>(ctx->d_K64), nullptr);
-        k_residual<double, double, double, DPN><<<kCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
+        k_residual<double, double, double, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
     } else {
         Op<float> op = make_op<float>(ctx, dptr<float>(ctx->d_K32), nullptr);
-        k_residual<float, double, double, DPN><<<kCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
+        k_residual<float, double, double, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
     }
-    static thread_local double hp[2 * kCtas];
-    CK(cudaMemcpyAsync(hp, part, sizeof(double) * 2 * kCtas, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    double a = 0.0, c = 0.0;
-    for (int q = 0; q < kCtas; ++q) {
-        a += hp[2 * q];
-        c += hp[2 * q + 1];
-    }
+    int rc = ASTRO_OK;
+    const double a = sum_parts(ctx, W, 0, &rc);
+    if (rc) return rc;
+    double c = 0.0;
+    for (int q = 0; q < W.nRowCtas; ++q) c += W.hp[2 * q + 1];
     *rel = (c > 0.0) ? std::sqrt(a / c) : std::sqrt(a);
+    if (rnorm) *rnorm = std::sqrt(a);
+    if (bnorm) *bnorm = std::sqrt(c);
     return ASTRO_OK;
 }
 
@@ -544,62 +586,45 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     GmresWork W;
     int rc = ASTRO_OK;
     int iters = 0, cycles = 0, refinements = 0;
-    double rel = 0.0, est = 0.0;
+    double rel = 0.0, est = 0.0, rn = 0.0, bn = 0.0;
+    const bool fp64 = o->method == ASTRO_SOLVER_GMRES_JACOBI_FP64;
+    if (fp64 && !ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
+    if (!fp64 && !ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
+    if ((rc = work_alloc(ctx, W, m, fp64 ? sizeof(double) : sizeof(float)))) {
+        work_free(W);
+        return rc;
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     cudaEventRecord(e0, ctx->stream);
-    if (o->method == ASTRO_SOLVER_GMRES_JACOBI_FP64) {
-        if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
-        if ((rc = work_alloc(ctx, W, m, sizeof(double)))) return rc;
+    double *r = dptr<double>(W.rres);
+    if (fp64) {
         Op<double> op = make_op<double>(ctx, dptr<double>(ctx->d_K64), nullptr);
         k_dinv<double><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(op, dptr<double>(W.dinv));
-        // ||b|| for the absolute target
-        double bn;
-        double *r = dptr<double>(W.rres);
-        rc = true_residual<DPN>(ctx, W, 64, nullptr, d_b, &bn, r);  // x = NULL -> r = b, rel = 1
-        {
-            // recompute ||b|| explicitly
-            static thread_local double hp[2 * kCtas];
-            CK(cudaMemcpyAsync(hp, W.part.p, sizeof(double) * 2 * kCtas, cudaMemcpyDeviceToHost, ctx->stream));
-            CK(cudaStreamSynchronize(ctx->stream));
-            double c = 0.0;
-            for (int q = 0; q < kCtas; ++q) c += hp[2 * q + 1];
-            bn = std::sqrt(c);
-        }
+        rc = true_residual<DPN>(ctx, W, 64, nullptr, d_b, &rel, r, &rn, &bn);
         const double tgt = o->rtol * bn;
-        for (int outer = 0; outer < 1000 && rc == ASTRO_OK; ++outer) {
-            int it0 = iters;
-            rc = gmres_solve<double, double, DPN>(ctx, W, dptr<double>(ctx->d_K64), d_x, d_b, tgt,
-                                                  maxCycles - cycles, m, &iters, &cycles, &est, 1);
-            (void)it0;
-            int rc2 = true_residual<DPN>(ctx, W, 64, d_x, d_b, &rel, r);
-            if (rc2) {
-                rc = rc2;
+        while (rc == ASTRO_OK) {
+            int grc = gmres_solve<double, double, DPN>(ctx, W, dptr<double>(ctx->d_K64), d_x, d_b, tgt, maxCycles - cycles, m,
+                                                       &iters, &cycles, &est);
+            if ((rc = true_residual<DPN>(ctx, W, 64, d_x, d_b, &rel, r))) break;
+            if (rel <= o->rtol) break;
+            if (grc == ASTRO_ERR_NAN) {
+                rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in GMRES");
                 break;
             }
-            if (rel <= o->rtol) {
-                rc = ASTRO_OK;
-                break;
-            }
-            if (rc == ASTRO_ERR_MAXIT || cycles >= maxCycles) {
+            if (grc == ASTRO_ERR_MAXIT || cycles >= maxCycles) {
                 rc = ASTRO_ERR_MAXIT;
                 break;
             }
-            if (rc == ASTRO_ERR_NAN) break;
-            rc = ASTRO_OK;  // estimate met but true residual not yet: continue cycles
         }
     } else {
-        if (!ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
-        if ((rc = work_alloc(ctx, W, m, sizeof(float)))) return rc;
         Op<float> op32 = make_op<float>(ctx, dptr<float>(ctx->d_K32), nullptr);
         k_dinv<float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(op32, dptr<double>(W.dinv));
-        double *r = dptr<double>(W.rres);
         float *d32 = dptr<float>(W.xs);
         const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
-        for (refinements = 0; refinements < 100; ++refinements) {
-            rc = true_residual<DPN>(ctx, W, 32, d_x, d_b, &rel, r);
-            if (rc) break;
+        for (refinements = 0; refinements < 200; ++refinements) {
+            if ((rc = true_residual<DPN>(ctx, W, 32, d_x, d_b, &rel, r, &rn))) break;
             if (rel <= o->rtol) break;
             if (!std::isfinite(rel)) {
                 rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite residual in refinement");
@@ -609,16 +634,9 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 rc = ASTRO_ERR_MAXIT;
                 break;
             }
-            // inner: A d = r in FP32 from d = 0, to inner * ||r||
             k_zero_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d32, n);
-            static thread_local double hp[2 * kCtas];
-            CK(cudaMemcpyAsync(hp, W.part.p, sizeof(double) * 2 * kCtas, cudaMemcpyDeviceToHost, ctx->stream));
-            CK(cudaStreamSynchronize(ctx->stream));
-            double rr = 0.0;
-            for (int q = 0; q < kCtas; ++q) rr += hp[2 * q];
-            const double tgt = inner * std::sqrt(rr);
-            int rci = gmres_solve<float, float, DPN>(ctx, W, dptr<float>(ctx->d_K32), d32, r, tgt, maxCycles - cycles, m,
-                                                     &iters, &cycles, &est, 0);
+            int rci = gmres_solve<float, float, DPN>(ctx, W, dptr<float>(ctx->d_K32), d32, r, inner * rn, maxCycles - cycles,
+                                                     m, &iters, &cycles, &est);
             if (rci == ASTRO_ERR_NAN) {
                 rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the FP32 inner solve");
                 break;
@@ -652,11 +670,12 @@ int krylov_solve_static(astro_ctx *ctx, const double *d_b, double *d_x, const as
     return solve_static_dev<6>(ctx, d_b, d_x, o, st);
 }
 
-// y = (K + C^T C) x in FP64 (K from K64), for tests of the operator.
+// y = (K + C^T C) x for device vectors (internal layout).
 int krylov_apply(astro_ctx *ctx, int kind, const double *d_x, double *d_y) {
-    // r = 0 - A x  -> y = -r
     GmresWork W;
-    int rc = dev_alloc(ctx, W.part, sizeof(double) * 2 * kCtas);
+    W.n = ctx->P.n;
+    W.nRowCtas = (ctx->P.N + kWarps - 1) / kWarps;
+    int rc = dev_alloc(ctx, W.part, sizeof(double) * 2 * W.nRowCtas);
     if (rc) return rc;
     DevBuf zb;
     if ((rc = dev_alloc(ctx, zb, sizeof(double) * ctx->P.n))) return rc;

@@ -229,6 +229,19 @@ int astro_prep_build(astro_ctx *c, const astro_model *m) {
         P.colorEls.resize(E);
         std::vector<int> fill(P.colorPtr.begin(), P.colorPtr.end() - 1);
         for (int e = 0; e < E; ++e) P.colorEls[fill[col[e]]++] = e;
+        // first-touch flags in colour order (lets an assembly pass write without zeroing first)
+        P.elFirst.assign(E, 0ull);
+        std::vector<char> seen(P.nb, 0);
+        for (int q = 0; q < E; ++q) {
+            const int e = P.colorEls[q];
+            for (int ab = 0; ab < npe * npe; ++ab) {
+                const int k = P.elBlk[(size_t)e * npe * npe + ab];
+                if (!seen[k]) {
+                    seen[k] = 1;
+                    P.elFirst[e] |= (1ull << ab);
+                }
+            }
+        }
     }
     // reference CSR positions: per node, the first-insertion sequence of (component, node)
     {

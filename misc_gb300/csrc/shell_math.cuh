@@ -49,6 +49,9 @@ __device__ __forceinline__ double reT(double x) { return x; }
 __device__ __forceinline__ double reT(cplx x) { return x.re; }
 __device__ __forceinline__ double imT(double) { return 0.0; }
 __device__ __forceinline__ double imT(cplx x) { return x.im; }
+template <class T> __device__ __forceinline__ T pert_i(double h);  // i*h for complex, 0 for real
+template <> __device__ __forceinline__ double pert_i<double>(double) { return 0.0; }
+template <> __device__ __forceinline__ cplx pert_i<cplx>(double h) { return cplx(0.0, h); }
 __device__ __forceinline__ bool isZeroT(double x) { return x == 0.0; }
 __device__ __forceinline__ bool isZeroT(cplx x) { return x.re == 0.0 && x.im == 0.0; }
 

@@ -2,12 +2,6 @@
 // ASTRO_ERR_UNSUPPORTED with a message; none falls back to a CPU computation.
 #include "astro_internal.h"
 
-int shell_sections_prepare(astro_ctx *ctx, const astro_model *) { (void)ctx; return ASTRO_OK; }
-
-int launch_shell4_assemble(astro_ctx *ctx, const astro_state *, double *, double *, int, double *, double *) {
-    return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "shell4 element kernel not available in this build");
-}
-
 extern "C" int astro_convert_to_ltri(astro_ctx *ctx, double *) {
     return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "convert_to_ltri not available in this build");
 }
