@@ -59,7 +59,7 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 static void free_all(astro_ctx *c) {
     DevBuf *bufs[] = {&c->d_nodes,  &c->d_elist,   &c->d_elMat,   &c->d_esec,    &c->d_secABD,   &c->d_secOrient,
                       &c->d_colorEls, &c->d_elBlk, &c->d_rank,    &c->d_bRowPtr, &c->d_bCol,     &c->d_bRow,
-                      &c->d_etype,  &c->d_elFirst, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
+                      &c->d_etype,  &c->d_elFirst, &c->d_K64p, &c->d_K32p, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
                       &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status};
@@ -326,7 +326,10 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
         dev_free(dl);
         return rc;
     }
-    if (build_mat == 1) ctx->haveK64 = 1;
+    if (build_mat == 1) {
+        ctx->haveK64 = 1;
+        ctx->k64Version++;
+    }
     // load back to reference numbering
     DevBuf dref;
     if ((rc = dev_alloc(ctx, dref, sizeof(double) * n))) return rc;
@@ -356,12 +359,14 @@ extern "C" int astro_assemble_fp32(astro_ctx *ctx) {
     if ((rc = launch_hex8_assemble(ctx, 32, 1))) return rc;
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->haveK32 = 1;
+    ctx->k32Version++;
     return ASTRO_OK;
 }
 
 // Timed-path variant used by the benchmark: assembly only, no synchronisation.
 extern "C" int astro_assemble_fp32_async(astro_ctx *ctx) {
     if (!ctx || !ctx->d_K32.p) return ASTRO_ERR_STATE;
+    ctx->k32Version++;
     return launch_hex8_assemble(ctx, 32, 1);
 }
 

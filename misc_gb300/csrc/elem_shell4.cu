@@ -17,26 +17,23 @@
 // rotation of the derivative terms uses the element's own nodes (the reference's loop reads a
 // stale column offset there; its evident intent is kept).
 //
-// Mapping: one warp per element, lane l owns element DOF l+1 (component-major: 24 nodal, then 8
-// internal).  Each lane forms its column of d def and of K; the 4x(3x16) frame derivatives come
-// from ten lanes in parallel; the 8x8 internal block is factorised by lane 0 and each nodal
-// column condensed by its lane.  Elements are processed colour by colour so the 6x6 block
-// updates of one launch never collide (no atomics).
+// Mapping: the evaluation is a pipeline of one-thread-per-item kernels (elem_shell4_pipe.cuh)
+// over per-element global scratch, run one element colour at a time; elements of a colour share
+// no node, so their 6x6 block updates never collide (no atomics, deterministic).
+#include <algorithm>
+
 #include "astro_internal.h"
-#include "elem_shell4_dev.cuh"
+#include "elem_shell4_pipe.cuh"
 
 // Resource attributes of the shell kernels (no launch), for diagnostics.
 int shell_kernel_attrs(char *buf, int len) {
     cudaFuncAttributes a{}, b{};
     size_t stack = 0;
-    cudaError_t e1 = cudaFuncGetAttributes(&a, shell_kernel);
-    cudaError_t e2 = cudaFuncGetAttributes(&b, shell_props_kernel);
+    cudaError_t e1 = cudaFuncGetAttributes(&a, k_shell_kcol);
+    cudaError_t e2 = cudaFuncGetAttributes(&b, k_shell_frame);
     cudaError_t e3 = cudaDeviceGetLimit(&stack, cudaLimitStackSize);
-    snprintf(buf, len,
-             "shell_kernel: err=%d regs=%d local=%zu shared=%zu maxThreads=%d | props: err=%d regs=%d local=%zu | "
-             "stackLimit=%zu (err=%d)",
-             (int)e1, a.numRegs, a.localSizeBytes, a.sharedSizeBytes, a.maxThreadsPerBlock, (int)e2, b.numRegs,
-             b.localSizeBytes, stack, (int)e3);
+    snprintf(buf, len, "k_shell_kcol: err=%d regs=%d local=%zu | k_shell_frame: err=%d regs=%d local=%zu | stackLimit=%zu (err=%d)",
+             (int)e1, a.numRegs, a.localSizeBytes, (int)e2, b.numRegs, b.localSizeBytes, stack, (int)e3);
     return ASTRO_OK;
 }
 
@@ -89,41 +86,58 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
 int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_loadInt, double *d_intLoad, int buildMat,
                            double *d_ke, double *d_ru) {
     const AstroPrep &P = ctx->P;
-    ShellArgs A = {};
-    A.disp = st.disp;
-    A.pdisp = st.pdisp;
-    A.pvel = st.pvel;
-    A.pacc = st.pacc;
-    A.idisp = st.idisp;
-    A.pidisp = st.pidisp;
-    A.dynamic = st.dynamic;
-    A.beta = st.beta;
-    A.gamma = st.gamma;
-    A.delT = st.delT;
+    int maxc = 0;
+    for (int col = 0; col < P.ncolors; ++col) maxc = std::max(maxc, P.colorPtr[col + 1] - P.colorPtr[col]);
+    DevBuf fr, gp, de, kf;
+    int rc;
+    if ((rc = dev_alloc(ctx, fr, sizeof(ShellFrame) * (size_t)maxc))) return rc;
+    if ((rc = dev_alloc(ctx, gp, sizeof(ShellGP) * 4 * (size_t)maxc))) return rc;
+    if ((rc = dev_alloc(ctx, de, sizeof(double) * 4 * 32 * 9 * (size_t)maxc))) return rc;
+    if ((rc = dev_alloc(ctx, kf, sizeof(double) * 32 * 33 * (size_t)maxc))) return rc;
+    ShellPipe A = {};
     A.nodes = dptr<double>(ctx->d_nodes);
     A.elist = dptr<int>(ctx->d_elist);
     A.rank = dptr<int>(ctx->d_rank);
     A.elBlk = dptr<int>(ctx->d_elBlk);
     A.props = dptr<ShellProps>(ctx->d_secABD);
+    A.disp = st.disp;
+    A.pdisp = st.pdisp;
+    A.pvel = st.pvel;
+    A.pacc = st.pacc;
+    A.idisp = st.idisp;
+    A.dynamic = st.dynamic;
+    A.beta = st.beta;
+    A.gamma = st.gamma;
+    A.delT = st.delT;
     A.buildMat = buildMat;
-    A.status = dptr<int>(ctx->d_status);
-    A.nE = P.E;
-    A.nN = P.N;
-    A.nn = P.n;
-    A.nnb = P.nb;
-    A.quirkMeanRot = ctx->quirkShellMeanRot;
+    A.quirk = ctx->quirkShellMeanRot;
+    A.fr = dptr<ShellFrame>(fr);
+    A.gp = dptr<ShellGP>(gp);
+    A.dedU = dptr<double>(de);
+    A.Kf = dptr<double>(kf);
     A.K = (buildMat && !d_ke) ? dptr<double>(ctx->d_K64) : nullptr;
     A.load = d_loadInt;
     A.intLoad = d_intLoad;
     A.intMat = (buildMat && !d_ke) ? dptr<double>(ctx->d_intMat) : nullptr;
     A.keOut = d_ke;
     A.ruOut = d_ru;
+    cudaStream_t s = ctx->stream;
     for (int col = 0; col < P.ncolors; ++col) {
         const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
         if (!cnt) continue;
-        A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+        A.els = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
         A.count = cnt;
-        shell_kernel<<<(cnt + kSW - 1) / kSW, 32 * kSW, 0, ctx->stream>>>(A);
+        k_shell_frame<<<(cnt + 63) / 64, 64, 0, s>>>(A);
+        k_shell_gauss<<<(4 * cnt + 127) / 128, 128, 0, s>>>(A);
+        k_shell_dedu<<<(128 * cnt + 127) / 128, 128, 0, s>>>(A);
+        k_shell_kcol<<<(32 * cnt + 127) / 128, 128, 0, s>>>(A);
+        k_shell_condense<<<(cnt + 63) / 64, 64, 0, s>>>(A);
     }
-    return cuda_check(ctx, cudaGetLastError(), "shell kernel launch");
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    dev_free(fr);
+    dev_free(gp);
+    dev_free(de);
+    dev_free(kf);
+    return cuda_check(ctx, e, "shell pipeline");
 }

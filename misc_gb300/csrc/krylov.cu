@@ -46,7 +46,8 @@ struct GmresCtl {
 template <class TM> struct Op {
     const int *rowPtr;
     const int *col;
-    const TM *K;
+    const TM *K;        // block planes: entry q = i*dpn + j of block k at K[q*nb + k]
+    long long nb;
     const int *penPtr;  // (N+1) penalty entries per block row, or null
     const int *penRow;
     const int *penCol;
@@ -60,7 +61,9 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-// y_r = (A (s * dinv .* x))_r for block row r, one warp; result in all lanes.
+// y_r = (A (s * x))_r for block row r, one warp, one lane per block (block planes: each of the
+// dpn*dpn value loads is coalesced across the lanes, and x is gathered once per block column
+// component); result in all lanes.
 template <class TM, class TX, int DPN>
 __device__ __forceinline__ void row_apply(const Op<TM> &op, int r, const TX *__restrict__ x, double xs, double out[DPN]) {
     const int b0 = op.rowPtr[r], b1 = op.rowPtr[r + 1];
@@ -68,40 +71,26 @@ __device__ __forceinline__ void row_apply(const Op<TM> &op, int r, const TX *__r
     double acc[DPN];
 #pragma unroll
     for (int i = 0; i < DPN; ++i) acc[i] = 0.0;
-    const int nval = (b1 - b0) * DPN * DPN;
-    const TM *__restrict__ Kr = op.K + (size_t)b0 * DPN * DPN;
-    // four values per lane in flight: index loads, then gathers, then products
-    for (int t0 = lane; t0 < nval; t0 += 128) {
-        int cc[4], ii[4];
-        double kv[4];
+    for (int k = b0 + lane; k < b1; k += 32) {
+        const int c = __ldg(op.col + k) * DPN;
+        double xv[DPN];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int t = t0 + 32 * u;
-            const bool ok = t < nval;
-            const int tt = ok ? t : 0;
-            const int blk = tt / (DPN * DPN), rem = tt - blk * (DPN * DPN);
-            ii[u] = ok ? rem / DPN : -1;
-            cc[u] = __ldg(op.col + b0 + blk) * DPN + (rem - (rem / DPN) * DPN);
-            kv[u] = ok ? (double)Kr[tt] : 0.0;
-        }
-        double xv[4];
+        for (int j = 0; j < DPN; ++j) xv[j] = (double)x[c + j];
+        double kv[DPN * DPN];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            xv[u] = (double)x[cc[u]] * xs;
-            if (op.dinv) xv[u] *= op.dinv[cc[u]];
-        }
+        for (int q = 0; q < DPN * DPN; ++q) kv[q] = (double)op.K[(size_t)q * op.nb + k];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const double p = kv[u] * xv[u];
+        for (int i = 0; i < DPN; ++i) {
+            double s = 0.0;
 #pragma unroll
-            for (int q = 0; q < DPN; ++q) acc[q] += (q == ii[u]) ? p : 0.0;
+            for (int j = 0; j < DPN; ++j) s += kv[i * DPN + j] * xv[j];
+            acc[i] += s * xs;
         }
     }
     if (op.penPtr) {
         for (int t = op.penPtr[r] + lane; t < op.penPtr[r + 1]; t += 32) {
             const int c = op.penCol[t];
-            double xv = (double)x[c] * xs;
-            if (op.dinv) xv *= op.dinv[c];
+            const double xv = (double)x[c] * xs;
             const double p = op.penVal[t] * xv;
             const int i = op.penRow[t];
 #pragma unroll
@@ -112,10 +101,12 @@ __device__ __forceinline__ void row_apply(const Op<TM> &op, int r, const TX *__r
     for (int q = 0; q < DPN; ++q) out[q] = warp_sum(acc[q]);
 }
 
-// v_j = wprev * inv (rows of this warp written to V[j]); w = A D^-1 v_j.  One warp per block row.
+// v_j = wprev * inv (rows of this warp written to V[j]); w = A D^-1 v_j, reading the
+// Jacobi-scaled copy zprev = D^-1 wprev.  One warp per block row.
 template <class TM, class TV, int DPN>
 __global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restrict__ V, size_t ld, const TV *__restrict__ wprev,
-                                                        TV *__restrict__ w, const GmresCtl *__restrict__ ctl) {
+                                                        const TV *__restrict__ zprev, TV *__restrict__ w,
+                                                        const GmresCtl *__restrict__ ctl) {
     if (ctl->done) return;
     const int r = blockIdx.x * kWarps + (threadIdx.x >> 5);
     if (r >= op.N) return;
@@ -123,7 +114,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restric
     const int j = ctl->j;
     const double inv = ctl->inv;
     double y[DPN];
-    row_apply<TM, TV, DPN>(op, r, wprev, inv, y);
+    row_apply<TM, TV, DPN>(op, r, zprev, inv, y);
     if (lane < DPN) {
         const size_t i = (size_t)r * DPN + lane;
         double yv = 0.0;
@@ -174,7 +165,8 @@ __global__ void __launch_bounds__(kThreads) k_dots(int n, const TV *__restrict__
 // w -= V[0..j] h1; then either the partial dots with V (mode 0) or the partial ||w||^2 (mode 1)
 template <class TV>
 __global__ void __launch_bounds__(kThreads) k_update(int n, const TV *__restrict__ V, size_t ld, TV *__restrict__ w,
-                                                     const GmresCtl *__restrict__ ctl, double *part, int mode) {
+                                                     const GmresCtl *__restrict__ ctl, double *part, int mode,
+                                                     const double *__restrict__ dinv, TV *__restrict__ z) {
     if (ctl->done) return;
     __shared__ double sw[kChunk];
     __shared__ double sh[kMaxM + 1];
@@ -201,6 +193,7 @@ __global__ void __launch_bounds__(kThreads) k_update(int n, const TV *__restrict
         for (; k <= j; ++k) s -= sh[k] * (double)V[(size_t)k * ld + i];
         const TV wv = (TV)s;
         w[i] = wv;
+        if (z) z[i] = (TV)(dinv[i] * (double)wv);  // Jacobi-scaled copy read by the next SpMV
         sw[t] = (double)wv;
         nrm = (double)wv * (double)wv;
     }
@@ -337,7 +330,8 @@ __global__ void __launch_bounds__(kThreads) k_xupdate(int n, const TV *__restric
 // r = b - A x (FP64 arithmetic), partial ||r||^2 and ||b||^2 per CTA.  One warp per block row.
 template <class TM, class TX, class TR, int DPN>
 __global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *__restrict__ x, const double *__restrict__ b,
-                                                       TR *__restrict__ r, double *part) {
+                                                       TR *__restrict__ r, double *part, const double *__restrict__ dinv = nullptr,
+                                                       TR *__restrict__ z = nullptr) {
     __shared__ double sp[kWarps][2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int row = blockIdx.x * kWarps + wid;
@@ -357,6 +351,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *__re
             for (int q = 0; q < DPN; ++q) yv = (q == lane) ? y[q] : yv;
             const double v = b[i] - yv;
             r[i] = (TR)v;
+            if (z) z[i] = (TR)(dinv[i] * (double)(TR)v);
             rr = v * v;
             bb = b[i] * b[i];
         }
@@ -416,7 +411,7 @@ template <class TM> __global__ void k_dinv(Op<TM> op, double *dinv) {
     for (int k = op.rowPtr[r]; k < op.rowPtr[r + 1]; ++k)
         if (op.col[k] == r) kd = k;
     for (int q = 0; q < dpn; ++q) {
-        double d = (kd >= 0) ? (double)op.K[(size_t)kd * dpn * dpn + q * dpn + q] : 0.0;
+        double d = (kd >= 0) ? (double)op.K[(size_t)(q * dpn + q) * op.nb + kd] : 0.0;
         if (op.penPtr)
             for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t)
                 if (op.penRow[t] == q && op.penCol[t] == r * dpn + q) d += op.penVal[t];
@@ -429,18 +424,46 @@ template <class TM> __global__ void k_dinv(Op<TM> op, double *dinv) {
 // ---------------------------------------------------------------------------------------------
 
 struct GmresWork {
-    DevBuf V, w0, w1, part, ctl, dinv, rres, xs;
+    DevBuf V, w0, w1, z0, z1, part, ctl, dinv, rres, xs;
     int n = 0, m = 0;
     size_t ld = 0;
     int nChunks = 0, nRowCtas = 0;
     std::vector<double> hp;
 };
 
-template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *K, const double *dinv) {
+// block-CSR values (dpn x dpn row-major blocks) -> block planes (entry q of block k at q*nb + k)
+template <class T> __global__ void k_to_planes(const T *__restrict__ K, T *__restrict__ Kp, long long nb, int dd) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= nb * dd) return;
+    const long long k = t / dd;
+    const int q = (int)(t - k * dd);
+    Kp[(size_t)q * nb + k] = K[t];
+}
+
+// Solver copy of the assembled matrix in block-plane layout (rebuilt when the assembly changed).
+template <class TM> static const TM *planes_of(astro_ctx *ctx, int *rc) {
+    const bool f64 = sizeof(TM) == 8;
+    DevBuf &src = f64 ? ctx->d_K64 : ctx->d_K32;
+    DevBuf &dst = f64 ? ctx->d_K64p : ctx->d_K32p;
+    int &ver = f64 ? ctx->k64PlanesVersion : ctx->k32PlanesVersion;
+    const int cur = f64 ? ctx->k64Version : ctx->k32Version;
+    const long long dd = (long long)ctx->P.dpn * ctx->P.dpn, nb = ctx->P.nb;
+    *rc = ASTRO_OK;
+    if (!dst.p && (*rc = dev_alloc(ctx, dst, sizeof(TM) * nb * dd))) return nullptr;
+    if (ver != cur) {
+        k_to_planes<TM><<<(unsigned)((nb * dd + 255) / 256), 256, 0, ctx->stream>>>(dptr<TM>(src), dptr<TM>(dst), nb, (int)dd);
+        if ((*rc = cuda_check(ctx, cudaGetLastError(), "to_planes"))) return nullptr;
+        ver = cur;
+    }
+    return dptr<TM>(dst);
+}
+
+template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *Kplanes, const double *dinv) {
     Op<TM> op;
     op.rowPtr = dptr<int>(ctx->d_bRowPtr);
     op.col = dptr<int>(ctx->d_bCol);
-    op.K = K;
+    op.K = Kplanes;
+    op.nb = ctx->P.nb;
     op.penPtr = ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr;
     op.penRow = dptr<int>(ctx->d_penRow);
     op.penCol = dptr<int>(ctx->d_penCol);
@@ -455,18 +478,20 @@ template <class TM, class TV, int DPN>
 static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m) {
     cudaStream_t s = ctx->stream;
     TV *V = dptr<TV>(W.V), *wa = dptr<TV>(W.w0), *wb = dptr<TV>(W.w1);
+    TV *za = dptr<TV>(W.z0), *zb = dptr<TV>(W.z1);
     GmresCtl *ctl = dptr<GmresCtl>(W.ctl);
     double *part = dptr<double>(W.part);
+    const double *dinv = dptr<double>(W.dinv);
     const int n = W.n;
     for (int step = 0; step < m; ++step) {
-        TV *wprev = (step % 2 == 0) ? wa : wb;
-        TV *wnew = (step % 2 == 0) ? wb : wa;
-        k_spmv_step<TM, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, V, W.ld, wprev, wnew, ctl);
+        TV *wprev = (step % 2 == 0) ? wa : wb, *zprev = (step % 2 == 0) ? za : zb;
+        TV *wnew = (step % 2 == 0) ? wb : wa, *znew = (step % 2 == 0) ? zb : za;
+        k_spmv_step<TM, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, V, W.ld, wprev, zprev, wnew, ctl);
         k_dots<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part);
         k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, W.nChunks, 0);
-        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 0);
+        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 0, nullptr, nullptr);
         k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, W.nChunks, 1);
-        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 1);
+        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 1, dinv, znew);
         k_control<<<1, 32, 0, s>>>(ctl, part, W.nChunks, m);
     }
 }
@@ -495,7 +520,8 @@ static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const d
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(opNo, x, b, dptr<TV>(W.w0), part);
+    k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(opNo, x, b, dptr<TV>(W.w0), part, dptr<double>(W.dinv),
+                                                                 dptr<TV>(W.z0));
     k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, tgtAbs);
     enqueue_cycle<TM, TV, DPN>(ctx, W, op, m);
     k_lsq<<<1, 1, 0, s>>>(ctl);
@@ -538,6 +564,8 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
     if ((rc = dev_alloc(ctx, W.V, W.ld * (m + 1) * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.w0, (size_t)n * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.w1, (size_t)n * tv))) return rc;
+    if ((rc = dev_alloc(ctx, W.z0, (size_t)n * tv))) return rc;
+    if ((rc = dev_alloc(ctx, W.z1, (size_t)n * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.part, sizeof(double) * nparts))) return rc;
     if ((rc = dev_alloc(ctx, W.ctl, sizeof(GmresCtl)))) return rc;
     if ((rc = dev_alloc(ctx, W.dinv, sizeof(double) * (size_t)n))) return rc;
@@ -548,7 +576,7 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
 }
 
 static void work_free(GmresWork &W) {
-    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.part, &W.ctl, &W.dinv, &W.rres, &W.xs};
+    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.z0, &W.z1, &W.part, &W.ctl, &W.dinv, &W.rres, &W.xs};
     for (auto *x : b) dev_free(*x);
 }
 
@@ -558,11 +586,16 @@ static int true_residual(astro_ctx *ctx, GmresWork &W, int kind, const double *x
                          double *r_out, double *rnorm = nullptr, double *bnorm = nullptr) {
     cudaStream_t s = ctx->stream;
     double *part = dptr<double>(W.part);
+    int prc = ASTRO_OK;
     if (kind == 64) {
-        Op<double> op = make_op<double>(ctx, dptr<double>(ctx->d_K64), nullptr);
+        const double *Kp = planes_of<double>(ctx, &prc);
+        if (prc) return prc;
+        Op<double> op = make_op<double>(ctx, Kp, nullptr);
         k_residual<double, double, double, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
     } else {
-        Op<float> op = make_op<float>(ctx, dptr<float>(ctx->d_K32), nullptr);
+        const float *Kp = planes_of<float>(ctx, &prc);
+        if (prc) return prc;
+        Op<float> op = make_op<float>(ctx, Kp, nullptr);
         k_residual<float, double, double, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
     }
     int rc = ASTRO_OK;
@@ -600,12 +633,17 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     cudaEventRecord(e0, ctx->stream);
     double *r = dptr<double>(W.rres);
     if (fp64) {
-        Op<double> op = make_op<double>(ctx, dptr<double>(ctx->d_K64), nullptr);
+        const double *K64p = planes_of<double>(ctx, &rc);
+        if (rc) {
+            work_free(W);
+            return rc;
+        }
+        Op<double> op = make_op<double>(ctx, K64p, nullptr);
         k_dinv<double><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(op, dptr<double>(W.dinv));
         rc = true_residual<DPN>(ctx, W, 64, nullptr, d_b, &rel, r, &rn, &bn);
         const double tgt = o->rtol * bn;
         while (rc == ASTRO_OK) {
-            int grc = gmres_solve<double, double, DPN>(ctx, W, dptr<double>(ctx->d_K64), d_x, d_b, tgt, maxCycles - cycles, m,
+            int grc = gmres_solve<double, double, DPN>(ctx, W, K64p, d_x, d_b, tgt, maxCycles - cycles, m,
                                                        &iters, &cycles, &est);
             if ((rc = true_residual<DPN>(ctx, W, 64, d_x, d_b, &rel, r))) break;
             if (rel <= o->rtol) break;
@@ -619,7 +657,12 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
             }
         }
     } else {
-        Op<float> op32 = make_op<float>(ctx, dptr<float>(ctx->d_K32), nullptr);
+        const float *K32p = planes_of<float>(ctx, &rc);
+        if (rc) {
+            work_free(W);
+            return rc;
+        }
+        Op<float> op32 = make_op<float>(ctx, K32p, nullptr);
         k_dinv<float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(op32, dptr<double>(W.dinv));
         float *d32 = dptr<float>(W.xs);
         const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
@@ -635,7 +678,7 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 break;
             }
             k_zero_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d32, n);
-            int rci = gmres_solve<float, float, DPN>(ctx, W, dptr<float>(ctx->d_K32), d32, r, inner * rn, maxCycles - cycles,
+            int rci = gmres_solve<float, float, DPN>(ctx, W, K32p, d32, r, inner * rn, maxCycles - cycles,
                                                      m, &iters, &cycles, &est);
             if (rci == ASTRO_ERR_NAN) {
                 rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the FP32 inner solve");

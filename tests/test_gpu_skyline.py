@@ -1,0 +1,110 @@
+"""GPU parity of the reference's own solve path (convertToLTri, getSparseLDLFact,
+solveSparseLDLFact, gMRes with the skyline preconditioner) against the oracle through the C ABI.
+
+Tolerances: the profile matrix and the sparse products are bit-for-bit sums in the reference's
+order except for the element-level rounding of K (1e-12 relative); the factor and the triangular
+solves use block-parallel dot products, so they agree to a few ulps per entry (1e-10 relative in
+norm); the GMRES result is compared with the oracle's GMRES result and with a direct solve
+(1e-8 relative)."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from misc_gb300 import model as M
+from misc_gb300.astro import AstroError, AstroGPU
+from oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "hex": lambda: M.hex_block(nx=6, ny=3, nz=3),
+    "shell_beam": lambda: M.shell_beam(),
+    "cfg1": lambda: M.config1(),
+}
+
+
+@pytest.fixture(scope="module", params=list(CASES))
+def system(request):
+    m = CASES[request.param]()
+    o = Oracle(m)
+    A, b, mat, cols, mm, mr = o.static_system()
+    g = AstroGPU(m)
+    g.getElasticSolnLoad(1, export=False)
+    g.scaleElasticMPC()
+    lt_o = o.convert_to_ltri(mat, cols, mm)
+    return dict(name=request.param, o=o, g=g, A=A, b=b, mat=mat, cols=cols, mm=mm, lt_o=lt_o,
+                fac_o=o.ldl_fact(lt_o, o.lt_range))
+
+
+def _nrel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def test_convert_to_ltri(system):
+    lt = system["g"].convertToLTri()
+    lt_o = system["lt_o"]
+    assert lt.shape == lt_o.shape
+    assert np.abs(lt - lt_o).max() <= 1e-12 * np.abs(lt_o).max()
+
+
+def test_ldl_fact(system):
+    o, g = system["o"], system["g"]
+    fac = g.getSparseLDLFact(system["lt_o"], o.lt_range)
+    assert _nrel(fac, system["fac_o"]) < 1e-10
+    # the resident factor of the device profile succeeds too
+    g.convertToLTri()
+    g._check(g.L.astro_ldl_fact_resident(g.h))
+
+
+def test_ldl_solve(system):
+    o, g = system["o"], system["g"]
+    rng = np.random.default_rng(11)
+    rhs = rng.standard_normal(o.n)
+    x = g.solveSparseLDLFact(rhs, system["fac_o"], o.lt_range)
+    xo = o.ldl_solve(system["fac_o"], o.lt_range, rhs)
+    assert _nrel(x, xo) < 1e-10
+
+
+# (basis size, restart cycles) per model.  The reference's gMRes has no breakdown guard and skips
+# Givens rotations below 1e-10, so once the Krylov space is exhausted its iterates amplify
+# rounding: with the default 100 vectors a 1e-15 relative change of b moves the oracle's own
+# result by O(1) on these models.  The cases below are those where the oracle's result moves by
+# less than 1e-10 under that perturbation, so a GPU/oracle difference means a real discrepancy.
+GMRES_CASES = {"hex": [(40, 1), (10, 3), (5, 10)], "shell_beam": [(5, 3), (10, 1)], "cfg1": [(5, 3), (10, 1)]}
+
+
+def test_reference_gmres(system):
+    """gMRes preconditioned by the skyline factor of the profile part of K + C^T C."""
+    o, g, b = system["o"], system["g"], system["b"]
+    n = o.n
+    for num_vecs, cycles in GMRES_CASES[system["name"]]:
+        max_it = num_vecs * cycles - 1
+        xo, _ = o.gmres(system["mat"], system["cols"], system["mm"], system["fac_o"], b, num_vecs=num_vecs,
+                        max_it=max_it)
+        x = g.gMRes(np.zeros(n), system["mat"], system["cols"], o.el_mat_range, system["mm"], o.mpc_cols,
+                    o.mpc_range, system["fac_o"], o.lt_range, b, num_vecs, max_it)
+        assert _nrel(x, xo) < 1e-9, (num_vecs, cycles)
+    if system["name"] == "hex":   # GMRES(40) converges in one cycle here
+        xd = spla.spsolve(system["A"].tocsc(), b)
+        assert _nrel(x, xd) < 1e-8
+
+
+def test_reference_gmres_warm_start(system):
+    """x_vec is the initial guess (the reference reads it despite intent(out))."""
+    o, g, b = system["o"], system["g"], system["b"]
+    x0 = 1e-3 * np.random.default_rng(4).standard_normal(o.n)
+    xo, _ = o.gmres(system["mat"], system["cols"], system["mm"], system["fac_o"], b, x0=x0, num_vecs=5, max_it=4)
+    x = g.gMRes(x0, system["mat"], system["cols"], o.el_mat_range, system["mm"], o.mpc_cols, o.mpc_range,
+                system["fac_o"], o.lt_range, b, 5, 4)
+    assert _nrel(x, xo) < 1e-9
+
+
+def test_zero_pivot_reports_error():
+    """A profile with a zero diagonal entry stops with ASTRO_ERR_PIVOT instead of returning NaNs silently."""
+    m = M.hex_block(nx=2, ny=1, nz=1)
+    o = Oracle(m)
+    g = AstroGPU(m)
+    lt = np.zeros(o.lt_size)
+    with pytest.raises(AstroError) as e:
+        g.getSparseLDLFact(lt, o.lt_range)
+    assert e.value.code == 4
