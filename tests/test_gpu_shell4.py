@@ -91,3 +91,21 @@ def test_shell_static_system(model):
     x = np.random.default_rng(2).standard_normal(o.n)
     y = g.apply_operator(x, 64)
     assert np.linalg.norm(y - A @ x) <= 1e-13 * np.linalg.norm(A @ x)
+
+
+def test_shell_newmark_dynamic_state(plate):
+    """Newmark step (r_getElRu with r_getElRum): acceleration from disp/prev state, inertial
+    residual and K + c1 c2 M, against the oracle."""
+    m, g, o = plate
+    rng = np.random.default_rng(8)
+    n = o.n
+    st = M.make_state(n, disp=1e-3 * rng.standard_normal(n), prev_disp=1e-3 * rng.standard_normal(n),
+                      prev_vel=1e-1 * rng.standard_normal(n), prev_acc=10.0 * rng.standard_normal(n),
+                      internal_disp=1e-4 * rng.standard_normal(o.int_vec_size), dynamic=1, beta=0.25, gamma=0.5,
+                      del_t=1e-3)
+    load, iload, mat, cols, imat = g.getElasticSolnLoad(1, state=st)
+    oload, oiload, omat, ocols, oimat = o.el_soln_load(1, state=st)
+    assert np.linalg.norm(load - oload) <= 1e-11 * np.linalg.norm(oload)
+    assert np.linalg.norm(iload - oiload) <= 1e-11 * np.linalg.norm(oiload)
+    assert np.array_equal(cols, ocols)
+    assert np.abs(mat - omat).max() <= 1e-11 * np.abs(omat).max()

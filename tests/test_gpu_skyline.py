@@ -84,9 +84,9 @@ def test_reference_gmres(system):
         x = g.gMRes(np.zeros(n), system["mat"], system["cols"], o.el_mat_range, system["mm"], o.mpc_cols,
                     o.mpc_range, system["fac_o"], o.lt_range, b, num_vecs, max_it)
         assert _nrel(x, xo) < 1e-9, (num_vecs, cycles)
-    if system["name"] == "hex":   # GMRES(40) converges in one cycle here
-        xd = spla.spsolve(system["A"].tocsc(), b)
-        assert _nrel(x, xd) < 1e-8
+        if system["name"] == "hex" and num_vecs == 40:   # GMRES(40) converges in one cycle here
+            xd = spla.spsolve(system["A"].tocsc(), b)
+            assert _nrel(x, xd) < 1e-8
 
 
 def test_reference_gmres_warm_start(system):
