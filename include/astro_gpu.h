@@ -232,6 +232,20 @@ int astro_ldl_fact_resident(astro_ctx *ctx);
 int astro_ldl_solve(astro_ctx *ctx, double *soln, const double *rhs, const double *l_mat,
                     int32_t l_size, const int32_t *l_range, int32_t l_dim, double *z_vec);
 
+/* No counterpart in the reference.  The same solve as astro_ldl_solve for callers that must not
+ * allocate device memory during a solve: loops that have already filled HBM with the matrix,
+ * factor and Krylov basis, and callers with work on other streams that cudaFree would stall.
+ * All operands are the caller's DEVICE buffers (soln, rhs: l_dim; l_mat: the factor;
+ * l_range: l_dim+1 row ranges); the forward-sweep scratch is a fixed 2 MiB array in the
+ * library, so l_dim is limited to ASTRO_LDL_NOALLOC_MAX_DIM (larger sizes return
+ * ASTRO_ERR_ARG without touching the GPU).  The first call on each device looks up the
+ * scratch address (make it before any stream capture begins).  The scratch is shared by all
+ * contexts on a device: overlapping calls on one device race and must be serialised.
+ * Runs on the context's stream and returns after it completes. */
+#define ASTRO_LDL_NOALLOC_MAX_DIM 262144
+int astro_ldl_solve_device_noalloc(astro_ctx *ctx, double *d_soln, const double *d_rhs,
+                                   const double *d_l_mat, const int32_t *d_l_range, int32_t l_dim);
+
 /* gMRes (Working/AStrO_solvers.f90:128-297), same arguments: restarted, left-preconditioned
  * GMRES(numVecs) on A = Amat + Cmat^T Cmat with the skyline LDL^T factor Pmat as
  * preconditioner, convergence when the preconditioned residual norm is <= 1e-12 (single

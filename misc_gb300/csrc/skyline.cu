@@ -12,6 +12,7 @@
 // for; the large systems use the Jacobi/mixed-precision solvers of krylov.cu.
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 
 #include "astro_internal.h"
 
@@ -474,4 +475,75 @@ extern "C" int astro_gmres(astro_ctx *ctx, double *x_vec, const double *a_mat, c
     for (auto *p : bs) dev_free(*p);
     if (!rc && hout[1]) rc = set_err(ctx, hout[1], "non-finite residual in gmres");
     return rc;
+}
+
+// ---- allocation-free triangular solve ----------------------------------------------------------
+// Some callers cannot let a solve allocate device memory: a Newmark or Newton loop that has
+// already laid out nearly all of HBM for the matrix, the factor and the Krylov basis (an
+// allocation there can fail half-way through a run), and callers with work in flight on other
+// streams (cudaFree waits for the whole device, so a malloc/free pair around every
+// preconditioner apply serialises them).  astro_ldl_solve_device_noalloc serves them: all of its
+// operands are the caller's device buffers, and the forward-sweep vector z lives in the fixed
+// array below, which is part of the loaded module rather than a runtime allocation.
+static __device__ __align__(256) double g_ldl_noalloc_z[ASTRO_LDL_NOALLOC_MAX_DIM];  // 2 MiB
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double *g_noalloc_z[kMaxDevices] = {};  // address of g_ldl_noalloc_z on each device, once known
+
+// Same sweep as k_ldl_solve; the profile bandwidth is found on the device because the caller's
+// row ranges are device memory here.
+__global__ void __launch_bounds__(kT) k_ldl_solve_noalloc(double *soln, const double *rhs, const double *L,
+                                                          const int *R, int n, double *z) {
+    __shared__ int red[32];
+    int mb = 0;
+    for (int i = threadIdx.x + 1; i <= n; i += blockDim.x) mb = max(mb, R[i] - R[i - 1] - 1);
+    for (int o = 16; o; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mb;
+    __syncthreads();
+    mb = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) mb = max(mb, red[q]);
+    ldl_solve(soln, rhs, L, R, n, mb, z);
+}
+
+}  // namespace
+
+// The address of the scratch array is looked up on the first call made on each device (with that
+// device current) and kept; make that first call before any stream capture begins.  Nothing in
+// the scratch needs to start at zero: the forward sweep writes z(i) before any row reads it.
+// The scratch is shared by every context on a device, so calls that overlap in time on one
+// device (from several host threads) race on it and must be serialised by the caller.
+extern "C" int astro_ldl_solve_device_noalloc(astro_ctx *ctx, double *d_soln, const double *d_rhs,
+                                              const double *d_l_mat, const int32_t *d_l_range, int32_t l_dim) {
+    if (!ctx) return ASTRO_ERR_ARG;
+    if (l_dim > ASTRO_LDL_NOALLOC_MAX_DIM)
+        return set_err(ctx, ASTRO_ERR_ARG,
+                       "l_dim " + std::to_string(l_dim) + " exceeds the allocation-free solve's limit of " +
+                           std::to_string(ASTRO_LDL_NOALLOC_MAX_DIM) + " rows; use astro_ldl_solve");
+    if (l_dim <= 0 || !d_soln || !d_rhs || !d_l_mat || !d_l_range)
+        return set_err(ctx, ASTRO_ERR_ARG, "astro_ldl_solve_device_noalloc: null buffer or l_dim <= 0");
+    if (ctx->device < 0 || ctx->device >= kMaxDevices) return set_err(ctx, ASTRO_ERR_ARG, "device index out of range");
+    int prev = -1;
+    CK(cudaGetDevice(&prev));
+    if (prev != ctx->device) CK(cudaSetDevice(ctx->device));
+    double *z = nullptr;
+    cudaError_t e = cudaSuccess;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_z[ctx->device]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_ldl_noalloc_z);
+            if (e == cudaSuccess) g_noalloc_z[ctx->device] = static_cast<double *>(p);
+        }
+        z = g_noalloc_z[ctx->device];
+    }
+    if (e == cudaSuccess) {
+        k_ldl_solve_noalloc<<<1, kT, 0, ctx->stream>>>(d_soln, d_rhs, d_l_mat, d_l_range, l_dim, z);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (prev != ctx->device) cudaSetDevice(prev);
+    return cuda_check(ctx, e, "astro_ldl_solve_device_noalloc");
 }
