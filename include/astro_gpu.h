@@ -36,7 +36,7 @@ extern "C" {
 
 /* Design-variable categories supported by the complex-step path (reference dCategory/dSubCat). */
 #define ASTRO_DCAT_LAYUP_THICKNESS 1   /* 'layup' / 'thickness' of layer d_layer */
-#define ASTRO_DCAT_ELASTIC_MODULUS 2   /* 'elastic' / 'modulus' component d_component (1..3) */
+#define ASTRO_DCAT_ELASTIC_MODULUS 2   /* 'elastic' / 'modulus': materialElastic entry d_component (1..9) */
 
 /* Model arrays: the reference's module globals (Working/AStrO_globalData.f90) as flat arrays.
  * Element types: 8 = brick8 (2x2x2 Gauss), 41 = shell4 (4 Gauss points, 8 condensed
@@ -191,9 +191,11 @@ int astro_element_matrices(astro_ctx *ctx, int32_t precision, const astro_state 
                            double *ke_out, double *ru_out);
 
 /* Complex-step residual sensitivity dRu/dd for design variable dvar (1-based), at the nodal
- * state `state` (getdRelasticdD, Working/AStrO_commandFunctions.f90:1172-1375, element part):
- * the elements that depend on dvar are re-evaluated in complex FP64 with d_value[dvar] + i*h,
- * and drudd[n] = Im(Ru)/h is scattered in global DOF numbering (accumulated, not zeroed). */
+ * state `state` (getdRelasticdD, Working/AStrO_commandFunctions.f90:1172-1250, element part):
+ * the elements that depend on dvar are evaluated at d_value[dvar] + i*h and
+ * drudd[el_mat_dim] = Im(Ru) * (1/h) is summed at their global DOF, int_drudd[int_vec_size]
+ * (may be NULL) at their internal DOF.  Both outputs are zeroed first, as the reference does.
+ * The reference uses h = 1e-14 (compStep). */
 int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const astro_state *state,
                        double *drudd, double *int_drudd);
 

@@ -274,12 +274,13 @@ class AstroGPU:
                                        num_vecs, max_it))
         return x
 
-    def getdRelasticdD(self, dvar, h=1e-30, state=None):
+    def getdRelasticdD(self, dvar, h=1e-14, state=None):
+        """Complex-step dRu/dd of design variable dvar: (global DOF vector, internal-DOF vector)."""
         out = np.zeros(self.n)
         iout = np.zeros(max(self.int_vec_size, 1))
         self._check(self.L.astro_drdd_complex(self.h, dvar, h, C.byref(state) if state is not None else None,
                                               _d(out), _d(iout)))
-        return out, iout
+        return out, iout[:self.int_vec_size]
 
     # -- convenience ----------------------------------------------------------------------------
     def static_rhs(self, mpc_rhs_scaled=True):

@@ -95,6 +95,12 @@ struct astro_ctx {
     // skyline (reference DOF numbering) on device
     DevBuf d_ltRange, d_lt;
     int haveLT = 0, ltFactored = 0;
+    // design variables (host copies of the model's maps) and, for shells, the section inputs kept
+    // on the device for the complex-step property evaluation
+    int numDvars = 0;
+    std::vector<int> e2dRange, e2d, dCat, dComp, dLayer;
+    std::vector<double> e2c, dVal;
+    DevBuf d_shLayRange, d_shLay, d_shZoff, d_e2dR, d_e2d, d_e2c, d_dCat, d_dLayer, d_dVal;
     // scratch
     DevBuf d_scratch;
     DevBuf d_status;  // int status words written by kernels
@@ -139,3 +145,10 @@ int surface_load_dev(astro_ctx *ctx, int nf, const int *d_faceEl, const int *d_f
                      double pressure, double *d_loadInt);                   // assemble.cu
 int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt);       // elem_hex8.cu
 int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru);   // elem_hex8.cu
+// Complex-step residual sensitivity of the elements that depend on design variable dvar:
+// d_acc -= Im(Ru(d + i h)) accumulated in colour order (internal layout; shells also d_intAcc).
+int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *d_acc);          // elem_hex8.cu
+int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &s, double *d_acc,
+                double *d_intAcc);                                                              // elem_shell4.cu
+// host: elements depending on dvar, grouped by colour (colour c: list[ptr[c] .. ptr[c+1]))
+void dvar_elements_by_colour(const astro_ctx *ctx, int dvar, std::vector<int> &list, std::vector<int> &ptr);

@@ -62,7 +62,8 @@ static void free_all(astro_ctx *c) {
                       &c->d_etype,  &c->d_elFirst, &c->d_K64p, &c->d_K32p, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
                       &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
-                      &c->d_status};
+                      &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
+                      &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal};
     for (DevBuf *b : bufs) dev_free(*b);
 }
 
@@ -129,6 +130,30 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
         int s = ctx->esec[e];
         if (s < 1 || s > S) return fail(ASTRO_ERR_ARG, "element_section out of range");
     }
+    if (m->num_dvars > 0) {
+        if (!m->el_to_d_range || !m->el_to_d || !m->el_to_coef || !m->d_category || !m->d_value)
+            return fail(ASTRO_ERR_ARG, "design variables without their element maps");
+        for (int d = 0; d < m->num_dvars; ++d) {
+            int cat = m->d_category[d];
+            if (cat != ASTRO_DCAT_LAYUP_THICKNESS && cat != ASTRO_DCAT_ELASTIC_MODULUS)
+                return fail(ASTRO_ERR_UNSUPPORTED, "design-variable category not supported");
+            if (cat == ASTRO_DCAT_ELASTIC_MODULUS && (!m->d_component || m->d_component[d] < 1 || m->d_component[d] > 9))
+                return fail(ASTRO_ERR_ARG, "modulus design variable needs d_component in 1..9");
+        }
+        const int nE2D = m->el_to_d_range[P.E];
+        for (int q = 0; q < nE2D; ++q)
+            if (m->el_to_d[q] < 1 || m->el_to_d[q] > m->num_dvars) return fail(ASTRO_ERR_ARG, "el_to_d out of range");
+        ctx->numDvars = m->num_dvars;
+        ctx->e2dRange.assign(m->el_to_d_range, m->el_to_d_range + P.E + 1);
+        ctx->e2d.assign(m->el_to_d, m->el_to_d + nE2D);
+        ctx->e2c.assign(m->el_to_coef, m->el_to_coef + nE2D);
+        ctx->dCat.assign(m->d_category, m->d_category + m->num_dvars);
+        ctx->dVal.assign(m->d_value, m->d_value + m->num_dvars);
+        ctx->dComp.assign(m->num_dvars, 0);
+        ctx->dLayer.assign(m->num_dvars, 0);
+        if (m->d_component) ctx->dComp.assign(m->d_component, m->d_component + m->num_dvars);
+        if (m->d_layer) ctx->dLayer.assign(m->d_layer, m->d_layer + m->num_dvars);
+    }
     if (ctx->hasSolid) {
         ctx->elMat.resize(9 * (size_t)P.E);
         std::vector<double> orientEl(9 * (size_t)P.E);
@@ -137,6 +162,15 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
             int mat = m->section_mat_id[s - 1];
             if (mat < 1 || mat > m->num_materials) return fail(ASTRO_ERR_ARG, "section material out of range");
             for (int k = 0; k < 9; ++k) ctx->elMat[9 * (size_t)e + k] = m->material_elastic[9 * (size_t)(mat - 1) + k];
+            // elastic-modulus design variables: eProps(c) += coef * d (r_getMaterialStiffness)
+            if (m->num_dvars > 0)
+                for (int q = m->el_to_d_range[e]; q < m->el_to_d_range[e + 1]; ++q) {
+                    const int d = m->el_to_d[q];
+                    if (m->d_category[d - 1] == ASTRO_DCAT_ELASTIC_MODULUS) {
+                        double &v = ctx->elMat[9 * (size_t)e + m->d_component[d - 1] - 1];
+                        v = v + m->el_to_coef[q] * m->d_value[d - 1];
+                    }
+                }
             for (int k = 0; k < 9; ++k) {
                 double v = ctx->secOrient[9 * (s - 1) + k];
                 orientEl[9 * (size_t)e + k] = v;
@@ -147,13 +181,6 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
             return fail(rc, ctx->err);
         if ((rc = upload(ctx, ctx->d_secOrient, orientEl.data(), sizeof(double) * orientEl.size())))
             return fail(rc, ctx->err);
-    }
-    if (m->num_dvars > 0) {
-        for (int d = 0; d < m->num_dvars; ++d) {
-            int cat = m->d_category[d];
-            if (cat != ASTRO_DCAT_LAYUP_THICKNESS && cat != ASTRO_DCAT_ELASTIC_MODULUS)
-                return fail(ASTRO_ERR_UNSUPPORTED, "design-variable category not supported");
-        }
     }
     // device structures
     std::vector<int> rank1(P.N), bRow(P.nb), colorEls(P.colorEls);
@@ -368,6 +395,92 @@ extern "C" int astro_assemble_fp32_async(astro_ctx *ctx) {
     if (!ctx || !ctx->d_K32.p) return ASTRO_ERR_STATE;
     ctx->k32Version++;
     return launch_hex8_assemble(ctx, 32, 1);
+}
+
+void dvar_elements_by_colour(const astro_ctx *ctx, int dvar, std::vector<int> &list, std::vector<int> &ptr) {
+    const AstroPrep &P = ctx->P;
+    list.clear();
+    ptr.assign(1, 0);
+    for (int col = 0; col < P.ncolors; ++col) {
+        for (int k = P.colorPtr[col]; k < P.colorPtr[col + 1]; ++k) {
+            const int e = P.colorEls[k];
+            bool dep = false;
+            for (int q = ctx->e2dRange[e]; q < ctx->e2dRange[e + 1]; ++q) dep = dep || ctx->e2d[q] == dvar;
+            if (dep) list.push_back(e);
+        }
+        ptr.push_back((int)list.size());
+    }
+}
+
+__global__ void k_scale_neg(int n, const double *x, double s, double *y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = s * -x[i];
+}
+
+// getdRelasticdD, element part (Working/AStrO_commandFunctions.f90:1172-1250).  The elements that
+// depend on dvar contribute Im(Ru(d + i h)) / h.  Ru is linear in the element's material or
+// section stiffness (and section mass) at a real state, so Im(Ru) is the real residual evaluated
+// with the imaginary parts of the complex-step properties; the element kernels run in FP64 with
+// those properties and the complex path's constants (Gauss points +-0.577350269189626 as a
+// single-precision literal), and only the property evaluation is complex.
+extern "C" int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const astro_state *state, double *drudd,
+                                  double *int_drudd) {
+    if (!ctx || !drudd) return ASTRO_ERR_ARG;
+    if (dvar < 1 || dvar > ctx->numDvars)
+        return set_err(ctx, ASTRO_ERR_ARG, "design variable " + std::to_string(dvar) + " out of range");
+    if (!(h > 0.0)) return set_err(ctx, ASTRO_ERR_ARG, "complex step h must be positive");
+    const AstroPrep &P = ctx->P;
+    const int n = P.n;
+    int rc;
+    DevState S;
+    ShellDevState ds;
+    if (state) {
+        if ((rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
+        if (ctx->hasShell) {
+            if ((rc = state_vec_up(ctx, state->prev_disp, S.pdisp))) return rc;
+            if ((rc = state_vec_up(ctx, state->prev_vel, S.pvel))) return rc;
+            if ((rc = state_vec_up(ctx, state->prev_acc, S.pacc))) return rc;
+        }
+        if (state->dynamic && ctx->hasSolid)
+            return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
+    }
+    struct Tmp {
+        DevBuf acc, iacc, out;
+        ~Tmp() {
+            dev_free(acc);
+            dev_free(iacc);
+            dev_free(out);
+        }
+    } T;
+    DevBuf &acc = T.acc, &iacc = T.iacc, &out = T.out;
+    if ((rc = dev_alloc(ctx, acc, sizeof(double) * n))) return rc;
+    if ((rc = dev_alloc(ctx, out, sizeof(double) * n))) return rc;
+    CK(cudaMemsetAsync(acc.p, 0, sizeof(double) * n, ctx->stream));
+    const int ni = P.intVecSize;
+    if (ni > 0) {
+        if ((rc = dev_alloc(ctx, iacc, sizeof(double) * ni))) return rc;
+        CK(cudaMemsetAsync(iacc.p, 0, sizeof(double) * ni, ctx->stream));
+    }
+    if (ctx->hasSolid) {
+        rc = hex8_drdd(ctx, dvar, h, S.disp.p ? dptr<double>(S.disp) : nullptr, dptr<double>(acc));
+    } else {
+        if ((rc = shell_state(ctx, state, S, ds))) return rc;
+        rc = shell4_drdd(ctx, dvar, h, ds, dptr<double>(acc), ni > 0 ? dptr<double>(iacc) : nullptr);
+    }
+    if (rc) return rc;
+    // acc holds -sum Im(Ru): dRudD = Im(Ru) * (1/h) (compStepInv)
+    const double hInv = 1.0 / h;
+    k_scale_neg<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, dptr<double>(acc), hInv, dptr<double>(acc));
+    CK(cudaGetLastError());
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(acc), dptr<double>(out), n))) return rc;
+    CK(cudaMemcpyAsync(drudd, out.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (ni > 0 && int_drudd) {
+        k_scale_neg<<<(ni + 255) / 256, 256, 0, ctx->stream>>>(ni, dptr<double>(iacc), hInv, dptr<double>(iacc));
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(int_drudd, iacc.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
 }
 
 extern "C" int astro_element_matrices(astro_ctx *ctx, int32_t precision, const astro_state *state, double *ke_out,

@@ -18,10 +18,13 @@
 // Jacobian and displacement gradient by shuffles.  Elements are processed colour by colour so a
 // colour's blocks land in disjoint block rows: plain read-add-write, no atomics, bit-reproducible.
 #include "astro_internal.h"
+#include "shell_math.cuh"
 
 namespace {
 
 constexpr int kWarpsPerBlock = 4;
+constexpr double kRt3 = 0.57735026918962576451;  // r_1rt3 = 1/sqrt(3) in double
+constexpr double kRt3c = LIT(0.577350269189626);  // c_1rt3: a single-precision literal
 
 template <class T> struct Hex8Args {
     const double *nodes;     // (N,3) by node id
@@ -38,10 +41,12 @@ template <class T> struct Hex8Args {
     double *loadInt;         // internal-layout load, -= Ru (or nullptr)
     double *keOut;           // element matrices (E, 24,24) column-major, element DOF order, or nullptr
     double *ruOut;           // (E,24) or nullptr
+    double gpc;              // Gauss point coordinate (1/sqrt(3) of the real or the complex path)
+    const double *Cover;     // per listed element a 6x6 row-major C used instead of elMat, or nullptr
 };
 
 // C = S^-1 by the reference's unpivoted LU (r_GetInvLU / r_LUFactor / r_SolveLUxb).
-template <class T> __device__ void material_c(const double *ep, T C[6][6]) {
+template <class T, class P> __device__ void material_c(const P *ep, T C[6][6]) {
     T S[6][6];
     for (int i = 0; i < 6; ++i)
         for (int j = 0; j < 6; ++j) S[i][j] = T(0);
@@ -120,7 +125,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
     const int bA0 = lane >> 3, bA1 = (lane >> 3) + 4, bB = lane & 7;
     // material
     T C[6][6];
-    material_c<T>(A.elMat + 9 * (size_t)e, C);
+    if (A.Cover) {
+        for (int i = 0; i < 6; ++i)
+            for (int j = 0; j < 6; ++j) C[i][j] = T(A.Cover[36 * (size_t)item + 6 * i + j]);
+    } else {
+        material_c<T>(A.elMat + 9 * (size_t)e, C);
+    }
     T Or[3][3];
     if (GENERAL && A.orient) {
         for (int i = 0; i < 3; ++i)
@@ -144,7 +154,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
     const T sa = (a == 1 || a == 2 || a == 5 || a == 6) ? T(1) : T(-1);
     const T ta = (a == 2 || a == 3 || a == 6 || a == 7) ? T(1) : T(-1);
     const T ua = (a >= 4) ? T(1) : T(-1);
-    const T g = T(0.57735026918962576451);  // 1/sqrt(3) (r_1rt3)
+    const T g = T(A.gpc);  // 1/sqrt(3): r_1rt3, or the complex path's single-precision c_1rt3
     T acc0[3][3], acc1[3][3], ru[3] = {T(0), T(0), T(0)};
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) acc0[i][j] = acc1[i][j] = T(0);
@@ -303,13 +313,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
 //     shear moduli on the diagonal), the same matrix r_getMaterialStiffness forms by LU;
 //   * the eight Gauss-point Jacobians in two rounds: lane (g, a) with g = lane/8 (+4), a = lane%8
 //     forms node a's contribution to J at point g and the eight lanes of a point reduce it with
-//     three xor-shuffles, then invert it and write Nx(a) to shared memory;
-//   * lane l accumulates the node-pair blocks (l/8, l%8) and (l/8+4, l%8) over the points with
-//     the sparse orthotropic B^T C B (about 27 FMA per block per point);
-//   * the 3x3 blocks are added into the block-CSR matrix; the first element (in colour order) to
-//     touch a block writes it, so an assembly pass needs no zeroing, and the old values of the
-//     other blocks are fetched before the arithmetic so their latency overlaps it.
+//     three xor-shuffles, then invert it and write the gradient g_a to shared memory (float4);
+//   * lane l owns the node pairs (l/8, l%8) and (l/8+4, l%8).  For a pair (a, b) the 3x3
+//     moment M = sum_gp w detJ g_a g_b^T is accumulated (9 FMA per point), and the block follows
+//     from the orthotropic C in one contraction (21 products):
+//       K00 = C11 M00 + C44 M11 + C55 M22,  K01 = C12 M01 + C44 M10,  K02 = C13 M02 + C55 M20, ...
+//     which is the sparse B^T C B of the element summed over the points, reassociated;
+//   * the 64 blocks go through shared memory and are added into the block-CSR matrix three whole
+//     blocks (27 lanes, 9 contiguous floats each) per warp instruction, instead of one lane per
+//     block touching a different cache line for every float; the first element (in colour order)
+//     to touch a block writes it, so an assembly pass needs no zeroing, and the old values are
+//     fetched before the arithmetic so their latency overlaps it.
 constexpr int kFW = 8;  // warps per CTA
+constexpr int kRmwSteps = 22;  // ceil(64 blocks / 3 blocks per step)
 
 struct Hex8FastArgs {
     const double *nodes;
@@ -323,36 +339,47 @@ struct Hex8FastArgs {
     double *keOut;     // element matrices (E,24,24) column-major, element DOF order, or null
 };
 
-__global__ void __launch_bounds__(32 * kFW) hex8_fast_kernel(Hex8FastArgs A) {
-    __shared__ float sNx[kFW][8][8][3];
+struct OrthoC {
+    float C11, C12, C13, C22, C23, C33, C44, C55, C66;
+};
+
+__device__ __forceinline__ void ortho_block(const OrthoC &c, const float M[9], float K[9]) {
+    K[0] = c.C11 * M[0] + c.C44 * M[4] + c.C55 * M[8];
+    K[1] = c.C12 * M[1] + c.C44 * M[3];
+    K[2] = c.C13 * M[2] + c.C55 * M[6];
+    K[3] = c.C12 * M[3] + c.C44 * M[1];
+    K[4] = c.C22 * M[4] + c.C44 * M[0] + c.C66 * M[8];
+    K[5] = c.C23 * M[5] + c.C66 * M[7];
+    K[6] = c.C13 * M[6] + c.C55 * M[2];
+    K[7] = c.C23 * M[7] + c.C66 * M[5];
+    K[8] = c.C33 * M[8] + c.C55 * M[0] + c.C66 * M[4];
+}
+
+__global__ void __launch_bounds__(32 * kFW, 3) hex8_fast_kernel(Hex8FastArgs A) {
+    __shared__ float4 sG[kFW][8][8];  // [warp][gauss point][node]: gradient of N_a, w = 0
     __shared__ float sDet[kFW][8];
+    __shared__ float sK[kFW][64 * 9];  // element blocks, block j = 8a + b at 9j (row-major 3x3)
+    __shared__ int sBlk[kFW][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int item = blockIdx.x * kFW + w;
     if (item >= A.count) return;
     const int e = A.colorEls[item];
     const int a0 = lane >> 3, a1 = a0 + 4, b = lane & 7;
-    // block targets and old values (prefetched)
-    const int k0 = A.elBlk[64 * (size_t)e + a0 * 8 + b], k1 = A.elBlk[64 * (size_t)e + a1 * 8 + b];
+    // block targets; old values of the blocks this lane updates in the cooperative phase
+    // (lane = 9 grp + q: entry q of block 3 step + grp), prefetched
+    sBlk[w][lane] = A.elBlk[64 * (size_t)e + lane];
+    sBlk[w][lane + 32] = A.elBlk[64 * (size_t)e + lane + 32];
     const unsigned long long first = A.elFirst[e];
-    const bool f0 = (first >> (a0 * 8 + b)) & 1ull, f1 = (first >> (a1 * 8 + b)) & 1ull;
-    float o0[9], o1[9];
+    const int grp = lane / 9, qq = lane - 9 * grp;
+    __syncwarp();
+    float ov[kRmwSteps];
 #pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        o0[q] = (A.K && !f0) ? A.K[9 * (size_t)k0 + q] : 0.f;
-        o1[q] = (A.K && !f1) ? A.K[9 * (size_t)k1 + q] : 0.f;
+    for (int st = 0; st < kRmwSteps; ++st) {
+        const int j = 3 * st + grp;
+        ov[st] = 0.f;
+        if (A.K && grp < 3 && j < 64 && !((first >> j) & 1ull)) ov[st] = A.K[9 * (size_t)sBlk[w][j] + qq];
     }
-    // material: closed-form orthotropic C
-    const double *ep = A.elMat + 9 * (size_t)e;
-    const float E1 = (float)ep[0], E2 = (float)ep[1], E3 = (float)ep[2];
-    const float s11 = 1.f / E1, s22 = 1.f / E2, s33 = 1.f / E3;
-    const float s12 = -(float)ep[3] / E1, s13 = -(float)ep[4] / E1, s23 = -(float)ep[5] / E2;
-    const float c11c = s22 * s33 - s23 * s23, c12c = s13 * s23 - s12 * s33, c13c = s12 * s23 - s13 * s22;
-    const float det = s11 * c11c + s12 * c12c + s13 * c13c, id = 1.f / det;
-    const float C11 = c11c * id, C12 = c12c * id, C13 = c13c * id;
-    const float C22 = (s11 * s33 - s13 * s13) * id, C23 = (s13 * s12 - s11 * s23) * id;
-    const float C33 = (s11 * s22 - s12 * s12) * id;
-    const float C44 = (float)ep[6], C55 = (float)ep[7], C66 = (float)ep[8];
-    // node a = lane & 7 coordinates
+    // node b = lane & 7 coordinates
     const int na = A.elist[8 * (size_t)e + b];
     const float X0 = (float)A.nodes[3 * (size_t)(na - 1)], X1 = (float)A.nodes[3 * (size_t)(na - 1) + 1],
                 X2 = (float)A.nodes[3 * (size_t)(na - 1) + 2];
@@ -381,39 +408,57 @@ __global__ void __launch_bounds__(32 * kFW) hex8_fast_kernel(Hex8FastArgs A) {
                     I21 = di * (J[1] * J[6] - J[0] * J[7]);
         const float I02 = di * (J[1] * J[5] - J[2] * J[4]), I12 = di * (J[2] * J[3] - J[0] * J[5]),
                     I22 = di * (J[0] * J[4] - J[1] * J[3]);
-        sNx[w][gp][b][0] = n0 * I00 + n1 * I10 + n2 * I20;
-        sNx[w][gp][b][1] = n0 * I01 + n1 * I11 + n2 * I21;
-        sNx[w][gp][b][2] = n0 * I02 + n1 * I12 + n2 * I22;
+        sG[w][gp][b] = make_float4(n0 * I00 + n1 * I10 + n2 * I20, n0 * I01 + n1 * I11 + n2 * I21,
+                                   n0 * I02 + n1 * I12 + n2 * I22, 0.f);
         if (b == 0) sDet[w][gp] = dt;
     }
+    // material: closed-form orthotropic C (after the shuffles, so it is not live across them)
+    OrthoC c;
+    {
+        const double *ep = A.elMat + 9 * (size_t)e;
+        const float E1 = (float)ep[0], E2 = (float)ep[1], E3 = (float)ep[2];
+        const float s11 = 1.f / E1, s22 = 1.f / E2, s33 = 1.f / E3;
+        const float s12 = -(float)ep[3] / E1, s13 = -(float)ep[4] / E1, s23 = -(float)ep[5] / E2;
+        const float c11c = s22 * s33 - s23 * s23, c12c = s13 * s23 - s12 * s33, c13c = s12 * s23 - s13 * s22;
+        const float det = s11 * c11c + s12 * c12c + s13 * c13c, id = 1.f / det;
+        c.C11 = c11c * id;
+        c.C12 = c12c * id;
+        c.C13 = c13c * id;
+        c.C22 = (s11 * s33 - s13 * s13) * id;
+        c.C23 = (s13 * s12 - s11 * s23) * id;
+        c.C33 = (s11 * s22 - s12 * s12) * id;
+        c.C44 = (float)ep[6];
+        c.C55 = (float)ep[7];
+        c.C66 = (float)ep[8];
+    }
     __syncwarp();
-    float K0[9] = {}, K1[9] = {};
+    float M0[9] = {}, M1[9] = {};
 #pragma unroll
     for (int gp = 0; gp < 8; ++gp) {
         const float wd = sDet[w][gp];
-        const float h0 = sNx[w][gp][b][0] * wd, h1 = sNx[w][gp][b][1] * wd, h2 = sNx[w][gp][b][2] * wd;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int a = half ? a1 : a0;
-            const float g0 = sNx[w][gp][a][0], g1 = sNx[w][gp][a][1], g2 = sNx[w][gp][a][2];
-            float *Kb = half ? K1 : K0;
-            Kb[0] += g0 * C11 * h0 + g1 * C44 * h1 + g2 * C55 * h2;
-            Kb[1] += g0 * C12 * h1 + g1 * C44 * h0;
-            Kb[2] += g0 * C13 * h2 + g2 * C55 * h0;
-            Kb[3] += g1 * C12 * h0 + g0 * C44 * h1;
-            Kb[4] += g1 * C22 * h1 + g0 * C44 * h0 + g2 * C66 * h2;
-            Kb[5] += g1 * C23 * h2 + g2 * C66 * h1;
-            Kb[6] += g2 * C13 * h0 + g0 * C55 * h2;
-            Kb[7] += g2 * C23 * h1 + g1 * C66 * h2;
-            Kb[8] += g2 * C33 * h2 + g0 * C55 * h0 + g1 * C66 * h1;
-        }
+        const float4 hb = sG[w][gp][b], ga = sG[w][gp][a0], gc = sG[w][gp][a1];
+        const float h0 = hb.x * wd, h1 = hb.y * wd, h2 = hb.z * wd;
+        M0[0] += ga.x * h0; M0[1] += ga.x * h1; M0[2] += ga.x * h2;
+        M0[3] += ga.y * h0; M0[4] += ga.y * h1; M0[5] += ga.y * h2;
+        M0[6] += ga.z * h0; M0[7] += ga.z * h1; M0[8] += ga.z * h2;
+        M1[0] += gc.x * h0; M1[1] += gc.x * h1; M1[2] += gc.x * h2;
+        M1[3] += gc.y * h0; M1[4] += gc.y * h1; M1[5] += gc.y * h2;
+        M1[6] += gc.z * h0; M1[7] += gc.z * h1; M1[8] += gc.z * h2;
     }
+    float K0[9], K1[9];
+    ortho_block(c, M0, K0);
+    ortho_block(c, M1, K1);
     if (A.K) {
-        float *d0 = A.K + 9 * (size_t)k0, *d1 = A.K + 9 * (size_t)k1;
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
-            d0[q] = o0[q] + K0[q];
-            d1[q] = o1[q] + K1[q];
+            sK[w][9 * lane + q] = K0[q];
+            sK[w][9 * (lane + 32) + q] = K1[q];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int st = 0; st < kRmwSteps; ++st) {
+            const int j = 3 * st + grp;
+            if (grp < 3 && j < 64) A.K[9 * (size_t)sBlk[w][j] + qq] = ov[st] + sK[w][9 * j + qq];
         }
     }
     if (A.keOut) {
@@ -424,6 +469,28 @@ __global__ void __launch_bounds__(32 * kFW) hex8_fast_kernel(Hex8FastArgs A) {
                 ke[(size_t)(8 * j + b) * 24 + (8 * i + a1)] = (double)K1[3 * i + j];
             }
     }
+}
+
+// Imaginary part of the complex-step material stiffness of each listed element:
+// eProps(c) + coef (d + i h) for the elastic-modulus design variable dvar (the real parts of all
+// design-variable terms are already in elMat), then C = S^-1 in complex arithmetic.
+__global__ void k_hex_cim(int count, const int *__restrict__ els, const double *__restrict__ elMat,
+                          const int *__restrict__ e2dR, const int *__restrict__ e2d, const double *__restrict__ e2c,
+                          const int *__restrict__ dcat, const int *__restrict__ dcomp, int dvar, double h,
+                          double *__restrict__ Cim) {
+    const int item = blockIdx.x * blockDim.x + threadIdx.x;
+    if (item >= count) return;
+    const int e = els[item];
+    cplx ep[9];
+    for (int k = 0; k < 9; ++k) ep[k] = cplx(elMat[9 * (size_t)e + k]);
+    for (int q = e2dR[e]; q < e2dR[e + 1]; ++q) {
+        const int d = e2d[q];
+        if (d == dvar && dcat[d - 1] == ASTRO_DCAT_ELASTIC_MODULUS) ep[dcomp[d - 1] - 1] += cplx(0.0, e2c[q] * h);
+    }
+    cplx C[6][6];
+    material_c<cplx>(ep, C);
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) Cim[36 * (size_t)item + 6 * i + j] = C[i][j].im;
 }
 
 }  // namespace
@@ -473,6 +540,8 @@ static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_di
             A.loadInt = d_loadInt;
             A.keOut = d_ke;
             A.ruOut = d_ru;
+            A.gpc = kRt3;
+            A.Cover = nullptr;
             hex8_kernel<double, true><<<grid, block, 0, ctx->stream>>>(A);
         } else {
             Hex8Args<float> A;
@@ -490,6 +559,8 @@ static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_di
             A.loadInt = nullptr;
             A.keOut = d_ke;
             A.ruOut = nullptr;
+            A.gpc = kRt3;
+            A.Cover = nullptr;
             hex8_kernel<float, false><<<grid, block, 0, ctx->stream>>>(A);
         }
     }
@@ -520,4 +591,55 @@ int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
 
 int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru) {
     return hex8_run(ctx, 64, 0, d_disp, nullptr, d_ke, d_ru);
+}
+
+int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *d_acc) {
+    std::vector<int> list, ptr;
+    dvar_elements_by_colour(ctx, dvar, list, ptr);
+    const int cnt = (int)list.size();
+    if (!cnt) return ASTRO_OK;
+    DevBuf dl, dC, dR, dE, dEC, dCat, dComp;
+    struct Free {
+        DevBuf *b[7];
+        ~Free() {
+            for (auto *x : b) dev_free(*x);
+        }
+    } fr{{&dl, &dC, &dR, &dE, &dEC, &dCat, &dComp}};
+    int rc;
+    if ((rc = upload(ctx, dl, list.data(), sizeof(int) * cnt))) return rc;
+    if ((rc = dev_alloc(ctx, dC, sizeof(double) * 36 * (size_t)cnt))) return rc;
+    if ((rc = upload(ctx, dR, ctx->e2dRange.data(), sizeof(int) * ctx->e2dRange.size()))) return rc;
+    if ((rc = upload(ctx, dE, ctx->e2d.data(), sizeof(int) * ctx->e2d.size()))) return rc;
+    if ((rc = upload(ctx, dEC, ctx->e2c.data(), sizeof(double) * ctx->e2c.size()))) return rc;
+    if ((rc = upload(ctx, dCat, ctx->dCat.data(), sizeof(int) * ctx->dCat.size()))) return rc;
+    if ((rc = upload(ctx, dComp, ctx->dComp.data(), sizeof(int) * ctx->dComp.size()))) return rc;
+    k_hex_cim<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(cnt, dptr<int>(dl), dptr<double>(ctx->d_elMat), dptr<int>(dR),
+                                                          dptr<int>(dE), dptr<double>(dEC), dptr<int>(dCat),
+                                                          dptr<int>(dComp), dvar, h, dptr<double>(dC));
+    const AstroPrep &P = ctx->P;
+    for (int col = 0; col < P.ncolors; ++col) {
+        const int c = ptr[col + 1] - ptr[col];
+        if (!c) continue;
+        Hex8Args<double> A;
+        A.nodes = dptr<double>(ctx->d_nodes);
+        A.elist = dptr<int>(ctx->d_elist);
+        A.rank = dptr<int>(ctx->d_rank);
+        A.colorEls = dptr<int>(dl) + ptr[col];
+        A.count = c;
+        A.elBlk = dptr<int>(ctx->d_elBlk);
+        A.elMat = dptr<double>(ctx->d_elMat);
+        A.orient = ctx->orientIdentity ? nullptr : dptr<double>(ctx->d_secOrient);
+        A.disp = d_disp;
+        A.Kbsr = nullptr;
+        A.Kbsr64 = nullptr;
+        A.loadInt = d_acc;
+        A.keOut = nullptr;
+        A.ruOut = nullptr;
+        A.gpc = kRt3c;
+        A.Cover = dptr<double>(dC) + 36 * (size_t)ptr[col];
+        hex8_kernel<double, true><<<(c + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, ctx->stream>>>(A);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return cuda_check(ctx, e, "brick8 complex-step kernels");
 }

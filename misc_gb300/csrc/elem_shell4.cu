@@ -53,7 +53,9 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
     }
     std::vector<double> zo(S);
     for (int s = 0; s < S; ++s) zo[s] = m->section_z_offset ? m->section_z_offset[s] : 0.0;
-    DevBuf dlr, dlay, dzo, de2dR, de2d, de2c, dcat, dlayer, dval;
+    // the section inputs stay on the device for the complex-step property evaluation
+    DevBuf &dlr = ctx->d_shLayRange, &dlay = ctx->d_shLay, &dzo = ctx->d_shZoff, &de2dR = ctx->d_e2dR,
+           &de2d = ctx->d_e2d, &de2c = ctx->d_e2c, &dcat = ctx->d_dCat, &dlayer = ctx->d_dLayer, &dval = ctx->d_dVal;
     int rc;
     if ((rc = upload(ctx, dlr, lr.data(), sizeof(int) * lr.size()))) return rc;
     if ((rc = upload(ctx, dlay, lay.data(), sizeof(LayerDev) * lay.size()))) return rc;
@@ -61,11 +63,13 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
     const bool dv = m->num_dvars > 0 && m->el_to_d_range;
     if (dv) {
         const int nE2D = m->el_to_d_range[E];
+        std::vector<int> dl(m->num_dvars, 0);
+        if (m->d_layer) dl.assign(m->d_layer, m->d_layer + m->num_dvars);
         if ((rc = upload(ctx, de2dR, m->el_to_d_range, sizeof(int) * (E + 1)))) return rc;
         if ((rc = upload(ctx, de2d, m->el_to_d, sizeof(int) * std::max(nE2D, 1)))) return rc;
         if ((rc = upload(ctx, de2c, m->el_to_coef, sizeof(double) * std::max(nE2D, 1)))) return rc;
         if ((rc = upload(ctx, dcat, m->d_category, sizeof(int) * m->num_dvars))) return rc;
-        if ((rc = upload(ctx, dlayer, m->d_layer, sizeof(int) * m->num_dvars))) return rc;
+        if ((rc = upload(ctx, dlayer, dl.data(), sizeof(int) * m->num_dvars))) return rc;
         if ((rc = upload(ctx, dval, m->d_value, sizeof(double) * m->num_dvars))) return rc;
     }
     if ((rc = upload(ctx, ctx->d_secOrient, m->section_orient, sizeof(double) * 9 * S))) return rc;
@@ -77,17 +81,18 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
         dv ? dptr<int>(dlayer) : nullptr, dv ? dptr<double>(dval) : nullptr, dptr<ShellProps>(ctx->d_secABD));
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    DevBuf *bufs[] = {&dlr, &dlay, &dzo, &de2dR, &de2d, &de2c, &dcat, &dlayer, &dval};
-    for (auto *b : bufs) dev_free(*b);
     if (!ctx->d_intMat.p && (rc = dev_alloc(ctx, ctx->d_intMat, sizeof(double) * 256 * (size_t)E))) return rc;
     return cuda_check(ctx, e, "shell properties");
 }
 
-int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_loadInt, double *d_intLoad, int buildMat,
-                           double *d_ke, double *d_ru) {
-    const AstroPrep &P = ctx->P;
+// The five pipeline kernels over the elements of each colour in turn: colour c covers
+// els[ptr[c] .. ptr[c+1]) (device list).
+static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
+                          const ShellProps *props, double gpc, double *d_loadInt, double *d_intLoad, int buildMat,
+                          double *d_K, double *d_intMat, double *d_ke, double *d_ru) {
     int maxc = 0;
-    for (int col = 0; col < P.ncolors; ++col) maxc = std::max(maxc, P.colorPtr[col + 1] - P.colorPtr[col]);
+    for (size_t c = 0; c + 1 < ptr.size(); ++c) maxc = std::max(maxc, ptr[c + 1] - ptr[c]);
+    if (!maxc) return ASTRO_OK;
     DevBuf fr, gp, de, kf;
     int rc;
     if ((rc = dev_alloc(ctx, fr, sizeof(ShellFrame) * (size_t)maxc))) return rc;
@@ -99,7 +104,7 @@ int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_lo
     A.elist = dptr<int>(ctx->d_elist);
     A.rank = dptr<int>(ctx->d_rank);
     A.elBlk = dptr<int>(ctx->d_elBlk);
-    A.props = dptr<ShellProps>(ctx->d_secABD);
+    A.props = props;
     A.disp = st.disp;
     A.pdisp = st.pdisp;
     A.pvel = st.pvel;
@@ -111,21 +116,22 @@ int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_lo
     A.delT = st.delT;
     A.buildMat = buildMat;
     A.quirk = ctx->quirkShellMeanRot;
+    A.gpc = gpc;
     A.fr = dptr<ShellFrame>(fr);
     A.gp = dptr<ShellGP>(gp);
     A.dedU = dptr<double>(de);
     A.Kf = dptr<double>(kf);
-    A.K = (buildMat && !d_ke) ? dptr<double>(ctx->d_K64) : nullptr;
+    A.K = d_K;
     A.load = d_loadInt;
     A.intLoad = d_intLoad;
-    A.intMat = (buildMat && !d_ke) ? dptr<double>(ctx->d_intMat) : nullptr;
+    A.intMat = d_intMat;
     A.keOut = d_ke;
     A.ruOut = d_ru;
     cudaStream_t s = ctx->stream;
-    for (int col = 0; col < P.ncolors; ++col) {
-        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+    for (size_t col = 0; col + 1 < ptr.size(); ++col) {
+        const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
-        A.els = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+        A.els = d_els + ptr[col];
         A.count = cnt;
         k_shell_frame<<<(cnt + 63) / 64, 64, 0, s>>>(A);
         k_shell_gauss<<<(4 * cnt + 127) / 128, 128, 0, s>>>(A);
@@ -140,4 +146,66 @@ int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_lo
     dev_free(de);
     dev_free(kf);
     return cuda_check(ctx, e, "shell pipeline");
+}
+
+int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_loadInt, double *d_intLoad, int buildMat,
+                           double *d_ke, double *d_ru) {
+    const bool toK = buildMat && !d_ke;
+    return shell_pipeline(ctx, st, dptr<int>(ctx->d_colorEls), ctx->P.colorPtr, dptr<ShellProps>(ctx->d_secABD), kShellRt3,
+                          d_loadInt, d_intLoad, buildMat, toK ? dptr<double>(ctx->d_K64) : nullptr,
+                          toK ? dptr<double>(ctx->d_intMat) : nullptr, d_ke, d_ru);
+}
+
+// Complex-step properties of the listed elements: orientation (real part), imaginary parts of
+// ABD and of the section mass, written over a copy of the per-element properties.
+__global__ void k_shell_props_im(int count, const int *els, const double *nodes, const int *elist, const int *esec,
+                                 const double *secOrient, const int *layRange, const LayerDev *lay, const double *zoff,
+                                 const int *e2dR, const int *e2d, const double *e2c, const int *dcat, const int *dlay,
+                                 const double *dval, int dvar, double h, ShellProps *out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    const int e = els[q];
+    cplx o[3][3], ABD[9][9], M[6][6];
+    shell_props<cplx>(nodes, elist + 8 * (size_t)e, secOrient, esec[e], layRange, lay, zoff, e2dR, e2d, e2c, dcat, dlay,
+                      dval, e, dvar, h, o, ABD, M);
+    ShellProps &P = out[e];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) P.orient[3 * i + j] = o[i][j].re;
+    for (int i = 0; i < 9; ++i)
+        for (int j = 0; j < 9; ++j) P.ABD[9 * i + j] = ABD[i][j].im;
+    for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) P.M[6 * i + j] = M[i][j].im;
+}
+
+int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, double *d_acc, double *d_intAcc) {
+    std::vector<int> list, ptr;
+    dvar_elements_by_colour(ctx, dvar, list, ptr);
+    const int cnt = (int)list.size();
+    if (!cnt) return ASTRO_OK;
+    const int E = ctx->P.E;
+    DevBuf dl, props;
+    int rc;
+    if ((rc = upload(ctx, dl, list.data(), sizeof(int) * cnt))) return rc;
+    if ((rc = dev_alloc(ctx, props, sizeof(ShellProps) * (size_t)E))) {
+        dev_free(dl);
+        return rc;
+    }
+    cudaError_t e = cudaMemcpyAsync(props.p, ctx->d_secABD.p, sizeof(ShellProps) * (size_t)E, cudaMemcpyDeviceToDevice,
+                                    ctx->stream);
+    if (e == cudaSuccess) {
+        k_shell_props_im<<<(cnt + 63) / 64, 64, 0, ctx->stream>>>(
+            cnt, dptr<int>(dl), dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist), dptr<int>(ctx->d_esec),
+            dptr<double>(ctx->d_secOrient), dptr<int>(ctx->d_shLayRange), dptr<LayerDev>(ctx->d_shLay),
+            dptr<double>(ctx->d_shZoff), dptr<int>(ctx->d_e2dR), dptr<int>(ctx->d_e2d), dptr<double>(ctx->d_e2c),
+            dptr<int>(ctx->d_dCat), dptr<int>(ctx->d_dLayer), dptr<double>(ctx->d_dVal), dvar, h,
+            dptr<ShellProps>(props));
+        e = cudaGetLastError();
+    }
+    rc = cuda_check(ctx, e, "shell complex-step properties");
+    if (!rc)
+        rc = shell_pipeline(ctx, st, dptr<int>(dl), ptr, dptr<ShellProps>(props), kShellRt3c, d_acc, d_intAcc, 0, nullptr,
+                            nullptr, nullptr, nullptr);
+    dev_free(dl);
+    dev_free(props);
+    return rc;
 }

@@ -15,6 +15,9 @@
 
 namespace {
 
+constexpr double kShellRt3 = 0.57735026918962576451;  // r_1rt3
+constexpr double kShellRt3c = LIT(0.577350269189626);  // c_1rt3 (single-precision literal)
+
 struct ShellFrame {
     double io[16][9];   // instantaneous frame, block 4a+b (a,b = rotation components, 0 = none)
     double dr[16][3];   // axial vectors of the frame derivatives
@@ -42,6 +45,7 @@ struct ShellPipe {
     int dynamic;
     double beta, gamma, delT;
     int buildMat, quirk;
+    double gpc;      // Gauss point coordinate: r_1rt3, or the complex path's single-precision c_1rt3
     ShellFrame *fr;
     ShellGP *gp;     // count*4
     double *dedU;    // count*4*32*9
@@ -156,7 +160,7 @@ __device__ void pipe_gauss(const ShellPipe &A, int q, int g) {
     const ShellFrame &F = A.fr[q];
     ShellGP &G = A.gp[4 * (size_t)q + g];
     const ShellProps &P = A.props[A.els[q]];
-    const double r3 = 0.57735026918962576451;
+    const double r3 = A.gpc;
     const double s1 = (g & 1) ? r3 : -r3, s2 = (g & 2) ? r3 : -r3;
     double N[11], d0[11], d1[11];
     N[0] = 0.25 * (1 - s1) * (1 - s2); d0[0] = -0.25 * (1 - s2); d1[0] = -0.25 * (1 - s1);

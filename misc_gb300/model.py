@@ -185,6 +185,24 @@ def make_state(n, n_int=0, disp=None, vel=None, acc=None, prev_disp=None, prev_v
     return s
 
 
+def add_design_variables(m: Model, n_groups: int, category: int, layer: int = 1, component: int = 1,
+                         value: float = 0.0) -> Model:
+    """Attaches n_groups design variables of one category to m, one per contiguous group of
+    elements (element e belongs to group e * n_groups // num_els), each entering its elements
+    with coefficient 1: thickness of layer `layer` (+ d) or materialElastic entry `component`
+    (+ d).  The reference's dVec / elToD maps (Working/AStrO_input.f90 design-variable input)."""
+    E = m.num_els
+    grp = (np.arange(E) * n_groups) // E + 1
+    m.el_to_d_range = np.arange(E + 1, dtype=np.int32)
+    m.el_to_d = grp.astype(np.int32)
+    m.el_to_coef = np.ones(E)
+    m.d_category = np.full(n_groups, category, np.int32)
+    m.d_component = np.full(n_groups, component, np.int32)
+    m.d_layer = np.full(n_groups, layer, np.int32)
+    m.d_value = np.full(n_groups, float(value))
+    return m
+
+
 def _iso(E, nu, G=None):
     """materialElastic(9) for an isotropic material; G = E/(2(1+nu)) when not given
     (Working/AStrO_input.f90:807-809)."""

@@ -44,6 +44,7 @@ def _lib():
         L.orc_element_c.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_double,
                                     F64P, F64P, F64P, F64P]
         L.orc_element_matrices.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, F64P]
+        L.orc_drdd_complex.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p, F64P, F64P]
         L.orc_el_soln_load.argtypes = [C.c_void_p, C.c_int, C.c_void_p, F64P, F64P, F64P, I32P, F64P]
         L.orc_scale_mpc.argtypes = [F64P, C.c_int, F64P, F64P, I32P, C.c_int]
         L.orc_constraint_load.argtypes = [F64P, I32P, I32P, F64P, C.c_int, F64P, F64P]
@@ -123,6 +124,15 @@ class Oracle:
                                   _d(rr), _d(ri), kr.ctypes.data_as(F64P), ki.ctypes.data_as(F64P))
         assert rc == 0
         return rr + 1j * ri, kr + 1j * ki
+
+    def drdd_complex(self, dvar, h=1e-14, state=None):
+        """getdRelasticdD element part: (dRu/dd in global DOF, dRu/dd at the internal DOF)."""
+        out = np.zeros(self.n)
+        iout = np.zeros(max(self.int_vec_size, 1))
+        rc = self.L.orc_drdd_complex(self.h, dvar, h, C.byref(state) if state is not None else None, _d(out),
+                                     _d(iout))
+        assert rc == 0
+        return out, iout[:self.int_vec_size]
 
     def element_matrices(self, el0=1, el1=None, state=None):
         """Condensed nodal element matrices (24x24) of elements el0..el1 (1-based, inclusive)."""

@@ -401,6 +401,45 @@ int orc_element_c(const OracleCtx *c, int el, int buildMat, const astro_state *s
     return 0;
 }
 
+// getdRelasticdD element part, Working/AStrO_commandFunctions.f90:1172-1250: the elements that
+// depend on design variable dvar are re-evaluated in complex FP64 with d_value(dvar) + i h
+// (c_getElRu with buildMat = 0), and Im(Ru) * (1/h) is summed into dRudD at the element's global
+// DOF (Q10 resolved: the global index, not the element-local one) and into intdRudD at its
+// internal DOF.  Both outputs are zeroed first, as the reference does.  Elements are visited in
+// ascending order (the order getdToElComp lists them).
+int orc_drdd_complex(const OracleCtx *c, int dvar, double h, const astro_state *s, double *dRudD, double *intdRudD) {
+    const astro_model *m = c->m;
+    std::fill(dRudD, dRudD + c->elMatDim, 0.0);
+    if (intdRudD && c->intVecSize > 0) std::fill(intdRudD, intdRudD + c->intVecSize, 0.0);
+    if (dvar < 1 || dvar > m->num_dvars || !m->el_to_d_range) return 1;
+    const double hInv = 1.0 / h;
+    GState g = to_gstate(s);
+    DPert<cd> p;
+    p.dvar = dvar;
+    p.h = h;
+    for (int el = 1; el <= c->numEls; ++el) {
+        bool dep = false;
+        for (int q = m->el_to_d_range[el - 1]; q < m->el_to_d_range[el]; ++q) dep = dep || m->el_to_d[q] == dvar;
+        if (!dep) continue;
+        A1<cd, 33> Ru;
+        A2<cd, 33, 33> K;
+        ElemData<cd> e;
+        if (t_element(Ru, K, m, c->nDofIndex.data(), c->intVecRange.data(), el, 0, g, p, &e) != 0) return 1;
+        const int nd = e.numNds * e.dofPerNd;
+        for (int i = 1; i <= nd; ++i) {
+            const int var = e.dofTable[i - 1][0];
+            const int node = m->element_list[8 * (el - 1) + e.dofTable[i - 1][1] - 1];
+            const int dof = c->nDofIndex[6 * (node - 1) + var - 1];
+            dRudD[dof - 1] += hInv * Ru(i).imag();
+        }
+        if (e.numIntDof > 0 && intdRudD) {
+            int k = c->intVecRange[el - 1];
+            for (int i = nd + 1; i <= nd + e.numIntDof; ++i) intdRudD[k++] += hInv * Ru(i).imag();
+        }
+    }
+    return 0;
+}
+
 // Element matrices of elements el0..el1 (1-based, inclusive) in FP64 after static condensation,
 // nodal part only (nd x nd per element, column-major, nd = numNds*dofPerNd = 24).  Used by the
 // CPU baseline timing and the per-element parity tests.

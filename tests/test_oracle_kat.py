@@ -131,3 +131,51 @@ def test_solver_max_bw_wraps_like_fortran_integers():
     while b**3 < t32:
         b += 1
     assert b == 1289
+
+
+def _fd_drdd(model_fn, dvar, state_fn, rel=1e-6):
+    """Central difference of the residual (-elastic_load) with respect to design variable dvar."""
+    m0 = model_fn()
+    step = rel * max(1.0, abs(m0.d_value[dvar - 1]))
+    if m0.d_category[dvar - 1] == M.DCAT_LAYUP_THICKNESS:
+        step = rel * float(m0.layup_thickness[0])
+    elif m0.d_category[dvar - 1] == M.DCAT_ELASTIC_MODULUS:
+        step = rel * float(m0.material_elastic[0, m0.d_component[dvar - 1] - 1])
+    out = []
+    for sgn in (1.0, -1.0):
+        m = model_fn()
+        m.d_value = m.d_value.copy()
+        m.d_value[dvar - 1] += sgn * step
+        o = Oracle(m)
+        load, iload, *_ = o.el_soln_load(0, state=state_fn(o))
+        out.append((-load, -iload[:o.int_vec_size]))
+    return (out[0][0] - out[1][0]) / (2 * step), (out[0][1] - out[1][1]) / (2 * step)
+
+
+@pytest.mark.parametrize("kind", ["shell_thickness", "brick_modulus"])
+def test_complex_step_matches_central_difference(kind):
+    """The oracle's complex twin (getdRelasticdD) against a central difference of the real
+    residual.  The complex path's Gauss points are the single-precision 1/sqrt(3), so the two
+    differ at the 1e-8 level; the check is 1e-5 relative."""
+    if kind == "shell_thickness":
+        def model_fn():
+            m = M.plate_shell(nx=4, ny=3, lx=2.0, ly=1.0, t=0.03, E=7e10, nu=0.33)
+            return M.add_design_variables(m, 3, M.DCAT_LAYUP_THICKNESS)
+    else:
+        def model_fn():
+            m = M.hex_block(nx=3, ny=2, nz=2, jitter=0.1, seed=3)
+            return M.add_design_variables(m, 2, M.DCAT_ELASTIC_MODULUS, component=1)
+
+    def state_fn(o):
+        rng = np.random.default_rng(7)
+        return M.make_state(o.n, disp=1e-3 * rng.standard_normal(o.n),
+                            internal_disp=1e-4 * rng.standard_normal(max(o.int_vec_size, 1)))
+
+    o = Oracle(model_fn())
+    for dvar in (1, 2):
+        cs, ics = o.drdd_complex(dvar, 1e-14, state=state_fn(o))
+        fd, ifd = _fd_drdd(model_fn, dvar, state_fn)
+        assert np.linalg.norm(cs) > 0
+        assert np.linalg.norm(cs - fd) <= 1e-5 * np.linalg.norm(fd)
+        if o.int_vec_size:
+            assert np.linalg.norm(ics - ifd) <= 1e-5 * np.linalg.norm(ifd)
