@@ -274,9 +274,16 @@ struct DevState {
     }
 };
 
-static int state_vec_up(astro_ctx *ctx, const double *h, DevBuf &dst) {
+// A state vector that is all zero stays null on the device: every kernel reads a null state
+// vector as zeros, and the brick kernels take the zero-state path.
+static int state_vec_up(astro_ctx *ctx, const double *h, DevBuf &dst, bool zero_is_null = true) {
     if (!h) return ASTRO_OK;
     const int n = ctx->P.n;
+    if (zero_is_null) {
+        bool nz = false;
+        for (int i = 0; i < n && !nz; ++i) nz = h[i] != 0.0;
+        if (!nz) return ASTRO_OK;
+    }
     DevBuf tmp;
     int rc = upload(ctx, tmp, h, sizeof(double) * n);
     if (!rc) rc = dev_alloc(ctx, dst, sizeof(double) * n);
@@ -326,10 +333,11 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
         }
     }
     DevBuf dl;
-    if ((rc = state_vec_up(ctx, elastic_load, dl))) return rc;
+    if ((rc = state_vec_up(ctx, elastic_load, dl, false))) return rc;
     if (build_mat == 1) {
         if ((rc = ensure_K(ctx, 2))) return rc;
-        if ((rc = bsr_zero(ctx, 2))) return rc;
+        // the brick zero-state kernel writes every block (first touch), the other paths add
+        if (!(ctx->hasSolid && !S.disp.p) && (rc = bsr_zero(ctx, 2))) return rc;
     }
     if (state && state->dynamic && ctx->hasSolid)
         return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
@@ -620,7 +628,7 @@ extern "C" int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t 
     int rc;
     if ((rc = upload(ctx, dfe, face_el, sizeof(int) * nfaces))) return rc;
     if ((rc = upload(ctx, dfn, face_num, sizeof(int) * nfaces))) return rc;
-    if ((rc = state_vec_up(ctx, elastic_load, dl))) return rc;
+    if ((rc = state_vec_up(ctx, elastic_load, dl, false))) return rc;
     if ((rc = surface_load_dev(ctx, nfaces, dptr<int>(dfe), dptr<int>(dfn), tr, pressure, dptr<double>(dl)))) return rc;
     if ((rc = dev_alloc(ctx, dref, sizeof(double) * P.n))) return rc;
     if ((rc = int_to_ref_vec(ctx, dptr<double>(dl), dptr<double>(dref), P.n))) return rc;
@@ -647,8 +655,8 @@ extern "C" int astro_solve_static(astro_ctx *ctx, const double *f, double *u, co
     const int n = ctx->P.n;
     DevBuf db, dx;
     int rc;
-    if ((rc = state_vec_up(ctx, f, db))) return rc;
-    if ((rc = state_vec_up(ctx, u, dx))) return rc;
+    if ((rc = state_vec_up(ctx, f, db, false))) return rc;
+    if ((rc = state_vec_up(ctx, u, dx, false))) return rc;
     rc = krylov_solve_static(ctx, dptr<double>(db), dptr<double>(dx), opts, stats);
     if (rc && rc != ASTRO_ERR_MAXIT) {
         dev_free(db);
@@ -674,7 +682,7 @@ extern "C" int astro_apply_operator(astro_ctx *ctx, int32_t kind, const double *
     const int n = ctx->P.n;
     DevBuf dx, dy, dref;
     int rc;
-    if ((rc = state_vec_up(ctx, x, dx))) return rc;
+    if ((rc = state_vec_up(ctx, x, dx, false))) return rc;
     if ((rc = dev_alloc(ctx, dy, sizeof(double) * n))) return rc;
     if ((rc = krylov_apply(ctx, kind, dptr<double>(dx), dptr<double>(dy)))) return rc;
     if ((rc = dev_alloc(ctx, dref, sizeof(double) * n))) return rc;

@@ -307,27 +307,47 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
 }
 
 // ---------------------------------------------------------------------------------------------
-// FP32 assembly kernel for the zero state with identity section orientation (the small-strain
-// stiffness of the brick8 element, the mixed-precision solver's matrix).  Per element (one warp):
+// Zero-state brick8 stiffness and assembly: FP32 for the mixed-precision solver's matrix, FP64
+// for getElasticSolnLoad from the undeformed state (where the residual is exactly zero and the
+// tangent is the small-strain stiffness).  Per element (one warp):
 //   * C from the orthotropic engineering constants in closed form (3x3 normal block inverse,
 //     shear moduli on the diagonal), the same matrix r_getMaterialStiffness forms by LU;
+//   * the node coordinates in the section frame (orient X, as r_getElementData stages them);
 //   * the eight Gauss-point Jacobians in two rounds: lane (g, a) with g = lane/8 (+4), a = lane%8
 //     forms node a's contribution to J at point g and the eight lanes of a point reduce it with
-//     three xor-shuffles, then invert it and write the gradient g_a to shared memory (float4);
+//     three xor-shuffles, then invert it and write the gradient g_a to shared memory;
 //   * lane l owns the node pairs (l/8, l%8) and (l/8+4, l%8).  For a pair (a, b) the 3x3
 //     moment M = sum_gp w detJ g_a g_b^T is accumulated (9 FMA per point), and the block follows
 //     from the orthotropic C in one contraction (21 products):
 //       K00 = C11 M00 + C44 M11 + C55 M22,  K01 = C12 M01 + C44 M10,  K02 = C13 M02 + C55 M20, ...
-//     which is the sparse B^T C B of the element summed over the points, reassociated;
+//     which is the sparse B^T C B of the element summed over the points, reassociated; a rotated
+//     section frame maps the block back with orient^T K orient;
 //   * the 64 blocks go through shared memory and are added into the block-CSR matrix three whole
-//     blocks (27 lanes, 9 contiguous floats each) per warp instruction, instead of one lane per
-//     block touching a different cache line for every float; the first element (in colour order)
-//     to touch a block writes it, so an assembly pass needs no zeroing, and the old values are
-//     fetched before the arithmetic so their latency overlaps it.
-constexpr int kFW = 8;  // warps per CTA
+//     blocks (27 lanes, 9 contiguous values each) per warp instruction, instead of one lane per
+//     block touching a different cache line for every value; the first element (in colour order)
+//     to touch a block writes it, so an assembly pass needs no zeroing.  In FP32 the old values
+//     are fetched before the arithmetic so their latency overlaps it (in FP64 the registers are
+//     better spent on occupancy).
 constexpr int kRmwSteps = 22;  // ceil(64 blocks / 3 blocks per step)
 
-struct Hex8FastArgs {
+struct __align__(32) Dbl4 {
+    double x, y, z, w;
+};
+template <class T> struct FastCfg;
+template <> struct FastCfg<float> {
+    using V4 = float4;
+    static constexpr int FW = 8, MINB = 3;  // warps per CTA, CTAs per SM
+    static constexpr bool PREFETCH = true;
+    static __device__ __forceinline__ float4 make(float x, float y, float z) { return make_float4(x, y, z, 0.f); }
+};
+template <> struct FastCfg<double> {
+    using V4 = Dbl4;
+    static constexpr int FW = 4, MINB = 4;
+    static constexpr bool PREFETCH = false;
+    static __device__ __forceinline__ Dbl4 make(double x, double y, double z) { return Dbl4{x, y, z, 0.0}; }
+};
+
+template <class T> struct Hex8FastArgs {
     const double *nodes;
     const int *elist;
     const int *colorEls;
@@ -335,15 +355,16 @@ struct Hex8FastArgs {
     const int *elBlk;
     const unsigned long long *elFirst;
     const double *elMat;
-    float *K;          // BSR FP32 or null
-    double *keOut;     // element matrices (E,24,24) column-major, element DOF order, or null
+    const double *orient;  // (E,9) column-major section orientation (used when ROT)
+    T *K;                  // BSR values or null
+    double *keOut;         // element matrices (E,24,24) column-major, element DOF order, or null
 };
 
-struct OrthoC {
-    float C11, C12, C13, C22, C23, C33, C44, C55, C66;
+template <class T> struct OrthoC {
+    T C11, C12, C13, C22, C23, C33, C44, C55, C66;
 };
 
-__device__ __forceinline__ void ortho_block(const OrthoC &c, const float M[9], float K[9]) {
+template <class T> __device__ __forceinline__ void ortho_block(const OrthoC<T> &c, const T M[9], T K[9]) {
     K[0] = c.C11 * M[0] + c.C44 * M[4] + c.C55 * M[8];
     K[1] = c.C12 * M[1] + c.C44 * M[3];
     K[2] = c.C13 * M[2] + c.C55 * M[6];
@@ -355,89 +376,121 @@ __device__ __forceinline__ void ortho_block(const OrthoC &c, const float M[9], f
     K[8] = c.C33 * M[8] + c.C55 * M[0] + c.C66 * M[4];
 }
 
-__global__ void __launch_bounds__(32 * kFW, 3) hex8_fast_kernel(Hex8FastArgs A) {
-    __shared__ float4 sG[kFW][8][8];  // [warp][gauss point][node]: gradient of N_a, w = 0
-    __shared__ float sDet[kFW][8];
-    __shared__ float sK[kFW][64 * 9];  // element blocks, block j = 8a + b at 9j (row-major 3x3)
-    __shared__ int sBlk[kFW][64];
+// K <- Or^T K Or (row-major 3x3)
+template <class T> __device__ __forceinline__ void rotate_block(const T Or[3][3], T K[9]) {
+    T W[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) W[k][j] = K[3 * k] * Or[0][j] + K[3 * k + 1] * Or[1][j] + K[3 * k + 2] * Or[2][j];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) K[3 * i + j] = Or[0][i] * W[0][j] + Or[1][i] * W[1][j] + Or[2][i] * W[2][j];
+}
+
+template <class T, bool ROT>
+__global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fast_kernel(Hex8FastArgs<T> A) {
+    constexpr int FW = FastCfg<T>::FW;
+    constexpr bool PREFETCH = FastCfg<T>::PREFETCH;
+    using V4 = typename FastCfg<T>::V4;
+    __shared__ V4 sG[FW][8][8];  // [warp][gauss point][node]: gradient of N_a, w = 0
+    __shared__ T sDet[FW][8];
+    __shared__ T sK[FW][64 * 9];  // element blocks, block j = 8a + b at 9j (row-major 3x3)
+    __shared__ int sBlk[FW][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int item = blockIdx.x * kFW + w;
+    const int item = blockIdx.x * FW + w;
     if (item >= A.count) return;
     const int e = A.colorEls[item];
     const int a0 = lane >> 3, a1 = a0 + 4, b = lane & 7;
-    // block targets; old values of the blocks this lane updates in the cooperative phase
-    // (lane = 9 grp + q: entry q of block 3 step + grp), prefetched
+    // block targets; in the cooperative phase lane = 9 grp + qq handles entry qq of block 3 st + grp
     sBlk[w][lane] = A.elBlk[64 * (size_t)e + lane];
     sBlk[w][lane + 32] = A.elBlk[64 * (size_t)e + lane + 32];
     const unsigned long long first = A.elFirst[e];
     const int grp = lane / 9, qq = lane - 9 * grp;
     __syncwarp();
-    float ov[kRmwSteps];
+    T ov[PREFETCH ? kRmwSteps : 1];
+    if (PREFETCH) {
 #pragma unroll
-    for (int st = 0; st < kRmwSteps; ++st) {
-        const int j = 3 * st + grp;
-        ov[st] = 0.f;
-        if (A.K && grp < 3 && j < 64 && !((first >> j) & 1ull)) ov[st] = A.K[9 * (size_t)sBlk[w][j] + qq];
+        for (int st = 0; st < kRmwSteps; ++st) {
+            const int j = 3 * st + grp;
+            ov[st] = T(0);
+            if (A.K && grp < 3 && j < 64 && !((first >> j) & 1ull)) ov[st] = A.K[9 * (size_t)sBlk[w][j] + qq];
+        }
     }
-    // node b = lane & 7 coordinates
+    // node b = lane & 7 coordinates, in the section frame
     const int na = A.elist[8 * (size_t)e + b];
-    const float X0 = (float)A.nodes[3 * (size_t)(na - 1)], X1 = (float)A.nodes[3 * (size_t)(na - 1) + 1],
-                X2 = (float)A.nodes[3 * (size_t)(na - 1) + 2];
-    const float sa = (b == 1 || b == 2 || b == 5 || b == 6) ? 1.f : -1.f;
-    const float ta = (b == 2 || b == 3 || b == 6 || b == 7) ? 1.f : -1.f;
-    const float ua = (b >= 4) ? 1.f : -1.f;
-    const float g = 0.57735026918962576451f;
+    T X0 = (T)A.nodes[3 * (size_t)(na - 1)], X1 = (T)A.nodes[3 * (size_t)(na - 1) + 1],
+      X2 = (T)A.nodes[3 * (size_t)(na - 1) + 2];
+    T Or[3][3];
+    if (ROT) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Or[i][j] = (T)A.orient[9 * (size_t)e + 3 * j + i];
+        const T y0 = Or[0][0] * X0 + Or[0][1] * X1 + Or[0][2] * X2;
+        const T y1 = Or[1][0] * X0 + Or[1][1] * X1 + Or[1][2] * X2;
+        const T y2 = Or[2][0] * X0 + Or[2][1] * X1 + Or[2][2] * X2;
+        X0 = y0;
+        X1 = y1;
+        X2 = y2;
+    }
+    const T sa = (b == 1 || b == 2 || b == 5 || b == 6) ? T(1) : T(-1);
+    const T ta = (b == 2 || b == 3 || b == 6 || b == 7) ? T(1) : T(-1);
+    const T ua = (b >= 4) ? T(1) : T(-1);
+    const T g = (T)kRt3;
+    const T eighth = T(0.125);
 #pragma unroll
     for (int half = 0; half < 2; ++half) {
         const int gp = a0 + 4 * half;  // Gauss point of this 8-lane group
-        const float s1 = (gp & 1) ? g : -g, s2 = (gp & 2) ? g : -g, s3 = (gp & 4) ? g : -g;
-        const float n0 = 0.125f * sa * (1.f + ta * s2) * (1.f + ua * s3);
-        const float n1 = 0.125f * ta * (1.f + sa * s1) * (1.f + ua * s3);
-        const float n2 = 0.125f * ua * (1.f + sa * s1) * (1.f + ta * s2);
-        float J[9] = {X0 * n0, X0 * n1, X0 * n2, X1 * n0, X1 * n1, X1 * n2, X2 * n0, X2 * n1, X2 * n2};
+        const T s1 = (gp & 1) ? g : -g, s2 = (gp & 2) ? g : -g, s3 = (gp & 4) ? g : -g;
+        const T n0 = eighth * sa * (T(1) + ta * s2) * (T(1) + ua * s3);
+        const T n1 = eighth * ta * (T(1) + sa * s1) * (T(1) + ua * s3);
+        const T n2 = eighth * ua * (T(1) + sa * s1) * (T(1) + ta * s2);
+        T J[9] = {X0 * n0, X0 * n1, X0 * n2, X1 * n0, X1 * n1, X1 * n2, X2 * n0, X2 * n1, X2 * n2};
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             J[q] += __shfl_xor_sync(0xffffffffu, J[q], 1);
             J[q] += __shfl_xor_sync(0xffffffffu, J[q], 2);
             J[q] += __shfl_xor_sync(0xffffffffu, J[q], 4);
         }
-        const float a11 = J[4] * J[8] - J[5] * J[7], a12 = J[5] * J[6] - J[3] * J[8], a13 = J[3] * J[7] - J[4] * J[6];
-        const float dt = J[0] * a11 + J[1] * a12 + J[2] * a13, di = 1.f / dt;
-        const float I00 = di * a11, I10 = di * a12, I20 = di * a13;
-        const float I01 = di * (J[2] * J[7] - J[1] * J[8]), I11 = di * (J[0] * J[8] - J[2] * J[6]),
-                    I21 = di * (J[1] * J[6] - J[0] * J[7]);
-        const float I02 = di * (J[1] * J[5] - J[2] * J[4]), I12 = di * (J[2] * J[3] - J[0] * J[5]),
-                    I22 = di * (J[0] * J[4] - J[1] * J[3]);
-        sG[w][gp][b] = make_float4(n0 * I00 + n1 * I10 + n2 * I20, n0 * I01 + n1 * I11 + n2 * I21,
-                                   n0 * I02 + n1 * I12 + n2 * I22, 0.f);
+        const T a11 = J[4] * J[8] - J[5] * J[7], a12 = J[5] * J[6] - J[3] * J[8], a13 = J[3] * J[7] - J[4] * J[6];
+        const T dt = J[0] * a11 + J[1] * a12 + J[2] * a13, di = T(1) / dt;
+        const T I00 = di * a11, I10 = di * a12, I20 = di * a13;
+        const T I01 = di * (J[2] * J[7] - J[1] * J[8]), I11 = di * (J[0] * J[8] - J[2] * J[6]),
+                I21 = di * (J[1] * J[6] - J[0] * J[7]);
+        const T I02 = di * (J[1] * J[5] - J[2] * J[4]), I12 = di * (J[2] * J[3] - J[0] * J[5]),
+                I22 = di * (J[0] * J[4] - J[1] * J[3]);
+        sG[w][gp][b] = FastCfg<T>::make(n0 * I00 + n1 * I10 + n2 * I20, n0 * I01 + n1 * I11 + n2 * I21,
+                                        n0 * I02 + n1 * I12 + n2 * I22);
         if (b == 0) sDet[w][gp] = dt;
     }
     // material: closed-form orthotropic C (after the shuffles, so it is not live across them)
-    OrthoC c;
+    OrthoC<T> c;
     {
         const double *ep = A.elMat + 9 * (size_t)e;
-        const float E1 = (float)ep[0], E2 = (float)ep[1], E3 = (float)ep[2];
-        const float s11 = 1.f / E1, s22 = 1.f / E2, s33 = 1.f / E3;
-        const float s12 = -(float)ep[3] / E1, s13 = -(float)ep[4] / E1, s23 = -(float)ep[5] / E2;
-        const float c11c = s22 * s33 - s23 * s23, c12c = s13 * s23 - s12 * s33, c13c = s12 * s23 - s13 * s22;
-        const float det = s11 * c11c + s12 * c12c + s13 * c13c, id = 1.f / det;
+        const T E1 = (T)ep[0], E2 = (T)ep[1], E3 = (T)ep[2];
+        const T s11 = T(1) / E1, s22 = T(1) / E2, s33 = T(1) / E3;
+        const T s12 = -(T)ep[3] / E1, s13 = -(T)ep[4] / E1, s23 = -(T)ep[5] / E2;
+        const T c11c = s22 * s33 - s23 * s23, c12c = s13 * s23 - s12 * s33, c13c = s12 * s23 - s13 * s22;
+        const T det = s11 * c11c + s12 * c12c + s13 * c13c, id = T(1) / det;
         c.C11 = c11c * id;
         c.C12 = c12c * id;
         c.C13 = c13c * id;
         c.C22 = (s11 * s33 - s13 * s13) * id;
         c.C23 = (s13 * s12 - s11 * s23) * id;
         c.C33 = (s11 * s22 - s12 * s12) * id;
-        c.C44 = (float)ep[6];
-        c.C55 = (float)ep[7];
-        c.C66 = (float)ep[8];
+        c.C44 = (T)ep[6];
+        c.C55 = (T)ep[7];
+        c.C66 = (T)ep[8];
     }
     __syncwarp();
-    float M0[9] = {}, M1[9] = {};
+    T M0[9] = {}, M1[9] = {};
 #pragma unroll
     for (int gp = 0; gp < 8; ++gp) {
-        const float wd = sDet[w][gp];
-        const float4 hb = sG[w][gp][b], ga = sG[w][gp][a0], gc = sG[w][gp][a1];
-        const float h0 = hb.x * wd, h1 = hb.y * wd, h2 = hb.z * wd;
+        const T wd = sDet[w][gp];
+        const V4 hb = sG[w][gp][b], ga = sG[w][gp][a0], gc = sG[w][gp][a1];
+        const T h0 = hb.x * wd, h1 = hb.y * wd, h2 = hb.z * wd;
         M0[0] += ga.x * h0; M0[1] += ga.x * h1; M0[2] += ga.x * h2;
         M0[3] += ga.y * h0; M0[4] += ga.y * h1; M0[5] += ga.y * h2;
         M0[6] += ga.z * h0; M0[7] += ga.z * h1; M0[8] += ga.z * h2;
@@ -445,9 +498,13 @@ __global__ void __launch_bounds__(32 * kFW, 3) hex8_fast_kernel(Hex8FastArgs A) 
         M1[3] += gc.y * h0; M1[4] += gc.y * h1; M1[5] += gc.y * h2;
         M1[6] += gc.z * h0; M1[7] += gc.z * h1; M1[8] += gc.z * h2;
     }
-    float K0[9], K1[9];
-    ortho_block(c, M0, K0);
-    ortho_block(c, M1, K1);
+    T K0[9], K1[9];
+    ortho_block<T>(c, M0, K0);
+    ortho_block<T>(c, M1, K1);
+    if (ROT) {
+        rotate_block<T>(Or, K0);
+        rotate_block<T>(Or, K1);
+    }
     if (A.K) {
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
@@ -458,7 +515,15 @@ __global__ void __launch_bounds__(32 * kFW, 3) hex8_fast_kernel(Hex8FastArgs A) 
 #pragma unroll
         for (int st = 0; st < kRmwSteps; ++st) {
             const int j = 3 * st + grp;
-            if (grp < 3 && j < 64) A.K[9 * (size_t)sBlk[w][j] + qq] = ov[st] + sK[w][9 * j + qq];
+            if (grp < 3 && j < 64) {
+                T *dst = A.K + 9 * (size_t)sBlk[w][j] + qq;
+                T old;
+                if (PREFETCH)
+                    old = ov[PREFETCH ? st : 0];
+                else
+                    old = ((first >> j) & 1ull) ? T(0) : *dst;
+                *dst = old + sK[w][9 * j + qq];
+            }
         }
     }
     if (A.keOut) {
@@ -495,24 +560,38 @@ __global__ void k_hex_cim(int count, const int *__restrict__ els, const double *
 
 }  // namespace
 
-static int hex8_fast_run(astro_ctx *ctx, float *K, double *d_ke) {
+template <class T, bool ROT> static void hex8_fast_launch(astro_ctx *ctx, const Hex8FastArgs<T> &A0) {
     const AstroPrep &P = ctx->P;
-    Hex8FastArgs A;
-    A.nodes = dptr<double>(ctx->d_nodes);
-    A.elist = dptr<int>(ctx->d_elist);
-    A.elBlk = dptr<int>(ctx->d_elBlk);
-    A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
-    A.elMat = dptr<double>(ctx->d_elMat);
-    A.K = K;
-    A.keOut = d_ke;
+    constexpr int FW = FastCfg<T>::FW;
+    Hex8FastArgs<T> A = A0;
     for (int col = 0; col < P.ncolors; ++col) {
         const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
         if (!cnt) continue;
         A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
         A.count = cnt;
-        hex8_fast_kernel<<<(cnt + kFW - 1) / kFW, 32 * kFW, 0, ctx->stream>>>(A);
+        hex8_fast_kernel<T, ROT><<<(cnt + FW - 1) / FW, 32 * FW, 0, ctx->stream>>>(A);
     }
-    return cuda_check(ctx, cudaGetLastError(), "hex8 fast kernel launch");
+}
+
+// Zero-state stiffness of every element, colour by colour, into K (block-CSR, written without a
+// prior zeroing) and/or the element matrices d_ke.
+template <class T> static int hex8_fast_run(astro_ctx *ctx, T *K, double *d_ke) {
+    Hex8FastArgs<T> A;
+    A.nodes = dptr<double>(ctx->d_nodes);
+    A.elist = dptr<int>(ctx->d_elist);
+    A.colorEls = nullptr;
+    A.count = 0;
+    A.elBlk = dptr<int>(ctx->d_elBlk);
+    A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
+    A.elMat = dptr<double>(ctx->d_elMat);
+    A.orient = dptr<double>(ctx->d_secOrient);
+    A.K = K;
+    A.keOut = d_ke;
+    if (ctx->orientIdentity)
+        hex8_fast_launch<T, false>(ctx, A);
+    else
+        hex8_fast_launch<T, true>(ctx, A);
+    return cuda_check(ctx, cudaGetLastError(), "brick8 zero-state kernel launch");
 }
 
 // precision 64: general FP64 kernel (state, orientation); 32: FP32 kernel at zero state.
@@ -568,28 +647,26 @@ static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_di
 }
 
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
-    if (precision == 32) {
-        if (!ctx->orientIdentity)
-            return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 brick8 kernel needs identity section orientation");
-        return hex8_fast_run(ctx, (store & 1) ? dptr<float>(ctx->d_K32) : nullptr, nullptr);
-    }
-    return hex8_run(ctx, precision, store, nullptr, nullptr, nullptr, nullptr);
+    if (precision == 32) return hex8_fast_run<float>(ctx, (store & 1) ? dptr<float>(ctx->d_K32) : nullptr, nullptr);
+    return hex8_fast_run<double>(ctx, (store & 2) ? dptr<double>(ctx->d_K64) : nullptr, nullptr);
 }
 
+// getElasticSolnLoad for bricks.  From the undeformed state (no displacement) the residual is
+// zero and the tangent is the small-strain stiffness, which the zero-state kernel writes into the
+// block-CSR matrix without a prior zeroing; any other state takes the general kernel (Green-
+// Lagrange strain, stress stiffness, residual), which adds into a zeroed matrix.
 int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt) {
+    if (!d_disp) return buildMat ? hex8_fast_run<double>(ctx, dptr<double>(ctx->d_K64), nullptr) : ASTRO_OK;
     return hex8_run(ctx, 64, buildMat ? 2 : 0, d_disp, d_loadInt, nullptr, nullptr);
 }
 
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
-    if (precision == 32) {
-        if (!ctx->orientIdentity)
-            return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 brick8 kernel needs identity section orientation");
-        return hex8_fast_run(ctx, nullptr, d_ke);
-    }
-    return hex8_run(ctx, precision, 0, nullptr, nullptr, d_ke, nullptr);
+    if (precision == 32) return hex8_fast_run<float>(ctx, nullptr, d_ke);
+    return hex8_fast_run<double>(ctx, nullptr, d_ke);
 }
 
 int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru) {
+    if (!d_disp && !d_ru) return hex8_fast_run<double>(ctx, nullptr, d_ke);
     return hex8_run(ctx, 64, 0, d_disp, nullptr, d_ke, d_ru);
 }
 
