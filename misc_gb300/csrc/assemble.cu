@@ -20,7 +20,7 @@ __global__ void export_csr_kernel(const double *__restrict__ K, const int *__res
     const int ra = bRow[k], rb = bCol[k];
     const int dofRow = ra + 1 + i * N;  // 1-based reference DOF
     const long long idx = (long long)elMatRange[dofRow - 1] + csrPos[(long long)k * dpn + j];
-    mat[idx] = K[t];
+    if (mat) mat[idx] = K[t];
     if (cols) cols[idx] = rb + 1 + j * N;
 }
 
@@ -113,28 +113,15 @@ int bsr_zero(astro_ctx *ctx, int which) {
     return ASTRO_OK;
 }
 
-int export_csr(astro_ctx *ctx, double *elastic_mat, int32_t *el_mat_cols) {
+// The reference CSR (values in d_mat and/or column numbers in d_cols, device buffers of
+// elMatSize) from the block-CSR matrix, on stream s.  The column numbers depend on the mesh only.
+int export_csr_dev(astro_ctx *ctx, cudaStream_t s, double *d_mat, int *d_cols) {
     const AstroPrep &P = ctx->P;
-    DevBuf dm, dc;
-    int rc = dev_alloc(ctx, dm, sizeof(double) * (size_t)P.elMatSize);
-    if (rc) return rc;
-    if (el_mat_cols && (rc = dev_alloc(ctx, dc, sizeof(int) * (size_t)P.elMatSize))) {
-        dev_free(dm);
-        return rc;
-    }
     const long long total = (long long)P.nb * P.dpn * P.dpn;
-    export_csr_kernel<<<(unsigned)((total + 255) / 256), 256, 0, ctx->stream>>>(
+    export_csr_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
         dptr<double>(ctx->d_K64), dptr<int>(ctx->d_bRow), dptr<int>(ctx->d_bCol), dptr<int>(ctx->d_csrPos),
-        dptr<int>(ctx->d_elMatRangeRank), P.nb, P.dpn, P.N, dptr<double>(dm), el_mat_cols ? dptr<int>(dc) : nullptr);
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(elastic_mat, dm.p, sizeof(double) * (size_t)P.elMatSize, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess && el_mat_cols)
-        e = cudaMemcpyAsync(el_mat_cols, dc.p, sizeof(int) * (size_t)P.elMatSize, cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    dev_free(dm);
-    dev_free(dc);
-    return e == cudaSuccess ? ASTRO_OK : cuda_check(ctx, e, "export_csr");
+        dptr<int>(ctx->d_elMatRangeRank), P.nb, P.dpn, P.N, d_mat, d_cols);
+    return cuda_check(ctx, cudaGetLastError(), "export_csr");
 }
 
 double bsr_absmax(astro_ctx *ctx, int *status) {

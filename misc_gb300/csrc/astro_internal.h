@@ -63,6 +63,7 @@ struct AstroPrep {
 struct astro_ctx {
     std::string err;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // copies that overlap the element kernels
     int device = 0;
     AstroPrep P;
     // host model copy
@@ -77,6 +78,7 @@ struct astro_ctx {
     int orientIdentity = 1;
     // device model
     DevBuf d_nodes, d_elist, d_elMat, d_esec, d_secABD, d_secOrient, d_colorEls, d_elBlk;
+    DevBuf d_elC;           // per brick element the orthotropic C (C11 C12 C13 C22 C23 C33 C44 C55 C66)
     DevBuf d_rank;          // currentRank (N) 1-based
     DevBuf d_bRowPtr, d_bCol, d_bRow, d_etype, d_elFirst;
     DevBuf d_K64, d_K32;    // BSR values
@@ -101,6 +103,9 @@ struct astro_ctx {
     std::vector<int> e2dRange, e2d, dCat, dComp, dLayer;
     std::vector<double> e2c, dVal;
     DevBuf d_shLayRange, d_shLay, d_shZoff, d_e2dR, d_e2d, d_e2c, d_dCat, d_dLayer, d_dVal;
+    // persistent buffers of the getElasticSolnLoad boundary: load vector in both numberings,
+    // exported CSR values and column numbers
+    DevBuf d_ioRef, d_ioInt, d_exMat, d_exCols;
     // scratch
     DevBuf d_scratch;
     DevBuf d_status;  // int status words written by kernels
@@ -125,6 +130,7 @@ int astro_prep_build(astro_ctx *c, const astro_model *m);
 
 // kernels' host entry points
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store);           // elem_hex8.cu
+int hex8_prepare(astro_ctx *ctx);  // per-element material stiffness, once per context (elem_hex8.cu)
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *ke_host); // elem_hex8.cu
 // device state of a shell evaluation (internal layout; any pointer may be null = zeros)
 struct ShellDevState {
@@ -137,7 +143,7 @@ int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &s, double *d_loa
                            int buildMat, double *d_ke, double *d_ru);  // elem_shell4.cu
 int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // elem_shell4.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu
-int export_csr(astro_ctx *ctx, double *elastic_mat, int32_t *el_mat_cols);  // assemble.cu
+int export_csr_dev(astro_ctx *ctx, cudaStream_t s, double *d_mat, int *d_cols);  // assemble.cu
 double bsr_absmax(astro_ctx *ctx, int *status);                             // assemble.cu
 int ref_to_int_vec(astro_ctx *ctx, const double *d_ref, double *d_int, int n); // assemble.cu
 int int_to_ref_vec(astro_ctx *ctx, const double *d_int, double *d_ref, int n); // assemble.cu

@@ -63,7 +63,8 @@ static void free_all(astro_ctx *c) {
                       &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
-                      &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal};
+                      &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_ioRef,
+                      &c->d_ioInt, &c->d_exMat, &c->d_exCols};
     for (DevBuf *b : bufs) dev_free(*b);
 }
 
@@ -123,6 +124,7 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
         set_err(nullptr, code, msg);
         free_all(ctx);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
+        if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
         delete ctx;
         return code;
     };
@@ -206,6 +208,7 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
     if ((rc = dev_alloc(ctx, ctx->d_status, 256))) return fail(rc, ctx->err);
     cudaMemset(ctx->d_status.p, 0, 256);
     if (ctx->hasShell && (rc = shell_sections_prepare(ctx, m))) return fail(rc, ctx->err);
+    if (ctx->hasSolid && (rc = hex8_prepare(ctx))) return fail(rc, ctx->err);
     // unscaled constraints in internal numbering
     ctx->mpcScaledHost = P.mpcMat;
     ctx->mpcRhsScaledHost = P.mpcRhs;
@@ -218,6 +221,10 @@ extern "C" int astro_ctx_destroy(astro_ctx *ctx) {
     cudaStreamSynchronize(ctx->stream);
     free_all(ctx);
     cudaStreamDestroy(ctx->stream);
+    if (ctx->stream2) {
+        cudaStreamSynchronize(ctx->stream2);
+        cudaStreamDestroy(ctx->stream2);
+    }
     delete ctx;
     return ASTRO_OK;
 }
@@ -316,13 +323,34 @@ static int shell_state(astro_ctx *ctx, const astro_state *state, DevState &S, Sh
     return ASTRO_OK;
 }
 
+// Persistent device buffers of the getElasticSolnLoad boundary, allocated on first use.
+static int ensure_io(astro_ctx *ctx, bool exportMat) {
+    const AstroPrep &P = ctx->P;
+    int rc;
+    if (!ctx->d_ioRef.p && (rc = dev_alloc(ctx, ctx->d_ioRef, sizeof(double) * P.n))) return rc;
+    if (!ctx->d_ioInt.p && (rc = dev_alloc(ctx, ctx->d_ioInt, sizeof(double) * P.n))) return rc;
+    if (exportMat) {
+        if (!ctx->d_exMat.p && (rc = dev_alloc(ctx, ctx->d_exMat, sizeof(double) * (size_t)P.elMatSize))) return rc;
+        if (!ctx->d_exCols.p && (rc = dev_alloc(ctx, ctx->d_exCols, sizeof(int) * (size_t)P.elMatSize))) return rc;
+    }
+    if (!ctx->stream2) CK(cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking));
+    return ASTRO_OK;
+}
+
+// getElasticSolnLoad (Working/AStrO_commandFunctions.f90:260-351).  The reference CSR column
+// numbers depend on the mesh only, so they are formed on a second stream and copied to the host
+// while the element kernels run; the values follow the last colour.
 extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro_state *state, double *elastic_load,
                                   double *int_elastic_load, double *elastic_mat, int32_t *el_mat_cols,
                                   double *int_elastic_mat) {
     if (!ctx || !elastic_load) return ASTRO_ERR_ARG;
+    if (state && state->dynamic && ctx->hasSolid)
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
     const AstroPrep &P = ctx->P;
     const int n = P.n;
+    const bool exportMat = build_mat == 1 && (elastic_mat || el_mat_cols);
     int rc;
+    if ((rc = ensure_io(ctx, exportMat))) return rc;
     DevState S;
     if (state) {
         if ((rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
@@ -332,17 +360,18 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
             if ((rc = state_vec_up(ctx, state->prev_acc, S.pacc))) return rc;
         }
     }
-    DevBuf dl;
-    if ((rc = state_vec_up(ctx, elastic_load, dl, false))) return rc;
+    if (exportMat && el_mat_cols && (rc = export_csr_dev(ctx, ctx->stream2, nullptr, dptr<int>(ctx->d_exCols))))
+        return rc;
+    double *dRef = dptr<double>(ctx->d_ioRef), *dl = dptr<double>(ctx->d_ioInt);
+    CK(cudaMemcpyAsync(dRef, elastic_load, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = ref_to_int_vec(ctx, dRef, dl, n))) return rc;
     if (build_mat == 1) {
         if ((rc = ensure_K(ctx, 2))) return rc;
         // the brick zero-state kernel writes every block (first touch), the other paths add
         if (!(ctx->hasSolid && !S.disp.p) && (rc = bsr_zero(ctx, 2))) return rc;
     }
-    if (state && state->dynamic && ctx->hasSolid)
-        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
     if (ctx->hasSolid) {
-        rc = hex8_soln_load(ctx, build_mat == 1, S.disp.p ? dptr<double>(S.disp) : nullptr, dptr<double>(dl));
+        rc = hex8_soln_load(ctx, build_mat == 1, S.disp.p ? dptr<double>(S.disp) : nullptr, dl);
     } else {
         DevBuf il;
         if (int_elastic_load && P.intVecSize) {
@@ -350,35 +379,38 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
         }
         ShellDevState ds;
         if ((rc = shell_state(ctx, state, S, ds))) return rc;
-        rc = launch_shell4_assemble(ctx, ds, dptr<double>(dl), il.p ? dptr<double>(il) : nullptr, build_mat == 1,
-                                    nullptr, nullptr);
+        rc = launch_shell4_assemble(ctx, ds, dl, il.p ? dptr<double>(il) : nullptr, build_mat == 1, nullptr, nullptr);
         if (!rc && il.p)
             rc = cuda_check(ctx, cudaMemcpy(int_elastic_load, il.p, sizeof(double) * P.intVecSize, cudaMemcpyDeviceToHost),
                             "int load download");
         dev_free(il);
     }
     if (rc) {
-        dev_free(dl);
+        cudaStreamSynchronize(ctx->stream2);
         return rc;
     }
+    // a copy into pageable host memory returns when it is done, so it is issued after the element
+    // kernels have been launched and runs while they execute
+    if (exportMat && el_mat_cols)
+        CK(cudaMemcpyAsync(el_mat_cols, ctx->d_exCols.p, sizeof(int) * (size_t)P.elMatSize, cudaMemcpyDeviceToHost,
+                           ctx->stream2));
     if (build_mat == 1) {
         ctx->haveK64 = 1;
         ctx->k64Version++;
     }
     // load back to reference numbering
-    DevBuf dref;
-    if ((rc = dev_alloc(ctx, dref, sizeof(double) * n))) return rc;
-    if ((rc = int_to_ref_vec(ctx, dptr<double>(dl), dptr<double>(dref), n))) return rc;
-    CK(cudaMemcpyAsync(elastic_load, dref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = int_to_ref_vec(ctx, dl, dRef, n))) return rc;
+    CK(cudaMemcpyAsync(elastic_load, dRef, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (exportMat && elastic_mat) {
+        if ((rc = export_csr_dev(ctx, ctx->stream, dptr<double>(ctx->d_exMat), nullptr))) return rc;
+        CK(cudaMemcpyAsync(elastic_mat, ctx->d_exMat.p, sizeof(double) * (size_t)P.elMatSize, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    }
+    if (build_mat == 1 && int_elastic_mat && P.intMatSize && ctx->d_intMat.p)
+        CK(cudaMemcpyAsync(int_elastic_mat, ctx->d_intMat.p, sizeof(double) * P.intMatSize, cudaMemcpyDeviceToHost,
+                           ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    dev_free(dref);
-    dev_free(dl);
-    if (build_mat == 1 && elastic_mat) {
-        if ((rc = export_csr(ctx, elastic_mat, el_mat_cols))) return rc;
-    }
-    if (build_mat == 1 && int_elastic_mat && P.intMatSize && ctx->d_intMat.p) {
-        CK(cudaMemcpy(int_elastic_mat, ctx->d_intMat.p, sizeof(double) * P.intMatSize, cudaMemcpyDeviceToHost));
-    }
+    CK(cudaStreamSynchronize(ctx->stream2));
     ctx->mpcScaled = 0;
     ctx->haveLT = 0;
     ctx->ltFactored = 0;

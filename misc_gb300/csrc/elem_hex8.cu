@@ -310,18 +310,22 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
 // Zero-state brick8 stiffness and assembly: FP32 for the mixed-precision solver's matrix, FP64
 // for getElasticSolnLoad from the undeformed state (where the residual is exactly zero and the
 // tangent is the small-strain stiffness).  Per element (one warp):
-//   * C from the orthotropic engineering constants in closed form (3x3 normal block inverse,
-//     shear moduli on the diagonal), the same matrix r_getMaterialStiffness forms by LU;
+//   * the orthotropic C of the element, computed once per context by the reference's LU
+//     (r_getMaterialStiffness);
 //   * the node coordinates in the section frame (orient X, as r_getElementData stages them);
-//   * the eight Gauss-point Jacobians in two rounds: lane (g, a) with g = lane/8 (+4), a = lane%8
-//     forms node a's contribution to J at point g and the eight lanes of a point reduce it with
-//     three xor-shuffles, then invert it and write the gradient g_a to shared memory;
+//   * the eight Gauss-point Jacobians in one round: lane (g, s) with g = lane/4, s = lane%4 forms
+//     the contribution of nodes 2s and 2s+1 to J at point g, the four lanes of a point reduce it
+//     with two xor-shuffles, invert it, and write the gradients g_a and w detJ g_a of their two
+//     nodes to shared memory;
 //   * lane l owns the node pairs (l/8, l%8) and (l/8+4, l%8).  For a pair (a, b) the 3x3
-//     moment M = sum_gp w detJ g_a g_b^T is accumulated (9 FMA per point), and the block follows
-//     from the orthotropic C in one contraction (21 products):
+//     moment M = sum_gp w detJ g_a g_b^T is accumulated (9 products per point), and the block
+//     follows from the orthotropic C in one contraction (21 products):
 //       K00 = C11 M00 + C44 M11 + C55 M22,  K01 = C12 M01 + C44 M10,  K02 = C13 M02 + C55 M20, ...
 //     which is the sparse B^T C B of the element summed over the points, reassociated; a rotated
-//     section frame maps the block back with orient^T K orient;
+//     section frame maps the block back with orient^T K orient.  GB300 issues FP64 at 1/64 of
+//     its FP32 rate, so in the FP64 kernel the moments, which are most of the arithmetic, are
+//     accumulated in double-float (pairs of floats with error-free products and sums, about 48
+//     significant bits) and only the Jacobians and the final contraction run in FP64;
 //   * the 64 blocks go through shared memory and are added into the block-CSR matrix three whole
 //     blocks (27 lanes, 9 contiguous values each) per warp instruction, instead of one lane per
 //     block touching a different cache line for every value; the first element (in colour order)
@@ -330,21 +334,35 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
 //     better spent on occupancy).
 constexpr int kRmwSteps = 22;  // ceil(64 blocks / 3 blocks per step)
 
-struct __align__(32) Dbl4 {
-    double x, y, z, w;
+// double-float: x = hi + lo with |lo| <= ulp(hi)/2
+struct DF {
+    float hi, lo;
 };
+__device__ __forceinline__ DF df_split(double x) {
+    const float h = __double2float_rn(x);
+    return DF{h, __double2float_rn(x - (double)h)};
+}
+// s += a b (error-free product of the high parts, first-order cross terms, two-sum into s)
+__device__ __forceinline__ void df_fma(DF &s, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float t = __fadd_rn(s.hi, p);
+    const float v = __fsub_rn(t, s.hi);
+    const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, v)), __fsub_rn(p, v));
+    s.lo = __fadd_rn(s.lo, __fadd_rn(err, e));
+    s.hi = t;
+}
+
 template <class T> struct FastCfg;
 template <> struct FastCfg<float> {
-    using V4 = float4;
     static constexpr int FW = 8, MINB = 3;  // warps per CTA, CTAs per SM
     static constexpr bool PREFETCH = true;
-    static __device__ __forceinline__ float4 make(float x, float y, float z) { return make_float4(x, y, z, 0.f); }
 };
 template <> struct FastCfg<double> {
-    using V4 = Dbl4;
-    static constexpr int FW = 4, MINB = 4;
+    static constexpr int FW = 4, MINB = 3;
     static constexpr bool PREFETCH = false;
-    static __device__ __forceinline__ Dbl4 make(double x, double y, double z) { return Dbl4{x, y, z, 0.0}; }
 };
 
 template <class T> struct Hex8FastArgs {
@@ -354,7 +372,7 @@ template <class T> struct Hex8FastArgs {
     int count;
     const int *elBlk;
     const unsigned long long *elFirst;
-    const double *elMat;
+    const double *elC;     // (E,9) orthotropic C
     const double *orient;  // (E,9) column-major section orientation (used when ROT)
     T *K;                  // BSR values or null
     double *keOut;         // element matrices (E,24,24) column-major, element DOF order, or null
@@ -389,20 +407,81 @@ template <class T> __device__ __forceinline__ void rotate_block(const T Or[3][3]
         for (int j = 0; j < 3; ++j) K[3 * i + j] = Or[0][i] * W[0][j] + Or[1][i] * W[1][j] + Or[2][i] * W[2][j];
 }
 
+// per-warp shared staging of the Gauss-point gradients: g_a and h_a = w detJ g_a
+template <class T> struct GradSmem;
+template <> struct GradSmem<float> {
+    float4 g[8][8], h[8][8];  // [gauss point][node]
+    __device__ void put(int gp, int a, float gx, float gy, float gz, float d) {
+        g[gp][a] = make_float4(gx, gy, gz, 0.f);
+        h[gp][a] = make_float4(d * gx, d * gy, d * gz, 0.f);
+    }
+};
+template <> struct GradSmem<double> {
+    float4 gh[8][8], gl[8][8], hh[8][8], hl[8][8];  // double-float parts
+    __device__ void put(int gp, int a, double gx, double gy, double gz, double d) {
+        const DF x = df_split(gx), y = df_split(gy), z = df_split(gz);
+        const DF u = df_split(d * gx), v = df_split(d * gy), w = df_split(d * gz);
+        gh[gp][a] = make_float4(x.hi, y.hi, z.hi, 0.f);
+        gl[gp][a] = make_float4(x.lo, y.lo, z.lo, 0.f);
+        hh[gp][a] = make_float4(u.hi, v.hi, w.hi, 0.f);
+        hl[gp][a] = make_float4(u.lo, v.lo, w.lo, 0.f);
+    }
+};
+
+// 3x3 moments of the pairs (a0, b) and (a1, b): M = sum_gp g_a h_b^T
+__device__ __forceinline__ void pair_moments(const GradSmem<float> &S, int a0, int a1, int b, float M0[9],
+                                             float M1[9]) {
+#pragma unroll
+    for (int q = 0; q < 9; ++q) M0[q] = M1[q] = 0.f;
+#pragma unroll
+    for (int gp = 0; gp < 8; ++gp) {
+        const float4 hb = S.h[gp][b], ga = S.g[gp][a0], gc = S.g[gp][a1];
+        M0[0] += ga.x * hb.x; M0[1] += ga.x * hb.y; M0[2] += ga.x * hb.z;
+        M0[3] += ga.y * hb.x; M0[4] += ga.y * hb.y; M0[5] += ga.y * hb.z;
+        M0[6] += ga.z * hb.x; M0[7] += ga.z * hb.y; M0[8] += ga.z * hb.z;
+        M1[0] += gc.x * hb.x; M1[1] += gc.x * hb.y; M1[2] += gc.x * hb.z;
+        M1[3] += gc.y * hb.x; M1[4] += gc.y * hb.y; M1[5] += gc.y * hb.z;
+        M1[6] += gc.z * hb.x; M1[7] += gc.z * hb.y; M1[8] += gc.z * hb.z;
+    }
+}
+__device__ __forceinline__ void pair_moments(const GradSmem<double> &S, int a0, int a1, int b, double M0[9],
+                                             double M1[9]) {
+    DF m0[9], m1[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) m0[q] = m1[q] = DF{0.f, 0.f};
+#pragma unroll
+    for (int gp = 0; gp < 8; ++gp) {
+        const float4 hh = S.hh[gp][b], hl = S.hl[gp][b];
+        const float4 ah = S.gh[gp][a0], al = S.gl[gp][a0], ch = S.gh[gp][a1], cl = S.gl[gp][a1];
+        const float gah[3] = {ah.x, ah.y, ah.z}, gal[3] = {al.x, al.y, al.z};
+        const float gch[3] = {ch.x, ch.y, ch.z}, gcl[3] = {cl.x, cl.y, cl.z};
+        const float hbh[3] = {hh.x, hh.y, hh.z}, hbl[3] = {hl.x, hl.y, hl.z};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                df_fma(m0[3 * i + j], gah[i], gal[i], hbh[j], hbl[j]);
+                df_fma(m1[3 * i + j], gch[i], gcl[i], hbh[j], hbl[j]);
+            }
+    }
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        M0[q] = (double)m0[q].hi + (double)m0[q].lo;
+        M1[q] = (double)m1[q].hi + (double)m1[q].lo;
+    }
+}
+
 template <class T, bool ROT>
 __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fast_kernel(Hex8FastArgs<T> A) {
     constexpr int FW = FastCfg<T>::FW;
     constexpr bool PREFETCH = FastCfg<T>::PREFETCH;
-    using V4 = typename FastCfg<T>::V4;
-    __shared__ V4 sG[FW][8][8];  // [warp][gauss point][node]: gradient of N_a, w = 0
-    __shared__ T sDet[FW][8];
+    __shared__ GradSmem<T> sG[FW];
     __shared__ T sK[FW][64 * 9];  // element blocks, block j = 8a + b at 9j (row-major 3x3)
     __shared__ int sBlk[FW][64];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int item = blockIdx.x * FW + w;
     if (item >= A.count) return;
     const int e = A.colorEls[item];
-    const int a0 = lane >> 3, a1 = a0 + 4, b = lane & 7;
     // block targets; in the cooperative phase lane = 9 grp + qq handles entry qq of block 3 st + grp
     sBlk[w][lane] = A.elBlk[64 * (size_t)e + lane];
     sBlk[w][lane + 32] = A.elBlk[64 * (size_t)e + lane + 32];
@@ -418,41 +497,49 @@ __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fa
             if (A.K && grp < 3 && j < 64 && !((first >> j) & 1ull)) ov[st] = A.K[9 * (size_t)sBlk[w][j] + qq];
         }
     }
-    // node b = lane & 7 coordinates, in the section frame
-    const int na = A.elist[8 * (size_t)e + b];
-    T X0 = (T)A.nodes[3 * (size_t)(na - 1)], X1 = (T)A.nodes[3 * (size_t)(na - 1) + 1],
-      X2 = (T)A.nodes[3 * (size_t)(na - 1) + 2];
-    T Or[3][3];
-    if (ROT) {
+    // Jacobian at Gauss point gp = lane/4 from nodes 2s, 2s+1 (s = lane%4), in the section frame
+    {
+        const int gp = lane >> 2, s = lane & 3;
+        T Or[3][3];
+        if (ROT) {
 #pragma unroll
-        for (int i = 0; i < 3; ++i)
+            for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) Or[i][j] = (T)A.orient[9 * (size_t)e + 3 * j + i];
-        const T y0 = Or[0][0] * X0 + Or[0][1] * X1 + Or[0][2] * X2;
-        const T y1 = Or[1][0] * X0 + Or[1][1] * X1 + Or[1][2] * X2;
-        const T y2 = Or[2][0] * X0 + Or[2][1] * X1 + Or[2][2] * X2;
-        X0 = y0;
-        X1 = y1;
-        X2 = y2;
-    }
-    const T sa = (b == 1 || b == 2 || b == 5 || b == 6) ? T(1) : T(-1);
-    const T ta = (b == 2 || b == 3 || b == 6 || b == 7) ? T(1) : T(-1);
-    const T ua = (b >= 4) ? T(1) : T(-1);
-    const T g = (T)kRt3;
-    const T eighth = T(0.125);
+                for (int j = 0; j < 3; ++j) Or[i][j] = (T)A.orient[9 * (size_t)e + 3 * j + i];
+        }
+        const T gq = (T)kRt3, eighth = T(0.125);
+        const T s1 = (gp & 1) ? gq : -gq, s2 = (gp & 2) ? gq : -gq, s3 = (gp & 4) ? gq : -gq;
+        T J[9], n[2][3];
 #pragma unroll
-    for (int half = 0; half < 2; ++half) {
-        const int gp = a0 + 4 * half;  // Gauss point of this 8-lane group
-        const T s1 = (gp & 1) ? g : -g, s2 = (gp & 2) ? g : -g, s3 = (gp & 4) ? g : -g;
-        const T n0 = eighth * sa * (T(1) + ta * s2) * (T(1) + ua * s3);
-        const T n1 = eighth * ta * (T(1) + sa * s1) * (T(1) + ua * s3);
-        const T n2 = eighth * ua * (T(1) + sa * s1) * (T(1) + ta * s2);
-        T J[9] = {X0 * n0, X0 * n1, X0 * n2, X1 * n0, X1 * n1, X1 * n2, X2 * n0, X2 * n1, X2 * n2};
+        for (int q = 0; q < 9; ++q) J[q] = T(0);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int a = 2 * s + k;
+            const int na = A.elist[8 * (size_t)e + a];
+            T X0 = (T)A.nodes[3 * (size_t)(na - 1)], X1 = (T)A.nodes[3 * (size_t)(na - 1) + 1],
+              X2 = (T)A.nodes[3 * (size_t)(na - 1) + 2];
+            if (ROT) {
+                const T y0 = Or[0][0] * X0 + Or[0][1] * X1 + Or[0][2] * X2;
+                const T y1 = Or[1][0] * X0 + Or[1][1] * X1 + Or[1][2] * X2;
+                const T y2 = Or[2][0] * X0 + Or[2][1] * X1 + Or[2][2] * X2;
+                X0 = y0;
+                X1 = y1;
+                X2 = y2;
+            }
+            const T sa = (a == 1 || a == 2 || a == 5 || a == 6) ? T(1) : T(-1);
+            const T ta = (a == 2 || a == 3 || a == 6 || a == 7) ? T(1) : T(-1);
+            const T ua = (a >= 4) ? T(1) : T(-1);
+            n[k][0] = eighth * sa * (T(1) + ta * s2) * (T(1) + ua * s3);
+            n[k][1] = eighth * ta * (T(1) + sa * s1) * (T(1) + ua * s3);
+            n[k][2] = eighth * ua * (T(1) + sa * s1) * (T(1) + ta * s2);
+            J[0] += X0 * n[k][0]; J[1] += X0 * n[k][1]; J[2] += X0 * n[k][2];
+            J[3] += X1 * n[k][0]; J[4] += X1 * n[k][1]; J[5] += X1 * n[k][2];
+            J[6] += X2 * n[k][0]; J[7] += X2 * n[k][1]; J[8] += X2 * n[k][2];
+        }
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             J[q] += __shfl_xor_sync(0xffffffffu, J[q], 1);
             J[q] += __shfl_xor_sync(0xffffffffu, J[q], 2);
-            J[q] += __shfl_xor_sync(0xffffffffu, J[q], 4);
         }
         const T a11 = J[4] * J[8] - J[5] * J[7], a12 = J[5] * J[6] - J[3] * J[8], a13 = J[3] * J[7] - J[4] * J[6];
         const T dt = J[0] * a11 + J[1] * a12 + J[2] * a13, di = T(1) / dt;
@@ -461,47 +548,38 @@ __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fa
                 I21 = di * (J[1] * J[6] - J[0] * J[7]);
         const T I02 = di * (J[1] * J[5] - J[2] * J[4]), I12 = di * (J[2] * J[3] - J[0] * J[5]),
                 I22 = di * (J[0] * J[4] - J[1] * J[3]);
-        sG[w][gp][b] = FastCfg<T>::make(n0 * I00 + n1 * I10 + n2 * I20, n0 * I01 + n1 * I11 + n2 * I21,
-                                        n0 * I02 + n1 * I12 + n2 * I22);
-        if (b == 0) sDet[w][gp] = dt;
-    }
-    // material: closed-form orthotropic C (after the shuffles, so it is not live across them)
-    OrthoC<T> c;
-    {
-        const double *ep = A.elMat + 9 * (size_t)e;
-        const T E1 = (T)ep[0], E2 = (T)ep[1], E3 = (T)ep[2];
-        const T s11 = T(1) / E1, s22 = T(1) / E2, s33 = T(1) / E3;
-        const T s12 = -(T)ep[3] / E1, s13 = -(T)ep[4] / E1, s23 = -(T)ep[5] / E2;
-        const T c11c = s22 * s33 - s23 * s23, c12c = s13 * s23 - s12 * s33, c13c = s12 * s23 - s13 * s22;
-        const T det = s11 * c11c + s12 * c12c + s13 * c13c, id = T(1) / det;
-        c.C11 = c11c * id;
-        c.C12 = c12c * id;
-        c.C13 = c13c * id;
-        c.C22 = (s11 * s33 - s13 * s13) * id;
-        c.C23 = (s13 * s12 - s11 * s23) * id;
-        c.C33 = (s11 * s22 - s12 * s12) * id;
-        c.C44 = (T)ep[6];
-        c.C55 = (T)ep[7];
-        c.C66 = (T)ep[8];
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+            sG[w].put(gp, 2 * s + k, n[k][0] * I00 + n[k][1] * I10 + n[k][2] * I20,
+                      n[k][0] * I01 + n[k][1] * I11 + n[k][2] * I21, n[k][0] * I02 + n[k][1] * I12 + n[k][2] * I22,
+                      dt);
     }
     __syncwarp();
-    T M0[9] = {}, M1[9] = {};
-#pragma unroll
-    for (int gp = 0; gp < 8; ++gp) {
-        const T wd = sDet[w][gp];
-        const V4 hb = sG[w][gp][b], ga = sG[w][gp][a0], gc = sG[w][gp][a1];
-        const T h0 = hb.x * wd, h1 = hb.y * wd, h2 = hb.z * wd;
-        M0[0] += ga.x * h0; M0[1] += ga.x * h1; M0[2] += ga.x * h2;
-        M0[3] += ga.y * h0; M0[4] += ga.y * h1; M0[5] += ga.y * h2;
-        M0[6] += ga.z * h0; M0[7] += ga.z * h1; M0[8] += ga.z * h2;
-        M1[0] += gc.x * h0; M1[1] += gc.x * h1; M1[2] += gc.x * h2;
-        M1[3] += gc.y * h0; M1[4] += gc.y * h1; M1[5] += gc.y * h2;
-        M1[6] += gc.z * h0; M1[7] += gc.z * h1; M1[8] += gc.z * h2;
+    const int a0 = lane >> 3, a1 = a0 + 4, b = lane & 7;
+    T M0[9], M1[9];
+    pair_moments(sG[w], a0, a1, b, M0, M1);
+    OrthoC<T> c;
+    {
+        const double *cp = A.elC + 9 * (size_t)e;
+        c.C11 = (T)cp[0];
+        c.C12 = (T)cp[1];
+        c.C13 = (T)cp[2];
+        c.C22 = (T)cp[3];
+        c.C23 = (T)cp[4];
+        c.C33 = (T)cp[5];
+        c.C44 = (T)cp[6];
+        c.C55 = (T)cp[7];
+        c.C66 = (T)cp[8];
     }
     T K0[9], K1[9];
     ortho_block<T>(c, M0, K0);
     ortho_block<T>(c, M1, K1);
     if (ROT) {
+        T Or[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Or[i][j] = (T)A.orient[9 * (size_t)e + 3 * j + i];
         rotate_block<T>(Or, K0);
         rotate_block<T>(Or, K1);
     }
@@ -534,6 +612,25 @@ __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fa
                 ke[(size_t)(8 * j + b) * 24 + (8 * i + a1)] = (double)K1[3 * i + j];
             }
     }
+}
+
+// Orthotropic C of every brick element by the reference's LU (r_getMaterialStiffness): the
+// normal 3x3 block and the shear diagonal of C = S^-1.
+__global__ void k_elem_c(int E, const double *__restrict__ elMat, double *__restrict__ elC) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double C[6][6];
+    material_c<double>(elMat + 9 * (size_t)e, C);
+    double *o = elC + 9 * (size_t)e;
+    o[0] = C[0][0];
+    o[1] = C[0][1];
+    o[2] = C[0][2];
+    o[3] = C[1][1];
+    o[4] = C[1][2];
+    o[5] = C[2][2];
+    o[6] = C[3][3];
+    o[7] = C[4][4];
+    o[8] = C[5][5];
 }
 
 // Imaginary part of the complex-step material stiffness of each listed element:
@@ -583,7 +680,7 @@ template <class T> static int hex8_fast_run(astro_ctx *ctx, T *K, double *d_ke) 
     A.count = 0;
     A.elBlk = dptr<int>(ctx->d_elBlk);
     A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
-    A.elMat = dptr<double>(ctx->d_elMat);
+    A.elC = dptr<double>(ctx->d_elC);
     A.orient = dptr<double>(ctx->d_secOrient);
     A.K = K;
     A.keOut = d_ke;
@@ -644,6 +741,16 @@ static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_di
         }
     }
     return cuda_check(ctx, cudaGetLastError(), "hex8 kernel launch");
+}
+
+int hex8_prepare(astro_ctx *ctx) {
+    const int E = ctx->P.E;
+    int rc;
+    if ((rc = dev_alloc(ctx, ctx->d_elC, sizeof(double) * 9 * (size_t)E))) return rc;
+    k_elem_c<<<(E + 127) / 128, 128, 0, ctx->stream>>>(E, dptr<double>(ctx->d_elMat), dptr<double>(ctx->d_elC));
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    return cuda_check(ctx, e, "brick8 material stiffness");
 }
 
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
