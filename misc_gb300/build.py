@@ -33,7 +33,8 @@ def _deps_newer(obj, src):
     if not os.path.exists(obj):
         return True
     t = os.path.getmtime(obj)
-    hdrs = glob.glob(os.path.join(CSRC, "*.h")) + [os.path.join(HERE, "..", "include", "astro_gpu.h")]
+    hdrs = (glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+            [os.path.join(HERE, "..", "include", "astro_gpu.h")])
     return any(os.path.getmtime(p) > t for p in [src] + hdrs)
 
 

@@ -79,6 +79,7 @@ struct astro_ctx {
     // device model
     DevBuf d_nodes, d_elist, d_elMat, d_esec, d_secABD, d_secOrient, d_colorEls, d_elBlk;
     DevBuf d_elC;           // per brick element the orthotropic C (C11 C12 C13 C22 C23 C33 C44 C55 C66)
+    DevBuf d_elXdf, d_elCdf;  // per brick element: node coordinates (section frame) and C in double-float
     DevBuf d_rank;          // currentRank (N) 1-based
     DevBuf d_bRowPtr, d_bCol, d_bRow, d_etype, d_elFirst;
     DevBuf d_K64, d_K32;    // BSR values

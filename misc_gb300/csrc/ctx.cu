@@ -63,7 +63,7 @@ static void free_all(astro_ctx *c) {
                       &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
-                      &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_ioRef,
+                      &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_elXdf, &c->d_elCdf, &c->d_ioRef,
                       &c->d_ioInt, &c->d_exMat, &c->d_exCols};
     for (DevBuf *b : bufs) dev_free(*b);
 }

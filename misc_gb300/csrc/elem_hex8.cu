@@ -18,6 +18,7 @@
 // Jacobian and displacement gradient by shuffles.  Elements are processed colour by colour so a
 // colour's blocks land in disjoint block rows: plain read-add-write, no atomics, bit-reproducible.
 #include "astro_internal.h"
+#include "dfloat.cuh"
 #include "shell_math.cuh"
 
 namespace {
@@ -334,37 +335,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A
 //     better spent on occupancy).
 constexpr int kRmwSteps = 22;  // ceil(64 blocks / 3 blocks per step)
 
-// double-float: x = hi + lo with |lo| <= ulp(hi)/2
-struct DF {
-    float hi, lo;
-};
-__device__ __forceinline__ DF df_split(double x) {
-    const float h = __double2float_rn(x);
-    return DF{h, __double2float_rn(x - (double)h)};
-}
-// s += a b (error-free product of the high parts, first-order cross terms, two-sum into s)
-__device__ __forceinline__ void df_fma(DF &s, float ah, float al, float bh, float bl) {
-    const float p = __fmul_rn(ah, bh);
-    float e = __fmaf_rn(ah, bh, -p);
-    e = __fmaf_rn(ah, bl, e);
-    e = __fmaf_rn(al, bh, e);
-    const float t = __fadd_rn(s.hi, p);
-    const float v = __fsub_rn(t, s.hi);
-    const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(t, v)), __fsub_rn(p, v));
-    s.lo = __fadd_rn(s.lo, __fadd_rn(err, e));
-    s.hi = t;
-}
-
 template <class T> struct FastCfg;
 template <> struct FastCfg<float> {
     static constexpr int FW = 8, MINB = 3;  // warps per CTA, CTAs per SM
     static constexpr bool PREFETCH = true;
 };
-template <> struct FastCfg<double> {
-    static constexpr int FW = 4, MINB = 3;
-    static constexpr bool PREFETCH = false;
-};
-
 template <class T> struct Hex8FastArgs {
     const double *nodes;
     const int *elist;
@@ -416,18 +391,6 @@ template <> struct GradSmem<float> {
         h[gp][a] = make_float4(d * gx, d * gy, d * gz, 0.f);
     }
 };
-template <> struct GradSmem<double> {
-    float4 gh[8][8], gl[8][8], hh[8][8], hl[8][8];  // double-float parts
-    __device__ void put(int gp, int a, double gx, double gy, double gz, double d) {
-        const DF x = df_split(gx), y = df_split(gy), z = df_split(gz);
-        const DF u = df_split(d * gx), v = df_split(d * gy), w = df_split(d * gz);
-        gh[gp][a] = make_float4(x.hi, y.hi, z.hi, 0.f);
-        gl[gp][a] = make_float4(x.lo, y.lo, z.lo, 0.f);
-        hh[gp][a] = make_float4(u.hi, v.hi, w.hi, 0.f);
-        hl[gp][a] = make_float4(u.lo, v.lo, w.lo, 0.f);
-    }
-};
-
 // 3x3 moments of the pairs (a0, b) and (a1, b): M = sum_gp g_a h_b^T
 __device__ __forceinline__ void pair_moments(const GradSmem<float> &S, int a0, int a1, int b, float M0[9],
                                              float M1[9]) {
@@ -444,33 +407,6 @@ __device__ __forceinline__ void pair_moments(const GradSmem<float> &S, int a0, i
         M1[6] += gc.z * hb.x; M1[7] += gc.z * hb.y; M1[8] += gc.z * hb.z;
     }
 }
-__device__ __forceinline__ void pair_moments(const GradSmem<double> &S, int a0, int a1, int b, double M0[9],
-                                             double M1[9]) {
-    DF m0[9], m1[9];
-#pragma unroll
-    for (int q = 0; q < 9; ++q) m0[q] = m1[q] = DF{0.f, 0.f};
-#pragma unroll
-    for (int gp = 0; gp < 8; ++gp) {
-        const float4 hh = S.hh[gp][b], hl = S.hl[gp][b];
-        const float4 ah = S.gh[gp][a0], al = S.gl[gp][a0], ch = S.gh[gp][a1], cl = S.gl[gp][a1];
-        const float gah[3] = {ah.x, ah.y, ah.z}, gal[3] = {al.x, al.y, al.z};
-        const float gch[3] = {ch.x, ch.y, ch.z}, gcl[3] = {cl.x, cl.y, cl.z};
-        const float hbh[3] = {hh.x, hh.y, hh.z}, hbl[3] = {hl.x, hl.y, hl.z};
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                df_fma(m0[3 * i + j], gah[i], gal[i], hbh[j], hbl[j]);
-                df_fma(m1[3 * i + j], gch[i], gcl[i], hbh[j], hbl[j]);
-            }
-    }
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        M0[q] = (double)m0[q].hi + (double)m0[q].lo;
-        M1[q] = (double)m1[q].hi + (double)m1[q].lo;
-    }
-}
-
 template <class T, bool ROT>
 __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fast_kernel(Hex8FastArgs<T> A) {
     constexpr int FW = FastCfg<T>::FW;
@@ -614,6 +550,220 @@ __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fa
     }
 }
 
+// FP64 zero-state kernel in double-float.  Same mapping as hex8_fast_kernel; the Jacobians,
+// their inverses, the gradients, the moments and the contraction with C run on the FP32 pipe in
+// double-float, from node coordinates (section frame) and C split once per context; FP64 is
+// used for the delivered blocks (and the rotation back from a rotated section frame).
+struct Hex8DfArgs {
+    const int *colorEls;
+    int count;
+    const int *elBlk;
+    const unsigned long long *elFirst;
+    const float2 *Xdf;     // (E,8,3) node coordinates in the section frame, double-float
+    const float2 *Cdf;     // (E,9) orthotropic C, double-float
+    const double *orient;  // (E,9) column-major section orientation (used when ROT)
+    double *K;             // BSR values or null
+    double *keOut;         // element matrices (E,24,24) column-major, element DOF order, or null
+};
+
+constexpr int kDfW = 4;  // warps per CTA
+constexpr float kRt3Hi = (float)kRt3;
+constexpr float kRt3Lo = (float)(kRt3 - (double)kRt3Hi);
+
+struct DfGrad {
+    float4 gh[8][8], gl[8][8], hh[8][8], hl[8][8];  // [gauss point][node]: g_a and w detJ g_a
+};
+
+__device__ __forceinline__ void df_ortho(const DF c[9], const DF M[9], DF K[9]) {
+    // c = C11 C12 C13 C22 C23 C33 C44 C55 C66
+    K[0] = df_add(df_add(df_mul(c[0], M[0]), df_mul(c[6], M[4])), df_mul(c[7], M[8]));
+    K[1] = df_add(df_mul(c[1], M[1]), df_mul(c[6], M[3]));
+    K[2] = df_add(df_mul(c[2], M[2]), df_mul(c[7], M[6]));
+    K[3] = df_add(df_mul(c[1], M[3]), df_mul(c[6], M[1]));
+    K[4] = df_add(df_add(df_mul(c[3], M[4]), df_mul(c[6], M[0])), df_mul(c[8], M[8]));
+    K[5] = df_add(df_mul(c[4], M[5]), df_mul(c[8], M[7]));
+    K[6] = df_add(df_mul(c[2], M[6]), df_mul(c[7], M[2]));
+    K[7] = df_add(df_mul(c[4], M[7]), df_mul(c[8], M[5]));
+    K[8] = df_add(df_add(df_mul(c[5], M[8]), df_mul(c[7], M[0])), df_mul(c[8], M[4]));
+}
+
+template <bool ROT> __global__ void __launch_bounds__(32 * kDfW, 3) hex8_df_kernel(Hex8DfArgs A) {
+    __shared__ DfGrad sG[kDfW];
+    __shared__ double sK[kDfW][64 * 9];
+    __shared__ int sBlk[kDfW][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int item = blockIdx.x * kDfW + w;
+    if (item >= A.count) return;
+    const int e = A.colorEls[item];
+    sBlk[w][lane] = A.elBlk[64 * (size_t)e + lane];
+    sBlk[w][lane + 32] = A.elBlk[64 * (size_t)e + lane + 32];
+    const unsigned long long first = A.elFirst[e];
+    const int grp = lane / 9, qq = lane - 9 * grp;
+    // Jacobian at Gauss point gp = lane/4 from nodes 2s, 2s+1 (s = lane%4)
+    {
+        const int gp = lane >> 2, s = lane & 3;
+        const DF G{kRt3Hi, kRt3Lo}, one{1.f, 0.f};
+        const DF s1 = (gp & 1) ? G : df_neg(G), s2 = (gp & 2) ? G : df_neg(G), s3 = (gp & 4) ? G : df_neg(G);
+        DF J[9], n[2][3];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) J[q] = DF{0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int a = 2 * s + k;
+            const float2 *xp = A.Xdf + 24 * (size_t)e + 3 * a;
+            const float2 x0 = xp[0], x1 = xp[1], x2 = xp[2];
+            const DF X[3] = {DF{x0.x, x0.y}, DF{x1.x, x1.y}, DF{x2.x, x2.y}};
+            const bool sp = (a == 1 || a == 2 || a == 5 || a == 6), tp = (a == 2 || a == 3 || a == 6 || a == 7),
+                       up = (a >= 4);
+            const DF p1 = df_add(one, sp ? s1 : df_neg(s1));  // 1 + sa s1
+            const DF p2 = df_add(one, tp ? s2 : df_neg(s2));
+            const DF p3 = df_add(one, up ? s3 : df_neg(s3));
+            n[k][0] = df_scale2(df_mul(p2, p3), sp ? 0.125f : -0.125f);
+            n[k][1] = df_scale2(df_mul(p1, p3), tp ? 0.125f : -0.125f);
+            n[k][2] = df_scale2(df_mul(p1, p2), up ? 0.125f : -0.125f);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) J[3 * i + j] = df_add(J[3 * i + j], df_mul(X[i], n[k][j]));
+        }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+#pragma unroll
+            for (int m = 1; m <= 2; m <<= 1) {
+                const DF o{__shfl_xor_sync(0xffffffffu, J[q].hi, m), __shfl_xor_sync(0xffffffffu, J[q].lo, m)};
+                J[q] = df_add(J[q], o);
+            }
+        }
+        const DF a11 = df_sub(df_mul(J[4], J[8]), df_mul(J[5], J[7]));
+        const DF a12 = df_sub(df_mul(J[5], J[6]), df_mul(J[3], J[8]));
+        const DF a13 = df_sub(df_mul(J[3], J[7]), df_mul(J[4], J[6]));
+        const DF dt = df_add(df_add(df_mul(J[0], a11), df_mul(J[1], a12)), df_mul(J[2], a13));
+        const DF di = df_rcp(dt);
+        DF I[3][3];
+        I[0][0] = df_mul(di, a11);
+        I[1][0] = df_mul(di, a12);
+        I[2][0] = df_mul(di, a13);
+        I[0][1] = df_mul(di, df_sub(df_mul(J[2], J[7]), df_mul(J[1], J[8])));
+        I[1][1] = df_mul(di, df_sub(df_mul(J[0], J[8]), df_mul(J[2], J[6])));
+        I[2][1] = df_mul(di, df_sub(df_mul(J[1], J[6]), df_mul(J[0], J[7])));
+        I[0][2] = df_mul(di, df_sub(df_mul(J[1], J[5]), df_mul(J[2], J[4])));
+        I[1][2] = df_mul(di, df_sub(df_mul(J[2], J[3]), df_mul(J[0], J[5])));
+        I[2][2] = df_mul(di, df_sub(df_mul(J[0], J[4]), df_mul(J[1], J[3])));
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            DF g[3], h[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                g[j] = df_add(df_add(df_mul(n[k][0], I[0][j]), df_mul(n[k][1], I[1][j])), df_mul(n[k][2], I[2][j]));
+                h[j] = df_mul(dt, g[j]);  // unit Gauss weights
+            }
+            const int a = 2 * s + k;
+            sG[w].gh[gp][a] = make_float4(g[0].hi, g[1].hi, g[2].hi, 0.f);
+            sG[w].gl[gp][a] = make_float4(g[0].lo, g[1].lo, g[2].lo, 0.f);
+            sG[w].hh[gp][a] = make_float4(h[0].hi, h[1].hi, h[2].hi, 0.f);
+            sG[w].hl[gp][a] = make_float4(h[0].lo, h[1].lo, h[2].lo, 0.f);
+        }
+    }
+    __syncwarp();
+    const int a0 = lane >> 3, a1 = a0 + 4, b = lane & 7;
+    DF M0[9], M1[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) M0[q] = M1[q] = DF{0.f, 0.f};
+#pragma unroll
+    for (int gp = 0; gp < 8; ++gp) {
+        const float4 hh = sG[w].hh[gp][b], hl = sG[w].hl[gp][b];
+        const float4 ah = sG[w].gh[gp][a0], al = sG[w].gl[gp][a0], ch = sG[w].gh[gp][a1], cl = sG[w].gl[gp][a1];
+        const float gah[3] = {ah.x, ah.y, ah.z}, gal[3] = {al.x, al.y, al.z};
+        const float gch[3] = {ch.x, ch.y, ch.z}, gcl[3] = {cl.x, cl.y, cl.z};
+        const float hbh[3] = {hh.x, hh.y, hh.z}, hbl[3] = {hl.x, hl.y, hl.z};
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                df_acc(M0[3 * i + j], gah[i], gal[i], hbh[j], hbl[j]);
+                df_acc(M1[3 * i + j], gch[i], gcl[i], hbh[j], hbl[j]);
+            }
+    }
+    DF c[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const float2 v = A.Cdf[9 * (size_t)e + q];
+        c[q] = DF{v.x, v.y};
+        M0[q] = df_norm(M0[q]);
+        M1[q] = df_norm(M1[q]);
+    }
+    double K0[9], K1[9];
+    {
+        DF k0[9], k1[9];
+        df_ortho(c, M0, k0);
+        df_ortho(c, M1, k1);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            K0[q] = df_to_double(k0[q]);
+            K1[q] = df_to_double(k1[q]);
+        }
+    }
+    if (ROT) {
+        double Or[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Or[i][j] = A.orient[9 * (size_t)e + 3 * j + i];
+        rotate_block<double>(Or, K0);
+        rotate_block<double>(Or, K1);
+    }
+    if (A.K) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            sK[w][9 * lane + q] = K0[q];
+            sK[w][9 * (lane + 32) + q] = K1[q];
+        }
+        __syncwarp();
+#pragma unroll
+        for (int st = 0; st < kRmwSteps; ++st) {
+            const int j = 3 * st + grp;
+            if (grp < 3 && j < 64) {
+                double *dst = A.K + 9 * (size_t)sBlk[w][j] + qq;
+                const double v = sK[w][9 * j + qq];
+                *dst = ((first >> j) & 1ull) ? v : *dst + v;
+            }
+        }
+    }
+    if (A.keOut) {
+        double *ke = A.keOut + 576 * (size_t)e;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                ke[(size_t)(8 * j + b) * 24 + (8 * i + a0)] = K0[3 * i + j];
+                ke[(size_t)(8 * j + b) * 24 + (8 * i + a1)] = K1[3 * i + j];
+            }
+    }
+}
+
+// Node coordinates of every brick element in its section frame (orient X, FP64) and its C, both
+// split into double-float for hex8_df_kernel.
+__global__ void k_elem_df(int E, const double *__restrict__ nodes, const int *__restrict__ elist,
+                          const double *__restrict__ orient, const double *__restrict__ elC, float2 *__restrict__ Xdf,
+                          float2 *__restrict__ Cdf) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double Or[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Or[i][j] = orient ? orient[9 * (size_t)e + 3 * j + i] : (i == j ? 1.0 : 0.0);
+    for (int a = 0; a < 8; ++a) {
+        const int nd = elist[8 * (size_t)e + a];
+        const double *x = nodes + 3 * (size_t)(nd - 1);
+        for (int i = 0; i < 3; ++i) {
+            const double y = Or[i][0] * x[0] + Or[i][1] * x[1] + Or[i][2] * x[2];
+            const DF d = df_from_double(y);
+            Xdf[24 * (size_t)e + 3 * a + i] = make_float2(d.hi, d.lo);
+        }
+    }
+    for (int q = 0; q < 9; ++q) {
+        const DF d = df_from_double(elC[9 * (size_t)e + q]);
+        Cdf[9 * (size_t)e + q] = make_float2(d.hi, d.lo);
+    }
+}
+
 // Orthotropic C of every brick element by the reference's LU (r_getMaterialStiffness): the
 // normal 3x3 block and the shear diagonal of C = S^-1.
 __global__ void k_elem_c(int E, const double *__restrict__ elMat, double *__restrict__ elC) {
@@ -743,11 +893,41 @@ static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_di
     return cuda_check(ctx, cudaGetLastError(), "hex8 kernel launch");
 }
 
+// FP64 zero-state stiffness (double-float kernel), colour by colour.
+static int hex8_df_run(astro_ctx *ctx, double *K, double *d_ke) {
+    const AstroPrep &P = ctx->P;
+    Hex8DfArgs A;
+    A.elBlk = dptr<int>(ctx->d_elBlk);
+    A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
+    A.Xdf = dptr<float2>(ctx->d_elXdf);
+    A.Cdf = dptr<float2>(ctx->d_elCdf);
+    A.orient = dptr<double>(ctx->d_secOrient);
+    A.K = K;
+    A.keOut = d_ke;
+    for (int col = 0; col < P.ncolors; ++col) {
+        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+        if (!cnt) continue;
+        A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+        A.count = cnt;
+        const unsigned grid = (cnt + kDfW - 1) / kDfW;
+        if (ctx->orientIdentity)
+            hex8_df_kernel<false><<<grid, 32 * kDfW, 0, ctx->stream>>>(A);
+        else
+            hex8_df_kernel<true><<<grid, 32 * kDfW, 0, ctx->stream>>>(A);
+    }
+    return cuda_check(ctx, cudaGetLastError(), "brick8 FP64 zero-state kernel launch");
+}
+
 int hex8_prepare(astro_ctx *ctx) {
     const int E = ctx->P.E;
     int rc;
     if ((rc = dev_alloc(ctx, ctx->d_elC, sizeof(double) * 9 * (size_t)E))) return rc;
     k_elem_c<<<(E + 127) / 128, 128, 0, ctx->stream>>>(E, dptr<double>(ctx->d_elMat), dptr<double>(ctx->d_elC));
+    if ((rc = dev_alloc(ctx, ctx->d_elXdf, sizeof(float2) * 24 * (size_t)E))) return rc;
+    if ((rc = dev_alloc(ctx, ctx->d_elCdf, sizeof(float2) * 9 * (size_t)E))) return rc;
+    k_elem_df<<<(E + 127) / 128, 128, 0, ctx->stream>>>(
+        E, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist), ctx->orientIdentity ? nullptr : dptr<double>(ctx->d_secOrient),
+        dptr<double>(ctx->d_elC), dptr<float2>(ctx->d_elXdf), dptr<float2>(ctx->d_elCdf));
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     return cuda_check(ctx, e, "brick8 material stiffness");
@@ -755,7 +935,7 @@ int hex8_prepare(astro_ctx *ctx) {
 
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
     if (precision == 32) return hex8_fast_run<float>(ctx, (store & 1) ? dptr<float>(ctx->d_K32) : nullptr, nullptr);
-    return hex8_fast_run<double>(ctx, (store & 2) ? dptr<double>(ctx->d_K64) : nullptr, nullptr);
+    return hex8_df_run(ctx, (store & 2) ? dptr<double>(ctx->d_K64) : nullptr, nullptr);
 }
 
 // getElasticSolnLoad for bricks.  From the undeformed state (no displacement) the residual is
@@ -763,17 +943,17 @@ int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
 // block-CSR matrix without a prior zeroing; any other state takes the general kernel (Green-
 // Lagrange strain, stress stiffness, residual), which adds into a zeroed matrix.
 int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt) {
-    if (!d_disp) return buildMat ? hex8_fast_run<double>(ctx, dptr<double>(ctx->d_K64), nullptr) : ASTRO_OK;
+    if (!d_disp) return buildMat ? hex8_df_run(ctx, dptr<double>(ctx->d_K64), nullptr) : ASTRO_OK;
     return hex8_run(ctx, 64, buildMat ? 2 : 0, d_disp, d_loadInt, nullptr, nullptr);
 }
 
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
     if (precision == 32) return hex8_fast_run<float>(ctx, nullptr, d_ke);
-    return hex8_fast_run<double>(ctx, nullptr, d_ke);
+    return hex8_df_run(ctx, nullptr, d_ke);
 }
 
 int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru) {
-    if (!d_disp && !d_ru) return hex8_fast_run<double>(ctx, nullptr, d_ke);
+    if (!d_disp && !d_ru) return hex8_df_run(ctx, nullptr, d_ke);
     return hex8_run(ctx, 64, 0, d_disp, nullptr, d_ke, d_ru);
 }
 
