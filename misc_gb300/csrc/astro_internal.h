@@ -84,7 +84,11 @@ struct astro_ctx {
     DevBuf d_bRowPtr, d_bCol, d_bRow, d_etype, d_elFirst;
     DevBuf d_K64, d_K32;    // BSR values
     int haveK64 = 0, haveK32 = 0;
-    DevBuf d_K64p, d_K32p;  // solver copies in block-plane layout (entry q of block k at q*nb + k)
+    // solver copies in slot-major block-ELL layout: entry q of the s-th block of block row r at
+    // (s*dpn*dpn + q)*ellLd + r, its block column at d_ellCol[s*ellLd + r] (empty slots: the row
+    // itself with zero values)
+    DevBuf d_K64p, d_K32p, d_ellCol;
+    int ellSlots = 0, ellLd = 0;
     int k64Version = 0, k32Version = 0, k64PlanesVersion = -1, k32PlanesVersion = -1;
     DevBuf d_csrPos, d_elMatRangeRank;  // export tables
     DevBuf d_intMat;        // condensed internal rows (shell), E*256 doubles

@@ -59,7 +59,7 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 static void free_all(astro_ctx *c) {
     DevBuf *bufs[] = {&c->d_nodes,  &c->d_elist,   &c->d_elMat,   &c->d_esec,    &c->d_secABD,   &c->d_secOrient,
                       &c->d_colorEls, &c->d_elBlk, &c->d_rank,    &c->d_bRowPtr, &c->d_bCol,     &c->d_bRow,
-                      &c->d_etype,  &c->d_elFirst, &c->d_K64p, &c->d_K32p, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
+                      &c->d_etype,  &c->d_elFirst, &c->d_K64p, &c->d_K32p, &c->d_ellCol, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
                       &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,

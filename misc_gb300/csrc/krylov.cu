@@ -1,21 +1,25 @@
 // Restarted GMRES(m) on A = K + C^T C for the spec solvers.
 //
-//   * K is the device block-CSR matrix (dpn x dpn blocks, FP64 or FP32 values); C^T C (the
-//     scaled penalty of scaleElasticMPC) is kept in FP64 as a per-block-row list and fused into
-//     the SpMV, which runs one warp per block row (coalesced block values, gathered x);
+//   * K is kept for the solvers as a slot-major block-ELL copy of the assembled block-CSR matrix:
+//     the s-th block of every block row is contiguous across rows, so the SpMV runs one thread
+//     per block row with every value load coalesced across the warp and no cross-lane reduction.
+//     GB300 issues FP64 at 1/64 of its FP32 rate, so the products are accumulated in the
+//     precision of the matrix (FP32 for the inner solver, FP64 for the comparator) and no FP64
+//     warp reductions remain.  C^T C (the scaled penalty of scaleElasticMPC) stays in FP64 as a
+//     per-block-row list and is added by the same thread;
 //   * preconditioner: Jacobi on the right (A D^-1 y = b, x = D^-1 y), so the Arnoldi residual
 //     estimate is the residual of the unpreconditioned system;
 //   * orthogonalisation: classical Gram-Schmidt with one re-orthogonalisation (CGS2).  The Krylov
-//     basis is stored vector-major (V[k*ld + i]); every pass is bandwidth-shaped: the dot
-//     products stage a chunk of w in shared memory and let each warp stream whole basis vectors
-//     over that chunk (one warp reduction per vector), the updates run one thread per row.
-//     Dot products are reduced deterministically (per-CTA partials, then one reduction CTA).
-//     Givens rotations and the stopping test run on the device; one Arnoldi step is 7 launches
-//     and a restart cycle is captured once as a CUDA graph and replayed, the host reading one
-//     status word per cycle;
+//     basis is stored vector-major (V[k*ld + i]); the dot products stage a chunk of w in shared
+//     memory and let each warp stream whole basis vectors over that chunk, the updates run one
+//     thread per row; both work in the precision of the basis.  Dot products are reduced
+//     deterministically (per-CTA partials in FP64, then one reduction CTA).  Givens rotations
+//     and the stopping test run on the device; one Arnoldi step is 7 launches and a restart
+//     cycle is captured once as a CUDA graph and replayed, the host reading one status word per
+//     cycle;
 //   * precision: the plain solver runs in FP64 throughout (the comparator).  The mixed solver
-//     runs the Krylov cycles in FP32 (FP32 matrix and basis; dot products accumulated in FP64)
-//     inside an FP64 iterative refinement whose residual b - A x is formed in FP64.
+//     runs the Krylov cycles in FP32 (FP32 matrix and basis) inside an FP64 iterative refinement
+//     whose residual b - A x is formed in FP64 arithmetic.
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -44,15 +48,13 @@ struct GmresCtl {
 };
 
 template <class TM> struct Op {
-    const int *rowPtr;
-    const int *col;
-    const TM *K;        // block planes: entry q = i*dpn + j of block k at K[q*nb + k]
-    long long nb;
+    const TM *K;        // block-ELL values: entry q of slot s of block row r at (s*DPN*DPN + q)*ld + r
+    const int *col;     // block column of slot s of row r at col[s*ld + r]
+    int S, ld;          // slots per row, row stride
     const int *penPtr;  // (N+1) penalty entries per block row, or null
     const int *penRow;
     const int *penCol;
     const double *penVal;
-    const double *dinv;  // Jacobi inverse diagonal (n) or null
     int N, dpn;
 };
 
@@ -60,93 +62,82 @@ __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
-
-// y_r = (A (s * x))_r for block row r, one warp, one lane per block (block planes: each of the
-// dpn*dpn value loads is coalesced across the lanes, and x is gathered once per block column
-// component); result in all lanes.
-template <class TM, class TX, int DPN>
-__device__ __forceinline__ void row_apply(const Op<TM> &op, int r, const TX *__restrict__ x, double xs, double out[DPN]) {
-    const int b0 = op.rowPtr[r], b1 = op.rowPtr[r + 1];
-    const int lane = threadIdx.x & 31;
-    double acc[DPN];
-#pragma unroll
-    for (int i = 0; i < DPN; ++i) acc[i] = 0.0;
-    for (int k = b0 + lane; k < b1; k += 32) {
-        const int c = __ldg(op.col + k) * DPN;
-        double xv[DPN];
-#pragma unroll
-        for (int j = 0; j < DPN; ++j) xv[j] = (double)x[c + j];
-        double kv[DPN * DPN];
-#pragma unroll
-        for (int q = 0; q < DPN * DPN; ++q) kv[q] = (double)op.K[(size_t)q * op.nb + k];
-#pragma unroll
-        for (int i = 0; i < DPN; ++i) {
-            double s = 0.0;
-#pragma unroll
-            for (int j = 0; j < DPN; ++j) s += kv[i * DPN + j] * xv[j];
-            acc[i] += s * xs;
-        }
-    }
-    if (op.penPtr) {
-        for (int t = op.penPtr[r] + lane; t < op.penPtr[r + 1]; t += 32) {
-            const int c = op.penCol[t];
-            const double xv = (double)x[c] * xs;
-            const double p = op.penVal[t] * xv;
-            const int i = op.penRow[t];
-#pragma unroll
-            for (int q = 0; q < DPN; ++q) acc[q] += (q == i) ? p : 0.0;
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < DPN; ++q) out[q] = warp_sum(acc[q]);
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
 }
 
-// v_j = wprev * inv (rows of this warp written to V[j]); w = A D^-1 v_j, reading the
-// Jacobi-scaled copy zprev = D^-1 wprev.  One warp per block row.
+// y = (A x)_r for block row r, one thread: the products accumulate in TA (the matrix precision
+// for the Krylov steps, FP64 for true residuals).
+template <class TA, class TM, class TX, int DPN>
+__device__ __forceinline__ void ell_row(const Op<TM> &op, int r, const TX *__restrict__ x, TA y[DPN]) {
+#pragma unroll
+    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
+    const size_t ld = (size_t)op.ld;
+    for (int s = 0; s < op.S; ++s) {
+        const int c = __ldg(op.col + (size_t)s * ld + r);
+        TA xv[DPN];
+#pragma unroll
+        for (int j = 0; j < DPN; ++j) xv[j] = (TA)x[(size_t)c * DPN + j];
+        const TM *kp = op.K + (size_t)s * DPN * DPN * ld + r;
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int j = 0; j < DPN; ++j) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + j) * ld) * xv[j];
+    }
+    if (op.penPtr) {
+        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
+            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
+            const int i = op.penRow[t];
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
+        }
+    }
+}
+
+// v_j = wprev * inv (written to V[j]); w = A D^-1 v_j = inv * A zprev with zprev = D^-1 wprev.
+// One thread per block row.
 template <class TM, class TV, int DPN>
 __global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restrict__ V, size_t ld, const TV *__restrict__ wprev,
                                                         const TV *__restrict__ zprev, TV *__restrict__ w,
                                                         const GmresCtl *__restrict__ ctl) {
     if (ctl->done) return;
-    const int r = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int r = blockIdx.x * kThreads + threadIdx.x;
     if (r >= op.N) return;
-    const int lane = threadIdx.x & 31;
     const int j = ctl->j;
-    const double inv = ctl->inv;
-    double y[DPN];
-    row_apply<TM, TV, DPN>(op, r, zprev, inv, y);
-    if (lane < DPN) {
-        const size_t i = (size_t)r * DPN + lane;
-        double yv = 0.0;
+    const TV inv = (TV)ctl->inv;
+    TV y[DPN];
+    ell_row<TV, TM, TV, DPN>(op, r, zprev, y);
 #pragma unroll
-        for (int q = 0; q < DPN; ++q) yv = (q == lane) ? y[q] : yv;
-        V[(size_t)j * ld + i] = (TV)((double)wprev[i] * inv);
-        w[i] = (TV)yv;
+    for (int q = 0; q < DPN; ++q) {
+        const size_t i = (size_t)r * DPN + q;
+        V[(size_t)j * ld + i] = wprev[i] * inv;
+        w[i] = y[q] * inv;
     }
 }
 
 // partial dot products of w with V[0..j] over a chunk of rows: part[cta][k]
 template <class TV>
-__device__ __forceinline__ void chunk_dots(int n, const TV *__restrict__ V, size_t ld, const double *sw, int row0, int cnt,
+__device__ __forceinline__ void chunk_dots(int n, const TV *__restrict__ V, size_t ld, const TV *sw, int row0, int cnt,
                                            int j, double *part) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     // kChunk = 256 rows: eight values per lane per basis vector, loaded together
     for (int k = wid; k <= j; k += kWarps) {
         const TV *__restrict__ vk = V + (size_t)k * ld + row0;
-        double v[kChunk / 32];
+        TV v[kChunk / 32];
 #pragma unroll
         for (int u = 0; u < kChunk / 32; ++u) {
             const int t = lane + 32 * u;
-            v[u] = (t < cnt) ? (double)vk[t] : 0.0;
+            v[u] = (t < cnt) ? vk[t] : TV(0);
         }
-        double s = 0.0;
+        TV s = TV(0);
 #pragma unroll
         for (int u = 0; u < kChunk / 32; ++u) {
             const int t = lane + 32 * u;
-            s += (t < cnt) ? v[u] * sw[t] : 0.0;
+            s += (t < cnt) ? v[u] * sw[t] : TV(0);
         }
         s = warp_sum(s);
-        if (lane == 0) part[(size_t)blockIdx.x * (kMaxM + 1) + k] = s;
+        if (lane == 0) part[(size_t)blockIdx.x * (kMaxM + 1) + k] = (double)s;
     }
 }
 
@@ -154,55 +145,55 @@ template <class TV>
 __global__ void __launch_bounds__(kThreads) k_dots(int n, const TV *__restrict__ V, size_t ld, const TV *__restrict__ w,
                                                    const GmresCtl *__restrict__ ctl, double *part) {
     if (ctl->done) return;
-    __shared__ double sw[kChunk];
+    __shared__ TV sw[kChunk];
     const int row0 = blockIdx.x * kChunk;
     const int cnt = min(kChunk, n - row0);
-    for (int t = threadIdx.x; t < cnt; t += kThreads) sw[t] = (double)w[row0 + t];
+    for (int t = threadIdx.x; t < cnt; t += kThreads) sw[t] = w[row0 + t];
     __syncthreads();
     chunk_dots<TV>(n, V, ld, sw, row0, cnt, ctl->j, part);
 }
 
-// w -= V[0..j] h1; then either the partial dots with V (mode 0) or the partial ||w||^2 (mode 1)
+// w -= V[0..j] h1; then either the partial dots with V (mode 0) or the partial ||w||^2 (mode 1),
+// in mode 1 also the Jacobi-scaled copy z = D^-1 w read by the next SpMV.
 template <class TV>
 __global__ void __launch_bounds__(kThreads) k_update(int n, const TV *__restrict__ V, size_t ld, TV *__restrict__ w,
                                                      const GmresCtl *__restrict__ ctl, double *part, int mode,
-                                                     const double *__restrict__ dinv, TV *__restrict__ z) {
+                                                     const TV *__restrict__ dinv, TV *__restrict__ z) {
     if (ctl->done) return;
-    __shared__ double sw[kChunk];
-    __shared__ double sh[kMaxM + 1];
+    __shared__ TV sw[kChunk];
+    __shared__ TV sh[kMaxM + 1];
     __shared__ double sred[kWarps];
     const int j = ctl->j;
-    for (int k = threadIdx.x; k <= j; k += kThreads) sh[k] = ctl->h1[k];
+    for (int k = threadIdx.x; k <= j; k += kThreads) sh[k] = (TV)ctl->h1[k];
     __syncthreads();
     const int row0 = blockIdx.x * kChunk;
     const int cnt = min(kChunk, n - row0);
-    double nrm = 0.0;
+    TV nrm = TV(0);
     const int t = threadIdx.x;  // kChunk == kThreads: one row per thread
     if (t < cnt) {
         const int i = row0 + t;
-        double s = (double)w[i];
+        TV s = w[i];
         int k = 0;
         // eight basis values in flight per thread
         for (; k + 8 <= j + 1; k += 8) {
-            double v[8];
+            TV v[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = (double)V[(size_t)(k + u) * ld + i];
+            for (int u = 0; u < 8; ++u) v[u] = V[(size_t)(k + u) * ld + i];
 #pragma unroll
             for (int u = 0; u < 8; ++u) s -= sh[k + u] * v[u];
         }
-        for (; k <= j; ++k) s -= sh[k] * (double)V[(size_t)k * ld + i];
-        const TV wv = (TV)s;
-        w[i] = wv;
-        if (z) z[i] = (TV)(dinv[i] * (double)wv);  // Jacobi-scaled copy read by the next SpMV
-        sw[t] = (double)wv;
-        nrm = (double)wv * (double)wv;
+        for (; k <= j; ++k) s -= sh[k] * V[(size_t)k * ld + i];
+        w[i] = s;
+        if (z) z[i] = dinv[i] * s;
+        sw[t] = s;
+        nrm = s * s;
     }
     __syncthreads();
     if (mode == 0) {
         chunk_dots<TV>(n, V, ld, sw, row0, cnt, j, part);
     } else {
         nrm = warp_sum(nrm);
-        if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = nrm;
+        if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = (double)nrm;
         __syncthreads();
         if (threadIdx.x == 0) {
             double s = 0.0;
@@ -306,54 +297,54 @@ __global__ void k_lsq(GmresCtl *ctl) {
 
 // x += D^-1 V[0..j-1] y
 template <class TV, class TX>
-__global__ void __launch_bounds__(kThreads) k_xupdate(int n, const TV *__restrict__ V, size_t ld, const double *__restrict__ dinv,
+__global__ void __launch_bounds__(kThreads) k_xupdate(int n, const TV *__restrict__ V, size_t ld, const TV *__restrict__ dinv,
                                                       const GmresCtl *__restrict__ ctl, TX *__restrict__ x) {
-    __shared__ double sy[kMaxM];
+    __shared__ TV sy[kMaxM];
     const int j = ctl->j;
-    for (int k = threadIdx.x; k < j; k += kThreads) sy[k] = ctl->y[k];
+    for (int k = threadIdx.x; k < j; k += kThreads) sy[k] = (TV)ctl->y[k];
     __syncthreads();
     for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-        double s = 0.0;
+        TV s = TV(0);
         int k = 0;
         for (; k + 8 <= j; k += 8) {
-            double v[8];
+            TV v[8];
 #pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = (double)V[(size_t)(k + u) * ld + i];
+            for (int u = 0; u < 8; ++u) v[u] = V[(size_t)(k + u) * ld + i];
 #pragma unroll
             for (int u = 0; u < 8; ++u) s += sy[k + u] * v[u];
         }
-        for (; k < j; ++k) s += sy[k] * (double)V[(size_t)k * ld + i];
-        x[i] = (TX)((double)x[i] + dinv[i] * s);
+        for (; k < j; ++k) s += sy[k] * V[(size_t)k * ld + i];
+        x[i] = (TX)(x[i] + dinv[i] * s);
     }
 }
 
-// r = b - A x (FP64 arithmetic), partial ||r||^2 and ||b||^2 per CTA.  One warp per block row.
+// r = b - A x with the products accumulated in FP64, partial ||r||^2 and ||b||^2 per CTA; with
+// z also the Jacobi-scaled copy z = D^-1 r.  One thread per block row.
 template <class TM, class TX, class TR, int DPN>
 __global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *__restrict__ x, const double *__restrict__ b,
-                                                       TR *__restrict__ r, double *part, const double *__restrict__ dinv = nullptr,
+                                                       TR *__restrict__ r, double *part, const TR *__restrict__ dinv = nullptr,
                                                        TR *__restrict__ z = nullptr) {
     __shared__ double sp[kWarps][2];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int row = blockIdx.x * kWarps + wid;
+    const int row = blockIdx.x * kThreads + threadIdx.x;
     double rr = 0.0, bb = 0.0;
     if (row < op.N) {
         double y[DPN];
         if (x) {
-            row_apply<TM, TX, DPN>(op, row, x, 1.0, y);
+            ell_row<double, TM, TX, DPN>(op, row, x, y);
         } else {
 #pragma unroll
             for (int q = 0; q < DPN; ++q) y[q] = 0.0;
         }
-        if (lane < DPN) {
-            const size_t i = (size_t)row * DPN + lane;
-            double yv = 0.0;
 #pragma unroll
-            for (int q = 0; q < DPN; ++q) yv = (q == lane) ? y[q] : yv;
-            const double v = b[i] - yv;
-            r[i] = (TR)v;
-            if (z) z[i] = (TR)(dinv[i] * (double)(TR)v);
-            rr = v * v;
-            bb = b[i] * b[i];
+        for (int q = 0; q < DPN; ++q) {
+            const size_t i = (size_t)row * DPN + q;
+            const double v = b[i] - y[q];
+            const TR rv = (TR)v;
+            r[i] = rv;
+            if (z) z[i] = dinv[i] * rv;
+            rr += v * v;
+            bb += b[i] * b[i];
         }
     }
     rr = warp_sum(rr);
@@ -402,21 +393,39 @@ __global__ void k_axpy_f2d(double *x, const float *d, int n) {
     if (i < n) x[i] += (double)d[i];
 }
 
-// Jacobi inverse diagonal: 1 / (K_ii + (C^T C)_ii)
-template <class TM> __global__ void k_dinv(Op<TM> op, double *dinv) {
+// Jacobi inverse diagonal 1 / (K_ii + (C^T C)_ii) from the block-CSR values, in FP64 and in the
+// precision of the Krylov basis.
+template <class TM, class TV>
+__global__ void k_dinv(const TM *__restrict__ K, const int *__restrict__ rowPtr, const int *__restrict__ bCol, int N,
+                       int dpn, const int *penPtr, const int *penRow, const int *penCol, const double *penVal,
+                       double *dinv, TV *dinvT) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= op.N) return;
-    const int dpn = op.dpn;
+    if (r >= N) return;
     int kd = -1;
-    for (int k = op.rowPtr[r]; k < op.rowPtr[r + 1]; ++k)
-        if (op.col[k] == r) kd = k;
+    for (int k = rowPtr[r]; k < rowPtr[r + 1]; ++k)
+        if (bCol[k] == r) kd = k;
     for (int q = 0; q < dpn; ++q) {
-        double d = (kd >= 0) ? (double)op.K[(size_t)(q * dpn + q) * op.nb + kd] : 0.0;
-        if (op.penPtr)
-            for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t)
-                if (op.penRow[t] == q && op.penCol[t] == r * dpn + q) d += op.penVal[t];
-        dinv[(size_t)r * dpn + q] = (d != 0.0) ? 1.0 / d : 1.0;
+        double d = (kd >= 0) ? (double)K[(size_t)kd * dpn * dpn + q * dpn + q] : 0.0;
+        if (penPtr)
+            for (int t = penPtr[r]; t < penPtr[r + 1]; ++t)
+                if (penRow[t] == q && penCol[t] == r * dpn + q) d += penVal[t];
+        const double v = (d != 0.0) ? 1.0 / d : 1.0;
+        dinv[(size_t)r * dpn + q] = v;
+        dinvT[(size_t)r * dpn + q] = (TV)v;
     }
+}
+
+// block-CSR (dd-value row-major blocks) -> slot-major block-ELL, one thread per (row, slot)
+template <class T>
+__global__ void k_to_ell(const T *__restrict__ K, const int *__restrict__ rowPtr, const int *__restrict__ bCol, int N,
+                         int S, int ld, int dd, T *__restrict__ Ke, int *__restrict__ colE) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)S * ld) return;
+    const int s = (int)(t / ld), r = (int)(t - (long long)s * ld);
+    const int k = (r < N) ? rowPtr[r] + s : -1;
+    const bool has = r < N && k < rowPtr[r + 1];
+    if (colE) colE[t] = has ? bCol[k] : (r < N ? r : 0);
+    for (int q = 0; q < dd; ++q) Ke[((size_t)s * dd + q) * ld + r] = has ? K[(size_t)k * dd + q] : T(0);
 }
 
 }  // namespace
@@ -424,51 +433,58 @@ template <class TM> __global__ void k_dinv(Op<TM> op, double *dinv) {
 // ---------------------------------------------------------------------------------------------
 
 struct GmresWork {
-    DevBuf V, w0, w1, z0, z1, part, ctl, dinv, rres, xs;
+    DevBuf V, w0, w1, z0, z1, part, ctl, dinv, dinvT, rres, xs;
     int n = 0, m = 0;
     size_t ld = 0;
     int nChunks = 0, nRowCtas = 0;
     std::vector<double> hp;
 };
 
-// block-CSR values (dpn x dpn row-major blocks) -> block planes (entry q of block k at q*nb + k)
-template <class T> __global__ void k_to_planes(const T *__restrict__ K, T *__restrict__ Kp, long long nb, int dd) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= nb * dd) return;
-    const long long k = t / dd;
-    const int q = (int)(t - k * dd);
-    Kp[(size_t)q * nb + k] = K[t];
-}
-
-// Solver copy of the assembled matrix in block-plane layout (rebuilt when the assembly changed).
-template <class TM> static const TM *planes_of(astro_ctx *ctx, int *rc) {
+// Solver copy of the assembled matrix in slot-major block-ELL layout (rebuilt when the assembly
+// changed).
+template <class TM> static const TM *ell_of(astro_ctx *ctx, int *rc) {
     const bool f64 = sizeof(TM) == 8;
     DevBuf &src = f64 ? ctx->d_K64 : ctx->d_K32;
     DevBuf &dst = f64 ? ctx->d_K64p : ctx->d_K32p;
     int &ver = f64 ? ctx->k64PlanesVersion : ctx->k32PlanesVersion;
     const int cur = f64 ? ctx->k64Version : ctx->k32Version;
-    const long long dd = (long long)ctx->P.dpn * ctx->P.dpn, nb = ctx->P.nb;
+    const AstroPrep &P = ctx->P;
+    const int dd = P.dpn * P.dpn;
     *rc = ASTRO_OK;
-    if (!dst.p && (*rc = dev_alloc(ctx, dst, sizeof(TM) * nb * dd))) return nullptr;
-    if (ver != cur) {
-        k_to_planes<TM><<<(unsigned)((nb * dd + 255) / 256), 256, 0, ctx->stream>>>(dptr<TM>(src), dptr<TM>(dst), nb, (int)dd);
-        if ((*rc = cuda_check(ctx, cudaGetLastError(), "to_planes"))) return nullptr;
+    if (!ctx->ellSlots) {
+        int S = 0;
+        for (int r = 0; r < P.N; ++r) S = std::max(S, P.bRowPtr[r + 1] - P.bRowPtr[r]);
+        ctx->ellSlots = S;
+        ctx->ellLd = (P.N + 31) / 32 * 32;
+    }
+    const int S = ctx->ellSlots, ld = ctx->ellLd;
+    bool needCol = false;
+    if (!ctx->d_ellCol.p) {
+        if ((*rc = dev_alloc(ctx, ctx->d_ellCol, sizeof(int) * (size_t)S * ld))) return nullptr;
+        needCol = true;
+    }
+    if (!dst.p && (*rc = dev_alloc(ctx, dst, sizeof(TM) * (size_t)S * dd * ld))) return nullptr;
+    if (ver != cur || needCol) {
+        const long long tot = (long long)S * ld;
+        k_to_ell<TM><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(
+            dptr<TM>(src), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), P.N, S, ld, dd, dptr<TM>(dst),
+            needCol ? dptr<int>(ctx->d_ellCol) : nullptr);
+        if ((*rc = cuda_check(ctx, cudaGetLastError(), "to_ell"))) return nullptr;
         ver = cur;
     }
     return dptr<TM>(dst);
 }
 
-template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *Kplanes, const double *dinv) {
+template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *Kell) {
     Op<TM> op;
-    op.rowPtr = dptr<int>(ctx->d_bRowPtr);
-    op.col = dptr<int>(ctx->d_bCol);
-    op.K = Kplanes;
-    op.nb = ctx->P.nb;
+    op.K = Kell;
+    op.col = dptr<int>(ctx->d_ellCol);
+    op.S = ctx->ellSlots;
+    op.ld = ctx->ellLd;
     op.penPtr = ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr;
     op.penRow = dptr<int>(ctx->d_penRow);
     op.penCol = dptr<int>(ctx->d_penCol);
     op.penVal = dptr<double>(ctx->d_penVal);
-    op.dinv = dinv;
     op.N = ctx->P.N;
     op.dpn = ctx->P.dpn;
     return op;
@@ -481,7 +497,7 @@ static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m)
     TV *za = dptr<TV>(W.z0), *zb = dptr<TV>(W.z1);
     GmresCtl *ctl = dptr<GmresCtl>(W.ctl);
     double *part = dptr<double>(W.part);
-    const double *dinv = dptr<double>(W.dinv);
+    const TV *dinv = dptr<TV>(W.dinvT);
     const int n = W.n;
     for (int step = 0; step < m; ++step) {
         TV *wprev = (step % 2 == 0) ? wa : wb, *zprev = (step % 2 == 0) ? za : zb;
@@ -513,19 +529,18 @@ template <class TM, class TV, int DPN>
 static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const double *b, double tgtAbs, int maxCycles,
                        int m, int *iters, int *cycles, double *finalRes) {
     cudaStream_t s = ctx->stream;
-    Op<TM> op = make_op<TM>(ctx, K, dptr<double>(W.dinv));
-    Op<TM> opNo = make_op<TM>(ctx, K, nullptr);
+    Op<TM> op = make_op<TM>(ctx, K);
     GmresCtl *ctl = dptr<GmresCtl>(W.ctl);
     double *part = dptr<double>(W.part);
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(opNo, x, b, dptr<TV>(W.w0), part, dptr<double>(W.dinv),
+    k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, dptr<TV>(W.w0), part, dptr<TV>(W.dinvT),
                                                                  dptr<TV>(W.z0));
     k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, tgtAbs);
     enqueue_cycle<TM, TV, DPN>(ctx, W, op, m);
     k_lsq<<<1, 1, 0, s>>>(ctl);
-    k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<double>(W.dinv), ctl, x);
+    k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x);
     CK(cudaStreamEndCapture(s, &graph));
     CK(cudaGraphInstantiate(&exec, graph, 0));
     int status = ASTRO_OK;
@@ -558,7 +573,7 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
     W.m = m;
     W.ld = ((size_t)n + 31) / 32 * 32;
     W.nChunks = (n + kChunk - 1) / kChunk;
-    W.nRowCtas = (ctx->P.N + kWarps - 1) / kWarps;
+    W.nRowCtas = (ctx->P.N + kThreads - 1) / kThreads;
     const size_t nparts = std::max((size_t)W.nChunks * (kMaxM + 1), (size_t)2 * W.nRowCtas);
     int rc;
     if ((rc = dev_alloc(ctx, W.V, W.ld * (m + 1) * tv))) return rc;
@@ -569,6 +584,7 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
     if ((rc = dev_alloc(ctx, W.part, sizeof(double) * nparts))) return rc;
     if ((rc = dev_alloc(ctx, W.ctl, sizeof(GmresCtl)))) return rc;
     if ((rc = dev_alloc(ctx, W.dinv, sizeof(double) * (size_t)n))) return rc;
+    if ((rc = dev_alloc(ctx, W.dinvT, (size_t)n * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.rres, sizeof(double) * (size_t)n))) return rc;
     if ((rc = dev_alloc(ctx, W.xs, sizeof(float) * (size_t)n))) return rc;
     CK(cudaMemsetAsync(W.ctl.p, 0, sizeof(GmresCtl), ctx->stream));
@@ -576,7 +592,7 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
 }
 
 static void work_free(GmresWork &W) {
-    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.z0, &W.z1, &W.part, &W.ctl, &W.dinv, &W.rres, &W.xs};
+    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.z0, &W.z1, &W.part, &W.ctl, &W.dinv, &W.dinvT, &W.rres, &W.xs};
     for (auto *x : b) dev_free(*x);
 }
 
@@ -588,14 +604,14 @@ static int true_residual(astro_ctx *ctx, GmresWork &W, int kind, const double *x
     double *part = dptr<double>(W.part);
     int prc = ASTRO_OK;
     if (kind == 64) {
-        const double *Kp = planes_of<double>(ctx, &prc);
+        const double *Kp = ell_of<double>(ctx, &prc);
         if (prc) return prc;
-        Op<double> op = make_op<double>(ctx, Kp, nullptr);
+        Op<double> op = make_op<double>(ctx, Kp);
         k_residual<double, double, double, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
     } else {
-        const float *Kp = planes_of<float>(ctx, &prc);
+        const float *Kp = ell_of<float>(ctx, &prc);
         if (prc) return prc;
-        Op<float> op = make_op<float>(ctx, Kp, nullptr);
+        Op<float> op = make_op<float>(ctx, Kp);
         k_residual<float, double, double, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, r_out, part);
     }
     int rc = ASTRO_OK;
@@ -633,13 +649,15 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     cudaEventRecord(e0, ctx->stream);
     double *r = dptr<double>(W.rres);
     if (fp64) {
-        const double *K64p = planes_of<double>(ctx, &rc);
+        const double *K64p = ell_of<double>(ctx, &rc);
         if (rc) {
             work_free(W);
             return rc;
         }
-        Op<double> op = make_op<double>(ctx, K64p, nullptr);
-        k_dinv<double><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(op, dptr<double>(W.dinv));
+        k_dinv<double, double><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
+            dptr<double>(ctx->d_K64), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn,
+            ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
+            dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<double>(W.dinvT));
         rc = true_residual<DPN>(ctx, W, 64, nullptr, d_b, &rel, r, &rn, &bn);
         const double tgt = o->rtol * bn;
         while (rc == ASTRO_OK) {
@@ -657,13 +675,15 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
             }
         }
     } else {
-        const float *K32p = planes_of<float>(ctx, &rc);
+        const float *K32p = ell_of<float>(ctx, &rc);
         if (rc) {
             work_free(W);
             return rc;
         }
-        Op<float> op32 = make_op<float>(ctx, K32p, nullptr);
-        k_dinv<float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(op32, dptr<double>(W.dinv));
+        k_dinv<float, float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
+            dptr<float>(ctx->d_K32), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn,
+            ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
+            dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<float>(W.dinvT));
         float *d32 = dptr<float>(W.xs);
         const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
         for (refinements = 0; refinements < 200; ++refinements) {
@@ -717,7 +737,7 @@ int krylov_solve_static(astro_ctx *ctx, const double *d_b, double *d_x, const as
 int krylov_apply(astro_ctx *ctx, int kind, const double *d_x, double *d_y) {
     GmresWork W;
     W.n = ctx->P.n;
-    W.nRowCtas = (ctx->P.N + kWarps - 1) / kWarps;
+    W.nRowCtas = (ctx->P.N + kThreads - 1) / kThreads;
     int rc = dev_alloc(ctx, W.part, sizeof(double) * 2 * W.nRowCtas);
     if (rc) return rc;
     DevBuf zb;
