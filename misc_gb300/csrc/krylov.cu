@@ -31,7 +31,10 @@ namespace {
 constexpr int kMaxM = 64;
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kChunk = 256;   // rows per CTA in the dot-product passes (one row per thread)
+constexpr int kGsThreads = 1024;  // threads per CTA of the Gram-Schmidt passes
+constexpr int kGsWarps = kGsThreads / 32;
+constexpr int kChunk = 1024;      // vector rows per CTA in the Gram-Schmidt passes (one per thread)
+constexpr int kRowThreads = 4;    // threads per block row in the SpMV
 
 struct GmresCtl {
     double H[(kMaxM + 1) * kMaxM];  // column-major (m+1) x m, Givens-rotated in place
@@ -45,6 +48,9 @@ struct GmresCtl {
     int done;        // converged / broke down / cycle full: later steps are no-ops
     int breakdown;
     int nonfinite;
+    unsigned arrive[3];  // CTAs finished in the current dots / update / update-and-norm launch
+    int reorth;          // this step's first pass lost more than half of ||w||^2: run the second
+    int reorths;         // second passes run in this cycle
 };
 
 template <class TM> struct Op {
@@ -68,22 +74,32 @@ __device__ __forceinline__ float warp_sum(float v) {
 }
 
 // y = (A x)_r for block row r, one thread: the products accumulate in TA (the matrix precision
-// for the Krylov steps, FP64 for true residuals).
+// for the Krylov steps, FP64 for true residuals).  Slots are taken three at a time so that their
+// column, x and value loads are in flight together.
 template <class TA, class TM, class TX, int DPN>
 __device__ __forceinline__ void ell_row(const Op<TM> &op, int r, const TX *__restrict__ x, TA y[DPN]) {
+    constexpr int G = 3;
 #pragma unroll
     for (int i = 0; i < DPN; ++i) y[i] = TA(0);
     const size_t ld = (size_t)op.ld;
-    for (int s = 0; s < op.S; ++s) {
-        const int c = __ldg(op.col + (size_t)s * ld + r);
-        TA xv[DPN];
+    for (int s0 = 0; s0 < op.S; s0 += G) {
+        int c[G];
 #pragma unroll
-        for (int j = 0; j < DPN; ++j) xv[j] = (TA)x[(size_t)c * DPN + j];
-        const TM *kp = op.K + (size_t)s * DPN * DPN * ld + r;
+        for (int g = 0; g < G; ++g) c[g] = (s0 + g < op.S) ? __ldg(op.col + (size_t)(s0 + g) * ld + r) : -1;
+        TA xv[G][DPN];
 #pragma unroll
-        for (int i = 0; i < DPN; ++i)
+        for (int g = 0; g < G; ++g)
 #pragma unroll
-            for (int j = 0; j < DPN; ++j) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + j) * ld) * xv[j];
+            for (int jj = 0; jj < DPN; ++jj) xv[g][jj] = (c[g] >= 0) ? (TA)x[(size_t)c[g] * DPN + jj] : TA(0);
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            if (s0 + g >= op.S) break;
+            const TM *kp = op.K + (size_t)(s0 + g) * DPN * DPN * ld + r;
+#pragma unroll
+            for (int i = 0; i < DPN; ++i)
+#pragma unroll
+                for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + jj) * ld) * xv[g][jj];
+        }
     }
     if (op.penPtr) {
         for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
@@ -95,157 +111,144 @@ __device__ __forceinline__ void ell_row(const Op<TM> &op, int r, const TX *__res
     }
 }
 
-// v_j = wprev * inv (written to V[j]); w = A D^-1 v_j = inv * A zprev with zprev = D^-1 wprev.
-// One thread per block row.
-template <class TM, class TV, int DPN>
-__global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restrict__ V, size_t ld, const TV *__restrict__ wprev,
-                                                        const TV *__restrict__ zprev, TV *__restrict__ w,
-                                                        const GmresCtl *__restrict__ ctl) {
-    if (ctl->done) return;
-    const int r = blockIdx.x * kThreads + threadIdx.x;
-    if (r >= op.N) return;
-    const int j = ctl->j;
-    const TV inv = (TV)ctl->inv;
-    TV y[DPN];
-    ell_row<TV, TM, TV, DPN>(op, r, zprev, y);
+// Partial (A x)_r over the slots s = sub, sub + kRowThreads, ... of block row r; the products
+// accumulate in TA.  The kRowThreads threads of a row are adjacent lanes and combine their
+// partials with xor-shuffles (result in all of them); thread sub == 0 adds the penalty.
+template <class TA, class TM, class TX, int DPN>
+__device__ __forceinline__ void ell_row_part(const Op<TM> &op, int r, int sub, const TX *__restrict__ x, TA y[DPN]) {
 #pragma unroll
-    for (int q = 0; q < DPN; ++q) {
-        const size_t i = (size_t)r * DPN + q;
-        V[(size_t)j * ld + i] = wprev[i] * inv;
-        w[i] = y[q] * inv;
+    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
+    const size_t ld = (size_t)op.ld;
+    for (int s = sub; s < op.S; s += kRowThreads) {
+        const int c = __ldg(op.col + (size_t)s * ld + r);
+        TA xv[DPN];
+#pragma unroll
+        for (int jj = 0; jj < DPN; ++jj) xv[jj] = (TA)x[(size_t)c * DPN + jj];
+        const TM *kp = op.K + (size_t)s * DPN * DPN * ld + r;
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + jj) * ld) * xv[jj];
     }
+    if (sub == 0 && op.penPtr) {
+        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
+            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
+            const int i = op.penRow[t];
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
+        }
+    }
+#pragma unroll
+    for (int m = 1; m < kRowThreads; m <<= 1)
+#pragma unroll
+        for (int i = 0; i < DPN; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], m);
 }
 
-// partial dot products of w with V[0..j] over a chunk of rows: part[cta][k]
-template <class TV>
-__device__ __forceinline__ void chunk_dots(int n, const TV *__restrict__ V, size_t ld, const TV *sw, int row0, int cnt,
-                                           int j, double *part) {
+// Partial dot products of the staged tile sw (cnt vector rows from row0, at most ROWS) with
+// V[0..j], and with itself when self is set (stored as vector kMaxM): part[k * nCh + cta].
+// Warp-per-vector, ROWS/32 rows per lane, eight loads in flight; full tiles take the unguarded
+// multiply-add path.  Lane 0 of each warp makes its partials visible device-wide.
+template <class TV, int ROWS>
+__device__ __forceinline__ void chunk_dots(const TV *__restrict__ V, size_t ld, const TV *sw, int row0, int cnt, int j,
+                                           double *part, int nCh, bool self) {
+    static_assert(ROWS % 256 == 0, "tile rows: a multiple of 32 lanes x 8 loads");
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    // kChunk = 256 rows: eight values per lane per basis vector, loaded together
-    for (int k = wid; k <= j; k += kWarps) {
-        const TV *__restrict__ vk = V + (size_t)k * ld + row0;
-        TV v[kChunk / 32];
-#pragma unroll
-        for (int u = 0; u < kChunk / 32; ++u) {
-            const int t = lane + 32 * u;
-            v[u] = (t < cnt) ? vk[t] : TV(0);
-        }
+    const int nv = j + 1 + (self ? 1 : 0);
+    for (int kk = wid; kk < nv; kk += kGsWarps) {
+        const bool isSelf = kk > j;
+        const TV *__restrict__ vk = isSelf ? sw : V + (size_t)kk * ld + row0;
         TV s = TV(0);
+        if (cnt == ROWS) {
 #pragma unroll
-        for (int u = 0; u < kChunk / 32; ++u) {
-            const int t = lane + 32 * u;
-            s += (t < cnt) ? v[u] * sw[t] : TV(0);
+            for (int u0 = 0; u0 < ROWS / 32; u0 += 8) {
+                TV v[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) v[u] = vk[lane + 32 * (u0 + u)];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) s = fma(v[u], sw[lane + 32 * (u0 + u)], s);
+            }
+        } else {
+            for (int t = lane; t < cnt; t += 32) s = fma(vk[t], sw[t], s);
         }
-        s = warp_sum(s);
-        if (lane == 0) part[(size_t)blockIdx.x * (kMaxM + 1) + k] = (double)s;
-    }
-}
-
-template <class TV>
-__global__ void __launch_bounds__(kThreads) k_dots(int n, const TV *__restrict__ V, size_t ld, const TV *__restrict__ w,
-                                                   const GmresCtl *__restrict__ ctl, double *part) {
-    if (ctl->done) return;
-    __shared__ TV sw[kChunk];
-    const int row0 = blockIdx.x * kChunk;
-    const int cnt = min(kChunk, n - row0);
-    for (int t = threadIdx.x; t < cnt; t += kThreads) sw[t] = w[row0 + t];
-    __syncthreads();
-    chunk_dots<TV>(n, V, ld, sw, row0, cnt, ctl->j, part);
-}
-
-// w -= V[0..j] h1; then either the partial dots with V (mode 0) or the partial ||w||^2 (mode 1),
-// in mode 1 also the Jacobi-scaled copy z = D^-1 w read by the next SpMV.
-template <class TV>
-__global__ void __launch_bounds__(kThreads) k_update(int n, const TV *__restrict__ V, size_t ld, TV *__restrict__ w,
-                                                     const GmresCtl *__restrict__ ctl, double *part, int mode,
-                                                     const TV *__restrict__ dinv, TV *__restrict__ z) {
-    if (ctl->done) return;
-    __shared__ TV sw[kChunk];
-    __shared__ TV sh[kMaxM + 1];
-    __shared__ double sred[kWarps];
-    const int j = ctl->j;
-    for (int k = threadIdx.x; k <= j; k += kThreads) sh[k] = (TV)ctl->h1[k];
-    __syncthreads();
-    const int row0 = blockIdx.x * kChunk;
-    const int cnt = min(kChunk, n - row0);
-    TV nrm = TV(0);
-    const int t = threadIdx.x;  // kChunk == kThreads: one row per thread
-    if (t < cnt) {
-        const int i = row0 + t;
-        TV s = w[i];
-        int k = 0;
-        // eight basis values in flight per thread
-        for (; k + 8 <= j + 1; k += 8) {
-            TV v[8];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) v[u] = V[(size_t)(k + u) * ld + i];
-#pragma unroll
-            for (int u = 0; u < 8; ++u) s -= sh[k + u] * v[u];
-        }
-        for (; k <= j; ++k) s -= sh[k] * V[(size_t)k * ld + i];
-        w[i] = s;
-        if (z) z[i] = dinv[i] * s;
-        sw[t] = s;
-        nrm = s * s;
-    }
-    __syncthreads();
-    if (mode == 0) {
-        chunk_dots<TV>(n, V, ld, sw, row0, cnt, j, part);
-    } else {
-        nrm = warp_sum(nrm);
-        if ((threadIdx.x & 31) == 0) sred[threadIdx.x >> 5] = (double)nrm;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0.0;
-            for (int q = 0; q < kWarps; ++q) s += sred[q];
-            part[(size_t)blockIdx.x * (kMaxM + 1)] = s;
-        }
-    }
-}
-
-// sum of part[q*stride + off] over q = lane, lane+32, ... < nparts, eight loads in flight
-__device__ __forceinline__ double lane_sum(const double *part, int nparts, size_t stride, int off, int lane) {
-    double s = 0.0;
-    for (int q0 = lane; q0 < nparts; q0 += 256) {
-        double v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int q = q0 + 32 * u;
-            v[u] = (q < nparts) ? part[(size_t)q * stride + off] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) s += v[u];
-    }
-    return s;
-}
-
-// Reduction of the per-CTA dot partials: mode 0 sets h1 and H[:,j], mode 1 sets h1 and adds it
-// to H[:,j].
-__global__ void k_reduce_dots(GmresCtl *ctl, const double *part, int nparts, int mode) {
-    if (ctl->done) return;
-    const int j = ctl->j;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int k = wid; k <= j; k += blockDim.x >> 5) {
-        double s = 0.0;
-        s = lane_sum(part, nparts, kMaxM + 1, k, lane);
         s = warp_sum(s);
         if (lane == 0) {
-            ctl->h1[k] = s;
-            if (mode == 0) ctl->H[(size_t)j * (kMaxM + 1) + k] = s;
-            else ctl->H[(size_t)j * (kMaxM + 1) + k] += s;
+            part[(size_t)(isSelf ? kMaxM : kk) * nCh + blockIdx.x] = (double)s;
+            __threadfence();
         }
     }
 }
 
-// Norm, Hessenberg subdiagonal, Givens rotation, residual estimate and stopping test.
-__global__ void k_control(GmresCtl *ctl, const double *part, int nparts, int m) {
-    if (ctl->done) return;
-    const int j = ctl->j;
-    const int lane = threadIdx.x;
+// True in the last CTA of the launch to arrive; the threads that wrote partials have fenced them
+// before the barrier.  That CTA resets the counter for the next launch.  No CTA waits for another.
+__device__ __forceinline__ bool last_to_arrive(unsigned *counter) {
+    __shared__ bool amLast;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(counter, 1u);
+        amLast = (prev == gridDim.x - 1);
+        if (amLast) *counter = 0u;
+    }
+    __syncthreads();
+    if (amLast) __threadfence();
+    return amLast;
+}
+
+// h[k] = sum of the nCh CTA partials of vector k in a fixed order (one warp per vector, reads
+// bypassing L1); recorded in h1 and in the Hessenberg column (mode 0) or added to it (mode 1).
+// In mode 0 the partials also carry ||w||^2 (vector kMaxM), and the second pass is requested when
+// the first removed more than half of it: ||w - V h||^2 = ||w||^2 - ||h||^2 < ||w||^2 / 2
+// (the "twice is enough" test of Kahan and Parlett).
+__device__ __forceinline__ void reduce_h(GmresCtl *ctl, const double *part, int nCh, int j, int mode) {
+    __shared__ double shh[kGsWarps], sww;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    double *Hc = ctl->H + (size_t)j * (kMaxM + 1);
+    double hh = 0.0;
+    const int nv = j + 1 + (mode == 0 ? 1 : 0);
+    for (int kk = wid; kk < nv; kk += kGsWarps) {
+        const int k = kk > j ? kMaxM : kk;
+        double s = 0.0;
+        for (int q0 = lane; q0 < nCh; q0 += 256) {
+            double v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int q = q0 + 32 * u;
+                v[u] = (q < nCh) ? __ldcg(part + (size_t)k * nCh + q) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += v[u];
+        }
+        s = warp_sum(s);
+        if (lane == 0) {
+            if (kk > j) {
+                sww = s;
+            } else {
+                ctl->h1[k] = s;
+                Hc[k] = (mode == 0) ? s : Hc[k] + s;
+                hh += s * s;
+            }
+        }
+    }
+    if (mode != 0) return;
+    if (lane == 0) shh[wid] = hh;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < kGsWarps; ++q) t += shh[q];
+        ctl->reorth = (sww - t < 0.5 * sww) ? 1 : 0;
+        ctl->reorths += ctl->reorth;
+    }
+}
+
+// Norm of w from the CTA partials, Hessenberg subdiagonal, Givens rotation, residual estimate
+// and stopping test (thread 0 of the last CTA).
+__device__ void step_control(GmresCtl *ctl, const double *part, int nCh, int m) {
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
     double s = 0.0;
-    s = lane_sum(part, nparts, kMaxM + 1, 0, lane);
+    for (int q = lane; q < nCh; q += 32) s += __ldcg(part + q);
     s = warp_sum(s);
     if (lane != 0) return;
+    const int j = ctl->j;
     const double nrm = sqrt(s);
     double *Hc = ctl->H + (size_t)j * (kMaxM + 1);
     Hc[j + 1] = nrm;
@@ -283,6 +286,129 @@ __global__ void k_control(GmresCtl *ctl, const double *part, int nparts, int m) 
     }
     ctl->inv = 1.0 / nrm;
     if (ctl->resest <= ctl->target || ctl->j >= m) ctl->done = 1;
+}
+
+// v_j = wprev * inv (written to V[j]); w = A D^-1 v_j = inv * A zprev with zprev = D^-1 wprev.
+// kRowThreads threads per block row; the products accumulate in the precision of the basis.
+template <class TM, class TV, int DPN>
+__global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restrict__ V, size_t ld, const TV *__restrict__ wprev,
+                                                        const TV *__restrict__ zprev, TV *__restrict__ w,
+                                                        const GmresCtl *__restrict__ ctl) {
+    if (ctl->done) return;
+    const int tid = blockIdx.x * kThreads + threadIdx.x;
+    const int r = tid / kRowThreads, sub = tid % kRowThreads;
+    // every lane takes part in the row shuffles: lanes past the last row work on the last row
+    // and write nothing
+    const bool valid = r < op.N;
+    const int rr = valid ? r : op.N - 1;
+    const int j = ctl->j;
+    const TV inv = (TV)ctl->inv;
+    TV y[DPN];
+    ell_row_part<TV, TM, TV, DPN>(op, rr, sub, zprev, y);
+    if (!valid) return;
+#pragma unroll
+    for (int q = 0; q < DPN; ++q) {
+        if (q % kRowThreads != sub) continue;
+        const size_t i = (size_t)r * DPN + q;
+        V[(size_t)j * ld + i] = wprev[i] * inv;
+        w[i] = y[q] * inv;
+    }
+}
+
+// First Gram-Schmidt pass: partial dots of w with V[0..j] and with itself over this CTA's rows;
+// the last CTA reduces them into h1 and decides whether a second pass is needed.
+template <class TV>
+__global__ void __launch_bounds__(kGsThreads, 2) k_dots(int n, const TV *__restrict__ V, size_t ld, const TV *__restrict__ w,
+                                                        GmresCtl *__restrict__ ctl, double *part, int nCh) {
+    if (ctl->done) return;
+    __shared__ TV sw[kChunk];
+    const int row0 = blockIdx.x * kChunk;
+    const int cnt = min(kChunk, n - row0);
+    const int j = ctl->j;
+    for (int t = threadIdx.x; t < cnt; t += kGsThreads) sw[t] = w[row0 + t];
+    __syncthreads();
+    chunk_dots<TV, kChunk>(V, ld, sw, row0, cnt, j, part, nCh, true);
+    if (last_to_arrive(&ctl->arrive[0])) reduce_h(ctl, part, nCh, j, 0);
+}
+
+// One Gram-Schmidt update on this CTA's rows: w -= V[0..j] h1.  The first update (pass 0) is
+// followed by the second pass's partial dots when the first pass asked for it (its last CTA then
+// adds the correction to the Hessenberg column); otherwise, and after the second update
+// (pass 1), the step finishes here: the partial ||w||^2, the Jacobi-scaled copy z = D^-1 w read
+// by the next SpMV, and the step control in the last CTA.  The second update returns at once
+// when no second pass was requested.
+template <class TV>
+__global__ void __launch_bounds__(kGsThreads, 2) k_update(int n, const TV *__restrict__ V, size_t ld, TV *__restrict__ w,
+                                                          GmresCtl *__restrict__ ctl, double *__restrict__ partDots,
+                                                          double *__restrict__ partNorm, int nCh, int pass,
+                                                          const TV *__restrict__ dinv, TV *__restrict__ z, int m) {
+    constexpr int ROWS = kChunk;
+    if (ctl->done) return;
+    const bool second = ctl->reorth != 0;
+    if (pass == 1 && !second) return;
+    const bool finish = (pass == 1) || !second;
+    __shared__ TV sw[ROWS];
+    __shared__ TV sh[kMaxM + 1];
+    __shared__ double sred[kGsWarps];
+    const int j = ctl->j;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = threadIdx.x; k <= j; k += kGsThreads) sh[k] = (TV)ctl->h1[k];
+    __syncthreads();
+    const int row0 = blockIdx.x * ROWS;
+    const int cnt = min(ROWS, n - row0);
+    TV nrm = TV(0);
+    for (int t = threadIdx.x; t < cnt; t += kGsThreads) {
+        const int i = row0 + t;
+        TV s = w[i];
+        int k = 0;
+        for (; k + 8 <= j + 1; k += 8) {
+            TV v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = V[(size_t)(k + u) * ld + i];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s -= sh[k + u] * v[u];
+        }
+        for (; k <= j; ++k) s -= sh[k] * V[(size_t)k * ld + i];
+        w[i] = s;
+        if (!finish) {
+            sw[t] = s;
+        } else {
+            z[i] = dinv[i] * s;
+            nrm += s * s;
+        }
+    }
+    if (!finish) {
+        __syncthreads();
+        chunk_dots<TV, ROWS>(V, ld, sw, row0, cnt, j, partDots, nCh, false);
+        if (last_to_arrive(&ctl->arrive[1])) reduce_h(ctl, partDots, nCh, j, 1);
+    } else {
+        nrm = warp_sum(nrm);
+        if (lane == 0) sred[wid] = (double)nrm;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0.0;
+            for (int q = 0; q < kGsWarps; ++q) s += sred[q];
+            partNorm[blockIdx.x] = s;
+            __threadfence();
+        }
+        if (last_to_arrive(&ctl->arrive[2])) step_control(ctl, partNorm, nCh, m);
+    }
+}
+
+// sum of part[q*stride + off] over q = lane, lane+32, ... < nparts, eight loads in flight
+__device__ __forceinline__ double lane_sum(const double *part, int nparts, size_t stride, int off, int lane) {
+    double s = 0.0;
+    for (int q0 = lane; q0 < nparts; q0 += 256) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int q = q0 + 32 * u;
+            v[u] = (q < nparts) ? part[(size_t)q * stride + off] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    return s;
 }
 
 // Least squares H y = g (upper triangular j x j), one thread.
@@ -374,6 +500,8 @@ __global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, dou
     if (lane != 0) return;
     const double beta = sqrt(a);
     ctl->j = 0;
+    ctl->reorth = 0;
+    ctl->reorths = 0;
     ctl->breakdown = 0;
     ctl->nonfinite = !isfinite(beta);
     ctl->g[0] = beta;
@@ -499,16 +627,16 @@ static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m)
     double *part = dptr<double>(W.part);
     const TV *dinv = dptr<TV>(W.dinvT);
     const int n = W.n;
+    double *partB = part + (size_t)(kMaxM + 1) * W.nChunks;
+    double *partN = partB + (size_t)(kMaxM + 1) * W.nChunks;  // per-CTA ||w||^2 of the step's last update
+    const unsigned spmvGrid = (unsigned)(((long long)ctx->P.N * kRowThreads + kThreads - 1) / kThreads);
     for (int step = 0; step < m; ++step) {
         TV *wprev = (step % 2 == 0) ? wa : wb, *zprev = (step % 2 == 0) ? za : zb;
         TV *wnew = (step % 2 == 0) ? wb : wa, *znew = (step % 2 == 0) ? zb : za;
-        k_spmv_step<TM, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, V, W.ld, wprev, zprev, wnew, ctl);
-        k_dots<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part);
-        k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, W.nChunks, 0);
-        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 0, nullptr, nullptr);
-        k_reduce_dots<<<1, 1024, 0, s>>>(ctl, part, W.nChunks, 1);
-        k_update<TV><<<W.nChunks, kThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, 1, dinv, znew);
-        k_control<<<1, 32, 0, s>>>(ctl, part, W.nChunks, m);
+        k_spmv_step<TM, TV, DPN><<<spmvGrid, kThreads, 0, s>>>(op, V, W.ld, wprev, zprev, wnew, ctl);
+        k_dots<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, W.nChunks);
+        k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 0, dinv, znew, m);
+        k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 1, dinv, znew, m);
     }
 }
 
@@ -574,7 +702,7 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
     W.ld = ((size_t)n + 31) / 32 * 32;
     W.nChunks = (n + kChunk - 1) / kChunk;
     W.nRowCtas = (ctx->P.N + kThreads - 1) / kThreads;
-    const size_t nparts = std::max((size_t)W.nChunks * (kMaxM + 1), (size_t)2 * W.nRowCtas);
+    const size_t nparts = std::max((size_t)3 * W.nChunks * (kMaxM + 1), (size_t)2 * W.nRowCtas);
     int rc;
     if ((rc = dev_alloc(ctx, W.V, W.ld * (m + 1) * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.w0, (size_t)n * tv))) return rc;
