@@ -176,6 +176,15 @@ int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro_state *sta
                        double *elastic_load, double *int_elastic_load,
                        double *elastic_mat, int32_t *el_mat_cols, double *int_elastic_mat);
 
+/* updateExternalRHS (Working/AStrO_commandFunctions.f90:568-607), loop over the internal rows
+ * as intended: ext_vec[el_mat_dim] -= K_ni K_ii^-1 int_vec for every element with internal DOF,
+ * using the condensed internal rows of the last astro_el_soln_load(build_mat = 1). */
+int astro_update_external_rhs(astro_ctx *ctx, double *ext_vec, const double *int_vec);
+/* updateInternalSoln (:609-651), same resolution: int_soln[int_vec_size] +=
+ * K_ii^-1 (int_rhs - K_in ext_soln) per element; int_rhs may be NULL (zeros). */
+int astro_update_internal_soln(astro_ctx *ctx, const double *ext_soln, double *int_soln,
+                               const double *int_rhs);
+
 /* Mixed-precision assembly used by the refinement solvers: element matrices evaluated in FP32
  * (isotropic/orthotropic sparse-B formulation) and assembled at zero state into the device
  * block-CSR matrix in both FP32 and FP64 storage.  The FP64 copy is the system matrix A. */
@@ -264,6 +273,27 @@ int astro_gmres(astro_ctx *ctx, double *x_vec, const double *a_mat, const int32_
  * u is the initial guess on entry.  Convergence is judged by the FP64 true relative residual. */
 int astro_solve_static(astro_ctx *ctx, const double *f, double *u, const astro_solve_opts *opts,
                        astro_solve_stats *stats);
+
+/* Implicit Newmark time stepping: the dynamic branch of solve (Working/AStrO_commandFunctions.f90:
+ * 751-815) with stepSolve (:681-749) for linear geometry.  K_eff = K + c1 c2 M (c1 = 0.5/beta,
+ * c2 = 2/del_t^2) is assembled at the initial state and the constraints scaled; then every step
+ * t = k del_t forms the residual with the Newmark inertia, adds load_amplitude[k] * load_pattern
+ * (load_pattern: el_mat_dim, may be NULL) and the constraint load, condenses the internal DOF,
+ * solves K_eff du = r by FP64 Jacobi-GMRES (restart, max_iters per step, relative tolerance rtol)
+ * warm-started from the previous increment, recovers the internal DOF and updates the state
+ * (acc, vel, previous values).  disp/vel/acc (el_mat_dim) and int_disp (int_vec_size, may be
+ * NULL) hold the initial state on entry (loadInitialState) and the final state on exit;
+ * disp_history (num_steps x el_mat_dim, may be NULL) receives the displacement of every step.
+ * Shell meshes (the Newmark inertia of the element library is implemented for shell4). */
+typedef struct astro_newmark_opts {
+    int32_t num_steps;
+    double del_t, nm_beta, nm_gamma;
+    int32_t restart, max_iters;  /* GMRES per step */
+    double rtol;
+} astro_newmark_opts;
+int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *opts, const double *load_pattern,
+                      const double *load_amplitude, double *disp, double *vel, double *acc,
+                      double *int_disp, double *disp_history, astro_solve_stats *stats);
 
 /* y = (K + C^T C) x for host vectors in global DOF numbering, with the device-resident K
  * (kind 64: FP64 values from astro_el_soln_load, 32: FP32 values from astro_assemble_fp32) and

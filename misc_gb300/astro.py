@@ -50,6 +50,11 @@ class SolveStatsC(C.Structure):
                 ("status", C.c_int32), ("rel_residual", C.c_double), ("seconds", C.c_double)]
 
 
+class NewmarkOptsC(C.Structure):
+    _fields_ = [("num_steps", C.c_int32), ("del_t", C.c_double), ("nm_beta", C.c_double), ("nm_gamma", C.c_double),
+                ("restart", C.c_int32), ("max_iters", C.c_int32), ("rtol", C.c_double)]
+
+
 def lib_path():
     return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libastro_gpu.so")
 
@@ -87,6 +92,10 @@ def load_library():
         "astro_solve_static": ([vp, F64P, F64P, C.POINTER(SolveOptsC), C.POINTER(SolveStatsC)], C.c_int),
         "astro_apply_operator": ([vp, C.c_int32, F64P, F64P], C.c_int),
         "astro_ctx_stream": ([vp], C.c_void_p),
+        "astro_update_external_rhs": ([vp, F64P, F64P], C.c_int),
+        "astro_newmark_run": ([vp, C.POINTER(NewmarkOptsC), F64P, F64P, F64P, F64P, F64P, F64P, F64P,
+                               C.POINTER(SolveStatsC)], C.c_int),
+        "astro_update_internal_soln": ([vp, F64P, F64P, F64P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -273,6 +282,36 @@ class AstroGPU:
                                        _i(cr), len(cm), len(cr) - 1, _d(pm), _i(pr), len(pm), _d(_f64(b_vec)),
                                        num_vecs, max_it))
         return x
+
+    def updateExternalRHS(self, ext_vec, int_vec):
+        """ext_vec -= K_ni K_ii^-1 int_vec over the shell elements (returns a new array)."""
+        out = _f64(ext_vec).copy()
+        self._check(self.L.astro_update_external_rhs(self.h, _d(out), _d(_f64(int_vec))))
+        return out
+
+    def updateInternalSoln(self, ext_soln, int_soln, int_rhs=None):
+        """int_soln + K_ii^-1 (int_rhs - K_in ext_soln) over the shell elements (new array)."""
+        out = _f64(int_soln).copy()
+        rhs = None if int_rhs is None else _d(_f64(int_rhs))
+        self._check(self.L.astro_update_internal_soln(self.h, _d(_f64(ext_soln)), _d(out), rhs))
+        return out
+
+    def newmark_run(self, num_steps, del_t, beta=0.25, gamma=0.5, load_pattern=None, load_amplitude=None, disp=None,
+                    vel=None, acc=None, int_disp=None, restart=50, max_iters=2000, rtol=1e-12, history=True):
+        """solve() dynamic branch on the device: returns (disp, vel, acc, int_disp, history, stats)."""
+        n, ni = self.n, self.int_vec_size
+        u = np.zeros(n) if disp is None else _f64(disp).copy()
+        v = np.zeros(n) if vel is None else _f64(vel).copy()
+        a = np.zeros(n) if acc is None else _f64(acc).copy()
+        iu = np.zeros(max(ni, 1)) if int_disp is None else _f64(int_disp).copy()
+        hist = np.zeros((num_steps, n)) if history else None
+        o = NewmarkOptsC(num_steps, del_t, beta, gamma, restart, max_iters, rtol)
+        st = SolveStatsC()
+        pat = None if load_pattern is None else _d(_f64(load_pattern))
+        amp = None if load_amplitude is None else _d(_f64(load_amplitude))
+        self._check(self.L.astro_newmark_run(self.h, C.byref(o), pat, amp, _d(u), _d(v), _d(a), _d(iu),
+                                             _d(hist) if history else None, C.byref(st)))
+        return u, v, a, iu[:ni], hist, st
 
     def getdRelasticdD(self, dvar, h=1e-14, state=None):
         """Complex-step dRu/dd of design variable dvar: (global DOF vector, internal-DOF vector)."""

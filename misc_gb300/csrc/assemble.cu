@@ -24,10 +24,11 @@ __global__ void export_csr_kernel(const double *__restrict__ K, const int *__res
     if (cols) cols[idx] = rb + 1 + j * N;
 }
 
-__global__ void absmax_kernel(const double *__restrict__ v, long long n, unsigned long long *out) {
+template <class T>
+__global__ void absmax_kernel(const T *__restrict__ v, long long n, unsigned long long *out) {
     double m = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        m = fmax(m, fabs(v[i]));
+        m = fmax(m, fabs((double)v[i]));
     for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
     __shared__ double s[32];
     if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = m;
@@ -52,6 +53,27 @@ __global__ void int_to_ref_kernel(const double *__restrict__ in, double *__restr
     if (t >= N * dpn) return;
     const int r = t % N, c = t / N;
     ref[t] = in[(size_t)r * dpn + c];
+}
+
+// getElasticConstraintLoad (Working/AStrO_commandFunctions.f90:506-535): load += C^T (rhs - C u)
+// with the scaled constraints in internal numbering (col < 0: empty slot).  The row residuals are
+// formed in parallel, the scatter runs in the reference's row and term order (one thread: the
+// constraint set is small and its rows may share DOF).
+__global__ void constraint_load_kernel(int mdim, const int *__restrict__ range, const int *__restrict__ col,
+                                       const double *__restrict__ val, const double *__restrict__ rhs,
+                                       const double *__restrict__ u, double *__restrict__ t, double *__restrict__ load) {
+    for (int r = threadIdx.x; r < mdim; r += blockDim.x) {
+        double s = rhs[r];
+        if (u)
+            for (int k = range[r]; k < range[r + 1]; ++k)
+                if (col[k] >= 0) s -= val[k] * u[col[k]];
+        t[r] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int r = 0; r < mdim; ++r)
+        for (int k = range[r]; k < range[r + 1]; ++k)
+            if (col[k] >= 0) load[col[k]] += val[k] * t[r];
 }
 
 // Consistent face load.  One thread per face; faces of one call may share nodes, so the
@@ -124,12 +146,16 @@ int export_csr_dev(astro_ctx *ctx, cudaStream_t s, double *d_mat, int *d_cols) {
     return cuda_check(ctx, cudaGetLastError(), "export_csr");
 }
 
-double bsr_absmax(astro_ctx *ctx, int *status) {
+// max |K| of the FP64 (kind 64) or FP32 (kind 32) block-CSR values
+double bsr_absmax(astro_ctx *ctx, int *status, int kind) {
     const long long nv = (long long)ctx->P.nb * ctx->P.dpn * ctx->P.dpn;
     unsigned long long *d = dptr<unsigned long long>(ctx->d_status) + 1;
     unsigned long long h = 0;
     cudaMemsetAsync(d, 0, sizeof(unsigned long long), ctx->stream);
-    absmax_kernel<<<4 * 152, 256, 0, ctx->stream>>>(dptr<double>(ctx->d_K64), nv, d);
+    if (kind == 64)
+        absmax_kernel<double><<<4 * 152, 256, 0, ctx->stream>>>(dptr<double>(ctx->d_K64), nv, d);
+    else
+        absmax_kernel<float><<<4 * 152, 256, 0, ctx->stream>>>(dptr<float>(ctx->d_K32), nv, d);
     cudaError_t e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     *status = (e == cudaSuccess) ? ASTRO_OK : cuda_check(ctx, e, "absmax");
@@ -137,6 +163,16 @@ double bsr_absmax(astro_ctx *ctx, int *status) {
     long long bits = (long long)h;
     memcpy(&v, &bits, sizeof(v));
     return v;
+}
+
+int constraint_load_dev(astro_ctx *ctx, const double *d_u, double *d_loadInt) {
+    const int md = ctx->P.mpcDim;
+    if (md == 0) return ASTRO_OK;
+    if (!ctx->d_mpcVal.p) return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run first");
+    constraint_load_kernel<<<1, 256, 0, ctx->stream>>>(md, dptr<int>(ctx->d_mpcRange), dptr<int>(ctx->d_mpcCol),
+                                                      dptr<double>(ctx->d_mpcVal), dptr<double>(ctx->d_mpcRhs), d_u,
+                                                      dptr<double>(ctx->d_mpcT), d_loadInt);
+    return cuda_check(ctx, cudaGetLastError(), "constraint load");
 }
 
 int ref_to_int_vec(astro_ctx *ctx, const double *d_ref, double *d_int, int n) {

@@ -84,6 +84,7 @@ struct astro_ctx {
     DevBuf d_bRowPtr, d_bCol, d_bRow, d_etype, d_elFirst;
     DevBuf d_K64, d_K32;    // BSR values
     int haveK64 = 0, haveK32 = 0;
+    int haveIntMat = 0;      // d_intMat holds the condensed internal rows of the last FP64 assembly
     // solver copies in slot-major block-ELL layout: entry q of the s-th block of block row r at
     // (s*dpn*dpn + q)*ellLd + r, its block column at d_ellCol[s*ellLd + r] (empty slots: the row
     // itself with zero values)
@@ -92,8 +93,10 @@ struct astro_ctx {
     int k64Version = 0, k32Version = 0, k64PlanesVersion = -1, k32PlanesVersion = -1;
     DevBuf d_csrPos, d_elMatRangeRank;  // export tables
     DevBuf d_intMat;        // condensed internal rows (shell), E*256 doubles
+    DevBuf d_shFr, d_shGp, d_shDe, d_shKf;  // shell pipeline scratch for shScratchEls elements
+    int shScratchEls = 0;
     // constraints on device (internal DOF numbering)
-    DevBuf d_mpcRange, d_mpcCol, d_mpcVal, d_mpcRhs;
+    DevBuf d_mpcRange, d_mpcCol, d_mpcVal, d_mpcRhs, d_mpcT;  // scaled, after astro_scale_mpc
     int mpcScaled = 0;
     // penalty C^T C as CSR over internal rows (host-built after scaling)
     DevBuf d_penRow, d_penPtr, d_penCol, d_penVal;
@@ -145,11 +148,15 @@ struct ShellDevState {
     double beta = 0.25, gamma = 0.5, delT = 0.0;
 };
 int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &s, double *d_loadInt, double *d_intLoad,
-                           int buildMat, double *d_ke, double *d_ru);  // elem_shell4.cu
+                           int buildMat, double *d_ke, double *d_ru, bool sync = true);  // elem_shell4.cu
 int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // elem_shell4.cu
+int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt);          // elem_shell4.cu
+int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln,
+                                const double *d_intRhs);                                           // elem_shell4.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu
 int export_csr_dev(astro_ctx *ctx, cudaStream_t s, double *d_mat, int *d_cols);  // assemble.cu
-double bsr_absmax(astro_ctx *ctx, int *status);                             // assemble.cu
+double bsr_absmax(astro_ctx *ctx, int *status, int kind);                   // assemble.cu
+int constraint_load_dev(astro_ctx *ctx, const double *d_u, double *d_loadInt);  // assemble.cu
 int ref_to_int_vec(astro_ctx *ctx, const double *d_ref, double *d_int, int n); // assemble.cu
 int int_to_ref_vec(astro_ctx *ctx, const double *d_int, double *d_ref, int n); // assemble.cu
 int surface_load_dev(astro_ctx *ctx, int nf, const int *d_faceEl, const int *d_faceNum, const double *tr,
@@ -161,5 +168,8 @@ int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, 
 int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *d_acc);          // elem_hex8.cu
 int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &s, double *d_acc,
                 double *d_intAcc);                                                              // elem_shell4.cu
+int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,
+                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup, double *d_hist,
+                   astro_solve_stats *st);  // krylov.cu
 // host: elements depending on dvar, grouped by colour (colour c: list[ptr[c] .. ptr[c+1]))
 void dvar_elements_by_colour(const astro_ctx *ctx, int dvar, std::vector<int> &list, std::vector<int> &ptr);

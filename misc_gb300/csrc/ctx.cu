@@ -60,11 +60,11 @@ static void free_all(astro_ctx *c) {
     DevBuf *bufs[] = {&c->d_nodes,  &c->d_elist,   &c->d_elMat,   &c->d_esec,    &c->d_secABD,   &c->d_secOrient,
                       &c->d_colorEls, &c->d_elBlk, &c->d_rank,    &c->d_bRowPtr, &c->d_bCol,     &c->d_bRow,
                       &c->d_etype,  &c->d_elFirst, &c->d_K64p, &c->d_K32p, &c->d_ellCol, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
-                      &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs,   &c->d_penRow,
+                      &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs, &c->d_mpcT, &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
                       &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_elXdf, &c->d_elCdf, &c->d_ioRef,
-                      &c->d_ioInt, &c->d_exMat, &c->d_exCols};
+                      &c->d_ioInt, &c->d_exMat, &c->d_exCols, &c->d_shFr, &c->d_shGp, &c->d_shDe, &c->d_shKf};
     for (DevBuf *b : bufs) dev_free(*b);
 }
 
@@ -397,6 +397,7 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
     if (build_mat == 1) {
         ctx->haveK64 = 1;
         ctx->k64Version++;
+        ctx->haveIntMat = ctx->hasShell;
     }
     // load back to reference numbering
     if ((rc = int_to_ref_vec(ctx, dl, dRef, n))) return rc;
@@ -414,6 +415,136 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
     ctx->mpcScaled = 0;
     ctx->haveLT = 0;
     ctx->ltFactored = 0;
+    return ASTRO_OK;
+}
+
+// updateExternalRHS (Working/AStrO_commandFunctions.f90:568-607) with the loop over the internal
+// rows (nodalDof+1 .. totalDof, the evident intent of its empty loop bound): for every shell
+// element ext_vec(nodal DOF) -= K_ni K_ii^-1 int_vec(element's internal DOF).
+extern "C" int astro_update_external_rhs(astro_ctx *ctx, double *ext_vec, const double *int_vec) {
+    if (!ctx || !ext_vec || !int_vec) return ASTRO_ERR_ARG;
+    if (!ctx->hasShell || !ctx->P.intVecSize) return ASTRO_OK;  // no internal DOF: nothing to condense
+    if (!ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
+    const int n = ctx->P.n;
+    int rc;
+    if ((rc = ensure_io(ctx, false))) return rc;
+    DevBuf iv;
+    if ((rc = upload(ctx, iv, int_vec, sizeof(double) * ctx->P.intVecSize))) return rc;
+    double *dRef = dptr<double>(ctx->d_ioRef), *dInt = dptr<double>(ctx->d_ioInt);
+    cudaError_t e = cudaMemcpyAsync(dRef, ext_vec, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && !(rc = ref_to_int_vec(ctx, dRef, dInt, n)) &&
+        !(rc = shell4_update_external_rhs(ctx, dptr<double>(iv), dInt)) && !(rc = int_to_ref_vec(ctx, dInt, dRef, n))) {
+        e = cudaMemcpyAsync(ext_vec, dRef, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    dev_free(iv);
+    if (rc) return rc;
+    return cuda_check(ctx, e, "update_external_rhs");
+}
+
+// updateInternalSoln (:609-651), loop bound resolved likewise: for every shell element
+// int_soln += K_ii^-1 (int_rhs - K_in ext_soln); int_rhs may be NULL (zeros).
+extern "C" int astro_update_internal_soln(astro_ctx *ctx, const double *ext_soln, double *int_soln,
+                                          const double *int_rhs) {
+    if (!ctx || !ext_soln || !int_soln) return ASTRO_ERR_ARG;
+    if (!ctx->hasShell || !ctx->P.intVecSize) return ASTRO_OK;
+    if (!ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
+    const int n = ctx->P.n, ni = ctx->P.intVecSize;
+    int rc;
+    if ((rc = ensure_io(ctx, false))) return rc;
+    DevBuf is, ir;
+    if ((rc = upload(ctx, is, int_soln, sizeof(double) * ni))) return rc;
+    if (int_rhs && (rc = upload(ctx, ir, int_rhs, sizeof(double) * ni))) {
+        dev_free(is);
+        return rc;
+    }
+    double *dRef = dptr<double>(ctx->d_ioRef), *dInt = dptr<double>(ctx->d_ioInt);
+    cudaError_t e = cudaMemcpyAsync(dRef, ext_soln, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess && !(rc = ref_to_int_vec(ctx, dRef, dInt, n)) &&
+        !(rc = shell4_update_internal_soln(ctx, dInt, dptr<double>(is), ir.p ? dptr<double>(ir) : nullptr))) {
+        e = cudaMemcpyAsync(int_soln, is.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    dev_free(is);
+    dev_free(ir);
+    if (rc) return rc;
+    return cuda_check(ctx, e, "update_internal_soln");
+}
+
+extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, const double *load_pattern,
+                                 const double *load_amplitude, double *disp, double *vel, double *acc, double *int_disp,
+                                 double *disp_history, astro_solve_stats *stats) {
+    if (!ctx || !o || !disp || !vel || !acc || o->num_steps < 0 || !(o->del_t > 0.0) || !(o->nm_beta > 0.0) ||
+        (load_pattern && !load_amplitude))
+        return ASTRO_ERR_ARG;
+    if (!ctx->hasShell) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark stepping is implemented for shell4 meshes");
+    const AstroPrep &P = ctx->P;
+    const int n = P.n, ni = P.intVecSize;
+    int rc;
+    struct Bufs {
+        DevBuf u, up, vp, ap, iu, iup, pat, hist;
+        ~Bufs() {
+            DevBuf *b[] = {&u, &up, &vp, &ap, &iu, &iup, &pat, &hist};
+            for (auto *x : b) dev_free(*x);
+        }
+    } B;
+    // loadInitialState: the previous state is the initial one, the previous internal DOF zero
+    if ((rc = state_vec_up(ctx, disp, B.u, false))) return rc;
+    if ((rc = state_vec_up(ctx, vel, B.vp, false))) return rc;
+    if ((rc = state_vec_up(ctx, acc, B.ap, false))) return rc;
+    if ((rc = dev_alloc(ctx, B.up, sizeof(double) * n))) return rc;
+    CK(cudaMemcpyAsync(B.up.p, B.u.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (ni) {
+        if ((rc = dev_alloc(ctx, B.iu, sizeof(double) * ni))) return rc;
+        if ((rc = dev_alloc(ctx, B.iup, sizeof(double) * ni))) return rc;
+        CK(cudaMemsetAsync(B.iup.p, 0, sizeof(double) * ni, ctx->stream));
+        if (int_disp) CK(cudaMemcpyAsync(B.iu.p, int_disp, sizeof(double) * ni, cudaMemcpyHostToDevice, ctx->stream));
+        else CK(cudaMemsetAsync(B.iu.p, 0, sizeof(double) * ni, ctx->stream));
+    }
+    if (load_pattern && (rc = state_vec_up(ctx, load_pattern, B.pat, false))) return rc;
+    if (disp_history && o->num_steps > 0 && (rc = dev_alloc(ctx, B.hist, sizeof(double) * n * (size_t)o->num_steps)))
+        return rc;
+    // K_eff = K + c1 c2 M at the initial state (getElasticSolnLoad(1) with the dynamic flag), then
+    // scaleElasticMPC
+    ShellDevState ds;
+    ds.disp = dptr<double>(B.u);
+    ds.pdisp = dptr<double>(B.up);
+    ds.pvel = dptr<double>(B.vp);
+    ds.pacc = dptr<double>(B.ap);
+    ds.idisp = ni ? dptr<double>(B.iu) : nullptr;
+    ds.pidisp = ni ? dptr<double>(B.iup) : nullptr;
+    ds.dynamic = 1;
+    ds.beta = o->nm_beta;
+    ds.gamma = o->nm_gamma;
+    ds.delT = o->del_t;
+    if ((rc = ensure_K(ctx, 2))) return rc;
+    if ((rc = bsr_zero(ctx, 2))) return rc;
+    if ((rc = launch_shell4_assemble(ctx, ds, nullptr, nullptr, 1, nullptr, nullptr))) return rc;
+    ctx->haveK64 = 1;
+    ctx->k64Version++;
+    ctx->haveIntMat = 1;
+    ctx->haveLT = 0;
+    ctx->ltFactored = 0;
+    if ((rc = astro_scale_mpc(ctx, nullptr, nullptr))) return rc;
+    rc = krylov_newmark(ctx, o, B.pat.p ? dptr<double>(B.pat) : nullptr, load_amplitude, dptr<double>(B.u),
+                        dptr<double>(B.up), dptr<double>(B.vp), dptr<double>(B.ap), ni ? dptr<double>(B.iu) : nullptr,
+                        ni ? dptr<double>(B.iup) : nullptr, B.hist.p ? dptr<double>(B.hist) : nullptr, stats);
+    if (rc) return rc;
+    // final state (after the swap the previous values are the current ones)
+    if ((rc = ensure_io(ctx, false))) return rc;
+    double *dRef = dptr<double>(ctx->d_ioRef);
+    const double *src[3] = {dptr<double>(B.u), dptr<double>(B.vp), dptr<double>(B.ap)};
+    double *dst[3] = {disp, vel, acc};
+    for (int q = 0; q < 3; ++q) {
+        if ((rc = int_to_ref_vec(ctx, src[q], dRef, n))) return rc;
+        CK(cudaMemcpyAsync(dst[q], dRef, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    if (ni && int_disp) CK(cudaMemcpyAsync(int_disp, B.iu.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream));
+    if (B.hist.p)
+        CK(cudaMemcpyAsync(disp_history, B.hist.p, sizeof(double) * n * (size_t)o->num_steps, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return ASTRO_OK;
 }
 
@@ -600,13 +731,9 @@ extern "C" int astro_scale_mpc(astro_ctx *ctx, double *mpc_mat, double *mpc_rhs)
     double maxMat = 0.0;
     int st = ASTRO_OK;
     if (ctx->haveK64) {
-        maxMat = bsr_absmax(ctx, &st);
+        maxMat = bsr_absmax(ctx, &st, 64);
     } else if (ctx->haveK32) {
-        // max |K| of the FP32 matrix, through an FP64 staging copy
-        const size_t nv = (size_t)P.nb * P.dpn * P.dpn;
-        std::vector<float> h(nv);
-        CK(cudaMemcpy(h.data(), ctx->d_K32.p, nv * sizeof(float), cudaMemcpyDeviceToHost));
-        for (float v : h) maxMat = std::max(maxMat, (double)std::fabs(v));
+        maxMat = bsr_absmax(ctx, &st, 32);
     } else {
         return set_err(ctx, ASTRO_ERR_STATE, "scale_mpc called before the stiffness was assembled");
     }
@@ -624,6 +751,21 @@ extern "C" int astro_scale_mpc(astro_ctx *ctx, double *mpc_mat, double *mpc_rhs)
     for (auto &v : ctx->mpcRhsScaledHost) v = 100.0 * maxMat * v;
     int rc = build_penalty(ctx);
     if (rc) return rc;
+    // the scaled constraints in internal numbering, for the device constraint load
+    if (P.mpcDim > 0) {
+        std::vector<int> colInt(P.mpcCols.size());
+        for (size_t k = 0; k < colInt.size(); ++k) {
+            const int d = P.mpcCols[k];  // 1-based reference DOF (component-major), 0 = empty
+            colInt[k] = d ? ((d - 1) % P.N) * P.dpn + (d - 1) / P.N : -1;
+        }
+        if ((rc = upload(ctx, ctx->d_mpcRange, P.mpcRange.data(), sizeof(int) * P.mpcRange.size()))) return rc;
+        if ((rc = upload(ctx, ctx->d_mpcCol, colInt.data(), sizeof(int) * colInt.size()))) return rc;
+        if ((rc = upload(ctx, ctx->d_mpcVal, ctx->mpcScaledHost.data(), sizeof(double) * ctx->mpcScaledHost.size())))
+            return rc;
+        if ((rc = upload(ctx, ctx->d_mpcRhs, ctx->mpcRhsScaledHost.data(), sizeof(double) * ctx->mpcRhsScaledHost.size())))
+            return rc;
+        if ((rc = dev_alloc(ctx, ctx->d_mpcT, sizeof(double) * P.mpcDim))) return rc;
+    }
     ctx->mpcScaled = 1;
     if (mpc_mat) std::copy(ctx->mpcScaledHost.begin(), ctx->mpcScaledHost.end(), mpc_mat);
     if (mpc_rhs) std::copy(ctx->mpcRhsScaledHost.begin(), ctx->mpcRhsScaledHost.end(), mpc_rhs);
@@ -633,14 +775,20 @@ extern "C" int astro_scale_mpc(astro_ctx *ctx, double *mpc_mat, double *mpc_rhs)
 extern "C" int astro_constraint_load(astro_ctx *ctx, const double *node_disp, double *elastic_load) {
     if (!ctx || !elastic_load) return ASTRO_ERR_ARG;
     const AstroPrep &P = ctx->P;
-    // tiny (one entry per constrained DOF): C^T (rhs - C u) on the host, in the reference's order
-    std::vector<double> t(ctx->mpcRhsScaledHost);
-    for (int r = 0; r < P.mpcDim; ++r)
-        for (int k = P.mpcRange[r]; k < P.mpcRange[r + 1]; ++k)
-            if (P.mpcCols[k] && node_disp) t[r] -= ctx->mpcScaledHost[k] * node_disp[P.mpcCols[k] - 1];
-    for (int r = 0; r < P.mpcDim; ++r)
-        for (int k = P.mpcRange[r]; k < P.mpcRange[r + 1]; ++k)
-            if (P.mpcCols[k]) elastic_load[P.mpcCols[k] - 1] += ctx->mpcScaledHost[k] * t[r];
+    if (P.mpcDim == 0) return ASTRO_OK;
+    if (!ctx->mpcScaled) return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run first");
+    const int n = P.n;
+    int rc;
+    if ((rc = ensure_io(ctx, false))) return rc;
+    DevState S;
+    if ((rc = state_vec_up(ctx, node_disp, S.disp))) return rc;
+    double *dRef = dptr<double>(ctx->d_ioRef), *dInt = dptr<double>(ctx->d_ioInt);
+    CK(cudaMemcpyAsync(dRef, elastic_load, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = ref_to_int_vec(ctx, dRef, dInt, n))) return rc;
+    if ((rc = constraint_load_dev(ctx, S.disp.p ? dptr<double>(S.disp) : nullptr, dInt))) return rc;
+    if ((rc = int_to_ref_vec(ctx, dInt, dRef, n))) return rc;
+    CK(cudaMemcpyAsync(elastic_load, dRef, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     return ASTRO_OK;
 }
 

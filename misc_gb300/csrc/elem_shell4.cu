@@ -89,16 +89,20 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
 // els[ptr[c] .. ptr[c+1]) (device list).
 static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
                           const ShellProps *props, double gpc, double *d_loadInt, double *d_intLoad, int buildMat,
-                          double *d_K, double *d_intMat, double *d_ke, double *d_ru) {
+                          double *d_K, double *d_intMat, double *d_ke, double *d_ru, bool sync = true) {
     int maxc = 0;
     for (size_t c = 0; c + 1 < ptr.size(); ++c) maxc = std::max(maxc, ptr[c + 1] - ptr[c]);
     if (!maxc) return ASTRO_OK;
-    DevBuf fr, gp, de, kf;
+    // per-element scratch of the pipeline, kept in the context (grown on demand)
+    DevBuf &fr = ctx->d_shFr, &gp = ctx->d_shGp, &de = ctx->d_shDe, &kf = ctx->d_shKf;
     int rc;
-    if ((rc = dev_alloc(ctx, fr, sizeof(ShellFrame) * (size_t)maxc))) return rc;
-    if ((rc = dev_alloc(ctx, gp, sizeof(ShellGP) * 4 * (size_t)maxc))) return rc;
-    if ((rc = dev_alloc(ctx, de, sizeof(double) * 4 * 32 * 9 * (size_t)maxc))) return rc;
-    if ((rc = dev_alloc(ctx, kf, sizeof(double) * 32 * 33 * (size_t)maxc))) return rc;
+    if (maxc > ctx->shScratchEls) {
+        if ((rc = dev_alloc(ctx, fr, sizeof(ShellFrame) * (size_t)maxc))) return rc;
+        if ((rc = dev_alloc(ctx, gp, sizeof(ShellGP) * 4 * (size_t)maxc))) return rc;
+        if ((rc = dev_alloc(ctx, de, sizeof(double) * 4 * 32 * 9 * (size_t)maxc))) return rc;
+        if ((rc = dev_alloc(ctx, kf, sizeof(double) * 32 * 33 * (size_t)maxc))) return rc;
+        ctx->shScratchEls = maxc;
+    }
     ShellPipe A = {};
     A.nodes = dptr<double>(ctx->d_nodes);
     A.elist = dptr<int>(ctx->d_elist);
@@ -140,20 +144,16 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
         k_shell_condense<<<(cnt + 63) / 64, 64, 0, s>>>(A);
     }
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    dev_free(fr);
-    dev_free(gp);
-    dev_free(de);
-    dev_free(kf);
+    if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);
     return cuda_check(ctx, e, "shell pipeline");
 }
 
 int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_loadInt, double *d_intLoad, int buildMat,
-                           double *d_ke, double *d_ru) {
+                           double *d_ke, double *d_ru, bool sync) {
     const bool toK = buildMat && !d_ke;
     return shell_pipeline(ctx, st, dptr<int>(ctx->d_colorEls), ctx->P.colorPtr, dptr<ShellProps>(ctx->d_secABD), kShellRt3,
                           d_loadInt, d_intLoad, buildMat, toK ? dptr<double>(ctx->d_K64) : nullptr,
-                          toK ? dptr<double>(ctx->d_intMat) : nullptr, d_ke, d_ru);
+                          toK ? dptr<double>(ctx->d_intMat) : nullptr, d_ke, d_ru, sync);
 }
 
 // Complex-step properties of the listed elements: orientation (real part), imaginary parts of
@@ -208,4 +208,73 @@ int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, dou
     dev_free(dl);
     dev_free(props);
     return rc;
+}
+
+// ---- internal-DOF recovery (updateExternalRHS / updateInternalSoln) ------------------------------
+// The condensed internal rows of each shell element (8 rows x 32 columns: the coupling K_in to the
+// 24 nodal DOF and the LU factors of K_ii, column-major as intElasticMat) stay on the device
+// after the last assembly.
+
+// ext -= K_ni K_ii^-1 int for the shells of one colour (they share no node, so the nodal
+// updates of a launch never collide).
+__global__ void k_shell_ext_rhs(int count, const int *__restrict__ els, const int *__restrict__ elist,
+                                const int *__restrict__ rank, const double *__restrict__ intMat,
+                                const double *__restrict__ intVec, double *__restrict__ extInt) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= count) return;
+    const int e = els[q];
+    const double *M = intMat + 256 * (size_t)e;
+    double L[8][8], b[8], x[8];
+    for (int r = 0; r < 8; ++r)
+        for (int c = 0; c < 8; ++c) L[r][c] = M[8 * (24 + c) + r];
+    for (int k = 0; k < 8; ++k) b[k] = intVec[8 * (size_t)e + k];
+    a_lu_solve<double, 8>(&L[0][0], b, x, 8);
+    const int *el = elist + 8 * (size_t)e;
+    for (int i = 0; i < 24; ++i) {  // component-major element DOF: i = 4 (var) + node
+        const int var = i / 4, a = i % 4;
+        double s = 0.0;
+        for (int k = 0; k < 8; ++k) s += M[8 * i + k] * x[k];
+        extInt[6 * (size_t)(rank[el[a] - 1] - 1) + var] -= s;
+    }
+}
+
+// int += K_ii^-1 (rhs - K_in ext), one thread per shell element.
+__global__ void k_shell_int_soln(int E, const int *__restrict__ elist, const int *__restrict__ rank,
+                                 const double *__restrict__ intMat, const double *__restrict__ extInt,
+                                 const double *__restrict__ intRhs, double *__restrict__ intSoln) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    const double *M = intMat + 256 * (size_t)e;
+    const int *el = elist + 8 * (size_t)e;
+    double L[8][8], b[8], x[8];
+    for (int r = 0; r < 8; ++r)
+        for (int c = 0; c < 8; ++c) L[r][c] = M[8 * (24 + c) + r];
+    for (int k = 0; k < 8; ++k) b[k] = intRhs ? intRhs[8 * (size_t)e + k] : 0.0;
+    for (int i = 0; i < 24; ++i) {
+        const int var = i / 4, a = i % 4;
+        const double u = extInt[6 * (size_t)(rank[el[a] - 1] - 1) + var];
+        for (int k = 0; k < 8; ++k) b[k] -= M[8 * i + k] * u;
+    }
+    a_lu_solve<double, 8>(&L[0][0], b, x, 8);
+    for (int k = 0; k < 8; ++k) intSoln[8 * (size_t)e + k] += x[k];
+}
+
+int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt) {
+    const AstroPrep &P = ctx->P;
+    for (int col = 0; col < P.ncolors; ++col) {
+        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+        if (!cnt) continue;
+        k_shell_ext_rhs<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
+            cnt, dptr<int>(ctx->d_colorEls) + P.colorPtr[col], dptr<int>(ctx->d_elist), dptr<int>(ctx->d_rank),
+            dptr<double>(ctx->d_intMat), d_intVec, d_extInt);
+    }
+    return cuda_check(ctx, cudaGetLastError(), "shell external rhs");
+}
+
+int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln, const double *d_intRhs) {
+    const int E = ctx->P.E;
+    k_shell_int_soln<<<(E + 127) / 128, 128, 0, ctx->stream>>>(E, dptr<int>(ctx->d_elist), dptr<int>(ctx->d_rank),
+                                                               dptr<double>(ctx->d_intMat), d_extInt, d_intRhs,
+                                                               d_intSoln);
+    return cuda_check(ctx, cudaGetLastError(), "shell internal solution");
 }

@@ -492,7 +492,8 @@ __global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *__re
 }
 
 // Start of a cycle: beta = ||r||, inv = 1/beta, g = [beta, 0...], j = 0.
-__global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, double targetAbs) {
+__global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, const double *targetAbsPtr) {
+    const double targetAbs = *targetAbsPtr;
     const int lane = threadIdx.x;
     double a = 0.0;
     a = lane_sum(part, nparts, 2, 0, lane);
@@ -561,7 +562,11 @@ __global__ void k_to_ell(const T *__restrict__ K, const int *__restrict__ rowPtr
 // ---------------------------------------------------------------------------------------------
 
 struct GmresWork {
-    DevBuf V, w0, w1, z0, z1, part, ctl, dinv, dinvT, rres, xs;
+    DevBuf V, w0, w1, z0, z1, part, ctl, dinv, dinvT, rres, xs, tgt;
+    // restart cycle captured as a graph, reused while the matrix and vectors stay the same
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const void *gK = nullptr, *gx = nullptr, *gb = nullptr;
     int n = 0, m = 0;
     size_t ld = 0;
     int nChunks = 0, nRowCtas = 0;
@@ -660,17 +665,27 @@ static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const d
     Op<TM> op = make_op<TM>(ctx, K);
     GmresCtl *ctl = dptr<GmresCtl>(W.ctl);
     double *part = dptr<double>(W.part);
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, dptr<TV>(W.w0), part, dptr<TV>(W.dinvT),
-                                                                 dptr<TV>(W.z0));
-    k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, tgtAbs);
-    enqueue_cycle<TM, TV, DPN>(ctx, W, op, m);
-    k_lsq<<<1, 1, 0, s>>>(ctl);
-    k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x);
-    CK(cudaStreamEndCapture(s, &graph));
-    CK(cudaGraphInstantiate(&exec, graph, 0));
+    // the absolute target is read by the graph from device memory
+    CK(cudaMemcpyAsync(W.tgt.p, &tgtAbs, sizeof(double), cudaMemcpyHostToDevice, s));
+    if (!(W.exec && W.gK == K && W.gx == x && W.gb == b)) {
+        if (W.exec) cudaGraphExecDestroy(W.exec);
+        if (W.graph) cudaGraphDestroy(W.graph);
+        W.exec = nullptr;
+        W.graph = nullptr;
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, dptr<TV>(W.w0), part, dptr<TV>(W.dinvT),
+                                                                     dptr<TV>(W.z0));
+        k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, dptr<double>(W.tgt));
+        enqueue_cycle<TM, TV, DPN>(ctx, W, op, m);
+        k_lsq<<<1, 1, 0, s>>>(ctl);
+        k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x);
+        CK(cudaStreamEndCapture(s, &W.graph));
+        CK(cudaGraphInstantiate(&W.exec, W.graph, 0));
+        W.gK = K;
+        W.gx = x;
+        W.gb = b;
+    }
+    cudaGraphExec_t exec = W.exec;
     int status = ASTRO_OK;
     struct {
         double resest;
@@ -690,8 +705,6 @@ static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const d
         if (hc.resest <= tgtAbs || hc.breakdown) break;
         if (cyc == maxCycles - 1) status = ASTRO_ERR_MAXIT;
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
     return status;
 }
 
@@ -715,12 +728,17 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
     if ((rc = dev_alloc(ctx, W.dinvT, (size_t)n * tv))) return rc;
     if ((rc = dev_alloc(ctx, W.rres, sizeof(double) * (size_t)n))) return rc;
     if ((rc = dev_alloc(ctx, W.xs, sizeof(float) * (size_t)n))) return rc;
+    if ((rc = dev_alloc(ctx, W.tgt, sizeof(double)))) return rc;
     CK(cudaMemsetAsync(W.ctl.p, 0, sizeof(GmresCtl), ctx->stream));
     return ASTRO_OK;
 }
 
 static void work_free(GmresWork &W) {
-    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.z0, &W.z1, &W.part, &W.ctl, &W.dinv, &W.dinvT, &W.rres, &W.xs};
+    if (W.exec) cudaGraphExecDestroy(W.exec);
+    if (W.graph) cudaGraphDestroy(W.graph);
+    W.exec = nullptr;
+    W.graph = nullptr;
+    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.z0, &W.z1, &W.part, &W.ctl, &W.dinv, &W.dinvT, &W.rres, &W.xs, &W.tgt};
     for (auto *x : b) dev_free(*x);
 }
 
@@ -876,5 +894,131 @@ int krylov_apply(astro_ctx *ctx, int kind, const double *d_x, double *d_y) {
     else rc = true_residual<6>(ctx, W, kind, d_x, dptr<double>(zb), &rel, d_y);
     dev_free(zb);
     dev_free(W.part);
+    return rc;
+}
+
+// ---- implicit Newmark time stepping (solve, dynamic branch) --------------------------------------
+
+namespace {
+
+__global__ void k_axpy(int n, double a, const double *__restrict__ x, double *__restrict__ y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+
+// acc = c1 (c2 (u - u_p - dt v_p) - (1 - 2 beta) a_p), vel = v_p + dt ((1 - gamma) a_p + gamma acc),
+// then the previous state takes the new one (Working/AStrO_commandFunctions.f90:798-809)
+__global__ void k_newmark_update(int n, double c1, double c2, double dt, double beta, double gamma,
+                                 const double *__restrict__ u, double *__restrict__ up, double *__restrict__ vp,
+                                 double *__restrict__ ap) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double acc = c1 * (c2 * (u[i] - up[i] - dt * vp[i]) - (1.0 - 2.0 * beta) * ap[i]);
+    const double vel = vp[i] + dt * ((1.0 - gamma) * ap[i] + gamma * acc);
+    up[i] = u[i];
+    vp[i] = vel;
+    ap[i] = acc;
+}
+
+}  // namespace
+
+// Time loop on the device.  K_eff = K + c1 c2 M is assembled and the constraints scaled before the
+// call; every step forms the residual with the Newmark inertia at the current state, adds the
+// applied load amp[step] * pattern and the constraint load, condenses the internal DOF, solves
+// K_eff du = r by FP64 Jacobi-GMRES warm-started from the previous increment (as the reference's
+// gMRes), recovers the internal DOF, updates u and the Newmark state.  All vectors are device
+// buffers in internal layout; the displacement of every step can be written to hist (reference
+// numbering).
+int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,
+                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup, double *d_hist,
+                   astro_solve_stats *st) {
+    const AstroPrep &P = ctx->P;
+    const int n = P.n, ni = P.intVecSize;
+    if (P.dpn != 6) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark stepping is implemented for shell4 meshes");
+    const int m = o->restart > 0 ? std::min(o->restart, kMaxM) : 50;
+    const int maxCycles = o->max_iters > 0 ? (o->max_iters + m - 1) / m : 200;
+    const double rtol = o->rtol > 0 ? o->rtol : 1e-10;
+    const double beta = o->nm_beta, gamma = o->nm_gamma, dt = o->del_t;
+    const double c1 = 0.5 / beta, c2 = 2.0 / (dt * dt);
+    GmresWork W;
+    DevBuf load, iload, du;
+    int rc = work_alloc(ctx, W, m, sizeof(double));
+    if (!rc) rc = dev_alloc(ctx, load, sizeof(double) * n);
+    if (!rc) rc = dev_alloc(ctx, du, sizeof(double) * n);
+    if (!rc && ni) rc = dev_alloc(ctx, iload, sizeof(double) * ni);
+    const double *K = rc ? nullptr : ell_of<double>(ctx, &rc);
+    cudaStream_t s = ctx->stream;
+    int iters = 0, cycles = 0, worst = ASTRO_OK;
+    double worstRel = 0.0;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    if (!rc) {
+        k_dinv<double, double><<<(P.N + 255) / 256, 256, 0, s>>>(
+            dptr<double>(ctx->d_K64), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), P.N, P.dpn,
+            ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
+            dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<double>(W.dinvT));
+        rc = cuda_check(ctx, cudaMemsetAsync(du.p, 0, sizeof(double) * n, s), "newmark init");
+    }
+    ShellDevState ds;
+    ds.disp = d_u;
+    ds.pdisp = d_up;
+    ds.pvel = d_vp;
+    ds.pacc = d_ap;
+    ds.idisp = d_iu;
+    ds.pidisp = d_iup;
+    ds.dynamic = 1;
+    ds.beta = beta;
+    ds.gamma = gamma;
+    ds.delT = dt;
+    const int grid = (n + 255) / 256;
+    for (int step = 0; step < o->num_steps && !rc; ++step) {
+        CK(cudaMemsetAsync(load.p, 0, sizeof(double) * n, s));
+        if (ni) CK(cudaMemsetAsync(iload.p, 0, sizeof(double) * ni, s));
+        // getElasticSolnLoad(0): load -= Ru (with the Newmark inertia at the current state)
+        if ((rc = launch_shell4_assemble(ctx, ds, dptr<double>(load), ni ? dptr<double>(iload) : nullptr, 0, nullptr,
+                                         nullptr, false)))
+            break;
+        if (d_pattern && h_amp) k_axpy<<<grid, 256, 0, s>>>(n, h_amp[step], d_pattern, dptr<double>(load));
+        if ((rc = constraint_load_dev(ctx, d_u, dptr<double>(load)))) break;
+        if (ni && (rc = shell4_update_external_rhs(ctx, dptr<double>(iload), dptr<double>(load)))) break;
+        double rel = 0.0, rn = 0.0, bn = 0.0;
+        if ((rc = true_residual<6>(ctx, W, 64, nullptr, dptr<double>(load), &rel, dptr<double>(W.rres), &rn, &bn)))
+            break;
+        double est = 0.0;
+        int grc = gmres_solve<double, double, 6>(ctx, W, K, dptr<double>(du), dptr<double>(load), rtol * bn, maxCycles, m,
+                                                 &iters, &cycles, &est);
+        if (grc == ASTRO_ERR_NAN) {
+            rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the Newmark step solve");
+            break;
+        }
+        if (grc != ASTRO_OK) worst = grc;
+        if (bn > 0.0) worstRel = std::max(worstRel, est / bn);
+        if (ni && (rc = shell4_update_internal_soln(ctx, dptr<double>(du), d_iu, dptr<double>(iload)))) break;
+        k_axpy<<<grid, 256, 0, s>>>(n, 1.0, dptr<double>(du), d_u);
+        k_newmark_update<<<grid, 256, 0, s>>>(n, c1, c2, dt, beta, gamma, d_u, d_up, d_vp, d_ap);
+        if (ni) CK(cudaMemcpyAsync(d_iup, d_iu, sizeof(double) * ni, cudaMemcpyDeviceToDevice, s));
+        if (d_hist && (rc = int_to_ref_vec(ctx, d_u, d_hist + (size_t)step * n, n))) break;
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "newmark step"))) break;
+    }
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    work_free(W);
+    dev_free(load);
+    dev_free(iload);
+    dev_free(du);
+    if (st) {
+        st->iterations = iters;
+        st->restarts = cycles;
+        st->refinements = 0;
+        st->status = rc ? rc : worst;
+        st->rel_residual = worstRel;
+        st->seconds = ms * 1e-3;
+    }
     return rc;
 }

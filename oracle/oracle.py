@@ -45,6 +45,8 @@ def _lib():
                                     F64P, F64P, F64P, F64P]
         L.orc_element_matrices.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, F64P]
         L.orc_drdd_complex.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p, F64P, F64P]
+        L.orc_update_external_rhs.argtypes = [C.c_void_p, F64P, F64P, F64P]
+        L.orc_update_internal_soln.argtypes = [C.c_void_p, F64P, F64P, F64P, F64P]
         L.orc_el_soln_load.argtypes = [C.c_void_p, C.c_int, C.c_void_p, F64P, F64P, F64P, I32P, F64P]
         L.orc_scale_mpc.argtypes = [F64P, C.c_int, F64P, F64P, I32P, C.c_int]
         L.orc_constraint_load.argtypes = [F64P, I32P, I32P, F64P, C.c_int, F64P, F64P]
@@ -124,6 +126,19 @@ class Oracle:
                                   _d(rr), _d(ri), kr.ctypes.data_as(F64P), ki.ctypes.data_as(F64P))
         assert rc == 0
         return rr + 1j * ri, kr + 1j * ki
+
+    def update_external_rhs(self, ext_vec, int_vec, int_mat):
+        out = np.ascontiguousarray(ext_vec, np.float64).copy()
+        self.L.orc_update_external_rhs(self.h, _d(out), _d(np.ascontiguousarray(int_vec, np.float64)),
+                                       _d(np.ascontiguousarray(int_mat, np.float64)))
+        return out
+
+    def update_internal_soln(self, ext_soln, int_soln, int_rhs, int_mat):
+        out = np.ascontiguousarray(int_soln, np.float64).copy()
+        rhs = None if int_rhs is None else _d(np.ascontiguousarray(int_rhs, np.float64))
+        self.L.orc_update_internal_soln(self.h, _d(np.ascontiguousarray(ext_soln, np.float64)), _d(out), rhs,
+                                        _d(np.ascontiguousarray(int_mat, np.float64)))
+        return out
 
     def drdd_complex(self, dvar, h=1e-14, state=None):
         """getdRelasticdD element part: (dRu/dd in global DOF, dRu/dd at the internal DOF)."""

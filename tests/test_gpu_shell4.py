@@ -109,3 +109,23 @@ def test_shell_newmark_dynamic_state(plate):
     assert np.linalg.norm(iload - oiload) <= 1e-11 * np.linalg.norm(oiload)
     assert np.array_equal(cols, ocols)
     assert np.abs(mat - omat).max() <= 1e-11 * np.abs(omat).max()
+
+
+def test_internal_dof_recovery(plate):
+    """updateExternalRHS / updateInternalSoln on the GPU against the oracle, from the condensed
+    internal rows of the last assembly (1e-11 relative)."""
+    m, g, o = plate
+    g.getElasticSolnLoad(1)
+    _, _, _, _, imat = o.el_soln_load(1)
+    rng = np.random.default_rng(12)
+    ext, iv = rng.standard_normal(o.n), rng.standard_normal(o.int_vec_size)
+    e_g = g.updateExternalRHS(ext, iv)
+    e_o = o.update_external_rhs(ext, iv, imat)
+    assert np.linalg.norm(e_g - e_o) <= 1e-11 * np.linalg.norm(e_o)
+    i0, rhs = rng.standard_normal(o.int_vec_size), rng.standard_normal(o.int_vec_size)
+    s_g = g.updateInternalSoln(ext, i0, rhs)
+    s_o = o.update_internal_soln(ext, i0, rhs, imat)
+    assert np.linalg.norm(s_g - s_o) <= 1e-11 * np.linalg.norm(s_o)
+    s_g0 = g.updateInternalSoln(ext, i0)
+    s_o0 = o.update_internal_soln(ext, i0, None, imat)
+    assert np.linalg.norm(s_g0 - s_o0) <= 1e-11 * np.linalg.norm(s_o0)

@@ -179,3 +179,39 @@ def test_complex_step_matches_central_difference(kind):
         assert np.linalg.norm(cs - fd) <= 1e-5 * np.linalg.norm(fd)
         if o.int_vec_size:
             assert np.linalg.norm(ics - ifd) <= 1e-5 * np.linalg.norm(ifd)
+
+
+def test_static_condensation_round_trip():
+    """Condensed solve + internal-DOF recovery (updateExternalRHS / updateInternalSoln with the
+    intended loop bounds) equals the solve of the full nodal + incompatible-mode system assembled
+    from the uncondensed element matrices."""
+    import scipy.sparse as sp
+    m = M.plate_shell(nx=4, ny=3, lx=2.0, ly=1.0, t=0.03, E=7e10, nu=0.33)
+    o = Oracle(m)
+    n, ni = o.n, o.int_vec_size
+    load, iload, mat, cols, imat = o.el_soln_load(1)
+    mm, mr = o.scale_mpc(mat)
+    Cm = o.mpc_scipy(mm)
+    rows, cls, vals = [], [], []
+    for el in range(1, m.num_els + 1):
+        _, K = o.element(el, 1)
+        dofs = []
+        for i in range(24):
+            comp, lnd = i // 4 + 1, i % 4 + 1
+            nd = int(m.element_list[el - 1, lnd - 1])
+            dofs.append(int(o.n_dof_index[nd - 1, comp - 1]) - 1)
+        dofs += [n + 8 * (el - 1) + k for k in range(8)]   # intVecRange: 8 incompatible modes per shell
+        for a in range(32):
+            for b in range(32):
+                rows.append(dofs[a]); cls.append(dofs[b]); vals.append(K[a, b])
+    Kf = sp.csr_matrix((vals, (rows, cls)), shape=(n + ni, n + ni))
+    P = sp.bmat([[Cm.T @ Cm, None], [None, sp.csr_matrix((ni, ni))]])
+    rng = np.random.default_rng(6)
+    f, g = rng.standard_normal(n), rng.standard_normal(ni)
+    full = spla.spsolve((Kf + P).tocsc(), np.concatenate([f, g]))
+    rhs = o.update_external_rhs(f, g, imat)
+    A = (o.csr_scipy(mat, cols) + Cm.T @ Cm).tocsc()
+    u = spla.spsolve(A, rhs)
+    a = o.update_internal_soln(u, np.zeros(ni), g, imat)
+    assert np.linalg.norm(u - full[:n]) <= 1e-8 * np.linalg.norm(full[:n])
+    assert np.linalg.norm(a - full[n:]) <= 1e-8 * np.linalg.norm(full[n:])
