@@ -3,6 +3,9 @@
 // scaling (scaleElasticMPC, :537-566), vector layout changes between the reference's
 // component-major DOF numbering and the rank-major device layout, and the consistent surface
 // load (intended semantics of r_getElSurfaceTraction, Working/AStrO_r_elementEqns.f90:1923-2018).
+#include <algorithm>
+#include <vector>
+
 #include "astro_internal.h"
 
 namespace {
@@ -56,32 +59,42 @@ __global__ void int_to_ref_kernel(const double *__restrict__ in, double *__restr
 }
 
 // getElasticConstraintLoad (Working/AStrO_commandFunctions.f90:506-535): load += C^T (rhs - C u)
-// with the scaled constraints in internal numbering (col < 0: empty slot).  The row residuals are
-// formed in parallel, the scatter runs in the reference's row and term order (one thread: the
-// constraint set is small and its rows may share DOF).
-__global__ void constraint_load_kernel(int mdim, const int *__restrict__ range, const int *__restrict__ col,
+// with the scaled constraints in internal numbering (col < 0: empty slot).  First the row
+// residuals t = rhs - C u (thread per row), then the scatter as a gather per target DOF: gPtr/gTerm
+// list, for each constrained DOF gRow[g], its terms in the reference's row-and-term order.
+__global__ void constraint_rows_kernel(int mdim, const int *__restrict__ range, const int *__restrict__ col,
                                        const double *__restrict__ val, const double *__restrict__ rhs,
-                                       const double *__restrict__ u, double *__restrict__ t, double *__restrict__ load) {
-    for (int r = threadIdx.x; r < mdim; r += blockDim.x) {
-        double s = rhs[r];
-        if (u)
-            for (int k = range[r]; k < range[r + 1]; ++k)
-                if (col[k] >= 0) s -= val[k] * u[col[k]];
-        t[r] = s;
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    for (int r = 0; r < mdim; ++r)
+                                       const double *__restrict__ u, double *__restrict__ t) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= mdim) return;
+    double s = rhs[r];
+    if (u)
         for (int k = range[r]; k < range[r + 1]; ++k)
-            if (col[k] >= 0) load[col[k]] += val[k] * t[r];
+            if (col[k] >= 0) s -= val[k] * u[col[k]];
+    t[r] = s;
+}
+__global__ void constraint_gather_kernel(int ng, const int *__restrict__ gPtr, const int *__restrict__ gTerm,
+                                         const int *__restrict__ gRow, const int *__restrict__ termRow,
+                                         const double *__restrict__ val, const double *__restrict__ t,
+                                         double *__restrict__ load) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    double s = load[gRow[g]];
+    for (int q = gPtr[g]; q < gPtr[g + 1]; ++q) {
+        const int k = gTerm[q];
+        s += val[k] * t[termRow[k]];
+    }
+    load[gRow[g]] = s;
 }
 
-// Consistent face load.  One thread per face; faces of one call may share nodes, so the
-// contributions go through FP64 atomics (the load is a one-off right-hand side).
+// Consistent face load.  One thread per face forms the face's nodal forces (summed over its
+// Gauss points) and their target rows; faces of one call may share nodes, so a second kernel adds
+// them into the load in face order (deterministic).
 __global__ void surface_load_kernel(const double *__restrict__ nodes, const int *__restrict__ elist,
                                     const int *__restrict__ etype, const int *__restrict__ rank, int nf,
                                     const int *__restrict__ faceEl, const int *__restrict__ faceNum, double t0,
-                                    double t1, double t2, double pressure, int dpn, double *__restrict__ loadInt) {
+                                    double t1, double t2, double pressure, int dpn, double *__restrict__ fval,
+                                    int *__restrict__ frow) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= nf) return;
     const int hexF[6][4] = {{4, 3, 2, 1}, {5, 6, 7, 8}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {4, 1, 5, 8}};
@@ -105,6 +118,7 @@ __global__ void surface_load_kernel(const double *__restrict__ nodes, const int 
     const double inv = 1.0 / sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
     const double tr[3] = {t0 - pressure * nv[0] * inv, t1 - pressure * nv[1] * inv, t2 - pressure * nv[2] * inv};
     const double g = 0.57735026918962576451;
+    double acc[4][3] = {};
     for (int gp = 0; gp < 4; ++gp) {
         const double s = (gp & 1) ? g : -g, r = (gp & 2) ? g : -g;
         const double N_[4] = {0.25 * (1 - s) * (1 - r), 0.25 * (1 + s) * (1 - r), 0.25 * (1 + s) * (1 + r),
@@ -119,12 +133,35 @@ __global__ void surface_load_kernel(const double *__restrict__ nodes, const int 
             }
         const double cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
         const double dA = sqrt(cx * cx + cy * cy + cz * cz);
-        for (int k = 0; k < 4; ++k) {
-            const int rr = rank[nd[k] - 1] - 1;
-            for (int d = 0; d < 3; ++d) atomicAdd(loadInt + (size_t)rr * dpn + d, tr[d] * N_[k] * dA);
-        }
+        for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d) acc[k][d] += tr[d] * N_[k] * dA;
+    }
+    for (int k = 0; k < 4; ++k) {
+        frow[4 * f + k] = (rank[nd[k] - 1] - 1) * dpn;
+        for (int d = 0; d < 3; ++d) fval[12 * f + 3 * k + d] = acc[k][d];
     }
 }
+
+// adds the face forces into the load, one thread per target node, in face order (gPtr/gSlot list
+// for node row gRow[g] its (face, corner) slots f*4 + k in increasing face order)
+__global__ void face_gather_kernel(int ng, const int *__restrict__ gPtr, const int *__restrict__ gSlot,
+                                   const int *__restrict__ gRow, const double *__restrict__ fval,
+                                   double *__restrict__ loadInt) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    const int row = gRow[g];
+    double s0 = loadInt[row], s1 = loadInt[row + 1], s2 = loadInt[row + 2];
+    for (int q = gPtr[g]; q < gPtr[g + 1]; ++q) {
+        const int sl = gSlot[q];
+        s0 += fval[3 * sl];
+        s1 += fval[3 * sl + 1];
+        s2 += fval[3 * sl + 2];
+    }
+    loadInt[row] = s0;
+    loadInt[row + 1] = s1;
+    loadInt[row + 2] = s2;
+}
+
 
 }  // namespace
 
@@ -169,9 +206,13 @@ int constraint_load_dev(astro_ctx *ctx, const double *d_u, double *d_loadInt) {
     const int md = ctx->P.mpcDim;
     if (md == 0) return ASTRO_OK;
     if (!ctx->d_mpcVal.p) return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run first");
-    constraint_load_kernel<<<1, 256, 0, ctx->stream>>>(md, dptr<int>(ctx->d_mpcRange), dptr<int>(ctx->d_mpcCol),
-                                                      dptr<double>(ctx->d_mpcVal), dptr<double>(ctx->d_mpcRhs), d_u,
-                                                      dptr<double>(ctx->d_mpcT), d_loadInt);
+    constraint_rows_kernel<<<(md + 255) / 256, 256, 0, ctx->stream>>>(
+        md, dptr<int>(ctx->d_mpcRange), dptr<int>(ctx->d_mpcCol), dptr<double>(ctx->d_mpcVal), dptr<double>(ctx->d_mpcRhs),
+        d_u, dptr<double>(ctx->d_mpcT));
+    const int ng = ctx->mpcTargets;
+    constraint_gather_kernel<<<(ng + 255) / 256, 256, 0, ctx->stream>>>(
+        ng, dptr<int>(ctx->d_mpcGPtr), dptr<int>(ctx->d_mpcGTerm), dptr<int>(ctx->d_mpcGRow), dptr<int>(ctx->d_mpcTermRow),
+        dptr<double>(ctx->d_mpcVal), dptr<double>(ctx->d_mpcT), d_loadInt);
     return cuda_check(ctx, cudaGetLastError(), "constraint load");
 }
 
@@ -188,8 +229,45 @@ int int_to_ref_vec(astro_ctx *ctx, const double *d_int, double *d_ref, int n) {
 int surface_load_dev(astro_ctx *ctx, int nf, const int *d_faceEl, const int *d_faceNum, const double *tr,
                      double pressure, double *d_loadInt) {
     if (nf <= 0) return ASTRO_OK;
+    DevBuf fv, fr;
+    int rc;
+    if ((rc = dev_alloc(ctx, fv, sizeof(double) * 12 * (size_t)nf))) return rc;
+    if ((rc = dev_alloc(ctx, fr, sizeof(int) * 4 * (size_t)nf))) {
+        dev_free(fv);
+        return rc;
+    }
     surface_load_kernel<<<(nf + 127) / 128, 128, 0, ctx->stream>>>(
-        dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist), dptr<int>(ctx->d_etype),
-        dptr<int>(ctx->d_rank), nf, d_faceEl, d_faceNum, tr[0], tr[1], tr[2], pressure, ctx->P.dpn, d_loadInt);
-    return cuda_check(ctx, cudaGetLastError(), "surface_load");
+        dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist), dptr<int>(ctx->d_etype), dptr<int>(ctx->d_rank), nf,
+        d_faceEl, d_faceNum, tr[0], tr[1], tr[2], pressure, ctx->P.dpn, dptr<double>(fv), dptr<int>(fr));
+    // gather lists: the (face, corner) slots of every target row, in face order
+    std::vector<int> hrow(4 * (size_t)nf);
+    cudaError_t e = cudaMemcpyAsync(hrow.data(), fr.p, sizeof(int) * hrow.size(), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    DevBuf gp, gs, gr;
+    if (e == cudaSuccess) {
+        std::vector<int> order(hrow.size());
+        for (size_t q = 0; q < order.size(); ++q) order[q] = (int)q;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hrow[a] < hrow[b]; });
+        std::vector<int> ptr(1, 0), row;
+        for (size_t q = 0; q < order.size(); ++q) {
+            if (q == 0 || hrow[order[q]] != hrow[order[q - 1]]) {
+                if (q) ptr.push_back((int)q);
+                row.push_back(hrow[order[q]]);
+            }
+        }
+        ptr.push_back((int)order.size());
+        const int ng = (int)row.size();
+        if (!(rc = upload(ctx, gp, ptr.data(), sizeof(int) * ptr.size())) &&
+            !(rc = upload(ctx, gs, order.data(), sizeof(int) * order.size())) &&
+            !(rc = upload(ctx, gr, row.data(), sizeof(int) * row.size()))) {
+            face_gather_kernel<<<(ng + 127) / 128, 128, 0, ctx->stream>>>(ng, dptr<int>(gp), dptr<int>(gs), dptr<int>(gr),
+                                                                         dptr<double>(fv), d_loadInt);
+            e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        }
+    }
+    DevBuf *bufs[] = {&fv, &fr, &gp, &gs, &gr};
+    for (auto *b : bufs) dev_free(*b);
+    if (rc) return rc;
+    return cuda_check(ctx, e, "surface_load");
 }

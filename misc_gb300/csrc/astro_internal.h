@@ -97,6 +97,8 @@ struct astro_ctx {
     int shScratchEls = 0;
     // constraints on device (internal DOF numbering)
     DevBuf d_mpcRange, d_mpcCol, d_mpcVal, d_mpcRhs, d_mpcT;  // scaled, after astro_scale_mpc
+    DevBuf d_mpcGPtr, d_mpcGTerm, d_mpcGRow, d_mpcTermRow;      // constraint load gather lists
+    int mpcTargets = 0;
     int mpcScaled = 0;
     // penalty C^T C as CSR over internal rows (host-built after scaling)
     DevBuf d_penRow, d_penPtr, d_penCol, d_penVal;

@@ -60,7 +60,7 @@ static void free_all(astro_ctx *c) {
     DevBuf *bufs[] = {&c->d_nodes,  &c->d_elist,   &c->d_elMat,   &c->d_esec,    &c->d_secABD,   &c->d_secOrient,
                       &c->d_colorEls, &c->d_elBlk, &c->d_rank,    &c->d_bRowPtr, &c->d_bCol,     &c->d_bRow,
                       &c->d_etype,  &c->d_elFirst, &c->d_K64p, &c->d_K32p, &c->d_ellCol, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
-                      &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs, &c->d_mpcT, &c->d_penRow,
+                      &c->d_intMat, &c->d_mpcRange, &c->d_mpcCol, &c->d_mpcVal,  &c->d_mpcRhs, &c->d_mpcT, &c->d_mpcGPtr, &c->d_mpcGTerm, &c->d_mpcGRow, &c->d_mpcTermRow, &c->d_penRow,
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
                       &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_elXdf, &c->d_elCdf, &c->d_ioRef,
@@ -765,6 +765,30 @@ extern "C" int astro_scale_mpc(astro_ctx *ctx, double *mpc_mat, double *mpc_rhs)
         if ((rc = upload(ctx, ctx->d_mpcRhs, ctx->mpcRhsScaledHost.data(), sizeof(double) * ctx->mpcRhsScaledHost.size())))
             return rc;
         if ((rc = dev_alloc(ctx, ctx->d_mpcT, sizeof(double) * P.mpcDim))) return rc;
+        // gather lists of the constraint load: the terms of every constrained DOF in row order
+        std::vector<int> termRow(colInt.size()), order;
+        for (int r = 0; r < P.mpcDim; ++r)
+            for (int k = P.mpcRange[r]; k < P.mpcRange[r + 1]; ++k) {
+                termRow[k] = r;
+                if (colInt[k] >= 0) order.push_back(k);
+            }
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return colInt[a] < colInt[b]; });
+        std::vector<int> gptr(1, 0), grow;
+        for (size_t q = 0; q < order.size(); ++q)
+            if (q == 0 || colInt[order[q]] != colInt[order[q - 1]]) {
+                if (q) gptr.push_back((int)q);
+                grow.push_back(colInt[order[q]]);
+            }
+        gptr.push_back((int)order.size());
+        ctx->mpcTargets = (int)grow.size();
+        if ((rc = upload(ctx, ctx->d_mpcGPtr, gptr.data(), sizeof(int) * gptr.size()))) return rc;
+        if (order.empty()) {
+            order.push_back(0);  // placeholders, never read (no target)
+            grow.push_back(0);
+        }
+        if ((rc = upload(ctx, ctx->d_mpcGTerm, order.data(), sizeof(int) * order.size()))) return rc;
+        if ((rc = upload(ctx, ctx->d_mpcGRow, grow.data(), sizeof(int) * grow.size()))) return rc;
+        if ((rc = upload(ctx, ctx->d_mpcTermRow, termRow.data(), sizeof(int) * termRow.size()))) return rc;
     }
     ctx->mpcScaled = 1;
     if (mpc_mat) std::copy(ctx->mpcScaledHost.begin(), ctx->mpcScaledHost.end(), mpc_mat);

@@ -341,13 +341,12 @@ template <> struct FastCfg<float> {
     static constexpr bool PREFETCH = true;
 };
 template <class T> struct Hex8FastArgs {
-    const double *nodes;
-    const int *elist;
     const int *colorEls;
     int count;
     const int *elBlk;
     const unsigned long long *elFirst;
-    const double *elC;     // (E,9) orthotropic C
+    const float2 *Xdf;     // (E,8,3) node coordinates in the section frame, double-float (high parts used)
+    const float2 *Cdf;     // (E,9) orthotropic C, double-float (high parts used)
     const double *orient;  // (E,9) column-major section orientation (used when ROT)
     T *K;                  // BSR values or null
     double *keOut;         // element matrices (E,24,24) column-major, element DOF order, or null
@@ -433,16 +432,10 @@ __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fa
             if (A.K && grp < 3 && j < 64 && !((first >> j) & 1ull)) ov[st] = A.K[9 * (size_t)sBlk[w][j] + qq];
         }
     }
-    // Jacobian at Gauss point gp = lane/4 from nodes 2s, 2s+1 (s = lane%4), in the section frame
+    // Jacobian at Gauss point gp = lane/4 from nodes 2s, 2s+1 (s = lane%4), from the node
+    // coordinates in the section frame (single-precision parts of the double-float copy)
     {
         const int gp = lane >> 2, s = lane & 3;
-        T Or[3][3];
-        if (ROT) {
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) Or[i][j] = (T)A.orient[9 * (size_t)e + 3 * j + i];
-        }
         const T gq = (T)kRt3, eighth = T(0.125);
         const T s1 = (gp & 1) ? gq : -gq, s2 = (gp & 2) ? gq : -gq, s3 = (gp & 4) ? gq : -gq;
         T J[9], n[2][3];
@@ -451,18 +444,9 @@ __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fa
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const int a = 2 * s + k;
-            const int na = A.elist[8 * (size_t)e + a];
-            T X0 = (T)A.nodes[3 * (size_t)(na - 1)], X1 = (T)A.nodes[3 * (size_t)(na - 1) + 1],
-              X2 = (T)A.nodes[3 * (size_t)(na - 1) + 2];
-            if (ROT) {
-                const T y0 = Or[0][0] * X0 + Or[0][1] * X1 + Or[0][2] * X2;
-                const T y1 = Or[1][0] * X0 + Or[1][1] * X1 + Or[1][2] * X2;
-                const T y2 = Or[2][0] * X0 + Or[2][1] * X1 + Or[2][2] * X2;
-                X0 = y0;
-                X1 = y1;
-                X2 = y2;
-            }
-            const T sa = (a == 1 || a == 2 || a == 5 || a == 6) ? T(1) : T(-1);
+            const float2 *xp = A.Xdf + 24 * (size_t)e + 3 * a;
+            const T X0 = xp[0].x, X1 = xp[1].x, X2 = xp[2].x;
+        const T sa = (a == 1 || a == 2 || a == 5 || a == 6) ? T(1) : T(-1);
             const T ta = (a == 2 || a == 3 || a == 6 || a == 7) ? T(1) : T(-1);
             const T ua = (a >= 4) ? T(1) : T(-1);
             n[k][0] = eighth * sa * (T(1) + ta * s2) * (T(1) + ua * s3);
@@ -496,16 +480,16 @@ __global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fa
     pair_moments(sG[w], a0, a1, b, M0, M1);
     OrthoC<T> c;
     {
-        const double *cp = A.elC + 9 * (size_t)e;
-        c.C11 = (T)cp[0];
-        c.C12 = (T)cp[1];
-        c.C13 = (T)cp[2];
-        c.C22 = (T)cp[3];
-        c.C23 = (T)cp[4];
-        c.C33 = (T)cp[5];
-        c.C44 = (T)cp[6];
-        c.C55 = (T)cp[7];
-        c.C66 = (T)cp[8];
+        const float2 *cp = A.Cdf + 9 * (size_t)e;
+        c.C11 = cp[0].x;
+        c.C12 = cp[1].x;
+        c.C13 = cp[2].x;
+        c.C22 = cp[3].x;
+        c.C23 = cp[4].x;
+        c.C33 = cp[5].x;
+        c.C44 = cp[6].x;
+        c.C55 = cp[7].x;
+        c.C66 = cp[8].x;
     }
     T K0[9], K1[9];
     ortho_block<T>(c, M0, K0);
@@ -824,13 +808,12 @@ template <class T, bool ROT> static void hex8_fast_launch(astro_ctx *ctx, const 
 // prior zeroing) and/or the element matrices d_ke.
 template <class T> static int hex8_fast_run(astro_ctx *ctx, T *K, double *d_ke) {
     Hex8FastArgs<T> A;
-    A.nodes = dptr<double>(ctx->d_nodes);
-    A.elist = dptr<int>(ctx->d_elist);
     A.colorEls = nullptr;
     A.count = 0;
     A.elBlk = dptr<int>(ctx->d_elBlk);
     A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
-    A.elC = dptr<double>(ctx->d_elC);
+    A.Xdf = dptr<float2>(ctx->d_elXdf);
+    A.Cdf = dptr<float2>(ctx->d_elCdf);
     A.orient = dptr<double>(ctx->d_secOrient);
     A.K = K;
     A.keOut = d_ke;
