@@ -29,6 +29,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+TRAFFIC_PER_PASS = 284929792  # bytes, see the roofline comment in run_ours
 METRIC = "element mats/s (64x32x32 brick8 block: element eval + assembly); s to 1e-10 FP64 rel resid"
 UNIT = "elements/s"
 
@@ -251,14 +252,21 @@ def run_ours(a):
     nnz = g.dims.num_blocks * 9
     alg_bytes = nnz * 4 + m.num_nodes * 24 + E * (8 * 4 + 9 * 8)
     achieved = alg_bytes / (ms_step * 1e-3) / 1e9
+    # DRAM bytes (read + write) of the 8 colour launches of one FP32 assembly pass, measured by ncu
+    # with the caches flushed before every launch (the assembly kernel's ncu summary under
+    # profiles/); only for the default 64x32x32 block
+    traffic = TRAFFIC_PER_PASS if (a.nx, a.ny, a.nz) == (64, 32, 32) else None
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic", "config": _config(a),
             "e2e": {"value": E / e2e_dt, "unit": UNIT, "path": "astro_el_soln_load FP64 with host buffers",
-                    "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": n * 8 + g.el_mat_size * 12},
+                    "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8 + g.el_mat_size * 12,
+                    "note": "state is the undeformed one (all-zero displacement is not copied); copied per call: "
+                            "the load vector in, the load, CSR values and CSR columns out"},
             "gpu_launches": a.steps * g.dims.num_colors,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": None, "kernel": "hex8_kernel<float> (8 colour launches = 1 assembly pass)",
+                         "traffic": traffic, "traffic_note": "ncu, caches flushed before each colour launch",
+                         "kernel": "hex8_fast_kernel<float> (8 colour launches = 1 assembly pass)",
                          "algorithmic_bytes": alg_bytes, "peak_source": "measured" if peaks else "fallback"},
             "clocks": clocks, "wall_s": wall}
     if not a.no_solve and rank == 0:
