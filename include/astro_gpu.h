@@ -101,16 +101,37 @@ typedef struct astro_state {
     double nm_beta, nm_gamma, del_t;
 } astro_state;
 
+/* Polynomial graph-convolution preconditioner of the learned solver (no counterpart in the
+ * reference, whose gMRes is preconditioned by a diagonal).  With D the diagonal of
+ * A = K + C^T C, lambda = lambda_scale times a power-iteration estimate of the largest
+ * eigenvalue of D^-1 A, and xi(mu) = (2 mu / lambda - (1 + 1/ratio)) / (1 - 1/ratio) the map
+ * of [lambda/ratio, lambda] onto [-1, 1], the preconditioner is
+ *     P v = (1/lambda) sum_{k=0..degree} W_k T_k(xi(D^-1 A)) D^-1 v
+ * with T_k the Chebyshev polynomials (one sparse matrix-vector product per hop) and W_k one
+ * dpn x dpn weight per hop, shared by all nodes: a linear graph network on the mesh whose node
+ * features are the DOF of a node.  weights[(k * dpn + i) * dpn + j] = W_k[i][j]. */
+#define ASTRO_PRECOND_MAX_DEGREE 16
+typedef struct astro_precond {
+    int32_t degree;          /* 1..ASTRO_PRECOND_MAX_DEGREE */
+    int32_t dpn;             /* DOF per node of the model the weights are for (3 or 6) */
+    double ratio;            /* lambda_max / lambda_min of the fitted interval (> 1) */
+    double lambda_scale;     /* safety factor on the eigenvalue estimate (>= 1) */
+    double weights[(ASTRO_PRECOND_MAX_DEGREE + 1) * 36];
+} astro_precond;
+
 /* Options and statistics of the spec solvers (astro_solve_static). */
 #define ASTRO_SOLVER_GMRES_JACOBI_FP64 0   /* plain FP64 Jacobi-GMRES(m): the comparator */
 #define ASTRO_SOLVER_FGMRES_MIXED 1        /* FP32 inner Jacobi-GMRES, FP64 refinement */
-#define ASTRO_SOLVER_FGMRES_LEARNED 2      /* FP32 inner FGMRES with the learned preconditioner */
+#define ASTRO_SOLVER_FGMRES_LEARNED 2      /* FP32 inner GMRES right-preconditioned by the
+                                              polynomial network, FP64 refinement */
 typedef struct astro_solve_opts {
     int32_t method;          /* ASTRO_SOLVER_* */
     int32_t restart;         /* Krylov basis size m (50) */
     int32_t max_iters;       /* total inner iterations cap */
     double rtol;             /* target ||b - A x||_2 / ||b||_2 in FP64 with A = K + C^T C */
     double inner_rtol;       /* inner relative tolerance for the refinement methods */
+    const astro_precond *precond;  /* ASTRO_SOLVER_FGMRES_LEARNED: the network (NULL: the
+                                      Chebyshev initialisation of degree 8, ratio 100) */
 } astro_solve_opts;
 
 typedef struct astro_solve_stats {
@@ -299,6 +320,31 @@ int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *opts, const doub
  * (kind 64: FP64 values from astro_el_soln_load, 32: FP32 values from astro_assemble_fp32) and
  * the scaled constraints; the operator of the gMRes matvec (Working/AStrO_solvers.f90:143-169). */
 int astro_apply_operator(astro_ctx *ctx, int32_t kind, const double *x, double *y);
+
+/* ---- polynomial preconditioner: initialisation, eigenvalue estimate, training -------------- */
+
+/* Host only: the untrained network, W_k = c_k I with c the least-squares fit of
+ * nu sum_k c_k T_k(x(nu)) = 1 over 400 Chebyshev nodes of nu in [1/ratio, 1]; lambda_scale 1.05. */
+int astro_precond_init(int32_t degree, double ratio, int32_t dpn, astro_precond *p);
+
+/* Largest eigenvalue of D^-1 A by 50 power iterations on the device from a fixed start vector
+ * (deterministic), with the FP64 (kind 64) or FP32 (kind 32) device-resident K. */
+int astro_precond_lambda(astro_ctx *ctx, int32_t kind, double *lambda);
+
+/* Training loss of the network on num_samples vectors v_s (host, num_samples x el_mat_dim, global
+ * DOF numbering; each is normalised to unit length first) with the FP64 device-resident K:
+ *     loss = (1/S) sum_s || v_s - A P v_s ||^2
+ * and its gradient with respect to the weights (same layout as astro_precond.weights; A is
+ * symmetric).  Everything in FP64 on the device; lambda from astro_precond_lambda(kind 64). */
+int astro_precond_loss_grad(astro_ctx *ctx, const astro_precond *p, const double *samples, int32_t num_samples,
+                            double *loss, double *grad);
+
+/* Trains the weights of p in place on the samples: iters steps of conjugate gradients
+ * (Polak-Ribiere+) with an exact line search (the loss is quadratic in the weights), each step
+ * one gradient and one line-search evaluation on the device.  loss_history (iters + 1, may be
+ * NULL) receives the loss before every step and after the last. */
+int astro_precond_train(astro_ctx *ctx, astro_precond *p, const double *samples, int32_t num_samples, int32_t iters,
+                        double *loss_history);
 
 #ifdef __cplusplus
 }

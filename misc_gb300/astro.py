@@ -40,9 +40,29 @@ class DimsC(C.Structure):
                                          "num_blocks", "num_colors")]
 
 
+PRECOND_MAX_DEGREE = 16
+
+
+class PrecondC(C.Structure):
+    """astro_precond: polynomial graph-convolution preconditioner (degree, dpn, interval, weights)."""
+    _fields_ = [("degree", C.c_int32), ("dpn", C.c_int32), ("ratio", C.c_double), ("lambda_scale", C.c_double),
+                ("weights", C.c_double * ((PRECOND_MAX_DEGREE + 1) * 36))]
+
+    def weight_array(self):
+        """W as an array (degree + 1, dpn, dpn) (a copy)."""
+        k, d = self.degree + 1, self.dpn
+        return np.array(self.weights[:k * d * d]).reshape(k, d, d)
+
+    def set_weights(self, w):
+        w = np.asarray(w, dtype=np.float64).reshape(-1)
+        assert w.size == (self.degree + 1) * self.dpn * self.dpn
+        for i, x in enumerate(w):
+            self.weights[i] = float(x)
+
+
 class SolveOptsC(C.Structure):
     _fields_ = [("method", C.c_int32), ("restart", C.c_int32), ("max_iters", C.c_int32), ("rtol", C.c_double),
-                ("inner_rtol", C.c_double)]
+                ("inner_rtol", C.c_double), ("precond", C.POINTER(PrecondC))]
 
 
 class SolveStatsC(C.Structure):
@@ -96,6 +116,10 @@ def load_library():
         "astro_newmark_run": ([vp, C.POINTER(NewmarkOptsC), F64P, F64P, F64P, F64P, F64P, F64P, F64P,
                                C.POINTER(SolveStatsC)], C.c_int),
         "astro_update_internal_soln": ([vp, F64P, F64P, F64P], C.c_int),
+        "astro_precond_init": ([C.c_int32, C.c_double, C.c_int32, C.POINTER(PrecondC)], C.c_int),
+        "astro_precond_lambda": ([vp, C.c_int32, F64P], C.c_int),
+        "astro_precond_loss_grad": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, F64P, F64P], C.c_int),
+        "astro_precond_train": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, C.c_int32, F64P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -123,6 +147,15 @@ def _f64(a):
 
 def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def precond_init(degree=8, ratio=100.0, dpn=3):
+    """Untrained polynomial preconditioner: W_k = c_k I from the Chebyshev least-squares fit of 1/nu."""
+    p = PrecondC()
+    rc = load_library().astro_precond_init(degree, ratio, dpn, C.byref(p))
+    if rc != ASTRO_OK:
+        raise AstroError(rc, "astro_precond_init: bad degree, ratio or dpn")
+    return p
 
 
 class AstroGPU:
@@ -241,9 +274,10 @@ class AstroGPU:
 
     # -- solves ---------------------------------------------------------------------------------
     def solve_static(self, f, u0=None, method=SOLVER_GMRES_JACOBI_FP64, restart=50, rtol=1e-10, max_iters=200000,
-                     inner_rtol=1e-4, allow_maxit=False):
+                     inner_rtol=1e-4, allow_maxit=False, precond=None):
         u = np.zeros(self.n) if u0 is None else _f64(u0).copy()
-        o = SolveOptsC(method, restart, max_iters, rtol, inner_rtol)
+        o = SolveOptsC(method, restart, max_iters, rtol, inner_rtol,
+                       C.pointer(precond) if precond is not None else C.POINTER(PrecondC)())
         st = SolveStatsC()
         rc = self.L.astro_solve_static(self.h, _d(_f64(f)), _d(u), C.byref(o), C.byref(st))
         self._check(rc, allow=(7,) if allow_maxit else ())
@@ -321,6 +355,27 @@ class AstroGPU:
                                               _d(out), _d(iout)))
         return out, iout[:self.int_vec_size]
 
+    # -- polynomial preconditioner ----------------------------------------------------------------
+    def precond_lambda(self, kind=64):
+        lam = np.zeros(1)
+        self._check(self.L.astro_precond_lambda(self.h, kind, _d(lam)))
+        return float(lam[0])
+
+    def precond_loss_grad(self, p, samples):
+        """(loss, gradient (degree + 1, dpn, dpn)) of the network p on samples (S x el_mat_dim)."""
+        S = _f64(samples).reshape(-1, self.n)
+        loss = np.zeros(1)
+        g = np.zeros((p.degree + 1) * p.dpn * p.dpn)
+        self._check(self.L.astro_precond_loss_grad(self.h, C.byref(p), _d(S), S.shape[0], _d(loss), _d(g)))
+        return float(loss[0]), g.reshape(p.degree + 1, p.dpn, p.dpn)
+
+    def precond_train(self, p, samples, iters=50):
+        """Trains p in place; returns the loss history (iters + 1)."""
+        S = _f64(samples).reshape(-1, self.n)
+        hist = np.zeros(iters + 1)
+        self._check(self.L.astro_precond_train(self.h, C.byref(p), _d(S), S.shape[0], iters, _d(hist)))
+        return hist
+
     # -- convenience ----------------------------------------------------------------------------
     def static_rhs(self, mpc_rhs_scaled=True):
         """b = constraint load (zero displacement) + applied load, after scaleElasticMPC."""
@@ -331,7 +386,7 @@ class AstroGPU:
 
 
 __all__ = ["AstroGPU", "AstroError", "load_library", "make_state", "AstroStateC", "SOLVER_GMRES_JACOBI_FP64",
-           "SOLVER_FGMRES_MIXED", "SOLVER_FGMRES_LEARNED"]
+           "SOLVER_FGMRES_MIXED", "SOLVER_FGMRES_LEARNED", "PrecondC", "precond_init", "PRECOND_MAX_DEGREE"]
 
 
 def _set_option(self, option, value):

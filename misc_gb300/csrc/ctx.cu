@@ -854,8 +854,8 @@ extern "C" int astro_solve_static(astro_ctx *ctx, const double *f, double *u, co
     if (opts->rtol <= 0) return set_err(ctx, ASTRO_ERR_ARG, "rtol must be positive");
     if (!ctx->mpcScaled && ctx->P.mpcDim > 0)
         return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run before the solve");
-    if (opts->method == ASTRO_SOLVER_FGMRES_LEARNED)
-        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "learned preconditioner not available in this build");
+    if (opts->method < ASTRO_SOLVER_GMRES_JACOBI_FP64 || opts->method > ASTRO_SOLVER_FGMRES_LEARNED)
+        return set_err(ctx, ASTRO_ERR_ARG, "unknown solver method");
     const int n = ctx->P.n;
     DevBuf db, dx;
     int rc;

@@ -25,124 +25,11 @@
 #include <vector>
 
 #include "astro_internal.h"
+#include "krylov_ops.cuh"
+
+using namespace astro_kry;
 
 namespace {
-
-constexpr int kMaxM = 64;
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
-constexpr int kGsThreads = 1024;  // threads per CTA of the Gram-Schmidt passes
-constexpr int kGsWarps = kGsThreads / 32;
-constexpr int kChunk = 1024;      // vector rows per CTA in the Gram-Schmidt passes (one per thread)
-constexpr int kRowThreads = 4;    // threads per block row in the SpMV
-
-struct GmresCtl {
-    double H[(kMaxM + 1) * kMaxM];  // column-major (m+1) x m, Givens-rotated in place
-    double cs[kMaxM], sn[kMaxM], g[kMaxM + 1];
-    double h1[kMaxM + 1];
-    double y[kMaxM];
-    double inv;      // 1 / ||w|| of the last step (scales w into the next basis vector)
-    double target;   // absolute residual target
-    double resest;   // |g[j]| after the last step
-    int j;           // completed Arnoldi steps in this cycle
-    int done;        // converged / broke down / cycle full: later steps are no-ops
-    int breakdown;
-    int nonfinite;
-    unsigned arrive[3];  // CTAs finished in the current dots / update / update-and-norm launch
-    int reorth;          // this step's first pass lost more than half of ||w||^2: run the second
-    int reorths;         // second passes run in this cycle
-};
-
-template <class TM> struct Op {
-    const TM *K;        // block-ELL values: entry q of slot s of block row r at (s*DPN*DPN + q)*ld + r
-    const int *col;     // block column of slot s of row r at col[s*ld + r]
-    int S, ld;          // slots per row, row stride
-    const int *penPtr;  // (N+1) penalty entries per block row, or null
-    const int *penRow;
-    const int *penCol;
-    const double *penVal;
-    int N, dpn;
-};
-
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-__device__ __forceinline__ float warp_sum(float v) {
-    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// y = (A x)_r for block row r, one thread: the products accumulate in TA (the matrix precision
-// for the Krylov steps, FP64 for true residuals).  Slots are taken three at a time so that their
-// column, x and value loads are in flight together.
-template <class TA, class TM, class TX, int DPN>
-__device__ __forceinline__ void ell_row(const Op<TM> &op, int r, const TX *__restrict__ x, TA y[DPN]) {
-    constexpr int G = 3;
-#pragma unroll
-    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
-    const size_t ld = (size_t)op.ld;
-    for (int s0 = 0; s0 < op.S; s0 += G) {
-        int c[G];
-#pragma unroll
-        for (int g = 0; g < G; ++g) c[g] = (s0 + g < op.S) ? __ldg(op.col + (size_t)(s0 + g) * ld + r) : -1;
-        TA xv[G][DPN];
-#pragma unroll
-        for (int g = 0; g < G; ++g)
-#pragma unroll
-            for (int jj = 0; jj < DPN; ++jj) xv[g][jj] = (c[g] >= 0) ? (TA)x[(size_t)c[g] * DPN + jj] : TA(0);
-#pragma unroll
-        for (int g = 0; g < G; ++g) {
-            if (s0 + g >= op.S) break;
-            const TM *kp = op.K + (size_t)(s0 + g) * DPN * DPN * ld + r;
-#pragma unroll
-            for (int i = 0; i < DPN; ++i)
-#pragma unroll
-                for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + jj) * ld) * xv[g][jj];
-        }
-    }
-    if (op.penPtr) {
-        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
-            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
-            const int i = op.penRow[t];
-#pragma unroll
-            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
-        }
-    }
-}
-
-// Partial (A x)_r over the slots s = sub, sub + kRowThreads, ... of block row r; the products
-// accumulate in TA.  The kRowThreads threads of a row are adjacent lanes and combine their
-// partials with xor-shuffles (result in all of them); thread sub == 0 adds the penalty.
-template <class TA, class TM, class TX, int DPN>
-__device__ __forceinline__ void ell_row_part(const Op<TM> &op, int r, int sub, const TX *__restrict__ x, TA y[DPN]) {
-#pragma unroll
-    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
-    const size_t ld = (size_t)op.ld;
-    for (int s = sub; s < op.S; s += kRowThreads) {
-        const int c = __ldg(op.col + (size_t)s * ld + r);
-        TA xv[DPN];
-#pragma unroll
-        for (int jj = 0; jj < DPN; ++jj) xv[jj] = (TA)x[(size_t)c * DPN + jj];
-        const TM *kp = op.K + (size_t)s * DPN * DPN * ld + r;
-#pragma unroll
-        for (int i = 0; i < DPN; ++i)
-#pragma unroll
-            for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + jj) * ld) * xv[jj];
-    }
-    if (sub == 0 && op.penPtr) {
-        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
-            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
-            const int i = op.penRow[t];
-#pragma unroll
-            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
-        }
-    }
-#pragma unroll
-    for (int m = 1; m < kRowThreads; m <<= 1)
-#pragma unroll
-        for (int i = 0; i < DPN; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], m);
-}
 
 // Partial dot products of the staged tile sw (cnt vector rows from row0, at most ROWS) with
 // V[0..j], and with itself when self is set (stored as vector kMaxM): part[k * nCh + cta].
@@ -176,21 +63,6 @@ __device__ __forceinline__ void chunk_dots(const TV *__restrict__ V, size_t ld, 
             __threadfence();
         }
     }
-}
-
-// True in the last CTA of the launch to arrive; the threads that wrote partials have fenced them
-// before the barrier.  That CTA resets the counter for the next launch.  No CTA waits for another.
-__device__ __forceinline__ bool last_to_arrive(unsigned *counter) {
-    __shared__ bool amLast;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const unsigned prev = atomicAdd(counter, 1u);
-        amLast = (prev == gridDim.x - 1);
-        if (amLast) *counter = 0u;
-    }
-    __syncthreads();
-    if (amLast) __threadfence();
-    return amLast;
 }
 
 // h[k] = sum of the nCh CTA partials of vector k in a fixed order (one warp per vector, reads
@@ -315,6 +187,124 @@ __global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restric
     }
 }
 
+// One hop of the polynomial preconditioner P v = sum_k W_k T_k(xi(D^-1 A)) D^-1 v / lambda:
+// with u = D^-1 A y_k, y_{k+1} = c (u - theta y_k) - [k > 0] y_{k-1} (the Chebyshev three-term
+// recurrence in the shifted and scaled variable), and z += W_{k+1} y_{k+1} per node (the first hop
+// also adds W_0 y_0).  kRowThreads threads per block row as in the SpMV; each thread then has the
+// whole node's y_{k+1} and writes its share of the components.  Weights arrive in the parameter
+// space already divided by lambda.
+struct HopArgs {
+    float w[36];   // W_{k+1} / lambda, row-major dpn x dpn
+    float w0[36];  // W_0 / lambda (first hop)
+    float theta, c;
+    int first;
+};
+
+template <class TM, class TV, int DPN>
+__global__ void __launch_bounds__(kThreads) k_poly_hop(Op<TM> op, const TV *__restrict__ dinv, const TV *__restrict__ yk,
+                                                       const TV *__restrict__ ykm1, TV *__restrict__ ykp1,
+                                                       TV *__restrict__ zacc, const HopArgs h,
+                                                       const GmresCtl *__restrict__ ctl, int always) {
+    if (!always && ctl->done) return;
+    const int tid = blockIdx.x * kThreads + threadIdx.x;
+    const int r = tid / kRowThreads, sub = tid % kRowThreads;
+    const bool valid = r < op.N;
+    const int rr = valid ? r : op.N - 1;
+    TV t[DPN];
+    ell_row_part<TV, TM, TV, DPN>(op, rr, sub, yk, t);
+    if (!valid) return;
+    const size_t base = (size_t)r * DPN;
+    TV yc[DPN], yn[DPN];
+#pragma unroll
+    for (int q = 0; q < DPN; ++q) yc[q] = yk[base + q];
+#pragma unroll
+    for (int q = 0; q < DPN; ++q) {
+        const TV u = dinv[base + q] * t[q] - (TV)h.theta * yc[q];
+        yn[q] = (TV)h.c * u;
+        if (!h.first) yn[q] -= ykm1[base + q];
+    }
+#pragma unroll
+    for (int q = 0; q < DPN; ++q) {
+        if (q % kRowThreads != sub) continue;
+        if (ykp1) ykp1[base + q] = yn[q];
+        TV z = h.first ? TV(0) : zacc[base + q];
+        if (h.first) {
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w0[q * DPN + jj] * yc[jj];
+        }
+#pragma unroll
+        for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w[q * DPN + jj] * yn[jj];
+        zacc[base + q] = z;
+    }
+}
+
+// Power iteration for the largest eigenvalue of D^-1 A: y = s D^-1 A x with s = scal[0] (the
+// reciprocal norm of x from the previous step), one thread per block row; the last CTA sums the
+// per-CTA ||y||^2 in CTA order and sets scal[1] = ||y||, scal[0] = 1 / ||y||.  Every CTA reads
+// scal[0] before it arrives, so the last one may overwrite it.
+template <class TM, class TV, int DPN>
+__global__ void __launch_bounds__(kThreads) k_power_step(Op<TM> op, const TV *__restrict__ dinv, const TV *__restrict__ x,
+                                                         TV *__restrict__ y, double *part, unsigned *counter,
+                                                         double *scal) {
+    __shared__ double sp[kWarps];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int row = blockIdx.x * kThreads + threadIdx.x;
+    const TV s = (TV)scal[0];
+    double yy = 0.0;
+    if (row < op.N) {
+        TV t[DPN];
+        ell_row<TV, TM, TV, DPN>(op, row, x, t);
+#pragma unroll
+        for (int q = 0; q < DPN; ++q) {
+            const size_t i = (size_t)row * DPN + q;
+            const TV v = s * dinv[i] * t[q];
+            y[i] = v;
+            yy += (double)v * (double)v;
+        }
+    }
+    yy = warp_sum(yy);
+    if (lane == 0) sp[wid] = yy;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (int q = 0; q < kWarps; ++q) a += sp[q];
+        part[blockIdx.x] = a;
+        __threadfence();
+    }
+    if (last_to_arrive(counter) && threadIdx.x == 0) {
+        double a = 0.0;
+        for (unsigned q = 0; q < gridDim.x; ++q) a += __ldcg(part + q);
+        const double nrm = sqrt(a);
+        scal[1] = nrm;
+        scal[0] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+    }
+}
+
+// Start vector of the power iteration: a fixed pseudo-random pattern in [-1, 1) (an integer hash
+// of the index), so that every eigenvector has a component and the estimate is reproducible.
+template <class TV>
+__global__ void k_power_init(TV *x, int n, double *scal) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) {
+        scal[0] = 1.0;
+        scal[1] = 0.0;
+    }
+    if (i >= n) return;
+    unsigned h = (unsigned)i * 2654435761u + 0x9e3779b9u;
+    h ^= h >> 16;
+    h *= 0x85ebca6bu;
+    h ^= h >> 13;
+    h *= 0xc2b2ae35u;
+    h ^= h >> 16;
+    x[i] = (TV)((double)(h >> 8) * (2.0 / 16777216.0) - 1.0);
+}
+
+template <class TV>
+__global__ void k_add(int n, TV *__restrict__ x, const TV *__restrict__ d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += d[i];
+}
+
 // First Gram-Schmidt pass: partial dots of w with V[0..j] and with itself over this CTA's rows;
 // the last CTA reduces them into h1 and decides whether a second pass is needed.
 template <class TV>
@@ -421,10 +411,12 @@ __global__ void k_lsq(GmresCtl *ctl) {
     }
 }
 
-// x += D^-1 V[0..j-1] y
+// x += D^-1 V[0..j-1] y, or with out the preconditioner input out = D^-1 V[0..j-1] y (the
+// polynomial preconditioner then maps it to the update)
 template <class TV, class TX>
 __global__ void __launch_bounds__(kThreads) k_xupdate(int n, const TV *__restrict__ V, size_t ld, const TV *__restrict__ dinv,
-                                                      const GmresCtl *__restrict__ ctl, TX *__restrict__ x) {
+                                                      const GmresCtl *__restrict__ ctl, TX *__restrict__ x,
+                                                      TV *__restrict__ out = nullptr) {
     __shared__ TV sy[kMaxM];
     const int j = ctl->j;
     for (int k = threadIdx.x; k < j; k += kThreads) sy[k] = (TV)ctl->y[k];
@@ -440,7 +432,8 @@ __global__ void __launch_bounds__(kThreads) k_xupdate(int n, const TV *__restric
             for (int u = 0; u < 8; ++u) s += sy[k + u] * v[u];
         }
         for (; k < j; ++k) s += sy[k] * V[(size_t)k * ld + i];
-        x[i] = (TX)(x[i] + dinv[i] * s);
+        if (out) out[i] = dinv[i] * s;
+        else x[i] = (TX)(x[i] + dinv[i] * s);
     }
 }
 
@@ -561,8 +554,18 @@ __global__ void k_to_ell(const T *__restrict__ K, const int *__restrict__ rowPtr
 
 // ---------------------------------------------------------------------------------------------
 
+// Polynomial preconditioner of one solve: hop parameters with the weights already divided by
+// the eigenvalue bound (host copy, passed to the hop kernels by value).
+struct PolyHost {
+    int deg = 0;
+    float theta = 0.f, delta = 0.f;
+    float W[(ASTRO_PRECOND_MAX_DEGREE + 1) * 36];
+};
+
 struct GmresWork {
     DevBuf V, w0, w1, z0, z1, part, ctl, dinv, dinvT, rres, xs, tgt;
+    DevBuf yB0, yB1, zacc, pw;  // polynomial preconditioner: hop vectors, output, power-iteration scratch
+    const PolyHost *poly = nullptr;
     // restart cycle captured as a graph, reused while the matrix and vectors stay the same
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -623,6 +626,35 @@ template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *Kell) {
     return op;
 }
 
+// Enqueues the hops of the polynomial preconditioner on y0 = D^-1 v (overwritten: the three-term
+// recurrence rotates through y0 and two scratch vectors) and returns the output vector P v.
+// always: run even when the cycle has finished (the final update of x).
+template <class TM, class TV, int DPN>
+static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, TV *y0, int always) {
+    const PolyHost &P = *W.poly;
+    cudaStream_t s = ctx->stream;
+    const int dd = DPN * DPN;
+    TV *buf[3] = {y0, dptr<TV>(W.yB0), dptr<TV>(W.yB1)};
+    TV *z = dptr<TV>(W.zacc);
+    const unsigned grid = (unsigned)(((long long)ctx->P.N * kRowThreads + kThreads - 1) / kThreads);
+    HopArgs h;
+    std::memset(&h, 0, sizeof(h));
+    for (int q = 0; q < dd; ++q) h.w0[q] = P.W[q];
+    h.theta = P.theta;
+    int cur = 0;
+    for (int k = 0; k < P.deg; ++k) {
+        const int nxt = (cur + 1) % 3, prv = (cur + 2) % 3;
+        for (int q = 0; q < dd; ++q) h.w[q] = P.W[(k + 1) * dd + q];
+        h.first = (k == 0);
+        h.c = (k == 0 ? 1.f : 2.f) / P.delta;
+        k_poly_hop<TM, TV, DPN><<<grid, kThreads, 0, s>>>(op, dptr<TV>(W.dinvT), buf[cur], buf[prv],
+                                                          k + 1 < P.deg ? buf[nxt] : nullptr, z, h,
+                                                          dptr<GmresCtl>(W.ctl), always);
+        cur = nxt;
+    }
+    return z;
+}
+
 template <class TM, class TV, int DPN>
 static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m) {
     cudaStream_t s = ctx->stream;
@@ -638,7 +670,8 @@ static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m)
     for (int step = 0; step < m; ++step) {
         TV *wprev = (step % 2 == 0) ? wa : wb, *zprev = (step % 2 == 0) ? za : zb;
         TV *wnew = (step % 2 == 0) ? wb : wa, *znew = (step % 2 == 0) ? zb : za;
-        k_spmv_step<TM, TV, DPN><<<spmvGrid, kThreads, 0, s>>>(op, V, W.ld, wprev, zprev, wnew, ctl);
+        const TV *zin = W.poly ? enqueue_poly<TM, TV, DPN>(ctx, W, op, zprev, 0) : zprev;
+        k_spmv_step<TM, TV, DPN><<<spmvGrid, kThreads, 0, s>>>(op, V, W.ld, wprev, zin, wnew, ctl);
         k_dots<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, W.nChunks);
         k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 0, dinv, znew, m);
         k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 1, dinv, znew, m);
@@ -678,7 +711,14 @@ static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const d
         k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, dptr<double>(W.tgt));
         enqueue_cycle<TM, TV, DPN>(ctx, W, op, m);
         k_lsq<<<1, 1, 0, s>>>(ctl);
-        k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x);
+        if (W.poly) {
+            TV *y0 = dptr<TV>(W.z0);
+            k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x, y0);
+            TV *dz = enqueue_poly<TM, TV, DPN>(ctx, W, op, y0, 1);
+            k_add<TV><<<(W.n + 255) / 256, 256, 0, s>>>(W.n, x, dz);
+        } else {
+            k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x);
+        }
         CK(cudaStreamEndCapture(s, &W.graph));
         CK(cudaGraphInstantiate(&W.exec, W.graph, 0));
         W.gK = K;
@@ -738,7 +778,8 @@ static void work_free(GmresWork &W) {
     if (W.graph) cudaGraphDestroy(W.graph);
     W.exec = nullptr;
     W.graph = nullptr;
-    DevBuf *b[] = {&W.V, &W.w0, &W.w1, &W.z0, &W.z1, &W.part, &W.ctl, &W.dinv, &W.dinvT, &W.rres, &W.xs, &W.tgt};
+    DevBuf *b[] = {&W.V,    &W.w0,   &W.w1,    &W.z0, &W.z1,  &W.part, &W.ctl, &W.dinv,
+                   &W.dinvT, &W.rres, &W.xs,  &W.tgt, &W.yB0, &W.yB1,  &W.zacc, &W.pw};
     for (auto *x : b) dev_free(*x);
 }
 
@@ -771,6 +812,49 @@ static int true_residual(astro_ctx *ctx, GmresWork &W, int kind, const double *x
     return ASTRO_OK;
 }
 
+// 50 power iterations of D^-1 A (deterministic start vector and reductions); lam = the last
+// norm ratio, which approaches the largest eigenvalue from below.
+template <class TM, class TV, int DPN>
+static int power_lambda(astro_ctx *ctx, const Op<TM> &op, const TV *dinv, double *lam) {
+    const int n = ctx->P.n;
+    const int nCta = (ctx->P.N + kThreads - 1) / kThreads;
+    cudaStream_t s = ctx->stream;
+    DevBuf a, b, part, cnt, scal;
+    int rc;
+    if ((rc = dev_alloc(ctx, a, sizeof(TV) * n)) || (rc = dev_alloc(ctx, b, sizeof(TV) * n)) ||
+        (rc = dev_alloc(ctx, part, sizeof(double) * nCta)) || (rc = dev_alloc(ctx, cnt, sizeof(unsigned))) ||
+        (rc = dev_alloc(ctx, scal, 2 * sizeof(double)))) {
+        dev_free(a), dev_free(b), dev_free(part), dev_free(cnt), dev_free(scal);
+        return rc;
+    }
+    cudaMemsetAsync(cnt.p, 0, sizeof(unsigned), s);
+    k_power_init<TV><<<(n + 255) / 256, 256, 0, s>>>(dptr<TV>(a), n, dptr<double>(scal));
+    for (int it = 0; it < 50; ++it) {
+        TV *x = dptr<TV>(it % 2 ? b : a), *y = dptr<TV>(it % 2 ? a : b);
+        k_power_step<TM, TV, DPN><<<nCta, kThreads, 0, s>>>(op, dinv, x, y, dptr<double>(part), dptr<unsigned>(cnt),
+                                                            dptr<double>(scal));
+    }
+    double h[2] = {0.0, 0.0};
+    cudaError_t e = cudaMemcpyAsync(h, scal.p, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    rc = cuda_check(ctx, e, "power iteration");
+    dev_free(a), dev_free(b), dev_free(part), dev_free(cnt), dev_free(scal);
+    *lam = h[1];
+    if (!rc && !(std::isfinite(h[1]) && h[1] > 0.0)) rc = set_err(ctx, ASTRO_ERR_NAN, "eigenvalue estimate is not positive");
+    return rc;
+}
+
+// Checks the network against the model (degree, DOF per node, interval, finite weights).
+static int precond_check(astro_ctx *ctx, const astro_precond *p) {
+    if (p->degree < 1 || p->degree > ASTRO_PRECOND_MAX_DEGREE) return set_err(ctx, ASTRO_ERR_ARG, "precond degree out of range");
+    if (p->dpn != ctx->P.dpn) return set_err(ctx, ASTRO_ERR_ARG, "precond DOF per node differs from the model's");
+    if (!(p->ratio > 1.0) || !(p->lambda_scale > 0.0) || !std::isfinite(p->ratio) || !std::isfinite(p->lambda_scale))
+        return set_err(ctx, ASTRO_ERR_ARG, "precond ratio must be > 1 and lambda_scale > 0");
+    for (int q = 0; q < (p->degree + 1) * p->dpn * p->dpn; ++q)
+        if (!std::isfinite(p->weights[q])) return set_err(ctx, ASTRO_ERR_ARG, "non-finite precond weight");
+    return ASTRO_OK;
+}
+
 template <int DPN>
 static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, const astro_solve_opts *o,
                             astro_solve_stats *st) {
@@ -783,6 +867,15 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     int iters = 0, cycles = 0, refinements = 0;
     double rel = 0.0, est = 0.0, rn = 0.0, bn = 0.0;
     const bool fp64 = o->method == ASTRO_SOLVER_GMRES_JACOBI_FP64;
+    const bool learned = o->method == ASTRO_SOLVER_FGMRES_LEARNED;
+    astro_precond pdef;
+    const astro_precond *pc = o->precond;
+    if (learned && !pc) {
+        astro_precond_init(8, 100.0, ctx->P.dpn, &pdef);
+        pc = &pdef;
+    }
+    if (learned && (rc = precond_check(ctx, pc))) return rc;
+    PolyHost ph;
     if (fp64 && !ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
     if (!fp64 && !ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
     if ((rc = work_alloc(ctx, W, m, fp64 ? sizeof(double) : sizeof(float)))) {
@@ -830,6 +923,23 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
             dptr<float>(ctx->d_K32), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn,
             ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
             dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<float>(W.dinvT));
+        if (learned) {
+            // the network's hop vectors, and the interval [lambda/ratio, lambda] from the
+            // eigenvalue estimate on the FP32 operator (inside the timed solve)
+            double lam = 0.0;
+            if ((rc = dev_alloc(ctx, W.yB0, sizeof(float) * n)) || (rc = dev_alloc(ctx, W.yB1, sizeof(float) * n)) ||
+                (rc = dev_alloc(ctx, W.zacc, sizeof(float) * n)) ||
+                (rc = power_lambda<float, float, DPN>(ctx, make_op<float>(ctx, K32p), dptr<float>(W.dinvT), &lam))) {
+                work_free(W);
+                return rc;
+            }
+            lam *= pc->lambda_scale;
+            ph.deg = pc->degree;
+            ph.theta = (float)(0.5 * lam * (1.0 + 1.0 / pc->ratio));
+            ph.delta = (float)(0.5 * lam * (1.0 - 1.0 / pc->ratio));
+            for (int q = 0; q < (pc->degree + 1) * DPN * DPN; ++q) ph.W[q] = (float)(pc->weights[q] / lam);
+            W.poly = &ph;
+        }
         float *d32 = dptr<float>(W.xs);
         const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
         for (refinements = 0; refinements < 200; ++refinements) {
@@ -877,6 +987,65 @@ int krylov_solve_static(astro_ctx *ctx, const double *d_b, double *d_x, const as
                         astro_solve_stats *st) {
     if (ctx->P.dpn == 3) return solve_static_dev<3>(ctx, d_b, d_x, o, st);
     return solve_static_dev<6>(ctx, d_b, d_x, o, st);
+}
+
+int krylov_op64(astro_ctx *ctx, Op<double> *op) {
+    if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
+    int rc = ASTRO_OK;
+    const double *Kp = ell_of<double>(ctx, &rc);
+    if (!rc) *op = make_op<double>(ctx, Kp);
+    return rc;
+}
+
+int krylov_op32(astro_ctx *ctx, Op<float> *op) {
+    if (!ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
+    int rc = ASTRO_OK;
+    const float *Kp = ell_of<float>(ctx, &rc);
+    if (!rc) *op = make_op<float>(ctx, Kp);
+    return rc;
+}
+
+int krylov_dinv(astro_ctx *ctx, int kind, double *d_dinv) {
+    const unsigned grid = (ctx->P.N + 255) / 256;
+    cudaStream_t s = ctx->stream;
+    const int *pp = ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr;
+    if (kind == 64) {
+        if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
+        k_dinv<double, double><<<grid, 256, 0, s>>>(dptr<double>(ctx->d_K64), dptr<int>(ctx->d_bRowPtr),
+                                                    dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn, pp,
+                                                    dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
+                                                    dptr<double>(ctx->d_penVal), d_dinv, d_dinv);
+    } else {
+        if (!ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
+        k_dinv<float, double><<<grid, 256, 0, s>>>(dptr<float>(ctx->d_K32), dptr<int>(ctx->d_bRowPtr),
+                                                   dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn, pp,
+                                                   dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
+                                                   dptr<double>(ctx->d_penVal), d_dinv, d_dinv);
+    }
+    return cuda_check(ctx, cudaGetLastError(), "dinv");
+}
+
+int krylov_power_lambda(astro_ctx *ctx, int kind, double *lam) {
+    if (kind != 64 && kind != 32) return set_err(ctx, ASTRO_ERR_ARG, "kind must be 64 or 32");
+    DevBuf dv;
+    int rc = dev_alloc(ctx, dv, sizeof(double) * ctx->P.n);
+    if (!rc) rc = krylov_dinv(ctx, kind, dptr<double>(dv));
+    if (!rc) {
+        // the iteration runs in FP64 vectors over either matrix
+        if (kind == 64) {
+            Op<double> op;
+            if (!(rc = krylov_op64(ctx, &op)))
+                rc = ctx->P.dpn == 3 ? power_lambda<double, double, 3>(ctx, op, dptr<double>(dv), lam)
+                                     : power_lambda<double, double, 6>(ctx, op, dptr<double>(dv), lam);
+        } else {
+            Op<float> op;
+            if (!(rc = krylov_op32(ctx, &op)))
+                rc = ctx->P.dpn == 3 ? power_lambda<float, double, 3>(ctx, op, dptr<double>(dv), lam)
+                                     : power_lambda<float, double, 6>(ctx, op, dptr<double>(dv), lam);
+        }
+    }
+    dev_free(dv);
+    return rc;
 }
 
 // y = (K + C^T C) x for device vectors (internal layout).

@@ -1,0 +1,150 @@
+// Building blocks shared by the Krylov solvers and the polynomial preconditioner: launch
+// constants, the solver's device control block, the block-ELL operator descriptor and its row
+// products, warp sums, and the last-CTA-to-arrive test used for deterministic reductions.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace astro_kry {
+
+constexpr int kMaxM = 64;
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kGsThreads = 1024;  // threads per CTA of the Gram-Schmidt passes
+constexpr int kGsWarps = kGsThreads / 32;
+constexpr int kChunk = 1024;      // vector rows per CTA in the Gram-Schmidt passes (one per thread)
+constexpr int kRowThreads = 4;    // threads per block row in the SpMV
+
+struct GmresCtl {
+    double H[(kMaxM + 1) * kMaxM];  // column-major (m+1) x m, Givens-rotated in place
+    double cs[kMaxM], sn[kMaxM], g[kMaxM + 1];
+    double h1[kMaxM + 1];
+    double y[kMaxM];
+    double inv;      // 1 / ||w|| of the last step (scales w into the next basis vector)
+    double target;   // absolute residual target
+    double resest;   // |g[j]| after the last step
+    int j;           // completed Arnoldi steps in this cycle
+    int done;        // converged / broke down / cycle full: later steps are no-ops
+    int breakdown;
+    int nonfinite;
+    unsigned arrive[3];  // CTAs finished in the current dots / update / update-and-norm launch
+    int reorth;          // this step's first pass lost more than half of ||w||^2: run the second
+    int reorths;         // second passes run in this cycle
+};
+
+template <class TM> struct Op {
+    const TM *K;        // block-ELL values: entry q of slot s of block row r at (s*DPN*DPN + q)*ld + r
+    const int *col;     // block column of slot s of row r at col[s*ld + r]
+    int S, ld;          // slots per row, row stride
+    const int *penPtr;  // (N+1) penalty entries per block row, or null
+    const int *penRow;
+    const int *penCol;
+    const double *penVal;
+    int N, dpn;
+};
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// y = (A x)_r for block row r, one thread: the products accumulate in TA (the matrix precision
+// for the Krylov steps, FP64 for true residuals).  Slots are taken three at a time so that their
+// column, x and value loads are in flight together.
+template <class TA, class TM, class TX, int DPN>
+__device__ __forceinline__ void ell_row(const Op<TM> &op, int r, const TX *__restrict__ x, TA y[DPN]) {
+    constexpr int G = 3;
+#pragma unroll
+    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
+    const size_t ld = (size_t)op.ld;
+    for (int s0 = 0; s0 < op.S; s0 += G) {
+        int c[G];
+#pragma unroll
+        for (int g = 0; g < G; ++g) c[g] = (s0 + g < op.S) ? __ldg(op.col + (size_t)(s0 + g) * ld + r) : -1;
+        TA xv[G][DPN];
+#pragma unroll
+        for (int g = 0; g < G; ++g)
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) xv[g][jj] = (c[g] >= 0) ? (TA)x[(size_t)c[g] * DPN + jj] : TA(0);
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            if (s0 + g >= op.S) break;
+            const TM *kp = op.K + (size_t)(s0 + g) * DPN * DPN * ld + r;
+#pragma unroll
+            for (int i = 0; i < DPN; ++i)
+#pragma unroll
+                for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + jj) * ld) * xv[g][jj];
+        }
+    }
+    if (op.penPtr) {
+        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
+            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
+            const int i = op.penRow[t];
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
+        }
+    }
+}
+
+// Partial (A x)_r over the slots s = sub, sub + kRowThreads, ... of block row r; the products
+// accumulate in TA.  The kRowThreads threads of a row are adjacent lanes and combine their
+// partials with xor-shuffles (result in all of them); thread sub == 0 adds the penalty.
+template <class TA, class TM, class TX, int DPN>
+__device__ __forceinline__ void ell_row_part(const Op<TM> &op, int r, int sub, const TX *__restrict__ x, TA y[DPN]) {
+#pragma unroll
+    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
+    const size_t ld = (size_t)op.ld;
+    for (int s = sub; s < op.S; s += kRowThreads) {
+        const int c = __ldg(op.col + (size_t)s * ld + r);
+        TA xv[DPN];
+#pragma unroll
+        for (int jj = 0; jj < DPN; ++jj) xv[jj] = (TA)x[(size_t)c * DPN + jj];
+        const TM *kp = op.K + (size_t)s * DPN * DPN * ld + r;
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + jj) * ld) * xv[jj];
+    }
+    if (sub == 0 && op.penPtr) {
+        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
+            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
+            const int i = op.penRow[t];
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
+        }
+    }
+#pragma unroll
+    for (int m = 1; m < kRowThreads; m <<= 1)
+#pragma unroll
+        for (int i = 0; i < DPN; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], m);
+}
+
+// True in the last CTA of the launch to arrive; the threads that wrote partials have fenced them
+// before the barrier.  That CTA resets the counter for the next launch.  No CTA waits for another.
+__device__ __forceinline__ bool last_to_arrive(unsigned *counter) {
+    __shared__ bool amLast;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned prev = atomicAdd(counter, 1u);
+        amLast = (prev == gridDim.x - 1);
+        if (amLast) *counter = 0u;
+    }
+    __syncthreads();
+    if (amLast) __threadfence();
+    return amLast;
+}
+
+}  // namespace astro_kry
+
+struct astro_ctx;
+// Block-ELL operator of A = K + C^T C over the FP64 (kind 64) or FP32 (kind 32) device-resident
+// K (the solver copy is rebuilt when the assembly changed); the pointer type follows the kind.
+int krylov_op64(astro_ctx *ctx, astro_kry::Op<double> *op);
+int krylov_op32(astro_ctx *ctx, astro_kry::Op<float> *op);
+// 1 / diag(A) in FP64 (n values, internal layout) from the kind's K.
+int krylov_dinv(astro_ctx *ctx, int kind, double *d_dinv);
+// Largest eigenvalue of D^-1 A: 50 power iterations from a fixed start vector (deterministic).
+int krylov_power_lambda(astro_ctx *ctx, int kind, double *lam);

@@ -1,0 +1,150 @@
+"""Polynomial graph-convolution preconditioner on the GPU, through the C ABI:
+eigenvalue estimate, training loss and gradient against the numpy restatement (FP64, 1e-9) and
+against central differences of the device loss, monotone training, and the learned solver
+(FP32 inner GMRES right-preconditioned by the network, FP64 refinement) against the direct
+solution and against the Jacobi-preconditioned mixed solver on a held-out mesh."""
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from misc_gb300 import model as M
+from misc_gb300.astro import (SOLVER_FGMRES_LEARNED, SOLVER_FGMRES_MIXED, AstroError, AstroGPU, precond_init)
+from oracle import Oracle
+import poly_ref as R
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(m, fp32=False):
+    g, o = AstroGPU(m), Oracle(m)
+    g.getElasticSolnLoad(1, export=False)
+    if fp32:
+        g.assemble_fp32()
+    g.scaleElasticMPC()
+    A, b, *_ = o.static_system()
+    return g, o, A.tocsr(), b
+
+
+def _samples(A, S, seed, smooth=(0, 2, 8)):
+    """white noise and Jacobi-smoothed vectors (the low end of the spectrum)"""
+    rng = np.random.default_rng(seed)
+    dinv = 1.0 / A.diagonal()
+    out = []
+    for s in range(S):
+        v = rng.standard_normal(A.shape[0])
+        for _ in range(smooth[s % len(smooth)]):
+            v = v - 0.3 * dinv * (A @ v)
+        out.append(v)
+    return np.array(out)
+
+
+def _shell():
+    m = M.plate_shell(nx=8, ny=4, lx=2.0, ly=1.0, t=0.03, E=7e10, nu=0.33)
+    rng = np.random.default_rng(2)
+    X = m.node_list.copy()
+    X[:, 2] += 0.02 * rng.uniform(-1, 1, len(X))
+    m.node_list = X
+    return m
+
+
+CASES = {"brick": (lambda: M.config2(nx=6, ny=4, nz=4, seed=3), 3),
+         "shell": (_shell, 6)}
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_lambda_bounds(case):
+    mk, dpn = CASES[case]
+    g, o, A, _ = _system(mk(), fp32=(dpn == 3))  # the FP32 assembly covers brick8 meshes
+    d = np.sqrt(1.0 / A.diagonal())
+    lam_true = spla.eigsh((A.multiply(d[:, None]).multiply(d[None, :])).tocsr(), k=1, which="LA",
+                          return_eigenvectors=False)[0]
+    lam64 = g.precond_lambda(64)
+    # power iteration approaches the largest eigenvalue from below
+    assert 0.7 * lam_true <= lam64 <= lam_true * (1 + 1e-9), (lam64, lam_true)
+    if dpn == 3:
+        lam32 = g.precond_lambda(32)
+        assert abs(lam32 - lam64) <= 1e-3 * lam64
+    assert g.precond_lambda(64) == lam64  # deterministic
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_loss_grad_matches_numpy(case):
+    mk, dpn = CASES[case]
+    g, o, A, _ = _system(mk())
+    p = precond_init(4, 50.0, dpn)
+    rng = np.random.default_rng(7)
+    W = p.weight_array() + 0.1 * rng.standard_normal((5, dpn, dpn))
+    p.set_weights(W)
+    S = _samples(A, 4, 11)
+    L, G = g.precond_loss_grad(p, S)
+    lam = g.precond_lambda(64) * p.lambda_scale
+    Lr, Gr = R.loss_grad(A, 1.0 / A.diagonal(), lam, p.ratio, W, S, R.node_index(o, dpn))
+    assert abs(L - Lr) <= 1e-9 * Lr, (L, Lr)
+    assert np.linalg.norm(G - Gr) <= 1e-9 * np.linalg.norm(Gr)
+
+
+def test_gradient_central_difference():
+    m, dpn = CASES["brick"][0](), 3
+    g, o, A, _ = _system(m)
+    p = precond_init(3, 30.0, dpn)
+    S = _samples(A, 3, 5)
+    L0, G = g.precond_loss_grad(p, S)
+    W = p.weight_array()
+    rng = np.random.default_rng(3)
+    D = rng.standard_normal(W.shape)
+    h = 1e-4
+    p.set_weights(W + h * D)
+    Lp, _ = g.precond_loss_grad(p, S)
+    p.set_weights(W - h * D)
+    Lm, _ = g.precond_loss_grad(p, S)
+    fd = (Lp - Lm) / (2 * h)
+    # the loss is quadratic in W: the central difference is exact up to rounding
+    assert abs(fd - np.sum(G * D)) <= 1e-6 * max(abs(fd), 1e-12), (fd, np.sum(G * D))
+
+
+def test_training_decreases_loss():
+    g, o, A, _ = _system(M.config2(nx=8, ny=4, nz=4, seed=1))
+    p = precond_init(6, 100.0, 3)
+    S = _samples(A, 8, 21)
+    hist = g.precond_train(p, S, iters=25)
+    assert np.all(np.diff(hist) <= 1e-12 * hist[0]), hist
+    assert hist[-1] < hist[0]
+    L, _ = g.precond_loss_grad(p, S)
+    assert abs(L - hist[-1]) <= 1e-10 * hist[-1]
+
+
+def test_learned_solver_converges_with_fewer_iterations():
+    """The network trained on one mesh, applied to a held-out mesh of the same family: the
+    solution matches the direct solve and the Krylov iterations drop against Jacobi."""
+    gt, ot, At, _ = _system(M.config2(nx=8, ny=4, nz=4, seed=1))
+    p = precond_init(8, 100.0, 3)
+    gt.precond_train(p, _samples(At, 8, 4), iters=20)
+    m = M.config2(nx=16, ny=8, nz=8, seed=9)
+    g, o, A, bo = _system(m, fp32=True)
+    b = g.static_rhs()
+    ul, stl = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=1e-10, precond=p)
+    um, stm = g.solve_static(b, method=SOLVER_FGMRES_MIXED, rtol=1e-10)
+    ud, std_ = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=1e-10)  # untrained default network
+    assert stl.status == 0 and stl.rel_residual <= 1e-10
+    assert std_.status == 0 and std_.rel_residual <= 1e-10
+    ur = spla.spsolve(A.tocsc(), bo)
+    for u in (ul, ud):
+        # FP32 element matrices: the system differs from the FP64 one at ~1e-7 x conditioning
+        assert np.linalg.norm(u - ur) <= 5e-5 * np.linalg.norm(ur)
+    assert np.linalg.norm(ul - um) <= 1e-8 * np.linalg.norm(um)
+    assert stl.iterations * 5 < stm.iterations, (stl.iterations, stm.iterations)
+
+
+def test_precond_errors():
+    g, o, A, _ = _system(M.config2(nx=4, ny=2, nz=2), fp32=True)
+    b = g.static_rhs()
+    p6 = precond_init(4, 100.0, 6)
+    with pytest.raises(AstroError):
+        g.solve_static(b, method=SOLVER_FGMRES_LEARNED, precond=p6)  # DOF per node differs
+    p = precond_init(4, 100.0, 3)
+    p.degree = 0
+    with pytest.raises(AstroError):
+        g.solve_static(b, method=SOLVER_FGMRES_LEARNED, precond=p)
+    p = precond_init(4, 100.0, 3)
+    with pytest.raises(AstroError):
+        g.precond_loss_grad(p, np.zeros((1, g.n)))  # zero sample
