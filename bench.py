@@ -40,8 +40,8 @@ def _parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=20)
-    p.add_argument("--precond-degree", type=int, default=8)
-    p.add_argument("--precond-ratio", type=float, default=100.0)
+    p.add_argument("--precond-degree", type=int, default=24)
+    p.add_argument("--precond-ratio", type=float, default=3000.0)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nx", type=int, default=64)
@@ -282,22 +282,29 @@ def run_ours(a):
         # white-noise samples; the training is a one-off cost outside the solve
         gt = AstroGPU(M.config2(nx=16, ny=8, nz=8, seed=101))
         gt.getElasticSolnLoad(1, export=False)
+        gt.assemble_fp32()
         gt.scaleElasticMPC()
-        p = precond_init(a.precond_degree, a.precond_ratio, 3)
+        p0 = precond_init(a.precond_degree, a.precond_ratio, 3)
         samples = np.random.default_rng(5).standard_normal((8, gt.n))
         t0 = time.perf_counter()
-        hist = gt.precond_train(p, samples, iters=20)
+        p, tinfo = gt.precond_train_validated(p0, samples, iters=20)
         train_s = time.perf_counter() - t0
         del gt
         for name, meth in (("fgmres_learned", SOLVER_FGMRES_LEARNED), ("fgmres_mixed", SOLVER_FGMRES_MIXED),
                            ("gmres_fp64", SOLVER_GMRES_JACOBI_FP64)):
-            u, stt = g.solve_static(b, method=meth, rtol=1e-10, restart=50, max_iters=a.solve_max_iters,
-                                    allow_maxit=True, precond=p if meth == SOLVER_FGMRES_LEARNED else None)
-            res[name] = {"seconds": stt.seconds, "iterations": stt.iterations, "restarts": stt.restarts,
-                         "refinements": stt.refinements, "rel_residual": stt.rel_residual, "status": stt.status}
+            # first call: workspace allocation, graph capture and instantiation included; the
+            # second call reuses them (the steady state of repeated solves on one model)
+            kw = dict(method=meth, rtol=1e-10, restart=50, max_iters=a.solve_max_iters, allow_maxit=True,
+                      precond=p if meth == SOLVER_FGMRES_LEARNED else None)
+            u, st1 = g.solve_static(b, **kw)
+            u, stt = g.solve_static(b, **kw)
+            res[name] = {"seconds": stt.seconds, "first_call_seconds": st1.seconds, "iterations": stt.iterations, "restarts": stt.restarts,
+                         "refinements": stt.refinements, "rel_residual": stt.rel_residual, "status": stt.status,
+                         "conditional_graph": stt.conditional_graph}
         res["fgmres_learned"].update({"degree": p.degree, "ratio": p.ratio, "train_seconds": train_s,
-                                      "train_loss": [float(hist[0]), float(hist[-1])],
-                                      "train_mesh": "16x8x8 block, seed 101, 8 white-noise samples, 20 CG steps"})
+                                      "training": tinfo,
+                                      "train_mesh": "16x8x8 block, seed 101, 8 white-noise samples, 20 CG steps, "
+                                                    "validated by a solve of that block"})
         res["metric"] = "s to 1e-10 FP64 rel resid (restart 50; the learned solver includes its eigenvalue estimate)"
         line["solve"] = res
     # CPU baseline: oracle, 1 core, bounded sample

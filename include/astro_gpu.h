@@ -110,7 +110,7 @@ typedef struct astro_state {
  * with T_k the Chebyshev polynomials (one sparse matrix-vector product per hop) and W_k one
  * dpn x dpn weight per hop, shared by all nodes: a linear graph network on the mesh whose node
  * features are the DOF of a node.  weights[(k * dpn + i) * dpn + j] = W_k[i][j]. */
-#define ASTRO_PRECOND_MAX_DEGREE 16
+#define ASTRO_PRECOND_MAX_DEGREE 32
 typedef struct astro_precond {
     int32_t degree;          /* 1..ASTRO_PRECOND_MAX_DEGREE */
     int32_t dpn;             /* DOF per node of the model the weights are for (3 or 6) */
@@ -131,7 +131,7 @@ typedef struct astro_solve_opts {
     double rtol;             /* target ||b - A x||_2 / ||b||_2 in FP64 with A = K + C^T C */
     double inner_rtol;       /* inner relative tolerance for the refinement methods */
     const astro_precond *precond;  /* ASTRO_SOLVER_FGMRES_LEARNED: the network (NULL: the
-                                      Chebyshev initialisation of degree 8, ratio 100) */
+                                      Chebyshev initialisation of degree 24, ratio 3000) */
 } astro_solve_opts;
 
 typedef struct astro_solve_stats {
@@ -141,6 +141,9 @@ typedef struct astro_solve_stats {
     int32_t status;          /* ASTRO_OK or error code */
     double rel_residual;     /* final FP64 true relative residual */
     double seconds;          /* device time of the solve, CUDA events */
+    int32_t conditional_graph;  /* 1: the restart cycles ran as CUDA graphs whose Arnoldi steps sit
+                                   behind conditional nodes (skipped after convergence); 0: the
+                                   unrolled graph (the driver refused conditional nodes) */
 } astro_solve_stats;
 
 typedef struct astro_ctx astro_ctx;

@@ -40,7 +40,7 @@ class DimsC(C.Structure):
                                          "num_blocks", "num_colors")]
 
 
-PRECOND_MAX_DEGREE = 16
+PRECOND_MAX_DEGREE = 32
 
 
 class PrecondC(C.Structure):
@@ -67,7 +67,8 @@ class SolveOptsC(C.Structure):
 
 class SolveStatsC(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("restarts", C.c_int32), ("refinements", C.c_int32),
-                ("status", C.c_int32), ("rel_residual", C.c_double), ("seconds", C.c_double)]
+                ("status", C.c_int32), ("rel_residual", C.c_double), ("seconds", C.c_double),
+                ("conditional_graph", C.c_int32)]
 
 
 class NewmarkOptsC(C.Structure):
@@ -149,7 +150,7 @@ def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
-def precond_init(degree=8, ratio=100.0, dpn=3):
+def precond_init(degree=24, ratio=3000.0, dpn=3):
     """Untrained polynomial preconditioner: W_k = c_k I from the Chebyshev least-squares fit of 1/nu."""
     p = PrecondC()
     rc = load_library().astro_precond_init(degree, ratio, dpn, C.byref(p))
@@ -375,6 +376,24 @@ class AstroGPU:
         hist = np.zeros(iters + 1)
         self._check(self.L.astro_precond_train(self.h, C.byref(p), _d(S), S.shape[0], iters, _d(hist)))
         return hist
+
+    def precond_train_validated(self, p, samples, iters=20, rhs=None, rtol=1e-8):
+        """Trains a copy of p on samples, then solves this model (right-hand side rhs, default the
+        static load; needs the FP32 assembly) with the learned solver under both weight sets and
+        keeps the trained weights only when they need fewer Krylov iterations.  The quadratic
+        training loss weights the spectrum by the samples, and a lower loss does not always mean
+        faster GMRES convergence; the validation solve guards against that.
+        Returns (network, info)."""
+        q = PrecondC()
+        C.memmove(C.byref(q), C.byref(p), C.sizeof(PrecondC))
+        hist = self.precond_train(q, samples, iters)
+        b = self.static_rhs() if rhs is None else rhs
+        _, s0 = self.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=rtol, precond=p, allow_maxit=True)
+        _, s1 = self.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=rtol, precond=q, allow_maxit=True)
+        ok = s1.status == ASTRO_OK and (s0.status != ASTRO_OK or s1.iterations < s0.iterations)
+        info = {"loss": [float(hist[0]), float(hist[-1])], "val_iters_initial": int(s0.iterations),
+                "val_iters_trained": int(s1.iterations), "selected": "trained" if ok else "initial"}
+        return (q if ok else p), info
 
     # -- convenience ----------------------------------------------------------------------------
     def static_rhs(self, mpc_rhs_scaled=True):

@@ -62,6 +62,9 @@ struct AstroPrep {
 
 struct astro_ctx {
     std::string err;
+    // workspaces of the static solvers (FP64, mixed, learned), kept with their restart-cycle graphs
+    // across solves; owned by the Krylov unit (krylov_release)
+    void *solveWork[3] = {nullptr, nullptr, nullptr};
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // copies that overlap the element kernels
     int device = 0;
@@ -170,6 +173,7 @@ int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, 
 int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *d_acc);          // elem_hex8.cu
 int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &s, double *d_acc,
                 double *d_intAcc);                                                              // elem_shell4.cu
+void krylov_release(astro_ctx *ctx);
 int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,
                    double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup, double *d_hist,
                    astro_solve_stats *st);  // krylov.cu

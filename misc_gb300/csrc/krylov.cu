@@ -20,6 +20,8 @@
 //   * precision: the plain solver runs in FP64 throughout (the comparator).  The mixed solver
 //     runs the Krylov cycles in FP32 (FP32 matrix and basis) inside an FP64 iterative refinement
 //     whose residual b - A x is formed in FP64 arithmetic.
+#include <cuda_fp16.h>
+
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -30,6 +32,18 @@
 using namespace astro_kry;
 
 namespace {
+
+// Device-side control of a restart cycle captured as a chain of conditional IF nodes, each holding
+// two Arnoldi steps: the kernel that finishes a step (and the cycle start) sets the next node's
+// condition to "not done", and a node whose condition is zero skips its steps without launching
+// them.  The chain has a fixed length, so the number of steps is bounded whatever the conditions.
+struct LoopCond {
+    cudaGraphConditionalHandle h;
+    int use;
+};
+__device__ __forceinline__ void loop_cond_set(const LoopCond &lc, unsigned v) {
+    if (lc.use) cudaGraphSetConditional(lc.h, v);
+}
 
 // Partial dot products of the staged tile sw (cnt vector rows from row0, at most ROWS) with
 // V[0..j], and with itself when self is set (stored as vector kMaxM): part[k * nCh + cta].
@@ -161,38 +175,51 @@ __device__ void step_control(GmresCtl *ctl, const double *part, int nCh, int m) 
 }
 
 // v_j = wprev * inv (written to V[j]); w = A D^-1 v_j = inv * A zprev with zprev = D^-1 wprev.
-// kRowThreads threads per block row; the products accumulate in the precision of the basis.
+// Warp-per-slot-group mapping (kRowThreads warps per 32 block rows, partials met in shared
+// memory); the products accumulate in the precision of the basis.
 template <class TM, class TV, int DPN>
 __global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restrict__ V, size_t ld, const TV *__restrict__ wprev,
                                                         const TV *__restrict__ zprev, TV *__restrict__ w,
                                                         const GmresCtl *__restrict__ ctl) {
     if (ctl->done) return;
-    const int tid = blockIdx.x * kThreads + threadIdx.x;
-    const int r = tid / kRowThreads, sub = tid % kRowThreads;
-    // every lane takes part in the row shuffles: lanes past the last row work on the last row
-    // and write nothing
-    const bool valid = r < op.N;
-    const int rr = valid ? r : op.N - 1;
+    const CtaRow c = cta_row(op.N);  // (the FP64 branch keeps the CTA's 64 rows, lane-grouped)
     const int j = ctl->j;
     const TV inv = (TV)ctl->inv;
-    TV y[DPN];
-    ell_row_part<TV, TM, TV, DPN>(op, rr, sub, zprev, y);
-    if (!valid) return;
+    TV y[DPN] = {};
+    if (sizeof(TM) == 8) {
+        // FP64 comparator: kRowThreads adjacent lanes per block row, partials combined by shuffles
+        // (the FP64 products bound this kernel, not its loads); same grid, rows renumbered
+        const int r = blockIdx.x * kCtaRows + (int)threadIdx.x / kRowThreads, sub = threadIdx.x % kRowThreads;
+        const int rr = r < op.N ? r : op.N - 1;
+        ell_row_part<TV, TM, TV, DPN>(op, rr, sub, zprev, y);
+        if (r >= op.N) return;
+#pragma unroll
+        for (int q = 0; q < DPN; ++q) {
+            if (q % kRowThreads != sub) continue;
+            const size_t i = (size_t)r * DPN + q;
+            V[(size_t)j * ld + i] = wprev[i] * inv;
+            w[i] = y[q] * inv;
+        }
+        return;
+    }
+    if (c.valid) ell_row_group<TV, TM, TV, DPN>(op, c.r, c.sub, zprev, y);
+    if (!ell_cta_reduce<TV, DPN>(y, c) || !c.valid) return;
 #pragma unroll
     for (int q = 0; q < DPN; ++q) {
-        if (q % kRowThreads != sub) continue;
-        const size_t i = (size_t)r * DPN + q;
+        const size_t i = (size_t)c.r * DPN + q;
         V[(size_t)j * ld + i] = wprev[i] * inv;
         w[i] = y[q] * inv;
     }
 }
 
-// One hop of the polynomial preconditioner P v = sum_k W_k T_k(xi(D^-1 A)) D^-1 v / lambda:
-// with u = D^-1 A y_k, y_{k+1} = c (u - theta y_k) - [k > 0] y_{k-1} (the Chebyshev three-term
-// recurrence in the shifted and scaled variable), and z += W_{k+1} y_{k+1} per node (the first hop
-// also adds W_0 y_0).  kRowThreads threads per block row as in the SpMV; each thread then has the
-// whole node's y_{k+1} and writes its share of the components.  Weights arrive in the parameter
-// space already divided by lambda.
+// One hop of the polynomial preconditioner P v = sum_k W_k T_k(xi(D^-1 A)) D^-1 v / lambda,
+// evaluated in the symmetrically scaled space: with S = D^-1/2 and A^ = S A S (unit diagonal,
+// entries in [-1, 1], kept in FP16), T_k(xi(D^-1 A)) D^-1 = S T_k(xi(A^)) S, so the hops run on
+// y^_k = T_k(xi(A^)) S v and the node outputs are W_k (S y^_k).  With u = A^ y^_k,
+// y^_{k+1} = c (u - theta y^_k) - [k > 0] y^_{k-1} (the Chebyshev three-term recurrence in the
+// shifted and scaled variable) and z += W_{k+1} S y^_{k+1} per node (the first hop also adds
+// W_0 S y^_0).  Same row mapping as the SpMV step; the slot-group-0 thread of a row then has the
+// whole node's A^ y^_k and finishes the row.  The weights arrive already divided by lambda.
 struct HopArgs {
     float w[36];   // W_{k+1} / lambda, row-major dpn x dpn
     float w0[36];  // W_0 / lambda (first hop)
@@ -201,63 +228,99 @@ struct HopArgs {
 };
 
 template <class TM, class TV, int DPN>
-__global__ void __launch_bounds__(kThreads) k_poly_hop(Op<TM> op, const TV *__restrict__ dinv, const TV *__restrict__ yk,
+__global__ void __launch_bounds__(kThreads) k_poly_hop(Op<TM> op, const TV *__restrict__ dsq, const TV *__restrict__ yk,
                                                        const TV *__restrict__ ykm1, TV *__restrict__ ykp1,
                                                        TV *__restrict__ zacc, const HopArgs h,
                                                        const GmresCtl *__restrict__ ctl, int always) {
     if (!always && ctl->done) return;
-    const int tid = blockIdx.x * kThreads + threadIdx.x;
-    const int r = tid / kRowThreads, sub = tid % kRowThreads;
-    const bool valid = r < op.N;
-    const int rr = valid ? r : op.N - 1;
-    TV t[DPN];
-    ell_row_part<TV, TM, TV, DPN>(op, rr, sub, yk, t);
-    if (!valid) return;
-    const size_t base = (size_t)r * DPN;
-    TV yc[DPN], yn[DPN];
-#pragma unroll
-    for (int q = 0; q < DPN; ++q) yc[q] = yk[base + q];
+    const CtaRow c = cta_row(op.N);
+    TV t[DPN] = {};
+    if (c.valid) ell_row_group<TV, TM, TV, DPN>(op, c.r, c.sub, yk, t);
+    if (!ell_cta_reduce<TV, DPN>(t, c) || !c.valid) return;
+    const size_t base = (size_t)c.r * DPN;
+    TV yc[DPN], yn[DPN], sc[DPN];
 #pragma unroll
     for (int q = 0; q < DPN; ++q) {
-        const TV u = dinv[base + q] * t[q] - (TV)h.theta * yc[q];
-        yn[q] = (TV)h.c * u;
+        yc[q] = yk[base + q];
+        sc[q] = dsq[base + q];
+    }
+#pragma unroll
+    for (int q = 0; q < DPN; ++q) {
+        yn[q] = (TV)h.c * (t[q] - (TV)h.theta * yc[q]);
         if (!h.first) yn[q] -= ykm1[base + q];
     }
 #pragma unroll
     for (int q = 0; q < DPN; ++q) {
-        if (q % kRowThreads != sub) continue;
         if (ykp1) ykp1[base + q] = yn[q];
         TV z = h.first ? TV(0) : zacc[base + q];
         if (h.first) {
 #pragma unroll
-            for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w0[q * DPN + jj] * yc[jj];
+            for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w0[q * DPN + jj] * (sc[jj] * yc[jj]);
         }
 #pragma unroll
-        for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w[q * DPN + jj] * yn[jj];
+        for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w[q * DPN + jj] * (sc[jj] * yn[jj]);
         zacc[base + q] = z;
     }
 }
 
+// A^ = S A S in FP16 block-ELL (same slots and columns as the solver copy), S = diag(dsq):
+// one thread per (row, slot); and the scaled penalty values of the rows.
+template <int DPN>
+__global__ void k_scaled_half(const float *__restrict__ K, const int *__restrict__ col, int S, int ld, int N,
+                              const float *__restrict__ dsq, __half *__restrict__ Kh) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)S * ld) return;
+    const int s = (int)(t / ld), r = (int)(t - (long long)s * ld);
+    constexpr int dd = DPN * DPN;
+    if (r >= N) {
+        for (int q = 0; q < dd; ++q) Kh[((size_t)s * dd + q) * ld + r] = __float2half_rn(0.f);
+        return;
+    }
+    const int c = col[(size_t)s * ld + r];
+#pragma unroll
+    for (int i = 0; i < DPN; ++i)
+#pragma unroll
+        for (int j = 0; j < DPN; ++j) {
+            const size_t a = ((size_t)s * dd + i * DPN + j) * ld + r;
+            Kh[a] = __float2half_rn(K[a] * dsq[(size_t)r * DPN + i] * dsq[(size_t)c * DPN + j]);
+        }
+}
+
+__global__ void k_scaled_pen(const int *__restrict__ penPtr, const int *__restrict__ penRow,
+                             const int *__restrict__ penCol, const double *__restrict__ penVal, int N, int dpn,
+                             const double *__restrict__ dinv, double *__restrict__ out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= N) return;
+    for (int t = penPtr[r]; t < penPtr[r + 1]; ++t)
+        out[t] = penVal[t] * sqrt(dinv[(size_t)r * dpn + penRow[t]] * dinv[penCol[t]]);
+}
+
+__global__ void k_sqrt_f(const double *__restrict__ dinv, float *__restrict__ dsq, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dsq[i] = (float)sqrt(dinv[i]);
+}
+
 // Power iteration for the largest eigenvalue of D^-1 A: y = s D^-1 A x with s = scal[0] (the
-// reciprocal norm of x from the previous step), one thread per block row; the last CTA sums the
+// reciprocal norm of x from the previous step), SpMV-step row mapping; the last CTA sums the
 // per-CTA ||y||^2 in CTA order and sets scal[1] = ||y||, scal[0] = 1 / ||y||.  Every CTA reads
-// scal[0] before it arrives, so the last one may overwrite it.
+// scal[0] before it arrives, so the last one may overwrite it.  dinv null: the operator is
+// already scaled (A^ = D^-1/2 A D^-1/2, the same spectrum as D^-1 A).
 template <class TM, class TV, int DPN>
 __global__ void __launch_bounds__(kThreads) k_power_step(Op<TM> op, const TV *__restrict__ dinv, const TV *__restrict__ x,
                                                          TV *__restrict__ y, double *part, unsigned *counter,
                                                          double *scal) {
     __shared__ double sp[kWarps];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int row = blockIdx.x * kThreads + threadIdx.x;
+    const CtaRow c = cta_row(op.N);
     const TV s = (TV)scal[0];
     double yy = 0.0;
-    if (row < op.N) {
-        TV t[DPN];
-        ell_row<TV, TM, TV, DPN>(op, row, x, t);
+    TV t[DPN] = {};
+    if (c.valid) ell_row_group<TV, TM, TV, DPN>(op, c.r, c.sub, x, t);
+    if (ell_cta_reduce<TV, DPN>(t, c) && c.valid) {
 #pragma unroll
         for (int q = 0; q < DPN; ++q) {
-            const size_t i = (size_t)row * DPN + q;
-            const TV v = s * dinv[i] * t[q];
+            const size_t i = (size_t)c.r * DPN + q;
+            const TV v = s * (dinv ? dinv[i] : TV(1)) * t[q];
             y[i] = v;
             yy += (double)v * (double)v;
         }
@@ -331,7 +394,8 @@ template <class TV>
 __global__ void __launch_bounds__(kGsThreads, 2) k_update(int n, const TV *__restrict__ V, size_t ld, TV *__restrict__ w,
                                                           GmresCtl *__restrict__ ctl, double *__restrict__ partDots,
                                                           double *__restrict__ partNorm, int nCh, int pass,
-                                                          const TV *__restrict__ dinv, TV *__restrict__ z, int m) {
+                                                          const TV *__restrict__ dinv, TV *__restrict__ z, int m,
+                                                          LoopCond lc) {
     constexpr int ROWS = kChunk;
     if (ctl->done) return;
     const bool second = ctl->reorth != 0;
@@ -381,7 +445,10 @@ __global__ void __launch_bounds__(kGsThreads, 2) k_update(int n, const TV *__res
             partNorm[blockIdx.x] = s;
             __threadfence();
         }
-        if (last_to_arrive(&ctl->arrive[2])) step_control(ctl, partNorm, nCh, m);
+        if (last_to_arrive(&ctl->arrive[2])) {
+            step_control(ctl, partNorm, nCh, m);
+            if (threadIdx.x == 0) loop_cond_set(lc, ctl->done ? 0u : 1u);
+        }
     }
 }
 
@@ -485,7 +552,7 @@ __global__ void __launch_bounds__(kThreads) k_residual(Op<TM> op, const TX *__re
 }
 
 // Start of a cycle: beta = ||r||, inv = 1/beta, g = [beta, 0...], j = 0.
-__global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, const double *targetAbsPtr) {
+__global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, const double *targetAbsPtr, LoopCond lc) {
     const double targetAbs = *targetAbsPtr;
     const int lane = threadIdx.x;
     double a = 0.0;
@@ -504,6 +571,7 @@ __global__ void k_cycle_start(GmresCtl *ctl, const double *part, int nparts, con
     ctl->inv = beta > 0.0 ? 1.0 / beta : 0.0;
     ctl->target = targetAbs;
     ctl->done = (beta <= targetAbs || beta == 0.0 || ctl->nonfinite) ? 1 : 0;
+    loop_cond_set(lc, ctl->done ? 0u : 1u);
 }
 
 __global__ void k_zero_f(float *a, int n) {
@@ -559,17 +627,25 @@ __global__ void k_to_ell(const T *__restrict__ K, const int *__restrict__ rowPtr
 struct PolyHost {
     int deg = 0;
     float theta = 0.f, delta = 0.f;
-    float W[(ASTRO_PRECOND_MAX_DEGREE + 1) * 36];
+    float W[(ASTRO_PRECOND_MAX_DEGREE + 1) * 36] = {};
 };
 
 struct GmresWork {
     DevBuf V, w0, w1, z0, z1, part, ctl, dinv, dinvT, rres, xs, tgt;
+    DevBuf x64, b64;  // FP64 solver: the solve's x and b live here, so its graph is reused across solves
     DevBuf yB0, yB1, zacc, pw;  // polynomial preconditioner: hop vectors, output, power-iteration scratch
+    DevBuf Kh, penS, dsqT;      // its operator A^ = S A S (FP16 block-ELL, scaled penalty) and S
+    cudaStream_t bodyStream = nullptr;  // captures the bodies of the cycle's IF nodes
+    bool condOk = true;                 // conditional graph nodes available
+    Op<__half> hop;
     const PolyHost *poly = nullptr;
+    // vector that scales a residual into the preconditioner's input: D^-1 (Jacobi) or S (poly)
+    template <class TV> const TV *y0s() { return poly ? dptr<TV>(dsqT) : dptr<TV>(dinvT); }
     // restart cycle captured as a graph, reused while the matrix and vectors stay the same
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     const void *gK = nullptr, *gx = nullptr, *gb = nullptr;
+    PolyHost gPoly;  // the hop parameters the graph was captured with
     int n = 0, m = 0;
     size_t ld = 0;
     int nChunks = 0, nRowCtas = 0;
@@ -630,13 +706,12 @@ template <class TM> static Op<TM> make_op(astro_ctx *ctx, const TM *Kell) {
 // recurrence rotates through y0 and two scratch vectors) and returns the output vector P v.
 // always: run even when the cycle has finished (the final update of x).
 template <class TM, class TV, int DPN>
-static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, TV *y0, int always) {
+static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, TV *y0, int always, cudaStream_t s) {
     const PolyHost &P = *W.poly;
-    cudaStream_t s = ctx->stream;
     const int dd = DPN * DPN;
     TV *buf[3] = {y0, dptr<TV>(W.yB0), dptr<TV>(W.yB1)};
     TV *z = dptr<TV>(W.zacc);
-    const unsigned grid = (unsigned)(((long long)ctx->P.N * kRowThreads + kThreads - 1) / kThreads);
+    const unsigned grid = (unsigned)((ctx->P.N + kCtaRows - 1) / kCtaRows);
     HopArgs h;
     std::memset(&h, 0, sizeof(h));
     for (int q = 0; q < dd; ++q) h.w0[q] = P.W[q];
@@ -647,7 +722,7 @@ static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, TV *y0, 
         for (int q = 0; q < dd; ++q) h.w[q] = P.W[(k + 1) * dd + q];
         h.first = (k == 0);
         h.c = (k == 0 ? 1.f : 2.f) / P.delta;
-        k_poly_hop<TM, TV, DPN><<<grid, kThreads, 0, s>>>(op, dptr<TV>(W.dinvT), buf[cur], buf[prv],
+        k_poly_hop<__half, TV, DPN><<<grid, kThreads, 0, s>>>(W.hop, dptr<TV>(W.dsqT), buf[cur], buf[prv],
                                                           k + 1 < P.deg ? buf[nxt] : nullptr, z, h,
                                                           dptr<GmresCtl>(W.ctl), always);
         cur = nxt;
@@ -655,26 +730,28 @@ static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, TV *y0, 
     return z;
 }
 
+// Enqueues Arnoldi steps first..first+nsteps-1 on s (the w/z buffers alternate with the step's
+// parity); with lc.use each step's control sets the condition lc (of the next IF node).
 template <class TM, class TV, int DPN>
-static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m) {
-    cudaStream_t s = ctx->stream;
+static void enqueue_cycle(astro_ctx *ctx, GmresWork &W, const Op<TM> &op, int m, int first, int nsteps,
+                          cudaStream_t s, LoopCond lc) {
     TV *V = dptr<TV>(W.V), *wa = dptr<TV>(W.w0), *wb = dptr<TV>(W.w1);
     TV *za = dptr<TV>(W.z0), *zb = dptr<TV>(W.z1);
     GmresCtl *ctl = dptr<GmresCtl>(W.ctl);
     double *part = dptr<double>(W.part);
-    const TV *dinv = dptr<TV>(W.dinvT);
+    const TV *dinv = W.y0s<TV>();
     const int n = W.n;
     double *partB = part + (size_t)(kMaxM + 1) * W.nChunks;
     double *partN = partB + (size_t)(kMaxM + 1) * W.nChunks;  // per-CTA ||w||^2 of the step's last update
-    const unsigned spmvGrid = (unsigned)(((long long)ctx->P.N * kRowThreads + kThreads - 1) / kThreads);
-    for (int step = 0; step < m; ++step) {
+    const unsigned spmvGrid = (unsigned)((ctx->P.N + kCtaRows - 1) / kCtaRows);
+    for (int step = first; step < first + nsteps; ++step) {
         TV *wprev = (step % 2 == 0) ? wa : wb, *zprev = (step % 2 == 0) ? za : zb;
         TV *wnew = (step % 2 == 0) ? wb : wa, *znew = (step % 2 == 0) ? zb : za;
-        const TV *zin = W.poly ? enqueue_poly<TM, TV, DPN>(ctx, W, op, zprev, 0) : zprev;
+        const TV *zin = W.poly ? enqueue_poly<TM, TV, DPN>(ctx, W, zprev, 0, s) : zprev;
         k_spmv_step<TM, TV, DPN><<<spmvGrid, kThreads, 0, s>>>(op, V, W.ld, wprev, zin, wnew, ctl);
         k_dots<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, part, W.nChunks);
-        k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 0, dinv, znew, m);
-        k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 1, dinv, znew, m);
+        k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 0, dinv, znew, m, lc);
+        k_update<TV><<<W.nChunks, kGsThreads, 0, s>>>(n, V, W.ld, wnew, ctl, partB, partN, W.nChunks, 1, dinv, znew, m, lc);
     }
 }
 
@@ -700,27 +777,102 @@ static int gmres_solve(astro_ctx *ctx, GmresWork &W, const TM *K, TV *x, const d
     double *part = dptr<double>(W.part);
     // the absolute target is read by the graph from device memory
     CK(cudaMemcpyAsync(W.tgt.p, &tgtAbs, sizeof(double), cudaMemcpyHostToDevice, s));
-    if (!(W.exec && W.gK == K && W.gx == x && W.gb == b)) {
+    const bool samePoly = W.poly ? (W.gPoly.deg == W.poly->deg && std::memcmp(&W.gPoly, W.poly, sizeof(PolyHost)) == 0)
+                                 : W.gPoly.deg == 0;
+    if (!(W.exec && W.gK == K && W.gx == x && W.gb == b && samePoly)) {
         if (W.exec) cudaGraphExecDestroy(W.exec);
         if (W.graph) cudaGraphDestroy(W.graph);
         W.exec = nullptr;
         W.graph = nullptr;
-        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, dptr<TV>(W.w0), part, dptr<TV>(W.dinvT),
-                                                                     dptr<TV>(W.z0));
-        k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, dptr<double>(W.tgt));
-        enqueue_cycle<TM, TV, DPN>(ctx, W, op, m);
-        k_lsq<<<1, 1, 0, s>>>(ctl);
-        if (W.poly) {
-            TV *y0 = dptr<TV>(W.z0);
-            k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x, y0);
-            TV *dz = enqueue_poly<TM, TV, DPN>(ctx, W, op, y0, 1);
-            k_add<TV><<<(W.n + 255) / 256, 256, 0, s>>>(W.n, x, dz);
-        } else {
-            k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x);
+        const LoopCond none{0, 0};
+        // the Arnoldi steps of a cycle behind conditional IF nodes (two steps each), or, when the
+        // driver does not take conditional nodes, unrolled to m steps that turn into no-ops once
+        // the cycle has finished
+        bool cond = W.condOk;
+        for (int attempt = 0; attempt < 2 && !W.graph; ++attempt) {
+            CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            k_residual<TM, TV, TV, DPN><<<W.nRowCtas, kThreads, 0, s>>>(op, x, b, dptr<TV>(W.w0), part, W.y0s<TV>(),
+                                                                         dptr<TV>(W.z0));
+            // one handle per IF node (a handle belongs to one node): the cycle start sets the first,
+            // the steps behind node i set the handle of node i + 1; every handle starts each
+            // launch at 0, so the nodes after a skipped one are skipped too
+            const int nIf = (m + 1) / 2;
+            std::vector<cudaGraphConditionalHandle> hs(nIf, 0);
+            cudaGraph_t cg = nullptr;
+            cudaError_t ce = cudaSuccess;
+            bool useCond = false;
+            if (cond) {
+                cudaStreamCaptureStatus cs;
+                ce = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg);
+                for (int i = 0; i < nIf && ce == cudaSuccess; ++i)
+                    ce = cudaGraphConditionalHandleCreate(&hs[i], cg, 0, cudaGraphCondAssignDefault);
+                useCond = ce == cudaSuccess;
+            }
+            k_cycle_start<<<1, 32, 0, s>>>(ctl, part, W.nRowCtas, dptr<double>(W.tgt),
+                                           useCond ? LoopCond{hs[0], 1} : none);
+            if (useCond) {
+                // ceil(m/2) IF nodes in sequence, two steps in each
+                for (int first = 0; first < m && ce == cudaSuccess; first += 2) {
+                    const int i = first / 2;
+                    const LoopCond next = (i + 1 < nIf) ? LoopCond{hs[i + 1], 1} : none;
+                    cudaStreamCaptureStatus cs;
+                    const cudaGraphNode_t *deps = nullptr;
+                    const cudaGraphEdgeData *ed = nullptr;
+                    size_t nd = 0;
+                    ce = cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, &ed, &nd);
+                    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+                    cp.conditional.handle = hs[i];
+                    cp.conditional.type = cudaGraphCondTypeIf;
+                    cp.conditional.size = 1;
+                    cudaGraphNode_t cn = nullptr;
+                    if (ce == cudaSuccess) ce = cudaGraphAddNode(&cn, cg, deps, ed, nd, &cp);
+                    if (ce == cudaSuccess)
+                        ce = cudaStreamBeginCaptureToGraph(W.bodyStream, cp.conditional.phGraph_out[0], nullptr, nullptr,
+                                                           0, cudaStreamCaptureModeRelaxed);
+                    if (ce == cudaSuccess) {
+                        enqueue_cycle<TM, TV, DPN>(ctx, W, op, m, first, std::min(2, m - first), W.bodyStream, next);
+                        cudaGraph_t body = nullptr;
+                        ce = cudaStreamEndCapture(W.bodyStream, &body);
+                    }
+                    if (ce == cudaSuccess)
+                        ce = cudaStreamUpdateCaptureDependencies(s, &cn, nullptr, 1, cudaStreamSetCaptureDependencies);
+                }
+            } else {
+                enqueue_cycle<TM, TV, DPN>(ctx, W, op, m, 0, m, s, none);
+            }
+            k_lsq<<<1, 1, 0, s>>>(ctl);
+            if (W.poly) {
+                TV *y0 = dptr<TV>(W.z0);
+                k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, W.y0s<TV>(), ctl, x, y0);
+                TV *dz = enqueue_poly<TM, TV, DPN>(ctx, W, y0, 1, s);
+                k_add<TV><<<(W.n + 255) / 256, 256, 0, s>>>(W.n, x, dz);
+            } else {
+                k_xupdate<TV, TV><<<4 * 152, kThreads, 0, s>>>(W.n, dptr<TV>(W.V), W.ld, dptr<TV>(W.dinvT), ctl, x);
+            }
+            cudaGraph_t g = nullptr;
+            cudaError_t ee = cudaStreamEndCapture(s, &g);
+            if (cond && (ce != cudaSuccess || ee != cudaSuccess)) {
+                // conditional nodes refused: clear the error state and capture the unrolled cycle
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                cond = W.condOk = false;
+                continue;
+            }
+            CK(ee);
+            cudaError_t ie = cudaGraphInstantiate(&W.exec, g, 0);
+            if (cond && ie != cudaSuccess) {
+                cudaGraphDestroy(g);
+                W.exec = nullptr;
+                cudaGetLastError();
+                cond = W.condOk = false;
+                continue;
+            }
+            if (ie != cudaSuccess) cudaGraphDestroy(g);
+            CK(ie);
+            W.graph = g;
         }
-        CK(cudaStreamEndCapture(s, &W.graph));
-        CK(cudaGraphInstantiate(&W.exec, W.graph, 0));
+        if (W.poly) W.gPoly = *W.poly;
+        else W.gPoly.deg = 0;
         W.gK = K;
         W.gx = x;
         W.gb = b;
@@ -770,17 +922,51 @@ static int work_alloc(astro_ctx *ctx, GmresWork &W, int m, int tv) {
     if ((rc = dev_alloc(ctx, W.xs, sizeof(float) * (size_t)n))) return rc;
     if ((rc = dev_alloc(ctx, W.tgt, sizeof(double)))) return rc;
     CK(cudaMemsetAsync(W.ctl.p, 0, sizeof(GmresCtl), ctx->stream));
+    CK(cudaStreamCreateWithFlags(&W.bodyStream, cudaStreamNonBlocking));
     return ASTRO_OK;
 }
 
 static void work_free(GmresWork &W) {
+    if (W.bodyStream) cudaStreamDestroy(W.bodyStream);
+    W.bodyStream = nullptr;
     if (W.exec) cudaGraphExecDestroy(W.exec);
     if (W.graph) cudaGraphDestroy(W.graph);
     W.exec = nullptr;
     W.graph = nullptr;
     DevBuf *b[] = {&W.V,    &W.w0,   &W.w1,    &W.z0, &W.z1,  &W.part, &W.ctl, &W.dinv,
-                   &W.dinvT, &W.rres, &W.xs,  &W.tgt, &W.yB0, &W.yB1,  &W.zacc, &W.pw};
+                   &W.dinvT, &W.rres, &W.xs,  &W.tgt, &W.yB0, &W.yB1,  &W.zacc, &W.pw,
+                   &W.Kh,    &W.penS, &W.dsqT, &W.x64, &W.b64};
     for (auto *x : b) dev_free(*x);
+}
+
+// Solver workspace of one method kept on the context (slot 0 FP64, 1 mixed, 2 learned), with its
+// captured restart-cycle graph; reallocated when the basis size changes.
+static GmresWork *work_get(astro_ctx *ctx, int slot, int m, int tv, int *rc) {
+    GmresWork *W = static_cast<GmresWork *>(ctx->solveWork[slot]);
+    if (W && W->m == m && W->n == ctx->P.n) return W;
+    if (W) {
+        work_free(*W);
+        delete W;
+    }
+    W = new GmresWork();
+    ctx->solveWork[slot] = W;
+    if ((*rc = work_alloc(ctx, *W, m, tv))) {
+        work_free(*W);
+        delete W;
+        ctx->solveWork[slot] = nullptr;
+        return nullptr;
+    }
+    return W;
+}
+
+void krylov_release(astro_ctx *ctx) {
+    for (void *&p : ctx->solveWork) {
+        if (!p) continue;
+        GmresWork *W = static_cast<GmresWork *>(p);
+        work_free(*W);
+        delete W;
+        p = nullptr;
+    }
 }
 
 // r = b - A x with A from K64 (kind 64) or K32 (kind 32); returns ||r||/||b|| (||r|| if b = 0).
@@ -817,7 +1003,7 @@ static int true_residual(astro_ctx *ctx, GmresWork &W, int kind, const double *x
 template <class TM, class TV, int DPN>
 static int power_lambda(astro_ctx *ctx, const Op<TM> &op, const TV *dinv, double *lam) {
     const int n = ctx->P.n;
-    const int nCta = (ctx->P.N + kThreads - 1) / kThreads;
+    const int nCta = (ctx->P.N + kCtaRows - 1) / kCtaRows;
     cudaStream_t s = ctx->stream;
     DevBuf a, b, part, cnt, scal;
     int rc;
@@ -862,7 +1048,6 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     const int m = o->restart > 0 ? (o->restart > kMaxM ? kMaxM : o->restart) : 50;
     const int maxIters = o->max_iters > 0 ? o->max_iters : 200000;
     const int maxCycles = (maxIters + m - 1) / m;
-    GmresWork W;
     int rc = ASTRO_OK;
     int iters = 0, cycles = 0, refinements = 0;
     double rel = 0.0, est = 0.0, rn = 0.0, bn = 0.0;
@@ -871,17 +1056,17 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     astro_precond pdef;
     const astro_precond *pc = o->precond;
     if (learned && !pc) {
-        astro_precond_init(8, 100.0, ctx->P.dpn, &pdef);
+        astro_precond_init(24, 3000.0, ctx->P.dpn, &pdef);
         pc = &pdef;
     }
     if (learned && (rc = precond_check(ctx, pc))) return rc;
     PolyHost ph;
     if (fp64 && !ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
     if (!fp64 && !ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
-    if ((rc = work_alloc(ctx, W, m, fp64 ? sizeof(double) : sizeof(float)))) {
-        work_free(W);
-        return rc;
-    }
+    GmresWork *Wp = work_get(ctx, fp64 ? 0 : (learned ? 2 : 1), m, fp64 ? sizeof(double) : sizeof(float), &rc);
+    if (!Wp) return rc;
+    GmresWork &W = *Wp;
+    W.poly = nullptr;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -889,20 +1074,25 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     double *r = dptr<double>(W.rres);
     if (fp64) {
         const double *K64p = ell_of<double>(ctx, &rc);
-        if (rc) {
-            work_free(W);
-            return rc;
-        }
+        if (rc) return rc;
         k_dinv<double, double><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
             dptr<double>(ctx->d_K64), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn,
             ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
             dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<double>(W.dinvT));
-        rc = true_residual<DPN>(ctx, W, 64, nullptr, d_b, &rel, r, &rn, &bn);
+        if (!W.x64.p && ((rc = dev_alloc(ctx, W.x64, sizeof(double) * n)) || (rc = dev_alloc(ctx, W.b64, sizeof(double) * n)))) {
+            dev_free(W.x64);
+            return rc;
+        }
+        double *x = dptr<double>(W.x64);
+        const double *bb = dptr<double>(W.b64);
+        CK(cudaMemcpyAsync(W.x64.p, d_x, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(W.b64.p, d_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+        rc = true_residual<DPN>(ctx, W, 64, nullptr, bb, &rel, r, &rn, &bn);
         const double tgt = o->rtol * bn;
         while (rc == ASTRO_OK) {
-            int grc = gmres_solve<double, double, DPN>(ctx, W, K64p, d_x, d_b, tgt, maxCycles - cycles, m,
+            int grc = gmres_solve<double, double, DPN>(ctx, W, K64p, x, bb, tgt, maxCycles - cycles, m,
                                                        &iters, &cycles, &est);
-            if ((rc = true_residual<DPN>(ctx, W, 64, d_x, d_b, &rel, r))) break;
+            if ((rc = true_residual<DPN>(ctx, W, 64, x, bb, &rel, r))) break;
             if (rel <= o->rtol) break;
             if (grc == ASTRO_ERR_NAN) {
                 rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in GMRES");
@@ -913,26 +1103,43 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 break;
             }
         }
+        CK(cudaMemcpyAsync(d_x, W.x64.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     } else {
         const float *K32p = ell_of<float>(ctx, &rc);
-        if (rc) {
-            work_free(W);
-            return rc;
-        }
+        if (rc) return rc;
         k_dinv<float, float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
             dptr<float>(ctx->d_K32), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn,
             ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
             dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<float>(W.dinvT));
         if (learned) {
-            // the network's hop vectors, and the interval [lambda/ratio, lambda] from the
-            // eigenvalue estimate on the FP32 operator (inside the timed solve)
+            // the network's hop vectors, its operator A^ = S A S in FP16 with S = D^-1/2, and the
+            // interval [lambda/ratio, lambda] from the eigenvalue estimate on A^ (inside the timed
+            // solve)
             double lam = 0.0;
-            if ((rc = dev_alloc(ctx, W.yB0, sizeof(float) * n)) || (rc = dev_alloc(ctx, W.yB1, sizeof(float) * n)) ||
-                (rc = dev_alloc(ctx, W.zacc, sizeof(float) * n)) ||
-                (rc = power_lambda<float, float, DPN>(ctx, make_op<float>(ctx, K32p), dptr<float>(W.dinvT), &lam))) {
-                work_free(W);
+            const int S = ctx->ellSlots, ld = ctx->ellLd, dd = DPN * DPN;
+            // allocated once per workspace: the captured graph holds these pointers
+            if (!W.Kh.p &&
+                ((rc = dev_alloc(ctx, W.yB0, sizeof(float) * n)) || (rc = dev_alloc(ctx, W.yB1, sizeof(float) * n)) ||
+                 (rc = dev_alloc(ctx, W.zacc, sizeof(float) * n)) || (rc = dev_alloc(ctx, W.dsqT, sizeof(float) * n)) ||
+                 (rc = dev_alloc(ctx, W.penS, sizeof(double) * std::max(1, ctx->penRows))) ||  // penalty entries
+                 (rc = dev_alloc(ctx, W.Kh, sizeof(__half) * (size_t)S * dd * ld)))) {
+                dev_free(W.Kh);
                 return rc;
             }
+            k_sqrt_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(dptr<double>(W.dinv), dptr<float>(W.dsqT), n);
+            const long long tot = (long long)S * ld;
+            k_scaled_half<DPN><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(
+                K32p, dptr<int>(ctx->d_ellCol), S, ld, ctx->P.N, dptr<float>(W.dsqT), dptr<__half>(W.Kh));
+            W.hop = make_op<__half>(ctx, dptr<__half>(W.Kh));
+            if (ctx->penRows) {
+                k_scaled_pen<<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
+                    dptr<int>(ctx->d_penPtr), dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
+                    dptr<double>(ctx->d_penVal), ctx->P.N, DPN, dptr<double>(W.dinv), dptr<double>(W.penS));
+                W.hop.penVal = dptr<double>(W.penS);
+            }
+            if ((rc = cuda_check(ctx, cudaGetLastError(), "preconditioner operator")) ||
+                (rc = power_lambda<__half, float, DPN>(ctx, W.hop, (const float *)nullptr, &lam)))
+                return rc;
             lam *= pc->lambda_scale;
             ph.deg = pc->degree;
             ph.theta = (float)(0.5 * lam * (1.0 + 1.0 / pc->ratio));
@@ -970,7 +1177,6 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    work_free(W);
     if (st) {
         st->iterations = iters;
         st->restarts = cycles;
@@ -978,6 +1184,7 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
         st->status = rc;
         st->rel_residual = rel;
         st->seconds = ms * 1e-3;
+        st->conditional_graph = W.condOk ? 1 : 0;
     }
     if (rc == ASTRO_ERR_MAXIT) set_err(ctx, rc, "iteration limit reached before the residual tolerance");
     return rc;
@@ -1188,6 +1395,7 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
         st->status = rc ? rc : worst;
         st->rel_residual = worstRel;
         st->seconds = ms * 1e-3;
+        st->conditional_graph = W.condOk ? 1 : 0;
     }
     return rc;
 }

@@ -122,6 +122,94 @@ __device__ __forceinline__ void ell_row_part(const Op<TM> &op, int r, int sub, c
         for (int i = 0; i < DPN; ++i) y[i] += __shfl_xor_sync(0xffffffffu, y[i], m);
 }
 
+// Warp-per-slot-group SpMV mapping: a CTA of kThreads covers kCtaRows = 32 * kThreads / (32 *
+// kRowThreads) block rows; warp w takes the 32 consecutive rows (w / kRowThreads) * 32 + lane
+// and the slots s = w % kRowThreads, + kRowThreads, ...  Every value, column and penalty load of
+// a warp instruction then covers 32 consecutive rows of one (slot, entry) plane: one contiguous
+// segment.  The kRowThreads partials of a row meet in shared memory (ell_cta_reduce).
+constexpr int kCtaRows = kThreads / kRowThreads;
+
+struct CtaRow {
+    int r;     // block row
+    int sub;   // slot group (warp-uniform)
+    int rloc;  // row within the CTA
+    bool valid;
+};
+__device__ __forceinline__ CtaRow cta_row(int N) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    CtaRow c;
+    c.sub = w % kRowThreads;
+    c.rloc = (w / kRowThreads) * 32 + lane;
+    c.r = blockIdx.x * kCtaRows + c.rloc;
+    c.valid = c.r < N;
+    return c;
+}
+
+// Partial (A x)_r over the slots s = sub, sub + kRowThreads, ...; slot group 0 adds the penalty.
+template <class TA, class TM, class TX, int DPN>
+__device__ __forceinline__ void ell_row_group(const Op<TM> &op, int r, int sub, const TX *__restrict__ x, TA y[DPN]) {
+#pragma unroll
+    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
+    const size_t ld = (size_t)op.ld;
+    int s = sub;
+    // two slots per trip so that their column, x and value loads are in flight together
+    for (; s + kRowThreads < op.S; s += 2 * kRowThreads) {
+        const int c0 = __ldg(op.col + (size_t)s * ld + r);
+        const int c1 = __ldg(op.col + (size_t)(s + kRowThreads) * ld + r);
+        TA x0[DPN], x1[DPN];
+#pragma unroll
+        for (int jj = 0; jj < DPN; ++jj) {
+            x0[jj] = (TA)x[(size_t)c0 * DPN + jj];
+            x1[jj] = (TA)x[(size_t)c1 * DPN + jj];
+        }
+        const TM *k0 = op.K + (size_t)s * DPN * DPN * ld + r;
+        const TM *k1 = op.K + (size_t)(s + kRowThreads) * DPN * DPN * ld + r;
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj)
+                y[i] += (TA)__ldg(k0 + (size_t)(i * DPN + jj) * ld) * x0[jj] +
+                        (TA)__ldg(k1 + (size_t)(i * DPN + jj) * ld) * x1[jj];
+    }
+    if (s < op.S) {
+        const int c = __ldg(op.col + (size_t)s * ld + r);
+        TA xv[DPN];
+#pragma unroll
+        for (int jj = 0; jj < DPN; ++jj) xv[jj] = (TA)x[(size_t)c * DPN + jj];
+        const TM *kp = op.K + (size_t)s * DPN * DPN * ld + r;
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)__ldg(kp + (size_t)(i * DPN + jj) * ld) * xv[jj];
+    }
+    if (sub == 0 && op.penPtr) {
+        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
+            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
+            const int i = op.penRow[t];
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
+        }
+    }
+}
+
+// Adds the partials of slot groups 1.. to those of group 0 (in group order); true for the
+// group-0 thread, which then holds (A x)_r.  Every thread of the CTA must call it.
+template <class TA, int DPN>
+__device__ __forceinline__ bool ell_cta_reduce(TA y[DPN], const CtaRow &c) {
+    __shared__ TA sp[kRowThreads - 1][kCtaRows][DPN];
+    if (c.sub > 0) {
+#pragma unroll
+        for (int q = 0; q < DPN; ++q) sp[c.sub - 1][c.rloc][q] = y[q];
+    }
+    __syncthreads();
+    if (c.sub != 0) return false;
+#pragma unroll
+    for (int g = 0; g < kRowThreads - 1; ++g)
+#pragma unroll
+        for (int q = 0; q < DPN; ++q) y[q] += sp[g][c.rloc][q];
+    return true;
+}
+
 // True in the last CTA of the launch to arrive; the threads that wrote partials have fenced them
 // before the barrier.  That CTA resets the counter for the next launch.  No CTA waits for another.
 __device__ __forceinline__ bool last_to_arrive(unsigned *counter) {

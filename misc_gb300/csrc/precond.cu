@@ -292,6 +292,11 @@ struct TrainSet {
         *loss = L / S;
         if (!grad) return ASTRO_OK;
         const size_t smem = sizeof(double) * kTW * deg1 * dd;
+        if (smem > 48 * 1024) {  // above the default dynamic shared memory limit (dpn 6, high degree)
+            cudaError_t e = dpn == 3 ? cudaFuncSetAttribute(k_tr_grad<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                     : cudaFuncSetAttribute(k_tr_grad<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if ((rc = cuda_check(ctx, e, "gradient shared memory"))) return rc;
+        }
         if (dpn == 3)
             k_tr_grad<3><<<gr, kT, smem, ctx->stream>>>(op, dptr<double>(E), dptr<double>(Y), dptr<double>(part), n, deg1);
         else

@@ -113,6 +113,19 @@ def test_training_decreases_loss():
     assert abs(L - hist[-1]) <= 1e-10 * hist[-1]
 
 
+def test_validated_training_is_never_worse():
+    g, o, A, _ = _system(M.config2(nx=8, ny=4, nz=4, seed=1), fp32=True)
+    for deg, ratio in ((8, 100.0), (16, 1000.0)):
+        p0 = precond_init(deg, ratio, 3)
+        p, info = g.precond_train_validated(p0, _samples(A, 8, 4), iters=20)
+        assert info["loss"][1] < info["loss"][0]
+        if info["selected"] == "trained":
+            assert info["val_iters_trained"] < info["val_iters_initial"]
+            assert p is not p0
+        else:
+            assert p is p0
+
+
 def test_learned_solver_converges_with_fewer_iterations():
     """The network trained on one mesh, applied to a held-out mesh of the same family: the
     solution matches the direct solve and the Krylov iterations drop against Jacobi."""
@@ -127,6 +140,7 @@ def test_learned_solver_converges_with_fewer_iterations():
     ud, std_ = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=1e-10)  # untrained default network
     assert stl.status == 0 and stl.rel_residual <= 1e-10
     assert std_.status == 0 and std_.rel_residual <= 1e-10
+    assert stl.conditional_graph == 1 and stm.conditional_graph == 1
     ur = spla.spsolve(A.tocsc(), bo)
     for u in (ul, ud):
         # FP32 element matrices: the system differs from the FP64 one at ~1e-7 x conditioning
@@ -148,3 +162,17 @@ def test_precond_errors():
     p = precond_init(4, 100.0, 3)
     with pytest.raises(AstroError):
         g.precond_loss_grad(p, np.zeros((1, g.n)))  # zero sample
+
+
+@pytest.mark.parametrize("method", [SOLVER_FGMRES_LEARNED, SOLVER_FGMRES_MIXED, 0])
+def test_repeated_solves_reuse_workspace(method):
+    """The workspace and the captured restart-cycle graph stay on the context: a repeated solve
+    gives the same bits, and a new right-hand side (2 b) flows through the reused graph."""
+    g, o, A, bo = _system(M.config2(nx=8, ny=4, nz=4, seed=2), fp32=True)
+    b = g.static_rhs()
+    u1, s1 = g.solve_static(b, method=method, rtol=1e-10)
+    u2, s2 = g.solve_static(2 * b, method=method, rtol=1e-10)
+    u3, s3 = g.solve_static(b, method=method, rtol=1e-10)
+    assert s1.status == s2.status == s3.status == 0
+    assert np.array_equal(u1, u3) and s1.iterations == s3.iterations
+    assert np.linalg.norm(u2 - 2 * u1) <= 1e-8 * np.linalg.norm(u2)
