@@ -175,6 +175,11 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
  * nodal rotation, which r_getInstDof (Working/AStrO_r_elementEqns.f90:835-858) omits; with it the
  * tangent is invariant under rigid rotations.  No counterpart in the reference. */
 #define ASTRO_OPT_SHELL_MEAN_ROT_TERM 1
+/* ASTRO_OPT_UNROLLED_CYCLES (default 0): when 1, the static solvers capture their restart cycles
+ * as m unrolled Arnoldi steps (kernels that return at once after convergence) instead of
+ * conditional graph nodes; the same kernels in the same order, so the results are identical.
+ * For profilers that do not look inside conditional nodes, and for drivers without them. */
+#define ASTRO_OPT_UNROLLED_CYCLES 2
 int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value);
 
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that order their own work

@@ -65,6 +65,7 @@ struct astro_ctx {
     // workspaces of the static solvers (FP64, mixed, learned), kept with their restart-cycle graphs
     // across solves; owned by the Krylov unit (krylov_release)
     void *solveWork[3] = {nullptr, nullptr, nullptr};
+    int unrolledCycles = 0;  // ASTRO_OPT_UNROLLED_CYCLES
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // copies that overlap the element kernels
     int device = 0;

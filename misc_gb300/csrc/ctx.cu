@@ -962,5 +962,10 @@ extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
         ctx->quirkShellMeanRot = value ? 1 : 0;
         return ASTRO_OK;
     }
+    if (option == ASTRO_OPT_UNROLLED_CYCLES) {
+        ctx->unrolledCycles = value ? 1 : 0;
+        krylov_release(ctx);  // recapture the cycles in the chosen form
+        return ASTRO_OK;
+    }
     return set_err(ctx, ASTRO_ERR_ARG, "unknown option");
 }

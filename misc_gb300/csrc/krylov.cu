@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restric
     const int j = ctl->j;
     const TV inv = (TV)ctl->inv;
     TV y[DPN] = {};
-    if (sizeof(TM) == 8) {
+    if constexpr (sizeof(TM) == 8) {
         // FP64 comparator: kRowThreads adjacent lanes per block row, partials combined by shuffles
         // (the FP64 products bound this kernel, not its loads); same grid, rows renumbered
         const int r = blockIdx.x * kCtaRows + (int)threadIdx.x / kRowThreads, sub = threadIdx.x % kRowThreads;
@@ -200,15 +200,15 @@ __global__ void __launch_bounds__(kThreads) k_spmv_step(Op<TM> op, TV *__restric
             V[(size_t)j * ld + i] = wprev[i] * inv;
             w[i] = y[q] * inv;
         }
-        return;
-    }
-    if (c.valid) ell_row_group<TV, TM, TV, DPN>(op, c.r, c.sub, zprev, y);
-    if (!ell_cta_reduce<TV, DPN>(y, c) || !c.valid) return;
+    } else {
+        if (c.valid) ell_row_group<TV, TM, TV, DPN>(op, c.r, c.sub, zprev, y);
+        if (!ell_cta_reduce<TV, DPN>(y, c) || !c.valid) return;
 #pragma unroll
-    for (int q = 0; q < DPN; ++q) {
-        const size_t i = (size_t)c.r * DPN + q;
-        V[(size_t)j * ld + i] = wprev[i] * inv;
-        w[i] = y[q] * inv;
+        for (int q = 0; q < DPN; ++q) {
+            const size_t i = (size_t)c.r * DPN + q;
+            V[(size_t)j * ld + i] = wprev[i] * inv;
+            w[i] = y[q] * inv;
+        }
     }
 }
 
@@ -301,8 +301,8 @@ __global__ void k_sqrt_f(const double *__restrict__ dinv, float *__restrict__ ds
 }
 
 // Power iteration for the largest eigenvalue of D^-1 A: y = s D^-1 A x with s = scal[0] (the
-// reciprocal norm of x from the previous step), SpMV-step row mapping; the last CTA sums the
-// per-CTA ||y||^2 in CTA order and sets scal[1] = ||y||, scal[0] = 1 / ||y||.  Every CTA reads
+// reciprocal norm of x from the previous step), SpMV-step row mapping; warp 0 of the last CTA
+// sums the per-CTA ||y||^2 in a fixed order and sets scal[1] = ||y||, scal[0] = 1 / ||y||.  Every CTA reads
 // scal[0] before it arrives, so the last one may overwrite it.  dinv null: the operator is
 // already scaled (A^ = D^-1/2 A D^-1/2, the same spectrum as D^-1 A).
 template <class TM, class TV, int DPN>
@@ -334,12 +334,16 @@ __global__ void __launch_bounds__(kThreads) k_power_step(Op<TM> op, const TV *__
         part[blockIdx.x] = a;
         __threadfence();
     }
-    if (last_to_arrive(counter) && threadIdx.x == 0) {
+    if (last_to_arrive(counter) && threadIdx.x < 32) {
+        // warp 0 sums the CTA partials (lane-strided, then a fixed shuffle tree)
         double a = 0.0;
-        for (unsigned q = 0; q < gridDim.x; ++q) a += __ldcg(part + q);
-        const double nrm = sqrt(a);
-        scal[1] = nrm;
-        scal[0] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+        for (unsigned q = threadIdx.x; q < gridDim.x; q += 32) a += __ldcg(part + q);
+        a = warp_sum(a);
+        if (threadIdx.x == 0) {
+            const double nrm = sqrt(a);
+            scal[1] = nrm;
+            scal[0] = nrm > 0.0 ? 1.0 / nrm : 0.0;
+        }
     }
 }
 
@@ -949,6 +953,7 @@ static GmresWork *work_get(astro_ctx *ctx, int slot, int m, int tv, int *rc) {
         delete W;
     }
     W = new GmresWork();
+    W->condOk = !ctx->unrolledCycles;
     ctx->solveWork[slot] = W;
     if ((*rc = work_alloc(ctx, *W, m, tv))) {
         work_free(*W);

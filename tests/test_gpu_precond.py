@@ -176,3 +176,17 @@ def test_repeated_solves_reuse_workspace(method):
     assert s1.status == s2.status == s3.status == 0
     assert np.array_equal(u1, u3) and s1.iterations == s3.iterations
     assert np.linalg.norm(u2 - 2 * u1) <= 1e-8 * np.linalg.norm(u2)
+
+
+@pytest.mark.parametrize("method", [SOLVER_FGMRES_LEARNED, 0])
+def test_unrolled_cycles_match_conditional(method):
+    """ASTRO_OPT_UNROLLED_CYCLES captures the same kernels without conditional nodes: identical
+    iterations and bits."""
+    g, o, A, bo = _system(M.config2(nx=8, ny=4, nz=4, seed=2), fp32=True)
+    b = g.static_rhs()
+    u1, s1 = g.solve_static(b, method=method, rtol=1e-10)
+    g.set_option(2, 1)
+    u2, s2 = g.solve_static(b, method=method, rtol=1e-10)
+    g.set_option(2, 0)
+    assert s1.conditional_graph == 1 and s2.conditional_graph == 0
+    assert s1.iterations == s2.iterations and np.array_equal(u1, u2)
