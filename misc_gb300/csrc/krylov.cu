@@ -227,15 +227,15 @@ struct HopArgs {
     int first;
 };
 
-template <class TM, class TV, int DPN>
-__global__ void __launch_bounds__(kThreads) k_poly_hop(Op<TM> op, const TV *__restrict__ dsq, const TV *__restrict__ yk,
+template <class OP, class TV, int DPN>
+__global__ void __launch_bounds__(kThreads) k_poly_hop(OP op, const TV *__restrict__ dsq, const TV *__restrict__ yk,
                                                        const TV *__restrict__ ykm1, TV *__restrict__ ykp1,
                                                        TV *__restrict__ zacc, const HopArgs h,
                                                        const GmresCtl *__restrict__ ctl, int always) {
     if (!always && ctl->done) return;
     const CtaRow c = cta_row(op.N);
     TV t[DPN] = {};
-    if (c.valid) ell_row_group<TV, TM, TV, DPN>(op, c.r, c.sub, yk, t);
+    if (c.valid) row_group<TV, DPN>(op, c.r, c.sub, yk, t);
     if (!ell_cta_reduce<TV, DPN>(t, c) || !c.valid) return;
     const size_t base = (size_t)c.r * DPN;
     TV yc[DPN], yn[DPN], sc[DPN];
@@ -263,27 +263,45 @@ __global__ void __launch_bounds__(kThreads) k_poly_hop(Op<TM> op, const TV *__re
     }
 }
 
-// A^ = S A S in FP16 block-ELL (same slots and columns as the solver copy), S = diag(dsq):
-// one thread per (row, slot); and the scaled penalty values of the rows.
+// A^ = S A S in the FP16 block-vector layout of OpH (same slots and columns as the solver copy),
+// S = diag(dsq): one thread per (row, slot); padding rows and slots get zero blocks.
 template <int DPN>
-__global__ void k_scaled_half(const float *__restrict__ K, const int *__restrict__ col, int S, int ld, int N,
-                              const float *__restrict__ dsq, __half *__restrict__ Kh) {
+__global__ void k_scaled_bv(const float *__restrict__ K, const int *__restrict__ col, int S, int ld, int N,
+                            const float *__restrict__ dsq, uint4 *__restrict__ Kv, void *__restrict__ KrRaw) {
+    using Sh = BvShape<DPN>;
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)S * ld) return;
     const int s = (int)(t / ld), r = (int)(t - (long long)s * ld);
-    constexpr int dd = DPN * DPN;
-    if (r >= N) {
-        for (int q = 0; q < dd; ++q) Kh[((size_t)s * dd + q) * ld + r] = __float2half_rn(0.f);
-        return;
+    unsigned short h[Sh::NV * 8 + 4] = {};
+    if (r < N) {
+        const int c = col[(size_t)s * ld + r];
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int j = 0; j < DPN; ++j) {
+                const float v = K[((size_t)s * Sh::DD + i * DPN + j) * ld + r] * dsq[(size_t)r * DPN + i] *
+                                dsq[(size_t)c * DPN + j];
+                h[i * DPN + j] = __half_as_ushort(__float2half_rn(v));
+            }
     }
-    const int c = col[(size_t)s * ld + r];
 #pragma unroll
-    for (int i = 0; i < DPN; ++i)
-#pragma unroll
-        for (int j = 0; j < DPN; ++j) {
-            const size_t a = ((size_t)s * dd + i * DPN + j) * ld + r;
-            Kh[a] = __float2half_rn(K[a] * dsq[(size_t)r * DPN + i] * dsq[(size_t)c * DPN + j]);
-        }
+    for (int p = 0; p < Sh::NV; ++p) {
+        uint4 u;
+        u.x = h[8 * p] | ((unsigned)h[8 * p + 1] << 16);
+        u.y = h[8 * p + 2] | ((unsigned)h[8 * p + 3] << 16);
+        u.z = h[8 * p + 4] | ((unsigned)h[8 * p + 5] << 16);
+        u.w = h[8 * p + 6] | ((unsigned)h[8 * p + 7] << 16);
+        Kv[((size_t)s * Sh::NV + p) * ld + r] = u;
+    }
+    const int b = 8 * Sh::NV;
+    if constexpr (Sh::REM == 1) {
+        static_cast<unsigned short *>(KrRaw)[(size_t)s * ld + r] = h[b];
+    } else {
+        uint2 u;
+        u.x = h[b] | ((unsigned)h[b + 1] << 16);
+        u.y = h[b + 2] | ((unsigned)h[b + 3] << 16);
+        static_cast<uint2 *>(KrRaw)[(size_t)s * ld + r] = u;
+    }
 }
 
 __global__ void k_scaled_pen(const int *__restrict__ penPtr, const int *__restrict__ penRow,
@@ -305,8 +323,8 @@ __global__ void k_sqrt_f(const double *__restrict__ dinv, float *__restrict__ ds
 // sums the per-CTA ||y||^2 in a fixed order and sets scal[1] = ||y||, scal[0] = 1 / ||y||.  Every CTA reads
 // scal[0] before it arrives, so the last one may overwrite it.  dinv null: the operator is
 // already scaled (A^ = D^-1/2 A D^-1/2, the same spectrum as D^-1 A).
-template <class TM, class TV, int DPN>
-__global__ void __launch_bounds__(kThreads) k_power_step(Op<TM> op, const TV *__restrict__ dinv, const TV *__restrict__ x,
+template <class OP, class TV, int DPN>
+__global__ void __launch_bounds__(kThreads) k_power_step(OP op, const TV *__restrict__ dinv, const TV *__restrict__ x,
                                                          TV *__restrict__ y, double *part, unsigned *counter,
                                                          double *scal) {
     __shared__ double sp[kWarps];
@@ -315,7 +333,7 @@ __global__ void __launch_bounds__(kThreads) k_power_step(Op<TM> op, const TV *__
     const TV s = (TV)scal[0];
     double yy = 0.0;
     TV t[DPN] = {};
-    if (c.valid) ell_row_group<TV, TM, TV, DPN>(op, c.r, c.sub, x, t);
+    if (c.valid) row_group<TV, DPN>(op, c.r, c.sub, x, t);
     if (ell_cta_reduce<TV, DPN>(t, c) && c.valid) {
 #pragma unroll
         for (int q = 0; q < DPN; ++q) {
@@ -638,10 +656,10 @@ struct GmresWork {
     DevBuf V, w0, w1, z0, z1, part, ctl, dinv, dinvT, rres, xs, tgt;
     DevBuf x64, b64;  // FP64 solver: the solve's x and b live here, so its graph is reused across solves
     DevBuf yB0, yB1, zacc, pw;  // polynomial preconditioner: hop vectors, output, power-iteration scratch
-    DevBuf Kh, penS, dsqT;      // its operator A^ = S A S (FP16 block-ELL, scaled penalty) and S
+    DevBuf Kh, Kr, penS, dsqT;  // its operator A^ = S A S (FP16 block-vector planes, scaled penalty) and S
     cudaStream_t bodyStream = nullptr;  // captures the bodies of the cycle's IF nodes
     bool condOk = true;                 // conditional graph nodes available
-    Op<__half> hop;
+    OpH hop;
     const PolyHost *poly = nullptr;
     // vector that scales a residual into the preconditioner's input: D^-1 (Jacobi) or S (poly)
     template <class TV> const TV *y0s() { return poly ? dptr<TV>(dsqT) : dptr<TV>(dinvT); }
@@ -726,7 +744,7 @@ static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, TV *y0, int always, cudaSt
         for (int q = 0; q < dd; ++q) h.w[q] = P.W[(k + 1) * dd + q];
         h.first = (k == 0);
         h.c = (k == 0 ? 1.f : 2.f) / P.delta;
-        k_poly_hop<__half, TV, DPN><<<grid, kThreads, 0, s>>>(W.hop, dptr<TV>(W.dsqT), buf[cur], buf[prv],
+        k_poly_hop<OpH, TV, DPN><<<grid, kThreads, 0, s>>>(W.hop, dptr<TV>(W.dsqT), buf[cur], buf[prv],
                                                           k + 1 < P.deg ? buf[nxt] : nullptr, z, h,
                                                           dptr<GmresCtl>(W.ctl), always);
         cur = nxt;
@@ -939,7 +957,7 @@ static void work_free(GmresWork &W) {
     W.graph = nullptr;
     DevBuf *b[] = {&W.V,    &W.w0,   &W.w1,    &W.z0, &W.z1,  &W.part, &W.ctl, &W.dinv,
                    &W.dinvT, &W.rres, &W.xs,  &W.tgt, &W.yB0, &W.yB1,  &W.zacc, &W.pw,
-                   &W.Kh,    &W.penS, &W.dsqT, &W.x64, &W.b64};
+                   &W.Kh,    &W.Kr,   &W.penS, &W.dsqT, &W.x64, &W.b64};
     for (auto *x : b) dev_free(*x);
 }
 
@@ -1005,8 +1023,8 @@ static int true_residual(astro_ctx *ctx, GmresWork &W, int kind, const double *x
 
 // 50 power iterations of D^-1 A (deterministic start vector and reductions); lam = the last
 // norm ratio, which approaches the largest eigenvalue from below.
-template <class TM, class TV, int DPN>
-static int power_lambda(astro_ctx *ctx, const Op<TM> &op, const TV *dinv, double *lam) {
+template <class OP, class TV, int DPN>
+static int power_lambda(astro_ctx *ctx, const OP &op, const TV *dinv, double *lam) {
     const int n = ctx->P.n;
     const int nCta = (ctx->P.N + kCtaRows - 1) / kCtaRows;
     cudaStream_t s = ctx->stream;
@@ -1022,7 +1040,7 @@ static int power_lambda(astro_ctx *ctx, const Op<TM> &op, const TV *dinv, double
     k_power_init<TV><<<(n + 255) / 256, 256, 0, s>>>(dptr<TV>(a), n, dptr<double>(scal));
     for (int it = 0; it < 50; ++it) {
         TV *x = dptr<TV>(it % 2 ? b : a), *y = dptr<TV>(it % 2 ? a : b);
-        k_power_step<TM, TV, DPN><<<nCta, kThreads, 0, s>>>(op, dinv, x, y, dptr<double>(part), dptr<unsigned>(cnt),
+        k_power_step<OP, TV, DPN><<<nCta, kThreads, 0, s>>>(op, dinv, x, y, dptr<double>(part), dptr<unsigned>(cnt),
                                                             dptr<double>(scal));
     }
     double h[2] = {0.0, 0.0};
@@ -1127,15 +1145,20 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 ((rc = dev_alloc(ctx, W.yB0, sizeof(float) * n)) || (rc = dev_alloc(ctx, W.yB1, sizeof(float) * n)) ||
                  (rc = dev_alloc(ctx, W.zacc, sizeof(float) * n)) || (rc = dev_alloc(ctx, W.dsqT, sizeof(float) * n)) ||
                  (rc = dev_alloc(ctx, W.penS, sizeof(double) * std::max(1, ctx->penRows))) ||  // penalty entries
-                 (rc = dev_alloc(ctx, W.Kh, sizeof(__half) * (size_t)S * dd * ld)))) {
+                 (rc = dev_alloc(ctx, W.Kr, sizeof(uint16_t) * BvShape<DPN>::REM * (size_t)S * ld)) ||
+                 (rc = dev_alloc(ctx, W.Kh, sizeof(uint4) * BvShape<DPN>::NV * (size_t)S * ld)))) {
                 dev_free(W.Kh);
                 return rc;
             }
             k_sqrt_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(dptr<double>(W.dinv), dptr<float>(W.dsqT), n);
             const long long tot = (long long)S * ld;
-            k_scaled_half<DPN><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(
-                K32p, dptr<int>(ctx->d_ellCol), S, ld, ctx->P.N, dptr<float>(W.dsqT), dptr<__half>(W.Kh));
-            W.hop = make_op<__half>(ctx, dptr<__half>(W.Kh));
+            k_scaled_bv<DPN><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(
+                K32p, dptr<int>(ctx->d_ellCol), S, ld, ctx->P.N, dptr<float>(W.dsqT), dptr<uint4>(W.Kh), W.Kr.p);
+            {
+                const Op<float> o32 = make_op<float>(ctx, K32p);
+                W.hop = OpH{dptr<uint4>(W.Kh), W.Kr.p, o32.col,    o32.S,      o32.ld,    o32.penPtr,
+                            o32.penRow,         o32.penCol, o32.penVal, o32.N, o32.dpn};
+            }
             if (ctx->penRows) {
                 k_scaled_pen<<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
                     dptr<int>(ctx->d_penPtr), dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
@@ -1143,7 +1166,7 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 W.hop.penVal = dptr<double>(W.penS);
             }
             if ((rc = cuda_check(ctx, cudaGetLastError(), "preconditioner operator")) ||
-                (rc = power_lambda<__half, float, DPN>(ctx, W.hop, (const float *)nullptr, &lam)))
+                (rc = power_lambda<OpH, float, DPN>(ctx, W.hop, (const float *)nullptr, &lam)))
                 return rc;
             lam *= pc->lambda_scale;
             ph.deg = pc->degree;
@@ -1247,13 +1270,13 @@ int krylov_power_lambda(astro_ctx *ctx, int kind, double *lam) {
         if (kind == 64) {
             Op<double> op;
             if (!(rc = krylov_op64(ctx, &op)))
-                rc = ctx->P.dpn == 3 ? power_lambda<double, double, 3>(ctx, op, dptr<double>(dv), lam)
-                                     : power_lambda<double, double, 6>(ctx, op, dptr<double>(dv), lam);
+                rc = ctx->P.dpn == 3 ? power_lambda<Op<double>, double, 3>(ctx, op, dptr<double>(dv), lam)
+                                     : power_lambda<Op<double>, double, 6>(ctx, op, dptr<double>(dv), lam);
         } else {
             Op<float> op;
             if (!(rc = krylov_op32(ctx, &op)))
-                rc = ctx->P.dpn == 3 ? power_lambda<float, double, 3>(ctx, op, dptr<double>(dv), lam)
-                                     : power_lambda<float, double, 6>(ctx, op, dptr<double>(dv), lam);
+                rc = ctx->P.dpn == 3 ? power_lambda<Op<float>, double, 3>(ctx, op, dptr<double>(dv), lam)
+                                     : power_lambda<Op<float>, double, 6>(ctx, op, dptr<double>(dv), lam);
         }
     }
     dev_free(dv);

@@ -2,6 +2,7 @@
 // constants, the solver's device control block, the block-ELL operator descriptor and its row
 // products, warp sums, and the last-CTA-to-arrive test used for deterministic reductions.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 namespace astro_kry {
@@ -190,6 +191,122 @@ __device__ __forceinline__ void ell_row_group(const Op<TM> &op, int r, int sub, 
             for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
         }
     }
+}
+
+// FP16 block-vector operator of the polynomial preconditioner: the dpn x dpn block of slot s of
+// block row r is stored as NV = dpn^2 / 8 uint4 planes (eight FP16 entries each, row-major) at
+// Kv[(s * NV + p) * ld + r] and a remainder plane of REM = dpn^2 mod 8 entries at
+// Kr[s * ld + r] (one __half for dpn 3, a uint2 of four for dpn 6).  A warp instruction then
+// moves 16 bytes per lane over 32 consecutive rows, so one slot costs NV + 1 value loads instead
+// of dpn^2.
+template <int DPN> struct BvShape {
+    static constexpr int DD = DPN * DPN, NV = DD / 8, REM = DD % 8;
+};
+template <int REM> struct BvRem;
+template <> struct BvRem<1> {
+    using T = unsigned short;
+};
+template <> struct BvRem<4> {
+    using T = uint2;
+};
+
+struct OpH {
+    const uint4 *Kv;
+    const void *Kr;
+    const int *col;
+    int S, ld;
+    const int *penPtr;  // penalty lists as in Op (values scaled like the matrix)
+    const int *penRow;
+    const int *penCol;
+    const double *penVal;
+    int N, dpn;
+};
+
+__device__ __forceinline__ float h2f_bits(unsigned short b) { return __half2float(__ushort_as_half(b)); }
+
+// the block's entries as floats, row-major
+template <int DPN>
+__device__ __forceinline__ void bv_load(const OpH &op, int s, int r, float v[DPN * DPN]) {
+    using Sh = BvShape<DPN>;
+    const size_t ld = (size_t)op.ld;
+    const size_t sr = (size_t)s * ld + r;
+#pragma unroll
+    for (int p = 0; p < Sh::NV; ++p) {
+        const uint4 u = __ldg(op.Kv + ((size_t)s * Sh::NV + p) * ld + r);
+        const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            v[8 * p + 2 * k] = h2f_bits((unsigned short)(w[k] & 0xffffu));
+            v[8 * p + 2 * k + 1] = h2f_bits((unsigned short)(w[k] >> 16));
+        }
+    }
+    const typename BvRem<Sh::REM>::T *kr = static_cast<const typename BvRem<Sh::REM>::T *>(op.Kr);
+    if constexpr (Sh::REM == 1) {
+        v[8 * Sh::NV] = h2f_bits(__ldg(kr + sr));
+    } else {
+        const uint2 u = __ldg(kr + sr);
+        v[8 * Sh::NV] = h2f_bits((unsigned short)(u.x & 0xffffu));
+        v[8 * Sh::NV + 1] = h2f_bits((unsigned short)(u.x >> 16));
+        v[8 * Sh::NV + 2] = h2f_bits((unsigned short)(u.y & 0xffffu));
+        v[8 * Sh::NV + 3] = h2f_bits((unsigned short)(u.y >> 16));
+    }
+}
+
+// Partial (A^ x)_r over the slot group, FP32 products, block-vector loads (two slots per trip).
+template <class TA, class TX, int DPN>
+__device__ __forceinline__ void ell_row_group(const OpH &op, int r, int sub, const TX *__restrict__ x, TA y[DPN]) {
+    constexpr int DD = DPN * DPN;
+#pragma unroll
+    for (int i = 0; i < DPN; ++i) y[i] = TA(0);
+    const size_t ld = (size_t)op.ld;
+    int s = sub;
+    for (; s + kRowThreads < op.S; s += 2 * kRowThreads) {
+        const int c0 = __ldg(op.col + (size_t)s * ld + r);
+        const int c1 = __ldg(op.col + (size_t)(s + kRowThreads) * ld + r);
+        float k0[DD], k1[DD];
+        bv_load<DPN>(op, s, r, k0);
+        bv_load<DPN>(op, s + kRowThreads, r, k1);
+        TA x0[DPN], x1[DPN];
+#pragma unroll
+        for (int jj = 0; jj < DPN; ++jj) {
+            x0[jj] = (TA)x[(size_t)c0 * DPN + jj];
+            x1[jj] = (TA)x[(size_t)c1 * DPN + jj];
+        }
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)k0[i * DPN + jj] * x0[jj] + (TA)k1[i * DPN + jj] * x1[jj];
+    }
+    if (s < op.S) {
+        const int c = __ldg(op.col + (size_t)s * ld + r);
+        float kv[DD];
+        bv_load<DPN>(op, s, r, kv);
+        TA xv[DPN];
+#pragma unroll
+        for (int jj = 0; jj < DPN; ++jj) xv[jj] = (TA)x[(size_t)c * DPN + jj];
+#pragma unroll
+        for (int i = 0; i < DPN; ++i)
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) y[i] += (TA)kv[i * DPN + jj] * xv[jj];
+    }
+    if (sub == 0 && op.penPtr) {
+        for (int t = op.penPtr[r]; t < op.penPtr[r + 1]; ++t) {
+            const TA p = (TA)(op.penVal[t] * (double)x[op.penCol[t]]);
+            const int i = op.penRow[t];
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) y[q] += (q == i) ? p : TA(0);
+        }
+    }
+}
+
+// One entry point for the row products of both operator kinds.
+template <class TA, int DPN, class TM>
+__device__ __forceinline__ void row_group(const Op<TM> &op, int r, int sub, const TA *__restrict__ x, TA y[DPN]) {
+    ell_row_group<TA, TM, TA, DPN>(op, r, sub, x, y);
+}
+template <class TA, int DPN>
+__device__ __forceinline__ void row_group(const OpH &op, int r, int sub, const TA *__restrict__ x, TA y[DPN]) {
+    ell_row_group<TA, TA, DPN>(op, r, sub, x, y);
 }
 
 // Adds the partials of slot groups 1.. to those of group 0 (in group order); true for the
