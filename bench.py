@@ -49,6 +49,8 @@ def _parse():
     p.add_argument("--nz", type=int, default=32)
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--solve-max-iters", type=int, default=60000)
+    p.add_argument("--no-learned-eval", action="store_true")
+    p.add_argument("--eval-nx", type=int, default=96)
     return p.parse_args()
 
 
@@ -307,6 +309,9 @@ def run_ours(a):
                                                     "validated by a solve of that block"})
         res["metric"] = "s to 1e-10 FP64 rel resid (restart 50; the learned solver includes its eigenvalue estimate)"
         line["solve"] = res
+    if not a.no_solve and not a.no_learned_eval and rank == 0:
+        del g
+        line["learned_solve"] = _learned_eval(a)
     # CPU baseline: oracle, 1 core, bounded sample
     if rank == 0:
         rate, dt = _oracle_rate(m, 1024, 1)
@@ -317,6 +322,42 @@ def run_ours(a):
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def _learned_eval(a):
+    """The learned-preconditioner evaluation: a 96x48x48 brick block (698,691 DOF) with a
+    Gaussian-correlated log-normal modulus (correlation length 0.5 of the box width, sigma 0.65,
+    seed 4000) solved to 1e-8 relative FP64 residual by the learned solver (the trained network
+    shipped with the package when present, else the Chebyshev initialisation) and by the plain
+    FP64 Jacobi-GMRES(50), CUDA events, the second call of each (the first also reported)."""
+    from misc_gb300 import model as M
+    from misc_gb300.astro import SOLVER_FGMRES_LEARNED, SOLVER_GMRES_JACOBI_FP64, precond_init
+    from misc_gb300 import learned as LN
+    nx = a.eval_nx
+    m = M.config4_block(nx, nx // 2, nx // 2, 4000, corr_len=0.5, sigma=0.65)
+    t0 = time.perf_counter()
+    g, b = LN.block_system(m, fp32=True)
+    setup = time.perf_counter() - t0
+    path = os.path.join(ROOT, "misc_gb300", "data", "precond_cfg4.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        p, src = LN.from_json(d), {"network": "trained", "training": d.get("meta")}
+    else:
+        p, src = precond_init(a.precond_degree, a.precond_ratio, 3), {"network": "Chebyshev initialisation"}
+    out = {"workload": f"{nx}x{nx // 2}x{nx // 2} brick8, correlated log-normal E (corr 0.5 width, sigma 0.65, "
+                       f"seed 4000)", "dof": g.n, "rtol": 1e-8, "setup_seconds": setup}
+    for name, meth, pc in (("fgmres_learned", SOLVER_FGMRES_LEARNED, p), ("gmres_fp64", SOLVER_GMRES_JACOBI_FP64, None)):
+        kw = dict(method=meth, rtol=1e-8, restart=50, max_iters=a.solve_max_iters, allow_maxit=True, precond=pc)
+        _, s1 = g.solve_static(b, **kw)
+        _, s2 = g.solve_static(b, **kw)
+        out[name] = {"seconds": s2.seconds, "first_call_seconds": s1.seconds, "iterations": s2.iterations,
+                     "refinements": s2.refinements, "rel_residual": s2.rel_residual, "status": s2.status,
+                     "conditional_graph": s2.conditional_graph, "fallback": s2.fallback}
+    out["fgmres_learned"].update({"degree": p.degree, "ratio": p.ratio, **src})
+    out["speedup_vs_fp64_gmres"] = out["gmres_fp64"]["seconds"] / out["fgmres_learned"]["seconds"]
+    out["dof_per_second_learned"] = g.n / out["fgmres_learned"]["seconds"]
+    return out
 
 
 def main():

@@ -144,6 +144,9 @@ typedef struct astro_solve_stats {
     int32_t conditional_graph;  /* 1: the restart cycles ran as CUDA graphs whose Arnoldi steps sit
                                    behind conditional nodes (skipped after convergence); 0: the
                                    unrolled graph (the driver refused conditional nodes) */
+    int32_t fallback;        /* learned solver: 1 when it ended in a non-finite value, a breakdown or
+                                the iteration cap and the FP32 Jacobi solver finished the solve from
+                                the initial guess (the counts and seconds then cover both) */
 } astro_solve_stats;
 
 typedef struct astro_ctx astro_ctx;

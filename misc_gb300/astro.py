@@ -68,7 +68,7 @@ class SolveOptsC(C.Structure):
 class SolveStatsC(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("restarts", C.c_int32), ("refinements", C.c_int32),
                 ("status", C.c_int32), ("rel_residual", C.c_double), ("seconds", C.c_double),
-                ("conditional_graph", C.c_int32)]
+                ("conditional_graph", C.c_int32), ("fallback", C.c_int32)]
 
 
 class NewmarkOptsC(C.Structure):

@@ -1189,7 +1189,10 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 break;
             }
             k_zero_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d32, n);
-            int rci = gmres_solve<float, float, DPN>(ctx, W, K32p, d32, r, inner * rn, maxCycles - cycles,
+            // the last refinements need only the reduction that reaches rtol (with a margin),
+            // floored near what the FP32 inner solve can resolve
+            const double innerK = std::max(std::min(inner, 0.3 * o->rtol / rel), 1e-6);
+            int rci = gmres_solve<float, float, DPN>(ctx, W, K32p, d32, r, innerK * rn, maxCycles - cycles,
                                                      m, &iters, &cycles, &est);
             if (rci == ASTRO_ERR_NAN) {
                 rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the FP32 inner solve");
@@ -1218,10 +1221,47 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     return rc;
 }
 
-int krylov_solve_static(astro_ctx *ctx, const double *d_b, double *d_x, const astro_solve_opts *o,
-                        astro_solve_stats *st) {
+static int solve_static_dpn(astro_ctx *ctx, const double *d_b, double *d_x, const astro_solve_opts *o,
+                            astro_solve_stats *st) {
     if (ctx->P.dpn == 3) return solve_static_dev<3>(ctx, d_b, d_x, o, st);
     return solve_static_dev<6>(ctx, d_b, d_x, o, st);
+}
+
+// The learned solver falls back to the FP32 Jacobi solver (from the caller's initial guess) when
+// it ends in a non-finite value, a breakdown or the iteration cap; the statistics then add both
+// runs and set fallback.
+int krylov_solve_static(astro_ctx *ctx, const double *d_b, double *d_x, const astro_solve_opts *o,
+                        astro_solve_stats *st) {
+    if (o->method != ASTRO_SOLVER_FGMRES_LEARNED) {
+        const int rc = solve_static_dpn(ctx, d_b, d_x, o, st);
+        if (st) st->fallback = 0;
+        return rc;
+    }
+    const size_t bytes = sizeof(double) * ctx->P.n;
+    DevBuf x0;
+    int rc = dev_alloc(ctx, x0, bytes);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(x0.p, d_x, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    astro_solve_stats s1{};
+    rc = solve_static_dpn(ctx, d_b, d_x, o, &s1);
+    s1.fallback = 0;
+    if (rc == ASTRO_ERR_NAN || rc == ASTRO_ERR_MAXIT || rc == ASTRO_ERR_BREAKDOWN) {
+        CK(cudaMemcpyAsync(d_x, x0.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        astro_solve_opts o2 = *o;
+        o2.method = ASTRO_SOLVER_FGMRES_MIXED;
+        o2.precond = nullptr;
+        astro_solve_stats s2{};
+        rc = solve_static_dpn(ctx, d_b, d_x, &o2, &s2);
+        s2.iterations += s1.iterations;
+        s2.restarts += s1.restarts;
+        s2.refinements += s1.refinements;
+        s2.seconds += s1.seconds;
+        s2.fallback = 1;
+        s1 = s2;
+    }
+    dev_free(x0);
+    if (st) *st = s1;
+    return rc;
 }
 
 int krylov_op64(astro_ctx *ctx, Op<double> *op) {

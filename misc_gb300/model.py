@@ -331,6 +331,39 @@ def hex_block(nx=64, ny=32, nz=32, lx=4.0, ly=2.0, lz=2.0, jitter=0.1, seed=0, E
     return m
 
 
+def correlated_log_normal(nx, ny, nz, h, corr_len, sigma, E_med=2.0e11, seed=0):
+    """Per-element modulus field E = E_med * exp(sigma * z) with z a Gaussian-correlated,
+    unit-variance field on the (nz, ny, nx) element grid: white noise filtered in Fourier space by
+    exp(-(k * corr_len)^2 / 2) (k in rad per unit length, element spacing h = (hx, hy, hz)), then
+    standardised.  Returns shape (nz, ny, nx)."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal((nz, ny, nx))
+    kz = 2 * np.pi * np.fft.fftfreq(nz, d=h[2])
+    ky = 2 * np.pi * np.fft.fftfreq(ny, d=h[1])
+    kx = 2 * np.pi * np.fft.rfftfreq(nx, d=h[0])
+    k2 = kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2
+    z = np.fft.irfftn(np.fft.rfftn(w) * np.exp(-0.5 * k2 * corr_len ** 2), s=(nz, ny, nx))
+    z = (z - z.mean()) / max(z.std(), 1e-300)
+    return E_med * np.exp(sigma * z)
+
+
+def config4_block(nx, ny, nz, seed, corr_len=None, sigma=None):
+    """Learned-preconditioner family: a brick8 block with the element size of the 64x32x32 block
+    (box (nx, ny, nz) / 16), interior jitter 10 %, nu = 0.3, x = 0 clamped, traction 1e6 Pa on the
+    far x face, and a Gaussian-correlated log-normal modulus (median 2e11) whose correlation
+    length (a fraction U[0.2, 1.0] of the box width) and sigma (U[0.3, 1.0]) are drawn from the
+    seed unless given.  Training blocks are 32x16x16, the evaluation block 96x48x48."""
+    rng = np.random.default_rng(seed)
+    lx, ly, lz = nx / 16.0, ny / 16.0, nz / 16.0
+    frac = rng.uniform(0.2, 1.0) if corr_len is None else corr_len
+    sig = rng.uniform(0.3, 1.0) if sigma is None else sigma
+    E = correlated_log_normal(nx, ny, nz, (lx / nx, ly / ny, lz / nz), frac * ly, sig, seed=seed + 1)
+    m = hex_block(nx=nx, ny=ny, nz=nz, lx=lx, ly=ly, lz=lz, seed=seed, E_field=E,
+                  name=f"cfg4_block_{nx}x{ny}x{nz}_seed{seed}")
+    m.field = {"corr_len_frac": float(frac), "sigma": float(sig)}
+    return m
+
+
 def shell_beam():
     """Working/shellBeamModelInput.yaml: 10 shell4 elements on [0,10]x[-0.5,0.5], t = 0.1,
     E = 1e6, nu = 0.3, G = 384615; root nodes (1, 12) clamped in all 6 DOF; unit z load on each

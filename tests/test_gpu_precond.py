@@ -190,3 +190,19 @@ def test_unrolled_cycles_match_conditional(method):
     g.set_option(2, 0)
     assert s1.conditional_graph == 1 and s2.conditional_graph == 0
     assert s1.iterations == s2.iterations and np.array_equal(u1, u2)
+
+
+def test_learned_solver_falls_back_on_non_finite():
+    """Weights that overflow FP32 in the hops make the inner Arnoldi values non-finite: the solve
+    restarts from the initial guess with the FP32 Jacobi solver and still converges, flagged."""
+    g, o, A, bo = _system(M.config2(nx=8, ny=4, nz=4, seed=2), fp32=True)
+    b = g.static_rhs()
+    p = precond_init(8, 100.0, 3)
+    p.set_weights(p.weight_array() * 1e37)
+    u, st = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=1e-10, precond=p)
+    assert st.status == 0 and st.fallback == 1 and st.rel_residual <= 1e-10
+    um, sm = g.solve_static(b, method=SOLVER_FGMRES_MIXED, rtol=1e-10)
+    assert sm.fallback == 0
+    assert np.linalg.norm(u - um) <= 1e-7 * np.linalg.norm(um)
+    ul, sl = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=1e-10)
+    assert sl.fallback == 0
