@@ -50,6 +50,11 @@ def _parse():
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--solve-max-iters", type=int, default=60000)
     p.add_argument("--no-learned-eval", action="store_true")
+    p.add_argument("--learned-only", action="store_true",
+                   help="run only the learned-preconditioner evaluation and print its JSON object")
+    p.add_argument("--unrolled-cycles", action="store_true",
+                   help="capture the restart cycles unrolled (profilers do not look inside conditional nodes)")
+    p.add_argument("--no-fp64", action="store_true", help="learned evaluation without the FP64 comparator")
     p.add_argument("--eval-nx", type=int, default=96)
     return p.parse_args()
 
@@ -337,6 +342,8 @@ def _learned_eval(a):
     m = M.config4_block(nx, nx // 2, nx // 2, 4000, corr_len=0.5, sigma=0.65)
     t0 = time.perf_counter()
     g, b = LN.block_system(m, fp32=True)
+    if a.unrolled_cycles:
+        g.set_option(2, 1)
     setup = time.perf_counter() - t0
     path = os.path.join(ROOT, "misc_gb300", "data", "precond_cfg4.json")
     if os.path.exists(path):
@@ -347,7 +354,10 @@ def _learned_eval(a):
         p, src = precond_init(a.precond_degree, a.precond_ratio, 3), {"network": "Chebyshev initialisation"}
     out = {"workload": f"{nx}x{nx // 2}x{nx // 2} brick8, correlated log-normal E (corr 0.5 width, sigma 0.65, "
                        f"seed 4000)", "dof": g.n, "rtol": 1e-8, "setup_seconds": setup}
-    for name, meth, pc in (("fgmres_learned", SOLVER_FGMRES_LEARNED, p), ("gmres_fp64", SOLVER_GMRES_JACOBI_FP64, None)):
+    runs = [("fgmres_learned", SOLVER_FGMRES_LEARNED, p)]
+    if not a.no_fp64:
+        runs.append(("gmres_fp64", SOLVER_GMRES_JACOBI_FP64, None))
+    for name, meth, pc in runs:
         kw = dict(method=meth, rtol=1e-8, restart=50, max_iters=a.solve_max_iters, allow_maxit=True, precond=pc)
         _, s1 = g.solve_static(b, **kw)
         _, s2 = g.solve_static(b, **kw)
@@ -355,13 +365,27 @@ def _learned_eval(a):
                      "refinements": s2.refinements, "rel_residual": s2.rel_residual, "status": s2.status,
                      "conditional_graph": s2.conditional_graph, "fallback": s2.fallback}
     out["fgmres_learned"].update({"degree": p.degree, "ratio": p.ratio, **src})
-    out["speedup_vs_fp64_gmres"] = out["gmres_fp64"]["seconds"] / out["fgmres_learned"]["seconds"]
+    if "gmres_fp64" in out:
+        out["speedup_vs_fp64_gmres"] = out["gmres_fp64"]["seconds"] / out["fgmres_learned"]["seconds"]
+    # roofline of the solve's dominant kernel (the preconditioner hop, about 85 % of the learned
+    # solve): its bytes per launch over its CUDA-event time; the operator (FP16 planes and columns,
+    # about 157 MB at this size) streams from HBM and L2
+    us, by = g.precond_time_hop(200)
+    peaks = _peaks()
+    hbm = peaks["hbm_gbs"] if peaks else 6800.0
+    ach = by / (us * 1e-6) / 1e9
+    out["hop_roofline"] = {"bound": "hbm", "kernel": "k_poly_hop<OpH,float,3>", "us_per_launch": us,
+                           "bytes_per_launch": by, "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                           "peak_source": "measured" if peaks else "fallback"}
     out["dof_per_second_learned"] = g.n / out["fgmres_learned"]["seconds"]
     return out
 
 
 def main():
     a = _parse()
+    if a.learned_only:
+        print(json.dumps(_learned_eval(a)))
+        return 0
     if a.impl == "reference":
         return run_reference(a)
     return run_ours(a)

@@ -357,6 +357,12 @@ int astro_precond_loss_grad(astro_ctx *ctx, const astro_precond *p, const double
 int astro_precond_train(astro_ctx *ctx, astro_precond *p, const double *samples, int32_t num_samples, int32_t iters,
                         double *loss_history);
 
+/* Measurement hook: the average device time (CUDA events, reps launches after five warm-up
+ * launches) of one preconditioner hop on the operator of the last learned solve of this context,
+ * and the bytes one hop moves (FP16 block planes, columns, and the hop's vector loads and stores).
+ * No counterpart in the reference. */
+int astro_precond_time_hop(astro_ctx *ctx, int32_t reps, double *us_per_hop, double *bytes_per_hop);
+
 #ifdef __cplusplus
 }
 #endif

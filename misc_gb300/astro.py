@@ -121,6 +121,7 @@ def load_library():
         "astro_precond_lambda": ([vp, C.c_int32, F64P], C.c_int),
         "astro_precond_loss_grad": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, F64P, F64P], C.c_int),
         "astro_precond_train": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, C.c_int32, F64P], C.c_int),
+        "astro_precond_time_hop": ([vp, C.c_int32, F64P, F64P], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -376,6 +377,12 @@ class AstroGPU:
         hist = np.zeros(iters + 1)
         self._check(self.L.astro_precond_train(self.h, C.byref(p), _d(S), S.shape[0], iters, _d(hist)))
         return hist
+
+    def precond_time_hop(self, reps=200):
+        """(microseconds per hop, bytes per hop) on the operator of the last learned solve."""
+        us, by = np.zeros(1), np.zeros(1)
+        self._check(self.L.astro_precond_time_hop(self.h, reps, _d(us), _d(by)))
+        return float(us[0]), float(by[0])
 
     def precond_train_validated(self, p, samples, iters=20, rhs=None, rtol=1e-8):
         """Trains a copy of p on samples, then solves this model (right-hand side rhs, default the

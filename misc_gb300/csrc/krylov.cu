@@ -1189,9 +1189,10 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 break;
             }
             k_zero_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d32, n);
-            // the last refinements need only the reduction that reaches rtol (with a margin),
-            // floored near what the FP32 inner solve can resolve
-            const double innerK = std::max(std::min(inner, 0.3 * o->rtol / rel), 1e-6);
+            // the last refinement needs only the reduction that reaches rtol (with a margin); a
+            // refinement asks for at most ten times the usual inner reduction, as the FP32 inner
+            // solve stalls near its own rounding level
+            const double innerK = std::max(std::min(inner, 0.3 * o->rtol / rel), 0.1 * inner);
             int rci = gmres_solve<float, float, DPN>(ctx, W, K32p, d32, r, innerK * rn, maxCycles - cycles,
                                                      m, &iters, &cycles, &est);
             if (rci == ASTRO_ERR_NAN) {
@@ -1262,6 +1263,52 @@ int krylov_solve_static(astro_ctx *ctx, const double *d_b, double *d_x, const as
     dev_free(x0);
     if (st) *st = s1;
     return rc;
+}
+
+// Times reps launches of one preconditioner hop on the operator of the last learned solve (the
+// hop of the Chebyshev recurrence with zero weights: same loads and stores, no accumulation).
+template <int DPN>
+static int time_hop(astro_ctx *ctx, GmresWork &W, int reps, double *us, double *bytes) {
+    using Sh = BvShape<DPN>;
+    cudaStream_t s = ctx->stream;
+    HopArgs h;
+    std::memset(&h, 0, sizeof(h));
+    h.theta = 0.5f;
+    h.c = 1.0f;
+    const unsigned grid = (unsigned)((ctx->P.N + kCtaRows - 1) / kCtaRows);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto launch = [&]() {
+        k_poly_hop<OpH, float, DPN><<<grid, kThreads, 0, s>>>(W.hop, dptr<float>(W.dsqT), dptr<float>(W.z0),
+                                                             dptr<float>(W.yB0), dptr<float>(W.yB1),
+                                                             dptr<float>(W.zacc), h, dptr<GmresCtl>(W.ctl), 1);
+    };
+    for (int i = 0; i < 5; ++i) launch();
+    cudaEventRecord(e0, s);
+    for (int i = 0; i < reps; ++i) launch();
+    cudaEventRecord(e1, s);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    int rc = cuda_check(ctx, e == cudaSuccess ? cudaGetLastError() : e, "hop timing");
+    if (rc) return rc;
+    *us = 1e3 * ms / reps;
+    // matrix planes and columns of every slot, then per block row the loads of y_k, y_{k-1}, S and
+    // z and the stores of y_{k+1} and z (the gathered y_k are counted once)
+    const double sl = (double)W.hop.S * W.hop.ld;
+    *bytes = sl * (16.0 * Sh::NV + 2.0 * Sh::REM + 4.0) + (double)ctx->P.n * 4.0 * 6.0;
+    return ASTRO_OK;
+}
+
+extern "C" int astro_precond_time_hop(astro_ctx *ctx, int32_t reps, double *us_per_hop, double *bytes_per_hop) {
+    if (!ctx || reps < 1 || !us_per_hop || !bytes_per_hop) return ASTRO_ERR_ARG;
+    GmresWork *W = static_cast<GmresWork *>(ctx->solveWork[2]);
+    if (!W || !W->Kh.p) return set_err(ctx, ASTRO_ERR_STATE, "no learned solve has run on this context");
+    return ctx->P.dpn == 3 ? time_hop<3>(ctx, *W, reps, us_per_hop, bytes_per_hop)
+                           : time_hop<6>(ctx, *W, reps, us_per_hop, bytes_per_hop);
 }
 
 int krylov_op64(astro_ctx *ctx, Op<double> *op) {
