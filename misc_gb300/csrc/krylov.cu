@@ -649,6 +649,7 @@ __global__ void k_to_ell(const T *__restrict__ K, const int *__restrict__ rowPtr
 struct PolyHost {
     int deg = 0;
     float theta = 0.f, delta = 0.f;
+    double apwKey = 0.0;  // the L2 window the hop launches carry (part of the graph's key)
     float W[(ASTRO_PRECOND_MAX_DEGREE + 1) * 36] = {};
 };
 
@@ -660,6 +661,10 @@ struct GmresWork {
     cudaStream_t bodyStream = nullptr;  // captures the bodies of the cycle's IF nodes
     bool condOk = true;                 // conditional graph nodes available
     OpH hop;
+    // L2 persistence window over the operator's block planes for the hop launches (a launch
+    // attribute, so captured into the graph nodes); off when the device has no persisting L2
+    cudaAccessPolicyWindow apw = {};
+    bool apwOn = false;
     const PolyHost *poly = nullptr;
     // vector that scales a residual into the preconditioner's input: D^-1 (Jacobi) or S (poly)
     template <class TV> const TV *y0s() { return poly ? dptr<TV>(dsqT) : dptr<TV>(dinvT); }
@@ -744,9 +749,18 @@ static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, TV *y0, int always, cudaSt
         for (int q = 0; q < dd; ++q) h.w[q] = P.W[(k + 1) * dd + q];
         h.first = (k == 0);
         h.c = (k == 0 ? 1.f : 2.f) / P.delta;
-        k_poly_hop<OpH, TV, DPN><<<grid, kThreads, 0, s>>>(W.hop, dptr<TV>(W.dsqT), buf[cur], buf[prv],
-                                                          k + 1 < P.deg ? buf[nxt] : nullptr, z, h,
-                                                          dptr<GmresCtl>(W.ctl), always);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(kThreads);
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        at[0].val.accessPolicyWindow = W.apw;
+        cfg.attrs = at;
+        cfg.numAttrs = W.apwOn ? 1 : 0;
+        cudaLaunchKernelEx(&cfg, k_poly_hop<OpH, TV, DPN>, W.hop, (const TV *)dptr<TV>(W.dsqT), (const TV *)buf[cur],
+                           (const TV *)buf[prv], k + 1 < P.deg ? buf[nxt] : (TV *)nullptr, z, h,
+                           (const GmresCtl *)dptr<GmresCtl>(W.ctl), always);
         cur = nxt;
     }
     return z;
@@ -1053,6 +1067,35 @@ static int power_lambda(astro_ctx *ctx, const OP &op, const TV *dinv, double *la
     return rc;
 }
 
+// Persisting L2 for the hops: when the operator (plus the vectors) does not fit in L2, every hop
+// streams it from HBM and LRU evicts each part before its reuse; a window that keeps a fixed share
+// of the block planes resident (half of the persisting set-aside) cuts that traffic.  The
+// set-aside is a limit of this CUDA context: persist_begin raises it to the device's maximum and
+// fills the workspace's window; persist_end releases the persisting lines and restores the limit.
+static bool persist_begin(astro_ctx *ctx, GmresWork &W, size_t *prev) {
+    int maxPersist = 0, maxWin = 0;
+    cudaDeviceGetAttribute(&maxPersist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device);
+    cudaDeviceGetAttribute(&maxWin, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device);
+    W.apwOn = false;
+    if (!(maxPersist > 0 && maxWin > 0 && cudaDeviceGetLimit(prev, cudaLimitPersistingL2CacheSize) == cudaSuccess &&
+          cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)maxPersist) == cudaSuccess)) {
+        cudaGetLastError();
+        return false;
+    }
+    W.apw.base_ptr = W.Kh.p;
+    W.apw.num_bytes = std::min(W.Kh.bytes, (size_t)maxWin);
+    W.apw.hitRatio = (float)std::min(1.0, 0.5 * maxPersist / (double)W.apw.num_bytes);
+    W.apw.hitProp = cudaAccessPropertyPersisting;
+    W.apw.missProp = cudaAccessPropertyStreaming;
+    W.apwOn = true;
+    return true;
+}
+static void persist_end(size_t prev) {
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, prev);
+    cudaGetLastError();
+}
+
 // Checks the network against the model (degree, DOF per node, interval, finite weights).
 static int precond_check(astro_ctx *ctx, const astro_precond *p) {
     if (p->degree < 1 || p->degree > ASTRO_PRECOND_MAX_DEGREE) return set_err(ctx, ASTRO_ERR_ARG, "precond degree out of range");
@@ -1084,6 +1127,9 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     }
     if (learned && (rc = precond_check(ctx, pc))) return rc;
     PolyHost ph;
+    std::memset(&ph, 0, sizeof(ph));  // compared bytewise as the graph's key
+    size_t persistPrev = 0;
+    bool persistSet = false;
     if (fp64 && !ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
     if (!fp64 && !ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
     GmresWork *Wp = work_get(ctx, fp64 ? 0 : (learned ? 2 : 1), m, fp64 ? sizeof(double) : sizeof(float), &rc);
@@ -1174,6 +1220,8 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
             ph.delta = (float)(0.5 * lam * (1.0 - 1.0 / pc->ratio));
             for (int q = 0; q < (pc->degree + 1) * DPN * DPN; ++q) ph.W[q] = (float)(pc->weights[q] / lam);
             W.poly = &ph;
+            persistSet = persist_begin(ctx, W, &persistPrev);
+            if (W.apwOn) ph.apwKey = (double)W.apw.hitRatio * 1e12 + (double)W.apw.num_bytes;
         }
         float *d32 = dptr<float>(W.xs);
         const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
@@ -1189,10 +1237,11 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 break;
             }
             k_zero_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(d32, n);
-            // the last refinement needs only the reduction that reaches rtol (with a margin); a
-            // refinement asks for at most ten times the usual inner reduction, as the FP32 inner
-            // solve stalls near its own rounding level
-            const double innerK = std::max(std::min(inner, 0.3 * o->rtol / rel), 0.1 * inner);
+            // a refinement asks for the usual inner reduction, except when the reduction left to
+            // reach rtol is within what one FP32 inner solve resolves (1e-6): then it asks for
+            // just that, with a margin, so that it is the last one
+            const double need = 0.3 * o->rtol / rel;
+            const double innerK = need >= 1e-6 ? need : inner;
             int rci = gmres_solve<float, float, DPN>(ctx, W, K32p, d32, r, innerK * rn, maxCycles - cycles,
                                                      m, &iters, &cycles, &est);
             if (rci == ASTRO_ERR_NAN) {
@@ -1209,6 +1258,7 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (persistSet) persist_end(persistPrev);
     if (st) {
         st->iterations = iters;
         st->restarts = cycles;
@@ -1279,10 +1329,21 @@ static int time_hop(astro_ctx *ctx, GmresWork &W, int reps, double *us, double *
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    size_t prev = 0;
+    const bool ps = persist_begin(ctx, W, &prev);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    at[0].val.accessPolicyWindow = W.apw;
+    cfg.attrs = at;
+    cfg.numAttrs = W.apwOn ? 1 : 0;
     auto launch = [&]() {
-        k_poly_hop<OpH, float, DPN><<<grid, kThreads, 0, s>>>(W.hop, dptr<float>(W.dsqT), dptr<float>(W.z0),
-                                                             dptr<float>(W.yB0), dptr<float>(W.yB1),
-                                                             dptr<float>(W.zacc), h, dptr<GmresCtl>(W.ctl), 1);
+        cudaLaunchKernelEx(&cfg, k_poly_hop<OpH, float, DPN>, W.hop, (const float *)dptr<float>(W.dsqT),
+                           (const float *)dptr<float>(W.z0), (const float *)dptr<float>(W.yB0), dptr<float>(W.yB1),
+                           dptr<float>(W.zacc), h, (const GmresCtl *)dptr<GmresCtl>(W.ctl), 1);
     };
     for (int i = 0; i < 5; ++i) launch();
     cudaEventRecord(e0, s);
@@ -1294,6 +1355,7 @@ static int time_hop(astro_ctx *ctx, GmresWork &W, int reps, double *us, double *
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     int rc = cuda_check(ctx, e == cudaSuccess ? cudaGetLastError() : e, "hop timing");
+    if (ps) persist_end(prev);
     if (rc) return rc;
     *us = 1e3 * ms / reps;
     // matrix planes and columns of every slot, then per block row the loads of y_k, y_{k-1}, S and
