@@ -357,6 +357,21 @@ int astro_precond_loss_grad(astro_ctx *ctx, const astro_precond *p, const double
 int astro_precond_train(astro_ctx *ctx, astro_precond *p, const double *samples, int32_t num_samples, int32_t iters,
                         double *loss_history);
 
+/* getTotaldLdD for a static analysis (Working/AStrO_commandFunctions.f90:1377-1410) with the elastic
+ * branch of solveDynamicAdjoint (:917-966; dLdv = dLda = 0): the adjoint K lambda = dLdu after
+ * updateExternalRHS with int_dldu, the internal lambda by updateInternalSoln, then for every design
+ * variable d = 1..num_dvars
+ *     dldd[d-1] = dldd_explicit[d-1] - lambda . dRudD(d) - lambda_int . intdRudD(d)
+ * with dRudD by the complex step of step h at state (getdRelasticdD).  The objective's partials come
+ * from the caller (getdObjdU / getdObjdD): dldu (el_mat_dim, global DOF numbering), int_dldu
+ * (int_vec_size, may be NULL), dldd_explicit (num_dvars, may be NULL).  K (astro_el_soln_load with
+ * build_mat = 1 at the same state) and the scaled constraints must be resident; the adjoint solve
+ * runs the GPU solver of opts instead of the reference's LDL-preconditioned gMRes, converged on the
+ * FP64 true residual.  disp_adj (el_mat_dim) and int_disp_adj (int_vec_size) may be NULL. */
+int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double h, const double *dldu, const double *int_dldu,
+                     const double *dldd_explicit, const astro_solve_opts *opts, double *dldd, double *disp_adj,
+                     double *int_disp_adj, astro_solve_stats *stats);
+
 /* Measurement hook: the average device time (CUDA events, reps launches after five warm-up
  * launches) of one preconditioner hop on the operator of the last learned solve of this context,
  * and the bytes one hop moves (FP16 block planes, columns, and the hop's vector loads and stores).

@@ -122,6 +122,8 @@ def load_library():
         "astro_precond_loss_grad": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, F64P, F64P], C.c_int),
         "astro_precond_train": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, C.c_int32, F64P], C.c_int),
         "astro_precond_time_hop": ([vp, C.c_int32, F64P, F64P], C.c_int),
+        "astro_total_dldd": ([vp, vp, C.c_double, F64P, F64P, F64P, C.POINTER(SolveOptsC), F64P, F64P, F64P,
+                              C.POINTER(SolveStatsC)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -356,6 +358,23 @@ class AstroGPU:
         self._check(self.L.astro_drdd_complex(self.h, dvar, h, C.byref(state) if state is not None else None,
                                               _d(out), _d(iout)))
         return out, iout[:self.int_vec_size]
+
+    def getTotaldLdD(self, dldu, int_dldu=None, dldd_explicit=None, state=None, h=1e-14,
+                     method=SOLVER_GMRES_JACOBI_FP64, rtol=1e-12, restart=50, max_iters=200000, precond=None):
+        """Static design gradient: (dLdD, dispAdj, intDispAdj, stats) with the adjoint solved on the
+        device (needs getElasticSolnLoad(1) at the state and scaleElasticMPC first)."""
+        nd = len(self.model.d_value) if getattr(self.model, "d_value", None) is not None else 0
+        dldd = np.zeros(max(nd, 1))
+        lam = np.zeros(self.n)
+        ilam = np.zeros(max(self.int_vec_size, 1))
+        o = SolveOptsC(method, restart, max_iters, rtol, 1e-4,
+                       C.pointer(precond) if precond is not None else C.POINTER(PrecondC)())
+        st = SolveStatsC()
+        self._check(self.L.astro_total_dldd(self.h, C.byref(state) if state is not None else None, h, _d(_f64(dldu)),
+                                            None if int_dldu is None else _d(_f64(int_dldu)),
+                                            None if dldd_explicit is None else _d(_f64(dldd_explicit)),
+                                            C.byref(o), _d(dldd), _d(lam), _d(ilam), C.byref(st)))
+        return dldd[:nd], lam, ilam[:self.int_vec_size], st
 
     # -- polynomial preconditioner ----------------------------------------------------------------
     def precond_lambda(self, kind=64):

@@ -595,6 +595,45 @@ __global__ void k_scale_neg(int n, const double *x, double s, double *y) {
 // with the imaginary parts of the complex-step properties; the element kernels run in FP64 with
 // those properties and the complex path's constants (Gauss points +-0.577350269189626 as a
 // single-precision literal), and only the property evaluation is complex.
+// Device state of a complex-step evaluation, uploaded once for any number of design variables.
+struct DrddState {
+    DevState S;
+    ShellDevState ds;
+};
+static int drdd_state(astro_ctx *ctx, const astro_state *state, DrddState &D) {
+    int rc;
+    if (!state) return ASTRO_OK;
+    if ((rc = state_vec_up(ctx, state->node_disp, D.S.disp))) return rc;
+    if (ctx->hasShell) {
+        if ((rc = state_vec_up(ctx, state->prev_disp, D.S.pdisp))) return rc;
+        if ((rc = state_vec_up(ctx, state->prev_vel, D.S.pvel))) return rc;
+        if ((rc = state_vec_up(ctx, state->prev_acc, D.S.pacc))) return rc;
+    }
+    if (state->dynamic && ctx->hasSolid)
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
+    if (ctx->hasShell && (rc = shell_state(ctx, state, D.S, D.ds))) return rc;
+    return ASTRO_OK;
+}
+
+// dRu/dd of design variable dvar into d_acc (n, internal layout) and d_iacc (internal DOF, may be
+// null): the complex step's -sum Im(Ru) scaled by -1/h (getdRelasticdD's compStepInv).
+static int drdd_device(astro_ctx *ctx, int dvar, double h, DrddState &D, double *d_acc, double *d_iacc) {
+    const int n = ctx->P.n, ni = ctx->P.intVecSize;
+    int rc;
+    CK(cudaMemsetAsync(d_acc, 0, sizeof(double) * n, ctx->stream));
+    if (ni > 0 && d_iacc) CK(cudaMemsetAsync(d_iacc, 0, sizeof(double) * ni, ctx->stream));
+    if (ctx->hasSolid) {
+        rc = hex8_drdd(ctx, dvar, h, D.S.disp.p ? dptr<double>(D.S.disp) : nullptr, d_acc);
+    } else {
+        rc = shell4_drdd(ctx, dvar, h, D.ds, d_acc, ni > 0 ? d_iacc : nullptr);
+    }
+    if (rc) return rc;
+    const double hInv = 1.0 / h;
+    k_scale_neg<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, d_acc, hInv, d_acc);
+    if (ni > 0 && d_iacc) k_scale_neg<<<(ni + 255) / 256, 256, 0, ctx->stream>>>(ni, d_iacc, hInv, d_iacc);
+    return cuda_check(ctx, cudaGetLastError(), "drdd");
+}
+
 extern "C" int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const astro_state *state, double *drudd,
                                   double *int_drudd) {
     if (!ctx || !drudd) return ASTRO_ERR_ARG;
@@ -604,18 +643,8 @@ extern "C" int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const 
     const AstroPrep &P = ctx->P;
     const int n = P.n;
     int rc;
-    DevState S;
-    ShellDevState ds;
-    if (state) {
-        if ((rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
-        if (ctx->hasShell) {
-            if ((rc = state_vec_up(ctx, state->prev_disp, S.pdisp))) return rc;
-            if ((rc = state_vec_up(ctx, state->prev_vel, S.pvel))) return rc;
-            if ((rc = state_vec_up(ctx, state->prev_acc, S.pacc))) return rc;
-        }
-        if (state->dynamic && ctx->hasSolid)
-            return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
-    }
+    DrddState D;
+    if ((rc = drdd_state(ctx, state, D))) return rc;
     struct Tmp {
         DevBuf acc, iacc, out;
         ~Tmp() {
@@ -627,31 +656,45 @@ extern "C" int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const 
     DevBuf &acc = T.acc, &iacc = T.iacc, &out = T.out;
     if ((rc = dev_alloc(ctx, acc, sizeof(double) * n))) return rc;
     if ((rc = dev_alloc(ctx, out, sizeof(double) * n))) return rc;
-    CK(cudaMemsetAsync(acc.p, 0, sizeof(double) * n, ctx->stream));
     const int ni = P.intVecSize;
-    if (ni > 0) {
-        if ((rc = dev_alloc(ctx, iacc, sizeof(double) * ni))) return rc;
-        CK(cudaMemsetAsync(iacc.p, 0, sizeof(double) * ni, ctx->stream));
-    }
-    if (ctx->hasSolid) {
-        rc = hex8_drdd(ctx, dvar, h, S.disp.p ? dptr<double>(S.disp) : nullptr, dptr<double>(acc));
-    } else {
-        if ((rc = shell_state(ctx, state, S, ds))) return rc;
-        rc = shell4_drdd(ctx, dvar, h, ds, dptr<double>(acc), ni > 0 ? dptr<double>(iacc) : nullptr);
-    }
-    if (rc) return rc;
-    // acc holds -sum Im(Ru): dRudD = Im(Ru) * (1/h) (compStepInv)
-    const double hInv = 1.0 / h;
-    k_scale_neg<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, dptr<double>(acc), hInv, dptr<double>(acc));
-    CK(cudaGetLastError());
+    if (ni > 0 && (rc = dev_alloc(ctx, iacc, sizeof(double) * ni))) return rc;
+    if ((rc = drdd_device(ctx, dvar, h, D, dptr<double>(acc), ni > 0 ? dptr<double>(iacc) : nullptr))) return rc;
     if ((rc = int_to_ref_vec(ctx, dptr<double>(acc), dptr<double>(out), n))) return rc;
     CK(cudaMemcpyAsync(drudd, out.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
-    if (ni > 0 && int_drudd) {
-        k_scale_neg<<<(ni + 255) / 256, 256, 0, ctx->stream>>>(ni, dptr<double>(iacc), hInv, dptr<double>(iacc));
-        CK(cudaGetLastError());
+    if (ni > 0 && int_drudd)
         CK(cudaMemcpyAsync(int_drudd, iacc.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream));
-    }
     CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}
+
+// Per-CTA partial sums of a . b (256 threads per CTA); the host adds them in CTA order.
+__global__ void k_dot_part(const double *__restrict__ a, const double *__restrict__ b, int n, double *part) {
+    __shared__ double sp[8];
+    double s = 0.0;
+    for (int i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) s += a[i] * b[i];
+    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) sp[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t += sp[q];
+        part[blockIdx.x] = t;
+    }
+}
+
+static int dev_dot(astro_ctx *ctx, const double *a, const double *b, int n, DevBuf &part, double *out) {
+    constexpr int kCtas = 152;
+    if (!part.p) {
+        int rc = dev_alloc(ctx, part, sizeof(double) * kCtas);
+        if (rc) return rc;
+    }
+    k_dot_part<<<kCtas, 256, 0, ctx->stream>>>(a, b, n, dptr<double>(part));
+    double h[kCtas];
+    CK(cudaMemcpyAsync(h, part.p, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    double s = 0.0;
+    for (int q = 0; q < kCtas; ++q) s += h[q];
+    *out = s;
     return ASTRO_OK;
 }
 
@@ -968,4 +1011,71 @@ extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
         return ASTRO_OK;
     }
     return set_err(ctx, ASTRO_ERR_ARG, "unknown option");
+}
+
+// getTotaldLdD, static branch (Working/AStrO_commandFunctions.f90:1384-1410), with the elastic
+// branch of solveDynamicAdjoint (:932-956; with dLdv = dLda = 0 its accAdj vanishes): the adjoint
+// lambda solves K lambda = dLdu after updateExternalRHS(dLdu, intdLdu) (K is symmetric, and the
+// reference solves with K itself), updateInternalSoln gives the internal lambda, and each design
+// variable d adds -lambda . dRudD(d) - lambda_int . intdRudD(d) to dLdD(d), dRudD by the complex
+// step at the given state.  All vectors stay on the device; the dot products reduce in a fixed order.
+extern "C" int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double h, const double *dldu,
+                                const double *int_dldu, const double *dldd_explicit, const astro_solve_opts *opts,
+                                double *dldd, double *disp_adj, double *int_disp_adj, astro_solve_stats *stats) {
+    if (!ctx || !dldu || !opts || !dldd) return ASTRO_ERR_ARG;
+    if (!(h > 0.0)) return set_err(ctx, ASTRO_ERR_ARG, "complex step h must be positive");
+    if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "needs the FP64 stiffness of astro_el_soln_load(build_mat = 1)");
+    if (!ctx->mpcScaled && ctx->P.mpcDim > 0) return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run before the adjoint");
+    const int n = ctx->P.n, ni = ctx->P.intVecSize, nd = ctx->numDvars;
+    const bool hasInt = ctx->hasShell && ni > 0;
+    if (hasInt && !ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
+    struct Tmp {
+        DevBuf b, x, il, ir, acc, iacc, part, ref;
+        ~Tmp() {
+            DevBuf *v[] = {&b, &x, &il, &ir, &acc, &iacc, &part, &ref};
+            for (DevBuf *p : v) dev_free(*p);
+        }
+    } T;
+    int rc;
+    if ((rc = state_vec_up(ctx, dldu, T.b, false))) return rc;
+    if ((rc = dev_alloc(ctx, T.x, sizeof(double) * n))) return rc;
+    CK(cudaMemsetAsync(T.x.p, 0, sizeof(double) * n, ctx->stream));
+    if (hasInt) {
+        if ((rc = dev_alloc(ctx, T.il, sizeof(double) * ni))) return rc;
+        CK(cudaMemsetAsync(T.il.p, 0, sizeof(double) * ni, ctx->stream));
+        if (int_dldu) {
+            if ((rc = upload(ctx, T.ir, int_dldu, sizeof(double) * ni))) return rc;
+            if ((rc = shell4_update_external_rhs(ctx, dptr<double>(T.ir), dptr<double>(T.b)))) return rc;
+        }
+    }
+    astro_solve_stats st{};
+    rc = krylov_solve_static(ctx, dptr<double>(T.b), dptr<double>(T.x), opts, &st);
+    if (stats) *stats = st;
+    if (rc) return rc;
+    if (hasInt && (rc = shell4_update_internal_soln(ctx, dptr<double>(T.x), dptr<double>(T.il),
+                                                    T.ir.p ? dptr<double>(T.ir) : nullptr)))
+        return rc;
+    // dLdD = explicit part - lambda . dRudD for every design variable
+    if (nd > 0) {
+        DrddState D;
+        if ((rc = drdd_state(ctx, state, D))) return rc;
+        if ((rc = dev_alloc(ctx, T.acc, sizeof(double) * n))) return rc;
+        if (hasInt && (rc = dev_alloc(ctx, T.iacc, sizeof(double) * ni))) return rc;
+        for (int d = 1; d <= nd; ++d) {
+            if ((rc = drdd_device(ctx, d, h, D, dptr<double>(T.acc), hasInt ? dptr<double>(T.iacc) : nullptr))) return rc;
+            double s = 0.0, si = 0.0;
+            if ((rc = dev_dot(ctx, dptr<double>(T.x), dptr<double>(T.acc), n, T.part, &s))) return rc;
+            if (hasInt && (rc = dev_dot(ctx, dptr<double>(T.il), dptr<double>(T.iacc), ni, T.part, &si))) return rc;
+            dldd[d - 1] = (dldd_explicit ? dldd_explicit[d - 1] : 0.0) - s - si;
+        }
+    }
+    if (disp_adj) {
+        if ((rc = dev_alloc(ctx, T.ref, sizeof(double) * n))) return rc;
+        if ((rc = int_to_ref_vec(ctx, dptr<double>(T.x), dptr<double>(T.ref), n))) return rc;
+        CK(cudaMemcpyAsync(disp_adj, T.ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    if (int_disp_adj && hasInt)
+        CK(cudaMemcpyAsync(int_disp_adj, T.il.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
 }

@@ -245,6 +245,31 @@ class Oracle:
         keep = self.mpc_cols > 0
         return sp.csr_matrix((mpc_mat[keep], (rows[keep], self.mpc_cols[keep] - 1)), shape=(self.mpc_dim, self.n))
 
+    def total_dldd(self, dldu, int_dldu=None, dldd_explicit=None, state=None, h=1e-14):
+        """getTotaldLdD, static branch (Working/AStrO_commandFunctions.f90:1377-1410) with the elastic
+        branch of solveDynamicAdjoint (:917-966, dLdv = dLda = 0): tangent and scaled constraints at
+        the state, condensation of (dldu, int_dldu), the adjoint by a direct solve of
+        (K + C^T C) lambda = b, the internal lambda, then dLdD(d) = explicit(d) - lambda . dRudD(d)
+        - lambda_int . intdRudD(d).  Returns (dLdD, lambda, lambda_int)."""
+        import scipy.sparse.linalg as spla
+        _, _, mat, cols, imat = self.el_soln_load(1, state=state)
+        mm, _ = self.scale_mpc(mat)
+        A = (self.csr_scipy(mat, cols) + self.mpc_scipy(mm).T @ self.mpc_scipy(mm)).tocsc()
+        b = np.asarray(dldu, np.float64).copy()
+        ni = self.int_vec_size
+        if ni and int_dldu is not None:
+            b = self.update_external_rhs(b, int_dldu, imat)
+        lam = spla.spsolve(A, b)
+        lam_i = np.zeros(ni)
+        if ni:
+            lam_i = self.update_internal_soln(lam, np.zeros(ni), int_dldu, imat)[:ni]
+        nd = len(self.model.d_value)
+        out = np.zeros(nd) if dldd_explicit is None else np.asarray(dldd_explicit, np.float64).copy()
+        for d in range(1, nd + 1):
+            dr, dri = self.drdd_complex(d, h, state=state)
+            out[d - 1] -= lam @ dr + (lam_i @ dri[:ni] if ni else 0.0)
+        return out, lam, lam_i
+
     def static_system(self):
         """(A = K + C^T C, b) of the linear static step from zero state with the scaled constraints."""
         load, iload, mat, cols, imat = self.el_soln_load(1)

@@ -215,3 +215,34 @@ def test_static_condensation_round_trip():
     a = o.update_internal_soln(u, np.zeros(ni), g, imat)
     assert np.linalg.norm(u - full[:n]) <= 1e-8 * np.linalg.norm(full[:n])
     assert np.linalg.norm(a - full[n:]) <= 1e-8 * np.linalg.norm(full[n:])
+
+
+def test_static_adjoint_gradient_matches_central_difference():
+    """getTotaldLdD (static) for the compliance L(d) = b . u(d): the adjoint gradient at the solved
+    state equals central differences of L over re-assembled systems (modulus design variables,
+    relative step 1e-4 of E).  The adjoint uses the tangent at the solved state, whose stress
+    stiffness is of the order of the strain: a 1e2 Pa traction keeps it near 1e-9."""
+    import scipy.sparse.linalg as spla
+
+    def build(dv):
+        m = M.hex_block(nx=4, ny=2, nz=2, jitter=0.1, seed=3, traction=1.0e2)
+        m = M.add_design_variables(m, 2, M.DCAT_ELASTIC_MODULUS, component=1)
+        m.d_value = np.asarray(dv, np.float64)
+        return m
+
+    def compliance(dv):
+        o = Oracle(build(dv))
+        A, b, *_ = o.static_system()
+        u = spla.spsolve(A.tocsc(), b)
+        return b @ u, u, b, o
+
+    d0 = np.zeros(2)
+    L0, u, b, o = compliance(d0)
+    st = M.make_state(o.n, disp=u)
+    g, lam, _ = o.total_dldd(b, state=st)
+    step = 1e-4 * 2.0e11
+    for k in range(2):
+        e = np.zeros(2)
+        e[k] = step
+        fd = (compliance(d0 + e)[0] - compliance(d0 - e)[0]) / (2 * step)
+        assert abs(g[k] - fd) <= 1e-5 * abs(fd), (k, g[k], fd)
