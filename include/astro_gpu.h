@@ -372,6 +372,45 @@ int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double h, const d
                      const double *dldd_explicit, const astro_solve_opts *opts, double *dldd, double *disp_adj,
                      double *int_disp_adj, astro_solve_stats *stats);
 
+/* getTotaldLdD for a Newmark analysis (Working/AStrO_commandFunctions.f90:1411-1465): the backward
+ * sweep i = num_steps..1 over the stored states, each step augmentdLdu (:819-915; i < num_steps),
+ * the objective's partials at t_i, solveDynamicAdjoint's elastic branch (:917-966) with K_eff at
+ * (state i, previous state i-1) and the complex-step dRu/dD at that state:
+ *     dldd[d-1] = dldd_explicit[d-1] - sum_i (lambda_i . dRudD_i(d) + lambda_int_i . intdRudD_i(d)).
+ * The states are the records of SolutionHistory<i> (i = 0..num_steps): disp, vel, acc
+ * ((num_steps + 1) x el_mat_dim) and int_disp ((num_steps + 1) x int_vec_size, may be NULL).  The
+ * objective's partials per step are rows i-1 of dldu, dldv, dlda (num_steps x el_mat_dim) and
+ * int_dldu (num_steps x int_vec_size); any may be NULL (zero).  Faithful to the reference: the
+ * 1e-20 scaling round trip around augmentdLdu, the warm start of each adjoint solve from the
+ * previous one, and the internal adjoint accumulated across steps (updateInternalSoln adds).
+ * Shell meshes (the Newmark inertia is implemented for shell4).  disp_adj (el_mat_dim, may be NULL)
+ * receives the adjoint of step 1; stats sums the solves. */
+typedef struct astro_transient_adjoint {
+    int32_t num_steps;
+    double del_t, nm_beta, nm_gamma;
+    double h;                               /* complex step of getdRelasticdD */
+    const double *disp, *vel, *acc, *int_disp;
+    const double *dldu, *dldv, *dlda, *int_dldu;
+    const double *dldd_explicit;            /* num_dvars (getdObjdD summed over the steps), may be NULL */
+    astro_solve_opts solve;                 /* the adjoint solves */
+} astro_transient_adjoint;
+int astro_total_dldd_transient(astro_ctx *ctx, const astro_transient_adjoint *a, double *dldd, double *disp_adj,
+                               astro_solve_stats *stats);
+
+/* Solution-history step file of the reference (writeBinarySolution / readBinarySolution,
+ * Working/AStrO_output.f90:761-784, Working/AStrO_input.f90:1740-1768): Fortran unformatted
+ * sequential records (4-byte length markers before and after each record) of prevTemp
+ * (num_nodes), prevTdot (num_nodes), prevDisp (el_mat_dim), prevIntDisp (int_vec_size; written when
+ * int_vec_size >= 1, read when int_vec_size > 1, as the reference does), prevVel, prevAcc.  Host
+ * only.  NULL temperature arrays write zeros / skip the values on reading.  The reader returns
+ * ASTRO_ERR_ARG when the file cannot be opened or is short (the reference's errFlag). */
+int astro_write_step_file(const char *path, int32_t num_nodes, int32_t el_mat_dim, int32_t int_vec_size,
+                          const double *prev_temp, const double *prev_tdot, const double *prev_disp,
+                          const double *prev_int_disp, const double *prev_vel, const double *prev_acc);
+int astro_read_step_file(const char *path, int32_t num_nodes, int32_t el_mat_dim, int32_t int_vec_size,
+                         double *prev_temp, double *prev_tdot, double *prev_disp, double *prev_int_disp,
+                         double *prev_vel, double *prev_acc);
+
 /* Measurement hook: the average device time (CUDA events, reps launches after five warm-up
  * launches) of one preconditioner hop on the operator of the last learned solve of this context,
  * and the bytes one hop moves (FP16 block planes, columns, and the hop's vector loads and stores).

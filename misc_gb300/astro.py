@@ -65,6 +65,13 @@ class SolveOptsC(C.Structure):
                 ("inner_rtol", C.c_double), ("precond", C.POINTER(PrecondC))]
 
 
+class TransientAdjointC(C.Structure):
+    _fields_ = [("num_steps", C.c_int32), ("del_t", C.c_double), ("nm_beta", C.c_double), ("nm_gamma", C.c_double),
+                ("h", C.c_double), ("disp", F64P), ("vel", F64P), ("acc", F64P), ("int_disp", F64P),
+                ("dldu", F64P), ("dldv", F64P), ("dlda", F64P), ("int_dldu", F64P), ("dldd_explicit", F64P),
+                ("solve", SolveOptsC)]
+
+
 class SolveStatsC(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("restarts", C.c_int32), ("refinements", C.c_int32),
                 ("status", C.c_int32), ("rel_residual", C.c_double), ("seconds", C.c_double),
@@ -122,6 +129,12 @@ def load_library():
         "astro_precond_loss_grad": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, F64P, F64P], C.c_int),
         "astro_precond_train": ([vp, C.POINTER(PrecondC), F64P, C.c_int32, C.c_int32, F64P], C.c_int),
         "astro_precond_time_hop": ([vp, C.c_int32, F64P, F64P], C.c_int),
+        "astro_total_dldd_transient": ([vp, C.POINTER(TransientAdjointC), F64P, F64P, C.POINTER(SolveStatsC)],
+                                       C.c_int),
+        "astro_write_step_file": ([C.c_char_p, C.c_int32, C.c_int32, C.c_int32, F64P, F64P, F64P, F64P, F64P, F64P],
+                                  C.c_int),
+        "astro_read_step_file": ([C.c_char_p, C.c_int32, C.c_int32, C.c_int32, F64P, F64P, F64P, F64P, F64P, F64P],
+                                 C.c_int),
         "astro_total_dldd": ([vp, vp, C.c_double, F64P, F64P, F64P, C.POINTER(SolveOptsC), F64P, F64P, F64P,
                               C.POINTER(SolveStatsC)], C.c_int),
     }
@@ -151,6 +164,30 @@ def _f64(a):
 
 def _i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def write_step_file(path, num_nodes, disp, vel, acc, int_disp=None, temp=None, tdot=None):
+    """SolutionHistory<i>.out in the reference's record layout (writeBinarySolution)."""
+    disp, vel, acc = _f64(disp), _f64(vel), _f64(acc)
+    ni = 0 if int_disp is None else len(int_disp)
+    rc = load_library().astro_write_step_file(str(path).encode(), num_nodes, len(disp), ni,
+                                              None if temp is None else _d(_f64(temp)),
+                                              None if tdot is None else _d(_f64(tdot)), _d(disp),
+                                              None if int_disp is None else _d(_f64(int_disp)), _d(vel), _d(acc))
+    if rc != ASTRO_OK:
+        raise AstroError(rc, f"cannot write {path}")
+
+
+def read_step_file(path, num_nodes, el_mat_dim, int_vec_size=0):
+    """(temp, tdot, disp, int_disp, vel, acc) of a SolutionHistory<i>.out file (readBinarySolution)."""
+    t, td = np.zeros(max(num_nodes, 1)), np.zeros(max(num_nodes, 1))
+    u, v, a = np.zeros(el_mat_dim), np.zeros(el_mat_dim), np.zeros(el_mat_dim)
+    iu = np.zeros(max(int_vec_size, 1))
+    rc = load_library().astro_read_step_file(str(path).encode(), num_nodes, el_mat_dim, int_vec_size, _d(t), _d(td),
+                                             _d(u), _d(iu), _d(v), _d(a))
+    if rc != ASTRO_OK:
+        raise AstroError(rc, f"cannot read {path}")
+    return t[:num_nodes], td[:num_nodes], u, iu[:int_vec_size], v, a
 
 
 def precond_init(degree=24, ratio=3000.0, dpn=3):
@@ -375,6 +412,31 @@ class AstroGPU:
                                             None if dldd_explicit is None else _d(_f64(dldd_explicit)),
                                             C.byref(o), _d(dldd), _d(lam), _d(ilam), C.byref(st)))
         return dldd[:nd], lam, ilam[:self.int_vec_size], st
+
+    def getTotaldLdD_transient(self, disp, vel, acc, int_disp, del_t, beta=0.25, gamma=0.5, dldu=None, dldv=None,
+                               dlda=None, int_dldu=None, dldd_explicit=None, h=1e-14,
+                               method=SOLVER_GMRES_JACOBI_FP64, rtol=1e-12, restart=50, max_iters=200000):
+        """Transient design gradient over stored Newmark states (rows 0..N of disp/vel/acc/int_disp)
+        and per-step objective partials (rows 0..N-1 for t_1..t_N): (dLdD, adjoint of step 1, stats)."""
+        N = np.asarray(disp).shape[0] - 1
+        nd = len(self.model.d_value) if getattr(self.model, "d_value", None) is not None else 0
+        keep = []
+
+        def arr(x):
+            if x is None:
+                return None
+            a = np.ascontiguousarray(x, np.float64)
+            keep.append(a)
+            return _d(a)
+
+        a = TransientAdjointC(N, del_t, beta, gamma, h, arr(disp), arr(vel), arr(acc), arr(int_disp), arr(dldu),
+                              arr(dldv), arr(dlda), arr(int_dldu), arr(dldd_explicit),
+                              SolveOptsC(method, restart, max_iters, rtol, 1e-4, C.POINTER(PrecondC)()))
+        dldd = np.zeros(max(nd, 1))
+        lam = np.zeros(self.n)
+        st = SolveStatsC()
+        self._check(self.L.astro_total_dldd_transient(self.h, C.byref(a), _d(dldd), _d(lam), C.byref(st)))
+        return dldd[:nd], lam, st
 
     # -- polynomial preconditioner ----------------------------------------------------------------
     def precond_lambda(self, kind=64):

@@ -270,6 +270,71 @@ class Oracle:
             out[d - 1] -= lam @ dr + (lam_i @ dri[:ni] if ni else 0.0)
         return out, lam, lam_i
 
+    def total_dldd_transient(self, disp, vel, acc, int_disp, del_t, beta, gamma, dldu=None, dldv=None, dlda=None,
+                             int_dldu=None, dldd_explicit=None, h=1e-14, accumulate_internal=True):
+        """getTotaldLdD, dynamic branch (Working/AStrO_commandFunctions.f90:1411-1465): the backward
+        sweep over the stored states (rows 0..N), augmentdLdu (:819-915) with the 1e-20 scaling round
+        trip, solveDynamicAdjoint's elastic branch (:917-966) by direct solves of K_eff at (state i,
+        state i-1), the internal adjoint accumulated as updateInternalSoln does, and the complex-step
+        dRu/dD at each state.  Returns (dLdD, adjoint of step 1)."""
+        import scipy.sparse.linalg as spla
+        from misc_gb300 import model as M
+        n, ni = self.n, self.int_vec_size
+        N = len(disp) - 1
+        nd = len(self.model.d_value)
+        f = 1e-20
+        rt = lambda x: (np.asarray(x, np.float64) * f) * (1.0 / f)
+        iud = (lambda i: np.asarray(int_disp[i], np.float64)) if int_disp is not None else (lambda i: np.zeros(ni))
+        lam, ilam = np.zeros(n), np.zeros(ni)
+        velAdj, accAdj = np.zeros(n), np.zeros(n)
+        out = np.zeros(nd) if dldd_explicit is None else np.asarray(dldd_explicit, np.float64).copy()
+
+        def st(u, v, a, iu, pu, pv, pa, piu):
+            return M.make_state(n, disp=u, vel=v, acc=a, internal_disp=iu, prev_disp=pu, prev_vel=pv, prev_acc=pa,
+                                prev_int_disp=piu, dynamic=1, beta=beta, gamma=gamma, del_t=del_t)
+
+        for i in range(N, 0, -1):
+            dLdu, dLdv, dLda, idLdu = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(ni)
+            u, v, a, iu = (np.asarray(disp[i], np.float64), np.asarray(vel[i], np.float64),
+                           np.asarray(acc[i], np.float64), iud(i))
+            if i < N:
+                nu, nv, na, niu = (np.asarray(disp[i + 1]) * f, np.asarray(vel[i + 1]) * f,
+                                   np.asarray(acc[i + 1]) * f, iud(i + 1) * f)
+                pu, pv, pa, piu = u * f, v * f, a * f, iu * f
+                load, iload, *_ = self.el_soln_load(0, state=st(nu, nv, na, niu, lam, pv, pa, ilam))
+                dLdu += load + accAdj
+                idLdu += iload[:ni]
+                load, *_ = self.el_soln_load(0, state=st(nu, nv, na, niu, pu, pv, lam, piu))
+                dLda += load + 0.5 * del_t * del_t * (1 - 2 * beta) * accAdj + del_t * (1 - gamma) * velAdj
+                load, *_ = self.el_soln_load(0, state=st(nu, nv, na, niu, pu, lam, pa, piu))
+                dLdv += load + del_t * accAdj + velAdj
+                u, v, a, iu = rt(u), rt(v), rt(a), rt(iu)
+            if dldu is not None:
+                dLdu += dldu[i - 1]
+            if dldv is not None:
+                dLdv += dldv[i - 1]
+            if dlda is not None:
+                dLda += dlda[i - 1]
+            if int_dldu is not None:
+                idLdu += int_dldu[i - 1]
+            velAdj = dLdv.copy()
+            accAdj = (-1.0 / (del_t * del_t * beta)) * (dLda + del_t * gamma * velAdj)
+            dLdu = dLdu - accAdj
+            s = st(u, v, a, iu, np.asarray(disp[i - 1], np.float64), np.asarray(vel[i - 1], np.float64),
+                   np.asarray(acc[i - 1], np.float64), iud(i - 1))
+            _, _, mat, cols, imat = self.el_soln_load(1, state=s)
+            mm, _ = self.scale_mpc(mat)
+            A = (self.csr_scipy(mat, cols) + self.mpc_scipy(mm).T @ self.mpc_scipy(mm)).tocsc()
+            if ni:
+                dLdu = self.update_external_rhs(dLdu, idLdu, imat)
+            lam = spla.spsolve(A, dLdu)
+            if ni:
+                ilam = self.update_internal_soln(lam, ilam if accumulate_internal else np.zeros(ni), idLdu, imat)[:ni]
+            for d in range(1, nd + 1):
+                dr, dri = self.drdd_complex(d, h, state=s)
+                out[d - 1] -= lam @ dr + (ilam @ dri[:ni] if ni else 0.0)
+        return out, lam
+
     def static_system(self):
         """(A = K + C^T C, b) of the linear static step from zero state with the scaled constraints."""
         load, iload, mat, cols, imat = self.el_soln_load(1)

@@ -69,3 +69,31 @@ def test_adjoint_needs_assembly():
     g = AstroGPU(m)
     with pytest.raises(AstroError):
         g.getTotaldLdD(np.ones(g.n))
+
+
+def test_transient_adjoint_matches_oracle():
+    """The Newmark backward sweep (astro_total_dldd_transient) against the oracle's restatement on
+    the same stored states: dL/dD and the adjoint of step 1, with objective partials in u, v, a and
+    at the internal DOF."""
+    import newmark_ref as NR
+
+    m = M.plate_shell(nx=6, ny=4, lx=1.0, ly=0.5, t=0.01, E=7e10, nu=0.33, rho=2700.0, pressure=0.0)
+    m = M.add_design_variables(m, 3, M.DCAT_LAYUP_THICKNESS)
+    o, g = Oracle(m), AstroGPU(m)
+    n, ni = o.n, o.int_vec_size
+    dt, beta, gamma, steps = 1e-4, 0.25, 0.5, 4
+    pattern = np.zeros(n)
+    pattern[o.n_dof_index[m.num_nodes - 1, 2] - 1] = 1.0
+    amp = 50.0 * np.sin(2 * np.pi * 500.0 * dt * np.arange(1, steps + 1))
+    D, V, A, I = NR.newmark_states(o, pattern, amp, dt, beta, gamma, steps)
+    rng = np.random.default_rng(8)
+    w = rng.standard_normal((steps, n))
+    wv = 1e-3 * rng.standard_normal((steps, n))
+    wa = 1e-7 * rng.standard_normal((steps, n))
+    wi = rng.standard_normal((steps, ni))
+    dldd, lam, st = g.getTotaldLdD_transient(D, V, A, I, dt, beta, gamma, dldu=w, dldv=wv, dlda=wa, int_dldu=wi,
+                                             rtol=1e-13)
+    od, olam = o.total_dldd_transient(D, V, A, I, dt, beta, gamma, dldu=w, dldv=wv, dlda=wa, int_dldu=wi)
+    assert st.status == 0
+    assert _rel(lam, olam) < 1e-6
+    assert _rel(dldd, od) < 1e-6
