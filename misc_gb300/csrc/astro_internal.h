@@ -68,6 +68,9 @@ struct astro_ctx {
     int unrolledCycles = 0;  // ASTRO_OPT_UNROLLED_CYCLES
     cudaStream_t stream = nullptr;
     cudaStream_t stream2 = nullptr;  // copies that overlap the element kernels
+    // the FP32 assembly pass (one launch per colour) captured once as a graph and replayed
+    cudaGraph_t asmGraph = nullptr;
+    cudaGraphExec_t asmExec = nullptr;
     int device = 0;
     AstroPrep P;
     // host model copy

@@ -58,6 +58,10 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 
 static void free_all(astro_ctx *c) {
     krylov_release(c);
+    if (c->asmExec) cudaGraphExecDestroy(c->asmExec);
+    if (c->asmGraph) cudaGraphDestroy(c->asmGraph);
+    c->asmExec = nullptr;
+    c->asmGraph = nullptr;
     DevBuf *bufs[] = {&c->d_nodes,  &c->d_elist,   &c->d_elMat,   &c->d_esec,    &c->d_secABD,   &c->d_secOrient,
                       &c->d_colorEls, &c->d_elBlk, &c->d_rank,    &c->d_bRowPtr, &c->d_bCol,     &c->d_bRow,
                       &c->d_etype,  &c->d_elFirst, &c->d_K64p, &c->d_K32p, &c->d_ellCol, &c->d_K64,     &c->d_K32,     &c->d_csrPos,  &c->d_elMatRangeRank,
@@ -566,7 +570,29 @@ extern "C" int astro_assemble_fp32(astro_ctx *ctx) {
 extern "C" int astro_assemble_fp32_async(astro_ctx *ctx) {
     if (!ctx || !ctx->d_K32.p) return ASTRO_ERR_STATE;
     ctx->k32Version++;
-    return launch_hex8_assemble(ctx, 32, 1);
+    if (!ctx->hasSolid || ctx->hasShell) return launch_hex8_assemble(ctx, 32, 1);
+    // the colour launches of a pass depend on one another only through the stream order; as a
+    // graph they are issued together, without a host launch per colour
+    if (!ctx->asmExec) {
+        int rc;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        rc = launch_hex8_assemble(ctx, 32, 1);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CK(e);
+        e = cudaGraphInstantiate(&ctx->asmExec, g, 0);
+        if (e != cudaSuccess) {
+            cudaGraphDestroy(g);
+            ctx->asmExec = nullptr;
+            return cuda_check(ctx, e, "assembly graph");
+        }
+        ctx->asmGraph = g;
+    }
+    return cuda_check(ctx, cudaGraphLaunch(ctx->asmExec, ctx->stream), "assembly graph launch");
 }
 
 void dvar_elements_by_colour(const astro_ctx *ctx, int dvar, std::vector<int> &list, std::vector<int> &ptr) {
