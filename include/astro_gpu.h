@@ -322,6 +322,10 @@ typedef struct astro_newmark_opts {
     double del_t, nm_beta, nm_gamma;
     int32_t restart, max_iters;  /* GMRES per step */
     double rtol;
+    int32_t method;                /* ASTRO_SOLVER_*: 0 FP64 Jacobi-GMRES (the default, as above);
+                                      1 mixed or 2 learned FGMRES on K_eff, FP32 copy converted
+                                      from the FP64 K_eff, FP64 refinement */
+    const astro_precond *precond;  /* method 2: the network (NULL: the default network) */
 } astro_newmark_opts;
 int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *opts, const double *load_pattern,
                       const double *load_amplitude, double *disp, double *vel, double *acc,

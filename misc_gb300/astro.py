@@ -80,7 +80,8 @@ class SolveStatsC(C.Structure):
 
 class NewmarkOptsC(C.Structure):
     _fields_ = [("num_steps", C.c_int32), ("del_t", C.c_double), ("nm_beta", C.c_double), ("nm_gamma", C.c_double),
-                ("restart", C.c_int32), ("max_iters", C.c_int32), ("rtol", C.c_double)]
+                ("restart", C.c_int32), ("max_iters", C.c_int32), ("rtol", C.c_double), ("method", C.c_int32),
+                ("precond", C.POINTER(PrecondC))]
 
 
 def lib_path():
@@ -372,7 +373,8 @@ class AstroGPU:
         return out
 
     def newmark_run(self, num_steps, del_t, beta=0.25, gamma=0.5, load_pattern=None, load_amplitude=None, disp=None,
-                    vel=None, acc=None, int_disp=None, restart=50, max_iters=2000, rtol=1e-12, history=True):
+                    vel=None, acc=None, int_disp=None, restart=50, max_iters=2000, rtol=1e-12, history=True,
+                    method=SOLVER_GMRES_JACOBI_FP64, precond=None):
         """solve() dynamic branch on the device: returns (disp, vel, acc, int_disp, history, stats)."""
         n, ni = self.n, self.int_vec_size
         u = np.zeros(n) if disp is None else _f64(disp).copy()
@@ -380,7 +382,8 @@ class AstroGPU:
         a = np.zeros(n) if acc is None else _f64(acc).copy()
         iu = np.zeros(max(ni, 1)) if int_disp is None else _f64(int_disp).copy()
         hist = np.zeros((num_steps, n)) if history else None
-        o = NewmarkOptsC(num_steps, del_t, beta, gamma, restart, max_iters, rtol)
+        o = NewmarkOptsC(num_steps, del_t, beta, gamma, restart, max_iters, rtol, method,
+                         C.pointer(precond) if precond is not None else C.POINTER(PrecondC)())
         st = SolveStatsC()
         pat = None if load_pattern is None else _d(_f64(load_pattern))
         amp = None if load_amplitude is None else _d(_f64(load_amplitude))

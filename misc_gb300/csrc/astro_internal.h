@@ -110,6 +110,7 @@ struct astro_ctx {
     // penalty C^T C as CSR over internal rows (host-built after scaling)
     DevBuf d_penRow, d_penPtr, d_penCol, d_penVal;
     int penRows = 0;
+    int penVersion = 0;  // incremented whenever the penalty lists are rebuilt (astro_scale_mpc)
     std::vector<double> mpcScaledHost, mpcRhsScaledHost;
     // skyline (reference DOF numbering) on device
     DevBuf d_ltRange, d_lt;

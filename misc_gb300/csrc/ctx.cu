@@ -792,6 +792,7 @@ static int build_penalty(astro_ctx *ctx) {
     if ((rc = upload(ctx, ctx->d_penRow, prow.data(), sizeof(int) * prow.size()))) return rc;
     if ((rc = upload(ctx, ctx->d_penCol, pcol.data(), sizeof(int) * pcol.size()))) return rc;
     if ((rc = upload(ctx, ctx->d_penVal, pval.data(), sizeof(double) * pval.size()))) return rc;
+    ctx->penVersion++;
     return ASTRO_OK;
 }
 

@@ -627,9 +627,10 @@ __global__ void k_dinv(const TM *__restrict__ K, const int *__restrict__ rowPtr,
     }
 }
 
-// block-CSR (dd-value row-major blocks) -> slot-major block-ELL, one thread per (row, slot)
-template <class T>
-__global__ void k_to_ell(const T *__restrict__ K, const int *__restrict__ rowPtr, const int *__restrict__ bCol, int N,
+// block-CSR (dd-value row-major blocks) -> slot-major block-ELL, one thread per (row, slot); the
+// values are converted to the ELL's type (an FP32 solver copy of the FP64 matrix)
+template <class TS, class T>
+__global__ void k_to_ell(const TS *__restrict__ K, const int *__restrict__ rowPtr, const int *__restrict__ bCol, int N,
                          int S, int ld, int dd, T *__restrict__ Ke, int *__restrict__ colE) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= (long long)S * ld) return;
@@ -637,7 +638,7 @@ __global__ void k_to_ell(const T *__restrict__ K, const int *__restrict__ rowPtr
     const int k = (r < N) ? rowPtr[r] + s : -1;
     const bool has = r < N && k < rowPtr[r + 1];
     if (colE) colE[t] = has ? bCol[k] : (r < N ? r : 0);
-    for (int q = 0; q < dd; ++q) Ke[((size_t)s * dd + q) * ld + r] = has ? K[(size_t)k * dd + q] : T(0);
+    for (int q = 0; q < dd; ++q) Ke[((size_t)s * dd + q) * ld + r] = has ? (T)K[(size_t)k * dd + q] : T(0);
 }
 
 }  // namespace
@@ -661,6 +662,8 @@ struct GmresWork {
     cudaStream_t bodyStream = nullptr;  // captures the bodies of the cycle's IF nodes
     bool condOk = true;                 // conditional graph nodes available
     OpH hop;
+    int hopVersion = -1;  // version of the matrix the operator and lamEst were built from
+    double lamEst = 0.0;  // power-iteration estimate of the largest eigenvalue of D^-1 A
     // L2 persistence window over the operator's block planes for the hop launches (a launch
     // attribute, so captured into the graph nodes); off when the device has no persisting L2
     cudaAccessPolicyWindow apw = {};
@@ -679,14 +682,20 @@ struct GmresWork {
     std::vector<double> hp;
 };
 
+// Version of the matrix the FP32 solver copy comes from: the FP32 assembly when there is one,
+// else the FP64 matrix converted (the shell path has no FP32 element kernels).
+static int k32_source_version(const astro_ctx *ctx) {
+    return ctx->haveK32 ? ctx->k32Version : 1000000 + ctx->k64Version;
+}
+
 // Solver copy of the assembled matrix in slot-major block-ELL layout (rebuilt when the assembly
-// changed).
+// changed).  The FP32 copy converts the FP64 matrix when no FP32 assembly exists.
 template <class TM> static const TM *ell_of(astro_ctx *ctx, int *rc) {
     const bool f64 = sizeof(TM) == 8;
-    DevBuf &src = f64 ? ctx->d_K64 : ctx->d_K32;
+    const bool cvt = !f64 && !ctx->haveK32;
     DevBuf &dst = f64 ? ctx->d_K64p : ctx->d_K32p;
     int &ver = f64 ? ctx->k64PlanesVersion : ctx->k32PlanesVersion;
-    const int cur = f64 ? ctx->k64Version : ctx->k32Version;
+    const int cur = f64 ? ctx->k64Version : k32_source_version(ctx);
     const AstroPrep &P = ctx->P;
     const int dd = P.dpn * P.dpn;
     *rc = ASTRO_OK;
@@ -705,9 +714,14 @@ template <class TM> static const TM *ell_of(astro_ctx *ctx, int *rc) {
     if (!dst.p && (*rc = dev_alloc(ctx, dst, sizeof(TM) * (size_t)S * dd * ld))) return nullptr;
     if (ver != cur || needCol) {
         const long long tot = (long long)S * ld;
-        k_to_ell<TM><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(
-            dptr<TM>(src), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), P.N, S, ld, dd, dptr<TM>(dst),
-            needCol ? dptr<int>(ctx->d_ellCol) : nullptr);
+        const unsigned g = (unsigned)((tot + 255) / 256);
+        int *colOut = needCol ? dptr<int>(ctx->d_ellCol) : nullptr;
+        if (f64 || cvt)
+            k_to_ell<double, TM><<<g, 256, 0, ctx->stream>>>(dptr<double>(ctx->d_K64), dptr<int>(ctx->d_bRowPtr),
+                                                             dptr<int>(ctx->d_bCol), P.N, S, ld, dd, dptr<TM>(dst), colOut);
+        else
+            k_to_ell<float, TM><<<g, 256, 0, ctx->stream>>>(dptr<float>(ctx->d_K32), dptr<int>(ctx->d_bRowPtr),
+                                                            dptr<int>(ctx->d_bCol), P.N, S, ld, dd, dptr<TM>(dst), colOut);
         if ((*rc = cuda_check(ctx, cudaGetLastError(), "to_ell"))) return nullptr;
         ver = cur;
     }
@@ -1131,7 +1145,7 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     size_t persistPrev = 0;
     bool persistSet = false;
     if (fp64 && !ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "FP64 stiffness not assembled");
-    if (!fp64 && !ctx->haveK32) return set_err(ctx, ASTRO_ERR_STATE, "FP32 stiffness not assembled");
+    if (!fp64 && !ctx->haveK32 && !ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "stiffness not assembled");
     GmresWork *Wp = work_get(ctx, fp64 ? 0 : (learned ? 2 : 1), m, fp64 ? sizeof(double) : sizeof(float), &rc);
     if (!Wp) return rc;
     GmresWork &W = *Wp;
@@ -1176,10 +1190,17 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     } else {
         const float *K32p = ell_of<float>(ctx, &rc);
         if (rc) return rc;
-        k_dinv<float, float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
-            dptr<float>(ctx->d_K32), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn,
-            ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
-            dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<float>(W.dinvT));
+        const int* pp = ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr;
+        if (ctx->haveK32)
+            k_dinv<float, float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
+                dptr<float>(ctx->d_K32), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn, pp,
+                dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol), dptr<double>(ctx->d_penVal), dptr<double>(W.dinv),
+                dptr<float>(W.dinvT));
+        else
+            k_dinv<double, float><<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
+                dptr<double>(ctx->d_K64), dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), ctx->P.N, ctx->P.dpn, pp,
+                dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol), dptr<double>(ctx->d_penVal), dptr<double>(W.dinv),
+                dptr<float>(W.dinvT));
         if (learned) {
             // the network's hop vectors, its operator A^ = S A S in FP16 with S = D^-1/2, and the
             // interval [lambda/ratio, lambda] from the eigenvalue estimate on A^ (inside the timed
@@ -1196,25 +1217,29 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
                 dev_free(W.Kh);
                 return rc;
             }
-            k_sqrt_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(dptr<double>(W.dinv), dptr<float>(W.dsqT), n);
-            const long long tot = (long long)S * ld;
-            k_scaled_bv<DPN><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(
-                K32p, dptr<int>(ctx->d_ellCol), S, ld, ctx->P.N, dptr<float>(W.dsqT), dptr<uint4>(W.Kh), W.Kr.p);
-            {
+            // the operator and its eigenvalue estimate depend only on the matrix: rebuilt when the
+            // matrix (or its constraint scaling) changed, reused by repeated solves (time steps)
+            const int opVer = k32_source_version(ctx) * 64 + (ctx->penVersion & 63);
+            if (W.hopVersion != opVer) {
+                k_sqrt_f<<<(n + 255) / 256, 256, 0, ctx->stream>>>(dptr<double>(W.dinv), dptr<float>(W.dsqT), n);
+                const long long tot = (long long)S * ld;
+                k_scaled_bv<DPN><<<(unsigned)((tot + 255) / 256), 256, 0, ctx->stream>>>(
+                    K32p, dptr<int>(ctx->d_ellCol), S, ld, ctx->P.N, dptr<float>(W.dsqT), dptr<uint4>(W.Kh), W.Kr.p);
                 const Op<float> o32 = make_op<float>(ctx, K32p);
                 W.hop = OpH{dptr<uint4>(W.Kh), W.Kr.p, o32.col,    o32.S,      o32.ld,    o32.penPtr,
                             o32.penRow,         o32.penCol, o32.penVal, o32.N, o32.dpn};
+                if (ctx->penRows) {
+                    k_scaled_pen<<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
+                        dptr<int>(ctx->d_penPtr), dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
+                        dptr<double>(ctx->d_penVal), ctx->P.N, DPN, dptr<double>(W.dinv), dptr<double>(W.penS));
+                    W.hop.penVal = dptr<double>(W.penS);
+                }
+                if ((rc = cuda_check(ctx, cudaGetLastError(), "preconditioner operator")) ||
+                    (rc = power_lambda<OpH, float, DPN>(ctx, W.hop, (const float *)nullptr, &W.lamEst)))
+                    return rc;
+                W.hopVersion = opVer;
             }
-            if (ctx->penRows) {
-                k_scaled_pen<<<(ctx->P.N + 255) / 256, 256, 0, ctx->stream>>>(
-                    dptr<int>(ctx->d_penPtr), dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol),
-                    dptr<double>(ctx->d_penVal), ctx->P.N, DPN, dptr<double>(W.dinv), dptr<double>(W.penS));
-                W.hop.penVal = dptr<double>(W.penS);
-            }
-            if ((rc = cuda_check(ctx, cudaGetLastError(), "preconditioner operator")) ||
-                (rc = power_lambda<OpH, float, DPN>(ctx, W.hop, (const float *)nullptr, &lam)))
-                return rc;
-            lam *= pc->lambda_scale;
+            lam = W.lamEst * pc->lambda_scale;
             ph.deg = pc->degree;
             ph.theta = (float)(0.5 * lam * (1.0 + 1.0 / pc->ratio));
             ph.delta = (float)(0.5 * lam * (1.0 - 1.0 / pc->ratio));
@@ -1225,8 +1250,11 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
         }
         float *d32 = dptr<float>(W.xs);
         const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
+        // the outer residual is formed with the FP64 matrix when it is resident (the system the
+        // tolerance refers to), else with the FP32 assembly's values in FP64 arithmetic
+        const int refKind = ctx->haveK64 ? 64 : 32;
         for (refinements = 0; refinements < 200; ++refinements) {
-            if ((rc = true_residual<DPN>(ctx, W, 32, d_x, d_b, &rel, r, &rn))) break;
+            if ((rc = true_residual<DPN>(ctx, W, refKind, d_x, d_b, &rel, r, &rn))) break;
             if (rel <= o->rtol) break;
             if (!std::isfinite(rel)) {
                 rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite residual in refinement");
@@ -1501,8 +1529,11 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
     if (!rc && ni) rc = dev_alloc(ctx, iload, sizeof(double) * ni);
     const double *K = rc ? nullptr : ell_of<double>(ctx, &rc);
     cudaStream_t s = ctx->stream;
-    int iters = 0, cycles = 0, worst = ASTRO_OK;
+    int iters = 0, cycles = 0, refs = 0, worst = ASTRO_OK;
     double worstRel = 0.0;
+    if (o->method != ASTRO_SOLVER_GMRES_JACOBI_FP64 && o->method != ASTRO_SOLVER_FGMRES_MIXED &&
+        o->method != ASTRO_SOLVER_FGMRES_LEARNED)
+        return set_err(ctx, ASTRO_ERR_ARG, "unknown solver method");
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -1536,18 +1567,45 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
         if (d_pattern && h_amp) k_axpy<<<grid, 256, 0, s>>>(n, h_amp[step], d_pattern, dptr<double>(load));
         if ((rc = constraint_load_dev(ctx, d_u, dptr<double>(load)))) break;
         if (ni && (rc = shell4_update_external_rhs(ctx, dptr<double>(iload), dptr<double>(load)))) break;
-        double rel = 0.0, rn = 0.0, bn = 0.0;
-        if ((rc = true_residual<6>(ctx, W, 64, nullptr, dptr<double>(load), &rel, dptr<double>(W.rres), &rn, &bn)))
-            break;
-        double est = 0.0;
-        int grc = gmres_solve<double, double, 6>(ctx, W, K, dptr<double>(du), dptr<double>(load), rtol * bn, maxCycles, m,
-                                                 &iters, &cycles, &est);
-        if (grc == ASTRO_ERR_NAN) {
-            rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the Newmark step solve");
-            break;
+        if (o->method != ASTRO_SOLVER_GMRES_JACOBI_FP64) {
+            // the mixed or learned static solver on K_eff (its workspace, FP16 operator and
+            // eigenvalue estimate are reused across the steps), warm-started from the last increment
+            astro_solve_opts so{};
+            so.method = o->method;
+            so.restart = m;
+            so.max_iters = o->max_iters > 0 ? o->max_iters : 200000;
+            so.rtol = rtol;
+            so.inner_rtol = 1e-4;
+            so.precond = o->precond;
+            astro_solve_stats s2{};
+            const int grc = krylov_solve_static(ctx, dptr<double>(load), dptr<double>(du), &so, &s2);
+            iters += s2.iterations;
+            cycles += s2.restarts;
+            refs += s2.refinements;
+            if (grc == ASTRO_ERR_NAN) {
+                rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the Newmark step solve");
+                break;
+            }
+            if (grc != ASTRO_OK && grc != ASTRO_ERR_MAXIT) {
+                rc = grc;
+                break;
+            }
+            if (grc != ASTRO_OK) worst = grc;
+            worstRel = std::max(worstRel, s2.rel_residual);
+        } else {
+            double rel = 0.0, rn = 0.0, bn = 0.0;
+            if ((rc = true_residual<6>(ctx, W, 64, nullptr, dptr<double>(load), &rel, dptr<double>(W.rres), &rn, &bn)))
+                break;
+            double est = 0.0;
+            int grc = gmres_solve<double, double, 6>(ctx, W, K, dptr<double>(du), dptr<double>(load), rtol * bn, maxCycles,
+                                                     m, &iters, &cycles, &est);
+            if (grc == ASTRO_ERR_NAN) {
+                rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the Newmark step solve");
+                break;
+            }
+            if (grc != ASTRO_OK) worst = grc;
+            if (bn > 0.0) worstRel = std::max(worstRel, est / bn);
         }
-        if (grc != ASTRO_OK) worst = grc;
-        if (bn > 0.0) worstRel = std::max(worstRel, est / bn);
         if (ni && (rc = shell4_update_internal_soln(ctx, dptr<double>(du), d_iu, dptr<double>(iload)))) break;
         k_axpy<<<grid, 256, 0, s>>>(n, 1.0, dptr<double>(du), d_u);
         k_newmark_update<<<grid, 256, 0, s>>>(n, c1, c2, dt, beta, gamma, d_u, d_up, d_vp, d_ap);
@@ -1568,7 +1626,7 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
     if (st) {
         st->iterations = iters;
         st->restarts = cycles;
-        st->refinements = 0;
+        st->refinements = refs;
         st->status = rc ? rc : worst;
         st->rel_residual = worstRel;
         st->seconds = ms * 1e-3;
