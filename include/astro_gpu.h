@@ -361,6 +361,22 @@ int astro_precond_loss_grad(astro_ctx *ctx, const astro_precond *p, const double
 int astro_precond_train(astro_ctx *ctx, astro_precond *p, const double *samples, int32_t num_samples, int32_t iters,
                         double *loss_history);
 
+/* stepSolve, elastic static branch (Working/AStrO_commandFunctions.f90:681-749): from node_disp
+ * (el_mat_dim, global DOF numbering, in/out) and internal_disp (int_vec_size, in/out, may be NULL),
+ * iterate while fewer than 1 (nl_geom = 0) or 20 (nl_geom = 1) iterations have run and
+ * max|delDisp| > 1e-12 (the reference's single-precision literal): residual at the state (the
+ * tangent too when nl_geom = 1; the constraint penalty keeps the scaling of the last
+ * astro_scale_mpc), plus applied_load (getElasticAppliedLoad(time), el_mat_dim, may be NULL) and
+ * the constraint load, condensation, the solve of opts->solve warm-started from the previous
+ * increment, internal-DOF recovery, u += delDisp.  Needs astro_el_soln_load(build_mat = 1) and
+ * astro_scale_mpc first.  *iterations (may be NULL) receives the Newton iterations run. */
+typedef struct astro_step_opts {
+    int32_t nl_geom;            /* nLGeom */
+    astro_solve_opts solve;     /* the step's linear solves */
+} astro_step_opts;
+int astro_step_solve(astro_ctx *ctx, const astro_step_opts *o, const double *applied_load, double *node_disp,
+                     double *internal_disp, int32_t *iterations, astro_solve_stats *stats);
+
 /* getTotaldLdD for a static analysis (Working/AStrO_commandFunctions.f90:1377-1410) with the elastic
  * branch of solveDynamicAdjoint (:917-966; dLdv = dLda = 0): the adjoint K lambda = dLdu after
  * updateExternalRHS with int_dldu, the internal lambda by updateInternalSoln, then for every design

@@ -65,6 +65,10 @@ class SolveOptsC(C.Structure):
                 ("inner_rtol", C.c_double), ("precond", C.POINTER(PrecondC))]
 
 
+class StepOptsC(C.Structure):
+    _fields_ = [("nl_geom", C.c_int32), ("solve", SolveOptsC)]
+
+
 class TransientAdjointC(C.Structure):
     _fields_ = [("num_steps", C.c_int32), ("del_t", C.c_double), ("nm_beta", C.c_double), ("nm_gamma", C.c_double),
                 ("h", C.c_double), ("disp", F64P), ("vel", F64P), ("acc", F64P), ("int_disp", F64P),
@@ -136,6 +140,7 @@ def load_library():
                                   C.c_int),
         "astro_read_step_file": ([C.c_char_p, C.c_int32, C.c_int32, C.c_int32, F64P, F64P, F64P, F64P, F64P, F64P],
                                  C.c_int),
+        "astro_step_solve": ([vp, C.POINTER(StepOptsC), F64P, F64P, F64P, I32P, C.POINTER(SolveStatsC)], C.c_int),
         "astro_total_dldd": ([vp, vp, C.c_double, F64P, F64P, F64P, C.POINTER(SolveOptsC), F64P, F64P, F64P,
                               C.POINTER(SolveStatsC)], C.c_int),
     }
@@ -398,6 +403,20 @@ class AstroGPU:
         self._check(self.L.astro_drdd_complex(self.h, dvar, h, C.byref(state) if state is not None else None,
                                               _d(out), _d(iout)))
         return out, iout[:self.int_vec_size]
+
+    def stepSolve(self, applied_load, node_disp=None, internal_disp=None, nl_geom=0, method=SOLVER_GMRES_JACOBI_FP64,
+                  rtol=1e-12, restart=50, max_iters=200000, precond=None):
+        """stepSolve on the device (needs getElasticSolnLoad(1) and scaleElasticMPC first):
+        (node_disp, internal_disp, Newton iterations, stats)."""
+        u = np.zeros(self.n) if node_disp is None else _f64(node_disp).copy()
+        iu = np.zeros(max(self.int_vec_size, 1)) if internal_disp is None else _f64(internal_disp).copy()
+        o = StepOptsC(nl_geom, SolveOptsC(method, restart, max_iters, rtol, 1e-4,
+                                          C.pointer(precond) if precond is not None else C.POINTER(PrecondC)()))
+        its = np.zeros(1, np.int32)
+        st = SolveStatsC()
+        self._check(self.L.astro_step_solve(self.h, C.byref(o), None if applied_load is None else _d(_f64(applied_load)),
+                                            _d(u), _d(iu), _i(its), C.byref(st)))
+        return u, iu[:self.int_vec_size], int(its[0]), st
 
     def getTotaldLdD(self, dldu, int_dldu=None, dldd_explicit=None, state=None, h=1e-14,
                      method=SOLVER_GMRES_JACOBI_FP64, rtol=1e-12, restart=50, max_iters=200000, precond=None):

@@ -1106,3 +1106,126 @@ extern "C" int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double
     CK(cudaStreamSynchronize(ctx->stream));
     return ASTRO_OK;
 }
+
+// Per-CTA maxima of |x| (256 threads per CTA); the host takes the maximum.
+__global__ void k_absmax_part(const double *__restrict__ x, int n, double *part) {
+    __shared__ double sp[8];
+    double m = 0.0;
+    for (int i = blockIdx.x * 256 + threadIdx.x; i < n; i += gridDim.x * 256) m = fmax(m, fabs(x[i]));
+    for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) sp[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int q = 0; q < 8; ++q) t = fmax(t, sp[q]);
+        part[blockIdx.x] = t;
+    }
+}
+
+__global__ void k_axpy_d(int n, double a, const double *__restrict__ x, double *__restrict__ y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += a * x[i];
+}
+
+// stepSolve, elastic static branch (Working/AStrO_commandFunctions.f90:681-749): up to 1 (linear
+// geometry) or 20 (nonlinear) iterations, while max|delDisp| > 1e-12 (a single-precision literal in
+// the reference): residual at the current state (and, for nonlinear geometry, the tangent; the
+// constraint penalty keeps the scaling it had, as scaleElasticMPC is not repeated), plus the
+// applied load and the constraint load, condensation, the solve warm-started from the previous
+// increment, internal-DOF recovery, u += delDisp.  The state stays on the device for all
+// iterations.
+extern "C" int astro_step_solve(astro_ctx *ctx, const astro_step_opts *o, const double *applied_load, double *node_disp,
+                                double *internal_disp, int32_t *iterations, astro_solve_stats *stats) {
+    if (!ctx || !o || !node_disp) return ASTRO_ERR_ARG;
+    if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "needs the stiffness of astro_el_soln_load(build_mat = 1)");
+    if (ctx->P.mpcDim > 0 && !ctx->penRows && !ctx->mpcScaled)
+        return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run before the step");
+    const AstroPrep &P = ctx->P;
+    const int n = P.n, ni = P.intVecSize;
+    const bool hasInt = ctx->hasShell && ni > 0;
+    if (hasInt && !ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load");
+    const int maxNLIt = o->nl_geom ? 20 : 1;
+    const double tol = (double)1e-12f;
+    struct Tmp {
+        DevBuf u, iu, f, load, iload, du, part, ref;
+        ~Tmp() {
+            DevBuf *v[] = {&u, &iu, &f, &load, &iload, &du, &part, &ref};
+            for (DevBuf *p : v) dev_free(*p);
+        }
+    } T;
+    int rc;
+    if ((rc = state_vec_up(ctx, node_disp, T.u, false))) return rc;
+    if (applied_load && (rc = state_vec_up(ctx, applied_load, T.f, false))) return rc;
+    if ((rc = dev_alloc(ctx, T.load, sizeof(double) * n)) || (rc = dev_alloc(ctx, T.du, sizeof(double) * n)) ||
+        (rc = dev_alloc(ctx, T.part, sizeof(double) * 152)))
+        return rc;
+    CK(cudaMemsetAsync(T.du.p, 0, sizeof(double) * n, ctx->stream));
+    if (hasInt) {
+        if ((rc = dev_alloc(ctx, T.iload, sizeof(double) * ni))) return rc;
+        if (internal_disp) {
+            if ((rc = upload(ctx, T.iu, internal_disp, sizeof(double) * ni))) return rc;
+        } else {
+            if ((rc = dev_alloc(ctx, T.iu, sizeof(double) * ni))) return rc;
+            CK(cudaMemsetAsync(T.iu.p, 0, sizeof(double) * ni, ctx->stream));
+        }
+    }
+    astro_solve_stats acc{};
+    double delUNorm = 1.0;
+    int it = 0;
+    const unsigned g = (n + 255) / 256;
+    while (it < maxNLIt && delUNorm > tol) {
+        CK(cudaMemsetAsync(T.load.p, 0, sizeof(double) * n, ctx->stream));
+        if (hasInt) CK(cudaMemsetAsync(T.iload.p, 0, sizeof(double) * ni, ctx->stream));
+        const int build = o->nl_geom ? 1 : 0;
+        if (build) {
+            if ((rc = ensure_K(ctx, 2))) return rc;
+            if ((rc = bsr_zero(ctx, 2))) return rc;
+        }
+        if (ctx->hasSolid) {
+            rc = hex8_soln_load(ctx, build, dptr<double>(T.u), dptr<double>(T.load));
+        } else {
+            ShellDevState ds;
+            ds.disp = dptr<double>(T.u);
+            ds.idisp = hasInt ? dptr<double>(T.iu) : nullptr;
+            rc = launch_shell4_assemble(ctx, ds, dptr<double>(T.load), hasInt ? dptr<double>(T.iload) : nullptr, build,
+                                        nullptr, nullptr);
+        }
+        if (rc) return rc;
+        if (build) {
+            ctx->k64Version++;
+            ctx->haveIntMat = ctx->hasShell;
+        }
+        if (T.f.p) k_axpy_d<<<g, 256, 0, ctx->stream>>>(n, 1.0, dptr<double>(T.f), dptr<double>(T.load));
+        if ((rc = constraint_load_dev(ctx, dptr<double>(T.u), dptr<double>(T.load)))) return rc;
+        if (hasInt && (rc = shell4_update_external_rhs(ctx, dptr<double>(T.iload), dptr<double>(T.load)))) return rc;
+        astro_solve_stats s{};
+        rc = krylov_solve_static(ctx, dptr<double>(T.load), dptr<double>(T.du), &o->solve, &s);
+        acc.iterations += s.iterations;
+        acc.restarts += s.restarts;
+        acc.refinements += s.refinements;
+        acc.seconds += s.seconds;
+        acc.rel_residual = std::max(acc.rel_residual, s.rel_residual);
+        acc.conditional_graph = s.conditional_graph;
+        acc.fallback |= s.fallback;
+        if (rc && rc != ASTRO_ERR_MAXIT) return rc;
+        if (rc == ASTRO_ERR_MAXIT) acc.status = rc;
+        if (hasInt && (rc = shell4_update_internal_soln(ctx, dptr<double>(T.du), dptr<double>(T.iu), dptr<double>(T.iload))))
+            return rc;
+        k_axpy_d<<<g, 256, 0, ctx->stream>>>(n, 1.0, dptr<double>(T.du), dptr<double>(T.u));
+        k_absmax_part<<<152, 256, 0, ctx->stream>>>(dptr<double>(T.du), n, dptr<double>(T.part));
+        double hp[152];
+        CK(cudaMemcpyAsync(hp, T.part.p, sizeof(hp), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        delUNorm = 0.0;
+        for (double v : hp) delUNorm = std::max(delUNorm, v);
+        ++it;
+    }
+    if (iterations) *iterations = it;
+    if ((rc = dev_alloc(ctx, T.ref, sizeof(double) * n))) return rc;
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(T.u), dptr<double>(T.ref), n))) return rc;
+    CK(cudaMemcpyAsync(node_disp, T.ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    if (hasInt && internal_disp) CK(cudaMemcpyAsync(internal_disp, T.iu.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (stats) *stats = acc;
+    return acc.status ? acc.status : ASTRO_OK;
+}
