@@ -116,6 +116,7 @@ def load_library():
         "astro_scale_mpc": ([vp, F64P, F64P], C.c_int),
         "astro_constraint_load": ([vp, F64P, F64P], C.c_int),
         "astro_surface_load": ([vp, C.c_int32, I32P, I32P, F64P, C.c_double, F64P], C.c_int),
+        "astro_body_load": ([vp, C.c_int32, F64P, I32P, C.c_int32, C.c_void_p, F64P], C.c_int),
         "astro_convert_to_ltri": ([vp, F64P], C.c_int),
         "astro_ldl_fact": ([vp, F64P, C.c_int32, I32P, C.c_int32], C.c_int),
         "astro_ldl_fact_resident": ([vp], C.c_int),
@@ -307,6 +308,19 @@ class AstroGPU:
         fe, fn = _i32(face_el), _i32(face_num)
         tr = _f64(traction)
         self._check(self.L.astro_surface_load(self.h, len(fe), _i(fe), _i(fn), _d(tr), float(pressure), _d(load)))
+        return load
+
+    def body_load(self, kind, vals, elements=None, state=None, elastic_load=None):
+        """getElasticAppliedLoad body-force branch: kind 0 bodyForce, 1 gravitational, 2 centrifugal
+        (vals = axis point, axis direction, angular velocity) over the listed 1-based elements
+        (None = every element), added into elastic_load."""
+        load = np.zeros(self.n) if elastic_load is None else elastic_load
+        v = np.zeros(7)
+        v[:len(vals)] = vals
+        els = None if elements is None else _i32(elements)
+        self._check(self.L.astro_body_load(self.h, int(kind), _d(v), None if els is None else _i(els),
+                                           0 if els is None else len(els),
+                                           C.byref(state) if state is not None else None, _d(load)))
         return load
 
     def applied_load(self, load=None):

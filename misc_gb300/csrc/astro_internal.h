@@ -78,6 +78,7 @@ struct astro_ctx {
     std::vector<int> elist;     // (E,8)
     std::vector<int> etype, esec;
     std::vector<double> elMat;  // per element materialElastic(9) (solids)
+    std::vector<double> elDensity;  // per element materialDensity (solids)
     std::vector<double> secABD, secMass;  // per section ABD(9,9), sMass(6,6) (shells)
     std::vector<double> secOrient;        // per section 3x3 column-major
     std::vector<double> elThickness;      // per element total shell thickness (complex step / loads)
@@ -156,6 +157,7 @@ struct ShellDevState {
     const double *idisp = nullptr, *pidisp = nullptr;
     int dynamic = 0;
     double beta = 0.25, gamma = 0.5, delT = 0.0;
+    int massOnly = 0;  // residual = the Newmark mass term alone (needs dynamic, no matrix)
 };
 int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &s, double *d_loadInt, double *d_intLoad,
                            int buildMat, double *d_ke, double *d_ru, bool sync = true);  // elem_shell4.cu

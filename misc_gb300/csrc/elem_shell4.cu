@@ -115,6 +115,7 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
     A.pacc = st.pacc;
     A.idisp = st.idisp;
     A.dynamic = st.dynamic;
+    A.massOnly = st.massOnly;
     A.beta = st.beta;
     A.gamma = st.gamma;
     A.delT = st.delT;

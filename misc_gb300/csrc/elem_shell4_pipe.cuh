@@ -45,6 +45,7 @@ struct ShellPipe {
     int dynamic;
     double beta, gamma, delT;
     int buildMat, quirk;
+    int massOnly;    // residual = the Newmark mass term alone (the gravitational load)
     double gpc;      // Gauss point coordinate: r_1rt3, or the complex path's single-precision c_1rt3
     ShellFrame *fr;
     ShellGP *gp;     // count*4
@@ -346,7 +347,7 @@ __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
         const double wd = G.wdet;
         bool stressed = false;
         for (int a = 0; a < 9; ++a) {
-            ru += G.F[a] * (wd * dj[a]);
+            if (!A.massOnly) ru += G.F[a] * (wd * dj[a]);
             if (G.F[a] != 0.0) stressed = true;
         }
         if (!A.buildMat) continue;

@@ -1,0 +1,207 @@
+// Body, gravitational and centrifugal loads: the body-force branch of getElasticAppliedLoad
+// (Working/AStrO_commandFunctions.f90:393-441) with r_getElBodyForce
+// (Working/AStrO_r_elementEqns.f90:1801-1869) and r_getElCentAcc (:1871-1921).
+//   bricks: one thread per listed element, launched colour by colour (no two elements of a colour
+//           share a node, so the additions need no atomics and have a fixed order); the nodal
+//           forces are b or rho a (the brick's consistent mass times a uniform acceleration)
+//           times the integral of N over the element;
+//   shells: the gravitational load is the element mass residual for a uniform acceleration
+//           (r_getElRum with the static frame of the element's mean rotation), which the shell
+//           pipeline evaluates as the Newmark mass term: run alone (massOnly) with a
+//           previous-acceleration field that makes the Newmark acceleration the imposed one.
+#include <cmath>
+#include <vector>
+
+#include "astro_internal.h"
+
+namespace {
+
+struct BodyVals {
+    double v[7];
+};
+
+// one listed brick element of a colour per thread
+__global__ void k_hex_body(int kind, BodyVals bv, const int *__restrict__ els, int cnt, const double *__restrict__ nodes,
+                           const int *__restrict__ elist, const int *__restrict__ rank, const double *__restrict__ disp,
+                           const double *__restrict__ den, const double *__restrict__ mult,
+                           double *__restrict__ load) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt) return;
+    const int e = els[i];
+    double X[8][3];
+    int r[8];
+    for (int k = 0; k < 8; ++k) {
+        const int nd = elist[8 * (size_t)e + k] - 1;
+        r[k] = rank[nd] - 1;
+        for (int d = 0; d < 3; ++d) X[k][d] = nodes[3 * (size_t)nd + d];
+    }
+    double a[3];
+    if (kind == 2) {
+        // r_getElCentAcc: omega^2 times the centroid's distance vector from the axis
+        double c[3] = {0.0, 0.0, 0.0};
+        for (int k = 0; k < 8; ++k)
+            for (int d = 0; d < 3; ++d) c[d] = c[d] + X[k][d] + (disp ? disp[3 * (size_t)r[k] + d] : 0.0);
+        const double nnInv = 1.0 / 8.0;
+        double pos[3], unit[3];
+        for (int d = 0; d < 3; ++d) pos[d] = nnInv * c[d] - bv.v[d];
+        double dp = bv.v[3] * bv.v[3] + bv.v[4] * bv.v[4] + bv.v[5] * bv.v[5];
+        const double mag = sqrt(dp);
+        for (int d = 0; d < 3; ++d) unit[d] = (1.0 / mag) * bv.v[3 + d];
+        dp = pos[0] * unit[0] + pos[1] * unit[1] + pos[2] * unit[2];
+        for (int d = 0; d < 3; ++d) a[d] = bv.v[6] * bv.v[6] * (pos[d] - dp * unit[d]);
+    } else {
+        for (int d = 0; d < 3; ++d) a[d] = bv.v[d];
+    }
+    const double f = ((kind >= 1) ? den[e] : 1.0) * mult[i];
+    // integral of N_k over the element, 2 x 2 x 2 Gauss points at +-1/sqrt(3)
+    const double g = 1.0 / sqrt(3.0);
+    const double sx[8] = {-1, 1, 1, -1, -1, 1, 1, -1}, sy[8] = {-1, -1, 1, 1, -1, -1, 1, 1},
+                 sz[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
+    double w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int gp = 0; gp < 8; ++gp) {
+        const double s1 = g * sx[gp], s2 = g * sy[gp], s3 = g * sz[gp];
+        double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, N[8];
+        for (int k = 0; k < 8; ++k) {
+            const double a1 = 1.0 + sx[k] * s1, a2 = 1.0 + sy[k] * s2, a3 = 1.0 + sz[k] * s3;
+            N[k] = 0.125 * a1 * a2 * a3;
+            const double d1 = 0.125 * sx[k] * a2 * a3, d2 = 0.125 * sy[k] * a1 * a3, d3 = 0.125 * sz[k] * a1 * a2;
+            for (int d = 0; d < 3; ++d) {
+                J[d][0] += X[k][d] * d1;
+                J[d][1] += X[k][d] * d2;
+                J[d][2] += X[k][d] * d3;
+            }
+        }
+        const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                           J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        for (int k = 0; k < 8; ++k) w[k] += N[k] * det;
+    }
+    for (int k = 0; k < 8; ++k)
+        for (int d = 0; d < 3; ++d) load[3 * (size_t)r[k] + d] += f * a[d] * w[k];
+}
+
+// out -= b (the pipeline's output is the load -Ru)
+__global__ void k_sub(int n, const double *__restrict__ b, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] -= b[i];
+}
+
+}  // namespace
+
+extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals, const int32_t *elements, int32_t count,
+                               const astro_state *state, double *elastic_load) {
+    if (!ctx || !vals || !elastic_load || kind < 0 || kind > 2 || count < 0) return ASTRO_ERR_ARG;
+    const AstroPrep &P = ctx->P;
+    const int n = P.n;
+    if (ctx->hasShell && ctx->hasSolid) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "body loads on mixed meshes");
+    if (elements)
+        for (int k = 0; k < count; ++k)
+            if (elements[k] < 1 || elements[k] > P.E) return set_err(ctx, ASTRO_ERR_ARG, "element number out of range");
+    if (elements && count == 0) return ASTRO_OK;
+    bool wholeMesh = true;
+    if (elements) {
+        std::vector<int> seen((size_t)P.E, 0);
+        for (int k = 0; k < count; ++k) ++seen[elements[k] - 1];
+        for (int e = 0; e < P.E && wholeMesh; ++e) wholeMesh = seen[e] == 1;
+    }
+    if (ctx->hasShell && (kind != 1 || !wholeMesh))
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED,
+                       "shell body loads: the gravitational load over the whole mesh (body-force and centrifugal "
+                       "loads of shells are not implemented)");
+    struct Tmp {
+        DevBuf ref, li, u, b, list, mult, den, pa, iu;
+        ~Tmp() {
+            DevBuf *v[] = {&ref, &li, &u, &b, &list, &mult, &den, &pa, &iu};
+            for (DevBuf *p : v) dev_free(*p);
+        }
+    } T;
+    int rc;
+    if ((rc = dev_alloc(ctx, T.ref, sizeof(double) * n)) || (rc = dev_alloc(ctx, T.li, sizeof(double) * n))) return rc;
+    CK(cudaMemcpyAsync(T.ref.p, elastic_load, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = ref_to_int_vec(ctx, dptr<double>(T.ref), dptr<double>(T.li), n))) return rc;
+    if (state && state->node_disp) {
+        DevBuf h;
+        rc = upload(ctx, h, state->node_disp, sizeof(double) * n);
+        if (!rc) rc = dev_alloc(ctx, T.u, sizeof(double) * n);
+        if (!rc) rc = ref_to_int_vec(ctx, dptr<double>(h), dptr<double>(T.u), n);
+        if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "state upload");
+        dev_free(h);
+        if (rc) return rc;
+    }
+    if (ctx->hasSolid) {
+        // the listed elements, colour by colour
+        // (an element listed twice adds its load twice)
+        std::vector<int> on((size_t)P.E, elements ? 0 : 1);
+        if (elements)
+            for (int k = 0; k < count; ++k) ++on[elements[k] - 1];
+        std::vector<int> list, ptr(1, 0);
+        std::vector<double> mult;
+        for (int col = 0; col < P.ncolors; ++col) {
+            for (int k = P.colorPtr[col]; k < P.colorPtr[col + 1]; ++k)
+                if (on[P.colorEls[k]]) {
+                    list.push_back(P.colorEls[k]);
+                    mult.push_back((double)on[P.colorEls[k]]);
+                }
+            ptr.push_back((int)list.size());
+        }
+        if (!list.empty()) {
+            if ((rc = upload(ctx, T.list, list.data(), sizeof(int) * list.size())) ||
+                (rc = upload(ctx, T.mult, mult.data(), sizeof(double) * mult.size())) ||
+                (rc = upload(ctx, T.den, ctx->elDensity.data(), sizeof(double) * ctx->elDensity.size())))
+                return rc;
+            BodyVals bv;
+            for (int k = 0; k < 7; ++k) bv.v[k] = (kind == 2 || k < 6) ? vals[k] : 0.0;
+            for (int col = 0; col < P.ncolors; ++col) {
+                const int cnt = ptr[col + 1] - ptr[col];
+                if (!cnt) continue;
+                k_hex_body<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
+                    kind, bv, dptr<int>(T.list) + ptr[col], cnt, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist),
+                    dptr<int>(ctx->d_rank), T.u.p ? dptr<double>(T.u) : nullptr, dptr<double>(T.den),
+                    dptr<double>(T.mult) + ptr[col], dptr<double>(T.li));
+            }
+            if ((rc = cuda_check(ctx, cudaGetLastError(), "body load"))) return rc;
+        }
+    } else {
+        // shells, gravitational: load += Rum, the Newmark mass residual alone (the elastic part is
+        // left out, not subtracted: at a displaced state it is orders of magnitude larger)
+        if (!T.u.p) {
+            if ((rc = dev_alloc(ctx, T.u, sizeof(double) * n))) return rc;
+            CK(cudaMemsetAsync(T.u.p, 0, sizeof(double) * n, ctx->stream));
+        }
+        const int ni = P.intVecSize;
+        if (ni > 0) {
+            if (state && state->internal_disp) {
+                if ((rc = upload(ctx, T.iu, state->internal_disp, sizeof(double) * ni))) return rc;
+            } else {
+                if ((rc = dev_alloc(ctx, T.iu, sizeof(double) * ni))) return rc;
+                CK(cudaMemsetAsync(T.iu.p, 0, sizeof(double) * ni, ctx->stream));
+            }
+        }
+        // previous acceleration -a at every node: with u = u_prev, v_prev = 0 and beta = 1/4 the
+        // Newmark acceleration is a
+        std::vector<double> pa((size_t)n);
+        for (int r = 0; r < P.N; ++r)
+            for (int c = 0; c < P.dpn; ++c) pa[(size_t)r * P.dpn + c] = -vals[c];
+        if ((rc = upload(ctx, T.pa, pa.data(), sizeof(double) * n))) return rc;
+        if ((rc = dev_alloc(ctx, T.b, sizeof(double) * n))) return rc;
+        CK(cudaMemsetAsync(T.b.p, 0, sizeof(double) * n, ctx->stream));
+        ShellDevState s1;
+        s1.disp = dptr<double>(T.u);
+        s1.idisp = ni > 0 ? dptr<double>(T.iu) : nullptr;
+        s1.pdisp = s1.disp;
+        s1.pacc = dptr<double>(T.pa);
+        s1.pidisp = s1.idisp;
+        s1.dynamic = 1;
+        s1.beta = 0.25;
+        s1.gamma = 0.5;
+        s1.delT = 1.0;
+        s1.massOnly = 1;
+        if ((rc = launch_shell4_assemble(ctx, s1, dptr<double>(T.b), nullptr, 0, nullptr, nullptr))) return rc;
+        k_sub<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, dptr<double>(T.b), dptr<double>(T.li));
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "shell gravity load"))) return rc;
+    }
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(T.li), dptr<double>(T.ref), n))) return rc;
+    CK(cudaMemcpyAsync(elastic_load, T.ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}

@@ -342,7 +342,7 @@ def correlated_log_normal(nx, ny, nz, h, corr_len, sigma, E_med=2.0e11, seed=0):
     ky = 2 * np.pi * np.fft.fftfreq(ny, d=h[1])
     kx = 2 * np.pi * np.fft.rfftfreq(nx, d=h[0])
     k2 = kz[:, None, None] ** 2 + ky[None, :, None] ** 2 + kx[None, None, :] ** 2
-    z = np.fft.irfftn(np.fft.rfftn(w) * np.exp(-0.5 * k2 * corr_len ** 2), s=(nz, ny, nx))
+    z = np.fft.irfftn(np.fft.rfftn(w) * np.exp(-0.5 * k2 * corr_len ** 2), s=(nz, ny, nx), axes=(0, 1, 2))
     z = (z - z.mean()) / max(z.std(), 1e-300)
     return E_med * np.exp(sigma * z)
 

@@ -60,6 +60,8 @@ def _lib():
         L.orc_update_external_rhs.argtypes = [C.c_void_p, F64P, F64P, F64P]
         L.orc_update_internal_soln.argtypes = [C.c_void_p, F64P, F64P, F64P, F64P]
         L.orc_surface_load.argtypes = [C.c_void_p, C.c_int, I32P, I32P, F64P, C.c_double, F64P]
+        L.orc_body_load.restype = C.c_int
+        L.orc_body_load.argtypes = [C.c_void_p, C.c_int, F64P, C.c_int, I32P, C.c_void_p, F64P]
         _LIB = L
     return _LIB
 
@@ -181,6 +183,18 @@ class Oracle:
     def constraint_load(self, mpc_mat, mpc_rhs, node_disp, elastic_load):
         self.L.orc_constraint_load(_d(mpc_mat), _i(self.mpc_cols), _i(self.mpc_range), _d(mpc_rhs), self.mpc_dim,
                                    _d(node_disp), _d(elastic_load))
+
+    def body_load(self, kind, vals, elements=None, state=None, load=None):
+        """getElasticAppliedLoad body-force branch: kind 0 bodyForce, 1 gravitational,
+        2 centrifugal (vals = center, axis, angVel) over the listed elements (1-based; None = all)."""
+        load = np.zeros(self.n) if load is None else load
+        els = None if elements is None else np.ascontiguousarray(elements, np.int32)
+        v = np.zeros(7)
+        v[:len(vals)] = vals
+        rc = self.L.orc_body_load(self.h, kind, _d(v), 0 if els is None else len(els), None if els is None else _i(els),
+                                  C.byref(state) if state is not None else None, _d(load))
+        assert rc == 0
+        return load
 
     def applied_load(self, load=None):
         """Consistent surface load of the model's faces plus its point loads."""

@@ -854,6 +854,99 @@ void orc_update_internal_soln(const OracleCtx *c, const double *extSoln, double 
 // faces from r_getElementFaces :288-332): Q8 resolved -- true face area (|dx/ds x dx/dt|), face
 // shape function k applied to the face's k-th element node, contributions accumulated over faces.
 // t = traction - pressure * n, with n the face normal of r_getElSurfaceNormal.
+// getElasticAppliedLoad, body-force branch (Working/AStrO_commandFunctions.f90:393-441): for the
+// listed elements (1-based; every element when nels = 0) r_getElBodyForce
+// (Working/AStrO_r_elementEqns.f90:1801-1869) scattered into elasticLoad.  kind 0 'bodyForce'
+// (vals = force per volume, 6 components), 1 'gravitational' (vals = acceleration, 6 components),
+// 2 'centrifugal' (vals = center(3), axis(3), angVel; r_getElCentAcc, :1871-1921).
+int orc_body_load(const OracleCtx *c, int kind, const double *vals, int nels, const int32_t *els, const astro_state *s,
+                  double *elasticLoad) {
+    const astro_model *m = c->m;
+    GState g = to_gstate(s);
+    DPert<double> p;
+    const int count = nels > 0 ? nels : c->numEls;
+    for (int k = 0; k < count; ++k) {
+        const int el = nels > 0 ? els[k] : k + 1;
+        ElemData<double> e;
+        if (t_getElementData(e, m, c->nDofIndex.data(), c->intVecRange.data(), el, g, p) != 0) return 1;
+        double bdy[6];
+        if (kind == 2) {
+            double cent[3] = {0.0, 0.0, 0.0};
+            for (int i1 = 1; i1 <= e.numNds; ++i1)
+                for (int i2 = 1; i2 <= 3; ++i2) cent[i2 - 1] = cent[i2 - 1] + e.globNds(i2, i1) + e.disp(i2, i1);
+            double nnInv = (double)e.numNds;
+            nnInv = 1.0 / nnInv;
+            for (int i2 = 0; i2 < 3; ++i2) cent[i2] = nnInv * cent[i2];
+            double pos[3], unit[3];
+            for (int i2 = 0; i2 < 3; ++i2) pos[i2] = cent[i2] - vals[i2];
+            double dp = vals[3] * vals[3] + vals[4] * vals[4] + vals[5] * vals[5];
+            const double mag = std::sqrt(dp);
+            for (int i2 = 0; i2 < 3; ++i2) unit[i2] = (1.0 / mag) * vals[3 + i2];
+            dp = pos[0] * unit[0] + pos[1] * unit[1] + pos[2] * unit[2];
+            for (int i2 = 0; i2 < 3; ++i2) pos[i2] = pos[i2] - dp * unit[i2];
+            for (int i2 = 0; i2 < 3; ++i2) bdy[i2] = vals[6] * vals[6] * pos[i2];
+            bdy[3] = bdy[4] = bdy[5] = 0.0;
+        } else {
+            for (int i2 = 0; i2 < 6; ++i2) bdy[i2] = vals[i2];
+        }
+        A1<double, 33> ndFrc;
+        ndFrc.fill(0.0);
+        if (kind >= 1) {
+            // isGrav: the element's mass residual for the acceleration bdy at every node, with the
+            // static orientation of the element's mean rotation
+            A1<double, 3> statRot;
+            statRot.fill(0.0);
+            for (int i4 = 1; i4 <= e.numNds; ++i4)
+                for (int q = 1; q <= 3; ++q) statRot(q) = statRot(q) + e.disp(3 + q, i4);
+            double nnInv = (double)e.numNds;
+            nnInv = 1.0 / nnInv;
+            for (int q = 1; q <= 3; ++q) statRot(q) = nnInv * statRot(q);
+            A2<double, 3, 48> statInOri;
+            A2<double, 3, 16> statdrIdrG;
+            t_getInstOrient(statInOri, statdrIdrG, e.orient, statRot);
+            for (int cc = 4; cc <= 48; ++cc)
+                for (int r = 1; r <= 3; ++r) statInOri(r, cc) = 0.0;
+            for (int cc = 4; cc <= 16; ++cc)
+                for (int r = 1; r <= 3; ++r) statdrIdrG(r, cc) = 0.0;
+            A2<double, 6, 11> fakeAcc;
+            fakeAcc.fill(0.0);
+            for (int i1 = 1; i1 <= e.numNds; ++i1)
+                for (int r = 1; r <= 6; ++r) fakeAcc(r, i1) = bdy[r - 1];
+            A2<double, 33, 33> dRdA;
+            t_getElRum(ndFrc, dRdA, 0, e, statInOri, statdrIdrG, statRot, e.disp, fakeAcc);
+        } else {
+            for (int i1 = 1; i1 <= e.numIntPts; ++i1) {
+                A1<double, 11> Nvec;
+                A2<double, 11, 3> Nx;
+                double detJ;
+                t_getIntPtData(Nvec, Nx, detJ, e.locNds, e.intPts[i1 - 1], e.eType, e.numNds);
+                const int i3 = e.numNds * e.dofPerNd;
+                detJ = detJ * e.ipWt[i1 - 1];
+                for (int i2 = 1; i2 <= i3; ++i2) {
+                    const int i4 = e.dofTable[i2 - 1][0], i5 = e.dofTable[i2 - 1][1];
+                    ndFrc(i2) = ndFrc(i2) + bdy[i4 - 1] * Nvec(i5) * detJ;
+                }
+            }
+            if (e.eType == 41) {
+                // r_getElThickOffset: the section's total thickness
+                const int sec = m->element_section[el - 1];
+                double thick = 0.0;
+                for (int i1 = m->sec_layup_range[sec - 1] + 1, ln = 1; i1 <= m->sec_layup_range[sec]; ++i1, ++ln)
+                    thick = thick + layer_thickness(m, el, ln, i1, p);
+                for (int q = 1; q <= 33; ++q) ndFrc(q) = thick * ndFrc(q);
+            }
+        }
+        const int ndDof = e.numNds * e.dofPerNd;
+        for (int i4 = 1; i4 <= ndDof; ++i4) {
+            const int i5 = e.dofTable[i4 - 1][0];
+            const int i6 = m->element_list[8 * (el - 1) + e.dofTable[i4 - 1][1] - 1];
+            const int i7 = c->nDofIndex[6 * (i6 - 1) + i5 - 1];
+            elasticLoad[i7 - 1] += ndFrc(i4);
+        }
+    }
+    return 0;
+}
+
 void orc_surface_load(const OracleCtx *c, int nfaces, const int32_t *faceEl, const int32_t *faceNum,
                       const double *traction, double pressure, double *elasticLoad) {
     const astro_model *m = c->m;

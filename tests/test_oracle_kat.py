@@ -332,3 +332,28 @@ def test_static_adjoint_shell_matches_central_difference_with_consistent_tangent
             assert abs(g[k] - fd) <= 1e-5 * abs(fd), (k, g[k], fd)
     finally:
         o0.L.orc_set_quirk(1, 0)
+
+
+def test_body_load_totals():
+    """Body loads: the nodal forces add up to the resultant (the shape functions' partition of
+    unity): b V for a body force, rho V a for gravity, rho w^2 sum(V_e r_e) for the centrifugal
+    load about the z axis (r_e = element centroid's distance from the axis), rho t A a for the
+    shell's gravitational load."""
+    lx, ly, lz, rho = 1.5, 1.0, 0.75, 7800.0
+    m = M.hex_block(6, 4, 3, lx=lx, ly=ly, lz=lz, jitter=0.0, rho=rho)
+    o = Oracle(m)
+    V = lx * ly * lz
+    tot = lambda v: v.reshape(3, -1).sum(axis=1)
+    assert np.allclose(tot(o.body_load(0, [1.5, -2.0, 3.0])), np.array([1.5, -2.0, 3.0]) * V, rtol=1e-12)
+    assert np.allclose(tot(o.body_load(1, [0.0, 0.0, -9.81])), [0.0, 0.0, -9.81 * rho * V], rtol=1e-12, atol=1e-9)
+    w = 12.0
+    c = tot(o.body_load(2, [0.0, 0.0, 0.0, 0.0, 0.0, 2.0, w]))
+    assert np.allclose(c, [rho * w * w * V * lx / 2, rho * w * w * V * ly / 2, 0.0], rtol=1e-12, atol=1e-6)
+    # a subset: the elements of the first x layer only
+    els = [e + 1 for e in range(m.num_els) if e % 6 == 0]
+    assert np.allclose(tot(o.body_load(0, [0.0, 1.0, 0.0], elements=els)), [0.0, V / 6, 0.0], rtol=1e-12, atol=1e-12)
+    p = M.plate_shell(nx=5, ny=4, lx=2.0, ly=1.0, t=0.03, rho=2700.0)
+    op = Oracle(p)
+    s = op.body_load(1, [0.0, 0.0, -9.81, 0.0, 0.0, 0.0]).reshape(6, -1).sum(axis=1)
+    assert np.isclose(s[2], -9.81 * 2700.0 * 0.03 * 2.0, rtol=1e-12)
+    assert np.allclose(s[[0, 1, 3, 4, 5]], 0.0, atol=1e-9)
