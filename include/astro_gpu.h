@@ -275,6 +275,32 @@ int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el,
 int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals, const int32_t *elements, int32_t count,
                     const astro_state *state, double *elastic_load);
 
+/* ---- batched panels ----------------------------------------------------------------------- */
+
+/* A model made of many independent panels (the connected components of its mesh; constraints
+ * may not couple two of them), each solved with a direct LDL^T factorisation of K + C^T C as the
+ * reference solves one model with getSparseLDLFact / solveSparseLDLFact
+ * (Working/AStrO_solvers.f90:10-126), all panels in one persistent launch: a blocked band LDL^T
+ * in FP64 with one thread-block cluster per panel, panels ordered along their longest extent.
+ * The FP64 stiffness must be assembled (astro_el_soln_load) and the constraints scaled
+ * (astro_scale_mpc).  cluster_size: CTAs per panel (1, 2, 4 or 8; 0 = 8). */
+typedef struct astro_panels_info {
+    int32_t num_panels;
+    int32_t max_bandwidth;   /* largest lower bandwidth in DOF */
+    int64_t band_bytes;      /* device storage of the band factors */
+    int32_t cluster_size;
+    int32_t workers;         /* clusters of the factor launch */
+    double factor_seconds;   /* band fill + factorisation, wall clock */
+    double solve_seconds;    /* the last astro_panels_solve, wall clock with the copies */
+} astro_panels_info;
+int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *info);
+/* X = (K + C^T C)^-1 B for num_rhs right-hand sides: rhs and x are num_rhs x el_mat_dim (column
+ * k at rhs + k * el_mat_dim), global DOF numbering.  Needs a current astro_panels_factor. */
+int astro_panels_solve(astro_ctx *ctx, int32_t num_rhs, const double *rhs, double *x, astro_panels_info *info);
+/* Factor (when the stiffness or the constraints changed since the last factorisation) and solve. */
+int astro_panels_solve_batched(astro_ctx *ctx, int32_t num_rhs, const double *rhs, double *x,
+                               astro_panels_info *info);
+
 /* ---- linear solve ------------------------------------------------------------------------- */
 
 /* convertToLTri (Working/AStrO_bookKeeping.f90:754-792): row-skyline lTri = (K inside the

@@ -34,6 +34,12 @@ class AstroError(RuntimeError):
         self.code = code
 
 
+class PanelsInfoC(C.Structure):
+    _fields_ = [("num_panels", C.c_int32), ("max_bandwidth", C.c_int32), ("band_bytes", C.c_int64),
+                ("cluster_size", C.c_int32), ("workers", C.c_int32), ("factor_seconds", C.c_double),
+                ("solve_seconds", C.c_double)]
+
+
 class DimsC(C.Structure):
     _fields_ = [(k, C.c_int32) for k in ("el_mat_dim", "el_mat_size", "el_mat_lt_size", "el_mpc_dim", "el_mpc_size",
                                          "int_vec_size", "int_mat_size", "solver_max_bw", "dof_per_node",
@@ -117,6 +123,9 @@ def load_library():
         "astro_constraint_load": ([vp, F64P, F64P], C.c_int),
         "astro_surface_load": ([vp, C.c_int32, I32P, I32P, F64P, C.c_double, F64P], C.c_int),
         "astro_body_load": ([vp, C.c_int32, F64P, I32P, C.c_int32, C.c_void_p, F64P], C.c_int),
+        "astro_panels_factor": ([vp, C.c_int32, C.POINTER(PanelsInfoC)], C.c_int),
+        "astro_panels_solve": ([vp, C.c_int32, F64P, F64P, C.POINTER(PanelsInfoC)], C.c_int),
+        "astro_panels_solve_batched": ([vp, C.c_int32, F64P, F64P, C.POINTER(PanelsInfoC)], C.c_int),
         "astro_convert_to_ltri": ([vp, F64P], C.c_int),
         "astro_ldl_fact": ([vp, F64P, C.c_int32, I32P, C.c_int32], C.c_int),
         "astro_ldl_fact_resident": ([vp], C.c_int),
@@ -343,6 +352,24 @@ class AstroGPU:
         rc = self.L.astro_solve_static(self.h, _d(_f64(f)), _d(u), C.byref(o), C.byref(st))
         self._check(rc, allow=(7,) if allow_maxit else ())
         return u, st
+
+    def panels_factor(self, cluster_size=0):
+        """Band LDL^T of K + C^T C of every panel (connected component) in one launch."""
+        info = PanelsInfoC()
+        self._check(self.L.astro_panels_factor(self.h, int(cluster_size), C.byref(info)))
+        return info
+
+    def panels_solve(self, B, batched=False):
+        """X = (K + C^T C)^-1 B for the columns of B (n x k or n), with the panel factors."""
+        B = _f64(B)
+        one = B.ndim == 1
+        Bt = np.ascontiguousarray(B.reshape(self.n, -1).T)
+        X = np.zeros_like(Bt)
+        info = PanelsInfoC()
+        fn = self.L.astro_panels_solve_batched if batched else self.L.astro_panels_solve
+        self._check(fn(self.h, Bt.shape[0], _d(Bt), _d(X), C.byref(info)))
+        X = X.T
+        return (X[:, 0] if one else np.ascontiguousarray(X)), info
 
     def apply_operator(self, x, kind=64):
         y = np.zeros(self.n)

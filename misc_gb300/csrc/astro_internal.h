@@ -112,6 +112,10 @@ struct astro_ctx {
     DevBuf d_penRow, d_penPtr, d_penCol, d_penVal;
     int penRows = 0;
     int penVersion = 0;  // incremented whenever the penalty lists are rebuilt (astro_scale_mpc)
+    std::vector<int> penI, penJ;  // the same entries on the host (internal row, internal column)
+    std::vector<double> penV;
+    // batched panel factorisation (panels.cu), opaque
+    void *panels = nullptr;
     std::vector<double> mpcScaledHost, mpcRhsScaledHost;
     // skyline (reference DOF numbering) on device
     DevBuf d_ltRange, d_lt;
@@ -165,6 +169,7 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // el
 int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt);          // elem_shell4.cu
 int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln,
                                 const double *d_intRhs);                                           // elem_shell4.cu
+void panels_release(astro_ctx *ctx);                                         // panels.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu
 int export_csr_dev(astro_ctx *ctx, cudaStream_t s, double *d_mat, int *d_cols);  // assemble.cu
 double bsr_absmax(astro_ctx *ctx, int *status, int kind);                   // assemble.cu

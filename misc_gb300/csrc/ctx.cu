@@ -58,6 +58,7 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 
 static void free_all(astro_ctx *c) {
     krylov_release(c);
+    panels_release(c);
     if (c->asmExec) cudaGraphExecDestroy(c->asmExec);
     if (c->asmGraph) cudaGraphDestroy(c->asmGraph);
     c->asmExec = nullptr;
@@ -781,6 +782,14 @@ static int build_penalty(astro_ctx *ctx) {
     pcol.resize(pen.size());
     pval.resize(pen.size());
     std::vector<int> fill(ptr.begin(), ptr.end() - 1);
+    ctx->penI.clear();
+    ctx->penJ.clear();
+    ctx->penV.clear();
+    for (auto &kv : pen) {
+        ctx->penI.push_back(kv.first.first);
+        ctx->penJ.push_back(kv.first.second);
+        ctx->penV.push_back(kv.second);
+    }
     for (auto &kv : pen) {
         int br = kv.first.first / P.dpn;
         int t = fill[br]++;

@@ -1,0 +1,659 @@
+// Batched panels: LDL^T factorisation and multi-right-hand-side solves of a model made of many
+// independent panels (the connected components of its mesh), K + C^T C of the device-resident FP64
+// stiffness, in one persistent launch per phase.
+//
+// The reference solves such a batch one model at a time with the row-skyline LDL^T of
+// getSparseLDLFact / solveSparseLDLFact (Working/AStrO_solvers.f90:10-126): the same factorisation
+// without pivoting, in exact arithmetic the same factor on the envelope.  Here:
+//   ordering  each panel's nodes sorted by their coordinate along the panel's longest extent, then
+//             the next (a structured panel becomes column by column along its short side: the
+//             lower bandwidth is about dpn * (short side + 2) DOF);
+//   storage   per panel the lower band in 32 x 32 FP64 tiles, column-major within a tile: tile
+//             (J, d) holds block row J + d of block column J, d = 0 .. bt (bt = ceil(bw / 32));
+//   factor    right-looking blocked LDL^T, one thread-block cluster per panel: every CTA of the
+//             cluster factors the diagonal tile in shared memory, the CTAs split the panel rows
+//             below it (L = A L_JJ^-T D^-1) and then the band's trailing tile updates
+//             (A_IK -= L_IJ D_J L_KJ^T), with a cluster barrier after each of the two phases.
+//             Panels are assigned to clusters by longest-processing-time first on the host, so a
+//             cluster never waits on another (no spin-waits, no inter-cluster dependencies);
+//   solve     one CTA per (panel, group of up to 8 right-hand sides): forward sweep with unit L,
+//             D^-1, backward sweep with L^T; the eight warps split the band's tiles of a block row
+//             and warp 0 reduces and solves the diagonal tile with shuffles.
+// FP64 throughout: the factor is FP64-pipe bound (n bw^2 / 2 FMA per panel).
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <numeric>
+#include <vector>
+
+#include "astro_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace {
+
+constexpr int TB = 32;  // tile edge
+constexpr int TT = TB * TB;
+constexpr int kThreads = 256;
+constexpr int kGroups = kThreads / TB;  // warps per CTA
+constexpr int kSolveCols = 8;           // right-hand sides per solve CTA
+
+struct PanelMeta {
+    long long band;   // first double of the panel's tiles
+    long long xUnit;  // rows of the padded right-hand-side layout before this panel (times nrhs)
+    int n;            // DOF
+    int nbc;          // block columns, ceil(n / 32)
+    int bt;           // tiles below the diagonal tile in a block column
+    int pad;
+};
+
+struct SolveItem {
+    int panel, col0, ncol, pad;
+};
+
+struct PanelPlan {
+    int np = 0;
+    int cs = 0, workers = 0;
+    int factored = 0, kVersion = -1, penVersion = -1;
+    int maxBw = 0;
+    long long bandDoubles = 0, xRows = 0;
+    std::vector<PanelMeta> meta;
+    std::vector<int> panelOf, pos;  // per rank (0-based)
+    std::vector<double> work;
+    std::vector<int> sched, schedPtr;
+    DevBuf d_meta, d_sched, d_schedPtr, d_panelOf, d_pos, d_band, d_status, d_penI, d_penJ, d_penV;
+    int penCount = 0;
+    double factorSeconds = 0.0;
+};
+
+__device__ __forceinline__ size_t tile_off(const PanelMeta &M, int J, int d) {
+    return (size_t)M.band + ((size_t)J * (M.bt + 1) + d) * TT;
+}
+
+// lower-band entries of the BSR stiffness (dpn x dpn row-major blocks) into the tiles
+__global__ void k_band_fill(int nb, int dpn, const int *__restrict__ bRow, const int *__restrict__ bCol,
+                            const double *__restrict__ K, const int *__restrict__ panelOf, const int *__restrict__ pos,
+                            const PanelMeta *__restrict__ meta, double *__restrict__ band) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int bs = dpn * dpn;
+    if (t >= (long long)nb * bs) return;
+    const int b = (int)(t / bs), q = (int)(t % bs), a = q / dpn, c = q % dpn;
+    const int r = bRow[b], col = bCol[b];
+    const int i = pos[r] * dpn + a, j = pos[col] * dpn + c;
+    if (j > i) return;
+    const PanelMeta &M = meta[panelOf[r]];
+    const int I = i / TB, J = j / TB;
+    band[tile_off(M, J, I - J) + (j % TB) * TB + (i % TB)] = K[(size_t)b * bs + q];
+}
+
+// + C^T C (penalty entries, internal numbering; each (row, column) once)
+__global__ void k_band_pen(int cnt, int dpn, const int *__restrict__ pi, const int *__restrict__ pj,
+                           const double *__restrict__ pv, const int *__restrict__ panelOf, const int *__restrict__ pos,
+                           const PanelMeta *__restrict__ meta, double *__restrict__ band) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const int ri = pi[t] / dpn, rj = pj[t] / dpn;
+    const int i = pos[ri] * dpn + pi[t] % dpn, j = pos[rj] * dpn + pj[t] % dpn;
+    if (j > i) return;
+    const PanelMeta &M = meta[panelOf[ri]];
+    const int I = i / TB, J = j / TB;
+    band[tile_off(M, J, I - J) + (j % TB) * TB + (i % TB)] += pv[t];
+}
+
+// unit diagonal on the padding rows of each panel's last block
+__global__ void k_band_pad(const PanelMeta *__restrict__ meta, double *__restrict__ band) {
+    const PanelMeta M = meta[blockIdx.x];
+    const int i = M.n + threadIdx.x;
+    if (i >= M.nbc * TB) return;
+    band[tile_off(M, i / TB, 0) + (i % TB) * TB + (i % TB)] = 1.0;
+}
+
+// Blocked band LDL^T, one cluster per panel (the cluster's panels listed in sched).
+__global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restrict__ meta, const int *__restrict__ sched,
+                                                       const int *__restrict__ schedPtr, double *band, int *status) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int crank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
+    const int worker = blockIdx.x / cs;
+    __shared__ double sL[TB][TB + 1];  // diagonal tile: L below the diagonal, D on it
+    __shared__ double sA[TB][TB + 1], sB[TB][TB + 1];
+    const int t = threadIdx.x;
+    for (int q = schedPtr[worker]; q < schedPtr[worker + 1]; ++q) {
+        const int p = sched[q];
+        const PanelMeta M = meta[p];
+        for (int J = 0; J < M.nbc; ++J) {
+            // A. the diagonal tile, factored by every CTA of the cluster into its shared memory
+            double *Td = band + tile_off(M, J, 0);
+            for (int e = t; e < TT; e += kThreads) sL[e % TB][e / TB] = __ldcg(Td + e);
+            __syncthreads();
+            for (int k = 0; k < TB; ++k) {
+                const double inv = 1.0 / sL[k][k];
+                const int j = t % TB;
+                if (j > k)
+                    for (int i = t / TB; i < TB; i += kGroups)
+                        if (i >= j) sL[i][j] -= sL[i][k] * sL[j][k] * inv;
+                __syncthreads();
+                if (t > k && t < TB) sL[t][k] *= inv;
+                __syncthreads();
+            }
+            if (crank == 0 && t < TB && J * TB + t < M.n) {
+                const double dk = sL[t][t];
+                if (!(dk != 0.0 && isfinite(dk))) atomicCAS(status, 0, p + 1);
+            }
+            // B. the tiles below: L_IJ = A_IJ L_JJ^-T D^-1, one row per thread across the cluster
+            for (int rho = crank * kThreads + t; rho < M.bt * TB; rho += cs * kThreads) {
+                const int d = 1 + rho / TB, r = rho % TB;
+                if (J + d >= M.nbc) continue;
+                double *T = band + tile_off(M, J, d);
+                double w[TB];
+#pragma unroll
+                for (int c = 0; c < TB; ++c) w[c] = __ldcg(T + c * TB + r);
+#pragma unroll
+                for (int k = 1; k < TB; ++k) {
+                    double s = w[k];
+#pragma unroll
+                    for (int m = 0; m < k; ++m) s -= w[m] * sL[k][m];
+                    w[k] = s;
+                }
+#pragma unroll
+                for (int c = 0; c < TB; ++c) __stcg(T + c * TB + r, w[c] / sL[c][c]);
+            }
+            __threadfence();
+            cl.sync();
+            // every CTA has read the unfactored diagonal tile: store the factored one
+            if (crank == 0)
+                for (int e = t; e < TT; e += kThreads) __stcg(Td + e, sL[e % TB][e / TB]);
+            // C. trailing update of the band: tile (J+e, d-e) -= L_{J+d,J} D_J L_{J+e,J}^T, 1 <= e <= d
+            const int nt = M.bt * (M.bt + 1) / 2;
+            for (int u = crank; u < nt; u += cs) {
+                int d = 1, rem = u;
+                while (rem >= d) {
+                    rem -= d;
+                    ++d;
+                }
+                const int e = 1 + rem;
+                if (J + d >= M.nbc) continue;
+                const double *Ld = band + tile_off(M, J, d), *Le = band + tile_off(M, J, e);
+                __syncthreads();
+                for (int x = t; x < TT; x += kThreads) {
+                    const int r = x % TB, c = x / TB;
+                    sA[r][c] = __ldcg(Ld + x) * sL[c][c];
+                    sB[r][c] = __ldcg(Le + x);
+                }
+                __syncthreads();
+                const int r = t % TB, c0 = (t / TB) * 4;
+                double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 8
+                for (int k = 0; k < TB; ++k) {
+                    const double a = sA[r][k];
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) acc[cc] += a * sB[c0 + cc][k];
+                }
+                double *Tt = band + tile_off(M, J + e, d - e);
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) {
+                    double *pt = Tt + (c0 + cc) * TB + r;
+                    __stcg(pt, __ldcg(pt) - acc[cc]);
+                }
+            }
+            __threadfence();
+            cl.sync();
+        }
+    }
+}
+
+// Forward and backward sweeps for the right-hand sides col0 .. col0+ncol-1 of one panel, in
+// place in X (panel block: nrhs columns of npad rows).
+__global__ void __launch_bounds__(kThreads) k_band_solve(const PanelMeta *__restrict__ meta,
+                                                         const SolveItem *__restrict__ items,
+                                                         const double *__restrict__ band, double *X, int nrhs) {
+    extern __shared__ double sm[];
+    double(*sT)[TB][TB + 1] = reinterpret_cast<double(*)[TB][TB + 1]>(sm);
+    double(*sP)[TB][kSolveCols + 1] = reinterpret_cast<double(*)[TB][kSolveCols + 1]>(sm + kGroups * TB * (TB + 1));
+    const SolveItem it = items[blockIdx.x];
+    const PanelMeta M = meta[it.panel];
+    const int npad = M.nbc * TB, ncol = it.ncol;
+    double *Xp = X + (size_t)M.xUnit * nrhs + (size_t)it.col0 * npad;
+    const int t = threadIdx.x, r = t % TB, g = t / TB;
+    // forward: L y = b
+    for (int I = 0; I < M.nbc; ++I) {
+        double acc[kSolveCols];
+#pragma unroll
+        for (int c = 0; c < kSolveCols; ++c) acc[c] = 0.0;
+        const int dmax = min(M.bt, I);
+        for (int d = 1 + g; d <= dmax; d += kGroups) {
+            const double *L = band + tile_off(M, I - d, d);
+            const double *y = Xp + (size_t)(I - d) * TB;
+            for (int k = 0; k < TB; ++k) {
+                const double l = L[k * TB + r];
+#pragma unroll
+                for (int c = 0; c < kSolveCols; ++c)
+                    if (c < ncol) acc[c] += l * y[(size_t)c * npad + k];
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < kSolveCols; ++c) sP[g][r][c] = acc[c];
+        __syncthreads();
+        if (g == 0) {
+            const double *Ld = band + tile_off(M, I, 0);
+            double v[kSolveCols];
+#pragma unroll
+            for (int c = 0; c < kSolveCols; ++c) {
+                double s = 0.0;
+                for (int q = 0; q < kGroups; ++q) s += sP[q][r][c];
+                v[c] = (c < ncol) ? Xp[(size_t)c * npad + I * TB + r] - s : 0.0;
+            }
+            for (int k = 0; k < TB; ++k) {
+                const double lk = Ld[k * TB + r];
+#pragma unroll
+                for (int c = 0; c < kSolveCols; ++c) {
+                    const double yk = __shfl_sync(0xffffffffu, v[c], k);
+                    if (r > k) v[c] -= lk * yk;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < kSolveCols; ++c)
+                if (c < ncol) Xp[(size_t)c * npad + I * TB + r] = v[c];
+        }
+        __syncthreads();
+    }
+    // backward: L^T x = D^-1 y
+    for (int J = M.nbc - 1; J >= 0; --J) {
+        double acc[kSolveCols];
+#pragma unroll
+        for (int c = 0; c < kSolveCols; ++c) acc[c] = 0.0;
+        const int dmax = min(M.bt, M.nbc - 1 - J);
+        for (int d = 1 + g; d <= dmax; d += kGroups) {
+            const double *L = band + tile_off(M, J, d);
+            for (int col = 0; col < TB; ++col) sT[g][r][col] = L[col * TB + r];
+            __syncwarp();
+            const double *x = Xp + (size_t)(J + d) * TB;
+            for (int k = 0; k < TB; ++k) {
+                const double l = sT[g][k][r];
+#pragma unroll
+                for (int c = 0; c < kSolveCols; ++c)
+                    if (c < ncol) acc[c] += l * x[(size_t)c * npad + k];
+            }
+            __syncwarp();
+        }
+#pragma unroll
+        for (int c = 0; c < kSolveCols; ++c) sP[g][r][c] = acc[c];
+        __syncthreads();
+        if (g == 0) {
+            const double *Ld = band + tile_off(M, J, 0);
+            for (int col = 0; col < TB; ++col) sT[0][r][col] = Ld[col * TB + r];
+            __syncwarp();
+            const double dinv = 1.0 / sT[0][r][r];
+            double v[kSolveCols];
+#pragma unroll
+            for (int c = 0; c < kSolveCols; ++c) {
+                double s = 0.0;
+                for (int q = 0; q < kGroups; ++q) s += sP[q][r][c];
+                v[c] = (c < ncol) ? Xp[(size_t)c * npad + J * TB + r] * dinv - s : 0.0;
+            }
+            for (int k = TB - 1; k >= 0; --k) {
+                const double lkr = sT[0][k][r];
+#pragma unroll
+                for (int c = 0; c < kSolveCols; ++c) {
+                    const double xk = __shfl_sync(0xffffffffu, v[c], k);
+                    if (r < k) v[c] -= lkr * xk;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < kSolveCols; ++c)
+                if (c < ncol) Xp[(size_t)c * npad + J * TB + r] = v[c];
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+}
+
+// internal-layout columns (nrhs x n) <-> the padded panel layout
+__global__ void k_panel_move(int n, int dpn, int nrhs, double *__restrict__ vec, const int *__restrict__ panelOf,
+                             const int *__restrict__ pos, const PanelMeta *__restrict__ meta, double *__restrict__ X,
+                             int toPanel) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)n * nrhs) return;
+    const int c = (int)(t / n), i = (int)(t % n), r = i / dpn, a = i % dpn;
+    const PanelMeta &M = meta[panelOf[r]];
+    const size_t xi = (size_t)M.xUnit * nrhs + (size_t)c * M.nbc * TB + (size_t)pos[r] * dpn + a;
+    if (toPanel)
+        X[xi] = vec[t];
+    else
+        vec[t] = X[xi];
+}
+
+constexpr size_t kSolveSmem = sizeof(double) * (kGroups * TB * (TB + 1) + kGroups * TB * (kSolveCols + 1));
+
+// connected components, orderings, bandwidths, storage and the cluster schedule
+int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
+    const AstroPrep &P = ctx->P;
+    const int N = P.N, dpn = P.dpn;
+    // union-find over nodes (1-based ids) through the elements
+    std::vector<int> par(N + 1);
+    std::iota(par.begin(), par.end(), 0);
+    auto find = [&](int x) {
+        while (par[x] != x) x = par[x] = par[par[x]];
+        return x;
+    };
+    for (int e = 0; e < P.E; ++e) {
+        int first = 0;
+        for (int k = 0; k < 8; ++k) {
+            const int nd = ctx->elist[8 * (size_t)e + k];
+            if (nd < 1) continue;
+            if (!first) {
+                first = nd;
+                continue;
+            }
+            const int a = find(first), b = find(nd);
+            if (a != b) par[std::max(a, b)] = std::min(a, b);
+        }
+    }
+    std::vector<int> compId(N + 1, -1), roots;
+    for (int nd = 1; nd <= N; ++nd) {
+        const int r = find(nd);
+        if (compId[r] < 0) {
+            compId[r] = (int)roots.size();
+            roots.push_back(r);
+        }
+        compId[nd] = compId[r];
+    }
+    const int np = (int)roots.size();
+    std::vector<std::vector<int>> members(np);
+    for (int nd = 1; nd <= N; ++nd) members[compId[nd]].push_back(nd);
+    L.np = np;
+    L.panelOf.assign(N, 0);
+    L.pos.assign(N, 0);
+    for (int p = 0; p < np; ++p) {
+        auto &mb = members[p];
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (int nd : mb)
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = std::min(lo[d], ctx->nodes[3 * (size_t)(nd - 1) + d]);
+                hi[d] = std::max(hi[d], ctx->nodes[3 * (size_t)(nd - 1) + d]);
+            }
+        int ax[3] = {0, 1, 2};
+        std::stable_sort(ax, ax + 3, [&](int a, int b) { return hi[a] - lo[a] > hi[b] - lo[b]; });
+        std::stable_sort(mb.begin(), mb.end(), [&](int a, int b) {
+            for (int k = 0; k < 3; ++k) {
+                const double xa = ctx->nodes[3 * (size_t)(a - 1) + ax[k]], xb = ctx->nodes[3 * (size_t)(b - 1) + ax[k]];
+                if (xa != xb) return xa < xb;
+            }
+            return a < b;
+        });
+        for (int k = 0; k < (int)mb.size(); ++k) {
+            const int r = P.currentRank[mb[k]] - 1;
+            L.panelOf[r] = p;
+            L.pos[r] = k;
+        }
+    }
+    // node bandwidth of each panel from the block pattern and the penalty couplings
+    std::vector<int> bwn(np, 0);
+    for (int r = 0; r < N; ++r)
+        for (int q = P.bRowPtr[r]; q < P.bRowPtr[r + 1]; ++q) {
+            const int c = P.bCol[q];
+            if (L.panelOf[c] != L.panelOf[r]) return set_err(ctx, ASTRO_ERR_ARG, "panels: coupled components");
+            bwn[L.panelOf[r]] = std::max(bwn[L.panelOf[r]], std::abs(L.pos[r] - L.pos[c]));
+        }
+    for (size_t k = 0; k < ctx->penI.size(); ++k) {
+        const int ri = ctx->penI[k] / dpn, rj = ctx->penJ[k] / dpn;
+        if (L.panelOf[ri] != L.panelOf[rj])
+            return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "panels: a constraint couples two panels");
+        bwn[L.panelOf[ri]] = std::max(bwn[L.panelOf[ri]], std::abs(L.pos[ri] - L.pos[rj]));
+    }
+    L.meta.assign(np, PanelMeta{});
+    L.work.assign(np, 0.0);
+    long long band = 0, xr = 0;
+    L.maxBw = 0;
+    for (int p = 0; p < np; ++p) {
+        PanelMeta &M = L.meta[p];
+        M.n = (int)members[p].size() * dpn;
+        M.nbc = (M.n + TB - 1) / TB;
+        const int bw = bwn[p] * dpn + dpn - 1;
+        L.maxBw = std::max(L.maxBw, bw);
+        M.bt = (bw + TB - 1) / TB;
+        M.band = band;
+        M.xUnit = xr;
+        band += (long long)M.nbc * (M.bt + 1) * TT;
+        xr += (long long)M.nbc * TB;
+        L.work[p] = (double)M.nbc * (0.5 * M.bt * (M.bt + 1) + 2.0);
+    }
+    L.bandDoubles = band;
+    L.xRows = xr;
+    // clusters: as many as fit at once, panels by longest processing time first
+    L.cs = cs;
+    int maxClusters = 0;
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs * 64);
+        cfg.blockDim = dim3(kThreads);
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        if (cudaOccupancyMaxActiveClusters(&maxClusters, k_band_ldl, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            maxClusters = 0;
+        }
+    }
+    if (maxClusters < 1) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+        maxClusters = std::max(1, sms / cs);
+    }
+    L.workers = std::max(1, std::min(np, maxClusters));
+    std::vector<int> order(np);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return L.work[a] > L.work[b]; });
+    std::vector<double> load(L.workers, 0.0);
+    std::vector<std::vector<int>> lists(L.workers);
+    for (int p : order) {
+        const int w = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        lists[w].push_back(p);
+        load[w] += L.work[p];
+    }
+    L.sched.clear();
+    L.schedPtr.assign(1, 0);
+    for (auto &l : lists) {
+        L.sched.insert(L.sched.end(), l.begin(), l.end());
+        L.schedPtr.push_back((int)L.sched.size());
+    }
+    int rc;
+    if ((rc = upload(ctx, L.d_meta, L.meta.data(), sizeof(PanelMeta) * np)) ||
+        (rc = upload(ctx, L.d_sched, L.sched.data(), sizeof(int) * L.sched.size())) ||
+        (rc = upload(ctx, L.d_schedPtr, L.schedPtr.data(), sizeof(int) * L.schedPtr.size())) ||
+        (rc = upload(ctx, L.d_panelOf, L.panelOf.data(), sizeof(int) * N)) ||
+        (rc = upload(ctx, L.d_pos, L.pos.data(), sizeof(int) * N)) ||
+        (rc = dev_alloc(ctx, L.d_status, sizeof(int))))
+        return rc;
+    return ASTRO_OK;
+}
+
+void plan_free(PanelPlan *L) {
+    DevBuf *b[] = {&L->d_meta, &L->d_sched, &L->d_schedPtr, &L->d_panelOf, &L->d_pos, &L->d_band,
+                   &L->d_status, &L->d_penI,  &L->d_penJ,     &L->d_penV};
+    for (DevBuf *x : b) dev_free(*x);
+}
+
+void fill_info(const PanelPlan &L, astro_panels_info *info) {
+    if (!info) return;
+    info->num_panels = L.np;
+    info->max_bandwidth = L.maxBw;
+    info->band_bytes = L.bandDoubles * (long long)sizeof(double);
+    info->cluster_size = L.cs;
+    info->workers = L.workers;
+    info->factor_seconds = L.factorSeconds;
+}
+
+}  // namespace
+
+void panels_release(astro_ctx *ctx) {
+    if (!ctx->panels) return;
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    plan_free(L);
+    delete L;
+    ctx->panels = nullptr;
+}
+
+extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *info) {
+    if (!ctx) return ASTRO_ERR_ARG;
+    if (cluster_size == 0) cluster_size = 8;
+    if (cluster_size != 1 && cluster_size != 2 && cluster_size != 4 && cluster_size != 8)
+        return set_err(ctx, ASTRO_ERR_ARG, "panels: cluster_size must be 1, 2, 4 or 8");
+    if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "panels: FP64 stiffness not assembled");
+    if (ctx->P.mpcDim > 0 && !ctx->mpcScaled)
+        return set_err(ctx, ASTRO_ERR_STATE, "panels: constraints not scaled (astro_scale_mpc)");
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    if (L && L->cs != cluster_size) {
+        panels_release(ctx);
+        L = nullptr;
+    }
+    int rc;
+    if (!L) {
+        L = new PanelPlan();
+        ctx->panels = L;
+        if ((rc = plan_build(ctx, *L, cluster_size))) {
+            panels_release(ctx);
+            return rc;
+        }
+    }
+    const auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = ctx->stream;
+    const AstroPrep &P = ctx->P;
+    if (!L->d_band.p && (rc = dev_alloc(ctx, L->d_band, sizeof(double) * (size_t)L->bandDoubles))) return rc;
+    if (L->penVersion != ctx->penVersion) {
+        L->penCount = (int)ctx->penI.size();
+        if (L->penCount &&
+            ((rc = upload(ctx, L->d_penI, ctx->penI.data(), sizeof(int) * L->penCount)) ||
+             (rc = upload(ctx, L->d_penJ, ctx->penJ.data(), sizeof(int) * L->penCount)) ||
+             (rc = upload(ctx, L->d_penV, ctx->penV.data(), sizeof(double) * L->penCount))))
+            return rc;
+    }
+    CK(cudaMemsetAsync(L->d_band.p, 0, sizeof(double) * (size_t)L->bandDoubles, s));
+    CK(cudaMemsetAsync(L->d_status.p, 0, sizeof(int), s));
+    const long long fillN = (long long)P.nb * P.dpn * P.dpn;
+    k_band_fill<<<(unsigned)((fillN + 255) / 256), 256, 0, s>>>(
+        P.nb, P.dpn, dptr<int>(ctx->d_bRow), dptr<int>(ctx->d_bCol), dptr<double>(ctx->d_K64),
+        dptr<int>(L->d_panelOf), dptr<int>(L->d_pos), dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_band));
+    if (L->penCount)
+        k_band_pen<<<(L->penCount + 255) / 256, 256, 0, s>>>(
+            L->penCount, P.dpn, dptr<int>(L->d_penI), dptr<int>(L->d_penJ), dptr<double>(L->d_penV),
+            dptr<int>(L->d_panelOf), dptr<int>(L->d_pos), dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_band));
+    k_band_pad<<<L->np, TB, 0, s>>>(dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_band));
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "panel band fill"))) return rc;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(L->workers * L->cs);
+    cfg.blockDim = dim3(kThreads);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = L->cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, k_band_ldl, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+                          (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
+                          dptr<double>(L->d_band), dptr<int>(L->d_status)));
+    int status = 0;
+    CK(cudaMemcpyAsync(&status, L->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    L->factorSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    L->kVersion = ctx->k64Version;
+    L->penVersion = ctx->penVersion;
+    L->factored = status == 0;
+    fill_info(*L, info);
+    if (status) return set_err(ctx, ASTRO_ERR_PIVOT, "panels: zero or non-finite pivot in panel " + std::to_string(status - 1));
+    return ASTRO_OK;
+}
+
+static int panels_solve_dev(astro_ctx *ctx, PanelPlan *L, int nrhs, double *d_vec, DevBuf &X) {
+    const AstroPrep &P = ctx->P;
+    cudaStream_t s = ctx->stream;
+    int rc;
+    const size_t xs = (size_t)L->xRows * nrhs;
+    if ((rc = dev_alloc(ctx, X, sizeof(double) * xs))) return rc;
+    CK(cudaMemsetAsync(X.p, 0, sizeof(double) * xs, s));
+    const long long mv = (long long)P.n * nrhs;
+    const unsigned mg = (unsigned)((mv + 255) / 256);
+    k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nrhs, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
+                                    dptr<PanelMeta>(L->d_meta), dptr<double>(X), 1);
+    // one item per (panel, group of right-hand sides), the largest panels first
+    const int groups = (nrhs + kSolveCols - 1) / kSolveCols;
+    std::vector<int> order(L->np);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (double)L->meta[a].n * (L->meta[a].bt + 1) > (double)L->meta[b].n * (L->meta[b].bt + 1);
+    });
+    std::vector<SolveItem> items;
+    for (int p : order) {
+        int c0 = 0;
+        for (int gidx = 0; gidx < groups; ++gidx) {
+            const int nc = nrhs / groups + (gidx < nrhs % groups ? 1 : 0);
+            items.push_back({p, c0, nc, 0});
+            c0 += nc;
+        }
+    }
+    DevBuf dItems;
+    if ((rc = upload(ctx, dItems, items.data(), sizeof(SolveItem) * items.size()))) return rc;
+    CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem));
+    k_band_solve<<<(unsigned)items.size(), kThreads, kSolveSmem, s>>>(
+        dptr<PanelMeta>(L->d_meta), dptr<SolveItem>(dItems), dptr<double>(L->d_band), dptr<double>(X), nrhs);
+    k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nrhs, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
+                                    dptr<PanelMeta>(L->d_meta), dptr<double>(X), 0);
+    rc = cuda_check(ctx, cudaGetLastError(), "panel solve");
+    if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(s), "panel solve");
+    dev_free(dItems);
+    return rc;
+}
+
+extern "C" int astro_panels_solve(astro_ctx *ctx, int32_t num_rhs, const double *rhs, double *x,
+                                  astro_panels_info *info) {
+    if (!ctx || num_rhs < 1 || !rhs || !x) return ASTRO_ERR_ARG;
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    if (!L || !L->factored || L->kVersion != ctx->k64Version || L->penVersion != ctx->penVersion)
+        return set_err(ctx, ASTRO_ERR_STATE, "panels: no current factorisation (astro_panels_factor)");
+    const int n = ctx->P.n;
+    const auto t0 = std::chrono::steady_clock::now();
+    DevBuf ref, vec, X;
+    int rc = dev_alloc(ctx, ref, sizeof(double) * (size_t)n * num_rhs);
+    if (!rc) rc = dev_alloc(ctx, vec, sizeof(double) * (size_t)n * num_rhs);
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(ref.p, rhs, sizeof(double) * (size_t)n * num_rhs, cudaMemcpyHostToDevice,
+                                        ctx->stream);
+        rc = cuda_check(ctx, e, "panels: upload");
+    }
+    for (int c = 0; c < num_rhs && !rc; ++c)
+        rc = ref_to_int_vec(ctx, dptr<double>(ref) + (size_t)c * n, dptr<double>(vec) + (size_t)c * n, n);
+    if (!rc) rc = panels_solve_dev(ctx, L, num_rhs, dptr<double>(vec), X);
+    for (int c = 0; c < num_rhs && !rc; ++c)
+        rc = int_to_ref_vec(ctx, dptr<double>(vec) + (size_t)c * n, dptr<double>(ref) + (size_t)c * n, n);
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(x, ref.p, sizeof(double) * (size_t)n * num_rhs, cudaMemcpyDeviceToHost,
+                                        ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        rc = cuda_check(ctx, e, "panels: download");
+    }
+    dev_free(ref);
+    dev_free(vec);
+    dev_free(X);
+    if (info) {
+        fill_info(*L, info);
+        info->solve_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return rc;
+}
+
+extern "C" int astro_panels_solve_batched(astro_ctx *ctx, int32_t num_rhs, const double *rhs, double *x,
+                                          astro_panels_info *info) {
+    if (!ctx) return ASTRO_ERR_ARG;
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    int rc;
+    if (!L || !L->factored || L->kVersion != ctx->k64Version || L->penVersion != ctx->penVersion)
+        if ((rc = astro_panels_factor(ctx, L ? L->cs : 0, info))) return rc;
+    return astro_panels_solve(ctx, num_rhs, rhs, x, info);
+}

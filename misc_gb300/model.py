@@ -264,6 +264,76 @@ def plate_shell(nx=40, ny=8, lx=10.0, ly=2.0, t=0.05, E=7.0e10, nu=0.33, rho=270
     return m
 
 
+def panel_batch(num_panels=512, seed0=1000, n_range=(8, 96), t_range=(0.01, 0.1), p_range=(1.0e2, 1.0e4),
+                n_dvars=32, h=0.1, E=7.0e10, nu=0.33, rho=2700.0, name="panels"):
+    """Batch of independent shell4 panels as one model (its connected components): panel p has
+    n_x, n_y ~ U{n_range} elements of size h (its own generator, seed seed0 + p), thickness
+    t ~ U(t_range) (one section per panel), all six DOF clamped on its x = 0 edge, and a pressure
+    ~ U(p_range) on all its elements.  n_dvars design variables: layup thickness groups of equal
+    element count within every panel (element k of a panel with e elements is in group
+    k * n_dvars // e); design variable g covers group g of every panel.  The panels lie side by
+    side in z (disconnected).  Extra attributes: panel_el_ptr, panel_node_ptr (per panel first
+    element / node, 0-based, plus the totals), panel_pressure, panel_thickness, panel_n."""
+    nodes, els, sec, thick, pres, nxy = [], [], [], [], [], []
+    mpc_nodes, el_ptr, nd_ptr = [], [0], [0]
+    grp = []
+    nn = 0
+    for p in range(num_panels):
+        rng = np.random.default_rng(seed0 + p)
+        nx, ny = (int(v) for v in rng.integers(n_range[0], n_range[1] + 1, 2))
+        t = float(rng.uniform(*t_range))
+        pr = float(rng.uniform(*p_range))
+        xs = np.arange(nx + 1) * h
+        ys = np.arange(ny + 1) * h
+        X, Y = np.meshgrid(xs, ys, indexing="xy")
+        nodes.append(np.stack([X.ravel(), Y.ravel(), np.full(X.size, float(p))], axis=1))
+        nid = lambda i, j: nn + j * (nx + 1) + i + 1
+        e = np.zeros((nx * ny, 8), np.int32)
+        jj, ii = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+        ii, jj = ii.ravel(), jj.ravel()
+        e[:, 0], e[:, 1], e[:, 2], e[:, 3] = nid(ii, jj), nid(ii + 1, jj), nid(ii + 1, jj + 1), nid(ii, jj + 1)
+        els.append(e)
+        ne = nx * ny
+        sec.append(np.full(ne, p + 1, np.int32))
+        grp.append((np.arange(ne) * n_dvars) // ne + 1)
+        mpc_nodes += [nid(0, j) for j in range(ny + 1)]
+        thick.append(t)
+        pres.append(pr)
+        nxy.append((nx, ny))
+        nn += (nx + 1) * (ny + 1)
+        el_ptr.append(el_ptr[-1] + ne)
+        nd_ptr.append(nn)
+    nodes = np.vstack(nodes)
+    els = np.vstack(els)
+    E_ = els.shape[0]
+    S = num_panels
+    m = Model(
+        node_list=nodes, element_list=els, element_type=np.full(E_, 41, np.int32),
+        element_section=np.concatenate(sec), section_mat_id=np.ones(S, np.int32),
+        section_orient=np.broadcast_to(np.eye(3), (S, 3, 3)).copy(),
+        sec_layup_range=np.arange(S + 1, dtype=np.int32), layup_mat_id=np.ones(S, np.int32),
+        layup_thickness=np.array(thick), layup_angle=np.zeros(S), section_z_offset=np.zeros(S),
+        material_elastic=np.array([_iso(E, nu)]), material_density=np.array([rho]), name=name)
+    m.mpc_range, m.mpc_node, m.mpc_dof, m.mpc_coef, m.mpc_rhs = _clamp_mpc(mpc_nodes, range(1, 7))
+    m.face_el = np.arange(1, E_ + 1, dtype=np.int32)
+    m.face_num = np.ones(E_, np.int32)
+    m.pressure = 0.0
+    if n_dvars:
+        m.el_to_d_range = np.arange(E_ + 1, dtype=np.int32)
+        m.el_to_d = np.concatenate(grp).astype(np.int32)
+        m.el_to_coef = np.ones(E_)
+        m.d_category = np.full(n_dvars, 1, np.int32)
+        m.d_component = np.ones(n_dvars, np.int32)
+        m.d_layer = np.ones(n_dvars, np.int32)
+        m.d_value = np.zeros(n_dvars)
+    m.panel_el_ptr = np.array(el_ptr)
+    m.panel_node_ptr = np.array(nd_ptr)
+    m.panel_pressure = np.array(pres)
+    m.panel_thickness = np.array(thick)
+    m.panel_n = np.array(nxy)
+    return m
+
+
 def hex_block(nx=64, ny=32, nz=32, lx=4.0, ly=2.0, lz=2.0, jitter=0.1, seed=0, E_med=2.0e11, sigma=0.5,
               nu=0.3, rho=7800.0, traction=1.0e6, E_field=None, name="block"):
     """brick8 block; interior nodes jittered U(-jitter*h, +jitter*h) per axis; per-element modulus

@@ -1,0 +1,67 @@
+"""Batched panels with complex-step sensitivities: many independent shell panels solved for
+their pressure load and for the complex-step design sensitivities of their thickness groups.
+
+For every panel the reference would run one model: assembly (getElasticSolnLoad), the
+constraint scaling, the applied pressure load, getdRelasticdD per design variable
+(Working/AStrO_commandFunctions.f90:1172-1375) and a linear solve per right-hand side.  Here the
+panels are one model (its connected components) and every step runs once for all of them: the
+FP64 assembly, the complex-step dR/dd of each thickness group (a design variable covers its group
+in every panel), and one batched LDL^T factorisation plus one multi-right-hand-side solve
+(astro_panels_factor / astro_panels_solve)."""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+
+from .astro import AstroGPU
+from .model import make_state
+
+
+def pressure_load(g: AstroGPU, m) -> np.ndarray:
+    """Consistent load of each panel's own pressure (the unit-pressure load of all faces scaled
+    panel by panel: the load is linear in the pressure and local to the panel)."""
+    unit = g.surface_load(m.face_el, m.face_num, pressure=1.0)
+    node_p = np.repeat(m.panel_pressure, np.diff(m.panel_node_ptr))
+    scale = np.zeros(g.n)
+    idx = g.n_dof_index[:, :g.dims.dof_per_node] - 1
+    scale[idx] = node_p[:, None]
+    return unit * scale
+
+
+def sensitivity_rhs(g: AstroGPU, n_dvars: int, state=None, h: float = 1e-14) -> np.ndarray:
+    """Columns dRu/dd of design variables 1..n_dvars (complex step at the given state), condensed
+    to the nodal DOF (updateExternalRHS): the right-hand sides of the sensitivity solves."""
+    cols = []
+    for d in range(1, n_dvars + 1):
+        dr, idr = g.getdRelasticdD(d, h, state=state)
+        cols.append(g.updateExternalRHS(dr, idr) if g.int_vec_size else dr)
+    return np.column_stack(cols)
+
+
+def solve_batch(g: AstroGPU, m, n_dvars: int, cluster_size: int = 0, load_scale: float = 1.0):
+    """Assembly, pressure load, batched factorisation and displacement solve, the complex-step
+    dRu/dd of every thickness group at the solved state, and one batched solve of all of them:
+    returns (u, du_dd, timings) with du_dd[:, k] = -(K + C^T C)^-1 dRu/dd_k, the direct design
+    sensitivity of the displacement (exact for the linear response; at a large displacement the
+    complex step differentiates the element's nonlinear residual at that state)."""
+    t = {}
+    t0 = time.perf_counter()
+    g.getElasticSolnLoad(1, export=False)
+    g.scaleElasticMPC()
+    f = load_scale * pressure_load(g, m)
+    t["assembly_s"] = time.perf_counter() - t0
+    info = g.panels_factor(cluster_size)
+    t["factor_s"] = info.factor_seconds
+    u, s1 = g.panels_solve(f)
+    t["solve_u_s"] = s1.solve_seconds
+    t0 = time.perf_counter()
+    iu = g.updateInternalSoln(u, np.zeros(g.int_vec_size)) if g.int_vec_size else None
+    st = make_state(g.n, disp=u, internal_disp=iu)
+    R = sensitivity_rhs(g, n_dvars, state=st)
+    t["rhs_s"] = time.perf_counter() - t0
+    dU, s2 = g.panels_solve(R)
+    t["solve_dU_s"] = s2.solve_seconds
+    t["info"] = info
+    t["f"], t["R"], t["state"] = f, R, st
+    return u, -dU, t
