@@ -361,15 +361,14 @@ class AstroGPU:
 
     def panels_solve(self, B, batched=False):
         """X = (K + C^T C)^-1 B for the columns of B (n x k or n), with the panel factors."""
-        B = _f64(B)
-        one = B.ndim == 1
-        Bt = np.ascontiguousarray(B.reshape(self.n, -1).T)
-        X = np.zeros_like(Bt)
+        one = np.ndim(B) == 1
+        # column k of B contiguous (Fortran order) is the C ABI's layout: no copy when B has it
+        Bf = np.asfortranarray(np.asarray(B, dtype=np.float64).reshape(self.n, -1))
+        X = np.empty(Bf.shape, dtype=np.float64, order="F")
         info = PanelsInfoC()
         fn = self.L.astro_panels_solve_batched if batched else self.L.astro_panels_solve
-        self._check(fn(self.h, Bt.shape[0], _d(Bt), _d(X), C.byref(info)))
-        X = X.T
-        return (X[:, 0] if one else np.ascontiguousarray(X)), info
+        self._check(fn(self.h, Bf.shape[1], _d(Bf), _d(X), C.byref(info)))
+        return (X[:, 0] if one else X), info
 
     def apply_operator(self, x, kind=64):
         y = np.zeros(self.n)

@@ -36,7 +36,7 @@ def sensitivity_rhs(g: AstroGPU, n_dvars: int, state=None, h: float = 1e-14) -> 
     for d in range(1, n_dvars + 1):
         dr, idr = g.getdRelasticdD(d, h, state=state)
         cols.append(g.updateExternalRHS(dr, idr) if g.int_vec_size else dr)
-    return np.column_stack(cols)
+    return np.asfortranarray(np.column_stack(cols))
 
 
 def solve_batch(g: AstroGPU, m, n_dvars: int, cluster_size: int = 0, load_scale: float = 1.0):
