@@ -275,6 +275,57 @@ int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el,
 int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals, const int32_t *elements, int32_t count,
                     const astro_state *state, double *elastic_load);
 
+/* ---- thermal path --------------------------------------------------------------------------- */
+
+/* Thermal material data (not part of astro_model) and the thermal constraints: equations whose
+ * terms are temperature DOF (reference DOF 7), expanded per node like astro_model's constraints
+ * (buildThermalMPC, Working/AStrO_bookKeeping.f90:614-752). */
+typedef struct astro_thermal_props {
+    int32_t num_materials;
+    const double *material_therm_cond;  /* materialThermCond(6, num_materials): k11 k22 k33 k12 k13 k23 */
+    const double *material_spec_heat;   /* materialSpecHeat(num_materials) */
+    int32_t num_mpc;                    /* thermal constraint equations */
+    const int32_t *mpc_range;           /* (0:num_mpc) prefix sums over terms */
+    const int32_t *mpc_node;            /* node per term */
+    const double *mpc_coef;             /* coefficient per term */
+    const double *mpc_rhs;              /* right-hand side per equation */
+} astro_thermal_props;
+
+/* Thermal state, node vectors in rank order (nodeTemp(currentRank(node)), as the reference);
+ * NULL = zeros.  dynamic: add the capacitance term with Tdot from the generalised trapezoid rule
+ * (r_getElRt, Working/AStrO_r_elementEqns.f90:2176-2204). */
+typedef struct astro_thermal_state {
+    const double *node_temp, *prev_temp, *prev_tdot;
+    int32_t dynamic;
+    double nm_gamma, del_t;
+} astro_thermal_state;
+
+/* Per-element thermal properties (r_getMaterialThermCond / r_getShellThermCond and the specific
+ * heats, Working/AStrO_r_designPropertyFunctions.f90:129-186, 527-644), the thermal CSR layout
+ * (allocateThermalMat, bookKeeping :413-472: rows by rank, 1 + neighbours) and the constraint
+ * rows.  Outputs thermMatSize and thermMPCDim.  Brick or shell meshes. */
+int astro_thermal_setup(astro_ctx *ctx, const astro_thermal_props *props, int32_t *therm_mat_size,
+                        int32_t *therm_mpc_dim);
+/* getThermalSolnLoad(buildMat) (Working/AStrO_commandFunctions.f90:16-72): thermal_load[N] -= Rt
+ * (rank order); for build_mat = 1 the conductivity (+ capacitance / (gamma dt)) matrix stays on
+ * the device and, when therm_mat / therm_cols are non-NULL, is exported as the reference's CSR
+ * (thermMat, thermMatCols: 1-based rank columns in find-or-insert order). */
+int astro_thermal_soln_load(astro_ctx *ctx, int32_t build_mat, const astro_thermal_state *state,
+                            double *thermal_load, double *therm_mat, int32_t *therm_cols);
+/* scaleThermalMPC (:230-258): rows to unit length, times 100 max|thermMat|; the scaled rows out
+ * (may be NULL) and C^T C kept for the solve. */
+int astro_thermal_scale_mpc(astro_ctx *ctx, double *mpc_mat, double *mpc_rhs);
+/* getThermalConstraintLoad (:197-228): thermal_load += C^T (c - C T). */
+int astro_thermal_constraint_load(astro_ctx *ctx, const double *node_temp, double *thermal_load);
+/* getThermalAppliedLoad's bodyHeatGen branch (:96-139): heat generation q per unit volume on the
+ * listed elements (1-based; NULL = all), integral of N (times the thickness for shells). */
+int astro_thermal_heat_gen(astro_ctx *ctx, double q, const int32_t *elements, int32_t count, double *thermal_load);
+/* (K_T + C^T C) dtemp = rhs by Jacobi-preconditioned conjugate gradients in FP64 on the device,
+ * from dtemp's input value, to ||r|| <= rtol ||rhs|| (in place of the reference's gMRes with
+ * its skyline LDL^T preconditioner on the thermal system, stepSolve :689-703). */
+int astro_thermal_solve(astro_ctx *ctx, const double *rhs, double *dtemp, double rtol, int32_t max_iters,
+                        astro_solve_stats *stats);
+
 /* ---- batched panels ----------------------------------------------------------------------- */
 
 /* A model made of many independent panels (the connected components of its mesh; constraints

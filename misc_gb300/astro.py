@@ -34,6 +34,45 @@ class AstroError(RuntimeError):
         self.code = code
 
 
+class ThermalPropsC(C.Structure):
+    _fields_ = [("num_materials", C.c_int32), ("material_therm_cond", F64P), ("material_spec_heat", F64P),
+                ("num_mpc", C.c_int32), ("mpc_range", I32P), ("mpc_node", I32P), ("mpc_coef", F64P),
+                ("mpc_rhs", F64P)]
+
+
+class ThermalStateC(C.Structure):
+    _fields_ = [("node_temp", F64P), ("prev_temp", F64P), ("prev_tdot", F64P), ("dynamic", C.c_int32),
+                ("nm_gamma", C.c_double), ("del_t", C.c_double)]
+
+
+def thermal_props(cond, spec_heat, mpc=None):
+    """astro_thermal_props over float64/int32 arrays: cond (M, 6), spec_heat (M,), mpc =
+    (range, node, coef, rhs) of the temperature constraints or None."""
+    keep = {"c": _f64(np.asarray(cond).reshape(-1)), "s": _f64(spec_heat)}
+    p = ThermalPropsC()
+    p.num_materials = len(keep["s"])
+    p.material_therm_cond = _d(keep["c"])
+    p.material_spec_heat = _d(keep["s"])
+    if mpc is not None:
+        keep.update(r=_i32(mpc[0]), n=_i32(mpc[1]), k=_f64(mpc[2]), h=_f64(mpc[3]))
+        p.num_mpc = len(keep["r"]) - 1
+        p.mpc_range, p.mpc_node, p.mpc_coef, p.mpc_rhs = _i(keep["r"]), _i(keep["n"]), _d(keep["k"]), _d(keep["h"])
+    p._keep = keep
+    return p
+
+
+def thermal_state(temp=None, prev_temp=None, prev_tdot=None, dynamic=0, gamma=0.5, del_t=0.0):
+    keep = {}
+    s = ThermalStateC()
+    for name, arr in (("node_temp", temp), ("prev_temp", prev_temp), ("prev_tdot", prev_tdot)):
+        if arr is not None:
+            keep[name] = _f64(arr)
+            setattr(s, name, _d(keep[name]))
+    s.dynamic, s.nm_gamma, s.del_t = dynamic, gamma, del_t
+    s._keep = keep
+    return s
+
+
 class PanelsInfoC(C.Structure):
     _fields_ = [("num_panels", C.c_int32), ("max_bandwidth", C.c_int32), ("band_bytes", C.c_int64),
                 ("cluster_size", C.c_int32), ("workers", C.c_int32), ("factor_seconds", C.c_double),
@@ -123,6 +162,12 @@ def load_library():
         "astro_constraint_load": ([vp, F64P, F64P], C.c_int),
         "astro_surface_load": ([vp, C.c_int32, I32P, I32P, F64P, C.c_double, F64P], C.c_int),
         "astro_body_load": ([vp, C.c_int32, F64P, I32P, C.c_int32, C.c_void_p, F64P], C.c_int),
+        "astro_thermal_setup": ([vp, C.POINTER(ThermalPropsC), I32P, I32P], C.c_int),
+        "astro_thermal_soln_load": ([vp, C.c_int32, C.POINTER(ThermalStateC), F64P, F64P, I32P], C.c_int),
+        "astro_thermal_scale_mpc": ([vp, F64P, F64P], C.c_int),
+        "astro_thermal_constraint_load": ([vp, F64P, F64P], C.c_int),
+        "astro_thermal_heat_gen": ([vp, C.c_double, I32P, C.c_int32, F64P], C.c_int),
+        "astro_thermal_solve": ([vp, F64P, F64P, C.c_double, C.c_int32, C.POINTER(SolveStatsC)], C.c_int),
         "astro_panels_factor": ([vp, C.c_int32, C.POINTER(PanelsInfoC)], C.c_int),
         "astro_panels_solve": ([vp, C.c_int32, F64P, F64P, C.POINTER(PanelsInfoC)], C.c_int),
         "astro_panels_solve_batched": ([vp, C.c_int32, F64P, F64P, C.POINTER(PanelsInfoC)], C.c_int),
@@ -353,6 +398,53 @@ class AstroGPU:
         self._check(rc, allow=(7,) if allow_maxit else ())
         return u, st
 
+    # -- thermal path ---------------------------------------------------------------------------
+    def thermal_setup(self, props):
+        ms, md = C.c_int32(), C.c_int32()
+        self._thermal_props = props
+        self._check(self.L.astro_thermal_setup(self.h, C.byref(props), C.byref(ms), C.byref(md)))
+        self.therm_mat_size, self.therm_mpc_dim = ms.value, md.value
+        return ms.value, md.value
+
+    def getThermalSolnLoad(self, buildMat=1, state=None, thermal_load=None, export=True):
+        """(thermal load in rank order, CSR values, CSR columns) of getThermalSolnLoad."""
+        N = self.model.num_nodes
+        load = np.zeros(N) if thermal_load is None else thermal_load
+        mat = cols = None
+        if buildMat == 1 and export:
+            mat, cols = np.zeros(self.therm_mat_size), np.zeros(self.therm_mat_size, np.int32)
+        self._check(self.L.astro_thermal_soln_load(self.h, int(buildMat), C.byref(state) if state is not None else None,
+                                                   _d(load), _d(mat) if mat is not None else None,
+                                                   _i(cols) if cols is not None else None))
+        return load, mat, cols
+
+    def scaleThermalMPC(self):
+        k = max(self._thermal_props.num_mpc, 1)
+        mm = np.zeros(max(int(self._thermal_props.mpc_range[k]) if self._thermal_props.num_mpc else 1, 1))
+        mr = np.zeros(k)
+        self._check(self.L.astro_thermal_scale_mpc(self.h, _d(mm), _d(mr)))
+        return mm, mr
+
+    def getThermalConstraintLoad(self, node_temp=None, thermal_load=None):
+        load = np.zeros(self.model.num_nodes) if thermal_load is None else thermal_load
+        self._check(self.L.astro_thermal_constraint_load(self.h, None if node_temp is None else _d(_f64(node_temp)),
+                                                         _d(load)))
+        return load
+
+    def thermal_heat_gen(self, q, elements=None, thermal_load=None):
+        load = np.zeros(self.model.num_nodes) if thermal_load is None else thermal_load
+        els = None if elements is None else _i32(elements)
+        self._check(self.L.astro_thermal_heat_gen(self.h, float(q), None if els is None else _i(els),
+                                                  0 if els is None else len(els), _d(load)))
+        return load
+
+    def thermal_solve(self, rhs, dtemp0=None, rtol=1e-12, max_iters=100000):
+        x = np.zeros(self.model.num_nodes) if dtemp0 is None else _f64(dtemp0).copy()
+        st = SolveStatsC()
+        self._check(self.L.astro_thermal_solve(self.h, _d(_f64(rhs)), _d(x), float(rtol), int(max_iters),
+                                               C.byref(st)))
+        return x, st
+
     def panels_factor(self, cluster_size=0):
         """Band LDL^T of K + C^T C of every panel (connected component) in one launch."""
         info = PanelsInfoC()
@@ -555,6 +647,7 @@ class AstroGPU:
 
 
 __all__ = ["AstroGPU", "AstroError", "load_library", "make_state", "AstroStateC", "SOLVER_GMRES_JACOBI_FP64",
+           "thermal_props", "thermal_state",
            "SOLVER_FGMRES_MIXED", "SOLVER_FGMRES_LEARNED", "PrecondC", "precond_init", "PRECOND_MAX_DEGREE"]
 
 

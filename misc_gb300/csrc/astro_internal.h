@@ -79,6 +79,10 @@ struct astro_ctx {
     std::vector<int> etype, esec;
     std::vector<double> elMat;  // per element materialElastic(9) (solids)
     std::vector<double> elDensity;  // per element materialDensity (solids)
+    std::vector<int> elMatId;       // per element material (solids, 1-based)
+    std::vector<int> layMat;        // per layup layer material (shells, 1-based)
+    // thermal path (thermal.cu), opaque
+    void *thermal = nullptr;
     std::vector<double> secABD, secMass;  // per section ABD(9,9), sMass(6,6) (shells)
     std::vector<double> secOrient;        // per section 3x3 column-major
     std::vector<double> elThickness;      // per element total shell thickness (complex step / loads)
@@ -170,6 +174,7 @@ int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d
 int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln,
                                 const double *d_intRhs);                                           // elem_shell4.cu
 void panels_release(astro_ctx *ctx);                                         // panels.cu
+void thermal_release(astro_ctx *ctx);                                        // thermal.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu
 int export_csr_dev(astro_ctx *ctx, cudaStream_t s, double *d_mat, int *d_cols);  // assemble.cu
 double bsr_absmax(astro_ctx *ctx, int *status, int kind);                   // assemble.cu

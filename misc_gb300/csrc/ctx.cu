@@ -59,6 +59,7 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 static void free_all(astro_ctx *c) {
     krylov_release(c);
     panels_release(c);
+    thermal_release(c);
     if (c->asmExec) cudaGraphExecDestroy(c->asmExec);
     if (c->asmGraph) cudaGraphDestroy(c->asmGraph);
     c->asmExec = nullptr;
@@ -165,6 +166,7 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
     if (ctx->hasSolid) {
         ctx->elMat.resize(9 * (size_t)P.E);
         ctx->elDensity.assign((size_t)P.E, 0.0);
+        ctx->elMatId.assign((size_t)P.E, 0);
         std::vector<double> orientEl(9 * (size_t)P.E);
         for (int e = 0; e < P.E; ++e) {
             int s = ctx->esec[e];
@@ -172,6 +174,7 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
             if (mat < 1 || mat > m->num_materials) return fail(ASTRO_ERR_ARG, "section material out of range");
             for (int k = 0; k < 9; ++k) ctx->elMat[9 * (size_t)e + k] = m->material_elastic[9 * (size_t)(mat - 1) + k];
             if (m->material_density) ctx->elDensity[e] = m->material_density[mat - 1];
+            ctx->elMatId[e] = mat;
             // elastic-modulus design variables: eProps(c) += coef * d (r_getMaterialStiffness)
             if (m->num_dvars > 0)
                 for (int q = m->el_to_d_range[e]; q < m->el_to_d_range[e + 1]; ++q) {

@@ -44,6 +44,7 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
     for (int s = 0; s <= S; ++s) lr[s] = m->sec_layup_range[s];
     const int NL = lr[S];
     std::vector<LayerDev> lay(std::max(NL, 1));
+    ctx->layMat.assign(m->layup_mat_id, m->layup_mat_id + NL);
     for (int l = 0; l < NL; ++l) {
         const int mat = m->layup_mat_id[l];
         if (mat < 1 || mat > m->num_materials) return set_err(ctx, ASTRO_ERR_ARG, "layup material out of range");

@@ -60,6 +60,9 @@ def _lib():
         L.orc_update_external_rhs.argtypes = [C.c_void_p, F64P, F64P, F64P]
         L.orc_update_internal_soln.argtypes = [C.c_void_p, F64P, F64P, F64P, F64P]
         L.orc_surface_load.argtypes = [C.c_void_p, C.c_int, I32P, I32P, F64P, C.c_double, F64P]
+        L.orc_thermal_soln_load.restype = C.c_int
+        L.orc_thermal_soln_load.argtypes = [C.c_void_p, F64P, F64P, C.c_int, F64P, F64P, F64P, C.c_int, C.c_double,
+                                            C.c_double, F64P, F64P, I32P, I32P]
         L.orc_body_load.restype = C.c_int
         L.orc_body_load.argtypes = [C.c_void_p, C.c_int, F64P, C.c_int, I32P, C.c_void_p, F64P]
         _LIB = L
@@ -195,6 +198,104 @@ class Oracle:
                                   C.byref(state) if state is not None else None, _d(load))
         assert rc == 0
         return load
+
+    # -- thermal path (restated in oracle_api.cpp: orc_thermal_soln_load; the constraint
+    #    bookkeeping below in numpy) ----------------------------------------------------------
+    def thermal_soln_load(self, cond, spec_heat, build_mat=1, temp=None, prev_temp=None, prev_tdot=None, dynamic=0,
+                          gamma=0.5, del_t=0.0, load=None):
+        """getThermalSolnLoad: (thermal load in rank order, thermMat, thermMatCols, thermMatRange)."""
+        N = self.model.num_nodes
+        load = np.zeros(N) if load is None else load
+        cond = np.ascontiguousarray(cond, np.float64).reshape(-1)
+        sh = np.ascontiguousarray(spec_heat, np.float64)
+        rng = np.zeros(N + 1, np.int32)
+        scratch = np.zeros(N)
+        opt = lambda a: None if a is None else _d(np.ascontiguousarray(a, np.float64))
+        keep = [np.ascontiguousarray(a, np.float64) if a is not None else None for a in (temp, prev_temp, prev_tdot)]
+        rc = self.L.orc_thermal_soln_load(self.h, _d(cond), _d(sh), 0, opt(keep[0]), opt(keep[1]), opt(keep[2]), 0,
+                                          gamma, del_t, _d(scratch), None, None, _i(rng))
+        assert rc == 0
+        mat = np.zeros(max(int(rng[N]), 1))
+        cols = np.zeros(max(int(rng[N]), 1), np.int32)
+        rc = self.L.orc_thermal_soln_load(self.h, _d(cond), _d(sh), build_mat, opt(keep[0]), opt(keep[1]),
+                                          opt(keep[2]), dynamic, gamma, del_t, _d(load), _d(mat), _i(cols), None)
+        assert rc == 0
+        return load, mat[:rng[N]], cols[:rng[N]], rng
+
+    def thermal_mpc(self, mpc_range, mpc_node, mpc_coef, mpc_rhs):
+        """buildThermalMPC (Working/AStrO_bookKeeping.f90:614-752) for expanded equations: rows of
+        (1-based rank column, coefficient), duplicate columns skipped (slot stays 0)."""
+        rows = []
+        for r in range(len(mpc_range) - 1):
+            t0, t1 = mpc_range[r], mpc_range[r + 1]
+            cols, vals = [0] * (t1 - t0), [0.0] * (t1 - t0)
+            for t in range(t0, t1):
+                c = int(self.current_rank[mpc_node[t] - 1])
+                for s_ in range(t1 - t0):
+                    if cols[s_] == 0:
+                        cols[s_], vals[s_] = c, float(mpc_coef[t])
+                        break
+                    if cols[s_] == c:
+                        break
+            rows.append((cols, vals, float(mpc_rhs[r])))
+        return rows
+
+    @staticmethod
+    def scale_thermal_mpc(therm_mat, rows):
+        """scaleThermalMPC (Working/AStrO_commandFunctions.f90:230-258)."""
+        mx = float(np.abs(therm_mat).max()) if len(therm_mat) else 0.0
+        out = []
+        for cols, vals, rhs in rows:
+            mag = np.sqrt(sum(v * v for v in vals))
+            out.append((cols, [100.0 * mx * ((1.0 / mag) * v) for v in vals], 100.0 * mx * ((1.0 / mag) * rhs)))
+        return out
+
+    @staticmethod
+    def thermal_constraint_load(rows, temp, load):
+        """getThermalConstraintLoad (:197-228), node vectors in rank order."""
+        for cols, vals, rhs in rows:
+            v = rhs
+            for c, k in zip(cols, vals):
+                if c:
+                    v = v - k * temp[c - 1]
+            for c, k in zip(cols, vals):
+                if c:
+                    load[c - 1] += k * v
+        return load
+
+    def thermal_heat_gen(self, q, elements=None, load=None):
+        """getThermalAppliedLoad's bodyHeatGen branch (:96-139): r_getElBodyForce with the heat
+        generation as the first body-force component; component-1 entries to the element nodes'
+        thermal DOF (rank order)."""
+        N = self.model.num_nodes
+        load = np.zeros(N) if load is None else load
+        el = self.body_load(0, [q, 0, 0, 0, 0, 0], elements=elements)
+        for nd in range(1, N + 1):
+            load[self.current_rank[nd - 1] - 1] += el[self.n_dof_index[nd - 1, 0] - 1]
+        return load
+
+    def thermal_system(self, cond, spec_heat, mpc=None):
+        """(A = K_T + C^T C over ranks, b = constraint load at zero temperature, rows) of a steady
+        thermal step from the zero state."""
+        import scipy.sparse as sp
+        N = self.model.num_nodes
+        load, mat, cols, rng = self.thermal_soln_load(cond, spec_heat, 1)
+        K = sp.csr_matrix((mat, cols - 1, rng), shape=(N, N))
+        b = np.zeros(N)
+        rows = []
+        if mpc is not None:
+            rows = self.scale_thermal_mpc(mat, self.thermal_mpc(*mpc))
+            r_, c_, v_ = [], [], []
+            for i, (cols_, vals, _) in enumerate(rows):
+                for c, k in zip(cols_, vals):
+                    if c:
+                        r_.append(i)
+                        c_.append(c - 1)
+                        v_.append(k)
+            Cm = sp.csr_matrix((v_, (r_, c_)), shape=(len(rows), N))
+            K = K + Cm.T @ Cm
+            self.thermal_constraint_load(rows, np.zeros(N), b)
+        return K.tocsr(), b, rows
 
     def applied_load(self, load=None):
         """Consistent surface load of the model's faces plus its point loads."""

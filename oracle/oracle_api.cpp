@@ -999,4 +999,185 @@ void orc_surface_load(const OracleCtx *c, int nfaces, const int32_t *faceEl, con
     }
 }
 
+// ---- thermal path ---------------------------------------------------------------------------
+// Thermal material data are not part of astro_model: materialThermCond(6, num_materials)
+// (k11 k22 k33 k12 k13 k23) and materialSpecHeat(num_materials) are passed beside it.
+
+// r_getMaterialThermCond (Working/AStrO_r_designPropertyFunctions.f90:129-161) for solids and
+// r_getShellThermCond (:527-600) for shells (sum over layers of the layer thickness times the
+// layer conductivity rotated by the layup angle); thisSH as r_getElRtm selects it
+// (Working/AStrO_r_elementEqns.f90:2143-2149): density x specHeat for solids, r_getShellSpecHeat
+// (designProp :602-644: sum of thickness x density x specHeat) for shells.
+static void therm_props(const astro_model *m, const double *cond, const double *sh, int el, double tc[3][3],
+                        double &thisSH) {
+    DPert<double> p;
+    const int et = m->element_type[el - 1], sec = m->element_section[el - 1];
+    auto fill = [](double t[3][3], const double *v) {
+        t[0][0] = v[0];
+        t[1][1] = v[1];
+        t[2][2] = v[2];
+        t[0][1] = t[1][0] = v[3];
+        t[0][2] = t[2][0] = v[4];
+        t[1][2] = t[2][1] = v[5];
+    };
+    if (et != 41) {
+        const int mat = m->section_mat_id[sec - 1];
+        fill(tc, cond + 6 * (mat - 1));
+        thisSH = m->material_density[mat - 1] * sh[mat - 1];
+        return;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) tc[i][j] = 0.0;
+    thisSH = 0.0;
+    for (int i1 = m->sec_layup_range[sec - 1] + 1, ln = 1; i1 <= m->sec_layup_range[sec]; ++i1, ++ln) {
+        const int mat = m->layup_mat_id[i1 - 1];
+        double tl[3][3], al[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1.0}}, pr[3][3], tg[3][3];
+        fill(tl, cond + 6 * (mat - 1));
+        const double lt = layer_thickness(m, el, ln, i1, p), ang = m->layup_angle[i1 - 1];
+        al[0][0] = t_cos(ang);
+        al[1][0] = t_sin(ang);
+        al[0][1] = -al[1][0];
+        al[1][1] = al[0][0];
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                pr[a][b] = 0.0;
+                for (int k = 0; k < 3; ++k) pr[a][b] = pr[a][b] + tl[a][k] * al[b][k];
+            }
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) {
+                tg[a][b] = 0.0;
+                for (int k = 0; k < 3; ++k) tg[a][b] = tg[a][b] + al[a][k] * pr[k][b];
+            }
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) tc[a][b] = tc[a][b] + lt * tg[a][b];
+        thisSH = thisSH + lt * m->material_density[mat - 1] * sh[mat - 1];
+    }
+}
+
+// getThermalSolnLoad (Working/AStrO_commandFunctions.f90:16-72) with r_getElRt / r_getElRtk /
+// r_getElRtm (Working/AStrO_r_elementEqns.f90:2062-2204): thermalLoad(rank) -= Rt, and for
+// buildMat the CSR thermMat over ranks with find-or-insert columns (0 = empty slot).  Node
+// vectors (temperature, previous temperature and rate) are in rank order, as nodeTemp.  The CSR
+// row ranges (thermMatRange: 1 + the node's neighbours, allocateThermalMat, bookKeeping
+// :413-441) are returned in range (0:numNodes) when non-null.
+int orc_thermal_soln_load(const OracleCtx *c, const double *cond, const double *sh, int buildMat,
+                          const double *nodeTemp, const double *prevTemp, const double *prevTdot, int dynamic,
+                          double gamma, double delT, double *thermalLoad, double *thermMat, int32_t *thermCols,
+                          int32_t *range) {
+    const astro_model *m = c->m;
+    const int N = c->numNodes;
+    std::vector<int> tr(N + 1, 0);
+    for (int i1 = 1; i1 <= N; ++i1) {
+        const int i3 = c->currentRank[i1 - 1];
+        tr[i3] = tr[i3] + 1;
+        for (int i4 = c->nCRange[i1 - 1] + 1; i4 <= c->nCRange[i1]; ++i4)
+            if (c->nodalConn[i4 - 1] != 0) tr[i3] = tr[i3] + 1;
+    }
+    for (int i1 = 2; i1 <= N; ++i1) tr[i1] += tr[i1 - 1];
+    if (range)
+        for (int i = 0; i <= N; ++i) range[i] = tr[i];
+    if (buildMat == 1)
+        for (int i = 0; i < tr[N]; ++i) {
+            thermMat[i] = 0.0;
+            thermCols[i] = 0;
+        }
+    GState g;
+    DPert<double> p;
+    for (int el = 1; el <= c->numEls; ++el) {
+        ElemData<double> e;
+        if (t_getElementData(e, m, c->nDofIndex.data(), c->intVecRange.data(), el, g, p) != 0) return 1;
+        double tc[3][3], thisSH;
+        therm_props(m, cond, sh, el, tc, thisSH);
+        const int nn = e.numNds;
+        double temp[10] = {0}, pT[10] = {0}, pTd[10] = {0};
+        for (int i = 0; i < nn; ++i) {
+            const int rk = c->currentRank[m->element_list[8 * (el - 1) + i] - 1];
+            temp[i] = nodeTemp ? nodeTemp[rk - 1] : 0.0;
+            pT[i] = prevTemp ? prevTemp[rk - 1] : 0.0;
+            pTd[i] = prevTdot ? prevTdot[rk - 1] : 0.0;
+        }
+        double Rt[10] = {0}, dRdt[10][10] = {{0}};
+        // r_getElRtk
+        for (int i1 = 1; i1 <= e.numIntPts; ++i1) {
+            A1<double, 11> Nvec;
+            A2<double, 11, 3> Nx;
+            double detJ;
+            t_getIntPtData(Nvec, Nx, detJ, e.locNds, e.intPts[i1 - 1], e.eType, nn);
+            double Tx[3] = {0, 0, 0}, q[3] = {0, 0, 0};
+            for (int i2 = 1; i2 <= nn; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3) Tx[i3 - 1] = Tx[i3 - 1] + Nx(i2, i3) * temp[i2 - 1];
+            for (int i2 = 0; i2 < 3; ++i2)
+                for (int i3 = 0; i3 < 3; ++i3) q[i2] = q[i2] + tc[i2][i3] * Tx[i3];
+            const double wd = detJ * e.ipWt[i1 - 1];
+            for (int k = 0; k < 3; ++k) q[k] = wd * q[k];
+            for (int i2 = 1; i2 <= nn; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3) Rt[i2 - 1] = Rt[i2 - 1] + Nx(i2, i3) * q[i3 - 1];
+            if (buildMat == 1) {
+                double kNx[11][3] = {{0}};
+                for (int i2 = 1; i2 <= nn; ++i2)
+                    for (int i3 = 1; i3 <= 3; ++i3)
+                        for (int i4 = 1; i4 <= 3; ++i4) kNx[i2 - 1][i3 - 1] = kNx[i2 - 1][i3 - 1] + Nx(i2, i4) * tc[i4 - 1][i3 - 1];
+                for (int i2 = 0; i2 < nn; ++i2)
+                    for (int k = 0; k < 3; ++k) kNx[i2][k] = wd * kNx[i2][k];
+                for (int i2 = 1; i2 <= nn; ++i2)
+                    for (int i3 = 1; i3 <= nn; ++i3)
+                        for (int i4 = 1; i4 <= 3; ++i4) dRdt[i2 - 1][i3 - 1] = dRdt[i2 - 1][i3 - 1] + Nx(i2, i4) * kNx[i3 - 1][i4 - 1];
+            }
+        }
+        if (dynamic == 1) {
+            // r_getElRtm with Tdot from the generalised trapezoid rule
+            double Td[10];
+            for (int i1 = 0; i1 < nn; ++i1)
+                Td[i1] = (1.0 / gamma) * ((1.0 / delT) * (temp[i1] - pT[i1]) - 1.0 * (1.0 - gamma) * pTd[i1]);
+            double Rtm[10] = {0}, dRdTd[10][10] = {{0}};
+            for (int i1 = 1; i1 <= e.numIntPts; ++i1) {
+                A1<double, 11> Nvec;
+                A2<double, 11, 3> Nx;
+                double detJ;
+                t_getIntPtData(Nvec, Nx, detJ, e.locNds, e.intPts[i1 - 1], e.eType, nn);
+                double pt = 0.0;
+                for (int i2 = 1; i2 <= nn; ++i2) pt = pt + Td[i2 - 1] * Nvec(i2);
+                pt = detJ * e.ipWt[i1 - 1] * thisSH * pt;
+                for (int i2 = 1; i2 <= nn; ++i2) Rtm[i2 - 1] = Rtm[i2 - 1] + pt * Nvec(i2);
+                if (buildMat == 1) {
+                    double cpN[11];
+                    for (int i2 = 1; i2 <= 11; ++i2) cpN[i2 - 1] = detJ * e.ipWt[i1 - 1] * thisSH * Nvec(i2);
+                    for (int i2 = 1; i2 <= nn; ++i2)
+                        for (int i3 = 1; i3 <= nn; ++i3) dRdTd[i2 - 1][i3 - 1] = dRdTd[i2 - 1][i3 - 1] + Nvec(i2) * cpN[i3 - 1];
+                }
+            }
+            for (int k = 0; k < nn; ++k) Rt[k] = Rt[k] + Rtm[k];
+            if (buildMat == 1)
+                for (int a = 0; a < nn; ++a)
+                    for (int b = 0; b < nn; ++b) dRdt[a][b] = dRdt[a][b] + (1.0 / (gamma * delT)) * dRdTd[a][b];
+        }
+        for (int i2 = 1; i2 <= nn; ++i2) {
+            const int i3 = c->currentRank[m->element_list[8 * (el - 1) + i2 - 1] - 1];
+            thermalLoad[i3 - 1] = thermalLoad[i3 - 1] - Rt[i2 - 1];
+        }
+        if (buildMat == 1)
+            for (int i2 = 1; i2 <= nn; ++i2) {
+                const int Kgi = c->currentRank[m->element_list[8 * (el - 1) + i2 - 1] - 1];
+                for (int i3 = 1; i3 <= nn; ++i3) {
+                    const int Kgj = c->currentRank[m->element_list[8 * (el - 1) + i3 - 1] - 1];
+                    int i4 = tr[Kgi - 1] + 1;
+                    int inserted = 0;
+                    while (inserted == 0 && i4 <= tr[Kgi]) {
+                        const int i6 = thermCols[i4 - 1];
+                        if (i6 == 0) {
+                            thermMat[i4 - 1] = dRdt[i2 - 1][i3 - 1];
+                            thermCols[i4 - 1] = Kgj;
+                            inserted = 1;
+                        } else if (i6 == Kgj) {
+                            thermMat[i4 - 1] = thermMat[i4 - 1] + dRdt[i2 - 1][i3 - 1];
+                            inserted = 1;
+                        }
+                        i4 = i4 + 1;
+                    }
+                }
+            }
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -357,3 +357,38 @@ def test_body_load_totals():
     s = op.body_load(1, [0.0, 0.0, -9.81, 0.0, 0.0, 0.0]).reshape(6, -1).sum(axis=1)
     assert np.isclose(s[2], -9.81 * 2700.0 * 0.03 * 2.0, rtol=1e-12)
     assert np.allclose(s[[0, 1, 3, 4, 5]], 0.0, atol=1e-9)
+
+
+def test_thermal_conduction_kats():
+    """Thermal path of the oracle: steady conduction through a brick bar with the end faces held
+    at 20 and 80 gives the linear profile (penalty constraints: 1e-4) and the heat flux k A dT/dx
+    through the end; uniform heating of the capacitance term gives rho c V Tdot; heat generation
+    integrates to q V (bricks) and q t A (shells); the shell conductivity matrix annihilates a
+    uniform temperature."""
+    import scipy.sparse.linalg as spla
+    m = M.hex_block(6, 2, 2, lx=3.0, ly=1.0, lz=1.0, jitter=0.0)
+    o = Oracle(m)
+    nm = len(m.material_density)
+    k = 45.0
+    cond, sh = np.tile([k, k, k, 0, 0, 0], (nm, 1)), np.full(nm, 460.0)
+    X = m.node_list
+    left = np.nonzero(X[:, 0] == 0)[0] + 1
+    right = np.nonzero(np.isclose(X[:, 0], 3.0))[0] + 1
+    nodes = np.concatenate([left, right])
+    rhs = np.concatenate([np.full(len(left), 20.0), np.full(len(right), 80.0)])
+    mpc = (np.arange(len(nodes) + 1), nodes, np.ones(len(nodes)), rhs)
+    A, b, _ = o.thermal_system(cond, sh, mpc)
+    T = spla.spsolve(A.tocsc(), b)
+    assert np.abs(T[o.current_rank - 1] - (20 + 60 * X[:, 0] / 3.0)).max() < 1e-4
+    load, *_ = o.thermal_soln_load(cond, sh, 0, temp=T)
+    assert abs(load[o.current_rank[left - 1] - 1].sum() - k * 1.0 * 20.0) < 1e-3
+    N = m.num_nodes
+    load2, *_ = o.thermal_soln_load(cond, sh, 0, temp=np.ones(N), prev_temp=np.zeros(N), prev_tdot=np.zeros(N),
+                                    dynamic=1, gamma=0.5, del_t=0.1)
+    assert np.isclose(-load2.sum(), 7800.0 * 460.0 * 3.0 * (1 / 0.5) * (1 / 0.1), rtol=1e-12)
+    assert np.isclose(o.thermal_heat_gen(5.0).sum(), 15.0, rtol=1e-12)
+    p = M.plate_shell(nx=4, ny=2, lx=2.0, ly=1.0, t=0.02)
+    op = Oracle(p)
+    assert np.isclose(op.thermal_heat_gen(3.0).sum(), 3.0 * 2.0 * 0.02, rtol=1e-12)
+    Ap, _, _ = op.thermal_system([[k, k, k, 0, 0, 0]], [900.0])
+    assert np.abs(Ap @ np.ones(p.num_nodes)).max() < 1e-12 * abs(Ap).max()
