@@ -57,6 +57,7 @@ def _parse():
     p.add_argument("--no-fp64", action="store_true", help="learned evaluation without the FP64 comparator")
     p.add_argument("--eval-nx", type=int, default=96)
     p.add_argument("--panels", type=int, default=512, help="panels of the batched-panel leg (0: skip it)")
+    p.add_argument("--newmark-steps", type=int, default=200, help="time steps of the Newmark leg (0: skip it)")
     p.add_argument("--panels-only", action="store_true", help="only the batched-panel leg")
     p.add_argument("--panels-cluster", type=int, default=0, help="cluster size (0: autotuned over 2, 4, 8)")
     return p.parse_args()
@@ -336,6 +337,8 @@ def run_ours(a):
         line["learned_solve"] = _learned_eval(a)
     if a.panels > 0 and rank == 0:
         line["batched_panels"] = _panels_eval(a)
+    if a.newmark_steps > 0 and rank == 0:
+        line["newmark"] = _newmark_eval(a)
     # CPU baseline: oracle, 1 core, bounded sample
     if rank == 0:
         rate, dt = _oracle_rate(m, 1024, 1)
@@ -482,6 +485,43 @@ def _panels_eval(a):
                              "frac": (2 * fma_f / fac / 1e12 / pk) if pk else None,
                              "peak_source": "measured: torch.matmul float64 4096^3 (cuBLAS DGEMM) on this GPU",
                              "solve_fma": fma_s, "solve_tflops": 2 * fma_s / sol / 1e12}}
+    del g
+    gc.collect()
+    return out
+
+
+def _newmark_eval(a):
+    """Implicit Newmark dynamics on the config-5 plate: 128x128 shell4 on 1 x 1 m, t = 0.01,
+    E = 7e10, nu = 0.33, rho = 2700, simply supported edges (w = 0), beta 0.25, gamma 0.5,
+    dt = 1e-5, point force 100 sin(2 pi 500 t) N at the centre; a.newmark_steps steps of the
+    device time loop per method (the second run timed; CUDA events), each step solved to 1e-10:
+    FP64 Jacobi-GMRES and the learned FGMRES (degree 8, ratio 100)."""
+    import gc
+    from misc_gb300 import model as M
+    from misc_gb300.astro import SOLVER_FGMRES_LEARNED, AstroGPU, precond_init
+    gc.collect()
+    nx = 128
+    m = M.plate_shell(nx=nx, ny=nx, lx=1.0, ly=1.0, t=0.01, E=7e10, nu=0.33, rho=2700.0, pressure=0.0, clamp="ss",
+                      y0=0.0)
+    g = AstroGPU(m)
+    centre = (nx // 2) * (nx + 1) + nx // 2 + 1
+    pattern = np.zeros(g.n)
+    pattern[g.n_dof_index[centre - 1, 2] - 1] = 1.0
+    steps, dt = a.newmark_steps, 1e-5
+    amp = 100.0 * np.sin(2 * np.pi * 500.0 * dt * np.arange(1, steps + 1))
+    out = {"workload": "128x128 shell4 plate (99,846 DOF), simply supported, dt 1e-5, centre point force "
+                       "100 sin(2 pi 500 t) N", "steps": steps, "rtol": 1e-10}
+    res = {}
+    for name, kw in (("gmres_fp64", {}), ("fgmres_learned", dict(method=SOLVER_FGMRES_LEARNED,
+                                                                  precond=precond_init(8, 100.0, 6)))):
+        for _ in range(2):
+            u, v, acc, iu, hist, st = g.newmark_run(steps, dt, 0.25, 0.5, pattern, amp, rtol=1e-10, history=False, **kw)
+        res[name] = u
+        out[name] = {"ms_per_step": 1e3 * st.seconds / steps, "seconds": st.seconds, "inner_iterations": st.iterations,
+                     "refinements": st.refinements, "status": st.status}
+    out["speedup_learned_vs_fp64"] = out["gmres_fp64"]["ms_per_step"] / out["fgmres_learned"]["ms_per_step"]
+    out["rel_diff_final_disp"] = float(np.linalg.norm(res["fgmres_learned"] - res["gmres_fp64"]) /
+                                       max(np.linalg.norm(res["gmres_fp64"]), 1e-300))
     del g
     gc.collect()
     return out
