@@ -259,16 +259,16 @@ int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el,
 /* Body loads: the bodyForce / gravitational / centrifugal branch of getElasticAppliedLoad
  * (Working/AStrO_commandFunctions.f90:393-441) with r_getElBodyForce and r_getElCentAcc
  * (Working/AStrO_r_elementEqns.f90:1801-1921), added into elastic_load[n] (reference numbering).
- *   kind ASTRO_BODY_FORCE (0): vals[0..5] = force per unit volume (per unit area x thickness for
- *        shells); bricks only;
+ *   kind ASTRO_BODY_FORCE (0): vals[0..5] = force per unit volume (per unit volume of the section
+ *        for shells: times the section thickness);
  *   kind ASTRO_BODY_GRAVITY (1): vals[0..5] = acceleration (translational, then rotational), the
- *        load being the element mass residual for that acceleration at every node; bricks over any
- *        element list, shells over the whole mesh (elements NULL or all of them);
+ *        load being the element mass residual for that acceleration at every node;
  *   kind ASTRO_BODY_CENTRIFUGAL (2): vals = axis point(3), axis direction(3), angular velocity,
- *        the acceleration evaluated at each element's displaced centroid; bricks only.
- * elements: 1-based element numbers (count of them), or NULL for every element.  state: the
- * displacement (centrifugal centroid; shell orientation), may be NULL.  Unsupported element /
- * kind combinations and meshes mixing shells and bricks return ASTRO_ERR_UNSUPPORTED. */
+ *        the acceleration evaluated at each element's displaced centroid.
+ * Bricks and shells, any element list.  elements: 1-based element numbers (count of them; an
+ * element listed twice adds twice), or NULL for every element.  state: the displacement
+ * (centrifugal centroid; shell frame), may be NULL.  Meshes mixing shells and bricks return
+ * ASTRO_ERR_UNSUPPORTED. */
 #define ASTRO_BODY_FORCE 0
 #define ASTRO_BODY_GRAVITY 1
 #define ASTRO_BODY_CENTRIFUGAL 2

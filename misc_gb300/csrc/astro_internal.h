@@ -170,6 +170,8 @@ struct ShellDevState {
 int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &s, double *d_loadInt, double *d_intLoad,
                            int buildMat, double *d_ke, double *d_ru, bool sync = true);  // elem_shell4.cu
 int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // elem_shell4.cu
+int shell4_residual_list(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
+                         double *d_loadInt);                                 // elem_shell4.cu
 int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt);          // elem_shell4.cu
 int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln,
                                 const double *d_intRhs);                                           // elem_shell4.cu

@@ -150,6 +150,14 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
     return cuda_check(ctx, e, "shell pipeline");
 }
 
+// The pipeline over a colour-grouped element list (device list d_els, colour c covering
+// ptr[c] .. ptr[c+1]), residual only, into d_loadInt (load -= Ru).
+int shell4_residual_list(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
+                         double *d_loadInt) {
+    return shell_pipeline(ctx, st, d_els, ptr, dptr<ShellProps>(ctx->d_secABD), kShellRt3, d_loadInt, nullptr, 0,
+                          nullptr, nullptr, nullptr, nullptr);
+}
+
 int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_loadInt, double *d_intLoad, int buildMat,
                            double *d_ke, double *d_ru, bool sync) {
     const bool toK = buildMat && !d_ke;

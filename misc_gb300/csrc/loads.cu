@@ -5,14 +5,20 @@
 //           share a node, so the additions need no atomics and have a fixed order); the nodal
 //           forces are b or rho a (the brick's consistent mass times a uniform acceleration)
 //           times the integral of N over the element;
-//   shells: the gravitational load is the element mass residual for a uniform acceleration
-//           (r_getElRum with the static frame of the element's mean rotation), which the shell
-//           pipeline evaluates as the Newmark mass term: run alone (massOnly) with a
-//           previous-acceleration field that makes the Newmark acceleration the imposed one.
+//   shells: body force: one thread per element, t b times the integral of N over the element in
+//           its frame (all six nodal components); gravitational and centrifugal loads: the
+//           element mass residual for the acceleration (r_getElRum with the static frame of the
+//           element's mean rotation), which the shell pipeline evaluates as the Newmark mass term:
+//           run alone (massOnly) with a previous-acceleration field that makes the Newmark
+//           acceleration the imposed one.  The centrifugal acceleration differs per element; it
+//           goes into the field at the element's nodes one colour at a time (a colour's elements
+//           share no node).  An element listed k times is evaluated in k passes.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
 #include "astro_internal.h"
+#include "shell_props.cuh"
 
 namespace {
 
@@ -81,6 +87,96 @@ __global__ void k_hex_body(int kind, BodyVals bv, const int *__restrict__ els, i
 }
 
 // out -= b (the pipeline's output is the load -Ru)
+// centripetal acceleration omega^2 (pos - (pos . axis) axis) at centroid c (r_getElCentAcc)
+__device__ __forceinline__ void cent_acc(const BodyVals &bv, const double c[3], double a[3]) {
+    double pos[3], unit[3];
+    for (int d = 0; d < 3; ++d) pos[d] = c[d] - bv.v[d];
+    double dp = bv.v[3] * bv.v[3] + bv.v[4] * bv.v[4] + bv.v[5] * bv.v[5];
+    const double mag = sqrt(dp);
+    for (int d = 0; d < 3; ++d) unit[d] = (1.0 / mag) * bv.v[3 + d];
+    dp = pos[0] * unit[0] + pos[1] * unit[1] + pos[2] * unit[2];
+    for (int d = 0; d < 3; ++d) a[d] = bv.v[6] * bv.v[6] * (pos[d] - dp * unit[d]);
+}
+
+// shell body force: t b_c times the integral of N_a over the element (frame of its properties)
+__global__ void k_shell_body(BodyVals bv, const int *__restrict__ els, int cnt, const double *__restrict__ nodes,
+                             const int *__restrict__ elist, const int *__restrict__ rank,
+                             const ShellProps *__restrict__ props, const int *__restrict__ esec,
+                             const int *__restrict__ layRange, const LayerDev *__restrict__ lay,
+                             const int *__restrict__ e2dR, const int *__restrict__ e2d, const double *__restrict__ e2c,
+                             const int *__restrict__ dcat, const int *__restrict__ dlay, const double *__restrict__ dval,
+                             const double *__restrict__ mult, double *__restrict__ load) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt) return;
+    const int e = els[i];
+    double Xl[4][3];
+    int r[4];
+    for (int a = 0; a < 4; ++a) {
+        const int nd = elist[8 * (size_t)e + a] - 1;
+        r[a] = rank[nd] - 1;
+        for (int k = 0; k < 3; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < 3; ++j) s += props[e].orient[3 * k + j] * nodes[3 * (size_t)nd + j];
+            Xl[a][k] = s;
+        }
+    }
+    // section thickness with the layer-thickness design variables
+    const int sec = esec[e];
+    double t = 0.0;
+    for (int li = layRange[sec - 1], ln = 1; li < layRange[sec]; ++li, ++ln) {
+        double tl = lay[li].t;
+        if (e2dR)
+            for (int q = e2dR[e]; q < e2dR[e + 1]; ++q) {
+                const int d = e2d[q] - 1;
+                if (dcat[d] == ASTRO_DCAT_LAYUP_THICKNESS && dlay[d] == ln) tl = tl + e2c[q] * dval[d];
+            }
+        t = t + tl;
+    }
+    const double g = 1.0 / sqrt(3.0);
+    const double sx[4] = {-1.0, 1.0, 1.0, -1.0}, sy[4] = {-1.0, -1.0, 1.0, 1.0};
+    double w[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int gp = 0; gp < 4; ++gp) {
+        const double s1 = (gp & 1) ? g : -g, s2 = (gp & 2) ? g : -g;
+        double J[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, N[4];
+        for (int a = 0; a < 4; ++a) {
+            N[a] = 0.25 * (1.0 + sx[a] * s1) * (1.0 + sy[a] * s2);
+            const double d0 = 0.25 * sx[a] * (1.0 + sy[a] * s2), d1 = 0.25 * sy[a] * (1.0 + sx[a] * s1);
+            for (int k = 0; k < 2; ++k) {
+                J[k][0] += Xl[a][k] * d0;
+                J[k][1] += Xl[a][k] * d1;
+            }
+        }
+        // dxds(3,3) = 1 and no thickness-direction parameter: det = J00 J11 - J01 J10
+        const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        for (int a = 0; a < 4; ++a) w[a] += N[a] * det;
+    }
+    for (int a = 0; a < 4; ++a)
+        for (int c = 0; c < 6; ++c) load[6 * (size_t)r[a] + c] += mult[i] * (t * (bv.v[c] * w[a]));
+}
+
+// centrifugal acceleration of each listed element (displaced centroid) into the previous-
+// acceleration field at its nodes, negated (the Newmark acceleration then equals it)
+__global__ void k_shell_cent_pacc(BodyVals bv, const int *__restrict__ els, int cnt, const double *__restrict__ nodes,
+                                  const int *__restrict__ elist, const int *__restrict__ rank,
+                                  const double *__restrict__ disp, double *__restrict__ pacc) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= cnt) return;
+    const int e = els[i];
+    int r[4];
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < 4; ++a) {
+        const int nd = elist[8 * (size_t)e + a] - 1;
+        r[a] = rank[nd] - 1;
+        for (int d = 0; d < 3; ++d) c[d] = c[d] + nodes[3 * (size_t)nd + d] + (disp ? disp[6 * (size_t)r[a] + d] : 0.0);
+    }
+    const double nnInv = 1.0 / 4.0;
+    for (int d = 0; d < 3; ++d) c[d] = nnInv * c[d];
+    double acc[3];
+    cent_acc(bv, c, acc);
+    for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 6; ++d) pacc[6 * (size_t)r[a] + d] = d < 3 ? -acc[d] : 0.0;
+}
+
 __global__ void k_sub(int n, const double *__restrict__ b, double *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] -= b[i];
@@ -98,16 +194,6 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
         for (int k = 0; k < count; ++k)
             if (elements[k] < 1 || elements[k] > P.E) return set_err(ctx, ASTRO_ERR_ARG, "element number out of range");
     if (elements && count == 0) return ASTRO_OK;
-    bool wholeMesh = true;
-    if (elements) {
-        std::vector<int> seen((size_t)P.E, 0);
-        for (int k = 0; k < count; ++k) ++seen[elements[k] - 1];
-        for (int e = 0; e < P.E && wholeMesh; ++e) wholeMesh = seen[e] == 1;
-    }
-    if (ctx->hasShell && (kind != 1 || !wholeMesh))
-        return set_err(ctx, ASTRO_ERR_UNSUPPORTED,
-                       "shell body loads: the gravitational load over the whole mesh (body-force and centrifugal "
-                       "loads of shells are not implemented)");
     struct Tmp {
         DevBuf ref, li, u, b, list, mult, den, pa, iu;
         ~Tmp() {
@@ -128,12 +214,14 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
         dev_free(h);
         if (rc) return rc;
     }
-    if (ctx->hasSolid) {
-        // the listed elements, colour by colour
-        // (an element listed twice adds its load twice)
-        std::vector<int> on((size_t)P.E, elements ? 0 : 1);
-        if (elements)
-            for (int k = 0; k < count; ++k) ++on[elements[k] - 1];
+    // the listed elements, colour by colour, with their multiplicity (an element listed twice
+    // adds its load twice)
+    std::vector<int> on((size_t)P.E, elements ? 0 : 1);
+    if (elements)
+        for (int k = 0; k < count; ++k) ++on[elements[k] - 1];
+    BodyVals bv;
+    for (int k = 0; k < 7; ++k) bv.v[k] = (kind == 2 || k < 6) ? vals[k] : 0.0;
+    if (ctx->hasSolid || kind == 0) {
         std::vector<int> list, ptr(1, 0);
         std::vector<double> mult;
         for (int col = 0; col < P.ncolors; ++col) {
@@ -146,25 +234,37 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
         }
         if (!list.empty()) {
             if ((rc = upload(ctx, T.list, list.data(), sizeof(int) * list.size())) ||
-                (rc = upload(ctx, T.mult, mult.data(), sizeof(double) * mult.size())) ||
+                (rc = upload(ctx, T.mult, mult.data(), sizeof(double) * mult.size())))
+                return rc;
+            if (ctx->hasSolid &&
                 (rc = upload(ctx, T.den, ctx->elDensity.data(), sizeof(double) * ctx->elDensity.size())))
                 return rc;
-            BodyVals bv;
-            for (int k = 0; k < 7; ++k) bv.v[k] = (kind == 2 || k < 6) ? vals[k] : 0.0;
+            const bool dv = ctx->numDvars > 0 && ctx->d_e2dR.p;
             for (int col = 0; col < P.ncolors; ++col) {
                 const int cnt = ptr[col + 1] - ptr[col];
                 if (!cnt) continue;
-                k_hex_body<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
-                    kind, bv, dptr<int>(T.list) + ptr[col], cnt, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist),
-                    dptr<int>(ctx->d_rank), T.u.p ? dptr<double>(T.u) : nullptr, dptr<double>(T.den),
-                    dptr<double>(T.mult) + ptr[col], dptr<double>(T.li));
+                if (ctx->hasSolid)
+                    k_hex_body<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
+                        kind, bv, dptr<int>(T.list) + ptr[col], cnt, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist),
+                        dptr<int>(ctx->d_rank), T.u.p ? dptr<double>(T.u) : nullptr, dptr<double>(T.den),
+                        dptr<double>(T.mult) + ptr[col], dptr<double>(T.li));
+                else
+                    k_shell_body<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
+                        bv, dptr<int>(T.list) + ptr[col], cnt, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist),
+                        dptr<int>(ctx->d_rank), dptr<ShellProps>(ctx->d_secABD), dptr<int>(ctx->d_esec),
+                        dptr<int>(ctx->d_shLayRange), dptr<LayerDev>(ctx->d_shLay), dv ? dptr<int>(ctx->d_e2dR) : nullptr,
+                        dv ? dptr<int>(ctx->d_e2d) : nullptr, dv ? dptr<double>(ctx->d_e2c) : nullptr,
+                        dv ? dptr<int>(ctx->d_dCat) : nullptr, dv ? dptr<int>(ctx->d_dLayer) : nullptr,
+                        dv ? dptr<double>(ctx->d_dVal) : nullptr, dptr<double>(T.mult) + ptr[col], dptr<double>(T.li));
             }
             if ((rc = cuda_check(ctx, cudaGetLastError(), "body load"))) return rc;
         }
     } else {
-        // shells, gravitational: load += Rum, the Newmark mass residual alone (the elastic part is
-        // left out, not subtracted: at a displaced state it is orders of magnitude larger)
-        if (!T.u.p) {
+        // shells, gravitational / centrifugal: load += Rum, the Newmark mass residual alone (the
+        // elastic part is left out, not subtracted: at a displaced state it is orders of
+        // magnitude larger)
+        const bool zeroState = !T.u.p;
+        if (zeroState) {
             if ((rc = dev_alloc(ctx, T.u, sizeof(double) * n))) return rc;
             CK(cudaMemsetAsync(T.u.p, 0, sizeof(double) * n, ctx->stream));
         }
@@ -177,11 +277,12 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
                 CK(cudaMemsetAsync(T.iu.p, 0, sizeof(double) * ni, ctx->stream));
             }
         }
-        // previous acceleration -a at every node: with u = u_prev, v_prev = 0 and beta = 1/4 the
+        // previous acceleration -a at the nodes: with u = u_prev, v_prev = 0 and beta = 1/4 the
         // Newmark acceleration is a
-        std::vector<double> pa((size_t)n);
-        for (int r = 0; r < P.N; ++r)
-            for (int c = 0; c < P.dpn; ++c) pa[(size_t)r * P.dpn + c] = -vals[c];
+        std::vector<double> pa((size_t)n, 0.0);
+        if (kind == 1)
+            for (int r = 0; r < P.N; ++r)
+                for (int c = 0; c < P.dpn; ++c) pa[(size_t)r * P.dpn + c] = -vals[c];
         if ((rc = upload(ctx, T.pa, pa.data(), sizeof(double) * n))) return rc;
         if ((rc = dev_alloc(ctx, T.b, sizeof(double) * n))) return rc;
         CK(cudaMemsetAsync(T.b.p, 0, sizeof(double) * n, ctx->stream));
@@ -196,9 +297,33 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
         s1.gamma = 0.5;
         s1.delT = 1.0;
         s1.massOnly = 1;
-        if ((rc = launch_shell4_assemble(ctx, s1, dptr<double>(T.b), nullptr, 0, nullptr, nullptr))) return rc;
+        const int maxMult = *std::max_element(on.begin(), on.end());
+        for (int pass = 0; pass < maxMult; ++pass) {
+            std::vector<int> list, ptr(1, 0);
+            for (int col = 0; col < P.ncolors; ++col) {
+                for (int k = P.colorPtr[col]; k < P.colorPtr[col + 1]; ++k)
+                    if (on[P.colorEls[k]] > pass) list.push_back(P.colorEls[k]);
+                ptr.push_back((int)list.size());
+            }
+            if (list.empty()) continue;
+            dev_free(T.list);
+            if ((rc = upload(ctx, T.list, list.data(), sizeof(int) * list.size()))) return rc;
+            if (kind == 1) {
+                if ((rc = shell4_residual_list(ctx, s1, dptr<int>(T.list), ptr, dptr<double>(T.b)))) return rc;
+                continue;
+            }
+            for (int col = 0; col < P.ncolors; ++col) {
+                const int cnt = ptr[col + 1] - ptr[col];
+                if (!cnt) continue;
+                k_shell_cent_pacc<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
+                    bv, dptr<int>(T.list) + ptr[col], cnt, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist),
+                    dptr<int>(ctx->d_rank), zeroState ? nullptr : dptr<double>(T.u), dptr<double>(T.pa));
+                const std::vector<int> one = {ptr[col], ptr[col + 1]};
+                if ((rc = shell4_residual_list(ctx, s1, dptr<int>(T.list), one, dptr<double>(T.b)))) return rc;
+            }
+        }
         k_sub<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, dptr<double>(T.b), dptr<double>(T.li));
-        if ((rc = cuda_check(ctx, cudaGetLastError(), "shell gravity load"))) return rc;
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "shell mass load"))) return rc;
     }
     if ((rc = int_to_ref_vec(ctx, dptr<double>(T.li), dptr<double>(T.ref), n))) return rc;
     CK(cudaMemcpyAsync(elastic_load, T.ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));

@@ -1,7 +1,7 @@
 """GPU parity of the body loads (getElasticAppliedLoad's bodyForce / gravitational / centrifugal
-branch) against the oracle through the C ABI: bricks for all three kinds over whole meshes and
-element subsets, shells for the gravitational load over the whole mesh at zero and displaced
-states.  Loads agree to 1e-12 relative (bricks) and 1e-11 relative (shells)."""
+branch) against the oracle through the C ABI: bricks and shells, all three kinds, whole meshes
+and element subsets (repeated elements), zero and displaced states.  Loads agree to 1e-12
+relative (bricks) and 1e-11 relative (shells)."""
 import numpy as np
 import pytest
 
@@ -119,15 +119,31 @@ def test_shell_gravity_displaced_state(plate):
     _close(g.body_load(1, vals, elements=els, state=st), lo, 1e-11)
 
 
-def test_shell_unsupported_and_bad_arguments(plate):
+@pytest.mark.parametrize("kind,vals", [
+    (0, [1.0, -2.0, 0.5, 0.3, -0.2, 0.1]),
+    (1, [0.5, 0.0, -9.81, 0.0, 0.0, 0.0]),
+    (2, [0.3, 0.2, 0.0, 0.0, 0.2, 1.0, 30.0]),
+])
+def test_shell_loads_subsets_and_states(plate, kind, vals):
+    """Shell body force, gravity and centrifugal loads over element subsets (repeats add twice)
+    and the whole mesh, at the zero and a displaced state, accumulated into a load."""
     m, g, o = plate
-    with pytest.raises(AstroError) as e:
-        g.body_load(0, [1.0, 0.0, 0.0])
-    assert e.value.code == 3
-    with pytest.raises(AstroError) as e:
-        g.body_load(1, [0.0, 0.0, -9.81], elements=[1, 2])
-    assert e.value.code == 3
+    rng = np.random.default_rng(11)
+    u = 1e-2 * rng.standard_normal(o.n)
+    iv = 1e-4 * rng.standard_normal(o.int_vec_size)
+    st = M.make_state(o.n, disp=u, internal_disp=iv)
+    els = np.array([3, 1, 7, 7, m.num_els, 12])
+    base = rng.standard_normal(o.n)
+    for e_, s_ in ((None, None), (els, None), (els, st), (None, st)):
+        lg = g.body_load(kind, vals, elements=e_, state=s_, elastic_load=base.copy())
+        lo = o.body_load(kind, vals, elements=e_, state=s_, load=base.copy())
+        _close(lg - base, lo - base, 1e-11)
+
+
+def test_shell_bad_arguments(plate):
+    m, g, o = plate
     with pytest.raises(AstroError):
         g.body_load(1, [0.0, 0.0, -9.81], elements=[m.num_els + 1])
     with pytest.raises(AstroError):
         g.body_load(5, [0.0, 0.0, -9.81])
+    assert np.array_equal(g.body_load(0, [1.0, 0, 0], elements=[]), np.zeros(o.n))
