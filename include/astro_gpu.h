@@ -320,6 +320,11 @@ int astro_thermal_constraint_load(astro_ctx *ctx, const double *node_temp, doubl
 /* getThermalAppliedLoad's bodyHeatGen branch (:96-139): heat generation q per unit volume on the
  * listed elements (1-based; NULL = all), integral of N (times the thickness for shells). */
 int astro_thermal_heat_gen(astro_ctx *ctx, double q, const int32_t *elements, int32_t count, double *thermal_load);
+/* getThermalAppliedLoad's surfaceFlux branch (:140-176): the flux as the first component of a
+ * surface traction on the given element faces (as astro_surface_load), thermal_load -= the
+ * component-1 nodal values (rank order). */
+int astro_thermal_surface_flux(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el, const int32_t *face_num,
+                               double flux, double *thermal_load);
 /* (K_T + C^T C) dtemp = rhs by Jacobi-preconditioned conjugate gradients in FP64 on the device,
  * from dtemp's input value, to ||r|| <= rtol ||rhs|| (in place of the reference's gMRes with
  * its skyline LDL^T preconditioner on the thermal system, stepSolve :689-703). */

@@ -167,6 +167,7 @@ def load_library():
         "astro_thermal_scale_mpc": ([vp, F64P, F64P], C.c_int),
         "astro_thermal_constraint_load": ([vp, F64P, F64P], C.c_int),
         "astro_thermal_heat_gen": ([vp, C.c_double, I32P, C.c_int32, F64P], C.c_int),
+        "astro_thermal_surface_flux": ([vp, C.c_int32, I32P, I32P, C.c_double, F64P], C.c_int),
         "astro_thermal_solve": ([vp, F64P, F64P, C.c_double, C.c_int32, C.POINTER(SolveStatsC)], C.c_int),
         "astro_panels_factor": ([vp, C.c_int32, C.POINTER(PanelsInfoC)], C.c_int),
         "astro_panels_solve": ([vp, C.c_int32, F64P, F64P, C.POINTER(PanelsInfoC)], C.c_int),
@@ -436,6 +437,12 @@ class AstroGPU:
         els = None if elements is None else _i32(elements)
         self._check(self.L.astro_thermal_heat_gen(self.h, float(q), None if els is None else _i(els),
                                                   0 if els is None else len(els), _d(load)))
+        return load
+
+    def thermal_surface_flux(self, face_el, face_num, flux, thermal_load=None):
+        load = np.zeros(self.model.num_nodes) if thermal_load is None else thermal_load
+        fe, fn = _i32(face_el), _i32(face_num)
+        self._check(self.L.astro_thermal_surface_flux(self.h, len(fe), _i(fe), _i(fn), float(flux), _d(load)))
         return load
 
     def thermal_solve(self, rhs, dtemp0=None, rtol=1e-12, max_iters=100000):

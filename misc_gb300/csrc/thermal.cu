@@ -732,6 +732,47 @@ extern "C" int astro_thermal_heat_gen(astro_ctx *ctx, double q, const int32_t *e
     return rc;
 }
 
+// thermal -= component 1 of the traction load (the surfaceFlux branch takes the flux as the first
+// traction component and subtracts the element's component-1 nodal forces)
+__global__ void k_th_flux_extract(int N, int dpn, const double *__restrict__ el, double *__restrict__ load) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < N) load[r] = load[r] - el[(size_t)r * dpn];
+}
+
+extern "C" int astro_thermal_surface_flux(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el,
+                                          const int32_t *face_num, double flux, double *thermal_load) {
+    if (!ctx || !thermal_load || nfaces < 0 || (nfaces && (!face_el || !face_num))) return ASTRO_ERR_ARG;
+    if (!plan_of(ctx)) return set_err(ctx, ASTRO_ERR_STATE, "thermal: astro_thermal_setup not called");
+    const AstroPrep &P = ctx->P;
+    for (int f = 0; f < nfaces; ++f) {
+        const int e = face_el[f], fn = face_num[f];
+        if (e < 1 || e > P.E) return set_err(ctx, ASTRO_ERR_ARG, "face element out of range");
+        if (fn < 1 || fn > (ctx->etype[e - 1] == 8 ? 6 : 2)) return set_err(ctx, ASTRO_ERR_ARG, "face number out of range");
+    }
+    if (!nfaces) return ASTRO_OK;
+    DevBuf dfe, dfn, del, dL;
+    int rc = upload(ctx, dfe, face_el, sizeof(int) * nfaces);
+    if (!rc) rc = upload(ctx, dfn, face_num, sizeof(int) * nfaces);
+    if (!rc) rc = dev_alloc(ctx, del, sizeof(double) * P.n);
+    if (!rc) rc = upload(ctx, dL, thermal_load, sizeof(double) * P.N);
+    if (!rc) {
+        cudaMemsetAsync(del.p, 0, sizeof(double) * P.n, ctx->stream);
+        const double tr[3] = {flux, 0.0, 0.0};
+        rc = surface_load_dev(ctx, nfaces, dptr<int>(dfe), dptr<int>(dfn), tr, 0.0, dptr<double>(del));
+    }
+    if (!rc) {
+        k_th_flux_extract<<<(P.N + 255) / 256, 256, 0, ctx->stream>>>(P.N, P.dpn, dptr<double>(del), dptr<double>(dL));
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(thermal_load, dL.p, sizeof(double) * P.N, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        rc = cuda_check(ctx, e, "surface flux");
+    }
+    DevBuf *v[] = {&dfe, &dfn, &del, &dL};
+    for (DevBuf *x : v) dev_free(*x);
+    return rc;
+}
+
 extern "C" int astro_thermal_solve(astro_ctx *ctx, const double *rhs, double *dtemp, double rtol, int32_t max_iters,
                                    astro_solve_stats *stats) {
     if (!ctx || !rhs || !dtemp || !(rtol > 0.0) || max_iters < 1) return ASTRO_ERR_ARG;

@@ -274,6 +274,19 @@ class Oracle:
             load[self.current_rank[nd - 1] - 1] += el[self.n_dof_index[nd - 1, 0] - 1]
         return load
 
+    def thermal_surface_flux(self, face_el, face_num, flux, load=None):
+        """getThermalAppliedLoad's surfaceFlux branch: r_getElSurfaceTraction with the flux as
+        the first traction component; thermalLoad -= the component-1 nodal values."""
+        N = self.model.num_nodes
+        load = np.zeros(N) if load is None else load
+        el = np.zeros(self.n)
+        fe = np.ascontiguousarray(face_el, np.int32)
+        fn = np.ascontiguousarray(face_num, np.int32)
+        self.L.orc_surface_load(self.h, len(fe), _i(fe), _i(fn), _d(np.array([flux, 0.0, 0.0])), 0.0, _d(el))
+        for nd in range(1, N + 1):
+            load[self.current_rank[nd - 1] - 1] -= el[self.n_dof_index[nd - 1, 0] - 1]
+        return load
+
     def thermal_system(self, cond, spec_heat, mpc=None):
         """(A = K_T + C^T C over ranks, b = constraint load at zero temperature, rows) of a steady
         thermal step from the zero state."""

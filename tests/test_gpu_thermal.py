@@ -91,6 +91,9 @@ def test_thermal_constraints_heat_gen_and_solve(case):
     _close(g.getThermalConstraintLoad(T), o.thermal_constraint_load(rows, T, np.zeros(N)), 1e-12)
     els = np.array([1, 3, 3, m.num_els])
     _close(g.thermal_heat_gen(7.0, elements=els), o.thermal_heat_gen(7.0, elements=els), 1e-12)
+    fe = np.array([1, 2, m.num_els], np.int32)
+    fn = np.array([4, 2, 1], np.int32) if m.element_type[0] == 8 else np.array([1, 2, 1], np.int32)
+    _close(g.thermal_surface_flux(fe, fn, 3.5), o.thermal_surface_flux(fe, fn, 3.5), 1e-12)
     q = g.thermal_heat_gen(7.0)
     _close(q, o.thermal_heat_gen(7.0), 1e-12)
     rhs = g.getThermalConstraintLoad(None, q.copy())

@@ -387,6 +387,9 @@ def test_thermal_conduction_kats():
                                     dynamic=1, gamma=0.5, del_t=0.1)
     assert np.isclose(-load2.sum(), 7800.0 * 460.0 * 3.0 * (1 / 0.5) * (1 / 0.1), rtol=1e-12)
     assert np.isclose(o.thermal_heat_gen(5.0).sum(), 15.0, rtol=1e-12)
+    # surface flux on the x = L faces (area 1): the nodal values sum to -flux * area
+    xf = [e + 1 for e in range(m.num_els) if e % 6 == 5]
+    assert np.isclose(o.thermal_surface_flux(xf, [4] * len(xf), 2.0).sum(), -2.0, rtol=1e-12)
     p = M.plate_shell(nx=4, ny=2, lx=2.0, ly=1.0, t=0.02)
     op = Oracle(p)
     assert np.isclose(op.thermal_heat_gen(3.0).sum(), 3.0 * 2.0 * 0.02, rtol=1e-12)
