@@ -461,3 +461,85 @@ def write_model_input(m: Model, path, node_sets=None, point_loads=None):
             out.append(f"          - [{int(nd)}, " + ", ".join(_r(x) for x in vals) + "]")
     with open(path, "w") as f:
         f.write("\n".join(out) + "\n")
+
+
+# design-variable categories the device complex step evaluates (astro_model d_category)
+_DCAT = {("layup", "thickness"): 1, ("elastic", "modulus"): 2}
+
+
+def read_design_var_input(path, mi: ModelInput):
+    """readDesignVarInput (Working/AStrO_input.f90:1099-1408): one entry per 'category:' with its
+    subCategory, component, layer, activeTime, the element (or node) set it acts on and its
+    coefficients (one value for every member, or a list).  Returns a list of dicts."""
+    with open(path) as f:
+        lines = [ln.rstrip("\n").replace("\t", "    ").split("#", 1)[0] for ln in f]
+    dvs = []
+    i = 0
+    while i < len(lines):
+        ln = lines[i]
+        k = _key(ln)
+        dv = dvs[-1] if dvs else None
+        if k == "category:":
+            dvs.append(dict(category=_after(ln).split()[0], subCategory="", component=0, layer=0,
+                            activeTime=[0.0, 0.0], elements=[], nodes=[], coefficients=None))
+        elif dv is not None and k == "subCategory:":
+            dv["subCategory"] = _after(ln).split()[0]
+        elif dv is not None and k in ("component:", "layer:"):
+            dv[k[:-1]] = int(float(_after(ln).split()[0]))
+        elif dv is not None and k == "activeTime:":
+            b = _bracket(ln)
+            dv["activeTime"] = [_num(b[0]), _num(b[1])] if b else [_num(_after(ln).split()[0]), 1e100]
+        elif dv is not None and k == "elementSet:":
+            dv["elements"] += list(mi.element_sets.get(_after(ln).split()[0], []))
+        elif dv is not None and k == "nodeSet:":
+            dv["nodes"] += list(mi.node_sets.get(_after(ln).split()[0], []))
+        elif dv is not None and k == "coefficients:":
+            head = _after(ln)
+            members = len(dv["elements"]) or len(dv["nodes"])
+            if head:
+                dv["coefficients"] = [_num(head.split()[0])] * members
+            else:
+                cs = []
+                i += 1
+                while i < len(lines) and ":" not in lines[i]:
+                    if "-" in lines[i]:
+                        cs.append(_num(lines[i].split("-", 1)[1].split()[0]))
+                    i += 1
+                dv["coefficients"] = (cs + [1.0] * members)[:members]
+                continue
+        i += 1
+    for dv in dvs:
+        if dv["coefficients"] is None:
+            dv["coefficients"] = [1.0] * (len(dv["elements"]) or len(dv["nodes"]))
+    return dvs
+
+
+def apply_design_vars(m: Model, dvs, values=None, strict=True):
+    """Attaches the element design variables the complex step evaluates (layup thickness,
+    elastic modulus) to m as elToD / elToCoef (per element, the variables in input order, an
+    element listed twice for one variable kept once).  Other categories raise (strict) or are
+    left out; returns the input numbers (1-based) of the variables kept."""
+    keep = []
+    for k, dv in enumerate(dvs):
+        cat = _DCAT.get((dv["category"], dv["subCategory"]))
+        if cat is None:
+            if strict:
+                raise ValueError(f"design variable {k + 1}: {dv['category']}/{dv['subCategory']} is not evaluated "
+                                 f"by the device complex step")
+            continue
+        keep.append(k)
+    E = m.num_els
+    per_el = [[] for _ in range(E)]
+    for j, k in enumerate(keep):
+        dv = dvs[k]
+        for e, c in zip(dv["elements"], dv["coefficients"]):
+            if all(d != j + 1 for d, _ in per_el[e - 1]):
+                per_el[e - 1].append((j + 1, c))
+    m.el_to_d_range = np.cumsum([0] + [len(p) for p in per_el]).astype(np.int32)
+    m.el_to_d = np.array([d for p in per_el for d, _ in p], np.int32)
+    m.el_to_coef = np.array([c for p in per_el for _, c in p], np.float64)
+    m.d_category = np.array([_DCAT[(dvs[k]["category"], dvs[k]["subCategory"])] for k in keep], np.int32)
+    m.d_component = np.array([max(dvs[k]["component"], 1) for k in keep], np.int32)
+    m.d_layer = np.array([max(dvs[k]["layer"], 1) for k in keep], np.int32)
+    m.d_value = np.zeros(len(keep)) if values is None else np.asarray(values, np.float64)[keep]
+    return [k + 1 for k in keep]

@@ -179,3 +179,25 @@ def test_read_model_solves_on_the_gpu():
     assert np.linalg.norm(b - bo) <= 1e-13 * np.linalg.norm(bo)
     x = np.random.default_rng(0).standard_normal(o.n)
     assert np.linalg.norm(g.apply_operator(x, 64) - A @ x) <= 1e-12 * np.linalg.norm(A @ x)
+
+
+def test_design_variable_input():
+    """The reference's example design-variable file: a layup thickness variable (evaluated by
+    the complex step) and a layup modulus variable (not: strict mode refuses, otherwise it is
+    left out); the thickness variable then moves the oracle's element stiffness like a thicker
+    layer."""
+    mi = IF.read_model_input(FIX)
+    dvs = IF.read_design_var_input(FIX.with_name("shell_beam_dvar_input.yaml"), mi)
+    assert [(d["category"], d["subCategory"], d["layer"], d["component"]) for d in dvs] == \
+        [("layup", "thickness", 1, 0), ("layup", "modulus", 1, 1)]
+    assert dvs[0]["elements"] == list(range(1, 11)) and dvs[1]["coefficients"] == [2.0] * 10
+    m = mi.model()
+    with pytest.raises(ValueError):
+        IF.apply_design_vars(m, dvs)
+    kept = IF.apply_design_vars(m, dvs, values=[0.01, 5.0], strict=False)
+    assert kept == [1]
+    assert m.el_to_d_range.tolist() == list(range(11)) and np.all(m.el_to_d == 1) and np.all(m.el_to_coef == 1.0)
+    ke = Oracle(m).element_matrices()
+    m2 = mi.model()
+    m2.layup_thickness = m2.layup_thickness + 0.01
+    assert np.allclose(ke, Oracle(m2).element_matrices(), rtol=1e-12, atol=1e-9 * np.abs(ke).max())
