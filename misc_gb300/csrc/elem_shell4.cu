@@ -140,6 +140,8 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
         A.els = d_els + ptr[col];
         A.count = cnt;
         k_shell_frame<<<(cnt + 63) / 64, 64, 0, s>>>(A);
+        k_shell_frame_rot<<<(10 * cnt + 63) / 64, 64, 0, s>>>(A);
+        k_shell_frame_rest<<<(cnt + 63) / 64, 64, 0, s>>>(A);
         k_shell_gauss<<<(4 * cnt + 127) / 128, 128, 0, s>>>(A);
         k_shell_dedu<<<(128 * cnt + 127) / 128, 128, 0, s>>>(A);
         k_shell_kcol<<<(32 * cnt + 127) / 128, 128, 0, s>>>(A);

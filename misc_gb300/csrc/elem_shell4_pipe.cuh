@@ -1,9 +1,11 @@
 // shell4 element evaluation as a pipeline of one-thread-per-item kernels over per-element global
 // scratch (device code; the algorithm is described in elem_shell4.cu).  For one colour's
 // elements at a time:
-//   frame    thread per element:            state gather, instantaneous frame and its first and
-//                                            second rotation derivatives (ten rotations), the
-//                                            (0,0) instantaneous DOF, Newmark acceleration
+//   frame    thread per element:            state gather; then thread per (element, rotation):
+//                                            the instantaneous frame and its first and second
+//                                            rotation derivatives (ten rotations); then thread
+//                                            per element: axial vectors, the (0,0) instantaneous
+//                                            DOF, Newmark acceleration
 //   gauss    thread per (element, point):    shape functions, Jacobian, section forces ABD def
 //   dedu     thread per (element, point, i): first derivative of the deformation vector
 //   kcol     thread per (element, column j): column j of K (material + stress part) and Ru_j,
@@ -54,7 +56,10 @@ struct ShellPipe {
     double *K, *load, *intLoad, *intMat, *keOut, *ruOut;
 };
 
-__device__ void pipe_frame(const ShellPipe &A, int q) {
+// The frame stage in three parts: the gather (per element), the ten frame rotations (per
+// element and rotation: the instantaneous frame and its first and second derivatives, the costly
+// part), then the axial vectors, the (0,0) instantaneous DOF and the Newmark acceleration.
+__device__ void pipe_frame_gather(const ShellPipe &A, int q) {
     const int e = A.els[q];
     const int *el = A.elist + 8 * (size_t)e;
     const ShellProps &P = A.props[e];
@@ -82,8 +87,16 @@ __device__ void pipe_frame(const ShellPipe &A, int q) {
     for (int a = 0; a < 4; ++a)
         for (int i = 0; i < 3; ++i) F.Xl[a][i] = orient[i][0] * F.X[a][0] + orient[i][1] * F.X[a][1] + orient[i][2] * F.X[a][2];
     for (int k = 0; k < 3; ++k) F.rot[k] = 0.25 * (F.u[3 + k][0] + F.u[3 + k][1] + F.u[3 + k][2] + F.u[3 + k][3]);
+}
+
+__device__ void pipe_frame_rot(const ShellPipe &A, int q, int v) {
+    const int e = A.els[q];
+    const ShellProps &P = A.props[e];
+    ShellFrame &F = A.fr[q];
+    double orient[3][3];
+    for (int i = 0; i < 9; ++i) orient[i / 3][i % 3] = P.orient[i];
     // frame and derivatives (r_getInstOrient): (0,0), (i,0) and (i,j) i <= j
-    for (int v = 0; v < 10; ++v) {
+    {
         const int bi = (v == 0) ? 0 : (v < 4 ? v : (v < 7 ? 1 : (v < 9 ? 2 : 3)));
         const int bj = (v < 4) ? 0 : (v < 7 ? v - 3 : (v < 9 ? v - 5 : 3));
         double out[3][3];
@@ -102,6 +115,17 @@ __device__ void pipe_frame(const ShellPipe &A, int q) {
             F.io[b2][t] = out[t / 3][t % 3];
         }
     }
+}
+
+__device__ void pipe_frame_rest(const ShellPipe &A, int q) {
+    const int e = A.els[q];
+    const int *el = A.elist + 8 * (size_t)e;
+    const ShellProps &P = A.props[e];
+    ShellFrame &F = A.fr[q];
+    double orient[3][3];
+    for (int i = 0; i < 9; ++i) orient[i / 3][i % 3] = P.orient[i];
+    int rk[4];
+    for (int a = 0; a < 4; ++a) rk[a] = A.rank[el[a] - 1] - 1;
     for (int v = 1; v < 10; ++v) {
         const int bi = (v < 4) ? v : (v < 7 ? 1 : (v < 9 ? 2 : 3));
         const int bj = (v < 4) ? 0 : (v < 7 ? v - 3 : (v < 9 ? v - 5 : 3));
@@ -488,7 +512,15 @@ __device__ void pipe_condense(const ShellPipe &A, int q) {
 
 __global__ void k_shell_frame(ShellPipe A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.count) pipe_frame(A, q);
+    if (q < A.count) pipe_frame_gather(A, q);
+}
+__global__ void k_shell_frame_rot(ShellPipe A) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 10 * A.count) pipe_frame_rot(A, t / 10, t % 10);
+}
+__global__ void k_shell_frame_rest(ShellPipe A) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < A.count) pipe_frame_rest(A, q);
 }
 __global__ void k_shell_gauss(ShellPipe A) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;

@@ -7,7 +7,7 @@ import pytest
 import scipy.sparse.linalg as spla
 
 from misc_gb300 import model as M
-from misc_gb300.astro import AstroError, AstroGPU
+from misc_gb300.astro import SOLVER_FGMRES_LEARNED, AstroError, AstroGPU
 from oracle import Oracle
 
 pytestmark = pytest.mark.gpu
@@ -48,7 +48,9 @@ def test_adjoint_gradient_shell_internal_dof():
     g.scaleElasticMPC()
     dldu = rng.standard_normal(n)
     idldu = rng.standard_normal(ni)
-    dldd, lam, ilam, s = g.getTotaldLdD(dldu, int_dldu=idldu, state=st, rtol=1e-13)
+    # the learned solver: plain FP64 Jacobi-GMRES stalls near 1e-12 on this shell system (its
+    # last digits move with the rounding of the element kernels)
+    dldd, lam, ilam, s = g.getTotaldLdD(dldu, int_dldu=idldu, state=st, rtol=1e-12, method=SOLVER_FGMRES_LEARNED)
     od, olam, oilam = o.total_dldd(dldu, int_dldu=idldu, state=st)
     assert s.status == 0
     # the shell system is ill-conditioned (drilling DOF): its element matrices agree with the
