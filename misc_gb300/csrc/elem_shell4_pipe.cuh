@@ -29,6 +29,7 @@ struct ShellFrame {
     double Xl[4][3];    // local coordinates (orient X)
     double rot[3];      // element mean rotation
     double acc[6][4];   // Newmark acceleration of the nodal DOF (dynamic)
+    double inam[6][4];  // section mass times the instantaneous nodal acceleration (dynamic)
 };
 
 struct ShellGP {
@@ -358,6 +359,26 @@ __device__ __forceinline__ void mass_dof(const ShellFrame &F, int i, int &nd, do
         for (int r = 0; r < 3; ++r) bv[3 + r] = F.dr[var - 3][r];
 }
 
+// instNodalAcc = sum_i acc(var_i, nd_i) * d instU / d u_i (nodal part) and iNAM = M instNodalAcc
+// for node n of the element (r_getElRum), the DOF of the node in their order
+__device__ void pipe_inam(const ShellPipe &A, int q, int n) {
+    const ShellProps &P = A.props[A.els[q]];
+    ShellFrame &F = A.fr[q];
+    double ina[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int var = 1; var <= 6; ++var) {
+        int nd;
+        double bv[6];
+        mass_dof(F, (var - 1) * 4 + n, nd, bv);
+        const double a = F.acc[var - 1][nd - 1];
+        for (int r = 0; r < 6; ++r) ina[r] += a * bv[r];
+    }
+    for (int r = 0; r < 6; ++r) {
+        double s = 0.0;
+        for (int k = 0; k < 6; ++k) s += P.M[6 * r + k] * ina[k];
+        F.inam[r][n] = s;
+    }
+}
+
 __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
     const ShellProps &P = A.props[A.els[q]];
     const ShellFrame &F = A.fr[q];
@@ -399,23 +420,7 @@ __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
     }
     if (A.dynamic && j < 24) {
         const double c1 = 0.5 / A.beta, c2 = 2.0 / (A.delT * A.delT);
-        // instNodalAcc = sum_i acc(var_i, nd_i) * d instU / d u_i (nodal part), iNAM = M instNodalAcc
-        double ina[6][4] = {};
-        for (int i = 0; i < 24; ++i) {
-            int nd, var, ndd;
-            double bv[6];
-            mass_dof(F, i, nd, bv);
-            dof_of(i, var, ndd);
-            const double a = F.acc[var - 1][nd - 1];
-            for (int r = 0; r < 6; ++r) ina[r][nd - 1] += a * bv[r];
-        }
-        double inam[6][4];
-        for (int r = 0; r < 6; ++r)
-            for (int n = 0; n < 4; ++n) {
-                double s = 0.0;
-                for (int k = 0; k < 6; ++k) s += P.M[6 * r + k] * ina[k][n];
-                inam[r][n] = s;
-            }
+        const double(*inam)[4] = F.inam;
         int ndj;
         double bj[6];
         mass_dof(F, j, ndj, bj);
@@ -521,6 +526,27 @@ __global__ void k_shell_frame_rot(ShellPipe A) {
 __global__ void k_shell_frame_rest(ShellPipe A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q < A.count) pipe_frame_rest(A, q);
+}
+__global__ void k_shell_inam(ShellPipe A) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 4 * A.count) pipe_inam(A, t / 4, t % 4);
+}
+// residual scatter without a matrix: one thread per (element, DOF) (a colour's elements share no
+// node, an element's DOF are distinct entries)
+__global__ void k_shell_scatter(ShellPipe A) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 32 * A.count) return;
+    const int q = t / 32, i = t % 32;
+    const int e = A.els[q];
+    const double ru = A.Kf[(size_t)q * 32 * 33 + 33 * i + 32];
+    if (i < 24) {
+        const int var = i / 4, a = i % 4;
+        const int r = A.rank[A.elist[8 * (size_t)e + a] - 1] - 1;
+        if (A.load) A.load[6 * (size_t)r + var] -= ru;
+        if (A.ruOut) A.ruOut[24 * (size_t)e + i] = ru;
+    } else if (A.intLoad) {
+        A.intLoad[8 * (size_t)e + i - 24] -= ru;
+    }
 }
 __global__ void k_shell_gauss(ShellPipe A) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
