@@ -146,10 +146,11 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
         k_shell_gauss<<<(4 * cnt + 127) / 128, 128, 0, s>>>(A);
         k_shell_dedu<<<(128 * cnt + 127) / 128, 128, 0, s>>>(A);
         k_shell_kcol<<<(32 * cnt + 127) / 128, 128, 0, s>>>(A);
-        if (A.buildMat)
-            k_shell_condense<<<(cnt + 63) / 64, 64, 0, s>>>(A);
-        else
-            k_shell_scatter<<<(32 * cnt + 127) / 128, 128, 0, s>>>(A);
+        if (A.buildMat) {
+            k_shell_cond_lu<<<(cnt + 63) / 64, 64, 0, s>>>(A);
+            k_shell_cond_col<<<(24 * cnt + 127) / 128, 128, 0, s>>>(A);
+        }
+        k_shell_scatter<<<(32 * cnt + 127) / 128, 128, 0, s>>>(A);
     }
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);

@@ -10,8 +10,10 @@
 //   dedu     thread per (element, point, i): first derivative of the deformation vector
 //   kcol     thread per (element, column j): column j of K (material + stress part) and Ru_j,
 //                                            plus the Newmark mass column
-//   condense thread per element:             8x8 internal LU, condensation, outputs and the
-//                                            colour-ordered block-CSR update
+//   cond     thread per element:             8x8 internal LU; then thread per (element,
+//                                            column): condensation, outputs and the colour-ordered
+//                                            block-CSR update (with a matrix only)
+//   scatter  thread per (element, DOF):      residual into the load vectors
 #pragma once
 #include "shell_props.cuh"
 
@@ -460,59 +462,63 @@ __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
     out[32] = ru;
 }
 
-// static condensation (r_condenseMat on rows/cols 25..32) in place on the element scratch, then
-// outputs: residual scatter, internal rows, element matrix, block-CSR update.
-__device__ void pipe_condense(const ShellPipe &A, int q) {
+// static condensation (r_condenseMat on rows/cols 25..32) with a matrix, split: the 8x8 internal
+// LU per element, then one thread per (element, column j < 24) for the column's solve, its
+// update, and its outputs (block-CSR, element matrix, internal rows); the residual is scattered
+// by k_shell_scatter
+__device__ void pipe_cond_lu(const ShellPipe &A, int q) {
     const int e = A.els[q];
-    const int *el = A.elist + 8 * (size_t)e;
-    double *Kq = A.Kf + (size_t)q * 32 * 33;  // K(i,j) = Kq[33*j + i], Ru_j = Kq[33*j + 32]
-    if (A.buildMat) {
-        double L[8][8];
-        for (int r = 0; r < 8; ++r)
-            for (int c = 0; c < 8; ++c) L[r][c] = Kq[33 * (24 + c) + 24 + r];
-        a_lu<double, 8>(&L[0][0], 8);
-        for (int r = 0; r < 8; ++r)
-            for (int c = 0; c < 8; ++c) Kq[33 * (24 + c) + 24 + r] = L[r][c];
-        for (int j = 0; j < 24; ++j) {
-            double b[8], x[8];
-            for (int k = 0; k < 8; ++k) b[k] = Kq[33 * j + 24 + k];
-            a_lu_solve<double, 8>(&L[0][0], b, x, 8);
-            for (int i = 0; i < 24; ++i) {
-                double s = Kq[33 * j + i];
-                for (int k = 0; k < 8; ++k) s -= Kq[33 * (24 + k) + i] * x[k];
-                Kq[33 * j + i] = s;
-            }
-        }
-        if (A.intMat) {
-            double *dst = A.intMat + 256 * (size_t)e;
-            for (int c = 0; c < 32; ++c)
-                for (int k = 0; k < 8; ++k) dst[8 * c + k] = Kq[33 * c + 24 + k];
-        }
+    double *Kq = A.Kf + (size_t)q * 32 * 33;
+    double L[8][8];
+    for (int r = 0; r < 8; ++r)
+        for (int c = 0; c < 8; ++c) L[r][c] = Kq[33 * (24 + c) + 24 + r];
+    a_lu<double, 8>(&L[0][0], 8);
+    for (int r = 0; r < 8; ++r)
+        for (int c = 0; c < 8; ++c) Kq[33 * (24 + c) + 24 + r] = L[r][c];
+    if (A.intMat) {
+        double *dst = A.intMat + 256 * (size_t)e;
+        for (int c = 24; c < 32; ++c)
+            for (int k = 0; k < 8; ++k) dst[8 * c + k] = Kq[33 * c + 24 + k];
     }
-    for (int i = 0; i < 32; ++i) {
-        const double ru = Kq[33 * i + 32];
-        if (i < 24) {
-            const int var = i / 4, a = i % 4;
-            const int r = A.rank[el[a] - 1] - 1;
-            if (A.load) A.load[6 * (size_t)r + var] -= ru;
-            if (A.ruOut) A.ruOut[24 * (size_t)e + i] = ru;
-        } else if (A.intLoad) {
-            A.intLoad[8 * (size_t)e + i - 24] -= ru;
-        }
+}
+
+__device__ void pipe_cond_col(const ShellPipe &A, int q, int j) {
+    const int e = A.els[q];
+    double *Kq = A.Kf + (size_t)q * 32 * 33;
+    double L[8][8];
+    for (int r = 0; r < 8; ++r)
+        for (int c = 0; c < 8; ++c) L[r][c] = Kq[33 * (24 + c) + 24 + r];
+    double b[8], x[8];
+    for (int k = 0; k < 8; ++k) b[k] = Kq[33 * j + 24 + k];
+    a_lu_solve<double, 8>(&L[0][0], b, x, 8);
+    for (int i = 0; i < 24; ++i) {
+        double s = Kq[33 * j + i];
+        for (int k = 0; k < 8; ++k) s -= Kq[33 * (24 + k) + i] * x[k];
+        Kq[33 * j + i] = s;
     }
-    if (!A.buildMat) return;
-    for (int j = 0; j < 24; ++j) {
-        const int cvar = j / 4, b = j % 4;
-        for (int i = 0; i < 24; ++i) {
-            const double v = Kq[33 * j + i];
-            if (A.K) {
-                const int rvar = i / 4, a = i % 4;
-                const int blk = A.elBlk[16 * (size_t)e + 4 * a + b];
-                A.K[36 * (size_t)blk + 6 * rvar + cvar] += v;
-            }
-            if (A.keOut) A.keOut[576 * (size_t)e + 24 * (size_t)j + i] = v;
-        }
+    if (A.intMat) {
+        double *dst = A.intMat + 256 * (size_t)e;
+        for (int k = 0; k < 8; ++k) dst[8 * j + k] = Kq[33 * j + 24 + k];
     }
+    const int cvar = j / 4, bn = j % 4;
+    for (int i = 0; i < 24; ++i) {
+        const double v = Kq[33 * j + i];
+        if (A.K) {
+            const int rvar = i / 4, a = i % 4;
+            const int blk = A.elBlk[16 * (size_t)e + 4 * a + bn];
+            A.K[36 * (size_t)blk + 6 * rvar + cvar] += v;
+        }
+        if (A.keOut) A.keOut[576 * (size_t)e + 24 * (size_t)j + i] = v;
+    }
+}
+
+__global__ void k_shell_cond_lu(ShellPipe A) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < A.count) pipe_cond_lu(A, q);
+}
+__global__ void k_shell_cond_col(ShellPipe A) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < 24 * A.count) pipe_cond_col(A, t / 24, t % 24);
 }
 
 __global__ void k_shell_frame(ShellPipe A) {
@@ -559,10 +565,6 @@ __global__ void k_shell_dedu(ShellPipe A) {
 __global__ void k_shell_kcol(ShellPipe A) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < 32 * A.count) pipe_kcol(A, t / 32, t % 32);
-}
-__global__ void k_shell_condense(ShellPipe A) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < A.count) pipe_condense(A, q);
 }
 
 }  // namespace
