@@ -240,6 +240,14 @@ int astro_element_matrices(astro_ctx *ctx, int32_t precision, const astro_state 
 int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const astro_state *state,
                        double *drudd, double *int_drudd);
 
+/* The complex-step dRu/dd of num design variables (1-based numbers in dvars) at the state, each
+ * condensed to the nodal DOF as updateExternalRHS does (shells; needs the internal rows of the
+ * last astro_el_soln_load(build_mat = 1)), into drudd (num x el_mat_dim, variable k at
+ * drudd + k * el_mat_dim): the right-hand sides of the direct sensitivity solves, formed on the
+ * device and copied out once. */
+int astro_drdd_complex_condensed(astro_ctx *ctx, int32_t num, const int32_t *dvars, double h,
+                                 const astro_state *state, double *drudd);
+
 /* ---- constraints and loads ---------------------------------------------------------------- */
 
 /* scaleElasticMPC (Working/AStrO_commandFunctions.f90:537-566): rows of C normalised to unit

@@ -162,6 +162,7 @@ def load_library():
         "astro_constraint_load": ([vp, F64P, F64P], C.c_int),
         "astro_surface_load": ([vp, C.c_int32, I32P, I32P, F64P, C.c_double, F64P], C.c_int),
         "astro_body_load": ([vp, C.c_int32, F64P, I32P, C.c_int32, C.c_void_p, F64P], C.c_int),
+        "astro_drdd_complex_condensed": ([vp, C.c_int32, I32P, C.c_double, vp, F64P], C.c_int),
         "astro_thermal_setup": ([vp, C.POINTER(ThermalPropsC), I32P, I32P], C.c_int),
         "astro_thermal_soln_load": ([vp, C.c_int32, C.POINTER(ThermalStateC), F64P, F64P, I32P], C.c_int),
         "astro_thermal_scale_mpc": ([vp, F64P, F64P], C.c_int),
@@ -542,6 +543,15 @@ class AstroGPU:
         self._check(self.L.astro_drdd_complex(self.h, dvar, h, C.byref(state) if state is not None else None,
                                               _d(out), _d(iout)))
         return out, iout[:self.int_vec_size]
+
+    def drdd_condensed(self, dvars, h=1e-14, state=None):
+        """Condensed complex-step dRu/dd of the listed design variables: (n, len(dvars)), Fortran
+        order (the right-hand-side layout of panels_solve)."""
+        dv = _i32(dvars)
+        out = np.empty((self.n, len(dv)), dtype=np.float64, order="F")
+        self._check(self.L.astro_drdd_complex_condensed(self.h, len(dv), _i(dv), float(h),
+                                                        C.byref(state) if state is not None else None, _d(out)))
+        return out
 
     def stepSolve(self, applied_load, node_disp=None, internal_disp=None, nl_geom=0, method=SOLVER_GMRES_JACOBI_FP64,
                   rtol=1e-12, restart=50, max_iters=200000, precond=None):

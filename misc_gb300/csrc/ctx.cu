@@ -699,6 +699,45 @@ extern "C" int astro_drdd_complex(astro_ctx *ctx, int32_t dvar, double h, const 
     return ASTRO_OK;
 }
 
+extern "C" int astro_drdd_complex_condensed(astro_ctx *ctx, int32_t num, const int32_t *dvars, double h,
+                                            const astro_state *state, double *drudd) {
+    if (!ctx || num < 0 || (num > 0 && (!dvars || !drudd))) return ASTRO_ERR_ARG;
+    for (int k = 0; k < num; ++k)
+        if (dvars[k] < 1 || dvars[k] > ctx->numDvars)
+            return set_err(ctx, ASTRO_ERR_ARG, "design variable " + std::to_string(dvars[k]) + " out of range");
+    if (!(h > 0.0)) return set_err(ctx, ASTRO_ERR_ARG, "complex step h must be positive");
+    const AstroPrep &P = ctx->P;
+    const int n = P.n, ni = P.intVecSize;
+    const bool condense = ctx->hasShell && ni > 0;
+    if (condense && !ctx->haveIntMat)
+        return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
+    if (num == 0) return ASTRO_OK;
+    int rc;
+    DrddState D;
+    if ((rc = drdd_state(ctx, state, D))) return rc;
+    struct Tmp {
+        DevBuf acc, iacc, out;
+        ~Tmp() {
+            dev_free(acc);
+            dev_free(iacc);
+            dev_free(out);
+        }
+    } T;
+    if ((rc = dev_alloc(ctx, T.acc, sizeof(double) * n)) ||
+        (rc = dev_alloc(ctx, T.out, sizeof(double) * (size_t)n * num)))
+        return rc;
+    if (ni > 0 && (rc = dev_alloc(ctx, T.iacc, sizeof(double) * ni))) return rc;
+    for (int k = 0; k < num; ++k) {
+        if ((rc = drdd_device(ctx, dvars[k], h, D, dptr<double>(T.acc), ni > 0 ? dptr<double>(T.iacc) : nullptr)))
+            return rc;
+        if (condense && (rc = shell4_update_external_rhs(ctx, dptr<double>(T.iacc), dptr<double>(T.acc)))) return rc;
+        if ((rc = int_to_ref_vec(ctx, dptr<double>(T.acc), dptr<double>(T.out) + (size_t)k * n, n))) return rc;
+    }
+    CK(cudaMemcpyAsync(drudd, T.out.p, sizeof(double) * (size_t)n * num, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}
+
 // Per-CTA partial sums of a . b (256 threads per CTA); the host adds them in CTA order.
 __global__ void k_dot_part(const double *__restrict__ a, const double *__restrict__ b, int n, double *part) {
     __shared__ double sp[8];

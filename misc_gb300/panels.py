@@ -31,12 +31,9 @@ def pressure_load(g: AstroGPU, m) -> np.ndarray:
 
 def sensitivity_rhs(g: AstroGPU, n_dvars: int, state=None, h: float = 1e-14) -> np.ndarray:
     """Columns dRu/dd of design variables 1..n_dvars (complex step at the given state), condensed
-    to the nodal DOF (updateExternalRHS): the right-hand sides of the sensitivity solves."""
-    cols = []
-    for d in range(1, n_dvars + 1):
-        dr, idr = g.getdRelasticdD(d, h, state=state)
-        cols.append(g.updateExternalRHS(dr, idr) if g.int_vec_size else dr)
-    return np.asfortranarray(np.column_stack(cols))
+    to the nodal DOF (updateExternalRHS) on the device: the right-hand sides of the sensitivity
+    solves."""
+    return g.drdd_condensed(np.arange(1, n_dvars + 1), h, state=state)
 
 
 def solve_batch(g: AstroGPU, m, n_dvars: int, cluster_size: int = 0, load_scale: float = 1.0):

@@ -154,3 +154,19 @@ def _surface(o, m, e0, e1, pressure):
     tr = np.zeros(3)
     o.L.orc_surface_load(o.h, len(fe), _i(fe), _i(fn), _d(tr), C.c_double(pressure), _d(load))
     return load
+
+
+def test_condensed_complex_step_batch(batch):
+    """astro_drdd_complex_condensed equals astro_drdd_complex + astro_update_external_rhs per
+    design variable, bit for bit."""
+    m, g, o, A = batch
+    g.getElasticSolnLoad(1, export=False)
+    g.scaleElasticMPC()
+    rng = np.random.default_rng(9)
+    st = M.make_state(g.n, disp=1e-5 * rng.standard_normal(g.n), internal_disp=1e-6 * rng.standard_normal(g.int_vec_size))
+    R = g.drdd_condensed([3, 1, 4], state=st)
+    for k, d in enumerate((3, 1, 4)):
+        dr, idr = g.getdRelasticdD(d, state=st)
+        assert np.array_equal(R[:, k], g.updateExternalRHS(dr, idr))
+    with pytest.raises(AstroError):
+        g.drdd_condensed([5])
