@@ -8,8 +8,8 @@ Working/AStrO_output.f90:10-152: 'time:', 'timeStep:', then per field '    - [no
 
 Supported: *readModelInput, *readDesignVarInput (the categories the device complex step
 evaluates), *solve (elastic static, linear or nonlinear geometry; elastic Newmark dynamics;
-steady thermal), *writeNodeResults (temperature, displacement, velocity, acceleration,
-reactionForce, reactionHeatGen).  Other commands (*modalAnalysis, objectives, element results)
+steady and transient thermal), *writeNodeResults (temperature, tdot, displacement, velocity,
+acceleration, reactionForce, reactionHeatGen).  Other commands (*modalAnalysis, objectives, element results)
 are logged as not run.
 
 Loads of the model file, at a time t (a load acts when activeTime[0] <= t <= activeTime[1]):
@@ -95,6 +95,8 @@ class Job:
             rank = self.g.current_rank - 1
             self.temp = np.zeros(m.num_nodes)
             self.temp[rank] = ini["temperature"]
+            self.tdot = np.zeros(m.num_nodes)
+            self.tdot[rank] = ini["tdot"]
         return self.g
 
     def _shell(self):
@@ -219,7 +221,10 @@ class Job:
         dynamic = yes("dynamic", "no")
         t_load = float(kv.get("staticLoadTime") or 0.0)
         g = self._gpu()
-        if thermal:
+        if thermal and dynamic:
+            self._thermal_dynamic(float(kv["timeStep"]), float(kv.get("simPeriod") or 0.0),
+                                  float(kv.get("newmarkGamma") or 0.5))
+        elif thermal:
             self._thermal_solve(t_load)
         if elastic and not dynamic:
             g.getElasticSolnLoad(1, export=False)
@@ -266,10 +271,7 @@ class Job:
 
     def _thermal_solve(self, t):
         g = self.g
-        cond, sh, mpc = self.mi.thermal()
-        if not self.thermal_ready:
-            g.thermal_setup(thermal_props(cond, sh, mpc if len(mpc[0]) > 1 else None))
-            self.thermal_ready = True
+        self._thermal_setup()
         st = thermal_state(self.temp)
         load = self.thermal_load(t)
         f = load.copy()
@@ -283,6 +285,38 @@ class Job:
         self.therm_load = after
         self.log.append(f"thermal step: {stats.iterations} CG iterations, status {stats.status}")
 
+    def _thermal_setup(self):
+        if not self.thermal_ready:
+            cond, sh, mpc = self.mi.thermal()
+            self.g.thermal_setup(thermal_props(cond, sh, mpc if len(mpc[0]) > 1 else None))
+            self.thermal_ready = True
+
+    def _thermal_dynamic(self, dt, period, gamma):
+        """The thermal branch of solve's time loop (Working/AStrO_commandFunctions.f90:751-817 with
+        stepSolve :689-703): the conductivity + capacitance / (gamma dt) matrix built once at the
+        initial state, then per step the residual at the current temperature, the applied and
+        constraint loads, one solve, and the rate update of the generalised trapezoid rule."""
+        g = self.g
+        self._thermal_setup()
+        N = self.model.num_nodes
+        T = self.temp.copy()
+        pT = T.copy()
+        pTd = self.tdot.copy() if getattr(self, "tdot", None) is not None else np.zeros(N)
+        g.getThermalSolnLoad(1, state=thermal_state(T, pT, pTd, 1, gamma, dt), thermal_load=np.zeros(N), export=False)
+        g.scaleThermalMPC()
+        nsteps = int(round(period / dt)) if period > 0 else 0
+        for k in range(1, nsteps + 1):
+            load = self.thermal_load(k * dt)
+            g.getThermalSolnLoad(0, state=thermal_state(T, pT, pTd, 1, gamma, dt), thermal_load=load, export=False)
+            g.getThermalConstraintLoad(T, load)
+            dT, st = g.thermal_solve(load, rtol=1e-12)
+            T = T + dT
+            Td = (1.0 / gamma) * ((1.0 / dt) * (T - pT) - (1.0 - gamma) * pTd)
+            pT, pTd = T.copy(), Td
+        self.temp, self.tdot = T, pTd
+        self.time, self.step = nsteps * dt, nsteps
+        self.log.append(f"thermal time loop: {nsteps} steps")
+
     def cmd_writeNodeResults(self, kv):
         g = self.g
         m = self.model
@@ -294,9 +328,14 @@ class Job:
         fmt = lambda v: f"{float(v):.12G}"
         out = [f" time: {fmt(self.time)}", f" timeStep: {self.step}"]
         for fld in fields:
-            if fld in ("temperature", "reactionHeatGen"):
-                vec = self.temp if fld == "temperature" else -(self.therm_load if self.therm_load is not None
-                                                              else np.zeros(m.num_nodes))
+            if fld in ("temperature", "tdot", "reactionHeatGen"):
+                if fld == "temperature":
+                    vec = self.temp
+                elif fld == "tdot":
+                    vec = getattr(self, "tdot", None)
+                    vec = np.zeros(m.num_nodes) if vec is None else vec
+                else:
+                    vec = -(self.therm_load if self.therm_load is not None else np.zeros(m.num_nodes))
                 out.append(f" {fld}:")
                 for nd in nodes:
                     out.append(f"     - [{nd}, {fmt(vec[g.current_rank[nd - 1] - 1])}]")

@@ -108,3 +108,49 @@ def test_newmark_job_segments(tmp_path):
     ug = np.array([[u[g.n_dof_index[nd - 1, k] - 1] for k in range(6)] for nd in range(1, m.num_nodes + 1)])
     uj = np.array([res["displacement"][nd] for nd in range(1, m.num_nodes + 1)])
     assert np.linalg.norm(uj - ug) <= 1e-6 * np.linalg.norm(ug)
+
+
+def test_transient_thermal_job(tmp_path):
+    """solve's thermal time loop: a brick bar at 0 with its left end held at 100, five steps of
+    the generalised trapezoid rule, against the same loop on the oracle's matrices."""
+    m = M.hex_block(6, 2, 2, lx=3.0, ly=1.0, lz=1.0, jitter=0.0)
+    X = m.node_list
+    left = list(np.nonzero(X[:, 0] == 0)[0] + 1)
+    IF.write_model_input(m, tmp_path / "bar.yaml", node_sets={"left": left})
+    txt = (tmp_path / "bar.yaml").read_text()
+    txt = txt[:txt.index("constraints:")]
+    txt = txt.replace("      elastic:\n", "      thermal:\n          conductivity: 45.0\n          specificHeat: 460.0\n"
+                                         "      elastic:\n")
+    txt += "constraints:\n    matrix:\n        - [1, left, 7, 1.0]\n    rhs:\n        - 100.0\n"
+    (tmp_path / "bar.yaml").write_text(txt)
+    (tmp_path / "job.txt").write_text(
+        "*readModelInput:\n    fileName: bar.yaml\n*solve:\n    elastic: no\n    thermal: yes\n    dynamic: yes\n"
+        "    timeStep: 50.0\n    simPeriod: 250.0\n    newmarkGamma: 0.6\n"
+        "*writeNodeResults:\n    fileName: temp.txt\n    fields:\n        - temperature\n        - tdot\n")
+    J.Job(tmp_path).run(tmp_path / "job.txt")
+    res = J.read_node_results(tmp_path / "temp.txt")
+    Tj = np.array([res["temperature"][nd][0] for nd in range(1, m.num_nodes + 1)])
+    # the oracle's loop (rank order)
+    mi = IF.read_model_input(tmp_path / "bar.yaml")
+    o = Oracle(mi.model())
+    cond, sh, mpc = mi.thermal()
+    N, dt, gm = m.num_nodes, 50.0, 0.6
+    T, pT, pTd = np.zeros(N), np.zeros(N), np.zeros(N)
+    _, mat, cols, rng = o.thermal_soln_load(cond, sh, 1, temp=T, prev_temp=pT, prev_tdot=pTd, dynamic=1, gamma=gm,
+                                            del_t=dt)
+    import scipy.sparse as sp
+    K = sp.csr_matrix((mat, cols - 1, rng), shape=(N, N))
+    rows = o.scale_thermal_mpc(mat, o.thermal_mpc(*mpc))
+    r_, c_, v_ = zip(*[(i, c - 1, k) for i, (cs, vs, _) in enumerate(rows) for c, k in zip(cs, vs) if c])
+    Cm = sp.csr_matrix((v_, (r_, c_)), shape=(len(rows), N))
+    A = (K + Cm.T @ Cm).tocsc()
+    for _ in range(5):
+        load = np.zeros(N)
+        o.thermal_soln_load(cond, sh, 0, temp=T, prev_temp=pT, prev_tdot=pTd, dynamic=1, gamma=gm, del_t=dt, load=load)
+        o.thermal_constraint_load(rows, T, load)
+        T = T + spla.spsolve(A, load)
+        Td = (1 / gm) * ((1 / dt) * (T - pT) - (1 - gm) * pTd)
+        pT, pTd = T.copy(), Td
+    To = T[o.current_rank - 1]
+    assert np.linalg.norm(Tj - To) <= 1e-8 * np.linalg.norm(To)
+    assert To.max() > 50.0 and To.min() < 10.0   # heat has entered from the left end, not reached the right
