@@ -80,7 +80,8 @@ class Clocks:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        import tempfile
+        self.path = os.path.join(tempfile.gettempdir(), f"misc_gb300_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
