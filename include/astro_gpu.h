@@ -277,6 +277,15 @@ int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t *face_el,
  * element listed twice adds twice), or NULL for every element.  state: the displacement
  * (centrifugal centroid; shell frame), may be NULL.  Meshes mixing shells and bricks return
  * ASTRO_ERR_UNSUPPORTED. */
+/* The load branch of getdRelasticdD for body loads (Working/AStrO_commandFunctions.f90:1250-1300):
+ * drudd[n] -= d(body load)/d(design variable dvar) for the listed elements that depend on it
+ * (arguments as astro_body_load; h the complex step).  Together with astro_drdd_complex it gives
+ * the reference's dRudD when such loads act.  Brick body loads depend on none of the supported
+ * design-variable categories (the call leaves drudd unchanged); for shells the layup-thickness
+ * variables move the body force (linearly) and the mass of the gravitational and centrifugal
+ * loads (complex step of the mass term). */
+int astro_body_load_drdd(astro_ctx *ctx, int32_t dvar, double h, int32_t kind, const double *vals,
+                         const int32_t *elements, int32_t count, const astro_state *state, double *drudd);
 #define ASTRO_BODY_FORCE 0
 #define ASTRO_BODY_GRAVITY 1
 #define ASTRO_BODY_CENTRIFUGAL 2

@@ -162,6 +162,8 @@ def load_library():
         "astro_constraint_load": ([vp, F64P, F64P], C.c_int),
         "astro_surface_load": ([vp, C.c_int32, I32P, I32P, F64P, C.c_double, F64P], C.c_int),
         "astro_body_load": ([vp, C.c_int32, F64P, I32P, C.c_int32, C.c_void_p, F64P], C.c_int),
+        "astro_body_load_drdd": ([vp, C.c_int32, C.c_double, C.c_int32, F64P, I32P, C.c_int32, C.c_void_p, F64P],
+                                 C.c_int),
         "astro_drdd_complex_condensed": ([vp, C.c_int32, I32P, C.c_double, vp, F64P], C.c_int),
         "astro_thermal_setup": ([vp, C.POINTER(ThermalPropsC), I32P, I32P], C.c_int),
         "astro_thermal_soln_load": ([vp, C.c_int32, C.POINTER(ThermalStateC), F64P, F64P, I32P], C.c_int),
@@ -378,6 +380,17 @@ class AstroGPU:
                                            0 if els is None else len(els),
                                            C.byref(state) if state is not None else None, _d(load)))
         return load
+
+    def body_load_drdd(self, dvar, kind, vals, elements=None, state=None, drudd=None, h=1e-14):
+        """drudd -= d(body load)/d(design variable dvar) (the load branch of getdRelasticdD)."""
+        out = np.zeros(self.n) if drudd is None else drudd
+        v = np.zeros(7)
+        v[:len(vals)] = vals
+        els = None if elements is None else _i32(elements)
+        self._check(self.L.astro_body_load_drdd(self.h, int(dvar), float(h), int(kind), _d(v),
+                                                None if els is None else _i(els), 0 if els is None else len(els),
+                                                C.byref(state) if state is not None else None, _d(out)))
+        return out
 
     def applied_load(self, load=None):
         """Consistent surface load of the model's faces plus its point loads (getElasticAppliedLoad)."""

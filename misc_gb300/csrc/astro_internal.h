@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -172,6 +173,9 @@ int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &s, double *d_loa
 int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // elem_shell4.cu
 int shell4_residual_list(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
                          double *d_loadInt);                                 // elem_shell4.cu
+int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, const std::vector<int> &list,
+                     const std::vector<int> &ptr, double *d_acc, double *d_intAcc,
+                     const std::function<int(const int *, int)> &hook);     // elem_shell4.cu
 int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt);          // elem_shell4.cu
 int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln,
                                 const double *d_intRhs);                                           // elem_shell4.cu

@@ -21,6 +21,7 @@
 // over per-element global scratch, run one element colour at a time; elements of a colour share
 // no node, so their 6x6 block updates never collide (no atomics, deterministic).
 #include <algorithm>
+#include <functional>
 
 #include "astro_internal.h"
 #include "elem_shell4_pipe.cuh"
@@ -194,9 +195,12 @@ __global__ void k_shell_props_im(int count, const int *els, const double *nodes,
         for (int j = 0; j < 6; ++j) P.M[6 * i + j] = M[i][j].im;
 }
 
-int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, double *d_acc, double *d_intAcc) {
-    std::vector<int> list, ptr;
-    dvar_elements_by_colour(ctx, dvar, list, ptr);
+// Complex step of the pipeline's residual over a colour-grouped element list (colour c covering
+// list[ptr[c] .. ptr[c+1])): d_acc -= Im(Ru(d + i h)) (unscaled).  hook, when given, runs before
+// each colour (with that colour's device list and count) and the colours then launch one by one.
+int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, const std::vector<int> &list,
+                     const std::vector<int> &ptr, double *d_acc, double *d_intAcc,
+                     const std::function<int(const int *, int)> &hook) {
     const int cnt = (int)list.size();
     if (!cnt) return ASTRO_OK;
     const int E = ctx->P.E;
@@ -219,12 +223,27 @@ int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, dou
         e = cudaGetLastError();
     }
     rc = cuda_check(ctx, e, "shell complex-step properties");
-    if (!rc)
+    if (!rc && !hook)
         rc = shell_pipeline(ctx, st, dptr<int>(dl), ptr, dptr<ShellProps>(props), kShellRt3c, d_acc, d_intAcc, 0, nullptr,
                             nullptr, nullptr, nullptr);
+    for (size_t c = 0; !rc && hook && c + 1 < ptr.size(); ++c) {
+        const int n = ptr[c + 1] - ptr[c];
+        if (!n) continue;
+        rc = hook(dptr<int>(dl) + ptr[c], n);
+        const std::vector<int> one = {ptr[c], ptr[c + 1]};
+        if (!rc)
+            rc = shell_pipeline(ctx, st, dptr<int>(dl), one, dptr<ShellProps>(props), kShellRt3c, d_acc, d_intAcc, 0,
+                                nullptr, nullptr, nullptr, nullptr);
+    }
     dev_free(dl);
     dev_free(props);
     return rc;
+}
+
+int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, double *d_acc, double *d_intAcc) {
+    std::vector<int> list, ptr;
+    dvar_elements_by_colour(ctx, dvar, list, ptr);
+    return shell4_drdd_list(ctx, dvar, h, st, list, ptr, d_acc, d_intAcc, nullptr);
 }
 
 // ---- internal-DOF recovery (updateExternalRHS / updateInternalSoln) ------------------------------

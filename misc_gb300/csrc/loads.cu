@@ -15,6 +15,8 @@
 //           share no node).  An element listed k times is evaluated in k passes.
 #include <algorithm>
 #include <cmath>
+#include <functional>
+#include <string>
 #include <vector>
 
 #include "astro_internal.h"
@@ -86,6 +88,12 @@ __global__ void k_hex_body(int kind, BodyVals bv, const int *__restrict__ els, i
         for (int d = 0; d < 3; ++d) load[3 * (size_t)r[k] + d] += f * a[d] * w[k];
 }
 
+// out += s a
+__global__ void k_add_scaled(int n, double s, const double *__restrict__ a, double *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += s * a[i];
+}
+
 // out -= b (the pipeline's output is the load -Ru)
 // centripetal acceleration omega^2 (pos - (pos . axis) axis) at centroid c (r_getElCentAcc)
 __device__ __forceinline__ void cent_acc(const BodyVals &bv, const double c[3], double a[3]) {
@@ -105,7 +113,8 @@ __global__ void k_shell_body(BodyVals bv, const int *__restrict__ els, int cnt, 
                              const int *__restrict__ layRange, const LayerDev *__restrict__ lay,
                              const int *__restrict__ e2dR, const int *__restrict__ e2d, const double *__restrict__ e2c,
                              const int *__restrict__ dcat, const int *__restrict__ dlay, const double *__restrict__ dval,
-                             const double *__restrict__ mult, double *__restrict__ load) {
+                             const double *__restrict__ mult, const double *__restrict__ tOverride,
+                             double *__restrict__ load) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= cnt) return;
     const int e = els[i];
@@ -120,10 +129,11 @@ __global__ void k_shell_body(BodyVals bv, const int *__restrict__ els, int cnt, 
             Xl[a][k] = s;
         }
     }
-    // section thickness with the layer-thickness design variables
+    // section thickness with the layer-thickness design variables (or the given per-element factor)
     const int sec = esec[e];
     double t = 0.0;
-    for (int li = layRange[sec - 1], ln = 1; li < layRange[sec]; ++li, ++ln) {
+    if (tOverride) t = tOverride[e];
+    for (int li = layRange[sec - 1], ln = 1; !tOverride && li < layRange[sec]; ++li, ++ln) {
         double tl = lay[li].t;
         if (e2dR)
             for (int q = e2dR[e]; q < e2dR[e + 1]; ++q) {
@@ -255,7 +265,8 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
                         dptr<int>(ctx->d_shLayRange), dptr<LayerDev>(ctx->d_shLay), dv ? dptr<int>(ctx->d_e2dR) : nullptr,
                         dv ? dptr<int>(ctx->d_e2d) : nullptr, dv ? dptr<double>(ctx->d_e2c) : nullptr,
                         dv ? dptr<int>(ctx->d_dCat) : nullptr, dv ? dptr<int>(ctx->d_dLayer) : nullptr,
-                        dv ? dptr<double>(ctx->d_dVal) : nullptr, dptr<double>(T.mult) + ptr[col], dptr<double>(T.li));
+                        dv ? dptr<double>(ctx->d_dVal) : nullptr, dptr<double>(T.mult) + ptr[col], nullptr,
+                        dptr<double>(T.li));
             }
             if ((rc = cuda_check(ctx, cudaGetLastError(), "body load"))) return rc;
         }
@@ -327,6 +338,150 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
     }
     if ((rc = int_to_ref_vec(ctx, dptr<double>(T.li), dptr<double>(T.ref), n))) return rc;
     CK(cudaMemcpyAsync(elastic_load, T.ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}
+
+// d(body load)/d(design variable): drudd -= dF/dd for the listed elements that depend on dvar,
+// the load branch of getdRelasticdD (Working/AStrO_commandFunctions.f90:1250-1300).  Brick body
+// loads depend on none of the design-variable categories of the device complex step; for shells
+// the body force is linear in the section thickness (dF/dd = (dt/dd) b integral of N), and the
+// gravitational and centrifugal loads, the mass residual, are differentiated by the complex step
+// of the pipeline's mass term alone.
+extern "C" int astro_body_load_drdd(astro_ctx *ctx, int32_t dvar, double h, int32_t kind, const double *vals,
+                                    const int32_t *elements, int32_t count, const astro_state *state, double *drudd) {
+    if (!ctx || !vals || !drudd || kind < 0 || kind > 2 || count < 0) return ASTRO_ERR_ARG;
+    if (dvar < 1 || dvar > ctx->numDvars)
+        return set_err(ctx, ASTRO_ERR_ARG, "design variable " + std::to_string(dvar) + " out of range");
+    if (!(h > 0.0)) return set_err(ctx, ASTRO_ERR_ARG, "complex step h must be positive");
+    const AstroPrep &P = ctx->P;
+    const int n = P.n;
+    if (ctx->hasShell && ctx->hasSolid) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "body loads on mixed meshes");
+    if (elements)
+        for (int k = 0; k < count; ++k)
+            if (elements[k] < 1 || elements[k] > P.E) return set_err(ctx, ASTRO_ERR_ARG, "element number out of range");
+    if (ctx->hasSolid || (elements && count == 0)) return ASTRO_OK;
+    // listed elements that depend on dvar, with multiplicity; per element dt/dd
+    std::vector<int> on((size_t)P.E, 0);
+    std::vector<double> dt((size_t)P.E, 0.0);
+    for (int e = 0; e < P.E; ++e)
+        for (int q = ctx->e2dRange[e]; q < ctx->e2dRange[e + 1]; ++q)
+            if (ctx->e2d[q] == dvar) {
+                on[e] = 1;
+                if (ctx->dCat[dvar - 1] == ASTRO_DCAT_LAYUP_THICKNESS) dt[e] += ctx->e2c[q];
+            }
+    if (elements) {
+        std::vector<int> cnt((size_t)P.E, 0);
+        for (int k = 0; k < count; ++k) ++cnt[elements[k] - 1];
+        for (int e = 0; e < P.E; ++e) on[e] *= cnt[e];
+    }
+    const int maxMult = *std::max_element(on.begin(), on.end());
+    if (!maxMult) return ASTRO_OK;
+    struct Tmp {
+        DevBuf ref, li, u, iu, pa, acc, list, mult, dt;
+        ~Tmp() {
+            DevBuf *v[] = {&ref, &li, &u, &iu, &pa, &acc, &list, &mult, &dt};
+            for (DevBuf *p : v) dev_free(*p);
+        }
+    } T;
+    int rc;
+    if ((rc = dev_alloc(ctx, T.ref, sizeof(double) * n)) || (rc = dev_alloc(ctx, T.li, sizeof(double) * n)) ||
+        (rc = dev_alloc(ctx, T.acc, sizeof(double) * n)))
+        return rc;
+    CK(cudaMemcpyAsync(T.ref.p, drudd, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    if ((rc = ref_to_int_vec(ctx, dptr<double>(T.ref), dptr<double>(T.li), n))) return rc;
+    CK(cudaMemsetAsync(T.acc.p, 0, sizeof(double) * n, ctx->stream));
+    BodyVals bv;
+    for (int k = 0; k < 7; ++k) bv.v[k] = (kind == 2 || k < 6) ? vals[k] : 0.0;
+    if (kind == 0) {
+        // dF/dd into acc, then li -= acc
+        std::vector<int> list, ptr(1, 0);
+        std::vector<double> mult;
+        for (int col = 0; col < P.ncolors; ++col) {
+            for (int k = P.colorPtr[col]; k < P.colorPtr[col + 1]; ++k)
+                if (on[P.colorEls[k]]) {
+                    list.push_back(P.colorEls[k]);
+                    mult.push_back((double)on[P.colorEls[k]]);
+                }
+            ptr.push_back((int)list.size());
+        }
+        if ((rc = upload(ctx, T.list, list.data(), sizeof(int) * list.size())) ||
+            (rc = upload(ctx, T.mult, mult.data(), sizeof(double) * mult.size())) ||
+            (rc = upload(ctx, T.dt, dt.data(), sizeof(double) * dt.size())))
+            return rc;
+        for (int col = 0; col < P.ncolors; ++col) {
+            const int cnt = ptr[col + 1] - ptr[col];
+            if (!cnt) continue;
+            k_shell_body<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
+                bv, dptr<int>(T.list) + ptr[col], cnt, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist),
+                dptr<int>(ctx->d_rank), dptr<ShellProps>(ctx->d_secABD), dptr<int>(ctx->d_esec),
+                dptr<int>(ctx->d_shLayRange), dptr<LayerDev>(ctx->d_shLay), nullptr, nullptr, nullptr, nullptr, nullptr,
+                nullptr, dptr<double>(T.mult) + ptr[col], dptr<double>(T.dt), dptr<double>(T.acc));
+        }
+        k_sub<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, dptr<double>(T.acc), dptr<double>(T.li));
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "body load derivative"))) return rc;
+    } else {
+        if (state && state->node_disp) {
+            DevBuf hb;
+            rc = upload(ctx, hb, state->node_disp, sizeof(double) * n);
+            if (!rc) rc = dev_alloc(ctx, T.u, sizeof(double) * n);
+            if (!rc) rc = ref_to_int_vec(ctx, dptr<double>(hb), dptr<double>(T.u), n);
+            if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "state upload");
+            dev_free(hb);
+            if (rc) return rc;
+        } else {
+            if ((rc = dev_alloc(ctx, T.u, sizeof(double) * n))) return rc;
+            CK(cudaMemsetAsync(T.u.p, 0, sizeof(double) * n, ctx->stream));
+        }
+        const int ni = P.intVecSize;
+        if (ni > 0) {
+            if (state && state->internal_disp) {
+                if ((rc = upload(ctx, T.iu, state->internal_disp, sizeof(double) * ni))) return rc;
+            } else {
+                if ((rc = dev_alloc(ctx, T.iu, sizeof(double) * ni))) return rc;
+                CK(cudaMemsetAsync(T.iu.p, 0, sizeof(double) * ni, ctx->stream));
+            }
+        }
+        std::vector<double> pa((size_t)n, 0.0);
+        if (kind == 1)
+            for (int r = 0; r < P.N; ++r)
+                for (int c = 0; c < P.dpn; ++c) pa[(size_t)r * P.dpn + c] = -vals[c];
+        if ((rc = upload(ctx, T.pa, pa.data(), sizeof(double) * n))) return rc;
+        ShellDevState s1;
+        s1.disp = dptr<double>(T.u);
+        s1.idisp = ni > 0 ? dptr<double>(T.iu) : nullptr;
+        s1.pdisp = s1.disp;
+        s1.pacc = dptr<double>(T.pa);
+        s1.pidisp = s1.idisp;
+        s1.dynamic = 1;
+        s1.beta = 0.25;
+        s1.gamma = 0.5;
+        s1.delT = 1.0;
+        s1.massOnly = 1;
+        const bool zeroState = !(state && state->node_disp);
+        for (int pass = 0; pass < maxMult; ++pass) {
+            std::vector<int> list, ptr(1, 0);
+            for (int col = 0; col < P.ncolors; ++col) {
+                for (int k = P.colorPtr[col]; k < P.colorPtr[col + 1]; ++k)
+                    if (on[P.colorEls[k]] > pass) list.push_back(P.colorEls[k]);
+                ptr.push_back((int)list.size());
+            }
+            std::function<int(const int *, int)> hook;
+            if (kind == 2)
+                hook = [&](const int *d_els, int cnt) {
+                    k_shell_cent_pacc<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(
+                        bv, d_els, cnt, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist), dptr<int>(ctx->d_rank),
+                        zeroState ? nullptr : dptr<double>(T.u), dptr<double>(T.pa));
+                    return cuda_check(ctx, cudaGetLastError(), "centrifugal acceleration");
+                };
+            if ((rc = shell4_drdd_list(ctx, dvar, h, s1, list, ptr, dptr<double>(T.acc), nullptr, hook))) return rc;
+        }
+        // acc = -Im(Rum(d + i h)): dF/dd = -acc / h, drudd -= dF/dd
+        k_add_scaled<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, 1.0 / h, dptr<double>(T.acc), dptr<double>(T.li));
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "body load derivative"))) return rc;
+    }
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(T.li), dptr<double>(T.ref), n))) return rc;
+    CK(cudaMemcpyAsync(drudd, T.ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return ASTRO_OK;
 }

@@ -147,3 +147,39 @@ def test_shell_bad_arguments(plate):
     with pytest.raises(AstroError):
         g.body_load(5, [0.0, 0.0, -9.81])
     assert np.array_equal(g.body_load(0, [1.0, 0, 0], elements=[]), np.zeros(o.n))
+
+
+@pytest.mark.parametrize("kind,vals", [
+    (0, [1.0, -2.0, 0.5, 0.3, -0.2, 0.1]),
+    (1, [0.5, 0.0, -9.81, 0.1, 0.0, 0.0]),
+    (2, [0.3, 0.2, 0.0, 0.0, 0.2, 1.0, 30.0]),
+])
+def test_shell_body_load_design_derivative(kind, vals):
+    """d(load)/d(thickness group) for shell body loads (getdRelasticdD's load branch) against
+    central differences of the oracle's body load over the design variable's value; element
+    subsets with repeats, a displaced state; bricks add nothing."""
+    def mk(dv=None):
+        m = M.add_design_variables(_plate(), 3, M.DCAT_LAYUP_THICKNESS)
+        if dv is not None:
+            m.d_value = np.asarray(dv, np.float64)
+        return m
+    m = mk()
+    g = AstroGPU(m)
+    rng = np.random.default_rng(2)
+    st = M.make_state(g.n, disp=1e-3 * rng.standard_normal(g.n), internal_disp=1e-5 * rng.standard_normal(g.int_vec_size))
+    for els in (None, np.array([1, 2, 2, 9, m.num_els])):
+        for d in (1, 3):
+            got = g.body_load_drdd(d, kind, vals, elements=els, state=st)
+            step = 1e-6
+            e = np.zeros(3)
+            e[d - 1] = step
+            fp = Oracle(mk(e)).body_load(kind, vals, elements=els, state=st)
+            fm = Oracle(mk(-e)).body_load(kind, vals, elements=els, state=st)
+            fd = -(fp - fm) / (2 * step)
+            if np.linalg.norm(fd) == 0.0:
+                assert np.linalg.norm(got) == 0.0
+            else:
+                _close(got, fd, 1e-6)
+    b = M.add_design_variables(M.hex_block(3, 2, 2, seed=1), 2, M.DCAT_ELASTIC_MODULUS)
+    gb = AstroGPU(b)
+    assert np.array_equal(gb.body_load_drdd(1, 1, [0, 0, -9.81]), np.zeros(gb.n))
