@@ -58,6 +58,7 @@ def _parse():
     p.add_argument("--eval-nx", type=int, default=96)
     p.add_argument("--panels", type=int, default=512, help="panels of the batched-panel leg (0: skip it)")
     p.add_argument("--newmark-steps", type=int, default=200, help="time steps of the Newmark leg (0: skip it)")
+    p.add_argument("--no-widened", action="store_true", help="skip the thermal / adjoint / body-load leg")
     p.add_argument("--panels-only", action="store_true", help="only the batched-panel leg")
     p.add_argument("--panels-cluster", type=int, default=0, help="cluster size (0: autotuned over 2, 4, 8)")
     return p.parse_args()
@@ -340,6 +341,8 @@ def run_ours(a):
         line["batched_panels"] = _panels_eval(a)
     if a.newmark_steps > 0 and rank == 0:
         line["newmark"] = _newmark_eval(a)
+    if not a.no_widened and rank == 0:
+        line["widened"] = _widened_eval(a)
     # CPU baseline: oracle, 1 core, bounded sample
     if rank == 0:
         rate, dt = _oracle_rate(m, 1024, 1)
@@ -527,6 +530,53 @@ def _newmark_eval(a):
     out["speedup_learned_vs_fp64"] = out["gmres_fp64"]["ms_per_step"] / out["fgmres_learned"]["ms_per_step"]
     out["rel_diff_final_disp"] = float(np.linalg.norm(res["fgmres_learned"] - res["gmres_fp64"]) /
                                        max(np.linalg.norm(res["gmres_fp64"]), 1e-300))
+    del g
+    gc.collect()
+    return out
+
+
+def _widened_eval(a):
+    """Device times of the widened rows on the 64x32x32 brick block (212,355 DOF), CUDA-synchronous
+    host clock, best of three: the gravitational body load (astro_body_load), the static design
+    gradient for 8 modulus variables (astro_total_dldd: adjoint solve by the learned solver to
+    1e-10 plus eight complex-step dR/dd), the thermal conductivity assembly
+    (astro_thermal_soln_load) and the thermal CG solve to 1e-10 with the x = 0 face held."""
+    import gc
+    from misc_gb300 import model as M
+    from misc_gb300.astro import SOLVER_FGMRES_LEARNED, AstroGPU, make_state, thermal_props
+    gc.collect()
+    m = M.add_design_variables(M.config2(), 8, M.DCAT_ELASTIC_MODULUS)
+    g = AstroGPU(m)
+    g.getElasticSolnLoad(1, export=False)
+    g.assemble_fp32()
+    g.scaleElasticMPC()
+    b = g.static_rhs()
+    u, _ = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=1e-10)
+    st = make_state(g.n, disp=u)
+
+    def best(fn, k=3):
+        ts = []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        return min(ts)
+    out = {"workload": "64x32x32 brick8 block (212,355 DOF), 8 elastic-modulus design variables"}
+    out["body_load_gravity_s"] = best(lambda: g.body_load(1, [0.0, 0.0, -9.81]))
+    w = np.random.default_rng(3).standard_normal(g.n)
+    out["total_dldd_s"] = best(lambda: g.getTotaldLdD(w, state=st, rtol=1e-10, method=SOLVER_FGMRES_LEARNED), k=2)
+    nm = len(m.material_density)
+    X = m.node_list
+    left = np.nonzero(X[:, 0] == 0)[0] + 1
+    mpc = (np.arange(len(left) + 1), left, np.ones(len(left)), np.full(len(left), 100.0))
+    g.thermal_setup(thermal_props(np.tile([45.0, 45.0, 45.0, 0.0, 0.0, 0.0], (nm, 1)), np.full(nm, 460.0), mpc))
+    out["thermal_assembly_s"] = best(lambda: g.getThermalSolnLoad(1, export=False))
+    g.scaleThermalMPC()
+    q = g.thermal_heat_gen(1.0e3)
+    rhs = g.getThermalConstraintLoad(None, q.copy())
+    x, ts = g.thermal_solve(rhs, rtol=1e-10)
+    out["thermal_solve"] = {"seconds": ts.seconds, "iterations": ts.iterations, "rel_residual": ts.rel_residual,
+                            "nodes": m.num_nodes}
     del g
     gc.collect()
     return out
