@@ -783,9 +783,6 @@ extern "C" int astro_thermal_solve(astro_ctx *ctx, const double *rhs, double *dt
     const AstroPrep &P = ctx->P;
     const int N = P.N;
     cudaStream_t s = ctx->stream;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
     DevBuf b, x, r, z, p, Ap, dinv, part, sc;
     int rc;
     if ((rc = upload(ctx, b, rhs, sizeof(double) * N)) || (rc = upload(ctx, x, dtemp, sizeof(double) * N)) ||
@@ -797,6 +794,9 @@ extern "C" int astro_thermal_solve(astro_ctx *ctx, const double *rhs, double *dt
         for (DevBuf *q : v) dev_free(*q);
         return rc;
     }
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
     const unsigned rg = (N + 255) / 256;
     const int *pp = T->mpcDim ? dptr<int>(T->d_penPtr) : nullptr;
     double *S = dptr<double>(sc);

@@ -206,6 +206,9 @@ class Job:
         self.mi = IF.read_model_input(self.dir / kv["fileName"])
         self.model = self.mi.model(name=Path(kv["fileName"]).stem)
         self.g = None
+        self.thermal_ready = False
+        if hasattr(self, "_exterior"):
+            del self._exterior
         self.log.append(f"read model {kv['fileName']}: {self.mi.num_nodes} nodes, {self.mi.num_els} elements")
 
     def cmd_readDesignVarInput(self, kv):
