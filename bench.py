@@ -208,6 +208,7 @@ def run_ours(a):
     cudart.cudaEventElapsedTime.argtypes = [C.POINTER(C.c_float), C.c_void_p, C.c_void_p]
     cudart.cudaEventSynchronize.argtypes = [C.c_void_p]
     cudart.cudaDeviceSynchronize.argtypes = []
+    cudart.cudaMemsetAsync.argtypes = [C.c_void_p, C.c_int, C.c_size_t, C.c_void_p]
     s = L.astro_ctx_stream(g.h)
     ev = [C.c_void_p() for _ in range(2 * a.steps)]
     for e in ev:
@@ -222,9 +223,11 @@ def run_ours(a):
     clk = Clocks()
     clk.start()
     t0 = time.perf_counter()
+    # the L2 flush is queued on the library's stream ahead of each step, and the host does not
+    # wait between steps: the events bracket the device work of the pass alone, not the host's
+    # launch latency (that latency is in the end-to-end figure)
     for k in range(a.steps):
-        flush.fill_(k & 0xFF)
-        torch.cuda.synchronize()
+        assert cudart.cudaMemsetAsync(flush.data_ptr(), k & 0xFF, flush.numel(), s) == 0
         cudart.cudaEventRecord(ev[2 * k], s)
         rc = L.astro_assemble_fp32_async(g.h)
         assert rc == 0
