@@ -337,7 +337,7 @@ constexpr int kRmwSteps = 22;  // ceil(64 blocks / 3 blocks per step)
 
 template <class T> struct FastCfg;
 template <> struct FastCfg<float> {
-    static constexpr int FW = 8, MINB = 3;  // warps per CTA, CTAs per SM
+    static constexpr int FW = 2, MINB = 14;  // warps per CTA, CTAs per SM (small CTAs: shorter colour tails)
     static constexpr bool PREFETCH = true;
 };
 template <class T> struct Hex8FastArgs {
