@@ -33,6 +33,8 @@ extern "C" {
 #define ASTRO_ERR_MAXIT 7        /* iteration limit reached before the tolerance */
 #define ASTRO_ERR_STATE 8        /* call out of order (e.g. solve before factorisation) */
 #define ASTRO_ERR_NOMEM 9        /* device allocation failed */
+#define ASTRO_ERR_BOUNDS 10      /* library built with ASTRO_BOUNDS_CHECK only: a device index guard
+                                    found an index outside its buffer and skipped the access */
 
 /* Design-variable categories supported by the complex-step path (reference dCategory/dSubCat). */
 #define ASTRO_DCAT_LAYUP_THICKNESS 1   /* 'layup' / 'thickness' of layer d_layer */
@@ -147,6 +149,11 @@ typedef struct astro_solve_stats {
     int32_t fallback;        /* learned solver: 1 when it ended in a non-finite value, a breakdown or
                                 the iteration cap and the FP32 Jacobi solver finished the solve from
                                 the initial guess (the counts and seconds then cover both) */
+    int32_t residual_kind;   /* the matrix values rel_residual was formed with: 64 = the FP64
+                                assembly (astro_el_soln_load), the system the tolerance refers to;
+                                32 = only the FP32 assembly was resident (astro_assemble_fp32 alone),
+                                so rel_residual is that of the FP32-rounded system, computed in FP64
+                                arithmetic; 0 = no solve ran */
 } astro_solve_stats;
 
 typedef struct astro_ctx astro_ctx;
@@ -399,10 +406,11 @@ int astro_ldl_solve(astro_ctx *ctx, double *soln, const double *rhs, const doubl
  * All operands are the caller's DEVICE buffers (soln, rhs: l_dim; l_mat: the factor;
  * l_range: l_dim+1 row ranges); the forward-sweep scratch is a fixed 2 MiB array in the
  * library, so l_dim is limited to ASTRO_LDL_NOALLOC_MAX_DIM (larger sizes return
- * ASTRO_ERR_ARG without touching the GPU).  The first call on each device looks up the
- * scratch address (make it before any stream capture begins).  The scratch is shared by all
- * contexts on a device: overlapping calls on one device race and must be serialised.
- * Runs on the context's stream and returns after it completes. */
+ * ASTRO_ERR_ARG without touching the GPU).  Every call looks up the scratch's device address
+ * with the context's device current; the first lookup on a device may load the library's module,
+ * so make the first call before any stream capture begins.  The scratch is shared by all contexts
+ * on a device and keeps the last call's values: overlapping calls on one device race and must be
+ * serialised.  Runs on the context's stream and returns after it completes. */
 #define ASTRO_LDL_NOALLOC_MAX_DIM 262144
 int astro_ldl_solve_device_noalloc(astro_ctx *ctx, double *d_soln, const double *d_rhs,
                                    const double *d_l_mat, const int32_t *d_l_range, int32_t l_dim);

@@ -20,7 +20,7 @@ F64P = C.POINTER(C.c_double)
 ASTRO_OK = 0
 ERRORS = {1: "ASTRO_ERR_ARG", 2: "ASTRO_ERR_CUDA", 3: "ASTRO_ERR_UNSUPPORTED", 4: "ASTRO_ERR_PIVOT",
           5: "ASTRO_ERR_NAN", 6: "ASTRO_ERR_BREAKDOWN", 7: "ASTRO_ERR_MAXIT", 8: "ASTRO_ERR_STATE",
-          9: "ASTRO_ERR_NOMEM"}
+          9: "ASTRO_ERR_NOMEM", 10: "ASTRO_ERR_BOUNDS"}
 SOLVER_GMRES_JACOBI_FP64 = 0
 SOLVER_FGMRES_MIXED = 1
 SOLVER_FGMRES_LEARNED = 2
@@ -124,7 +124,7 @@ class TransientAdjointC(C.Structure):
 class SolveStatsC(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("restarts", C.c_int32), ("refinements", C.c_int32),
                 ("status", C.c_int32), ("rel_residual", C.c_double), ("seconds", C.c_double),
-                ("conditional_graph", C.c_int32), ("fallback", C.c_int32)]
+                ("conditional_graph", C.c_int32), ("fallback", C.c_int32), ("residual_kind", C.c_int32)]
 
 
 class NewmarkOptsC(C.Structure):
@@ -134,7 +134,10 @@ class NewmarkOptsC(C.Structure):
 
 
 def lib_path():
-    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libastro_gpu.so")
+    """The in-tree library; with ASTRO_BOUNDS_CHECK=1 in the environment, the checked build
+    (device index guards that return ASTRO_ERR_BOUNDS instead of touching memory out of bounds)."""
+    name = "libastro_gpu_checked.so" if os.environ.get("ASTRO_BOUNDS_CHECK") else "libastro_gpu.so"
+    return os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", name)
 
 
 def load_library():

@@ -1,7 +1,10 @@
 """Builds libastro_gpu.so in-tree with nvcc for sm_103a (no torch involved).
 
 Each translation unit under csrc/ is compiled in parallel to an object file, then linked into
-misc_gb300/_lib/libastro_gpu.so.  Rebuilds only what changed.
+misc_gb300/_lib/libastro_gpu.so.  Rebuilds only what changed.  With ASTRO_BOUNDS_CHECK=1 in the
+environment the checked build (device index guards, csrc/bounds.cuh) goes to
+misc_gb300/_lib/libastro_gpu_checked.so instead, which misc_gb300.astro loads under the same
+variable.
 """
 from __future__ import annotations
 
@@ -23,6 +26,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", 
 if os.environ.get("ASTRO_BOUNDS_CHECK"):
     FLAGS += ["-DASTRO_BOUNDS_CHECK"]
     BUILD = BUILD + "_checked"
+    LIB = os.path.join(OUT, "libastro_gpu_checked.so")
 
 
 def lib_path():

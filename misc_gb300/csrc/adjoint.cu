@@ -142,6 +142,7 @@ extern "C" int astro_total_dldd_transient(astro_ctx *ctx, const astro_transient_
         acc.seconds += s.seconds;
         acc.rel_residual = std::max(acc.rel_residual, s.rel_residual);
         acc.conditional_graph = s.conditional_graph;
+        acc.residual_kind = s.residual_kind;
         if (rc) {
             acc.status = rc;
             if (stats) *stats = acc;

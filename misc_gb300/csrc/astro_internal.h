@@ -137,12 +137,14 @@ struct astro_ctx {
     // scratch
     DevBuf d_scratch;
     DevBuf d_status;  // int status words written by kernels
+    DevBuf d_guard;   // checked build: site of the first failed index guard (bounds.cuh), else 0
     int quirkShellMeanRot = 0;
 };
 
 // error helpers
 int set_err(astro_ctx *c, int code, const std::string &msg);
 int cuda_check(astro_ctx *c, cudaError_t e, const char *what);
+int guard_status(astro_ctx *c, const char *what);
 #define CK(call)                                                  \
     do {                                                          \
         cudaError_t e__ = (call);                                 \

@@ -22,6 +22,17 @@ int set_err(astro_ctx *c, int code, const std::string &msg) {
     return code;
 }
 
+// Checked build: the site of the first index guard that failed since the last call (bounds.cuh),
+// as ASTRO_ERR_BOUNDS; the word is cleared for the next launch.
+int guard_status(astro_ctx *c, const char *what) {
+    int site = 0;
+    cudaError_t e = cudaMemcpy(&site, c->d_guard.p, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_check(c, e, what);
+    if (!site) return ASTRO_OK;
+    cudaMemset(c->d_guard.p, 0, sizeof(int));
+    return set_err(c, ASTRO_ERR_BOUNDS, std::string(what) + ": index guard " + std::to_string(site) + " failed");
+}
+
 int cuda_check(astro_ctx *c, cudaError_t e, const char *what) {
     if (e == cudaSuccess) return ASTRO_OK;
     return set_err(c, e == cudaErrorMemoryAllocation ? ASTRO_ERR_NOMEM : ASTRO_ERR_CUDA,
@@ -71,7 +82,8 @@ static void free_all(astro_ctx *c) {
                       &c->d_penPtr, &c->d_penCol,  &c->d_penVal,  &c->d_ltRange, &c->d_lt,       &c->d_scratch,
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
                       &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_elXdf, &c->d_elCdf, &c->d_ioRef,
-                      &c->d_ioInt, &c->d_exMat, &c->d_exCols, &c->d_shFr, &c->d_shGp, &c->d_shDe, &c->d_shKf};
+                      &c->d_ioInt, &c->d_exMat, &c->d_exCols, &c->d_shFr, &c->d_shGp, &c->d_shDe, &c->d_shKf,
+                      &c->d_guard};
     for (DevBuf *b : bufs) dev_free(*b);
 }
 
@@ -218,6 +230,8 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
 #undef UP
     if ((rc = dev_alloc(ctx, ctx->d_status, 256))) return fail(rc, ctx->err);
     cudaMemset(ctx->d_status.p, 0, 256);
+    if ((rc = dev_alloc(ctx, ctx->d_guard, sizeof(int)))) return fail(rc, ctx->err);
+    cudaMemset(ctx->d_guard.p, 0, sizeof(int));
     if (ctx->hasShell && (rc = shell_sections_prepare(ctx, m))) return fail(rc, ctx->err);
     if (ctx->hasSolid && (rc = hex8_prepare(ctx))) return fail(rc, ctx->err);
     // unscaled constraints in internal numbering
@@ -1260,6 +1274,7 @@ extern "C" int astro_step_solve(astro_ctx *ctx, const astro_step_opts *o, const 
         acc.rel_residual = std::max(acc.rel_residual, s.rel_residual);
         acc.conditional_graph = s.conditional_graph;
         acc.fallback |= s.fallback;
+        acc.residual_kind = s.residual_kind;
         if (rc && rc != ASTRO_ERR_MAXIT) return rc;
         if (rc == ASTRO_ERR_MAXIT) acc.status = rc;
         if (hasInt && (rc = shell4_update_internal_soln(ctx, dptr<double>(T.du), dptr<double>(T.iu), dptr<double>(T.iload))))

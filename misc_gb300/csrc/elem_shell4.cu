@@ -24,6 +24,7 @@
 #include <functional>
 
 #include "astro_internal.h"
+#include "bounds.cuh"
 #include "elem_shell4_pipe.cuh"
 
 // Resource attributes of the shell kernels (no launch), for diagnostics.
@@ -134,6 +135,11 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
     A.intMat = d_intMat;
     A.keOut = d_ke;
     A.ruOut = d_ru;
+    A.nNodes = ctx->P.N;
+    A.nEls = ctx->P.E;
+    A.nBlocks = ctx->P.nb;
+    A.scratchEls = ctx->shScratchEls;
+    A.status = ASTRO_CHECKED ? dptr<int>(ctx->d_guard) : nullptr;
     cudaStream_t s = ctx->stream;
     for (size_t col = 0; col + 1 < ptr.size(); ++col) {
         const int cnt = ptr[col + 1] - ptr[col];
@@ -154,7 +160,8 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
         k_shell_scatter<<<(32 * cnt + 127) / 128, 128, 0, s>>>(A);
     }
     cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess && sync) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && (sync || ASTRO_CHECKED)) e = cudaStreamSynchronize(s);
+    if (e == cudaSuccess && ASTRO_CHECKED) return guard_status(ctx, "shell pipeline");
     return cuda_check(ctx, e, "shell pipeline");
 }
 

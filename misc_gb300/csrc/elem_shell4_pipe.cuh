@@ -15,6 +15,7 @@
 //                                            block-CSR update (with a matrix only)
 //   scatter  thread per (element, DOF):      residual into the load vectors
 #pragma once
+#include "bounds.cuh"
 #include "shell_props.cuh"
 
 namespace {
@@ -57,14 +58,21 @@ struct ShellPipe {
     double *dedU;    // count*4*32*9
     double *Kf;      // count*32*33: column j = 33 values (K(0..31, j), Ru_j)
     double *K, *load, *intLoad, *intMat, *keOut, *ruOut;
+    // sizes the index guards of the checked build test against (bounds.cuh): nodes, elements,
+    // block-CSR blocks, elements the scratch above holds; status receives the failing guard's site
+    int nNodes, nEls, nBlocks, scratchEls;
+    int *status;
 };
 
 // The frame stage in three parts: the gather (per element), the ten frame rotations (per
 // element and rotation: the instantaneous frame and its first and second derivatives, the costly
 // part), then the axial vectors, the (0,0) instantaneous DOF and the Newmark acceleration.
 __device__ void pipe_frame_gather(const ShellPipe &A, int q) {
+    ASTRO_GUARD(A.status, 101, ASTRO_IN(q, A.scratchEls));
     const int e = A.els[q];
+    ASTRO_GUARD(A.status, 102, ASTRO_IN(e, A.nEls));
     const int *el = A.elist + 8 * (size_t)e;
+    for (int a = 0; a < 4; ++a) ASTRO_GUARD(A.status, 103, ASTRO_IN(el[a] - 1, A.nNodes));
     const ShellProps &P = A.props[e];
     ShellFrame &F = A.fr[q];
     double orient[3][3];
@@ -78,6 +86,7 @@ __device__ void pipe_frame_gather(const ShellPipe &A, int q) {
         }
     int rk[4];
     for (int a = 0; a < 4; ++a) rk[a] = A.rank[el[a] - 1] - 1;
+    for (int a = 0; a < 4; ++a) ASTRO_GUARD(A.status, 104, ASTRO_IN(rk[a], A.nNodes));
     if (A.disp)
         for (int a = 0; a < 4; ++a)
             for (int v = 0; v < 6; ++v) F.u[v][a] = A.disp[6 * (size_t)rk[a] + v];
@@ -85,6 +94,7 @@ __device__ void pipe_frame_gather(const ShellPipe &A, int q) {
         for (int k = 24; k < 32; ++k) {
             int var, nd;
             dof_of(k, var, nd);
+            ASTRO_GUARD(A.status, 105, ASTRO_IN(var - 1, 6) && ASTRO_IN(nd - 1, 11));
             F.u[var - 1][nd - 1] = A.idisp[8 * (size_t)e + k - 24];
         }
     for (int a = 0; a < 4; ++a)
@@ -93,7 +103,9 @@ __device__ void pipe_frame_gather(const ShellPipe &A, int q) {
 }
 
 __device__ void pipe_frame_rot(const ShellPipe &A, int q, int v) {
+    ASTRO_GUARD(A.status, 111, ASTRO_IN(q, A.scratchEls) && ASTRO_IN(v, 10));
     const int e = A.els[q];
+    ASTRO_GUARD(A.status, 112, ASTRO_IN(e, A.nEls));
     const ShellProps &P = A.props[e];
     ShellFrame &F = A.fr[q];
     double orient[3][3];
@@ -102,6 +114,7 @@ __device__ void pipe_frame_rot(const ShellPipe &A, int q, int v) {
     {
         const int bi = (v == 0) ? 0 : (v < 4 ? v : (v < 7 ? 1 : (v < 9 ? 2 : 3)));
         const int bj = (v < 4) ? 0 : (v < 7 ? v - 3 : (v < 9 ? v - 5 : 3));
+        ASTRO_GUARD(A.status, 113, ASTRO_IN(bi, 4) && ASTRO_IN(bj, 4));
         double out[3][3];
         a_rotate<double>(out, orient, F.rot, bi, bj);
         int b1, b2;
@@ -121,7 +134,9 @@ __device__ void pipe_frame_rot(const ShellPipe &A, int q, int v) {
 }
 
 __device__ void pipe_frame_rest(const ShellPipe &A, int q) {
+    ASTRO_GUARD(A.status, 121, ASTRO_IN(q, A.scratchEls));
     const int e = A.els[q];
+    ASTRO_GUARD(A.status, 122, ASTRO_IN(e, A.nEls));
     const int *el = A.elist + 8 * (size_t)e;
     const ShellProps &P = A.props[e];
     ShellFrame &F = A.fr[q];
@@ -129,10 +144,12 @@ __device__ void pipe_frame_rest(const ShellPipe &A, int q) {
     for (int i = 0; i < 9; ++i) orient[i / 3][i % 3] = P.orient[i];
     int rk[4];
     for (int a = 0; a < 4; ++a) rk[a] = A.rank[el[a] - 1] - 1;
+    for (int a = 0; a < 4; ++a) ASTRO_GUARD(A.status, 123, ASTRO_IN(rk[a], A.nNodes));
     for (int v = 1; v < 10; ++v) {
         const int bi = (v < 4) ? v : (v < 7 ? 1 : (v < 9 ? 2 : 3));
         const int bj = (v < 4) ? 0 : (v < 7 ? v - 3 : (v < 9 ? v - 5 : 3));
         const int blk = (bj == 0) ? bi : 4 * bi + bj;
+        ASTRO_GUARD(A.status, 124, ASTRO_IN(blk, 16) && ASTRO_IN(4 * bi + bj, 16) && ASTRO_IN(4 * bj + bi, 16));
         double pr[3][3];
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b)
@@ -170,6 +187,7 @@ __device__ void pipe_frame_rest(const ShellPipe &A, int q) {
     for (int k = 24; k < 32; ++k) {
         int var, nd;
         dof_of(k, var, nd);
+        ASTRO_GUARD(A.status, 125, ASTRO_IN(var - 1, 6) && ASTRO_IN(nd - 1, 11));
         F.U0[var - 1][nd - 1] = F.u[var - 1][nd - 1];
     }
     if (A.dynamic) {
@@ -185,6 +203,7 @@ __device__ void pipe_frame_rest(const ShellPipe &A, int q) {
 }
 
 __device__ void pipe_gauss(const ShellPipe &A, int q, int g) {
+    ASTRO_GUARD(A.status, 131, ASTRO_IN(q, A.scratchEls) && ASTRO_IN(g, 4) && ASTRO_IN(A.els[q], A.nEls));
     const ShellFrame &F = A.fr[q];
     ShellGP &G = A.gp[4 * (size_t)q + g];
     const ShellProps &P = A.props[A.els[q]];
@@ -342,6 +361,12 @@ __device__ void def_second(const ShellFrame &F, const ShellGP &G, int i, int j, 
 }
 
 __device__ void pipe_dedu(const ShellPipe &A, int q, int g, int i) {
+    ASTRO_GUARD(A.status, 141, ASTRO_IN(q, A.scratchEls) && ASTRO_IN(g, 4) && ASTRO_IN(i, 32));
+    {
+        int var, nd;
+        dof_of(i, var, nd);
+        ASTRO_GUARD(A.status, 142, var >= 1 && var <= 6 && nd >= 1 && nd <= 10);
+    }
     double d[9];
     def_first(A.fr[q], A.gp[4 * (size_t)q + g], i, A.quirk, d);
     double *o = A.dedU + (((size_t)q * 4 + g) * 32 + i) * 9;
@@ -364,6 +389,7 @@ __device__ __forceinline__ void mass_dof(const ShellFrame &F, int i, int &nd, do
 // instNodalAcc = sum_i acc(var_i, nd_i) * d instU / d u_i (nodal part) and iNAM = M instNodalAcc
 // for node n of the element (r_getElRum), the DOF of the node in their order
 __device__ void pipe_inam(const ShellPipe &A, int q, int n) {
+    ASTRO_GUARD(A.status, 151, ASTRO_IN(q, A.scratchEls) && ASTRO_IN(n, 4) && ASTRO_IN(A.els[q], A.nEls));
     const ShellProps &P = A.props[A.els[q]];
     ShellFrame &F = A.fr[q];
     double ina[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
@@ -382,6 +408,7 @@ __device__ void pipe_inam(const ShellPipe &A, int q, int n) {
 }
 
 __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
+    ASTRO_GUARD(A.status, 161, ASTRO_IN(q, A.scratchEls) && ASTRO_IN(j, 32) && ASTRO_IN(A.els[q], A.nEls));
     const ShellProps &P = A.props[A.els[q]];
     const ShellFrame &F = A.fr[q];
     double *out = A.Kf + ((size_t)q * 32 + j) * 33;
@@ -467,7 +494,9 @@ __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
 // update, and its outputs (block-CSR, element matrix, internal rows); the residual is scattered
 // by k_shell_scatter
 __device__ void pipe_cond_lu(const ShellPipe &A, int q) {
+    ASTRO_GUARD(A.status, 171, ASTRO_IN(q, A.scratchEls));
     const int e = A.els[q];
+    ASTRO_GUARD(A.status, 172, ASTRO_IN(e, A.nEls));
     double *Kq = A.Kf + (size_t)q * 32 * 33;
     double L[8][8];
     for (int r = 0; r < 8; ++r)
@@ -483,7 +512,9 @@ __device__ void pipe_cond_lu(const ShellPipe &A, int q) {
 }
 
 __device__ void pipe_cond_col(const ShellPipe &A, int q, int j) {
+    ASTRO_GUARD(A.status, 181, ASTRO_IN(q, A.scratchEls) && ASTRO_IN(j, 24));
     const int e = A.els[q];
+    ASTRO_GUARD(A.status, 182, ASTRO_IN(e, A.nEls));
     double *Kq = A.Kf + (size_t)q * 32 * 33;
     double L[8][8];
     for (int r = 0; r < 8; ++r)
@@ -506,6 +537,7 @@ __device__ void pipe_cond_col(const ShellPipe &A, int q, int j) {
         if (A.K) {
             const int rvar = i / 4, a = i % 4;
             const int blk = A.elBlk[16 * (size_t)e + 4 * a + bn];
+            ASTRO_GUARD(A.status, 183, ASTRO_IN(blk, A.nBlocks));
             A.K[36 * (size_t)blk + 6 * rvar + cvar] += v;
         }
         if (A.keOut) A.keOut[576 * (size_t)e + 24 * (size_t)j + i] = v;
@@ -543,11 +575,15 @@ __global__ void k_shell_scatter(ShellPipe A) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 32 * A.count) return;
     const int q = t / 32, i = t % 32;
+    ASTRO_GUARD(A.status, 191, ASTRO_IN(q, A.scratchEls));
     const int e = A.els[q];
+    ASTRO_GUARD(A.status, 192, ASTRO_IN(e, A.nEls));
     const double ru = A.Kf[(size_t)q * 32 * 33 + 33 * i + 32];
     if (i < 24) {
         const int var = i / 4, a = i % 4;
+        ASTRO_GUARD(A.status, 193, ASTRO_IN(A.elist[8 * (size_t)e + a] - 1, A.nNodes));
         const int r = A.rank[A.elist[8 * (size_t)e + a] - 1] - 1;
+        ASTRO_GUARD(A.status, 194, ASTRO_IN(r, A.nNodes));
         if (A.load) A.load[6 * (size_t)r + var] -= ru;
         if (A.ruOut) A.ruOut[24 * (size_t)e + i] = ru;
     } else if (A.intLoad) {

@@ -1133,6 +1133,8 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
     double rel = 0.0, est = 0.0, rn = 0.0, bn = 0.0;
     const bool fp64 = o->method == ASTRO_SOLVER_GMRES_JACOBI_FP64;
     const bool learned = o->method == ASTRO_SOLVER_FGMRES_LEARNED;
+    // the matrix the true residual is formed with: the FP64 assembly whenever it is resident
+    const int resKind = ctx->haveK64 ? 64 : 32;
     astro_precond pdef;
     const astro_precond *pc = o->precond;
     if (learned && !pc) {
@@ -1252,7 +1254,7 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
         const double inner = o->inner_rtol > 0 ? o->inner_rtol : 1e-4;
         // the outer residual is formed with the FP64 matrix when it is resident (the system the
         // tolerance refers to), else with the FP32 assembly's values in FP64 arithmetic
-        const int refKind = ctx->haveK64 ? 64 : 32;
+        const int refKind = resKind;
         for (refinements = 0; refinements < 200; ++refinements) {
             if ((rc = true_residual<DPN>(ctx, W, refKind, d_x, d_b, &rel, r, &rn))) break;
             if (rel <= o->rtol) break;
@@ -1295,6 +1297,7 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
         st->rel_residual = rel;
         st->seconds = ms * 1e-3;
         st->conditional_graph = W.condOk ? 1 : 0;
+        st->residual_kind = resKind;
     }
     if (rc == ASTRO_ERR_MAXIT) set_err(ctx, rc, "iteration limit reached before the residual tolerance");
     return rc;
@@ -1631,6 +1634,7 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
         st->rel_residual = worstRel;
         st->seconds = ms * 1e-3;
         st->conditional_graph = W.condOk ? 1 : 0;
+        st->residual_kind = 64;
     }
     return rc;
 }

@@ -12,7 +12,6 @@
 // for; the large systems use the Jacobi/mixed-precision solvers of krylov.cu.
 #include <algorithm>
 #include <cmath>
-#include <mutex>
 
 #include "astro_internal.h"
 
@@ -489,10 +488,6 @@ static __device__ __align__(256) double g_ldl_noalloc_z[ASTRO_LDL_NOALLOC_MAX_DI
 
 namespace {
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-double *g_noalloc_z[kMaxDevices] = {};  // address of g_ldl_noalloc_z on each device, once known
-
 // Same sweep as k_ldl_solve; the profile bandwidth is found on the device because the caller's
 // row ranges are device memory here.
 __global__ void __launch_bounds__(kT) k_ldl_solve_noalloc(double *soln, const double *rhs, const double *L,
@@ -510,11 +505,13 @@ __global__ void __launch_bounds__(kT) k_ldl_solve_noalloc(double *soln, const do
 
 }  // namespace
 
-// The address of the scratch array is looked up on the first call made on each device (with that
-// device current) and kept; make that first call before any stream capture begins.  Nothing in
-// the scratch needs to start at zero: the forward sweep writes z(i) before any row reads it.
-// The scratch is shared by every context on a device, so calls that overlap in time on one
-// device (from several host threads) race on it and must be serialised by the caller.
+// The address of the scratch array is looked up on every call, with the context's device current:
+// after the first lookup on a device (which may load the module, so make the first call before any
+// stream capture begins) it is a table read, and a module loaded again after a device reset is
+// never reached through a stale pointer.  Nothing in the scratch needs to start at zero: the
+// forward sweep writes z(i) before any row reads it.  The scratch is shared by every context on a
+// device, so calls that overlap in time on one device (from several host threads) race on it and
+// must be serialised by the caller.
 extern "C" int astro_ldl_solve_device_noalloc(astro_ctx *ctx, double *d_soln, const double *d_rhs,
                                               const double *d_l_mat, const int32_t *d_l_range, int32_t l_dim) {
     if (!ctx) return ASTRO_ERR_ARG;
@@ -524,23 +521,14 @@ extern "C" int astro_ldl_solve_device_noalloc(astro_ctx *ctx, double *d_soln, co
                            std::to_string(ASTRO_LDL_NOALLOC_MAX_DIM) + " rows; use astro_ldl_solve");
     if (l_dim <= 0 || !d_soln || !d_rhs || !d_l_mat || !d_l_range)
         return set_err(ctx, ASTRO_ERR_ARG, "astro_ldl_solve_device_noalloc: null buffer or l_dim <= 0");
-    if (ctx->device < 0 || ctx->device >= kMaxDevices) return set_err(ctx, ASTRO_ERR_ARG, "device index out of range");
     int prev = -1;
     CK(cudaGetDevice(&prev));
     if (prev != ctx->device) CK(cudaSetDevice(ctx->device));
-    double *z = nullptr;
-    cudaError_t e = cudaSuccess;
-    {
-        std::lock_guard<std::mutex> lock(g_noalloc_mu);
-        if (!g_noalloc_z[ctx->device]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_ldl_noalloc_z);
-            if (e == cudaSuccess) g_noalloc_z[ctx->device] = static_cast<double *>(p);
-        }
-        z = g_noalloc_z[ctx->device];
-    }
+    void *z = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&z, g_ldl_noalloc_z);
     if (e == cudaSuccess) {
-        k_ldl_solve_noalloc<<<1, kT, 0, ctx->stream>>>(d_soln, d_rhs, d_l_mat, d_l_range, l_dim, z);
+        k_ldl_solve_noalloc<<<1, kT, 0, ctx->stream>>>(d_soln, d_rhs, d_l_mat, d_l_range, l_dim,
+                                                      static_cast<double *>(z));
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);

@@ -855,6 +855,7 @@ extern "C" int astro_thermal_solve(astro_ctx *ctx, const double *rhs, double *dt
         stats->iterations = it;
         stats->status = rc ? rc : status;
         stats->rel_residual = bn > 0.0 ? std::sqrt(rr) / bn : 0.0;
+        stats->residual_kind = 64;
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
         stats->seconds = ms * 1e-3;

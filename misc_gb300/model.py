@@ -265,20 +265,22 @@ def plate_shell(nx=40, ny=8, lx=10.0, ly=2.0, t=0.05, E=7.0e10, nu=0.33, rho=270
 
 
 def panel_batch(num_panels=512, seed0=1000, n_range=(8, 96), t_range=(0.01, 0.1), p_range=(1.0e2, 1.0e4),
-                n_dvars=32, h=0.1, E=7.0e10, nu=0.33, rho=2700.0, name="panels"):
+                n_dvars=32, h=0.1, E=7.0e10, nu=0.33, rho=2700.0, name="panels", indices=None):
     """Batch of independent shell4 panels as one model (its connected components): panel p has
     n_x, n_y ~ U{n_range} elements of size h (its own generator, seed seed0 + p), thickness
     t ~ U(t_range) (one section per panel), all six DOF clamped on its x = 0 edge, and a pressure
     ~ U(p_range) on all its elements.  n_dvars design variables: layup thickness groups of equal
     element count within every panel (element k of a panel with e elements is in group
     k * n_dvars // e); design variable g covers group g of every panel.  The panels lie side by
-    side in z (disconnected).  Extra attributes: panel_el_ptr, panel_node_ptr (per panel first
-    element / node, 0-based, plus the totals), panel_pressure, panel_thickness, panel_n."""
+    side in z (disconnected).  indices: the panels of the num_panels-panel batch to build (default
+    all), each identical to its copy in the whole batch.  Extra attributes: panel_el_ptr,
+    panel_node_ptr (per panel first element / node, 0-based, plus the totals), panel_pressure,
+    panel_thickness, panel_n."""
     nodes, els, sec, thick, pres, nxy = [], [], [], [], [], []
     mpc_nodes, el_ptr, nd_ptr = [], [0], [0]
     grp = []
     nn = 0
-    for p in range(num_panels):
+    for p in (range(num_panels) if indices is None else indices):
         rng = np.random.default_rng(seed0 + p)
         nx, ny = (int(v) for v in rng.integers(n_range[0], n_range[1] + 1, 2))
         t = float(rng.uniform(*t_range))
@@ -294,7 +296,7 @@ def panel_batch(num_panels=512, seed0=1000, n_range=(8, 96), t_range=(0.01, 0.1)
         e[:, 0], e[:, 1], e[:, 2], e[:, 3] = nid(ii, jj), nid(ii + 1, jj), nid(ii + 1, jj + 1), nid(ii, jj + 1)
         els.append(e)
         ne = nx * ny
-        sec.append(np.full(ne, p + 1, np.int32))
+        sec.append(np.full(ne, len(thick) + 1, np.int32))
         grp.append((np.arange(ne) * n_dvars) // ne + 1)
         mpc_nodes += [nid(0, j) for j in range(ny + 1)]
         thick.append(t)
@@ -306,7 +308,7 @@ def panel_batch(num_panels=512, seed0=1000, n_range=(8, 96), t_range=(0.01, 0.1)
     nodes = np.vstack(nodes)
     els = np.vstack(els)
     E_ = els.shape[0]
-    S = num_panels
+    S = len(thick)
     m = Model(
         node_list=nodes, element_list=els, element_type=np.full(E_, 41, np.int32),
         element_section=np.concatenate(sec), section_mat_id=np.ones(S, np.int32),

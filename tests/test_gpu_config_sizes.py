@@ -1,0 +1,180 @@
+"""GPU parity at the sizes of the benchmark workloads, against the oracle, through the C ABI.
+
+* The 64x32x32 brick block (65,536 brick8, 212,355 DOF, seed 0):
+  - element matrices of a 4,096+-element sample (every element on the clamped face x = 0 and on
+    the traction face x = 4, the 512 most distorted elements of the jittered mesh, the rest drawn
+    uniformly), FP64 to 1e-12 and FP32 to 2e-6 relative (Frobenius norm per element);
+  - the residual and tangent of a sample at a displaced state (the general kernel), 1e-12;
+  - the whole assembled CSR matrix and residual load at that displaced state, 1e-12 of the
+    largest entry / of the load's norm, columns bit-exact;
+  - the operator K + C^T C of the FP64 assembly applied to random vectors, 1e-13 relative.
+* The 128x128 simply supported shell plate (99,846 DOF, dt 1e-5): five Newmark steps against
+  the oracle's time loop with a direct solve of K_eff, 1e-8 per step.
+* 16 of the 512 panels of the batched-panel workload (every 32nd): the band LDL^T solutions of
+  the pressure load and of design-sensitivity right-hand sides against sparse direct solves of the
+  oracle's K + C^T C, 1e-10.
+* The 96x48x48 evaluation block of the learned preconditioner (698,691 DOF): the learned FGMRES
+  solution at 1e-8 FP64 relative residual against the FP64 solution (Jacobi-GMRES to 1e-12).  The
+  forward error of a solve with relative residual rho is at most kappa(A) rho; the test asserts
+  the measured error stays within 20 times the error of the plain FP64 solve at the same rho (the
+  mixed-precision refinement loses nothing to the FP64 solver), and reports both.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import scipy.sparse.linalg as spla
+
+from misc_gb300 import model as M
+from misc_gb300 import panels as PN
+from misc_gb300.astro import (OPT_SHELL_MEAN_ROT_TERM, SOLVER_FGMRES_LEARNED, SOLVER_GMRES_JACOBI_FP64, AstroGPU)
+from oracle import Oracle
+from oracle import oracle as OO
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b, axis=(1, 2)) / np.linalg.norm(b, axis=(1, 2))
+
+
+def _sample(m, nx, ny, nz, count=4096, seed=0):
+    """Element numbers (1-based) of the parity sample: the clamped face, the traction face, the
+    most distorted elements, then uniform draws up to count."""
+    ex = (np.arange(m.num_els) % nx)
+    clamped = np.nonzero(ex == 0)[0]
+    traction = np.nonzero(ex == nx - 1)[0]
+    # distortion: the nodes' distance from the regular grid (the jitter), summed per element
+    h = np.array([4.0 / 64, 2.0 / 32, 2.0 / 32])   # element size of the block
+    X = m.node_list
+    off = np.linalg.norm(X / h - np.round(X / h), axis=1)
+    dist = off[m.element_list[:, :8] - 1].sum(axis=1)
+    worst = np.argsort(dist)[-512:]
+    base = np.unique(np.concatenate([clamped, traction, worst]))
+    rest = np.setdiff1d(np.arange(m.num_els), base)
+    extra = np.random.default_rng(seed).choice(rest, max(0, count - len(base)), replace=False)
+    return np.sort(np.concatenate([base, extra])) + 1
+
+
+@pytest.fixture(scope="module")
+def cfg2():
+    m = M.config2()
+    return m, AstroGPU(m), Oracle(m)
+
+
+def test_cfg2_element_matrices_sample(cfg2):
+    m, g, o = cfg2
+    els = _sample(m, 64, 32, 32)
+    assert len(els) >= 4096
+    ke_o = np.array([o.element(int(e))[1][:24, :24] for e in els])
+    ke64 = g.element_matrices(64)[els - 1]
+    assert _rel(ke64, ke_o).max() < 1e-12
+    ke32 = g.element_matrices(32)[els - 1]
+    assert _rel(ke32, ke_o).max() < 2e-6
+
+
+def test_cfg2_displaced_state(cfg2):
+    """The general-state brick kernel (Green-Lagrange strain, stress stiffness, residual) at a
+    displaced state of the whole block: a sample of element residuals and tangents, and the whole
+    assembled CSR matrix and residual load."""
+    m, g, o = cfg2
+    rng = np.random.default_rng(3)
+    u = 2e-3 * rng.standard_normal(o.n)
+    st = M.make_state(o.n, disp=u)
+    ke, ru = g.element_matrices(64, state=st, with_residual=True)
+    els = _sample(m, 64, 32, 32, count=1024, seed=1)
+    for e in els:
+        r_o, k_o = o.element(int(e), 1, st)
+        assert np.linalg.norm(ru[e - 1] - r_o[:24]) <= 1e-12 * np.linalg.norm(r_o[:24]), e
+        assert np.linalg.norm(ke[e - 1] - k_o[:24, :24]) <= 1e-12 * np.linalg.norm(k_o[:24, :24]), e
+    load, _, mat, cols, _ = g.getElasticSolnLoad(1, state=st)
+    oload, _, omat, ocols, _ = o.el_soln_load(1, state=st)
+    assert np.array_equal(cols, ocols)
+    assert np.abs(mat - omat).max() <= 1e-12 * np.abs(omat).max()
+    assert np.linalg.norm(load - oload) <= 1e-12 * np.linalg.norm(oload)
+
+
+def test_cfg2_operator(cfg2):
+    m, g, o = cfg2
+    _, _, mat, cols, _ = g.getElasticSolnLoad(1)
+    mm, _ = g.scaleElasticMPC()
+    _, _, omat, ocols, _ = o.el_soln_load(1)
+    omm, _ = o.scale_mpc(omat)
+    assert np.array_equal(cols, ocols)
+    assert np.allclose(mm, omm, rtol=1e-14, atol=0)
+    Cm = o.mpc_scipy(omm)
+    A = o.csr_scipy(omat, ocols) + Cm.T @ Cm
+    rng = np.random.default_rng(11)
+    for _ in range(3):
+        x = rng.standard_normal(o.n)
+        y, yo = g.apply_operator(x, 64), A @ x
+        assert np.linalg.norm(y - yo) <= 1e-13 * np.linalg.norm(yo)
+
+
+def _set_quirk(v):
+    L = OO._lib()
+    L.orc_set_quirk.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.orc_set_quirk(1, v)
+
+
+def test_cfg5_newmark_steps():
+    """Five steps of the 128x128 plate's time loop (consistent shell tangent, as the Newmark
+    benchmark runs it) against the oracle's loop with a direct K_eff solve."""
+    from newmark_ref import newmark_states
+    nx = 128
+    m = M.plate_shell(nx=nx, ny=nx, lx=1.0, ly=1.0, t=0.01, E=7e10, nu=0.33, rho=2700.0, pressure=0.0, clamp="ss",
+                      y0=0.0)
+    g = AstroGPU(m)
+    g.set_option(OPT_SHELL_MEAN_ROT_TERM, 1)
+    centre = (nx // 2) * (nx + 1) + nx // 2 + 1
+    pattern = np.zeros(g.n)
+    pattern[g.n_dof_index[centre - 1, 2] - 1] = 1.0
+    dt, beta, gamma, steps = 1e-5, 0.25, 0.5, 5
+    amp = 100.0 * np.sin(2 * np.pi * 500.0 * dt * np.arange(1, steps + 1))
+    _set_quirk(1)
+    try:
+        o = Oracle(m)
+        D, V, A, _ = newmark_states(o, pattern, amp, dt, beta, gamma, steps)
+    finally:
+        _set_quirk(0)
+    u, v, a, iu, hist, st = g.newmark_run(steps, dt, beta, gamma, pattern, amp, rtol=1e-13)
+    assert st.status == 0
+    for k in range(steps):
+        assert np.linalg.norm(hist[k] - D[k + 1]) <= 1e-8 * np.linalg.norm(D[k + 1]), k
+    assert np.linalg.norm(v - V[-1]) <= 1e-7 * np.linalg.norm(V[-1])
+
+
+def test_cfg3_panel_subset():
+    """Every 32nd panel of the 512-panel batch (the same panels, seeds 1000 + p): band LDL^T
+    solutions of the pressure load, four design-sensitivity right-hand sides and four random ones
+    against sparse direct solves of the oracle's system."""
+    m = M.panel_batch(num_panels=512, indices=range(0, 512, 32))
+    g, o = AstroGPU(m), Oracle(m)
+    g.getElasticSolnLoad(1, export=False)
+    g.scaleElasticMPC()
+    f = PN.pressure_load(g, m)
+    R = PN.sensitivity_rhs(g, 4)
+    B = np.column_stack([f, R, np.random.default_rng(2).standard_normal((g.n, 4))])
+    g.panels_factor(4)
+    X, _ = g.panels_solve(B)
+    A = o.static_system()[0].tocsc()
+    lu = spla.splu(A)
+    for c in range(B.shape[1]):
+        xr = lu.solve(B[:, c])
+        assert np.linalg.norm(X[:, c] - xr) <= 1e-10 * np.linalg.norm(xr), c
+
+
+def test_cfg4_learned_solution_error():
+    from misc_gb300 import learned as LN
+    m = M.config4_block(96, 48, 48, 4000, corr_len=0.5, sigma=0.65)
+    g, b = LN.block_system(m, fp32=True)
+    ul, sl = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=1e-8, restart=50)
+    assert sl.status == 0 and sl.fallback == 0 and sl.residual_kind == 64 and sl.rel_residual <= 1e-8
+    u64, s64 = g.solve_static(b, method=SOLVER_GMRES_JACOBI_FP64, rtol=1e-8, restart=50, max_iters=400000)
+    uref, sref = g.solve_static(b, u0=u64, method=SOLVER_GMRES_JACOBI_FP64, rtol=1e-12, restart=50,
+                                max_iters=400000)
+    assert sref.status == 0
+    err_l = np.linalg.norm(ul - uref) / np.linalg.norm(uref)
+    err_64 = np.linalg.norm(u64 - uref) / np.linalg.norm(uref)
+    print(f"config-4 evaluation block: learned error {err_l:.3e}, FP64 GMRES error {err_64:.3e} at 1e-8")
+    assert err_l <= 20.0 * max(err_64, 1e-10), (err_l, err_64)

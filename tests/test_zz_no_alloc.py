@@ -1,6 +1,7 @@
 """The allocation-free skyline triangular solve (astro_ldl_solve_device_noalloc) against the
-ordinary one (astro_ldl_solve), through the C ABI.  Both run the same sweep, so the results agree
-to rounding (tolerance 1e-12 relative); two calls in a row check that the shared scratch carries
+ordinary one (astro_ldl_solve), through the C ABI, and against the oracle's solveSparseLDLFact
+restatement on the CPU (so that a fault in the device sweep the two entry points share cannot pass
+unseen).  Tolerance 1e-12 relative; two calls in a row check that the shared scratch carries
 nothing from one call into the next.  This file is collected last on purpose: it must pass both in
 a fresh process and after every other GPU test has run in the same process."""
 import ctypes as C
@@ -43,6 +44,7 @@ def test_noalloc_solve_matches_ldl_solve(model):
     rng = np.random.default_rng(21)
     rhs = [rng.standard_normal(o.n) for _ in range(2)]
     x_ref = [g.solveSparseLDLFact(r, fac, o.lt_range) for r in rhs]
+    x_orc = [o.ldl_solve(fac, o.lt_range, r) for r in rhs]
     d_b = [torch.tensor(r, dtype=torch.float64, device=dev) for r in rhs]
     d_x = [torch.full((o.n,), float("nan"), dtype=torch.float64, device=dev) for _ in rhs]
     torch.cuda.synchronize()
@@ -51,6 +53,7 @@ def test_noalloc_solve_matches_ldl_solve(model):
     for call in range(2):
         x = d_x[call].cpu().numpy()
         assert np.linalg.norm(x - x_ref[call]) <= 1e-12 * np.linalg.norm(x_ref[call]), call
+        assert np.linalg.norm(x - x_orc[call]) <= 1e-12 * np.linalg.norm(x_orc[call]), call
 
 
 def test_noalloc_solve_rejects_oversize():
