@@ -13,9 +13,9 @@
 // constants (r_getMaterialStiffness, Working/AStrO_r_designPropertyFunctions.f90:8-80) is formed
 // per element by an unpivoted LU exactly as the reference.
 //
-// Mapping: one warp per element; lane l owns the node-pair blocks (a,b) = (l/8, l%8) and
-// (l/8+4, l%8), i.e. 18 accumulators; lanes 0..7 evaluate node a's shape data and reduce the
-// Jacobian and displacement gradient by shuffles.  Elements are processed colour by colour so a
+// Kernels, one warp per element: hex8_fast_kernel (FP32, zero state), hex8_df_kernel (FP64 zero
+// state in double-float), hex8_gen_kernel (any state and orientation, double-float; also the
+// complex step with the imaginary part of C).  Elements are processed colour by colour so a
 // colour's blocks land in disjoint block rows: plain read-add-write, no atomics, bit-reproducible.
 #include "astro_internal.h"
 #include "dfloat.cuh"
@@ -23,28 +23,8 @@
 
 namespace {
 
-constexpr int kWarpsPerBlock = 4;
 constexpr double kRt3 = 0.57735026918962576451;  // r_1rt3 = 1/sqrt(3) in double
 constexpr double kRt3c = LIT(0.577350269189626);  // c_1rt3: a single-precision literal
-
-template <class T> struct Hex8Args {
-    const double *nodes;     // (N,3) by node id
-    const int *elist;        // (E,8)
-    const int *rank;         // currentRank (N) 1-based, indexed by node id - 1
-    const int *colorEls;     // element ids of this colour
-    int count;               // elements in this colour
-    const int *elBlk;        // (E,64)
-    const double *elMat;     // (E,9) engineering constants
-    const double *orient;    // (E,9) column-major orientation, or nullptr for identity
-    const double *disp;      // internal-layout displacement (rank-major, 3 per node) or nullptr
-    T *Kbsr;                 // BSR values (nb*9) or nullptr
-    double *Kbsr64;          // FP64 BSR to add into as well (FP32 kernel writing both) or nullptr
-    double *loadInt;         // internal-layout load, -= Ru (or nullptr)
-    double *keOut;           // element matrices (E, 24,24) column-major, element DOF order, or nullptr
-    double *ruOut;           // (E,24) or nullptr
-    double gpc;              // Gauss point coordinate (1/sqrt(3) of the real or the complex path)
-    const double *Cover;     // per listed element a 6x6 row-major C used instead of elMat, or nullptr
-};
 
 // C = S^-1 by the reference's unpivoted LU (r_GetInvLU / r_LUFactor / r_SolveLUxb).
 template <class T, class P> __device__ void material_c(const P *ep, T C[6][6]) {
@@ -86,224 +66,6 @@ template <class T, class P> __device__ void material_c(const P *ep, T C[6][6]) {
             x[i] = f * (z[i] - dp);
         }
         for (int i = 0; i < 6; ++i) C[i][col] = x[i];
-    }
-}
-
-// M = Bloc(g)^T C Bloc(h), Bloc the 6x3 small-strain operator in Voigt order
-// [e11, e22, e33, g12, g13, g23].
-template <class T> __device__ __forceinline__ void btcb(const T C[6][6], const T g[3], const T h[3], T M[3][3]) {
-    T CB[6][3];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        CB[i][0] = C[i][0] * h[0] + C[i][3] * h[1] + C[i][4] * h[2];
-        CB[i][1] = C[i][1] * h[1] + C[i][3] * h[0] + C[i][5] * h[2];
-        CB[i][2] = C[i][2] * h[2] + C[i][4] * h[0] + C[i][5] * h[1];
-    }
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        M[0][k] = g[0] * CB[0][k] + g[1] * CB[3][k] + g[2] * CB[4][k];
-        M[1][k] = g[1] * CB[1][k] + g[0] * CB[3][k] + g[2] * CB[5][k];
-        M[2][k] = g[2] * CB[2][k] + g[0] * CB[4][k] + g[1] * CB[5][k];
-    }
-}
-
-template <class T> __device__ __forceinline__ T wsum8(T v) {
-    // sum over lanes 0..7 (the other lanes hold zeros) delivered to all lanes
-    v += __shfl_xor_sync(0xffffffffu, v, 1);
-    v += __shfl_xor_sync(0xffffffffu, v, 2);
-    v += __shfl_xor_sync(0xffffffffu, v, 4);
-    return __shfl_sync(0xffffffffu, v, 0);
-}
-
-template <class T, bool GENERAL>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) hex8_kernel(Hex8Args<T> A) {
-    __shared__ T sNx[kWarpsPerBlock][8][3];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int item = blockIdx.x * kWarpsPerBlock + w;
-    if (item >= A.count) return;
-    const int e = A.colorEls[item];
-    const int a = lane & 7;   // node handled in the per-node phase (lanes 0..7 meaningful)
-    const int bA0 = lane >> 3, bA1 = (lane >> 3) + 4, bB = lane & 7;
-    // material
-    T C[6][6];
-    if (A.Cover) {
-        for (int i = 0; i < 6; ++i)
-            for (int j = 0; j < 6; ++j) C[i][j] = T(A.Cover[36 * (size_t)item + 6 * i + j]);
-    } else {
-        material_c<T>(A.elMat + 9 * (size_t)e, C);
-    }
-    T Or[3][3];
-    if (GENERAL && A.orient) {
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) Or[i][j] = T(A.orient[9 * (size_t)e + 3 * j + i]);
-    } else {
-        for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) Or[i][j] = (i == j) ? T(1) : T(0);
-    }
-    // node data (lanes 0..7)
-    const int nd = A.elist[8 * (size_t)e + a];
-    T X[3], U[3] = {T(0), T(0), T(0)};
-    {
-        T g0 = T(A.nodes[3 * (size_t)(nd - 1)]), g1 = T(A.nodes[3 * (size_t)(nd - 1) + 1]),
-          g2 = T(A.nodes[3 * (size_t)(nd - 1) + 2]);
-        for (int i = 0; i < 3; ++i) X[i] = Or[i][0] * g0 + Or[i][1] * g1 + Or[i][2] * g2;
-        if (GENERAL && A.disp) {
-            const int r = A.rank[nd - 1] - 1;
-            for (int i = 0; i < 3; ++i) U[i] = T(A.disp[3 * (size_t)r + i]);
-        }
-    }
-    const T sa = (a == 1 || a == 2 || a == 5 || a == 6) ? T(1) : T(-1);
-    const T ta = (a == 2 || a == 3 || a == 6 || a == 7) ? T(1) : T(-1);
-    const T ua = (a >= 4) ? T(1) : T(-1);
-    const T g = T(A.gpc);  // 1/sqrt(3): r_1rt3, or the complex path's single-precision c_1rt3
-    T acc0[3][3], acc1[3][3], ru[3] = {T(0), T(0), T(0)};
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) acc0[i][j] = acc1[i][j] = T(0);
-    for (int gp = 0; gp < 8; ++gp) {
-        const T s1 = (gp & 1) ? g : -g, s2 = (gp & 2) ? g : -g, s3 = (gp & 4) ? g : -g;
-        // shape derivatives of node a (r_EvalNs brick8 branch)
-        T Ns[3];
-        Ns[0] = T(0.125) * sa * (T(1) + ta * s2) * (T(1) + ua * s3);
-        Ns[1] = T(0.125) * ta * (T(1) + sa * s1) * (T(1) + ua * s3);
-        Ns[2] = T(0.125) * ua * (T(1) + sa * s1) * (T(1) + ta * s2);
-        const bool act = lane < 8;
-        T J[3][3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) J[i][j] = wsum8<T>(act ? X[i] * Ns[j] : T(0));
-        // cofactor inverse (r_getDetInv)
-        T a11 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        T a12 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        T a13 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        T det = J[0][0] * a11 + J[0][1] * a12 + J[0][2] * a13;
-        T di = T(1) / det;
-        T I[3][3];
-        I[0][0] = di * a11;
-        I[1][0] = di * a12;
-        I[2][0] = di * a13;
-        I[0][1] = di * (J[0][2] * J[2][1] - J[0][1] * J[2][2]);
-        I[1][1] = di * (J[0][0] * J[2][2] - J[0][2] * J[2][0]);
-        I[2][1] = di * (J[0][1] * J[2][0] - J[0][0] * J[2][1]);
-        I[0][2] = di * (J[0][1] * J[1][2] - J[0][2] * J[1][1]);
-        I[1][2] = di * (J[0][2] * J[1][0] - J[0][0] * J[1][2]);
-        I[2][2] = di * (J[0][0] * J[1][1] - J[0][1] * J[1][0]);
-        T nx[3];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) nx[j] = Ns[0] * I[0][j] + Ns[1] * I[1][j] + Ns[2] * I[2][j];
-        if (act) {
-            sNx[w][a][0] = nx[0];
-            sNx[w][a][1] = nx[1];
-            sNx[w][a][2] = nx[2];
-        }
-        __syncwarp();
-        const T wdet = det;  // unit Gauss weights
-        T Gm[3][3], S3[3][3], stress[6];
-        bool nonlin = false;
-        if (GENERAL) {
-            T ux[3][3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) ux[i][j] = wsum8<T>(act ? U[i] * nx[j] : T(0));
-            // Green-Lagrange strain (r_getNLStrain dv = dv2 = 0)
-            T uxL[3][3];
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) uxL[i][j] = Or[i][0] * ux[0][j] + Or[i][1] * ux[1][j] + Or[i][2] * ux[2][j];
-            T st[6];
-            st[0] = uxL[0][0] + T(0.5) * (ux[0][0] * ux[0][0] + ux[1][0] * ux[1][0] + ux[2][0] * ux[2][0]);
-            st[1] = uxL[1][1] + T(0.5) * (ux[0][1] * ux[0][1] + ux[1][1] * ux[1][1] + ux[2][1] * ux[2][1]);
-            st[2] = uxL[2][2] + T(0.5) * (ux[0][2] * ux[0][2] + ux[1][2] * ux[1][2] + ux[2][2] * ux[2][2]);
-            st[3] = uxL[0][1] + uxL[1][0] + ux[0][0] * ux[0][1] + ux[1][0] * ux[1][1] + ux[2][0] * ux[2][1];
-            st[4] = uxL[0][2] + uxL[2][0] + ux[0][0] * ux[0][2] + ux[1][0] * ux[1][2] + ux[2][0] * ux[2][2];
-            st[5] = uxL[1][2] + uxL[2][1] + ux[0][2] * ux[0][1] + ux[1][2] * ux[1][1] + ux[2][2] * ux[2][1];
-            for (int i = 0; i < 6; ++i) {
-                stress[i] = T(0);
-                for (int k = 0; k < 6; ++k) stress[i] += C[i][k] * st[k];
-            }
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) {
-                    Gm[i][j] = Or[i][j] + ux[j][i];
-                    if (Gm[i][j] != ((i == j) ? T(1) : T(0))) nonlin = true;
-                }
-            S3[0][0] = stress[0];
-            S3[1][1] = stress[1];
-            S3[2][2] = stress[2];
-            S3[0][1] = S3[1][0] = stress[3];
-            S3[0][2] = S3[2][0] = stress[4];
-            S3[1][2] = S3[2][1] = stress[5];
-            // residual of node a (lanes 0..7)
-            if (act) {
-                T bs[3];  // Bloc(nx)^T stress
-                bs[0] = nx[0] * stress[0] + nx[1] * stress[3] + nx[2] * stress[4];
-                bs[1] = nx[1] * stress[1] + nx[0] * stress[3] + nx[2] * stress[5];
-                bs[2] = nx[2] * stress[2] + nx[0] * stress[4] + nx[1] * stress[5];
-                for (int v = 0; v < 3; ++v) ru[v] += wdet * (Gm[0][v] * bs[0] + Gm[1][v] * bs[1] + Gm[2][v] * bs[2]);
-            }
-        }
-        // blocks (bA0,bB) and (bA1,bB)
-        T h[3] = {sNx[w][bB][0], sNx[w][bB][1], sNx[w][bB][2]};
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int ia = half ? bA1 : bA0;
-            T gg[3] = {sNx[w][ia][0], sNx[w][ia][1], sNx[w][ia][2]};
-            T M[3][3];
-            btcb<T>(C, gg, h, M);
-            T (&acc)[3][3] = half ? acc1 : acc0;
-            if (GENERAL && nonlin) {
-                T MG[3][3];
-                for (int i = 0; i < 3; ++i)
-                    for (int k = 0; k < 3; ++k) MG[i][k] = M[i][0] * Gm[0][k] + M[i][1] * Gm[1][k] + M[i][2] * Gm[2][k];
-                T geo = T(0);
-                for (int i = 0; i < 3; ++i)
-                    for (int j = 0; j < 3; ++j) geo += gg[i] * S3[i][j] * h[j];
-                for (int i = 0; i < 3; ++i)
-                    for (int k = 0; k < 3; ++k)
-                        acc[i][k] += wdet * (Gm[0][i] * MG[0][k] + Gm[1][i] * MG[1][k] + Gm[2][i] * MG[2][k] +
-                                             ((i == k) ? geo : T(0)));
-            } else {
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) acc[i][k] += wdet * M[i][k];
-            }
-        }
-        __syncwarp();
-    }
-    // outputs
-    const int *blk = A.elBlk + 64 * (size_t)e;
-#pragma unroll
-    for (int half = 0; half < 2; ++half) {
-        const int ia = half ? bA1 : bA0;
-        T (&acc)[3][3] = half ? acc1 : acc0;
-        const int k = blk[ia * 8 + bB];
-        if (A.Kbsr) {
-            T *dst = A.Kbsr + 9 * (size_t)k;
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) dst[3 * i + j] += acc[i][j];
-        }
-        if (A.Kbsr64) {
-            double *dst = A.Kbsr64 + 9 * (size_t)k;
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j) dst[3 * i + j] += (double)acc[i][j];
-        }
-        if (A.keOut) {
-            double *ke = A.keOut + 576 * (size_t)e;
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) ke[(size_t)(8 * j + bB) * 24 + (8 * i + ia)] = (double)acc[i][j];
-        }
-    }
-    if (GENERAL && lane < 8) {
-        if (A.loadInt) {
-            const int r = A.rank[nd - 1] - 1;
-            for (int v = 0; v < 3; ++v) A.loadInt[3 * (size_t)r + v] -= (double)ru[v];
-        }
-        if (A.ruOut)
-            for (int v = 0; v < 3; ++v) A.ruOut[24 * (size_t)e + 8 * v + a] = (double)ru[v];
     }
 }
 
@@ -724,8 +486,396 @@ template <bool ROT> __global__ void __launch_bounds__(32 * kDfW, 4) hex8_df_kern
     }
 }
 
-// Node coordinates of every brick element in its section frame (orient X, FP64) and its C, both
-// split into double-float for hex8_df_kernel.
+// ---------------------------------------------------------------------------------------------
+// General-state brick8 element (Green-Lagrange strain, stress stiffness, residual, any section
+// orientation) in double-float: the quantities of hex8_kernel<double, true> reorganised for the
+// FP32 pipe.  With G = Or + ux^T at a Gauss point (Or the section orientation, ux the gradient of
+// the global displacement along the local axes) and Bloc(g) the 6x3 small-strain operator of the
+// shape gradient g, the nonlinear strain-displacement block of node a is P_a = Bloc(g_a) G (6x3),
+// and with Q_b = w detJ C P_b, S the stress tensor and t_b = w detJ S g_b:
+//   K_ab = sum_gp ( P_a^T Q_b + (g_a . t_b) I3 ),   Ru_a = sum_gp w detJ P_a^T stress.
+// Phase 1, lane (gp, s) = (lane / 4, lane % 4) handles nodes 2s and 2s+1 at point gp: the
+// Jacobian and displacement gradient are reduced over the four lanes of the point, then the lane
+// writes P, Q, g and t of its two nodes to shared memory (double-float) and keeps their residual.
+// Phase 2 (with a matrix), the 36 node-pair tiles a <= b times the 8 Gauss points are 288 units,
+// nine consecutive ones per lane in tile-major order, so every lane finishes one tile it shares
+// with a neighbour and starts the next: each tile is the sum of at most two partials (fixed order,
+// deterministic), and K_ba = K_ab^T fills the lower half.  Phase 3 writes the 64 blocks through
+// shared memory into the block-CSR matrix, three whole blocks per warp instruction; the first
+// element (in colour order) to touch a block writes it instead of adding.
+struct Hex8GenArgs {
+    const int *colorEls;
+    int count;
+    const int *elBlk;
+    const unsigned long long *elFirst;
+    const int *elist, *rank;
+    const float2 *Xdf;     // (E,8,3) node coordinates in the section frame, double-float
+    const float2 *Cdf;     // (E,9) orthotropic C, double-float (indexed by element)
+    const float2 *CdfItem; // (count,9) C per listed element (indexed by list position) or null
+    const double *orient;  // (E,9) column-major section orientation (ROT)
+    const double *disp;    // internal-layout displacement (3 per node, rank-major) or null
+    double *K;             // BSR values or null
+    double *loadInt;       // internal-layout load, -= Ru (or null)
+    double *keOut;         // element matrices (E,24,24) column-major, element DOF order, or null
+    double *ruOut;         // (E,24) or null
+    float gpcHi, gpcLo;    // Gauss point coordinate (1/sqrt(3) of the real or the complex path)
+};
+
+constexpr int kGenW = 2;  // warps per CTA
+
+struct GenSmem {
+    union {
+        struct {
+            float Ph[64][18], Pl[64][18], Qh[64][18], Ql[64][18];  // item gp*8 + a: 6x3 row-major
+            float4 gh[64], gl[64], th[64], tl[64];
+        } u;
+        struct {
+            float part[36][2][20];  // tile partials: 9 entries + geometric term, (hi, lo) pairs
+            double K[64 * 9];       // element blocks, block j = 8a + b at 9j (row-major 3x3)
+        } o;
+    };
+    int blk[64];
+};
+
+__constant__ unsigned char c_tileA[36], c_tileB[36];
+
+__device__ __forceinline__ DF df_shfl_xor(DF v, int m) {
+    return DF{__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+}
+__device__ __forceinline__ DF df_fma(DF a, DF b, DF c) { return df_add(df_mul(a, b), c); }
+
+template <bool ROT, bool BUILD>
+__global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
+    __shared__ GenSmem sm[kGenW];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int item = blockIdx.x * kGenW + w;
+    if (item >= A.count) return;
+    GenSmem &S = sm[w];
+    const int e = A.colorEls[item];
+    if (BUILD) {
+        S.blk[lane] = A.elBlk[64 * (size_t)e + lane];
+        S.blk[lane + 32] = A.elBlk[64 * (size_t)e + lane + 32];
+    }
+    const DF one{1.f, 0.f}, zero{0.f, 0.f};
+    DF c[9];  // C11 C12 C13 C22 C23 C33 C44 C55 C66
+    {
+        const float2 *cp = A.CdfItem ? A.CdfItem + 9 * (size_t)item : A.Cdf + 9 * (size_t)e;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) c[q] = DF{cp[q].x, cp[q].y};
+    }
+    DF Or[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            Or[i][j] = ROT ? df_from_double(A.orient[9 * (size_t)e + 3 * j + i]) : ((i == j) ? one : zero);
+    // ---- phase 1: lane (gp, s), nodes 2s and 2s+1 ---------------------------------------------
+    const int gp = lane >> 2, s = lane & 3;
+    DF ru[2][3];
+    {
+        const DF G{A.gpcHi, A.gpcLo};
+        const DF s1 = (gp & 1) ? G : df_neg(G), s2 = (gp & 2) ? G : df_neg(G), s3 = (gp & 4) ? G : df_neg(G);
+        DF J[9], n[2][3], U[2][3];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) J[q] = zero;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int a = 2 * s + k;
+            const float2 *xp = A.Xdf + 24 * (size_t)e + 3 * a;
+            const float2 x0 = xp[0], x1 = xp[1], x2 = xp[2];
+            const DF X[3] = {DF{x0.x, x0.y}, DF{x1.x, x1.y}, DF{x2.x, x2.y}};
+            const bool sp = (a == 1 || a == 2 || a == 5 || a == 6), tp = (a == 2 || a == 3 || a == 6 || a == 7),
+                       up = (a >= 4);
+            const DF p1 = df_add(one, sp ? s1 : df_neg(s1));
+            const DF p2 = df_add(one, tp ? s2 : df_neg(s2));
+            const DF p3 = df_add(one, up ? s3 : df_neg(s3));
+            n[k][0] = df_scale2(df_mul(p2, p3), sp ? 0.125f : -0.125f);
+            n[k][1] = df_scale2(df_mul(p1, p3), tp ? 0.125f : -0.125f);
+            n[k][2] = df_scale2(df_mul(p1, p2), up ? 0.125f : -0.125f);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) J[3 * i + j] = df_fma(X[i], n[k][j], J[3 * i + j]);
+            if (A.disp) {
+                const int nd = A.elist[8 * (size_t)e + a];
+                const int r = A.rank[nd - 1] - 1;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) U[k][i] = df_from_double(A.disp[3 * (size_t)r + i]);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) U[k][i] = zero;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            J[q] = df_add(J[q], df_shfl_xor(J[q], 1));
+            J[q] = df_add(J[q], df_shfl_xor(J[q], 2));
+        }
+        const DF a11 = df_sub(df_mul(J[4], J[8]), df_mul(J[5], J[7]));
+        const DF a12 = df_sub(df_mul(J[5], J[6]), df_mul(J[3], J[8]));
+        const DF a13 = df_sub(df_mul(J[3], J[7]), df_mul(J[4], J[6]));
+        const DF dt = df_add(df_add(df_mul(J[0], a11), df_mul(J[1], a12)), df_mul(J[2], a13));
+        const DF di = df_rcp(dt);
+        DF I[3][3];
+        I[0][0] = df_mul(di, a11);
+        I[1][0] = df_mul(di, a12);
+        I[2][0] = df_mul(di, a13);
+        I[0][1] = df_mul(di, df_sub(df_mul(J[2], J[7]), df_mul(J[1], J[8])));
+        I[1][1] = df_mul(di, df_sub(df_mul(J[0], J[8]), df_mul(J[2], J[6])));
+        I[2][1] = df_mul(di, df_sub(df_mul(J[1], J[6]), df_mul(J[0], J[7])));
+        I[0][2] = df_mul(di, df_sub(df_mul(J[1], J[5]), df_mul(J[2], J[4])));
+        I[1][2] = df_mul(di, df_sub(df_mul(J[2], J[3]), df_mul(J[0], J[5])));
+        I[2][2] = df_mul(di, df_sub(df_mul(J[0], J[4]), df_mul(J[1], J[3])));
+        DF g[2][3];
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                g[k][j] = df_add(df_add(df_mul(n[k][0], I[0][j]), df_mul(n[k][1], I[1][j])), df_mul(n[k][2], I[2][j]));
+        // displacement gradient ux[i][j] = sum_a U_a[i] g_a[j] (global components, local axes)
+        DF ux[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                DF v = df_add(df_mul(U[0][i], g[0][j]), df_mul(U[1][i], g[1][j]));
+                v = df_add(v, df_shfl_xor(v, 1));
+                ux[i][j] = df_add(v, df_shfl_xor(v, 2));
+            }
+        // Green-Lagrange strain in the section frame, stress, and G = Or + ux^T
+        DF uxL[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                uxL[i][j] = ROT ? df_add(df_add(df_mul(Or[i][0], ux[0][j]), df_mul(Or[i][1], ux[1][j])),
+                                         df_mul(Or[i][2], ux[2][j]))
+                                : ux[i][j];
+        DF st[6];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            DF q2 = df_add(df_add(df_mul(ux[0][j], ux[0][j]), df_mul(ux[1][j], ux[1][j])), df_mul(ux[2][j], ux[2][j]));
+            st[j] = df_add(uxL[j][j], df_scale2(q2, 0.5f));
+        }
+        {
+            const int pi[3] = {0, 0, 2}, pj[3] = {1, 2, 1};  // shear pairs (e12, e13, e23)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const int i = pi[q], j = pj[q];
+                DF v = df_add(uxL[i][j], uxL[j][i]);
+                v = df_add(v, df_add(df_add(df_mul(ux[0][i], ux[0][j]), df_mul(ux[1][i], ux[1][j])),
+                                     df_mul(ux[2][i], ux[2][j])));
+                st[3 + q] = v;
+            }
+        }
+        // w detJ (unit Gauss weights) folded into C and the stress
+        DF cw[9], sw[6];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) cw[q] = df_mul(dt, c[q]);
+        sw[0] = df_add(df_add(df_mul(cw[0], st[0]), df_mul(cw[1], st[1])), df_mul(cw[2], st[2]));
+        sw[1] = df_add(df_add(df_mul(cw[1], st[0]), df_mul(cw[3], st[1])), df_mul(cw[4], st[2]));
+        sw[2] = df_add(df_add(df_mul(cw[2], st[0]), df_mul(cw[4], st[1])), df_mul(cw[5], st[2]));
+        sw[3] = df_mul(cw[6], st[3]);
+        sw[4] = df_mul(cw[7], st[4]);
+        sw[5] = df_mul(cw[8], st[5]);
+        DF Gm[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Gm[i][j] = df_add(Or[i][j], ux[j][i]);
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int a = 2 * s + k;
+            const DF g0 = g[k][0], g1 = g[k][1], g2 = g[k][2];
+            DF P[6][3];
+#pragma unroll
+            for (int v = 0; v < 3; ++v) {
+                P[0][v] = df_mul(g0, Gm[0][v]);
+                P[1][v] = df_mul(g1, Gm[1][v]);
+                P[2][v] = df_mul(g2, Gm[2][v]);
+                P[3][v] = df_add(df_mul(g1, Gm[0][v]), df_mul(g0, Gm[1][v]));
+                P[4][v] = df_add(df_mul(g2, Gm[0][v]), df_mul(g0, Gm[2][v]));
+                P[5][v] = df_add(df_mul(g2, Gm[1][v]), df_mul(g1, Gm[2][v]));
+            }
+            // residual of node a at this point: P^T (w detJ stress)
+#pragma unroll
+            for (int v = 0; v < 3; ++v) {
+                DF r = df_mul(P[0][v], sw[0]);
+#pragma unroll
+                for (int q = 1; q < 6; ++q) r = df_fma(P[q][v], sw[q], r);
+                ru[k][v] = r;
+            }
+            if (BUILD) {
+                const int it = gp * 8 + a;
+#pragma unroll
+                for (int q = 0; q < 6; ++q)
+#pragma unroll
+                    for (int v = 0; v < 3; ++v) {
+                        S.u.Ph[it][3 * q + v] = P[q][v].hi;
+                        S.u.Pl[it][3 * q + v] = P[q][v].lo;
+                    }
+#pragma unroll
+                for (int v = 0; v < 3; ++v) {
+                    DF Q[6];
+                    Q[0] = df_add(df_add(df_mul(cw[0], P[0][v]), df_mul(cw[1], P[1][v])), df_mul(cw[2], P[2][v]));
+                    Q[1] = df_add(df_add(df_mul(cw[1], P[0][v]), df_mul(cw[3], P[1][v])), df_mul(cw[4], P[2][v]));
+                    Q[2] = df_add(df_add(df_mul(cw[2], P[0][v]), df_mul(cw[4], P[1][v])), df_mul(cw[5], P[2][v]));
+                    Q[3] = df_mul(cw[6], P[3][v]);
+                    Q[4] = df_mul(cw[7], P[4][v]);
+                    Q[5] = df_mul(cw[8], P[5][v]);
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) {
+                        S.u.Qh[it][3 * q + v] = Q[q].hi;
+                        S.u.Ql[it][3 * q + v] = Q[q].lo;
+                    }
+                }
+                // t = (w detJ S) g with S the symmetric stress tensor of the Voigt vector
+                const DF t0 = df_add(df_add(df_mul(sw[0], g0), df_mul(sw[3], g1)), df_mul(sw[4], g2));
+                const DF t1 = df_add(df_add(df_mul(sw[3], g0), df_mul(sw[1], g1)), df_mul(sw[5], g2));
+                const DF t2 = df_add(df_add(df_mul(sw[4], g0), df_mul(sw[5], g1)), df_mul(sw[2], g2));
+                S.u.gh[it] = make_float4(g0.hi, g1.hi, g2.hi, 0.f);
+                S.u.gl[it] = make_float4(g0.lo, g1.lo, g2.lo, 0.f);
+                S.u.th[it] = make_float4(t0.hi, t1.hi, t2.hi, 0.f);
+                S.u.tl[it] = make_float4(t0.lo, t1.lo, t2.lo, 0.f);
+            }
+        }
+    }
+    // residual: sum over the eight points (lanes with the same s), delivered by lanes 0..3
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int v = 0; v < 3; ++v)
+#pragma unroll
+            for (int m = 4; m <= 16; m <<= 1) ru[k][v] = df_add(ru[k][v], df_shfl_xor(ru[k][v], m));
+    if (lane < 4) {
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const int a = 2 * lane + k;
+            if (A.loadInt) {
+                const int r = A.rank[A.elist[8 * (size_t)e + a] - 1] - 1;
+#pragma unroll
+                for (int v = 0; v < 3; ++v) A.loadInt[3 * (size_t)r + v] -= df_to_double(ru[k][v]);
+            }
+            if (A.ruOut)
+#pragma unroll
+                for (int v = 0; v < 3; ++v) A.ruOut[24 * (size_t)e + 8 * v + a] = df_to_double(ru[k][v]);
+        }
+    }
+    if (!BUILD) return;
+    __syncwarp();
+    // ---- phase 2: units 9 lane .. 9 lane + 8 of the 288 (tile, point) units ------------------------
+    const int u0 = 9 * lane;
+    const int tA = u0 >> 3;                 // first tile (shared with the previous lane unless u0 % 8 == 0)
+    const int usw = 8 * (tA + 1) - u0;      // unit at which the second tile starts (1..8)
+    DF acc[9], geo = zero, acc0[9], geo0 = zero;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] = acc0[q] = zero;
+#pragma unroll
+    for (int u = 0; u < 9; ++u) {
+        if (u == usw) {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                acc0[q] = acc[q];
+                acc[q] = zero;
+            }
+            geo0 = geo;
+            geo = zero;
+        }
+        const int unit = u0 + u, t = unit >> 3, p = unit & 7;
+        const int ia = 8 * p + c_tileA[t], ib = 8 * p + c_tileB[t];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            float ph[3], pl[3], qh[3], ql[3];
+#pragma unroll
+            for (int v = 0; v < 3; ++v) {
+                ph[v] = S.u.Ph[ia][3 * q + v];
+                pl[v] = S.u.Pl[ia][3 * q + v];
+                qh[v] = S.u.Qh[ib][3 * q + v];
+                ql[v] = S.u.Ql[ib][3 * q + v];
+            }
+#pragma unroll
+            for (int v = 0; v < 3; ++v)
+#pragma unroll
+                for (int x = 0; x < 3; ++x) df_acc(acc[3 * v + x], ph[v], pl[v], qh[x], ql[x]);
+        }
+        const float4 gh = S.u.gh[ia], gl = S.u.gl[ia], th = S.u.th[ib], tl = S.u.tl[ib];
+        df_acc(geo, gh.x, gl.x, th.x, tl.x);
+        df_acc(geo, gh.y, gl.y, th.y, tl.y);
+        df_acc(geo, gh.z, gl.z, th.z, tl.z);
+    }
+    __syncwarp();
+    // partials: the first tile to slot 0 when it starts on this lane (u0 % 8 == 0), else slot 1;
+    // the second tile starts here, slot 0
+    {
+        float *d0 = S.o.part[tA][(u0 & 7) ? 1 : 0];
+        float *d1 = S.o.part[tA + 1][0];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const DF x0 = df_norm(acc0[q]), x1 = df_norm(acc[q]);
+            d0[2 * q] = x0.hi;
+            d0[2 * q + 1] = x0.lo;
+            d1[2 * q] = x1.hi;
+            d1[2 * q + 1] = x1.lo;
+        }
+        const DF y0 = df_norm(geo0), y1 = df_norm(geo);
+        d0[18] = y0.hi;
+        d0[19] = y0.lo;
+        d1[18] = y1.hi;
+        d1[19] = y1.lo;
+    }
+    __syncwarp();
+    // ---- phase 3: blocks (a0, b) and (a1, b), a0 = lane / 8, a1 = a0 + 4, b = lane % 8 -----------
+    const int b = lane & 7;
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+        const int a = (lane >> 3) + 4 * half;
+        const int lo = min(a, b), hi = max(a, b);
+        const int t = lo * 8 - (lo * (lo - 1)) / 2 + (hi - lo);  // row-major upper-triangle index
+        const bool two = (8 * t) / 9 != (8 * t + 7) / 9;        // the tile spans two lanes
+        const float *p0 = S.o.part[t][0], *p1 = S.o.part[t][1];
+        double Kb[9];
+        const DF gs = two ? df_add(DF{p0[18], p0[19]}, DF{p1[18], p1[19]}) : DF{p0[18], p0[19]};
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            DF v = two ? df_add(DF{p0[2 * q], p0[2 * q + 1]}, DF{p1[2 * q], p1[2 * q + 1]}) : DF{p0[2 * q], p0[2 * q + 1]};
+            if (q == 0 || q == 4 || q == 8) v = df_add(v, gs);
+            Kb[q] = df_to_double(v);
+        }
+        double *dst = S.o.K + 9 * (8 * a + b);
+        // tile (lo, hi) holds K_lo,hi; block (a, b) with a > b is its transpose
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) dst[3 * i + j] = (a <= b) ? Kb[3 * i + j] : Kb[3 * j + i];
+    }
+    __syncwarp();
+    if (A.K) {
+        const unsigned long long first = A.elFirst[e];
+        const int grp = lane / 9, qq = lane - 9 * grp;
+#pragma unroll
+        for (int stp = 0; stp < kRmwSteps; ++stp) {
+            const int j = 3 * stp + grp;
+            if (grp < 3 && j < 64) {
+                double *dst = A.K + 9 * (size_t)S.blk[j] + qq;
+                const double v = S.o.K[9 * j + qq];
+                *dst = ((first >> j) & 1ull) ? v : *dst + v;
+            }
+        }
+    }
+    if (A.keOut) {
+        double *ke = A.keOut + 576 * (size_t)e;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int a = (lane >> 3) + 4 * half;
+            const double *src = S.o.K + 9 * (8 * a + b);
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) ke[(size_t)(8 * j + b) * 24 + (8 * i + a)] = src[3 * i + j];
+        }
+    }
+}
+
+// Node coordinates of every brick element in its section frame (orient X, relative to the
+// element's first node, FP64) and its C, both split into double-float for the element kernels.
 __global__ void k_elem_df(int E, const double *__restrict__ nodes, const int *__restrict__ elist,
                           const double *__restrict__ orient, const double *__restrict__ elC, float2 *__restrict__ Xdf,
                           float2 *__restrict__ Cdf) {
@@ -734,9 +884,14 @@ __global__ void k_elem_df(int E, const double *__restrict__ nodes, const int *__
     double Or[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) Or[i][j] = orient ? orient[9 * (size_t)e + 3 * j + i] : (i == j ? 1.0 : 0.0);
+    // relative to the element's first node: the Jacobian only sees coordinate differences, and
+    // taking them here in FP64 keeps the FP32 kernel from losing bits to cancellation (absolute
+    // coordinates are up to about 60 element sizes larger than the differences in a block)
+    const double *x0 = nodes + 3 * (size_t)(elist[8 * (size_t)e] - 1);
     for (int a = 0; a < 8; ++a) {
         const int nd = elist[8 * (size_t)e + a];
-        const double *x = nodes + 3 * (size_t)(nd - 1);
+        const double *xa = nodes + 3 * (size_t)(nd - 1);
+        const double x[3] = {xa[0] - x0[0], xa[1] - x0[1], xa[2] - x0[2]};
         for (int i = 0; i < 3; ++i) {
             const double y = Or[i][0] * x[0] + Or[i][1] * x[1] + Or[i][2] * x[2];
             const DF d = df_from_double(y);
@@ -774,7 +929,7 @@ __global__ void k_elem_c(int E, const double *__restrict__ elMat, double *__rest
 __global__ void k_hex_cim(int count, const int *__restrict__ els, const double *__restrict__ elMat,
                           const int *__restrict__ e2dR, const int *__restrict__ e2d, const double *__restrict__ e2c,
                           const int *__restrict__ dcat, const int *__restrict__ dcomp, int dvar, double h,
-                          double *__restrict__ Cim) {
+                          float2 *__restrict__ Cim) {
     const int item = blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= count) return;
     const int e = els[item];
@@ -786,8 +941,13 @@ __global__ void k_hex_cim(int count, const int *__restrict__ els, const double *
     }
     cplx C[6][6];
     material_c<cplx>(ep, C);
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) Cim[36 * (size_t)item + 6 * i + j] = C[i][j].im;
+    // the orthotropic entries C11 C12 C13 C22 C23 C33 C44 C55 C66 of Im(C), in double-float
+    const double v[9] = {C[0][0].im, C[0][1].im, C[0][2].im, C[1][1].im, C[1][2].im,
+                         C[2][2].im, C[3][3].im, C[4][4].im, C[5][5].im};
+    for (int q = 0; q < 9; ++q) {
+        const DF d = df_from_double(v[q]);
+        Cim[9 * (size_t)item + q] = make_float2(d.hi, d.lo);
+    }
 }
 
 }  // namespace
@@ -825,56 +985,58 @@ template <class T> static int hex8_fast_run(astro_ctx *ctx, T *K, double *d_ke) 
     return cuda_check(ctx, cudaGetLastError(), "brick8 zero-state kernel launch");
 }
 
-// precision 64: general FP64 kernel (state, orientation); 32: FP32 kernel at zero state.
-// store bit 1: FP32 BSR, bit 2: FP64 BSR (the FP32 kernel adds its values into both when asked).
-static int hex8_run(astro_ctx *ctx, int precision, int store, const double *d_disp, double *d_loadInt, double *d_ke,
-                    double *d_ru) {
-    const AstroPrep &P = ctx->P;
-    for (int col = 0; col < P.ncolors; ++col) {
-        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+// General-state element kernel (double-float), colour by colour over the elements of list
+// (colour c covering list[ptr[c] .. ptr[c+1])): the block-CSR matrix (with BUILD), the residual
+// into d_loadInt (load -= Ru), element matrices and residuals.  CdfItem: per listed element its C
+// (double-float, the complex step's imaginary part) instead of the element's own; gpc the Gauss
+// point coordinate.
+static int hex8_gen_run(astro_ctx *ctx, const int *d_list, const std::vector<int> &ptr, bool build, double *K,
+                        const double *d_disp, double *d_loadInt, double *d_ke, double *d_ru, const float2 *CdfItem,
+                        double gpc) {
+    Hex8GenArgs A;
+    A.elBlk = dptr<int>(ctx->d_elBlk);
+    A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
+    A.elist = dptr<int>(ctx->d_elist);
+    A.rank = dptr<int>(ctx->d_rank);
+    A.Xdf = dptr<float2>(ctx->d_elXdf);
+    A.Cdf = dptr<float2>(ctx->d_elCdf);
+    A.orient = dptr<double>(ctx->d_secOrient);
+    A.disp = d_disp;
+    A.K = K;
+    A.loadInt = d_loadInt;
+    A.keOut = d_ke;
+    A.ruOut = d_ru;
+    const DF g = df_from_double(gpc);
+    A.gpcHi = g.hi;
+    A.gpcLo = g.lo;
+    const bool rot = !ctx->orientIdentity;
+    for (size_t col = 0; col + 1 < ptr.size(); ++col) {
+        const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
-        dim3 grid((cnt + kWarpsPerBlock - 1) / kWarpsPerBlock), block(32 * kWarpsPerBlock);
-        if (precision == 64) {
-            Hex8Args<double> A;
-            A.nodes = dptr<double>(ctx->d_nodes);
-            A.elist = dptr<int>(ctx->d_elist);
-            A.rank = dptr<int>(ctx->d_rank);
-            A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
-            A.count = cnt;
-            A.elBlk = dptr<int>(ctx->d_elBlk);
-            A.elMat = dptr<double>(ctx->d_elMat);
-            A.orient = ctx->orientIdentity ? nullptr : dptr<double>(ctx->d_secOrient);
-            A.disp = d_disp;
-            A.Kbsr = (store & 2) ? dptr<double>(ctx->d_K64) : nullptr;
-            A.Kbsr64 = nullptr;
-            A.loadInt = d_loadInt;
-            A.keOut = d_ke;
-            A.ruOut = d_ru;
-            A.gpc = kRt3;
-            A.Cover = nullptr;
-            hex8_kernel<double, true><<<grid, block, 0, ctx->stream>>>(A);
+        A.colorEls = d_list + ptr[col];
+        A.count = cnt;
+        A.CdfItem = CdfItem ? CdfItem + 9 * (size_t)ptr[col] : nullptr;
+        const unsigned grid = (cnt + kGenW - 1) / kGenW;
+        if (build) {
+            if (rot)
+                hex8_gen_kernel<true, true><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
+            else
+                hex8_gen_kernel<false, true><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
         } else {
-            Hex8Args<float> A;
-            A.nodes = dptr<double>(ctx->d_nodes);
-            A.elist = dptr<int>(ctx->d_elist);
-            A.rank = dptr<int>(ctx->d_rank);
-            A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
-            A.count = cnt;
-            A.elBlk = dptr<int>(ctx->d_elBlk);
-            A.elMat = dptr<double>(ctx->d_elMat);
-            A.orient = nullptr;
-            A.disp = nullptr;
-            A.Kbsr = (store & 1) ? dptr<float>(ctx->d_K32) : nullptr;
-            A.Kbsr64 = (store & 2) ? dptr<double>(ctx->d_K64) : nullptr;
-            A.loadInt = nullptr;
-            A.keOut = d_ke;
-            A.ruOut = nullptr;
-            A.gpc = kRt3;
-            A.Cover = nullptr;
-            hex8_kernel<float, false><<<grid, block, 0, ctx->stream>>>(A);
+            if (rot)
+                hex8_gen_kernel<true, false><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
+            else
+                hex8_gen_kernel<false, false><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
         }
     }
-    return cuda_check(ctx, cudaGetLastError(), "hex8 kernel launch");
+    return cuda_check(ctx, cudaGetLastError(), "brick8 general-state kernel launch");
+}
+
+// every element of the context, colour by colour
+static int hex8_run(astro_ctx *ctx, bool build, double *K, const double *d_disp, double *d_loadInt, double *d_ke,
+                    double *d_ru) {
+    return hex8_gen_run(ctx, dptr<int>(ctx->d_colorEls), ctx->P.colorPtr, build || d_ke, K, d_disp, d_loadInt, d_ke,
+                        d_ru, nullptr, kRt3);
 }
 
 // FP64 zero-state stiffness (double-float kernel), colour by colour.
@@ -905,6 +1067,15 @@ static int hex8_df_run(astro_ctx *ctx, double *K, double *d_ke) {
 int hex8_prepare(astro_ctx *ctx) {
     const int E = ctx->P.E;
     int rc;
+    // node-pair tiles (a, b), a <= b, in row-major upper-triangle order, for hex8_gen_kernel
+    unsigned char ta[36], tb[36];
+    for (int a = 0, t = 0; a < 8; ++a)
+        for (int b = a; b < 8; ++b, ++t) {
+            ta[t] = (unsigned char)a;
+            tb[t] = (unsigned char)b;
+        }
+    CK(cudaMemcpyToSymbol(c_tileA, ta, sizeof(ta)));
+    CK(cudaMemcpyToSymbol(c_tileB, tb, sizeof(tb)));
     if ((rc = dev_alloc(ctx, ctx->d_elC, sizeof(double) * 9 * (size_t)E))) return rc;
     k_elem_c<<<(E + 127) / 128, 128, 0, ctx->stream>>>(E, dptr<double>(ctx->d_elMat), dptr<double>(ctx->d_elC));
     if ((rc = dev_alloc(ctx, ctx->d_elXdf, sizeof(float2) * 24 * (size_t)E))) return rc;
@@ -928,7 +1099,8 @@ int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
 // Lagrange strain, stress stiffness, residual), which adds into a zeroed matrix.
 int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt) {
     if (!d_disp) return buildMat ? hex8_df_run(ctx, dptr<double>(ctx->d_K64), nullptr) : ASTRO_OK;
-    return hex8_run(ctx, 64, buildMat ? 2 : 0, d_disp, d_loadInt, nullptr, nullptr);
+    return hex8_run(ctx, buildMat != 0, buildMat ? dptr<double>(ctx->d_K64) : nullptr, d_disp, d_loadInt, nullptr,
+                    nullptr);
 }
 
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
@@ -938,7 +1110,7 @@ int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
 
 int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru) {
     if (!d_disp && !d_ru) return hex8_df_run(ctx, nullptr, d_ke);
-    return hex8_run(ctx, 64, 0, d_disp, nullptr, d_ke, d_ru);
+    return hex8_run(ctx, d_ke != nullptr, nullptr, d_disp, nullptr, d_ke, d_ru);
 }
 
 int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *d_acc) {
@@ -955,7 +1127,7 @@ int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *
     } fr{{&dl, &dC, &dR, &dE, &dEC, &dCat, &dComp}};
     int rc;
     if ((rc = upload(ctx, dl, list.data(), sizeof(int) * cnt))) return rc;
-    if ((rc = dev_alloc(ctx, dC, sizeof(double) * 36 * (size_t)cnt))) return rc;
+    if ((rc = dev_alloc(ctx, dC, sizeof(float2) * 9 * (size_t)cnt))) return rc;
     if ((rc = upload(ctx, dR, ctx->e2dRange.data(), sizeof(int) * ctx->e2dRange.size()))) return rc;
     if ((rc = upload(ctx, dE, ctx->e2d.data(), sizeof(int) * ctx->e2d.size()))) return rc;
     if ((rc = upload(ctx, dEC, ctx->e2c.data(), sizeof(double) * ctx->e2c.size()))) return rc;
@@ -963,31 +1135,12 @@ int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *
     if ((rc = upload(ctx, dComp, ctx->dComp.data(), sizeof(int) * ctx->dComp.size()))) return rc;
     k_hex_cim<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(cnt, dptr<int>(dl), dptr<double>(ctx->d_elMat), dptr<int>(dR),
                                                           dptr<int>(dE), dptr<double>(dEC), dptr<int>(dCat),
-                                                          dptr<int>(dComp), dvar, h, dptr<double>(dC));
-    const AstroPrep &P = ctx->P;
-    for (int col = 0; col < P.ncolors; ++col) {
-        const int c = ptr[col + 1] - ptr[col];
-        if (!c) continue;
-        Hex8Args<double> A;
-        A.nodes = dptr<double>(ctx->d_nodes);
-        A.elist = dptr<int>(ctx->d_elist);
-        A.rank = dptr<int>(ctx->d_rank);
-        A.colorEls = dptr<int>(dl) + ptr[col];
-        A.count = c;
-        A.elBlk = dptr<int>(ctx->d_elBlk);
-        A.elMat = dptr<double>(ctx->d_elMat);
-        A.orient = ctx->orientIdentity ? nullptr : dptr<double>(ctx->d_secOrient);
-        A.disp = d_disp;
-        A.Kbsr = nullptr;
-        A.Kbsr64 = nullptr;
-        A.loadInt = d_acc;
-        A.keOut = nullptr;
-        A.ruOut = nullptr;
-        A.gpc = kRt3c;
-        A.Cover = dptr<double>(dC) + 36 * (size_t)ptr[col];
-        hex8_kernel<double, true><<<(c + kWarpsPerBlock - 1) / kWarpsPerBlock, 32 * kWarpsPerBlock, 0, ctx->stream>>>(A);
-    }
-    cudaError_t e = cudaGetLastError();
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+                                                          dptr<int>(dComp), dvar, h, dptr<float2>(dC));
+    // the residual is linear in C: its imaginary part is the residual evaluated with Im(C), at the
+    // complex path's Gauss points
+    if ((rc = hex8_gen_run(ctx, dptr<int>(dl), ptr, false, nullptr, d_disp, d_acc, nullptr, nullptr, dptr<float2>(dC),
+                           kRt3c)))
+        return rc;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
     return cuda_check(ctx, e, "brick8 complex-step kernels");
 }

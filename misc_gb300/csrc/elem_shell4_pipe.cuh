@@ -375,7 +375,9 @@ __device__ void pipe_dedu(const ShellPipe &A, int q, int g, int i) {
 
 // Newmark mass column j (< 24) of r_getElRum: the static frame keeps only its first columns, so
 // the derivative of the instantaneous DOF is sparse: translation var at node nd maps to io0(:,var),
-// rotation v at node nd to drIdrG(:,v).
+// rotation v at node nd to drIdrG(:,v).  With the consistent rotation derivative (quirk) a rotation
+// DOF also moves the element mean rotation, so every node's instantaneous rotation changes by
+// -drIdrG(:,v)/4: at a point the derivative is then drIdrG(:,v) (N(nd) - sum_k N(k) / 4).
 __device__ __forceinline__ void mass_dof(const ShellFrame &F, int i, int &nd, double bv[6]) {
     int var;
     dof_of(i, var, nd);
@@ -388,6 +390,14 @@ __device__ __forceinline__ void mass_dof(const ShellFrame &F, int i, int &nd, do
 
 // instNodalAcc = sum_i acc(var_i, nd_i) * d instU / d u_i (nodal part) and iNAM = M instNodalAcc
 // for node n of the element (r_getElRum), the DOF of the node in their order
+// the shape-function weight of DOF (var, nd) in the derivative of the instantaneous DOF at a
+// point (see mass_dof)
+__device__ __forceinline__ double mass_weight(const ShellGP &G, int var, int nd, int quirk) {
+    double w = G.Nv[nd - 1];
+    if (quirk && var >= 4) w -= 0.25 * (G.Nv[0] + G.Nv[1] + G.Nv[2] + G.Nv[3]);
+    return w;
+}
+
 __device__ void pipe_inam(const ShellPipe &A, int q, int n) {
     ASTRO_GUARD(A.status, 151, ASTRO_IN(q, A.scratchEls) && ASTRO_IN(n, 4) && ASTRO_IN(A.els[q], A.nEls));
     const ShellProps &P = A.props[A.els[q]];
@@ -400,6 +410,14 @@ __device__ void pipe_inam(const ShellPipe &A, int q, int n) {
         const double a = F.acc[var - 1][nd - 1];
         for (int r = 0; r < 6; ++r) ina[r] += a * bv[r];
     }
+    // consistent rotation derivative: the rotation DOF of every node also reach node n through the
+    // mean rotation, -1/4 each
+    if (A.quirk)
+        for (int v = 1; v <= 3; ++v)
+            for (int j = 0; j < 4; ++j) {
+                const double a = 0.25 * F.acc[2 + v][j];
+                for (int r = 0; r < 3; ++r) ina[3 + r] -= a * F.dr[v][r];
+            }
     for (int r = 0; r < 6; ++r) {
         double s = 0.0;
         for (int k = 0; k < 6; ++k) s += P.M[6 * r + k] * ina[k];
@@ -450,17 +468,22 @@ __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
     if (A.dynamic && j < 24) {
         const double c1 = 0.5 / A.beta, c2 = 2.0 / (A.delT * A.delT);
         const double(*inam)[4] = F.inam;
-        int ndj;
+        int ndj, varj;
         double bj[6];
         mass_dof(F, j, ndj, bj);
+        {
+            int t;
+            dof_of(j, varj, t);
+        }
         double rum = 0.0, mcol[24];
         for (int i = 0; i < 24; ++i) mcol[i] = 0.0;
         for (int g = 0; g < 4; ++g) {
             const ShellGP &G = A.gp[4 * (size_t)q + g];
             const double wd = G.wdet;
             double du[6], fi[6];
+            const double wj = mass_weight(G, varj, ndj, A.quirk);
             for (int r = 0; r < 6; ++r) {
-                du[r] = bj[r] * G.Nv[ndj - 1];
+                du[r] = bj[r] * wj;
                 fi[r] = inam[r][0] * G.Nv[0] + inam[r][1] * G.Nv[1] + inam[r][2] * G.Nv[2] + inam[r][3] * G.Nv[3];
             }
             for (int r = 0; r < 6; ++r) rum += fi[r] * (wd * du[r]);
@@ -472,11 +495,13 @@ __device__ void pipe_kcol(const ShellPipe &A, int q, int j) {
                     Mdu[r] = wd * s;
                 }
                 for (int i = 0; i < 24; ++i) {
-                    int ndi;
+                    int ndi, vari, t;
                     double bi[6];
                     mass_dof(F, i, ndi, bi);
+                    dof_of(i, vari, t);
+                    const double wi = mass_weight(G, vari, ndi, A.quirk);
                     double s = 0.0;
-                    for (int r = 0; r < 6; ++r) s += (bi[r] * G.Nv[ndi - 1]) * Mdu[r];
+                    for (int r = 0; r < 6; ++r) s += (bi[r] * wi) * Mdu[r];
                     mcol[i] += s;
                 }
             }

@@ -7,12 +7,18 @@
   - the residual and tangent of a sample at a displaced state (the general kernel), 1e-12;
   - the whole assembled CSR matrix and residual load at that displaced state, 1e-12 of the
     largest entry / of the load's norm, columns bit-exact;
-  - the operator K + C^T C of the FP64 assembly applied to random vectors, 1e-13 relative.
+  - the operator K + C^T C of the FP64 assembly applied to random vectors: 1e-13 relative against
+    the same operator built from the exported matrix and scaled constraints (the device product),
+    and 1e-12 against the oracle's own assembly and scaling (the element-matrix tolerance; the
+    penalty scale 100 max|K| inherits it).
 * The 128x128 simply supported shell plate (99,846 DOF, dt 1e-5): five Newmark steps against
   the oracle's time loop with a direct solve of K_eff, 1e-8 per step.
 * 16 of the 512 panels of the batched-panel workload (every 32nd): the band LDL^T solutions of
-  the pressure load and of design-sensitivity right-hand sides against sparse direct solves of the
-  oracle's K + C^T C, 1e-10.
+  the pressure load, of design-sensitivity right-hand sides and of random ones against sparse
+  direct solves of the oracle's K + C^T C.  Both factorisations are backward stable; the thin
+  panels (t down to 0.01 at an element size of 0.1) are ill-conditioned in bending, so the test
+  holds the band solve's residual within 10 times the sparse solve's and the two solutions within
+  1e-7 of each other (their distance is bounded by kappa times the rounding of either).
 * The 96x48x48 evaluation block of the learned preconditioner (698,691 DOF): the learned FGMRES
   solution at 1e-8 FP64 relative residual against the FP64 solution (Jacobi-GMRES to 1e-12).  The
   forward error of a solve with relative residual rho is at most kappa(A) rho; the test asserts
@@ -101,14 +107,17 @@ def test_cfg2_operator(cfg2):
     _, _, omat, ocols, _ = o.el_soln_load(1)
     omm, _ = o.scale_mpc(omat)
     assert np.array_equal(cols, ocols)
-    assert np.allclose(mm, omm, rtol=1e-14, atol=0)
-    Cm = o.mpc_scipy(omm)
-    A = o.csr_scipy(omat, ocols) + Cm.T @ Cm
+    assert np.allclose(mm, omm, rtol=1e-12, atol=0)
+    Cg, Co = o.mpc_scipy(mm), o.mpc_scipy(omm)
+    Ag = o.csr_scipy(mat, cols) + Cg.T @ Cg
+    Ao = o.csr_scipy(omat, ocols) + Co.T @ Co
     rng = np.random.default_rng(11)
     for _ in range(3):
         x = rng.standard_normal(o.n)
-        y, yo = g.apply_operator(x, 64), A @ x
-        assert np.linalg.norm(y - yo) <= 1e-13 * np.linalg.norm(yo)
+        y = g.apply_operator(x, 64)
+        yg, yo = Ag @ x, Ao @ x
+        assert np.linalg.norm(y - yg) <= 1e-13 * np.linalg.norm(yg)
+        assert np.linalg.norm(y - yo) <= 1e-12 * np.linalg.norm(yo)
 
 
 def _set_quirk(v):
@@ -161,7 +170,9 @@ def test_cfg3_panel_subset():
     lu = spla.splu(A)
     for c in range(B.shape[1]):
         xr = lu.solve(B[:, c])
-        assert np.linalg.norm(X[:, c] - xr) <= 1e-10 * np.linalg.norm(xr), c
+        r, r_ref = np.linalg.norm(A @ X[:, c] - B[:, c]), np.linalg.norm(A @ xr - B[:, c])
+        assert r <= 10.0 * r_ref + 1e-14 * np.linalg.norm(B[:, c]), (c, r, r_ref)
+        assert np.linalg.norm(X[:, c] - xr) <= 1e-7 * np.linalg.norm(xr), c
 
 
 def test_cfg4_learned_solution_error():
