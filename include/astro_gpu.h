@@ -41,8 +41,9 @@ extern "C" {
 #define ASTRO_DCAT_ELASTIC_MODULUS 2   /* 'elastic' / 'modulus': materialElastic entry d_component (1..9) */
 
 /* Model arrays: the reference's module globals (Working/AStrO_globalData.f90) as flat arrays.
- * Element types: 8 = brick8 (2x2x2 Gauss), 41 = shell4 (4 Gauss points, 8 condensed
- * incompatible-mode DOF).  Constraints are given as expanded equations: equation k has terms
+ * Element types: 8 = brick8 (2x2x2 Gauss), 81 = brickIM (brick8 plus three incompatible bubbles,
+ * 9 condensed internal DOF), 41 = shell4 (4 Gauss points, 8 condensed incompatible-mode DOF);
+ * solid (8, 81) and shell elements are not mixed in one model.  Constraints are given as expanded equations: equation k has terms
  * mpc_range[k-1]..mpc_range[k]-1 (0-based term index), each term (node, dof, coef). */
 typedef struct astro_model {
     int32_t num_nodes;
@@ -442,7 +443,7 @@ int astro_solve_static(astro_ctx *ctx, const double *f, double *u, const astro_s
  * (acc, vel, previous values).  disp/vel/acc (el_mat_dim) and int_disp (int_vec_size, may be
  * NULL) hold the initial state on entry (loadInitialState) and the final state on exit;
  * disp_history (num_steps x el_mat_dim, may be NULL) receives the displacement of every step.
- * Shell meshes (the Newmark inertia of the element library is implemented for shell4). */
+ * Shell and solid meshes (r_getElRum's shell and solid branches). */
 typedef struct astro_newmark_opts {
     int32_t num_steps;
     double del_t, nm_beta, nm_gamma;
@@ -529,7 +530,7 @@ int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double h, const d
  * int_dldu (num_steps x int_vec_size); any may be NULL (zero).  Faithful to the reference: the
  * 1e-20 scaling round trip around augmentdLdu, the warm start of each adjoint solve from the
  * previous one, and the internal adjoint accumulated across steps (updateInternalSoln adds).
- * Shell meshes (the Newmark inertia is implemented for shell4).  disp_adj (el_mat_dim, may be NULL)
+ * Shell and solid meshes.  disp_adj (el_mat_dim, may be NULL)
  * receives the adjoint of step 1; stats sums the solves. */
 typedef struct astro_transient_adjoint {
     int32_t num_steps;

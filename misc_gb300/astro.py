@@ -521,13 +521,13 @@ class AstroGPU:
         return x
 
     def updateExternalRHS(self, ext_vec, int_vec):
-        """ext_vec -= K_ni K_ii^-1 int_vec over the shell elements (returns a new array)."""
+        """ext_vec -= K_ni K_ii^-1 int_vec over the elements with internal DOF (returns a new array)."""
         out = _f64(ext_vec).copy()
         self._check(self.L.astro_update_external_rhs(self.h, _d(out), _d(_f64(int_vec))))
         return out
 
     def updateInternalSoln(self, ext_soln, int_soln, int_rhs=None):
-        """int_soln + K_ii^-1 (int_rhs - K_in ext_soln) over the shell elements (new array)."""
+        """int_soln + K_ii^-1 (int_rhs - K_in ext_soln) over the elements with internal DOF (new array)."""
         out = _f64(int_soln).copy()
         rhs = None if int_rhs is None else _d(_f64(int_rhs))
         self._check(self.L.astro_update_internal_soln(self.h, _d(_f64(ext_soln)), _d(out), rhs))

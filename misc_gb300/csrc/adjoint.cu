@@ -26,8 +26,6 @@ extern "C" int astro_total_dldd_transient(astro_ctx *ctx, const astro_transient_
     if (!ctx || !a || !dldd || !a->disp || !a->vel || !a->acc || a->num_steps < 1 || !(a->del_t > 0.0) ||
         !(a->nm_beta > 0.0) || !(a->h > 0.0))
         return ASTRO_ERR_ARG;
-    if (!ctx->hasShell || ctx->hasSolid)
-        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "the transient adjoint needs the Newmark inertia of shell4 meshes");
     astro_dims dims;
     int rc;
     if ((rc = astro_get_dims(ctx, &dims))) return rc;

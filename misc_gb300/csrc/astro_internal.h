@@ -138,6 +138,11 @@ struct astro_ctx {
     DevBuf d_scratch;
     DevBuf d_status;  // int status words written by kernels
     DevBuf d_guard;   // checked build: site of the first failed index guard (bounds.cuh), else 0
+    // solid meshes: the colour-grouped element lists split by type (brick8, brickIM), the
+    // internal-DOF offsets (intVecRange, intMatRange) and the per-element density on the device
+    std::vector<int> c8Els, c8Ptr, c81Els, c81Ptr;
+    DevBuf d_c8Els, d_c81Els, d_intVecOff, d_intMatOff, d_elRho;
+    int has81 = 0;
     int quirkShellMeanRot = 0;
 };
 
@@ -162,20 +167,21 @@ int astro_prep_build(astro_ctx *c, const astro_model *m);
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store);           // elem_hex8.cu
 int hex8_prepare(astro_ctx *ctx);  // per-element material stiffness, once per context (elem_hex8.cu)
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *ke_host); // elem_hex8.cu
-// device state of a shell evaluation (internal layout; any pointer may be null = zeros)
-struct ShellDevState {
+// device state of an element evaluation (internal layout: nodal vectors rank-major, dpn per node;
+// internal-DOF vectors in intVecRange order; any pointer may be null = zeros)
+struct ElemDevState {
     const double *disp = nullptr, *pdisp = nullptr, *pvel = nullptr, *pacc = nullptr;
     const double *idisp = nullptr, *pidisp = nullptr;
     int dynamic = 0;
     double beta = 0.25, gamma = 0.5, delT = 0.0;
     int massOnly = 0;  // residual = the Newmark mass term alone (needs dynamic, no matrix)
 };
-int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &s, double *d_loadInt, double *d_intLoad,
+int launch_shell4_assemble(astro_ctx *ctx, const ElemDevState &s, double *d_loadInt, double *d_intLoad,
                            int buildMat, double *d_ke, double *d_ru, bool sync = true);  // elem_shell4.cu
 int shell_sections_prepare(astro_ctx *ctx, const astro_model *m);          // elem_shell4.cu
-int shell4_residual_list(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
+int shell4_residual_list(astro_ctx *ctx, const ElemDevState &st, const int *d_els, const std::vector<int> &ptr,
                          double *d_loadInt);                                 // elem_shell4.cu
-int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, const std::vector<int> &list,
+int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ElemDevState &st, const std::vector<int> &list,
                      const std::vector<int> &ptr, double *d_acc, double *d_intAcc,
                      const std::function<int(const int *, int)> &hook);     // elem_shell4.cu
 int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt);          // elem_shell4.cu
@@ -191,12 +197,32 @@ int ref_to_int_vec(astro_ctx *ctx, const double *d_ref, double *d_int, int n); /
 int int_to_ref_vec(astro_ctx *ctx, const double *d_int, double *d_ref, int n); // assemble.cu
 int surface_load_dev(astro_ctx *ctx, int nf, const int *d_faceEl, const int *d_faceNum, const double *tr,
                      double pressure, double *d_loadInt);                   // assemble.cu
-int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt);       // elem_hex8.cu
-int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru);   // elem_hex8.cu
+// Solid elements (brick8 and brickIM), colour by colour, at state s: load -= Ru into d_loadInt
+// (nodal, internal layout) and d_intLoad (internal DOF); with build = 1 the tangent (K, plus
+// c1 c2 M when s.dynamic) goes into the FP64 block-CSR matrix and the condensed internal rows of
+// the brickIM elements into d_intMat, or, when d_ke is given, the condensed element matrices
+// into d_ke (E x 24 x 24) instead; d_ru receives the element residuals (E x 24).
+int solid_soln_load(astro_ctx *ctx, int build, const ElemDevState &s, double *d_loadInt, double *d_intLoad,
+                    double *d_ke, double *d_ru);                                                   // elem_hex8.cu
+int hex81_run(astro_ctx *ctx, const int *d_list, const std::vector<int> &ptr, int build, double *K,
+              const ElemDevState &st, const double *CItem, double gpc, double *d_loadInt, double *d_intLoad,
+              double *d_intMat, double *d_ke, double *d_ru);                                       // elem_hex81.cu
+int hex81_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt);          // elem_hex81.cu
+int hex81_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln,
+                               const double *d_intRhs);                                            // elem_hex81.cu
+// getElasticSolnLoad on device vectors for any mesh (ctx.cu): load -= Ru, and with build = 1 the
+// FP64 block-CSR tangent (zeroed first for shells; the solid kernels write every block first)
+int elem_soln_load_dev(astro_ctx *ctx, const ElemDevState &s, double *d_loadInt, double *d_intLoad, int build,
+                       bool sync);
+// updateExternalRHS / updateInternalSoln of the context's elements with internal DOF (shell4 or
+// brickIM), device vectors in internal layout (ctx.cu)
+int elem_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt);
+int elem_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln, const double *d_intRhs);
 // Complex-step residual sensitivity of the elements that depend on design variable dvar:
 // d_acc -= Im(Ru(d + i h)) accumulated in colour order (internal layout; shells also d_intAcc).
-int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *d_acc);          // elem_hex8.cu
-int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &s, double *d_acc,
+int hex8_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
+              double *d_intAcc);                                                                    // elem_hex8.cu
+int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
                 double *d_intAcc);                                                              // elem_shell4.cu
 void krylov_release(astro_ctx *ctx);
 int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,

@@ -18,10 +18,22 @@
             return;                                                \
         }                                                          \
     } while (0)
+// the same for kernels whose warps synchronise: the whole warp evaluates the test (each lane
+// its own condition) and leaves together, so no lane waits at a warp barrier for one that left
+#define ASTRO_GUARD_WARP(status, site, ok)                                       \
+    do {                                                                         \
+        if (!__all_sync(0xffffffffu, (ok))) {                                    \
+            if ((threadIdx.x & 31) == 0 && (status)) atomicCAS((status), 0, (site)); \
+            return;                                                              \
+        }                                                                        \
+    } while (0)
 #else
 #define ASTRO_CHECKED 0
 #define ASTRO_GUARD(status, site, ok) \
     do {                              \
+    } while (0)
+#define ASTRO_GUARD_WARP(status, site, ok) \
+    do {                                   \
     } while (0)
 #endif
 

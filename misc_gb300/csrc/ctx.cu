@@ -83,7 +83,7 @@ static void free_all(astro_ctx *c) {
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
                       &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_elXdf, &c->d_elCdf, &c->d_ioRef,
                       &c->d_ioInt, &c->d_exMat, &c->d_exCols, &c->d_shFr, &c->d_shGp, &c->d_shDe, &c->d_shKf,
-                      &c->d_guard};
+                      &c->d_guard, &c->d_c8Els, &c->d_c81Els, &c->d_intVecOff, &c->d_intMatOff, &c->d_elRho};
     for (DevBuf *b : bufs) dev_free(*b);
 }
 
@@ -233,7 +233,32 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
     if ((rc = dev_alloc(ctx, ctx->d_guard, sizeof(int)))) return fail(rc, ctx->err);
     cudaMemset(ctx->d_guard.p, 0, sizeof(int));
     if (ctx->hasShell && (rc = shell_sections_prepare(ctx, m))) return fail(rc, ctx->err);
-    if (ctx->hasSolid && (rc = hex8_prepare(ctx))) return fail(rc, ctx->err);
+    if (ctx->hasSolid) {
+        // colour-grouped element lists by type (brick8 / brickIM), internal-DOF offsets, density
+        ctx->c8Ptr.assign(1, 0);
+        ctx->c81Ptr.assign(1, 0);
+        for (int col = 0; col < P.ncolors; ++col) {
+            for (int k = P.colorPtr[col]; k < P.colorPtr[col + 1]; ++k) {
+                const int e = P.colorEls[k];
+                (ctx->etype[e] == 81 ? ctx->c81Els : ctx->c8Els).push_back(e);
+            }
+            ctx->c8Ptr.push_back((int)ctx->c8Els.size());
+            ctx->c81Ptr.push_back((int)ctx->c81Els.size());
+        }
+        ctx->has81 = !ctx->c81Els.empty();
+        std::vector<int> c8(ctx->c8Els), c81(ctx->c81Els);
+        if (c8.empty()) c8.push_back(0);
+        if (c81.empty()) c81.push_back(0);
+        if ((rc = upload(ctx, ctx->d_c8Els, c8.data(), sizeof(int) * c8.size())) ||
+            (rc = upload(ctx, ctx->d_c81Els, c81.data(), sizeof(int) * c81.size())) ||
+            (rc = upload(ctx, ctx->d_intVecOff, P.intVecRange.data(), sizeof(int) * P.intVecRange.size())) ||
+            (rc = upload(ctx, ctx->d_intMatOff, P.intMatRange.data(), sizeof(int) * P.intMatRange.size())) ||
+            (rc = upload(ctx, ctx->d_elRho, ctx->elDensity.data(), sizeof(double) * ctx->elDensity.size())))
+            return fail(rc, ctx->err);
+        if (P.intMatSize && (rc = dev_alloc(ctx, ctx->d_intMat, sizeof(double) * (size_t)P.intMatSize)))
+            return fail(rc, ctx->err);
+        if ((rc = hex8_prepare(ctx))) return fail(rc, ctx->err);
+    }
     // unscaled constraints in internal numbering
     ctx->mpcScaledHost = P.mpcMat;
     ctx->mpcRhsScaledHost = P.mpcRhs;
@@ -325,9 +350,9 @@ static int state_vec_up(astro_ctx *ctx, const double *h, DevBuf &dst, bool zero_
     return rc;
 }
 
-// Shell evaluation state on the device: nodal vectors converted to the internal layout (in S),
-// internal-DOF vectors uploaded as they are (all elements are shell4, 8 internal DOF each).
-static int shell_state(astro_ctx *ctx, const astro_state *state, DevState &S, ShellDevState &ds) {
+// Element evaluation state on the device: nodal vectors converted to the internal layout (in S),
+// internal-DOF vectors uploaded as they are (intVecRange order).
+static int elem_state(astro_ctx *ctx, const astro_state *state, DevState &S, ElemDevState &ds) {
     int rc;
     if (!state) return ASTRO_OK;
     const size_t ni = (size_t)ctx->P.intVecSize;
@@ -369,8 +394,6 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
                                   double *int_elastic_load, double *elastic_mat, int32_t *el_mat_cols,
                                   double *int_elastic_mat) {
     if (!ctx || !elastic_load) return ASTRO_ERR_ARG;
-    if (state && state->dynamic && ctx->hasSolid)
-        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
     const AstroPrep &P = ctx->P;
     const int n = P.n;
     const bool exportMat = build_mat == 1 && (elastic_mat || el_mat_cols);
@@ -379,7 +402,7 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
     DevState S;
     if (state) {
         if ((rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
-        if (ctx->hasShell) {
+        if (ctx->hasShell || state->dynamic) {
             if ((rc = state_vec_up(ctx, state->prev_disp, S.pdisp))) return rc;
             if ((rc = state_vec_up(ctx, state->prev_vel, S.pvel))) return rc;
             if ((rc = state_vec_up(ctx, state->prev_acc, S.pacc))) return rc;
@@ -392,19 +415,21 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
     if ((rc = ref_to_int_vec(ctx, dRef, dl, n))) return rc;
     if (build_mat == 1) {
         if ((rc = ensure_K(ctx, 2))) return rc;
-        // the brick zero-state kernel writes every block (first touch), the other paths add
-        if (!(ctx->hasSolid && !S.disp.p) && (rc = bsr_zero(ctx, 2))) return rc;
+        // the solid kernels write every block (first touch in colour order), the shell one adds
+        if (ctx->hasShell && (rc = bsr_zero(ctx, 2))) return rc;
     }
-    if (ctx->hasSolid) {
-        rc = hex8_soln_load(ctx, build_mat == 1, S.disp.p ? dptr<double>(S.disp) : nullptr, dl);
-    } else {
+    {
         DevBuf il;
         if (int_elastic_load && P.intVecSize) {
             if ((rc = upload(ctx, il, int_elastic_load, sizeof(double) * P.intVecSize))) return rc;
         }
-        ShellDevState ds;
-        if ((rc = shell_state(ctx, state, S, ds))) return rc;
-        rc = launch_shell4_assemble(ctx, ds, dl, il.p ? dptr<double>(il) : nullptr, build_mat == 1, nullptr, nullptr);
+        ElemDevState ds;
+        if ((rc = elem_state(ctx, state, S, ds))) return rc;
+        if (ctx->hasSolid)
+            rc = solid_soln_load(ctx, build_mat == 1, ds, dl, il.p ? dptr<double>(il) : nullptr, nullptr, nullptr);
+        else
+            rc = launch_shell4_assemble(ctx, ds, dl, il.p ? dptr<double>(il) : nullptr, build_mat == 1, nullptr,
+                                        nullptr);
         if (!rc && il.p)
             rc = cuda_check(ctx, cudaMemcpy(int_elastic_load, il.p, sizeof(double) * P.intVecSize, cudaMemcpyDeviceToHost),
                             "int load download");
@@ -422,7 +447,7 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
     if (build_mat == 1) {
         ctx->haveK64 = 1;
         ctx->k64Version++;
-        ctx->haveIntMat = ctx->hasShell;
+        ctx->haveIntMat = P.intVecSize > 0;
     }
     // load back to reference numbering
     if ((rc = int_to_ref_vec(ctx, dl, dRef, n))) return rc;
@@ -443,12 +468,37 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
     return ASTRO_OK;
 }
 
+int elem_soln_load_dev(astro_ctx *ctx, const ElemDevState &s, double *d_loadInt, double *d_intLoad, int build,
+                       bool sync) {
+    if (ctx->hasSolid) {
+        const int rc = solid_soln_load(ctx, build, s, d_loadInt, d_intLoad, nullptr, nullptr);
+        if (rc || !sync) return rc;
+        return cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "solid elements");
+    }
+    if (build) {
+        const int rc = bsr_zero(ctx, 2);
+        if (rc) return rc;
+    }
+    return launch_shell4_assemble(ctx, s, d_loadInt, d_intLoad, build, nullptr, nullptr, sync);
+}
+
+int elem_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_extInt) {
+    if (!ctx->P.intVecSize) return ASTRO_OK;
+    return ctx->hasShell ? shell4_update_external_rhs(ctx, d_intVec, d_extInt)
+                         : hex81_update_external_rhs(ctx, d_intVec, d_extInt);
+}
+int elem_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln, const double *d_intRhs) {
+    if (!ctx->P.intVecSize) return ASTRO_OK;
+    return ctx->hasShell ? shell4_update_internal_soln(ctx, d_extInt, d_intSoln, d_intRhs)
+                         : hex81_update_internal_soln(ctx, d_extInt, d_intSoln, d_intRhs);
+}
+
 // updateExternalRHS (Working/AStrO_commandFunctions.f90:568-607) with the loop over the internal
-// rows (nodalDof+1 .. totalDof, the evident intent of its empty loop bound): for every shell
-// element ext_vec(nodal DOF) -= K_ni K_ii^-1 int_vec(element's internal DOF).
+// rows (nodalDof+1 .. totalDof, the evident intent of its empty loop bound): for every element
+// with internal DOF (shell4, brickIM) ext_vec(nodal DOF) -= K_ni K_ii^-1 int_vec(its internal DOF).
 extern "C" int astro_update_external_rhs(astro_ctx *ctx, double *ext_vec, const double *int_vec) {
     if (!ctx || !ext_vec || !int_vec) return ASTRO_ERR_ARG;
-    if (!ctx->hasShell || !ctx->P.intVecSize) return ASTRO_OK;  // no internal DOF: nothing to condense
+    if (!ctx->P.intVecSize) return ASTRO_OK;  // no internal DOF: nothing to condense
     if (!ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
     const int n = ctx->P.n;
     int rc;
@@ -458,7 +508,7 @@ extern "C" int astro_update_external_rhs(astro_ctx *ctx, double *ext_vec, const 
     double *dRef = dptr<double>(ctx->d_ioRef), *dInt = dptr<double>(ctx->d_ioInt);
     cudaError_t e = cudaMemcpyAsync(dRef, ext_vec, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && !(rc = ref_to_int_vec(ctx, dRef, dInt, n)) &&
-        !(rc = shell4_update_external_rhs(ctx, dptr<double>(iv), dInt)) && !(rc = int_to_ref_vec(ctx, dInt, dRef, n))) {
+        !(rc = elem_update_external_rhs(ctx, dptr<double>(iv), dInt)) && !(rc = int_to_ref_vec(ctx, dInt, dRef, n))) {
         e = cudaMemcpyAsync(ext_vec, dRef, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     }
@@ -467,12 +517,12 @@ extern "C" int astro_update_external_rhs(astro_ctx *ctx, double *ext_vec, const 
     return cuda_check(ctx, e, "update_external_rhs");
 }
 
-// updateInternalSoln (:609-651), loop bound resolved likewise: for every shell element
+// updateInternalSoln (:609-651), loop bound resolved likewise: for every element with internal DOF
 // int_soln += K_ii^-1 (int_rhs - K_in ext_soln); int_rhs may be NULL (zeros).
 extern "C" int astro_update_internal_soln(astro_ctx *ctx, const double *ext_soln, double *int_soln,
                                           const double *int_rhs) {
     if (!ctx || !ext_soln || !int_soln) return ASTRO_ERR_ARG;
-    if (!ctx->hasShell || !ctx->P.intVecSize) return ASTRO_OK;
+    if (!ctx->P.intVecSize) return ASTRO_OK;
     if (!ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
     const int n = ctx->P.n, ni = ctx->P.intVecSize;
     int rc;
@@ -486,7 +536,7 @@ extern "C" int astro_update_internal_soln(astro_ctx *ctx, const double *ext_soln
     double *dRef = dptr<double>(ctx->d_ioRef), *dInt = dptr<double>(ctx->d_ioInt);
     cudaError_t e = cudaMemcpyAsync(dRef, ext_soln, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && !(rc = ref_to_int_vec(ctx, dRef, dInt, n)) &&
-        !(rc = shell4_update_internal_soln(ctx, dInt, dptr<double>(is), ir.p ? dptr<double>(ir) : nullptr))) {
+        !(rc = elem_update_internal_soln(ctx, dInt, dptr<double>(is), ir.p ? dptr<double>(ir) : nullptr))) {
         e = cudaMemcpyAsync(int_soln, is.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     }
@@ -502,7 +552,6 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
     if (!ctx || !o || !disp || !vel || !acc || o->num_steps < 0 || !(o->del_t > 0.0) || !(o->nm_beta > 0.0) ||
         (load_pattern && !load_amplitude))
         return ASTRO_ERR_ARG;
-    if (!ctx->hasShell) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark stepping is implemented for shell4 meshes");
     const AstroPrep &P = ctx->P;
     const int n = P.n, ni = P.intVecSize;
     int rc;
@@ -531,7 +580,7 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
         return rc;
     // K_eff = K + c1 c2 M at the initial state (getElasticSolnLoad(1) with the dynamic flag), then
     // scaleElasticMPC
-    ShellDevState ds;
+    ElemDevState ds;
     ds.disp = dptr<double>(B.u);
     ds.pdisp = dptr<double>(B.up);
     ds.pvel = dptr<double>(B.vp);
@@ -543,11 +592,10 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
     ds.gamma = o->nm_gamma;
     ds.delT = o->del_t;
     if ((rc = ensure_K(ctx, 2))) return rc;
-    if ((rc = bsr_zero(ctx, 2))) return rc;
-    if ((rc = launch_shell4_assemble(ctx, ds, nullptr, nullptr, 1, nullptr, nullptr))) return rc;
+    if ((rc = elem_soln_load_dev(ctx, ds, nullptr, nullptr, 1, true))) return rc;
     ctx->haveK64 = 1;
     ctx->k64Version++;
-    ctx->haveIntMat = 1;
+    ctx->haveIntMat = ni > 0;
     ctx->haveLT = 0;
     ctx->ltFactored = 0;
     if ((rc = astro_scale_mpc(ctx, nullptr, nullptr))) return rc;
@@ -575,7 +623,8 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
 
 extern "C" int astro_assemble_fp32(astro_ctx *ctx) {
     if (!ctx) return ASTRO_ERR_ARG;
-    if (!ctx->hasSolid) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 assembly is implemented for brick8 meshes");
+    if (!ctx->hasSolid || ctx->has81)
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 assembly is implemented for brick8 meshes");
     int rc;
     if ((rc = ensure_K(ctx, 1))) return rc;
     // every block is written first by its first-touching element: no zeroing pass
@@ -644,21 +693,18 @@ __global__ void k_scale_neg(int n, const double *x, double s, double *y) {
 // Device state of a complex-step evaluation, uploaded once for any number of design variables.
 struct DrddState {
     DevState S;
-    ShellDevState ds;
+    ElemDevState ds;
 };
 static int drdd_state(astro_ctx *ctx, const astro_state *state, DrddState &D) {
     int rc;
     if (!state) return ASTRO_OK;
     if ((rc = state_vec_up(ctx, state->node_disp, D.S.disp))) return rc;
-    if (ctx->hasShell) {
+    if (ctx->hasShell || state->dynamic) {
         if ((rc = state_vec_up(ctx, state->prev_disp, D.S.pdisp))) return rc;
         if ((rc = state_vec_up(ctx, state->prev_vel, D.S.pvel))) return rc;
         if ((rc = state_vec_up(ctx, state->prev_acc, D.S.pacc))) return rc;
     }
-    if (state->dynamic && ctx->hasSolid)
-        return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark inertia terms are implemented for shell4 meshes");
-    if (ctx->hasShell && (rc = shell_state(ctx, state, D.S, D.ds))) return rc;
-    return ASTRO_OK;
+    return elem_state(ctx, state, D.S, D.ds);
 }
 
 // dRu/dd of design variable dvar into d_acc (n, internal layout) and d_iacc (internal DOF, may be
@@ -669,7 +715,7 @@ static int drdd_device(astro_ctx *ctx, int dvar, double h, DrddState &D, double 
     CK(cudaMemsetAsync(d_acc, 0, sizeof(double) * n, ctx->stream));
     if (ni > 0 && d_iacc) CK(cudaMemsetAsync(d_iacc, 0, sizeof(double) * ni, ctx->stream));
     if (ctx->hasSolid) {
-        rc = hex8_drdd(ctx, dvar, h, D.S.disp.p ? dptr<double>(D.S.disp) : nullptr, d_acc);
+        rc = hex8_drdd(ctx, dvar, h, D.ds, d_acc, ni > 0 ? d_iacc : nullptr);
     } else {
         rc = shell4_drdd(ctx, dvar, h, D.ds, d_acc, ni > 0 ? d_iacc : nullptr);
     }
@@ -722,7 +768,7 @@ extern "C" int astro_drdd_complex_condensed(astro_ctx *ctx, int32_t num, const i
     if (!(h > 0.0)) return set_err(ctx, ASTRO_ERR_ARG, "complex step h must be positive");
     const AstroPrep &P = ctx->P;
     const int n = P.n, ni = P.intVecSize;
-    const bool condense = ctx->hasShell && ni > 0;
+    const bool condense = ni > 0;
     if (condense && !ctx->haveIntMat)
         return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
     if (num == 0) return ASTRO_OK;
@@ -744,7 +790,7 @@ extern "C" int astro_drdd_complex_condensed(astro_ctx *ctx, int32_t num, const i
     for (int k = 0; k < num; ++k) {
         if ((rc = drdd_device(ctx, dvars[k], h, D, dptr<double>(T.acc), ni > 0 ? dptr<double>(T.iacc) : nullptr)))
             return rc;
-        if (condense && (rc = shell4_update_external_rhs(ctx, dptr<double>(T.iacc), dptr<double>(T.acc)))) return rc;
+        if (condense && (rc = elem_update_external_rhs(ctx, dptr<double>(T.iacc), dptr<double>(T.acc)))) return rc;
         if ((rc = int_to_ref_vec(ctx, dptr<double>(T.acc), dptr<double>(T.out) + (size_t)k * n, n))) return rc;
     }
     CK(cudaMemcpyAsync(drudd, T.out.p, sizeof(double) * (size_t)n * num, cudaMemcpyDeviceToHost, ctx->stream));
@@ -794,17 +840,26 @@ extern "C" int astro_element_matrices(astro_ctx *ctx, int32_t precision, const a
     DevState S;
     if (state && state->node_disp && (rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
     if (ctx->hasSolid) {
+        if (state && (state->dynamic || ctx->has81)) {
+            if ((state->dynamic && ((rc = state_vec_up(ctx, state->prev_disp, S.pdisp)) ||
+                                    (rc = state_vec_up(ctx, state->prev_vel, S.pvel)) ||
+                                    (rc = state_vec_up(ctx, state->prev_acc, S.pacc)))))
+                return rc;
+        }
+        ElemDevState ds;
+        if ((rc = elem_state(ctx, state, S, ds))) return rc;
         if (precision == 32) {
-            if (S.disp.p) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 element kernel evaluates the zero state only");
+            if (S.disp.p || ds.dynamic || ctx->has81)
+                return set_err(ctx, ASTRO_ERR_UNSUPPORTED,
+                               "the FP32 element kernel evaluates brick8 elements at the zero state only");
             rc = launch_hex8_element_mats(ctx, 32, dptr<double>(dk));
         } else {
-            rc = hex8_element_mats_state(ctx, S.disp.p ? dptr<double>(S.disp) : nullptr, dptr<double>(dk),
-                                         dr.p ? dptr<double>(dr) : nullptr);
+            rc = solid_soln_load(ctx, 1, ds, nullptr, nullptr, dptr<double>(dk), dr.p ? dptr<double>(dr) : nullptr);
         }
     } else {
         if (precision == 32) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "FP32 shell kernel not provided");
-        ShellDevState ds;
-        if ((rc = shell_state(ctx, state, S, ds))) return rc;
+        ElemDevState ds;
+        if ((rc = elem_state(ctx, state, S, ds))) return rc;
         rc = launch_shell4_assemble(ctx, ds, nullptr, nullptr, 1, dptr<double>(dk), dr.p ? dptr<double>(dr) : nullptr);
     }
     if (rc) return rc;
@@ -1121,7 +1176,7 @@ extern "C" int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double
     if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "needs the FP64 stiffness of astro_el_soln_load(build_mat = 1)");
     if (!ctx->mpcScaled && ctx->P.mpcDim > 0) return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run before the adjoint");
     const int n = ctx->P.n, ni = ctx->P.intVecSize, nd = ctx->numDvars;
-    const bool hasInt = ctx->hasShell && ni > 0;
+    const bool hasInt = ni > 0;
     if (hasInt && !ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load(build_mat = 1)");
     struct Tmp {
         DevBuf b, x, il, ir, acc, iacc, part, ref;
@@ -1139,14 +1194,14 @@ extern "C" int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double
         CK(cudaMemsetAsync(T.il.p, 0, sizeof(double) * ni, ctx->stream));
         if (int_dldu) {
             if ((rc = upload(ctx, T.ir, int_dldu, sizeof(double) * ni))) return rc;
-            if ((rc = shell4_update_external_rhs(ctx, dptr<double>(T.ir), dptr<double>(T.b)))) return rc;
+            if ((rc = elem_update_external_rhs(ctx, dptr<double>(T.ir), dptr<double>(T.b)))) return rc;
         }
     }
     astro_solve_stats st{};
     rc = krylov_solve_static(ctx, dptr<double>(T.b), dptr<double>(T.x), opts, &st);
     if (stats) *stats = st;
     if (rc) return rc;
-    if (hasInt && (rc = shell4_update_internal_soln(ctx, dptr<double>(T.x), dptr<double>(T.il),
+    if (hasInt && (rc = elem_update_internal_soln(ctx, dptr<double>(T.x), dptr<double>(T.il),
                                                     T.ir.p ? dptr<double>(T.ir) : nullptr)))
         return rc;
     // dLdD = explicit part - lambda . dRudD for every design variable
@@ -1209,7 +1264,7 @@ extern "C" int astro_step_solve(astro_ctx *ctx, const astro_step_opts *o, const 
         return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run before the step");
     const AstroPrep &P = ctx->P;
     const int n = P.n, ni = P.intVecSize;
-    const bool hasInt = ctx->hasShell && ni > 0;
+    const bool hasInt = ni > 0;
     if (hasInt && !ctx->haveIntMat) return set_err(ctx, ASTRO_ERR_STATE, "needs the internal rows of astro_el_soln_load");
     const int maxNLIt = o->nl_geom ? 20 : 1;
     const double tol = (double)1e-12f;
@@ -1246,25 +1301,25 @@ extern "C" int astro_step_solve(astro_ctx *ctx, const astro_step_opts *o, const 
         const int build = o->nl_geom ? 1 : 0;
         if (build) {
             if ((rc = ensure_K(ctx, 2))) return rc;
-            if ((rc = bsr_zero(ctx, 2))) return rc;
+            if (ctx->hasShell && (rc = bsr_zero(ctx, 2))) return rc;
         }
-        if (ctx->hasSolid) {
-            rc = hex8_soln_load(ctx, build, dptr<double>(T.u), dptr<double>(T.load));
-        } else {
-            ShellDevState ds;
-            ds.disp = dptr<double>(T.u);
-            ds.idisp = hasInt ? dptr<double>(T.iu) : nullptr;
+        ElemDevState ds;
+        ds.disp = dptr<double>(T.u);
+        ds.idisp = hasInt ? dptr<double>(T.iu) : nullptr;
+        if (ctx->hasSolid)
+            rc = solid_soln_load(ctx, build, ds, dptr<double>(T.load), hasInt ? dptr<double>(T.iload) : nullptr, nullptr,
+                                 nullptr);
+        else
             rc = launch_shell4_assemble(ctx, ds, dptr<double>(T.load), hasInt ? dptr<double>(T.iload) : nullptr, build,
                                         nullptr, nullptr);
-        }
         if (rc) return rc;
         if (build) {
             ctx->k64Version++;
-            ctx->haveIntMat = ctx->hasShell;
+            ctx->haveIntMat = hasInt;
         }
         if (T.f.p) k_axpy_d<<<g, 256, 0, ctx->stream>>>(n, 1.0, dptr<double>(T.f), dptr<double>(T.load));
         if ((rc = constraint_load_dev(ctx, dptr<double>(T.u), dptr<double>(T.load)))) return rc;
-        if (hasInt && (rc = shell4_update_external_rhs(ctx, dptr<double>(T.iload), dptr<double>(T.load)))) return rc;
+        if (hasInt && (rc = elem_update_external_rhs(ctx, dptr<double>(T.iload), dptr<double>(T.load)))) return rc;
         astro_solve_stats s{};
         rc = krylov_solve_static(ctx, dptr<double>(T.load), dptr<double>(T.du), &o->solve, &s);
         acc.iterations += s.iterations;
@@ -1277,7 +1332,7 @@ extern "C" int astro_step_solve(astro_ctx *ctx, const astro_step_opts *o, const 
         acc.residual_kind = s.residual_kind;
         if (rc && rc != ASTRO_ERR_MAXIT) return rc;
         if (rc == ASTRO_ERR_MAXIT) acc.status = rc;
-        if (hasInt && (rc = shell4_update_internal_soln(ctx, dptr<double>(T.du), dptr<double>(T.iu), dptr<double>(T.iload))))
+        if (hasInt && (rc = elem_update_internal_soln(ctx, dptr<double>(T.du), dptr<double>(T.iu), dptr<double>(T.iload))))
             return rc;
         k_axpy_d<<<g, 256, 0, ctx->stream>>>(n, 1.0, dptr<double>(T.du), dptr<double>(T.u));
         k_absmax_part<<<152, 256, 0, ctx->stream>>>(dptr<double>(T.du), n, dptr<double>(T.part));

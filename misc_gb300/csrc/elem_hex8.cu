@@ -493,7 +493,10 @@ template <bool ROT> __global__ void __launch_bounds__(32 * kDfW, 4) hex8_df_kern
 // the global displacement along the local axes) and Bloc(g) the 6x3 small-strain operator of the
 // shape gradient g, the nonlinear strain-displacement block of node a is P_a = Bloc(g_a) G (6x3),
 // and with Q_b = w detJ C P_b, S the stress tensor and t_b = w detJ S g_b:
-//   K_ab = sum_gp ( P_a^T Q_b + (g_a . t_b) I3 ),   Ru_a = sum_gp w detJ P_a^T stress.
+//   K_ab = sum_gp ( P_a^T Q_b + (g_a . t_b) I3 ),   Ru_a = sum_gp w detJ P_a^T stress,
+// plus, for a Newmark state, the consistent mass c1 c2 rho w detJ N_a N_b I3 in K and the
+// inertia rho w detJ N_a (sum_b N_b acc_b) in Ru (the fourth components of g and t carry N_a and
+// c1 c2 rho w detJ N_b, so the pair loop adds the mass with the stress term).
 // Phase 1, lane (gp, s) = (lane / 4, lane % 4) handles nodes 2s and 2s+1 at point gp: the
 // Jacobian and displacement gradient are reduced over the four lanes of the point, then the lane
 // writes P, Q, g and t of its two nodes to shared memory (double-float) and keeps their residual.
@@ -514,6 +517,11 @@ struct Hex8GenArgs {
     const float2 *CdfItem; // (count,9) C per listed element (indexed by list position) or null
     const double *orient;  // (E,9) column-major section orientation (ROT)
     const double *disp;    // internal-layout displacement (3 per node, rank-major) or null
+    // Newmark inertia (r_getElRum solid branch, Working/AStrO_r_elementEqns.f90:2628-2653): the
+    // previous displacement, velocity and acceleration, density per element; dyn = 0 without it
+    const double *pdisp, *pvel, *pacc, *rho;
+    int dyn;
+    double beta, delT;
     double *K;             // BSR values or null
     double *loadInt;       // internal-layout load, -= Ru (or null)
     double *keOut;         // element matrices (E,24,24) column-major, element DOF order, or null
@@ -575,7 +583,7 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
     {
         const DF G{A.gpcHi, A.gpcLo};
         const DF s1 = (gp & 1) ? G : df_neg(G), s2 = (gp & 2) ? G : df_neg(G), s3 = (gp & 4) ? G : df_neg(G);
-        DF J[9], n[2][3], U[2][3];
+        DF J[9], n[2][3], U[2][3], Nv[2], Ac[2][3];
 #pragma unroll
         for (int q = 0; q < 9; ++q) J[q] = zero;
 #pragma unroll
@@ -592,18 +600,27 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
             n[k][0] = df_scale2(df_mul(p2, p3), sp ? 0.125f : -0.125f);
             n[k][1] = df_scale2(df_mul(p1, p3), tp ? 0.125f : -0.125f);
             n[k][2] = df_scale2(df_mul(p1, p2), up ? 0.125f : -0.125f);
+            Nv[k] = df_scale2(df_mul(df_mul(p1, p2), p3), 0.125f);
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = 0; j < 3; ++j) J[3 * i + j] = df_fma(X[i], n[k][j], J[3 * i + j]);
-            if (A.disp) {
-                const int nd = A.elist[8 * (size_t)e + a];
-                const int r = A.rank[nd - 1] - 1;
+            const int nd = A.elist[8 * (size_t)e + a];
+            const int r = A.rank[nd - 1] - 1;
 #pragma unroll
-                for (int i = 0; i < 3; ++i) U[k][i] = df_from_double(A.disp[3 * (size_t)r + i]);
-            } else {
-#pragma unroll
-                for (int i = 0; i < 3; ++i) U[k][i] = zero;
+            for (int i = 0; i < 3; ++i) {
+                const size_t ix = 3 * (size_t)r + i;
+                const double u = A.disp ? A.disp[ix] : 0.0;
+                U[k][i] = df_from_double(u);
+                double ac = 0.0;
+                if (A.dyn) {
+                    // accNext of r_getElRu (:2684-2696) in FP64
+                    const double c1 = 0.5 / A.beta, c2 = 2.0 / (A.delT * A.delT);
+                    const double pd = A.pdisp ? A.pdisp[ix] : 0.0, pv = A.pvel ? A.pvel[ix] : 0.0,
+                                 pa = A.pacc ? A.pacc[ix] : 0.0;
+                    ac = c1 * (c2 * (u - pd - A.delT * pv) - (1.0 - 2.0 * A.beta) * pa);
+                }
+                Ac[k][i] = df_from_double(ac);
             }
         }
 #pragma unroll
@@ -683,6 +700,19 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) Gm[i][j] = df_add(Or[i][j], ux[j][i]);
+        // Newmark inertia: acceleration at the point, rho w detJ, and c1 c2 rho w detJ
+        DF ag[3] = {zero, zero, zero}, rw = zero, mw = zero;
+        if (A.dyn) {
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                DF v = df_add(df_mul(Nv[0], Ac[0][i]), df_mul(Nv[1], Ac[1][i]));
+                v = df_add(v, df_shfl_xor(v, 1));
+                ag[i] = df_add(v, df_shfl_xor(v, 2));
+            }
+            const double c1 = 0.5 / A.beta, c2 = 2.0 / (A.delT * A.delT);
+            rw = df_mul(df_from_double(A.rho[e]), dt);
+            mw = df_mul(df_from_double(c1 * c2), rw);
+        }
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             const int a = 2 * s + k;
@@ -697,12 +727,13 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
                 P[4][v] = df_add(df_mul(g2, Gm[0][v]), df_mul(g0, Gm[2][v]));
                 P[5][v] = df_add(df_mul(g2, Gm[1][v]), df_mul(g1, Gm[2][v]));
             }
-            // residual of node a at this point: P^T (w detJ stress)
+            // residual of node a at this point: P^T (w detJ stress), plus the inertia
 #pragma unroll
             for (int v = 0; v < 3; ++v) {
                 DF r = df_mul(P[0][v], sw[0]);
 #pragma unroll
                 for (int q = 1; q < 6; ++q) r = df_fma(P[q][v], sw[q], r);
+                if (A.dyn) r = df_fma(df_mul(rw, Nv[k]), ag[v], r);
                 ru[k][v] = r;
             }
             if (BUILD) {
@@ -733,10 +764,11 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
                 const DF t0 = df_add(df_add(df_mul(sw[0], g0), df_mul(sw[3], g1)), df_mul(sw[4], g2));
                 const DF t1 = df_add(df_add(df_mul(sw[3], g0), df_mul(sw[1], g1)), df_mul(sw[5], g2));
                 const DF t2 = df_add(df_add(df_mul(sw[4], g0), df_mul(sw[5], g1)), df_mul(sw[2], g2));
-                S.u.gh[it] = make_float4(g0.hi, g1.hi, g2.hi, 0.f);
-                S.u.gl[it] = make_float4(g0.lo, g1.lo, g2.lo, 0.f);
-                S.u.th[it] = make_float4(t0.hi, t1.hi, t2.hi, 0.f);
-                S.u.tl[it] = make_float4(t0.lo, t1.lo, t2.lo, 0.f);
+                const DF na = A.dyn ? Nv[k] : zero, mn = A.dyn ? df_mul(mw, Nv[k]) : zero;
+                S.u.gh[it] = make_float4(g0.hi, g1.hi, g2.hi, na.hi);
+                S.u.gl[it] = make_float4(g0.lo, g1.lo, g2.lo, na.lo);
+                S.u.th[it] = make_float4(t0.hi, t1.hi, t2.hi, mn.hi);
+                S.u.tl[it] = make_float4(t0.lo, t1.lo, t2.lo, mn.lo);
             }
         }
     }
@@ -802,6 +834,7 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
         df_acc(geo, gh.x, gl.x, th.x, tl.x);
         df_acc(geo, gh.y, gl.y, th.y, tl.y);
         df_acc(geo, gh.z, gl.z, th.z, tl.z);
+        df_acc(geo, gh.w, gl.w, th.w, tl.w);  // consistent mass (zero without inertia)
     }
     __syncwarp();
     // partials: the first tile to slot 0 when it starts on this lane (u0 % 8 == 0), else slot 1;
@@ -925,11 +958,13 @@ __global__ void k_elem_c(int E, const double *__restrict__ elMat, double *__rest
 
 // Imaginary part of the complex-step material stiffness of each listed element:
 // eProps(c) + coef (d + i h) for the elastic-modulus design variable dvar (the real parts of all
-// design-variable terms are already in elMat), then C = S^-1 in complex arithmetic.
-__global__ void k_hex_cim(int count, const int *__restrict__ els, const double *__restrict__ elMat,
+// design-variable terms are already in elMat), then C = S^-1 in complex arithmetic.  The first n8
+// listed elements (brick8) get the orthotropic entries C11 C12 C13 C22 C23 C33 C44 C55 C66 of
+// Im(C) in double-float, the rest (brickIM) in FP64.
+__global__ void k_hex_cim(int count, int n8, const int *__restrict__ els, const double *__restrict__ elMat,
                           const int *__restrict__ e2dR, const int *__restrict__ e2d, const double *__restrict__ e2c,
                           const int *__restrict__ dcat, const int *__restrict__ dcomp, int dvar, double h,
-                          float2 *__restrict__ Cim) {
+                          float2 *__restrict__ Cim8, double *__restrict__ Cim81) {
     const int item = blockIdx.x * blockDim.x + threadIdx.x;
     if (item >= count) return;
     const int e = els[item];
@@ -941,32 +976,35 @@ __global__ void k_hex_cim(int count, const int *__restrict__ els, const double *
     }
     cplx C[6][6];
     material_c<cplx>(ep, C);
-    // the orthotropic entries C11 C12 C13 C22 C23 C33 C44 C55 C66 of Im(C), in double-float
     const double v[9] = {C[0][0].im, C[0][1].im, C[0][2].im, C[1][1].im, C[1][2].im,
                          C[2][2].im, C[3][3].im, C[4][4].im, C[5][5].im};
     for (int q = 0; q < 9; ++q) {
-        const DF d = df_from_double(v[q]);
-        Cim[9 * (size_t)item + q] = make_float2(d.hi, d.lo);
+        if (item < n8) {
+            const DF d = df_from_double(v[q]);
+            Cim8[9 * (size_t)item + q] = make_float2(d.hi, d.lo);
+        } else {
+            Cim81[9 * (size_t)(item - n8) + q] = v[q];
+        }
     }
 }
 
 }  // namespace
 
 template <class T, bool ROT> static void hex8_fast_launch(astro_ctx *ctx, const Hex8FastArgs<T> &A0) {
-    const AstroPrep &P = ctx->P;
     constexpr int FW = FastCfg<T>::FW;
     Hex8FastArgs<T> A = A0;
-    for (int col = 0; col < P.ncolors; ++col) {
-        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+    const std::vector<int> &ptr = ctx->c8Ptr;
+    for (size_t col = 0; col + 1 < ptr.size(); ++col) {
+        const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
-        A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+        A.colorEls = dptr<int>(ctx->d_c8Els) + ptr[col];
         A.count = cnt;
         hex8_fast_kernel<T, ROT><<<(cnt + FW - 1) / FW, 32 * FW, 0, ctx->stream>>>(A);
     }
 }
 
-// Zero-state stiffness of every element, colour by colour, into K (block-CSR, written without a
-// prior zeroing) and/or the element matrices d_ke.
+// Zero-state stiffness of every brick8 element, colour by colour, into K (block-CSR, written
+// without a prior zeroing) and/or the element matrices d_ke.
 template <class T> static int hex8_fast_run(astro_ctx *ctx, T *K, double *d_ke) {
     Hex8FastArgs<T> A;
     A.colorEls = nullptr;
@@ -985,13 +1023,13 @@ template <class T> static int hex8_fast_run(astro_ctx *ctx, T *K, double *d_ke) 
     return cuda_check(ctx, cudaGetLastError(), "brick8 zero-state kernel launch");
 }
 
-// General-state element kernel (double-float), colour by colour over the elements of list
-// (colour c covering list[ptr[c] .. ptr[c+1])): the block-CSR matrix (with BUILD), the residual
-// into d_loadInt (load -= Ru), element matrices and residuals.  CdfItem: per listed element its C
-// (double-float, the complex step's imaginary part) instead of the element's own; gpc the Gauss
-// point coordinate.
+// General-state element kernel (double-float), colour by colour over the brick8 elements of list
+// (colour c covering list[ptr[c] .. ptr[c+1])): the block-CSR matrix (with build), the residual
+// into d_loadInt (load -= Ru), element matrices and residuals, at state s (with the Newmark
+// inertia when s.dynamic).  CdfItem: per listed element its C (double-float, the complex step's
+// imaginary part) instead of the element's own; gpc the Gauss point coordinate.
 static int hex8_gen_run(astro_ctx *ctx, const int *d_list, const std::vector<int> &ptr, bool build, double *K,
-                        const double *d_disp, double *d_loadInt, double *d_ke, double *d_ru, const float2 *CdfItem,
+                        const ElemDevState &s, double *d_loadInt, double *d_ke, double *d_ru, const float2 *CdfItem,
                         double gpc) {
     Hex8GenArgs A;
     A.elBlk = dptr<int>(ctx->d_elBlk);
@@ -1001,7 +1039,14 @@ static int hex8_gen_run(astro_ctx *ctx, const int *d_list, const std::vector<int
     A.Xdf = dptr<float2>(ctx->d_elXdf);
     A.Cdf = dptr<float2>(ctx->d_elCdf);
     A.orient = dptr<double>(ctx->d_secOrient);
-    A.disp = d_disp;
+    A.disp = s.disp;
+    A.pdisp = s.pdisp;
+    A.pvel = s.pvel;
+    A.pacc = s.pacc;
+    A.rho = dptr<double>(ctx->d_elRho);
+    A.dyn = s.dynamic ? 1 : 0;
+    A.beta = s.beta;
+    A.delT = s.delT;
     A.K = K;
     A.loadInt = d_loadInt;
     A.keOut = d_ke;
@@ -1032,16 +1077,9 @@ static int hex8_gen_run(astro_ctx *ctx, const int *d_list, const std::vector<int
     return cuda_check(ctx, cudaGetLastError(), "brick8 general-state kernel launch");
 }
 
-// every element of the context, colour by colour
-static int hex8_run(astro_ctx *ctx, bool build, double *K, const double *d_disp, double *d_loadInt, double *d_ke,
-                    double *d_ru) {
-    return hex8_gen_run(ctx, dptr<int>(ctx->d_colorEls), ctx->P.colorPtr, build || d_ke, K, d_disp, d_loadInt, d_ke,
-                        d_ru, nullptr, kRt3);
-}
-
-// FP64 zero-state stiffness (double-float kernel), colour by colour.
-static int hex8_df_run(astro_ctx *ctx, double *K, double *d_ke) {
-    const AstroPrep &P = ctx->P;
+// FP64 zero-state stiffness of brick8 elements (double-float kernel), colour by colour over list
+// (colour c covering list[ptr[c] .. ptr[c+1])).
+static int hex8_df_run(astro_ctx *ctx, double *K, double *d_ke, const int *d_list, const std::vector<int> &ptr) {
     Hex8DfArgs A;
     A.elBlk = dptr<int>(ctx->d_elBlk);
     A.elFirst = dptr<unsigned long long>(ctx->d_elFirst);
@@ -1050,10 +1088,10 @@ static int hex8_df_run(astro_ctx *ctx, double *K, double *d_ke) {
     A.orient = dptr<double>(ctx->d_secOrient);
     A.K = K;
     A.keOut = d_ke;
-    for (int col = 0; col < P.ncolors; ++col) {
-        const int cnt = P.colorPtr[col + 1] - P.colorPtr[col];
+    for (size_t col = 0; col + 1 < ptr.size(); ++col) {
+        const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
-        A.colorEls = dptr<int>(ctx->d_colorEls) + P.colorPtr[col];
+        A.colorEls = d_list + ptr[col];
         A.count = cnt;
         const unsigned grid = (cnt + kDfW - 1) / kDfW;
         if (ctx->orientIdentity)
@@ -1090,34 +1128,69 @@ int hex8_prepare(astro_ctx *ctx) {
 
 int launch_hex8_assemble(astro_ctx *ctx, int precision, int store) {
     if (precision == 32) return hex8_fast_run<float>(ctx, (store & 1) ? dptr<float>(ctx->d_K32) : nullptr, nullptr);
-    return hex8_df_run(ctx, (store & 2) ? dptr<double>(ctx->d_K64) : nullptr, nullptr);
+    return hex8_df_run(ctx, (store & 2) ? dptr<double>(ctx->d_K64) : nullptr, nullptr, dptr<int>(ctx->d_c8Els),
+                       ctx->c8Ptr);
 }
 
-// getElasticSolnLoad for bricks.  From the undeformed state (no displacement) the residual is
-// zero and the tangent is the small-strain stiffness, which the zero-state kernel writes into the
-// block-CSR matrix without a prior zeroing; any other state takes the general kernel (Green-
-// Lagrange strain, stress stiffness, residual), which adds into a zeroed matrix.
-int hex8_soln_load(astro_ctx *ctx, int buildMat, const double *d_disp, double *d_loadInt) {
-    if (!d_disp) return buildMat ? hex8_df_run(ctx, dptr<double>(ctx->d_K64), nullptr) : ASTRO_OK;
-    return hex8_run(ctx, buildMat != 0, buildMat ? dptr<double>(ctx->d_K64) : nullptr, d_disp, d_loadInt, nullptr,
-                    nullptr);
+// getElasticSolnLoad for solid meshes.  brick8: from the undeformed state without inertia the
+// residual is zero and the tangent is the small-strain stiffness (the zero-state double-float
+// kernel); any other state takes the general kernel.  brickIM: the FP64 brickIM kernel, which also
+// writes the condensed internal rows and the internal load.  Both write each block of the
+// block-CSR matrix first (colour order), so no zeroing pass is needed.
+int solid_soln_load(astro_ctx *ctx, int build, const ElemDevState &s, double *d_loadInt, double *d_intLoad,
+                    double *d_ke, double *d_ru) {
+    const bool toK = build && !d_ke, mat = build || d_ke;
+    double *K = toK ? dptr<double>(ctx->d_K64) : nullptr;
+    const bool zero8 = !s.disp && !s.dynamic && !d_ru;  // brick8 residual is zero: zero-state kernel
+    // one pass over the colours with the given brick8 and brickIM colour lists
+    auto pass = [&](const std::vector<int> &p8, const std::vector<int> &p81) -> int {
+        int rc;
+        if (p8.back() > p8.front()) {
+            if (zero8) {
+                if (mat && (rc = hex8_df_run(ctx, K, d_ke, dptr<int>(ctx->d_c8Els), p8))) return rc;
+            } else if ((rc = hex8_gen_run(ctx, dptr<int>(ctx->d_c8Els), p8, mat, K, s, d_loadInt, d_ke, d_ru, nullptr,
+                                          kRt3))) {
+                return rc;
+            }
+        }
+        if (p81.back() > p81.front() &&
+            (rc = hex81_run(ctx, dptr<int>(ctx->d_c81Els), p81, mat ? 1 : 0, K, s, nullptr, kRt3, d_loadInt, d_intLoad,
+                            toK ? dptr<double>(ctx->d_intMat) : nullptr, d_ke, d_ru)))
+            return rc;
+        return ASTRO_OK;
+    };
+    if (!ctx->has81 || ctx->c8Els.empty()) return pass(ctx->c8Ptr, ctx->c81Ptr);
+    // both types: colour by colour, so that the first element (in colour order) to touch a
+    // block of the matrix is the one that writes it
+    for (size_t col = 0; col + 1 < ctx->c8Ptr.size(); ++col) {
+        const std::vector<int> p8 = {ctx->c8Ptr[col], ctx->c8Ptr[col + 1]}, p81 = {ctx->c81Ptr[col], ctx->c81Ptr[col + 1]};
+        const int rc = pass(p8, p81);
+        if (rc) return rc;
+    }
+    return ASTRO_OK;
 }
 
 int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
     if (precision == 32) return hex8_fast_run<float>(ctx, nullptr, d_ke);
-    return hex8_df_run(ctx, nullptr, d_ke);
+    ElemDevState s;
+    return solid_soln_load(ctx, 1, s, nullptr, nullptr, d_ke, nullptr);
 }
 
-int hex8_element_mats_state(astro_ctx *ctx, const double *d_disp, double *d_ke, double *d_ru) {
-    if (!d_disp && !d_ru) return hex8_df_run(ctx, nullptr, d_ke);
-    return hex8_run(ctx, d_ke != nullptr, nullptr, d_disp, nullptr, d_ke, d_ru);
-}
-
-int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *d_acc) {
+// Complex step of the solid residual for design variable dvar: d_acc -= Im(Ru(d + i h)) of the
+// elements that depend on it (internal DOF of brickIM elements into d_intAcc).  The residual is
+// linear in C: its imaginary part is the residual evaluated with Im(C), at the complex path's
+// Gauss points.
+int hex8_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc, double *d_intAcc) {
     std::vector<int> list, ptr;
     dvar_elements_by_colour(ctx, dvar, list, ptr);
-    const int cnt = (int)list.size();
-    if (!cnt) return ASTRO_OK;
+    if (list.empty()) return ASTRO_OK;
+    // split by element type, colour by colour
+    std::vector<int> l8, p8(1, 0), l81, p81(1, 0);
+    for (size_t col = 0; col + 1 < ptr.size(); ++col) {
+        for (int k = ptr[col]; k < ptr[col + 1]; ++k) (ctx->etype[list[k]] == 81 ? l81 : l8).push_back(list[k]);
+        p8.push_back((int)l8.size());
+        p81.push_back((int)l81.size());
+    }
     DevBuf dl, dC, dR, dE, dEC, dCat, dComp;
     struct Free {
         DevBuf *b[7];
@@ -1126,21 +1199,28 @@ int hex8_drdd(astro_ctx *ctx, int dvar, double h, const double *d_disp, double *
         }
     } fr{{&dl, &dC, &dR, &dE, &dEC, &dCat, &dComp}};
     int rc;
-    if ((rc = upload(ctx, dl, list.data(), sizeof(int) * cnt))) return rc;
-    if ((rc = dev_alloc(ctx, dC, sizeof(float2) * 9 * (size_t)cnt))) return rc;
+    const int n8 = (int)l8.size(), n81 = (int)l81.size();
+    std::vector<int> all(l8);
+    all.insert(all.end(), l81.begin(), l81.end());
+    if ((rc = upload(ctx, dl, all.data(), sizeof(int) * all.size()))) return rc;
+    // Im(C) per listed element: double-float for the brick8 kernel, FP64 for the brickIM one
+    if ((rc = dev_alloc(ctx, dC, sizeof(float2) * 9 * (size_t)n8 + sizeof(double) * 9 * (size_t)n81))) return rc;
     if ((rc = upload(ctx, dR, ctx->e2dRange.data(), sizeof(int) * ctx->e2dRange.size()))) return rc;
     if ((rc = upload(ctx, dE, ctx->e2d.data(), sizeof(int) * ctx->e2d.size()))) return rc;
     if ((rc = upload(ctx, dEC, ctx->e2c.data(), sizeof(double) * ctx->e2c.size()))) return rc;
     if ((rc = upload(ctx, dCat, ctx->dCat.data(), sizeof(int) * ctx->dCat.size()))) return rc;
     if ((rc = upload(ctx, dComp, ctx->dComp.data(), sizeof(int) * ctx->dComp.size()))) return rc;
-    k_hex_cim<<<(cnt + 127) / 128, 128, 0, ctx->stream>>>(cnt, dptr<int>(dl), dptr<double>(ctx->d_elMat), dptr<int>(dR),
-                                                          dptr<int>(dE), dptr<double>(dEC), dptr<int>(dCat),
-                                                          dptr<int>(dComp), dvar, h, dptr<float2>(dC));
-    // the residual is linear in C: its imaginary part is the residual evaluated with Im(C), at the
-    // complex path's Gauss points
-    if ((rc = hex8_gen_run(ctx, dptr<int>(dl), ptr, false, nullptr, d_disp, d_acc, nullptr, nullptr, dptr<float2>(dC),
-                           kRt3c)))
+    float2 *c8 = dptr<float2>(dC);
+    double *c81 = reinterpret_cast<double *>(c8 + 9 * (size_t)n8);
+    const int tot = n8 + n81;
+    k_hex_cim<<<(tot + 127) / 128, 128, 0, ctx->stream>>>(tot, n8, dptr<int>(dl), dptr<double>(ctx->d_elMat),
+                                                          dptr<int>(dR), dptr<int>(dE), dptr<double>(dEC),
+                                                          dptr<int>(dCat), dptr<int>(dComp), dvar, h, c8, c81);
+    if (n8 && (rc = hex8_gen_run(ctx, dptr<int>(dl), p8, false, nullptr, s, d_acc, nullptr, nullptr, c8, kRt3c)))
+        return rc;
+    if (n81 && (rc = hex81_run(ctx, dptr<int>(dl) + n8, p81, 0, nullptr, s, c81, kRt3c, d_acc, d_intAcc, nullptr,
+                               nullptr, nullptr)))
         return rc;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    return cuda_check(ctx, e, "brick8 complex-step kernels");
+    return cuda_check(ctx, e, "solid complex-step kernels");
 }

@@ -90,7 +90,7 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
 
 // The five pipeline kernels over the elements of each colour in turn: colour c covers
 // els[ptr[c] .. ptr[c+1]) (device list).
-static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
+static int shell_pipeline(astro_ctx *ctx, const ElemDevState &st, const int *d_els, const std::vector<int> &ptr,
                           const ShellProps *props, double gpc, double *d_loadInt, double *d_intLoad, int buildMat,
                           double *d_K, double *d_intMat, double *d_ke, double *d_ru, bool sync = true) {
     int maxc = 0;
@@ -167,13 +167,13 @@ static int shell_pipeline(astro_ctx *ctx, const ShellDevState &st, const int *d_
 
 // The pipeline over a colour-grouped element list (device list d_els, colour c covering
 // ptr[c] .. ptr[c+1]), residual only, into d_loadInt (load -= Ru).
-int shell4_residual_list(astro_ctx *ctx, const ShellDevState &st, const int *d_els, const std::vector<int> &ptr,
+int shell4_residual_list(astro_ctx *ctx, const ElemDevState &st, const int *d_els, const std::vector<int> &ptr,
                          double *d_loadInt) {
     return shell_pipeline(ctx, st, d_els, ptr, dptr<ShellProps>(ctx->d_secABD), kShellRt3, d_loadInt, nullptr, 0,
                           nullptr, nullptr, nullptr, nullptr);
 }
 
-int launch_shell4_assemble(astro_ctx *ctx, const ShellDevState &st, double *d_loadInt, double *d_intLoad, int buildMat,
+int launch_shell4_assemble(astro_ctx *ctx, const ElemDevState &st, double *d_loadInt, double *d_intLoad, int buildMat,
                            double *d_ke, double *d_ru, bool sync) {
     const bool toK = buildMat && !d_ke;
     return shell_pipeline(ctx, st, dptr<int>(ctx->d_colorEls), ctx->P.colorPtr, dptr<ShellProps>(ctx->d_secABD), kShellRt3,
@@ -205,7 +205,7 @@ __global__ void k_shell_props_im(int count, const int *els, const double *nodes,
 // Complex step of the pipeline's residual over a colour-grouped element list (colour c covering
 // list[ptr[c] .. ptr[c+1])): d_acc -= Im(Ru(d + i h)) (unscaled).  hook, when given, runs before
 // each colour (with that colour's device list and count) and the colours then launch one by one.
-int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, const std::vector<int> &list,
+int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ElemDevState &st, const std::vector<int> &list,
                      const std::vector<int> &ptr, double *d_acc, double *d_intAcc,
                      const std::function<int(const int *, int)> &hook) {
     const int cnt = (int)list.size();
@@ -247,7 +247,7 @@ int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ShellDevState &st
     return rc;
 }
 
-int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ShellDevState &st, double *d_acc, double *d_intAcc) {
+int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &st, double *d_acc, double *d_intAcc) {
     std::vector<int> list, ptr;
     dvar_elements_by_colour(ctx, dvar, list, ptr);
     return shell4_drdd_list(ctx, dvar, h, st, list, ptr, d_acc, d_intAcc, nullptr);

@@ -1513,12 +1513,12 @@ __global__ void k_newmark_update(int n, double c1, double c2, double dt, double 
 // gMRes), recovers the internal DOF, updates u and the Newmark state.  All vectors are device
 // buffers in internal layout; the displacement of every step can be written to hist (reference
 // numbering).
-int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,
-                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup, double *d_hist,
-                   astro_solve_stats *st) {
+template <int DPN>
+static int krylov_newmark_dpn(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern,
+                              const double *h_amp, double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu,
+                              double *d_iup, double *d_hist, astro_solve_stats *st) {
     const AstroPrep &P = ctx->P;
     const int n = P.n, ni = P.intVecSize;
-    if (P.dpn != 6) return set_err(ctx, ASTRO_ERR_UNSUPPORTED, "Newmark stepping is implemented for shell4 meshes");
     const int m = o->restart > 0 ? std::min(o->restart, kMaxM) : 50;
     const int maxCycles = o->max_iters > 0 ? (o->max_iters + m - 1) / m : 200;
     const double rtol = o->rtol > 0 ? o->rtol : 1e-10;
@@ -1548,7 +1548,7 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
             dptr<double>(ctx->d_penVal), dptr<double>(W.dinv), dptr<double>(W.dinvT));
         rc = cuda_check(ctx, cudaMemsetAsync(du.p, 0, sizeof(double) * n, s), "newmark init");
     }
-    ShellDevState ds;
+    ElemDevState ds;
     ds.disp = d_u;
     ds.pdisp = d_up;
     ds.pvel = d_vp;
@@ -1564,12 +1564,11 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
         CK(cudaMemsetAsync(load.p, 0, sizeof(double) * n, s));
         if (ni) CK(cudaMemsetAsync(iload.p, 0, sizeof(double) * ni, s));
         // getElasticSolnLoad(0): load -= Ru (with the Newmark inertia at the current state)
-        if ((rc = launch_shell4_assemble(ctx, ds, dptr<double>(load), ni ? dptr<double>(iload) : nullptr, 0, nullptr,
-                                         nullptr, false)))
+        if ((rc = elem_soln_load_dev(ctx, ds, dptr<double>(load), ni ? dptr<double>(iload) : nullptr, 0, false)))
             break;
         if (d_pattern && h_amp) k_axpy<<<grid, 256, 0, s>>>(n, h_amp[step], d_pattern, dptr<double>(load));
         if ((rc = constraint_load_dev(ctx, d_u, dptr<double>(load)))) break;
-        if (ni && (rc = shell4_update_external_rhs(ctx, dptr<double>(iload), dptr<double>(load)))) break;
+        if (ni && (rc = elem_update_external_rhs(ctx, dptr<double>(iload), dptr<double>(load)))) break;
         if (o->method != ASTRO_SOLVER_GMRES_JACOBI_FP64) {
             // the mixed or learned static solver on K_eff (its workspace, FP16 operator and
             // eigenvalue estimate are reused across the steps), warm-started from the last increment
@@ -1597,10 +1596,10 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
             worstRel = std::max(worstRel, s2.rel_residual);
         } else {
             double rel = 0.0, rn = 0.0, bn = 0.0;
-            if ((rc = true_residual<6>(ctx, W, 64, nullptr, dptr<double>(load), &rel, dptr<double>(W.rres), &rn, &bn)))
+            if ((rc = true_residual<DPN>(ctx, W, 64, nullptr, dptr<double>(load), &rel, dptr<double>(W.rres), &rn, &bn)))
                 break;
             double est = 0.0;
-            int grc = gmres_solve<double, double, 6>(ctx, W, K, dptr<double>(du), dptr<double>(load), rtol * bn, maxCycles,
+            int grc = gmres_solve<double, double, DPN>(ctx, W, K, dptr<double>(du), dptr<double>(load), rtol * bn, maxCycles,
                                                      m, &iters, &cycles, &est);
             if (grc == ASTRO_ERR_NAN) {
                 rc = set_err(ctx, ASTRO_ERR_NAN, "non-finite value in the Newmark step solve");
@@ -1609,7 +1608,7 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
             if (grc != ASTRO_OK) worst = grc;
             if (bn > 0.0) worstRel = std::max(worstRel, est / bn);
         }
-        if (ni && (rc = shell4_update_internal_soln(ctx, dptr<double>(du), d_iu, dptr<double>(iload)))) break;
+        if (ni && (rc = elem_update_internal_soln(ctx, dptr<double>(du), d_iu, dptr<double>(iload)))) break;
         k_axpy<<<grid, 256, 0, s>>>(n, 1.0, dptr<double>(du), d_u);
         k_newmark_update<<<grid, 256, 0, s>>>(n, c1, c2, dt, beta, gamma, d_u, d_up, d_vp, d_ap);
         if (ni) CK(cudaMemcpyAsync(d_iup, d_iu, sizeof(double) * ni, cudaMemcpyDeviceToDevice, s));
@@ -1637,4 +1636,12 @@ int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_
         st->residual_kind = 64;
     }
     return rc;
+}
+
+int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,
+                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup, double *d_hist,
+                   astro_solve_stats *st) {
+    if (ctx->P.dpn == 3)
+        return krylov_newmark_dpn<3>(ctx, o, d_pattern, h_amp, d_u, d_up, d_vp, d_ap, d_iu, d_iup, d_hist, st);
+    return krylov_newmark_dpn<6>(ctx, o, d_pattern, h_amp, d_u, d_up, d_vp, d_ap, d_iu, d_iup, d_hist, st);
 }

@@ -297,7 +297,7 @@ extern "C" int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals,
         if ((rc = upload(ctx, T.pa, pa.data(), sizeof(double) * n))) return rc;
         if ((rc = dev_alloc(ctx, T.b, sizeof(double) * n))) return rc;
         CK(cudaMemsetAsync(T.b.p, 0, sizeof(double) * n, ctx->stream));
-        ShellDevState s1;
+        ElemDevState s1;
         s1.disp = dptr<double>(T.u);
         s1.idisp = ni > 0 ? dptr<double>(T.iu) : nullptr;
         s1.pdisp = s1.disp;
@@ -447,7 +447,7 @@ extern "C" int astro_body_load_drdd(astro_ctx *ctx, int32_t dvar, double h, int3
             for (int r = 0; r < P.N; ++r)
                 for (int c = 0; c < P.dpn; ++c) pa[(size_t)r * P.dpn + c] = -vals[c];
         if ((rc = upload(ctx, T.pa, pa.data(), sizeof(double) * n))) return rc;
-        ShellDevState s1;
+        ElemDevState s1;
         s1.disp = dptr<double>(T.u);
         s1.idisp = ni > 0 ? dptr<double>(T.iu) : nullptr;
         s1.pdisp = s1.disp;

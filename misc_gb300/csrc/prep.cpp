@@ -38,11 +38,12 @@ int astro_prep_build(astro_ctx *c, const astro_model *m) {
     int nSolidEl = 0, nShellEl = 0;
     for (int e = 0; e < E; ++e) {
         int t = m->element_type[e];
-        if (t == 8) nSolidEl++;
+        if (t == 8 || t == 81) nSolidEl++;
         else if (t == 41) nShellEl++;
-        else return set_err(c, ASTRO_ERR_UNSUPPORTED, "element type " + std::to_string(t) + " is not supported (8 = brick8, 41 = shell4)");
+        else return set_err(c, ASTRO_ERR_UNSUPPORTED, "element type " + std::to_string(t) +
+                                                          " is not supported (8 = brick8, 81 = brickIM, 41 = shell4)");
     }
-    if (nSolidEl && nShellEl) return set_err(c, ASTRO_ERR_UNSUPPORTED, "meshes mixing brick8 and shell4 elements are not supported");
+    if (nSolidEl && nShellEl) return set_err(c, ASTRO_ERR_UNSUPPORTED, "meshes mixing solid and shell4 elements are not supported");
     c->hasSolid = nSolidEl > 0;
     c->hasShell = nShellEl > 0;
     P.dpn = c->hasShell ? 6 : 3;
@@ -169,13 +170,14 @@ int astro_prep_build(astro_ctx *c, const astro_model *m) {
     }
     P.elMatSize = P.elMatRange[n];
     P.ltSize = P.elMatLTRange[n];
-    // internal DOF ranges (shell4: 8 internal DOF, 8 x 32 condensed rows)
+    // internal DOF ranges (allocateElasticMat, Working/AStrO_bookKeeping.f90:978-1003): shell4 8
+    // internal DOF, 8 x 32 condensed rows; brickIM 9 internal DOF, 9 x 33 rows
     P.intVecRange.assign(E + 1, 0);
     P.intMatRange.assign(E + 1, 0);
     for (int e = 1; e <= E; ++e) {
         int t = m->element_type[e - 1];
-        P.intVecRange[e] = P.intVecRange[e - 1] + (t == 41 ? 8 : 0);
-        P.intMatRange[e] = P.intMatRange[e - 1] + (t == 41 ? 256 : 0);
+        P.intVecRange[e] = P.intVecRange[e - 1] + (t == 41 ? 8 : (t == 81 ? 9 : 0));
+        P.intMatRange[e] = P.intMatRange[e - 1] + (t == 41 ? 256 : (t == 81 ? 297 : 0));
     }
     P.intVecSize = P.intVecRange[E];
     P.intMatSize = P.intMatRange[E];

@@ -219,6 +219,9 @@ OracleCtx *orc_create(const astro_model *m) {
         if (t == 41) {
             c->intVecRange[i1] = 8;
             c->intMatRange[i1] = 256;
+        } else if (t == 81) {  // allocateElasticMat's internal sizes (Working/AStrO_bookKeeping.f90:978-1003)
+            c->intVecRange[i1] = 9;
+            c->intMatRange[i1] = 297;
         } else if (t != 8) {
             delete c;
             return nullptr;
@@ -452,6 +455,7 @@ int orc_element_matrices(const OracleCtx *c, int el0, int el1, const astro_state
         if (t_element(R, K, c->m, c->nDofIndex.data(), c->intVecRange.data(), el, 1, g, p) != 0) return 1;
         int t = c->m->element_type[el - 1];
         if (t == 41) t_condenseMat(K, 25, 32);
+        if (t == 81) t_condenseMat(K, 25, 33);
         double *o = ke_out + (size_t)(el - el0) * 576;
         for (int j = 1; j <= 24; ++j)
             for (int i = 1; i <= 24; ++i) o[(j - 1) * 24 + i - 1] = K(i, j);
@@ -803,8 +807,10 @@ int orc_gmres(double *xVec, const double *Amat, const int32_t *Acols, const int3
 void orc_update_external_rhs(const OracleCtx *c, double *extVec, const double *intVec, const double *intElasticMat) {
     const astro_model *m = c->m;
     for (int i1 = 1; i1 <= c->numEls; ++i1) {
-        if (m->element_type[i1 - 1] != 41) continue;
-        const int nodalDof = 24, totalDof = 32;
+        const int et = m->element_type[i1 - 1];
+        if (et != 41 && et != 81) continue;
+        // r_getElementProfile: shell4 4 nodes x 6 DOF + 8 internal, brickIM 8 nodes x 3 DOF + 9
+        const int nn = (et == 41) ? 4 : 8, nodalDof = 24, numInt = (et == 41) ? 8 : 9, totalDof = nodalDof + numInt;
         A2<double, 33, 33> K;
         K.fill(0.0);
         int i4 = c->intMatRange[i1 - 1] + 1;
@@ -812,10 +818,10 @@ void orc_update_external_rhs(const OracleCtx *c, double *extVec, const double *i
             for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) K(i3, i2) = intElasticMat[(i4++) - 1];
         double t1[33] = {0}, t2[33] = {0}, z[33] = {0};
         int v0 = c->intVecRange[i1 - 1];
-        for (int k = 1; k <= 8; ++k) t2[nodalDof + k - 1] = intVec[v0 + k - 1];
+        for (int k = 1; k <= numInt; ++k) t2[nodalDof + k - 1] = intVec[v0 + k - 1];
         t_SolveLUxb(t1, &K(1, 1), t2, z, 33, nodalDof + 1, totalDof);
         for (int i2 = 1; i2 <= nodalDof; ++i2) {
-            int comp = (i2 - 1) / 4 + 1, lnd = (i2 - 1) % 4 + 1;
+            int comp = (i2 - 1) / nn + 1, lnd = (i2 - 1) % nn + 1;
             int nd = m->element_list[8 * (i1 - 1) + lnd - 1];
             int i6 = c->nDofIndex[6 * (nd - 1) + comp - 1];
             for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) extVec[i6 - 1] -= K(i3, i2) * t1[i3 - 1];
@@ -828,8 +834,9 @@ void orc_update_internal_soln(const OracleCtx *c, const double *extSoln, double 
                               const double *intElasticMat) {
     const astro_model *m = c->m;
     for (int i1 = 1; i1 <= c->numEls; ++i1) {
-        if (m->element_type[i1 - 1] != 41) continue;
-        const int nodalDof = 24, totalDof = 32;
+        const int et = m->element_type[i1 - 1];
+        if (et != 41 && et != 81) continue;
+        const int nn = (et == 41) ? 4 : 8, nodalDof = 24, numInt = (et == 41) ? 8 : 9, totalDof = nodalDof + numInt;
         A2<double, 33, 33> K;
         K.fill(0.0);
         int i4 = c->intMatRange[i1 - 1] + 1;
@@ -837,15 +844,15 @@ void orc_update_internal_soln(const OracleCtx *c, const double *extSoln, double 
             for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) K(i3, i2) = intElasticMat[(i4++) - 1];
         double t1[33] = {0}, t2[33] = {0}, z[33] = {0};
         int v0 = c->intVecRange[i1 - 1];
-        for (int k = 1; k <= 8; ++k) t2[nodalDof + k - 1] = intRHS ? intRHS[v0 + k - 1] : 0.0;
+        for (int k = 1; k <= numInt; ++k) t2[nodalDof + k - 1] = intRHS ? intRHS[v0 + k - 1] : 0.0;
         for (int i2 = 1; i2 <= nodalDof; ++i2) {
-            int comp = (i2 - 1) / 4 + 1, lnd = (i2 - 1) % 4 + 1;
+            int comp = (i2 - 1) / nn + 1, lnd = (i2 - 1) % nn + 1;
             int nd = m->element_list[8 * (i1 - 1) + lnd - 1];
             int i6 = c->nDofIndex[6 * (nd - 1) + comp - 1];
             for (int i3 = nodalDof + 1; i3 <= totalDof; ++i3) t2[i3 - 1] -= K(i3, i2) * extSoln[i6 - 1];
         }
         t_SolveLUxb(t1, &K(1, 1), t2, z, 33, nodalDof + 1, totalDof);
-        for (int k = 1; k <= 8; ++k) intSoln[v0 + k - 1] += t1[nodalDof + k - 1];
+        for (int k = 1; k <= numInt; ++k) intSoln[v0 + k - 1] += t1[nodalDof + k - 1];
     }
 }
 
@@ -956,7 +963,7 @@ void orc_surface_load(const OracleCtx *c, int nfaces, const int32_t *faceEl, con
     for (int f = 0; f < nfaces; ++f) {
         int el = faceEl[f], fn = faceNum[f];
         int t = m->element_type[el - 1];
-        const int *fl = (t == 8) ? hexF[fn - 1] : shF[fn - 1];
+        const int *fl = (t == 8 || t == 81) ? hexF[fn - 1] : shF[fn - 1];
         double X[4][3];
         int nodes[4];
         for (int k = 0; k < 4; ++k) {

@@ -35,21 +35,30 @@ template <class T> static T dval(const astro_model *m, int d, const DPert<T> &p)
     return v;
 }
 
-// r_getElementProfile, Working/AStrO_r_elementEqns.f90:334-449 (types 8 and 41)
+// r_getElementProfile, Working/AStrO_r_elementEqns.f90:334-449 (types 8, 81 and 41)
 template <class T> static int t_getElementProfile(ElemData<T> &e, int eType) {
     std::memset(e.dofTable, 0, sizeof(e.dofTable));
     const double rt3 = KC<T>::rt3();
     e.eType = eType;
-    if (eType == 8) {
+    if (eType == 8 || eType == 81) {
         e.numNds = 8;
         e.dofPerNd = 3;
-        e.numIntDof = 0;
+        e.numIntDof = (eType == 81) ? 9 : 0;
         e.numIntPts = 8;
         const int sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {-1, 1, -1}, {1, 1, -1},
                               {-1, -1, 1},  {1, -1, 1},  {-1, 1, 1},  {1, 1, 1}};
         for (int g = 0; g < 8; ++g) {
             for (int k = 0; k < 3; ++k) e.intPts[g][k] = T(rt3 * (double)sg[g][k]);
             e.ipWt[g] = 1.0;
+        }
+        if (eType == 81) {  // internal DOF 25..33: component-major over the bubbles 9..11 (:390-397)
+            int i3 = 24;
+            for (int i1 = 1; i1 <= 3; ++i1)
+                for (int i2 = 9; i2 <= 11; ++i2) {
+                    e.dofTable[i3][0] = i1;
+                    e.dofTable[i3][1] = i2;
+                    ++i3;
+                }
         }
     } else if (eType == 41) {
         e.numNds = 4;
@@ -298,7 +307,7 @@ static int t_getElementData(ElemData<T> &e, const astro_model *m, const int *nDo
     for (int i1 = 1; i1 <= 3; ++i1)
         for (int i2 = 1; i2 <= 10; ++i2)
             for (int i3 = 1; i3 <= 3; ++i3) e.locNds(i1, i2) = e.locNds(i1, i2) + e.orient(i1, i3) * e.globNds(i3, i2);
-    if (eType == 8) {
+    if (eType == 8 || eType == 81) {
         t_getMaterialStiffness(e.cMat, m, el, p);
         int mat = m->section_mat_id[sec - 1];
         e.den = T(m->material_density ? m->material_density[mat - 1] : 0.0);

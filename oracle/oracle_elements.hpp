@@ -478,12 +478,12 @@ void t_rotateAlpha(A2<T, 3, 3> &aGI, const A2<T, 3, 3> &aGL, const A1<T, 3> &rot
 
 // ---- Working/AStrO_r_elementEqns.f90 -------------------------------------------------------
 
-// r_EvalN, :11-89 (types 8 and 41)
+// r_EvalN, :11-89 (types 8, 81 and 41)
 template <class T> void t_EvalN(A1<T, 11> &n, const T *s, int eType) {
     const T s1 = s[0], s2 = s[1], s3 = s[2];
     const T one(1.0);
     n.fill(T(0.0));
-    if (eType == 8) {
+    if (eType == 8 || eType == 81) {
         n(1) = 0.125 * (one - s1) * (one - s2) * (one - s3);
         n(2) = 0.125 * (one + s1) * (one - s2) * (one - s3);
         n(3) = 0.125 * (one + s1) * (one + s2) * (one - s3);
@@ -492,6 +492,11 @@ template <class T> void t_EvalN(A1<T, 11> &n, const T *s, int eType) {
         n(6) = 0.125 * (one + s1) * (one - s2) * (one + s3);
         n(7) = 0.125 * (one + s1) * (one + s2) * (one + s3);
         n(8) = 0.125 * (one - s1) * (one + s2) * (one + s3);
+    }
+    if (eType == 81) {  // incompatible-mode bubbles (:38-42)
+        n(9) = one - s1 * s1;
+        n(10) = one - s2 * s2;
+        n(11) = one - s3 * s3;
     }
     if (eType == 41) {
         n(1) = 0.25 * (one - s1) * (one - s2);
@@ -512,7 +517,7 @@ template <class T> void t_EvalNs(A2<T, 11, 3> &Ns, const T *s, int eType) {
     const T s1 = s[0], s2 = s[1], s3 = s[2];
     const T one(1.0);
     Ns.fill(T(0.0));
-    if (eType == 8) {
+    if (eType == 8 || eType == 81) {
         Ns(1, 1) = -0.125 * (one - s2) * (one - s3);
         Ns(2, 1) = 0.125 * (one - s2) * (one - s3);
         Ns(3, 1) = 0.125 * (one + s2) * (one - s3);
@@ -537,6 +542,11 @@ template <class T> void t_EvalNs(A2<T, 11, 3> &Ns, const T *s, int eType) {
         Ns(6, 3) = 0.125 * (one + s1) * (one - s2);
         Ns(7, 3) = 0.125 * (one + s1) * (one + s2);
         Ns(8, 3) = 0.125 * (one - s1) * (one + s2);
+    }
+    if (eType == 81) {  // :138-142
+        Ns(9, 1) = -s1 - s1;
+        Ns(10, 2) = -s2 - s2;
+        Ns(11, 3) = -s3 - s3;
     }
     if (eType == 41) {
         Ns(1, 1) = -0.25 * (one - s2);

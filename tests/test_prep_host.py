@@ -58,7 +58,18 @@ CASES = {
     "plate_cfg1": M.config1,
     "plate_ss": lambda: M.plate_shell(nx=9, ny=7, lx=1.0, ly=1.0, clamp="ss", y0=0.0),
     "block_cfg2_8x4x4": lambda: M.config2(nx=8, ny=4, nz=4),
+    "brickIM_mixed": lambda: _mixed_brick_im(),
 }
+
+
+def _mixed_brick_im():
+    """brick8 and brickIM (type 81) elements in one block: the same node structure, plus the
+    internal-DOF ranges of the incompatible modes."""
+    m = M.hex_block(4, 3, 2, lx=1.0, ly=0.75, lz=0.5, seed=3)
+    t = np.full(m.num_els, 8, np.int32)
+    t[::3] = 81
+    m.element_type = t
+    return m
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
@@ -68,6 +79,7 @@ def test_prep_matches_oracle(name):
     d, rank, ndi, rng, lt, cols, ncol = _prep_host(m)
     assert d.el_mat_dim == o.n and d.el_mat_size == o.el_mat_size and d.el_mat_lt_size == o.lt_size
     assert d.solver_max_bw == o.solver_max_bw
+    assert d.int_vec_size == o.int_vec_size and d.int_mat_size == o.int_mat_size
     assert np.array_equal(rank, o.current_rank)
     assert np.array_equal(ndi, o.n_dof_index)
     assert np.array_equal(rng, o.el_mat_range)
