@@ -36,9 +36,21 @@ extern "C" {
 #define ASTRO_ERR_BOUNDS 10      /* library built with ASTRO_BOUNDS_CHECK only: a device index guard
                                     found an index outside its buffer and skipped the access */
 
-/* Design-variable categories supported by the complex-step path (reference dCategory/dSubCat). */
-#define ASTRO_DCAT_LAYUP_THICKNESS 1   /* 'layup' / 'thickness' of layer d_layer */
-#define ASTRO_DCAT_ELASTIC_MODULUS 2   /* 'elastic' / 'modulus': materialElastic entry d_component (1..9) */
+/* Design-variable categories (reference dCategory / dSubCat, Working/AStrO_r_designPropertyFunctions.f90).
+ * Element categories enter through el_to_d, node categories through nd_to_d. */
+#define ASTRO_DCAT_LAYUP_THICKNESS 1   /* 'layup' / 'thickness' of layer d_layer (:242, :299) */
+#define ASTRO_DCAT_ELASTIC_MODULUS 2   /* 'elastic' / 'modulus': materialElastic entry d_component (1..9) (:46) */
+#define ASTRO_DCAT_DENSITY 3           /* 'density': solid material density (r_getMaterialDensity, :98) */
+#define ASTRO_DCAT_ORIENTATION 4       /* 'orientation': component d_component (1..3) of the local rotation
+                                          vector applied to the section orientation (r_getOrientation, :203) */
+#define ASTRO_DCAT_LAYUP_ZOFFSET 5     /* 'layup' / 'zOffset' of the section (r_getElThickOffset, :252) */
+#define ASTRO_DCAT_LAYUP_ANGLE 6       /* 'layup' / 'angle' of layer d_layer, radians (:301) */
+#define ASTRO_DCAT_LAYUP_DENSITY 7     /* 'layup' / 'density' of layer d_layer (r_getShellMass, :505) */
+#define ASTRO_DCAT_NODE_COORD 8        /* 'nodeCoord': coordinate d_component (1..3) of the nodes of nd_to_d
+                                          (r_getNodeCoord, :945-968) */
+#define ASTRO_DCAT_NODE_LOAD 9         /* 'nodeLoad' / 'elastic': nodal load component d_component (1..6) at the
+                                          nodes of nd_to_d while d_act_time[0] < t < d_act_time[1]
+                                          (r_getNodeDLoad, :970-994) */
 
 /* Model arrays: the reference's module globals (Working/AStrO_globalData.f90) as flat arrays.
  * Element types: 8 = brick8 (2x2x2 Gauss), 81 = brickIM (brick8 plus three incompatible bubbles,
@@ -77,6 +89,11 @@ typedef struct astro_model {
     const int32_t *d_component;     /* dComponent */
     const int32_t *d_layer;         /* dLayer */
     const double *d_value;          /* r_dVec */
+    const int32_t *nd_to_d_range;   /* ndToDRange(0:num_nodes), or NULL (no node design variables) */
+    const int32_t *nd_to_d;         /* ndToD: design variable per entry */
+    const double *nd_to_coef;       /* ndToCoef */
+    const double *d_act_time;       /* dActTime(2, num_dvars): activity window of nodeLoad variables, or NULL
+                                       (always active) */
 } astro_model;
 
 /* Sizes produced by analysis preparation (reference analysisPrep, Working/AStrO_bookKeeping.f90:794). */
@@ -299,6 +316,15 @@ int astro_body_load_drdd(astro_ctx *ctx, int32_t dvar, double h, int32_t kind, c
 #define ASTRO_BODY_CENTRIFUGAL 2
 int astro_body_load(astro_ctx *ctx, int32_t kind, const double *vals, const int32_t *elements, int32_t count,
                     const astro_state *state, double *elastic_load);
+
+/* getElasticAppliedLoad's nodal design loads (Working/AStrO_commandFunctions.f90:494-502 with
+ * r_getNodeDLoad, Working/AStrO_r_designPropertyFunctions.f90:970-994): elastic_load[n] (reference
+ * numbering) += the nodal loads of the ASTRO_DCAT_NODE_LOAD variables active at `time`. */
+int astro_design_node_load(astro_ctx *ctx, double time, double *elastic_load);
+/* The nodal-load branch of getdRelasticdD (Working/AStrO_commandFunctions.f90:1364-1373): drudd[n]
+ * -= d(nodal design load)/d(dvar) at `time`.  With astro_drdd_complex (element part) and
+ * astro_body_load_drdd it gives the reference's dRudD. */
+int astro_node_load_drdd(astro_ctx *ctx, int32_t dvar, double time, double *drudd);
 
 /* ---- thermal path --------------------------------------------------------------------------- */
 

@@ -161,6 +161,8 @@ def load_library():
         "astro_assemble_fp32_async": ([vp], C.c_int),
         "astro_element_matrices": ([vp, C.c_int32, vp, F64P, F64P], C.c_int),
         "astro_drdd_complex": ([vp, C.c_int32, C.c_double, vp, F64P, F64P], C.c_int),
+        "astro_design_node_load": ([vp, C.c_double, F64P], C.c_int),
+        "astro_node_load_drdd": ([vp, C.c_int32, C.c_double, F64P], C.c_int),
         "astro_scale_mpc": ([vp, F64P, F64P], C.c_int),
         "astro_constraint_load": ([vp, F64P, F64P], C.c_int),
         "astro_surface_load": ([vp, C.c_int32, I32P, I32P, F64P, C.c_double, F64P], C.c_int),
@@ -559,6 +561,18 @@ class AstroGPU:
         self._check(self.L.astro_drdd_complex(self.h, dvar, h, C.byref(state) if state is not None else None,
                                               _d(out), _d(iout)))
         return out, iout[:self.int_vec_size]
+
+    def design_node_load(self, time, elastic_load=None):
+        """The nodal design loads active at time, added to elastic_load (returns a new array)."""
+        out = np.zeros(self.n) if elastic_load is None else _f64(elastic_load).copy()
+        self._check(self.L.astro_design_node_load(self.h, float(time), _d(out)))
+        return out
+
+    def node_load_drdd(self, dvar, time, drudd=None):
+        """drudd - d(nodal design load)/d(dvar) at time (returns a new array)."""
+        out = np.zeros(self.n) if drudd is None else _f64(drudd).copy()
+        self._check(self.L.astro_node_load_drdd(self.h, int(dvar), float(time), _d(out)))
+        return out
 
     def drdd_condensed(self, dvars, h=1e-14, state=None):
         """Condensed complex-step dRu/dd of the listed design variables: (n, len(dvars)), Fortran

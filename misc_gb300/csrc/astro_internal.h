@@ -143,6 +143,11 @@ struct astro_ctx {
     std::vector<int> c8Els, c8Ptr, c81Els, c81Ptr;
     DevBuf d_c8Els, d_c81Els, d_intVecOff, d_intMatOff, d_elRho;
     int has81 = 0;
+    // node design-variable maps (ndToD) and the activity windows of nodeLoad variables; the
+    // section orientations as given (the complex step rotates them itself)
+    std::vector<int> n2dRange, n2d;
+    std::vector<double> n2c, dActTime;
+    DevBuf d_n2dR, d_n2d, d_n2c, d_dComp, d_secOrig;
     int quirkShellMeanRot = 0;
 };
 
@@ -220,8 +225,11 @@ int elem_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d_e
 int elem_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln, const double *d_intRhs);
 // Complex-step residual sensitivity of the elements that depend on design variable dvar:
 // d_acc -= Im(Ru(d + i h)) accumulated in colour order (internal layout; shells also d_intAcc).
-int hex8_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
-              double *d_intAcc);                                                                    // elem_hex8.cu
+int solid_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
+               double *d_intAcc);                                                                   // elem_solid_cstep.cu
+// per-element orientation of solid meshes with orientation design variables (r_getOrientation's
+// rotation of the section frame by their real values), into d_secOrient (elem_solid_cstep.cu)
+int solid_orient_prepare(astro_ctx *ctx);
 int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
                 double *d_intAcc);                                                              // elem_shell4.cu
 void krylov_release(astro_ctx *ctx);

@@ -83,7 +83,8 @@ static void free_all(astro_ctx *c) {
                       &c->d_status, &c->d_shLayRange, &c->d_shLay, &c->d_shZoff, &c->d_e2dR, &c->d_e2d,
                       &c->d_e2c, &c->d_dCat, &c->d_dLayer, &c->d_dVal, &c->d_elC, &c->d_elXdf, &c->d_elCdf, &c->d_ioRef,
                       &c->d_ioInt, &c->d_exMat, &c->d_exCols, &c->d_shFr, &c->d_shGp, &c->d_shDe, &c->d_shKf,
-                      &c->d_guard, &c->d_c8Els, &c->d_c81Els, &c->d_intVecOff, &c->d_intMatOff, &c->d_elRho};
+                      &c->d_guard, &c->d_c8Els, &c->d_c81Els, &c->d_intVecOff, &c->d_intMatOff, &c->d_elRho,
+                      &c->d_secOrig, &c->d_n2dR, &c->d_n2d, &c->d_n2c, &c->d_dComp};
     for (DevBuf *b : bufs) dev_free(*b);
 }
 
@@ -155,15 +156,41 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
         if (!m->el_to_d_range || !m->el_to_d || !m->el_to_coef || !m->d_category || !m->d_value)
             return fail(ASTRO_ERR_ARG, "design variables without their element maps");
         for (int d = 0; d < m->num_dvars; ++d) {
-            int cat = m->d_category[d];
-            if (cat != ASTRO_DCAT_LAYUP_THICKNESS && cat != ASTRO_DCAT_ELASTIC_MODULUS)
+            const int cat = m->d_category[d];
+            if (cat < ASTRO_DCAT_LAYUP_THICKNESS || cat > ASTRO_DCAT_NODE_LOAD)
                 return fail(ASTRO_ERR_UNSUPPORTED, "design-variable category not supported");
-            if (cat == ASTRO_DCAT_ELASTIC_MODULUS && (!m->d_component || m->d_component[d] < 1 || m->d_component[d] > 9))
-                return fail(ASTRO_ERR_ARG, "modulus design variable needs d_component in 1..9");
+            const int comp = m->d_component ? m->d_component[d] : 0;
+            const int maxComp = cat == ASTRO_DCAT_ELASTIC_MODULUS ? 9 : (cat == ASTRO_DCAT_NODE_LOAD ? 6 : 3);
+            if ((cat == ASTRO_DCAT_ELASTIC_MODULUS || cat == ASTRO_DCAT_ORIENTATION || cat == ASTRO_DCAT_NODE_COORD ||
+                 cat == ASTRO_DCAT_NODE_LOAD) &&
+                (comp < 1 || comp > maxComp))
+                return fail(ASTRO_ERR_ARG, "design variable " + std::to_string(d + 1) + " needs d_component in 1.." +
+                                               std::to_string(maxComp));
+            if ((cat == ASTRO_DCAT_LAYUP_THICKNESS || cat == ASTRO_DCAT_LAYUP_ANGLE || cat == ASTRO_DCAT_LAYUP_DENSITY) &&
+                (!m->d_layer || m->d_layer[d] < 1))
+                return fail(ASTRO_ERR_ARG, "layer design variable needs d_layer >= 1");
         }
         const int nE2D = m->el_to_d_range[P.E];
         for (int q = 0; q < nE2D; ++q)
             if (m->el_to_d[q] < 1 || m->el_to_d[q] > m->num_dvars) return fail(ASTRO_ERR_ARG, "el_to_d out of range");
+        if (m->nd_to_d_range) {
+            if (!m->nd_to_d || !m->nd_to_coef) return fail(ASTRO_ERR_ARG, "nd_to_d_range without nd_to_d / nd_to_coef");
+            const int nN2D = m->nd_to_d_range[P.N];
+            for (int q = 0; q < nN2D; ++q)
+                if (m->nd_to_d[q] < 1 || m->nd_to_d[q] > m->num_dvars) return fail(ASTRO_ERR_ARG, "nd_to_d out of range");
+            ctx->n2dRange.assign(m->nd_to_d_range, m->nd_to_d_range + P.N + 1);
+            ctx->n2d.assign(m->nd_to_d, m->nd_to_d + nN2D);
+            ctx->n2c.assign(m->nd_to_coef, m->nd_to_coef + nN2D);
+            // r_getNodeCoord: the real values of the nodeCoord variables move the nodes of every
+            // element (the complex step adds its own imaginary part)
+            for (int nd = 1; nd <= P.N; ++nd)
+                for (int q = ctx->n2dRange[nd - 1]; q < ctx->n2dRange[nd]; ++q) {
+                    const int d = ctx->n2d[q];
+                    if (m->d_category[d - 1] == ASTRO_DCAT_NODE_COORD)
+                        ctx->nodes[3 * (size_t)(nd - 1) + m->d_component[d - 1] - 1] += ctx->n2c[q] * m->d_value[d - 1];
+                }
+        }
+        if (m->d_act_time) ctx->dActTime.assign(m->d_act_time, m->d_act_time + 2 * (size_t)m->num_dvars);
         ctx->numDvars = m->num_dvars;
         ctx->e2dRange.assign(m->el_to_d_range, m->el_to_d_range + P.E + 1);
         ctx->e2d.assign(m->el_to_d, m->el_to_d + nE2D);
@@ -187,13 +214,19 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
             for (int k = 0; k < 9; ++k) ctx->elMat[9 * (size_t)e + k] = m->material_elastic[9 * (size_t)(mat - 1) + k];
             if (m->material_density) ctx->elDensity[e] = m->material_density[mat - 1];
             ctx->elMatId[e] = mat;
-            // elastic-modulus design variables: eProps(c) += coef * d (r_getMaterialStiffness)
+            // elastic-modulus design variables: eProps(c) += coef * d (r_getMaterialStiffness);
+            // density variables: den += coef * d (r_getMaterialDensity); orientation variables
+            // rotate the element's frame (applied on the device below)
             if (m->num_dvars > 0)
                 for (int q = m->el_to_d_range[e]; q < m->el_to_d_range[e + 1]; ++q) {
                     const int d = m->el_to_d[q];
                     if (m->d_category[d - 1] == ASTRO_DCAT_ELASTIC_MODULUS) {
                         double &v = ctx->elMat[9 * (size_t)e + m->d_component[d - 1] - 1];
                         v = v + m->el_to_coef[q] * m->d_value[d - 1];
+                    } else if (m->d_category[d - 1] == ASTRO_DCAT_DENSITY) {
+                        ctx->elDensity[e] += m->el_to_coef[q] * m->d_value[d - 1];
+                    } else if (m->d_category[d - 1] == ASTRO_DCAT_ORIENTATION) {
+                        ctx->orientIdentity = 0;
                     }
                 }
             for (int k = 0; k < 9; ++k) {
@@ -232,6 +265,27 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
     cudaMemset(ctx->d_status.p, 0, 256);
     if ((rc = dev_alloc(ctx, ctx->d_guard, sizeof(int)))) return fail(rc, ctx->err);
     cudaMemset(ctx->d_guard.p, 0, sizeof(int));
+    // section orientations as given, and the design-variable maps (the complex step's inputs)
+    if ((rc = upload(ctx, ctx->d_secOrig, ctx->secOrient.data(), sizeof(double) * ctx->secOrient.size())))
+        return fail(rc, ctx->err);
+    if (ctx->numDvars > 0) {
+        std::vector<int> e2d(ctx->e2d), n2d(ctx->n2d), n2r(ctx->n2dRange);
+        std::vector<double> e2c(ctx->e2c), n2c(ctx->n2c);
+        if (e2d.empty()) e2d.push_back(0), e2c.push_back(0.0);
+        if (n2d.empty()) n2d.push_back(0), n2c.push_back(0.0);
+        if (n2r.empty()) n2r.assign((size_t)P.N + 1, 0);
+        if ((rc = upload(ctx, ctx->d_e2dR, ctx->e2dRange.data(), sizeof(int) * ctx->e2dRange.size())) ||
+            (rc = upload(ctx, ctx->d_e2d, e2d.data(), sizeof(int) * e2d.size())) ||
+            (rc = upload(ctx, ctx->d_e2c, e2c.data(), sizeof(double) * e2c.size())) ||
+            (rc = upload(ctx, ctx->d_n2dR, n2r.data(), sizeof(int) * n2r.size())) ||
+            (rc = upload(ctx, ctx->d_n2d, n2d.data(), sizeof(int) * n2d.size())) ||
+            (rc = upload(ctx, ctx->d_n2c, n2c.data(), sizeof(double) * n2c.size())) ||
+            (rc = upload(ctx, ctx->d_dCat, ctx->dCat.data(), sizeof(int) * ctx->dCat.size())) ||
+            (rc = upload(ctx, ctx->d_dComp, ctx->dComp.data(), sizeof(int) * ctx->dComp.size())) ||
+            (rc = upload(ctx, ctx->d_dLayer, ctx->dLayer.data(), sizeof(int) * ctx->dLayer.size())) ||
+            (rc = upload(ctx, ctx->d_dVal, ctx->dVal.data(), sizeof(double) * ctx->dVal.size())))
+            return fail(rc, ctx->err);
+    }
     if (ctx->hasShell && (rc = shell_sections_prepare(ctx, m))) return fail(rc, ctx->err);
     if (ctx->hasSolid) {
         // colour-grouped element lists by type (brick8 / brickIM), internal-DOF offsets, density
@@ -257,6 +311,7 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
             return fail(rc, ctx->err);
         if (P.intMatSize && (rc = dev_alloc(ctx, ctx->d_intMat, sizeof(double) * (size_t)P.intMatSize)))
             return fail(rc, ctx->err);
+        if (!ctx->orientIdentity && ctx->numDvars > 0 && (rc = solid_orient_prepare(ctx))) return fail(rc, ctx->err);
         if ((rc = hex8_prepare(ctx))) return fail(rc, ctx->err);
     }
     // unscaled constraints in internal numbering
@@ -715,7 +770,7 @@ static int drdd_device(astro_ctx *ctx, int dvar, double h, DrddState &D, double 
     CK(cudaMemsetAsync(d_acc, 0, sizeof(double) * n, ctx->stream));
     if (ni > 0 && d_iacc) CK(cudaMemsetAsync(d_iacc, 0, sizeof(double) * ni, ctx->stream));
     if (ctx->hasSolid) {
-        rc = hex8_drdd(ctx, dvar, h, D.ds, d_acc, ni > 0 ? d_iacc : nullptr);
+        rc = solid_drdd(ctx, dvar, h, D.ds, d_acc, ni > 0 ? d_iacc : nullptr);
     } else {
         rc = shell4_drdd(ctx, dvar, h, D.ds, d_acc, ni > 0 ? d_iacc : nullptr);
     }

@@ -956,38 +956,6 @@ __global__ void k_elem_c(int E, const double *__restrict__ elMat, double *__rest
     o[8] = C[5][5];
 }
 
-// Imaginary part of the complex-step material stiffness of each listed element:
-// eProps(c) + coef (d + i h) for the elastic-modulus design variable dvar (the real parts of all
-// design-variable terms are already in elMat), then C = S^-1 in complex arithmetic.  The first n8
-// listed elements (brick8) get the orthotropic entries C11 C12 C13 C22 C23 C33 C44 C55 C66 of
-// Im(C) in double-float, the rest (brickIM) in FP64.
-__global__ void k_hex_cim(int count, int n8, const int *__restrict__ els, const double *__restrict__ elMat,
-                          const int *__restrict__ e2dR, const int *__restrict__ e2d, const double *__restrict__ e2c,
-                          const int *__restrict__ dcat, const int *__restrict__ dcomp, int dvar, double h,
-                          float2 *__restrict__ Cim8, double *__restrict__ Cim81) {
-    const int item = blockIdx.x * blockDim.x + threadIdx.x;
-    if (item >= count) return;
-    const int e = els[item];
-    cplx ep[9];
-    for (int k = 0; k < 9; ++k) ep[k] = cplx(elMat[9 * (size_t)e + k]);
-    for (int q = e2dR[e]; q < e2dR[e + 1]; ++q) {
-        const int d = e2d[q];
-        if (d == dvar && dcat[d - 1] == ASTRO_DCAT_ELASTIC_MODULUS) ep[dcomp[d - 1] - 1] += cplx(0.0, e2c[q] * h);
-    }
-    cplx C[6][6];
-    material_c<cplx>(ep, C);
-    const double v[9] = {C[0][0].im, C[0][1].im, C[0][2].im, C[1][1].im, C[1][2].im,
-                         C[2][2].im, C[3][3].im, C[4][4].im, C[5][5].im};
-    for (int q = 0; q < 9; ++q) {
-        if (item < n8) {
-            const DF d = df_from_double(v[q]);
-            Cim8[9 * (size_t)item + q] = make_float2(d.hi, d.lo);
-        } else {
-            Cim81[9 * (size_t)(item - n8) + q] = v[q];
-        }
-    }
-}
-
 }  // namespace
 
 template <class T, bool ROT> static void hex8_fast_launch(astro_ctx *ctx, const Hex8FastArgs<T> &A0) {
@@ -1174,53 +1142,4 @@ int launch_hex8_element_mats(astro_ctx *ctx, int precision, double *d_ke) {
     if (precision == 32) return hex8_fast_run<float>(ctx, nullptr, d_ke);
     ElemDevState s;
     return solid_soln_load(ctx, 1, s, nullptr, nullptr, d_ke, nullptr);
-}
-
-// Complex step of the solid residual for design variable dvar: d_acc -= Im(Ru(d + i h)) of the
-// elements that depend on it (internal DOF of brickIM elements into d_intAcc).  The residual is
-// linear in C: its imaginary part is the residual evaluated with Im(C), at the complex path's
-// Gauss points.
-int hex8_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc, double *d_intAcc) {
-    std::vector<int> list, ptr;
-    dvar_elements_by_colour(ctx, dvar, list, ptr);
-    if (list.empty()) return ASTRO_OK;
-    // split by element type, colour by colour
-    std::vector<int> l8, p8(1, 0), l81, p81(1, 0);
-    for (size_t col = 0; col + 1 < ptr.size(); ++col) {
-        for (int k = ptr[col]; k < ptr[col + 1]; ++k) (ctx->etype[list[k]] == 81 ? l81 : l8).push_back(list[k]);
-        p8.push_back((int)l8.size());
-        p81.push_back((int)l81.size());
-    }
-    DevBuf dl, dC, dR, dE, dEC, dCat, dComp;
-    struct Free {
-        DevBuf *b[7];
-        ~Free() {
-            for (auto *x : b) dev_free(*x);
-        }
-    } fr{{&dl, &dC, &dR, &dE, &dEC, &dCat, &dComp}};
-    int rc;
-    const int n8 = (int)l8.size(), n81 = (int)l81.size();
-    std::vector<int> all(l8);
-    all.insert(all.end(), l81.begin(), l81.end());
-    if ((rc = upload(ctx, dl, all.data(), sizeof(int) * all.size()))) return rc;
-    // Im(C) per listed element: double-float for the brick8 kernel, FP64 for the brickIM one
-    if ((rc = dev_alloc(ctx, dC, sizeof(float2) * 9 * (size_t)n8 + sizeof(double) * 9 * (size_t)n81))) return rc;
-    if ((rc = upload(ctx, dR, ctx->e2dRange.data(), sizeof(int) * ctx->e2dRange.size()))) return rc;
-    if ((rc = upload(ctx, dE, ctx->e2d.data(), sizeof(int) * ctx->e2d.size()))) return rc;
-    if ((rc = upload(ctx, dEC, ctx->e2c.data(), sizeof(double) * ctx->e2c.size()))) return rc;
-    if ((rc = upload(ctx, dCat, ctx->dCat.data(), sizeof(int) * ctx->dCat.size()))) return rc;
-    if ((rc = upload(ctx, dComp, ctx->dComp.data(), sizeof(int) * ctx->dComp.size()))) return rc;
-    float2 *c8 = dptr<float2>(dC);
-    double *c81 = reinterpret_cast<double *>(c8 + 9 * (size_t)n8);
-    const int tot = n8 + n81;
-    k_hex_cim<<<(tot + 127) / 128, 128, 0, ctx->stream>>>(tot, n8, dptr<int>(dl), dptr<double>(ctx->d_elMat),
-                                                          dptr<int>(dR), dptr<int>(dE), dptr<double>(dEC),
-                                                          dptr<int>(dCat), dptr<int>(dComp), dvar, h, c8, c81);
-    if (n8 && (rc = hex8_gen_run(ctx, dptr<int>(dl), p8, false, nullptr, s, d_acc, nullptr, nullptr, c8, kRt3c)))
-        return rc;
-    if (n81 && (rc = hex81_run(ctx, dptr<int>(dl) + n8, p81, 0, nullptr, s, c81, kRt3c, d_acc, d_intAcc, nullptr,
-                               nullptr, nullptr)))
-        return rc;
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    return cuda_check(ctx, e, "solid complex-step kernels");
 }

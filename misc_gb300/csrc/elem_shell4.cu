@@ -74,6 +74,9 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
         if ((rc = upload(ctx, dcat, m->d_category, sizeof(int) * m->num_dvars))) return rc;
         if ((rc = upload(ctx, dlayer, dl.data(), sizeof(int) * m->num_dvars))) return rc;
         if ((rc = upload(ctx, dval, m->d_value, sizeof(double) * m->num_dvars))) return rc;
+        std::vector<int> dc(m->num_dvars, 0);
+        if (m->d_component) dc.assign(m->d_component, m->d_component + m->num_dvars);
+        if ((rc = upload(ctx, ctx->d_dComp, dc.data(), sizeof(int) * m->num_dvars))) return rc;
     }
     if ((rc = upload(ctx, ctx->d_secOrient, m->section_orient, sizeof(double) * 9 * S))) return rc;
     if ((rc = dev_alloc(ctx, ctx->d_secABD, sizeof(ShellProps) * (size_t)E))) return rc;
@@ -81,7 +84,8 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
         E, dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist), dptr<int>(ctx->d_esec), dptr<double>(ctx->d_secOrient),
         dptr<int>(dlr), dptr<LayerDev>(dlay), dptr<double>(dzo), dv ? dptr<int>(de2dR) : nullptr,
         dv ? dptr<int>(de2d) : nullptr, dv ? dptr<double>(de2c) : nullptr, dv ? dptr<int>(dcat) : nullptr,
-        dv ? dptr<int>(dlayer) : nullptr, dv ? dptr<double>(dval) : nullptr, dptr<ShellProps>(ctx->d_secABD));
+        dv ? dptr<int>(dlayer) : nullptr, dv ? dptr<int>(ctx->d_dComp) : nullptr, dv ? dptr<double>(dval) : nullptr,
+        dptr<ShellProps>(ctx->d_secABD));
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (!ctx->d_intMat.p && (rc = dev_alloc(ctx, ctx->d_intMat, sizeof(double) * 256 * (size_t)E))) return rc;
@@ -186,13 +190,13 @@ int launch_shell4_assemble(astro_ctx *ctx, const ElemDevState &st, double *d_loa
 __global__ void k_shell_props_im(int count, const int *els, const double *nodes, const int *elist, const int *esec,
                                  const double *secOrient, const int *layRange, const LayerDev *lay, const double *zoff,
                                  const int *e2dR, const int *e2d, const double *e2c, const int *dcat, const int *dlay,
-                                 const double *dval, int dvar, double h, ShellProps *out) {
+                                 const int *dcomp, const double *dval, int dvar, double h, ShellProps *out) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= count) return;
     const int e = els[q];
     cplx o[3][3], ABD[9][9], M[6][6];
     shell_props<cplx>(nodes, elist + 8 * (size_t)e, secOrient, esec[e], layRange, lay, zoff, e2dR, e2d, e2c, dcat, dlay,
-                      dval, e, dvar, h, o, ABD, M);
+                      dcomp, dval, e, dvar, h, o, ABD, M);
     ShellProps &P = out[e];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) P.orient[3 * i + j] = o[i][j].re;
@@ -225,7 +229,7 @@ int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ElemDevState &st,
             cnt, dptr<int>(dl), dptr<double>(ctx->d_nodes), dptr<int>(ctx->d_elist), dptr<int>(ctx->d_esec),
             dptr<double>(ctx->d_secOrient), dptr<int>(ctx->d_shLayRange), dptr<LayerDev>(ctx->d_shLay),
             dptr<double>(ctx->d_shZoff), dptr<int>(ctx->d_e2dR), dptr<int>(ctx->d_e2d), dptr<double>(ctx->d_e2c),
-            dptr<int>(ctx->d_dCat), dptr<int>(ctx->d_dLayer), dptr<double>(ctx->d_dVal), dvar, h,
+            dptr<int>(ctx->d_dCat), dptr<int>(ctx->d_dLayer), dptr<int>(ctx->d_dComp), dptr<double>(ctx->d_dVal), dvar, h,
             dptr<ShellProps>(props));
         e = cudaGetLastError();
     }
@@ -248,6 +252,11 @@ int shell4_drdd_list(astro_ctx *ctx, int dvar, double h, const ElemDevState &st,
 }
 
 int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &st, double *d_acc, double *d_intAcc) {
+    const int cat = ctx->dCat[dvar - 1];
+    if (cat == ASTRO_DCAT_ORIENTATION || cat == ASTRO_DCAT_NODE_COORD)
+        return set_err(ctx, ASTRO_ERR_UNSUPPORTED,
+                       "complex step of shell orientation or node-coordinate design variables (they enter the shell "
+                       "kinematics, which run in real arithmetic) is not provided");
     std::vector<int> list, ptr;
     dvar_elements_by_colour(ctx, dvar, list, ptr);
     return shell4_drdd_list(ctx, dvar, h, st, list, ptr, d_acc, d_intAcc, nullptr);

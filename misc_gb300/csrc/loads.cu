@@ -485,3 +485,68 @@ extern "C" int astro_body_load_drdd(astro_ctx *ctx, int32_t dvar, double h, int3
     CK(cudaStreamSynchronize(ctx->stream));
     return ASTRO_OK;
 }
+
+// ---- nodal design loads --------------------------------------------------------------------
+// r_getNodeDLoad (Working/AStrO_r_designPropertyFunctions.f90:970-994, Q6 resolved: the loop runs
+// over the node's own ndToD terms): the elastic nodal load of the nodeLoad design variables active
+// at time t (dActTime(1) < t < dActTime(2)), one thread per node, in the internal layout (rank
+// major, dpn per node).  mode 0: load += coef * d of every variable (getElasticAppliedLoad,
+// Working/AStrO_commandFunctions.f90:494-502); mode 1: load -= coef for variable dvar only
+// (getdRelasticdD's nodal-load branch, :1364-1373: minus the derivative of the load).
+namespace {
+__global__ void k_node_dload(int N, int dpn, const int *__restrict__ rank, const int *__restrict__ n2dR,
+                             const int *__restrict__ n2d, const double *__restrict__ n2c, const int *__restrict__ dcat,
+                             const int *__restrict__ dcomp, const double *__restrict__ dval, const double *__restrict__ act,
+                             double t, int mode, int dvar, double *__restrict__ loadInt) {
+    const int nd = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nd >= N) return;
+    for (int q = n2dR[nd]; q < n2dR[nd + 1]; ++q) {
+        const int d = n2d[q];
+        if (dcat[d - 1] != ASTRO_DCAT_NODE_LOAD || (mode == 1 && d != dvar)) continue;
+        if (act && !(t > act[2 * (d - 1)] && act[2 * (d - 1) + 1] > t)) continue;
+        const int c = dcomp[d - 1];
+        if (c < 1 || c > dpn) continue;  // a solid node has no rotational DOF
+        const double v = mode == 0 ? n2c[q] * dval[d - 1] : -n2c[q];
+        loadInt[(size_t)dpn * (rank[nd] - 1) + c - 1] += v;
+    }
+}
+}  // namespace
+
+static int node_dload(astro_ctx *ctx, double t, int mode, int dvar, double *vec) {
+    const AstroPrep &P = ctx->P;
+    const int n = P.n;
+    if (ctx->n2dRange.empty()) return ASTRO_OK;
+    DevBuf ref, in, act;
+    int rc;
+    struct Free {
+        DevBuf *b[3];
+        ~Free() {
+            for (auto *x : b) dev_free(*x);
+        }
+    } fr{{&ref, &in, &act}};
+    if ((rc = upload(ctx, ref, vec, sizeof(double) * n)) || (rc = dev_alloc(ctx, in, sizeof(double) * n))) return rc;
+    if (!ctx->dActTime.empty() && (rc = upload(ctx, act, ctx->dActTime.data(), sizeof(double) * ctx->dActTime.size())))
+        return rc;
+    if ((rc = ref_to_int_vec(ctx, dptr<double>(ref), dptr<double>(in), n))) return rc;
+    k_node_dload<<<(P.N + 127) / 128, 128, 0, ctx->stream>>>(
+        P.N, P.dpn, dptr<int>(ctx->d_rank), dptr<int>(ctx->d_n2dR), dptr<int>(ctx->d_n2d), dptr<double>(ctx->d_n2c),
+        dptr<int>(ctx->d_dCat), dptr<int>(ctx->d_dComp), dptr<double>(ctx->d_dVal),
+        act.p ? dptr<double>(act) : nullptr, t, mode, dvar, dptr<double>(in));
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "nodal design load"))) return rc;
+    if ((rc = int_to_ref_vec(ctx, dptr<double>(in), dptr<double>(ref), n))) return rc;
+    CK(cudaMemcpyAsync(vec, ref.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}
+
+extern "C" int astro_design_node_load(astro_ctx *ctx, double time, double *elastic_load) {
+    if (!ctx || !elastic_load) return ASTRO_ERR_ARG;
+    return node_dload(ctx, time, 0, 0, elastic_load);
+}
+
+extern "C" int astro_node_load_drdd(astro_ctx *ctx, int32_t dvar, double time, double *drudd) {
+    if (!ctx || !drudd) return ASTRO_ERR_ARG;
+    if (dvar < 1 || dvar > ctx->numDvars)
+        return set_err(ctx, ASTRO_ERR_ARG, "design variable " + std::to_string(dvar) + " out of range");
+    return node_dload(ctx, time, 1, dvar, drudd);
+}

@@ -28,24 +28,42 @@ __device__ __forceinline__ void dof_of(int i, int &var, int &nd) {  // i = 0..31
     }
 }
 
-// Section properties of one element: orientation with correctAlpha (:240-286), ABD by layer
-// integration (r_getShellStiffness, designProp :259-363) and section mass (r_getShellMass,
-// :469-525).  Layer thicknesses include the design-variable terms (+ i h on `pertDvar`).
+// Section properties of one element: orientation (r_getOrientation, designProp :187-221) with
+// correctAlpha (:240-286), ABD by layer integration (r_getShellStiffness, :259-363) and section
+// mass (r_getShellMass, :469-525).  The design-variable terms of the element (+ i h on
+// `pertDvar`) enter as the reference applies them: orientation variables rotate the section frame,
+// layer thickness, layer angle and layer density variables the layer's values, zOffset variables
+// the section offset.
 template <class T>
 __device__ void shell_props(const double *nodes, const int *el, const double *secOrient, int sec, const int *layRange,
                             const LayerDev *lay, const double *zoff, const int *e2dR, const int *e2d, const double *e2c,
-                            const int *dcat, const int *dlay, const double *dval, int e, int pertDvar, double h,
-                            T orient[3][3], T ABD[9][9], T Ms[6][6]) {
+                            const int *dcat, const int *dlay, const int *dcomp, const double *dval, int e,
+                            int pertDvar, double h, T orient[3][3], T ABD[9][9], T Ms[6][6]) {
     T X[4][3];
     for (int a = 0; a < 4; ++a)
         for (int k = 0; k < 3; ++k) X[a][k] = T(nodes[3 * (el[a] - 1) + k]);
     T al[3][3];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) al[i][j] = T(secOrient[9 * (sec - 1) + 3 * j + i]);  // column-major input
-    // r_getOrientation with no orientation design variables: rotation by zero
+    // sum of the element's design-variable terms of one category (layer 0 = any)
+    auto dsum = [&](int cat, int layerNum, int comp) {
+        T s = T(0.0);
+        if (e2dR)
+            for (int q = e2dR[e]; q < e2dR[e + 1]; ++q) {
+                const int d = e2d[q] - 1;
+                if (dcat[d] != cat || (layerNum && dlay[d] != layerNum) || (comp && dcomp[d] != comp)) continue;
+                T dv = T(dval[d]);
+                if (d + 1 == pertDvar) dv = dv + pert_i<T>(h);
+                s = s + e2c[q] * dv;
+            }
+        return s;
+    };
+    // r_getOrientation: the section frame rotated by globRot = alOrig^T locRot
     {
-        const T z[3] = {T(0.0), T(0.0), T(0.0)};
-        a_rotate<T>(orient, al, z, 0, 0);
+        T loc[3], gr[3];
+        for (int k = 0; k < 3; ++k) loc[k] = dsum(ASTRO_DCAT_ORIENTATION, 0, k + 1);
+        for (int i = 0; i < 3; ++i) gr[i] = al[0][i] * loc[0] + al[1][i] * loc[1] + al[2][i] * loc[2];
+        a_rotate<T>(orient, al, gr, 0, 0);
     }
     // correctAlpha
     {
@@ -80,22 +98,10 @@ __device__ void shell_props(const double *nodes, const int *el, const double *se
     }
     // layer thicknesses with design variables
     const int l0 = layRange[sec - 1], l1 = layRange[sec];
-    auto thick = [&](int li, int layerNum) {
-        T t = T(lay[li].t);
-        if (e2dR)
-            for (int q = e2dR[e]; q < e2dR[e + 1]; ++q) {
-                const int d = e2d[q] - 1;
-                if (dcat[d] == ASTRO_DCAT_LAYUP_THICKNESS && dlay[d] == layerNum) {
-                    T dv = T(dval[d]);
-                    if (d + 1 == pertDvar) dv = dv + pert_i<T>(h);
-                    t = t + e2c[q] * dv;
-                }
-            }
-        return t;
-    };
+    auto thick = [&](int li, int layerNum) { return T(lay[li].t) + dsum(ASTRO_DCAT_LAYUP_THICKNESS, layerNum, 0); };
     T secT = T(0.0);
     for (int li = l0, ln = 1; li < l1; ++li, ++ln) secT = secT + thick(li, ln);
-    const T zo = T(zoff[sec - 1]);
+    const T zo = T(zoff[sec - 1]) + dsum(ASTRO_DCAT_LAYUP_ZOFFSET, 0, 0);  // r_getElThickOffset
     for (int i = 0; i < 9; ++i)
         for (int j = 0; j < 9; ++j) ABD[i][j] = T(0.0);
     for (int i = 0; i < 6; ++i)
@@ -117,7 +123,8 @@ __device__ void shell_props(const double *nodes, const int *el, const double *se
             a_lu_solve<T, 3>(&S[0][0], b, x, 3);
             for (int r = 0; r < 3; ++r) Q[r][c] = x[r];
         }
-        const T a11 = a_cos(T(L.angle)), a21 = a_sin(T(L.angle));
+        const T ang = T(L.angle) + dsum(ASTRO_DCAT_LAYUP_ANGLE, ln, 0);
+        const T a11 = a_cos(ang), a21 = a_sin(ang);
         const T a12 = -a21, a22 = a11;
         T Ts[3][3] = {{a11 * a11, a12 * a12, 2.0 * a11 * a12},
                       {a21 * a21, a22 * a22, 2.0 * a22 * a21},
@@ -150,8 +157,9 @@ __device__ void shell_props(const double *nodes, const int *el, const double *se
         z = zn;
         // mass (r_getShellMass)
         const T zn2 = zm + tl;
-        const T m0 = T(L.rho) * (zn2 - zm), m1 = 0.5 * L.rho * (zn2 * zn2 - zm * zm),
-                m2 = AK<T>::o3 * L.rho * (zn2 * zn2 * zn2 - zm * zm * zm);
+        const T rho = T(L.rho) + dsum(ASTRO_DCAT_LAYUP_DENSITY, ln, 0);
+        const T m0 = rho * (zn2 - zm), m1 = 0.5 * rho * (zn2 * zn2 - zm * zm),
+                m2 = AK<T>::o3 * rho * (zn2 * zn2 * zn2 - zm * zm * zm);
         for (int k = 0; k < 3; ++k) {
             Ms[k][k] = Ms[k][k] + m0;
             Ms[k + 3][k + 3] = Ms[k + 3][k + 3] + m2;
@@ -173,12 +181,12 @@ __device__ void shell_props(const double *nodes, const int *el, const double *se
 __global__ void shell_props_kernel(int E, const double *nodes, const int *elist, const int *esec, const double *secOrient,
                                    const int *layRange, const LayerDev *lay, const double *zoff, const int *e2dR,
                                    const int *e2d, const double *e2c, const int *dcat, const int *dlay,
-                                   const double *dval, ShellProps *out) {
+                                   const int *dcomp, const double *dval, ShellProps *out) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     double o[3][3], ABD[9][9], M[6][6];
     shell_props<double>(nodes, elist + 8 * (size_t)e, secOrient, esec[e], layRange, lay, zoff, e2dR, e2d, e2c, dcat, dlay,
-                        dval, e, 0, 0.0, o, ABD, M);
+                        dcomp, dval, e, 0, 0.0, o, ABD, M);
     ShellProps &P = out[e];
     for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) P.orient[3 * i + j] = o[i][j];

@@ -37,6 +37,7 @@ class AstroModelC(C.Structure):
         ("mpc_coef", F64P), ("mpc_rhs", F64P),
         ("num_dvars", C.c_int32), ("el_to_d_range", I32P), ("el_to_d", I32P), ("el_to_coef", F64P),
         ("d_category", I32P), ("d_component", I32P), ("d_layer", I32P), ("d_value", F64P),
+        ("nd_to_d_range", I32P), ("nd_to_d", I32P), ("nd_to_coef", F64P), ("d_act_time", F64P),
     ]
 
 
@@ -51,6 +52,13 @@ class AstroStateC(C.Structure):
 
 DCAT_LAYUP_THICKNESS = 1
 DCAT_ELASTIC_MODULUS = 2
+DCAT_DENSITY = 3
+DCAT_ORIENTATION = 4
+DCAT_LAYUP_ZOFFSET = 5
+DCAT_LAYUP_ANGLE = 6
+DCAT_LAYUP_DENSITY = 7
+DCAT_NODE_COORD = 8
+DCAT_NODE_LOAD = 9
 
 
 def _p(a, typ):
@@ -94,6 +102,10 @@ class Model:
     d_component: np.ndarray | None = None
     d_layer: np.ndarray | None = None
     d_value: np.ndarray | None = None
+    nd_to_d_range: np.ndarray | None = None   # (N+1,) node -> design variable map (ndToD)
+    nd_to_d: np.ndarray | None = None
+    nd_to_coef: np.ndarray | None = None
+    d_act_time: np.ndarray | None = None      # (num_dvars, 2): activity window of nodeLoad variables
     # loads (not part of the C model struct): faces carrying traction/pressure, point loads
     face_el: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
     face_num: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
@@ -152,13 +164,24 @@ class Model:
         m.mpc_rhs = _p(k("mrh", _f64(self.mpc_rhs)), F64P)
         if self.d_value is not None and len(self.d_value) > 0:
             m.num_dvars = len(self.d_value)
-            m.el_to_d_range = _p(k("edr", _i32(self.el_to_d_range)), I32P)
-            m.el_to_d = _p(k("ed", _i32(self.el_to_d)), I32P)
-            m.el_to_coef = _p(k("ec", _f64(self.el_to_coef)), F64P)
+            if self.el_to_d_range is not None:
+                m.el_to_d_range = _p(k("edr", _i32(self.el_to_d_range)), I32P)
+                m.el_to_d = _p(k("ed", _i32(self.el_to_d)), I32P)
+                m.el_to_coef = _p(k("ec", _f64(self.el_to_coef)), F64P)
             m.d_category = _p(k("dc", _i32(self.d_category)), I32P)
             m.d_component = _p(k("dco", _i32(self.d_component)), I32P)
             m.d_layer = _p(k("dl", _i32(self.d_layer)), I32P)
             m.d_value = _p(k("dv", _f64(self.d_value)), F64P)
+            if self.el_to_d_range is None:   # node design variables only
+                m.el_to_d_range = _p(k("edr", np.zeros(self.num_els + 1, np.int32)), I32P)
+                m.el_to_d = _p(k("ed", np.zeros(1, np.int32)), I32P)
+                m.el_to_coef = _p(k("ec", np.zeros(1)), F64P)
+            if self.nd_to_d_range is not None:
+                m.nd_to_d_range = _p(k("ndr", _i32(self.nd_to_d_range)), I32P)
+                m.nd_to_d = _p(k("nd", _i32(self.nd_to_d)), I32P)
+                m.nd_to_coef = _p(k("nc", _f64(self.nd_to_coef)), F64P)
+            if self.d_act_time is not None:
+                m.d_act_time = _p(k("dat", _f64(self.d_act_time)), F64P)
         else:
             m.num_dvars = 0
         m._keep = keep
@@ -200,6 +223,33 @@ def add_design_variables(m: Model, n_groups: int, category: int, layer: int = 1,
     m.d_component = np.full(n_groups, component, np.int32)
     m.d_layer = np.full(n_groups, layer, np.int32)
     m.d_value = np.full(n_groups, float(value))
+    return m
+
+
+def add_node_design_variables(m: Model, node_groups, category: int, component: int = 1, value: float = 0.0,
+                              act_time=None) -> Model:
+    """Attaches one design variable of a node category (nodeCoord, nodeLoad) per group of nodes
+    (1-based node numbers), each entering its nodes with coefficient 1 (the reference's ndToD
+    maps); act_time (start, end) is the activity window of nodeLoad variables.  Replaces any
+    design variables m already has."""
+    N = m.num_nodes
+    lists = [[] for _ in range(N)]
+    for g, nodes in enumerate(node_groups):
+        for nd in nodes:
+            lists[nd - 1].append(g + 1)
+    m.nd_to_d_range = np.concatenate([[0], np.cumsum([len(x) for x in lists])]).astype(np.int32)
+    m.nd_to_d = np.array([d for x in lists for d in x], np.int32)
+    m.nd_to_coef = np.ones(len(m.nd_to_d))
+    nd = len(node_groups)
+    m.el_to_d_range = np.zeros(m.num_els + 1, np.int32)
+    m.el_to_d = np.zeros(0, np.int32)
+    m.el_to_coef = np.zeros(0)
+    m.d_category = np.full(nd, category, np.int32)
+    m.d_component = np.full(nd, component, np.int32)
+    m.d_layer = np.ones(nd, np.int32)
+    m.d_value = np.full(nd, float(value))
+    if act_time is not None:
+        m.d_act_time = np.tile(np.asarray(act_time, np.float64), (nd, 1))
     return m
 
 

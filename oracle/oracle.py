@@ -45,6 +45,8 @@ def _lib():
                                     F64P, F64P, F64P, F64P]
         L.orc_element_matrices.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, F64P]
         L.orc_drdd_complex.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_void_p, F64P, F64P]
+        L.orc_design_node_load.argtypes = [C.c_void_p, C.c_double, F64P]
+        L.orc_node_load_drdd.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, F64P]
         L.orc_update_external_rhs.argtypes = [C.c_void_p, F64P, F64P, F64P]
         L.orc_update_internal_soln.argtypes = [C.c_void_p, F64P, F64P, F64P, F64P]
         L.orc_el_soln_load.argtypes = [C.c_void_p, C.c_int, C.c_void_p, F64P, F64P, F64P, I32P, F64P]
@@ -153,6 +155,18 @@ class Oracle:
                                      _d(iout))
         assert rc == 0
         return out, iout[:self.int_vec_size]
+
+    def design_node_load(self, t, load=None):
+        """getElasticAppliedLoad's nodal design loads at time t, added to load."""
+        load = np.zeros(self.n) if load is None else load
+        self.L.orc_design_node_load(self.h, float(t), _d(load))
+        return load
+
+    def node_load_drdd(self, dvar, t, h=1e-14, drudd=None):
+        """getdRelasticdD's nodal-load branch: drudd -= d(nodal design load)/d(dvar) at time t."""
+        drudd = np.zeros(self.n) if drudd is None else drudd
+        self.L.orc_node_load_drdd(self.h, int(dvar), float(t), float(h), _d(drudd))
+        return drudd
 
     def element_matrices(self, el0=1, el1=None, state=None):
         """Condensed nodal element matrices (24x24) of elements el0..el1 (1-based, inclusive)."""

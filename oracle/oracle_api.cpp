@@ -140,6 +140,23 @@ static GState to_gstate(const astro_state *s) {
     return g;
 }
 
+// r_getNodeDLoad (Working/AStrO_r_designPropertyFunctions.f90:970-994, Q6 resolved: the loop runs
+// over the node's own terms): the elastic nodal design load of a node at time t, components
+// 1..6, for the variables active (dActTime(1) < t < dActTime(2), r_greater), with design variable
+// pert (if any) at d + i h.
+template <class T> static void t_node_dload(const astro_model *m, int node, double t, const DPert<T> &p, T ld[6]) {
+    for (int k = 0; k < 6; ++k) ld[k] = T(0.0);
+    if (!m->nd_to_d_range || m->num_dvars <= 0) return;
+    for (int q = m->nd_to_d_range[node - 1]; q < m->nd_to_d_range[node]; ++q) {
+        const int d = m->nd_to_d[q];
+        if (m->d_category[d - 1] != ASTRO_DCAT_NODE_LOAD) continue;
+        if (m->d_act_time && !(t > m->d_act_time[2 * (d - 1)] && m->d_act_time[2 * (d - 1) + 1] > t)) continue;
+        const int comp = m->d_component ? m->d_component[d - 1] : 0;
+        if (comp < 1 || comp > 6) continue;
+        ld[comp - 1] = ld[comp - 1] + m->nd_to_coef[q] * dval(m, d, p);
+    }
+}
+
 extern "C" {
 
 // analysisPrep, Working/AStrO_bookKeeping.f90:794-1039, with allocateElasticMat (:333-411) and
@@ -414,15 +431,25 @@ int orc_drdd_complex(const OracleCtx *c, int dvar, double h, const astro_state *
     const astro_model *m = c->m;
     std::fill(dRudD, dRudD + c->elMatDim, 0.0);
     if (intdRudD && c->intVecSize > 0) std::fill(intdRudD, intdRudD + c->intVecSize, 0.0);
-    if (dvar < 1 || dvar > m->num_dvars || !m->el_to_d_range) return 1;
+    if (dvar < 1 || dvar > m->num_dvars) return 1;
     const double hInv = 1.0 / h;
     GState g = to_gstate(s);
     DPert<cd> p;
     p.dvar = dvar;
     p.h = h;
     for (int el = 1; el <= c->numEls; ++el) {
+        // getdToElComp (Working/AStrO_bookKeeping.f90:7-129): the element's own design variables
+        // and those of its nodes
         bool dep = false;
-        for (int q = m->el_to_d_range[el - 1]; q < m->el_to_d_range[el]; ++q) dep = dep || m->el_to_d[q] == dvar;
+        if (m->el_to_d_range)
+            for (int q = m->el_to_d_range[el - 1]; q < m->el_to_d_range[el]; ++q) dep = dep || m->el_to_d[q] == dvar;
+        if (m->nd_to_d_range)
+            for (int k = 0; k < 8; ++k) {
+                const int nd = m->element_list[8 * (el - 1) + k];
+                if (nd > 0)
+                    for (int q = m->nd_to_d_range[nd - 1]; q < m->nd_to_d_range[nd]; ++q)
+                        dep = dep || (m->nd_to_d[q] == dvar && m->d_category[dvar - 1] == ASTRO_DCAT_NODE_COORD);
+            }
         if (!dep) continue;
         A1<cd, 33> Ru;
         A2<cd, 33, 33> K;
@@ -800,6 +827,41 @@ int orc_gmres(double *xVec, const double *Amat, const int32_t *Acols, const int3
         i4++;
     }
     return i4;
+}
+
+// getElasticAppliedLoad's design nodal loads (Working/AStrO_commandFunctions.f90:494-502):
+// elasticLoad(nDofIndex(c, node)) += ndLd(c).
+void orc_design_node_load(const OracleCtx *c, double t, double *elasticLoad) {
+    DPert<double> p;
+    for (int nd = 1; nd <= c->numNodes; ++nd) {
+        double ld[6];
+        t_node_dload(c->m, nd, t, p, ld);
+        for (int k = 1; k <= 6; ++k) {
+            const int dof = c->nDofIndex[6 * (nd - 1) + k - 1];
+            if (dof > 0) elasticLoad[dof - 1] += ld[k - 1];
+        }
+    }
+}
+
+// getdRelasticdD's nodal-load branch (:1364-1373): dRudD(dof) -= Im(ndLd(d + i h)) / h at the nodes
+// of the design variable (dToNd).
+void orc_node_load_drdd(const OracleCtx *c, int dvar, double t, double h, double *dRudD) {
+    const astro_model *m = c->m;
+    if (!m->nd_to_d_range) return;
+    DPert<cd> p;
+    p.dvar = dvar;
+    p.h = h;
+    for (int nd = 1; nd <= c->numNodes; ++nd) {
+        bool dep = false;
+        for (int q = m->nd_to_d_range[nd - 1]; q < m->nd_to_d_range[nd]; ++q) dep = dep || m->nd_to_d[q] == dvar;
+        if (!dep) continue;
+        cd ld[6];
+        t_node_dload(m, nd, t, p, ld);
+        for (int k = 1; k <= 6; ++k) {
+            const int dof = c->nDofIndex[6 * (nd - 1) + k - 1];
+            if (dof > 0) dRudD[dof - 1] -= ld[k - 1].imag() / h;
+        }
+    }
 }
 
 // updateExternalRHS (Working/AStrO_commandFunctions.f90:568-607) with the Q9 loop bound resolved

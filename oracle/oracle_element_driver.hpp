@@ -35,6 +35,37 @@ template <class T> static T dval(const astro_model *m, int d, const DPert<T> &p)
     return v;
 }
 
+// sum over the element's design-variable terms of one category (and layer / component when
+// given, 0 = any): elToCoef(i) * dVec(elToD(i)), the loops of r_getMaterialDensity (:96-101),
+// r_getOrientation (:201-207), r_getElThickOffset (:249-255) and the layer loops of
+// r_getShellStiffness / r_getShellMass (:289-303, :502-510)
+template <class T>
+static T el_dsum(const astro_model *m, int el, int cat, int layer, int comp, const DPert<T> &p) {
+    T s = T(0.0);
+    if (m->num_dvars <= 0 || !m->el_to_d_range) return s;
+    for (int q = m->el_to_d_range[el - 1]; q < m->el_to_d_range[el]; ++q) {
+        const int d = m->el_to_d[q];
+        if (m->d_category[d - 1] != cat) continue;
+        if (layer && (!m->d_layer || m->d_layer[d - 1] != layer)) continue;
+        if (comp && (!m->d_component || m->d_component[d - 1] != comp)) continue;
+        s = s + m->el_to_coef[q] * dval(m, d, p);
+    }
+    return s;
+}
+
+// the same over a node's terms (ndToD, r_getNodeCoord :958-964)
+template <class T> static T nd_dsum(const astro_model *m, int node, int cat, int comp, const DPert<T> &p) {
+    T s = T(0.0);
+    if (m->num_dvars <= 0 || !m->nd_to_d_range) return s;
+    for (int q = m->nd_to_d_range[node - 1]; q < m->nd_to_d_range[node]; ++q) {
+        const int d = m->nd_to_d[q];
+        if (m->d_category[d - 1] != cat) continue;
+        if (comp && (!m->d_component || m->d_component[d - 1] != comp)) continue;
+        s = s + m->nd_to_coef[q] * dval(m, d, p);
+    }
+    return s;
+}
+
 // r_getElementProfile, Working/AStrO_r_elementEqns.f90:334-449 (types 8, 81 and 41)
 template <class T> static int t_getElementProfile(ElemData<T> &e, int eType) {
     std::memset(e.dofTable, 0, sizeof(e.dofTable));
@@ -174,7 +205,7 @@ static void t_getShellStiffness(A2<T, 9, 9> &ABD, const astro_model *m, int el, 
     int l0 = m->sec_layup_range[sec - 1], l1 = m->sec_layup_range[sec];
     T secThick = T(0.0);
     for (int i1 = l0 + 1, ln = 1; i1 <= l1; ++i1, ++ln) secThick = secThick + layer_thickness(m, el, ln, i1, p);
-    T zOff = T(m->section_z_offset[sec - 1]);
+    T zOff = T(m->section_z_offset[sec - 1]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_ZOFFSET, 0, 0, p);
     ABD.fill(T(0.0));
     T zCrd = -0.5 * secThick * (zOff + T(1.0));
     int layerNum = 0;
@@ -187,7 +218,7 @@ static void t_getShellStiffness(A2<T, 9, 9> &ABD, const astro_model *m, int el, 
         lp[2] = T(m->material_elastic[9 * (mat - 1) + 3]);
         lp[3] = T(m->material_elastic[9 * (mat - 1) + 6]);
         lp[4] = layer_thickness(m, el, layerNum, i1, p);
-        lp[5] = T(m->layup_angle[i1 - 1]);
+        lp[5] = T(m->layup_angle[i1 - 1]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_ANGLE, layerNum, 0, p);
         T zNext = zCrd + lp[4];
         A2<T, 3, 3> S, Q, Ts, Te, TeInv;
         S.fill(T(0.0));
@@ -246,14 +277,14 @@ static void t_getShellMass(A2<T, 6, 6> &M, const astro_model *m, int el, const D
     int l0 = m->sec_layup_range[sec - 1], l1 = m->sec_layup_range[sec];
     T secThick = T(0.0);
     for (int i1 = l0 + 1, ln = 1; i1 <= l1; ++i1, ++ln) secThick = secThick + layer_thickness(m, el, ln, i1, p);
-    T zOff = T(m->section_z_offset[sec - 1]);
+    T zOff = T(m->section_z_offset[sec - 1]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_ZOFFSET, 0, 0, p);
     M.fill(T(0.0));
     T zCrd = -0.5 * secThick * (zOff + T(1.0));
     int layerNum = 0;
     for (int i1 = l0 + 1; i1 <= l1; ++i1) {
         layerNum++;
         int mat = m->layup_mat_id[i1 - 1];
-        T den = T(m->material_density[mat - 1]);
+        T den = T(m->material_density[mat - 1]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_DENSITY, layerNum, 0, p);
         T th = layer_thickness(m, el, layerNum, i1, p);
         T zNext = zCrd + th;
         T f0 = den * (zNext - zCrd), f1 = 0.5 * den * (zNext * zNext - zCrd * zCrd);
@@ -287,21 +318,28 @@ static int t_getElementData(ElemData<T> &e, const astro_model *m, const int *nDo
                             int el, const GState &s, const DPert<T> &p) {
     int eType = m->element_type[el - 1];
     if (t_getElementProfile(e, eType) != 0) return -1;
-    // r_getNodeCoord (designProp :945-968): unused columns stay 1.0
+    // r_getNodeCoord (designProp :945-968): unused columns stay 1.0; nodeCoord design variables
+    // move coordinate dComponent of their nodes
     e.globNds.fill(T(1.0));
     for (int i1 = 1; i1 <= 8; ++i1) {
         int nd = m->element_list[8 * (el - 1) + i1 - 1];
         if (nd > 0)
-            for (int k = 1; k <= 3; ++k) e.globNds(k, i1) = T(m->node_list[3 * (nd - 1) + k - 1]);
+            for (int k = 1; k <= 3; ++k)
+                e.globNds(k, i1) = T(m->node_list[3 * (nd - 1) + k - 1]) + nd_dsum(m, nd, ASTRO_DCAT_NODE_COORD, k, p);
     }
-    // r_getOrientation (:187-221) with no orientation design variables: rotateAlpha by zero
+    // r_getOrientation (:187-221): the section orientation rotated by the orientation design
+    // variables' local rotation vector, expressed in global axes (globRot = alOrig^T locRot)
     int sec = m->element_section[el - 1];
     A2<T, 3, 3> alOrig;
     for (int j = 1; j <= 3; ++j)
         for (int i = 1; i <= 3; ++i) alOrig(i, j) = T(m->section_orient[9 * (sec - 1) + 3 * (j - 1) + (i - 1)]);
-    A1<T, 3> zero;
-    zero.fill(T(0.0));
-    t_rotateAlpha(e.orient, alOrig, zero, 0, 0);
+    A1<T, 3> locRot, globRot;
+    for (int k = 1; k <= 3; ++k) locRot(k) = el_dsum(m, el, ASTRO_DCAT_ORIENTATION, 0, k, p);
+    for (int i1 = 1; i1 <= 3; ++i1) {
+        globRot(i1) = T(0.0);
+        for (int i2 = 1; i2 <= 3; ++i2) globRot(i1) = globRot(i1) + alOrig(i2, i1) * locRot(i2);
+    }
+    t_rotateAlpha(e.orient, alOrig, globRot, 0, 0);
     if (eType == 41) t_correctAlpha(e.orient, e.globNds);
     e.locNds.fill(T(0.0));
     for (int i1 = 1; i1 <= 3; ++i1)
@@ -310,7 +348,8 @@ static int t_getElementData(ElemData<T> &e, const astro_model *m, const int *nDo
     if (eType == 8 || eType == 81) {
         t_getMaterialStiffness(e.cMat, m, el, p);
         int mat = m->section_mat_id[sec - 1];
-        e.den = T(m->material_density ? m->material_density[mat - 1] : 0.0);
+        e.den = T(m->material_density ? m->material_density[mat - 1] : 0.0) +
+                el_dsum(m, el, ASTRO_DCAT_DENSITY, 0, 0, p);  // r_getMaterialDensity (:82-103)
         e.ABD.fill(T(0.0));
         e.sMass.fill(T(0.0));
     } else {

@@ -470,3 +470,105 @@ def test_hex81_bending_without_shear_locking():
     d81, d8 = _cantilever(81), _cantilever(8)
     assert abs(d81 - exact) <= 0.03 * exact, (d81, exact)
     assert d8 < 0.8 * exact, (d8, exact)
+
+
+def _orthotropic(m):
+    me = m.material_elastic.copy()
+    me[:, 1] *= 0.5
+    me[:, 2] *= 0.3
+    me[:, 7] *= 0.7
+    m.material_elastic = me
+    return m
+
+
+def _brick(eltype=8):
+    m = _orthotropic(M.hex_block(nx=3, ny=2, nz=2, jitter=0.1, seed=3))
+    m.element_type = np.full(m.num_els, eltype, np.int32)
+    return m
+
+
+_CAT_CASES = {
+    # name: (model builder, step, dynamic state)
+    "brick_density": (lambda: M.add_design_variables(_brick(), 2, M.DCAT_DENSITY), 1e-6 * 7800.0, True),
+    "brick_orientation": (lambda: M.add_design_variables(_brick(), 2, M.DCAT_ORIENTATION, component=3), 1e-6, False),
+    "brickIM_orientation": (lambda: M.add_design_variables(_brick(81), 2, M.DCAT_ORIENTATION, component=1), 1e-6,
+                            False),
+    "brick_node_coord": (lambda: M.add_node_design_variables(_brick(), [[6, 7, 18], [11, 23]], M.DCAT_NODE_COORD,
+                                                             component=2), 1e-7, False),
+    "brickIM_node_coord": (lambda: M.add_node_design_variables(_brick(81), [[6, 7, 18], [11, 23]],
+                                                               M.DCAT_NODE_COORD, component=1), 1e-7, True),
+    "shell_zoffset": (lambda: M.add_design_variables(M.plate_shell(nx=4, ny=3, lx=2.0, ly=1.0, t=0.03), 2,
+                                                     M.DCAT_LAYUP_ZOFFSET), 1e-6, False),
+    "shell_layup_angle": (lambda: M.add_design_variables(_layered_plate(), 2, M.DCAT_LAYUP_ANGLE, layer=2), 1e-6,
+                          False),
+    "shell_layup_density": (lambda: M.add_design_variables(_layered_plate(), 2, M.DCAT_LAYUP_DENSITY, layer=1),
+                            1e-6 * 2700.0, True),
+}
+
+
+def _layered_plate():
+    """shell4 plate with a two-layer orthotropic laminate (0 and 0.4 rad): the layer angle moves
+    the in-plane and bending stiffness."""
+    m = M.plate_shell(nx=4, ny=3, lx=2.0, ly=1.0, t=0.03, E=7e10, nu=0.33)
+    me = m.material_elastic.copy()
+    me[0, 1] *= 0.4
+    me[0, 6] *= 0.6
+    m.material_elastic = me
+    m.sec_layup_range = np.array([0, 2], np.int32)
+    m.layup_mat_id = np.array([1, 1], np.int32)
+    m.layup_thickness = np.array([0.012, 0.018])
+    m.layup_angle = np.array([0.0, 0.4])
+    return m
+
+
+@pytest.mark.parametrize("case", sorted(_CAT_CASES))
+def test_design_categories_complex_step_matches_central_difference(case):
+    """Every design-variable category the oracle restates (density, orientation, node
+    coordinates, layup zOffset, layer angle and layer density) against a central difference of
+    its real residual; 1e-5 relative (the complex path's single-precision Gauss points)."""
+    build, step, dyn = _CAT_CASES[case]
+
+    def state_fn(o):
+        rng = np.random.default_rng(7)
+        n, ni = o.n, max(o.int_vec_size, 1)
+        kw = {}
+        if dyn:
+            kw = dict(prev_disp=1e-3 * rng.standard_normal(n), prev_vel=1e-1 * rng.standard_normal(n),
+                      prev_acc=10.0 * rng.standard_normal(n), prev_int_disp=1e-4 * rng.standard_normal(ni),
+                      dynamic=1, beta=0.25, gamma=0.5, del_t=1e-3)
+        return M.make_state(n, disp=1e-3 * rng.standard_normal(n), internal_disp=1e-4 * rng.standard_normal(ni),
+                            **kw)
+
+    o = Oracle(build())
+    for dvar in (1, 2):
+        cs, ics = o.drdd_complex(dvar, 1e-14, state=state_fn(o))
+        out = []
+        for sgn in (1.0, -1.0):
+            m = build()
+            m.d_value = m.d_value.copy()
+            m.d_value[dvar - 1] += sgn * step
+            oo = Oracle(m)
+            load, iload, *_ = oo.el_soln_load(0, state=state_fn(oo))
+            out.append((-load, -iload[:oo.int_vec_size]))
+        fd, ifd = (out[0][0] - out[1][0]) / (2 * step), (out[0][1] - out[1][1]) / (2 * step)
+        assert np.linalg.norm(cs) > 0, case
+        assert np.linalg.norm(cs - fd) <= 1e-5 * np.linalg.norm(fd), (case, dvar)
+        if o.int_vec_size and np.linalg.norm(ifd) > 0:
+            assert np.linalg.norm(ics - ifd) <= 1e-5 * np.linalg.norm(ifd), (case, dvar)
+
+
+def test_node_load_design_variables():
+    """nodeLoad variables: the applied nodal load is linear in them inside their activity window
+    and absent outside it; getdRelasticdD's load branch is minus the load per unit variable."""
+    m = M.add_node_design_variables(M.hex_block(nx=3, ny=2, nz=2, seed=3), [[5, 9], [12]], M.DCAT_NODE_LOAD,
+                                    component=2, value=3.0, act_time=(0.5, 2.0))
+    o = Oracle(m)
+    f = o.design_node_load(1.0)
+    expect = np.zeros(o.n)
+    for nd, d in ((5, 0), (9, 0), (12, 1)):
+        expect[o.n_dof_index[nd - 1, 1] - 1] += m.d_value[d]
+    assert np.array_equal(f, expect)
+    assert not np.any(o.design_node_load(3.0))
+    dr = o.node_load_drdd(1, 1.0)
+    assert np.allclose(dr, -expect / 3.0 * (np.arange(o.n) != o.n_dof_index[11, 1] - 1), rtol=0, atol=1e-12)
+    assert not np.any(o.node_load_drdd(1, 0.2))
