@@ -24,6 +24,7 @@ ERRORS = {1: "ASTRO_ERR_ARG", 2: "ASTRO_ERR_CUDA", 3: "ASTRO_ERR_UNSUPPORTED", 4
 SOLVER_GMRES_JACOBI_FP64 = 0
 SOLVER_FGMRES_MIXED = 1
 SOLVER_FGMRES_LEARNED = 2
+OPT_BAND_FP64_UPDATE = 3
 
 _LIB = None
 

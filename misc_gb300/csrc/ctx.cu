@@ -1214,6 +1214,10 @@ extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
         krylov_release(ctx);  // recapture the cycles in the chosen form
         return ASTRO_OK;
     }
+    if (option == ASTRO_OPT_BAND_FP64_UPDATE) {
+        ctx->bandFp64Update = value ? 1 : 0;
+        return ASTRO_OK;
+    }
     return set_err(ctx, ASTRO_ERR_ARG, "unknown option");
 }
 

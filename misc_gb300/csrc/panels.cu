@@ -19,8 +19,24 @@
 //   solve     one CTA per (panel, group of up to 8 right-hand sides): forward sweep with unit L,
 //             D^-1, backward sweep with L^T; the eight warps split the band's tiles of a block row
 //             and warp 0 reduces and solves the diagonal tile with shuffles.
-// FP64 throughout: the factor is FP64-pipe bound (n bw^2 / 2 FMA per panel).
+// The trailing tile updates carry almost all of the factor's arithmetic.  GB300 issues FP64 at
+// about 1/64 of its FP32 rate, so by default they run on the tensor cores as an FP64-exact
+// emulation (the error-free splitting of Ozaki, Ogita, Oishi and Rump, "Error-free transformations
+// of matrix multiplication by using fast routines of matrix multiplication and its applications",
+// Numer. Algorithms 59, 2012, with BF16 slices):
+//   * after the tiles L_IJ of block column J are formed, every row of D_J-scaled L_IJ and of L_IJ
+//     is scaled by a power of two 2^e (|row| / 2^e < 1) and cut into kSlices slices of 8 bits,
+//     t_p = trunc(2^(8p) x - ...), integers in [-255, 255] that BF16 holds exactly:
+//     x = sum_p t_p 2^(-8p) + O(2^(-8 kSlices));
+//   * for a tile pair the slice products with the same level l = p + q are summed by BF16 tensor
+//     core MMAs into one FP32 accumulator: every product is an integer below 2^16, 32 of them sum
+//     below 2^21 and at most 7 pairs share a level, so the FP32 sums are exact;
+//   * each output gets sum_l 2^(-8 l) S_l in FP64, scaled by 2^(e_row + e_col): 7 FP64 operations
+//     per output instead of 32 multiply-adds.  With 7 slices the update carries about 56 bits,
+//     beyond FP64's 53.
+// The FP64 update stays available (ASTRO_OPT_BAND_FP64_UPDATE) for comparison.
 #include <cooperative_groups.h>
+#include <cuda_bf16.h>
 
 #include <algorithm>
 #include <chrono>
@@ -39,6 +55,8 @@ constexpr int TT = TB * TB;
 constexpr int kThreads = 256;
 constexpr int kGroups = kThreads / TB;  // warps per CTA
 constexpr int kSolveCols = 8;           // right-hand sides per solve CTA
+constexpr int kSlices = 7;              // 8-bit slices per FP64 value in the emulated tile update
+constexpr int kLevels = kSlices;        // levels l = p + q = 2 .. kSlices + 1 of the slice products
 
 struct PanelMeta {
     long long band;   // first double of the panel's tiles
@@ -64,6 +82,9 @@ struct PanelPlan {
     std::vector<double> work;
     std::vector<int> sched, schedPtr;
     DevBuf d_meta, d_sched, d_schedPtr, d_panelOf, d_pos, d_band, d_status, d_penI, d_penJ, d_penV;
+    DevBuf d_slices, d_sexp;  // per worker: BF16 slices and row scales of one block column's tiles
+    long long sliceStride = 0;
+    int expStride = 0, maxBt = 0;
     int penCount = 0;
     double factorSeconds = 0.0;
 };
@@ -110,12 +131,63 @@ __global__ void k_band_pad(const PanelMeta *__restrict__ meta, double *__restric
     band[tile_off(M, i / TB, 0) + (i % TB) * TB + (i % TB)] = 1.0;
 }
 
-// Blocked band LDL^T, one cluster per panel (the cluster's panels listed in sched).
+// D = A B + D for one m16n8k16 BF16 tile with FP32 accumulation (tensor cores)
+__device__ __forceinline__ void mma_bf16(float d[4], const unsigned a[4], const unsigned b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__device__ __forceinline__ unsigned ld_pair(const uint16_t *p) { return __ldcg(reinterpret_cast<const unsigned *>(p)); }
+
+// Slices of one tile of block column J (tile d, version v: 0 = L D_J, 1 = L) by one warp: lane r
+// takes row r, its power-of-two scale e_r (|row| / 2^e_r < 1) and kSlices 8-bit slices as BF16
+// integers, row-major [r][k] per slice.
+__device__ void split_tile(const double *T, const double (*sL)[TB + 1], int v, uint16_t *S, int *E, int lane) {
+    double x[TB];
+    double mx = 0.0;
+#pragma unroll
+    for (int k = 0; k < TB; ++k) {
+        x[k] = __ldcg(T + k * TB + lane);
+        if (v == 0) x[k] *= sL[k][k];
+        mx = fmax(mx, fabs(x[k]));
+    }
+    int e = 0;
+    if (mx > 0.0) frexp(mx, &e);
+    E[lane] = e;
+#pragma unroll
+    for (int k = 0; k < TB; ++k) x[k] = ldexp(x[k], -e);
+    for (int p = 0; p < kSlices; ++p) {
+        uint16_t *Sp = S + (size_t)p * TT + lane * TB;
+#pragma unroll
+        for (int k = 0; k < TB; k += 2) {
+            const double y0 = x[k] * 256.0, y1 = x[k + 1] * 256.0;
+            const double t0 = trunc(y0), t1 = trunc(y1);
+            x[k] = y0 - t0;
+            x[k + 1] = y1 - t1;
+            const unsigned lo = __bfloat16_as_ushort(__float2bfloat16_rn((float)t0)),
+                           hi = __bfloat16_as_ushort(__float2bfloat16_rn((float)t1));
+            *reinterpret_cast<unsigned *>(Sp + k) = lo | (hi << 16);
+        }
+    }
+}
+
+// Blocked band LDL^T, one cluster per panel (the cluster's panels listed in sched).  TC: the
+// trailing updates as the tensor-core emulation described at the top of the file, with the
+// slices of each worker (cluster) in slices + worker * sliceStride and their scales in
+// sexp + worker * expStride.
+template <bool TC>
 __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restrict__ meta, const int *__restrict__ sched,
-                                                       const int *__restrict__ schedPtr, double *band, int *status) {
+                                                       const int *__restrict__ schedPtr, double *band, int *status,
+                                                       uint16_t *slices, int *sexp, long long sliceStride,
+                                                       int expStride) {
     cg::cluster_group cl = cg::this_cluster();
     const int crank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
     const int worker = blockIdx.x / cs;
+    uint16_t *wsl = TC ? slices + (size_t)worker * sliceStride : nullptr;
+    int *wex = TC ? sexp + (size_t)worker * expStride : nullptr;
     __shared__ double sL[TB][TB + 1];  // diagonal tile: L below the diagonal, D on it
     __shared__ double sA[TB][TB + 1], sB[TB][TB + 1];
     const int t = threadIdx.x;
@@ -164,8 +236,80 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
             // every CTA has read the unfactored diagonal tile: store the factored one
             if (crank == 0)
                 for (int e = t; e < TT; e += kThreads) __stcg(Td + e, sL[e % TB][e / TB]);
-            // C. trailing update of the band: tile (J+e, d-e) -= L_{J+d,J} D_J L_{J+e,J}^T, 1 <= e <= d
             const int nt = M.bt * (M.bt + 1) / 2;
+            if (TC) {
+                // B2. slices of the tiles below the diagonal (versions L D_J and L), one warp each
+                const int lane = t & 31, wg = crank * kGroups + (t >> 5);
+                for (int uu = wg; uu < 2 * M.bt; uu += cs * kGroups) {
+                    const int d = 1 + uu / 2, v = uu % 2;
+                    if (J + d >= M.nbc) continue;
+                    split_tile(band + tile_off(M, J, d), sL, v, wsl + (size_t)uu * kSlices * TT, wex + uu * TB, lane);
+                }
+                __threadfence();
+                cl.sync();
+                // C. trailing update, tensor cores: warp w computes the 16 x 8 block (mi, ni) of the
+                // 32 x 32 tile, every level l of the slice products in its own FP32 accumulator
+                const int w = t >> 5, g = lane >> 2, tg = lane & 3, mi = w >> 2, ni = w & 3;
+                for (int u = crank; u < nt; u += cs) {
+                    int d = 1, rem = u;
+                    while (rem >= d) {
+                        rem -= d;
+                        ++d;
+                    }
+                    const int e = 1 + rem;
+                    if (J + d >= M.nbc) continue;
+                    const uint16_t *SA = wsl + (size_t)(2 * (d - 1)) * kSlices * TT;
+                    const uint16_t *SB = wsl + (size_t)(2 * (e - 1) + 1) * kSlices * TT;
+                    unsigned a[kSlices][2][4], b[kSlices][2][2];
+                    const int ra = (16 * mi + g) * TB, rb = (8 * ni + g) * TB;
+#pragma unroll
+                    for (int p = 0; p < kSlices; ++p)
+#pragma unroll
+                        for (int ks = 0; ks < 2; ++ks) {
+                            const uint16_t *pa = SA + (size_t)p * TT + 16 * ks + 2 * tg;
+                            const uint16_t *pb = SB + (size_t)p * TT + 16 * ks + 2 * tg;
+                            a[p][ks][0] = ld_pair(pa + ra);
+                            a[p][ks][1] = ld_pair(pa + ra + 8 * TB);
+                            a[p][ks][2] = ld_pair(pa + ra + 8);
+                            a[p][ks][3] = ld_pair(pa + ra + 8 * TB + 8);
+                            b[p][ks][0] = ld_pair(pb + rb);
+                            b[p][ks][1] = ld_pair(pb + rb + 8);
+                        }
+                    float acc[kLevels][4];
+#pragma unroll
+                    for (int li = 0; li < kLevels; ++li)
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) acc[li][i] = 0.f;
+#pragma unroll
+                    for (int li = 0; li < kLevels; ++li) {  // level l = li + 2 = p + q
+#pragma unroll
+                        for (int p = 1; p <= kSlices; ++p) {
+                            const int q = li + 2 - p;
+                            if (q < 1 || q > kSlices) continue;
+#pragma unroll
+                            for (int ks = 0; ks < 2; ++ks) mma_bf16(acc[li], a[p - 1][ks], b[q - 1][ks]);
+                        }
+                    }
+                    double *Tt = band + tile_off(M, J + e, d - e);
+                    const int *EA = wex + 2 * (d - 1) * TB, *EB = wex + (2 * (e - 1) + 1) * TB;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const int rr = 16 * mi + g + (i >> 1) * 8, cc = 8 * ni + 2 * tg + (i & 1);
+                        double sum = 0.0, sc = 1.0 / 65536.0;  // 2^(-8 l), l = 2 ..
+#pragma unroll
+                        for (int li = 0; li < kLevels; ++li) {
+                            sum += (double)acc[li][i] * sc;
+                            sc *= 1.0 / 256.0;
+                        }
+                        double *pt = Tt + cc * TB + rr;
+                        __stcg(pt, __ldcg(pt) - ldexp(sum, __ldcg(EA + rr) + __ldcg(EB + cc)));
+                    }
+                }
+                __threadfence();
+                cl.sync();
+                continue;
+            }
+            // C. trailing update of the band: tile (J+e, d-e) -= L_{J+d,J} D_J L_{J+e,J}^T, 1 <= e <= d
             for (int u = crank; u < nt; u += cs) {
                 int d = 1, rem = u;
                 while (rem >= d) {
@@ -435,7 +579,7 @@ int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        if (cudaOccupancyMaxActiveClusters(&maxClusters, k_band_ldl, &cfg) != cudaSuccess) {
+        if (cudaOccupancyMaxActiveClusters(&maxClusters, k_band_ldl<true>, &cfg) != cudaSuccess) {
             cudaGetLastError();
             maxClusters = 0;
         }
@@ -462,7 +606,15 @@ int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
         L.sched.insert(L.sched.end(), l.begin(), l.end());
         L.schedPtr.push_back((int)L.sched.size());
     }
+    // slice scratch of the tensor-core trailing update, one block column's tiles per worker
+    L.maxBt = 0;
+    for (const PanelMeta &M : L.meta) L.maxBt = std::max(L.maxBt, M.bt);
+    L.sliceStride = 2LL * std::max(L.maxBt, 1) * kSlices * TT;
+    L.expStride = 2 * std::max(L.maxBt, 1) * TB;
     int rc;
+    if ((rc = dev_alloc(ctx, L.d_slices, sizeof(uint16_t) * (size_t)L.sliceStride * L.workers)) ||
+        (rc = dev_alloc(ctx, L.d_sexp, sizeof(int) * (size_t)L.expStride * L.workers)))
+        return rc;
     if ((rc = upload(ctx, L.d_meta, L.meta.data(), sizeof(PanelMeta) * np)) ||
         (rc = upload(ctx, L.d_sched, L.sched.data(), sizeof(int) * L.sched.size())) ||
         (rc = upload(ctx, L.d_schedPtr, L.schedPtr.data(), sizeof(int) * L.schedPtr.size())) ||
@@ -475,7 +627,7 @@ int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
 
 void plan_free(PanelPlan *L) {
     DevBuf *b[] = {&L->d_meta, &L->d_sched, &L->d_schedPtr, &L->d_panelOf, &L->d_pos, &L->d_band,
-                   &L->d_status, &L->d_penI,  &L->d_penJ,     &L->d_penV};
+                   &L->d_status, &L->d_penI,  &L->d_penJ,     &L->d_penV,  &L->d_slices, &L->d_sexp};
     for (DevBuf *x : b) dev_free(*x);
 }
 
@@ -556,9 +708,16 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    CK(cudaLaunchKernelEx(&cfg, k_band_ldl, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
-                          (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
-                          dptr<double>(L->d_band), dptr<int>(L->d_status)));
+    if (ctx->bandFp64Update)
+        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<false>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+                              (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
+                              dptr<double>(L->d_band), dptr<int>(L->d_status), (uint16_t *)nullptr, (int *)nullptr,
+                              0LL, 0));
+    else
+        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<true>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+                              (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
+                              dptr<double>(L->d_band), dptr<int>(L->d_status), dptr<uint16_t>(L->d_slices),
+                              dptr<int>(L->d_sexp), L->sliceStride, L->expStride));
     int status = 0;
     CK(cudaMemcpyAsync(&status, L->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
