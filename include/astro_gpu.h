@@ -489,6 +489,45 @@ int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *opts, const doub
                       const double *load_amplitude, double *disp, double *vel, double *acc,
                       double *int_disp, double *disp_history, astro_solve_stats *stats);
 
+/* ---- batched linear Newmark: many load cases through one factorisation ------------------
+ * The dynamic branch of solve with linear geometry (Working/AStrO_commandFunctions.f90:770-812:
+ * getElasticSolnLoad(1) with the dynamic flag, scaleElasticMPC, getSparseLDLFact of K_eff once,
+ * then per step stepSolve and the Newmark update of :796-799) for num_cases load histories
+ * f_k(t_j) = amplitudes[k * num_steps + j] * patterns[k * n + :] at once.  K (static) and
+ * K_eff = K + c1 c2 M (dynamic) are assembled at the zero state, condensed over the internal DOF;
+ * K_eff + C^T C is factored once by the band LDL^T (astro_panels_factor's kernels, tensor-core
+ * trailing updates), and every step solves all cases in one launch, the step captured as a CUDA
+ * graph and launched num_steps times without a host round trip.  The residual of a step is that
+ * of the linearised element equations, r = f - K u - M a_pred - C^T (C u - rhs) (a_pred: the
+ * acceleration at the start of the step); the reference's elements carry Green-Lagrange strain
+ * and finite rotations at every state, so the two loops differ by the geometric nonlinearity of
+ * the motion (and, for shells, only with the consistent tangent ASTRO_OPT_SHELL_MEAN_ROT_TERM do
+ * they agree).  disp, vel, acc: num_cases x n, the initial state in, the final state out;
+ * disp_history: num_steps x num_cases x n or NULL.  Leaves K_eff in the context's FP64 matrix
+ * and its factorisation in the panel plan. */
+#define ASTRO_NMC_FACTORED 0
+typedef struct astro_newmark_cases_opts {
+    int32_t num_steps, num_cases;
+    double del_t, nm_beta, nm_gamma;
+    int32_t method;    /* ASTRO_NMC_FACTORED */
+    int32_t no_graph;  /* 1: launch the step's kernels directly every step (no CUDA graph) */
+} astro_newmark_cases_opts;
+typedef struct astro_newmark_cases_info {
+    double factor_seconds;     /* band fill + LDL^T (host clock around the launch) */
+    double prepare_seconds;    /* uploads, both assemblies, scaling, factorisation, band copies */
+    double step_seconds;       /* CUDA events around the num_steps step launches */
+    double last_rel_residual;  /* max over cases of ||(K_eff + C^T C) du - r|| / ||r||, last step, FP64 */
+    int64_t band_bytes;        /* FP64 band of the factor */
+    int64_t df_band_bytes;     /* double-float band copies of the many-column solve */
+    int32_t bandwidth;         /* lower bandwidth (DOF) of the ordering */
+    int32_t panels;            /* connected components */
+    int32_t graph_nodes;       /* nodes of the captured step */
+    int32_t kernels_per_step;  /* kernel launches of one step */
+} astro_newmark_cases_info;
+int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opts *opts, const double *patterns,
+                        const double *amplitudes, double *disp, double *vel, double *acc, double *disp_history,
+                        astro_newmark_cases_info *info);
+
 /* y = (K + C^T C) x for host vectors in global DOF numbering, with the device-resident K
  * (kind 64: FP64 values from astro_el_soln_load, 32: FP32 values from astro_assemble_fp32) and
  * the scaled constraints; the operator of the gMRes matvec (Working/AStrO_solvers.f90:143-169). */

@@ -134,6 +134,21 @@ class NewmarkOptsC(C.Structure):
                 ("precond", C.POINTER(PrecondC))]
 
 
+class NewmarkCasesOptsC(C.Structure):
+    _fields_ = [("num_steps", C.c_int32), ("num_cases", C.c_int32), ("del_t", C.c_double), ("nm_beta", C.c_double),
+                ("nm_gamma", C.c_double), ("method", C.c_int32), ("no_graph", C.c_int32)]
+
+
+class NewmarkCasesInfoC(C.Structure):
+    _fields_ = [("factor_seconds", C.c_double), ("prepare_seconds", C.c_double), ("step_seconds", C.c_double),
+                ("last_rel_residual", C.c_double), ("band_bytes", C.c_int64), ("df_band_bytes", C.c_int64),
+                ("bandwidth", C.c_int32), ("panels", C.c_int32), ("graph_nodes", C.c_int32),
+                ("kernels_per_step", C.c_int32)]
+
+
+NMC_FACTORED = 0
+
+
 def lib_path():
     """The in-tree library; with ASTRO_BOUNDS_CHECK=1 in the environment, the checked build
     (device index guards that return ASTRO_ERR_BOUNDS instead of touching memory out of bounds)."""
@@ -193,6 +208,8 @@ def load_library():
         "astro_update_external_rhs": ([vp, F64P, F64P], C.c_int),
         "astro_newmark_run": ([vp, C.POINTER(NewmarkOptsC), F64P, F64P, F64P, F64P, F64P, F64P, F64P,
                                C.POINTER(SolveStatsC)], C.c_int),
+        "astro_newmark_cases": ([vp, C.POINTER(NewmarkCasesOptsC), F64P, F64P, F64P, F64P, F64P, F64P,
+                                 C.POINTER(NewmarkCasesInfoC)], C.c_int),
         "astro_update_internal_soln": ([vp, F64P, F64P, F64P], C.c_int),
         "astro_precond_init": ([C.c_int32, C.c_double, C.c_int32, C.POINTER(PrecondC)], C.c_int),
         "astro_precond_lambda": ([vp, C.c_int32, F64P], C.c_int),
@@ -554,6 +571,26 @@ class AstroGPU:
         self._check(self.L.astro_newmark_run(self.h, C.byref(o), pat, amp, _d(u), _d(v), _d(a), _d(iu),
                                              _d(hist) if history else None, C.byref(st)))
         return u, v, a, iu[:ni], hist, st
+
+    def newmark_cases(self, del_t, patterns, amplitudes, beta=0.25, gamma=0.5, disp=None, vel=None, acc=None,
+                      history=False, graph=True, method=NMC_FACTORED):
+        """Batched linear Newmark (astro_newmark_cases): patterns (cases, n), amplitudes (cases,
+        steps) in global DOF numbering; returns (disp, vel, acc, history or None, info), states
+        (cases, n), history (steps, cases, n)."""
+        P = np.ascontiguousarray(patterns, dtype=np.float64)
+        Am = np.ascontiguousarray(amplitudes, dtype=np.float64)
+        nc, n = P.shape
+        steps = Am.shape[1]
+        assert n == self.n and Am.shape[0] == nc
+        u = np.zeros((nc, n)) if disp is None else np.ascontiguousarray(disp, dtype=np.float64).copy()
+        v = np.zeros((nc, n)) if vel is None else np.ascontiguousarray(vel, dtype=np.float64).copy()
+        a = np.zeros((nc, n)) if acc is None else np.ascontiguousarray(acc, dtype=np.float64).copy()
+        hist = np.zeros((steps, nc, n)) if history else None
+        o = NewmarkCasesOptsC(steps, nc, del_t, beta, gamma, method, 0 if graph else 1)
+        info = NewmarkCasesInfoC()
+        self._check(self.L.astro_newmark_cases(self.h, C.byref(o), _d(P), _d(Am), _d(u), _d(v), _d(a),
+                                               _d(hist) if history else None, C.byref(info)))
+        return u, v, a, hist, info
 
     def getdRelasticdD(self, dvar, h=1e-14, state=None):
         """Complex-step dRu/dd of design variable dvar: (global DOF vector, internal-DOF vector)."""

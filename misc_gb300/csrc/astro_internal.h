@@ -194,6 +194,11 @@ int shell4_update_external_rhs(astro_ctx *ctx, const double *d_intVec, double *d
 int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_intSoln,
                                 const double *d_intRhs);                                           // elem_shell4.cu
 void panels_release(astro_ctx *ctx);                                         // panels.cu
+int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes);         // panels.cu
+int ensure_K(astro_ctx *ctx, int which);          // device BSR value arrays (ctx.cu)
+int ensure_io(astro_ctx *ctx, bool exportMat);    // host-vector staging buffers (ctx.cu)
+int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s);      // panels.cu
+void panels_shape(astro_ctx *ctx, int *np, int *bw, long long *bandBytes, double *factorSeconds);
 void thermal_release(astro_ctx *ctx);                                        // thermal.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu
 int export_csr_dev(astro_ctx *ctx, cudaStream_t s, double *d_mat, int *d_cols);  // assemble.cu

@@ -26,10 +26,11 @@ int set_err(astro_ctx *c, int code, const std::string &msg) {
 // as ASTRO_ERR_BOUNDS; the word is cleared for the next launch.
 int guard_status(astro_ctx *c, const char *what) {
     int site = 0;
-    cudaError_t e = cudaMemcpy(&site, c->d_guard.p, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaError_t e = cudaMemcpyAsync(&site, c->d_guard.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_check(c, e, what);
     if (!site) return ASTRO_OK;
-    cudaMemset(c->d_guard.p, 0, sizeof(int));
+    cudaMemsetAsync(c->d_guard.p, 0, sizeof(int), c->stream);
     return set_err(c, ASTRO_ERR_BOUNDS, std::string(what) + ": index guard " + std::to_string(site) + " failed");
 }
 
@@ -61,7 +62,10 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
     int rc = dev_alloc(c, b, bytes);
     if (rc) return rc;
     if (bytes) {
-        cudaError_t e = cudaMemcpy(b.p, h, bytes, cudaMemcpyHostToDevice);
+        // on the context's (non-blocking) stream, then waited for: a copy on the legacy stream is
+        // not ordered before the kernels that read it
+        cudaError_t e = cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
         if (e != cudaSuccess) return cuda_check(c, e, "upload");
     }
     return ASTRO_OK;
@@ -369,7 +373,7 @@ extern "C" int astro_get_prep(const astro_ctx *ctx, int32_t *current_rank, int32
     return ASTRO_OK;
 }
 
-static int ensure_K(astro_ctx *ctx, int which) {
+int ensure_K(astro_ctx *ctx, int which) {
     const size_t nv = (size_t)ctx->P.nb * ctx->P.dpn * ctx->P.dpn;
     int rc;
     if ((which & 2) && !ctx->d_K64.p && (rc = dev_alloc(ctx, ctx->d_K64, nv * sizeof(double)))) return rc;
@@ -429,7 +433,7 @@ static int elem_state(astro_ctx *ctx, const astro_state *state, DevState &S, Ele
 }
 
 // Persistent device buffers of the getElasticSolnLoad boundary, allocated on first use.
-static int ensure_io(astro_ctx *ctx, bool exportMat) {
+int ensure_io(astro_ctx *ctx, bool exportMat) {
     const AstroPrep &P = ctx->P;
     int rc;
     if (!ctx->d_ioRef.p && (rc = dev_alloc(ctx, ctx->d_ioRef, sizeof(double) * P.n))) return rc;
@@ -485,9 +489,12 @@ extern "C" int astro_el_soln_load(astro_ctx *ctx, int32_t build_mat, const astro
         else
             rc = launch_shell4_assemble(ctx, ds, dl, il.p ? dptr<double>(il) : nullptr, build_mat == 1, nullptr,
                                         nullptr);
-        if (!rc && il.p)
-            rc = cuda_check(ctx, cudaMemcpy(int_elastic_load, il.p, sizeof(double) * P.intVecSize, cudaMemcpyDeviceToHost),
-                            "int load download");
+        if (!rc && il.p) {
+            cudaError_t e = cudaMemcpyAsync(int_elastic_load, il.p, sizeof(double) * P.intVecSize,
+                                            cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            rc = cuda_check(ctx, e, "int load download");
+        }
         dev_free(il);
     }
     if (rc) {
@@ -894,13 +901,13 @@ extern "C" int astro_element_matrices(astro_ctx *ctx, int32_t precision, const a
     if (ru_out && (rc = dev_alloc(ctx, dr, sizeof(double) * 24 * (size_t)P.E))) return rc;
     DevState S;
     if (state && state->node_disp && (rc = state_vec_up(ctx, state->node_disp, S.disp))) return rc;
+    // the previous step's state, as the global load does: the shell kinematics and the Newmark
+    // inertia of either element family read it
+    if (state && (ctx->hasShell || state->dynamic) &&
+        ((rc = state_vec_up(ctx, state->prev_disp, S.pdisp)) || (rc = state_vec_up(ctx, state->prev_vel, S.pvel)) ||
+         (rc = state_vec_up(ctx, state->prev_acc, S.pacc))))
+        return rc;
     if (ctx->hasSolid) {
-        if (state && (state->dynamic || ctx->has81)) {
-            if ((state->dynamic && ((rc = state_vec_up(ctx, state->prev_disp, S.pdisp)) ||
-                                    (rc = state_vec_up(ctx, state->prev_vel, S.pvel)) ||
-                                    (rc = state_vec_up(ctx, state->prev_acc, S.pacc)))))
-                return rc;
-        }
         ElemDevState ds;
         if ((rc = elem_state(ctx, state, S, ds))) return rc;
         if (precision == 32) {
@@ -1071,7 +1078,7 @@ extern "C" int astro_surface_load(astro_ctx *ctx, int32_t nfaces, const int32_t 
     for (int f = 0; f < nfaces; ++f) {
         int e = face_el[f], fn = face_num[f];
         if (e < 1 || e > P.E) return set_err(ctx, ASTRO_ERR_ARG, "face element out of range");
-        int nfmax = ctx->etype[e - 1] == 8 ? 6 : 2;
+        int nfmax = (ctx->etype[e - 1] == 8 || ctx->etype[e - 1] == 81) ? 6 : 2;
         if (fn < 1 || fn > nfmax) return set_err(ctx, ASTRO_ERR_ARG, "face number out of range");
     }
     double tr[3] = {0, 0, 0};

@@ -45,6 +45,7 @@
 #include <vector>
 
 #include "astro_internal.h"
+#include "dfloat.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -87,6 +88,10 @@ struct PanelPlan {
     int expStride = 0, maxBt = 0;
     int penCount = 0;
     double factorSeconds = 0.0;
+    // double-float copies for the many-column solve (k_band_solve_cases), built from factor
+    // generation dfGen; the items and the right-hand-side block for casesCols columns
+    int factorGen = 0, dfGen = -1, casesCols = 0, ring = 0;
+    DevBuf d_Lf, d_Lb, d_Wf, d_Wb, d_Dinv, d_items, d_X;
 };
 
 __device__ __forceinline__ size_t tile_off(const PanelMeta &M, int J, int d) {
@@ -453,6 +458,201 @@ __global__ void __launch_bounds__(kThreads) k_band_solve(const PanelMeta *__rest
     }
 }
 
+// ---- many right-hand sides of one large band: the time-stepping solve ----------------------
+//
+// k_band_solve gives a (panel, group of columns) to one CTA, which suits many small panels.  A
+// single large band (a model's K_eff, factored once and solved at every time step) is instead a
+// chain of nbc dependent block rows per sweep, and FP64 runs at about 1/64 of the FP32 rate: one
+// CTA per column would spend tens of microseconds per block row.  So each (panel, column) gets a
+// cluster of kCS CTAs and the arithmetic runs in double-float on the FP32 pipe:
+//   * producer CTAs (ranks 1 .. kCS-1), one warp per tile: for block row I they form
+//     sum_{d >= 2} L_{I,I-d} y_{I-d} from the solved rows in their shared-memory ring, reduce it
+//     across the CTA and store it into the leader's shared memory (distributed shared memory);
+//   * the leader (rank 0) forms L_{I,I-1} y_{I-1} from the row it solved last, waits at the
+//     cluster barrier, subtracts the partials from b_I and applies W_I = L_II^-1 (inverted once
+//     after the factorisation): y_I = W_I (b_I - ...), pushed into every CTA's ring;
+//   * one cluster barrier per block row (release / acquire orders the stores into distributed
+//     shared memory); the producers run one row ahead of the leader (their tiles need rows
+//     up to I - 2 only);
+//   * backward sweep the same with L^T (transposed copies of the tiles and of W) on D^-1 y.
+// The band is copied once into double-float tiles in the forward (column-major) and backward
+// (row-major) layouts, so every tile load of a warp is 32 consecutive float2 per k.
+constexpr int kCS = 4;   // CTAs per cluster
+constexpr int kCW = 8;   // warps per CTA
+constexpr int kProdWarps = (kCS - 1) * kCW;
+constexpr int kPrepW = 4;  // warps per CTA of the band copy
+
+struct CaseItem {
+    int panel, col;
+};
+
+// DF copies of the band: off-diagonal tiles as they are (Lf) and transposed (Lb); per block
+// column W = L_JJ^-1 (unit lower) in both layouts and D^-1, one warp per block column
+__global__ void k_band_dfprep(const PanelMeta *__restrict__ meta, int np, const double *__restrict__ band,
+                              float2 *__restrict__ Lf, float2 *__restrict__ Lb, float2 *__restrict__ Wf,
+                              float2 *__restrict__ Wb, float2 *__restrict__ Dinv) {
+    __shared__ double sT[kPrepW][TB][TB + 1];
+    const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
+    // global block-column index over all panels
+    long long gJ = (long long)blockIdx.x * kPrepW + w;
+    int p = 0;
+    for (; p < np; ++p) {
+        if (gJ < meta[p].nbc) break;
+        gJ -= meta[p].nbc;
+    }
+    if (p >= np) return;
+    const PanelMeta M = meta[p];
+    const int J = (int)gJ;
+    for (int d = 1; d <= M.bt; ++d) {
+        if (J + d >= M.nbc) break;
+        const size_t o = tile_off(M, J, d);
+        for (int e = lane; e < TT; e += 32) {
+            const DF v = df_from_double(band[o + e]);
+            Lf[o + e] = make_float2(v.hi, v.lo);
+            sT[w][e % TB][e / TB] = band[o + e];  // [row][col]
+        }
+        __syncwarp();
+        // Lb[k * TB + r] = L[k][r]
+        for (int e = lane; e < TT; e += 32) {
+            const DF v = df_from_double(sT[w][e / TB][e % TB]);
+            Lb[o + e] = make_float2(v.hi, v.lo);
+        }
+        __syncwarp();
+    }
+    const size_t od = tile_off(M, J, 0);
+    for (int e = lane; e < TT; e += 32) sT[w][e % TB][e / TB] = band[od + e];
+    __syncwarp();
+    // column `lane` of W: L w = e_lane by forward substitution (unit diagonal)
+    double x[TB];
+#pragma unroll
+    for (int i = 0; i < TB; ++i) {
+        double v = (i == lane) ? 1.0 : 0.0;
+#pragma unroll
+        for (int k = 0; k < i; ++k) v -= sT[w][i][k] * x[k];
+        x[i] = v;
+    }
+    const size_t ow = (size_t)M.xUnit * TB + (size_t)J * TT;
+#pragma unroll
+    for (int i = 0; i < TB; ++i) {
+        const DF v = df_from_double(x[i]);  // W[i][lane]
+        Wf[ow + (size_t)lane * TB + i] = make_float2(v.hi, v.lo);  // column-major: W[i][k] at k*TB + i
+        Wb[ow + (size_t)i * TB + lane] = make_float2(v.hi, v.lo);  // row-major:    W[i][k] at i*TB + k
+    }
+    const DF dv = df_from_double(1.0 / sT[w][lane][lane]);
+    Dinv[(size_t)M.xUnit + (size_t)J * TB + lane] = make_float2(dv.hi, dv.lo);
+}
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// acc[r] += sum_{k in [k0, k1)} T[k * TB + r] v[k] (T a DF tile in global memory, v in shared)
+__device__ __forceinline__ void df_tile_rows(DF &acc, const float2 *__restrict__ T, const float2 *v, int r, int k0,
+                                             int k1) {
+    DF a2 = {0.f, 0.f};
+    int k = k0;
+    for (; k + 1 < k1; k += 2) {
+        const float2 l0 = __ldg(T + k * TB + r), l1 = __ldg(T + (k + 1) * TB + r);
+        const float2 y0 = v[k], y1 = v[k + 1];
+        df_acc(acc, l0.x, l0.y, y0.x, y0.y);
+        df_acc(a2, l1.x, l1.y, y1.x, y1.y);
+    }
+    if (k < k1) {
+        const float2 l0 = __ldg(T + k * TB + r);
+        const float2 y0 = v[k];
+        df_acc(acc, l0.x, l0.y, y0.x, y0.y);
+    }
+    acc = df_add(df_norm(acc), df_norm(a2));
+}
+
+__global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMeta *__restrict__ meta,
+                                                               const CaseItem *__restrict__ items,
+                                                               const float2 *__restrict__ Lf,
+                                                               const float2 *__restrict__ Lb,
+                                                               const float2 *__restrict__ Wf,
+                                                               const float2 *__restrict__ Wb,
+                                                               const float2 *__restrict__ Dinv, double *X, int nrhs,
+                                                               int ring) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    extern __shared__ float2 smf[];
+    float2 *sRing = smf;                           // [ring][TB]: solved rows
+    float2 *sRed = sRing + (size_t)ring * TB;      // [kCW][TB]: per-warp partials
+    float2 *sPart = sRed + kCW * TB;               // [2][kCS][TB]: CTA partials (leader)
+    float2 *sV = sPart + 2 * kCS * TB;             // [TB]
+    const CaseItem it = items[blockIdx.x / kCS];
+    const PanelMeta M = meta[it.panel];
+    const int w = threadIdx.x / 32, r = threadIdx.x % 32;
+    const int nbc = M.nbc, bt = M.bt;
+    double *Xp = X + (size_t)M.xUnit * nrhs + (size_t)it.col * nbc * TB;
+    const size_t wOff = (size_t)M.xUnit * TB;
+    float2 *leaderPart = cl.map_shared_rank(sPart, 0);
+    for (int sweep = 0; sweep < 2; ++sweep) {
+        const float2 *Lt = sweep == 0 ? Lf : Lb;
+        const float2 *Wt = sweep == 0 ? Wf : Wb;
+        for (int q = 0; q < nbc; ++q) {
+            const int I = sweep == 0 ? q : nbc - 1 - q;                 // block row solved now
+            const int dmax = sweep == 0 ? min(bt, I) : min(bt, nbc - 1 - I);
+            // tile (source row, d): forward L_{I,I-d} = tile (I-d, d); backward L_{I+d,I}^T = tile (I, d)
+            auto tile = [&](int d) { return Lt + tile_off(M, sweep == 0 ? I - d : I, d); };
+            auto src = [&](int d) { return sweep == 0 ? I - d : I + d; };
+            __syncthreads();  // the leader's last row is in its ring
+            if (rank > 0) {
+                DF acc = {0.f, 0.f};
+                for (int d = 2 + (rank - 1) * kCW + w; d <= dmax; d += kProdWarps)
+                    df_tile_rows(acc, tile(d), sRing + (size_t)(src(d) % ring) * TB, r, 0, TB);
+                sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
+                __syncthreads();
+                if (w == 0) {
+                    DF s = {0.f, 0.f};
+                    for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                    leaderPart[((q & 1) * kCS + rank) * TB + r] = make_float2(s.hi, s.lo);
+                }
+                cluster_barrier();
+            } else {
+                // L_{I,I+-1} times the row solved last, split over the warps by k
+                DF acc = {0.f, 0.f};
+                if (dmax >= 1) df_tile_rows(acc, tile(1), sRing + (size_t)(src(1) % ring) * TB, r, 4 * w, 4 * w + 4);
+                sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
+                cluster_barrier();
+                if (w == 0) {
+                    const double b = Xp[(size_t)I * TB + r];
+                    DF v = df_from_double(b);
+                    if (sweep == 1) {
+                        const float2 di = Dinv[M.xUnit + (size_t)I * TB + r];
+                        v = df_mul(v, DF{di.x, di.y});
+                    }
+                    DF s = {0.f, 0.f};
+                    for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                    for (int c = 1; c < kCS; ++c) {
+                        const float2 pc = sPart[((q & 1) * kCS + c) * TB + r];
+                        s = df_add(s, DF{pc.x, pc.y});
+                    }
+                    v = df_sub(v, s);
+                    sV[r] = make_float2(v.hi, v.lo);
+                }
+                __syncthreads();
+                // y_I = W v (forward) or x_I = W^T v (backward), split over the warps by k
+                DF a = {0.f, 0.f};
+                df_tile_rows(a, Wt + wOff + (size_t)I * TT, sV, r, 4 * w, 4 * w + 4);
+                sRed[w * TB + r] = make_float2(a.hi, a.lo);
+                __syncthreads();
+                if (w == 0) {
+                    DF y = {0.f, 0.f};
+                    for (int k = 0; k < kCW; ++k) y = df_add(y, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                    const float2 yv = make_float2(y.hi, y.lo);
+                    const size_t slot = (size_t)(I % ring) * TB + r;
+                    for (int c = 0; c < kCS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
+                    Xp[(size_t)I * TB + r] = df_to_double(y);
+                }
+            }
+        }
+        // the sweep's last rows are pushed before any CTA starts the next sweep or exits
+        cluster_barrier();
+    }
+}
+
 // internal-layout columns (nrhs x n) <-> the padded panel layout
 __global__ void k_panel_move(int n, int dpn, int nrhs, double *__restrict__ vec, const int *__restrict__ panelOf,
                              const int *__restrict__ pos, const PanelMeta *__restrict__ meta, double *__restrict__ X,
@@ -626,8 +826,10 @@ int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
 }
 
 void plan_free(PanelPlan *L) {
-    DevBuf *b[] = {&L->d_meta, &L->d_sched, &L->d_schedPtr, &L->d_panelOf, &L->d_pos, &L->d_band,
-                   &L->d_status, &L->d_penI,  &L->d_penJ,     &L->d_penV,  &L->d_slices, &L->d_sexp};
+    DevBuf *b[] = {&L->d_meta,  &L->d_sched, &L->d_schedPtr, &L->d_panelOf, &L->d_pos,  &L->d_band,
+                   &L->d_status, &L->d_penI, &L->d_penJ,     &L->d_penV,    &L->d_slices, &L->d_sexp,
+                   &L->d_Lf,    &L->d_Lb,    &L->d_Wf,       &L->d_Wb,      &L->d_Dinv,  &L->d_items,
+                   &L->d_X};
     for (DevBuf *x : b) dev_free(*x);
 }
 
@@ -725,6 +927,7 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
     L->kVersion = ctx->k64Version;
     L->penVersion = ctx->penVersion;
     L->factored = status == 0;
+    L->factorGen++;
     fill_info(*L, info);
     if (status) return set_err(ctx, ASTRO_ERR_PIVOT, "panels: zero or non-finite pivot in panel " + std::to_string(status - 1));
     return ASTRO_OK;
@@ -815,4 +1018,92 @@ extern "C" int astro_panels_solve_batched(astro_ctx *ctx, int32_t num_rhs, const
     if (!L || !L->factored || L->kVersion != ctx->k64Version || L->penVersion != ctx->penVersion)
         if ((rc = astro_panels_factor(ctx, L ? L->cs : 0, info))) return rc;
     return astro_panels_solve(ctx, num_rhs, rhs, x, info);
+}
+
+// ---- the many-column solve of one factorisation (time stepping) ---------------------------
+
+// Prepares k_band_solve_cases for ncols right-hand-side columns of the current factorisation:
+// the double-float band copies (once per factorisation), the (panel, column) items and the
+// panel-layout block.  Allocates; call before any stream capture.
+int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    if (!L || !L->factored || L->kVersion != ctx->k64Version || L->penVersion != ctx->penVersion)
+        return set_err(ctx, ASTRO_ERR_STATE, "panels: no current factorisation (astro_panels_factor)");
+    if (ncols < 1) return set_err(ctx, ASTRO_ERR_ARG, "panels: no right-hand sides");
+    cudaStream_t s = ctx->stream;
+    int rc;
+    if (L->dfGen != L->factorGen) {
+        const size_t nb = (size_t)L->bandDoubles, nd = (size_t)L->xRows;
+        if ((rc = dev_alloc(ctx, L->d_Lf, sizeof(float2) * nb)) || (rc = dev_alloc(ctx, L->d_Lb, sizeof(float2) * nb)) ||
+            (rc = dev_alloc(ctx, L->d_Wf, sizeof(float2) * nd * TB)) ||
+            (rc = dev_alloc(ctx, L->d_Wb, sizeof(float2) * nd * TB)) || (rc = dev_alloc(ctx, L->d_Dinv, sizeof(float2) * nd)))
+            return rc;
+        long long cols = 0;
+        for (const PanelMeta &M : L->meta) cols += M.nbc;
+        k_band_dfprep<<<(unsigned)((cols + kPrepW - 1) / kPrepW), kPrepW * 32, 0, s>>>(
+            dptr<PanelMeta>(L->d_meta), L->np, dptr<double>(L->d_band), dptr<float2>(L->d_Lf), dptr<float2>(L->d_Lb),
+            dptr<float2>(L->d_Wf), dptr<float2>(L->d_Wb), dptr<float2>(L->d_Dinv));
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "band double-float copy"))) return rc;
+        L->dfGen = L->factorGen;
+    }
+    if (L->casesCols != ncols) {
+        std::vector<CaseItem> items;
+        for (int p = 0; p < L->np; ++p)
+            for (int c = 0; c < ncols; ++c) items.push_back({p, c});
+        dev_free(L->d_items);
+        dev_free(L->d_X);
+        if ((rc = upload(ctx, L->d_items, items.data(), sizeof(CaseItem) * items.size())) ||
+            (rc = dev_alloc(ctx, L->d_X, sizeof(double) * (size_t)L->xRows * ncols)))
+            return rc;
+        CK(cudaMemsetAsync(L->d_X.p, 0, sizeof(double) * (size_t)L->xRows * ncols, s));
+        L->casesCols = ncols;
+    }
+    L->ring = L->maxBt + 2;
+    const size_t smem = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * kCS * TB + TB);
+    CK(cudaFuncSetAttribute(k_band_solve_cases, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (bytes) *bytes = 2 * sizeof(float2) * (size_t)L->bandDoubles;
+    return cuda_check(ctx, cudaStreamSynchronize(s), "panels cases prepare");
+}
+
+// x = (K + C^T C)^-1 b for the prepared number of columns, in place in d_vec (ncols x n, internal
+// numbering): moves, one cluster launch, moves.  No allocation, no synchronisation (capturable).
+int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s) {
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    if (!L || L->dfGen != L->factorGen || !L->casesCols) return set_err(ctx, ASTRO_ERR_STATE, "panels: cases not prepared");
+    const AstroPrep &P = ctx->P;
+    const int nc = L->casesCols;
+    const long long mv = (long long)P.n * nc;
+    const unsigned mg = (unsigned)((mv + 255) / 256);
+    k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nc, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
+                                    dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_X), 1);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(L->np * nc * kCS));
+    cfg.blockDim = dim3(kCW * 32);
+    cfg.dynamicSmemBytes = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * kCS * TB + TB);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kCS;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CK(cudaLaunchKernelEx(&cfg, k_band_solve_cases, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+                          (const CaseItem *)dptr<CaseItem>(L->d_items), (const float2 *)dptr<float2>(L->d_Lf),
+                          (const float2 *)dptr<float2>(L->d_Lb), (const float2 *)dptr<float2>(L->d_Wf),
+                          (const float2 *)dptr<float2>(L->d_Wb), (const float2 *)dptr<float2>(L->d_Dinv),
+                          dptr<double>(L->d_X), nc, L->ring));
+    k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nc, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
+                                    dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_X), 0);
+    return cuda_check(ctx, cudaGetLastError(), "panels cases solve");
+}
+
+// Shape of the current plan: panels, largest bandwidth (DOF), band bytes, factor seconds.
+void panels_shape(astro_ctx *ctx, int *np, int *bw, long long *bandBytes, double *factorSeconds) {
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    if (!L) return;
+    if (np) *np = L->np;
+    if (bw) *bw = L->maxBw;
+    if (bandBytes) *bandBytes = L->bandDoubles * (long long)sizeof(double);
+    if (factorSeconds) *factorSeconds = L->factorSeconds;
 }

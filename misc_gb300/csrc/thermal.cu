@@ -747,7 +747,7 @@ extern "C" int astro_thermal_surface_flux(astro_ctx *ctx, int32_t nfaces, const 
     for (int f = 0; f < nfaces; ++f) {
         const int e = face_el[f], fn = face_num[f];
         if (e < 1 || e > P.E) return set_err(ctx, ASTRO_ERR_ARG, "face element out of range");
-        if (fn < 1 || fn > (ctx->etype[e - 1] == 8 ? 6 : 2)) return set_err(ctx, ASTRO_ERR_ARG, "face number out of range");
+        if (fn < 1 || fn > ((ctx->etype[e - 1] == 8 || ctx->etype[e - 1] == 81) ? 6 : 2)) return set_err(ctx, ASTRO_ERR_ARG, "face number out of range");
     }
     if (!nfaces) return ASTRO_OK;
     DevBuf dfe, dfn, del, dL;

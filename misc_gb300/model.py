@@ -314,6 +314,30 @@ def plate_shell(nx=40, ny=8, lx=10.0, ly=2.0, t=0.05, E=7.0e10, nu=0.33, rho=270
     return m
 
 
+def config5_cases(m, n_dof_index, steps, dt, num_random=16, seed0=5000, force=100.0):
+    """Load cases of the Newmark benchmark plate (a square shell4 plate from plate_shell with
+    nx = ny): case 0 the centre force force * sin(2 pi 500 t) on w; cases 1 .. num_random a point
+    force on w at an interior node drawn uniformly (generator seed0 + k), amplitude
+    force * U(0.5, 1.5) * sin(2 pi f t + phi) with f ~ U(200, 800) Hz and phi ~ U(0, 2 pi).
+    Returns patterns (cases, n) and amplitudes (cases, steps), t = dt, 2 dt, ..."""
+    nx = int(round(np.sqrt(m.num_nodes))) - 1
+    n = int(n_dof_index.max())
+    t = dt * np.arange(1, steps + 1)
+    P = np.zeros((num_random + 1, n))
+    A = np.zeros((num_random + 1, steps))
+    centre = (nx // 2) * (nx + 1) + nx // 2 + 1
+    P[0, n_dof_index[centre - 1, 2] - 1] = 1.0
+    A[0] = force * np.sin(2 * np.pi * 500.0 * t)
+    for k in range(1, num_random + 1):
+        rng = np.random.default_rng(seed0 + k)
+        i, j = (int(v) for v in rng.integers(1, nx, 2))
+        nd = j * (nx + 1) + i + 1
+        P[k, n_dof_index[nd - 1, 2] - 1] = 1.0
+        A[k] = force * rng.uniform(0.5, 1.5) * np.sin(2 * np.pi * rng.uniform(200.0, 800.0) * t +
+                                                     rng.uniform(0.0, 2 * np.pi))
+    return P, A
+
+
 def panel_batch(num_panels=512, seed0=1000, n_range=(8, 96), t_range=(0.01, 0.1), p_range=(1.0e2, 1.0e4),
                 n_dvars=32, h=0.1, E=7.0e10, nu=0.33, rho=2700.0, name="panels", indices=None):
     """Batch of independent shell4 panels as one model (its connected components): panel p has
