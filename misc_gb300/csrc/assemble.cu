@@ -100,7 +100,7 @@ __global__ void surface_load_kernel(const double *__restrict__ nodes, const int 
     const int hexF[6][4] = {{4, 3, 2, 1}, {5, 6, 7, 8}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {4, 1, 5, 8}};
     const int shF[2][4] = {{1, 2, 3, 4}, {1, 4, 3, 2}};
     const int el = faceEl[f] - 1, fn = faceNum[f] - 1;
-    const int *fl = (etype[el] == 8) ? hexF[fn] : shF[fn];
+    const int *fl = (etype[el] == 8 || etype[el] == 81) ? hexF[fn] : shF[fn];
     double X[4][3];
     int nd[4];
     for (int k = 0; k < 4; ++k) {

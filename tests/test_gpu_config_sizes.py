@@ -172,7 +172,10 @@ def test_cfg3_panel_subset():
         xr = lu.solve(B[:, c])
         r, r_ref = np.linalg.norm(A @ X[:, c] - B[:, c]), np.linalg.norm(A @ xr - B[:, c])
         assert r <= 10.0 * r_ref + 1e-14 * np.linalg.norm(B[:, c]), (c, r, r_ref)
-        assert np.linalg.norm(X[:, c] - xr) <= 1e-7 * np.linalg.norm(xr), c
+        # forward difference: the thinnest panels (t / h down to 0.1) have condition numbers near
+        # 1e10, so two FP64-accurate factorisations (the residuals above) may differ by ~1e-7
+        # (measured 9e-8 with the FP64 trailing update, 1.2e-7 with the tensor-core one)
+        assert np.linalg.norm(X[:, c] - xr) <= 1e-6 * np.linalg.norm(xr), c
 
 
 def test_cfg4_learned_solution_error():
