@@ -511,6 +511,9 @@ typedef struct astro_newmark_cases_opts {
     double del_t, nm_beta, nm_gamma;
     int32_t method;    /* ASTRO_NMC_FACTORED */
     int32_t no_graph;  /* 1: launch the step's kernels directly every step (no CUDA graph) */
+    int32_t refine;    /* FP64 refinement passes per step (0..4): du -= A^-1 (A du - r) with the
+                          residual over the FP64 assembly; the many-column solve runs in
+                          double-float (about 48 bits), so ill-conditioned K_eff may want one */
 } astro_newmark_cases_opts;
 typedef struct astro_newmark_cases_info {
     double factor_seconds;     /* band fill + LDL^T (host clock around the launch) */

@@ -136,7 +136,7 @@ class NewmarkOptsC(C.Structure):
 
 class NewmarkCasesOptsC(C.Structure):
     _fields_ = [("num_steps", C.c_int32), ("num_cases", C.c_int32), ("del_t", C.c_double), ("nm_beta", C.c_double),
-                ("nm_gamma", C.c_double), ("method", C.c_int32), ("no_graph", C.c_int32)]
+                ("nm_gamma", C.c_double), ("method", C.c_int32), ("no_graph", C.c_int32), ("refine", C.c_int32)]
 
 
 class NewmarkCasesInfoC(C.Structure):
@@ -573,7 +573,7 @@ class AstroGPU:
         return u, v, a, iu[:ni], hist, st
 
     def newmark_cases(self, del_t, patterns, amplitudes, beta=0.25, gamma=0.5, disp=None, vel=None, acc=None,
-                      history=False, graph=True, method=NMC_FACTORED):
+                      history=False, graph=True, method=NMC_FACTORED, refine=0):
         """Batched linear Newmark (astro_newmark_cases): patterns (cases, n), amplitudes (cases,
         steps) in global DOF numbering; returns (disp, vel, acc, history or None, info), states
         (cases, n), history (steps, cases, n)."""
@@ -586,7 +586,7 @@ class AstroGPU:
         v = np.zeros((nc, n)) if vel is None else np.ascontiguousarray(vel, dtype=np.float64).copy()
         a = np.zeros((nc, n)) if acc is None else np.ascontiguousarray(acc, dtype=np.float64).copy()
         hist = np.zeros((steps, nc, n)) if history else None
-        o = NewmarkCasesOptsC(steps, nc, del_t, beta, gamma, method, 0 if graph else 1)
+        o = NewmarkCasesOptsC(steps, nc, del_t, beta, gamma, method, 0 if graph else 1, refine)
         info = NewmarkCasesInfoC()
         self._check(self.L.astro_newmark_cases(self.h, C.byref(o), _d(P), _d(Am), _d(u), _d(v), _d(a),
                                                _d(hist) if history else None, C.byref(info)))

@@ -102,6 +102,11 @@ __global__ void k_nmc_update(long long total, double c1, double c2, double dt, d
 
 __global__ void k_nmc_tick(int *dStep) { *dStep += 1; }
 
+__global__ void k_nmc_sub(long long total, double *__restrict__ D, const double *__restrict__ E) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < total) D[t] -= E[t];
+}
+
 // y = (K_eff + C^T C) x - r for the last step's check, thread per (block row, case)
 template <int DPN>
 __global__ void k_nmc_check(int N, int nc, const int *__restrict__ bRowPtr, const int *__restrict__ bCol,
@@ -147,8 +152,8 @@ struct NmcBufs {
 };
 
 template <int DPN>
-int enqueue_step(astro_ctx *ctx, NmcBufs &B, int nc, int steps, double dt, double beta, double gamma, cudaStream_t s,
-                 int *launches) {
+int enqueue_step(astro_ctx *ctx, NmcBufs &B, int nc, int steps, double dt, double beta, double gamma, int refine,
+                 cudaStream_t s, int *launches) {
     const AstroPrep &P = ctx->P;
     const int N = P.N, n = P.n;
     const double c1 = 0.5 / beta, c2 = 2.0 / (dt * dt);
@@ -162,12 +167,22 @@ int enqueue_step(astro_ctx *ctx, NmcBufs &B, int nc, int steps, double dt, doubl
     CK(cudaMemcpyAsync(B.D.p, B.R.p, sizeof(double) * (size_t)tot, cudaMemcpyDeviceToDevice, s));
     int rc = panels_cases_solve(ctx, dptr<double>(B.D), s);
     if (rc) return rc;
+    // FP64 refinement: du -= A^-1 (A du - r), the residual in FP64 over the assembled values
+    for (int q = 0; q < refine; ++q) {
+        k_nmc_check<DPN><<<(unsigned)((rows + 127) / 128), 128, 0, s>>>(
+            N, nc, dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), dptr<double>(ctx->d_K64), penPtr,
+            dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol), dptr<double>(ctx->d_penVal), dptr<double>(B.D),
+            dptr<double>(B.R), dptr<double>(B.E));
+        if ((rc = panels_cases_solve(ctx, dptr<double>(B.E), s))) return rc;
+        k_nmc_sub<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(tot, dptr<double>(B.D), dptr<double>(B.E));
+    }
     k_nmc_update<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(tot, c1, c2, dt, beta, gamma, dptr<double>(B.U),
                                                                dptr<double>(B.V), dptr<double>(B.A), dptr<double>(B.D),
                                                                B.hist.p ? dptr<double>(B.hist) : nullptr,
                                                                dptr<int>(B.step));
     k_nmc_tick<<<1, 1, 0, s>>>(dptr<int>(B.step));
-    *launches = 6;  // residual, (copy), move, solve, move, update, tick: six kernels
+    // residual, move, solve, move, update, tick; each refinement: check, move, solve, move, sub
+    *launches = 6 + 5 * refine;
     return cuda_check(ctx, cudaGetLastError(), "newmark cases step");
 }
 
@@ -180,6 +195,7 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
         !(o->del_t > 0.0) || !(o->nm_beta > 0.0))
         return ASTRO_ERR_ARG;
     if (o->method != ASTRO_NMC_FACTORED) return set_err(ctx, ASTRO_ERR_ARG, "newmark cases: unknown method");
+    if (o->refine < 0 || o->refine > 4) return set_err(ctx, ASTRO_ERR_ARG, "newmark cases: refine must be 0..4");
     const AstroPrep &P = ctx->P;
     const int n = P.n, nc = o->num_cases, steps = o->num_steps;
     const size_t cn = (size_t)n * nc;
@@ -197,6 +213,7 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
         (rc = dev_alloc(ctx, B.amp, sizeof(double) * (size_t)nc * std::max(steps, 1))))
         return rc;
     if (disp_history && steps > 0 && (rc = dev_alloc(ctx, B.hist, sizeof(double) * cn * steps))) return rc;
+    if ((rc = dev_alloc(ctx, B.E, sizeof(double) * cn))) return rc;
     // per-case vectors, global DOF numbering on the host -> internal numbering
     const double *src[4] = {disp, vel, acc, patterns};
     DevBuf *dst[4] = {&B.U, &B.V, &B.A, &B.P};
@@ -250,8 +267,8 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
     cudaGraphExec_t exec = nullptr;
     const bool useGraph = o->no_graph == 0;
     auto enqueue = [&](cudaStream_t st) {
-        return P.dpn == 3 ? enqueue_step<3>(ctx, B, nc, steps, o->del_t, o->nm_beta, o->nm_gamma, st, &launches)
-                          : enqueue_step<6>(ctx, B, nc, steps, o->del_t, o->nm_beta, o->nm_gamma, st, &launches);
+        return P.dpn == 3 ? enqueue_step<3>(ctx, B, nc, steps, o->del_t, o->nm_beta, o->nm_gamma, o->refine, st, &launches)
+                          : enqueue_step<6>(ctx, B, nc, steps, o->del_t, o->nm_beta, o->nm_gamma, o->refine, st, &launches);
     };
     size_t graphNodes = 0;
     if (useGraph && steps > 0) {
@@ -292,7 +309,6 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
     // the last step's solve against its residual: max over cases of ||A du - r|| / ||r||
     double worst = 0.0;
     if (steps > 0) {
-        if ((rc = dev_alloc(ctx, B.E, sizeof(double) * cn))) return rc;
         const long long rows = (long long)P.N * nc;
         const int *penPtr = ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr;
         if (P.dpn == 3)
