@@ -139,6 +139,32 @@ typedef struct astro_precond {
     double weights[(ASTRO_PRECOND_MAX_DEGREE + 1) * 36];
 } astro_precond;
 
+/* Per-node modulation of the polynomial network: the learned part that sees the model.
+ * Node features f(r), ASTRO_NODE_FEATURES per node, from the assembled A = K + C^T C (no element
+ * data, so any element family): with d_r the mean diagonal entry of node r's diagonal block of K,
+ * l_r = ln d_r and lbar the mean of l over the nodes,
+ *   f0 = l_r - lbar                               (the node's stiffness level)
+ *   f1 = mean over the neighbours c of (l_c - l_r)  (local contrast, e.g. of log E)
+ *   f2 = max over the neighbours of |l_c - l_r|
+ *   f3 = (neighbours + 1) / (most blocks of a row)  (interior, face, edge, corner)
+ *   f4 = ln(1 + p_r / d_r), p_r the mean penalty diagonal of the node's DOF (constraints)
+ *   f5 = ln(sum_{c != r} ||K_rc||_F / ||K_rr||_F)  (diagonal dominance)
+ * A two-layer perceptron maps them to per-node hop scales
+ *   a_k(r) = 1 + b2[k] + sum_h w2[k * hidden + h] tanh(b1[h] + sum_f w1[h * F + f] f_f(r))
+ * and the preconditioner becomes P v = (1/lambda) sum_k a_k(r) (W_k y_k)(r) at every node r.
+ * With w2 = b2 = 0 it is the polynomial network unchanged.  hidden = 0: no modulation.
+ * No counterpart in the reference (whose gMRes is preconditioned by a diagonal). */
+#define ASTRO_NODE_FEATURES 6
+#define ASTRO_MLP_MAX_HIDDEN 32
+typedef struct astro_precond_mlp {
+    int32_t hidden;   /* 0..ASTRO_MLP_MAX_HIDDEN */
+    int32_t outputs;  /* degree + 1 of the network it modulates */
+    double w1[ASTRO_MLP_MAX_HIDDEN * ASTRO_NODE_FEATURES];
+    double b1[ASTRO_MLP_MAX_HIDDEN];
+    double w2[(ASTRO_PRECOND_MAX_DEGREE + 1) * ASTRO_MLP_MAX_HIDDEN];
+    double b2[ASTRO_PRECOND_MAX_DEGREE + 1];
+} astro_precond_mlp;
+
 /* Options and statistics of the spec solvers (astro_solve_static). */
 #define ASTRO_SOLVER_GMRES_JACOBI_FP64 0   /* plain FP64 Jacobi-GMRES(m): the comparator */
 #define ASTRO_SOLVER_FGMRES_MIXED 1        /* FP32 inner Jacobi-GMRES, FP64 refinement */
@@ -152,6 +178,8 @@ typedef struct astro_solve_opts {
     double inner_rtol;       /* inner relative tolerance for the refinement methods */
     const astro_precond *precond;  /* ASTRO_SOLVER_FGMRES_LEARNED: the network (NULL: the
                                       Chebyshev initialisation of degree 24, ratio 3000) */
+    const astro_precond_mlp *mlp;  /* ASTRO_SOLVER_FGMRES_LEARNED: its per-node modulation (NULL:
+                                      none); outputs must equal the network's degree + 1 */
 } astro_solve_opts;
 
 typedef struct astro_solve_stats {
@@ -560,6 +588,22 @@ int astro_precond_loss_grad(astro_ctx *ctx, const astro_precond *p, const double
  * NULL) receives the loss before every step and after the last. */
 int astro_precond_train(astro_ctx *ctx, astro_precond *p, const double *samples, int32_t num_samples, int32_t iters,
                         double *loss_history);
+
+/* Node features (num_nodes x ASTRO_NODE_FEATURES, row = node id - 1) of the device-resident
+ * assembly (kind 64: FP64 values, 32: FP32 values) with the scaled constraints. */
+int astro_node_features(astro_ctx *ctx, int32_t kind, double *features);
+
+/* The per-node hop scales a_k(r) of mlp (num_nodes x mlp->outputs, row = node id - 1). */
+int astro_precond_mlp_scales(astro_ctx *ctx, int32_t kind, const astro_precond_mlp *mlp, double *scales);
+
+/* Training loss of the modulated network (the loss of astro_precond_loss_grad with
+ * P v = (1/lambda) sum_k a_k (W_k y_k)) and its gradients: grad_weights with respect to the hop
+ * weights (layout of astro_precond.weights, may be NULL) and grad_mlp with respect to the
+ * perceptron (layout of astro_precond_mlp; hidden and outputs copied from mlp; may be NULL).
+ * Forward and backward passes on the device in FP64; the node features from the FP64 assembly. */
+int astro_precond_mlp_loss_grad(astro_ctx *ctx, const astro_precond *p, const astro_precond_mlp *mlp,
+                                const double *samples, int32_t num_samples, double *loss, double *grad_weights,
+                                astro_precond_mlp *grad_mlp);
 
 /* stepSolve, elastic static branch (Working/AStrO_commandFunctions.f90:681-749): from node_disp
  * (el_mat_dim, global DOF numbering, in/out) and internal_disp (int_vec_size, in/out, may be NULL),

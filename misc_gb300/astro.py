@@ -106,9 +106,58 @@ class PrecondC(C.Structure):
             self.weights[i] = float(x)
 
 
+NODE_FEATURES = 6
+MLP_MAX_HIDDEN = 32
+
+
+class PrecondMlpC(C.Structure):
+    """astro_precond_mlp: per-node modulation of the polynomial network (node features -> hop
+    scales a_k = 1 + b2 + w2 tanh(w1 f + b1))."""
+    _fields_ = [("hidden", C.c_int32), ("outputs", C.c_int32),
+                ("w1", C.c_double * (MLP_MAX_HIDDEN * NODE_FEATURES)), ("b1", C.c_double * MLP_MAX_HIDDEN),
+                ("w2", C.c_double * ((PRECOND_MAX_DEGREE + 1) * MLP_MAX_HIDDEN)),
+                ("b2", C.c_double * (PRECOND_MAX_DEGREE + 1))]
+
+    def params(self):
+        """(w1 (H, F), b1 (H), w2 (K, H), b2 (K)) as arrays (copies)."""
+        H, K = self.hidden, self.outputs
+        return (np.array(self.w1[:H * NODE_FEATURES]).reshape(H, NODE_FEATURES), np.array(self.b1[:H]),
+                np.array(self.w2[:K * H]).reshape(K, H), np.array(self.b2[:K]))
+
+    def set_params(self, w1, b1, w2, b2):
+        H, K = self.hidden, self.outputs
+        for dst, src, cnt in ((self.w1, w1, H * NODE_FEATURES), (self.b1, b1, H), (self.w2, w2, K * H),
+                              (self.b2, b2, K)):
+            a = np.asarray(src, dtype=np.float64).reshape(-1)
+            assert a.size == cnt
+            for i in range(cnt):
+                dst[i] = float(a[i])
+
+    def vector(self):
+        return np.concatenate([x.reshape(-1) for x in self.params()])
+
+    def set_vector(self, v):
+        H, K, F = self.hidden, self.outputs, NODE_FEATURES
+        v = np.asarray(v, dtype=np.float64)
+        o = [0, H * F, H * F + H, H * F + H + K * H, H * F + H + K * H + K]
+        self.set_params(v[o[0]:o[1]], v[o[1]:o[2]], v[o[2]:o[3]], v[o[3]:o[4]])
+
+
+def mlp_init(hidden, outputs, seed=0, scale=None):
+    """A perceptron whose output layer is zero (a_k = 1: the unmodulated network) and whose first
+    layer is drawn N(0, 1/F) from seed."""
+    m = PrecondMlpC()
+    m.hidden, m.outputs = hidden, outputs
+    rng = np.random.default_rng(seed)
+    sc = (1.0 / np.sqrt(NODE_FEATURES)) if scale is None else scale
+    m.set_params(sc * rng.standard_normal((hidden, NODE_FEATURES)), np.zeros(hidden), np.zeros((outputs, hidden)),
+                 np.zeros(outputs))
+    return m
+
+
 class SolveOptsC(C.Structure):
     _fields_ = [("method", C.c_int32), ("restart", C.c_int32), ("max_iters", C.c_int32), ("rtol", C.c_double),
-                ("inner_rtol", C.c_double), ("precond", C.POINTER(PrecondC))]
+                ("inner_rtol", C.c_double), ("precond", C.POINTER(PrecondC)), ("mlp", C.POINTER(PrecondMlpC))]
 
 
 class StepOptsC(C.Structure):
@@ -208,6 +257,10 @@ def load_library():
         "astro_update_external_rhs": ([vp, F64P, F64P], C.c_int),
         "astro_newmark_run": ([vp, C.POINTER(NewmarkOptsC), F64P, F64P, F64P, F64P, F64P, F64P, F64P,
                                C.POINTER(SolveStatsC)], C.c_int),
+        "astro_node_features": ([vp, C.c_int32, F64P], C.c_int),
+        "astro_precond_mlp_scales": ([vp, C.c_int32, C.POINTER(PrecondMlpC), F64P], C.c_int),
+        "astro_precond_mlp_loss_grad": ([vp, C.POINTER(PrecondC), C.POINTER(PrecondMlpC), F64P, C.c_int32, F64P, F64P,
+                                         C.POINTER(PrecondMlpC)], C.c_int),
         "astro_newmark_cases": ([vp, C.POINTER(NewmarkCasesOptsC), F64P, F64P, F64P, F64P, F64P, F64P,
                                  C.POINTER(NewmarkCasesInfoC)], C.c_int),
         "astro_update_internal_soln": ([vp, F64P, F64P, F64P], C.c_int),
@@ -427,10 +480,11 @@ class AstroGPU:
 
     # -- solves ---------------------------------------------------------------------------------
     def solve_static(self, f, u0=None, method=SOLVER_GMRES_JACOBI_FP64, restart=50, rtol=1e-10, max_iters=200000,
-                     inner_rtol=1e-4, allow_maxit=False, precond=None):
+                     inner_rtol=1e-4, allow_maxit=False, precond=None, mlp=None):
         u = np.zeros(self.n) if u0 is None else _f64(u0).copy()
         o = SolveOptsC(method, restart, max_iters, rtol, inner_rtol,
-                       C.pointer(precond) if precond is not None else C.POINTER(PrecondC)())
+                       C.pointer(precond) if precond is not None else C.POINTER(PrecondC)(),
+                       C.pointer(mlp) if mlp is not None else C.POINTER(PrecondMlpC)())
         st = SolveStatsC()
         rc = self.L.astro_solve_static(self.h, _d(_f64(f)), _d(u), C.byref(o), C.byref(st))
         self._check(rc, allow=(7,) if allow_maxit else ())
@@ -690,6 +744,29 @@ class AstroGPU:
         g = np.zeros((p.degree + 1) * p.dpn * p.dpn)
         self._check(self.L.astro_precond_loss_grad(self.h, C.byref(p), _d(S), S.shape[0], _d(loss), _d(g)))
         return float(loss[0]), g.reshape(p.degree + 1, p.dpn, p.dpn)
+
+    def node_features(self, kind=64):
+        """Node features (num_nodes x NODE_FEATURES, row = node id - 1) of the resident assembly."""
+        F = np.zeros((self.model.num_nodes, NODE_FEATURES))
+        self._check(self.L.astro_node_features(self.h, kind, _d(F)))
+        return F
+
+    def mlp_scales(self, mlp, kind=64):
+        """Per-node hop scales (num_nodes x outputs) of the perceptron."""
+        A = np.zeros((self.model.num_nodes, mlp.outputs))
+        self._check(self.L.astro_precond_mlp_scales(self.h, kind, C.byref(mlp), _d(A)))
+        return A
+
+    def mlp_loss_grad(self, p, mlp, samples):
+        """(loss, gradient of the hop weights (degree + 1, dpn, dpn), gradient of the perceptron as
+        a PrecondMlpC) of the modulated network on samples (S x el_mat_dim)."""
+        S = _f64(samples).reshape(-1, self.n)
+        loss = np.zeros(1)
+        gw = np.zeros((p.degree + 1) * p.dpn * p.dpn)
+        gm = PrecondMlpC()
+        self._check(self.L.astro_precond_mlp_loss_grad(self.h, C.byref(p), C.byref(mlp), _d(S), S.shape[0], _d(loss),
+                                                       _d(gw), C.byref(gm)))
+        return float(loss[0]), gw.reshape(p.degree + 1, p.dpn, p.dpn), gm
 
     def precond_train(self, p, samples, iters=50):
         """Trains p in place; returns the loss history (iters + 1)."""

@@ -195,6 +195,11 @@ int shell4_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *
                                 const double *d_intRhs);                                           // elem_shell4.cu
 void panels_release(astro_ctx *ctx);                                         // panels.cu
 int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes);         // panels.cu
+int precond_node_features(astro_ctx *ctx, int kind, double *dF, DevBuf &L, DevBuf &pd, DevBuf &part,
+                          cudaStream_t s);                                  // precond.cu
+int precond_mlp_check(astro_ctx *ctx, const astro_precond_mlp *m, int degree);
+int precond_mlp_scales_f32(astro_ctx *ctx, const astro_precond_mlp *m, const double *dF, DevBuf &prm, float *a,
+                           cudaStream_t s);
 int ensure_K(astro_ctx *ctx, int which);          // device BSR value arrays (ctx.cu)
 int ensure_io(astro_ctx *ctx, bool exportMat);    // host-vector staging buffers (ctx.cu)
 int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s);      // panels.cu

@@ -225,6 +225,8 @@ struct HopArgs {
     float w0[36];  // W_0 / lambda (first hop)
     float theta, c;
     int first;
+    const float *amod;  // per-node hop scales a_k(r) at amod[k * N + r] (null: all 1)
+    int k1;             // k + 1, the hop whose output this launch adds
 };
 
 template <class OP, class TV, int DPN>
@@ -249,17 +251,23 @@ __global__ void __launch_bounds__(kThreads) k_poly_hop(OP op, const TV *__restri
         yn[q] = (TV)h.c * (t[q] - (TV)h.theta * yc[q]);
         if (!h.first) yn[q] -= ykm1[base + q];
     }
+    // the modulation network's scales of this hop (and of hop 0 on the first) at this node
+    const TV a1 = h.amod ? (TV)h.amod[(size_t)h.k1 * op.N + c.r] : TV(1);
+    const TV a0 = (h.amod && h.first) ? (TV)h.amod[c.r] : TV(1);
 #pragma unroll
     for (int q = 0; q < DPN; ++q) {
         if (ykp1) ykp1[base + q] = yn[q];
         TV z = h.first ? TV(0) : zacc[base + q];
         if (h.first) {
+            TV z0 = TV(0);
 #pragma unroll
-            for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w0[q * DPN + jj] * (sc[jj] * yc[jj]);
+            for (int jj = 0; jj < DPN; ++jj) z0 += (TV)h.w0[q * DPN + jj] * (sc[jj] * yc[jj]);
+            z += a0 * z0;
         }
+        TV z1 = TV(0);
 #pragma unroll
-        for (int jj = 0; jj < DPN; ++jj) z += (TV)h.w[q * DPN + jj] * (sc[jj] * yn[jj]);
-        zacc[base + q] = z;
+        for (int jj = 0; jj < DPN; ++jj) z1 += (TV)h.w[q * DPN + jj] * (sc[jj] * yn[jj]);
+        zacc[base + q] = z + a1 * z1;
     }
 }
 
@@ -650,6 +658,7 @@ __global__ void k_to_ell(const TS *__restrict__ K, const int *__restrict__ rowPt
 struct PolyHost {
     int deg = 0;
     float theta = 0.f, delta = 0.f;
+    const float *amod = nullptr;  // per-node hop scales of the modulation network (device), or null
     double apwKey = 0.0;  // the L2 window the hop launches carry (part of the graph's key)
     float W[(ASTRO_PRECOND_MAX_DEGREE + 1) * 36] = {};
 };
@@ -659,6 +668,7 @@ struct GmresWork {
     DevBuf x64, b64;  // FP64 solver: the solve's x and b live here, so its graph is reused across solves
     DevBuf yB0, yB1, zacc, pw;  // polynomial preconditioner: hop vectors, output, power-iteration scratch
     DevBuf Kh, Kr, penS, dsqT;  // its operator A^ = S A S (FP16 block-vector planes, scaled penalty) and S
+    DevBuf nfF, nfL, nfPd, nfPart, mlpPrm, amod;  // node features and the modulation network's scales
     cudaStream_t bodyStream = nullptr;  // captures the bodies of the cycle's IF nodes
     bool condOk = true;                 // conditional graph nodes available
     OpH hop;
@@ -757,11 +767,13 @@ static TV *enqueue_poly(astro_ctx *ctx, GmresWork &W, TV *y0, int always, cudaSt
     std::memset(&h, 0, sizeof(h));
     for (int q = 0; q < dd; ++q) h.w0[q] = P.W[q];
     h.theta = P.theta;
+    h.amod = P.amod;
     int cur = 0;
     for (int k = 0; k < P.deg; ++k) {
         const int nxt = (cur + 1) % 3, prv = (cur + 2) % 3;
         for (int q = 0; q < dd; ++q) h.w[q] = P.W[(k + 1) * dd + q];
         h.first = (k == 0);
+        h.k1 = k + 1;
         h.c = (k == 0 ? 1.f : 2.f) / P.delta;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(grid);
@@ -985,7 +997,8 @@ static void work_free(GmresWork &W) {
     W.graph = nullptr;
     DevBuf *b[] = {&W.V,    &W.w0,   &W.w1,    &W.z0, &W.z1,  &W.part, &W.ctl, &W.dinv,
                    &W.dinvT, &W.rres, &W.xs,  &W.tgt, &W.yB0, &W.yB1,  &W.zacc, &W.pw,
-                   &W.Kh,    &W.Kr,   &W.penS, &W.dsqT, &W.x64, &W.b64};
+                   &W.Kh,    &W.Kr,   &W.penS, &W.dsqT, &W.x64, &W.b64, &W.nfF, &W.nfL,
+                   &W.nfPd,  &W.nfPart, &W.mlpPrm, &W.amod};
     for (auto *x : b) dev_free(*x);
 }
 
@@ -1246,6 +1259,23 @@ static int solve_static_dev(astro_ctx *ctx, const double *d_b, double *d_x, cons
             ph.theta = (float)(0.5 * lam * (1.0 + 1.0 / pc->ratio));
             ph.delta = (float)(0.5 * lam * (1.0 - 1.0 / pc->ratio));
             for (int q = 0; q < (pc->degree + 1) * DPN * DPN; ++q) ph.W[q] = (float)(pc->weights[q] / lam);
+            if (o->mlp && o->mlp->hidden > 0) {
+                // the modulation network's per-node hop scales from the node features of the
+                // assembly (one pass over the matrix and one over the nodes per solve); the
+                // buffer is allocated once for the largest degree, so the graph's pointer holds
+                if ((rc = precond_mlp_check(ctx, o->mlp, pc->degree))) return rc;
+                const int N = ctx->P.N;
+                if (!W.amod.p && ((rc = dev_alloc(ctx, W.nfF, sizeof(double) * (size_t)N * ASTRO_NODE_FEATURES)) ||
+                                  (rc = dev_alloc(ctx, W.amod, sizeof(float) * (size_t)N *
+                                                                   (ASTRO_PRECOND_MAX_DEGREE + 1)))))
+                    return rc;
+                if ((rc = precond_node_features(ctx, ctx->haveK64 ? 64 : 32, dptr<double>(W.nfF), W.nfL, W.nfPd,
+                                                W.nfPart, ctx->stream)) ||
+                    (rc = precond_mlp_scales_f32(ctx, o->mlp, dptr<double>(W.nfF), W.mlpPrm, dptr<float>(W.amod),
+                                                 ctx->stream)))
+                    return rc;
+                ph.amod = dptr<float>(W.amod);
+            }
             W.poly = &ph;
             persistSet = persist_begin(ctx, W, &persistPrev);
             if (W.apwOn) ph.apwKey = (double)W.apw.hitRatio * 1e12 + (double)W.apw.num_bytes;

@@ -175,6 +175,338 @@ __global__ void k_tr_lsdots(Op<double> op, const double *__restrict__ ZD, const 
     cta_sum(qq, out + 1);
 }
 
+// ---- node features and the per-node modulation network ----------------------------------
+
+constexpr int kF = ASTRO_NODE_FEATURES;
+
+// l_r = ln(mean diagonal entry of the node's diagonal block), the node's penalty diagonal mean
+// p_r, and the CTA's share of sum_r l_r
+template <class TM, int DPN>
+__global__ void k_nf_diag(int N, const int *__restrict__ bRowPtr, const int *__restrict__ bCol,
+                          const TM *__restrict__ K, const int *__restrict__ penPtr, const int *__restrict__ penRow,
+                          const int *__restrict__ penCol, const double *__restrict__ penVal, double *__restrict__ L,
+                          double *__restrict__ pd, double *__restrict__ part) {
+    const int r = blockIdx.x * kT + threadIdx.x;
+    double l = 0.0;
+    if (r < N) {
+        double d = 0.0;
+        for (int b = bRowPtr[r]; b < bRowPtr[r + 1]; ++b)
+            if (bCol[b] == r) {
+#pragma unroll
+                for (int i = 0; i < DPN; ++i) d += (double)K[(size_t)b * DPN * DPN + i * DPN + i];
+            }
+        double p = 0.0;
+        if (penPtr)
+            for (int t = penPtr[r]; t < penPtr[r + 1]; ++t)
+                if (penCol[t] == r * DPN + penRow[t]) p += penVal[t];
+        d /= DPN;
+        l = log(fmax(fabs(d), 1e-300));
+        L[r] = l;
+        pd[r] = p / DPN;
+    }
+    cta_sum(l, part + blockIdx.x);
+}
+
+// features of every node (row-major N x kF, internal block-row order); part holds nParts CTA
+// shares of sum_r l_r
+template <class TM, int DPN>
+__global__ void k_nf_feat(int N, int maxBlocks, const int *__restrict__ bRowPtr, const int *__restrict__ bCol,
+                          const TM *__restrict__ K, const double *__restrict__ L, const double *__restrict__ pd,
+                          const double *__restrict__ part, int nParts, double *__restrict__ F) {
+    __shared__ double sMean;
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (int q = 0; q < nParts; ++q) a += part[q];
+        sMean = a / N;
+    }
+    __syncthreads();
+    const int r = blockIdx.x * kT + threadIdx.x;
+    if (r >= N) return;
+    const double lr = L[r];
+    double sum = 0.0, mx = 0.0, off = 0.0, dia = 0.0;
+    int nb = 0;
+    for (int b = bRowPtr[r]; b < bRowPtr[r + 1]; ++b) {
+        const int c = bCol[b];
+        double fro = 0.0;
+#pragma unroll
+        for (int q = 0; q < DPN * DPN; ++q) {
+            const double v = (double)K[(size_t)b * DPN * DPN + q];
+            fro += v * v;
+        }
+        fro = sqrt(fro);
+        if (c == r) {
+            dia = fro;
+        } else {
+            const double dl = L[c] - lr;
+            sum += dl;
+            mx = fmax(mx, fabs(dl));
+            off += fro;
+            ++nb;
+        }
+    }
+    const double d = exp(lr);
+    double *f = F + (size_t)r * kF;
+    f[0] = lr - sMean;
+    f[1] = nb ? sum / nb : 0.0;
+    f[2] = mx;
+    f[3] = (double)(nb + 1) / maxBlocks;
+    f[4] = log1p(pd[r] / d);
+    f[5] = (dia > 0.0 && off > 0.0) ? log(off / dia) : 0.0;
+}
+
+// MLP parameters packed on the device: w1 (H x kF), b1 (H), w2 (K x H), b2 (K)
+struct MlpDims {
+    int H, K;
+};
+
+// a_k(r) = 1 + b2[k] + sum_h w2[k][h] tanh(b1[h] + w1[h] . f(r)); a at A[k * N + r], the hidden
+// activations (when hid) at hid[r * H + h]
+template <class TA>
+__global__ void k_mlp_fwd(int N, MlpDims D, const double *__restrict__ F, const double *__restrict__ prm,
+                          TA *__restrict__ A, double *__restrict__ hid) {
+    const int r = blockIdx.x * kT + threadIdx.x;
+    if (r >= N) return;
+    const double *w1 = prm, *b1 = w1 + D.H * kF, *w2 = b1 + D.H, *b2 = w2 + D.K * D.H;
+    double f[kF], h[ASTRO_MLP_MAX_HIDDEN];
+#pragma unroll
+    for (int q = 0; q < kF; ++q) f[q] = F[(size_t)r * kF + q];
+    for (int j = 0; j < D.H; ++j) {
+        double a = b1[j];
+#pragma unroll
+        for (int q = 0; q < kF; ++q) a += w1[j * kF + q] * f[q];
+        h[j] = tanh(a);
+        if (hid) hid[(size_t)r * D.H + j] = h[j];
+    }
+    for (int k = 0; k < D.K; ++k) {
+        double o = 1.0 + b2[k];
+        for (int j = 0; j < D.H; ++j) o += w2[k * D.H + j] * h[j];
+        A[(size_t)k * N + r] = (TA)o;
+    }
+}
+
+// z_s = sum_k a_k(r) (Wl_k y_k) per node
+template <int DPN>
+__global__ void k_tr_apply_mod(const double *__restrict__ Y, const double *__restrict__ Wl,
+                               const double *__restrict__ amod, double *__restrict__ Z, int n, int N, int deg1) {
+    const int s = blockIdx.y;
+    const int r = blockIdx.x * kT + threadIdx.x;
+    if (r >= N) return;
+    const double *Ys = Y + (size_t)s * deg1 * n;
+    double z[DPN];
+#pragma unroll
+    for (int q = 0; q < DPN; ++q) z[q] = 0.0;
+    for (int k = 0; k < deg1; ++k) {
+        const double a = amod[(size_t)k * N + r];
+        const double *w = Wl + (size_t)k * DPN * DPN;
+#pragma unroll
+        for (int q = 0; q < DPN; ++q) {
+            double t = 0.0;
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) t += w[q * DPN + jj] * Ys[(size_t)k * n + (size_t)r * DPN + jj];
+            z[q] += a * t;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < DPN; ++q) Z[(size_t)s * n + (size_t)r * DPN + q] = z[q];
+}
+
+// Gradient partials of the modulated network, all samples in one pass per CTA (deterministic):
+// with t = (A e_s)_r,
+//   part[cta * deg1 * DD + k * DD + i * DPN + j] = sum_s sum_{r in cta} a_k(r) t_i (y_k)_{r,j}
+//   ga[k * N + r] = sum_s sum_i t_i (Wl_k y_k)_{r,i}
+template <int DPN>
+__global__ void __launch_bounds__(kT) k_tr_grad_mod(Op<double> op, const double *__restrict__ E,
+                                                    const double *__restrict__ Y, const double *__restrict__ Wl,
+                                                    const double *__restrict__ amod, double *__restrict__ part,
+                                                    double *__restrict__ ga, int n, int deg1, int S) {
+    constexpr int DD = DPN * DPN;
+    extern __shared__ double sw[];  // [kTW][deg1 * DD]
+    const int r = blockIdx.x * kT + threadIdx.x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const bool valid = r < op.N;
+    const int N = op.N;
+    for (int q = threadIdx.x; q < kTW * deg1 * DD; q += kT) sw[q] = 0.0;
+    __syncthreads();
+    for (int s = 0; s < S; ++s) {
+        double t[DPN];
+        if (valid) {
+            ell_row<double, double, double, DPN>(op, r, E + (size_t)s * n, t);
+        } else {
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) t[q] = 0.0;
+        }
+        const double *Ys = Y + (size_t)s * deg1 * n;
+        for (int k = 0; k < deg1; ++k) {
+            double y[DPN];
+#pragma unroll
+            for (int jj = 0; jj < DPN; ++jj) y[jj] = valid ? Ys[(size_t)k * n + (size_t)r * DPN + jj] : 0.0;
+            const double a = valid ? amod[(size_t)k * N + r] : 0.0;
+            const double *w = Wl + (size_t)k * DD;
+            double g = 0.0;
+#pragma unroll
+            for (int q = 0; q < DPN; ++q) {
+                double wy = 0.0;
+#pragma unroll
+                for (int jj = 0; jj < DPN; ++jj) wy += w[q * DPN + jj] * y[jj];
+                g += t[q] * wy;
+            }
+            if (valid) ga[(size_t)k * N + r] = (s == 0 ? 0.0 : ga[(size_t)k * N + r]) + g;
+#pragma unroll
+            for (int q = 0; q < DPN; ++q)
+#pragma unroll
+                for (int jj = 0; jj < DPN; ++jj) {
+                    const double v = warp_sum(a * t[q] * y[jj]);
+                    if (lane == 0) sw[(size_t)wid * deg1 * DD + k * DD + q * DPN + jj] += v;
+                }
+        }
+    }
+    __syncthreads();
+    double *out = part + (size_t)blockIdx.x * deg1 * DD;
+    for (int q = threadIdx.x; q < deg1 * DD; q += kT) {
+        double acc = 0.0;
+        for (int w = 0; w < kTW; ++w) acc += sw[(size_t)w * deg1 * DD + q];
+        out[q] = acc;
+    }
+}
+
+// Backward pass of the perceptron: with go_k(r) = scale * ga[k * N + r] = dL/da_k(r), this CTA's
+// shares of the gradients in the packed parameter layout (part[cta * P + p], P = H kF + H + K H + K)
+__global__ void __launch_bounds__(kT) k_mlp_bwd(int N, MlpDims D, const double *__restrict__ F,
+                                                const double *__restrict__ hid, const double *__restrict__ ga,
+                                                double scale, const double *__restrict__ prm,
+                                                double *__restrict__ part) {
+    __shared__ double sp[kTW];
+    const int r = blockIdx.x * kT + threadIdx.x;
+    const bool valid = r < N;
+    const int H = D.H, K = D.K;
+    const double *w2 = prm + H * kF + H;
+    double f[kF], h[ASTRO_MLP_MAX_HIDDEN], gp[ASTRO_MLP_MAX_HIDDEN];
+#pragma unroll
+    for (int q = 0; q < kF; ++q) f[q] = valid ? F[(size_t)r * kF + q] : 0.0;
+    for (int j = 0; j < H; ++j) {
+        h[j] = valid ? hid[(size_t)r * H + j] : 0.0;
+        double gh = 0.0;
+        for (int k = 0; k < K; ++k) gh += w2[k * H + j] * (valid ? scale * ga[(size_t)k * N + r] : 0.0);
+        gp[j] = gh * (1.0 - h[j] * h[j]);
+    }
+    const int P = H * kF + H + K * H + K;
+    double *out = part + (size_t)blockIdx.x * P;
+    for (int p = 0; p < P; ++p) {
+        double v;
+        if (p < H * kF) {
+            v = gp[p / kF] * f[p % kF];
+        } else if (p < H * kF + H) {
+            v = gp[p - H * kF];
+        } else if (p < H * kF + H + K * H) {
+            const int q = p - H * kF - H, k = q / H, j = q % H;
+            v = (valid ? scale * ga[(size_t)k * N + r] : 0.0) * h[j];
+        } else {
+            const int k = p - H * kF - H - K * H;
+            v = valid ? scale * ga[(size_t)k * N + r] : 0.0;
+        }
+        v = warp_sum(v);
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) sp[threadIdx.x >> 5] = v;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double a = 0.0;
+            for (int q = 0; q < kTW; ++q) a += sp[q];
+            out[p] = a;
+        }
+    }
+}
+
+void mlp_pack(const astro_precond_mlp *m, int K, std::vector<double> &out) {
+    const int H = m->hidden;
+    out.clear();
+    out.insert(out.end(), m->w1, m->w1 + H * kF);
+    out.insert(out.end(), m->b1, m->b1 + H);
+    out.insert(out.end(), m->w2, m->w2 + K * H);
+    out.insert(out.end(), m->b2, m->b2 + K);
+}
+
+void mlp_unpack(const double *g, int H, int K, astro_precond_mlp *m) {
+    std::memset(m, 0, sizeof(*m));
+    m->hidden = H;
+    m->outputs = K;
+    std::memcpy(m->w1, g, sizeof(double) * H * kF);
+    std::memcpy(m->b1, g + H * kF, sizeof(double) * H);
+    std::memcpy(m->w2, g + H * kF + H, sizeof(double) * K * H);
+    std::memcpy(m->b2, g + H * kF + H + K * H, sizeof(double) * K);
+}
+
+}  // namespace
+
+// Node features (internal block-row order, N x kF) of the FP64 (kind 64) or FP32 (kind 32)
+// assembly with the scaled constraints; L, pd, part: scratch (allocated on first use).
+int precond_node_features(astro_ctx *ctx, int kind, double *dF, DevBuf &L, DevBuf &pd, DevBuf &part, cudaStream_t s) {
+    const AstroPrep &P = ctx->P;
+    const int N = P.N, nCta = (N + kT - 1) / kT;
+    if (kind == 64 ? !ctx->haveK64 : !(ctx->haveK32 || ctx->haveK64))
+        return set_err(ctx, ASTRO_ERR_STATE, "node features: stiffness not assembled");
+    int rc;
+    if (!L.p && ((rc = dev_alloc(ctx, L, sizeof(double) * N)) || (rc = dev_alloc(ctx, pd, sizeof(double) * N)) ||
+                 (rc = dev_alloc(ctx, part, sizeof(double) * nCta))))
+        return rc;
+    int maxB = 1;
+    for (int r = 0; r < N; ++r) maxB = std::max(maxB, P.bRowPtr[r + 1] - P.bRowPtr[r]);
+    const bool f64 = kind == 64 || !ctx->haveK32;
+    const int *pp = ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr;
+    const int *br = dptr<int>(ctx->d_bRowPtr), *bc = dptr<int>(ctx->d_bCol);
+    const int *prow = dptr<int>(ctx->d_penRow), *pcol = dptr<int>(ctx->d_penCol);
+    const double *pval = dptr<double>(ctx->d_penVal);
+    double *dl = dptr<double>(L), *dp = dptr<double>(pd), *dq = dptr<double>(part);
+    if (f64) {
+        const double *K = dptr<double>(ctx->d_K64);
+        if (P.dpn == 3) {
+            k_nf_diag<double, 3><<<nCta, kT, 0, s>>>(N, br, bc, K, pp, prow, pcol, pval, dl, dp, dq);
+            k_nf_feat<double, 3><<<nCta, kT, 0, s>>>(N, maxB, br, bc, K, dl, dp, dq, nCta, dF);
+        } else {
+            k_nf_diag<double, 6><<<nCta, kT, 0, s>>>(N, br, bc, K, pp, prow, pcol, pval, dl, dp, dq);
+            k_nf_feat<double, 6><<<nCta, kT, 0, s>>>(N, maxB, br, bc, K, dl, dp, dq, nCta, dF);
+        }
+    } else {
+        const float *K = dptr<float>(ctx->d_K32);
+        if (P.dpn == 3) {
+            k_nf_diag<float, 3><<<nCta, kT, 0, s>>>(N, br, bc, K, pp, prow, pcol, pval, dl, dp, dq);
+            k_nf_feat<float, 3><<<nCta, kT, 0, s>>>(N, maxB, br, bc, K, dl, dp, dq, nCta, dF);
+        } else {
+            k_nf_diag<float, 6><<<nCta, kT, 0, s>>>(N, br, bc, K, pp, prow, pcol, pval, dl, dp, dq);
+            k_nf_feat<float, 6><<<nCta, kT, 0, s>>>(N, maxB, br, bc, K, dl, dp, dq, nCta, dF);
+        }
+    }
+    return cuda_check(ctx, cudaGetLastError(), "node features");
+}
+
+int precond_mlp_check(astro_ctx *ctx, const astro_precond_mlp *m, int degree) {
+    if (m->hidden < 0 || m->hidden > ASTRO_MLP_MAX_HIDDEN)
+        return set_err(ctx, ASTRO_ERR_ARG, "perceptron hidden width out of range");
+    if (m->outputs != degree + 1) return set_err(ctx, ASTRO_ERR_ARG, "perceptron outputs differ from degree + 1");
+    return ASTRO_OK;
+}
+
+// the per-node scales a (float, K x N) of the perceptron on the features dF (N x kF, internal
+// order); prm: packed parameters (allocated for the largest network on first use)
+int precond_mlp_scales_f32(astro_ctx *ctx, const astro_precond_mlp *m, const double *dF, DevBuf &prm, float *a,
+                           cudaStream_t s) {
+    const int H = m->hidden, K = m->outputs;
+    int rc;
+    const size_t maxP = (size_t)ASTRO_MLP_MAX_HIDDEN * (kF + 1) +
+                        (size_t)(ASTRO_PRECOND_MAX_DEGREE + 1) * (ASTRO_MLP_MAX_HIDDEN + 1);
+    if (!prm.p && (rc = dev_alloc(ctx, prm, sizeof(double) * maxP))) return rc;
+    std::vector<double> pk;
+    mlp_pack(m, K, pk);
+    if ((rc = cuda_check(ctx, cudaMemcpyAsync(prm.p, pk.data(), sizeof(double) * pk.size(), cudaMemcpyHostToDevice, s),
+                         "mlp upload")))
+        return rc;
+    const int N = ctx->P.N;
+    k_mlp_fwd<float><<<(N + kT - 1) / kT, kT, 0, s>>>(N, MlpDims{H, K}, dF, dptr<double>(prm), a, nullptr);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "perceptron forward"))) return rc;
+    return cuda_check(ctx, cudaStreamSynchronize(s), "perceptron forward");  // pk goes out of scope
+}
+
+namespace {
+
 // Device state of a training run: samples, features and work vectors for S samples.
 struct TrainSet {
     astro_ctx *ctx = nullptr;
@@ -182,10 +514,12 @@ struct TrainSet {
     int S = 0, deg = 0, deg1 = 0, dpn = 0, n = 0, N = 0, nCta = 0;
     double lam = 0.0, theta = 0.0, delta = 0.0;
     DevBuf v, dinv, Y, Z, E, part, Wl;
+    // the modulation network: node features, hidden activations, scales a, dL/da, parameters
+    DevBuf F, hid, amod, ga, prm, nfL, nfPd, nfPart, mpart;
     std::vector<double> hp;
 
     ~TrainSet() {
-        DevBuf *b[] = {&v, &dinv, &Y, &Z, &E, &part, &Wl};
+        DevBuf *b[] = {&v, &dinv, &Y, &Z, &E, &part, &Wl, &F, &hid, &amod, &ga, &prm, &nfL, &nfPd, &nfPart, &mpart};
         for (auto *x : b) dev_free(*x);
     }
 
@@ -310,6 +644,99 @@ struct TrainSet {
             for (int s = 0; s < S; ++s)
                 for (int c = 0; c < nCta; ++c) a += hp[((size_t)s * nCta + c) * per + q];
             grad[q] = -2.0 * a / (S * lam);
+        }
+        return ASTRO_OK;
+    }
+
+    // loss and gradients of the modulated network at (w, mlp): gw (deg1 dpn^2) and gm (packed
+    // perceptron parameters), either may be null
+    int loss_grad_mod(const double *w, const astro_precond_mlp *mlp, double *loss, double *gw, double *gm) {
+        const int H = mlp->hidden, K = deg1, dd = dpn * dpn;
+        const int P = H * kF + H + K * H + K;
+        int rc;
+        if (!F.p) {
+            if ((rc = dev_alloc(ctx, F, sizeof(double) * (size_t)N * kF)) ||
+                (rc = dev_alloc(ctx, hid, sizeof(double) * (size_t)N * std::max(H, 1))) ||
+                (rc = dev_alloc(ctx, amod, sizeof(double) * (size_t)N * K)) ||
+                (rc = dev_alloc(ctx, ga, sizeof(double) * (size_t)N * K)) ||
+                (rc = dev_alloc(ctx, prm, sizeof(double) * (size_t)std::max(P, 1))) ||
+                (rc = dev_alloc(ctx, mpart, sizeof(double) * (size_t)nCta * std::max(P, K * dd))))
+                return rc;
+            if ((rc = precond_node_features(ctx, 64, dptr<double>(F), nfL, nfPd, nfPart, ctx->stream))) return rc;
+        }
+        std::vector<double> pk;
+        mlp_pack(mlp, K, pk);
+        if ((rc = cuda_check(ctx, cudaMemcpyAsync(prm.p, pk.data(), sizeof(double) * P, cudaMemcpyHostToDevice,
+                                                  ctx->stream), "mlp upload")))
+            return rc;
+        const unsigned gN = (unsigned)nCta;
+        k_mlp_fwd<double><<<gN, kT, 0, ctx->stream>>>(N, MlpDims{H, K}, dptr<double>(F), dptr<double>(prm),
+                                                     dptr<double>(amod), H ? dptr<double>(hid) : nullptr);
+        std::vector<double> wl(w, w + (size_t)K * dd);
+        for (auto &x : wl) x /= lam;
+        if ((rc = cuda_check(ctx, cudaMemcpyAsync(Wl.p, wl.data(), sizeof(double) * K * dd, cudaMemcpyHostToDevice,
+                                                  ctx->stream), "weights upload")))
+            return rc;
+        const dim3 gr(nCta, S);
+        if (dpn == 3) {
+            k_tr_apply_mod<3><<<gr, kT, 0, ctx->stream>>>(dptr<double>(Y), dptr<double>(Wl), dptr<double>(amod),
+                                                         dptr<double>(Z), n, N, deg1);
+            k_tr_resid<3><<<gr, kT, 0, ctx->stream>>>(op, dptr<double>(v), dptr<double>(Z), dptr<double>(E),
+                                                     dptr<double>(part), n);
+        } else {
+            k_tr_apply_mod<6><<<gr, kT, 0, ctx->stream>>>(dptr<double>(Y), dptr<double>(Wl), dptr<double>(amod),
+                                                         dptr<double>(Z), n, N, deg1);
+            k_tr_resid<6><<<gr, kT, 0, ctx->stream>>>(op, dptr<double>(v), dptr<double>(Z), dptr<double>(E),
+                                                     dptr<double>(part), n);
+        }
+        if ((rc = fetch((size_t)S * nCta))) return rc;  // synchronises: pk and wl may go
+        double L = 0.0;
+        for (int s = 0; s < S; ++s) {
+            double a = 0.0;
+            for (int q = 0; q < nCta; ++q) a += hp[(size_t)s * nCta + q];
+            L += a;
+        }
+        *loss = L / S;
+        if (!gw && !gm) return ASTRO_OK;
+        const size_t smem = sizeof(double) * kTW * K * dd;
+        if (smem > 48 * 1024) {
+            cudaError_t e = dpn == 3 ? cudaFuncSetAttribute(k_tr_grad_mod<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                     : cudaFuncSetAttribute(k_tr_grad_mod<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if ((rc = cuda_check(ctx, e, "gradient shared memory"))) return rc;
+        }
+        if (dpn == 3)
+            k_tr_grad_mod<3><<<gN, kT, smem, ctx->stream>>>(op, dptr<double>(E), dptr<double>(Y), dptr<double>(Wl),
+                                                           dptr<double>(amod), dptr<double>(mpart), dptr<double>(ga), n,
+                                                           deg1, S);
+        else
+            k_tr_grad_mod<6><<<gN, kT, smem, ctx->stream>>>(op, dptr<double>(E), dptr<double>(Y), dptr<double>(Wl),
+                                                           dptr<double>(amod), dptr<double>(mpart), dptr<double>(ga), n,
+                                                           deg1, S);
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "modulated gradient"))) return rc;
+        // dL/dz_s = -(2 / S) A e_s: the weights' gradient carries 1/lambda, dL/da does not
+        // (Wl inside ga already holds it)
+        if (gw) {
+            if ((rc = fetch((size_t)nCta * K * dd))) return rc;
+            for (int q = 0; q < K * dd; ++q) {
+                double a = 0.0;
+                for (int c = 0; c < nCta; ++c) a += hp[(size_t)c * K * dd + q];
+                gw[q] = -2.0 * a / (S * lam);
+            }
+        }
+        if (gm) {
+            if (H > 0) {
+                k_mlp_bwd<<<gN, kT, 0, ctx->stream>>>(N, MlpDims{H, K}, dptr<double>(F), dptr<double>(hid),
+                                                     dptr<double>(ga), -2.0 / S, dptr<double>(prm), dptr<double>(mpart));
+                if ((rc = cuda_check(ctx, cudaGetLastError(), "perceptron backward"))) return rc;
+                if ((rc = fetch((size_t)nCta * P))) return rc;
+                for (int q = 0; q < P; ++q) {
+                    double a = 0.0;
+                    for (int c = 0; c < nCta; ++c) a += hp[(size_t)c * P + q];
+                    gm[q] = a;
+                }
+            } else {
+                for (int q = 0; q < P; ++q) gm[q] = 0.0;
+            }
         }
         return ASTRO_OK;
     }
@@ -463,5 +890,84 @@ extern "C" int astro_precond_train(astro_ctx *ctx, astro_precond *p, const doubl
         dPrev = d;
     }
     std::memcpy(p->weights, w.data(), sizeof(double) * nw);
+    return ASTRO_OK;
+}
+
+// node id order <-> internal block rows
+static void rows_to_nodes(astro_ctx *ctx, const std::vector<double> &in, int w, double *out) {
+    const AstroPrep &P = ctx->P;
+    for (int nd = 1; nd <= P.N; ++nd) {
+        const int r = P.currentRank[nd] - 1;
+        std::memcpy(out + (size_t)(nd - 1) * w, in.data() + (size_t)r * w, sizeof(double) * w);
+    }
+}
+
+extern "C" int astro_node_features(astro_ctx *ctx, int32_t kind, double *features) {
+    if (!ctx || !features || (kind != 64 && kind != 32)) return ASTRO_ERR_ARG;
+    if (!ctx->mpcScaled && ctx->P.mpcDim > 0) return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run first");
+    const int N = ctx->P.N;
+    DevBuf F, L, pd, part;
+    int rc = dev_alloc(ctx, F, sizeof(double) * (size_t)N * kF);
+    if (!rc) rc = precond_node_features(ctx, kind, dptr<double>(F), L, pd, part, ctx->stream);
+    std::vector<double> h((size_t)N * kF);
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(h.data(), F.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        rc = cuda_check(ctx, e, "features download");
+    }
+    if (!rc) rows_to_nodes(ctx, h, kF, features);
+    DevBuf *b[] = {&F, &L, &pd, &part};
+    for (auto *x : b) dev_free(*x);
+    return rc;
+}
+
+extern "C" int astro_precond_mlp_scales(astro_ctx *ctx, int32_t kind, const astro_precond_mlp *mlp, double *scales) {
+    if (!ctx || !mlp || !scales || (kind != 64 && kind != 32)) return ASTRO_ERR_ARG;
+    if (mlp->hidden < 0 || mlp->hidden > ASTRO_MLP_MAX_HIDDEN || mlp->outputs < 1 ||
+        mlp->outputs > ASTRO_PRECOND_MAX_DEGREE + 1)
+        return set_err(ctx, ASTRO_ERR_ARG, "perceptron shape out of range");
+    if (!ctx->mpcScaled && ctx->P.mpcDim > 0) return set_err(ctx, ASTRO_ERR_STATE, "astro_scale_mpc must run first");
+    const int N = ctx->P.N, K = mlp->outputs, H = mlp->hidden;
+    DevBuf F, L, pd, part, prm, a;
+    int rc = dev_alloc(ctx, F, sizeof(double) * (size_t)N * kF);
+    if (!rc) rc = dev_alloc(ctx, a, sizeof(double) * (size_t)N * K);
+    if (!rc) rc = precond_node_features(ctx, kind, dptr<double>(F), L, pd, part, ctx->stream);
+    std::vector<double> pk;
+    mlp_pack(mlp, K, pk);
+    if (!rc) rc = upload(ctx, prm, pk.data(), sizeof(double) * pk.size());
+    if (!rc) {
+        k_mlp_fwd<double><<<(N + kT - 1) / kT, kT, 0, ctx->stream>>>(N, MlpDims{H, K}, dptr<double>(F),
+                                                                    dptr<double>(prm), dptr<double>(a), nullptr);
+        rc = cuda_check(ctx, cudaGetLastError(), "perceptron forward");
+    }
+    std::vector<double> h((size_t)N * K), t((size_t)N * K);
+    if (!rc) {
+        cudaError_t e = cudaMemcpyAsync(h.data(), a.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        rc = cuda_check(ctx, e, "scales download");
+    }
+    if (!rc) {
+        for (int k = 0; k < K; ++k)
+            for (int r = 0; r < N; ++r) t[(size_t)r * K + k] = h[(size_t)k * N + r];
+        rows_to_nodes(ctx, t, K, scales);
+    }
+    DevBuf *b[] = {&F, &L, &pd, &part, &prm, &a};
+    for (auto *x : b) dev_free(*x);
+    return rc;
+}
+
+extern "C" int astro_precond_mlp_loss_grad(astro_ctx *ctx, const astro_precond *p, const astro_precond_mlp *mlp,
+                                           const double *samples, int32_t num_samples, double *loss,
+                                           double *grad_weights, astro_precond_mlp *grad_mlp) {
+    if (!ctx || !p || !mlp || !loss) return ASTRO_ERR_ARG;
+    int rc;
+    if ((rc = train_check(ctx, p, samples, num_samples))) return rc;
+    if ((rc = precond_mlp_check(ctx, mlp, p->degree))) return rc;
+    TrainSet T;
+    if ((rc = T.setup(ctx, p, samples, num_samples))) return rc;
+    const int H = mlp->hidden, K = p->degree + 1;
+    std::vector<double> gm((size_t)H * kF + H + (size_t)K * H + K);
+    if ((rc = T.loss_grad_mod(p->weights, mlp, loss, grad_weights, grad_mlp ? gm.data() : nullptr))) return rc;
+    if (grad_mlp) mlp_unpack(gm.data(), H, K, grad_mlp);
     return ASTRO_OK;
 }

@@ -14,6 +14,14 @@ untrained (Chebyshev) network.
 
 Command line (writes the network as JSON):
     python -m misc_gb300.learned --blocks 2000 --out trained.json
+
+The per-node modulation (astro_precond_mlp) is the part of the network that sees the model: a
+two-layer perceptron maps six features of every node of the assembled matrix (its stiffness
+level, the contrast to its neighbours, connectivity, constraints, diagonal dominance) to a
+scale of every Chebyshev hop at that node.  It is trained by Adam over a set of blocks of the
+family, every step one device forward and backward pass (astro_precond_mlp_loss_grad) on one
+block's samples:
+    python -m misc_gb300.learned --mlp --blocks 48 --epochs 60 --out precond_mlp_cfg4.json
 """
 from __future__ import annotations
 
@@ -24,7 +32,7 @@ import time
 import numpy as np
 
 from . import model as M
-from .astro import (SOLVER_FGMRES_LEARNED, SOLVER_GMRES_JACOBI_FP64, AstroGPU, PrecondC, precond_init)
+from .astro import (SOLVER_FGMRES_LEARNED, SOLVER_GMRES_JACOBI_FP64, AstroGPU, PrecondC, mlp_init, precond_init)
 
 
 def block_system(m, fp32=False):
@@ -101,6 +109,76 @@ def validate(p_init, p_trained, m, rtol=1e-8):
     return out[0][0], out[1][0], out[0][1], out[1][1]
 
 
+def mlp_to_json(p, mlp, meta=None):
+    w1, b1, w2, b2 = mlp.params()
+    d = {"network": to_json(p), "hidden": int(mlp.hidden), "outputs": int(mlp.outputs), "w1": w1.tolist(),
+         "b1": b1.tolist(), "w2": w2.tolist(), "b2": b2.tolist()}
+    if meta:
+        d["meta"] = meta
+    return d
+
+
+def mlp_from_json(d):
+    """(polynomial network, perceptron) of a file written by mlp_to_json."""
+    p = from_json(d["network"])
+    m = mlp_init(d["hidden"], d["outputs"])
+    m.set_params(np.array(d["w1"]), np.array(d["b1"]), np.array(d["w2"]), np.array(d["b2"]))
+    return p, m
+
+
+def train_mlp(p, seeds, hidden=16, epochs=60, lr=3e-3, white=3, gmres_steps=(10, 40, 160), seed=0, log=print):
+    """Adam over the blocks of seeds (32x16x16 of the config-4 family), one device forward and
+    backward pass of the modulated network per block and step, the polynomial network p fixed.
+    Returns (perceptron, mean loss over the blocks per epoch, mean loss of the unmodulated
+    network)."""
+    rng = np.random.default_rng(seed + 12345)
+    sets = []
+    for s in seeds:
+        g, b = block_system(M.config4_block(32, 16, 16, s))
+        S = np.vstack([gmres_residuals(g, b, gmres_steps), rng.standard_normal((white, g.n))])
+        sets.append((g, S))
+    mlp = mlp_init(hidden, p.degree + 1, seed=seed)
+    x = mlp.vector()
+    m1, m2 = np.zeros_like(x), np.zeros_like(x)
+    base = float(np.mean([g.precond_loss_grad(p, S)[0] for g, S in sets]))
+    hist, t = [], 0
+    order = np.arange(len(sets))
+    for ep in range(epochs):
+        rng.shuffle(order)
+        losses = []
+        for i in order:
+            g, S = sets[i]
+            mlp.set_vector(x)
+            L, _, gm = g.mlp_loss_grad(p, mlp, S)
+            losses.append(L)
+            gv = gm.vector()
+            t += 1
+            m1 = 0.9 * m1 + 0.1 * gv
+            m2 = 0.999 * m2 + 0.001 * gv * gv
+            x = x - lr * (m1 / (1 - 0.9 ** t)) / (np.sqrt(m2 / (1 - 0.999 ** t)) + 1e-12)
+        hist.append(float(np.mean(losses)))
+        if log and (ep % 10 == 0 or ep == epochs - 1):
+            log(f"epoch {ep + 1}/{epochs}: mean loss {hist[-1]:.5e} (unmodulated {base:.5e})")
+    mlp.set_vector(x)
+    return mlp, hist, base
+
+
+def validate_mlp(p, mlp, seeds, rtol=1e-8):
+    """Learned solves of held-out blocks without and with the modulation: per block (iterations,
+    seconds, status) of each, the second solve of each timed."""
+    out = []
+    for s in seeds:
+        g, b = block_system(M.config4_block(32, 16, 16, s), fp32=True)
+        r = {}
+        for name, kw in (("chebyshev", {}), ("modulated", {"mlp": mlp})):
+            for _ in range(2):
+                _, st = g.solve_static(b, method=SOLVER_FGMRES_LEARNED, rtol=rtol, precond=p, allow_maxit=True, **kw)
+            r[name] = (int(st.iterations), float(st.seconds), int(st.status))
+        out.append({"seed": int(s), **r})
+        del g
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--blocks", type=int, default=2000)
@@ -109,8 +187,28 @@ def main():
     ap.add_argument("--ratio", type=float, default=3000.0)
     ap.add_argument("--cg-steps", type=int, default=5)
     ap.add_argument("--out", required=True)
+    ap.add_argument("--mlp", action="store_true", help="train the per-node modulation (perceptron)")
+    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--hidden", type=int, default=16)
+    ap.add_argument("--lr", type=float, default=3e-3)
     a = ap.parse_args()
     t0 = time.time()
+    if a.mlp:
+        p = precond_init(a.degree, a.ratio, 3)
+        seeds = list(range(a.seed0, a.seed0 + a.blocks))
+        held = list(range(a.seed0 + a.blocks + 100, a.seed0 + a.blocks + 106))
+        mlp, hist, base = train_mlp(p, seeds, hidden=a.hidden, epochs=a.epochs, lr=a.lr)
+        t1 = time.time()
+        val = validate_mlp(p, mlp, held)
+        meta = {"family": "config-4 32x16x16 brick blocks (model.config4_block)", "training_seeds": [seeds[0], seeds[-1]],
+                "held_out_seeds": held,
+                "samples_per_block": "GMRES residuals after 10, 40, 160 steps + 3 white-noise vectors",
+                "optimizer": f"Adam lr {a.lr}, {a.epochs} epochs", "hidden": a.hidden, "loss_unmodulated": base,
+                "loss_per_epoch": hist, "train_seconds": t1 - t0, "validation": val}
+        print(json.dumps({k: v for k, v in meta.items() if k != "loss_per_epoch"}))
+        with open(a.out, "w") as f:
+            json.dump(mlp_to_json(p, mlp, meta), f, indent=1)
+        return
     p0 = precond_init(a.degree, a.ratio, 3)
     seeds = list(range(a.seed0, a.seed0 + a.blocks))
     p, hist = train_family(p0, seeds, cg_steps=a.cg_steps)
