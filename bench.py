@@ -57,7 +57,8 @@ def _parse():
     p.add_argument("--no-fp64", action="store_true", help="learned evaluation without the FP64 comparator")
     p.add_argument("--eval-nx", type=int, default=96)
     p.add_argument("--panels", type=int, default=512, help="panels of the batched-panel leg (0: skip it)")
-    p.add_argument("--newmark-steps", type=int, default=200, help="time steps of the Newmark leg (0: skip it)")
+    p.add_argument("--newmark-steps", type=int, default=0,
+                   help="time steps of the element-residual Newmark leg (astro_newmark_run; 0: skip it, the default)")
     p.add_argument("--nmc-steps", type=int, default=2000,
                    help="time steps of the batched linear Newmark leg (factored K_eff, 17 cases; 0: skip it)")
     p.add_argument("--nmc-cases", type=int, default=17, help="load cases of the batched Newmark leg")
