@@ -588,68 +588,120 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
     double *Xp = X + (size_t)M.xUnit * nrhs + (size_t)it.col * nbc * TB;
     const size_t wOff = (size_t)M.xUnit * TB;
     float2 *leaderPart = cl.map_shared_rank(sPart, 0);
-    for (int sweep = 0; sweep < 2; ++sweep) {
-        const float2 *Lt = sweep == 0 ? Lf : Lb;
-        const float2 *Wt = sweep == 0 ? Wf : Wb;
-        for (int q = 0; q < nbc; ++q) {
-            const int I = sweep == 0 ? q : nbc - 1 - q;                 // block row solved now
-            const int dmax = sweep == 0 ? min(bt, I) : min(bt, nbc - 1 - I);
-            // tile (source row, d): forward L_{I,I-d} = tile (I-d, d); backward L_{I+d,I}^T = tile (I, d)
-            auto tile = [&](int d) { return Lt + tile_off(M, sweep == 0 ? I - d : I, d); };
-            auto src = [&](int d) { return sweep == 0 ? I - d : I + d; };
-            __syncthreads();  // the leader's last row is in its ring
-            if (rank > 0) {
-                DF acc = {0.f, 0.f};
-                for (int d = 2 + (rank - 1) * kCW + w; d <= dmax; d += kProdWarps)
-                    df_tile_rows(acc, tile(d), sRing + (size_t)(src(d) % ring) * TB, r, 0, TB);
-                sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
-                __syncthreads();
-                if (w == 0) {
-                    DF s = {0.f, 0.f};
-                    for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
-                    leaderPart[((q & 1) * kCS + rank) * TB + r] = make_float2(s.hi, s.lo);
-                }
-                cluster_barrier();
-            } else {
-                // L_{I,I+-1} times the row solved last, split over the warps by k
-                DF acc = {0.f, 0.f};
-                if (dmax >= 1) df_tile_rows(acc, tile(1), sRing + (size_t)(src(1) % ring) * TB, r, 4 * w, 4 * w + 4);
-                sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
-                cluster_barrier();
-                if (w == 0) {
-                    const double b = Xp[(size_t)I * TB + r];
-                    DF v = df_from_double(b);
-                    if (sweep == 1) {
-                        const float2 di = Dinv[M.xUnit + (size_t)I * TB + r];
-                        v = df_mul(v, DF{di.x, di.y});
-                    }
-                    DF s = {0.f, 0.f};
-                    for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
-                    for (int c = 1; c < kCS; ++c) {
-                        const float2 pc = sPart[((q & 1) * kCS + c) * TB + r];
-                        s = df_add(s, DF{pc.x, pc.y});
-                    }
-                    v = df_sub(v, s);
-                    sV[r] = make_float2(v.hi, v.lo);
-                }
-                __syncthreads();
-                // y_I = W v (forward) or x_I = W^T v (backward), split over the warps by k
-                DF a = {0.f, 0.f};
-                df_tile_rows(a, Wt + wOff + (size_t)I * TT, sV, r, 4 * w, 4 * w + 4);
-                sRed[w * TB + r] = make_float2(a.hi, a.lo);
-                __syncthreads();
-                if (w == 0) {
-                    DF y = {0.f, 0.f};
-                    for (int k = 0; k < kCW; ++k) y = df_add(y, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
-                    const float2 yv = make_float2(y.hi, y.lo);
-                    const size_t slot = (size_t)(I % ring) * TB + r;
-                    for (int c = 0; c < kCS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
-                    Xp[(size_t)I * TB + r] = df_to_double(y);
-                }
+    // step t = 0 .. 2 nbc - 1: forward rows I = t, then backward rows I = 2 nbc - 1 - t
+    auto rowOf = [&](int t) { return t < nbc ? t : 2 * nbc - 1 - t; };
+    auto dmaxOf = [&](int t) { return t < nbc ? min(bt, t) : min(bt, 2 * nbc - 1 - t); };
+    // tile d of step t: forward L_{I,I-d} = tile (I-d, d) of Lf; backward L_{I+d,I}^T = tile (I, d) of Lb
+    auto tileOf = [&](int t, int d) {
+        const int I = rowOf(t);
+        return t < nbc ? Lf + tile_off(M, I - d, d) : Lb + tile_off(M, I, d);
+    };
+    auto srcOf = [&](int t, int d) { return t < nbc ? rowOf(t) - d : rowOf(t) + d; };
+    // Each warp's next tile is loaded into registers one step ahead, so the loads are in flight
+    // during the cluster barrier and the leader's part of the step: producers the first tile of
+    // the warp (pf, the lane's row of it), the leader its four columns of L_{I,I+-1} (pl) and of
+    // W (pw), and warp 0 the right-hand side (pb) and D^-1 (pd).
+    const int d0 = 2 + (rank - 1) * kCW + w;
+    float2 pf[TB], pl[4], pw[4], pd = make_float2(0.f, 0.f);
+    double pb = 0.0;
+    auto prefetch = [&](int t) {
+        if (t >= 2 * nbc) return;
+        const int dm = dmaxOf(t), I = rowOf(t);
+        if (rank > 0) {
+            if (d0 <= dm) {
+                const float2 *T = tileOf(t, d0);
+#pragma unroll
+                for (int k = 0; k < TB; ++k) pf[k] = __ldg(T + k * TB + r);
+            }
+        } else {
+            if (dm >= 1) {
+                const float2 *T = tileOf(t, 1);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) pl[k] = __ldg(T + (4 * w + k) * TB + r);
+            }
+            const float2 *Wt = (t < nbc ? Wf : Wb) + wOff + (size_t)I * TT;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) pw[k] = __ldg(Wt + (4 * w + k) * TB + r);
+            if (w == 0) {
+                pb = Xp[(size_t)I * TB + r];
+                if (t >= nbc) pd = __ldg(Dinv + M.xUnit + (size_t)I * TB + r);
             }
         }
-        // the sweep's last rows are pushed before any CTA starts the next sweep or exits
-        cluster_barrier();
+    };
+    prefetch(0);
+    for (int t = 0; t < 2 * nbc; ++t) {
+        const int I = rowOf(t), dmax = dmaxOf(t), q = t < nbc ? t : t - nbc;
+        __syncthreads();  // the leader's last row is in its ring
+        if (rank > 0) {
+            DF acc = {0.f, 0.f}, a2 = {0.f, 0.f};
+            if (d0 <= dmax) {
+                const float2 *v = sRing + (size_t)(srcOf(t, d0) % ring) * TB;
+#pragma unroll
+                for (int k = 0; k < TB; k += 2) {
+                    const float2 y0 = v[k], y1 = v[k + 1];
+                    df_acc(acc, pf[k].x, pf[k].y, y0.x, y0.y);
+                    df_acc(a2, pf[k + 1].x, pf[k + 1].y, y1.x, y1.y);
+                }
+                acc = df_add(df_norm(acc), df_norm(a2));
+            }
+            for (int d = d0 + kProdWarps; d <= dmax; d += kProdWarps)
+                df_tile_rows(acc, tileOf(t, d), sRing + (size_t)(srcOf(t, d) % ring) * TB, r, 0, TB);
+            prefetch(t + 1);
+            sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
+            __syncthreads();
+            if (w == 0) {
+                DF s = {0.f, 0.f};
+                for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                leaderPart[((q & 1) * kCS + rank) * TB + r] = make_float2(s.hi, s.lo);
+            }
+            cluster_barrier();
+        } else {
+            // L_{I,I+-1} times the row solved last, split over the warps by k
+            DF acc = {0.f, 0.f};
+            if (dmax >= 1) {
+                const float2 *v = sRing + (size_t)(srcOf(t, 1) % ring) * TB + 4 * w;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) df_acc(acc, pl[k].x, pl[k].y, v[k].x, v[k].y);
+                acc = df_norm(acc);
+            }
+            sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
+            cluster_barrier();
+            if (w == 0) {
+                DF v = df_from_double(pb);
+                if (t >= nbc) v = df_mul(v, DF{pd.x, pd.y});
+                DF s = {0.f, 0.f};
+                for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                for (int c = 1; c < kCS; ++c) {
+                    const float2 pc = sPart[((q & 1) * kCS + c) * TB + r];
+                    s = df_add(s, DF{pc.x, pc.y});
+                }
+                v = df_sub(v, s);
+                sV[r] = make_float2(v.hi, v.lo);
+            }
+            __syncthreads();
+            // y_I = W v (forward) or x_I = W^T v (backward), split over the warps by k
+            DF a = {0.f, 0.f};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float2 vk = sV[4 * w + k];
+                df_acc(a, pw[k].x, pw[k].y, vk.x, vk.y);
+            }
+            a = df_norm(a);
+            sRed[w * TB + r] = make_float2(a.hi, a.lo);
+            __syncthreads();
+            if (w == 0) {
+                DF y = {0.f, 0.f};
+                for (int k = 0; k < kCW; ++k) y = df_add(y, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                const float2 yv = make_float2(y.hi, y.lo);
+                const size_t slot = (size_t)(I % ring) * TB + r;
+                for (int c = 0; c < kCS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
+                Xp[(size_t)I * TB + r] = df_to_double(y);
+            }
+            prefetch(t + 1);  // after the row's store: the first backward row reads it back
+        }
+        // the forward sweep's last rows are pushed before the backward sweep, and every row
+        // before any CTA exits
+        if (t == nbc - 1 || t == 2 * nbc - 1) cluster_barrier();
     }
 }
 

@@ -599,9 +599,10 @@ struct TrainSet {
         return sync("apply");  // wl goes out of scope
     }
 
-    int fetch(size_t count) {
+    int fetch(size_t count, const DevBuf *src = nullptr) {
         hp.resize(count);
-        cudaError_t e = cudaMemcpyAsync(hp.data(), part.p, sizeof(double) * count, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaMemcpyAsync(hp.data(), (src ? *src : part).p, sizeof(double) * count,
+                                        cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         return cuda_check(ctx, e, "partials");
     }
@@ -716,7 +717,7 @@ struct TrainSet {
         // dL/dz_s = -(2 / S) A e_s: the weights' gradient carries 1/lambda, dL/da does not
         // (Wl inside ga already holds it)
         if (gw) {
-            if ((rc = fetch((size_t)nCta * K * dd))) return rc;
+            if ((rc = fetch((size_t)nCta * K * dd, &mpart))) return rc;
             for (int q = 0; q < K * dd; ++q) {
                 double a = 0.0;
                 for (int c = 0; c < nCta; ++c) a += hp[(size_t)c * K * dd + q];
@@ -728,7 +729,7 @@ struct TrainSet {
                 k_mlp_bwd<<<gN, kT, 0, ctx->stream>>>(N, MlpDims{H, K}, dptr<double>(F), dptr<double>(hid),
                                                      dptr<double>(ga), -2.0 / S, dptr<double>(prm), dptr<double>(mpart));
                 if ((rc = cuda_check(ctx, cudaGetLastError(), "perceptron backward"))) return rc;
-                if ((rc = fetch((size_t)nCta * P))) return rc;
+                if ((rc = fetch((size_t)nCta * P, &mpart))) return rc;
                 for (int q = 0; q < P; ++q) {
                     double a = 0.0;
                     for (int c = 0; c < nCta; ++c) a += hp[(size_t)c * P + q];
