@@ -516,6 +516,14 @@ typedef struct astro_newmark_opts {
 int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *opts, const double *load_pattern,
                       const double *load_amplitude, double *disp, double *vel, double *acc,
                       double *int_disp, double *disp_history, astro_solve_stats *stats);
+/* The same loop returning the state of every step, the records writeBinarySolution writes after
+ * each step (Working/AStrO_commandFunctions.f90:808-811, Working/AStrO_output.f90:761-784):
+ * disp, vel, acc histories (num_steps x el_mat_dim, global DOF numbering) and int_disp_history
+ * (num_steps x int_vec_size); any may be NULL. */
+int astro_newmark_run_states(astro_ctx *ctx, const astro_newmark_opts *opts, const double *load_pattern,
+                             const double *load_amplitude, double *disp, double *vel, double *acc, double *int_disp,
+                             double *disp_history, double *vel_history, double *acc_history,
+                             double *int_disp_history, astro_solve_stats *stats);
 
 /* ---- batched linear Newmark: many load cases through one factorisation ------------------
  * The dynamic branch of solve with linear geometry (Working/AStrO_commandFunctions.f90:770-812:

@@ -261,6 +261,8 @@ def load_library():
         "astro_precond_mlp_scales": ([vp, C.c_int32, C.POINTER(PrecondMlpC), F64P], C.c_int),
         "astro_precond_mlp_loss_grad": ([vp, C.POINTER(PrecondC), C.POINTER(PrecondMlpC), F64P, C.c_int32, F64P, F64P,
                                          C.POINTER(PrecondMlpC)], C.c_int),
+        "astro_newmark_run_states": ([vp, C.POINTER(NewmarkOptsC), F64P, F64P, F64P, F64P, F64P, F64P, F64P, F64P,
+                                      F64P, F64P, C.POINTER(SolveStatsC)], C.c_int),
         "astro_newmark_cases": ([vp, C.POINTER(NewmarkCasesOptsC), F64P, F64P, F64P, F64P, F64P, F64P,
                                  C.POINTER(NewmarkCasesInfoC)], C.c_int),
         "astro_update_internal_soln": ([vp, F64P, F64P, F64P], C.c_int),
@@ -645,6 +647,29 @@ class AstroGPU:
         self._check(self.L.astro_newmark_cases(self.h, C.byref(o), _d(P), _d(Am), _d(u), _d(v), _d(a),
                                                _d(hist) if history else None, C.byref(info)))
         return u, v, a, hist, info
+
+    def newmark_run_states(self, num_steps, del_t, beta=0.25, gamma=0.5, load_pattern=None, load_amplitude=None,
+                           disp=None, vel=None, acc=None, int_disp=None, restart=50, max_iters=2000, rtol=1e-12,
+                           method=SOLVER_GMRES_JACOBI_FP64, precond=None):
+        """newmark_run returning every step's state (astro_newmark_run_states): (disp, vel, acc,
+        int_disp, histories {disp, vel, acc (steps, n), int_disp (steps, int_vec_size)}, stats)."""
+        n, ni = self.n, self.int_vec_size
+        u = np.zeros(n) if disp is None else _f64(disp).copy()
+        v = np.zeros(n) if vel is None else _f64(vel).copy()
+        a = np.zeros(n) if acc is None else _f64(acc).copy()
+        iu = np.zeros(max(ni, 1)) if int_disp is None else _f64(int_disp).copy()
+        H = {"disp": np.zeros((num_steps, n)), "vel": np.zeros((num_steps, n)), "acc": np.zeros((num_steps, n)),
+             "int_disp": np.zeros((num_steps, max(ni, 1)))}
+        o = NewmarkOptsC(num_steps, del_t, beta, gamma, restart, max_iters, rtol, method,
+                         C.pointer(precond) if precond is not None else C.POINTER(PrecondC)())
+        st = SolveStatsC()
+        pat = None if load_pattern is None else _d(_f64(load_pattern))
+        amp = None if load_amplitude is None else _d(_f64(load_amplitude))
+        self._check(self.L.astro_newmark_run_states(self.h, C.byref(o), pat, amp, _d(u), _d(v), _d(a), _d(iu),
+                                                    _d(H["disp"]), _d(H["vel"]), _d(H["acc"]),
+                                                    _d(H["int_disp"]) if ni else None, C.byref(st)))
+        H["int_disp"] = H["int_disp"][:, :ni]
+        return u, v, a, iu[:ni], H, st
 
     def getdRelasticdD(self, dvar, h=1e-14, state=None):
         """Complex-step dRu/dd of design variable dvar: (global DOF vector, internal-DOF vector)."""

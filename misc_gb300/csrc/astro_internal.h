@@ -244,8 +244,12 @@ int solid_orient_prepare(astro_ctx *ctx);
 int shell4_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
                 double *d_intAcc);                                                              // elem_shell4.cu
 void krylov_release(astro_ctx *ctx);
+// per-step device histories of the time loop (reference numbering; any may be null)
+struct NewmarkHist {
+    double *disp = nullptr, *vel = nullptr, *acc = nullptr, *intDisp = nullptr;
+};
 int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,
-                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup, double *d_hist,
-                   astro_solve_stats *st);  // krylov.cu
+                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup,
+                   const NewmarkHist &hist, astro_solve_stats *st);  // krylov.cu
 // host: elements depending on dvar, grouped by colour (colour c: list[ptr[c] .. ptr[c+1]))
 void dvar_elements_by_colour(const astro_ctx *ctx, int dvar, std::vector<int> &list, std::vector<int> &ptr);

@@ -608,9 +608,11 @@ extern "C" int astro_update_internal_soln(astro_ctx *ctx, const double *ext_soln
     return cuda_check(ctx, e, "update_internal_soln");
 }
 
-extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, const double *load_pattern,
-                                 const double *load_amplitude, double *disp, double *vel, double *acc, double *int_disp,
-                                 double *disp_history, astro_solve_stats *stats) {
+// The time loop of astro_newmark_run with every history optional (astro_newmark_run_states).
+static int newmark_run_impl(astro_ctx *ctx, const astro_newmark_opts *o, const double *load_pattern,
+                            const double *load_amplitude, double *disp, double *vel, double *acc, double *int_disp,
+                            double *disp_history, double *vel_history, double *acc_history, double *int_disp_history,
+                            astro_solve_stats *stats) {
     if (!ctx || !o || !disp || !vel || !acc || o->num_steps < 0 || !(o->del_t > 0.0) || !(o->nm_beta > 0.0) ||
         (load_pattern && !load_amplitude))
         return ASTRO_ERR_ARG;
@@ -618,9 +620,9 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
     const int n = P.n, ni = P.intVecSize;
     int rc;
     struct Bufs {
-        DevBuf u, up, vp, ap, iu, iup, pat, hist;
+        DevBuf u, up, vp, ap, iu, iup, pat, hist, vhist, ahist, ihist;
         ~Bufs() {
-            DevBuf *b[] = {&u, &up, &vp, &ap, &iu, &iup, &pat, &hist};
+            DevBuf *b[] = {&u, &up, &vp, &ap, &iu, &iup, &pat, &hist, &vhist, &ahist, &ihist};
             for (auto *x : b) dev_free(*x);
         }
     } B;
@@ -639,6 +641,13 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
     }
     if (load_pattern && (rc = state_vec_up(ctx, load_pattern, B.pat, false))) return rc;
     if (disp_history && o->num_steps > 0 && (rc = dev_alloc(ctx, B.hist, sizeof(double) * n * (size_t)o->num_steps)))
+        return rc;
+    if (vel_history && o->num_steps > 0 && (rc = dev_alloc(ctx, B.vhist, sizeof(double) * n * (size_t)o->num_steps)))
+        return rc;
+    if (acc_history && o->num_steps > 0 && (rc = dev_alloc(ctx, B.ahist, sizeof(double) * n * (size_t)o->num_steps)))
+        return rc;
+    if (int_disp_history && ni && o->num_steps > 0 &&
+        (rc = dev_alloc(ctx, B.ihist, sizeof(double) * ni * (size_t)o->num_steps)))
         return rc;
     // K_eff = K + c1 c2 M at the initial state (getElasticSolnLoad(1) with the dynamic flag), then
     // scaleElasticMPC
@@ -661,9 +670,14 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
     ctx->haveLT = 0;
     ctx->ltFactored = 0;
     if ((rc = astro_scale_mpc(ctx, nullptr, nullptr))) return rc;
+    NewmarkHist H;
+    H.disp = B.hist.p ? dptr<double>(B.hist) : nullptr;
+    H.vel = B.vhist.p ? dptr<double>(B.vhist) : nullptr;
+    H.acc = B.ahist.p ? dptr<double>(B.ahist) : nullptr;
+    H.intDisp = B.ihist.p ? dptr<double>(B.ihist) : nullptr;
     rc = krylov_newmark(ctx, o, B.pat.p ? dptr<double>(B.pat) : nullptr, load_amplitude, dptr<double>(B.u),
                         dptr<double>(B.up), dptr<double>(B.vp), dptr<double>(B.ap), ni ? dptr<double>(B.iu) : nullptr,
-                        ni ? dptr<double>(B.iup) : nullptr, B.hist.p ? dptr<double>(B.hist) : nullptr, stats);
+                        ni ? dptr<double>(B.iup) : nullptr, H, stats);
     if (rc) return rc;
     // final state (after the swap the previous values are the current ones)
     if ((rc = ensure_io(ctx, false))) return rc;
@@ -676,11 +690,33 @@ extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, co
         CK(cudaStreamSynchronize(ctx->stream));
     }
     if (ni && int_disp) CK(cudaMemcpyAsync(int_disp, B.iu.p, sizeof(double) * ni, cudaMemcpyDeviceToHost, ctx->stream));
-    if (B.hist.p)
-        CK(cudaMemcpyAsync(disp_history, B.hist.p, sizeof(double) * n * (size_t)o->num_steps, cudaMemcpyDeviceToHost,
-                           ctx->stream));
+    const struct {
+        DevBuf *d;
+        double *h;
+        size_t len;
+    } outs[4] = {{&B.hist, disp_history, (size_t)n}, {&B.vhist, vel_history, (size_t)n},
+                 {&B.ahist, acc_history, (size_t)n}, {&B.ihist, int_disp_history, (size_t)ni}};
+    for (const auto &x : outs)
+        if (x.d->p)
+            CK(cudaMemcpyAsync(x.h, x.d->p, sizeof(double) * x.len * (size_t)o->num_steps, cudaMemcpyDeviceToHost,
+                               ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return ASTRO_OK;
+}
+
+extern "C" int astro_newmark_run(astro_ctx *ctx, const astro_newmark_opts *o, const double *load_pattern,
+                                 const double *load_amplitude, double *disp, double *vel, double *acc, double *int_disp,
+                                 double *disp_history, astro_solve_stats *stats) {
+    return newmark_run_impl(ctx, o, load_pattern, load_amplitude, disp, vel, acc, int_disp, disp_history, nullptr,
+                            nullptr, nullptr, stats);
+}
+
+extern "C" int astro_newmark_run_states(astro_ctx *ctx, const astro_newmark_opts *o, const double *load_pattern,
+                                        const double *load_amplitude, double *disp, double *vel, double *acc,
+                                        double *int_disp, double *disp_history, double *vel_history,
+                                        double *acc_history, double *int_disp_history, astro_solve_stats *stats) {
+    return newmark_run_impl(ctx, o, load_pattern, load_amplitude, disp, vel, acc, int_disp, disp_history, vel_history,
+                            acc_history, int_disp_history, stats);
 }
 
 extern "C" int astro_assemble_fp32(astro_ctx *ctx) {

@@ -1541,12 +1541,12 @@ __global__ void k_newmark_update(int n, double c1, double c2, double dt, double 
 // applied load amp[step] * pattern and the constraint load, condenses the internal DOF, solves
 // K_eff du = r by FP64 Jacobi-GMRES warm-started from the previous increment (as the reference's
 // gMRes), recovers the internal DOF, updates u and the Newmark state.  All vectors are device
-// buffers in internal layout; the displacement of every step can be written to hist (reference
-// numbering).
+// buffers in internal layout; the displacement, velocity, acceleration and internal DOF of every
+// step can be written to the histories (reference numbering).
 template <int DPN>
 static int krylov_newmark_dpn(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern,
                               const double *h_amp, double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu,
-                              double *d_iup, double *d_hist, astro_solve_stats *st) {
+                              double *d_iup, const NewmarkHist &H, astro_solve_stats *st) {
     const AstroPrep &P = ctx->P;
     const int n = P.n, ni = P.intVecSize;
     const int m = o->restart > 0 ? std::min(o->restart, kMaxM) : 50;
@@ -1642,7 +1642,11 @@ static int krylov_newmark_dpn(astro_ctx *ctx, const astro_newmark_opts *o, const
         k_axpy<<<grid, 256, 0, s>>>(n, 1.0, dptr<double>(du), d_u);
         k_newmark_update<<<grid, 256, 0, s>>>(n, c1, c2, dt, beta, gamma, d_u, d_up, d_vp, d_ap);
         if (ni) CK(cudaMemcpyAsync(d_iup, d_iu, sizeof(double) * ni, cudaMemcpyDeviceToDevice, s));
-        if (d_hist && (rc = int_to_ref_vec(ctx, d_u, d_hist + (size_t)step * n, n))) break;
+        if (H.disp && (rc = int_to_ref_vec(ctx, d_u, H.disp + (size_t)step * n, n))) break;
+        if (H.vel && (rc = int_to_ref_vec(ctx, d_vp, H.vel + (size_t)step * n, n))) break;
+        if (H.acc && (rc = int_to_ref_vec(ctx, d_ap, H.acc + (size_t)step * n, n))) break;
+        if (H.intDisp && ni)
+            CK(cudaMemcpyAsync(H.intDisp + (size_t)step * ni, d_iu, sizeof(double) * ni, cudaMemcpyDeviceToDevice, s));
         if ((rc = cuda_check(ctx, cudaGetLastError(), "newmark step"))) break;
     }
     cudaEventRecord(e1, s);
@@ -1669,9 +1673,9 @@ static int krylov_newmark_dpn(astro_ctx *ctx, const astro_newmark_opts *o, const
 }
 
 int krylov_newmark(astro_ctx *ctx, const astro_newmark_opts *o, const double *d_pattern, const double *h_amp,
-                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup, double *d_hist,
-                   astro_solve_stats *st) {
+                   double *d_u, double *d_up, double *d_vp, double *d_ap, double *d_iu, double *d_iup,
+                   const NewmarkHist &hist, astro_solve_stats *st) {
     if (ctx->P.dpn == 3)
-        return krylov_newmark_dpn<3>(ctx, o, d_pattern, h_amp, d_u, d_up, d_vp, d_ap, d_iu, d_iup, d_hist, st);
-    return krylov_newmark_dpn<6>(ctx, o, d_pattern, h_amp, d_u, d_up, d_vp, d_ap, d_iu, d_iup, d_hist, st);
+        return krylov_newmark_dpn<3>(ctx, o, d_pattern, h_amp, d_u, d_up, d_vp, d_ap, d_iu, d_iup, hist, st);
+    return krylov_newmark_dpn<6>(ctx, o, d_pattern, h_amp, d_u, d_up, d_vp, d_ap, d_iu, d_iup, hist, st);
 }

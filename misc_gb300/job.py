@@ -31,7 +31,7 @@ import numpy as np
 
 from . import inputfile as IF
 from .astro import (SOLVER_FGMRES_LEARNED, SOLVER_GMRES_JACOBI_FP64, AstroGPU, make_state, thermal_props,
-                    thermal_state)
+                    thermal_state, write_step_file)
 
 # element faces, local node numbers (r_getElementFaces)
 HEX_FACES = ((4, 3, 2, 1), (5, 6, 7, 8), (1, 2, 6, 5), (2, 3, 7, 6), (3, 4, 8, 7), (4, 1, 5, 8))
@@ -76,6 +76,8 @@ class Job:
         self.step = 0
         self.u = self.iu = self.v = self.a = None
         self.temp = None
+        self.tdot = None
+        self.save_hist = False
         self.therm_load = None
         self.reaction = None
         self.thermal_ready = False
@@ -222,6 +224,8 @@ class Job:
         elastic, thermal = yes("elastic", "yes"), yes("thermal", "no")
         nl = 1 if yes("nonLinearGeom", "no") else 0
         dynamic = yes("dynamic", "no")
+        # saveSolnHist (Working/AStrO_runJob.f90:183-186): the step files of the time loop
+        self.save_hist = yes("saveSolnHist", "no")
         t_load = float(kv.get("staticLoadTime") or 0.0)
         g = self._gpu()
         if thermal and dynamic:
@@ -252,11 +256,19 @@ class Job:
         g.getElasticSolnLoad(0, state=make_state(g.n, disp=u, internal_disp=iu), elastic_load=load, export=False)
         return load
 
+    def _write_step(self, i, u, v, a, iu):
+        """SolutionHistory<i>.out (writeBinarySolution, Working/AStrO_output.f90:761-784)."""
+        write_step_file(self.dir / f"SolutionHistory{i}.out", self.model.num_nodes, u, v, a,
+                        int_disp=iu if len(iu) else None, temp=self.temp, tdot=self.tdot)
+
     def _newmark(self, dt, period, beta, gamma):
         g = self.g
         nsteps = int(round(period / dt)) if period > 0 else 0
         g.getElasticSolnLoad(1, state=make_state(g.n, disp=self.u, internal_disp=self.iu), export=False)
         g.scaleElasticMPC()
+        if self.save_hist:
+            # step 0: the initial state, as loadInitialState leaves it (previous internal DOF zero)
+            self._write_step(0, self.u, self.v, self.a, np.zeros(g.int_vec_size))
         times = [(k + 1) * dt for k in range(nsteps)]
         k = 0
         while k < nsteps:
@@ -265,9 +277,15 @@ class Job:
             while j < nsteps and tuple(self._active(ld, times[j]) for ld in self.mi.loads) == act:
                 j += 1
             pattern = self.elastic_load(times[k])
-            self.u, self.v, self.a, self.iu, _, st = g.newmark_run(
-                j - k, dt, beta, gamma, pattern, np.ones(j - k), disp=self.u, vel=self.v, acc=self.a,
-                int_disp=self.iu, rtol=1e-10, history=False, method=self._method())
+            kw = dict(disp=self.u, vel=self.v, acc=self.a, int_disp=self.iu, rtol=1e-10, method=self._method())
+            if self.save_hist:
+                self.u, self.v, self.a, self.iu, H, st = g.newmark_run_states(j - k, dt, beta, gamma, pattern,
+                                                                              np.ones(j - k), **kw)
+                for q in range(j - k):
+                    self._write_step(k + q + 1, H["disp"][q], H["vel"][q], H["acc"][q], H["int_disp"][q])
+            else:
+                self.u, self.v, self.a, self.iu, _, st = g.newmark_run(j - k, dt, beta, gamma, pattern,
+                                                                       np.ones(j - k), history=False, **kw)
             self.log.append(f"Newmark steps {k + 1}..{j}: status {st.status}")
             k = j
         self.time, self.step = nsteps * dt, nsteps

@@ -154,3 +154,41 @@ def test_transient_thermal_job(tmp_path):
     To = T[o.current_rank - 1]
     assert np.linalg.norm(Tj - To) <= 1e-8 * np.linalg.norm(To)
     assert To.max() > 50.0 and To.min() < 10.0   # heat has entered from the left end, not reached the right
+
+
+def test_newmark_job_writes_solution_history(tmp_path):
+    """saveSolnHist: yes writes SolutionHistory0..N.out (writeBinarySolution's records after each
+    step of solve's time loop): the initial state, then each step's displacement, internal DOF,
+    velocity and acceleration, equal to the device loop's states."""
+    from misc_gb300.astro import read_step_file
+    m = M.plate_shell(nx=4, ny=4, lx=1.0, ly=1.0, t=0.01, E=7e10, nu=0.33, rho=2700.0, pressure=0.0, clamp="ss",
+                      y0=0.0)
+    centre = 2 * 5 + 2 + 1
+    IF.write_model_input(m, tmp_path / "plate.yaml", node_sets={"c": [centre]})
+    txt = (tmp_path / "plate.yaml").read_text()
+    txt = txt[:txt.index("loads:")] if "loads:" in txt else txt
+    txt += "loads:\n    - type: nodal\n      activeTime: [0.0, 1.0]\n      setLoads:\n" \
+           "          - [c, 0.0, 0.0, 100.0, 0.0, 0.0, 0.0, 0.0]\n"
+    (tmp_path / "plate.yaml").write_text(txt)
+    (tmp_path / "job.txt").write_text(
+        "*readModelInput:\n    fileName: plate.yaml\n*solve:\n    elastic: yes\n    dynamic: yes\n"
+        "    timeStep: 1e-5\n    simPeriod: 4e-5\n    saveSolnHist: yes\n")
+    job = J.Job(tmp_path).run(tmp_path / "job.txt")
+    g = job.g
+    n, ni, N = g.n, g.int_vec_size, m.num_nodes
+    files = sorted(tmp_path.glob("SolutionHistory*.out"))
+    assert len(files) == 5
+    _, _, u0, iu0, v0, a0 = read_step_file(tmp_path / "SolutionHistory0.out", N, n, ni)
+    assert not u0.any() and not iu0.any()
+    mi = IF.read_model_input(tmp_path / "plate.yaml")
+    g2 = AstroGPU(mi.model())
+    g2.getElasticSolnLoad(1, export=False)
+    g2.scaleElasticMPC()
+    pat = job.elastic_load(1e-5)
+    u, v, a, iu, H, st = g2.newmark_run_states(4, 1e-5, 0.25, 0.5, pat, np.ones(4), rtol=1e-10,
+                                               method=SOLVER_FGMRES_LEARNED)
+    for i in range(1, 5):
+        _, _, ui, iui, vi, ai = read_step_file(tmp_path / f"SolutionHistory{i}.out", N, n, ni)
+        for x, y in ((ui, H["disp"][i - 1]), (vi, H["vel"][i - 1]), (ai, H["acc"][i - 1]), (iui, H["int_disp"][i - 1])):
+            assert np.linalg.norm(x - y) <= 1e-9 * max(np.linalg.norm(y), 1e-300), i
+    assert np.array_equal(H["disp"][-1], u) and np.array_equal(H["vel"][-1], v) and np.array_equal(H["acc"][-1], a)
