@@ -236,10 +236,12 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
  * conditional graph nodes; the same kernels in the same order, so the results are identical.
  * For profilers that do not look inside conditional nodes, and for drivers without them. */
 #define ASTRO_OPT_UNROLLED_CYCLES 2
-/* ASTRO_OPT_BAND_FP64_UPDATE (default 0): when 1, the band LDL^T of astro_panels_factor runs its
- * trailing tile updates in FP64 arithmetic instead of the default FP64-exact tensor-core
- * emulation (BF16 slices of the Ozaki error-free splitting, summed exactly in FP32 per level and
- * combined in FP64).  For comparison and measurement. */
+/* ASTRO_OPT_BAND_FP64_UPDATE (default 1): the band LDL^T of astro_panels_factor (and of
+ * astro_newmark_cases) runs its trailing tile updates in FP64 arithmetic; 0 selects the
+ * tensor-core emulation (BF16 slices of the Ozaki error-free splitting, summed exactly in FP32 per
+ * level and combined in FP64; 56 bits relative to each row's largest entry).  On GB300 the
+ * emulation measured slower than the FP64 update on the 512-panel batch, so it is kept for
+ * comparison and measurement. */
 #define ASTRO_OPT_BAND_FP64_UPDATE 3
 int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value);
 

@@ -149,7 +149,7 @@ struct astro_ctx {
     std::vector<double> n2c, dActTime;
     DevBuf d_n2dR, d_n2d, d_n2c, d_dComp, d_secOrig;
     int quirkShellMeanRot = 0;
-    int bandFp64Update = 0;  // ASTRO_OPT_BAND_FP64_UPDATE
+    int bandFp64Update = 1;  // ASTRO_OPT_BAND_FP64_UPDATE
 };
 
 // error helpers

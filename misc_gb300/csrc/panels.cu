@@ -19,9 +19,11 @@
 //   solve     one CTA per (panel, group of up to 8 right-hand sides): forward sweep with unit L,
 //             D^-1, backward sweep with L^T; the eight warps split the band's tiles of a block row
 //             and warp 0 reduces and solves the diagonal tile with shuffles.
-// The trailing tile updates carry almost all of the factor's arithmetic.  GB300 issues FP64 at
-// about 1/64 of its FP32 rate, so by default they run on the tensor cores as an FP64-exact
-// emulation (the error-free splitting of Ozaki, Ogita, Oishi and Rump, "Error-free transformations
+// The trailing tile updates carry almost all of the factor's arithmetic.  They run in FP64 by
+// default; ASTRO_OPT_BAND_FP64_UPDATE = 0 runs them on the tensor cores as an FP64-exact
+// emulation instead (measured slower on GB300 than the FP64 update for these 32 x 32 tiles: 28
+// level products of legacy mma.sync per tile against 32 FP64 multiply-adds per output, plus the
+// slicing) (the error-free splitting of Ozaki, Ogita, Oishi and Rump, "Error-free transformations
 // of matrix multiplication by using fast routines of matrix multiplication and its applications",
 // Numer. Algorithms 59, 2012, with BF16 slices):
 //   * after the tiles L_IJ of block column J are formed, every row of D_J-scaled L_IJ and of L_IJ

@@ -173,21 +173,21 @@ def test_condensed_complex_step_batch(batch):
 
 
 def test_tensor_core_update_matches_fp64_update(batch):
-    """The band factor's trailing updates on the tensor cores (FP64-exact BF16 slice emulation, the
-    default) against the same factorisation with FP64 updates: the two solutions agree to 1e-10,
-    and the emulated one matches the sparse direct solve as the FP64 one does."""
+    """The band factor's trailing updates on the tensor cores (FP64-exact BF16 slice emulation,
+    an option) against the same factorisation with FP64 updates (the default): the two solutions
+    agree to 1e-10, and the emulated one matches the sparse direct solve as the FP64 one does."""
     from misc_gb300.astro import OPT_BAND_FP64_UPDATE
     m, g, o, A = batch
     B = np.random.default_rng(17).standard_normal((g.n, 9))
     Xr = spla.splu(A).solve(B)
-    g.set_option(OPT_BAND_FP64_UPDATE, 1)
+    g.set_option(OPT_BAND_FP64_UPDATE, 0)
     try:
         g.panels_factor(4)
-        X64, _ = g.panels_solve(B)
+        Xtc, _ = g.panels_solve(B)
     finally:
-        g.set_option(OPT_BAND_FP64_UPDATE, 0)
+        g.set_option(OPT_BAND_FP64_UPDATE, 1)
     g.panels_factor(4)
-    Xtc, _ = g.panels_solve(B)
+    X64, _ = g.panels_solve(B)
     _check(A, X64, B, Xr)
     _check(A, Xtc, B, Xr)
     assert np.linalg.norm(Xtc - X64) <= 1e-10 * np.linalg.norm(X64)
