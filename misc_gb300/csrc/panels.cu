@@ -592,7 +592,8 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
     float2 *leaderPart = cl.map_shared_rank(sPart, 0);
     // step t = 0 .. 2 nbc - 1: forward rows I = t, then backward rows I = 2 nbc - 1 - t
     auto rowOf = [&](int t) { return t < nbc ? t : 2 * nbc - 1 - t; };
-    auto dmaxOf = [&](int t) { return t < nbc ? min(bt, t) : min(bt, 2 * nbc - 1 - t); };
+    // tiles below (forward) or right of (backward) the row that exist: min(bt, I) / min(bt, nbc - 1 - I)
+    auto dmaxOf = [&](int t) { return t < nbc ? min(bt, t) : min(bt, t - nbc); };
     // tile d of step t: forward L_{I,I-d} = tile (I-d, d) of Lf; backward L_{I+d,I}^T = tile (I, d) of Lb
     auto tileOf = [&](int t, int d) {
         const int I = rowOf(t);
