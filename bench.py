@@ -63,6 +63,7 @@ def _parse():
                    help="time steps of the batched linear Newmark leg (factored K_eff, 17 cases; 0: skip it)")
     p.add_argument("--nmc-cases", type=int, default=17, help="load cases of the batched Newmark leg")
     p.add_argument("--no-widened", action="store_true", help="skip the thermal / adjoint / body-load leg")
+    p.add_argument("--no-cpu-legs", action="store_true", help="skip the CPU baseline legs of configs 1, 2 and 5")
     p.add_argument("--panels-only", action="store_true", help="only the batched-panel leg")
     p.add_argument("--panels-cluster", type=int, default=0, help="cluster size (0: autotuned over 2, 4, 8)")
     return p.parse_args()
@@ -411,6 +412,8 @@ def run_ours(a):
     # CPU baseline: oracle, 1 core, bounded sample
     if rank == 0:
         rate, dt = _oracle_rate(m, 1024, 1)
+        if not a.no_cpu_legs:
+            line["cpu_legs"] = _cpu_legs(a)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": "brick8 element matrices of elements 1..1024 (oracle restatement, FP64, "
                                           "single thread)"}
@@ -680,6 +683,135 @@ def _newmark_cases_eval(a, nm):
         out["gmres_element_loop_ms_per_step_one_case"] = nm["gmres_fp64"]["ms_per_step"]
     del g, g2
     gc.collect()
+    return out
+
+
+def _cpu_legs(a):
+    """The reference path timed on this machine's host cores through the oracle (the C++
+    restatement of the reference's algorithms, single thread, built -O2; the reference itself is
+    serial Fortran built at -O0 and cannot be compiled here), on bounded samples:
+    config 1 (40x8 shell cantilever): element matrices, the assembly (getElasticSolnLoad),
+    convertToLTri + the skyline LDL^T factor and solve, the reference gMRes with the skyline
+    preconditioner, the tip deflection;
+    config 2 (64x32x32 block): the assembly, and FP64 Jacobi-GMRES(50) (scipy, the GPU
+    comparator's algorithm) for a bounded number of steps, extrapolated to the GPU comparator's
+    step count at 1e-10;
+    config 5 (128x128 plate, consistent shell tangent): the factorisation of K_eff (scipy
+    SuperLU) and the first steps of the reference's loop (element residual, constraint load,
+    condensation, solve, recovery), per step."""
+    import gc
+    import scipy.sparse.linalg as spla
+    from misc_gb300 import model as M
+    from oracle import Oracle
+    from oracle import oracle as OO
+    out = {"kind": "port", "cores": 1, "threads_note": "oracle single thread; scipy SpMV single thread",
+           "host": {"nproc": os.cpu_count()}}
+    # config 1
+    m = M.config1()
+    o = Oracle(m)
+    t0 = time.perf_counter()
+    o.element_matrices()
+    t_el = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    load, iload, mat, cols, imat = o.el_soln_load(1)
+    t_as = time.perf_counter() - t0
+    mm, mr = o.scale_mpc(mat)
+    f = o.applied_load()
+    b = load + f
+    o.constraint_load(mm, mr, np.zeros(o.n), b)
+    rhs = o.update_external_rhs(b, iload[:o.int_vec_size], imat)
+    t0 = time.perf_counter()
+    lt = o.convert_to_ltri(mat, cols, mm)
+    fac = o.ldl_fact(lt, o.lt_range)
+    t_fac = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    u = o.ldl_solve(fac, o.lt_range, rhs)
+    t_sol = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    ug, cyc = o.gmres(mat, cols, mm, fac, rhs)
+    t_gm = time.perf_counter() - t0
+    tip = [k for k in range(m.num_nodes) if abs(m.node_list[k, 0] - 10.0) < 1e-9]
+    w_tip = float(np.mean([u[o.n_dof_index[k, 2] - 1] for k in tip]))
+    out["config1"] = {"workload": "40x8 shell4 cantilever (2,214 DOF)", "element_matrices_per_s": m.num_els / t_el,
+                      "assembly_s": t_as, "ldl_fact_s": t_fac, "ldl_solve_s": t_sol, "ref_gmres_s": t_gm,
+                      "ref_gmres_cycles": int(cyc), "tip_w": w_tip}
+    del o
+    gc.collect()
+    # config 2
+    m = M.config2(nx=a.nx, ny=a.ny, nz=a.nz)
+    o = Oracle(m)
+    t0 = time.perf_counter()
+    load, iload, mat, cols, imat = o.el_soln_load(1)
+    t_as = time.perf_counter() - t0
+    mm, mr = o.scale_mpc(mat)
+    Cm = o.mpc_scipy(mm)
+    A = (o.csr_scipy(mat, cols) + Cm.T @ Cm).tocsr()
+    b = o.applied_load() + load
+    o.constraint_load(mm, mr, np.zeros(o.n), b)
+    dinv = 1.0 / A.diagonal()
+    Mj = spla.LinearOperator(A.shape, matvec=lambda x: dinv * x)
+    steps = 300
+    it = [0]
+    t0 = time.perf_counter()
+    spla.gmres(A, b, rtol=1e-10, restart=50, maxiter=steps // 50, M=Mj, callback=lambda r: it.__setitem__(0, it[0] + 1),
+               callback_type="pr_norm")
+    t_gm = time.perf_counter() - t0
+    gpu_steps = 7735
+    out["config2"] = {"workload": f"{a.nx}x{a.ny}x{a.nz} brick8 block ({o.n} DOF)", "assembly_s": t_as,
+                      "element_matrices_per_s": m.num_els / t_as,
+                      "jacobi_gmres50": {"sample_steps": it[0], "sample_s": t_gm, "s_per_step": t_gm / max(it[0], 1),
+                                         "extrapolated_s_to_1e-10": t_gm / max(it[0], 1) * gpu_steps,
+                                         "extrapolated_at_steps": gpu_steps,
+                                         "note": "the step count of the GPU's FP64 Jacobi-GMRES(50) to 1e-10 on this "
+                                                 "block"}}
+    del o, A
+    gc.collect()
+    # config 5
+    L = OO._lib()
+    import ctypes
+    L.orc_set_quirk.argtypes = [ctypes.c_int, ctypes.c_int]
+    L.orc_set_quirk(1, 1)
+    try:
+        nx, dt, nsteps = 128, 1e-5, 3
+        m = M.plate_shell(nx=nx, ny=nx, lx=1.0, ly=1.0, t=0.01, E=7e10, nu=0.33, rho=2700.0, pressure=0.0, clamp="ss",
+                          y0=0.0)
+        o = Oracle(m)
+        n, ni = o.n, o.int_vec_size
+        centre = (nx // 2) * (nx + 1) + nx // 2 + 1
+        pattern = np.zeros(n)
+        pattern[o.n_dof_index[centre - 1, 2] - 1] = 1.0
+        amp = 100.0 * np.sin(2 * np.pi * 500.0 * dt * np.arange(1, nsteps + 1))
+        u, up, vp, ap = (np.zeros(n) for _ in range(4))
+        iu, iup = np.zeros(ni), np.zeros(ni)
+        st = lambda: M.make_state(n, disp=u, prev_disp=up, prev_vel=vp, prev_acc=ap, internal_disp=iu,
+                                  prev_int_disp=iup, dynamic=1, beta=0.25, gamma=0.5, del_t=dt)
+        t0 = time.perf_counter()
+        _, _, mat, cols, imat = o.el_soln_load(1, state=st())
+        mm, mr = o.scale_mpc(mat)
+        Cm = o.mpc_scipy(mm)
+        lu = spla.splu((o.csr_scipy(mat, cols) + Cm.T @ Cm).tocsc())
+        t_fac = time.perf_counter() - t0
+        c1, c2 = 2.0, 2.0 / (dt * dt)
+        t0 = time.perf_counter()
+        for k in range(nsteps):
+            load, iload, *_ = o.el_soln_load(0, state=st())
+            load = load + amp[k] * pattern
+            o.constraint_load(mm, mr, u, load)
+            r = o.update_external_rhs(load, iload[:ni], imat)
+            du = lu.solve(r)
+            iu = o.update_internal_soln(du, iu, iload[:ni], imat)[:ni]
+            u = u + du
+            acc = c1 * (c2 * (u - up - dt * vp) - (1.0 - 2.0 * 0.25) * ap)
+            vel = vp + dt * (0.5 * ap + 0.5 * acc)
+            up, vp, ap, iup = u.copy(), vel, acc, iu.copy()
+        t_steps = time.perf_counter() - t0
+        out["config5"] = {"workload": "128x128 shell4 plate (99,846 DOF), one load case, consistent tangent",
+                          "assembly_and_factor_s": t_fac, "steps_timed": nsteps, "s_per_step": t_steps / nsteps,
+                          "extrapolated_2000_steps_one_case_s": t_steps / nsteps * 2000,
+                          "solver": "scipy SuperLU of K_eff + C^T C (the reference's skyline LDL^T of this K_eff "
+                                    "would take longer)"}
+    finally:
+        L.orc_set_quirk(1, 0)
     return out
 
 
