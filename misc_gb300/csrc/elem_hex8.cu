@@ -802,7 +802,9 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
     DF acc[9], geo = zero, acc0[9], geo0 = zero;
 #pragma unroll
     for (int q = 0; q < 9; ++q) acc[q] = acc0[q] = zero;
-#pragma unroll
+    // one unit per trip: unrolled, the nine units' double-float bodies overflow the instruction
+    // cache (the kernel's leading stall was instruction fetch)
+#pragma unroll 1
     for (int u = 0; u < 9; ++u) {
         if (u == usw) {
 #pragma unroll

@@ -238,8 +238,10 @@ class Job:
             g.scaleElasticMPC()
             f = self.elastic_load(t_load)
             u0, iu0 = self.u.copy(), self.iu.copy()
+            # 1e-12 FP64 relative residual: the shell models of job files are slender (the
+            # reference's example beam, E = 1e6), so 1e-10 leaves the displacement near 1e-6
             self.u, self.iu, its, st = g.stepSolve(f, node_disp=self.u, internal_disp=self.iu, nl_geom=nl,
-                                                   method=self._method(), rtol=1e-10)
+                                                   method=self._method(), rtol=1e-12)
             self.time, self.step = t_load, 0
             # reactionForce is -elasticLoad as the step left it: the load of its last Newton
             # iteration, formed before that iteration's solve (the step's start for a linear step)
