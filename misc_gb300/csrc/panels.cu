@@ -548,6 +548,13 @@ __device__ __forceinline__ void cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
+// The cluster barrier of the many-column solve: only the warps that stored into distributed shared
+// memory fence (release, before they arrive); every thread arrives relaxed and waits with acquire.
+__device__ __forceinline__ void cluster_fence() { asm volatile("fence.acq_rel.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void cluster_barrier_relaxed() {
+    asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
 
 // acc[r] += sum_{k in [k0, k1)} T[k * TB + r] v[k] (T a DF tile in global memory, v in shared)
 __device__ __forceinline__ void df_tile_rows(DF &acc, const float2 *__restrict__ T, const float2 *v, int r, int k0,
@@ -656,8 +663,9 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 DF s = {0.f, 0.f};
                 for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
                 leaderPart[((q & 1) * kCS + rank) * TB + r] = make_float2(s.hi, s.lo);
+                cluster_fence();
             }
-            cluster_barrier();
+            cluster_barrier_relaxed();
         } else {
             // L_{I,I+-1} times the row solved last, split over the warps by k
             DF acc = {0.f, 0.f};
@@ -668,7 +676,8 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 acc = df_norm(acc);
             }
             sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
-            cluster_barrier();
+            __threadfence_block();  // this CTA's partials, read by warp 0 after the barrier
+            cluster_barrier_relaxed();
             if (w == 0) {
                 DF v = df_from_double(pb);
                 if (t >= nbc) v = df_mul(v, DF{pd.x, pd.y});
@@ -699,12 +708,13 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 const size_t slot = (size_t)(I % ring) * TB + r;
                 for (int c = 0; c < kCS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
                 Xp[(size_t)I * TB + r] = df_to_double(y);
+                cluster_fence();  // the pushed row, ordered before this warp's next arrival
             }
             prefetch(t + 1);  // after the row's store: the first backward row reads it back
         }
         // the forward sweep's last rows are pushed before the backward sweep, and every row
         // before any CTA exits
-        if (t == nbc - 1 || t == 2 * nbc - 1) cluster_barrier();
+        if (t == nbc - 1 || t == 2 * nbc - 1) cluster_barrier_relaxed();
     }
 }
 
