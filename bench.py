@@ -653,6 +653,16 @@ def _newmark_cases_eval(a, nm):
     g.set_option(OPT_SHELL_MEAN_ROT_TERM, 1)
     steps = a.nmc_steps
     P, A = M.config5_cases(m, g.n_dof_index, steps, dt, num_random=a.nmc_cases - 1)
+    # the autotuner picks the solve's CTAs per case (2, 4, 8) on this factorisation: one step to
+    # prepare it, then the timed candidates (kept in a scratch cache file, reported below)
+    import tempfile
+    from misc_gb300.astro import TUNE_CASES_CLUSTER
+    g.newmark_cases(dt, P, A[:, :1])
+    with tempfile.TemporaryDirectory() as td:
+        cache = os.path.join(td, "tune.txt")
+        choice = g.autotune(TUNE_CASES_CLUSTER, cache)[2]
+        with open(cache) as f:
+            tune = [ln.split() for ln in f if ln.strip()]
     u, v, acc, _, info = g.newmark_cases(dt, P, A)
     ms = 1e3 * info.step_seconds / max(steps, 1)
     nbc = (g.n + 31) // 32
@@ -663,7 +673,10 @@ def _newmark_cases_eval(a, nm):
            "prepare_seconds": info.prepare_seconds, "band_bytes": info.band_bytes,
            "df_band_bytes": info.df_band_bytes, "bandwidth_dof": info.bandwidth,
            "last_step_rel_residual": info.last_rel_residual, "graph_nodes": info.graph_nodes,
-           "kernels_per_step": info.kernels_per_step,
+           "kernels_per_step": info.kernels_per_step, "cluster_size": info.cluster_size,
+           "autotune": {"choice": choice, "cache_lines": tune,
+                        "note": "astro_autotune(ASTRO_TUNE_CASES_CLUSTER): the fastest of 2, 4, 8 CTAs per case, "
+                                "seconds per solve of all cases"},
            "solve_chain": {"block_rows_per_sweep": nbc, "us_per_block_row": 1e3 * ms / (2 * nbc),
                            "note": "each step solves every case by forward and backward sweeps over the band's "
                                    "32-row block rows; a row waits for the previous one (one cluster barrier per "

@@ -243,6 +243,12 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
  * emulation measured slower than the FP64 update on the 512-panel batch, so it is kept for
  * comparison and measurement. */
 #define ASTRO_OPT_BAND_FP64_UPDATE 3
+/* The launch shapes astro_autotune picks, set directly (0 = the default): the zero-state brick
+ * kernel's warps per CTA (1, 2, 4), the band factorisation's and the many-column band solve's
+ * CTAs per cluster (2, 4, 8). */
+#define ASTRO_OPT_BRICK_WARPS 4
+#define ASTRO_OPT_PANEL_CLUSTER 5
+#define ASTRO_OPT_CASES_CLUSTER 6
 int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value);
 
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that order their own work
@@ -527,6 +533,24 @@ int astro_newmark_run_states(astro_ctx *ctx, const astro_newmark_opts *opts, con
                              double *disp_history, double *vel_history, double *acc_history,
                              double *int_disp_history, astro_solve_stats *stats);
 
+/* ---- autotuner of the launch shapes (no counterpart in the reference) ----------------------
+ * Times the candidate launch shapes of the selected tunables on this context's model (CUDA events)
+ * and keeps the fastest for the context:
+ *   ASTRO_TUNE_BRICK_WARPS    the zero-state brick kernel's warps per CTA (1, 2, 4): FP32 assembly
+ *                             passes (brick8 meshes; leaves the FP32 assembly resident);
+ *   ASTRO_TUNE_PANEL_CLUSTER  the band factorisation's CTAs per cluster (2, 4, 8): one
+ *                             astro_panels_factor each (needs the FP64 assembly and the scaled
+ *                             constraints); astro_panels_factor with cluster_size 0 then uses it;
+ *   ASTRO_TUNE_CASES_CLUSTER  the many-column band solve's CTAs per cluster (2, 4, 8): solves of
+ *                             the factorisation prepared by the last astro_newmark_cases.
+ * cache_path (may be NULL): a text file of lines "<key> <choice> <seconds>", the key naming the
+ * GPU, the tunable and the model's size; a cached choice is applied without timing, and new
+ * results are appended.  choices (3, may be NULL) receives the context's choices (0 = default). */
+#define ASTRO_TUNE_BRICK_WARPS 1
+#define ASTRO_TUNE_PANEL_CLUSTER 2
+#define ASTRO_TUNE_CASES_CLUSTER 4
+int astro_autotune(astro_ctx *ctx, int32_t what, const char *cache_path, int32_t *choices);
+
 /* ---- batched linear Newmark: many load cases through one factorisation ------------------
  * The dynamic branch of solve with linear geometry (Working/AStrO_commandFunctions.f90:770-812:
  * getElasticSolnLoad(1) with the dynamic flag, scaleElasticMPC, getSparseLDLFact of K_eff once,
@@ -552,6 +576,8 @@ typedef struct astro_newmark_cases_opts {
     int32_t refine;    /* FP64 refinement passes per step (0..4): du -= A^-1 (A du - r) with the
                           residual over the FP64 assembly; the many-column solve runs in
                           double-float (about 48 bits), so ill-conditioned K_eff may want one */
+    int32_t autotune;  /* 1: pick the many-column solve's cluster size by timing (astro_autotune's
+                          ASTRO_TUNE_CASES_CLUSTER) unless the context already holds a choice */
 } astro_newmark_cases_opts;
 typedef struct astro_newmark_cases_info {
     double factor_seconds;     /* band fill + LDL^T (host clock around the launch) */
@@ -564,6 +590,7 @@ typedef struct astro_newmark_cases_info {
     int32_t panels;            /* connected components */
     int32_t graph_nodes;       /* nodes of the captured step */
     int32_t kernels_per_step;  /* kernel launches of one step */
+    int32_t cluster_size;      /* CTAs per case of the many-column solve */
 } astro_newmark_cases_info;
 int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opts *opts, const double *patterns,
                         const double *amplitudes, double *disp, double *vel, double *acc, double *disp_history,

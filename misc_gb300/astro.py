@@ -25,6 +25,7 @@ SOLVER_GMRES_JACOBI_FP64 = 0
 SOLVER_FGMRES_MIXED = 1
 SOLVER_FGMRES_LEARNED = 2
 OPT_BAND_FP64_UPDATE = 3
+OPT_BRICK_WARPS, OPT_PANEL_CLUSTER, OPT_CASES_CLUSTER = 4, 5, 6
 
 _LIB = None
 
@@ -185,17 +186,19 @@ class NewmarkOptsC(C.Structure):
 
 class NewmarkCasesOptsC(C.Structure):
     _fields_ = [("num_steps", C.c_int32), ("num_cases", C.c_int32), ("del_t", C.c_double), ("nm_beta", C.c_double),
-                ("nm_gamma", C.c_double), ("method", C.c_int32), ("no_graph", C.c_int32), ("refine", C.c_int32)]
+                ("nm_gamma", C.c_double), ("method", C.c_int32), ("no_graph", C.c_int32), ("refine", C.c_int32),
+                ("autotune", C.c_int32)]
 
 
 class NewmarkCasesInfoC(C.Structure):
     _fields_ = [("factor_seconds", C.c_double), ("prepare_seconds", C.c_double), ("step_seconds", C.c_double),
                 ("last_rel_residual", C.c_double), ("band_bytes", C.c_int64), ("df_band_bytes", C.c_int64),
                 ("bandwidth", C.c_int32), ("panels", C.c_int32), ("graph_nodes", C.c_int32),
-                ("kernels_per_step", C.c_int32)]
+                ("kernels_per_step", C.c_int32), ("cluster_size", C.c_int32)]
 
 
 NMC_FACTORED = 0
+TUNE_BRICK_WARPS, TUNE_PANEL_CLUSTER, TUNE_CASES_CLUSTER = 1, 2, 4
 
 
 def lib_path():
@@ -263,6 +266,7 @@ def load_library():
                                          C.POINTER(PrecondMlpC)], C.c_int),
         "astro_newmark_run_states": ([vp, C.POINTER(NewmarkOptsC), F64P, F64P, F64P, F64P, F64P, F64P, F64P, F64P,
                                       F64P, F64P, C.POINTER(SolveStatsC)], C.c_int),
+        "astro_autotune": ([vp, C.c_int32, C.c_char_p, C.POINTER(C.c_int32)], C.c_int),
         "astro_newmark_cases": ([vp, C.POINTER(NewmarkCasesOptsC), F64P, F64P, F64P, F64P, F64P, F64P,
                                  C.POINTER(NewmarkCasesInfoC)], C.c_int),
         "astro_update_internal_soln": ([vp, F64P, F64P, F64P], C.c_int),
@@ -629,7 +633,7 @@ class AstroGPU:
         return u, v, a, iu[:ni], hist, st
 
     def newmark_cases(self, del_t, patterns, amplitudes, beta=0.25, gamma=0.5, disp=None, vel=None, acc=None,
-                      history=False, graph=True, method=NMC_FACTORED, refine=0):
+                      history=False, graph=True, method=NMC_FACTORED, refine=0, autotune=False):
         """Batched linear Newmark (astro_newmark_cases): patterns (cases, n), amplitudes (cases,
         steps) in global DOF numbering; returns (disp, vel, acc, history or None, info), states
         (cases, n), history (steps, cases, n)."""
@@ -642,7 +646,7 @@ class AstroGPU:
         v = np.zeros((nc, n)) if vel is None else np.ascontiguousarray(vel, dtype=np.float64).copy()
         a = np.zeros((nc, n)) if acc is None else np.ascontiguousarray(acc, dtype=np.float64).copy()
         hist = np.zeros((steps, nc, n)) if history else None
-        o = NewmarkCasesOptsC(steps, nc, del_t, beta, gamma, method, 0 if graph else 1, refine)
+        o = NewmarkCasesOptsC(steps, nc, del_t, beta, gamma, method, 0 if graph else 1, refine, 1 if autotune else 0)
         info = NewmarkCasesInfoC()
         self._check(self.L.astro_newmark_cases(self.h, C.byref(o), _d(P), _d(Am), _d(u), _d(v), _d(a),
                                                _d(hist) if history else None, C.byref(info)))
@@ -670,6 +674,14 @@ class AstroGPU:
                                                     _d(H["int_disp"]) if ni else None, C.byref(st)))
         H["int_disp"] = H["int_disp"][:, :ni]
         return u, v, a, iu[:ni], H, st
+
+    def autotune(self, what, cache_path=None):
+        """astro_autotune: what = a sum of TUNE_* flags; returns the context's choices (brick warps
+        per CTA, panel cluster size, many-column solve cluster size; 0 = default)."""
+        ch = (C.c_int32 * 3)()
+        self._check(self.L.astro_autotune(self.h, int(what), None if cache_path is None else str(cache_path).encode(),
+                                          ch))
+        return tuple(int(x) for x in ch)
 
     def getdRelasticdD(self, dvar, h=1e-14, state=None):
         """Complex-step dRu/dd of design variable dvar: (global DOF vector, internal-DOF vector)."""

@@ -150,6 +150,10 @@ struct astro_ctx {
     DevBuf d_n2dR, d_n2d, d_n2c, d_dComp, d_secOrig;
     int quirkShellMeanRot = 0;
     int bandFp64Update = 1;  // ASTRO_OPT_BAND_FP64_UPDATE
+    // launch shapes picked by astro_autotune (0: the default)
+    int tuneHex8Warps = 0;   // zero-state brick kernel: warps per CTA (1, 2, 4)
+    int tuneCasesCluster = 0;  // many-column band solve: CTAs per cluster (2, 4, 8)
+    int tunePanelCluster = 0;  // band factorisation: CTAs per cluster (2, 4, 8)
 };
 
 // error helpers
@@ -203,6 +207,7 @@ int precond_mlp_scales_f32(astro_ctx *ctx, const astro_precond_mlp *m, const dou
 int ensure_K(astro_ctx *ctx, int which);          // device BSR value arrays (ctx.cu)
 int ensure_io(astro_ctx *ctx, bool exportMat);    // host-vector staging buffers (ctx.cu)
 int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s);      // panels.cu
+int panels_cases_columns(astro_ctx *ctx);                                   // panels.cu
 void panels_shape(astro_ctx *ctx, int *np, int *bw, long long *bandBytes, double *factorSeconds);
 void thermal_release(astro_ctx *ctx);                                        // thermal.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu

@@ -1261,6 +1261,23 @@ extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
         ctx->bandFp64Update = value ? 1 : 0;
         return ASTRO_OK;
     }
+    if (option == ASTRO_OPT_BRICK_WARPS || option == ASTRO_OPT_PANEL_CLUSTER || option == ASTRO_OPT_CASES_CLUSTER) {
+        const bool ok = option == ASTRO_OPT_BRICK_WARPS ? (value == 0 || value == 1 || value == 2 || value == 4)
+                                                        : (value == 0 || value == 2 || value == 4 || value == 8);
+        if (!ok) return set_err(ctx, ASTRO_ERR_ARG, "launch shape not among the candidates");
+        if (option == ASTRO_OPT_BRICK_WARPS) {
+            ctx->tuneHex8Warps = value;
+            if (ctx->asmExec) cudaGraphExecDestroy(ctx->asmExec);  // the captured pass holds the old shape
+            if (ctx->asmGraph) cudaGraphDestroy(ctx->asmGraph);
+            ctx->asmExec = nullptr;
+            ctx->asmGraph = nullptr;
+        } else if (option == ASTRO_OPT_PANEL_CLUSTER) {
+            ctx->tunePanelCluster = value;
+        } else {
+            ctx->tuneCasesCluster = value;
+        }
+        return ASTRO_OK;
+    }
     return set_err(ctx, ASTRO_ERR_ARG, "unknown option");
 }
 

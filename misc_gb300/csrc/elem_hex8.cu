@@ -99,9 +99,11 @@ constexpr int kRmwSteps = 22;  // ceil(64 blocks / 3 blocks per step)
 
 template <class T> struct FastCfg;
 template <> struct FastCfg<float> {
-    static constexpr int FW = 2, MINB = 14;  // warps per CTA, CTAs per SM (small CTAs: shorter colour tails)
     static constexpr bool PREFETCH = true;
 };
+// The zero-state kernel's warps per CTA (FW) is a template parameter: 1, 2 (the default: small
+// CTAs give shorter colour tails) or 4, picked per context by astro_autotune; the launch bounds ask
+// the register allocator for 28 warps per SM in every case.
 template <class T> struct Hex8FastArgs {
     const int *colorEls;
     int count;
@@ -168,9 +170,8 @@ __device__ __forceinline__ void pair_moments(const GradSmem<float> &S, int a0, i
         M1[6] += gc.z * hb.x; M1[7] += gc.z * hb.y; M1[8] += gc.z * hb.z;
     }
 }
-template <class T, bool ROT>
-__global__ void __launch_bounds__(32 * FastCfg<T>::FW, FastCfg<T>::MINB) hex8_fast_kernel(Hex8FastArgs<T> A) {
-    constexpr int FW = FastCfg<T>::FW;
+template <class T, bool ROT, int FW>
+__global__ void __launch_bounds__(32 * FW, 28 / FW) hex8_fast_kernel(Hex8FastArgs<T> A) {
     constexpr bool PREFETCH = FastCfg<T>::PREFETCH;
     __shared__ GradSmem<T> sG[FW];
     __shared__ T sK[FW][64 * 9];  // element blocks, block j = 8a + b at 9j (row-major 3x3)
@@ -960,8 +961,7 @@ __global__ void k_elem_c(int E, const double *__restrict__ elMat, double *__rest
 
 }  // namespace
 
-template <class T, bool ROT> static void hex8_fast_launch(astro_ctx *ctx, const Hex8FastArgs<T> &A0) {
-    constexpr int FW = FastCfg<T>::FW;
+template <class T, bool ROT, int FW> static void hex8_fast_launch(astro_ctx *ctx, const Hex8FastArgs<T> &A0) {
     Hex8FastArgs<T> A = A0;
     const std::vector<int> &ptr = ctx->c8Ptr;
     for (size_t col = 0; col + 1 < ptr.size(); ++col) {
@@ -969,7 +969,7 @@ template <class T, bool ROT> static void hex8_fast_launch(astro_ctx *ctx, const 
         if (!cnt) continue;
         A.colorEls = dptr<int>(ctx->d_c8Els) + ptr[col];
         A.count = cnt;
-        hex8_fast_kernel<T, ROT><<<(cnt + FW - 1) / FW, 32 * FW, 0, ctx->stream>>>(A);
+        hex8_fast_kernel<T, ROT, FW><<<(cnt + FW - 1) / FW, 32 * FW, 0, ctx->stream>>>(A);
     }
 }
 
@@ -986,10 +986,17 @@ template <class T> static int hex8_fast_run(astro_ctx *ctx, T *K, double *d_ke) 
     A.orient = dptr<double>(ctx->d_secOrient);
     A.K = K;
     A.keOut = d_ke;
-    if (ctx->orientIdentity)
-        hex8_fast_launch<T, false>(ctx, A);
-    else
-        hex8_fast_launch<T, true>(ctx, A);
+    // warps per CTA: the autotuned choice of this context (astro_autotune), else 2
+    switch (ctx->tuneHex8Warps) {
+        case 1:
+            ctx->orientIdentity ? hex8_fast_launch<T, false, 1>(ctx, A) : hex8_fast_launch<T, true, 1>(ctx, A);
+            break;
+        case 4:
+            ctx->orientIdentity ? hex8_fast_launch<T, false, 4>(ctx, A) : hex8_fast_launch<T, true, 4>(ctx, A);
+            break;
+        default:
+            ctx->orientIdentity ? hex8_fast_launch<T, false, 2>(ctx, A) : hex8_fast_launch<T, true, 2>(ctx, A);
+    }
     return cuda_check(ctx, cudaGetLastError(), "brick8 zero-state kernel launch");
 }
 

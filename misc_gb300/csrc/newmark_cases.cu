@@ -256,9 +256,11 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
     if ((rc = astro_scale_mpc(ctx, nullptr, nullptr))) return rc;
     if ((rc = constraint_load_dev(ctx, nullptr, dptr<double>(B.G)))) return rc;  // C^T rhs
     astro_panels_info pinfo{};
-    if ((rc = astro_panels_factor(ctx, 8, &pinfo))) return rc;
+    if ((rc = astro_panels_factor(ctx, 0, &pinfo))) return rc;  // the autotuned cluster size, else 8
     size_t dfBytes = 0;
     if ((rc = panels_cases_prepare(ctx, nc, &dfBytes))) return rc;
+    if (o->autotune && !ctx->tuneCasesCluster && (rc = astro_autotune(ctx, ASTRO_TUNE_CASES_CLUSTER, nullptr, nullptr)))
+        return rc;
     CK(cudaStreamSynchronize(s));
     const double prepSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     // the step as a graph, launched num_steps times
@@ -364,6 +366,7 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
         info->panels = np;
         info->graph_nodes = (int32_t)graphNodes;
         info->kernels_per_step = launches;
+        info->cluster_size = ctx->tuneCasesCluster ? ctx->tuneCasesCluster : 4;
     }
     return ASTRO_OK;
 }

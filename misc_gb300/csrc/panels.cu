@@ -466,8 +466,8 @@ __global__ void __launch_bounds__(kThreads) k_band_solve(const PanelMeta *__rest
 // single large band (a model's K_eff, factored once and solved at every time step) is instead a
 // chain of nbc dependent block rows per sweep, and FP64 runs at about 1/64 of the FP32 rate: one
 // CTA per column would spend tens of microseconds per block row.  So each (panel, column) gets a
-// cluster of kCS CTAs and the arithmetic runs in double-float on the FP32 pipe:
-//   * producer CTAs (ranks 1 .. kCS-1), one warp per tile: for block row I they form
+// cluster of CS CTAs (2, 4 or 8, autotuned) and the arithmetic runs in double-float on the FP32 pipe:
+//   * producer CTAs (ranks 1 .. CS-1), one warp per tile: for block row I they form
 //     sum_{d >= 2} L_{I,I-d} y_{I-d} from the solved rows in their shared-memory ring, reduce it
 //     across the CTA and store it into the leader's shared memory (distributed shared memory);
 //   * the leader (rank 0) forms L_{I,I-1} y_{I-1} from the row it solved last, waits at the
@@ -479,9 +479,7 @@ __global__ void __launch_bounds__(kThreads) k_band_solve(const PanelMeta *__rest
 //   * backward sweep the same with L^T (transposed copies of the tiles and of W) on D^-1 y.
 // The band is copied once into double-float tiles in the forward (column-major) and backward
 // (row-major) layouts, so every tile load of a warp is 32 consecutive float2 per k.
-constexpr int kCS = 4;   // CTAs per cluster
-constexpr int kCW = 8;   // warps per CTA
-constexpr int kProdWarps = (kCS - 1) * kCW;
+constexpr int kCW = 8;   // warps per CTA (the CTAs per cluster, CS, is a template parameter: 2, 4 or 8)
 constexpr int kPrepW = 4;  // warps per CTA of the band copy
 
 struct CaseItem {
@@ -575,6 +573,7 @@ __device__ __forceinline__ void df_tile_rows(DF &acc, const float2 *__restrict__
     acc = df_add(df_norm(acc), df_norm(a2));
 }
 
+template <int CS>
 __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMeta *__restrict__ meta,
                                                                const CaseItem *__restrict__ items,
                                                                const float2 *__restrict__ Lf,
@@ -583,14 +582,15 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                                                                const float2 *__restrict__ Wb,
                                                                const float2 *__restrict__ Dinv, double *X, int nrhs,
                                                                int ring) {
+    constexpr int kProdWarps = (CS - 1) * kCW;
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank();
     extern __shared__ float2 smf[];
     float2 *sRing = smf;                           // [ring][TB]: solved rows
     float2 *sRed = sRing + (size_t)ring * TB;      // [kCW][TB]: per-warp partials
-    float2 *sPart = sRed + kCW * TB;               // [2][kCS][TB]: CTA partials (leader)
-    float2 *sV = sPart + 2 * kCS * TB;             // [TB]
-    const CaseItem it = items[blockIdx.x / kCS];
+    float2 *sPart = sRed + kCW * TB;               // [2][CS][TB]: CTA partials (leader)
+    float2 *sV = sPart + 2 * CS * TB;             // [TB]
+    const CaseItem it = items[blockIdx.x / CS];
     const PanelMeta M = meta[it.panel];
     const int w = threadIdx.x / 32, r = threadIdx.x % 32;
     const int nbc = M.nbc, bt = M.bt;
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             if (w == 0) {
                 DF s = {0.f, 0.f};
                 for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
-                leaderPart[((q & 1) * kCS + rank) * TB + r] = make_float2(s.hi, s.lo);
+                leaderPart[((q & 1) * CS + rank) * TB + r] = make_float2(s.hi, s.lo);
                 cluster_fence();
             }
             cluster_barrier_relaxed();
@@ -683,8 +683,8 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 if (t >= nbc) v = df_mul(v, DF{pd.x, pd.y});
                 DF s = {0.f, 0.f};
                 for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
-                for (int c = 1; c < kCS; ++c) {
-                    const float2 pc = sPart[((q & 1) * kCS + c) * TB + r];
+                for (int c = 1; c < CS; ++c) {
+                    const float2 pc = sPart[((q & 1) * CS + c) * TB + r];
                     s = df_add(s, DF{pc.x, pc.y});
                 }
                 v = df_sub(v, s);
@@ -706,7 +706,7 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 for (int k = 0; k < kCW; ++k) y = df_add(y, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
                 const float2 yv = make_float2(y.hi, y.lo);
                 const size_t slot = (size_t)(I % ring) * TB + r;
-                for (int c = 0; c < kCS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
+                for (int c = 0; c < CS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
                 Xp[(size_t)I * TB + r] = df_to_double(y);
                 cluster_fence();  // the pushed row, ordered before this warp's next arrival
             }
@@ -920,7 +920,7 @@ void panels_release(astro_ctx *ctx) {
 
 extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *info) {
     if (!ctx) return ASTRO_ERR_ARG;
-    if (cluster_size == 0) cluster_size = 8;
+    if (cluster_size == 0) cluster_size = ctx->tunePanelCluster ? ctx->tunePanelCluster : 8;  // autotuned or 8
     if (cluster_size != 1 && cluster_size != 2 && cluster_size != 4 && cluster_size != 8)
         return set_err(ctx, ASTRO_ERR_ARG, "panels: cluster_size must be 1, 2, 4 or 8");
     if (!ctx->haveK64) return set_err(ctx, ASTRO_ERR_STATE, "panels: FP64 stiffness not assembled");
@@ -1124,8 +1124,10 @@ int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
         L->casesCols = ncols;
     }
     L->ring = L->maxBt + 2;
-    const size_t smem = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * kCS * TB + TB);
-    CK(cudaFuncSetAttribute(k_band_solve_cases, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * 8 * TB + TB);
+    CK(cudaFuncSetAttribute(k_band_solve_cases<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_solve_cases<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CK(cudaFuncSetAttribute(k_band_solve_cases<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (bytes) *bytes = 2 * sizeof(float2) * (size_t)L->bandDoubles;
     return cuda_check(ctx, cudaStreamSynchronize(s), "panels cases prepare");
 }
@@ -1141,19 +1143,22 @@ int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s) {
     const unsigned mg = (unsigned)((mv + 255) / 256);
     k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nc, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
                                     dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_X), 1);
+    // CTAs per case: the autotuned choice of this context (astro_autotune), else 4
+    const int cs = (ctx->tuneCasesCluster == 2 || ctx->tuneCasesCluster == 8) ? ctx->tuneCasesCluster : 4;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(L->np * nc * kCS));
+    cfg.gridDim = dim3((unsigned)(L->np * nc * cs));
     cfg.blockDim = dim3(kCW * 32);
-    cfg.dynamicSmemBytes = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * kCS * TB + TB);
+    cfg.dynamicSmemBytes = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * cs * TB + TB);
     cfg.stream = s;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = kCS;
+    at[0].val.clusterDim.x = cs;
     at[0].val.clusterDim.y = 1;
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    CK(cudaLaunchKernelEx(&cfg, k_band_solve_cases, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+    auto kern = cs == 2 ? k_band_solve_cases<2> : (cs == 8 ? k_band_solve_cases<8> : k_band_solve_cases<4>);
+    CK(cudaLaunchKernelEx(&cfg, kern, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
                           (const CaseItem *)dptr<CaseItem>(L->d_items), (const float2 *)dptr<float2>(L->d_Lf),
                           (const float2 *)dptr<float2>(L->d_Lb), (const float2 *)dptr<float2>(L->d_Wf),
                           (const float2 *)dptr<float2>(L->d_Wb), (const float2 *)dptr<float2>(L->d_Dinv),
@@ -1161,6 +1166,12 @@ int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s) {
     k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nc, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
                                     dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_X), 0);
     return cuda_check(ctx, cudaGetLastError(), "panels cases solve");
+}
+
+// Columns of the prepared many-column solve of the current factorisation (0: none prepared).
+int panels_cases_columns(astro_ctx *ctx) {
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    return (L && L->factored && L->dfGen == L->factorGen) ? L->casesCols : 0;
 }
 
 // Shape of the current plan: panels, largest bandwidth (DOF), band bytes, factor seconds.

@@ -135,7 +135,8 @@ def train_mlp(p, seeds, hidden=16, epochs=60, lr=3e-3, white=3, gmres_steps=(10,
     sets = []
     for s in seeds:
         g, b = block_system(M.config4_block(32, 16, 16, s))
-        S = np.vstack([gmres_residuals(g, b, gmres_steps), rng.standard_normal((white, g.n))])
+        parts = [gmres_residuals(g, b, gmres_steps)] if gmres_steps else []
+        S = np.vstack(parts + [rng.standard_normal((white, g.n))])
         sets.append((g, S))
     mlp = mlp_init(hidden, p.degree + 1, seed=seed)
     x = mlp.vector()
@@ -191,18 +192,24 @@ def main():
     ap.add_argument("--epochs", type=int, default=60)
     ap.add_argument("--hidden", type=int, default=16)
     ap.add_argument("--lr", type=float, default=3e-3)
+    ap.add_argument("--white", type=int, default=3, help="white-noise samples per block")
+    ap.add_argument("--gmres-steps", default="10,40,160",
+                    help="GMRES residual samples per block: the step counts (empty: none)")
     a = ap.parse_args()
     t0 = time.time()
     if a.mlp:
         p = precond_init(a.degree, a.ratio, 3)
         seeds = list(range(a.seed0, a.seed0 + a.blocks))
         held = list(range(a.seed0 + a.blocks + 100, a.seed0 + a.blocks + 106))
-        mlp, hist, base = train_mlp(p, seeds, hidden=a.hidden, epochs=a.epochs, lr=a.lr)
+        gsteps = tuple(int(x) for x in a.gmres_steps.split(",") if x.strip())
+        mlp, hist, base = train_mlp(p, seeds, hidden=a.hidden, epochs=a.epochs, lr=a.lr, white=a.white,
+                                    gmres_steps=gsteps)
         t1 = time.time()
         val = validate_mlp(p, mlp, held)
         meta = {"family": "config-4 32x16x16 brick blocks (model.config4_block)", "training_seeds": [seeds[0], seeds[-1]],
                 "held_out_seeds": held,
-                "samples_per_block": "GMRES residuals after 10, 40, 160 steps + 3 white-noise vectors",
+                "samples_per_block": (f"GMRES residuals after {', '.join(map(str, gsteps))} steps + " if gsteps else "") +
+                                     f"{a.white} white-noise vectors",
                 "optimizer": f"Adam lr {a.lr}, {a.epochs} epochs", "hidden": a.hidden, "loss_unmodulated": base,
                 "loss_per_epoch": hist, "train_seconds": t1 - t0, "validation": val}
         print(json.dumps({k: v for k, v in meta.items() if k != "loss_per_epoch"}))
