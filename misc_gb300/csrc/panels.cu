@@ -554,6 +554,15 @@ __device__ __forceinline__ void cluster_barrier_relaxed() {
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
 
+// sum of v[0 .. K-1] pairwise (log2 K dependent additions instead of K - 1)
+template <int K> __device__ __forceinline__ DF df_tree_sum(DF (&v)[K]) {
+#pragma unroll
+    for (int st = 1; st < K; st *= 2)
+#pragma unroll
+        for (int i = 0; i + st < K; i += 2 * st) v[i] = df_add(v[i], v[i + st]);
+    return v[0];
+}
+
 // acc[r] += sum_{k in [k0, k1)} T[k * TB + r] v[k] (T a DF tile in global memory, v in shared)
 __device__ __forceinline__ void df_tile_rows(DF &acc, const float2 *__restrict__ T, const float2 *v, int r, int k0,
                                              int k1) {
@@ -660,8 +669,10 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
             __syncthreads();
             if (w == 0) {
-                DF s = {0.f, 0.f};
-                for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                DF pv[kCW];
+#pragma unroll
+                for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
+                const DF s = df_tree_sum(pv);
                 leaderPart[((q & 1) * CS + rank) * TB + r] = make_float2(s.hi, s.lo);
                 cluster_fence();
             }
@@ -681,13 +692,16 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             if (w == 0) {
                 DF v = df_from_double(pb);
                 if (t >= nbc) v = df_mul(v, DF{pd.x, pd.y});
-                DF s = {0.f, 0.f};
-                for (int k = 0; k < kCW; ++k) s = df_add(s, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                DF pv[kCW + CS];  // the leader's warps' partials, then the producers' (slot CS: zero)
+#pragma unroll
+                for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
+                pv[kCW] = DF{0.f, 0.f};
+#pragma unroll
                 for (int c = 1; c < CS; ++c) {
                     const float2 pc = sPart[((q & 1) * CS + c) * TB + r];
-                    s = df_add(s, DF{pc.x, pc.y});
+                    pv[kCW + c] = DF{pc.x, pc.y};
                 }
-                v = df_sub(v, s);
+                v = df_sub(v, df_tree_sum(pv));
                 sV[r] = make_float2(v.hi, v.lo);
             }
             __syncthreads();
@@ -702,8 +716,10 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             sRed[w * TB + r] = make_float2(a.hi, a.lo);
             __syncthreads();
             if (w == 0) {
-                DF y = {0.f, 0.f};
-                for (int k = 0; k < kCW; ++k) y = df_add(y, DF{sRed[k * TB + r].x, sRed[k * TB + r].y});
+                DF pv[kCW];
+#pragma unroll
+                for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
+                const DF y = df_tree_sum(pv);
                 const float2 yv = make_float2(y.hi, y.lo);
                 const size_t slot = (size_t)(I % ring) * TB + r;
                 for (int c = 0; c < CS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
