@@ -448,12 +448,22 @@ def _learned_eval(a):
         p, src = precond_init(a.precond_degree, a.precond_ratio, 3), {"network": "Chebyshev initialisation"}
     out = {"workload": f"{nx}x{nx // 2}x{nx // 2} brick8, correlated log-normal E (corr 0.5 width, sigma 0.65, "
                        f"seed 4000)", "dof": g.n, "rtol": 1e-8, "setup_seconds": setup}
-    runs = [("fgmres_learned", SOLVER_FGMRES_LEARNED, p)]
+    # the per-node modulation trained on the config-4 family (committed weights), run beside
+    mpath = os.path.join(ROOT, "misc_gb300", "data", "precond_mlp_cfg4.json")
+    mlp = None
+    if os.path.exists(mpath):
+        with open(mpath) as f:
+            dm = json.load(f)
+        pm, mlp = LN.mlp_from_json(dm)
+    runs = [("fgmres_learned", SOLVER_FGMRES_LEARNED, p, None)]
+    if mlp is not None:
+        runs.append(("fgmres_learned_modulated", SOLVER_FGMRES_LEARNED, pm, mlp))
     if not a.no_fp64:
-        runs.append(("gmres_fp64", SOLVER_GMRES_JACOBI_FP64, None))
+        runs.append(("gmres_fp64", SOLVER_GMRES_JACOBI_FP64, None, None))
     sols = {}
-    for name, meth, pc in runs:
-        kw = dict(method=meth, rtol=1e-8, restart=50, max_iters=a.solve_max_iters, allow_maxit=True, precond=pc)
+    for name, meth, pc, ml in runs:
+        kw = dict(method=meth, rtol=1e-8, restart=50, max_iters=a.solve_max_iters, allow_maxit=True, precond=pc,
+                  mlp=ml)
         _, s1 = g.solve_static(b, **kw)
         # the FP32 matrix assembled again (same values): the second, timed learned solve rebuilds
         # its FP16 operator and eigenvalue estimate; workspace and captured graph are reused
@@ -465,6 +475,13 @@ def _learned_eval(a):
                      "conditional_graph": s2.conditional_graph, "fallback": s2.fallback,
                      "residual_kind": s2.residual_kind}
     out["fgmres_learned"].update({"degree": p.degree, "ratio": p.ratio, **src})
+    if "fgmres_learned_modulated" in out:
+        out["fgmres_learned_modulated"].update({
+            "network": "trained", "hidden": mlp.hidden, "training": {k: dm["meta"].get(k) for k in (
+                "family", "training_seeds", "samples_per_block", "optimizer", "loss_unmodulated")},
+            "loss_last_epoch": dm["meta"]["loss_per_epoch"][-1],
+            "note": "the per-node modulation (astro_precond_mlp) trained on 48 blocks of the family: its objective "
+                    "falls 3x, the Krylov step count does not (a recorded negative result)"})
     if "gmres_fp64" in out:
         out["speedup_vs_fp64_gmres"] = out["gmres_fp64"]["seconds"] / out["fgmres_learned"]["seconds"]
         # both solutions against a tighter FP64 solve (Jacobi-GMRES to 1e-12, warm-started from the
