@@ -546,13 +546,7 @@ __device__ __forceinline__ void cluster_barrier() {
     asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
     asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
 }
-// The cluster barrier of the many-column solve: only the warps that stored into distributed shared
-// memory fence (release, before they arrive); every thread arrives relaxed and waits with acquire.
-__device__ __forceinline__ void cluster_fence() { asm volatile("fence.acq_rel.cluster;\n" ::: "memory"); }
-__device__ __forceinline__ void cluster_barrier_relaxed() {
-    asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
-    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
-}
+
 
 // sum of v[0 .. K-1] pairwise (log2 K dependent additions instead of K - 1)
 template <int K> __device__ __forceinline__ DF df_tree_sum(DF (&v)[K]) {
@@ -674,9 +668,8 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
                 const DF s = df_tree_sum(pv);
                 leaderPart[((q & 1) * CS + rank) * TB + r] = make_float2(s.hi, s.lo);
-                cluster_fence();
             }
-            cluster_barrier_relaxed();
+            cluster_barrier();
         } else {
             // L_{I,I+-1} times the row solved last, split over the warps by k
             DF acc = {0.f, 0.f};
@@ -687,8 +680,7 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 acc = df_norm(acc);
             }
             sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
-            __threadfence_block();  // this CTA's partials, read by warp 0 after the barrier
-            cluster_barrier_relaxed();
+            cluster_barrier();
             if (w == 0) {
                 DF v = df_from_double(pb);
                 if (t >= nbc) v = df_mul(v, DF{pd.x, pd.y});
@@ -724,13 +716,12 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                 const size_t slot = (size_t)(I % ring) * TB + r;
                 for (int c = 0; c < CS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
                 Xp[(size_t)I * TB + r] = df_to_double(y);
-                cluster_fence();  // the pushed row, ordered before this warp's next arrival
             }
             prefetch(t + 1);  // after the row's store: the first backward row reads it back
         }
         // the forward sweep's last rows are pushed before the backward sweep, and every row
         // before any CTA exits
-        if (t == nbc - 1 || t == 2 * nbc - 1) cluster_barrier_relaxed();
+        if (t == nbc - 1 || t == 2 * nbc - 1) cluster_barrier();
     }
 }
 
