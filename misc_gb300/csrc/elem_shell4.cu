@@ -44,6 +44,10 @@ int shell_sections_prepare(astro_ctx *ctx, const astro_model *m) {
     const int S = m->num_sections, E = ctx->P.E;
     std::vector<int> lr(S + 1);
     for (int s = 0; s <= S; ++s) lr[s] = m->sec_layup_range[s];
+    // the layer loops of the section properties run over lr[s] .. lr[s+1]: a prefix sum from 0
+    if (lr[0] != 0) return set_err(ctx, ASTRO_ERR_ARG, "sec_layup_range must start at 0");
+    for (int s = 0; s < S; ++s)
+        if (lr[s + 1] < lr[s]) return set_err(ctx, ASTRO_ERR_ARG, "sec_layup_range must be nondecreasing");
     const int NL = lr[S];
     std::vector<LayerDev> lay(std::max(NL, 1));
     ctx->layMat.assign(m->layup_mat_id, m->layup_mat_id + NL);
