@@ -93,7 +93,7 @@ struct PanelPlan {
     // double-float copies for the many-column solve (k_band_solve_cases), built from factor
     // generation dfGen; the items and the right-hand-side block for casesCols columns
     int factorGen = 0, dfGen = -1, casesCols = 0, ring = 0;
-    DevBuf d_Lf, d_Lb, d_Wf, d_Wb, d_Dinv, d_items, d_X, d_Mf, d_Mb;
+    DevBuf d_Lf, d_Lb, d_Wf, d_Wb, d_Dinv, d_items, d_X;
 };
 
 __device__ __forceinline__ size_t tile_off(const PanelMeta &M, int J, int d) {
@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(kThreads) k_band_solve(const PanelMeta *__rest
 // The band is copied once into double-float tiles in the forward (column-major) and backward
 // (row-major) layouts, so every tile load of a warp is 32 consecutive float2 per k.
 constexpr int kCW = 8;   // warps per CTA (the CTAs per cluster, CS, is a template parameter: 2, 4 or 8)
-constexpr int kPrepW = 2;  // warps per CTA of the band copy (two 32 x 33 FP64 tiles each in shared memory)
+constexpr int kPrepW = 4;  // warps per CTA of the band copy
 
 struct CaseItem {
     int panel, col;
@@ -490,10 +490,8 @@ struct CaseItem {
 // column W = L_JJ^-1 (unit lower) in both layouts and D^-1, one warp per block column
 __global__ void k_band_dfprep(const PanelMeta *__restrict__ meta, int np, const double *__restrict__ band,
                               float2 *__restrict__ Lf, float2 *__restrict__ Lb, float2 *__restrict__ Wf,
-                              float2 *__restrict__ Wb, float2 *__restrict__ Dinv, float2 *__restrict__ Mf,
-                              float2 *__restrict__ Mb) {
+                              float2 *__restrict__ Wb, float2 *__restrict__ Dinv) {
     __shared__ double sT[kPrepW][TB][TB + 1];
-    __shared__ double sW[kPrepW][TB][TB + 1];
     const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
     // global block-column index over all panels
     long long gJ = (long long)blockIdx.x * kPrepW + w;
@@ -542,38 +540,6 @@ __global__ void k_band_dfprep(const PanelMeta *__restrict__ meta, int np, const 
     }
     const DF dv = df_from_double(1.0 / sT[w][lane][lane]);
     Dinv[(size_t)M.xUnit + (size_t)J * TB + lane] = make_float2(dv.hi, dv.lo);
-    // the products that fold the previous row's diagonal-neighbour tile into W (column `lane`):
-    // forward M_J = W_J L_{J,J-1} (tile (J-1, 1)), backward M'_J = W_J^T L_{J+1,J}^T (tile (J, 1)),
-    // both stored column-major like the tiles
-#pragma unroll
-    for (int i = 0; i < TB; ++i) sW[w][i][lane] = x[i];
-    __syncwarp();
-    if (M.bt >= 1 && J >= 1) {
-        const double *Lt = band + tile_off(M, J - 1, 1);  // L[k][c] at c * TB + k
-        double lc[TB];
-#pragma unroll
-        for (int k = 0; k < TB; ++k) lc[k] = Lt[(size_t)lane * TB + k];
-        for (int i = 0; i < TB; ++i) {
-            double v = 0.0;
-#pragma unroll
-            for (int k = 0; k < TB; ++k) v += sW[w][i][k] * lc[k];
-            const DF m = df_from_double(v);
-            Mf[ow + (size_t)lane * TB + i] = make_float2(m.hi, m.lo);
-        }
-    }
-    if (M.bt >= 1 && J + 1 < M.nbc) {
-        const double *Lt = band + tile_off(M, J, 1);  // L_{J+1,J}[c][k] at k * TB + c
-        double lr[TB];
-#pragma unroll
-        for (int k = 0; k < TB; ++k) lr[k] = Lt[(size_t)k * TB + lane];
-        for (int i = 0; i < TB; ++i) {
-            double v = 0.0;
-#pragma unroll
-            for (int k = 0; k < TB; ++k) v += sW[w][k][i] * lr[k];  // (W^T)[i][k] L^T[k][lane]
-            const DF m = df_from_double(v);
-            Mb[ow + (size_t)lane * TB + i] = make_float2(m.hi, m.lo);
-        }
-    }
 }
 
 __device__ __forceinline__ void cluster_barrier() {
@@ -617,8 +583,6 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
                                                                const float2 *__restrict__ Lb,
                                                                const float2 *__restrict__ Wf,
                                                                const float2 *__restrict__ Wb,
-                                                               const float2 *__restrict__ Mf,
-                                                               const float2 *__restrict__ Mb,
                                                                const float2 *__restrict__ Dinv, double *X, int nrhs,
                                                                int ring) {
     constexpr int kProdWarps = (CS - 1) * kCW;
@@ -628,7 +592,7 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
     float2 *sRing = smf;                           // [ring][TB]: solved rows
     float2 *sRed = sRing + (size_t)ring * TB;      // [kCW][TB]: per-warp partials
     float2 *sPart = sRed + kCW * TB;               // [2][CS][TB]: CTA partials (leader)
-    float2 *sV = sPart + 2 * CS * TB;              // [TB]
+    float2 *sV = sPart + 2 * CS * TB;             // [TB]
     const CaseItem it = items[blockIdx.x / CS];
     const PanelMeta M = meta[it.panel];
     const int w = threadIdx.x / 32, r = threadIdx.x % 32;
@@ -646,24 +610,16 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
         return t < nbc ? Lf + tile_off(M, I - d, d) : Lb + tile_off(M, I, d);
     };
     auto srcOf = [&](int t, int d) { return t < nbc ? rowOf(t) - d : rowOf(t) + d; };
-    // With W_I = L_II^-1 and M_I = W_I L_{I,I-1} (backward: W_I^T and W_I^T L_{I+1,I}^T):
-    //   y_I = W_I b_I - M_I y_{I-1} - W_I sum_{d >= 2} L_{I,I-d} y_{I-d}.
-    // The producers form the last term (their tiles, then W_I applied to their CTA's sum, one row
-    // ahead of the leader); the leader forms W_I b_I - M_I y_{I-1} split over its warps before the
-    // cluster barrier, and after it warp 0 only subtracts the producers' parts and pushes y_I.
-    // Every warp's next operands are loaded into registers one step ahead: producers the first
-    // tile of the warp (pf, the lane's row of it) and their four columns of W (pw), the leader
-    // its four columns of W and of M (pw, pm) and the right-hand side's four entries (pb, with
-    // D^-1 in the backward sweep).
+    // Each warp's next tile is loaded into registers one step ahead, so the loads are in flight
+    // during the cluster barrier and the leader's part of the step: producers the first tile of
+    // the warp (pf, the lane's row of it), the leader its four columns of L_{I,I+-1} (pl) and of
+    // W (pw), and warp 0 the right-hand side (pb) and D^-1 (pd).
     const int d0 = 2 + (rank - 1) * kCW + w;
-    float2 pf[TB], pw[4], pm[4], pd[4];
-    double pb[4];
+    float2 pf[TB], pl[4], pw[4], pd = make_float2(0.f, 0.f);
+    double pb = 0.0;
     auto prefetch = [&](int t) {
         if (t >= 2 * nbc) return;
         const int dm = dmaxOf(t), I = rowOf(t);
-        const float2 *Wt = (t < nbc ? Wf : Wb) + wOff + (size_t)I * TT;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) pw[k] = __ldg(Wt + (4 * w + k) * TB + r);
         if (rank > 0) {
             if (d0 <= dm) {
                 const float2 *T = tileOf(t, d0);
@@ -672,14 +628,16 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             }
         } else {
             if (dm >= 1) {
-                const float2 *Mt = (t < nbc ? Mf : Mb) + wOff + (size_t)I * TT;
+                const float2 *T = tileOf(t, 1);
 #pragma unroll
-                for (int k = 0; k < 4; ++k) pm[k] = __ldg(Mt + (4 * w + k) * TB + r);
+                for (int k = 0; k < 4; ++k) pl[k] = __ldg(T + (4 * w + k) * TB + r);
             }
+            const float2 *Wt = (t < nbc ? Wf : Wb) + wOff + (size_t)I * TT;
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                pb[k] = Xp[(size_t)I * TB + 4 * w + k];
-                if (t >= nbc) pd[k] = __ldg(Dinv + M.xUnit + (size_t)I * TB + 4 * w + k);
+            for (int k = 0; k < 4; ++k) pw[k] = __ldg(Wt + (4 * w + k) * TB + r);
+            if (w == 0) {
+                pb = Xp[(size_t)I * TB + r];
+                if (t >= nbc) pd = __ldg(Dinv + M.xUnit + (size_t)I * TB + r);
             }
         }
     };
@@ -701,17 +659,45 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             }
             for (int d = d0 + kProdWarps; d <= dmax; d += kProdWarps)
                 df_tile_rows(acc, tileOf(t, d), sRing + (size_t)(srcOf(t, d) % ring) * TB, r, 0, TB);
+            prefetch(t + 1);
             sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
             __syncthreads();
             if (w == 0) {
                 DF pv[kCW];
 #pragma unroll
                 for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
-                const DF sum = df_tree_sum(pv);
-                sV[r] = make_float2(sum.hi, sum.lo);
+                const DF s = df_tree_sum(pv);
+                leaderPart[((q & 1) * CS + rank) * TB + r] = make_float2(s.hi, s.lo);
+            }
+            cluster_barrier();
+        } else {
+            // L_{I,I+-1} times the row solved last, split over the warps by k
+            DF acc = {0.f, 0.f};
+            if (dmax >= 1) {
+                const float2 *v = sRing + (size_t)(srcOf(t, 1) % ring) * TB + 4 * w;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) df_acc(acc, pl[k].x, pl[k].y, v[k].x, v[k].y);
+                acc = df_norm(acc);
+            }
+            sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
+            cluster_barrier();
+            if (w == 0) {
+                DF v = df_from_double(pb);
+                if (t >= nbc) v = df_mul(v, DF{pd.x, pd.y});
+                DF pv[kCW + CS];  // the leader's warps' partials, then the producers' (slot CS: zero)
+#pragma unroll
+                for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
+                pv[kCW] = DF{0.f, 0.f};
+#pragma unroll
+                for (int c = 1; c < CS; ++c) {
+                    const float2 pc = sPart[((q & 1) * CS + c) * TB + r];
+                    pv[kCW + c] = DF{pc.x, pc.y};
+                }
+                v = df_sub(v, df_tree_sum(pv));
+                sV[r] = make_float2(v.hi, v.lo);
             }
             __syncthreads();
-            // W_I (backward W_I^T) times the CTA's sum, split over the warps by k
+            // y_I = W v (forward) or x_I = W^T v (backward), split over the warps by k
             DF a = {0.f, 0.f};
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
@@ -721,53 +707,17 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             a = df_norm(a);
             sRed[w * TB + r] = make_float2(a.hi, a.lo);
             __syncthreads();
-            prefetch(t + 1);
             if (w == 0) {
                 DF pv[kCW];
 #pragma unroll
                 for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
-                const DF sum = df_tree_sum(pv);
-                leaderPart[((q & 1) * CS + rank) * TB + r] = make_float2(sum.hi, sum.lo);
-            }
-            cluster_barrier();
-        } else {
-            // W_I c - M_I s over this warp's four k, c the right-hand side (backward D^-1 y_I),
-            // s the row solved last
-            DF acc = {0.f, 0.f};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                DF c = df_from_double(pb[k]);
-                if (t >= nbc) c = df_mul(c, DF{pd[k].x, pd[k].y});
-                df_acc(acc, pw[k].x, pw[k].y, c.hi, c.lo);
-            }
-            if (dmax >= 1) {
-                const float2 *v = sRing + (size_t)(srcOf(t, 1) % ring) * TB + 4 * w;
-#pragma unroll
-                for (int k = 0; k < 4; ++k) df_acc(acc, -pm[k].x, -pm[k].y, v[k].x, v[k].y);
-            }
-            acc = df_norm(acc);
-            sRed[w * TB + r] = make_float2(acc.hi, acc.lo);
-            cluster_barrier();
-            if (w == 0) {
-                DF pv[kCW + CS];  // the leader's warps' partials, then minus the producers' (slot kCW: zero)
-#pragma unroll
-                for (int k = 0; k < kCW; ++k) pv[k] = DF{sRed[k * TB + r].x, sRed[k * TB + r].y};
-                pv[kCW] = DF{0.f, 0.f};
-#pragma unroll
-                for (int c = 1; c < CS; ++c) {
-                    const float2 pc = sPart[((q & 1) * CS + c) * TB + r];
-                    pv[kCW + c] = DF{-pc.x, -pc.y};
-                }
                 const DF y = df_tree_sum(pv);
                 const float2 yv = make_float2(y.hi, y.lo);
                 const size_t slot = (size_t)(I % ring) * TB + r;
                 for (int c = 0; c < CS; ++c) cl.map_shared_rank(sRing, c)[slot] = yv;
                 Xp[(size_t)I * TB + r] = df_to_double(y);
             }
-            // the backward sweep's first row reads the forward sweep's last row back: the leader's
-            // warps synchronise so warp 0's store of it precedes their loads
-            if (t == nbc - 1) __syncthreads();
-            prefetch(t + 1);
+            prefetch(t + 1);  // after the row's store: the first backward row reads it back
         }
         // the forward sweep's last rows are pushed before the backward sweep, and every row
         // before any CTA exits
@@ -951,7 +901,7 @@ void plan_free(PanelPlan *L) {
     DevBuf *b[] = {&L->d_meta,  &L->d_sched, &L->d_schedPtr, &L->d_panelOf, &L->d_pos,  &L->d_band,
                    &L->d_status, &L->d_penI, &L->d_penJ,     &L->d_penV,    &L->d_slices, &L->d_sexp,
                    &L->d_Lf,    &L->d_Lb,    &L->d_Wf,       &L->d_Wb,      &L->d_Dinv,  &L->d_items,
-                   &L->d_X,     &L->d_Mf,    &L->d_Mb};
+                   &L->d_X};
     for (DevBuf *x : b) dev_free(*x);
 }
 
@@ -1158,18 +1108,13 @@ int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
         const size_t nb = (size_t)L->bandDoubles, nd = (size_t)L->xRows;
         if ((rc = dev_alloc(ctx, L->d_Lf, sizeof(float2) * nb)) || (rc = dev_alloc(ctx, L->d_Lb, sizeof(float2) * nb)) ||
             (rc = dev_alloc(ctx, L->d_Wf, sizeof(float2) * nd * TB)) ||
-            (rc = dev_alloc(ctx, L->d_Wb, sizeof(float2) * nd * TB)) || (rc = dev_alloc(ctx, L->d_Dinv, sizeof(float2) * nd)) ||
-            (rc = dev_alloc(ctx, L->d_Mf, sizeof(float2) * nd * TB)) || (rc = dev_alloc(ctx, L->d_Mb, sizeof(float2) * nd * TB)))
+            (rc = dev_alloc(ctx, L->d_Wb, sizeof(float2) * nd * TB)) || (rc = dev_alloc(ctx, L->d_Dinv, sizeof(float2) * nd)))
             return rc;
-        // rows without a neighbour tile keep zero products
-        CK(cudaMemsetAsync(L->d_Mf.p, 0, sizeof(float2) * nd * TB, s));
-        CK(cudaMemsetAsync(L->d_Mb.p, 0, sizeof(float2) * nd * TB, s));
         long long cols = 0;
         for (const PanelMeta &M : L->meta) cols += M.nbc;
         k_band_dfprep<<<(unsigned)((cols + kPrepW - 1) / kPrepW), kPrepW * 32, 0, s>>>(
             dptr<PanelMeta>(L->d_meta), L->np, dptr<double>(L->d_band), dptr<float2>(L->d_Lf), dptr<float2>(L->d_Lb),
-            dptr<float2>(L->d_Wf), dptr<float2>(L->d_Wb), dptr<float2>(L->d_Dinv), dptr<float2>(L->d_Mf),
-            dptr<float2>(L->d_Mb));
+            dptr<float2>(L->d_Wf), dptr<float2>(L->d_Wb), dptr<float2>(L->d_Dinv));
         if ((rc = cuda_check(ctx, cudaGetLastError(), "band double-float copy"))) return rc;
         L->dfGen = L->factorGen;
     }
@@ -1223,8 +1168,7 @@ int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s) {
     CK(cudaLaunchKernelEx(&cfg, kern, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
                           (const CaseItem *)dptr<CaseItem>(L->d_items), (const float2 *)dptr<float2>(L->d_Lf),
                           (const float2 *)dptr<float2>(L->d_Lb), (const float2 *)dptr<float2>(L->d_Wf),
-                          (const float2 *)dptr<float2>(L->d_Wb), (const float2 *)dptr<float2>(L->d_Mf),
-                          (const float2 *)dptr<float2>(L->d_Mb), (const float2 *)dptr<float2>(L->d_Dinv),
+                          (const float2 *)dptr<float2>(L->d_Wb), (const float2 *)dptr<float2>(L->d_Dinv),
                           dptr<double>(L->d_X), nc, L->ring));
     k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nc, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
                                     dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_X), 0);
