@@ -50,7 +50,14 @@ extern "C" {
                                           (r_getNodeCoord, :945-968) */
 #define ASTRO_DCAT_NODE_LOAD 9         /* 'nodeLoad' / 'elastic': nodal load component d_component (1..6) at the
                                           nodes of nd_to_d while d_act_time[0] < t < d_act_time[1]
-                                          (r_getNodeDLoad, :970-994) */
+                                          (r_getNodeDLoad, :970-994); d_component 7 = 'nodeLoad' / 'thermal',
+                                          the nodal heat input ndLd(7) */
+#define ASTRO_DCAT_THERMAL_COND 10     /* 'thermalCond': materialThermCond entry d_component (1..6: k11 k22 k33
+                                          k12 k13 k23) of a solid (r_getMaterialThermCond, :129-161) */
+#define ASTRO_DCAT_SPEC_HEAT 11        /* 'specHeat': solid specific heat (r_getMaterialSpecHeat, :164-186) */
+#define ASTRO_DCAT_LAYUP_THERMAL_COND 12 /* 'layup' / 'thermalCond': conductivity entry d_component (1..6) of layer
+                                            d_layer (r_getShellThermCond, :556) */
+#define ASTRO_DCAT_LAYUP_SPEC_HEAT 13  /* 'layup' / 'specHeat' of layer d_layer (r_getShellSpecHeat, :630) */
 
 /* Model arrays: the reference's module globals (Working/AStrO_globalData.f90) as flat arrays.
  * Element types: 8 = brick8 (2x2x2 Gauss), 81 = brickIM (brick8 plus three incompatible bubbles,
@@ -422,6 +429,35 @@ int astro_thermal_surface_flux(astro_ctx *ctx, int32_t nfaces, const int32_t *fa
  * its skyline LDL^T preconditioner on the thermal system, stepSolve :689-703). */
 int astro_thermal_solve(astro_ctx *ctx, const double *rhs, double *dtemp, double rtol, int32_t max_iters,
                         astro_solve_stats *stats);
+
+/* Thermal design sensitivities: getdRthermaldD (Working/AStrO_commandFunctions.f90:1016-1170).
+ * The design variables act on the thermal properties as the property routines apply them
+ * (Working/AStrO_r_designPropertyFunctions.f90): solids take 'thermalCond' (ASTRO_DCAT_THERMAL_COND),
+ * 'specHeat' and 'density' (the heat capacity is density x specific heat); shells take the
+ * layer's 'layup' thermalCond, specHeat, density, thickness and angle; node coordinates and
+ * solid orientation variables move the element geometry.  The real values d_value enter
+ * astro_thermal_setup's properties.
+ *
+ * Element part (:1040-1059): drtdd[N] (rank order) is zeroed, then for every element that depends
+ * on dvar (its el_to_d terms, or a nodeCoord term of one of its nodes) Rt is evaluated in complex
+ * FP64 with d_value(dvar) + i h at the given thermal state (capacitance included when dynamic)
+ * and Im(Rt) / h is added at the element's nodes: properties, section frame (orientation
+ * variables; correctAlpha for shells) and node coordinates all in complex arithmetic. */
+int astro_thermal_drdd(astro_ctx *ctx, int32_t dvar, double h, const astro_thermal_state *state, double *drtdd);
+/* bodyHeatGen branch (:1065-1108): drtdd -= d(heat-generation load)/d(dvar) for the listed
+ * elements (1-based, NULL = all; an element listed twice counts twice) that depend on dvar,
+ * by the complex step of the load (shell thickness, node coordinates). */
+int astro_thermal_heat_gen_drdd(astro_ctx *ctx, int32_t dvar, double h, double q, const int32_t *elements,
+                                int32_t count, double *drtdd);
+/* surfaceFlux branch (:1109-1152): drtdd += d(component-1 face load)/d(dvar) for the given faces
+ * whose element depends on dvar (node coordinates move the face). */
+int astro_thermal_surface_flux_drdd(astro_ctx *ctx, int32_t dvar, double h, int32_t nfaces, const int32_t *face_el,
+                                    const int32_t *face_num, double flux, double *drtdd);
+/* Nodal thermal design loads ('nodeLoad' / 'thermal', ASTRO_DCAT_NODE_LOAD with d_component 7):
+ * getThermalAppliedLoad's closing loop (:182-186) thermal_load[rank] += the active variables'
+ * coef x d, and getdRthermaldD's node branch (:1162-1167) drtdd[rank] -= coef for dvar. */
+int astro_thermal_design_node_load(astro_ctx *ctx, double time, double *thermal_load);
+int astro_thermal_node_load_drdd(astro_ctx *ctx, int32_t dvar, double time, double *drtdd);
 
 /* ---- batched panels ----------------------------------------------------------------------- */
 

@@ -245,6 +245,12 @@ def load_library():
         "astro_thermal_heat_gen": ([vp, C.c_double, I32P, C.c_int32, F64P], C.c_int),
         "astro_thermal_surface_flux": ([vp, C.c_int32, I32P, I32P, C.c_double, F64P], C.c_int),
         "astro_thermal_solve": ([vp, F64P, F64P, C.c_double, C.c_int32, C.POINTER(SolveStatsC)], C.c_int),
+        "astro_thermal_drdd": ([vp, C.c_int32, C.c_double, C.POINTER(ThermalStateC), F64P], C.c_int),
+        "astro_thermal_heat_gen_drdd": ([vp, C.c_int32, C.c_double, C.c_double, I32P, C.c_int32, F64P], C.c_int),
+        "astro_thermal_surface_flux_drdd": ([vp, C.c_int32, C.c_double, C.c_int32, I32P, I32P, C.c_double, F64P],
+                                            C.c_int),
+        "astro_thermal_design_node_load": ([vp, C.c_double, F64P], C.c_int),
+        "astro_thermal_node_load_drdd": ([vp, C.c_int32, C.c_double, F64P], C.c_int),
         "astro_panels_factor": ([vp, C.c_int32, C.POINTER(PanelsInfoC)], C.c_int),
         "astro_panels_solve": ([vp, C.c_int32, F64P, F64P, C.POINTER(PanelsInfoC)], C.c_int),
         "astro_panels_solve_batched": ([vp, C.c_int32, F64P, F64P, C.POINTER(PanelsInfoC)], C.c_int),
@@ -548,6 +554,38 @@ class AstroGPU:
         self._check(self.L.astro_thermal_solve(self.h, _d(_f64(rhs)), _d(x), float(rtol), int(max_iters),
                                                C.byref(st)))
         return x, st
+
+    def thermal_drdd(self, dvar, h=1e-14, state=None):
+        """getdRthermaldD element part: dRt/d(dvar) in rank order by the device complex step."""
+        out = np.zeros(self.model.num_nodes)
+        self._check(self.L.astro_thermal_drdd(self.h, int(dvar), float(h), C.byref(state) if state is not None else None,
+                                              _d(out)))
+        return out
+
+    def thermal_heat_gen_drdd(self, dvar, q, elements=None, h=1e-14, drtdd=None):
+        drtdd = np.zeros(self.model.num_nodes) if drtdd is None else drtdd
+        els = None if elements is None else _i32(elements)
+        self._check(self.L.astro_thermal_heat_gen_drdd(self.h, int(dvar), float(h), float(q),
+                                                       None if els is None else _i(els), 0 if els is None else len(els),
+                                                       _d(drtdd)))
+        return drtdd
+
+    def thermal_surface_flux_drdd(self, dvar, face_el, face_num, flux, h=1e-14, drtdd=None):
+        drtdd = np.zeros(self.model.num_nodes) if drtdd is None else drtdd
+        fe, fn = _i32(face_el), _i32(face_num)
+        self._check(self.L.astro_thermal_surface_flux_drdd(self.h, int(dvar), float(h), len(fe), _i(fe), _i(fn),
+                                                           float(flux), _d(drtdd)))
+        return drtdd
+
+    def thermal_design_node_load(self, t, thermal_load=None):
+        load = np.zeros(self.model.num_nodes) if thermal_load is None else thermal_load
+        self._check(self.L.astro_thermal_design_node_load(self.h, float(t), _d(load)))
+        return load
+
+    def thermal_node_load_drdd(self, dvar, t, drtdd=None):
+        drtdd = np.zeros(self.model.num_nodes) if drtdd is None else drtdd
+        self._check(self.L.astro_thermal_node_load_drdd(self.h, int(dvar), float(t), _d(drtdd)))
+        return drtdd
 
     def panels_factor(self, cluster_size=0):
         """Band LDL^T of K + C^T C of every panel (connected component) in one launch."""

@@ -28,6 +28,39 @@ __device__ __forceinline__ void dof_of(int i, int &var, int &nd) {  // i = 0..31
     }
 }
 
+// correctAlpha (Working/AStrO_r_elementEqns.f90:240-286, shell4 branch): the frame's third axis
+// turned onto the normal of the element's diagonals (orient rows are the local axes).
+template <class T> __device__ void shell_correct_alpha(T orient[3][3], const T X[4][3]) {
+    T v1[3], v2[3], v3[3];
+    for (int k = 0; k < 3; ++k) {
+        v1[k] = X[2][k] - X[0][k];
+        v2[k] = X[3][k] - X[1][k];
+    }
+    v3[0] = v1[1] * v2[2] - v1[2] * v2[1];
+    v3[1] = v1[2] * v2[0] - v1[0] * v2[2];
+    v3[2] = v1[0] * v2[1] - v1[1] * v2[0];
+    for (int k = 0; k < 3; ++k) v1[k] = orient[2][k];
+    T dp = v1[0] * v3[0] + v1[1] * v3[1] + v1[2] * v3[2];
+    if (a_greater(T(0.0), dp))
+        for (int k = 0; k < 3; ++k) v3[k] = -v3[k];
+    dp = v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2];
+    T mag = a_sqrt(dp);
+    for (int k = 0; k < 3; ++k) v2[k] = (T(1.0) / mag) * v3[k];
+    v3[0] = v1[1] * v2[2] - v1[2] * v2[1];
+    v3[1] = v1[2] * v2[0] - v1[0] * v2[2];
+    v3[2] = v1[0] * v2[1] - v1[1] * v2[0];
+    dp = v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2];
+    mag = a_sqrt(dp);
+    if (absT(mag) > LIT(1e-5)) {
+        const T th = a_asin(mag);
+        for (int k = 0; k < 3; ++k) v3[k] = (th / mag) * v3[k];
+        T a0[3][3];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) a0[i][j] = orient[i][j];
+        a_rotate<T>(orient, a0, v3, 0, 0);
+    }
+}
+
 // Section properties of one element: orientation (r_getOrientation, designProp :187-221) with
 // correctAlpha (:240-286), ABD by layer integration (r_getShellStiffness, :259-363) and section
 // mass (r_getShellMass, :469-525).  The design-variable terms of the element (+ i h on
@@ -65,37 +98,7 @@ __device__ void shell_props(const double *nodes, const int *el, const double *se
         for (int i = 0; i < 3; ++i) gr[i] = al[0][i] * loc[0] + al[1][i] * loc[1] + al[2][i] * loc[2];
         a_rotate<T>(orient, al, gr, 0, 0);
     }
-    // correctAlpha
-    {
-        T v1[3], v2[3], v3[3];
-        for (int k = 0; k < 3; ++k) {
-            v1[k] = X[2][k] - X[0][k];
-            v2[k] = X[3][k] - X[1][k];
-        }
-        v3[0] = v1[1] * v2[2] - v1[2] * v2[1];
-        v3[1] = v1[2] * v2[0] - v1[0] * v2[2];
-        v3[2] = v1[0] * v2[1] - v1[1] * v2[0];
-        for (int k = 0; k < 3; ++k) v1[k] = orient[2][k];
-        T dp = v1[0] * v3[0] + v1[1] * v3[1] + v1[2] * v3[2];
-        if (a_greater(T(0.0), dp))
-            for (int k = 0; k < 3; ++k) v3[k] = -v3[k];
-        dp = v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2];
-        T mag = a_sqrt(dp);
-        for (int k = 0; k < 3; ++k) v2[k] = (T(1.0) / mag) * v3[k];
-        v3[0] = v1[1] * v2[2] - v1[2] * v2[1];
-        v3[1] = v1[2] * v2[0] - v1[0] * v2[2];
-        v3[2] = v1[0] * v2[1] - v1[1] * v2[0];
-        dp = v3[0] * v3[0] + v3[1] * v3[1] + v3[2] * v3[2];
-        mag = a_sqrt(dp);
-        if (absT(mag) > LIT(1e-5)) {
-            const T th = a_asin(mag);
-            for (int k = 0; k < 3; ++k) v3[k] = (th / mag) * v3[k];
-            T a0[3][3];
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) a0[i][j] = orient[i][j];
-            a_rotate<T>(orient, a0, v3, 0, 0);
-        }
-    }
+    shell_correct_alpha<T>(orient, X);
     // layer thicknesses with design variables
     const int l0 = layRange[sec - 1], l1 = layRange[sec];
     auto thick = [&](int li, int layerNum) { return T(lay[li].t) + dsum(ASTRO_DCAT_LAYUP_THICKNESS, layerNum, 0); };

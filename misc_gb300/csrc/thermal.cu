@@ -44,19 +44,42 @@ struct ThermPlan {
 
 ThermPlan *plan_of(astro_ctx *ctx) { return static_cast<ThermPlan *>(ctx->thermal); }
 
-// per element: conductivity in the element frame and heat capacity per volume (per area for
-// shells, the section's layers summed), and the shell section thickness
-__global__ void k_th_props(int E, int shell, const int *__restrict__ esec, const int *__restrict__ elMatId,
-                           const double *__restrict__ elDen, const double *__restrict__ matCond,
-                           const double *__restrict__ matSH, const int *__restrict__ layRange,
-                           const LayerDev *__restrict__ lay, const double *__restrict__ layCond,
-                           const double *__restrict__ laySH, const int *__restrict__ e2dR, const int *__restrict__ e2d,
-                           const double *__restrict__ e2c, const int *__restrict__ dcat, const int *__restrict__ dlay,
-                           const double *__restrict__ dval, double *__restrict__ out) {
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
-    double *o = out + (size_t)kProps * e;
-    auto fill = [](double t[3][3], const double *v) {
+// Inputs of the per-element thermal properties: the material (solids) or layer (shells) values
+// as given, and the element design-variable maps.
+struct ThPropArgs {
+    int shell;
+    const int *esec, *elMatId;
+    const double *elDen;  // solid density, the real density design terms applied
+    const double *matCond, *matSH;
+    const int *layRange;
+    const LayerDev *lay;
+    const double *layCond, *laySH;
+    const int *e2dR, *e2d;  // null: no design variables
+    const double *e2c;
+    const int *dcat, *dlay, *dcomp;
+    const double *dval;
+};
+
+// One element's thermal properties with its design-variable terms, + i h on variable `pert`
+// (0 = none): the conductivity tc in the element frame, the heat capacity sh (density x specific
+// heat; per area for shells, the layers summed) and the shell section thickness secT.  Solids:
+// r_getMaterialThermCond / r_getMaterialSpecHeat (Working/AStrO_r_designPropertyFunctions.f90:129-186)
+// and r_getMaterialDensity (:82-103); shells: r_getShellThermCond / r_getShellSpecHeat
+// (:527-644), every layer's conductivity, specific heat, density, thickness and angle with its
+// 'layup' terms.  Each value takes its terms one at a time in the element's term order.
+template <class T>
+__device__ void th_props_t(const ThPropArgs &A, int e, int pert, double h, T tc[3][3], T &sh, T &secT) {
+    auto add_terms = [&](T &v, int cat, int layerNum, int comp) {
+        if (!A.e2dR) return;
+        for (int q = A.e2dR[e]; q < A.e2dR[e + 1]; ++q) {
+            const int d = A.e2d[q] - 1;
+            if (A.dcat[d] != cat || (layerNum && A.dlay[d] != layerNum) || (comp && A.dcomp[d] != comp)) continue;
+            T dv = T(A.dval[d]);
+            if (d + 1 == pert) dv = dv + pert_i<T>(h);
+            v = v + A.e2c[q] * dv;
+        }
+    };
+    auto fill = [](T t[3][3], const T *v) {
         t[0][0] = v[0];
         t[1][1] = v[1];
         t[2][2] = v[2];
@@ -64,57 +87,86 @@ __global__ void k_th_props(int E, int shell, const int *__restrict__ esec, const
         t[0][2] = t[2][0] = v[4];
         t[1][2] = t[2][1] = v[5];
     };
-    double tc[3][3];
-    if (!shell) {
-        const int mat = elMatId[e];
-        fill(tc, matCond + 6 * (mat - 1));
-        for (int i = 0; i < 9; ++i) o[i] = tc[i / 3][i % 3];
-        o[9] = elDen[e] * matSH[mat - 1];
-        o[10] = 0.0;
+    if (!A.shell) {
+        const int mat = A.elMatId[e];
+        T cv[6];
+        for (int k = 0; k < 6; ++k) {
+            cv[k] = T(A.matCond[6 * (mat - 1) + k]);
+            add_terms(cv[k], ASTRO_DCAT_THERMAL_COND, 0, k + 1);
+        }
+        fill(tc, cv);
+        T rho = T(A.elDen[e]);
+        if (pert && A.e2dR)
+            for (int q = A.e2dR[e]; q < A.e2dR[e + 1]; ++q)
+                if (A.e2d[q] == pert && A.dcat[pert - 1] == ASTRO_DCAT_DENSITY) rho = rho + A.e2c[q] * pert_i<T>(h);
+        T spec = T(A.matSH[mat - 1]);
+        add_terms(spec, ASTRO_DCAT_SPEC_HEAT, 0, 0);
+        sh = rho * spec;
+        secT = T(0.0);
         return;
     }
-    const int sec = esec[e];
+    const int sec = A.esec[e];
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) tc[i][j] = 0.0;
-    double sh = 0.0, secT = 0.0;
-    for (int li = layRange[sec - 1], ln = 1; li < layRange[sec]; ++li, ++ln) {
-        double t = lay[li].t;
-        if (e2dR)
-            for (int q = e2dR[e]; q < e2dR[e + 1]; ++q) {
-                const int d = e2d[q] - 1;
-                if (dcat[d] == ASTRO_DCAT_LAYUP_THICKNESS && dlay[d] == ln) t = t + e2c[q] * dval[d];
-            }
-        double tl[3][3], al[3][3] = {{0.0, 0.0, 0.0}, {0.0, 0.0, 0.0}, {0.0, 0.0, 1.0}}, pr[3][3];
-        fill(tl, layCond + 6 * li);
-        al[0][0] = a_cos(lay[li].angle);
-        al[1][0] = a_sin(lay[li].angle);
+        for (int j = 0; j < 3; ++j) tc[i][j] = T(0.0);
+    sh = T(0.0);
+    secT = T(0.0);
+    for (int li = A.layRange[sec - 1], ln = 1; li < A.layRange[sec]; ++li, ++ln) {
+        const LayerDev L = A.lay[li];
+        T t = T(L.t), ang = T(L.angle), rho = T(L.rho), spec = T(A.laySH[li]), cv[6];
+        add_terms(t, ASTRO_DCAT_LAYUP_THICKNESS, ln, 0);
+        add_terms(ang, ASTRO_DCAT_LAYUP_ANGLE, ln, 0);
+        add_terms(rho, ASTRO_DCAT_LAYUP_DENSITY, ln, 0);
+        add_terms(spec, ASTRO_DCAT_LAYUP_SPEC_HEAT, ln, 0);
+        for (int k = 0; k < 6; ++k) {
+            cv[k] = T(A.layCond[6 * li + k]);
+            add_terms(cv[k], ASTRO_DCAT_LAYUP_THERMAL_COND, ln, k + 1);
+        }
+        T tl[3][3], al[3][3], pr[3][3];
+        fill(tl, cv);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) al[i][j] = T(0.0);
+        al[2][2] = T(1.0);
+        al[0][0] = a_cos(ang);
+        al[1][0] = a_sin(ang);
         al[0][1] = -al[1][0];
         al[1][1] = al[0][0];
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
-                double s = 0.0;
-                for (int k = 0; k < 3; ++k) s = s + tl[a][k] * al[b][k];
-                pr[a][b] = s;
+                T v = T(0.0);
+                for (int k = 0; k < 3; ++k) v = v + tl[a][k] * al[b][k];
+                pr[a][b] = v;
             }
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
-                double s = 0.0;
-                for (int k = 0; k < 3; ++k) s = s + al[a][k] * pr[k][b];
-                tc[a][b] = tc[a][b] + t * s;
+                T v = T(0.0);
+                for (int k = 0; k < 3; ++k) v = v + al[a][k] * pr[k][b];
+                tc[a][b] = tc[a][b] + t * v;
             }
-        sh = sh + t * lay[li].rho * laySH[li];
+        sh = sh + t * rho * spec;
         secT = secT + t;
     }
+}
+
+// per element: conductivity in the element frame, heat capacity and shell thickness (real values
+// of the design variables applied)
+__global__ void k_th_props(ThPropArgs A, int E, double *__restrict__ out) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    double tc[3][3], sh, secT;
+    th_props_t<double>(A, e, 0, 0.0, tc, sh, secT);
+    double *o = out + (size_t)kProps * e;
     for (int i = 0; i < 9; ++i) o[i] = tc[i / 3][i % 3];
     o[9] = sh;
     o[10] = secT;
 }
 
 // Gauss point g of the element: shape functions, their global gradient in the element frame and
-// w detJ (r_getIntPtData; shells with dxds(3,3) = 1)
-__device__ __forceinline__ void th_point(int shell, const double Xl[8][3], int g, double N[8], double Nx[8][3],
-                                         double &wdet) {
-    const double r3 = 0.57735026918962576451;  // r_1rt3
+// w detJ (r_getIntPtData; shells with dxds(3,3) = 1).  r3 is the Gauss abscissa (the real path's
+// 1/sqrt(3) or the complex path's single-precision literal); the shape functions are real, the
+// geometry T.
+template <class T>
+__device__ __forceinline__ void th_point_t(int shell, const T Xl[8][3], double r3, int g, double N[8], T Nx[8][3],
+                                           T &wdet) {
     const int npe = shell ? 4 : 8;
     double dN[8][3];
     if (shell) {
@@ -138,20 +190,20 @@ __device__ __forceinline__ void th_point(int shell, const double Xl[8][3], int g
             dN[n][2] = 0.125 * sz[n] * a1 * a2;
         }
     }
-    double J[3][3];
+    T J[3][3];
     for (int a = 0; a < 3; ++a)
         for (int b = 0; b < 3; ++b) {
-            double s = 0.0;
+            T s = T(0.0);
             for (int n = 0; n < npe; ++n) s = s + Xl[n][a] * dN[n][b];
             J[a][b] = s;
         }
-    if (shell) J[2][2] = 1.0;
-    const double c11 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-    const double c12 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-    const double c13 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-    const double det = J[0][0] * c11 + J[0][1] * c12 + J[0][2] * c13;
-    const double di = 1.0 / det;
-    double I[3][3];
+    if (shell) J[2][2] = T(1.0);
+    const T c11 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const T c12 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const T c13 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    const T det = J[0][0] * c11 + J[0][1] * c12 + J[0][2] * c13;
+    const T di = T(1.0) / det;
+    T I[3][3];
     I[0][0] = di * c11;
     I[1][0] = di * c12;
     I[2][0] = di * c13;
@@ -164,6 +216,11 @@ __device__ __forceinline__ void th_point(int shell, const double Xl[8][3], int g
     for (int n = 0; n < npe; ++n)
         for (int b = 0; b < 3; ++b) Nx[n][b] = dN[n][0] * I[0][b] + dN[n][1] * I[1][b] + dN[n][2] * I[2][b];
     wdet = det;  // unit weights
+}
+
+__device__ __forceinline__ void th_point(int shell, const double Xl[8][3], int g, double N[8], double Nx[8][3],
+                                         double &wdet) {
+    th_point_t<double>(shell, Xl, AK<double>::rt3, g, N, Nx, wdet);
 }
 
 struct ThArgs {
@@ -403,6 +460,29 @@ void thermal_release(astro_ctx *ctx) {
     ctx->thermal = nullptr;
 }
 
+static ThPropArgs th_prop_args(astro_ctx *ctx, ThermPlan *T) {
+    ThPropArgs A = {};
+    const bool dv = ctx->numDvars > 0 && ctx->d_e2dR.p;
+    A.shell = ctx->hasShell;
+    A.esec = dptr<int>(ctx->d_esec);
+    A.elMatId = ctx->hasSolid ? dptr<int>(T->d_elMatId) : nullptr;
+    A.elDen = ctx->hasSolid ? dptr<double>(ctx->d_elRho) : nullptr;
+    A.matCond = dptr<double>(T->d_matCond);
+    A.matSH = dptr<double>(T->d_matSH);
+    A.layRange = ctx->hasShell ? dptr<int>(ctx->d_shLayRange) : nullptr;
+    A.lay = ctx->hasShell ? dptr<LayerDev>(ctx->d_shLay) : nullptr;
+    A.layCond = dptr<double>(T->d_layCond);
+    A.laySH = dptr<double>(T->d_laySH);
+    A.e2dR = dv ? dptr<int>(ctx->d_e2dR) : nullptr;
+    A.e2d = dv ? dptr<int>(ctx->d_e2d) : nullptr;
+    A.e2c = dv ? dptr<double>(ctx->d_e2c) : nullptr;
+    A.dcat = dv ? dptr<int>(ctx->d_dCat) : nullptr;
+    A.dlay = dv ? dptr<int>(ctx->d_dLayer) : nullptr;
+    A.dcomp = dv ? dptr<int>(ctx->d_dComp) : nullptr;
+    A.dval = dv ? dptr<double>(ctx->d_dVal) : nullptr;
+    return A;
+}
+
 extern "C" int astro_thermal_setup(astro_ctx *ctx, const astro_thermal_props *p, int32_t *therm_mat_size,
                                    int32_t *therm_mpc_dim) {
     if (!ctx || !p || p->num_materials < 1 || !p->material_therm_cond || !p->material_spec_heat) return ASTRO_ERR_ARG;
@@ -480,24 +560,10 @@ extern "C" int astro_thermal_setup(astro_ctx *ctx, const astro_thermal_props *p,
         (rc = dev_alloc(ctx, T->d_props, sizeof(double) * kProps * (size_t)E)) ||
         (rc = dev_alloc(ctx, T->d_val, sizeof(double) * (size_t)P.nb)))
         return rc;
-    DevBuf den;
-    if (ctx->hasSolid) {
-        if ((rc = upload(ctx, T->d_elMatId, ctx->elMatId.data(), sizeof(int) * E)) ||
-            (rc = upload(ctx, den, ctx->elDensity.data(), sizeof(double) * E)))
-            return rc;
-    }
-    const bool dv = ctx->numDvars > 0 && ctx->d_e2dR.p;
-    k_th_props<<<(E + 127) / 128, 128, 0, ctx->stream>>>(
-        E, ctx->hasShell, dptr<int>(ctx->d_esec), ctx->hasSolid ? dptr<int>(T->d_elMatId) : nullptr,
-        ctx->hasSolid ? dptr<double>(den) : nullptr, dptr<double>(T->d_matCond), dptr<double>(T->d_matSH),
-        ctx->hasShell ? dptr<int>(ctx->d_shLayRange) : nullptr, ctx->hasShell ? dptr<LayerDev>(ctx->d_shLay) : nullptr,
-        dptr<double>(T->d_layCond), dptr<double>(T->d_laySH), dv ? dptr<int>(ctx->d_e2dR) : nullptr,
-        dv ? dptr<int>(ctx->d_e2d) : nullptr, dv ? dptr<double>(ctx->d_e2c) : nullptr,
-        dv ? dptr<int>(ctx->d_dCat) : nullptr, dv ? dptr<int>(ctx->d_dLayer) : nullptr,
-        dv ? dptr<double>(ctx->d_dVal) : nullptr, dptr<double>(T->d_props));
+    if (ctx->hasSolid && (rc = upload(ctx, T->d_elMatId, ctx->elMatId.data(), sizeof(int) * E))) return rc;
+    k_th_props<<<(E + 127) / 128, 128, 0, ctx->stream>>>(th_prop_args(ctx, T), E, dptr<double>(T->d_props));
     rc = cuda_check(ctx, cudaGetLastError(), "thermal properties");
     if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(ctx->stream), "thermal properties");
-    dev_free(den);
     if (rc) return rc;
     if (therm_mat_size) *therm_mat_size = T->matSize;
     if (therm_mpc_dim) *therm_mpc_dim = T->mpcDim;
@@ -868,4 +934,487 @@ extern "C" int astro_thermal_solve(astro_ctx *ctx, const double *rhs, double *dt
     if (status == ASTRO_ERR_MAXIT) return set_err(ctx, ASTRO_ERR_MAXIT, "thermal solve: iteration limit");
     if (status == ASTRO_ERR_NAN) return set_err(ctx, ASTRO_ERR_NAN, "thermal solve: non-finite residual");
     return ASTRO_OK;
+}
+
+// ---- design sensitivities (getdRthermaldD, Working/AStrO_commandFunctions.f90:1016-1170) ---------
+// Complex step: the elements that depend on the design variable are evaluated in complex FP64
+// with d + i h, one thread per element, colour by colour (a colour's elements share no node), and
+// Im / h is accumulated at their nodes.  The complex path's Gauss points are the single-precision
+// 1/sqrt(3) of the reference's c_ constants.
+namespace {
+
+struct ThCsArgs {
+    int dvar;
+    double h;
+    const double *secOrig;  // (S,9) column-major section orientation as given
+    const int *n2dR, *n2d;  // node design maps (null: none)
+    const double *n2c;
+    const double *mult;     // per listed element: how often the load lists it (heat generation)
+    double q;               // heat generation per unit volume
+    double *out;            // rank-order derivative
+};
+
+// The element frame and its nodes in it, in T: nodes with + i h coef on d's nodeCoord terms
+// (r_getNodeCoord, designProp :945-968; the real offsets of every nodeCoord variable are already
+// in the node list), the section orientation rotated by its orientation variables
+// (r_getOrientation, :187-221) and, for shells, correctAlpha.
+template <class T>
+__device__ void th_frame_t(const ThArgs &A, const ThPropArgs &P, const ThCsArgs &C, int e, T Xl[8][3], int rk[8]) {
+    const int npe = A.shell ? 4 : 8;
+    const T ih = pert_i<T>(C.h);
+    T Xg[8][3];
+    for (int a = 0; a < npe; ++a) {
+        const int nd = A.elist[8 * (size_t)e + a];
+        rk[a] = A.rank[nd - 1] - 1;
+        for (int k = 0; k < 3; ++k) Xg[a][k] = T(A.nodes[3 * (size_t)(nd - 1) + k]);
+        if (C.n2dR)
+            for (int t = C.n2dR[nd - 1]; t < C.n2dR[nd]; ++t) {
+                const int d = C.n2d[t];
+                if (d == C.dvar && P.dcat[d - 1] == ASTRO_DCAT_NODE_COORD) Xg[a][P.dcomp[d - 1] - 1] += C.n2c[t] * ih;
+            }
+    }
+    T loc[3] = {T(0.0), T(0.0), T(0.0)};
+    if (P.e2dR)
+        for (int q = P.e2dR[e]; q < P.e2dR[e + 1]; ++q) {
+            const int d = P.e2d[q];
+            if (P.dcat[d - 1] != ASTRO_DCAT_ORIENTATION) continue;
+            T v = T(P.dval[d - 1]);
+            if (d == C.dvar) v = v + ih;
+            loc[P.dcomp[d - 1] - 1] = loc[P.dcomp[d - 1] - 1] + P.e2c[q] * v;
+        }
+    const int sec = P.esec[e];
+    T al[3][3], gr[3], orient[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) al[i][j] = T(C.secOrig[9 * (size_t)(sec - 1) + 3 * j + i]);
+    for (int i = 0; i < 3; ++i) gr[i] = al[0][i] * loc[0] + al[1][i] * loc[1] + al[2][i] * loc[2];
+    a_rotate<T>(orient, al, gr, 0, 0);
+    if (A.shell) {
+        T X4[4][3];
+        for (int a = 0; a < 4; ++a)
+            for (int k = 0; k < 3; ++k) X4[a][k] = Xg[a][k];
+        shell_correct_alpha<T>(orient, X4);
+    }
+    for (int a = 0; a < npe; ++a)
+        for (int i = 0; i < 3; ++i) Xl[a][i] = orient[i][0] * Xg[a][0] + orient[i][1] * Xg[a][1] + orient[i][2] * Xg[a][2];
+}
+
+// The complex Gauss point, called out of line.  Inlined into k_th_elem_cs, this CUDA 13.0 build
+// for sm_103a returned wrong shape-function gradients for every node but the first, although
+// the parametric derivatives and the inverse Jacobian inside the routine were right.  The same source
+// built for the host, built with -G, or called out of line gives the right gradients.
+__device__ __noinline__ void th_point_cs(int shell, const cplx Xl[8][3], int g, double N[8], cplx Nx[8][3],
+                                         cplx &wdet) {
+    th_point_t<cplx>(shell, Xl, AK<cplx>::rt3, g, N, Nx, wdet);
+}
+
+// element part: out[rank] += Im(Rt) / h (r_getElRtk + r_getElRtm in complex)
+__global__ void k_th_elem_cs(ThArgs A, ThPropArgs P, ThCsArgs C) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.count) return;
+    const int e = A.els[q];
+    const int npe = A.shell ? 4 : 8, ngp = A.shell ? 4 : 8;
+    cplx Xl[8][3];
+    int rk[8];
+    th_frame_t<cplx>(A, P, C, e, Xl, rk);
+    cplx tc[3][3], sh, secT;
+    th_props_t<cplx>(P, e, C.dvar, C.h, tc, sh, secT);
+    double T[8], Td[8];
+    for (int a = 0; a < npe; ++a) {
+        T[a] = A.temp ? A.temp[rk[a]] : 0.0;
+        Td[a] = 0.0;
+        if (A.dynamic) {
+            const double pT = A.ptemp ? A.ptemp[rk[a]] : 0.0, pTd = A.ptdot ? A.ptdot[rk[a]] : 0.0;
+            Td[a] = (1.0 / A.gamma) * ((1.0 / A.delT) * (T[a] - pT) - 1.0 * (1.0 - A.gamma) * pTd);
+        }
+    }
+    cplx Rt[8];
+    for (int g = 0; g < ngp; ++g) {
+        double N[8];
+        cplx Nx[8][3], wd;
+        th_point_cs(A.shell, Xl, g, N, Nx, wd);
+        cplx Tx[3];
+        for (int a = 0; a < npe; ++a)
+            for (int k = 0; k < 3; ++k) Tx[k] = Tx[k] + Nx[a][k] * T[a];
+        cplx qv[3];
+        for (int i = 0; i < 3; ++i) qv[i] = wd * (tc[i][0] * Tx[0] + tc[i][1] * Tx[1] + tc[i][2] * Tx[2]);
+        for (int a = 0; a < npe; ++a) Rt[a] = Rt[a] + Nx[a][0] * qv[0] + Nx[a][1] * qv[1] + Nx[a][2] * qv[2];
+        if (A.dynamic) {
+            double pt = 0.0;
+            for (int a = 0; a < npe; ++a) pt = pt + Td[a] * N[a];
+            const cplx c = (wd * sh) * pt;
+            for (int a = 0; a < npe; ++a) Rt[a] = Rt[a] + c * N[a];
+        }
+    }
+    const double hInv = 1.0 / C.h;
+    for (int a = 0; a < npe; ++a) C.out[rk[a]] += hInv * Rt[a].im;
+}
+
+// bodyHeatGen branch: out[rank] -= mult Im(q integral of N (times the section thickness for
+// shells)) / h
+__global__ void k_th_heatgen_cs(ThArgs A, ThPropArgs P, ThCsArgs C) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= A.count) return;
+    const int e = A.els[q];
+    const int npe = A.shell ? 4 : 8, ngp = A.shell ? 4 : 8;
+    cplx Xl[8][3];
+    int rk[8];
+    th_frame_t<cplx>(A, P, C, e, Xl, rk);
+    cplx w[8];
+    for (int g = 0; g < ngp; ++g) {
+        double N[8];
+        cplx Nx[8][3], wd;
+        th_point_cs(A.shell, Xl, g, N, Nx, wd);
+        for (int a = 0; a < npe; ++a) w[a] = w[a] + (C.q * N[a]) * wd;
+    }
+    cplx t = cplx(1.0);
+    if (A.shell) {
+        cplx tc[3][3], sh;
+        th_props_t<cplx>(P, e, C.dvar, C.h, tc, sh, t);
+    }
+    const double hInv = 1.0 / C.h;
+    for (int a = 0; a < npe; ++a) C.out[rk[a]] -= C.mult[q] * (hInv * (t * w[a]).im);
+}
+
+// surfaceFlux branch, one thread per face: the face's four nodal values Im(flux integral of
+// N dA) / h, dA the true area element (as the load itself), into fv[4 f + k]
+__global__ void k_th_flux_cs(int nf, const int *__restrict__ faceEl, const int *__restrict__ faceNum,
+                             const int *__restrict__ etype, const int *__restrict__ elist,
+                             const double *__restrict__ nodes, const int *__restrict__ n2dR,
+                             const int *__restrict__ n2d, const double *__restrict__ n2c, const int *__restrict__ dcat,
+                             const int *__restrict__ dcomp, int dvar, double h, double flux, double *__restrict__ fv) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    const int hexF[6][4] = {{4, 3, 2, 1}, {5, 6, 7, 8}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {4, 1, 5, 8}};
+    const int shF[2][4] = {{1, 2, 3, 4}, {1, 4, 3, 2}};
+    const int el = faceEl[f] - 1, fn = faceNum[f] - 1;
+    const int *fl = (etype[el] == 8 || etype[el] == 81) ? hexF[fn] : shF[fn];
+    cplx X[4][3];
+    for (int k = 0; k < 4; ++k) {
+        const int nd = elist[8 * (size_t)el + fl[k] - 1];
+        for (int d = 0; d < 3; ++d) X[k][d] = cplx(nodes[3 * (size_t)(nd - 1) + d]);
+        if (n2dR)
+            for (int t = n2dR[nd - 1]; t < n2dR[nd]; ++t)
+                if (n2d[t] == dvar && dcat[dvar - 1] == ASTRO_DCAT_NODE_COORD)
+                    X[k][dcomp[dvar - 1] - 1] += cplx(0.0, n2c[t] * h);
+    }
+    const double g = AK<cplx>::rt3;
+    cplx acc[4];
+    for (int gp = 0; gp < 4; ++gp) {
+        const double s = (gp & 1) ? g : -g, r = (gp & 2) ? g : -g;
+        const double N_[4] = {0.25 * (1 - s) * (1 - r), 0.25 * (1 + s) * (1 - r), 0.25 * (1 + s) * (1 + r),
+                              0.25 * (1 - s) * (1 + r)};
+        const double Ns[4] = {-0.25 * (1 - r), 0.25 * (1 - r), 0.25 * (1 + r), -0.25 * (1 + r)};
+        const double Nr[4] = {-0.25 * (1 - s), -0.25 * (1 + s), 0.25 * (1 + s), 0.25 * (1 - s)};
+        cplx a[3], b[3];
+        for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d) {
+                a[d] = a[d] + Ns[k] * X[k][d];
+                b[d] = b[d] + Nr[k] * X[k][d];
+            }
+        const cplx cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
+        const cplx s2 = cx * cx + cy * cy + cz * cz;
+        // principal square root to first order in the imaginary part (exact for the complex step)
+        const double re = sqrt(s2.re);
+        const cplx dA(re, s2.im / (2.0 * re));
+        for (int k = 0; k < 4; ++k) acc[k] = acc[k] + (flux * N_[k]) * dA;
+    }
+    for (int k = 0; k < 4; ++k) fv[4 * (size_t)f + k] = acc[k].im / h;
+}
+
+// out[row[g]] += the face values of its slots, in face order (gPtr / gSlot as face_gather_kernel)
+__global__ void k_th_face_gather(int ng, const int *__restrict__ gPtr, const int *__restrict__ gSlot,
+                                 const int *__restrict__ gRow, const double *__restrict__ fv, double *__restrict__ out) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ng) return;
+    double s = out[gRow[g]];
+    for (int q = gPtr[g]; q < gPtr[g + 1]; ++q) s = s + fv[gSlot[q]];
+    out[gRow[g]] = s;
+}
+
+// 'nodeLoad' / 'thermal' variables (d_component 7) active at t (dActTime(1) < t < dActTime(2)):
+// mode 0 load[rank] += coef d of every variable, mode 1 load[rank] -= coef for dvar only
+__global__ void k_th_node_dload(int N, const int *__restrict__ rank, const int *__restrict__ n2dR,
+                                const int *__restrict__ n2d, const double *__restrict__ n2c,
+                                const int *__restrict__ dcat, const int *__restrict__ dcomp,
+                                const double *__restrict__ dval, const double *__restrict__ act, double t, int mode,
+                                int dvar, double *__restrict__ load) {
+    const int nd = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nd >= N) return;
+    double v = load[rank[nd] - 1];
+    for (int q = n2dR[nd]; q < n2dR[nd + 1]; ++q) {
+        const int d = n2d[q];
+        if (dcat[d - 1] != ASTRO_DCAT_NODE_LOAD || dcomp[d - 1] != 7 || (mode == 1 && d != dvar)) continue;
+        if (act && !(t > act[2 * (d - 1)] && act[2 * (d - 1) + 1] > t)) continue;
+        v = v + (mode == 0 ? n2c[q] * dval[d - 1] : -n2c[q]);
+    }
+    load[rank[nd] - 1] = v;
+}
+
+}  // namespace
+
+// Per element (0-based): 1 when it depends on dvar (getdToElComp, Working/AStrO_bookKeeping.f90:7-129:
+// the element's own design variables, and the nodeCoord variables of its nodes).
+static std::vector<char> th_dependents(const astro_ctx *ctx, int dvar) {
+    const AstroPrep &P = ctx->P;
+    std::vector<char> dep((size_t)P.E, 0);
+    for (int e = 0; e < P.E; ++e)
+        for (int q = ctx->e2dRange[e]; q < ctx->e2dRange[e + 1]; ++q)
+            if (ctx->e2d[q] == dvar) dep[e] = 1;
+    if (!ctx->n2dRange.empty() && ctx->dCat[dvar - 1] == ASTRO_DCAT_NODE_COORD) {
+        std::vector<char> nd((size_t)P.N + 1, 0);
+        for (int n = 1; n <= P.N; ++n)
+            for (int q = ctx->n2dRange[n - 1]; q < ctx->n2dRange[n]; ++q)
+                if (ctx->n2d[q] == dvar) nd[n] = 1;
+        for (int e = 0; e < P.E; ++e)
+            for (int a = 0; a < P.npe; ++a)
+                if (nd[ctx->elist[8 * (size_t)e + a]]) dep[e] = 1;
+    }
+    return dep;
+}
+
+static int th_check_dvar(astro_ctx *ctx, int dvar, double h) {
+    if (!plan_of(ctx)) return set_err(ctx, ASTRO_ERR_STATE, "thermal: astro_thermal_setup not called");
+    if (dvar < 1 || dvar > ctx->numDvars)
+        return set_err(ctx, ASTRO_ERR_ARG, "design variable " + std::to_string(dvar) + " out of range");
+    if (!(h > 0.0)) return set_err(ctx, ASTRO_ERR_ARG, "complex step h must be positive");
+    return ASTRO_OK;
+}
+
+static ThCsArgs th_cs_args(astro_ctx *ctx, int dvar, double h, double *out) {
+    ThCsArgs C = {};
+    C.dvar = dvar;
+    C.h = h;
+    C.secOrig = dptr<double>(ctx->d_secOrig);
+    const bool nd = !ctx->n2dRange.empty();
+    C.n2dR = nd ? dptr<int>(ctx->d_n2dR) : nullptr;
+    C.n2d = nd ? dptr<int>(ctx->d_n2d) : nullptr;
+    C.n2c = nd ? dptr<double>(ctx->d_n2c) : nullptr;
+    C.out = out;
+    return C;
+}
+
+// The listed elements (with multiplicity, or all when elements is null) that depend on dvar, by
+// colour.
+static void th_listed_dependents(const astro_ctx *ctx, const std::vector<char> &dep, const int32_t *elements,
+                                 int count, std::vector<int> &list, std::vector<double> &mult, std::vector<int> &ptr) {
+    const AstroPrep &P = ctx->P;
+    std::vector<int> times((size_t)P.E, elements ? 0 : 1);
+    if (elements)
+        for (int k = 0; k < count; ++k) ++times[elements[k] - 1];
+    list.clear();
+    mult.clear();
+    ptr.assign(1, 0);
+    for (int col = 0; col < P.ncolors; ++col) {
+        for (int k = P.colorPtr[col]; k < P.colorPtr[col + 1]; ++k) {
+            const int e = P.colorEls[k];
+            if (dep[e] && times[e]) {
+                list.push_back(e);
+                mult.push_back((double)times[e]);
+            }
+        }
+        ptr.push_back((int)list.size());
+    }
+}
+
+// Runs `launch(els, count, mult)` over the colours of the listed elements with the derivative
+// vector on the device, then copies it back.
+template <class F>
+static int th_cs_run(astro_ctx *ctx, const std::vector<int> &list, const std::vector<double> &mult,
+                     const std::vector<int> &ptr, double *drtdd, bool zero, F launch) {
+    const int N = ctx->P.N;
+    DevBuf dl, dm, dout;
+    int rc = ASTRO_OK;
+    struct Free {
+        DevBuf *b[3];
+        ~Free() {
+            for (auto *x : b) dev_free(*x);
+        }
+    } fr{{&dl, &dm, &dout}};
+    if (zero) {
+        if ((rc = dev_alloc(ctx, dout, sizeof(double) * N))) return rc;
+        CK(cudaMemsetAsync(dout.p, 0, sizeof(double) * N, ctx->stream));
+    } else if ((rc = upload(ctx, dout, drtdd, sizeof(double) * N))) {
+        return rc;
+    }
+    if (!list.empty()) {
+        if ((rc = upload(ctx, dl, list.data(), sizeof(int) * list.size())) ||
+            (rc = upload(ctx, dm, mult.data(), sizeof(double) * mult.size())))
+            return rc;
+        for (size_t col = 0; col + 1 < ptr.size(); ++col) {
+            const int cnt = ptr[col + 1] - ptr[col];
+            if (cnt) launch(dptr<int>(dl) + ptr[col], cnt, dptr<double>(dm) + ptr[col], dptr<double>(dout));
+        }
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "thermal complex step"))) return rc;
+    }
+    CK(cudaMemcpyAsync(drtdd, dout.p, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}
+
+extern "C" int astro_thermal_drdd(astro_ctx *ctx, int32_t dvar, double h, const astro_thermal_state *st,
+                                  double *drtdd) {
+    if (!ctx || !drtdd) return ASTRO_ERR_ARG;
+    int rc;
+    if ((rc = th_check_dvar(ctx, dvar, h))) return rc;
+    if (st && st->dynamic && !(st->nm_gamma != 0.0 && st->del_t != 0.0))
+        return set_err(ctx, ASTRO_ERR_ARG, "thermal: dynamic step needs gamma and a time step");
+    ThermPlan *T = plan_of(ctx);
+    const int N = ctx->P.N;
+    std::vector<int> list, ptr;
+    std::vector<double> mult;
+    th_listed_dependents(ctx, th_dependents(ctx, dvar), nullptr, 0, list, mult, ptr);
+    DevBuf dT, dpT, dpTd;
+    struct Free {
+        DevBuf *b[3];
+        ~Free() {
+            for (auto *x : b) dev_free(*x);
+        }
+    } fr{{&dT, &dpT, &dpTd}};
+    if ((rc = up_opt(ctx, dT, st ? st->node_temp : nullptr, N)) ||
+        (rc = up_opt(ctx, dpT, st ? st->prev_temp : nullptr, N)) ||
+        (rc = up_opt(ctx, dpTd, st ? st->prev_tdot : nullptr, N)))
+        return rc;
+    ThArgs A = th_args(ctx, T);
+    A.temp = dT.p ? dptr<double>(dT) : nullptr;
+    A.ptemp = dpT.p ? dptr<double>(dpT) : nullptr;
+    A.ptdot = dpTd.p ? dptr<double>(dpTd) : nullptr;
+    A.dynamic = st ? st->dynamic : 0;
+    A.gamma = st ? st->nm_gamma : 0.5;
+    A.delT = st ? st->del_t : 0.0;
+    const ThPropArgs Pa = th_prop_args(ctx, T);
+    return th_cs_run(ctx, list, mult, ptr, drtdd, true, [&](const int *els, int cnt, const double *, double *out) {
+        ThArgs a = A;
+        a.els = els;
+        a.count = cnt;
+        k_th_elem_cs<<<(cnt + 63) / 64, 64, 0, ctx->stream>>>(a, Pa, th_cs_args(ctx, dvar, h, out));
+    });
+}
+
+extern "C" int astro_thermal_heat_gen_drdd(astro_ctx *ctx, int32_t dvar, double h, double q, const int32_t *elements,
+                                           int32_t count, double *drtdd) {
+    if (!ctx || !drtdd || count < 0) return ASTRO_ERR_ARG;
+    int rc;
+    if ((rc = th_check_dvar(ctx, dvar, h))) return rc;
+    const AstroPrep &P = ctx->P;
+    if (elements)
+        for (int k = 0; k < count; ++k)
+            if (elements[k] < 1 || elements[k] > P.E) return set_err(ctx, ASTRO_ERR_ARG, "element number out of range");
+    ThermPlan *T = plan_of(ctx);
+    std::vector<int> list, ptr;
+    std::vector<double> mult;
+    th_listed_dependents(ctx, th_dependents(ctx, dvar), elements, count, list, mult, ptr);
+    if (list.empty()) return ASTRO_OK;
+    const ThArgs A = th_args(ctx, T);
+    const ThPropArgs Pa = th_prop_args(ctx, T);
+    return th_cs_run(ctx, list, mult, ptr, drtdd, false, [&](const int *els, int cnt, const double *m, double *out) {
+        ThArgs a = A;
+        a.els = els;
+        a.count = cnt;
+        ThCsArgs C = th_cs_args(ctx, dvar, h, out);
+        C.mult = m;
+        C.q = q;
+        k_th_heatgen_cs<<<(cnt + 63) / 64, 64, 0, ctx->stream>>>(a, Pa, C);
+    });
+}
+
+extern "C" int astro_thermal_surface_flux_drdd(astro_ctx *ctx, int32_t dvar, double h, int32_t nfaces,
+                                               const int32_t *face_el, const int32_t *face_num, double flux,
+                                               double *drtdd) {
+    if (!ctx || !drtdd || nfaces < 0 || (nfaces && (!face_el || !face_num))) return ASTRO_ERR_ARG;
+    int rc;
+    if ((rc = th_check_dvar(ctx, dvar, h))) return rc;
+    const AstroPrep &P = ctx->P;
+    for (int f = 0; f < nfaces; ++f) {
+        const int e = face_el[f], fn = face_num[f];
+        if (e < 1 || e > P.E) return set_err(ctx, ASTRO_ERR_ARG, "face element out of range");
+        if (fn < 1 || fn > ((ctx->etype[e - 1] == 8 || ctx->etype[e - 1] == 81) ? 6 : 2))
+            return set_err(ctx, ASTRO_ERR_ARG, "face number out of range");
+    }
+    // the faces whose element depends on dvar, and the gather lists of their corner values
+    static const int hexF[6][4] = {{4, 3, 2, 1}, {5, 6, 7, 8}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {4, 1, 5, 8}};
+    static const int shF[2][4] = {{1, 2, 3, 4}, {1, 4, 3, 2}};
+    const std::vector<char> dep = th_dependents(ctx, dvar);
+    std::vector<int> fe, fnum, slotRow;
+    for (int f = 0; f < nfaces; ++f) {
+        const int e = face_el[f] - 1;
+        if (!dep[e]) continue;
+        fe.push_back(face_el[f]);
+        fnum.push_back(face_num[f]);
+        const int *fl = (ctx->etype[e] == 8 || ctx->etype[e] == 81) ? hexF[face_num[f] - 1] : shF[face_num[f] - 1];
+        for (int k = 0; k < 4; ++k) slotRow.push_back(P.currentRank[ctx->elist[8 * (size_t)e + fl[k] - 1]] - 1);
+    }
+    if (fe.empty()) return ASTRO_OK;
+    std::vector<int> order(slotRow.size());
+    for (size_t k = 0; k < order.size(); ++k) order[k] = (int)k;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return slotRow[a] < slotRow[b]; });
+    std::vector<int> gPtr(1, 0), gRow;
+    for (size_t k = 0; k < order.size(); ++k) {
+        if (k == 0 || slotRow[order[k]] != slotRow[order[k - 1]]) {
+            if (k) gPtr.push_back((int)k);
+            gRow.push_back(slotRow[order[k]]);
+        }
+    }
+    gPtr.push_back((int)order.size());
+    const int nf = (int)fe.size(), ng = (int)gRow.size(), N = P.N;
+    DevBuf dfe, dfn, dfv, dgp, dgs, dgr, dout;
+    struct Free {
+        DevBuf *b[7];
+        ~Free() {
+            for (auto *x : b) dev_free(*x);
+        }
+    } fr{{&dfe, &dfn, &dfv, &dgp, &dgs, &dgr, &dout}};
+    if ((rc = upload(ctx, dfe, fe.data(), sizeof(int) * nf)) || (rc = upload(ctx, dfn, fnum.data(), sizeof(int) * nf)) ||
+        (rc = dev_alloc(ctx, dfv, sizeof(double) * 4 * (size_t)nf)) ||
+        (rc = upload(ctx, dgp, gPtr.data(), sizeof(int) * gPtr.size())) ||
+        (rc = upload(ctx, dgs, order.data(), sizeof(int) * order.size())) ||
+        (rc = upload(ctx, dgr, gRow.data(), sizeof(int) * ng)) || (rc = upload(ctx, dout, drtdd, sizeof(double) * N)))
+        return rc;
+    const bool nd = !ctx->n2dRange.empty();
+    k_th_flux_cs<<<(nf + 127) / 128, 128, 0, ctx->stream>>>(
+        nf, dptr<int>(dfe), dptr<int>(dfn), dptr<int>(ctx->d_etype), dptr<int>(ctx->d_elist), dptr<double>(ctx->d_nodes),
+        nd ? dptr<int>(ctx->d_n2dR) : nullptr, nd ? dptr<int>(ctx->d_n2d) : nullptr,
+        nd ? dptr<double>(ctx->d_n2c) : nullptr, dptr<int>(ctx->d_dCat), dptr<int>(ctx->d_dComp), dvar, h, flux,
+        dptr<double>(dfv));
+    k_th_face_gather<<<(ng + 127) / 128, 128, 0, ctx->stream>>>(ng, dptr<int>(dgp), dptr<int>(dgs), dptr<int>(dgr),
+                                                                 dptr<double>(dfv), dptr<double>(dout));
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "surface flux derivative"))) return rc;
+    CK(cudaMemcpyAsync(drtdd, dout.p, sizeof(double) * N, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}
+
+static int th_node_dload(astro_ctx *ctx, double t, int mode, int dvar, double *vec) {
+    const AstroPrep &P = ctx->P;
+    if (ctx->n2dRange.empty()) return ASTRO_OK;
+    DevBuf dv, act;
+    int rc;
+    struct Free {
+        DevBuf *b[2];
+        ~Free() {
+            for (auto *x : b) dev_free(*x);
+        }
+    } fr{{&dv, &act}};
+    if ((rc = upload(ctx, dv, vec, sizeof(double) * P.N))) return rc;
+    if (!ctx->dActTime.empty() && (rc = upload(ctx, act, ctx->dActTime.data(), sizeof(double) * ctx->dActTime.size())))
+        return rc;
+    k_th_node_dload<<<(P.N + 127) / 128, 128, 0, ctx->stream>>>(
+        P.N, dptr<int>(ctx->d_rank), dptr<int>(ctx->d_n2dR), dptr<int>(ctx->d_n2d), dptr<double>(ctx->d_n2c),
+        dptr<int>(ctx->d_dCat), dptr<int>(ctx->d_dComp), dptr<double>(ctx->d_dVal), act.p ? dptr<double>(act) : nullptr,
+        t, mode, dvar, dptr<double>(dv));
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "thermal nodal design load"))) return rc;
+    CK(cudaMemcpyAsync(vec, dv.p, sizeof(double) * P.N, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return ASTRO_OK;
+}
+
+extern "C" int astro_thermal_design_node_load(astro_ctx *ctx, double time, double *thermal_load) {
+    if (!ctx || !thermal_load) return ASTRO_ERR_ARG;
+    return th_node_dload(ctx, time, 0, 0, thermal_load);
+}
+
+extern "C" int astro_thermal_node_load_drdd(astro_ctx *ctx, int32_t dvar, double time, double *drtdd) {
+    if (!ctx || !drtdd) return ASTRO_ERR_ARG;
+    if (dvar < 1 || dvar > ctx->numDvars)
+        return set_err(ctx, ASTRO_ERR_ARG, "design variable " + std::to_string(dvar) + " out of range");
+    return th_node_dload(ctx, time, 1, dvar, drtdd);
 }

@@ -59,6 +59,10 @@ DCAT_LAYUP_ANGLE = 6
 DCAT_LAYUP_DENSITY = 7
 DCAT_NODE_COORD = 8
 DCAT_NODE_LOAD = 9
+DCAT_THERMAL_COND = 10
+DCAT_SPEC_HEAT = 11
+DCAT_LAYUP_THERMAL_COND = 12
+DCAT_LAYUP_SPEC_HEAT = 13
 
 
 def _p(a, typ):

@@ -67,6 +67,16 @@ def _lib():
                                             C.c_double, F64P, F64P, I32P, I32P]
         L.orc_body_load.restype = C.c_int
         L.orc_body_load.argtypes = [C.c_void_p, C.c_int, F64P, C.c_int, I32P, C.c_void_p, F64P]
+        L.orc_thermal_drdd.restype = C.c_int
+        L.orc_thermal_drdd.argtypes = [C.c_void_p, F64P, F64P, C.c_int, C.c_double, F64P, F64P, F64P, C.c_int,
+                                       C.c_double, C.c_double, F64P]
+        L.orc_thermal_heat_gen_drdd.restype = C.c_int
+        L.orc_thermal_heat_gen_drdd.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_int, I32P, F64P]
+        L.orc_thermal_surface_flux_drdd.restype = C.c_int
+        L.orc_thermal_surface_flux_drdd.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, I32P, I32P, C.c_double,
+                                                    F64P]
+        L.orc_thermal_design_node_load.argtypes = [C.c_void_p, C.c_double, F64P]
+        L.orc_thermal_node_load_drdd.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, F64P]
         _LIB = L
     return _LIB
 
@@ -235,6 +245,50 @@ class Oracle:
                                           opt(keep[2]), dynamic, gamma, del_t, _d(load), _d(mat), _i(cols), None)
         assert rc == 0
         return load, mat[:rng[N]], cols[:rng[N]], rng
+
+    def thermal_drdd(self, cond, spec_heat, dvar, h=1e-14, temp=None, prev_temp=None, prev_tdot=None, dynamic=0,
+                     gamma=0.5, del_t=0.0):
+        """getdRthermaldD element part: dRt/dd in rank order (complex step)."""
+        N = self.model.num_nodes
+        out = np.zeros(N)
+        keep = [None if a is None else np.ascontiguousarray(a, np.float64) for a in (temp, prev_temp, prev_tdot)]
+        rc = self.L.orc_thermal_drdd(self.h, _d(np.ascontiguousarray(cond, np.float64).reshape(-1)),
+                                     _d(np.ascontiguousarray(spec_heat, np.float64)), int(dvar), float(h),
+                                     *[None if a is None else _d(a) for a in keep], int(dynamic), float(gamma),
+                                     float(del_t), _d(out))
+        assert rc == 0
+        return out
+
+    def thermal_heat_gen_drdd(self, dvar, q, elements=None, h=1e-14, drtdd=None):
+        """getdRthermaldD's bodyHeatGen branch: drtdd -= d(heat-generation load)/d(dvar)."""
+        drtdd = np.zeros(self.model.num_nodes) if drtdd is None else drtdd
+        els = None if elements is None else np.ascontiguousarray(elements, np.int32)
+        rc = self.L.orc_thermal_heat_gen_drdd(self.h, int(dvar), float(h), float(q), 0 if els is None else len(els),
+                                              None if els is None else _i(els), _d(drtdd))
+        assert rc == 0
+        return drtdd
+
+    def thermal_surface_flux_drdd(self, dvar, face_el, face_num, flux, h=1e-14, drtdd=None):
+        """getdRthermaldD's surfaceFlux branch: drtdd += d(flux face load)/d(dvar)."""
+        drtdd = np.zeros(self.model.num_nodes) if drtdd is None else drtdd
+        fe = np.ascontiguousarray(face_el, np.int32)
+        fn = np.ascontiguousarray(face_num, np.int32)
+        rc = self.L.orc_thermal_surface_flux_drdd(self.h, int(dvar), float(h), len(fe), _i(fe), _i(fn), float(flux),
+                                                  _d(drtdd))
+        assert rc == 0
+        return drtdd
+
+    def thermal_design_node_load(self, t, load=None):
+        """getThermalAppliedLoad's nodal design heat inputs at time t, added to load (rank order)."""
+        load = np.zeros(self.model.num_nodes) if load is None else load
+        self.L.orc_thermal_design_node_load(self.h, float(t), _d(load))
+        return load
+
+    def thermal_node_load_drdd(self, dvar, t, h=1e-14, drtdd=None):
+        """getdRthermaldD's node branch: drtdd -= d(nodal heat input)/d(dvar) at time t."""
+        drtdd = np.zeros(self.model.num_nodes) if drtdd is None else drtdd
+        self.L.orc_thermal_node_load_drdd(self.h, int(dvar), float(t), float(h), _d(drtdd))
+        return drtdd
 
     def thermal_mpc(self, mpc_range, mpc_node, mpc_coef, mpc_rhs):
         """buildThermalMPC (Working/AStrO_bookKeeping.f90:614-752) for expanded equations: rows of

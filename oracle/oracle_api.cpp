@@ -142,19 +142,86 @@ static GState to_gstate(const astro_state *s) {
 
 // r_getNodeDLoad (Working/AStrO_r_designPropertyFunctions.f90:970-994, Q6 resolved: the loop runs
 // over the node's own terms): the elastic nodal design load of a node at time t, components
-// 1..6, for the variables active (dActTime(1) < t < dActTime(2), r_greater), with design variable
+// 1..6 and the thermal ndLd(7), for the variables active (dActTime(1) < t < dActTime(2), r_greater), with design variable
 // pert (if any) at d + i h.
-template <class T> static void t_node_dload(const astro_model *m, int node, double t, const DPert<T> &p, T ld[6]) {
-    for (int k = 0; k < 6; ++k) ld[k] = T(0.0);
+template <class T> static void t_node_dload(const astro_model *m, int node, double t, const DPert<T> &p, T ld[7]) {
+    for (int k = 0; k < 7; ++k) ld[k] = T(0.0);
     if (!m->nd_to_d_range || m->num_dvars <= 0) return;
     for (int q = m->nd_to_d_range[node - 1]; q < m->nd_to_d_range[node]; ++q) {
         const int d = m->nd_to_d[q];
         if (m->d_category[d - 1] != ASTRO_DCAT_NODE_LOAD) continue;
         if (m->d_act_time && !(t > m->d_act_time[2 * (d - 1)] && m->d_act_time[2 * (d - 1) + 1] > t)) continue;
         const int comp = m->d_component ? m->d_component[d - 1] : 0;
-        if (comp < 1 || comp > 6) continue;
+        if (comp < 1 || comp > 7) continue;  // 7: the 'thermal' subcategory, ndLd(7)
         ld[comp - 1] = ld[comp - 1] + m->nd_to_coef[q] * dval(m, d, p);
     }
+}
+
+// One face of the surface load (the per-face body of orc_surface_load): nodes (r_getNodeCoord:
+// coordinates with the nodeCoord terms, design variable p.dvar at d + i h), the face normal, the
+// traction t - pressure n, and the consistent nodal values of the integral of N t dA on the true
+// area with the 2x2 Gauss rule (abscissa KC<T>::rt3).
+template <class T>
+static void t_face_load(const astro_model *m, int el, int fn, const double *traction, double pressure,
+                        const DPert<T> &p, int nodes[4], T val[4][3]) {
+    static const int hexF[6][4] = {{4, 3, 2, 1}, {5, 6, 7, 8}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {4, 1, 5, 8}};
+    static const int shF[2][4] = {{1, 2, 3, 4}, {1, 4, 3, 2}};
+    const double rt3 = KC<T>::rt3();
+    const int t = m->element_type[el - 1];
+    const int *fl = (t == 8 || t == 81) ? hexF[fn - 1] : shF[fn - 1];
+    T X[4][3];
+    for (int k = 0; k < 4; ++k) {
+        nodes[k] = m->element_list[8 * (el - 1) + fl[k] - 1];
+        for (int d = 0; d < 3; ++d)
+            X[k][d] = T(m->node_list[3 * (nodes[k] - 1) + d]) + nd_dsum(m, nodes[k], ASTRO_DCAT_NODE_COORD, d + 1, p);
+    }
+    T v1[3], v2[3], nv[3];
+    for (int d = 0; d < 3; ++d) {
+        v1[d] = X[2][d] - X[0][d];
+        v2[d] = X[3][d] - X[1][d];
+    }
+    nv[0] = v1[1] * v2[2] - v1[2] * v2[1];
+    nv[1] = v1[2] * v2[0] - v1[0] * v2[2];
+    nv[2] = v1[0] * v2[1] - v1[1] * v2[0];
+    const T mag = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+    for (int d = 0; d < 3; ++d) nv[d] = nv[d] / mag;
+    T tr[3];
+    for (int d = 0; d < 3; ++d) tr[d] = traction[d] - pressure * nv[d];
+    for (int k = 0; k < 4; ++k)
+        for (int d = 0; d < 3; ++d) val[k][d] = T(0.0);
+    const double gp[4][2] = {{-rt3, -rt3}, {rt3, -rt3}, {-rt3, rt3}, {rt3, rt3}};
+    for (int g = 0; g < 4; ++g) {
+        const double s = gp[g][0], r = gp[g][1];
+        const double N[4] = {0.25 * (1 - s) * (1 - r), 0.25 * (1 + s) * (1 - r), 0.25 * (1 + s) * (1 + r),
+                             0.25 * (1 - s) * (1 + r)};
+        const double Ns[4] = {-0.25 * (1 - r), 0.25 * (1 - r), 0.25 * (1 + r), -0.25 * (1 + r)};
+        const double Nr[4] = {-0.25 * (1 - s), -0.25 * (1 + s), 0.25 * (1 + s), 0.25 * (1 - s)};
+        T a[3] = {T(0.0), T(0.0), T(0.0)}, b[3] = {T(0.0), T(0.0), T(0.0)};
+        for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d) {
+                a[d] += Ns[k] * X[k][d];
+                b[d] += Nr[k] * X[k][d];
+            }
+        const T cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
+        const T dA = std::sqrt(cx * cx + cy * cy + cz * cz);
+        for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d) val[k][d] += tr[d] * N[k] * dA;
+    }
+}
+
+// getdToElComp (Working/AStrO_bookKeeping.f90:7-129): the element depends on dvar through its own
+// design-variable terms or a nodeCoord term of one of its nodes.
+static bool el_depends(const astro_model *m, int el, int dvar) {
+    bool dep = false;
+    if (m->el_to_d_range)
+        for (int q = m->el_to_d_range[el - 1]; q < m->el_to_d_range[el]; ++q) dep = dep || m->el_to_d[q] == dvar;
+    if (m->nd_to_d_range && m->d_category[dvar - 1] == ASTRO_DCAT_NODE_COORD)
+        for (int k = 0; k < 8; ++k) {
+            const int nd = m->element_list[8 * (el - 1) + k];
+            if (nd > 0)
+                for (int q = m->nd_to_d_range[nd - 1]; q < m->nd_to_d_range[nd]; ++q) dep = dep || m->nd_to_d[q] == dvar;
+        }
+    return dep;
 }
 
 extern "C" {
@@ -834,7 +901,7 @@ int orc_gmres(double *xVec, const double *Amat, const int32_t *Acols, const int3
 void orc_design_node_load(const OracleCtx *c, double t, double *elasticLoad) {
     DPert<double> p;
     for (int nd = 1; nd <= c->numNodes; ++nd) {
-        double ld[6];
+        double ld[7];
         t_node_dload(c->m, nd, t, p, ld);
         for (int k = 1; k <= 6; ++k) {
             const int dof = c->nDofIndex[6 * (nd - 1) + k - 1];
@@ -855,7 +922,7 @@ void orc_node_load_drdd(const OracleCtx *c, int dvar, double t, double h, double
         bool dep = false;
         for (int q = m->nd_to_d_range[nd - 1]; q < m->nd_to_d_range[nd]; ++q) dep = dep || m->nd_to_d[q] == dvar;
         if (!dep) continue;
-        cd ld[6];
+        cd ld[7];
         t_node_dload(m, nd, t, p, ld);
         for (int k = 1; k <= 6; ++k) {
             const int dof = c->nDofIndex[6 * (nd - 1) + k - 1];
@@ -1018,53 +1085,16 @@ int orc_body_load(const OracleCtx *c, int kind, const double *vals, int nels, co
 
 void orc_surface_load(const OracleCtx *c, int nfaces, const int32_t *faceEl, const int32_t *faceNum,
                       const double *traction, double pressure, double *elasticLoad) {
-    const astro_model *m = c->m;
-    static const int hexF[6][4] = {{4, 3, 2, 1}, {5, 6, 7, 8}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 4, 8, 7}, {4, 1, 5, 8}};
-    static const int shF[2][4] = {{1, 2, 3, 4}, {1, 4, 3, 2}};
-    const double rt3 = 1.0 / std::sqrt(3.0);
+    DPert<double> p;
     for (int f = 0; f < nfaces; ++f) {
-        int el = faceEl[f], fn = faceNum[f];
-        int t = m->element_type[el - 1];
-        const int *fl = (t == 8 || t == 81) ? hexF[fn - 1] : shF[fn - 1];
-        double X[4][3];
         int nodes[4];
-        for (int k = 0; k < 4; ++k) {
-            nodes[k] = m->element_list[8 * (el - 1) + fl[k] - 1];
-            for (int d = 0; d < 3; ++d) X[k][d] = m->node_list[3 * (nodes[k] - 1) + d];
-        }
-        double v1[3], v2[3], nv[3];
-        for (int d = 0; d < 3; ++d) {
-            v1[d] = X[2][d] - X[0][d];
-            v2[d] = X[3][d] - X[1][d];
-        }
-        nv[0] = v1[1] * v2[2] - v1[2] * v2[1];
-        nv[1] = v1[2] * v2[0] - v1[0] * v2[2];
-        nv[2] = v1[0] * v2[1] - v1[1] * v2[0];
-        double mag = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
-        for (int d = 0; d < 3; ++d) nv[d] /= mag;
-        double tr[3];
-        for (int d = 0; d < 3; ++d) tr[d] = traction[d] - pressure * nv[d];
-        const double gp[4][2] = {{-rt3, -rt3}, {rt3, -rt3}, {-rt3, rt3}, {rt3, rt3}};
-        for (int g = 0; g < 4; ++g) {
-            double s = gp[g][0], r = gp[g][1];
-            double N[4] = {0.25 * (1 - s) * (1 - r), 0.25 * (1 + s) * (1 - r), 0.25 * (1 + s) * (1 + r),
-                           0.25 * (1 - s) * (1 + r)};
-            double Ns[4] = {-0.25 * (1 - r), 0.25 * (1 - r), 0.25 * (1 + r), -0.25 * (1 + r)};
-            double Nr[4] = {-0.25 * (1 - s), -0.25 * (1 + s), 0.25 * (1 + s), 0.25 * (1 - s)};
-            double a[3] = {0, 0, 0}, b[3] = {0, 0, 0};
-            for (int k = 0; k < 4; ++k)
-                for (int d = 0; d < 3; ++d) {
-                    a[d] += Ns[k] * X[k][d];
-                    b[d] += Nr[k] * X[k][d];
-                }
-            double cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
-            double dA = std::sqrt(cx * cx + cy * cy + cz * cz);
-            for (int k = 0; k < 4; ++k)
-                for (int d = 0; d < 3; ++d) {
-                    int dof = c->nDofIndex[6 * (nodes[k] - 1) + d];
-                    elasticLoad[dof - 1] += tr[d] * N[k] * dA;
-                }
-        }
+        double val[4][3];
+        t_face_load(c->m, faceEl[f], faceNum[f], traction, pressure, p, nodes, val);
+        for (int k = 0; k < 4; ++k)
+            for (int d = 0; d < 3; ++d) {
+                const int dof = c->nDofIndex[6 * (nodes[k] - 1) + d];
+                elasticLoad[dof - 1] += val[k][d];
+            }
     }
 }
 
@@ -1072,16 +1102,35 @@ void orc_surface_load(const OracleCtx *c, int nfaces, const int32_t *faceEl, con
 // Thermal material data are not part of astro_model: materialThermCond(6, num_materials)
 // (k11 k22 k33 k12 k13 k23) and materialSpecHeat(num_materials) are passed beside it.
 
-// r_getMaterialThermCond (Working/AStrO_r_designPropertyFunctions.f90:129-161) for solids and
-// r_getShellThermCond (:527-600) for shells (sum over layers of the layer thickness times the
-// layer conductivity rotated by the layup angle); thisSH as r_getElRtm selects it
-// (Working/AStrO_r_elementEqns.f90:2143-2149): density x specHeat for solids, r_getShellSpecHeat
-// (designProp :602-644: sum of thickness x density x specHeat) for shells.
-static void therm_props(const astro_model *m, const double *cond, const double *sh, int el, double tc[3][3],
-                        double &thisSH) {
-    DPert<double> p;
+}  // extern "C"
+
+// v += the element's terms of one design category (layer / component 0 = any), one term at a time
+// in the element's term order, as the property routines loop over elToD.
+template <class T>
+static void th_terms(const astro_model *m, int el, T &v, int cat, int layer, int comp, const DPert<T> &p) {
+    if (m->num_dvars <= 0 || !m->el_to_d_range) return;
+    for (int q = m->el_to_d_range[el - 1]; q < m->el_to_d_range[el]; ++q) {
+        const int d = m->el_to_d[q];
+        if (m->d_category[d - 1] != cat) continue;
+        if (layer && (!m->d_layer || m->d_layer[d - 1] != layer)) continue;
+        if (comp && (!m->d_component || m->d_component[d - 1] != comp)) continue;
+        v = v + m->el_to_coef[q] * dval(m, d, p);
+    }
+}
+
+// r_getMaterialThermCond (Working/AStrO_r_designPropertyFunctions.f90:129-161, 'thermalCond' terms)
+// for solids and r_getShellThermCond (:527-600: sum over layers of the layer thickness times the
+// layer conductivity rotated by the layup angle, the layer's 'layup' thermalCond / angle /
+// thickness terms applied) for shells; thisSH as r_getElRtm selects it
+// (Working/AStrO_r_elementEqns.f90:2136-2142): density (r_getMaterialDensity :82-103) x specHeat
+// (r_getMaterialSpecHeat :164-186) for solids, r_getShellSpecHeat (:602-644: sum of thickness x
+// density x specHeat, each with its layer terms) for shells.  secThick: the shell section
+// thickness (r_getElThickOffset).  Design variable p.dvar at d + i h.
+template <class T>
+static void therm_props(const astro_model *m, const double *cond, const double *sh, int el, T tc[3][3], T &thisSH,
+                        T &secThick, const DPert<T> &p) {
     const int et = m->element_type[el - 1], sec = m->element_section[el - 1];
-    auto fill = [](double t[3][3], const double *v) {
+    auto fill = [](T t[3][3], const T *v) {
         t[0][0] = v[0];
         t[1][1] = v[1];
         t[2][2] = v[2];
@@ -1089,39 +1138,63 @@ static void therm_props(const astro_model *m, const double *cond, const double *
         t[0][2] = t[2][0] = v[4];
         t[1][2] = t[2][1] = v[5];
     };
+    secThick = T(0.0);
     if (et != 41) {
         const int mat = m->section_mat_id[sec - 1];
-        fill(tc, cond + 6 * (mat - 1));
-        thisSH = m->material_density[mat - 1] * sh[mat - 1];
+        T cv[6];
+        for (int k = 0; k < 6; ++k) {
+            cv[k] = T(cond[6 * (mat - 1) + k]);
+            th_terms(m, el, cv[k], ASTRO_DCAT_THERMAL_COND, 0, k + 1, p);
+        }
+        fill(tc, cv);
+        T den = T(m->material_density ? m->material_density[mat - 1] : 0.0), spec = T(sh[mat - 1]);
+        th_terms(m, el, den, ASTRO_DCAT_DENSITY, 0, 0, p);
+        th_terms(m, el, spec, ASTRO_DCAT_SPEC_HEAT, 0, 0, p);
+        thisSH = den * spec;
         return;
     }
     for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) tc[i][j] = 0.0;
-    thisSH = 0.0;
+        for (int j = 0; j < 3; ++j) tc[i][j] = T(0.0);
+    thisSH = T(0.0);
     for (int i1 = m->sec_layup_range[sec - 1] + 1, ln = 1; i1 <= m->sec_layup_range[sec]; ++i1, ++ln) {
         const int mat = m->layup_mat_id[i1 - 1];
-        double tl[3][3], al[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 1.0}}, pr[3][3], tg[3][3];
-        fill(tl, cond + 6 * (mat - 1));
-        const double lt = layer_thickness(m, el, ln, i1, p), ang = m->layup_angle[i1 - 1];
+        T cv[6], tl[3][3], al[3][3], pr[3][3], tg[3][3];
+        for (int k = 0; k < 6; ++k) {
+            cv[k] = T(cond[6 * (mat - 1) + k]);
+            th_terms(m, el, cv[k], ASTRO_DCAT_LAYUP_THERMAL_COND, ln, k + 1, p);
+        }
+        fill(tl, cv);
+        T ang = T(m->layup_angle[i1 - 1]), den = T(m->material_density ? m->material_density[mat - 1] : 0.0),
+          spec = T(sh[mat - 1]);
+        th_terms(m, el, ang, ASTRO_DCAT_LAYUP_ANGLE, ln, 0, p);
+        th_terms(m, el, den, ASTRO_DCAT_LAYUP_DENSITY, ln, 0, p);
+        th_terms(m, el, spec, ASTRO_DCAT_LAYUP_SPEC_HEAT, ln, 0, p);
+        const T lt = layer_thickness(m, el, ln, i1, p);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) al[a][b] = T(0.0);
+        al[2][2] = T(1.0);
         al[0][0] = t_cos(ang);
         al[1][0] = t_sin(ang);
         al[0][1] = -al[1][0];
         al[1][1] = al[0][0];
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
-                pr[a][b] = 0.0;
+                pr[a][b] = T(0.0);
                 for (int k = 0; k < 3; ++k) pr[a][b] = pr[a][b] + tl[a][k] * al[b][k];
             }
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) {
-                tg[a][b] = 0.0;
+                tg[a][b] = T(0.0);
                 for (int k = 0; k < 3; ++k) tg[a][b] = tg[a][b] + al[a][k] * pr[k][b];
             }
         for (int a = 0; a < 3; ++a)
             for (int b = 0; b < 3; ++b) tc[a][b] = tc[a][b] + lt * tg[a][b];
-        thisSH = thisSH + lt * m->material_density[mat - 1] * sh[mat - 1];
+        thisSH = thisSH + lt * den * spec;
+        secThick = secThick + lt;
     }
 }
+
+extern "C" {
 
 // getThermalSolnLoad (Working/AStrO_commandFunctions.f90:16-72) with r_getElRt / r_getElRtk /
 // r_getElRtm (Working/AStrO_r_elementEqns.f90:2062-2204): thermalLoad(rank) -= Rt, and for
@@ -1155,8 +1228,8 @@ int orc_thermal_soln_load(const OracleCtx *c, const double *cond, const double *
     for (int el = 1; el <= c->numEls; ++el) {
         ElemData<double> e;
         if (t_getElementData(e, m, c->nDofIndex.data(), c->intVecRange.data(), el, g, p) != 0) return 1;
-        double tc[3][3], thisSH;
-        therm_props(m, cond, sh, el, tc, thisSH);
+        double tc[3][3], thisSH, secThick;
+        therm_props(m, cond, sh, el, tc, thisSH, secThick, p);
         const int nn = e.numNds;
         double temp[10] = {0}, pT[10] = {0}, pTd[10] = {0};
         for (int i = 0; i < nn; ++i) {
@@ -1247,6 +1320,163 @@ int orc_thermal_soln_load(const OracleCtx *c, const double *cond, const double *
             }
     }
     return 0;
+}
+
+
+// getdRthermaldD (Working/AStrO_commandFunctions.f90:1016-1170), element part (:1040-1059):
+// dRtdD (rank order) zeroed, then for every element that depends on dvar c_getElRt with buildMat
+// 0 (c_getElRtk, plus c_getElRtm when dynamic, Working/AStrO_c_elementEqns.f90) at d + i h, and
+// Im(Rt) / h summed at the element's nodes.  Temperatures as orc_thermal_soln_load.
+int orc_thermal_drdd(const OracleCtx *c, const double *cond, const double *sh, int dvar, double h,
+                     const double *nodeTemp, const double *prevTemp, const double *prevTdot, int dynamic,
+                     double gamma, double delT, double *dRtdD) {
+    const astro_model *m = c->m;
+    std::fill(dRtdD, dRtdD + c->numNodes, 0.0);
+    if (dvar < 1 || dvar > m->num_dvars) return 1;
+    GState g;
+    DPert<cd> p;
+    p.dvar = dvar;
+    p.h = h;
+    for (int el = 1; el <= c->numEls; ++el) {
+        if (!el_depends(m, el, dvar)) continue;
+        ElemData<cd> e;
+        if (t_getElementData(e, m, c->nDofIndex.data(), c->intVecRange.data(), el, g, p) != 0) return 1;
+        cd tc[3][3], thisSH, secThick;
+        therm_props(m, cond, sh, el, tc, thisSH, secThick, p);
+        const int nn = e.numNds;
+        double temp[10] = {0}, Td[10] = {0};
+        int rk[10];
+        for (int i = 0; i < nn; ++i) {
+            rk[i] = c->currentRank[m->element_list[8 * (el - 1) + i] - 1];
+            temp[i] = nodeTemp ? nodeTemp[rk[i] - 1] : 0.0;
+            const double pT = prevTemp ? prevTemp[rk[i] - 1] : 0.0, pTd = prevTdot ? prevTdot[rk[i] - 1] : 0.0;
+            if (dynamic == 1) Td[i] = (1.0 / gamma) * ((1.0 / delT) * (temp[i] - pT) - 1.0 * (1.0 - gamma) * pTd);
+        }
+        cd Rt[10];
+        for (int i = 0; i < 10; ++i) Rt[i] = cd(0.0);
+        for (int i1 = 1; i1 <= e.numIntPts; ++i1) {
+            A1<cd, 11> Nvec;
+            A2<cd, 11, 3> Nx;
+            cd detJ;
+            t_getIntPtData(Nvec, Nx, detJ, e.locNds, e.intPts[i1 - 1], e.eType, nn);
+            cd Tx[3] = {cd(0.0), cd(0.0), cd(0.0)}, q[3] = {cd(0.0), cd(0.0), cd(0.0)};
+            for (int i2 = 1; i2 <= nn; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3) Tx[i3 - 1] = Tx[i3 - 1] + Nx(i2, i3) * temp[i2 - 1];
+            for (int i2 = 0; i2 < 3; ++i2)
+                for (int i3 = 0; i3 < 3; ++i3) q[i2] = q[i2] + tc[i2][i3] * Tx[i3];
+            const cd wd = detJ * e.ipWt[i1 - 1];
+            for (int k = 0; k < 3; ++k) q[k] = wd * q[k];
+            for (int i2 = 1; i2 <= nn; ++i2)
+                for (int i3 = 1; i3 <= 3; ++i3) Rt[i2 - 1] = Rt[i2 - 1] + Nx(i2, i3) * q[i3 - 1];
+        }
+        if (dynamic == 1) {
+            cd Rtm[10];
+            for (int i = 0; i < 10; ++i) Rtm[i] = cd(0.0);
+            for (int i1 = 1; i1 <= e.numIntPts; ++i1) {
+                A1<cd, 11> Nvec;
+                A2<cd, 11, 3> Nx;
+                cd detJ;
+                t_getIntPtData(Nvec, Nx, detJ, e.locNds, e.intPts[i1 - 1], e.eType, nn);
+                cd pt = cd(0.0);
+                for (int i2 = 1; i2 <= nn; ++i2) pt = pt + Td[i2 - 1] * Nvec(i2);
+                pt = detJ * e.ipWt[i1 - 1] * thisSH * pt;
+                for (int i2 = 1; i2 <= nn; ++i2) Rtm[i2 - 1] = Rtm[i2 - 1] + pt * Nvec(i2);
+            }
+            for (int k = 0; k < nn; ++k) Rt[k] = Rt[k] + Rtm[k];
+        }
+        for (int i = 0; i < nn; ++i) dRtdD[rk[i] - 1] += (1.0 / h) * Rt[i].imag();
+    }
+    return 0;
+}
+
+// getdRthermaldD's bodyHeatGen branch (:1065-1108): for the listed elements (all when nels = 0;
+// an element listed twice counts twice) that depend on dvar, c_getElBodyForce with the heat
+// generation q as the first body-force component (times the section thickness for shells), and
+// dRtdD(rank) -= Im(component-1 nodal value) / h.
+int orc_thermal_heat_gen_drdd(const OracleCtx *c, int dvar, double h, double q, int nels, const int32_t *els,
+                              double *dRtdD) {
+    const astro_model *m = c->m;
+    if (dvar < 1 || dvar > m->num_dvars) return 1;
+    GState g;
+    DPert<cd> p;
+    p.dvar = dvar;
+    p.h = h;
+    const int count = nels > 0 ? nels : c->numEls;
+    for (int k = 0; k < count; ++k) {
+        const int el = nels > 0 ? els[k] : k + 1;
+        if (!el_depends(m, el, dvar)) continue;
+        ElemData<cd> e;
+        if (t_getElementData(e, m, c->nDofIndex.data(), c->intVecRange.data(), el, g, p) != 0) return 1;
+        cd w[10];
+        for (int i = 0; i < 10; ++i) w[i] = cd(0.0);
+        for (int i1 = 1; i1 <= e.numIntPts; ++i1) {
+            A1<cd, 11> Nvec;
+            A2<cd, 11, 3> Nx;
+            cd detJ;
+            t_getIntPtData(Nvec, Nx, detJ, e.locNds, e.intPts[i1 - 1], e.eType, e.numNds);
+            detJ = detJ * e.ipWt[i1 - 1];
+            for (int a = 1; a <= e.numNds; ++a) w[a - 1] = w[a - 1] + q * Nvec(a) * detJ;
+        }
+        if (e.eType == 41) {
+            const int sec = m->element_section[el - 1];
+            cd thick = cd(0.0);
+            for (int i1 = m->sec_layup_range[sec - 1] + 1, ln = 1; i1 <= m->sec_layup_range[sec]; ++i1, ++ln)
+                thick = thick + layer_thickness(m, el, ln, i1, p);
+            for (int a = 0; a < e.numNds; ++a) w[a] = thick * w[a];
+        }
+        for (int a = 0; a < e.numNds; ++a)
+            dRtdD[c->currentRank[m->element_list[8 * (el - 1) + a] - 1] - 1] -= w[a].imag() / h;
+    }
+    return 0;
+}
+
+// getdRthermaldD's surfaceFlux branch (:1109-1152): for the given faces whose element depends on
+// dvar, the face load of the flux as the first traction component at d + i h, and
+// dRtdD(rank) += Im(component-1 nodal value) / h.
+int orc_thermal_surface_flux_drdd(const OracleCtx *c, int dvar, double h, int nfaces, const int32_t *faceEl,
+                                  const int32_t *faceNum, double flux, double *dRtdD) {
+    const astro_model *m = c->m;
+    if (dvar < 1 || dvar > m->num_dvars) return 1;
+    DPert<cd> p;
+    p.dvar = dvar;
+    p.h = h;
+    const double tr[3] = {flux, 0.0, 0.0};
+    for (int f = 0; f < nfaces; ++f) {
+        if (!el_depends(m, faceEl[f], dvar)) continue;
+        int nodes[4];
+        cd val[4][3];
+        t_face_load(m, faceEl[f], faceNum[f], tr, 0.0, p, nodes, val);
+        for (int k = 0; k < 4; ++k) dRtdD[c->currentRank[nodes[k] - 1] - 1] += val[k][0].imag() / h;
+    }
+    return 0;
+}
+
+// getThermalAppliedLoad's closing loop (:182-186): thermalLoad(rank) += ndLd(7) of every node.
+void orc_thermal_design_node_load(const OracleCtx *c, double t, double *thermalLoad) {
+    DPert<double> p;
+    for (int nd = 1; nd <= c->numNodes; ++nd) {
+        double ld[7];
+        t_node_dload(c->m, nd, t, p, ld);
+        thermalLoad[c->currentRank[nd - 1] - 1] += ld[6];
+    }
+}
+
+// getdRthermaldD's node branch (:1162-1167): dRtdD(rank) -= Im(ndLd(7)(d + i h)) / h at the nodes of
+// the design variable.
+void orc_thermal_node_load_drdd(const OracleCtx *c, int dvar, double t, double h, double *dRtdD) {
+    const astro_model *m = c->m;
+    if (!m->nd_to_d_range) return;
+    DPert<cd> p;
+    p.dvar = dvar;
+    p.h = h;
+    for (int nd = 1; nd <= c->numNodes; ++nd) {
+        bool dep = false;
+        for (int q = m->nd_to_d_range[nd - 1]; q < m->nd_to_d_range[nd]; ++q) dep = dep || m->nd_to_d[q] == dvar;
+        if (!dep) continue;
+        cd ld[7];
+        t_node_dload(m, nd, t, p, ld);
+        dRtdD[c->currentRank[nd - 1] - 1] -= ld[6].imag() / h;
+    }
 }
 
 }  // extern "C"
