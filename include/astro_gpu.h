@@ -58,6 +58,10 @@ extern "C" {
 #define ASTRO_DCAT_LAYUP_THERMAL_COND 12 /* 'layup' / 'thermalCond': conductivity entry d_component (1..6) of layer
                                             d_layer (r_getShellThermCond, :556) */
 #define ASTRO_DCAT_LAYUP_SPEC_HEAT 13  /* 'layup' / 'specHeat' of layer d_layer (r_getShellSpecHeat, :630) */
+#define ASTRO_DCAT_LAYUP_MODULUS 14    /* 'layup' / 'modulus', 'poissonRatio', 'shearModulus' of layer d_layer
+                                          (r_getShellStiffness, :289-303): d_component indexes the layer's
+                                          (E1, E2, nu12, G12), 1..4; poissonRatio is component 3 and
+                                          shearModulus component 4, as the reference maps them */
 
 /* Model arrays: the reference's module globals (Working/AStrO_globalData.f90) as flat arrays.
  * Element types: 8 = brick8 (2x2x2 Gauss), 81 = brickIM (brick8 plus three incompatible bubbles,

@@ -161,20 +161,23 @@ extern "C" int astro_ctx_create(const astro_model *m, astro_ctx **out) {
             return fail(ASTRO_ERR_ARG, "design variables without their element maps");
         for (int d = 0; d < m->num_dvars; ++d) {
             const int cat = m->d_category[d];
-            if (cat < ASTRO_DCAT_LAYUP_THICKNESS || cat > ASTRO_DCAT_LAYUP_SPEC_HEAT)
+            if (cat < ASTRO_DCAT_LAYUP_THICKNESS || cat > ASTRO_DCAT_LAYUP_MODULUS)
                 return fail(ASTRO_ERR_UNSUPPORTED, "design-variable category not supported");
             const int comp = m->d_component ? m->d_component[d] : 0;
             const int maxComp = cat == ASTRO_DCAT_ELASTIC_MODULUS ? 9
                                 : cat == ASTRO_DCAT_NODE_LOAD ? 7
                                 : (cat == ASTRO_DCAT_THERMAL_COND || cat == ASTRO_DCAT_LAYUP_THERMAL_COND) ? 6
+                                : cat == ASTRO_DCAT_LAYUP_MODULUS                                          ? 4
                                                                                                           : 3;
             if ((cat == ASTRO_DCAT_ELASTIC_MODULUS || cat == ASTRO_DCAT_ORIENTATION || cat == ASTRO_DCAT_NODE_COORD ||
-                 cat == ASTRO_DCAT_NODE_LOAD || cat == ASTRO_DCAT_THERMAL_COND || cat == ASTRO_DCAT_LAYUP_THERMAL_COND) &&
+                 cat == ASTRO_DCAT_NODE_LOAD || cat == ASTRO_DCAT_THERMAL_COND || cat == ASTRO_DCAT_LAYUP_THERMAL_COND ||
+                 cat == ASTRO_DCAT_LAYUP_MODULUS) &&
                 (comp < 1 || comp > maxComp))
                 return fail(ASTRO_ERR_ARG, "design variable " + std::to_string(d + 1) + " needs d_component in 1.." +
                                                std::to_string(maxComp));
             if ((cat == ASTRO_DCAT_LAYUP_THICKNESS || cat == ASTRO_DCAT_LAYUP_ANGLE || cat == ASTRO_DCAT_LAYUP_DENSITY ||
-                 cat == ASTRO_DCAT_LAYUP_THERMAL_COND || cat == ASTRO_DCAT_LAYUP_SPEC_HEAT) &&
+                 cat == ASTRO_DCAT_LAYUP_THERMAL_COND || cat == ASTRO_DCAT_LAYUP_SPEC_HEAT ||
+                 cat == ASTRO_DCAT_LAYUP_MODULUS) &&
                 (!m->d_layer || m->d_layer[d] < 1))
                 return fail(ASTRO_ERR_ARG, "layer design variable needs d_layer >= 1");
         }

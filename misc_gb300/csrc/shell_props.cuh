@@ -115,9 +115,10 @@ __device__ void shell_props(const double *nodes, const int *el, const double *se
         const LayerDev L = lay[li];
         const T tl = thick(li, ln);
         const T zn = z + tl;
-        T S[3][3] = {{T(1.0) / T(L.E1), -T(L.nu12) / T(L.E1), T(0.0)},
-                     {-T(L.nu12) / T(L.E1), T(1.0) / T(L.E2), T(0.0)},
-                     {T(0.0), T(0.0), T(1.0) / T(L.G12)}};
+        // the layer's (E1, E2, nu12, G12) with its 'layup' modulus / poissonRatio / shearModulus terms
+        const T E1 = T(L.E1) + dsum(ASTRO_DCAT_LAYUP_MODULUS, ln, 1), E2 = T(L.E2) + dsum(ASTRO_DCAT_LAYUP_MODULUS, ln, 2);
+        const T nu12 = T(L.nu12) + dsum(ASTRO_DCAT_LAYUP_MODULUS, ln, 3), G12 = T(L.G12) + dsum(ASTRO_DCAT_LAYUP_MODULUS, ln, 4);
+        T S[3][3] = {{T(1.0) / E1, -nu12 / E1, T(0.0)}, {-nu12 / E1, T(1.0) / E2, T(0.0)}, {T(0.0), T(0.0), T(1.0) / G12}};
         T Q[3][3];
         a_lu<T, 3>(&S[0][0], 3);
         for (int c = 0; c < 3; ++c) {

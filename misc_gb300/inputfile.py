@@ -463,8 +463,34 @@ def write_model_input(m: Model, path, node_sets=None, point_loads=None):
         f.write("\n".join(out) + "\n")
 
 
-# design-variable categories the device complex step evaluates (astro_model d_category)
-_DCAT = {("layup", "thickness"): 1, ("elastic", "modulus"): 2}
+# design-variable categories (astro_model d_category): (category, subCategory) -> (d_category,
+# component offset, node category).  The reference's property routines
+# (Working/AStrO_r_designPropertyFunctions.f90) select on these names: 'elastic' modulus /
+# poissonRatio / shearModulus index eProps (component, + 3, + 6; :46-53), the shell layer's
+# modulus / poissonRatio / shearModulus index layerProps (component, 3, 4; :292-298), and
+# 'nodeLoad' / 'thermal' is ndLd(7) (:986-987).
+_DCAT = {
+    ("layup", "thickness"): (1, 0, False), ("elastic", "modulus"): (2, 0, False),
+    ("elastic", "poissonRatio"): (2, 3, False), ("elastic", "shearModulus"): (2, 6, False),
+    ("density", ""): (3, 0, False), ("orientation", ""): (4, 0, False), ("layup", "zOffset"): (5, 0, False),
+    ("layup", "angle"): (6, 0, False), ("layup", "density"): (7, 0, False), ("nodeCoord", ""): (8, 0, True),
+    ("nodeLoad", "elastic"): (9, 0, True), ("nodeLoad", "thermal"): (9, None, True),
+    ("thermalCond", ""): (10, 0, False), ("specHeat", ""): (11, 0, False), ("layup", "thermalCond"): (12, 0, False),
+    ("layup", "specHeat"): (13, 0, False), ("layup", "modulus"): (14, 0, False),
+    ("layup", "poissonRatio"): (14, None, False), ("layup", "shearModulus"): (14, None, False),
+}
+# fixed components of the entries marked None above
+_FIXED_COMP = {("nodeLoad", "thermal"): 7, ("layup", "poissonRatio"): 3, ("layup", "shearModulus"): 4}
+
+
+def _dcat(dv):
+    """(d_category, d_component, node category) of one design variable, or None."""
+    key = (dv["category"], dv["subCategory"])
+    if key not in _DCAT:
+        return None
+    cat, off, node = _DCAT[key]
+    comp = _FIXED_COMP[key] if off is None else max(dv["component"], 1) + off
+    return cat, comp, node
 
 
 def read_design_var_input(path, mi: ModelInput):
@@ -515,31 +541,40 @@ def read_design_var_input(path, mi: ModelInput):
 
 
 def apply_design_vars(m: Model, dvs, values=None, strict=True):
-    """Attaches the element design variables the complex step evaluates (layup thickness,
-    elastic modulus) to m as elToD / elToCoef (per element, the variables in input order, an
-    element listed twice for one variable kept once).  Other categories raise (strict) or are
-    left out; returns the input numbers (1-based) of the variables kept."""
-    keep = []
+    """Attaches the design variables to m: element categories as elToD / elToCoef (per element,
+    the variables in input order, an element listed twice for one variable kept once), node
+    categories (nodeCoord, nodeLoad) as ndToD / ndToCoef over their node sets, with the activity
+    window of activeTime.  Categories the library does not evaluate raise (strict) or are left
+    out; returns the input numbers (1-based) of the variables kept."""
+    keep, cats = [], []
     for k, dv in enumerate(dvs):
-        cat = _DCAT.get((dv["category"], dv["subCategory"]))
-        if cat is None:
+        c = _dcat(dv)
+        if c is None:
             if strict:
                 raise ValueError(f"design variable {k + 1}: {dv['category']}/{dv['subCategory']} is not evaluated "
                                  f"by the device complex step")
             continue
         keep.append(k)
-    E = m.num_els
+        cats.append(c)
+    E, N = m.num_els, m.num_nodes
     per_el = [[] for _ in range(E)]
-    for j, k in enumerate(keep):
+    per_nd = [[] for _ in range(N)]
+    for j, (k, (_, _, node)) in enumerate(zip(keep, cats)):
         dv = dvs[k]
-        for e, c in zip(dv["elements"], dv["coefficients"]):
-            if all(d != j + 1 for d, _ in per_el[e - 1]):
-                per_el[e - 1].append((j + 1, c))
+        members, lists = (dv["nodes"], per_nd) if node else (dv["elements"], per_el)
+        for x, c in zip(members, dv["coefficients"]):
+            if all(d != j + 1 for d, _ in lists[x - 1]):
+                lists[x - 1].append((j + 1, c))
     m.el_to_d_range = np.cumsum([0] + [len(p) for p in per_el]).astype(np.int32)
     m.el_to_d = np.array([d for p in per_el for d, _ in p], np.int32)
     m.el_to_coef = np.array([c for p in per_el for _, c in p], np.float64)
-    m.d_category = np.array([_DCAT[(dvs[k]["category"], dvs[k]["subCategory"])] for k in keep], np.int32)
-    m.d_component = np.array([max(dvs[k]["component"], 1) for k in keep], np.int32)
+    if any(node for _, _, node in cats):
+        m.nd_to_d_range = np.cumsum([0] + [len(p) for p in per_nd]).astype(np.int32)
+        m.nd_to_d = np.array([d for p in per_nd for d, _ in p], np.int32)
+        m.nd_to_coef = np.array([c for p in per_nd for _, c in p], np.float64)
+        m.d_act_time = np.array([dvs[k]["activeTime"] for k in keep], np.float64).reshape(-1, 2)
+    m.d_category = np.array([c[0] for c in cats], np.int32)
+    m.d_component = np.array([c[1] for c in cats], np.int32)
     m.d_layer = np.array([max(dvs[k]["layer"], 1) for k in keep], np.int32)
     m.d_value = np.zeros(len(keep)) if values is None else np.asarray(values, np.float64)[keep]
     return [k + 1 for k in keep]

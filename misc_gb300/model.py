@@ -63,6 +63,7 @@ DCAT_THERMAL_COND = 10
 DCAT_SPEC_HEAT = 11
 DCAT_LAYUP_THERMAL_COND = 12
 DCAT_LAYUP_SPEC_HEAT = 13
+DCAT_LAYUP_MODULUS = 14
 
 
 def _p(a, typ):

@@ -213,10 +213,12 @@ static void t_getShellStiffness(A2<T, 9, 9> &ABD, const astro_model *m, int el, 
         layerNum++;
         int mat = m->layup_mat_id[i1 - 1];
         T lp[6];
-        lp[0] = T(m->material_elastic[9 * (mat - 1) + 0]);
-        lp[1] = T(m->material_elastic[9 * (mat - 1) + 1]);
-        lp[2] = T(m->material_elastic[9 * (mat - 1) + 3]);
-        lp[3] = T(m->material_elastic[9 * (mat - 1) + 6]);
+        // layerProps(1:4) = (E1, E2, nu12, G12) with the layer's 'layup' modulus (dComponent),
+        // poissonRatio (3) and shearModulus (4) terms (:289-303)
+        lp[0] = T(m->material_elastic[9 * (mat - 1) + 0]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_MODULUS, layerNum, 1, p);
+        lp[1] = T(m->material_elastic[9 * (mat - 1) + 1]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_MODULUS, layerNum, 2, p);
+        lp[2] = T(m->material_elastic[9 * (mat - 1) + 3]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_MODULUS, layerNum, 3, p);
+        lp[3] = T(m->material_elastic[9 * (mat - 1) + 6]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_MODULUS, layerNum, 4, p);
         lp[4] = layer_thickness(m, el, layerNum, i1, p);
         lp[5] = T(m->layup_angle[i1 - 1]) + el_dsum(m, el, ASTRO_DCAT_LAYUP_ANGLE, layerNum, 0, p);
         T zNext = zCrd + lp[4];

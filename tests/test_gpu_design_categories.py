@@ -2,8 +2,9 @@
 
 * The complex step of the element residual (getdRelasticdD's element part) for every category the
   device evaluates: solid density, orientation and node coordinates (brick8 and brickIM, the
-  complex element kernel) and shell layup zOffset, layer angle and layer density (the complex
-  section properties), at displaced (and, where density enters, dynamic) states: 1e-10 relative.
+  complex element kernel) and shell layup zOffset, layer angle, layer density and the layer's
+  elastic constants (the complex section properties), at displaced (and, where density enters,
+  dynamic) states: 1e-10 relative.
 * Models carrying nonzero real values of those variables: element matrices 1e-12 relative.
 * nodeLoad variables: the applied nodal design load and its derivative, exact.
 * The complex step of shell orientation / node-coordinate variables is refused
@@ -51,14 +52,17 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("case", ["brick_orientation", "brickIM_node_coord", "brick_density", "shell_zoffset",
-                                  "shell_layup_angle", "shell_layup_density"])
+                                  "shell_layup_angle", "shell_layup_density", "shell_layup_modulus",
+                                  "shell_layup_poisson"])
 def test_real_design_values_enter_the_element(case):
-    """Nonzero design values: rotated frames, moved nodes, changed density / offset / layer angle
-    and layer density, element matrices (with the Newmark mass where density enters)."""
+    """Nonzero design values: rotated frames, moved nodes, changed density / offset / layer angle,
+    layer density and layer elastic constants, element matrices (with the Newmark mass where
+    density enters)."""
     build, _, dyn = _CAT_CASES[case]
     m = build()
     scale = {"brick_orientation": 0.3, "brickIM_node_coord": 0.02, "brick_density": 500.0, "shell_zoffset": 0.4,
-             "shell_layup_angle": 0.5, "shell_layup_density": 900.0}[case]
+             "shell_layup_angle": 0.5, "shell_layup_density": 900.0, "shell_layup_modulus": 2.0e10,
+             "shell_layup_poisson": 0.05}[case]
     m.d_value = np.array([scale, -0.5 * scale])
     g, o = AstroGPU(m), Oracle(m)
     st = _state(o, dyn, seed=3)

@@ -182,22 +182,54 @@ def test_read_model_solves_on_the_gpu():
 
 
 def test_design_variable_input():
-    """The reference's example design-variable file: a layup thickness variable (evaluated by
-    the complex step) and a layup modulus variable (not: strict mode refuses, otherwise it is
-    left out); the thickness variable then moves the oracle's element stiffness like a thicker
-    layer."""
+    """The reference's example design-variable file: a layup thickness variable and a layup
+    modulus variable (E1 of layer 1, coefficient 2).  Both map to element categories; with values
+    they move the oracle's element stiffness like a thicker, stiffer layer.  A category the
+    library does not evaluate (thermal expansion) is refused in strict mode and left out
+    otherwise."""
     mi = IF.read_model_input(FIX)
     dvs = IF.read_design_var_input(FIX.with_name("shell_beam_dvar_input.yaml"), mi)
     assert [(d["category"], d["subCategory"], d["layer"], d["component"]) for d in dvs] == \
         [("layup", "thickness", 1, 0), ("layup", "modulus", 1, 1)]
     assert dvs[0]["elements"] == list(range(1, 11)) and dvs[1]["coefficients"] == [2.0] * 10
     m = mi.model()
-    with pytest.raises(ValueError):
-        IF.apply_design_vars(m, dvs)
-    kept = IF.apply_design_vars(m, dvs, values=[0.01, 5.0], strict=False)
-    assert kept == [1]
-    assert m.el_to_d_range.tolist() == list(range(11)) and np.all(m.el_to_d == 1) and np.all(m.el_to_coef == 1.0)
+    kept = IF.apply_design_vars(m, dvs, values=[0.01, 5.0e9])
+    assert kept == [1, 2]
+    assert m.d_category.tolist() == [M.DCAT_LAYUP_THICKNESS, M.DCAT_LAYUP_MODULUS]
+    assert m.d_component.tolist() == [1, 1] and m.d_layer.tolist() == [1, 1]
+    assert m.el_to_d_range.tolist() == list(range(0, 21, 2)) and m.el_to_d.tolist() == [1, 2] * 10
+    assert m.el_to_coef.tolist() == [1.0, 2.0] * 10
     ke = Oracle(m).element_matrices()
     m2 = mi.model()
     m2.layup_thickness = m2.layup_thickness + 0.01
+    me = m2.material_elastic.copy()
+    me[m2.layup_mat_id[0] - 1, 0] += 1.0e10
+    m2.material_elastic = me
     assert np.allclose(ke, Oracle(m2).element_matrices(), rtol=1e-12, atol=1e-9 * np.abs(ke).max())
+    extra = dict(category="thermalExp", subCategory="", component=1, layer=0, activeTime=[0.0, 0.0], elements=[1],
+                 nodes=[], coefficients=[1.0])
+    with pytest.raises(ValueError):
+        IF.apply_design_vars(mi.model(), dvs + [extra])
+    assert IF.apply_design_vars(mi.model(), dvs + [extra], strict=False) == [1, 2]
+
+
+def test_node_design_variable_input(tmp_path):
+    """nodeCoord and nodeLoad (elastic and thermal) variables over node sets, with the activity
+    window of activeTime, become ndToD terms."""
+    mi = IF.read_model_input(FIX)
+    m = mi.model()
+    name, nodes = next(iter(mi.node_sets.items()))
+    f = tmp_path / "dv.yaml"
+    f.write_text("designVariables:\n"
+                 f"    - category: nodeCoord\n      component: 2\n      nodeSet: {name}\n      coefficients: 1.0\n"
+                 f"    - category: nodeLoad\n      subCategory: thermal\n      activeTime: [0.5, 2.0]\n"
+                 f"      nodeSet: {name}\n      coefficients: 3.0\n")
+    dvs = IF.read_design_var_input(f, mi)
+    assert IF.apply_design_vars(m, dvs, values=[0.0, 1.0]) == [1, 2]
+    assert m.d_category.tolist() == [M.DCAT_NODE_COORD, M.DCAT_NODE_LOAD] and m.d_component.tolist() == [2, 7]
+    assert m.d_act_time[1].tolist() == [0.5, 2.0]
+    per = {nd: m.nd_to_d[m.nd_to_d_range[nd - 1]:m.nd_to_d_range[nd]].tolist() for nd in nodes}
+    assert all(v == [1, 2] for v in per.values())
+    o = Oracle(m)
+    q = o.thermal_design_node_load(1.0)
+    assert np.isclose(q.sum(), 3.0 * len(set(nodes)))

@@ -503,6 +503,12 @@ _CAT_CASES = {
                           False),
     "shell_layup_density": (lambda: M.add_design_variables(_layered_plate(), 2, M.DCAT_LAYUP_DENSITY, layer=1),
                             1e-6 * 2700.0, True),
+    "shell_layup_modulus": (lambda: M.add_design_variables(_layered_plate(), 2, M.DCAT_LAYUP_MODULUS, layer=2,
+                                                           component=1), 1e-6 * 7e10, False),
+    "shell_layup_poisson": (lambda: M.add_design_variables(_layered_plate(), 2, M.DCAT_LAYUP_MODULUS, layer=1,
+                                                           component=3), 1e-6, False),
+    "shell_layup_shear_modulus": (lambda: M.add_design_variables(_layered_plate(), 2, M.DCAT_LAYUP_MODULUS,
+                                                                 layer=2, component=4), 1e-6 * 1e10, False),
 }
 
 
@@ -524,7 +530,8 @@ def _layered_plate():
 @pytest.mark.parametrize("case", sorted(_CAT_CASES))
 def test_design_categories_complex_step_matches_central_difference(case):
     """Every design-variable category the oracle restates (density, orientation, node
-    coordinates, layup zOffset, layer angle and layer density) against a central difference of
+    coordinates, layup zOffset, layer angle, layer density and the layer's elastic constants)
+    against a central difference of
     its real residual; 1e-5 relative (the complex path's single-precision Gauss points)."""
     build, step, dyn = _CAT_CASES[case]
 
