@@ -577,6 +577,9 @@ def _panels_eval(a):
     for _ in range(2):
         facTcs.append(g.panels_factor(best).factor_seconds)
     Xtc, _ = g.panels_solve(B)
+    # the same emulation on mma.sync (identical factor)
+    g.set_option(OPT_BAND_FP64_UPDATE, 2)
+    facMma = min(g.panels_factor(best).factor_seconds for _ in range(2))
     g.set_option(OPT_BAND_FP64_UPDATE, 1)
     g.panels_factor(best)
     facTc = min(facTcs)
@@ -589,6 +592,8 @@ def _panels_eval(a):
                      "complex-step design sensitivities)",
            "trailing_update": "FP64 (the tensor-core emulation measured beside it)",
            "tensor_core_update_factor_seconds": facTc, "tensor_core_rel_diff_vs_fp64_update": diffTc,
+           "tensor_core_update_kernel": "tcgen05 (BF16 slices, accumulators in tensor memory)",
+           "mma_sync_update_factor_seconds": facMma,
            "seconds": tot, "factor_seconds": fac, "solve_seconds": sol, "panels": int(info.num_panels),
            "elements": m.num_els, "dof": g.n, "max_bandwidth": info.max_bandwidth, "band_bytes": info.band_bytes,
            "cluster_size": best, "autotune_factor_seconds": tune, "workers": info.workers,

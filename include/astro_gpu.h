@@ -249,10 +249,9 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
 #define ASTRO_OPT_UNROLLED_CYCLES 2
 /* ASTRO_OPT_BAND_FP64_UPDATE (default 1): the band LDL^T of astro_panels_factor (and of
  * astro_newmark_cases) runs its trailing tile updates in FP64 arithmetic; 0 selects the
- * tensor-core emulation (BF16 slices of the Ozaki error-free splitting, summed exactly in FP32 per
- * level and combined in FP64; 56 bits relative to each row's largest entry).  On GB300 the
- * emulation measured slower than the FP64 update on the 512-panel batch, so it is kept for
- * comparison and measurement. */
+ * tensor-core emulation on tcgen05 (BF16 slices of the Ozaki error-free splitting, summed exactly
+ * in FP32 per level in tensor memory and combined in FP64; 56 bits relative to each row's largest
+ * entry), 2 the same emulation on mma.sync (identical results). */
 #define ASTRO_OPT_BAND_FP64_UPDATE 3
 /* The launch shapes astro_autotune picks, set directly (0 = the default): the zero-state brick
  * kernel's warps per CTA (1, 2, 4), the band factorisation's and the many-column band solve's

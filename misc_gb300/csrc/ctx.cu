@@ -1265,7 +1265,8 @@ extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
         return ASTRO_OK;
     }
     if (option == ASTRO_OPT_BAND_FP64_UPDATE) {
-        ctx->bandFp64Update = value ? 1 : 0;
+        if (value < 0 || value > 2) return set_err(ctx, ASTRO_ERR_ARG, "ASTRO_OPT_BAND_FP64_UPDATE: 0, 1 or 2");
+        ctx->bandFp64Update = value;
         return ASTRO_OK;
     }
     if (option == ASTRO_OPT_BRICK_WARPS || option == ASTRO_OPT_PANEL_CLUSTER || option == ASTRO_OPT_CASES_CLUSTER) {

@@ -149,6 +149,65 @@ __device__ __forceinline__ void mma_bf16(float d[4], const unsigned a[4], const 
 
 __device__ __forceinline__ unsigned ld_pair(const uint16_t *p) { return __ldcg(reinterpret_cast<const unsigned *>(p)); }
 
+// ---- tcgen05 (5th-generation tensor cores) for the emulated trailing update -----------------------
+// One work item is a group of 4 block rows d0 .. d0+3 of block column J against block row e: the
+// 128 x 32 product of the 7 slices of L D_J (rows) and of L (columns), every level
+// l = p + q in its own 32-column FP32 accumulator in tensor memory (7 x 32 = 224 of the CTA's 256
+// columns).  Operands sit in shared memory in the no-swizzle K-major core-matrix layout: element
+// (r, k) of a slice at ((r / 8) * 4 + k / 8) * 64 + (r % 8) * 8 + k % 8, i.e. 8-row x 16-byte core
+// matrices, 128 B apart along K and 512 B apart along the rows.
+constexpr int kTcRows = 4 * TB;                          // rows of the A operand (4 block rows)
+constexpr int kTcSliceA = kTcRows * TB;                  // bf16 elements per A slice
+constexpr int kTcSliceB = TB * TB;                       // bf16 elements per B slice
+constexpr int kTcSmem = kSlices * (kTcSliceA + kTcSliceB) * 2;  // bytes of dynamic shared memory
+constexpr int kTcCols = 256;                             // tensor-memory columns per CTA
+constexpr int kTcWaitLimit = 1 << 24;                    // polls of the MMA-completion barrier
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ int tc_cm(int r, int k) { return ((r >> 3) * (TB / 8) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7); }
+
+// shared-memory matrix descriptor: start, leading (K) and stride (row-group) byte offsets, no
+// swizzle, descriptor version 1
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr) {
+    return (uint64_t)((saddr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(512 >> 4) << 32) |
+           ((uint64_t)1 << 46);
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N = 32, M = 128
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TB >> 3) << 17) | ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t tmem, uint64_t da, uint64_t db, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(kTcIdesc), "r"(accumulate));
+}
+
+// 16 consecutive FP32 columns of this warp's 32 tensor-memory lanes
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// one block row's 7 slices (rows row0 .. row0+31 of the operand) from the global scratch (row-major
+// [p][r][k]) into the core-matrix layout; zeros when src is null.  16 bytes per thread and step.
+__device__ __forceinline__ void tc_stage(const uint16_t *src, uint16_t *dst, int sliceElems, int row0, int t) {
+    for (int x = t; x < kSlices * TB * (TB / 8); x += kThreads) {
+        const int p = x / (TB * (TB / 8)), r = (x / (TB / 8)) % TB, k8 = x % (TB / 8);
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (src) v = __ldcg(reinterpret_cast<const uint4 *>(src + (size_t)p * TT + r * TB + k8 * 8));
+        *reinterpret_cast<uint4 *>(dst + (size_t)p * sliceElems + tc_cm(row0 + r, k8 * 8)) = v;
+    }
+}
+
 // Slices of one tile of block column J (tile d, version v: 0 = L D_J, 1 = L) by one warp: lane r
 // takes row r, its power-of-two scale e_r (|row| / 2^e_r < 1) and kSlices 8-bit slices as BF16
 // integers, row-major [r][k] per slice.
@@ -181,15 +240,18 @@ __device__ void split_tile(const double *T, const double (*sL)[TB + 1], int v, u
     }
 }
 
-// Blocked band LDL^T, one cluster per panel (the cluster's panels listed in sched).  TC: the
-// trailing updates as the tensor-core emulation described at the top of the file, with the
-// slices of each worker (cluster) in slices + worker * sliceStride and their scales in
-// sexp + worker * expStride.
-template <bool TC>
+// Blocked band LDL^T, one cluster per panel (the cluster's panels listed in sched).  MODE 0: the
+// trailing updates in FP64; MODE 1 and 2: the tensor-core emulation described at the top of the
+// file, MODE 1 on mma.sync (16 x 8 blocks per warp), MODE 2 on tcgen05 (128 x 32 per MMA, the
+// accumulators in tensor memory), with the slices of each worker (cluster) in
+// slices + worker * sliceStride and their scales in sexp + worker * expStride.  Both emulations
+// sum every level exactly and combine the levels in the same order: identical results.
+template <int MODE>
 __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restrict__ meta, const int *__restrict__ sched,
                                                        const int *__restrict__ schedPtr, double *band, int *status,
                                                        uint16_t *slices, int *sexp, long long sliceStride,
                                                        int expStride) {
+    constexpr bool TC = MODE != 0;
     cg::cluster_group cl = cg::this_cluster();
     const int crank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
     const int worker = blockIdx.x / cs;
@@ -198,6 +260,23 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
     __shared__ double sL[TB][TB + 1];  // diagonal tile: L below the diagonal, D on it
     __shared__ double sA[TB][TB + 1], sB[TB][TB + 1];
     const int t = threadIdx.x;
+    // MODE 2: tensor memory, the completion barrier of the MMAs and the operand staging
+    extern __shared__ __align__(1024) uint16_t tcSmem[];
+    __shared__ __align__(8) unsigned long long tcBar;
+    __shared__ uint32_t tcBase;
+    uint32_t tcPhase = 0;
+    bool tcFailed = false;
+    if constexpr (MODE == 2) {
+        if (t < 32) {
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tcBase)),
+                         "r"(kTcCols));
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        }
+        if (t == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&tcBar)), "r"(1));
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    }
     for (int q = schedPtr[worker]; q < schedPtr[worker + 1]; ++q) {
         const int p = sched[q];
         const PanelMeta M = meta[p];
@@ -254,6 +333,105 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
                 }
                 __threadfence();
                 cl.sync();
+                if constexpr (MODE == 2) {
+                    // C. trailing update on tcgen05: items (group gi of block rows d0 .. d0+3, block
+                    // column e <= d0 + 3), round-robin over the cluster; a CTA keeps its A operand
+                    // while consecutive items share the group
+                    uint16_t *sAop = tcSmem, *sBop = tcSmem + kSlices * kTcSliceA;
+                    const int ng = (M.bt + 3) / 4;
+                    int nItems = 0;
+                    for (int gi = 0; gi < ng; ++gi) nItems += min(4 * gi + 4, M.bt);
+                    int curG = -1, gi = 0, gBase = 0;  // item index of group gi's first item
+                    const int w = t >> 5;
+                    for (int u = crank; u < nItems; u += cs) {
+                        while (u >= gBase + min(4 * gi + 4, M.bt)) {
+                            gBase += min(4 * gi + 4, M.bt);
+                            ++gi;
+                        }
+                        const int d0 = 1 + 4 * gi, e = 1 + (u - gBase);
+                        if (J + e >= M.nbc || tcFailed) continue;
+                        if (gi != curG) {
+                            for (int b = 0; b < 4; ++b) {
+                                const int d = d0 + b;
+                                const bool ok = d <= M.bt && J + d < M.nbc;
+                                tc_stage(ok ? wsl + (size_t)(2 * (d - 1)) * kSlices * TT : nullptr, sAop, kTcSliceA,
+                                         b * TB, t);
+                            }
+                            curG = gi;
+                        }
+                        tc_stage(wsl + (size_t)(2 * (e - 1) + 1) * kSlices * TT, sBop, kTcSliceB, 0, t);
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                        __syncthreads();
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        if (t == 0) {
+                            const uint32_t aBase = smem_addr(sAop), bBase = smem_addr(sBop);
+#pragma unroll 1
+                            for (int li = 0; li < kLevels; ++li) {  // level l = li + 2 = p + q
+                                uint32_t acc = 0;
+#pragma unroll 1
+                                for (int p = 1; p <= kSlices; ++p) {
+                                    const int q = li + 2 - p;
+                                    if (q < 1 || q > kSlices) continue;
+#pragma unroll
+                                    for (int kk = 0; kk < 2; ++kk) {
+                                        tc_mma(tcBase + li * TB, tc_desc(aBase + (p - 1) * kTcSliceA * 2 + kk * 256),
+                                               tc_desc(bBase + (q - 1) * kTcSliceB * 2 + kk * 256), acc);
+                                        acc = 1;
+                                    }
+                                }
+                            }
+                            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                             smem_addr(&tcBar))
+                                         : "memory");
+                        }
+                        uint32_t done = 0;
+                        for (int it = 0; it < kTcWaitLimit && !done; ++it)
+                            asm volatile(
+                                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                                " selp.u32 %0, 1, 0, p;\n}"
+                                : "=r"(done)
+                                : "r"(smem_addr(&tcBar)), "r"(tcPhase)
+                                : "memory");
+                        tcPhase ^= 1u;
+                        if (!done) {
+                            tcFailed = true;
+                            atomicCAS(status, 0, -1);
+                        }
+                        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                        // epilogue: warp w reads lanes 32 (w % 4) .. of block row d0 + w % 4 and
+                        // columns 16 (w / 4) ..; the levels combined in FP64 as in MODE 1
+                        const int d = d0 + (w & 3), c0 = 16 * (w >> 2);
+                        if (done && d <= M.bt && J + d < M.nbc && d >= e) {
+                            double sum[16];
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) sum[j] = 0.0;
+                            double sc = 1.0 / 65536.0;  // 2^(-8 l), l = 2 ..
+#pragma unroll 1
+                            for (int li = 0; li < kLevels; ++li) {
+                                float v[16];
+                                tc_ld16(tcBase + ((uint32_t)(32 * (w & 3)) << 16) + li * TB + c0, v);
+#pragma unroll
+                                for (int j = 0; j < 16; ++j) sum[j] += (double)v[j] * sc;
+                                sc *= 1.0 / 256.0;
+                            }
+                            double *Tt = band + tile_off(M, J + e, d - e);
+                            const int rr = lane;
+                            const int ea = __ldcg(wex + 2 * (d - 1) * TB + rr);
+                            const int *EB = wex + (2 * (e - 1) + 1) * TB;
+#pragma unroll
+                            for (int j = 0; j < 16; ++j) {
+                                double *pt = Tt + (c0 + j) * TB + rr;
+                                __stcg(pt, __ldcg(pt) - ldexp(sum[j], ea + __ldcg(EB + c0 + j)));
+                            }
+                        }
+                        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                        __syncthreads();
+                    }
+                    __threadfence();
+                    cl.sync();
+                    continue;
+                }
                 // C. trailing update, tensor cores: warp w computes the 16 x 8 block (mi, ni) of the
                 // 32 x 32 tile, every level l of the slice products in its own FP32 accumulator
                 const int w = t >> 5, g = lane >> 2, tg = lane & 3, mi = w >> 2, ni = w & 3;
@@ -351,6 +529,12 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
             __threadfence();
             cl.sync();
         }
+    }
+    if constexpr (MODE == 2) {
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (t < 32)
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tcBase), "r"(kTcCols));
     }
 }
 
@@ -851,7 +1035,10 @@ int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        if (cudaOccupancyMaxActiveClusters(&maxClusters, k_band_ldl<true>, &cfg) != cudaSuccess) {
+        // the tcgen05 variant holds the most shared memory (and tensor memory): size the workers by it
+        cudaFuncSetAttribute(k_band_ldl<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
+        cfg.dynamicSmemBytes = kTcSmem;
+        if (cudaOccupancyMaxActiveClusters(&maxClusters, k_band_ldl<2>, &cfg) != cudaSuccess) {
             cudaGetLastError();
             maxClusters = 0;
         }
@@ -982,16 +1169,23 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    if (ctx->bandFp64Update)
-        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<false>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+    if (ctx->bandFp64Update == 1) {
+        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<0>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
                               (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
                               dptr<double>(L->d_band), dptr<int>(L->d_status), (uint16_t *)nullptr, (int *)nullptr,
                               0LL, 0));
-    else
-        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<true>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+    } else if (ctx->bandFp64Update == 2) {
+        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<1>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
                               (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
                               dptr<double>(L->d_band), dptr<int>(L->d_status), dptr<uint16_t>(L->d_slices),
                               dptr<int>(L->d_sexp), L->sliceStride, L->expStride));
+    } else {
+        cfg.dynamicSmemBytes = kTcSmem;
+        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<2>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+                              (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
+                              dptr<double>(L->d_band), dptr<int>(L->d_status), dptr<uint16_t>(L->d_slices),
+                              dptr<int>(L->d_sexp), L->sliceStride, L->expStride));
+    }
     int status = 0;
     CK(cudaMemcpyAsync(&status, L->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
@@ -1001,6 +1195,8 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
     L->factored = status == 0;
     L->factorGen++;
     fill_info(*L, info);
+    if (status < 0)
+        return set_err(ctx, ASTRO_ERR_STATE, "panels: the tensor-core MMAs of the trailing update did not complete");
     if (status) return set_err(ctx, ASTRO_ERR_PIVOT, "panels: zero or non-finite pivot in panel " + std::to_string(status - 1));
     return ASTRO_OK;
 }

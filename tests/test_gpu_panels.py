@@ -175,19 +175,25 @@ def test_condensed_complex_step_batch(batch):
 def test_tensor_core_update_matches_fp64_update(batch):
     """The band factor's trailing updates on the tensor cores (FP64-exact BF16 slice emulation,
     an option) against the same factorisation with FP64 updates (the default): the two solutions
-    agree to 1e-10, and the emulated one matches the sparse direct solve as the FP64 one does."""
+    agree to 1e-10, and the emulated one matches the sparse direct solve as the FP64 one does.
+    The tcgen05 emulation (option value 0) and the mma.sync one (2) sum every level exactly and
+    combine the levels in the same order: their factors, hence their solutions, are identical."""
     from misc_gb300.astro import OPT_BAND_FP64_UPDATE
     m, g, o, A = batch
     B = np.random.default_rng(17).standard_normal((g.n, 9))
     Xr = spla.splu(A).solve(B)
-    g.set_option(OPT_BAND_FP64_UPDATE, 0)
     try:
+        g.set_option(OPT_BAND_FP64_UPDATE, 0)
         g.panels_factor(4)
         Xtc, _ = g.panels_solve(B)
+        g.set_option(OPT_BAND_FP64_UPDATE, 2)
+        g.panels_factor(4)
+        Xmma, _ = g.panels_solve(B)
     finally:
         g.set_option(OPT_BAND_FP64_UPDATE, 1)
     g.panels_factor(4)
     X64, _ = g.panels_solve(B)
     _check(A, X64, B, Xr)
     _check(A, Xtc, B, Xr)
+    assert np.array_equal(Xtc, Xmma)
     assert np.linalg.norm(Xtc - X64) <= 1e-10 * np.linalg.norm(X64)
