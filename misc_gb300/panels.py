@@ -62,3 +62,30 @@ def solve_batch(g: AstroGPU, m, n_dvars: int, cluster_size: int = 0, load_scale:
     t["info"] = info
     t["f"], t["R"], t["state"] = f, R, st
     return u, -dU, t
+
+
+def _main(argv=None):
+    """Factor a generated batch with the trailing-update variants in turn and print each factor
+    time (ASTRO_OPT_BAND_FP64_UPDATE: 1 FP64, 2 emulation on mma.sync, 0 emulation on tcgen05)."""
+    import argparse
+
+    from . import model as M
+    from .astro import OPT_BAND_FP64_UPDATE
+    p = argparse.ArgumentParser(description=_main.__doc__)
+    p.add_argument("--panels", type=int, default=64)
+    p.add_argument("--cluster", type=int, default=4, help="CTAs per cluster (2, 4, 8)")
+    p.add_argument("--updates", default="1,2,0", help="option values, in launch order")
+    a = p.parse_args(argv)
+    m = M.panel_batch(num_panels=a.panels)
+    g = AstroGPU(m)
+    g.getElasticSolnLoad(1, export=False)
+    g.scaleElasticMPC()
+    for mode in (int(x) for x in a.updates.split(",")):
+        g.set_option(OPT_BAND_FP64_UPDATE, mode)
+        info = g.panels_factor(a.cluster)
+        print(f"update {mode}: factor {info.factor_seconds:.4f} s, {info.workers} clusters of {info.cluster_size}",
+              flush=True)
+
+
+if __name__ == "__main__":
+    _main()
