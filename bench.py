@@ -894,6 +894,32 @@ def _widened_eval(a):
                             "nodes": m.num_nodes}
     del g
     gc.collect()
+    # config 1 (40x8 shell cantilever): the reference's skyline path through the C ABI with host
+    # buffers (convertToLTri from the device matrix, getSparseLDLFact, solveSparseLDLFact), and
+    # the factor of the device-resident profile
+    m1 = M.config1()
+    g1 = AstroGPU(m1)
+    g1.getElasticSolnLoad(1, export=False)
+    g1.scaleElasticMPC()
+    lt = g1.convertToLTri()
+    fac = g1.getSparseLDLFact(lt, g1.lt_range)
+    rhs = np.random.default_rng(5).standard_normal(g1.n)
+
+    def resident():  # the profile is factored in place: a fresh copy before each timed factor
+        g1.convertToLTri()
+        t0 = time.perf_counter()
+        g1._check(g1.L.astro_ldl_fact_resident(g1.h))
+        return time.perf_counter() - t0
+    out["config1_skyline"] = {
+        "workload": f"40x8 shell4 cantilever ({g1.n} DOF, profile {g1.lt_size} entries)",
+        "convert_to_ltri_s": best(g1.convertToLTri),
+        "ldl_fact_s": best(lambda: g1.getSparseLDLFact(lt, g1.lt_range)),
+        "ldl_fact_resident_s": min(resident() for _ in range(3)),
+        "ldl_solve_s": best(lambda: g1.solveSparseLDLFact(rhs, fac, g1.lt_range)),
+        "path": "one 512-thread CTA sweeping the profile's rows, as the reference's row-sequential algorithm; "
+                "host clock, host buffers copied in and out"}
+    del g1
+    gc.collect()
     return out
 
 

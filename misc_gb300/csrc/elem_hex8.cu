@@ -186,15 +186,11 @@ __global__ void __launch_bounds__(32 * FW, 28 / FW) hex8_fast_kernel(Hex8FastArg
     const unsigned long long first = A.elFirst[e];
     const int grp = lane / 9, qq = lane - 9 * grp;
     __syncwarp();
-    T ov[PREFETCH ? kRmwSteps : 1];
-    if (PREFETCH) {
-#pragma unroll
-        for (int st = 0; st < kRmwSteps; ++st) {
-            const int j = 3 * st + grp;
-            ov[st] = T(0);
-            if (A.K && grp < 3 && j < 64 && !((first >> j) & 1ull)) ov[st] = A.K[9 * (size_t)sBlk[w][j] + qq];
-        }
-    }
+    // colour launches chain by programmatic dependent launch: the next colour's CTAs may be
+    // scheduled now and compute their element blocks while this colour finishes; the blocks a
+    // colour reads and adds into are the previous colour's output, so it waits for that grid
+    // before its first read of K (a no-op without a programmatic edge)
+    asm volatile("griddepcontrol.launch_dependents;");
     // Jacobian at Gauss point gp = lane/4 from nodes 2s, 2s+1 (s = lane%4), from the node
     // coordinates in the section frame (single-precision parts of the double-float copy)
     {
@@ -265,6 +261,16 @@ __global__ void __launch_bounds__(32 * FW, 28 / FW) hex8_fast_kernel(Hex8FastArg
             for (int j = 0; j < 3; ++j) Or[i][j] = (T)A.orient[9 * (size_t)e + 3 * j + i];
         rotate_block<T>(Or, K0);
         rotate_block<T>(Or, K1);
+    }
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    T ov[PREFETCH ? kRmwSteps : 1];
+    if (PREFETCH) {
+#pragma unroll
+        for (int st = 0; st < kRmwSteps; ++st) {
+            const int j = 3 * st + grp;
+            ov[st] = T(0);
+            if (A.K && grp < 3 && j < 64 && !((first >> j) & 1ull)) ov[st] = A.K[9 * (size_t)sBlk[w][j] + qq];
+        }
     }
     if (A.K) {
 #pragma unroll
@@ -347,6 +353,7 @@ template <bool ROT> __global__ void __launch_bounds__(32 * kDfW, 4) hex8_df_kern
     sBlk[w][lane + 32] = A.elBlk[64 * (size_t)e + lane + 32];
     const unsigned long long first = A.elFirst[e];
     const int grp = lane / 9, qq = lane - 9 * grp;
+    asm volatile("griddepcontrol.launch_dependents;");  // chained colours, as in hex8_fast_kernel
     // Jacobian at Gauss point gp = lane/4 from nodes 2s, 2s+1 (s = lane%4)
     {
         const int gp = lane >> 2, s = lane & 3;
@@ -460,6 +467,7 @@ template <bool ROT> __global__ void __launch_bounds__(32 * kDfW, 4) hex8_df_kern
         rotate_block<double>(Or, K0);
         rotate_block<double>(Or, K1);
     }
+    asm volatile("griddepcontrol.wait;" ::: "memory");  // the previous colour's blocks are complete
     if (A.K) {
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
@@ -561,6 +569,7 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
     if (item >= A.count) return;
     GenSmem &S = sm[w];
     const int e = A.colorEls[item];
+    asm volatile("griddepcontrol.launch_dependents;");  // chained colours, as in hex8_fast_kernel
     if (BUILD) {
         S.blk[lane] = A.elBlk[64 * (size_t)e + lane];
         S.blk[lane + 32] = A.elBlk[64 * (size_t)e + lane + 32];
@@ -780,6 +789,8 @@ __global__ void __launch_bounds__(32 * kGenW) hex8_gen_kernel(Hex8GenArgs A) {
         for (int v = 0; v < 3; ++v)
 #pragma unroll
             for (int m = 4; m <= 16; m <<= 1) ru[k][v] = df_add(ru[k][v], df_shfl_xor(ru[k][v], m));
+    // the previous colour's load entries and blocks are complete before the first update
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     if (lane < 4) {
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
@@ -961,15 +972,33 @@ __global__ void k_elem_c(int E, const double *__restrict__ elMat, double *__rest
 
 }  // namespace
 
+// One colour launch; a colour after the first chains on its predecessor by programmatic dependent
+// launch (the kernels wait for it before their first read-modify-write).
+template <class Kern, class Args>
+static void colour_launch(Kern kernel, unsigned grid, unsigned block, cudaStream_t s, bool chained, const Args &A) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = chained ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, A);
+}
+
 template <class T, bool ROT, int FW> static void hex8_fast_launch(astro_ctx *ctx, const Hex8FastArgs<T> &A0) {
     Hex8FastArgs<T> A = A0;
     const std::vector<int> &ptr = ctx->c8Ptr;
+    bool chained = false;  // a colour after the first: programmatic dependent launch on its predecessor
     for (size_t col = 0; col + 1 < ptr.size(); ++col) {
         const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
         A.colorEls = dptr<int>(ctx->d_c8Els) + ptr[col];
         A.count = cnt;
-        hex8_fast_kernel<T, ROT, FW><<<(cnt + FW - 1) / FW, 32 * FW, 0, ctx->stream>>>(A);
+        colour_launch(hex8_fast_kernel<T, ROT, FW>, (cnt + FW - 1) / FW, 32 * FW, ctx->stream, chained, A);
+        chained = true;
     }
 }
 
@@ -1032,6 +1061,7 @@ static int hex8_gen_run(astro_ctx *ctx, const int *d_list, const std::vector<int
     A.gpcHi = g.hi;
     A.gpcLo = g.lo;
     const bool rot = !ctx->orientIdentity;
+    bool chained = false;
     for (size_t col = 0; col + 1 < ptr.size(); ++col) {
         const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
@@ -1041,15 +1071,16 @@ static int hex8_gen_run(astro_ctx *ctx, const int *d_list, const std::vector<int
         const unsigned grid = (cnt + kGenW - 1) / kGenW;
         if (build) {
             if (rot)
-                hex8_gen_kernel<true, true><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
+                colour_launch(hex8_gen_kernel<true, true>, grid, 32 * kGenW, ctx->stream, chained, A);
             else
-                hex8_gen_kernel<false, true><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
+                colour_launch(hex8_gen_kernel<false, true>, grid, 32 * kGenW, ctx->stream, chained, A);
         } else {
             if (rot)
-                hex8_gen_kernel<true, false><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
+                colour_launch(hex8_gen_kernel<true, false>, grid, 32 * kGenW, ctx->stream, chained, A);
             else
-                hex8_gen_kernel<false, false><<<grid, 32 * kGenW, 0, ctx->stream>>>(A);
+                colour_launch(hex8_gen_kernel<false, false>, grid, 32 * kGenW, ctx->stream, chained, A);
         }
+        chained = true;
     }
     return cuda_check(ctx, cudaGetLastError(), "brick8 general-state kernel launch");
 }
@@ -1065,6 +1096,7 @@ static int hex8_df_run(astro_ctx *ctx, double *K, double *d_ke, const int *d_lis
     A.orient = dptr<double>(ctx->d_secOrient);
     A.K = K;
     A.keOut = d_ke;
+    bool chained = false;
     for (size_t col = 0; col + 1 < ptr.size(); ++col) {
         const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
@@ -1072,9 +1104,10 @@ static int hex8_df_run(astro_ctx *ctx, double *K, double *d_ke, const int *d_lis
         A.count = cnt;
         const unsigned grid = (cnt + kDfW - 1) / kDfW;
         if (ctx->orientIdentity)
-            hex8_df_kernel<false><<<grid, 32 * kDfW, 0, ctx->stream>>>(A);
+            colour_launch(hex8_df_kernel<false>, grid, 32 * kDfW, ctx->stream, chained, A);
         else
-            hex8_df_kernel<true><<<grid, 32 * kDfW, 0, ctx->stream>>>(A);
+            colour_launch(hex8_df_kernel<true>, grid, 32 * kDfW, ctx->stream, chained, A);
+        chained = true;
     }
     return cuda_check(ctx, cudaGetLastError(), "brick8 FP64 zero-state kernel launch");
 }
