@@ -259,6 +259,12 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
 #define ASTRO_OPT_BRICK_WARPS 4
 #define ASTRO_OPT_PANEL_CLUSTER 5
 #define ASTRO_OPT_CASES_CLUSTER 6
+/* ASTRO_OPT_CASES_TWIST (default 1): the many-column band solve of astro_newmark_cases on a
+ * single panel runs twisted: the band split into a top and a reversed bottom half that meet in a
+ * window of bandwidth-many block rows, both halves swept at once towards the window and back, so
+ * the sequential chain is about half as long.  0: off; 1: when the panel has at least 8 windows
+ * of block rows; 2: whenever the split is possible (for tests on small models). */
+#define ASTRO_OPT_CASES_TWIST 7
 int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value);
 
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that order their own work

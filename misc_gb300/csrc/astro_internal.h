@@ -153,6 +153,7 @@ struct astro_ctx {
     // launch shapes picked by astro_autotune (0: the default)
     int tuneHex8Warps = 0;   // zero-state brick kernel: warps per CTA (1, 2, 4)
     int tuneCasesCluster = 0;  // many-column band solve: CTAs per cluster (2, 4, 8)
+    int casesTwist = 1;        // ASTRO_OPT_CASES_TWIST
     int tunePanelCluster = 0;  // band factorisation: CTAs per cluster (2, 4, 8)
 };
 
@@ -207,7 +208,10 @@ int precond_mlp_scales_f32(astro_ctx *ctx, const astro_precond_mlp *m, const dou
 int ensure_K(astro_ctx *ctx, int which);          // device BSR value arrays (ctx.cu)
 int ensure_io(astro_ctx *ctx, bool exportMat);    // host-vector staging buffers (ctx.cu)
 int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s);      // panels.cu
-int panels_cases_columns(astro_ctx *ctx);                                   // panels.cu
+int panels_cases_columns(astro_ctx *ctx);
+int panels_cases_launches(astro_ctx *ctx);                                   // panels.cu
+int panels_cases_would_twist(astro_ctx *ctx);                                // panels.cu
+int panels_factor_impl(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *info, int factor);  // panels.cu
 void panels_shape(astro_ctx *ctx, int *np, int *bw, long long *bandBytes, double *factorSeconds);
 void thermal_release(astro_ctx *ctx);                                        // thermal.cu
 int bsr_zero(astro_ctx *ctx, int which);                                    // assemble.cu

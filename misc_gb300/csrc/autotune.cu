@@ -133,7 +133,7 @@ extern "C" int astro_autotune(astro_ctx *ctx, int32_t what, const char *cache_pa
         const int cols = panels_cases_columns(ctx);
         if (!cols) return set_err(ctx, ASTRO_ERR_STATE, "autotune: no prepared many-column solve (astro_newmark_cases)");
         const std::string key = gpu + "/cases_cluster/n" + std::to_string(P.n) + "/bw" + std::to_string(bw) + "/cols" +
-                                std::to_string(cols);
+                                std::to_string(cols) + (panels_cases_launches(ctx) == 7 ? "/twisted" : "");
         int best = 0;
         if (!cache_find(cache_path, key, &best)) {
             DevBuf v;

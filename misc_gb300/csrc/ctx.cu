@@ -1264,6 +1264,11 @@ extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
         krylov_release(ctx);  // recapture the cycles in the chosen form
         return ASTRO_OK;
     }
+    if (option == ASTRO_OPT_CASES_TWIST) {
+        if (value < 0 || value > 2) return set_err(ctx, ASTRO_ERR_ARG, "ASTRO_OPT_CASES_TWIST: 0, 1 or 2");
+        ctx->casesTwist = value;
+        return ASTRO_OK;
+    }
     if (option == ASTRO_OPT_BAND_FP64_UPDATE) {
         if (value < 0 || value > 2) return set_err(ctx, ASTRO_ERR_ARG, "ASTRO_OPT_BAND_FP64_UPDATE: 0, 1 or 2");
         ctx->bandFp64Update = value;

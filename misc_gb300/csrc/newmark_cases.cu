@@ -181,8 +181,9 @@ int enqueue_step(astro_ctx *ctx, NmcBufs &B, int nc, int steps, double dt, doubl
                                                                B.hist.p ? dptr<double>(B.hist) : nullptr,
                                                                dptr<int>(B.step));
     k_nmc_tick<<<1, 1, 0, s>>>(dptr<int>(B.step));
-    // residual, move, solve, move, update, tick; each refinement: check, move, solve, move, sub
-    *launches = 6 + 5 * refine;
+    // residual, the solve's launches, update, tick; each refinement: check, the solve's, sub
+    const int pl = panels_cases_launches(ctx);
+    *launches = 3 + pl + (2 + pl) * refine;
     return cuda_check(ctx, cudaGetLastError(), "newmark cases step");
 }
 
@@ -255,8 +256,11 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
     ctx->ltFactored = 0;
     if ((rc = astro_scale_mpc(ctx, nullptr, nullptr))) return rc;
     if ((rc = constraint_load_dev(ctx, nullptr, dptr<double>(B.G)))) return rc;  // C^T rhs
+    // the plan (the autotuned cluster size, else 8); the whole band's factorisation unless the
+    // many-column solve runs twisted, which factors its own halves
     astro_panels_info pinfo{};
-    if ((rc = astro_panels_factor(ctx, 0, &pinfo))) return rc;  // the autotuned cluster size, else 8
+    if ((rc = panels_factor_impl(ctx, 0, &pinfo, 0))) return rc;
+    if (!panels_cases_would_twist(ctx) && (rc = astro_panels_factor(ctx, 0, &pinfo))) return rc;
     size_t dfBytes = 0;
     if ((rc = panels_cases_prepare(ctx, nc, &dfBytes))) return rc;
     if (o->autotune && !ctx->tuneCasesCluster && (rc = astro_autotune(ctx, ASTRO_TUNE_CASES_CLUSTER, nullptr, nullptr)))

@@ -67,7 +67,7 @@ struct PanelMeta {
     int n;            // DOF
     int nbc;          // block columns, ceil(n / 32)
     int bt;           // tiles below the diagonal tile in a block column
-    int pad;
+    int nfac;         // block columns the factorisation eliminates (nbc; fewer for a partial factor)
 };
 
 struct SolveItem {
@@ -94,6 +94,14 @@ struct PanelPlan {
     // generation dfGen; the items and the right-hand-side block for casesCols columns
     int factorGen = 0, dfGen = -1, casesCols = 0, ring = 0;
     DevBuf d_Lf, d_Lb, d_Wf, d_Wb, d_Dinv, d_items, d_X;
+    // twisted many-column solve of a single panel (twist_prepare): panels top (block rows
+    // 0 .. K+m-1), bottom (block rows K .. nbc-1, reversed) and window (the m block rows K ..)
+    int twist = 0, twK = 0, twM = 0, twGen = -1, twCols = 0;
+    long long twBandDoubles = 0, twRows = 0;
+    double twFactorSeconds = 0.0;
+    std::vector<PanelMeta> twMeta;
+    DevBuf d_twMeta, d_twBand, d_twAw, d_twSched, d_twSchedPtr, d_twStatus, d_twLf, d_twLb, d_twWf, d_twWb, d_twDinv,
+        d_twItems, d_twX;
 };
 
 __device__ __forceinline__ size_t tile_off(const PanelMeta &M, int J, int d) {
@@ -280,7 +288,7 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
     for (int q = schedPtr[worker]; q < schedPtr[worker + 1]; ++q) {
         const int p = sched[q];
         const PanelMeta M = meta[p];
-        for (int J = 0; J < M.nbc; ++J) {
+        for (int J = 0; J < M.nfac; ++J) {
             // A. the diagonal tile, factored by every CTA of the cluster into its shared memory
             double *Td = band + tile_off(M, J, 0);
             for (int e = t; e < TT; e += kThreads) sL[e % TB][e / TB] = __ldcg(Td + e);
@@ -668,6 +676,7 @@ constexpr int kPrepW = 4;  // warps per CTA of the band copy
 
 struct CaseItem {
     int panel, col;
+    int t0, t1;  // steps t0 .. t1-1 of the sweep (0 .. nbc-1 forward, nbc .. 2 nbc-1 backward)
 };
 
 // DF copies of the band: off-diagonal tiles as they are (Lf) and transposed (Lb); per block
@@ -687,6 +696,21 @@ __global__ void k_band_dfprep(const PanelMeta *__restrict__ meta, int np, const 
     if (p >= np) return;
     const PanelMeta M = meta[p];
     const int J = (int)gJ;
+    if (J >= M.nfac) {
+        // a block column the (partial) factorisation left: no elimination, W = I, D^-1 = 1
+        for (int d = 1; d <= M.bt && J + d < M.nbc; ++d) {
+            const size_t o = tile_off(M, J, d);
+            for (int e = lane; e < TT; e += 32) Lf[o + e] = Lb[o + e] = make_float2(0.f, 0.f);
+        }
+        const size_t ow = (size_t)M.xUnit * TB + (size_t)J * TT;
+        for (int i = 0; i < TB; ++i) {
+            const float2 v = make_float2(i == lane ? 1.f : 0.f, 0.f);
+            Wf[ow + (size_t)lane * TB + i] = v;
+            Wb[ow + (size_t)i * TB + lane] = v;
+        }
+        Dinv[(size_t)M.xUnit + (size_t)J * TB + lane] = make_float2(1.f, 0.f);
+        return;
+    }
     for (int d = 1; d <= M.bt; ++d) {
         if (J + d >= M.nbc) break;
         const size_t o = tile_off(M, J, d);
@@ -801,8 +825,9 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
     const int d0 = 2 + (rank - 1) * kCW + w;
     float2 pf[TB], pl[4], pw[4], pd = make_float2(0.f, 0.f);
     double pb = 0.0;
+    const int t0 = it.t0, t1 = it.t1;
     auto prefetch = [&](int t) {
-        if (t >= 2 * nbc) return;
+        if (t >= t1) return;
         const int dm = dmaxOf(t), I = rowOf(t);
         if (rank > 0) {
             if (d0 <= dm) {
@@ -825,8 +850,17 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
             }
         }
     };
-    prefetch(0);
-    for (int t = 0; t < 2 * nbc; ++t) {
+    // a backward sweep that starts below the last row (the rows after it solved already, in X):
+    // those rows into every CTA's ring
+    if (t0 > nbc) {
+        const int I0 = 2 * nbc - 1 - t0;
+        for (int R = I0 + 1 + w; R <= min(nbc - 1, I0 + bt); R += kCW) {
+            const DF v = df_from_double(Xp[(size_t)R * TB + r]);
+            sRing[(size_t)(R % ring) * TB + r] = make_float2(v.hi, v.lo);
+        }
+    }
+    prefetch(t0);
+    for (int t = t0; t < t1; ++t) {
         const int I = rowOf(t), dmax = dmaxOf(t), q = t < nbc ? t : t - nbc;
         __syncthreads();  // the leader's last row is in its ring
         if (rank > 0) {
@@ -905,7 +939,7 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
         }
         // the forward sweep's last rows are pushed before the backward sweep, and every row
         // before any CTA exits
-        if (t == nbc - 1 || t == 2 * nbc - 1) cluster_barrier();
+        if (t == nbc - 1 || t == t1 - 1) cluster_barrier();
     }
 }
 
@@ -922,6 +956,111 @@ __global__ void k_panel_move(int n, int dpn, int nrhs, double *__restrict__ vec,
         X[xi] = vec[t];
     else
         vec[t] = X[xi];
+}
+
+// ---- twisted many-column solve of one panel ----------------------------------------------------
+// The panel's band A (n DOF, nbc block rows, bt tiles below the diagonal) is split at block row K
+// into a top panel T = A[0 : K+m, 0 : K+m] and a bottom panel B = A[K : nbc, K : nbc] taken in
+// reversed order (band position ig -> rev - ig, padded with unit rows at its start), overlapping in the
+// window of m = bt block rows K .. K+m-1.  T and B are factored (LDL^T) up to the window only, so
+// their window tiles hold the Schur complements S_T and S_B of their outer parts; the window
+// matrix S = S_T + S_B - A_window (B's part reversed) is factored as a third panel.  A solve is
+// then: forward sweeps of T and B (the window's tiles zero and its W the identity, so the window
+// rows come out as c_T = b_w - L_wT y_T and c_B), c = c_T + c_B - b_w, S x_w = c, and backward
+// sweeps of T and B from the window outwards: two chains of about nbc / 2 block rows each way
+// instead of one of nbc (the twisted factorisation of a band, assembled from Schur complements).
+struct TwistGeom {
+    int n, dpn, K32, nT, nbB32;  // DOF, DOF per node, window start, top rows, bottom padded rows
+    int rev;                     // B's row of band position ig >= K32: rev - ig (rev = nbB32 + K32 - 1)
+};
+
+__device__ __forceinline__ double *tw_at(double *band, const PanelMeta &M, int row, int col) {  // row >= col
+    const int J = col / TB;
+    return band + tile_off(M, J, row / TB - J) + (col % TB) * TB + (row % TB);
+}
+
+// BSR entries of K (and, with penalty, the C^T C entries) into T and B
+__global__ void k_tw_fill(int nb, TwistGeom G, const int *__restrict__ bRow, const int *__restrict__ bCol,
+                          const double *__restrict__ K, const int *__restrict__ pos, const PanelMeta *__restrict__ meta,
+                          double *__restrict__ band) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const int bs = G.dpn * G.dpn;
+    if (t >= (long long)nb * bs) return;
+    const int b = (int)(t / bs), q = (int)(t % bs), a = q / G.dpn, c = q % G.dpn;
+    const int i = pos[bRow[b]] * G.dpn + a, j = pos[bCol[b]] * G.dpn + c;
+    if (j > i) return;
+    const double v = K[(size_t)b * bs + q];
+    if (i < G.nT) *tw_at(band, meta[0], i, j) = v;
+    if (j >= G.K32) *tw_at(band, meta[1], G.rev - j, G.rev - i) = v;
+}
+
+__global__ void k_tw_pen(int cnt, TwistGeom G, const int *__restrict__ pi, const int *__restrict__ pj,
+                         const double *__restrict__ pv, const int *__restrict__ pos, const PanelMeta *__restrict__ meta,
+                         double *__restrict__ band) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const int i = pos[pi[t] / G.dpn] * G.dpn + pi[t] % G.dpn, j = pos[pj[t] / G.dpn] * G.dpn + pj[t] % G.dpn;
+    if (j > i) return;
+    if (i < G.nT) *tw_at(band, meta[0], i, j) += pv[t];
+    if (j >= G.K32) *tw_at(band, meta[1], G.rev - j, G.rev - i) += pv[t];
+}
+
+// unit diagonal on B's leading padding rows
+__global__ void k_tw_pad(TwistGeom G, const PanelMeta *__restrict__ meta, double *__restrict__ band) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < G.nbB32 - (G.n - G.K32)) *tw_at(band, meta[1], i, i) = 1.0;
+}
+
+// the window of T before its factorisation (A_window) into Aw (window panel layout), or, with
+// assemble, S = S_T + S_B - A_window into the window panel: one thread per lower entry
+__global__ void k_tw_window(TwistGeom G, int w, const PanelMeta *__restrict__ meta, double *__restrict__ band,
+                            double *__restrict__ Aw, int assemble) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)w * w) return;
+    const int s1 = (int)(t / w), s2 = (int)(t % w);
+    if (s2 > s1) return;
+    PanelMeta Ma = meta[2];  // the window panel's tile layout, from the start of Aw
+    Ma.band = 0;
+    double *pa = tw_at(Aw, Ma, s1, s2);
+    const double vt = *tw_at(band, meta[0], G.K32 + s1, G.K32 + s2);
+    if (!assemble) {
+        *pa = vt;
+        return;
+    }
+    const double vb = *tw_at(band, meta[1], G.nbB32 - 1 - s2, G.nbB32 - 1 - s1);
+    *tw_at(band, meta[2], s1, s2) = vt + vb - *pa;
+}
+
+// internal-layout columns -> T, B and the window's b_w (mode 0); c_w = c_T + c_B - b_w (mode 1);
+// x_w -> T and B (mode 2); T, window, B -> internal layout (mode 3)
+__global__ void k_tw_move(int nc, TwistGeom G, int w, double *__restrict__ vec, const int *__restrict__ pos,
+                          const PanelMeta *__restrict__ meta, double *__restrict__ X, int mode) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const PanelMeta &T = meta[0], &B = meta[1], &S = meta[2];
+    const int len = (mode == 1 || mode == 2) ? w : G.n;
+    if (t >= (long long)len * nc) return;
+    const int c = (int)(t / len), i = (int)(t % len);
+    double *XT = X + (size_t)T.xUnit * nc + (size_t)c * T.nbc * TB;
+    double *XB = X + (size_t)B.xUnit * nc + (size_t)c * B.nbc * TB;
+    double *XS = X + (size_t)S.xUnit * nc + (size_t)c * S.nbc * TB;
+    if (mode == 1) {
+        XS[i] = XT[G.K32 + i] + XB[G.nbB32 - 1 - i] - XS[i];
+        return;
+    }
+    if (mode == 2) {
+        XT[G.K32 + i] = XS[i];
+        XB[G.nbB32 - 1 - i] = XS[i];
+        return;
+    }
+    const int ig = pos[i / G.dpn] * G.dpn + i % G.dpn;
+    double *v = vec + (size_t)c * G.n + i;
+    if (mode == 0) {
+        if (ig < G.nT) XT[ig] = *v;
+        if (ig >= G.K32) XB[G.rev - ig] = *v;
+        if (ig >= G.K32 && ig < G.nT) XS[ig - G.K32] = *v;
+    } else {
+        *v = ig < G.K32 ? XT[ig] : (ig < G.nT ? XS[ig - G.K32] : XB[G.rev - ig]);
+    }
 }
 
 constexpr size_t kSolveSmem = sizeof(double) * (kGroups * TB * (TB + 1) + kGroups * TB * (kSolveCols + 1));
@@ -1015,6 +1154,7 @@ int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
         M.bt = (bw + TB - 1) / TB;
         M.band = band;
         M.xUnit = xr;
+        M.nfac = M.nbc;
         band += (long long)M.nbc * (M.bt + 1) * TT;
         xr += (long long)M.nbc * TB;
         L.work[p] = (double)M.nbc * (0.5 * M.bt * (M.bt + 1) + 2.0);
@@ -1088,7 +1228,9 @@ void plan_free(PanelPlan *L) {
     DevBuf *b[] = {&L->d_meta,  &L->d_sched, &L->d_schedPtr, &L->d_panelOf, &L->d_pos,  &L->d_band,
                    &L->d_status, &L->d_penI, &L->d_penJ,     &L->d_penV,    &L->d_slices, &L->d_sexp,
                    &L->d_Lf,    &L->d_Lb,    &L->d_Wf,       &L->d_Wb,      &L->d_Dinv,  &L->d_items,
-                   &L->d_X};
+                   &L->d_X,     &L->d_twMeta, &L->d_twBand, &L->d_twAw,  &L->d_twSched, &L->d_twSchedPtr,
+                   &L->d_twStatus, &L->d_twLf, &L->d_twLb, &L->d_twWf, &L->d_twWb, &L->d_twDinv,
+                   &L->d_twItems, &L->d_twX};
     for (DevBuf *x : b) dev_free(*x);
 }
 
@@ -1112,7 +1254,10 @@ void panels_release(astro_ctx *ctx) {
     ctx->panels = nullptr;
 }
 
-extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *info) {
+// The plan (orderings, storage, schedule) and, with factor, the band LDL^T of every panel; without
+// it only the plan and the constraint terms, for a caller that factors in its own layout
+// (the twisted many-column solve).
+int panels_factor_impl(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *info, int factor) {
     if (!ctx) return ASTRO_ERR_ARG;
     if (cluster_size == 0) cluster_size = ctx->tunePanelCluster ? ctx->tunePanelCluster : 8;  // autotuned or 8
     if (cluster_size != 1 && cluster_size != 2 && cluster_size != 4 && cluster_size != 8)
@@ -1137,7 +1282,6 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
     const auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = ctx->stream;
     const AstroPrep &P = ctx->P;
-    if (!L->d_band.p && (rc = dev_alloc(ctx, L->d_band, sizeof(double) * (size_t)L->bandDoubles))) return rc;
     if (L->penVersion != ctx->penVersion) {
         L->penCount = (int)ctx->penI.size();
         if (L->penCount &&
@@ -1146,6 +1290,15 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
              (rc = upload(ctx, L->d_penV, ctx->penV.data(), sizeof(double) * L->penCount))))
             return rc;
     }
+    if (!factor) {
+        L->kVersion = ctx->k64Version;
+        L->penVersion = ctx->penVersion;
+        L->factored = 0;
+        L->factorGen++;
+        fill_info(*L, info);
+        return ASTRO_OK;
+    }
+    if (!L->d_band.p && (rc = dev_alloc(ctx, L->d_band, sizeof(double) * (size_t)L->bandDoubles))) return rc;
     CK(cudaMemsetAsync(L->d_band.p, 0, sizeof(double) * (size_t)L->bandDoubles, s));
     CK(cudaMemsetAsync(L->d_status.p, 0, sizeof(int), s));
     const long long fillN = (long long)P.nb * P.dpn * P.dpn;
@@ -1199,6 +1352,10 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
         return set_err(ctx, ASTRO_ERR_STATE, "panels: the tensor-core MMAs of the trailing update did not complete");
     if (status) return set_err(ctx, ASTRO_ERR_PIVOT, "panels: zero or non-finite pivot in panel " + std::to_string(status - 1));
     return ASTRO_OK;
+}
+
+extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *info) {
+    return panels_factor_impl(ctx, cluster_size, info, 1);
 }
 
 static int panels_solve_dev(astro_ctx *ctx, PanelPlan *L, int nrhs, double *d_vec, DevBuf &X) {
@@ -1293,13 +1450,41 @@ extern "C" int astro_panels_solve_batched(astro_ctx *ctx, int32_t num_rhs, const
 // Prepares k_band_solve_cases for ncols right-hand-side columns of the current factorisation:
 // the double-float band copies (once per factorisation), the (panel, column) items and the
 // panel-layout block.  Allocates; call before any stream capture.
+static int twist_prepare(astro_ctx *ctx, PanelPlan *L, int ncols);
+
+// Whether the many-column solve of the current plan runs twisted (ASTRO_OPT_CASES_TWIST: 0 off, 1
+// when the single panel has at least 8 windows of block rows, 2 whenever the split leaves rows
+// outside the window).
+static bool twist_wanted(const astro_ctx *ctx, const PanelPlan *L) {
+    if (!L || L->np != 1) return false;
+    const PanelMeta &M0 = L->meta[0];
+    const int m = std::max(1, M0.bt), K = (M0.nbc - m) / 2;
+    if (K < 1) return false;
+    return ctx->casesTwist == 2 || (ctx->casesTwist == 1 && M0.nbc >= 8 * (m + 1));
+}
+
+int panels_cases_would_twist(astro_ctx *ctx) { return twist_wanted(ctx, static_cast<PanelPlan *>(ctx->panels)); }
+
 int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
     PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
-    if (!L || !L->factored || L->kVersion != ctx->k64Version || L->penVersion != ctx->penVersion)
-        return set_err(ctx, ASTRO_ERR_STATE, "panels: no current factorisation (astro_panels_factor)");
     if (ncols < 1) return set_err(ctx, ASTRO_ERR_ARG, "panels: no right-hand sides");
+    if (!L || L->kVersion != ctx->k64Version || L->penVersion != ctx->penVersion)
+        return set_err(ctx, ASTRO_ERR_STATE, "panels: no current plan (astro_panels_factor)");
     cudaStream_t s = ctx->stream;
     int rc;
+    L->twist = twist_wanted(ctx, L);
+    L->ring = L->maxBt + 2;
+    const size_t smem = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * 8 * TB + TB);
+    if (L->twist) {
+        if ((L->twGen != L->factorGen || L->twCols != ncols) && (rc = twist_prepare(ctx, L, ncols))) return rc;
+        L->factorSeconds = L->twFactorSeconds;
+        CK(cudaFuncSetAttribute(k_band_solve_cases<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaFuncSetAttribute(k_band_solve_cases<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CK(cudaFuncSetAttribute(k_band_solve_cases<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (bytes) *bytes = 2 * sizeof(float2) * (size_t)L->twBandDoubles;
+        return cuda_check(ctx, cudaStreamSynchronize(s), "panels cases prepare");
+    }
+    if (!L->factored) return set_err(ctx, ASTRO_ERR_STATE, "panels: no current factorisation (astro_panels_factor)");
     if (L->dfGen != L->factorGen) {
         const size_t nb = (size_t)L->bandDoubles, nd = (size_t)L->xRows;
         if ((rc = dev_alloc(ctx, L->d_Lf, sizeof(float2) * nb)) || (rc = dev_alloc(ctx, L->d_Lb, sizeof(float2) * nb)) ||
@@ -1317,7 +1502,7 @@ int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
     if (L->casesCols != ncols) {
         std::vector<CaseItem> items;
         for (int p = 0; p < L->np; ++p)
-            for (int c = 0; c < ncols; ++c) items.push_back({p, c});
+            for (int c = 0; c < ncols; ++c) items.push_back({p, c, 0, 2 * L->meta[p].nbc});
         dev_free(L->d_items);
         dev_free(L->d_X);
         if ((rc = upload(ctx, L->d_items, items.data(), sizeof(CaseItem) * items.size())) ||
@@ -1326,8 +1511,6 @@ int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
         CK(cudaMemsetAsync(L->d_X.p, 0, sizeof(double) * (size_t)L->xRows * ncols, s));
         L->casesCols = ncols;
     }
-    L->ring = L->maxBt + 2;
-    const size_t smem = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * 8 * TB + TB);
     CK(cudaFuncSetAttribute(k_band_solve_cases<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_band_solve_cases<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CK(cudaFuncSetAttribute(k_band_solve_cases<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1335,19 +1518,185 @@ int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
     return cuda_check(ctx, cudaStreamSynchronize(s), "panels cases prepare");
 }
 
+// The twisted solve's structures for one panel (see k_tw_fill): the three panels, their fill
+// and partial factorisations (FP64 trailing updates), the window matrix and its factor, the
+// double-float copies, the items of the three cluster launches and the right-hand-side blocks.
+static int twist_prepare(astro_ctx *ctx, PanelPlan *L, int ncols) {
+    const AstroPrep &P = ctx->P;
+    cudaStream_t s = ctx->stream;
+    const PanelMeta M0 = L->meta[0];
+    const int nbc = M0.nbc, bt = M0.bt, m = std::max(1, bt), K = (nbc - m) / 2;
+    const int nbcT = K + m, nbcB = nbc - K;
+    L->twK = K;
+    L->twM = m;
+    std::vector<PanelMeta> mt(3);
+    long long band = 0, rows = 0;
+    auto put = [&](PanelMeta &M, int n, int nb, int b, int nfac) {
+        M.n = n;
+        M.nbc = nb;
+        M.bt = b;
+        M.nfac = nfac;
+        M.band = band;
+        M.xUnit = rows;
+        band += (long long)nb * (b + 1) * TT;
+        rows += (long long)nb * TB;
+    };
+    put(mt[0], nbcT * TB, nbcT, bt, K);
+    put(mt[1], nbcB * TB, nbcB, bt, nbcB - m);
+    put(mt[2], m * TB, m, m - 1, m);
+    L->twMeta = mt;
+    L->twBandDoubles = band;
+    L->twRows = rows;
+    TwistGeom G;
+    G.n = M0.n;
+    G.dpn = P.dpn;
+    G.K32 = K * TB;
+    G.nT = nbcT * TB;
+    G.nbB32 = nbcB * TB;
+    G.rev = G.nbB32 + G.K32 - 1;
+    const int w = m * TB;
+    int rc;
+    const int sched[3] = {0, 1, 2}, schedPtr[3] = {0, 1, 2}, schedPtrS[2] = {0, 1};
+    if ((rc = upload(ctx, L->d_twMeta, mt.data(), sizeof(PanelMeta) * 3)) ||
+        (rc = upload(ctx, L->d_twSched, sched, sizeof(sched))) ||
+        (rc = upload(ctx, L->d_twSchedPtr, schedPtr, sizeof(schedPtr))) ||
+        (rc = dev_alloc(ctx, L->d_twBand, sizeof(double) * (size_t)band)) ||
+        (rc = dev_alloc(ctx, L->d_twAw, sizeof(double) * (size_t)m * m * TT)) ||
+        (rc = dev_alloc(ctx, L->d_twStatus, sizeof(int))))
+        return rc;
+    DevBuf dSchedPtrS;
+    if ((rc = upload(ctx, dSchedPtrS, schedPtrS, sizeof(schedPtrS)))) return rc;
+    const auto t0 = std::chrono::steady_clock::now();
+    const PanelMeta *dm = dptr<PanelMeta>(L->d_twMeta);
+    double *db = dptr<double>(L->d_twBand);
+    CK(cudaMemsetAsync(L->d_twBand.p, 0, sizeof(double) * (size_t)band, s));
+    CK(cudaMemsetAsync(L->d_twAw.p, 0, sizeof(double) * (size_t)m * m * TT, s));
+    CK(cudaMemsetAsync(L->d_twStatus.p, 0, sizeof(int), s));
+    const long long fillN = (long long)P.nb * P.dpn * P.dpn;
+    k_tw_fill<<<(unsigned)((fillN + 255) / 256), 256, 0, s>>>(P.nb, G, dptr<int>(ctx->d_bRow), dptr<int>(ctx->d_bCol),
+                                                            dptr<double>(ctx->d_K64), dptr<int>(L->d_pos), dm, db);
+    if (L->penCount)
+        k_tw_pen<<<(L->penCount + 255) / 256, 256, 0, s>>>(L->penCount, G, dptr<int>(L->d_penI), dptr<int>(L->d_penJ),
+                                                           dptr<double>(L->d_penV), dptr<int>(L->d_pos), dm, db);
+    k_tw_pad<<<(G.nbB32 + 255) / 256, 256, 0, s>>>(G, dm, db);
+    const unsigned wg = (unsigned)(((long long)w * w + 255) / 256);
+    k_tw_window<<<wg, 256, 0, s>>>(G, w, dm, db, dptr<double>(L->d_twAw), 0);
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "twisted band fill"))) return rc;
+    // the partial factorisations of T and B (one cluster each), the window matrix, its factor
+    auto factor = [&](int workers, const int *schedBase, const int *schedP) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(workers * L->cs);
+        cfg.blockDim = dim3(kThreads);
+        cfg.stream = s;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = L->cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_band_ldl<0>, dm, schedBase, schedP, db,
+                                  dptr<int>(L->d_twStatus), (uint16_t *)nullptr, (int *)nullptr, 0LL, 0);
+    };
+    CK(factor(2, dptr<int>(L->d_twSched), dptr<int>(L->d_twSchedPtr)));
+    k_tw_window<<<wg, 256, 0, s>>>(G, w, dm, db, dptr<double>(L->d_twAw), 1);
+    // the window panel alone: its schedule is sched + 2 (panel 2) with schedPtr {0, 1}
+    CK(factor(1, dptr<int>(L->d_twSched) + 2, dptr<int>(dSchedPtrS)));
+    int status = 0;
+    CK(cudaMemcpyAsync(&status, L->d_twStatus.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    dev_free(dSchedPtrS);
+    if (status) return set_err(ctx, ASTRO_ERR_PIVOT, "panels: zero or non-finite pivot in the twisted factorisation");
+    L->twFactorSeconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    const size_t nd = (size_t)rows;
+    if ((rc = dev_alloc(ctx, L->d_twLf, sizeof(float2) * (size_t)band)) ||
+        (rc = dev_alloc(ctx, L->d_twLb, sizeof(float2) * (size_t)band)) ||
+        (rc = dev_alloc(ctx, L->d_twWf, sizeof(float2) * nd * TB)) ||
+        (rc = dev_alloc(ctx, L->d_twWb, sizeof(float2) * nd * TB)) ||
+        (rc = dev_alloc(ctx, L->d_twDinv, sizeof(float2) * nd)))
+        return rc;
+    const long long cols = (long long)nbcT + nbcB + m;
+    k_band_dfprep<<<(unsigned)((cols + kPrepW - 1) / kPrepW), kPrepW * 32, 0, s>>>(
+        dm, 3, db, dptr<float2>(L->d_twLf), dptr<float2>(L->d_twLb), dptr<float2>(L->d_twWf), dptr<float2>(L->d_twWb),
+        dptr<float2>(L->d_twDinv));
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "twisted double-float copy"))) return rc;
+    // items: forward T and B, the window, backward T and B (from the row before the window)
+    std::vector<CaseItem> items;
+    for (int c = 0; c < ncols; ++c) {
+        items.push_back({0, c, 0, nbcT});
+        items.push_back({1, c, 0, nbcB});
+    }
+    for (int c = 0; c < ncols; ++c) items.push_back({2, c, 0, 2 * m});
+    for (int c = 0; c < ncols; ++c) {
+        items.push_back({0, c, nbcT + m, 2 * nbcT});
+        items.push_back({1, c, nbcB + m, 2 * nbcB});
+    }
+    dev_free(L->d_twX);
+    if ((rc = upload(ctx, L->d_twItems, items.data(), sizeof(CaseItem) * items.size())) ||
+        (rc = dev_alloc(ctx, L->d_twX, sizeof(double) * nd * ncols)))
+        return rc;
+    CK(cudaMemsetAsync(L->d_twX.p, 0, sizeof(double) * nd * ncols, s));
+    L->twCols = ncols;
+    L->twGen = L->factorGen;
+    return cuda_check(ctx, cudaStreamSynchronize(s), "twisted prepare");
+}
+
 // x = (K + C^T C)^-1 b for the prepared number of columns, in place in d_vec (ncols x n, internal
 // numbering): moves, one cluster launch, moves.  No allocation, no synchronisation (capturable).
 int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s) {
     PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
-    if (!L || L->dfGen != L->factorGen || !L->casesCols) return set_err(ctx, ASTRO_ERR_STATE, "panels: cases not prepared");
+    if (!L || (L->twist ? (L->twGen != L->factorGen || !L->twCols) : (L->dfGen != L->factorGen || !L->casesCols)))
+        return set_err(ctx, ASTRO_ERR_STATE, "panels: cases not prepared");
     const AstroPrep &P = ctx->P;
-    const int nc = L->casesCols;
+    const int nc = L->twist ? L->twCols : L->casesCols;
     const long long mv = (long long)P.n * nc;
     const unsigned mg = (unsigned)((mv + 255) / 256);
-    k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nc, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
-                                    dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_X), 1);
     // CTAs per case: the autotuned choice of this context (astro_autotune), else 4
     const int cs = (ctx->tuneCasesCluster == 2 || ctx->tuneCasesCluster == 8) ? ctx->tuneCasesCluster : 4;
+    if (L->twist) {
+        // move in, forward sweeps of T and B, window right-hand side, window solve, window
+        // solution to T and B, backward sweeps, move out
+        const PanelMeta *dm = dptr<PanelMeta>(L->d_twMeta);
+        TwistGeom G;
+        G.n = P.n;
+        G.dpn = P.dpn;
+        G.K32 = L->twK * TB;
+        G.nT = L->twMeta[0].nbc * TB;
+        G.nbB32 = L->twMeta[1].nbc * TB;
+        G.rev = G.nbB32 + G.K32 - 1;
+        const int w = L->twM * TB;
+        double *X = dptr<double>(L->d_twX);
+        const unsigned wgm = (unsigned)(((long long)w * nc + 255) / 256);
+        auto sweep = [&](int first, int count) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)(count * cs));
+            cfg.blockDim = dim3(kCW * 32);
+            cfg.dynamicSmemBytes = sizeof(float2) * ((size_t)L->ring * TB + kCW * TB + 2 * cs * TB + TB);
+            cfg.stream = s;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = cs;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            auto kern = cs == 2 ? k_band_solve_cases<2> : (cs == 8 ? k_band_solve_cases<8> : k_band_solve_cases<4>);
+            return cudaLaunchKernelEx(&cfg, kern, dm, (const CaseItem *)dptr<CaseItem>(L->d_twItems) + first,
+                                      (const float2 *)dptr<float2>(L->d_twLf), (const float2 *)dptr<float2>(L->d_twLb),
+                                      (const float2 *)dptr<float2>(L->d_twWf), (const float2 *)dptr<float2>(L->d_twWb),
+                                      (const float2 *)dptr<float2>(L->d_twDinv), X, nc, L->ring);
+        };
+        k_tw_move<<<mg, 256, 0, s>>>(nc, G, w, d_vec, dptr<int>(L->d_pos), dm, X, 0);
+        CK(sweep(0, 2 * nc));
+        k_tw_move<<<wgm, 256, 0, s>>>(nc, G, w, d_vec, dptr<int>(L->d_pos), dm, X, 1);
+        CK(sweep(2 * nc, nc));
+        k_tw_move<<<wgm, 256, 0, s>>>(nc, G, w, d_vec, dptr<int>(L->d_pos), dm, X, 2);
+        CK(sweep(3 * nc, 2 * nc));
+        k_tw_move<<<mg, 256, 0, s>>>(nc, G, w, d_vec, dptr<int>(L->d_pos), dm, X, 3);
+        return cuda_check(ctx, cudaGetLastError(), "panels twisted cases solve");
+    }
+    k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nc, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
+                                    dptr<PanelMeta>(L->d_meta), dptr<double>(L->d_X), 1);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(L->np * nc * cs));
     cfg.blockDim = dim3(kCW * 32);
@@ -1371,9 +1720,16 @@ int panels_cases_solve(astro_ctx *ctx, double *d_vec, cudaStream_t s) {
     return cuda_check(ctx, cudaGetLastError(), "panels cases solve");
 }
 
+// Kernel launches of one panels_cases_solve (3, or 7 for the twisted solve).
+int panels_cases_launches(astro_ctx *ctx) {
+    PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    return (L && L->twist) ? 7 : 3;
+}
+
 // Columns of the prepared many-column solve of the current factorisation (0: none prepared).
 int panels_cases_columns(astro_ctx *ctx) {
     PanelPlan *L = static_cast<PanelPlan *>(ctx->panels);
+    if (L && L->twist) return L->twGen == L->factorGen ? L->twCols : 0;
     return (L && L->factored && L->dfGen == L->factorGen) ? L->casesCols : 0;
 }
 
@@ -1383,6 +1739,6 @@ void panels_shape(astro_ctx *ctx, int *np, int *bw, long long *bandBytes, double
     if (!L) return;
     if (np) *np = L->np;
     if (bw) *bw = L->maxBw;
-    if (bandBytes) *bandBytes = L->bandDoubles * (long long)sizeof(double);
+    if (bandBytes) *bandBytes = (L->twist ? L->twBandDoubles : L->bandDoubles) * (long long)sizeof(double);
     if (factorSeconds) *factorSeconds = L->factorSeconds;
 }

@@ -116,6 +116,26 @@ def test_shell_cases_match_oracle_linear_loop(shell):
     assert info.last_rel_residual < 1e-10 and info.graph_nodes >= 6
 
 
+def test_twisted_solve_matches_oracle(shell):
+    """The twisted many-column solve (top and reversed bottom halves meeting in a window, forced
+    on this small plate) and the plain one against the oracle's batched loop, 1e-9 each."""
+    from misc_gb300.astro import OPT_CASES_TWIST
+    from newmark_cases_ref import newmark_cases
+    nx, m, o = shell
+    _quirk(1)
+    centre = (nx // 2) * (nx + 1) + nx // 2 + 1
+    P, A = _cases(o, [(centre, 2), (centre + 2, 2), (centre - nx, 0)], 10, 1e-5, 5)
+    A *= 100.0
+    Ho, *_ = newmark_cases(o, P, A, 1e-5, 0.25, 0.5, 10)
+    for twist, kernels in ((2, 10), (0, 6)):
+        g = AstroGPU(m)
+        g.set_option(OPT_SHELL_MEAN_ROT_TERM, 1)
+        g.set_option(OPT_CASES_TWIST, twist)
+        u, v, a, H, info = g.newmark_cases(1e-5, P, A, history=True)
+        _check(H, Ho, 1e-9)
+        assert info.kernels_per_step == kernels and info.last_rel_residual < 1e-10, twist
+
+
 def test_shell_cases_near_element_loop(shell):
     """The centre-load case against the reference's loop with the consistent shell tangent."""
     from newmark_ref import newmark_states
