@@ -171,7 +171,7 @@ __device__ __forceinline__ void pair_moments(const GradSmem<float> &S, int a0, i
     }
 }
 template <class T, bool ROT, int FW>
-__global__ void __launch_bounds__(32 * FW, 28 / FW) hex8_fast_kernel(Hex8FastArgs<T> A) {
+__global__ void __launch_bounds__(32 * FW, 32 / FW) hex8_fast_kernel(Hex8FastArgs<T> A) {
     constexpr bool PREFETCH = FastCfg<T>::PREFETCH;
     __shared__ GradSmem<T> sG[FW];
     __shared__ T sK[FW][64 * 9];  // element blocks, block j = 8a + b at 9j (row-major 3x3)
