@@ -341,7 +341,7 @@ __device__ __forceinline__ void df_ortho(const DF c[9], const DF M[9], DF K[9]) 
 }
 
 // 4 CTAs per SM: 128 registers, no spills (3 CTAs let ptxas take 167 and ran 11 % slower)
-template <bool ROT> __global__ void __launch_bounds__(32 * kDfW, 4) hex8_df_kernel(Hex8DfArgs A) {
+template <bool ROT> __global__ void __launch_bounds__(32 * kDfW, 6) hex8_df_kernel(Hex8DfArgs A) {
     __shared__ DfGrad sG[kDfW];
     __shared__ double sK[kDfW][64 * 9];
     __shared__ int sBlk[kDfW][64];
