@@ -29,75 +29,122 @@
 #include <vector>
 
 #include "astro_internal.h"
+#include "dfloat.cuh"
 
 namespace {
 
 // residual of every case, thread per (block row, case); R in internal numbering, case-major
+// r = amp p + C^T rhs - K (u - w) - K_eff w - C^T C u for every case: one warp per block row,
+// lane = case (32 cases per pass), so the row's blocks of K and K_eff are read once for all
+// cases (the lanes load the same entry: a broadcast) and only the vectors differ per lane; the
+// products in double-float on the FP32 pipe from double-float copies of the matrices and of
+// u - w and w.
 template <int DPN>
 __global__ void k_nmc_residual(int N, int nc, int steps, const int *__restrict__ bRowPtr, const int *__restrict__ bCol,
-                               const double *__restrict__ Kst, const double *__restrict__ Keff,
+                               const float2 *__restrict__ KstF, const float2 *__restrict__ KeffF,
                                const int *__restrict__ penPtr, const int *__restrict__ penRow,
                                const int *__restrict__ penCol, const double *__restrict__ penVal,
-                               const double *__restrict__ U, const double *__restrict__ V,
-                               const double *__restrict__ A, const double *__restrict__ P,
+                               const double *__restrict__ U, const float2 *__restrict__ UW,
+                               const float2 *__restrict__ WW, const double *__restrict__ P,
                                const double *__restrict__ amp, const int *__restrict__ dStep,
-                               const double *__restrict__ G, double dt, double c2, double beta,
-                               double *__restrict__ R) {
-    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (t >= (long long)N * nc) return;
-    const int r = (int)(t % N), c = (int)(t / N);
-    const size_t n = (size_t)N * DPN, base = (size_t)c * n;
+                               const double *__restrict__ G, double *__restrict__ R) {
+    const long long gw = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (gw >= N) return;
+    const int r = (int)gw;
+    const size_t n = (size_t)N * DPN;
     const int step = *dStep;
-    const double a = amp[(size_t)c * steps + step];
-    const double *Uc = U + base, *Vc = V + base, *Ac = A + base;
-    const double q = (1.0 - 2.0 * beta) / c2;
-    double y[DPN];
+    const int b0 = bRowPtr[r], b1 = bRowPtr[r + 1];
+    for (int c0 = 0; c0 < nc; c0 += 32) {
+        const int c = c0 + lane;
+        const bool on = c < nc;
+        const size_t base = (size_t)(on ? c : 0) * n;
+        const float2 *uwc = UW + base, *wc = WW + base;
+        DF y[DPN];
 #pragma unroll
-    for (int i = 0; i < DPN; ++i) y[i] = 0.0;
-    for (int b = bRowPtr[r]; b < bRowPtr[r + 1]; ++b) {
-        const int col = bCol[b];
-        double uw[DPN], wv[DPN];
+        for (int i = 0; i < DPN; ++i) y[i] = DF{0.f, 0.f};
+        for (int b = b0; b < b1; ++b) {
+            const int col = bCol[b];
+            float2 uw[DPN], wv[DPN];
 #pragma unroll
-        for (int j = 0; j < DPN; ++j) {
-            const size_t k = (size_t)col * DPN + j;
-            const double w = -(dt * Vc[k] + q * Ac[k]);
-            wv[j] = w;
-            uw[j] = Uc[k] - w;
+            for (int j = 0; j < DPN; ++j) {
+                uw[j] = uwc[(size_t)col * DPN + j];
+                wv[j] = wc[(size_t)col * DPN + j];
+            }
+            const float2 *ks = KstF + (size_t)b * DPN * DPN, *ke = KeffF + (size_t)b * DPN * DPN;
+#pragma unroll
+            for (int i = 0; i < DPN; ++i) {
+#pragma unroll
+                for (int j = 0; j < DPN; ++j) {
+                    const float2 kv = ks[i * DPN + j], ev = ke[i * DPN + j];
+                    df_acc(y[i], kv.x, kv.y, uw[j].x, uw[j].y);
+                    df_acc(y[i], ev.x, ev.y, wv[j].x, wv[j].y);
+                }
+                y[i] = df_norm(y[i]);
+            }
         }
-        const double *ks = Kst + (size_t)b * DPN * DPN, *ke = Keff + (size_t)b * DPN * DPN;
+        if (!on) continue;
+        const double a = amp[(size_t)c * steps + step];
+        const double *Uc = U + base;
+        double yp[DPN];
 #pragma unroll
-        for (int i = 0; i < DPN; ++i)
+        for (int i = 0; i < DPN; ++i) yp[i] = df_to_double(y[i]);
+        if (penPtr)
+            for (int p = penPtr[r]; p < penPtr[r + 1]; ++p) {
+                const double v = penVal[p] * Uc[penCol[p]];
+                const int i = penRow[p];
 #pragma unroll
-            for (int j = 0; j < DPN; ++j) y[i] += ks[i * DPN + j] * uw[j] + ke[i * DPN + j] * wv[j];
-    }
-    if (penPtr)
-        for (int p = penPtr[r]; p < penPtr[r + 1]; ++p) {
-            const double v = penVal[p] * Uc[penCol[p]];
-            const int i = penRow[p];
+                for (int k = 0; k < DPN; ++k) yp[k] += (k == i) ? v : 0.0;
+            }
 #pragma unroll
-            for (int k = 0; k < DPN; ++k) y[k] += (k == i) ? v : 0.0;
+        for (int i = 0; i < DPN; ++i) {
+            const size_t k = (size_t)r * DPN + i;
+            R[base + k] = a * P[base + k] + G[k] - yp[i];
         }
-#pragma unroll
-    for (int i = 0; i < DPN; ++i) {
-        const size_t k = (size_t)r * DPN + i;
-        R[base + k] = a * P[base + k] + G[k] - y[i];
     }
+}
+
+// double-float copies of a matrix's values
+__global__ void k_nmc_df(long long cnt, const double *__restrict__ v, float2 *__restrict__ out) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= cnt) return;
+    const DF d = df_from_double(v[t]);
+    out[t] = make_float2(d.hi, d.lo);
+}
+
+// u - w and w (w = -(dt v + (1 - 2 beta) a / c2), the predictor's correction) in double-float for
+// the next residual
+__device__ __forceinline__ void nmc_uw(double u, double v, double a, double dt, double q, float2 *uw, float2 *ww) {
+    const double w = -(dt * v + q * a);
+    const DF dw = df_from_double(w), duw = df_from_double(u - w);
+    *uw = make_float2(duw.hi, duw.lo);
+    *ww = make_float2(dw.hi, dw.lo);
+}
+
+__global__ void k_nmc_uw(long long total, double dt, double q, const double *__restrict__ U,
+                         const double *__restrict__ V, const double *__restrict__ A, float2 *__restrict__ UW,
+                         float2 *__restrict__ WW) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t < total) nmc_uw(U[t], V[t], A[t], dt, q, UW + t, WW + t);
 }
 
 // u += du, then the reference's update (AStrO_commandFunctions.f90:796-799) with the previous
 // values the current ones; the step's displacement into the history when there is one
 __global__ void k_nmc_update(long long total, double c1, double c2, double dt, double beta, double gamma,
                              double *__restrict__ U, double *__restrict__ V, double *__restrict__ A,
-                             const double *__restrict__ D, double *__restrict__ hist, const int *__restrict__ dStep) {
+                             const double *__restrict__ D, double *__restrict__ hist, const int *__restrict__ dStep,
+                             float2 *__restrict__ UW, float2 *__restrict__ WW) {
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= total) return;
     const double du = D[t], vp = V[t], ap = A[t];
     const double u = U[t] + du;
     const double an = c1 * (c2 * (du - dt * vp) - (1.0 - 2.0 * beta) * ap);
-    V[t] = vp + dt * ((1.0 - gamma) * ap + gamma * an);
+    const double vn = vp + dt * ((1.0 - gamma) * ap + gamma * an);
+    V[t] = vn;
     A[t] = an;
     U[t] = u;
     if (hist) hist[(size_t)(*dStep) * total + t] = u;
+    nmc_uw(u, vn, an, dt, (1.0 - 2.0 * beta) / c2, UW + t, WW + t);
 }
 
 __global__ void k_nmc_tick(int *dStep) { *dStep += 1; }
@@ -144,9 +191,9 @@ __global__ void k_nmc_check(int N, int nc, const int *__restrict__ bRowPtr, cons
 }
 
 struct NmcBufs {
-    DevBuf U, V, A, P, amp, R, D, G, hist, Kst, zero, step, E;
+    DevBuf U, V, A, P, amp, R, D, G, hist, Kst, zero, step, E, KstF, KeffF, UW, WW;
     ~NmcBufs() {
-        DevBuf *b[] = {&U, &V, &A, &P, &amp, &R, &D, &G, &hist, &Kst, &zero, &step, &E};
+        DevBuf *b[] = {&U, &V, &A, &P, &amp, &R, &D, &G, &hist, &Kst, &zero, &step, &E, &KstF, &KeffF, &UW, &WW};
         for (auto *x : b) dev_free(*x);
     }
 };
@@ -159,11 +206,11 @@ int enqueue_step(astro_ctx *ctx, NmcBufs &B, int nc, int steps, double dt, doubl
     const double c1 = 0.5 / beta, c2 = 2.0 / (dt * dt);
     const long long rows = (long long)N * nc, tot = (long long)n * nc;
     const int *penPtr = ctx->penRows ? dptr<int>(ctx->d_penPtr) : nullptr;
-    k_nmc_residual<DPN><<<(unsigned)((rows + 127) / 128), 128, 0, s>>>(
-        N, nc, steps, dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), dptr<double>(B.Kst), dptr<double>(ctx->d_K64),
+    k_nmc_residual<DPN><<<(unsigned)((N + 3) / 4), 128, 0, s>>>(
+        N, nc, steps, dptr<int>(ctx->d_bRowPtr), dptr<int>(ctx->d_bCol), dptr<float2>(B.KstF), dptr<float2>(B.KeffF),
         penPtr, dptr<int>(ctx->d_penRow), dptr<int>(ctx->d_penCol), dptr<double>(ctx->d_penVal), dptr<double>(B.U),
-        dptr<double>(B.V), dptr<double>(B.A), dptr<double>(B.P), dptr<double>(B.amp), dptr<int>(B.step),
-        dptr<double>(B.G), dt, c2, beta, dptr<double>(B.R));
+        dptr<float2>(B.UW), dptr<float2>(B.WW), dptr<double>(B.P), dptr<double>(B.amp), dptr<int>(B.step),
+        dptr<double>(B.G), dptr<double>(B.R));
     CK(cudaMemcpyAsync(B.D.p, B.R.p, sizeof(double) * (size_t)tot, cudaMemcpyDeviceToDevice, s));
     int rc = panels_cases_solve(ctx, dptr<double>(B.D), s);
     if (rc) return rc;
@@ -179,7 +226,8 @@ int enqueue_step(astro_ctx *ctx, NmcBufs &B, int nc, int steps, double dt, doubl
     k_nmc_update<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(tot, c1, c2, dt, beta, gamma, dptr<double>(B.U),
                                                                dptr<double>(B.V), dptr<double>(B.A), dptr<double>(B.D),
                                                                B.hist.p ? dptr<double>(B.hist) : nullptr,
-                                                               dptr<int>(B.step));
+                                                               dptr<int>(B.step), dptr<float2>(B.UW),
+                                                               dptr<float2>(B.WW));
     k_nmc_tick<<<1, 1, 0, s>>>(dptr<int>(B.step));
     // residual, the solve's launches, update, tick; each refinement: check, the solve's, sub
     const int pl = panels_cases_launches(ctx);
@@ -249,6 +297,21 @@ extern "C" int astro_newmark_cases(astro_ctx *ctx, const astro_newmark_cases_opt
     ds.dynamic = 1;
     if ((rc = elem_soln_load_dev(ctx, ds, nullptr, nullptr, 1, true))) return rc;
     dev_free(izero);
+    // double-float copies of K and K_eff, and u - w and w of the initial state, for the residual
+    {
+        const long long kv = (long long)P.nb * P.dpn * P.dpn, tot = (long long)cn;
+        if ((rc = dev_alloc(ctx, B.KstF, sizeof(float2) * (size_t)kv)) ||
+            (rc = dev_alloc(ctx, B.KeffF, sizeof(float2) * (size_t)kv)) ||
+            (rc = dev_alloc(ctx, B.UW, sizeof(float2) * cn)) || (rc = dev_alloc(ctx, B.WW, sizeof(float2) * cn)))
+            return rc;
+        k_nmc_df<<<(unsigned)((kv + 255) / 256), 256, 0, s>>>(kv, dptr<double>(B.Kst), dptr<float2>(B.KstF));
+        k_nmc_df<<<(unsigned)((kv + 255) / 256), 256, 0, s>>>(kv, dptr<double>(ctx->d_K64), dptr<float2>(B.KeffF));
+        const double c2 = 2.0 / (o->del_t * o->del_t);
+        k_nmc_uw<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(tot, o->del_t, (1.0 - 2.0 * o->nm_beta) / c2,
+                                                               dptr<double>(B.U), dptr<double>(B.V), dptr<double>(B.A),
+                                                               dptr<float2>(B.UW), dptr<float2>(B.WW));
+        if ((rc = cuda_check(ctx, cudaGetLastError(), "newmark cases double-float copies"))) return rc;
+    }
     ctx->haveK64 = 1;
     ctx->k64Version++;
     ctx->haveIntMat = P.intVecSize > 0;
