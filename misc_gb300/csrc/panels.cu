@@ -1175,10 +1175,12 @@ int plan_build(astro_ctx *ctx, PanelPlan &L, int cs) {
         at[0].val.clusterDim.z = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        // the tcgen05 variant holds the most shared memory (and tensor memory): size the workers by it
+        // workers as resident clusters of the variants without dynamic shared memory (FP64 and
+        // mma.sync updates); the tcgen05 variant's shared memory fits two CTAs per SM, so its
+        // surplus clusters wait for the resident ones (and at most two CTAs per SM hold tensor
+        // memory: the allocation never waits)
         cudaFuncSetAttribute(k_band_ldl<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem);
-        cfg.dynamicSmemBytes = kTcSmem;
-        if (cudaOccupancyMaxActiveClusters(&maxClusters, k_band_ldl<2>, &cfg) != cudaSuccess) {
+        if (cudaOccupancyMaxActiveClusters(&maxClusters, k_band_ldl<1>, &cfg) != cudaSuccess) {
             cudaGetLastError();
             maxClusters = 0;
         }
