@@ -134,6 +134,7 @@ struct astro_ctx {
     // persistent buffers of the getElasticSolnLoad boundary: load vector in both numberings,
     // exported CSR values and column numbers
     DevBuf d_ioRef, d_ioInt, d_exMat, d_exCols;
+    DevBuf d_sky[5];  // grow-only scratch of the host-buffer skyline entry points
     // scratch
     DevBuf d_scratch;
     DevBuf d_status;  // int status words written by kernels

@@ -90,6 +90,7 @@ static void free_all(astro_ctx *c) {
                       &c->d_guard, &c->d_c8Els, &c->d_c81Els, &c->d_intVecOff, &c->d_intMatOff, &c->d_elRho,
                       &c->d_secOrig, &c->d_n2dR, &c->d_n2d, &c->d_n2c, &c->d_dComp};
     for (DevBuf *b : bufs) dev_free(*b);
+    for (DevBuf &b : c->d_sky) dev_free(b);
 }
 
 // internal (rank-major) index of reference DOF d (1-based)

@@ -335,39 +335,50 @@ extern "C" int astro_convert_to_ltri(astro_ctx *ctx, double *l_tri) {
     return ASTRO_OK;
 }
 
+// b at least bytes long (grown, never shrunk: the buffers outlive the call)
+static int sky_scratch(astro_ctx *ctx, DevBuf &b, size_t bytes) {
+    return b.bytes >= bytes ? ASTRO_OK : dev_alloc(ctx, b, bytes);
+}
+
+// Threads of the row-sweeping factor and solve: the later rows a row updates (the profile's
+// longest row, maxBW) are split over the threads, so a CTA wider than that only adds barrier
+// cost: one warp up to 32, then multiples of 32 up to 512.
+static int sky_threads(int maxBW) { return std::min(kT, std::max(32, (maxBW + 31) / 32 * 32)); }
+
 static int ldl_fact_dev(astro_ctx *ctx, double *d_A, const int *d_R, const int *h_R, int n) {
     const int maxBW = skyline_maxbw(h_R, n);
-    DevBuf diag, dl;
+    DevBuf &diag = ctx->d_sky[3], &dl = ctx->d_sky[4];
     int rc;
-    if ((rc = dev_alloc(ctx, diag, sizeof(double) * (size_t)(n + 1)))) return rc;
-    if ((rc = dev_alloc(ctx, dl, sizeof(double) * (size_t)(maxBW + 2)))) return rc;
+    if ((rc = sky_scratch(ctx, diag, sizeof(double) * (size_t)(n + 1))) ||
+        (rc = sky_scratch(ctx, dl, sizeof(double) * (size_t)(maxBW + 2))))
+        return rc;
     int *st = dptr<int>(ctx->d_status);
     CK(cudaMemsetAsync(st, 0, sizeof(int), ctx->stream));
-    k_ldl_fact<<<1, kT, 0, ctx->stream>>>(d_A, d_R, n, maxBW, dptr<double>(diag), dptr<double>(dl), st);
+    k_ldl_fact<<<1, sky_threads(maxBW), 0, ctx->stream>>>(d_A, d_R, n, maxBW, dptr<double>(diag), dptr<double>(dl),
+                                                         st);
     CK(cudaGetLastError());
     int hs = 0;
     CK(cudaMemcpyAsync(&hs, st, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    dev_free(diag);
-    dev_free(dl);
     if (hs) return set_err(ctx, ASTRO_ERR_PIVOT, "zero or non-finite pivot in row " + std::to_string(hs));
     return ASTRO_OK;
 }
 
 extern "C" int astro_ldl_fact(astro_ctx *ctx, double *a_l_tri, int32_t a_size, const int32_t *a_range, int32_t n) {
     if (!ctx || !a_l_tri || !a_range || n <= 0 || a_size < a_range[n]) return ASTRO_ERR_ARG;
-    DevBuf dA, dR;
+    DevBuf &dA = ctx->d_sky[0], &dR = ctx->d_sky[1];
     int rc;
-    if ((rc = upload(ctx, dA, a_l_tri, sizeof(double) * (size_t)a_size))) return rc;
-    if ((rc = upload(ctx, dR, a_range, sizeof(int) * (size_t)(n + 1)))) return rc;
+    if ((rc = sky_scratch(ctx, dA, sizeof(double) * (size_t)a_size)) ||
+        (rc = sky_scratch(ctx, dR, sizeof(int) * (size_t)(n + 1))))
+        return rc;
+    CK(cudaMemcpyAsync(dA.p, a_l_tri, sizeof(double) * (size_t)a_size, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dR.p, a_range, sizeof(int) * (size_t)(n + 1), cudaMemcpyHostToDevice, ctx->stream));
     rc = ldl_fact_dev(ctx, dptr<double>(dA), dptr<int>(dR), a_range, n);
     if (rc == ASTRO_OK || rc == ASTRO_ERR_PIVOT) {
         cudaError_t e = cudaMemcpyAsync(a_l_tri, dA.p, sizeof(double) * (size_t)a_size, cudaMemcpyDeviceToHost, ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) rc = cuda_check(ctx, e, "ldl_fact download");
     }
-    dev_free(dA);
-    dev_free(dR);
     return rc;
 }
 
@@ -383,21 +394,23 @@ extern "C" int astro_ldl_solve(astro_ctx *ctx, double *soln, const double *rhs, 
                                const int32_t *l_range, int32_t l_dim, double *z_vec) {
     if (!ctx || !soln || !rhs || !l_mat || !l_range || l_dim <= 0 || l_size < l_range[l_dim]) return ASTRO_ERR_ARG;
     const int maxBW = skyline_maxbw(l_range, l_dim) - 1;
-    DevBuf dL, dR, dx, db, dz;
+    DevBuf &dL = ctx->d_sky[0], &dR = ctx->d_sky[1], &db = ctx->d_sky[2], &dx = ctx->d_sky[3], &dz = ctx->d_sky[4];
     int rc;
-    if ((rc = upload(ctx, dL, l_mat, sizeof(double) * (size_t)l_size))) return rc;
-    if ((rc = upload(ctx, dR, l_range, sizeof(int) * (size_t)(l_dim + 1)))) return rc;
-    if ((rc = upload(ctx, db, rhs, sizeof(double) * (size_t)l_dim))) return rc;
-    if ((rc = dev_alloc(ctx, dx, sizeof(double) * (size_t)l_dim))) return rc;
-    if ((rc = dev_alloc(ctx, dz, sizeof(double) * (size_t)l_dim))) return rc;
-    k_ldl_solve<<<1, kT, 0, ctx->stream>>>(dptr<double>(dx), dptr<double>(db), dptr<double>(dL), dptr<int>(dR), l_dim,
-                                           maxBW, dptr<double>(dz));
+    if ((rc = sky_scratch(ctx, dL, sizeof(double) * (size_t)l_size)) ||
+        (rc = sky_scratch(ctx, dR, sizeof(int) * (size_t)(l_dim + 1))) ||
+        (rc = sky_scratch(ctx, db, sizeof(double) * (size_t)l_dim)) ||
+        (rc = sky_scratch(ctx, dx, sizeof(double) * (size_t)l_dim)) ||
+        (rc = sky_scratch(ctx, dz, sizeof(double) * (size_t)l_dim)))
+        return rc;
+    CK(cudaMemcpyAsync(dL.p, l_mat, sizeof(double) * (size_t)l_size, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(dR.p, l_range, sizeof(int) * (size_t)(l_dim + 1), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(db.p, rhs, sizeof(double) * (size_t)l_dim, cudaMemcpyHostToDevice, ctx->stream));
+    k_ldl_solve<<<1, sky_threads(maxBW), 0, ctx->stream>>>(dptr<double>(dx), dptr<double>(db), dptr<double>(dL),
+                                                          dptr<int>(dR), l_dim, maxBW, dptr<double>(dz));
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(soln, dx.p, sizeof(double) * (size_t)l_dim, cudaMemcpyDeviceToHost, ctx->stream));
     if (z_vec) CK(cudaMemcpyAsync(z_vec, dz.p, sizeof(double) * (size_t)l_dim, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    DevBuf *b[] = {&dL, &dR, &dx, &db, &dz};
-    for (auto *p : b) dev_free(*p);
     return ASTRO_OK;
 }
 
