@@ -559,6 +559,35 @@ def _panels_eval(a):
     reps.sort()
     tot, fac, sol = reps[1]
     r = g.apply_operator(X[:, 0], 64) - B[:, 0]
+    # the solve's other sweep modes on the same factor: FP64 sweeps, double-float sweeps alone
+    from misc_gb300.astro import OPT_PANELS_SOLVE
+    sweeps = {}
+    for mode, name in ((1, "fp64"), (2, "double_float_alone")):
+        g.set_option(OPT_PANELS_SOLVE, mode)
+        Xm, sm = g.panels_solve(B)
+        rm = g.apply_operator(Xm[:, 0], 64) - B[:, 0]
+        sweeps[name] = {"solve_seconds": sm.solve_seconds,
+                        "rel_diff_vs_default": float(np.linalg.norm(Xm - X) / np.linalg.norm(X)),
+                        "rel_residual_u": float(np.linalg.norm(rm) / np.linalg.norm(B[:, 0]))}
+        del Xm
+    g.set_option(OPT_PANELS_SOLVE, 0)
+    # the same unit with the double-float trailing update (a 48-bit factor; the default solve
+    # refines against the FP64 operator)
+    from misc_gb300.astro import OPT_BAND_FP64_UPDATE
+    g.set_option(OPT_BAND_FP64_UPDATE, 3)
+    reps3 = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        info3 = g.panels_factor(best)
+        X3, si3 = g.panels_solve(B)
+        reps3.append((time.perf_counter() - t0, info3.factor_seconds, si3.solve_seconds))
+    g.set_option(OPT_BAND_FP64_UPDATE, 1)
+    reps3.sort()
+    r3 = g.apply_operator(X3[:, 0], 64) - B[:, 0]
+    df_update = {"seconds": reps3[1][0], "factor_seconds": reps3[1][1], "solve_seconds": reps3[1][2],
+                 "rel_residual_u": float(np.linalg.norm(r3) / np.linalg.norm(B[:, 0])),
+                 "rel_diff_vs_fp64_update": float(np.linalg.norm(X3 - X) / np.linalg.norm(X))}
+    del X3
     # FP64 multiply-adds of the tile algorithm (32^3 per trailing tile update, the diagonal and
     # panel tiles) and of the two sweeps per right-hand side
     fma_f, fma_s = 0.0, 0.0
@@ -594,7 +623,9 @@ def _panels_eval(a):
            "tensor_core_update_factor_seconds": facTc, "tensor_core_rel_diff_vs_fp64_update": diffTc,
            "tensor_core_update_kernel": "tcgen05 (BF16 slices, accumulators in tensor memory)",
            "mma_sync_update_factor_seconds": facMma,
-           "seconds": tot, "factor_seconds": fac, "solve_seconds": sol, "panels": int(info.num_panels),
+           "seconds": tot, "factor_seconds": fac, "solve_seconds": sol,
+           "solve_sweeps": "double-float sweeps from copies of the FP64 factor + one FP64 refinement pass",
+           "solve_other_sweeps": sweeps, "double_float_update": df_update, "panels": int(info.num_panels),
            "elements": m.num_els, "dof": g.n, "max_bandwidth": info.max_bandwidth, "band_bytes": info.band_bytes,
            "cluster_size": best, "autotune_factor_seconds": tune, "workers": info.workers,
            "rel_residual_u": float(np.linalg.norm(r) / np.linalg.norm(B[:, 0])),

@@ -251,7 +251,10 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
  * astro_newmark_cases) runs its trailing tile updates in FP64 arithmetic; 0 selects the
  * tensor-core emulation on tcgen05 (BF16 slices of the Ozaki error-free splitting, summed exactly
  * in FP32 per level in tensor memory and combined in FP64; 56 bits relative to each row's largest
- * entry), 2 the same emulation on mma.sync (identical results). */
+ * entry), 2 the same emulation on mma.sync (identical results), 3 the updates in double-float
+ * arithmetic on the FP32 pipe (about 48 significant bits; the operand tiles converted once per
+ * block column, the products subtracted from the FP64 band in FP64): a factor of lower precision
+ * for solves that refine against the FP64 operator (astro_panels_solve's default mode). */
 #define ASTRO_OPT_BAND_FP64_UPDATE 3
 /* The launch shapes astro_autotune picks, set directly (0 = the default): the zero-state brick
  * kernel's warps per CTA (1, 2, 4), the band factorisation's and the many-column band solve's
@@ -265,6 +268,13 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
  * the sequential chain is about half as long.  0: off; 1: when the panel has at least 8 windows
  * of block rows; 2: whenever the split is possible (for tests on small models). */
 #define ASTRO_OPT_CASES_TWIST 7
+/* ASTRO_OPT_PANELS_SOLVE (default 0): astro_panels_solve runs its forward and backward sweeps in
+ * double-float arithmetic on the FP32 pipe (about 48 significant bits per operation) from
+ * double-float copies of the FP64 factor, made once per factorisation, then one refinement pass:
+ * the residual b - A x with the FP64 operator (K and the scaled constraints) and a second
+ * double-float solve added to x.  1: the sweeps in FP64 from the factor itself (no copies, half
+ * the device memory); 2: the double-float sweeps without the refinement pass. */
+#define ASTRO_OPT_PANELS_SOLVE 8
 int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value);
 
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that order their own work

@@ -27,6 +27,7 @@ SOLVER_FGMRES_LEARNED = 2
 OPT_BAND_FP64_UPDATE = 3
 OPT_BRICK_WARPS, OPT_PANEL_CLUSTER, OPT_CASES_CLUSTER = 4, 5, 6
 OPT_CASES_TWIST = 7
+OPT_PANELS_SOLVE = 8
 
 _LIB = None
 

@@ -61,6 +61,8 @@ struct AstroPrep {
     std::vector<double> mpcMat, mpcRhs;
 };
 
+struct HostStage;  // hostcopy.cu: page-locked staging of large pageable copies
+
 struct astro_ctx {
     std::string err;
     // workspaces of the static solvers (FP64, mixed, learned), kept with their restart-cycle graphs
@@ -134,6 +136,7 @@ struct astro_ctx {
     // persistent buffers of the getElasticSolnLoad boundary: load vector in both numberings,
     // exported CSR values and column numbers
     DevBuf d_ioRef, d_ioInt, d_exMat, d_exCols;
+    HostStage *stage = nullptr;
     DevBuf d_sky[5];  // grow-only scratch of the host-buffer skyline entry points
     // scratch
     DevBuf d_scratch;
@@ -155,6 +158,7 @@ struct astro_ctx {
     int tuneHex8Warps = 0;   // zero-state brick kernel: warps per CTA (1, 2, 4)
     int tuneCasesCluster = 0;  // many-column band solve: CTAs per cluster (2, 4, 8)
     int casesTwist = 1;        // ASTRO_OPT_CASES_TWIST
+    int panelsSolve = 0;       // ASTRO_OPT_PANELS_SOLVE
     int tunePanelCluster = 0;  // band factorisation: CTAs per cluster (2, 4, 8)
 };
 
@@ -221,6 +225,11 @@ double bsr_absmax(astro_ctx *ctx, int *status, int kind);                   // a
 int constraint_load_dev(astro_ctx *ctx, const double *d_u, double *d_loadInt);  // assemble.cu
 int ref_to_int_vec(astro_ctx *ctx, const double *d_ref, double *d_int, int n); // assemble.cu
 int int_to_ref_vec(astro_ctx *ctx, const double *d_int, double *d_ref, int n); // assemble.cu
+// hostcopy.cu: large pageable copies through page-locked staging, complete on return
+int copy_to_device(astro_ctx *ctx, void *dst, const void *src, size_t bytes, const char *what);
+int copy_to_host(astro_ctx *ctx, void *dst, const void *src, size_t bytes, const char *what);
+void host_stage_release(astro_ctx *ctx);
+int krylov_residual64(astro_ctx *ctx, const double *d_x, const double *d_b, double *d_r);  // krylov.cu
 int surface_load_dev(astro_ctx *ctx, int nf, const int *d_faceEl, const int *d_faceNum, const double *tr,
                      double pressure, double *d_loadInt);                   // assemble.cu
 // Solid elements (brick8 and brickIM), colour by colour, at state s: load -= Ru into d_loadInt

@@ -72,6 +72,7 @@ int upload(astro_ctx *c, DevBuf &b, const void *h, size_t bytes) {
 }
 
 static void free_all(astro_ctx *c) {
+    host_stage_release(c);
     krylov_release(c);
     panels_release(c);
     thermal_release(c);
@@ -1270,8 +1271,13 @@ extern "C" int astro_set_option(astro_ctx *ctx, int32_t option, int32_t value) {
         ctx->casesTwist = value;
         return ASTRO_OK;
     }
+    if (option == ASTRO_OPT_PANELS_SOLVE) {
+        if (value < 0 || value > 2) return set_err(ctx, ASTRO_ERR_ARG, "ASTRO_OPT_PANELS_SOLVE: 0, 1 or 2");
+        ctx->panelsSolve = value;
+        return ASTRO_OK;
+    }
     if (option == ASTRO_OPT_BAND_FP64_UPDATE) {
-        if (value < 0 || value > 2) return set_err(ctx, ASTRO_ERR_ARG, "ASTRO_OPT_BAND_FP64_UPDATE: 0, 1 or 2");
+        if (value < 0 || value > 3) return set_err(ctx, ASTRO_ERR_ARG, "ASTRO_OPT_BAND_FP64_UPDATE: 0 .. 3");
         ctx->bandFp64Update = value;
         return ASTRO_OK;
     }

@@ -1511,6 +1511,21 @@ int krylov_apply(astro_ctx *ctx, int kind, const double *d_x, double *d_y) {
     return rc;
 }
 
+// r = b - A x with A the FP64 operator (K64 and the scaled constraints), device vectors in the
+// solver ordering; r may alias b.
+int krylov_residual64(astro_ctx *ctx, const double *d_x, const double *d_b, double *d_r) {
+    GmresWork W;
+    W.n = ctx->P.n;
+    W.nRowCtas = (ctx->P.N + kThreads - 1) / kThreads;
+    int rc = dev_alloc(ctx, W.part, sizeof(double) * 2 * W.nRowCtas);
+    if (rc) return rc;
+    double rel;
+    if (ctx->P.dpn == 3) rc = true_residual<3>(ctx, W, 64, d_x, d_b, &rel, d_r);
+    else rc = true_residual<6>(ctx, W, 64, d_x, d_b, &rel, d_r);
+    dev_free(W.part);
+    return rc;
+}
+
 // ---- implicit Newmark time stepping (solve, dynamic branch) --------------------------------------
 
 namespace {

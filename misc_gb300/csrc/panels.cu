@@ -94,6 +94,9 @@ struct PanelPlan {
     // generation dfGen; the items and the right-hand-side block for casesCols columns
     int factorGen = 0, dfGen = -1, casesCols = 0, ring = 0;
     DevBuf d_Lf, d_Lb, d_Wf, d_Wb, d_Dinv, d_items, d_X;
+    // astro_panels_solve's work buffers (grow-only): right-hand sides in both orderings, the
+    // refinement's residuals, the panel-layout block and the items
+    DevBuf d_sRef, d_sVec, d_sRes, d_sBi, d_sX, d_sItems;
     // twisted many-column solve of a single panel (twist_prepare): panels top (block rows
     // 0 .. K+m-1), bottom (block rows K .. nbc-1, reversed) and window (the m block rows K ..)
     int twist = 0, twK = 0, twM = 0, twGen = -1, twCols = 0;
@@ -259,11 +262,11 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
                                                        const int *__restrict__ schedPtr, double *band, int *status,
                                                        uint16_t *slices, int *sexp, long long sliceStride,
                                                        int expStride) {
-    constexpr bool TC = MODE != 0;
+    constexpr bool TC = MODE == 1 || MODE == 2;
     cg::cluster_group cl = cg::this_cluster();
     const int crank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
     const int worker = blockIdx.x / cs;
-    uint16_t *wsl = TC ? slices + (size_t)worker * sliceStride : nullptr;
+    uint16_t *wsl = MODE != 0 ? slices + (size_t)worker * sliceStride : nullptr;
     int *wex = TC ? sexp + (size_t)worker * expStride : nullptr;
     __shared__ double sL[TB][TB + 1];  // diagonal tile: L below the diagonal, D on it
     __shared__ double sA[TB][TB + 1], sB[TB][TB + 1];
@@ -331,7 +334,7 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
             if (crank == 0)
                 for (int e = t; e < TT; e += kThreads) __stcg(Td + e, sL[e % TB][e / TB]);
             const int nt = M.bt * (M.bt + 1) / 2;
-            if (TC) {
+            if constexpr (TC) {
                 // B2. slices of the tiles below the diagonal (versions L D_J and L), one warp each
                 const int lane = t & 31, wg = crank * kGroups + (t >> 5);
                 for (int uu = wg; uu < 2 * M.bt; uu += cs * kGroups) {
@@ -502,6 +505,60 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
                 cl.sync();
                 continue;
             }
+            if constexpr (MODE == 3) {
+                // B2. double-float copies of the tiles below the diagonal, L D_J (v = 0) and L
+                // (v = 1), in the worker's scratch: tile (d, v) at wdf + (2 (d-1) + v) TT
+                float2 *wdf = reinterpret_cast<float2 *>(wsl);
+                for (int x = crank * kThreads + t; x < 2 * M.bt * TT; x += cs * kThreads) {
+                    const int uu = x / TT, d = 1 + uu / 2, v = uu % 2, el = x % TT;
+                    if (J + d >= M.nbc) continue;
+                    double a = __ldcg(band + tile_off(M, J, d) + el);
+                    if (v == 0) a *= sL[el / TB][el / TB];
+                    const DF f = df_from_double(a);
+                    __stcg(wdf + x, make_float2(f.hi, f.lo));
+                }
+                __threadfence();
+                cl.sync();
+                // C. trailing update in double-float on the FP32 pipe, the result subtracted in FP64
+                float2(*fA)[TB + 1] = reinterpret_cast<float2(*)[TB + 1]>(sA);
+                float2(*fB)[TB + 1] = reinterpret_cast<float2(*)[TB + 1]>(sB);
+                for (int u = crank; u < nt; u += cs) {
+                    int d = 1, rem = u;
+                    while (rem >= d) {
+                        rem -= d;
+                        ++d;
+                    }
+                    const int e = 1 + rem;
+                    if (J + d >= M.nbc) continue;
+                    const float2 *Ad = wdf + (size_t)(2 * (d - 1)) * TT, *Be = wdf + (size_t)(2 * (e - 1) + 1) * TT;
+                    __syncthreads();
+                    for (int x = t; x < TT; x += kThreads) {
+                        fA[x % TB][x / TB] = __ldcg(Ad + x);
+                        fB[x % TB][x / TB] = __ldcg(Be + x);
+                    }
+                    __syncthreads();
+                    const int r = t % TB, c0 = (t / TB) * 4;
+                    DF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 8
+                    for (int k = 0; k < TB; ++k) {
+                        const float2 a = fA[r][k];
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) {
+                            const float2 b = fB[c0 + cc][k];
+                            df_acc(acc[cc], a.x, a.y, b.x, b.y);
+                        }
+                    }
+                    double *Tt = band + tile_off(M, J + e, d - e);
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        double *pt = Tt + (c0 + cc) * TB + r;
+                        __stcg(pt, __ldcg(pt) - df_to_double(df_norm(acc[cc])));
+                    }
+                }
+                __threadfence();
+                cl.sync();
+                continue;
+            }
             // C. trailing update of the band: tile (J+e, d-e) -= L_{J+d,J} D_J L_{J+e,J}^T, 1 <= e <= d
             for (int u = crank; u < nt; u += cs) {
                 int d = 1, rem = u;
@@ -652,6 +709,120 @@ __global__ void __launch_bounds__(kThreads) k_band_solve(const PanelMeta *__rest
     }
 }
 
+// The sweeps of k_band_solve in double-float on the FP32 pipe, from the copies k_band_dfprep makes
+// of the factor (off-diagonal tiles as stored, Lf, and transposed, Lb; W = L_JJ^-1 column-major,
+// Wf, and row-major, Wb; D^-1).  The warps split a block row's off-diagonal tiles as in
+// k_band_solve; the diagonal step is the product with W (one warp per right-hand side) instead of
+// a 32-step substitution.  The solved block rows stay in a shared-memory ring of `ring` >= bt + 1
+// rows; the forward sweep leaves y in X as (hi, lo) float pairs, which the backward sweep
+// overwrites with the FP64 value of the solution.  Items have 1 .. kSolveCols columns (a
+// template instantiation each).
+template <int NC>
+__device__ __forceinline__ void band_solve_df_item(const PanelMeta &M, const float2 *__restrict__ Lf,
+                                                   const float2 *__restrict__ Lb, const float2 *__restrict__ Wfp,
+                                                   const float2 *__restrict__ Wbp, const float2 *__restrict__ Dinv,
+                                                   double *Xp, int ring, float2 *sRing, float2 *sP, float2 *sV) {
+    const int npad = M.nbc * TB;
+    float2 *Yp = reinterpret_cast<float2 *>(Xp);
+    const int t = threadIdx.x, r = t % TB, g = t / TB;
+    for (int sweep = 0; sweep < 2; ++sweep) {
+        const bool fwd = sweep == 0;
+        const float2 *Lt = fwd ? Lf : Lb;
+        for (int s = 0; s < M.nbc; ++s) {
+            const int I = fwd ? s : M.nbc - 1 - s;
+            // partial products: forward sum_d L_{I,I-d} y_{I-d}; backward sum_d L_{I+d,I}^T x_{I+d}
+            DF acc[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) acc[c] = DF{0.f, 0.f};
+            const int dmax = min(M.bt, fwd ? I : M.nbc - 1 - I);
+            for (int d = 1 + g; d <= dmax; d += kGroups) {
+                const int J = fwd ? I - d : I + d;
+                const float2 *T = Lt + tile_off(M, fwd ? J : I, d);
+                const float2 *y = sRing + (size_t)(J % ring) * kSolveCols * TB;
+#pragma unroll 4
+                for (int k = 0; k < TB; ++k) {
+                    const float2 l = __ldg(T + k * TB + r);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        const float2 v = y[c * TB + k];
+                        df_acc(acc[c], l.x, l.y, v.x, v.y);
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const DF a = df_norm(acc[c]);
+                sP[(g * kSolveCols + c) * TB + r] = make_float2(a.hi, a.lo);
+            }
+            __syncthreads();
+            if (g < NC) {
+                const int c = g;
+                const size_t xi = (size_t)c * npad + (size_t)I * TB + r;
+                DF v;
+                if (fwd) {
+                    v = df_from_double(Xp[xi]);
+                } else {
+                    const float2 yv = Yp[xi], di = __ldg(Dinv + M.xUnit + (size_t)I * TB + r);
+                    v = df_mul(DF{yv.x, yv.y}, DF{di.x, di.y});
+                }
+                for (int q = 0; q < kGroups; ++q) {
+                    const float2 p = sP[(q * kSolveCols + c) * TB + r];
+                    v = df_sub(v, DF{p.x, p.y});
+                }
+                sV[c * TB + r] = make_float2(v.hi, v.lo);
+                __syncwarp();
+                // forward y = W v (W[r][k] at Wf[k TB + r]); backward x = W^T v (W[k][r] at Wb[k TB + r])
+                const float2 *W = (fwd ? Wfp : Wbp) + (size_t)I * TT;
+                DF o = {0.f, 0.f}, o2 = {0.f, 0.f};
+#pragma unroll 4
+                for (int k = 0; k < TB; k += 2) {
+                    const float2 w0 = __ldg(W + k * TB + r), w1 = __ldg(W + (k + 1) * TB + r);
+                    const float2 v0 = sV[c * TB + k], v1 = sV[c * TB + k + 1];
+                    df_acc(o, w0.x, w0.y, v0.x, v0.y);
+                    df_acc(o2, w1.x, w1.y, v1.x, v1.y);
+                }
+                o = df_add(df_norm(o), df_norm(o2));
+                sRing[((size_t)(I % ring) * kSolveCols + c) * TB + r] = make_float2(o.hi, o.lo);
+                if (fwd)
+                    Yp[xi] = make_float2(o.hi, o.lo);
+                else
+                    Xp[xi] = df_to_double(o);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_band_solve_df(const PanelMeta *__restrict__ meta,
+                                                            const SolveItem *__restrict__ items,
+                                                            const float2 *__restrict__ Lf,
+                                                            const float2 *__restrict__ Lb,
+                                                            const float2 *__restrict__ Wf,
+                                                            const float2 *__restrict__ Wb,
+                                                            const float2 *__restrict__ Dinv, double *X, int nrhs,
+                                                            int ring) {
+    extern __shared__ float2 sdf[];
+    float2 *sRing = sdf;                                // [ring][kSolveCols][TB]
+    float2 *sP = sRing + (size_t)ring * kSolveCols * TB;  // [kGroups][kSolveCols][TB]
+    float2 *sV = sP + kGroups * kSolveCols * TB;        // [kSolveCols][TB]
+    const SolveItem it = items[blockIdx.x];
+    const PanelMeta M = meta[it.panel];
+    double *Xp = X + (size_t)M.xUnit * nrhs + (size_t)it.col0 * (M.nbc * TB);
+    const float2 *Wfp = Wf + (size_t)M.xUnit * TB, *Wbp = Wb + (size_t)M.xUnit * TB;
+    // the work of a group is in proportion to its columns: the item's column count picks the
+    // instantiation
+    switch (it.ncol) {
+    case 1: band_solve_df_item<1>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    case 2: band_solve_df_item<2>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    case 3: band_solve_df_item<3>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    case 4: band_solve_df_item<4>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    case 5: band_solve_df_item<5>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    case 6: band_solve_df_item<6>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    case 7: band_solve_df_item<7>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    default: band_solve_df_item<kSolveCols>(M, Lf, Lb, Wfp, Wbp, Dinv, Xp, ring, sRing, sP, sV); break;
+    }
+}
+
 // ---- many right-hand sides of one large band: the time-stepping solve ----------------------
 //
 // k_band_solve gives a (panel, group of columns) to one CTA, which suits many small panels.  A
@@ -740,13 +911,22 @@ __global__ void k_band_dfprep(const PanelMeta *__restrict__ meta, int np, const 
         x[i] = v;
     }
     const size_t ow = (size_t)M.xUnit * TB + (size_t)J * TT;
+    const double dl = sT[w][lane][lane];
+    __syncwarp();
 #pragma unroll
     for (int i = 0; i < TB; ++i) {
         const DF v = df_from_double(x[i]);  // W[i][lane]
-        Wf[ow + (size_t)lane * TB + i] = make_float2(v.hi, v.lo);  // column-major: W[i][k] at k*TB + i
-        Wb[ow + (size_t)i * TB + lane] = make_float2(v.hi, v.lo);  // row-major:    W[i][k] at i*TB + k
+        Wb[ow + (size_t)i * TB + lane] = make_float2(v.hi, v.lo);  // row-major: W[i][k] at i*TB + k
+        sT[w][i][lane] = x[i];
     }
-    const DF dv = df_from_double(1.0 / sT[w][lane][lane]);
+    __syncwarp();
+    // column-major (W[i][k] at k*TB + i) through shared memory, so the stores are coalesced
+#pragma unroll 4
+    for (int k = 0; k < TB; ++k) {
+        const DF v = df_from_double(sT[w][lane][k]);
+        Wf[ow + (size_t)k * TB + lane] = make_float2(v.hi, v.lo);
+    }
+    const DF dv = df_from_double(1.0 / dl);
     Dinv[(size_t)M.xUnit + (size_t)J * TB + lane] = make_float2(dv.hi, dv.lo);
 }
 
@@ -944,6 +1124,11 @@ __global__ void __launch_bounds__(kCW * 32, 1) k_band_solve_cases(const PanelMet
 }
 
 // internal-layout columns (nrhs x n) <-> the padded panel layout
+__global__ void k_vec_add(long long n, const double *__restrict__ x, double *__restrict__ y) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] += x[i];
+}
+
 __global__ void k_panel_move(int n, int dpn, int nrhs, double *__restrict__ vec, const int *__restrict__ panelOf,
                              const int *__restrict__ pos, const PanelMeta *__restrict__ meta, double *__restrict__ X,
                              int toPanel) {
@@ -1232,7 +1417,8 @@ void plan_free(PanelPlan *L) {
                    &L->d_Lf,    &L->d_Lb,    &L->d_Wf,       &L->d_Wb,      &L->d_Dinv,  &L->d_items,
                    &L->d_X,     &L->d_twMeta, &L->d_twBand, &L->d_twAw,  &L->d_twSched, &L->d_twSchedPtr,
                    &L->d_twStatus, &L->d_twLf, &L->d_twLb, &L->d_twWf, &L->d_twWb, &L->d_twDinv,
-                   &L->d_twItems, &L->d_twX};
+                   &L->d_twItems, &L->d_twX, &L->d_sRef, &L->d_sVec, &L->d_sRes, &L->d_sBi, &L->d_sX,
+                   &L->d_sItems};
     for (DevBuf *x : b) dev_free(*x);
 }
 
@@ -1329,6 +1515,11 @@ int panels_factor_impl(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *
                               (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
                               dptr<double>(L->d_band), dptr<int>(L->d_status), (uint16_t *)nullptr, (int *)nullptr,
                               0LL, 0));
+    } else if (ctx->bandFp64Update == 3) {
+        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<3>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+                              (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
+                              dptr<double>(L->d_band), dptr<int>(L->d_status), dptr<uint16_t>(L->d_slices),
+                              (int *)nullptr, L->sliceStride, 0));
     } else if (ctx->bandFp64Update == 2) {
         CK(cudaLaunchKernelEx(&cfg, k_band_ldl<1>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
                               (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
@@ -1360,12 +1551,37 @@ extern "C" int astro_panels_factor(astro_ctx *ctx, int32_t cluster_size, astro_p
     return panels_factor_impl(ctx, cluster_size, info, 1);
 }
 
-static int panels_solve_dev(astro_ctx *ctx, PanelPlan *L, int nrhs, double *d_vec, DevBuf &X) {
+// A device buffer of at least `bytes`, reallocated only to grow.
+static int grow(astro_ctx *ctx, DevBuf &b, size_t bytes) {
+    return b.p && b.bytes >= bytes ? ASTRO_OK : dev_alloc(ctx, b, bytes);
+}
+
+// The double-float copies of the current factorisation (k_band_dfprep), made once per factor.
+static int panels_df_copies(astro_ctx *ctx, PanelPlan *L) {
+    if (L->dfGen == L->factorGen) return ASTRO_OK;
+    int rc;
+    const size_t nb = (size_t)L->bandDoubles, nd = (size_t)L->xRows;
+    if ((rc = grow(ctx, L->d_Lf, sizeof(float2) * nb)) || (rc = grow(ctx, L->d_Lb, sizeof(float2) * nb)) ||
+        (rc = grow(ctx, L->d_Wf, sizeof(float2) * nd * TB)) || (rc = grow(ctx, L->d_Wb, sizeof(float2) * nd * TB)) ||
+        (rc = grow(ctx, L->d_Dinv, sizeof(float2) * nd)))
+        return rc;
+    long long cols = 0;
+    for (const PanelMeta &M : L->meta) cols += M.nbc;
+    k_band_dfprep<<<(unsigned)((cols + kPrepW - 1) / kPrepW), kPrepW * 32, 0, ctx->stream>>>(
+        dptr<PanelMeta>(L->d_meta), L->np, dptr<double>(L->d_band), dptr<float2>(L->d_Lf), dptr<float2>(L->d_Lb),
+        dptr<float2>(L->d_Wf), dptr<float2>(L->d_Wb), dptr<float2>(L->d_Dinv));
+    if ((rc = cuda_check(ctx, cudaGetLastError(), "band double-float copy"))) return rc;
+    L->dfGen = L->factorGen;
+    return ASTRO_OK;
+}
+
+static int panels_solve_dev(astro_ctx *ctx, PanelPlan *L, int nrhs, double *d_vec) {
     const AstroPrep &P = ctx->P;
     cudaStream_t s = ctx->stream;
     int rc;
     const size_t xs = (size_t)L->xRows * nrhs;
-    if ((rc = dev_alloc(ctx, X, sizeof(double) * xs))) return rc;
+    DevBuf &X = L->d_sX;
+    if ((rc = grow(ctx, X, sizeof(double) * xs))) return rc;
     CK(cudaMemsetAsync(X.p, 0, sizeof(double) * xs, s));
     const long long mv = (long long)P.n * nrhs;
     const unsigned mg = (unsigned)((mv + 255) / 256);
@@ -1387,16 +1603,26 @@ static int panels_solve_dev(astro_ctx *ctx, PanelPlan *L, int nrhs, double *d_ve
             c0 += nc;
         }
     }
-    DevBuf dItems;
-    if ((rc = upload(ctx, dItems, items.data(), sizeof(SolveItem) * items.size()))) return rc;
-    CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem));
-    k_band_solve<<<(unsigned)items.size(), kThreads, kSolveSmem, s>>>(
-        dptr<PanelMeta>(L->d_meta), dptr<SolveItem>(dItems), dptr<double>(L->d_band), dptr<double>(X), nrhs);
+    DevBuf &dItems = L->d_sItems;
+    if ((rc = grow(ctx, dItems, sizeof(SolveItem) * items.size()))) return rc;
+    CK(cudaMemcpyAsync(dItems.p, items.data(), sizeof(SolveItem) * items.size(), cudaMemcpyHostToDevice, s));
+    if (ctx->panelsSolve == 1) {
+        CK(cudaFuncSetAttribute(k_band_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem));
+        k_band_solve<<<(unsigned)items.size(), kThreads, kSolveSmem, s>>>(
+            dptr<PanelMeta>(L->d_meta), dptr<SolveItem>(dItems), dptr<double>(L->d_band), dptr<double>(X), nrhs);
+    } else {
+        if ((rc = panels_df_copies(ctx, L))) return rc;
+        const int ring = L->maxBt + 1;
+        const size_t smem = sizeof(float2) * kSolveCols * TB * ((size_t)ring + kGroups + 1);
+        CK(cudaFuncSetAttribute(k_band_solve_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_band_solve_df<<<(unsigned)items.size(), kThreads, smem, s>>>(
+            dptr<PanelMeta>(L->d_meta), dptr<SolveItem>(dItems), dptr<float2>(L->d_Lf), dptr<float2>(L->d_Lb),
+            dptr<float2>(L->d_Wf), dptr<float2>(L->d_Wb), dptr<float2>(L->d_Dinv), dptr<double>(X), nrhs, ring);
+    }
     k_panel_move<<<mg, 256, 0, s>>>(P.n, P.dpn, nrhs, d_vec, dptr<int>(L->d_panelOf), dptr<int>(L->d_pos),
                                     dptr<PanelMeta>(L->d_meta), dptr<double>(X), 0);
     rc = cuda_check(ctx, cudaGetLastError(), "panel solve");
     if (!rc) rc = cuda_check(ctx, cudaStreamSynchronize(s), "panel solve");
-    dev_free(dItems);
     return rc;
 }
 
@@ -1408,28 +1634,35 @@ extern "C" int astro_panels_solve(astro_ctx *ctx, int32_t num_rhs, const double 
         return set_err(ctx, ASTRO_ERR_STATE, "panels: no current factorisation (astro_panels_factor)");
     const int n = ctx->P.n;
     const auto t0 = std::chrono::steady_clock::now();
-    DevBuf ref, vec, X;
-    int rc = dev_alloc(ctx, ref, sizeof(double) * (size_t)n * num_rhs);
-    if (!rc) rc = dev_alloc(ctx, vec, sizeof(double) * (size_t)n * num_rhs);
-    if (!rc) {
-        cudaError_t e = cudaMemcpyAsync(ref.p, rhs, sizeof(double) * (size_t)n * num_rhs, cudaMemcpyHostToDevice,
-                                        ctx->stream);
-        rc = cuda_check(ctx, e, "panels: upload");
-    }
+    const size_t nt = (size_t)n * num_rhs;
+    DevBuf &ref = L->d_sRef, &vec = L->d_sVec;
+    int rc = grow(ctx, ref, sizeof(double) * nt);
+    if (!rc) rc = grow(ctx, vec, sizeof(double) * nt);
+    if (!rc) rc = copy_to_device(ctx, ref.p, rhs, sizeof(double) * nt, "panels: upload");
     for (int c = 0; c < num_rhs && !rc; ++c)
         rc = ref_to_int_vec(ctx, dptr<double>(ref) + (size_t)c * n, dptr<double>(vec) + (size_t)c * n, n);
-    if (!rc) rc = panels_solve_dev(ctx, L, num_rhs, dptr<double>(vec), X);
+    if (!rc) rc = panels_solve_dev(ctx, L, num_rhs, dptr<double>(vec));
+    if (!rc && ctx->panelsSolve == 0) {
+        // one refinement pass: r = b - A x with the FP64 operator, x += the double-float solve of r
+        DevBuf &bi = L->d_sBi, &res = L->d_sRes;
+        rc = grow(ctx, bi, sizeof(double) * (size_t)n);
+        if (!rc) rc = grow(ctx, res, sizeof(double) * nt);
+        for (int c = 0; c < num_rhs && !rc; ++c) {
+            rc = ref_to_int_vec(ctx, dptr<double>(ref) + (size_t)c * n, dptr<double>(bi), n);
+            if (!rc)
+                rc = krylov_residual64(ctx, dptr<double>(vec) + (size_t)c * n, dptr<double>(bi),
+                                       dptr<double>(res) + (size_t)c * n);
+        }
+        if (!rc) rc = panels_solve_dev(ctx, L, num_rhs, dptr<double>(res));
+        if (!rc) {
+            k_vec_add<<<(unsigned)((nt + 255) / 256), 256, 0, ctx->stream>>>((long long)nt, dptr<double>(res),
+                                                                            dptr<double>(vec));
+            rc = cuda_check(ctx, cudaGetLastError(), "panels: refinement");
+        }
+    }
     for (int c = 0; c < num_rhs && !rc; ++c)
         rc = int_to_ref_vec(ctx, dptr<double>(vec) + (size_t)c * n, dptr<double>(ref) + (size_t)c * n, n);
-    if (!rc) {
-        cudaError_t e = cudaMemcpyAsync(x, ref.p, sizeof(double) * (size_t)n * num_rhs, cudaMemcpyDeviceToHost,
-                                        ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        rc = cuda_check(ctx, e, "panels: download");
-    }
-    dev_free(ref);
-    dev_free(vec);
-    dev_free(X);
+    if (!rc) rc = copy_to_host(ctx, x, ref.p, sizeof(double) * nt, "panels: download");
     if (info) {
         fill_info(*L, info);
         info->solve_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1487,20 +1720,7 @@ int panels_cases_prepare(astro_ctx *ctx, int ncols, size_t *bytes) {
         return cuda_check(ctx, cudaStreamSynchronize(s), "panels cases prepare");
     }
     if (!L->factored) return set_err(ctx, ASTRO_ERR_STATE, "panels: no current factorisation (astro_panels_factor)");
-    if (L->dfGen != L->factorGen) {
-        const size_t nb = (size_t)L->bandDoubles, nd = (size_t)L->xRows;
-        if ((rc = dev_alloc(ctx, L->d_Lf, sizeof(float2) * nb)) || (rc = dev_alloc(ctx, L->d_Lb, sizeof(float2) * nb)) ||
-            (rc = dev_alloc(ctx, L->d_Wf, sizeof(float2) * nd * TB)) ||
-            (rc = dev_alloc(ctx, L->d_Wb, sizeof(float2) * nd * TB)) || (rc = dev_alloc(ctx, L->d_Dinv, sizeof(float2) * nd)))
-            return rc;
-        long long cols = 0;
-        for (const PanelMeta &M : L->meta) cols += M.nbc;
-        k_band_dfprep<<<(unsigned)((cols + kPrepW - 1) / kPrepW), kPrepW * 32, 0, s>>>(
-            dptr<PanelMeta>(L->d_meta), L->np, dptr<double>(L->d_band), dptr<float2>(L->d_Lf), dptr<float2>(L->d_Lb),
-            dptr<float2>(L->d_Wf), dptr<float2>(L->d_Wb), dptr<float2>(L->d_Dinv));
-        if ((rc = cuda_check(ctx, cudaGetLastError(), "band double-float copy"))) return rc;
-        L->dfGen = L->factorGen;
-    }
+    if ((rc = panels_df_copies(ctx, L))) return rc;
     if (L->casesCols != ncols) {
         std::vector<CaseItem> items;
         for (int p = 0; p < L->np; ++p)

@@ -2,7 +2,9 @@
 LDL^T of K + C^T C of every panel in one launch against a sparse direct solve of the oracle's
 assembled system, for several cluster sizes, multi-tile bands, many right-hand sides, bricks
 (3 DOF per node) and the complex-step sensitivity pipeline.  Solutions agree to 1e-10 relative
-and the FP64 residual ||A X - B|| is within 10x of the sparse direct solve's per column."""
+and the FP64 residual ||A X - B|| is within 10x of the sparse direct solve's per column.  The
+solves run in the default mode (double-float sweeps and one FP64 refinement pass) unless a test
+selects another."""
 import numpy as np
 import pytest
 import scipy.sparse.linalg as spla
@@ -197,3 +199,53 @@ def test_tensor_core_update_matches_fp64_update(batch):
     _check(A, Xtc, B, Xr)
     assert np.array_equal(Xtc, Xmma)
     assert np.linalg.norm(Xtc - X64) <= 1e-10 * np.linalg.norm(X64)
+
+
+def test_solve_sweep_arithmetic(batch):
+    """astro_panels_solve's three sweep modes on one factor: double-float sweeps with one FP64
+    refinement pass (the default), FP64 sweeps, and double-float sweeps alone.  The first two
+    meet the sparse direct solve as above and agree to 1e-10; the double-float sweeps alone are
+    within 1e-8 of the FP64 ones (about 48 significant bits per operation)."""
+    from misc_gb300.astro import OPT_PANELS_SOLVE
+    m, g, o, A = batch
+    B = np.random.default_rng(23).standard_normal((g.n, 13))
+    Xr = spla.splu(A).solve(B)
+    g.panels_factor(4)
+    X = {}
+    try:
+        for mode in (0, 1, 2):
+            g.set_option(OPT_PANELS_SOLVE, mode)
+            X[mode], _ = g.panels_solve(B)
+    finally:
+        g.set_option(OPT_PANELS_SOLVE, 0)
+    _check(A, X[0], B, Xr)
+    _check(A, X[1], B, Xr)
+    assert np.linalg.norm(X[0] - X[1]) <= 1e-10 * np.linalg.norm(X[1])
+    assert np.linalg.norm(X[2] - X[1]) <= 1e-8 * np.linalg.norm(X[1])
+    with pytest.raises(AstroError):
+        g.set_option(OPT_PANELS_SOLVE, 3)
+
+
+def test_double_float_update_with_refined_solve(batch):
+    """The band factor with double-float trailing updates (option value 3: about 48 significant
+    bits) and the default solve (double-float sweeps, one FP64 refinement against the operator):
+    the solution meets the sparse direct solve as the FP64 factor's does and agrees with it to
+    1e-10; the unrefined double-float sweeps on that factor are within 1e-7."""
+    from misc_gb300.astro import OPT_BAND_FP64_UPDATE, OPT_PANELS_SOLVE
+    m, g, o, A = batch
+    B = np.random.default_rng(29).standard_normal((g.n, 10))
+    Xr = spla.splu(A).solve(B)
+    g.panels_factor(4)
+    X64, _ = g.panels_solve(B)
+    try:
+        g.set_option(OPT_BAND_FP64_UPDATE, 3)
+        g.panels_factor(4)
+        Xdf, _ = g.panels_solve(B)
+        g.set_option(OPT_PANELS_SOLVE, 2)
+        Xraw, _ = g.panels_solve(B)
+    finally:
+        g.set_option(OPT_PANELS_SOLVE, 0)
+        g.set_option(OPT_BAND_FP64_UPDATE, 1)
+    _check(A, Xdf, B, Xr)
+    assert np.linalg.norm(Xdf - X64) <= 1e-10 * np.linalg.norm(X64)
+    assert np.linalg.norm(Xraw - X64) <= 1e-7 * np.linalg.norm(X64)
