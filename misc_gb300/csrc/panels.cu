@@ -258,7 +258,7 @@ __device__ void split_tile(const double *T, const double (*sL)[TB + 1], int v, u
 // slices + worker * sliceStride and their scales in sexp + worker * expStride.  Both emulations
 // sum every level exactly and combine the levels in the same order: identical results.
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restrict__ meta, const int *__restrict__ sched,
+__global__ void __launch_bounds__(kThreads, MODE == 2 ? 1 : 2) k_band_ldl(const PanelMeta *__restrict__ meta, const int *__restrict__ sched,
                                                        const int *__restrict__ schedPtr, double *band, int *status,
                                                        uint16_t *slices, int *sexp, long long sliceStride,
                                                        int expStride) {
@@ -269,6 +269,7 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
     uint16_t *wsl = MODE != 0 ? slices + (size_t)worker * sliceStride : nullptr;
     int *wex = TC ? sexp + (size_t)worker * expStride : nullptr;
     __shared__ double sL[TB][TB + 1];  // diagonal tile: L below the diagonal, D on it
+    __shared__ double sDi[TB];         // D^-1
     __shared__ double sA[TB][TB + 1], sB[TB][TB + 1];
     const int t = threadIdx.x;
     // MODE 2: tensor memory, the completion barrier of the MMAs and the operand staging
@@ -310,6 +311,8 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
                 const double dk = sL[t][t];
                 if (!(dk != 0.0 && isfinite(dk))) atomicCAS(status, 0, p + 1);
             }
+            if (t < TB) sDi[t] = 1.0 / sL[t][t];
+            __syncthreads();
             // B. the tiles below: L_IJ = A_IJ L_JJ^-T D^-1, one row per thread across the cluster
             for (int rho = crank * kThreads + t; rho < M.bt * TB; rho += cs * kThreads) {
                 const int d = 1 + rho / TB, r = rho % TB;
@@ -326,7 +329,7 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
                     w[k] = s;
                 }
 #pragma unroll
-                for (int c = 0; c < TB; ++c) __stcg(T + c * TB + r, w[c] / sL[c][c]);
+                for (int c = 0; c < TB; ++c) __stcg(T + c * TB + r, w[c] * sDi[c]);
             }
             __threadfence();
             cl.sync();
@@ -519,25 +522,62 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
                 }
                 __threadfence();
                 cl.sync();
-                // C. trailing update in double-float on the FP32 pipe, the result subtracted in FP64
+                // C. trailing update in double-float on the FP32 pipe, the result subtracted in FP64.
+                // The next item's operand tiles and output values are loaded into registers while
+                // the current item computes (the scratch tiles come from L2, the band from HBM).
                 float2(*fA)[TB + 1] = reinterpret_cast<float2(*)[TB + 1]>(sA);
                 float2(*fB)[TB + 1] = reinterpret_cast<float2(*)[TB + 1]>(sB);
-                for (int u = crank; u < nt; u += cs) {
-                    int d = 1, rem = u;
+                const int r = t % TB, c0 = (t / TB) * 4;
+                auto item = [&](int u, int &d, int &e) {
+                    d = 1;
+                    int rem = u;
                     while (rem >= d) {
                         rem -= d;
                         ++d;
                     }
-                    const int e = 1 + rem;
-                    if (J + d >= M.nbc) continue;
+                    e = 1 + rem;
+                };
+                auto next = [&](int u) {  // the first item >= u of this CTA inside the band
+                    for (; u < nt; u += cs) {
+                        int d, e;
+                        item(u, d, e);
+                        if (J + d < M.nbc) break;
+                    }
+                    return u;
+                };
+                float2 ra[TT / kThreads], rb[TT / kThreads];
+                double ro[4];
+                auto fetch = [&](int u) {
+                    int d, e;
+                    item(u, d, e);
                     const float2 *Ad = wdf + (size_t)(2 * (d - 1)) * TT, *Be = wdf + (size_t)(2 * (e - 1) + 1) * TT;
+#pragma unroll
+                    for (int j = 0; j < TT / kThreads; ++j) {
+                        ra[j] = __ldcg(Ad + t + j * kThreads);
+                        rb[j] = __ldcg(Be + t + j * kThreads);
+                    }
+                    const double *Tt = band + tile_off(M, J + e, d - e);
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) ro[cc] = __ldcg(Tt + (c0 + cc) * TB + r);
+                };
+                int u = next(crank);
+                if (u < nt) fetch(u);
+                while (u < nt) {
+                    const int un = next(u + cs);
                     __syncthreads();
-                    for (int x = t; x < TT; x += kThreads) {
-                        fA[x % TB][x / TB] = __ldcg(Ad + x);
-                        fB[x % TB][x / TB] = __ldcg(Be + x);
+#pragma unroll
+                    for (int j = 0; j < TT / kThreads; ++j) {
+                        const int x = t + j * kThreads;
+                        fA[x % TB][x / TB] = ra[j];
+                        fB[x % TB][x / TB] = rb[j];
                     }
                     __syncthreads();
-                    const int r = t % TB, c0 = (t / TB) * 4;
+                    double o[4];
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) o[cc] = ro[cc];
+                    int d, e;
+                    item(u, d, e);
+                    if (un < nt) fetch(un);
                     DF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll 8
                     for (int k = 0; k < TB; ++k) {
@@ -550,10 +590,8 @@ __global__ void __launch_bounds__(kThreads) k_band_ldl(const PanelMeta *__restri
                     }
                     double *Tt = band + tile_off(M, J + e, d - e);
 #pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) {
-                        double *pt = Tt + (c0 + cc) * TB + r;
-                        __stcg(pt, __ldcg(pt) - df_to_double(df_norm(acc[cc])));
-                    }
+                    for (int cc = 0; cc < 4; ++cc) __stcg(Tt + (c0 + cc) * TB + r, o[cc] - df_to_double(df_norm(acc[cc])));
+                    u = un;
                 }
                 __threadfence();
                 cl.sync();
@@ -882,20 +920,20 @@ __global__ void k_band_dfprep(const PanelMeta *__restrict__ meta, int np, const 
         Dinv[(size_t)M.xUnit + (size_t)J * TB + lane] = make_float2(1.f, 0.f);
         return;
     }
+    // each value converted once (the conversions run on the FP64 pipe), the transpose from shared
+    // memory in double-float
+    float2(*sF)[TB + 1] = reinterpret_cast<float2(*)[TB + 1]>(&sT[w][0][0]);
     for (int d = 1; d <= M.bt; ++d) {
         if (J + d >= M.nbc) break;
         const size_t o = tile_off(M, J, d);
         for (int e = lane; e < TT; e += 32) {
             const DF v = df_from_double(band[o + e]);
             Lf[o + e] = make_float2(v.hi, v.lo);
-            sT[w][e % TB][e / TB] = band[o + e];  // [row][col]
+            sF[e % TB][e / TB] = make_float2(v.hi, v.lo);  // [row][col]
         }
         __syncwarp();
         // Lb[k * TB + r] = L[k][r]
-        for (int e = lane; e < TT; e += 32) {
-            const DF v = df_from_double(sT[w][e / TB][e % TB]);
-            Lb[o + e] = make_float2(v.hi, v.lo);
-        }
+        for (int e = lane; e < TT; e += 32) Lb[o + e] = sF[e / TB][e % TB];
         __syncwarp();
     }
     const size_t od = tile_off(M, J, 0);
@@ -917,15 +955,12 @@ __global__ void k_band_dfprep(const PanelMeta *__restrict__ meta, int np, const 
     for (int i = 0; i < TB; ++i) {
         const DF v = df_from_double(x[i]);  // W[i][lane]
         Wb[ow + (size_t)i * TB + lane] = make_float2(v.hi, v.lo);  // row-major: W[i][k] at i*TB + k
-        sT[w][i][lane] = x[i];
+        sF[i][lane] = make_float2(v.hi, v.lo);
     }
     __syncwarp();
     // column-major (W[i][k] at k*TB + i) through shared memory, so the stores are coalesced
 #pragma unroll 4
-    for (int k = 0; k < TB; ++k) {
-        const DF v = df_from_double(sT[w][lane][k]);
-        Wf[ow + (size_t)k * TB + lane] = make_float2(v.hi, v.lo);
-    }
+    for (int k = 0; k < TB; ++k) Wf[ow + (size_t)k * TB + lane] = sF[lane][k];
     const DF dv = df_from_double(1.0 / dl);
     Dinv[(size_t)M.xUnit + (size_t)J * TB + lane] = make_float2(dv.hi, dv.lo);
 }
