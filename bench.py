@@ -571,7 +571,7 @@ def _panels_eval(a):
                         "rel_residual_u": float(np.linalg.norm(rm) / np.linalg.norm(B[:, 0]))}
         del Xm
     g.set_option(OPT_PANELS_SOLVE, 0)
-    # the same unit with the double-float trailing update (a 48-bit factor; the default solve
+    # the same unit with the factorisation in double-float (a 48-bit factor; the default solve
     # refines against the FP64 operator)
     from misc_gb300.astro import OPT_BAND_FP64_UPDATE
     g.set_option(OPT_BAND_FP64_UPDATE, 3)
@@ -636,8 +636,10 @@ def _panels_eval(a):
                              "achieved_tflops": 2 * fma_f / fac / 1e12, "peak_tflops": pk,
                              "frac": (2 * fma_f / fac / 1e12 / pk) if pk else None,
                              "achieved_tflops_tensor_core_update": 2 * fma_f / facTc / 1e12,
+                             "achieved_tflops_double_float_factor": 2 * fma_f / df_update["factor_seconds"] / 1e12,
                              "note": "the factor's FP64 multiply-adds over its time; the tensor-core "
-                                     "emulation's rate is the same count over its own time",
+                                     "emulation's and the double-float factor's rates are the same count "
+                                     "over their own times",
                              "peak_source": "measured: torch.matmul float64 4096^3 (cuBLAS DGEMM) on this GPU",
                              "solve_fma": fma_s, "solve_tflops": 2 * fma_s / sol / 1e12}}
     del g

@@ -251,10 +251,10 @@ int astro_get_dims(const astro_ctx *ctx, astro_dims *out);
  * astro_newmark_cases) runs its trailing tile updates in FP64 arithmetic; 0 selects the
  * tensor-core emulation on tcgen05 (BF16 slices of the Ozaki error-free splitting, summed exactly
  * in FP32 per level in tensor memory and combined in FP64; 56 bits relative to each row's largest
- * entry), 2 the same emulation on mma.sync (identical results), 3 the updates in double-float
- * arithmetic on the FP32 pipe (about 48 significant bits; the operand tiles converted once per
- * block column, the products subtracted from the FP64 band in FP64): a factor of lower precision
- * for solves that refine against the FP64 operator (astro_panels_solve's default mode). */
+ * entry), 2 the same emulation on mma.sync (identical results), 3 the whole factorisation in
+ * double-float arithmetic on the FP32 pipe (the band converted in place to float pairs and back;
+ * about 48 significant bits per operation): a factor of lower precision for solves that refine
+ * against the FP64 operator (astro_panels_solve's default mode). */
 #define ASTRO_OPT_BAND_FP64_UPDATE 3
 /* The launch shapes astro_autotune picks, set directly (0 = the default): the zero-state brick
  * kernel's warps per CTA (1, 2, 4), the band factorisation's and the many-column band solve's

@@ -266,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, MODE == 2 ? 1 : 2) k_band_ldl(const 
     cg::cluster_group cl = cg::this_cluster();
     const int crank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
     const int worker = blockIdx.x / cs;
-    uint16_t *wsl = MODE != 0 ? slices + (size_t)worker * sliceStride : nullptr;
+    uint16_t *wsl = TC ? slices + (size_t)worker * sliceStride : nullptr;
     int *wex = TC ? sexp + (size_t)worker * expStride : nullptr;
     __shared__ double sL[TB][TB + 1];  // diagonal tile: L below the diagonal, D on it
     __shared__ double sDi[TB];         // D^-1
@@ -508,95 +508,6 @@ __global__ void __launch_bounds__(kThreads, MODE == 2 ? 1 : 2) k_band_ldl(const 
                 cl.sync();
                 continue;
             }
-            if constexpr (MODE == 3) {
-                // B2. double-float copies of the tiles below the diagonal, L D_J (v = 0) and L
-                // (v = 1), in the worker's scratch: tile (d, v) at wdf + (2 (d-1) + v) TT
-                float2 *wdf = reinterpret_cast<float2 *>(wsl);
-                for (int x = crank * kThreads + t; x < 2 * M.bt * TT; x += cs * kThreads) {
-                    const int uu = x / TT, d = 1 + uu / 2, v = uu % 2, el = x % TT;
-                    if (J + d >= M.nbc) continue;
-                    double a = __ldcg(band + tile_off(M, J, d) + el);
-                    if (v == 0) a *= sL[el / TB][el / TB];
-                    const DF f = df_from_double(a);
-                    __stcg(wdf + x, make_float2(f.hi, f.lo));
-                }
-                __threadfence();
-                cl.sync();
-                // C. trailing update in double-float on the FP32 pipe, the result subtracted in FP64.
-                // The next item's operand tiles and output values are loaded into registers while
-                // the current item computes (the scratch tiles come from L2, the band from HBM).
-                float2(*fA)[TB + 1] = reinterpret_cast<float2(*)[TB + 1]>(sA);
-                float2(*fB)[TB + 1] = reinterpret_cast<float2(*)[TB + 1]>(sB);
-                const int r = t % TB, c0 = (t / TB) * 4;
-                auto item = [&](int u, int &d, int &e) {
-                    d = 1;
-                    int rem = u;
-                    while (rem >= d) {
-                        rem -= d;
-                        ++d;
-                    }
-                    e = 1 + rem;
-                };
-                auto next = [&](int u) {  // the first item >= u of this CTA inside the band
-                    for (; u < nt; u += cs) {
-                        int d, e;
-                        item(u, d, e);
-                        if (J + d < M.nbc) break;
-                    }
-                    return u;
-                };
-                float2 ra[TT / kThreads], rb[TT / kThreads];
-                double ro[4];
-                auto fetch = [&](int u) {
-                    int d, e;
-                    item(u, d, e);
-                    const float2 *Ad = wdf + (size_t)(2 * (d - 1)) * TT, *Be = wdf + (size_t)(2 * (e - 1) + 1) * TT;
-#pragma unroll
-                    for (int j = 0; j < TT / kThreads; ++j) {
-                        ra[j] = __ldcg(Ad + t + j * kThreads);
-                        rb[j] = __ldcg(Be + t + j * kThreads);
-                    }
-                    const double *Tt = band + tile_off(M, J + e, d - e);
-#pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) ro[cc] = __ldcg(Tt + (c0 + cc) * TB + r);
-                };
-                int u = next(crank);
-                if (u < nt) fetch(u);
-                while (u < nt) {
-                    const int un = next(u + cs);
-                    __syncthreads();
-#pragma unroll
-                    for (int j = 0; j < TT / kThreads; ++j) {
-                        const int x = t + j * kThreads;
-                        fA[x % TB][x / TB] = ra[j];
-                        fB[x % TB][x / TB] = rb[j];
-                    }
-                    __syncthreads();
-                    double o[4];
-#pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) o[cc] = ro[cc];
-                    int d, e;
-                    item(u, d, e);
-                    if (un < nt) fetch(un);
-                    DF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-#pragma unroll 8
-                    for (int k = 0; k < TB; ++k) {
-                        const float2 a = fA[r][k];
-#pragma unroll
-                        for (int cc = 0; cc < 4; ++cc) {
-                            const float2 b = fB[c0 + cc][k];
-                            df_acc(acc[cc], a.x, a.y, b.x, b.y);
-                        }
-                    }
-                    double *Tt = band + tile_off(M, J + e, d - e);
-#pragma unroll
-                    for (int cc = 0; cc < 4; ++cc) __stcg(Tt + (c0 + cc) * TB + r, o[cc] - df_to_double(df_norm(acc[cc])));
-                    u = un;
-                }
-                __threadfence();
-                cl.sync();
-                continue;
-            }
             // C. trailing update of the band: tile (J+e, d-e) -= L_{J+d,J} D_J L_{J+e,J}^T, 1 <= e <= d
             for (int u = crank; u < nt; u += cs) {
                 int d = 1, rem = u;
@@ -638,6 +549,180 @@ __global__ void __launch_bounds__(kThreads, MODE == 2 ? 1 : 2) k_band_ldl(const 
         __syncthreads();
         if (t < 32)
             asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tcBase), "r"(kTcCols));
+    }
+}
+
+// ---- the band LDL^T carried in double-float (ASTRO_OPT_BAND_FP64_UPDATE = 3) ---------------
+//
+// The band converted in place to (hi, lo) float pairs (same 8 bytes per value), factored with
+// every step in double-float arithmetic on the FP32 pipe, then converted back to FP64: the steps
+// of k_band_ldl (the diagonal tile in shared memory in every CTA of the cluster, the rows below
+// split over the cluster, the trailing updates split over the cluster) with no FP64 instruction
+// inside.  About 48 significant bits per operation: a factor for solves that refine against the
+// FP64 operator.
+
+__global__ void k_band_df_convert(long long n, double *band, int toDf) {
+    float2 *bf = reinterpret_cast<float2 *>(band);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        if (toDf) {
+            const DF v = df_from_double(band[i]);
+            bf[i] = make_float2(v.hi, v.lo);
+        } else {
+            const float2 v = bf[i];
+            band[i] = (double)v.x + (double)v.y;
+        }
+    }
+}
+
+__device__ __forceinline__ DF df_of(float2 v) { return DF{v.x, v.y}; }
+__device__ __forceinline__ float2 f2_of(DF v) { return make_float2(v.hi, v.lo); }
+
+// scratch + worker * scratchStride: the block column's tiles below the diagonal times D_J, tile d
+// at (d - 1) TT
+__global__ void __launch_bounds__(kThreads, 2) k_band_ldl_df(const PanelMeta *__restrict__ meta,
+                                                             const int *__restrict__ sched,
+                                                             const int *__restrict__ schedPtr, float2 *band,
+                                                             int *status, float2 *scratch, long long scratchStride) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int crank = (int)cl.block_rank(), cs = (int)cl.num_blocks();
+    const int worker = blockIdx.x / cs;
+    float2 *wdf = scratch + (size_t)worker * scratchStride;
+    __shared__ float2 sL[TB][TB + 1];  // diagonal tile: L below the diagonal, D on it
+    __shared__ float2 sDi[TB];         // D^-1
+    __shared__ float2 fA[TB][TB + 1], fB[TB][TB + 1];
+    const int t = threadIdx.x;
+    for (int q = schedPtr[worker]; q < schedPtr[worker + 1]; ++q) {
+        const int p = sched[q];
+        const PanelMeta M = meta[p];
+        for (int J = 0; J < M.nfac; ++J) {
+            // A. the diagonal tile
+            float2 *Td = band + tile_off(M, J, 0);
+            for (int e = t; e < TT; e += kThreads) sL[e % TB][e / TB] = __ldcg(Td + e);
+            __syncthreads();
+            for (int k = 0; k < TB; ++k) {
+                const DF inv = df_rcp(df_of(sL[k][k]));
+                const int j = t % TB;
+                if (j > k) {
+                    const DF f = df_mul(df_of(sL[j][k]), inv);
+                    for (int i = t / TB; i < TB; i += kGroups)
+                        if (i >= j) sL[i][j] = f2_of(df_sub(df_of(sL[i][j]), df_mul(df_of(sL[i][k]), f)));
+                }
+                __syncthreads();
+                if (t > k && t < TB) sL[t][k] = f2_of(df_mul(df_of(sL[t][k]), inv));
+                __syncthreads();
+            }
+            if (crank == 0 && t < TB && J * TB + t < M.n) {
+                const float dk = sL[t][t].x;
+                if (!(dk != 0.f && isfinite(dk))) atomicCAS(status, 0, p + 1);
+            }
+            if (t < TB) sDi[t] = f2_of(df_rcp(df_of(sL[t][t])));
+            __syncthreads();
+            // B. the tiles below: L_IJ = A_IJ L_JJ^-T D^-1, one row per thread across the cluster
+            for (int rho = crank * kThreads + t; rho < M.bt * TB; rho += cs * kThreads) {
+                const int d = 1 + rho / TB, r = rho % TB;
+                if (J + d >= M.nbc) continue;
+                float2 *T = band + tile_off(M, J, d);
+                DF w[TB];
+#pragma unroll
+                for (int c = 0; c < TB; ++c) w[c] = df_of(__ldcg(T + c * TB + r));
+#pragma unroll
+                for (int k = 1; k < TB; ++k) {
+                    DF acc = {0.f, 0.f};
+#pragma unroll
+                    for (int m = 0; m < k; ++m) {
+                        const float2 l = sL[k][m];
+                        df_acc(acc, w[m].hi, w[m].lo, l.x, l.y);
+                    }
+                    w[k] = df_sub(w[k], df_norm(acc));
+                }
+#pragma unroll
+                for (int c = 0; c < TB; ++c) __stcg(T + c * TB + r, f2_of(df_mul(w[c], df_of(sDi[c]))));
+            }
+            __threadfence();
+            cl.sync();
+            // every CTA has read the unfactored diagonal tile: store the factored one
+            if (crank == 0)
+                for (int e = t; e < TT; e += kThreads) __stcg(Td + e, sL[e % TB][e / TB]);
+            // B2. L D_J of the tiles below into the worker's scratch
+            for (int x = crank * kThreads + t; x < M.bt * TT; x += cs * kThreads) {
+                const int d = 1 + x / TT, el = x % TT;
+                if (J + d >= M.nbc) continue;
+                __stcg(wdf + x, f2_of(df_mul(df_of(__ldcg(band + tile_off(M, J, d) + el)), df_of(sL[el / TB][el / TB]))));
+            }
+            __threadfence();
+            cl.sync();
+            // C. trailing update: tile (J+e, d-e) -= (L D_J)_{J+d} L_{J+e}^T, 1 <= e <= d; the next
+            // item's operands and outputs are loaded into registers while the current one computes
+            const int nt = M.bt * (M.bt + 1) / 2;
+            const int r = t % TB, c0 = (t / TB) * 4;
+            auto item = [&](int u, int &d, int &e) {
+                d = 1;
+                int rem = u;
+                while (rem >= d) {
+                    rem -= d;
+                    ++d;
+                }
+                e = 1 + rem;
+            };
+            auto next = [&](int u) {  // the first item >= u of this CTA inside the band
+                for (; u < nt; u += cs) {
+                    int d, e;
+                    item(u, d, e);
+                    if (J + d < M.nbc) break;
+                }
+                return u;
+            };
+            float2 ra[TT / kThreads], rb[TT / kThreads], ro[4];
+            auto fetch = [&](int u) {
+                int d, e;
+                item(u, d, e);
+                const float2 *Ad = wdf + (size_t)(d - 1) * TT, *Be = band + tile_off(M, J, e);
+#pragma unroll
+                for (int j = 0; j < TT / kThreads; ++j) {
+                    ra[j] = __ldcg(Ad + t + j * kThreads);
+                    rb[j] = __ldcg(Be + t + j * kThreads);
+                }
+                const float2 *Tt = band + tile_off(M, J + e, d - e);
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) ro[cc] = __ldcg(Tt + (c0 + cc) * TB + r);
+            };
+            int u = next(crank);
+            if (u < nt) fetch(u);
+            while (u < nt) {
+                const int un = next(u + cs);
+                __syncthreads();
+#pragma unroll
+                for (int j = 0; j < TT / kThreads; ++j) {
+                    const int x = t + j * kThreads;
+                    fA[x % TB][x / TB] = ra[j];
+                    fB[x % TB][x / TB] = rb[j];
+                }
+                __syncthreads();
+                float2 o[4];
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc) o[cc] = ro[cc];
+                int d, e;
+                item(u, d, e);
+                if (un < nt) fetch(un);
+                DF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 8
+                for (int k = 0; k < TB; ++k) {
+                    const float2 a = fA[r][k];
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) {
+                        const float2 b = fB[c0 + cc][k];
+                        df_acc(acc[cc], a.x, a.y, b.x, b.y);
+                    }
+                }
+                float2 *Tt = band + tile_off(M, J + e, d - e);
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc)
+                    __stcg(Tt + (c0 + cc) * TB + r, f2_of(df_sub(df_of(o[cc]), df_norm(acc[cc]))));
+                u = un;
+            }
+            __threadfence();
+            cl.sync();
+        }
     }
 }
 
@@ -1551,10 +1636,15 @@ int panels_factor_impl(astro_ctx *ctx, int32_t cluster_size, astro_panels_info *
                               dptr<double>(L->d_band), dptr<int>(L->d_status), (uint16_t *)nullptr, (int *)nullptr,
                               0LL, 0));
     } else if (ctx->bandFp64Update == 3) {
-        CK(cudaLaunchKernelEx(&cfg, k_band_ldl<3>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
+        // the band in double-float for the factorisation, FP64 again after it
+        const long long nb = L->bandDoubles;
+        const unsigned cgr = (unsigned)std::min<long long>((nb + 255) / 256, 152LL * 16);
+        k_band_df_convert<<<cgr, 256, 0, s>>>(nb, dptr<double>(L->d_band), 1);
+        CK(cudaLaunchKernelEx(&cfg, k_band_ldl_df, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
                               (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),
-                              dptr<double>(L->d_band), dptr<int>(L->d_status), dptr<uint16_t>(L->d_slices),
-                              (int *)nullptr, L->sliceStride, 0));
+                              dptr<float2>(L->d_band), dptr<int>(L->d_status), dptr<float2>(L->d_slices),
+                              L->sliceStride / 4));
+        k_band_df_convert<<<cgr, 256, 0, s>>>(nb, dptr<double>(L->d_band), 0);
     } else if (ctx->bandFp64Update == 2) {
         CK(cudaLaunchKernelEx(&cfg, k_band_ldl<1>, (const PanelMeta *)dptr<PanelMeta>(L->d_meta),
                               (const int *)dptr<int>(L->d_sched), (const int *)dptr<int>(L->d_schedPtr),

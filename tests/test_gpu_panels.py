@@ -227,8 +227,8 @@ def test_solve_sweep_arithmetic(batch):
 
 
 def test_double_float_update_with_refined_solve(batch):
-    """The band factor with double-float trailing updates (option value 3: about 48 significant
-    bits) and the default solve (double-float sweeps, one FP64 refinement against the operator):
+    """The band factor carried in double-float throughout (option value 3: about 48 significant
+    bits per operation) and the default solve (double-float sweeps, one FP64 refinement against the operator):
     the solution meets the sparse direct solve as the FP64 factor's does and agrees with it to
     1e-10; the unrefined double-float sweeps on that factor are within 1e-7."""
     from misc_gb300.astro import OPT_BAND_FP64_UPDATE, OPT_PANELS_SOLVE
