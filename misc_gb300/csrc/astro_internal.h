@@ -257,6 +257,9 @@ int elem_update_internal_soln(astro_ctx *ctx, const double *d_extInt, double *d_
 // d_acc -= Im(Ru(d + i h)) accumulated in colour order (internal layout; shells also d_intAcc).
 int solid_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
                double *d_intAcc);                                                                   // elem_solid_cstep.cu
+// design variables d0 .. d0+nd-1 into d_acc + (d-d0) n, d_intAcc + (d-d0) ni
+int solid_drdd_batch(astro_ctx *ctx, int d0, int nd, double h, const ElemDevState &s, double *d_acc,
+                     double *d_intAcc);  // elem_solid_cstep.cu
 // per-element orientation of solid meshes with orientation design variables (r_getOrientation's
 // rotation of the section frame by their real values), into d_secOrient (elem_solid_cstep.cu)
 int solid_orient_prepare(astro_ctx *ctx);

@@ -1349,12 +1349,41 @@ extern "C" int astro_total_dldd(astro_ctx *ctx, const astro_state *state, double
         if ((rc = drdd_state(ctx, state, D))) return rc;
         if ((rc = dev_alloc(ctx, T.acc, sizeof(double) * n))) return rc;
         if (hasInt && (rc = dev_alloc(ctx, T.iacc, sizeof(double) * ni))) return rc;
-        for (int d = 1; d <= nd; ++d) {
-            if ((rc = drdd_device(ctx, d, h, D, dptr<double>(T.acc), hasInt ? dptr<double>(T.iacc) : nullptr))) return rc;
-            double s = 0.0, si = 0.0;
-            if ((rc = dev_dot(ctx, dptr<double>(T.x), dptr<double>(T.acc), n, T.part, &s))) return rc;
-            if (hasInt && (rc = dev_dot(ctx, dptr<double>(T.il), dptr<double>(T.iacc), ni, T.part, &si))) return rc;
-            dldd[d - 1] = (dldd_explicit ? dldd_explicit[d - 1] : 0.0) - s - si;
+        if (ctx->hasSolid) {
+            // solids: up to kBatch variables per pass of the complex-step kernels, one launch per
+            // colour over all of them (the per-variable launches cover a few SMs each)
+            constexpr int kBatch = 16;
+            const int nb = std::min(nd, kBatch);
+            if ((rc = dev_alloc(ctx, T.acc, sizeof(double) * (size_t)n * nb))) return rc;
+            if (hasInt && (rc = dev_alloc(ctx, T.iacc, sizeof(double) * (size_t)ni * nb))) return rc;
+            for (int d0 = 1; d0 <= nd; d0 += nb) {
+                const int cnt = std::min(nb, nd - d0 + 1);
+                CK(cudaMemsetAsync(T.acc.p, 0, sizeof(double) * (size_t)n * cnt, ctx->stream));
+                if (hasInt) CK(cudaMemsetAsync(T.iacc.p, 0, sizeof(double) * (size_t)ni * cnt, ctx->stream));
+                if ((rc = solid_drdd_batch(ctx, d0, cnt, h, D.ds, dptr<double>(T.acc),
+                                           hasInt ? dptr<double>(T.iacc) : nullptr)))
+                    return rc;
+                for (int k = 0; k < cnt; ++k) {
+                    // dR/dd = -(sum of -Im Ru) / h: the dot with lambda scaled once
+                    double s = 0.0, si = 0.0;
+                    if ((rc = dev_dot(ctx, dptr<double>(T.x), dptr<double>(T.acc) + (size_t)k * n, n, T.part, &s)))
+                        return rc;
+                    if (hasInt && (rc = dev_dot(ctx, dptr<double>(T.il), dptr<double>(T.iacc) + (size_t)k * ni, ni,
+                                                T.part, &si)))
+                        return rc;
+                    const int d = d0 + k;
+                    dldd[d - 1] = (dldd_explicit ? dldd_explicit[d - 1] : 0.0) + (s + si) / h;
+                }
+            }
+        } else {
+            for (int d = 1; d <= nd; ++d) {
+                if ((rc = drdd_device(ctx, d, h, D, dptr<double>(T.acc), hasInt ? dptr<double>(T.iacc) : nullptr)))
+                    return rc;
+                double s = 0.0, si = 0.0;
+                if ((rc = dev_dot(ctx, dptr<double>(T.x), dptr<double>(T.acc), n, T.part, &s))) return rc;
+                if (hasInt && (rc = dev_dot(ctx, dptr<double>(T.il), dptr<double>(T.iacc), ni, T.part, &si))) return rc;
+                dldd[d - 1] = (dldd_explicit ? dldd_explicit[d - 1] : 0.0) - s - si;
+            }
         }
     }
     if (disp_adj) {

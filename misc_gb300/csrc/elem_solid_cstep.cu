@@ -36,6 +36,9 @@ struct SolidCsArgs {
     const int *dcat, *dcomp;
     const double *dval;
     int dvar;
+    const int *dvars;  // per listed element its design variable (batched form), or null: dvar
+    int dvarBase;      // batched form: variable d accumulates at (d - dvarBase) * stride
+    long long accStride, intAccStride;
     double h, gpc;
     const int *intVecOff;
     ElemDevState st;
@@ -72,6 +75,9 @@ __global__ void k_solid_cstep(SolidCsArgs A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= A.count) return;
     const int e = A.els[q];
+    const int dvar = A.dvars ? A.dvars[q] : A.dvar;
+    double *acc = A.dvars ? A.acc + (size_t)(dvar - A.dvarBase) * A.accStride : A.acc;
+    double *intAcc = A.intAcc && A.dvars ? A.intAcc + (size_t)(dvar - A.dvarBase) * A.intAccStride : A.intAcc;
     const int et = A.etype[e];
     const int nsf = (et == 81) ? 11 : 8;  // shape functions: nodes (+ bubbles)
     const cplx ih(0.0, A.h);
@@ -85,7 +91,7 @@ __global__ void k_solid_cstep(SolidCsArgs A) {
     cplx locRot[3];
     for (int t = A.e2dR[e]; t < A.e2dR[e + 1]; ++t) {
         const int d = A.e2d[t], cat = A.dcat[d - 1];
-        const bool mine = d == A.dvar;
+        const bool mine = d == dvar;
         if (cat == ASTRO_DCAT_ELASTIC_MODULUS && mine) ep[A.dcomp[d - 1] - 1] += A.e2c[t] * ih;
         if (cat == ASTRO_DCAT_DENSITY && mine) rho += A.e2c[t] * ih;
         if (cat == ASTRO_DCAT_ORIENTATION) {
@@ -119,7 +125,7 @@ __global__ void k_solid_cstep(SolidCsArgs A) {
         if (A.n2dR)
             for (int t = A.n2dR[nd - 1]; t < A.n2dR[nd]; ++t) {
                 const int d = A.n2d[t];
-                if (d == A.dvar && A.dcat[d - 1] == ASTRO_DCAT_NODE_COORD) g[A.dcomp[d - 1] - 1] += A.n2c[t] * ih;
+                if (d == dvar && A.dcat[d - 1] == ASTRO_DCAT_NODE_COORD) g[A.dcomp[d - 1] - 1] += A.n2c[t] * ih;
             }
         for (int i = 0; i < 3; ++i) X[a][i] = orient[i][0] * g[0] + orient[i][1] * g[1] + orient[i][2] * g[2];
         const int r = A.rank[nd - 1] - 1;
@@ -230,11 +236,11 @@ __global__ void k_solid_cstep(SolidCsArgs A) {
     }
     for (int a = 0; a < 8; ++a) {
         const int r = A.rank[A.elist[8 * (size_t)e + a] - 1] - 1;
-        for (int v = 0; v < 3; ++v) A.acc[3 * (size_t)r + v] -= ru[a][v].im;
+        for (int v = 0; v < 3; ++v) acc[3 * (size_t)r + v] -= ru[a][v].im;
     }
-    if (et == 81 && A.intAcc)
+    if (et == 81 && intAcc)
         for (int j = 0; j < 3; ++j)
-            for (int v = 0; v < 3; ++v) A.intAcc[ioff + 3 * v + j] -= ru[8 + j][v].im;
+            for (int v = 0; v < 3; ++v) intAcc[ioff + 3 * v + j] -= ru[8 + j][v].im;
 }
 
 }  // namespace
@@ -265,13 +271,8 @@ static void solid_dvar_elements(const astro_ctx *ctx, int dvar, std::vector<int>
     }
 }
 
-int solid_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc, double *d_intAcc) {
-    std::vector<int> list, ptr;
-    solid_dvar_elements(ctx, dvar, list, ptr);
-    if (list.empty()) return ASTRO_OK;
-    DevBuf dl;
-    int rc;
-    if ((rc = upload(ctx, dl, list.data(), sizeof(int) * list.size()))) return rc;
+static SolidCsArgs solid_cs_args(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc,
+                                 double *d_intAcc) {
     SolidCsArgs A;
     A.etype = dptr<int>(ctx->d_etype);
     A.elist = dptr<int>(ctx->d_elist);
@@ -297,6 +298,20 @@ int solid_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double
     A.st = s;
     A.acc = d_acc;
     A.intAcc = d_intAcc;
+    A.dvars = nullptr;
+    A.dvarBase = 1;
+    A.accStride = A.intAccStride = 0;
+    return A;
+}
+
+int solid_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double *d_acc, double *d_intAcc) {
+    std::vector<int> list, ptr;
+    solid_dvar_elements(ctx, dvar, list, ptr);
+    if (list.empty()) return ASTRO_OK;
+    DevBuf dl;
+    int rc;
+    if ((rc = upload(ctx, dl, list.data(), sizeof(int) * list.size()))) return rc;
+    SolidCsArgs A = solid_cs_args(ctx, dvar, h, s, d_acc, d_intAcc);
     for (size_t col = 0; col + 1 < ptr.size(); ++col) {
         const int cnt = ptr[col + 1] - ptr[col];
         if (!cnt) continue;
@@ -308,6 +323,54 @@ int solid_drdd(astro_ctx *ctx, int dvar, double h, const ElemDevState &s, double
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     dev_free(dl);
     return cuda_check(ctx, e, "solid complex-step kernel");
+}
+
+// Design variables d0 .. d0+nd-1 at once: one launch per colour over the (element, variable) pairs
+// of that colour, variable d accumulating at d_acc + (d-d0) n (and d_intAcc + (d-d0) ni).  Each
+// variable's accumulator receives its elements' terms in the same colour order as solid_drdd,
+// so the results are the same; the launches are nd times wider.
+int solid_drdd_batch(astro_ctx *ctx, int d0, int nd, double h, const ElemDevState &s, double *d_acc,
+                     double *d_intAcc) {
+    const int ncol = ctx->P.ncolors;
+    std::vector<std::vector<int>> els(ncol), dvs(ncol);
+    for (int d = d0; d < d0 + nd; ++d) {
+        std::vector<int> list, ptr;
+        solid_dvar_elements(ctx, d, list, ptr);
+        for (int col = 0; col + 1 < (int)ptr.size(); ++col)
+            for (int k = ptr[col]; k < ptr[col + 1]; ++k) {
+                els[col].push_back(list[k]);
+                dvs[col].push_back(d);
+            }
+    }
+    std::vector<int> all, allD, start(1, 0);
+    for (int col = 0; col < ncol; ++col) {
+        all.insert(all.end(), els[col].begin(), els[col].end());
+        allD.insert(allD.end(), dvs[col].begin(), dvs[col].end());
+        start.push_back((int)all.size());
+    }
+    if (all.empty()) return ASTRO_OK;
+    DevBuf dl, dd;
+    int rc;
+    if ((rc = upload(ctx, dl, all.data(), sizeof(int) * all.size())) ||
+        (rc = upload(ctx, dd, allD.data(), sizeof(int) * allD.size())))
+        return rc;
+    SolidCsArgs A = solid_cs_args(ctx, 0, h, s, d_acc, d_intAcc);
+    A.dvarBase = d0;
+    A.accStride = ctx->P.n;
+    A.intAccStride = ctx->P.intVecSize;
+    for (int col = 0; col < ncol; ++col) {
+        const int cnt = start[col + 1] - start[col];
+        if (!cnt) continue;
+        A.els = dptr<int>(dl) + start[col];
+        A.dvars = dptr<int>(dd) + start[col];
+        A.count = cnt;
+        k_solid_cstep<<<(cnt + 63) / 64, 64, 0, ctx->stream>>>(A);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    dev_free(dl);
+    dev_free(dd);
+    return cuda_check(ctx, e, "solid complex-step kernel (batched)");
 }
 
 namespace {

@@ -159,3 +159,24 @@ def test_brickim_modulus_complex_step():
         odr, oidr = o.drdd_complex(d, h=1e-30, state=st)
         assert np.linalg.norm(dr - odr) <= 1e-10 * np.linalg.norm(odr), d
         assert np.linalg.norm(idr - oidr[:o.int_vec_size]) <= 1e-10 * np.linalg.norm(oidr[:o.int_vec_size]), d
+
+
+def test_design_gradient_batched_complex_steps():
+    """astro_total_dldd on solids runs the complex-step kernels for up to 16 design variables per
+    pass (one launch per colour over all of them): 20 modulus variables on a mixed brick8 /
+    brickIM block (two passes, internal DOF), each gradient entry against explicit - lambda .
+    dR/dd - lambda_int . dR_int/dd from the per-variable getdRelasticdD, 1e-12."""
+    m = _im(M.hex_block(6, 3, 3, lx=1.5, ly=0.75, lz=0.75, seed=12), 2)
+    M.add_design_variables(m, 20, M.DCAT_ELASTIC_MODULUS, component=1)
+    g, o = AstroGPU(m), Oracle(m)
+    st = _state(o, np.random.default_rng(13))
+    g.getElasticSolnLoad(1, state=st, export=False)
+    g.scaleElasticMPC()
+    rng = np.random.default_rng(14)
+    dldu, idldu, expl = rng.standard_normal(g.n), rng.standard_normal(g.int_vec_size), rng.standard_normal(20)
+    dldd, lam, ilam, s = g.getTotaldLdD(dldu, int_dldu=idldu, dldd_explicit=expl, state=st, rtol=1e-10)
+    assert s.status == 0
+    for d in range(1, 21):
+        dr, idr = g.getdRelasticdD(d, state=st)
+        ref = expl[d - 1] - lam @ dr - ilam @ idr
+        assert abs(dldd[d - 1] - ref) <= 1e-12 * max(abs(ref), np.linalg.norm(lam) * np.linalg.norm(dr)), d
