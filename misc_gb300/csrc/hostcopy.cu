@@ -57,7 +57,7 @@ static bool stage_ready(astro_ctx *ctx) {
     HostStage *S = new HostStage;
     const unsigned hc = std::thread::hardware_concurrency();
     S->threads = std::max(1, std::min(kMaxThreads, hc ? (int)hc / 2 : 4));
-    bool ok = true;
+    bool ok = cudaSetDevice(ctx->device) == cudaSuccess;  // the streams belong to the context's device
     for (int t = 0; t < S->threads && ok; ++t) {
         for (int k = 0; k < 2 && ok; ++k)
             ok = cudaHostAlloc(&S->pinned[t][k], kSlot, cudaHostAllocDefault) == cudaSuccess &&
