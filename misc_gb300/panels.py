@@ -66,15 +66,22 @@ def solve_batch(g: AstroGPU, m, n_dvars: int, cluster_size: int = 0, load_scale:
 
 def _main(argv=None):
     """Factor a generated batch with the trailing-update variants in turn and print each factor
-    time (ASTRO_OPT_BAND_FP64_UPDATE: 1 FP64, 2 emulation on mma.sync, 0 emulation on tcgen05)."""
+    time (ASTRO_OPT_BAND_FP64_UPDATE: 1 FP64, 2 emulation on mma.sync, 0 emulation on tcgen05, 3
+    double-float factorisation); with --rhs, then solve a seeded random block of that many columns
+    in each ASTRO_OPT_PANELS_SOLVE mode (0 double-float + FP64 refinement, 1 FP64 sweeps, 2
+    double-float alone), twice each, and print the host-clock times and the distance to the first
+    mode's solution."""
     import argparse
 
     from . import model as M
-    from .astro import OPT_BAND_FP64_UPDATE
+    from .astro import OPT_BAND_FP64_UPDATE, OPT_PANELS_SOLVE
     p = argparse.ArgumentParser(description=_main.__doc__)
     p.add_argument("--panels", type=int, default=64)
     p.add_argument("--cluster", type=int, default=4, help="CTAs per cluster (2, 4, 8)")
     p.add_argument("--updates", default="1,2,0", help="option values, in launch order")
+    p.add_argument("--rhs", type=int, default=0, help="right-hand-side columns of the solves (0: no solve)")
+    p.add_argument("--solves", default="1,2,0", help="ASTRO_OPT_PANELS_SOLVE values, in order")
+    p.add_argument("--solve-update", type=int, default=1, help="the trailing-update option of the solves' factor")
     a = p.parse_args(argv)
     m = M.panel_batch(num_panels=a.panels)
     g = AstroGPU(m)
@@ -82,9 +89,28 @@ def _main(argv=None):
     g.scaleElasticMPC()
     for mode in (int(x) for x in a.updates.split(",")):
         g.set_option(OPT_BAND_FP64_UPDATE, mode)
-        info = g.panels_factor(a.cluster)
-        print(f"update {mode}: factor {info.factor_seconds:.4f} s, {info.workers} clusters of {info.cluster_size}",
-              flush=True)
+        for _ in range(2):
+            info = g.panels_factor(a.cluster)
+            print(f"update {mode}: factor {info.factor_seconds:.4f} s, {info.workers} clusters of "
+                  f"{info.cluster_size}", flush=True)
+    if a.rhs > 0:
+        g.set_option(OPT_BAND_FP64_UPDATE, a.solve_update)
+        g.panels_factor(a.cluster)
+        B = np.asfortranarray(np.random.default_rng(1).standard_normal((g.n, a.rhs)))
+        first = None
+        for mode in (int(x) for x in a.solves.split(",")):
+            g.set_option(OPT_PANELS_SOLVE, mode)
+            for rep in range(2):
+                t0 = time.perf_counter()
+                X, si = g.panels_solve(B)
+                print(f"solve mode {mode} rep {rep}: {time.perf_counter() - t0:.4f} s "
+                      f"(call {si.solve_seconds:.4f} s)", flush=True)
+            if first is None:
+                first = X
+            else:
+                print(f"  distance to the first mode's solution {np.linalg.norm(X - first) / np.linalg.norm(first):.3e}")
+        g.set_option(OPT_PANELS_SOLVE, 0)
+    g.set_option(OPT_BAND_FP64_UPDATE, 1)
 
 
 if __name__ == "__main__":
