@@ -625,7 +625,7 @@ def _panels_eval(a):
            "mma_sync_update_factor_seconds": facMma,
            "seconds": tot, "factor_seconds": fac, "solve_seconds": sol,
            "solve_sweeps": "double-float sweeps from copies of the FP64 factor + one FP64 refinement pass",
-           "solve_other_sweeps": sweeps, "double_float_update": df_update, "panels": int(info.num_panels),
+           "solve_other_sweeps": sweeps, "double_float_factorisation": df_update, "panels": int(info.num_panels),
            "elements": m.num_els, "dof": g.n, "max_bandwidth": info.max_bandwidth, "band_bytes": info.band_bytes,
            "cluster_size": best, "autotune_factor_seconds": tune, "workers": info.workers,
            "rel_residual_u": float(np.linalg.norm(r) / np.linalg.norm(B[:, 0])),

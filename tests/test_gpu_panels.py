@@ -226,7 +226,7 @@ def test_solve_sweep_arithmetic(batch):
         g.set_option(OPT_PANELS_SOLVE, 3)
 
 
-def test_double_float_update_with_refined_solve(batch):
+def test_double_float_factorisation_with_refined_solve(batch):
     """The band factor carried in double-float throughout (option value 3: about 48 significant
     bits per operation) and the default solve (double-float sweeps, one FP64 refinement against the operator):
     the solution meets the sparse direct solve as the FP64 factor's does and agrees with it to
