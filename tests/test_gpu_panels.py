@@ -249,3 +249,22 @@ def test_double_float_factorisation_with_refined_solve(batch):
     _check(A, Xdf, B, Xr)
     assert np.linalg.norm(Xdf - X64) <= 1e-10 * np.linalg.norm(X64)
     assert np.linalg.norm(Xraw - X64) <= 1e-7 * np.linalg.norm(X64)
+
+
+def test_staged_pageable_copies():
+    """A solve whose right-hand sides and solutions pass 64 MB each way goes through the staged
+    pageable copies (page-locked slots, host threads): every column equals the same column solved
+    alone (small plain copies), bit for bit: each column's sweeps and refinement are independent
+    of the others."""
+    m = M.panel_batch(num_panels=512, indices=range(0, 512, 32))
+    g = AstroGPU(m)
+    g.getElasticSolnLoad(1, export=False)
+    g.scaleElasticMPC()
+    g.panels_factor(4)
+    k = max(9, -(-80_000_000 // (8 * g.n)))  # at least 80 MB
+    assert 8 * g.n * k >= 64 << 20
+    B = np.random.default_rng(31).standard_normal((g.n, k))
+    X, _ = g.panels_solve(B)
+    for c in sorted({0, 1, k // 2, k - 1}):
+        x1, _ = g.panels_solve(B[:, c])
+        assert np.array_equal(X[:, c], x1), c
